@@ -1,0 +1,253 @@
+/*
+ * nt2g.h -- C ABI of libnt2gpu, the sm_103a evaluator for NT2's fused
+ * elementwise expressions over nt2::table and its sum/dot reductions.
+ *
+ * Plain pointers, sizes and status codes: no C++ or torch types cross this
+ * boundary.  Every call returns an nt2g_status; no call exits, throws or
+ * prints.  nt2g_last_error() holds the text of the last failure on the
+ * calling thread.  Device pointers are caller-owned; the calls are
+ * stream-ordered and asynchronous (a cudaStream_t is passed as void*).
+ *
+ * What each entry point replaces in NT2 (paths inside the NT2 source tree):
+ *   CSDK  = modules/core/sdk/include/nt2
+ *   TABLE = modules/core/container/table/include/nt2
+ *   SHM   = modules/arch/shared_memory/include/nt2
+ *   RED   = modules/core/reduction/include/nt2
+ *   CUDA  = modules/arch/cuda/include/nt2
+ */
+#ifndef NT2G_H
+#define NT2G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NT2G_ABI_VERSION 1
+
+typedef enum nt2g_status {
+    NT2G_OK = 0,
+    NT2G_ERR_INVALID = 1,     /* bad pointer, size, alignment, opcode or slot */
+    NT2G_ERR_UNSUPPORTED = 2, /* valid request this build cannot run */
+    NT2G_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+    NT2G_ERR_DEVICE_FLAG = 4, /* a kernel reported an error through its flag */
+    NT2G_ERR_NOMEM = 5        /* host or device allocation failed */
+} nt2g_status;
+
+/* Arithmetic policy of the float math.
+ * NT2G_PREC_FAST: fused multiply-add, approximate-reciprocal division with a
+ *   Newton step where the operands are known normal, erfc/normcdf on an exact
+ *   split of x^2; every functor within 4 ulp of FP64.
+ * NT2G_PREC_NT2: NT2's own scalar algorithms and operation order (unfused
+ *   fma/Horner, IEEE division and sqrt); bit-identical to NT2's CPU result. */
+typedef enum nt2g_precision { NT2G_PREC_FAST = 0, NT2G_PREC_NT2 = 1 } nt2g_precision;
+
+typedef enum nt2g_dtype { NT2G_F32 = 0, NT2G_U8 = 1 } nt2g_dtype;
+
+const char *nt2g_last_error(void);
+int nt2g_abi_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Fused expression programs: the lowered form of an nt2 expression.  */
+/* Replaces the transform_ overload on the shared_memory site         */
+/* (SHM/core/functions/shared_memory/transform.hpp:27-51) and the      */
+/* intended external_kernel code generator                             */
+/* (tools/external_kernel/backend.cpp:32-52) for site cuda_.           */
+/* ------------------------------------------------------------------ */
+
+/* Opcodes.  Values are numbered in program order (SSA): operand fields a,b,c
+ * name earlier instructions; LOAD/SCALAR/STORE name argument slots.  The
+ * result dtype of each instruction is op.dtype. */
+typedef enum nt2g_opcode {
+    NT2G_OP_LOAD = 1,      /* a = slot of a device table                     */
+    NT2G_OP_SCALAR = 2,    /* a = slot of a scalar argument (broadcast)      */
+    NT2G_OP_CONST = 3,     /* imm                                            */
+    NT2G_OP_STORE = 4,     /* a = value, b = slot of the output table        */
+    NT2G_OP_ADD = 10, NT2G_OP_SUB, NT2G_OP_MUL, NT2G_OP_DIV, NT2G_OP_NEG, NT2G_OP_ABS,
+    NT2G_OP_SQR, NT2G_OP_SQRT, NT2G_OP_REC, NT2G_OP_MIN, NT2G_OP_MAX,
+    NT2G_OP_FMA = 30,      /* a*b + c (unfused under NT2G_PREC_NT2)          */
+    NT2G_OP_FNMS,          /* c - a*b                                        */
+    NT2G_OP_EXP = 40, NT2G_OP_LOG, NT2G_OP_LOG1P, NT2G_OP_ERFC, NT2G_OP_NORMCDF,
+    NT2G_OP_FASTNORMCDF,
+    NT2G_OP_LT = 60, NT2G_OP_GT, NT2G_OP_LE, NT2G_OP_GE, NT2G_OP_EQ, NT2G_OP_NE, /* -> logical */
+    NT2G_OP_IF_ELSE = 70,  /* a ? b : c                                      */
+    NT2G_OP_SELINC,        /* a ? b+1 : b                                    */
+    NT2G_OP_SELDEC,        /* a ? b-1 : b                                    */
+    NT2G_OP_IF_ZERO_ELSE_ONE, /* a ? 0 : 1                                   */
+    NT2G_OP_ADDS           /* saturating add (uint8)                         */
+} nt2g_opcode;
+
+typedef struct nt2g_op {
+    int16_t code;  /* nt2g_opcode */
+    int16_t dtype; /* nt2g_dtype of the result (logical results: the dtype compared) */
+    int32_t a, b, c;
+    float imm;
+} nt2g_op;
+
+typedef struct nt2g_arg {
+    void *ptr;     /* device table (LOAD / STORE slots) */
+    double scalar; /* value of a SCALAR slot */
+    int32_t dtype; /* nt2g_dtype */
+    int32_t kind;  /* 0 = table, 1 = scalar */
+} nt2g_arg;
+
+typedef struct nt2g_program nt2g_program;
+
+typedef struct nt2g_program_info {
+    int32_t kernel;       /* 0 = generic interpreter, >0 = fused kernel id */
+    int32_t n_ops;        /* after common-subexpression and dead-code removal */
+    int32_t n_regs;       /* interpreter registers after allocation */
+    int32_t n_slots;
+    char kernel_name[48];
+} nt2g_program_info;
+
+/* Validate, canonicalise (CSE + DCE), register-allocate and bind a program.
+ * When the program is one of the fused kernels' expressions (Black-Scholes
+ * call+put, the NT2 demo Black-Scholes, saxpy, expr3, rgb2yuv, sigma-delta)
+ * it is bound to that kernel; otherwise to the generic interpreter. */
+nt2g_status nt2g_program_create(const nt2g_op *ops, int32_t n_ops, int32_t n_slots,
+                                nt2g_program **out);
+nt2g_status nt2g_program_info_get(const nt2g_program *p, nt2g_program_info *info);
+void nt2g_program_destroy(nt2g_program *p);
+
+/* transform(out, expr, range): evaluate elements [offset, offset+count) of
+ * every table slot (TABLE/core/functions/expr/transform.hpp:40-60 range
+ * semantics).  force_generic != 0 skips the fused-kernel binding. */
+nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t offset,
+                      int64_t count, int32_t precision, int32_t force_generic, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Fused kernels for the named expressions (also reached through      */
+/* nt2g_eval).  All tables have n elements.                           */
+/* ------------------------------------------------------------------ */
+
+/* Textbook Black-Scholes call+put (normcdf = Half*erfc(-Sqrt_2o_2*x),
+ * modules/core/statistics/include/nt2/statistics/functions/generic/normcdf.hpp:34).
+ * sigma == NULL selects the scalar sigma_s; r is a scalar. */
+nt2g_status nt2g_blackscholes_f32(const float *S, const float *K, const float *T, const float *sigma,
+                                  float sigma_s, float r, float *call, float *put, int64_t n,
+                                  int32_t precision, void *stream);
+
+/* NT2 demo form, call only, fastnormcdf
+ * (demo/blackscholes/nt2/blackandscholes_nt2.cpp:55-59).  r_t / v_t NULL
+ * select the scalars r / v. */
+nt2g_status nt2g_blackscholes_demo_f32(const float *S, const float *X, const float *T, const float *r_t,
+                                       float r, const float *v_t, float v, float *R, int64_t n,
+                                       int32_t precision, void *stream);
+
+/* Fused forward + reverse-mode (vector-Jacobian) Black-Scholes: given
+ * upstream gradients gc, gp it writes call, put and the per-option
+ * gradients of gc*call + gp*put w.r.t. S, K, T, sigma and r.  Intermediates
+ * are recomputed, not stored.  No NT2 counterpart (NT2 has no adjoint). */
+nt2g_status nt2g_blackscholes_vjp_f32(const float *S, const float *K, const float *T,
+                                      const float *sigma, float r, const float *gc, const float *gp,
+                                      float *call, float *put, float *dS, float *dK, float *dT,
+                                      float *dsigma, float *dr, int64_t n, void *stream);
+
+/* Y = alpha*X + Y (demo/saxpy/nt2/saxpy_nt2.cpp:41), two roundings. */
+nt2g_status nt2g_saxpy_f32(float alpha, const float *X, float *Y, int64_t n, void *stream);
+
+/* out = exp(-sqr(x))*sqrt(abs(y)) + log1p(abs(z)). */
+nt2g_status nt2g_expr3_f32(const float *x, const float *y, const float *z, float *out, int64_t n,
+                           int32_t precision, void *stream);
+
+/* y/u/v planes (demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:30-32), unfused as NT2. */
+nt2g_status nt2g_rgb2yuv_f32(const float *r, const float *g, const float *b, float *y, float *u,
+                             float *v, int64_t n, void *stream);
+
+/* One sigma-delta step on uint8 pixels, bkg/var updated in place, label
+ * written (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:38-57).  Bit-exact. */
+nt2g_status nt2g_sigmadelta_u8(const uint8_t *frame, uint8_t *bkg, uint8_t *var, uint8_t *label,
+                               int64_t n, void *stream);
+
+/* n_frames consecutive steps in one pass (frames and labels are n_frames
+ * planes of n pixels); bkg/var stay in registers between frames. */
+nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8_t *var,
+                                      uint8_t *labels, int64_t n, int32_t n_frames, void *stream);
+
+/* Element functions y = f(x) for the accuracy tests and simple maps.
+ * fn: 0 exp, 1 log, 2 log1p, 3 erfc, 4 normcdf, 5 fastnormcdf, 6 sqrt,
+ * 7 normcdf(-x) through the shared pair core. */
+nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision,
+                         void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Reductions: sum(x), dot(x,y) = sum(x*y), globalsum                  */
+/* (RED/reduction/functions/expr/dot.hpp:22-42,                       */
+/*  SHM/core/functions/shared_memory/inner_fold.hpp:25-64,            */
+/*  RED/core/functions/globalsum.hpp:43-45).                          */
+/* Compensated FP32 (TwoSum) per thread, warp and block; FP64 only in */
+/* the cross-block combine.  Deterministic for a given n and device.  */
+/* ------------------------------------------------------------------ */
+
+/* Device workspace bytes the reductions need for n elements. */
+nt2g_status nt2g_reduce_workspace_size(int64_t n, size_t *bytes);
+
+/* out64 (device, 1 double): the FP64-combined result; out32 (device, 1
+ * float, may be NULL): the same rounded to float, which is what NT2's
+ * sum(table<float>) returns.  y == NULL -> sum(x). */
+nt2g_status nt2g_reduce_f32(const float *x, const float *y, int64_t n, void *workspace,
+                            size_t workspace_bytes, double *out64, float *out32, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Batched uneven tables: one persistent launch over many tables, each */
+/* with its own expression.                                             */
+/* ------------------------------------------------------------------ */
+
+typedef enum nt2g_batch_expr {
+    NT2G_BATCH_BLACKSCHOLES = 0, /* in0=S in1=K in2=T, out0=call out1=put, s0=sigma s1=r */
+    NT2G_BATCH_SAXPY = 1,        /* in0=X, out0=Y (in place), s0=alpha */
+    NT2G_BATCH_EXPR3 = 2         /* in0=x in1=y in2=z, out0 */
+} nt2g_batch_expr;
+
+typedef struct nt2g_batch_item {
+    int32_t expr;
+    int32_t reserved;
+    int64_t n;
+    const float *in[3];
+    float *out[2];
+    float s[2];
+} nt2g_batch_item;
+
+typedef struct nt2g_batch_tune {
+    int32_t block_threads;     /* 128..1024, multiple of 32 */
+    int32_t blocks_per_sm;     /* resident blocks per SM of the persistent grid */
+    int32_t tile_vectors;      /* float4 vectors per tile per thread */
+    int32_t precision;         /* nt2g_precision */
+} nt2g_batch_tune;
+
+typedef struct nt2g_batch nt2g_batch;
+
+/* Upload the item table and its tile prefix sums (allocates device memory
+ * once, here; runs allocate nothing). */
+nt2g_status nt2g_batch_create(const nt2g_batch_item *items, int32_t n_items,
+                              const nt2g_batch_tune *tune, nt2g_batch **out);
+void nt2g_batch_destroy(nt2g_batch *b);
+/* One persistent launch over every tile of every table. */
+nt2g_status nt2g_batch_run(nt2g_batch *b, void *stream);
+/* The comparison path: one plain launch per table, same kernels. */
+nt2g_status nt2g_batch_run_per_table(nt2g_batch *b, void *stream);
+/* Capture nt2g_batch_run into a CUDA graph on `stream` once; later calls
+ * replay it. */
+nt2g_status nt2g_batch_run_graph(nt2g_batch *b, void *stream);
+/* Total elements and algorithmic bytes of the batch. */
+nt2g_status nt2g_batch_stats(const nt2g_batch *b, int64_t *elements, int64_t *bytes);
+
+/* ------------------------------------------------------------------ */
+/* Device memory for the table layer: nt2::table<T, device_> storage   */
+/* (CUDA/sdk/memory/cuda/allocator.hpp:59-74, copies                   */
+/* CUDA/memory/functions/cuda/copy.hpp:52-86).                         */
+/* ------------------------------------------------------------------ */
+nt2g_status nt2g_device_alloc(size_t bytes, void **ptr);
+nt2g_status nt2g_device_free(void *ptr);
+/* kind: 1 host->device, 2 device->host, 3 device->device */
+nt2g_status nt2g_memcpy(void *dst, const void *src, size_t bytes, int32_t kind, void *stream);
+nt2g_status nt2g_stream_synchronize(void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NT2G_H */

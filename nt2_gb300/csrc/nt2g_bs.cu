@@ -1,0 +1,241 @@
+// nt2g_bs.cu -- fused Black-Scholes kernels: call+put forward (both
+// arithmetic policies), the NT2 demo's call-only form, and the fused
+// forward + reverse-mode (vector-Jacobian) kernel.
+//
+// One pass over the option tables: 128-bit loads/stores of 4 options per
+// thread per step, grid-stride persistent blocks, every intermediate in
+// registers.  Work per option is ~140 FP32-pipe instructions (Fast) for 20
+// bytes of HBM traffic, so the kernel sits at the FP32-issue / HBM ridge.
+#include "nt2g_common.cuh"
+#include "nt2g_exprs.cuh"
+#include "nt2g_internal.h"
+
+namespace nt2g {
+
+template <class P, bool SIG_TAB>
+__global__ void __launch_bounds__(256) k_bs(const float *__restrict__ S, const float *__restrict__ K,
+                                            const float *__restrict__ T, const float *__restrict__ sig,
+                                            float sig_s, float r, float *__restrict__ call,
+                                            float *__restrict__ put, int64_t n, int vec)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (vec) {
+        const int64_t nv = n >> 2;
+        for (int64_t i = tid; i < nv; i += stride) {
+            float4 s = ld_stream((const float4 *)S + i), k = ld_stream((const float4 *)K + i),
+                   t = ld_stream((const float4 *)T + i);
+            float4 v = SIG_TAB ? ld_stream((const float4 *)sig + i) : make_float4(sig_s, sig_s, sig_s, sig_s);
+            float4 c, p;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float cj, pj;
+                bs_option<P>(get(s, j), get(k, j), get(t, j), get(v, j), r, cj, pj);
+                set(c, j, cj);
+                set(p, j, pj);
+            }
+            st_stream((float4 *)call + i, c);
+            st_stream((float4 *)put + i, p);
+        }
+        for (int64_t i = (nv << 2) + tid; i < n; i += stride) {
+            float cj, pj;
+            bs_option<P>(S[i], K[i], T[i], SIG_TAB ? sig[i] : sig_s, r, cj, pj);
+            call[i] = cj;
+            put[i] = pj;
+        }
+    } else {
+        for (int64_t i = tid; i < n; i += stride) {
+            float cj, pj;
+            bs_option<P>(S[i], K[i], T[i], SIG_TAB ? sig[i] : sig_s, r, cj, pj);
+            call[i] = cj;
+            put[i] = pj;
+        }
+    }
+}
+
+template <class P, bool RT, bool VT>
+__global__ void __launch_bounds__(256) k_bs_demo(const float *__restrict__ S, const float *__restrict__ X,
+                                                 const float *__restrict__ T, const float *__restrict__ rt,
+                                                 float r, const float *__restrict__ vt, float v,
+                                                 float *__restrict__ R, int64_t n, int vec)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if (vec) {
+        const int64_t nv = n >> 2;
+        for (int64_t i = tid; i < nv; i += stride) {
+            float4 s = ld_stream((const float4 *)S + i), x = ld_stream((const float4 *)X + i),
+                   t = ld_stream((const float4 *)T + i);
+            float4 rr = RT ? ld_stream((const float4 *)rt + i) : make_float4(r, r, r, r);
+            float4 vv = VT ? ld_stream((const float4 *)vt + i) : make_float4(v, v, v, v);
+            float4 o;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                set(o, j, bs_demo_option<P>(get(s, j), get(x, j), get(t, j), get(rr, j), get(vv, j)));
+            st_stream((float4 *)R + i, o);
+        }
+        done = nv << 2;
+    }
+    for (int64_t i = done + tid; i < n; i += stride)
+        R[i] = bs_demo_option<P>(S[i], X[i], T[i], RT ? rt[i] : r, VT ? vt[i] : v);
+}
+
+// ------------------------------------------------------------ adjoint ----
+// Reverse sweep of the Fast forward graph above, hand-derived, with every
+// forward intermediate recomputed in registers.  Seeds gc, gp.
+__device__ __forceinline__ void bs_vjp_option(float S, float K, float T, float sig, float r, float gc,
+                                              float gp, float &C, float &P_, float &dS, float &dK,
+                                              float &dT, float &dsig, float &dr)
+{
+    // forward
+    float sq = __fsqrt_rn(T);
+    float vs = Fast::mul(sig, sq);
+    float q = Fast::fdiv(S, K);
+    float lq = log<Fast>(q);
+    float a = Fast::fma(Fast::mul(sig, sig), 0.5f, r);
+    float num = Fast::fma(a, T, lq);
+    float inv_vs = Fast::fdiv(1.0f, vs);
+    float d1 = Fast::mul(num, inv_vs);
+    float d2 = Fast::fma(-sig, sq, d1);
+    float ert = exp<Fast>(Fast::mul(-r, T));
+    float e = Fast::mul(K, ert);
+    float n1, m1, n2, m2, g1, g2;  // g = exp(-d^2/2)
+    normcdf_pair_pdf(d1, n1, m1, g1);
+    normcdf_pair_pdf(d2, n2, m2, g2);
+    C = Fast::fma(-e, n2, Fast::mul(S, n1));
+    P_ = Fast::fma(-S, m1, Fast::mul(e, m2));
+    // reverse
+    const float inv_sqrt_2pi = 0.398942280401432678f;
+    float gs = Fast::add(gc, gp);
+    float bS = Fast::fma(gc, n1, -Fast::mul(gp, m1));
+    float be = Fast::fma(gp, m2, -Fast::mul(gc, n2));
+    // N'(d) = phi(d); through N(d1), N(-d1): phi1*S*(gc+gp); through d2: -phi2*e*(gc+gp)
+    float phi1 = Fast::mul(inv_sqrt_2pi, g1), phi2 = Fast::mul(inv_sqrt_2pi, g2);
+    float bd2 = -Fast::mul(Fast::mul(phi2, e), gs);
+    float bd1 = Fast::fma(Fast::mul(phi1, S), gs, bd2);
+    float bvs = -bd2;
+    float bnum = Fast::mul(bd1, inv_vs);
+    bvs = Fast::fma(-bd1, Fast::mul(d1, inv_vs), bvs);
+    float ba = Fast::mul(bnum, T);
+    float bT = Fast::mul(bnum, a);
+    float bq = Fast::fdiv(bnum, q);
+    bS = Fast::fma(bq, Fast::fdiv(1.0f, K), bS);
+    float bK = -Fast::mul(bq, Fast::fdiv(q, K));
+    float bsig = Fast::mul(ba, sig);
+    float br = ba;
+    bsig = Fast::fma(bvs, sq, bsig);
+    float bsq = Fast::mul(bvs, sig);
+    bT = Fast::fma(bsq, Fast::fdiv(0.5f, sq), bT);
+    bK = Fast::fma(be, ert, bK);
+    float bert = Fast::mul(be, K);
+    float bx = Fast::mul(bert, ert);  // d/d(-rT)
+    br = Fast::fma(-bx, T, br);
+    bT = Fast::fma(-bx, r, bT);
+    dS = bS; dK = bK; dT = bT; dsig = bsig; dr = br;
+}
+
+__global__ void __launch_bounds__(256) k_bs_vjp(const float *__restrict__ S, const float *__restrict__ K,
+                                                const float *__restrict__ T, const float *__restrict__ sig,
+                                                float r, const float *__restrict__ gc,
+                                                const float *__restrict__ gp, float *__restrict__ C,
+                                                float *__restrict__ P, float *__restrict__ dS,
+                                                float *__restrict__ dK, float *__restrict__ dT,
+                                                float *__restrict__ dsig, float *__restrict__ dr,
+                                                int64_t n, int vec)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if (vec) {
+        const int64_t nv = n >> 2;
+        for (int64_t i = tid; i < nv; i += stride) {
+            float4 s = ld_stream((const float4 *)S + i), k = ld_stream((const float4 *)K + i),
+                   t = ld_stream((const float4 *)T + i), v = ld_stream((const float4 *)sig + i),
+                   a = ld_stream((const float4 *)gc + i), b = ld_stream((const float4 *)gp + i);
+            float4 c, p, o0, o1, o2, o3, o4;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float cj, pj, x0, x1, x2, x3, x4;
+                bs_vjp_option(get(s, j), get(k, j), get(t, j), get(v, j), r, get(a, j), get(b, j), cj, pj,
+                              x0, x1, x2, x3, x4);
+                set(c, j, cj); set(p, j, pj);
+                set(o0, j, x0); set(o1, j, x1); set(o2, j, x2); set(o3, j, x3); set(o4, j, x4);
+            }
+            st_stream((float4 *)C + i, c);
+            st_stream((float4 *)P + i, p);
+            st_stream((float4 *)dS + i, o0);
+            st_stream((float4 *)dK + i, o1);
+            st_stream((float4 *)dT + i, o2);
+            st_stream((float4 *)dsig + i, o3);
+            st_stream((float4 *)dr + i, o4);
+        }
+        done = nv << 2;
+    }
+    for (int64_t i = done + tid; i < n; i += stride)
+        bs_vjp_option(S[i], K[i], T[i], sig[i], r, gc[i], gp[i], C[i], P[i], dS[i], dK[i], dT[i], dsig[i],
+                      dr[i]);
+}
+
+// ---------------------------------------------------------- launchers ----
+template <class KERN>
+static int grid_for(KERN k, int64_t n)
+{
+    return persistent_blocks(k, 256, 0, 256 * 4, n);
+}
+
+nt2g_status launch_bs(const float *S, const float *K, const float *T, const float *sig, float sig_s, float r,
+                      float *call, float *put, int64_t n, int precision, cudaStream_t st)
+{
+    if (n == 0) return NT2G_OK;
+    int vec = aligned16(S) && aligned16(K) && aligned16(T) && aligned16(call) && aligned16(put) &&
+              (!sig || aligned16(sig));
+    if (precision == NT2G_PREC_NT2) {
+        if (sig) k_bs<Nt2, true><<<grid_for(k_bs<Nt2, true>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r, call, put, n, vec);
+        else k_bs<Nt2, false><<<grid_for(k_bs<Nt2, false>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r, call, put, n, vec);
+    } else {
+        if (sig) k_bs<Fast, true><<<grid_for(k_bs<Fast, true>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r, call, put, n, vec);
+        else k_bs<Fast, false><<<grid_for(k_bs<Fast, false>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r, call, put, n, vec);
+    }
+    NT2G_LAUNCH_CHECK("blackscholes launch");
+    return NT2G_OK;
+}
+
+nt2g_status launch_bs_demo(const float *S, const float *X, const float *T, const float *rt, float r, const float *vt,
+                           float v, float *R, int64_t n, int precision, cudaStream_t st)
+{
+    if (n == 0) return NT2G_OK;
+    int vec = aligned16(S) && aligned16(X) && aligned16(T) && aligned16(R) && (!rt || aligned16(rt)) &&
+              (!vt || aligned16(vt));
+#define NT2G_DEMO(PP, A, B)                                                                                   \
+    k_bs_demo<PP, A, B><<<grid_for(k_bs_demo<PP, A, B>, n), 256, 0, st>>>(S, X, T, rt, r, vt, v, R, n, vec)
+    if (precision == NT2G_PREC_NT2) {
+        if (rt && vt) NT2G_DEMO(Nt2, true, true);
+        else if (rt) NT2G_DEMO(Nt2, true, false);
+        else if (vt) NT2G_DEMO(Nt2, false, true);
+        else NT2G_DEMO(Nt2, false, false);
+    } else {
+        if (rt && vt) NT2G_DEMO(Fast, true, true);
+        else if (rt) NT2G_DEMO(Fast, true, false);
+        else if (vt) NT2G_DEMO(Fast, false, true);
+        else NT2G_DEMO(Fast, false, false);
+    }
+#undef NT2G_DEMO
+    NT2G_LAUNCH_CHECK("blackscholes demo launch");
+    return NT2G_OK;
+}
+
+nt2g_status launch_bs_vjp(const float *S, const float *K, const float *T, const float *sig, float r, const float *gc,
+                          const float *gp, float *C, float *P, float *dS, float *dK, float *dT, float *dsig,
+                          float *dr, int64_t n, cudaStream_t st)
+{
+    if (n == 0) return NT2G_OK;
+    const void *ps[] = {S, K, T, sig, gc, gp, C, P, dS, dK, dT, dsig, dr};
+    int vec = 1;
+    for (const void *p : ps) vec &= aligned16(p);
+    k_bs_vjp<<<grid_for(k_bs_vjp, n), 256, 0, st>>>(S, K, T, sig, r, gc, gp, C, P, dS, dK, dT, dsig, dr, n, vec);
+    NT2G_LAUNCH_CHECK("blackscholes vjp launch");
+    return NT2G_OK;
+}
+
+}  // namespace nt2g

@@ -1,0 +1,784 @@
+// nt2g_capi.cu -- the C ABI of libnt2gpu: argument validation, status codes,
+// the expression-program compiler, and the dispatch from a compiled program
+// to a fused kernel or to the generic interpreter.
+//
+// The program compiler takes the lowered form of an nt2 expression (SSA op
+// list, see nt2g.h), and
+//   1. validates opcodes, operand order, dtypes and slot use;
+//   2. forwards stores to later loads of the same table (the element-
+//      synchronous semantics of NT2's tie(), TABLE/core/functions/expr/
+//      tie.hpp:40-121: a child may read a table an earlier child wrote);
+//   3. removes common subexpressions and dead code;
+//   4. allocates interpreter registers (linear scan);
+//   5. binds the program to a fused kernel when it is structurally one of
+//      the named expressions (same DAG modulo slot numbering), recording which
+//      argument slot plays which role.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+#include <map>
+#include <new>
+#include <tuple>
+#include <vector>
+#include "nt2g_common.cuh"
+#include "nt2g_internal.h"
+
+namespace nt2g {
+
+// ------------------------------------------------------------------ errors --
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+nt2g_status cuda_status(cudaError_t e, const char *what)
+{
+    set_error("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    cudaGetLastError();  // clear a non-sticky error so the context stays usable
+    return NT2G_ERR_CUDA;
+}
+
+int device_sm_count()
+{
+    static thread_local int cache_dev = -1, cache_sms = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != cache_dev) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+        cache_dev = dev;
+        cache_sms = sms;
+    }
+    return cache_sms;
+}
+
+// ---------------------------------------------------------------- patterns --
+// P_NEG matches -x: a NEG node over its child, or -- when the child is a
+// scalar role -- a constant or scalar argument holding the negated value
+// (what C++ produces for -r*T with a float r: the negation happens before
+// the expression is built).
+enum PKind { P_OP, P_TABLE, P_SCALAR, P_TABSCAL, P_CVAL, P_NEG };
+
+struct PNode {
+    PKind kind;
+    int code, dtype;
+    int ch[3];
+    int role;
+    float cval;
+};
+
+struct Pattern {
+    FusedKernel kernel;
+    const char *name;
+    std::vector<PNode> nodes;
+    std::vector<std::pair<int, int>> outs;  // (node, output role)
+    int n_roles;
+};
+
+struct PB {
+    Pattern p;
+    int add(PNode n) { p.nodes.push_back(n); return (int)p.nodes.size() - 1; }
+    int op(int code, int a, int b = -1, int c = -1, int dt = NT2G_F32)
+    {
+        return add(PNode{P_OP, code, dt, {a, b, c}, -1, 0.f});
+    }
+    int table(int role, int dt = NT2G_F32) { return add(PNode{P_TABLE, 0, dt, {-1, -1, -1}, role, 0.f}); }
+    int scalar(int role) { return add(PNode{P_SCALAR, 0, NT2G_F32, {-1, -1, -1}, role, 0.f}); }
+    int tabscal(int role) { return add(PNode{P_TABSCAL, 0, NT2G_F32, {-1, -1, -1}, role, 0.f}); }
+    int cval(float v, int dt = NT2G_F32) { return add(PNode{P_CVAL, 0, dt, {-1, -1, -1}, -1, v}); }
+    int neg(int a) { return add(PNode{P_NEG, NT2G_OP_NEG, NT2G_F32, {a, -1, -1}, -1, 0.f}); }
+    void out(int node, int role) { p.outs.push_back({node, role}); }
+};
+
+static std::vector<Pattern> build_patterns()
+{
+    std::vector<Pattern> v;
+    {  // textbook Black-Scholes; roles S0 K1 T2 SIG3 R4 | CALL5 PUT6
+        PB b;
+        b.p.kernel = kBlackScholes; b.p.name = "blackscholes"; b.p.n_roles = 7;
+        int S = b.table(0), K = b.table(1), T = b.table(2), sig = b.tabscal(3), r = b.scalar(4);
+        int sq = b.op(NT2G_OP_SQRT, T);
+        int lq = b.op(NT2G_OP_LOG, b.op(NT2G_OP_DIV, S, K));
+        int a = b.op(NT2G_OP_FMA, b.op(NT2G_OP_SQR, sig), b.cval(0.5f), r);
+        int d1 = b.op(NT2G_OP_DIV, b.op(NT2G_OP_ADD, lq, b.op(NT2G_OP_MUL, a, T)), b.op(NT2G_OP_MUL, sig, sq));
+        int d2 = b.op(NT2G_OP_FNMS, sig, sq, d1);
+        int e = b.op(NT2G_OP_MUL, K, b.op(NT2G_OP_EXP, b.op(NT2G_OP_MUL, b.neg(r), T)));
+        int call = b.op(NT2G_OP_FNMS, e, b.op(NT2G_OP_NORMCDF, d2), b.op(NT2G_OP_MUL, S, b.op(NT2G_OP_NORMCDF, d1)));
+        int put = b.op(NT2G_OP_FNMS, S, b.op(NT2G_OP_NORMCDF, b.neg(d1)),
+                       b.op(NT2G_OP_MUL, e, b.op(NT2G_OP_NORMCDF, b.neg(d2))));
+        b.out(call, 5);
+        b.out(put, 6);
+        v.push_back(b.p);
+    }
+    {  // NT2 demo Black-Scholes; roles S0 X1 T2 R3 V4 | OUT5
+        PB b;
+        b.p.kernel = kBlackScholesDemo; b.p.name = "blackscholes_demo"; b.p.n_roles = 6;
+        int S = b.table(0), X = b.table(1), T = b.table(2), r = b.tabscal(3), va = b.tabscal(4);
+        int da = b.op(NT2G_OP_SQRT, T);
+        int d1 = b.op(NT2G_OP_ADD, b.op(NT2G_OP_LOG, b.op(NT2G_OP_DIV, S, X)),
+                      b.op(NT2G_OP_DIV, b.op(NT2G_OP_MUL, b.op(NT2G_OP_FMA, b.op(NT2G_OP_SQR, va), b.cval(0.5f), r), T),
+                           b.op(NT2G_OP_MUL, va, da)));
+        int d2 = b.op(NT2G_OP_FNMS, va, da, d1);
+        int R = b.op(NT2G_OP_FNMS, b.op(NT2G_OP_MUL, X, b.op(NT2G_OP_EXP, b.op(NT2G_OP_MUL, b.neg(r), T))),
+                     b.op(NT2G_OP_FASTNORMCDF, d2), b.op(NT2G_OP_MUL, S, b.op(NT2G_OP_FASTNORMCDF, d1)));
+        b.out(R, 5);
+        v.push_back(b.p);
+    }
+    {  // saxpy; roles A0 X1 Y2 | OUT3
+        PB b;
+        b.p.kernel = kSaxpy; b.p.name = "saxpy"; b.p.n_roles = 4;
+        int A = b.scalar(0), X = b.table(1), Y = b.table(2);
+        b.out(b.op(NT2G_OP_ADD, b.op(NT2G_OP_MUL, A, X), Y), 3);
+        v.push_back(b.p);
+    }
+    {  // expr3; roles x0 y1 z2 | OUT3
+        PB b;
+        b.p.kernel = kExpr3; b.p.name = "expr3"; b.p.n_roles = 4;
+        int x = b.table(0), y = b.table(1), z = b.table(2);
+        int t = b.op(NT2G_OP_MUL, b.op(NT2G_OP_EXP, b.op(NT2G_OP_NEG, b.op(NT2G_OP_SQR, x))),
+                     b.op(NT2G_OP_SQRT, b.op(NT2G_OP_ABS, y)));
+        b.out(b.op(NT2G_OP_ADD, t, b.op(NT2G_OP_LOG1P, b.op(NT2G_OP_ABS, z))), 3);
+        v.push_back(b.p);
+    }
+    {  // rgb2yuv; roles r0 g1 b2 | Y3 U4 V5
+        PB b;
+        b.p.kernel = kRgb2Yuv; b.p.name = "rgb2yuv"; b.p.n_roles = 6;
+        int r = b.table(0), g = b.table(1), bl = b.table(2);
+        int y = b.op(NT2G_OP_ADD, b.op(NT2G_OP_ADD, b.op(NT2G_OP_MUL, b.cval(0.299f), r), b.op(NT2G_OP_MUL, b.cval(0.587f), g)),
+                     b.op(NT2G_OP_MUL, b.cval(0.114f), bl));
+        b.out(y, 3);
+        b.out(b.op(NT2G_OP_MUL, b.cval(0.492f), b.op(NT2G_OP_SUB, bl, y)), 4);
+        b.out(b.op(NT2G_OP_MUL, b.cval(0.877f), b.op(NT2G_OP_SUB, r, y)), 5);
+        v.push_back(b.p);
+    }
+    {  // sigma-delta; roles frame0 bkg1 var2 | BKG3 VAR4 LABEL5
+        PB b;
+        const int U = NT2G_U8;
+        b.p.kernel = kSigmaDelta; b.p.name = "sigmadelta"; b.p.n_roles = 6;
+        int f = b.table(0, U), bk = b.table(1, U), va = b.table(2, U);
+        int nb = b.op(NT2G_OP_SELINC, b.op(NT2G_OP_LT, bk, f, -1, U), b.op(NT2G_OP_SELDEC, b.op(NT2G_OP_GT, bk, f, -1, U), bk, -1, U), -1, U);
+        int d = b.op(NT2G_OP_SUB, b.op(NT2G_OP_MAX, nb, f, -1, U), b.op(NT2G_OP_MIN, nb, f, -1, U), -1, U);
+        int m = b.op(NT2G_OP_ADDS, b.op(NT2G_OP_ADDS, d, d, -1, U), d, -1, U);
+        int nv = b.op(NT2G_OP_IF_ELSE, b.op(NT2G_OP_NE, d, b.cval(0.f, U), -1, U),
+                      b.op(NT2G_OP_SELINC, b.op(NT2G_OP_LT, va, m, -1, U), b.op(NT2G_OP_SELDEC, b.op(NT2G_OP_GT, va, m, -1, U), va, -1, U), -1, U),
+                      va, U);
+        int lab = b.op(NT2G_OP_IF_ZERO_ELSE_ONE, b.op(NT2G_OP_LT, d, nv, -1, U), -1, -1, U);
+        b.out(nb, 3);
+        b.out(nv, 4);
+        b.out(lab, 5);
+        v.push_back(b.p);
+    }
+    return v;
+}
+
+static const std::vector<Pattern> &patterns()
+{
+    static const std::vector<Pattern> p = build_patterns();
+    return p;
+}
+
+// A role resolves to a table slot, a constant, or a scalar slot (possibly
+// holding the negated value).
+struct RoleBind {
+    int kind = -1;  // 0 table slot, 1 const, 2 scalar slot, 3 negated scalar slot
+    int slot = -1;
+    float value = 0.f;
+};
+
+struct DeferredConst {
+    int slot;
+    float value;
+};
+
+}  // namespace nt2g
+
+using namespace nt2g;
+
+struct nt2g_program {
+    std::vector<nt2g_op> ops;  // canonical SSA
+    std::vector<uint8_t> logical;
+    int n_slots = 0;
+    std::vector<int> slot_use;    // bit 1 load, 2 store, 4 scalar
+    std::vector<int> slot_dtype;
+    DProgram dprog{};
+    int kernel = kGeneric;
+    const char *kernel_name = "generic";
+    std::vector<RoleBind> roles;
+    std::vector<DeferredConst> deferred;
+};
+
+namespace nt2g {
+
+static bool is_value_op(int code) { return code != NT2G_OP_STORE; }
+
+static int n_operands(int code)
+{
+    switch (code) {
+    case NT2G_OP_LOAD: case NT2G_OP_SCALAR: case NT2G_OP_CONST: return 0;
+    case NT2G_OP_STORE: return 1;
+    case NT2G_OP_NEG: case NT2G_OP_ABS: case NT2G_OP_SQR: case NT2G_OP_SQRT: case NT2G_OP_REC:
+    case NT2G_OP_EXP: case NT2G_OP_LOG: case NT2G_OP_LOG1P: case NT2G_OP_ERFC: case NT2G_OP_NORMCDF:
+    case NT2G_OP_FASTNORMCDF: case NT2G_OP_IF_ZERO_ELSE_ONE: return 1;
+    case NT2G_OP_ADD: case NT2G_OP_SUB: case NT2G_OP_MUL: case NT2G_OP_DIV: case NT2G_OP_MIN: case NT2G_OP_MAX:
+    case NT2G_OP_LT: case NT2G_OP_GT: case NT2G_OP_LE: case NT2G_OP_GE: case NT2G_OP_EQ: case NT2G_OP_NE:
+    case NT2G_OP_SELINC: case NT2G_OP_SELDEC: case NT2G_OP_ADDS: return 2;
+    case NT2G_OP_FMA: case NT2G_OP_FNMS: case NT2G_OP_IF_ELSE: return 3;
+    default: return -1;
+    }
+}
+
+static bool float_only(int code)
+{
+    switch (code) {
+    case NT2G_OP_DIV: case NT2G_OP_SQRT: case NT2G_OP_REC: case NT2G_OP_FMA: case NT2G_OP_FNMS:
+    case NT2G_OP_EXP: case NT2G_OP_LOG: case NT2G_OP_LOG1P: case NT2G_OP_ERFC: case NT2G_OP_NORMCDF:
+    case NT2G_OP_FASTNORMCDF: return true;
+    default: return false;
+    }
+}
+
+static bool is_compare(int code) { return code >= NT2G_OP_LT && code <= NT2G_OP_NE; }
+
+// Structural match of program value v against pattern node pn.
+struct Matcher {
+    const nt2g_program &prog;
+    const Pattern &pat;
+    std::vector<int> pmap;  // pattern node -> program value
+    std::vector<RoleBind> roles;
+    std::vector<DeferredConst> deferred;
+
+    Matcher(const nt2g_program &p, const Pattern &q)
+        : prog(p), pat(q), pmap(q.nodes.size(), -1), roles(q.n_roles) {}
+
+    bool bind_role(int role, RoleBind rb)
+    {
+        RoleBind &r = roles[role];
+        if (r.kind < 0) { r = rb; return true; }
+        return r.kind == rb.kind && r.slot == rb.slot && (r.kind != 1 || r.value == rb.value);
+    }
+
+    bool match(int v, int pn)
+    {
+        if (pmap[pn] >= 0) return pmap[pn] == v;
+        const PNode &n = pat.nodes[pn];
+        const nt2g_op &o = prog.ops[v];
+        bool ok = false;
+        switch (n.kind) {
+        case P_TABLE:
+            ok = o.code == NT2G_OP_LOAD && o.dtype == n.dtype && bind_role(n.role, RoleBind{0, o.a, 0.f});
+            break;
+        case P_SCALAR:
+            ok = (o.code == NT2G_OP_CONST && o.dtype == NT2G_F32 && bind_role(n.role, RoleBind{1, -1, o.imm})) ||
+                 (o.code == NT2G_OP_SCALAR && o.dtype == NT2G_F32 && bind_role(n.role, RoleBind{2, o.a, 0.f}));
+            break;
+        case P_TABSCAL:
+            ok = (o.code == NT2G_OP_LOAD && o.dtype == NT2G_F32 && bind_role(n.role, RoleBind{0, o.a, 0.f})) ||
+                 (o.code == NT2G_OP_CONST && o.dtype == NT2G_F32 && bind_role(n.role, RoleBind{1, -1, o.imm})) ||
+                 (o.code == NT2G_OP_SCALAR && o.dtype == NT2G_F32 && bind_role(n.role, RoleBind{2, o.a, 0.f}));
+            break;
+        case P_CVAL:
+            if (o.code == NT2G_OP_CONST && o.dtype == n.dtype) ok = o.imm == n.cval;
+            else if (o.code == NT2G_OP_SCALAR && o.dtype == n.dtype) {
+                deferred.push_back(DeferredConst{o.a, n.cval});
+                ok = true;
+            }
+            break;
+        case P_NEG: {
+            const PNode &c = pat.nodes[n.ch[0]];
+            const bool scalar_role = c.kind == P_SCALAR || c.kind == P_TABSCAL;
+            if (o.code == NT2G_OP_NEG && o.dtype == NT2G_F32) ok = match(o.a, n.ch[0]);
+            else if (scalar_role && o.code == NT2G_OP_CONST && o.dtype == NT2G_F32)
+                ok = bind_role(c.role, RoleBind{1, -1, -o.imm});
+            else if (scalar_role && o.code == NT2G_OP_SCALAR && o.dtype == NT2G_F32)
+                ok = bind_role(c.role, RoleBind{3, o.a, 0.f});
+            break;
+        }
+        case P_OP:
+            if (o.code != n.code || o.dtype != n.dtype) break;
+            ok = true;
+            for (int k = 0; k < n_operands(n.code) && ok; ++k) {
+                int pv = k == 0 ? o.a : k == 1 ? o.b : o.c;
+                ok = match(pv, n.ch[k]);
+            }
+            break;
+        }
+        if (ok) pmap[pn] = v;
+        return ok;
+    }
+};
+
+static bool try_bind(nt2g_program &p, const Pattern &pat)
+{
+    // stores of the program, in order
+    std::vector<int> stores;
+    for (int i = 0; i < (int)p.ops.size(); ++i)
+        if (p.ops[i].code == NT2G_OP_STORE) stores.push_back(i);
+    if (stores.size() != pat.outs.size()) return false;
+    Matcher m(p, pat);
+    for (size_t k = 0; k < stores.size(); ++k) {
+        const nt2g_op &s = p.ops[stores[k]];
+        if (!m.bind_role(pat.outs[k].second, RoleBind{0, s.b, 0.f})) return false;
+        if (!m.match(s.a, pat.outs[k].first)) return false;
+    }
+    for (const RoleBind &r : m.roles)
+        if (r.kind < 0) return false;
+    p.kernel = pat.kernel;
+    p.kernel_name = pat.name;
+    p.roles = m.roles;
+    p.deferred = m.deferred;
+    return true;
+}
+
+}  // namespace nt2g
+
+// ------------------------------------------------------------------ C ABI --
+extern "C" const char *nt2g_last_error(void) { return g_err; }
+extern "C" int nt2g_abi_version(void) { return NT2G_ABI_VERSION; }
+
+extern "C" nt2g_status nt2g_program_create(const nt2g_op *ops, int32_t n_ops, int32_t n_slots, nt2g_program **out)
+{
+    NT2G_CHECK_ARG(out != nullptr, "nt2g_program_create: out is NULL");
+    *out = nullptr;
+    NT2G_CHECK_ARG(ops != nullptr && n_ops > 0, "nt2g_program_create: empty program");
+    NT2G_CHECK_ARG(n_slots > 0 && n_slots <= kMaxSlots, "nt2g_program_create: n_slots %d outside [1,%d]", n_slots,
+                   kMaxSlots);
+    std::vector<int> slot_use(n_slots, 0), slot_dtype(n_slots, -1);
+    std::vector<uint8_t> logical(n_ops, 0);
+    // 1. validation
+    for (int i = 0; i < n_ops; ++i) {
+        const nt2g_op &o = ops[i];
+        int na = n_operands(o.code);
+        NT2G_CHECK_ARG(na >= 0, "op %d: unknown opcode %d", i, o.code);
+        NT2G_CHECK_ARG(o.dtype == NT2G_F32 || o.dtype == NT2G_U8, "op %d: unknown dtype %d", i, o.dtype);
+        if (o.dtype == NT2G_U8 && float_only(o.code)) {
+            set_error("op %d: opcode %d is defined for float tables only", i, o.code);
+            return NT2G_ERR_UNSUPPORTED;
+        }
+        if (o.code == NT2G_OP_ADDS && o.dtype != NT2G_U8) {
+            set_error("op %d: saturating add is defined for uint8 tables only", i);
+            return NT2G_ERR_UNSUPPORTED;
+        }
+        const int32_t opnd[3] = {o.a, o.b, o.c};
+        if (o.code == NT2G_OP_LOAD || o.code == NT2G_OP_SCALAR) {
+            NT2G_CHECK_ARG(o.a >= 0 && o.a < n_slots, "op %d: slot %d outside [0,%d)", i, o.a, n_slots);
+            int use = o.code == NT2G_OP_LOAD ? 1 : 4;
+            NT2G_CHECK_ARG(!((slot_use[o.a] | use) & 4) || (slot_use[o.a] | use) == 4,
+                           "op %d: slot %d used both as a table and as a scalar", i, o.a);
+            NT2G_CHECK_ARG(slot_dtype[o.a] < 0 || slot_dtype[o.a] == o.dtype, "op %d: slot %d dtype mismatch", i, o.a);
+            slot_use[o.a] |= use;
+            slot_dtype[o.a] = o.dtype;
+            continue;
+        }
+        if (o.code == NT2G_OP_STORE) {
+            NT2G_CHECK_ARG(o.a >= 0 && o.a < i && is_value_op(ops[o.a].code), "op %d: store of invalid value %d", i, o.a);
+            NT2G_CHECK_ARG(o.b >= 0 && o.b < n_slots, "op %d: slot %d outside [0,%d)", i, o.b, n_slots);
+            NT2G_CHECK_ARG(!(slot_use[o.b] & 4), "op %d: store into scalar slot %d", i, o.b);
+            NT2G_CHECK_ARG(slot_dtype[o.b] < 0 || slot_dtype[o.b] == o.dtype, "op %d: slot %d dtype mismatch", i, o.b);
+            NT2G_CHECK_ARG(logical[o.a] || ops[o.a].dtype == o.dtype, "op %d: stored value dtype %d into dtype %d", i,
+                           ops[o.a].dtype, o.dtype);
+            slot_use[o.b] |= 2;
+            slot_dtype[o.b] = o.dtype;
+            continue;
+        }
+        for (int k = 0; k < na; ++k) {
+            NT2G_CHECK_ARG(opnd[k] >= 0 && opnd[k] < i && is_value_op(ops[opnd[k]].code),
+                           "op %d: operand %d refers to %d", i, k, opnd[k]);
+        }
+        bool cond_first = o.code == NT2G_OP_IF_ELSE || o.code == NT2G_OP_SELINC || o.code == NT2G_OP_SELDEC ||
+                          o.code == NT2G_OP_IF_ZERO_ELSE_ONE;
+        if (cond_first) NT2G_CHECK_ARG(logical[o.a], "op %d: condition operand is not a comparison result", i);
+        for (int k = cond_first ? 1 : 0; k < na; ++k)
+            NT2G_CHECK_ARG(!logical[opnd[k]] || o.code == NT2G_OP_IF_ELSE,
+                           "op %d: logical operand %d used as a number", i, k);
+        for (int k = cond_first ? 1 : 0; k < na; ++k)
+            NT2G_CHECK_ARG(logical[opnd[k]] || ops[opnd[k]].dtype == o.dtype, "op %d: operand %d dtype mismatch", i, k);
+        if (is_compare(o.code)) logical[i] = 1;
+        if (o.code == NT2G_OP_IF_ELSE) {
+            NT2G_CHECK_ARG(logical[o.b] == logical[o.c], "op %d: if_else branches of different kinds", i);
+            logical[i] = logical[o.b];
+        }
+    }
+    // 2-3. forwarding, CSE, then DCE
+    std::vector<int> remap(n_ops, -1), last_store(n_slots, -1);
+    std::vector<nt2g_op> cse;
+    std::vector<uint8_t> cse_logical;
+    std::map<std::tuple<int, int, int, int, int, uint32_t>, int> seen;
+    for (int i = 0; i < n_ops; ++i) {
+        nt2g_op o = ops[i];
+        if (o.code == NT2G_OP_LOAD && last_store[o.a] >= 0) {  // forward the stored value
+            remap[i] = last_store[o.a];
+            continue;
+        }
+        int na = n_operands(o.code);
+        if (o.code == NT2G_OP_STORE) {
+            o.a = remap[o.a];
+            last_store[o.b] = o.a;
+            cse.push_back(o);
+            cse_logical.push_back(logical[i]);
+            continue;
+        }
+        if (na >= 1 && o.code != NT2G_OP_LOAD && o.code != NT2G_OP_SCALAR) o.a = remap[o.a];
+        if (na >= 2) o.b = remap[o.b];
+        if (na >= 3) o.c = remap[o.c];
+        if (na < 1 && o.code == NT2G_OP_CONST) o.a = -1;
+        if (na < 2) o.b = -1;
+        if (na < 3) o.c = -1;
+        uint32_t immbits = 0;
+        if (o.code == NT2G_OP_CONST) memcpy(&immbits, &o.imm, 4);
+        else o.imm = 0.f;
+        auto key = std::make_tuple((int)o.code, (int)o.dtype, o.a, o.b, o.c, immbits);
+        auto it = seen.find(key);
+        if (it != seen.end()) { remap[i] = it->second; continue; }
+        remap[i] = (int)cse.size();
+        seen[key] = remap[i];
+        cse.push_back(o);
+        cse_logical.push_back(logical[i]);
+    }
+    // keep only the last store to each slot; mark live values
+    std::vector<uint8_t> live(cse.size(), 0);
+    std::vector<int> final_store(n_slots, -1);
+    for (int i = 0; i < (int)cse.size(); ++i)
+        if (cse[i].code == NT2G_OP_STORE) final_store[cse[i].b] = i;
+    for (int i = (int)cse.size() - 1; i >= 0; --i) {
+        const nt2g_op &o = cse[i];
+        if (o.code == NT2G_OP_STORE) {
+            if (final_store[o.b] != i) continue;
+            live[i] = 1;
+            live[o.a] = 1;
+            continue;
+        }
+        if (!live[i]) continue;
+        int na = n_operands(o.code);
+        if (o.code == NT2G_OP_LOAD || o.code == NT2G_OP_SCALAR || o.code == NT2G_OP_CONST) continue;
+        if (na >= 1) live[o.a] = 1;
+        if (na >= 2) live[o.b] = 1;
+        if (na >= 3) live[o.c] = 1;
+    }
+    nt2g_program *p = new (std::nothrow) nt2g_program();
+    if (!p) { set_error("nt2g_program_create: out of host memory"); return NT2G_ERR_NOMEM; }
+    std::vector<int> idx(cse.size(), -1);
+    for (int i = 0; i < (int)cse.size(); ++i) {
+        if (!live[i]) continue;
+        nt2g_op o = cse[i];
+        int na = n_operands(o.code);
+        bool slot_op = o.code == NT2G_OP_LOAD || o.code == NT2G_OP_SCALAR;
+        if (!slot_op && o.code != NT2G_OP_CONST) {
+            if (na >= 1) o.a = idx[o.a];
+            if (o.code != NT2G_OP_STORE && na >= 2) o.b = idx[o.b];
+            if (na >= 3) o.c = idx[o.c];
+        }
+        idx[i] = (int)p->ops.size();
+        p->ops.push_back(o);
+        p->logical.push_back(cse_logical[i]);
+    }
+    p->n_slots = n_slots;
+    p->slot_use = slot_use;
+    p->slot_dtype = slot_dtype;
+    bool has_store = false;
+    for (const nt2g_op &o : p->ops) has_store |= o.code == NT2G_OP_STORE;
+    if (!has_store) {
+        delete p;
+        set_error("nt2g_program_create: the program stores nothing");
+        return NT2G_ERR_INVALID;
+    }
+    // 4. register allocation for the interpreter
+    const int n = (int)p->ops.size();
+    if (n > kMaxInstr) {
+        delete p;
+        set_error("nt2g_program_create: %d instructions after simplification exceed %d", n, kMaxInstr);
+        return NT2G_ERR_UNSUPPORTED;
+    }
+    std::vector<int> last_use(n, -1), reg(n, -1);
+    for (int i = 0; i < n; ++i) {
+        const nt2g_op &o = p->ops[i];
+        if (o.code == NT2G_OP_LOAD || o.code == NT2G_OP_SCALAR || o.code == NT2G_OP_CONST) continue;
+        int na = n_operands(o.code);
+        if (na >= 1) last_use[o.a] = i;
+        if (na >= 2 && o.code != NT2G_OP_STORE) last_use[o.b] = i;
+        if (na >= 3) last_use[o.c] = i;
+    }
+    std::vector<int> free_regs;
+    int n_regs = 0;
+    DProgram &dp = p->dprog;
+    dp.n = n;
+    for (int i = 0; i < n; ++i) {
+        const nt2g_op &o = p->ops[i];
+        DInstr &d = dp.ins[i];
+        d = DInstr{};
+        d.op = (uint8_t)o.code;
+        d.dt = (uint8_t)o.dtype;
+        d.imm = o.imm;
+        int na = n_operands(o.code);
+        bool slot_op = o.code == NT2G_OP_LOAD || o.code == NT2G_OP_SCALAR;
+        if (slot_op) d.a = (uint8_t)o.a;
+        else if (o.code == NT2G_OP_STORE) {
+            d.a = (uint8_t)reg[o.a];
+            d.b = (uint8_t)o.b;
+            d.logical = p->logical[o.a];
+        } else if (o.code != NT2G_OP_CONST) {
+            if (na >= 1) d.a = (uint8_t)reg[o.a];
+            if (na >= 2) d.b = (uint8_t)reg[o.b];
+            if (na >= 3) d.c = (uint8_t)reg[o.c];
+            // comparisons carry the compared dtype; conditions are the logical operand
+        }
+        // release operands whose last use is here (an operand register may be
+        // reused as the destination: the interpreter reads element j of every
+        // operand before writing element j of the result)
+        if (!slot_op && o.code != NT2G_OP_CONST) {
+            int opv[3] = {o.a, o.code == NT2G_OP_STORE ? -1 : o.b, o.c};
+            for (int k = 0; k < (na < 3 ? na : 3); ++k) {
+                int v = opv[k];
+                if (v >= 0 && last_use[v] == i) {
+                    bool dup = false;
+                    for (int q = 0; q < k; ++q) dup |= opv[q] == v;
+                    if (!dup) free_regs.push_back(reg[v]);
+                }
+            }
+        }
+        if (o.code != NT2G_OP_STORE) {
+            if (last_use[i] < 0) { reg[i] = 0; d.dst = 0; continue; }  // unused value (cannot happen after DCE)
+            int r;
+            if (!free_regs.empty()) {
+                // lowest free register keeps the file compact
+                size_t best = 0;
+                for (size_t q = 1; q < free_regs.size(); ++q)
+                    if (free_regs[q] < free_regs[best]) best = q;
+                r = free_regs[best];
+                free_regs.erase(free_regs.begin() + best);
+            } else {
+                r = n_regs++;
+            }
+            reg[i] = r;
+            d.dst = (uint8_t)r;
+        }
+    }
+    dp.n_regs = n_regs;
+    if (n_regs > kMaxRegs) {
+        delete p;
+        set_error("nt2g_program_create: %d live values exceed the %d interpreter registers", n_regs, kMaxRegs);
+        return NT2G_ERR_UNSUPPORTED;
+    }
+    // 5. fused-kernel binding
+    for (const Pattern &pat : patterns())
+        if (try_bind(*p, pat)) break;
+    *out = p;
+    return NT2G_OK;
+}
+
+extern "C" nt2g_status nt2g_program_info_get(const nt2g_program *p, nt2g_program_info *info)
+{
+    NT2G_CHECK_ARG(p && info, "nt2g_program_info_get: NULL argument");
+    memset(info, 0, sizeof *info);
+    info->kernel = p->kernel;
+    info->n_ops = (int32_t)p->ops.size();
+    info->n_regs = p->dprog.n_regs;
+    info->n_slots = p->n_slots;
+    snprintf(info->kernel_name, sizeof info->kernel_name, "%s", p->kernel_name);
+    return NT2G_OK;
+}
+
+extern "C" void nt2g_program_destroy(nt2g_program *p) { delete p; }
+
+static size_t dtype_size(int dt) { return dt == NT2G_U8 ? 1 : 4; }
+
+extern "C" nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t offset,
+                                 int64_t count, int32_t precision, int32_t force_generic, void *stream)
+{
+    NT2G_CHECK_ARG(p != nullptr, "nt2g_eval: NULL program");
+    NT2G_CHECK_ARG(n_args >= p->n_slots && (args != nullptr || p->n_slots == 0),
+                   "nt2g_eval: %d arguments for %d slots", n_args, p->n_slots);
+    NT2G_CHECK_ARG(offset >= 0 && count >= 0, "nt2g_eval: negative range (%lld, %lld)", (long long)offset,
+                   (long long)count);
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_eval: precision %d", precision);
+    cudaStream_t st = (cudaStream_t)stream;
+    DArgs da{};
+    for (int s = 0; s < p->n_slots; ++s) {
+        const int use = p->slot_use[s];
+        if (!use) continue;
+        const nt2g_arg &a = args[s];
+        if (use & 4) {
+            NT2G_CHECK_ARG(a.kind == 1, "nt2g_eval: slot %d must be a scalar", s);
+            da.scal[s] = (float)a.scalar;
+            double u = a.scalar;
+            da.scal_u8[s] = (uint32_t)(u < 0 ? 0 : u > 255 ? 255 : u);
+            da.dtype[s] = p->slot_dtype[s];
+        } else {
+            NT2G_CHECK_ARG(a.kind == 0, "nt2g_eval: slot %d must be a table", s);
+            NT2G_CHECK_ARG(a.dtype == p->slot_dtype[s], "nt2g_eval: slot %d has dtype %d, program expects %d", s,
+                           a.dtype, p->slot_dtype[s]);
+            NT2G_CHECK_ARG(a.ptr != nullptr || count == 0, "nt2g_eval: slot %d table pointer is NULL", s);
+            da.ptr[s] = a.ptr ? (char *)a.ptr + offset * dtype_size(a.dtype) : nullptr;
+            da.dtype[s] = a.dtype;
+        }
+    }
+    if (count == 0) return NT2G_OK;
+    int kernel = force_generic ? kGeneric : p->kernel;
+    for (const DeferredConst &dc : p->deferred)
+        if ((float)args[dc.slot].scalar != dc.value) kernel = kGeneric;
+    if (kernel != kGeneric) {
+        auto T = [&](int role) -> float * { return (float *)da.ptr[p->roles[role].slot]; };
+        auto U8 = [&](int role) -> uint8_t * { return (uint8_t *)da.ptr[p->roles[role].slot]; };
+        auto V = [&](int role) -> float {
+            const RoleBind &r = p->roles[role];
+            return r.kind == 1 ? r.value : r.kind == 3 ? -da.scal[r.slot] : da.scal[r.slot];
+        };
+        auto TV = [&](int role) -> float * { return p->roles[role].kind == 0 ? T(role) : nullptr; };
+        switch (kernel) {
+        case kBlackScholes:
+            return launch_bs(T(0), T(1), T(2), TV(3), TV(3) ? 0.f : V(3), V(4), T(5), T(6), count, precision, st);
+        case kBlackScholesDemo:
+            return launch_bs_demo(T(0), T(1), T(2), TV(3), TV(3) ? 0.f : V(3), TV(4), TV(4) ? 0.f : V(4), T(5), count,
+                                  precision, st);
+        case kSaxpy: return launch_saxpy(V(0), T(1), T(2), T(3), count, st);
+        case kExpr3: return launch_expr3(T(0), T(1), T(2), T(3), count, precision, st);
+        case kRgb2Yuv: return launch_rgb2yuv(T(0), T(1), T(2), T(3), T(4), T(5), count, st);
+        case kSigmaDelta: {
+            // the fused kernel updates bkg/var in place: it needs the output
+            // roles to be the same tables as the inputs
+            if (p->roles[3].slot == p->roles[1].slot && p->roles[4].slot == p->roles[2].slot)
+                return launch_sigmadelta(U8(0), U8(1), U8(2), U8(5), count, st);
+            break;
+        }
+        default: break;
+        }
+    }
+    return launch_interp(p->dprog, da, count, precision, st);
+}
+
+// ------------------------------------------------------- direct kernels ----
+#define NT2G_REQ(ptr) NT2G_CHECK_ARG((ptr) != nullptr || n == 0, "%s: " #ptr " is NULL", __func__)
+#define NT2G_REQ_N() NT2G_CHECK_ARG(n >= 0, "%s: negative size %lld", __func__, (long long)n)
+#define NT2G_REQ_PREC()                                                                                        \
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "%s: precision %d", __func__,     \
+                   precision)
+
+extern "C" nt2g_status nt2g_blackscholes_f32(const float *S, const float *K, const float *T, const float *sigma,
+                                             float sigma_s, float r, float *call, float *put, int64_t n,
+                                             int32_t precision, void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(S); NT2G_REQ(K); NT2G_REQ(T); NT2G_REQ(call); NT2G_REQ(put); NT2G_REQ_PREC();
+    return launch_bs(S, K, T, sigma, sigma_s, r, call, put, n, precision, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_blackscholes_demo_f32(const float *S, const float *X, const float *T, const float *r_t,
+                                                  float r, const float *v_t, float v, float *R, int64_t n,
+                                                  int32_t precision, void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(S); NT2G_REQ(X); NT2G_REQ(T); NT2G_REQ(R); NT2G_REQ_PREC();
+    return launch_bs_demo(S, X, T, r_t, r, v_t, v, R, n, precision, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_blackscholes_vjp_f32(const float *S, const float *K, const float *T, const float *sigma,
+                                                 float r, const float *gc, const float *gp, float *call, float *put,
+                                                 float *dS, float *dK, float *dT, float *dsigma, float *dr, int64_t n,
+                                                 void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(S); NT2G_REQ(K); NT2G_REQ(T); NT2G_REQ(sigma); NT2G_REQ(gc); NT2G_REQ(gp);
+    NT2G_REQ(call); NT2G_REQ(put); NT2G_REQ(dS); NT2G_REQ(dK); NT2G_REQ(dT); NT2G_REQ(dsigma); NT2G_REQ(dr);
+    return launch_bs_vjp(S, K, T, sigma, r, gc, gp, call, put, dS, dK, dT, dsigma, dr, n, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_saxpy_f32(float alpha, const float *X, float *Y, int64_t n, void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(X); NT2G_REQ(Y);
+    return launch_saxpy(alpha, X, Y, Y, n, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_expr3_f32(const float *x, const float *y, const float *z, float *out, int64_t n,
+                                      int32_t precision, void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(x); NT2G_REQ(y); NT2G_REQ(z); NT2G_REQ(out); NT2G_REQ_PREC();
+    return launch_expr3(x, y, z, out, n, precision, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_rgb2yuv_f32(const float *r, const float *g, const float *b, float *y, float *u, float *v,
+                                        int64_t n, void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(r); NT2G_REQ(g); NT2G_REQ(b); NT2G_REQ(y); NT2G_REQ(u); NT2G_REQ(v);
+    return launch_rgb2yuv(r, g, b, y, u, v, n, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_sigmadelta_u8(const uint8_t *frame, uint8_t *bkg, uint8_t *var, uint8_t *label, int64_t n,
+                                          void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(frame); NT2G_REQ(bkg); NT2G_REQ(var); NT2G_REQ(label);
+    return launch_sigmadelta(frame, bkg, var, label, n, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8_t *var, uint8_t *labels,
+                                                 int64_t n, int32_t n_frames, void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(frames); NT2G_REQ(bkg); NT2G_REQ(var); NT2G_REQ(labels);
+    NT2G_CHECK_ARG(n_frames >= 0, "nt2g_sigmadelta_frames_u8: negative frame count %d", n_frames);
+    return launch_sigmadelta_frames(frames, bkg, var, labels, n, n_frames, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision, void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(x); NT2G_REQ(y); NT2G_REQ_PREC();
+    NT2G_CHECK_ARG(fn >= 0 && fn <= 7, "nt2g_map_f32: unknown function %d", fn);
+    return launch_map(fn, x, y, n, precision, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_reduce_workspace_size(int64_t n, size_t *bytes)
+{
+    NT2G_CHECK_ARG(bytes != nullptr, "nt2g_reduce_workspace_size: bytes is NULL");
+    NT2G_REQ_N();
+    return reduce_workspace_bytes(bytes);
+}
+
+extern "C" nt2g_status nt2g_reduce_f32(const float *x, const float *y, int64_t n, void *workspace,
+                                       size_t workspace_bytes, double *out64, float *out32, void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(x);
+    NT2G_CHECK_ARG(out64 != nullptr, "nt2g_reduce_f32: out64 is NULL");
+    size_t need = 0;
+    reduce_workspace_bytes(&need);
+    NT2G_CHECK_ARG(workspace != nullptr && workspace_bytes >= need,
+                   "nt2g_reduce_f32: workspace of %zu bytes, %zu needed", workspace_bytes, need);
+    NT2G_CHECK_ARG(((uintptr_t)workspace & 15u) == 0, "nt2g_reduce_f32: workspace not 16-byte aligned");
+    return launch_reduce(x, y, n, workspace, out64, out32, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------- memory ----
+extern "C" nt2g_status nt2g_device_alloc(size_t bytes, void **ptr)
+{
+    NT2G_CHECK_ARG(ptr != nullptr, "nt2g_device_alloc: ptr is NULL");
+    *ptr = nullptr;
+    if (bytes == 0) return NT2G_OK;
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        set_error("nt2g_device_alloc: %zu bytes: out of device memory", bytes);
+        return NT2G_ERR_NOMEM;
+    }
+    return e == cudaSuccess ? NT2G_OK : cuda_status(e, "nt2g_device_alloc");
+}
+
+extern "C" nt2g_status nt2g_device_free(void *ptr)
+{
+    if (!ptr) return NT2G_OK;
+    cudaError_t e = cudaFree(ptr);
+    return e == cudaSuccess ? NT2G_OK : cuda_status(e, "nt2g_device_free");
+}
+
+extern "C" nt2g_status nt2g_memcpy(void *dst, const void *src, size_t bytes, int32_t kind, void *stream)
+{
+    NT2G_CHECK_ARG(kind >= 1 && kind <= 3, "nt2g_memcpy: kind %d", kind);
+    if (bytes == 0) return NT2G_OK;
+    NT2G_CHECK_ARG(dst && src, "nt2g_memcpy: NULL pointer");
+    cudaMemcpyKind k = kind == 1 ? cudaMemcpyHostToDevice : kind == 2 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, k, (cudaStream_t)stream);
+    return e == cudaSuccess ? NT2G_OK : cuda_status(e, "nt2g_memcpy");
+}
+
+extern "C" nt2g_status nt2g_stream_synchronize(void *stream)
+{
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    return e == cudaSuccess ? NT2G_OK : cuda_status(e, "nt2g_stream_synchronize");
+}

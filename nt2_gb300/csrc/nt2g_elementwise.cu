@@ -1,0 +1,467 @@
+// nt2g_elementwise.cu -- fused elementwise kernels other than Black-Scholes
+// (saxpy, expr3, rgb2yuv, sigma-delta), element maps, and the generic
+// program interpreter that evaluates any lowered nt2 expression in one pass.
+#include "nt2g_common.cuh"
+#include "nt2g_exprs.cuh"
+#include "nt2g_internal.h"
+
+namespace nt2g {
+
+static constexpr int kThreads = 256;
+
+template <class KERN>
+static int grid_for(KERN k, int64_t units)
+{
+    return persistent_blocks(k, kThreads, 0, kThreads * 2, units);
+}
+
+// ------------------------------------------------------------------ saxpy --
+// Y = alpha*X + Y with NT2's two roundings (demo/saxpy/nt2/saxpy_nt2.cpp:41).
+__global__ void __launch_bounds__(kThreads) k_saxpy(float alpha, const float *__restrict__ X,
+                                                    const float *Y, float *O, int64_t n, int vec)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if (vec) {
+        const int64_t nv = n >> 2;
+        int64_t i = tid;
+        // two vectors in flight per thread
+        for (; i + stride < nv; i += 2 * stride) {
+            float4 x0 = ld_stream((const float4 *)X + i), y0 = ld_stream((const float4 *)Y + i);
+            float4 x1 = ld_stream((const float4 *)X + i + stride), y1 = ld_stream((const float4 *)Y + i + stride);
+            float4 o0, o1;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                set(o0, j, saxpy_elem(alpha, get(x0, j), get(y0, j)));
+                set(o1, j, saxpy_elem(alpha, get(x1, j), get(y1, j)));
+            }
+            st_stream((float4 *)O + i, o0);
+            st_stream((float4 *)O + i + stride, o1);
+        }
+        for (; i < nv; i += stride) {
+            float4 x0 = ld_stream((const float4 *)X + i), y0 = ld_stream((const float4 *)Y + i), o0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) set(o0, j, saxpy_elem(alpha, get(x0, j), get(y0, j)));
+            st_stream((float4 *)O + i, o0);
+        }
+        done = nv << 2;
+    }
+    for (int64_t i = done + tid; i < n; i += stride) O[i] = saxpy_elem(alpha, X[i], Y[i]);
+}
+
+// O may alias Y (the in-place form of the demo).
+nt2g_status launch_saxpy(float alpha, const float *X, const float *Y, float *O, int64_t n, cudaStream_t st)
+{
+    if (n == 0) return NT2G_OK;
+    int vec = aligned16(X) && aligned16(Y) && aligned16(O);
+    k_saxpy<<<grid_for(k_saxpy, (n + 3) / 4), kThreads, 0, st>>>(alpha, X, Y, O, n, vec);
+    NT2G_LAUNCH_CHECK("saxpy launch");
+    return NT2G_OK;
+}
+
+// ------------------------------------------------------------------ expr3 --
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_expr3(const float *__restrict__ x, const float *__restrict__ y,
+                                                    const float *__restrict__ z, float *__restrict__ o,
+                                                    int64_t n, int vec)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if (vec) {
+        const int64_t nv = n >> 2;
+        for (int64_t i = tid; i < nv; i += stride) {
+            float4 a = ld_stream((const float4 *)x + i), b = ld_stream((const float4 *)y + i),
+                   c = ld_stream((const float4 *)z + i), r;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) set(r, j, expr3_elem<P>(get(a, j), get(b, j), get(c, j)));
+            st_stream((float4 *)o + i, r);
+        }
+        done = nv << 2;
+    }
+    for (int64_t i = done + tid; i < n; i += stride) o[i] = expr3_elem<P>(x[i], y[i], z[i]);
+}
+
+nt2g_status launch_expr3(const float *x, const float *y, const float *z, float *out, int64_t n, int precision,
+                         cudaStream_t st)
+{
+    if (n == 0) return NT2G_OK;
+    int vec = aligned16(x) && aligned16(y) && aligned16(z) && aligned16(out);
+    if (precision == NT2G_PREC_NT2)
+        k_expr3<Nt2><<<grid_for(k_expr3<Nt2>, (n + 3) / 4), kThreads, 0, st>>>(x, y, z, out, n, vec);
+    else
+        k_expr3<Fast><<<grid_for(k_expr3<Fast>, (n + 3) / 4), kThreads, 0, st>>>(x, y, z, out, n, vec);
+    NT2G_LAUNCH_CHECK("expr3 launch");
+    return NT2G_OK;
+}
+
+// ---------------------------------------------------------------- rgb2yuv --
+__global__ void __launch_bounds__(kThreads) k_rgb2yuv(const float *__restrict__ r, const float *__restrict__ g,
+                                                      const float *__restrict__ b, float *__restrict__ y,
+                                                      float *__restrict__ u, float *__restrict__ v, int64_t n,
+                                                      int vec)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if (vec) {
+        const int64_t nv = n >> 2;
+        for (int64_t i = tid; i < nv; i += stride) {
+            float4 R = ld_stream((const float4 *)r + i), G = ld_stream((const float4 *)g + i),
+                   B = ld_stream((const float4 *)b + i), Y, U, V;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float yy, uu, vv;
+                yuv_px(get(R, j), get(G, j), get(B, j), yy, uu, vv);
+                set(Y, j, yy); set(U, j, uu); set(V, j, vv);
+            }
+            st_stream((float4 *)y + i, Y);
+            st_stream((float4 *)u + i, U);
+            st_stream((float4 *)v + i, V);
+        }
+        done = nv << 2;
+    }
+    for (int64_t i = done + tid; i < n; i += stride) yuv_px(r[i], g[i], b[i], y[i], u[i], v[i]);
+}
+
+nt2g_status launch_rgb2yuv(const float *r, const float *g, const float *b, float *y, float *u, float *v,
+                           int64_t n, cudaStream_t st)
+{
+    if (n == 0) return NT2G_OK;
+    int vec = aligned16(r) && aligned16(g) && aligned16(b) && aligned16(y) && aligned16(u) && aligned16(v);
+    k_rgb2yuv<<<grid_for(k_rgb2yuv, (n + 3) / 4), kThreads, 0, st>>>(r, g, b, y, u, v, n, vec);
+    NT2G_LAUNCH_CHECK("rgb2yuv launch");
+    return NT2G_OK;
+}
+
+// ------------------------------------------------------------ sigma-delta --
+__device__ __forceinline__ void sd_px(uint8_t f, uint8_t &b, uint8_t &v, uint8_t &lab)
+{
+    uint32_t bb = b, vv = v, l;
+    sd_word(f, bb, vv, l);
+    b = (uint8_t)bb; v = (uint8_t)vv; lab = (uint8_t)l;
+}
+
+__device__ __forceinline__ void sd_vec(const uint4 &f, uint4 &b, uint4 &v, uint4 &l)
+{
+    sd_word(f.x, b.x, v.x, l.x);
+    sd_word(f.y, b.y, v.y, l.y);
+    sd_word(f.z, b.z, v.z, l.z);
+    sd_word(f.w, b.w, v.w, l.w);
+}
+
+__global__ void __launch_bounds__(kThreads) k_sigmadelta(const uint8_t *__restrict__ fr, uint8_t *__restrict__ bkg,
+                                                         uint8_t *__restrict__ var, uint8_t *__restrict__ lab,
+                                                         int64_t n, int vec)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if (vec) {
+        const int64_t nv = n >> 4;  // 16 pixels per uint4
+        for (int64_t i = tid; i < nv; i += stride) {
+            uint4 f = ld_stream((const uint4 *)fr + i), b = ld_stream((const uint4 *)bkg + i),
+                  v = ld_stream((const uint4 *)var + i), l;
+            sd_vec(f, b, v, l);
+            st_stream((uint4 *)bkg + i, b);
+            st_stream((uint4 *)var + i, v);
+            st_stream((uint4 *)lab + i, l);
+        }
+        done = nv << 4;
+    }
+    for (int64_t i = done + tid; i < n; i += stride) sd_px(fr[i], bkg[i], var[i], lab[i]);
+}
+
+// Temporal fusion: a thread keeps 16 pixels' bkg/var in registers across all
+// frames; per pixel-frame HBM traffic drops from 6 B to 2 + 4/F B.
+__global__ void __launch_bounds__(kThreads) k_sigmadelta_frames(const uint8_t *__restrict__ frames,
+                                                                uint8_t *__restrict__ bkg,
+                                                                uint8_t *__restrict__ var,
+                                                                uint8_t *__restrict__ labels, int64_t n,
+                                                                int nf, int vec)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if (vec) {
+        const int64_t nv = n >> 4;
+        for (int64_t i = tid; i < nv; i += stride) {
+            uint4 b = ld_stream((const uint4 *)bkg + i), v = ld_stream((const uint4 *)var + i), l;
+            for (int k = 0; k < nf; ++k) {
+                uint4 f = ld_stream((const uint4 *)(frames + (int64_t)k * n) + i);
+                sd_vec(f, b, v, l);
+                st_stream((uint4 *)(labels + (int64_t)k * n) + i, l);
+            }
+            st_stream((uint4 *)bkg + i, b);
+            st_stream((uint4 *)var + i, v);
+        }
+        done = nv << 4;
+    }
+    for (int64_t i = done + tid; i < n; i += stride) {
+        uint8_t b = bkg[i], v = var[i], l;
+        for (int k = 0; k < nf; ++k) {
+            sd_px(frames[(int64_t)k * n + i], b, v, l);
+            labels[(int64_t)k * n + i] = l;
+        }
+        bkg[i] = b;
+        var[i] = v;
+    }
+}
+
+nt2g_status launch_sigmadelta(const uint8_t *frame, uint8_t *bkg, uint8_t *var, uint8_t *label, int64_t n,
+                              cudaStream_t st)
+{
+    if (n == 0) return NT2G_OK;
+    int vec = aligned16(frame) && aligned16(bkg) && aligned16(var) && aligned16(label);
+    k_sigmadelta<<<grid_for(k_sigmadelta, (n + 15) / 16), kThreads, 0, st>>>(frame, bkg, var, label, n, vec);
+    NT2G_LAUNCH_CHECK("sigmadelta launch");
+    return NT2G_OK;
+}
+
+nt2g_status launch_sigmadelta_frames(const uint8_t *frames, uint8_t *bkg, uint8_t *var, uint8_t *labels,
+                                     int64_t n, int nf, cudaStream_t st)
+{
+    if (n == 0 || nf == 0) return NT2G_OK;
+    // every frame plane must start 16-byte aligned for the vector path
+    int vec = aligned16(frames) && aligned16(bkg) && aligned16(var) && aligned16(labels) && (n % 16 == 0);
+    k_sigmadelta_frames<<<grid_for(k_sigmadelta_frames, (n + 15) / 16), kThreads, 0, st>>>(frames, bkg, var,
+                                                                                           labels, n, nf, vec);
+    NT2G_LAUNCH_CHECK("sigmadelta frames launch");
+    return NT2G_OK;
+}
+
+// ------------------------------------------------------------------- maps --
+template <class P, int FN>
+__device__ __forceinline__ float map_elem(float a)
+{
+    if (FN == 0) return exp<P>(a);
+    if (FN == 1) return log<P>(a);
+    if (FN == 2) return log1p<P>(a);
+    if (FN == 3) return erfc<P>(a);
+    if (FN == 4) return normcdf<P>(a);
+    if (FN == 5) return fastnormcdf<P>(a);
+    if (FN == 6) return P::sqrt(a);
+    float p, q;
+    normcdf_pair<P>(a, p, q);
+    return q;
+}
+
+template <class P, int FN>
+__global__ void __launch_bounds__(kThreads) k_map(const float *__restrict__ x, float *__restrict__ y, int64_t n)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        y[i] = map_elem<P, FN>(x[i]);
+}
+
+template <class P>
+static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream_t st)
+{
+#define NT2G_MAP(F) k_map<P, F><<<grid_for(k_map<P, F>, (n + 3) / 4), kThreads, 0, st>>>(x, y, n)
+    switch (fn) {
+    case 0: NT2G_MAP(0); break;
+    case 1: NT2G_MAP(1); break;
+    case 2: NT2G_MAP(2); break;
+    case 3: NT2G_MAP(3); break;
+    case 4: NT2G_MAP(4); break;
+    case 5: NT2G_MAP(5); break;
+    case 6: NT2G_MAP(6); break;
+    default: NT2G_MAP(7); break;
+    }
+#undef NT2G_MAP
+}
+
+nt2g_status launch_map(int fn, const float *x, float *y, int64_t n, int precision, cudaStream_t st)
+{
+    if (n == 0) return NT2G_OK;
+    if (precision == NT2G_PREC_NT2) map_dispatch<Nt2>(fn, x, y, n, st);
+    else map_dispatch<Fast>(fn, x, y, n, st);
+    NT2G_LAUNCH_CHECK("map launch");
+    return NT2G_OK;
+}
+
+// ------------------------------------------------------------ interpreter --
+// Each thread evaluates 4 consecutive elements per step; the register file
+// R[reg][4] is per-thread local memory (L1-resident).  The program is a
+// kernel parameter, so instruction fetch is a uniform constant-bank read and
+// the opcode switch never diverges.
+constexpr int kV = 4;
+
+template <class P>
+__device__ __forceinline__ float f_unary(int op, float a)
+{
+    switch (op) {
+    case NT2G_OP_NEG: return -a;
+    case NT2G_OP_ABS: return fabsf(a);
+    case NT2G_OP_SQR: return P::mul(a, a);
+    case NT2G_OP_SQRT: return P::sqrt(a);
+    case NT2G_OP_REC: return P::div(1.0f, a);
+    case NT2G_OP_EXP: return exp<P>(a);
+    case NT2G_OP_LOG: return log<P>(a);
+    case NT2G_OP_LOG1P: return log1p<P>(a);
+    case NT2G_OP_ERFC: return erfc<P>(a);
+    case NT2G_OP_NORMCDF: return normcdf<P>(a);
+    default: return fastnormcdf<P>(a);
+    }
+}
+
+template <class P>
+__global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs args, int64_t n, int vec)
+{
+    uint32_t R[kMaxRegs][kV];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kV; base < n; base += stride * kV) {
+        const int cnt = (int)((n - base) < kV ? (n - base) : kV);
+        const bool full = vec && cnt == kV;
+        for (int pc = 0; pc < prog.n; ++pc) {
+            const DInstr in = prog.ins[pc];
+            uint32_t *d = R[in.dst];
+            const uint32_t *A = R[in.a], *B = R[in.b], *C = R[in.c];
+            const bool f32 = in.dt == NT2G_F32;
+            switch (in.op) {
+            case NT2G_OP_LOAD:
+                if (f32) {
+                    const float *p = (const float *)args.ptr[in.a] + base;
+                    if (full) {
+                        float4 v = ld_stream((const float4 *)p);
+                        d[0] = __float_as_uint(v.x); d[1] = __float_as_uint(v.y);
+                        d[2] = __float_as_uint(v.z); d[3] = __float_as_uint(v.w);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < kV; ++j) d[j] = j < cnt ? __float_as_uint(p[j]) : 0u;
+                    }
+                } else {
+                    const uint8_t *p = (const uint8_t *)args.ptr[in.a] + base;
+#pragma unroll
+                    for (int j = 0; j < kV; ++j) d[j] = j < cnt ? p[j] : 0u;
+                }
+                break;
+            case NT2G_OP_SCALAR:
+#pragma unroll
+                for (int j = 0; j < kV; ++j) d[j] = f32 ? __float_as_uint(args.scal[in.a]) : args.scal_u8[in.a];
+                break;
+            case NT2G_OP_CONST:
+#pragma unroll
+                for (int j = 0; j < kV; ++j) d[j] = f32 ? __float_as_uint(in.imm) : ((uint32_t)in.imm & 255u);
+                break;
+            case NT2G_OP_STORE:
+                if (f32) {
+                    float *p = (float *)args.ptr[in.b] + base;
+                    float v[kV];
+#pragma unroll
+                    for (int j = 0; j < kV; ++j) v[j] = in.logical ? (float)A[j] : __uint_as_float(A[j]);
+                    if (full) {
+                        st_stream((float4 *)p, make_float4(v[0], v[1], v[2], v[3]));
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < kV; ++j)
+                            if (j < cnt) p[j] = v[j];
+                    }
+                } else {
+                    uint8_t *p = (uint8_t *)args.ptr[in.b] + base;
+#pragma unroll
+                    for (int j = 0; j < kV; ++j)
+                        if (j < cnt) p[j] = (uint8_t)A[j];
+                }
+                break;
+            case NT2G_OP_ADD: case NT2G_OP_SUB: case NT2G_OP_MUL: case NT2G_OP_DIV:
+            case NT2G_OP_MIN: case NT2G_OP_MAX: case NT2G_OP_ADDS:
+#pragma unroll
+                for (int j = 0; j < kV; ++j) {
+                    if (f32) {
+                        float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]), r;
+                        switch (in.op) {
+                        case NT2G_OP_ADD: r = P::add(x, y); break;
+                        case NT2G_OP_SUB: r = P::sub(x, y); break;
+                        case NT2G_OP_MUL: r = P::mul(x, y); break;
+                        case NT2G_OP_DIV: r = P::div(x, y); break;
+                        case NT2G_OP_MIN: r = fminf(x, y); break;
+                        default: r = fmaxf(x, y); break;
+                        }
+                        d[j] = __float_as_uint(r);
+                    } else {
+                        uint32_t x = A[j], y = B[j], r;
+                        switch (in.op) {
+                        case NT2G_OP_ADD: r = (x + y) & 255u; break;
+                        case NT2G_OP_SUB: r = (x - y) & 255u; break;
+                        case NT2G_OP_MUL: r = (x * y) & 255u; break;
+                        case NT2G_OP_MIN: r = x < y ? x : y; break;
+                        case NT2G_OP_MAX: r = x > y ? x : y; break;
+                        default: r = (x + y) > 255u ? 255u : (x + y); break;
+                        }
+                        d[j] = r;
+                    }
+                }
+                break;
+            case NT2G_OP_FMA: case NT2G_OP_FNMS:
+#pragma unroll
+                for (int j = 0; j < kV; ++j) {
+                    float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]), z = __uint_as_float(C[j]);
+                    d[j] = __float_as_uint(in.op == NT2G_OP_FMA ? P::fma(x, y, z) : P::fma(-x, y, z));
+                }
+                break;
+            case NT2G_OP_LT: case NT2G_OP_GT: case NT2G_OP_LE: case NT2G_OP_GE: case NT2G_OP_EQ:
+            case NT2G_OP_NE:
+#pragma unroll
+                for (int j = 0; j < kV; ++j) {
+                    bool r;
+                    if (f32) {
+                        float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]);
+                        r = in.op == NT2G_OP_LT ? x < y : in.op == NT2G_OP_GT ? x > y : in.op == NT2G_OP_LE ? x <= y
+                          : in.op == NT2G_OP_GE ? x >= y : in.op == NT2G_OP_EQ ? x == y : x != y;
+                    } else {
+                        uint32_t x = A[j], y = B[j];
+                        r = in.op == NT2G_OP_LT ? x < y : in.op == NT2G_OP_GT ? x > y : in.op == NT2G_OP_LE ? x <= y
+                          : in.op == NT2G_OP_GE ? x >= y : in.op == NT2G_OP_EQ ? x == y : x != y;
+                    }
+                    d[j] = r ? 1u : 0u;
+                }
+                break;
+            case NT2G_OP_IF_ELSE:
+#pragma unroll
+                for (int j = 0; j < kV; ++j) d[j] = A[j] ? B[j] : C[j];
+                break;
+            case NT2G_OP_SELINC: case NT2G_OP_SELDEC:
+#pragma unroll
+                for (int j = 0; j < kV; ++j) {
+                    if (f32) {
+                        float y = __uint_as_float(B[j]);
+                        d[j] = __float_as_uint(A[j] ? P::add(y, in.op == NT2G_OP_SELINC ? 1.0f : -1.0f) : y);
+                    } else {
+                        d[j] = A[j] ? ((in.op == NT2G_OP_SELINC ? B[j] + 1u : B[j] - 1u) & 255u) : B[j];
+                    }
+                }
+                break;
+            case NT2G_OP_IF_ZERO_ELSE_ONE:
+#pragma unroll
+                for (int j = 0; j < kV; ++j) d[j] = f32 ? __float_as_uint(A[j] ? 0.0f : 1.0f) : (A[j] ? 0u : 1u);
+                break;
+            default:  // unary float functions
+#pragma unroll
+                for (int j = 0; j < kV; ++j) {
+                    if (f32) d[j] = __float_as_uint(f_unary<P>(in.op, __uint_as_float(A[j])));
+                    else d[j] = in.op == NT2G_OP_NEG ? ((0u - A[j]) & 255u) : A[j];
+                }
+                break;
+            }
+        }
+    }
+}
+
+nt2g_status launch_interp(const DProgram &prog, const DArgs &args, int64_t count, int precision, cudaStream_t st)
+{
+    if (count == 0) return NT2G_OK;
+    int vec = 1;
+    for (int s = 0; s < kMaxSlots; ++s)
+        if (args.ptr[s] && args.dtype[s] == NT2G_F32) vec &= aligned16(args.ptr[s]);
+    int64_t units = (count + kV - 1) / kV;
+    if (precision == NT2G_PREC_NT2)
+        k_interp<Nt2><<<persistent_blocks(k_interp<Nt2>, 128, 0, 128, units), 128, 0, st>>>(prog, args, count, vec);
+    else
+        k_interp<Fast><<<persistent_blocks(k_interp<Fast>, 128, 0, 128, units), 128, 0, st>>>(prog, args, count, vec);
+    NT2G_LAUNCH_CHECK("interpreter launch");
+    return NT2G_OK;
+}
+
+}  // namespace nt2g

@@ -1,0 +1,76 @@
+// nt2g_internal.h -- declarations shared between the translation units of
+// libnt2gpu (kernel launchers, the device program format, error helpers).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "nt2g.h"
+
+namespace nt2g {
+
+// ---------------------------------------------------------------- program --
+// Device form of a compiled program: register-allocated three-address code,
+// passed to the interpreter kernel by value (it lands in the constant bank,
+// so every thread reads the same instruction word: no divergence).
+constexpr int kMaxInstr = 160;
+constexpr int kMaxRegs = 32;
+constexpr int kMaxSlots = 16;
+
+struct DInstr {
+    uint8_t op;    // nt2g_opcode (fits in 8 bits)
+    uint8_t dt;    // nt2g_dtype of the operands
+    uint8_t dst;   // register
+    uint8_t a, b, c;  // registers, or slot for LOAD/SCALAR/STORE (a)
+    uint8_t logical;  // operand a of STORE holds a logical (0/1) value
+    uint8_t pad;
+    float imm;
+};
+
+struct DProgram {
+    int32_t n;
+    int32_t n_regs;
+    DInstr ins[kMaxInstr];
+};
+
+struct DArgs {
+    void *ptr[kMaxSlots];
+    float scal[kMaxSlots];
+    uint32_t scal_u8[kMaxSlots];
+    int32_t dtype[kMaxSlots];
+};
+
+// Fused kernels a program can bind to.
+enum FusedKernel {
+    kGeneric = 0,
+    kBlackScholes = 1,       // slots: S K T sigma(table|scalar) r | call put
+    kBlackScholesDemo = 2,   // slots: S X T r v | R
+    kSaxpy = 3,              // slots: alpha X Y | Y
+    kExpr3 = 4,              // slots: x y z | out
+    kRgb2Yuv = 5,            // slots: r g b | y u v
+    kSigmaDelta = 6,         // slots: frame bkg var | bkg var label
+};
+
+// -------------------------------------------------------------- launchers --
+nt2g_status launch_bs(const float *S, const float *K, const float *T, const float *sig, float sig_s, float r,
+                      float *call, float *put, int64_t n, int precision, cudaStream_t st);
+nt2g_status launch_bs_demo(const float *S, const float *X, const float *T, const float *rt, float r,
+                           const float *vt, float v, float *R, int64_t n, int precision, cudaStream_t st);
+nt2g_status launch_bs_vjp(const float *S, const float *K, const float *T, const float *sig, float r,
+                          const float *gc, const float *gp, float *C, float *P, float *dS, float *dK,
+                          float *dT, float *dsig, float *dr, int64_t n, cudaStream_t st);
+nt2g_status launch_saxpy(float alpha, const float *X, const float *Y, float *O, int64_t n, cudaStream_t st);
+nt2g_status reduce_workspace_bytes(size_t *bytes);
+nt2g_status launch_reduce(const float *x, const float *y, int64_t n, void *ws, double *out64, float *out32,
+                          cudaStream_t st);
+nt2g_status launch_expr3(const float *x, const float *y, const float *z, float *out, int64_t n, int precision,
+                         cudaStream_t st);
+nt2g_status launch_rgb2yuv(const float *r, const float *g, const float *b, float *y, float *u, float *v,
+                           int64_t n, cudaStream_t st);
+nt2g_status launch_sigmadelta(const uint8_t *frame, uint8_t *bkg, uint8_t *var, uint8_t *label, int64_t n,
+                              cudaStream_t st);
+nt2g_status launch_sigmadelta_frames(const uint8_t *frames, uint8_t *bkg, uint8_t *var, uint8_t *labels,
+                                     int64_t n, int frames_n, cudaStream_t st);
+nt2g_status launch_map(int fn, const float *x, float *y, int64_t n, int precision, cudaStream_t st);
+nt2g_status launch_interp(const DProgram &prog, const DArgs &args, int64_t count, int precision,
+                          cudaStream_t st);
+
+}  // namespace nt2g

@@ -1,0 +1,400 @@
+// nt2g_math.cuh -- FP32 element math for the fused evaluator.
+//
+// Every function is a template on an arithmetic policy:
+//
+//  * Nt2  -- NT2's own scalar float algorithms with NT2's operation order:
+//            fma/fnms/Horner unfused (a*b then +c, two roundings), IEEE
+//            division and square root.  On the GPU the intrinsics __fmul_rn /
+//            __fadd_rn / __fdiv_rn / __fsqrt_rn stop the compiler from
+//            contracting, so results are bit-identical to NT2's scalar CPU
+//            evaluation.
+//  * Fast -- the default hot path: fused multiply-add, a reciprocal-approx
+//            division refined by one Newton step, and an erfc/normcdf built
+//            on an exact split of x^2 so the tail keeps FP32 accuracy (NT2's
+//            float erfc loses up to ~75 ulp there).
+//
+// The header also compiles as plain C++ (host), with std::fma, so the
+// accuracy of the Fast policy can be studied on a CPU; only the division
+// differs (host: IEEE division, device: rcp.approx + Newton, <= 1 ulp apart).
+//
+// NT2 sources followed (paths inside the NT2 tree):
+//   exp   modules/core/exponential/include/nt2/exponential/functions/
+//           scalar/impl/expo/{expo_base.hpp:58-69, f_expo_reduction.hpp:52-85,
+//           expo_scale.hpp:27-35}
+//   log   .../scalar/impl/logs/{f_log.hpp:59-88, f_kernel.hpp:43-75}
+//   log1p .../scalar/log1p.hpp:35-45
+//   erfc  modules/core/euler/include/nt2/euler/functions/scalar/erfc.hpp:83-104,
+//           details/erf_kernel.hpp:48-91
+//   normcdf / fastnormcdf  modules/core/statistics/include/nt2/statistics/
+//           functions/generic/{normcdf.hpp:34, fastnormcdf.hpp:39-54}
+#pragma once
+#include <stdint.h>
+#include <string.h>
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define NT2G_HD __host__ __device__ __forceinline__
+#else
+#define NT2G_HD inline
+#endif
+
+namespace nt2g {
+
+NT2G_HD float bits_f(uint32_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f; memcpy(&f, &u, 4); return f;
+#endif
+}
+NT2G_HD uint32_t f_bits(float f)
+{
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u; memcpy(&u, &f, 4); return u;
+#endif
+}
+
+// ----------------------------------------------------------- policies ----
+struct Nt2 {
+    static constexpr bool exact = true;
+#if defined(__CUDA_ARCH__)
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
+#else
+    static inline float mul(float a, float b) { volatile float r = a * b; return r; }
+    static inline float add(float a, float b) { volatile float r = a + b; return r; }
+    static inline float sub(float a, float b) { volatile float r = a - b; return r; }
+    static inline float div(float a, float b) { return a / b; }
+    static inline float sqrt(float a) { return sqrtf(a); }
+#endif
+    static NT2G_HD float fdiv(float a, float b) { return div(a, b); }
+    // NT2's generic fma is a*b+c with two roundings.
+    static NT2G_HD float fma(float a, float b, float c) { return add(mul(a, b), c); }
+};
+
+struct Fast {
+    static constexpr bool exact = false;
+#if defined(__CUDA_ARCH__)
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+    static __device__ __forceinline__ float rcp(float b)
+    {
+        float r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+        return r;
+    }
+    // IEEE division for user-visible '/', where operands are arbitrary.
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    // q0 = a*rcp(b), one Newton correction on the residual a - q0*b (<= 1 ulp
+    // from the rounded quotient).  Valid for finite normal b whose reciprocal
+    // is normal; used only inside kernels whose operands are known to be so.
+    static __device__ __forceinline__ float fdiv(float a, float b)
+    {
+        float r = rcp(b);
+        float q = a * r;
+        float e = __fmaf_rn(-q, b, a);
+        return __fmaf_rn(e, r, q);
+    }
+    static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
+#else
+    static inline float mul(float a, float b) { return a * b; }
+    static inline float add(float a, float b) { return a + b; }
+    static inline float sub(float a, float b) { return a - b; }
+    static inline float fma(float a, float b, float c) { return fmaf(a, b, c); }
+    static inline float rcp(float b) { return 1.0f / b; }
+    static inline float div(float a, float b) { return a / b; }
+    static inline float fdiv(float a, float b) { return a / b; }
+    static inline float sqrt(float a) { return sqrtf(a); }
+#endif
+};
+
+// Horner with NT2's coefficient order: first argument after x is the
+// highest degree; each step is fma(x, acc, c).
+template <class P> NT2G_HD float horner(float, float acc) { return acc; }
+template <class P, class... R>
+NT2G_HD float horner(float x, float acc, float c, R... rest)
+{
+    return horner<P>(x, P::fma(x, acc, c), rest...);
+}
+
+// ------------------------------------------------------------ constants --
+// NT2 float constants, by bit pattern (modules/core/exponential/include/nt2/
+// exponential/constants/*.hpp, modules/boost/simd/base/include/boost/simd/
+// constant/constants/*.hpp).
+#define NT2G_MAXLOG      0x42b0c0a5u
+#define NT2G_MINLOG      0xc2b0c0a5u
+#define NT2G_INVLOG_2    0x3fb8aa3bu
+#define NT2G_LOG_2HI     0x3f318000u
+#define NT2G_LOG_2LO     0xb95e8083u
+#define NT2G_SQRT_2O_2   0x3F3504F3u
+#define NT2G_SMALLESTPOS 0x00800000u
+#define NT2G_TWOTONMB    0x4B000000u
+#define NT2G_MLOGTWO2NMB 0xc17f1402u
+#define NT2G_TWOTHIRD    0x3f2aaaabu
+#define NT2G_INVSQRT_2PI 0x3ecc422au
+
+NT2G_HD float f_inf() { return bits_f(0x7f800000u); }
+NT2G_HD float f_nan() { return bits_f(0x7fc00000u); }
+NT2G_HD bool is_nan(float x) { return x != x; }
+
+// ------------------------------------------------------------------ exp --
+// NT2: k = round2even(x/ln2); r = x - k*ln2hi - k*ln2lo (unfused fnms);
+// degree-4 Remez for (e^r-1-r)/r^2; 2^k built in the exponent field.
+// Fast: same reduction with FMAs, k from the 1.5*2^23 shifter (round to
+// nearest even, so k equals NT2's except on exact ties), and its own degree-5
+// fit of q(r) = (e^r-1-r)/r^2 on |r| <= ln2/2 (truncation < 0.02 ulp).
+// exp_fast_parts returns e^x = (1 + s) * 2^k unassembled so that callers can
+// fold the "+1" into a following product (one rounding instead of two).
+NT2G_HD float exp_fast_parts(float a0, float &scale)
+{
+    const float shifter = 12582912.0f;  // 1.5 * 2^23
+    float kf = Fast::fma(a0, bits_f(NT2G_INVLOG_2), shifter);
+    float k = Fast::sub(kf, shifter);
+    int32_t ik = (int32_t)(f_bits(kf) - 0x4B400000u);
+    float x = Fast::fma(-k, bits_f(NT2G_LOG_2HI), a0);
+    x = Fast::fma(-k, bits_f(NT2G_LOG_2LO), x);
+    float q = horner<Fast>(x, 0x1.a157b2p-13f, 0x1.6d4926p-10f, 0x1.1110c4p-7f, 0x1.5554e4p-5f,
+                           0x1.555556p-3f, 0.5f);
+    scale = bits_f((uint32_t)(ik + 127) << 23);
+    return Fast::fma(q, Fast::mul(x, x), x);
+}
+
+template <class P> NT2G_HD float exp(float a0)
+{
+    if (P::exact) {
+        if (a0 >= bits_f(NT2G_MAXLOG)) return f_inf();
+        if (a0 <= bits_f(NT2G_MINLOG)) return 0.0f;
+        if (is_nan(a0)) return a0;
+        float k = rintf(P::mul(bits_f(NT2G_INVLOG_2), a0));
+        float x = P::sub(a0, P::mul(k, bits_f(NT2G_LOG_2HI)));
+        x = P::sub(x, P::mul(k, bits_f(NT2G_LOG_2LO)));
+        float y = horner<P>(x, bits_f(0x3ab778cfu), bits_f(0x3c098d8bu), bits_f(0x3d2aa957u),
+                            bits_f(0x3e2aa9a5u), bits_f(0x3f000000u));
+        float c = P::add(P::fma(y, P::mul(x, x), x), 1.0f);
+        return P::mul(c, bits_f((uint32_t)((int32_t)k + 127) << 23));
+    }
+    float scale;
+    float s = exp_fast_parts(a0, scale);
+    float r = Fast::mul(Fast::add(s, 1.0f), scale);
+    r = (a0 >= bits_f(NT2G_MAXLOG)) ? f_inf() : r;
+    r = (a0 <= bits_f(NT2G_MINLOG)) ? 0.0f : r;
+    return is_nan(a0) ? a0 : r;
+}
+
+// ------------------------------------------------------------------ log --
+template <class P> NT2G_HD float log(float a0)
+{
+    if (P::exact) {
+        if (a0 == f_inf()) return a0;
+        if (a0 == 0.0f) return -f_inf();
+        if (is_nan(a0) || a0 < 0.0f) return f_nan();
+    }
+    float z = a0, t = 0.0f;
+    bool den = fabsf(z) < bits_f(NT2G_SMALLESTPOS);
+    if (P::exact) {
+        if (den) { z = P::mul(z, bits_f(NT2G_TWOTONMB)); t = bits_f(NT2G_MLOGTWO2NMB); }
+    } else {
+        z = den ? P::mul(z, bits_f(NT2G_TWOTONMB)) : z;
+        t = den ? bits_f(NT2G_MLOGTWO2NMB) : 0.0f;
+    }
+    uint32_t u = f_bits(z);
+    int32_t e = (int32_t)((u & 0x7f800000u) >> 23) - 126;
+    float x = bits_f((u & ~0x7f800000u) | 0x3f000000u);
+    bool lt = x < bits_f(NT2G_SQRT_2O_2);
+    float fe = lt ? P::add((float)e, -1.0f) : (float)e;
+    x = P::sub(lt ? P::add(x, x) : x, 1.0f);
+    float x2 = P::mul(x, x);
+    float y = horner<P>(x, bits_f(0xbda5dff0u), bits_f(0x3e0229f9u), bits_f(0xbe04d6b7u),
+                        bits_f(0x3e116e80u), bits_f(0xbe2a6aa0u), bits_f(0x3e4cd0a3u),
+                        bits_f(0xbe800064u), bits_f(0x3eaaaaa9u));
+    y = P::mul(P::mul(y, x), x2);
+    y = P::fma(fe, bits_f(NT2G_LOG_2LO), y);
+    y = P::fma(-0.5f, x2, y);
+    float r = P::fma(bits_f(NT2G_LOG_2HI), fe, P::add(P::add(x, y), t));
+    if (!P::exact) {
+        r = (a0 == f_inf()) ? a0 : r;
+        r = (a0 == 0.0f) ? -f_inf() : r;
+        r = (is_nan(a0) || a0 < 0.0f) ? f_nan() : r;
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------- log1p --
+template <class P> NT2G_HD float log1p(float a0)
+{
+    if (P::exact) {
+        if (-1.0f > a0) return f_nan();
+        if (a0 == f_inf()) return f_inf();
+        if (a0 == -1.0f) return -f_inf();
+    }
+    float u = P::add(1.0f, a0);
+    float r;
+    if (P::exact) {
+        r = P::add(log<P>(u), P::div(P::sub(a0, P::sub(u, 1.0f)), u));
+    } else {
+        // u == 1 exactly (tiny a0): log(u) = 0, correction a0/1; the division
+        // runs only on normal u, so rcp.approx stays in range.
+        float uu = (u > 0.0f && u < f_inf()) ? u : 1.0f;
+        r = P::add(log<P>(u), P::div(P::sub(a0, P::sub(u, 1.0f)), uu));
+        r = (a0 == f_inf()) ? f_inf() : r;
+        r = (a0 == -1.0f) ? -f_inf() : r;
+        r = (-1.0f > a0 || is_nan(a0)) ? f_nan() : r;
+    }
+    return r;
+}
+
+// ------------------------------------------------------- NT2 erfc core --
+// erfc(|x|) before the sign fold (EUL/scalar/erfc.hpp:85-101).
+template <class P> NT2G_HD float erfc_core_nt2(float x)
+{
+    float z = P::div(x, P::add(x, 1.0f));
+    if (x < bits_f(NT2G_TWOTHIRD))
+        return P::mul(P::sub(1.0f, z),
+                      horner<P>(z, bits_f(0x41aa8e55u), bits_f(0x401b5680u), bits_f(0xc010d956u),
+                                bits_f(0x3f2cff3bu), bits_f(0xc016c985u), bits_f(0xbffc9284u),
+                                bits_f(0xbfa11698u), bits_f(0xbe036d7eu), bits_f(0x3f7ffffeu)));
+    if (x == f_inf()) return 0.0f;
+    z = P::sub(z, 0.4f);
+    return P::mul(exp<P>(-P::mul(x, x)),
+                  horner<P>(z, bits_f(0xc0283611u), bits_f(0x40d67e3bu), bits_f(0xc0cd1a85u),
+                            bits_f(0x4050b063u), bits_f(0xbfaea865u), bits_f(0x3e2006f0u),
+                            bits_f(0x3e1175c7u), bits_f(0x3ec4ca6eu), bits_f(0x3e243828u),
+                            bits_f(0xbf918a62u), bits_f(0x3f0a0e8bu)));
+}
+
+// ----------------------------------------------------- fast erfc tail --
+// For t >= 0:  erfc(t) = exp(-t^2) * w * R(w),  w = 1/(1 + t/2).
+// R is a degree-10 fit in w - 1/2 (coefficients from fit_erfc.py, highest
+// degree first).  exp(-t^2) is evaluated as exp(-hi) * (1 - lo) with hi + lo = t^2
+// exactly (FMA split), so the rounding of t^2 is not amplified in the tail.
+NT2G_HD float erfc_tail_poly(float w)
+{
+    // polynomial in d = w - 1/2 (exact for w >= 1/4; below that the rounding
+    // is an absolute 2^-26 that R barely feels)
+    float d = Fast::sub(w, 0.5f);
+    return horner<Fast>(d, 0x1.5af3d4p-5f, -0x1.38d8fcp-6f, -0x1.382c16p-4f, 0x1.c51560p-5f,
+                        0x1.908f48p-4f, -0x1.a94032p-4f, -0x1.604ccep-3f, 0x1.2a8c2ep-3f,
+                        0x1.1e2dc2p-1f, 0x1.5fd384p-1f, 0x1.058672p-1f);
+}
+
+// Tail value T(a) for a >= 0 with scale s:
+//   s = 1      : T = erfc(a)
+//   s = 1/sqrt2: T = erfc(a/sqrt2) = 2*normcdf(-a)
+// computed as exp(-(s*a)^2) * w * R(w), w = 1/(1 + (s/2)*a).  The square is
+// the exact split a^2 = hi + lo times s^2 (1 or 1/2: exact), and
+// exp(-s^2*hi) = (1 + e) * 2^k with e corrected for lo, so the result is
+// 2^k * fma(e, wR, wR): one rounding for the exponential's "+1" and the
+// product together.
+template <bool HALF_SQ> NT2G_HD float erfc_tail_fast(float a, float *expo = nullptr)
+{
+    const float q = HALF_SQ ? 0.353553390593273762f : 0.5f;  // (1/2)*s
+    // w ~ 1/den, den = 1 + q*a held as den + dlo.  The polynomial takes the
+    // rounded w; the multiplier uses w*(1 + r), r the residual of w against
+    // den + dlo, so the rounding of w and of den only reaches the result
+    // through R(w), whose log-derivative is <= 1.3 (<= 2.3 for w itself).
+    float den = Fast::fma(q, a, 1.0f);
+    float dlo = Fast::fma(q, a, Fast::sub(1.0f, den));
+    float w = Fast::rcp(den);
+    w = Fast::fma(w, Fast::fma(-den, w, 1.0f), w);
+    float r = Fast::fma(-dlo, w, Fast::fma(-den, w, 1.0f));
+    float hi = Fast::mul(a, a);
+    float lo = Fast::fma(a, a, -hi);
+    const float s2 = HALF_SQ ? -0.5f : -1.0f;
+    float scale;
+    float e = exp_fast_parts(Fast::mul(s2, hi), scale);
+    // (1 + e) * (1 + L) - 1 = e + L*(1 + e), L = s2*lo (|L| < 2^-18)
+    float L = Fast::mul(s2, lo);
+    e = Fast::add(e, Fast::fma(L, e, L));
+    float wr = Fast::mul(w, erfc_tail_poly(w));
+    wr = Fast::fma(wr, r, wr);
+    float res = Fast::mul(Fast::fma(e, wr, wr), scale);
+    // past amax the exponential leaves the normal range (its 2^k scale would
+    // underflow) and the true value is subnormal; the guard also keeps inf*0
+    // out of the split for a = inf.
+    const float amax = HALF_SQ ? 13.2f : 9.3f;
+    if (expo) *expo = (a < amax) ? Fast::mul(Fast::add(e, 1.0f), scale) : 0.0f;
+    return (a < amax) ? res : 0.0f;
+}
+
+// ---------------------------------------------------------------- erfc --
+template <class P> NT2G_HD float erfc(float a0)
+{
+    if (P::exact) {
+        float r1 = erfc_core_nt2<P>(fabsf(a0));
+        return (a0 < 0.0f) ? P::sub(2.0f, r1) : r1;
+    }
+    float r1 = erfc_tail_fast<false>(fabsf(a0));
+    r1 = (a0 < 0.0f) ? Fast::sub(2.0f, r1) : r1;
+    return is_nan(a0) ? a0 : r1;
+}
+
+// -------------------------------------------------------------- normcdf --
+// NT2: Half*erfc(-Sqrt_2o_2*x).  Both the call and the put of a fused
+// Black-Scholes need N(d) and N(-d): normcdf_pair returns both from one erfc
+// core, which in NT2 arithmetic is bit-identical to two separate calls
+// (|-c*d| == |c*d|; only the final 2-r select differs).
+template <class P> NT2G_HD void normcdf_pair(float x, float &n_pos, float &n_neg)
+{
+    if (P::exact) {
+        float t = P::mul(-bits_f(NT2G_SQRT_2O_2), x);
+        float r1 = erfc_core_nt2<P>(fabsf(t));
+        float r2 = P::sub(2.0f, r1);
+        // erfc(t): t<0 -> 2-r1.  normcdf(x) = 0.5*erfc(t), normcdf(-x) = 0.5*erfc(-t)
+        n_pos = P::mul(0.5f, (t < 0.0f) ? r2 : r1);
+        n_neg = P::mul(0.5f, (-t < 0.0f) ? r2 : r1);
+        return;
+    }
+    float half_tail = Fast::mul(0.5f, erfc_tail_fast<true>(fabsf(x)));  // normcdf(-|x|)
+    float other = Fast::sub(1.0f, half_tail);
+    bool neg = x < 0.0f;
+    n_pos = neg ? half_tail : other;
+    n_neg = neg ? other : half_tail;
+    if (is_nan(x)) { n_pos = x; n_neg = x; }
+}
+
+// Fast pair plus g = exp(-x^2/2) (the normal density times sqrt(2*pi)),
+// for the adjoint kernel.
+NT2G_HD void normcdf_pair_pdf(float x, float &n_pos, float &n_neg, float &g)
+{
+    float half_tail = Fast::mul(0.5f, erfc_tail_fast<true>(fabsf(x), &g));
+    float other = Fast::sub(1.0f, half_tail);
+    bool neg = x < 0.0f;
+    n_pos = neg ? half_tail : other;
+    n_neg = neg ? other : half_tail;
+}
+
+template <class P> NT2G_HD float normcdf(float x)
+{
+    float a, b;
+    normcdf_pair<P>(x, a, b);
+    return a;
+}
+
+// ---------------------------------------------------------- fastnormcdf --
+// NT2's Abramowitz-Stegun 26.2.17 form, identical in both policies except
+// for fusion.  (Its absolute error is ~7.5e-8 by construction.)
+template <class P> NT2G_HD float fastnormcdf(float a0)
+{
+    // Fast: clamp |x| (the result saturates long before 100) so the
+    // approximate reciprocal never sees inf; NaN is restored at the end.
+    float l = P::exact ? fabsf(a0) : fminf(fabsf(a0), 100.0f);
+    float k = P::fdiv(1.0f, P::fma(0.2316419f, l, 1.0f));
+    float w = horner<P>(k, bits_f(0x3faa466fu), bits_f(0xbfe91eeau), bits_f(0x3fe40778u),
+                        bits_f(0xbeb68f87u), bits_f(0x3ea385fau));
+    w = P::mul(w, P::mul(P::mul(k, bits_f(NT2G_INVSQRT_2PI)),
+                         exp<P>(P::mul(-P::mul(l, l), 0.5f))));
+    float r = (a0 > 0.0f) ? P::sub(1.0f, w) : w;
+    return (!P::exact && is_nan(a0)) ? a0 : r;
+}
+
+template <class P> NT2G_HD float sqr(float x) { return P::mul(x, x); }
+
+}  // namespace nt2g

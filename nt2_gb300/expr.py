@@ -1,0 +1,203 @@
+"""A Python mirror of NT2's expression surface over device tables.
+
+``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
+(exp, log, log1p, erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms,
+min, max, if_else, selinc, seldec, if_zero_else_one, adds) build an expression
+tree; ``assign(outs, exprs)`` is ``tie(outs...) = tie(exprs...)``: it lowers
+the trees to the SSA program of nt2g.h, compiles it once (cached by program
+text) and evaluates it through ``nt2g_eval`` -- the same path the C++ table
+layer takes (nt2_gb300/include/nt2/table.hpp).
+
+Mirrors: run_assign -> transform lowering, modules/core/base/include/nt2/dsl/
+functions/elementwise/run.hpp:21-36; tie, modules/core/container/table/include/
+nt2/core/functions/expr/tie.hpp:40-121; partial transform ranges,
+modules/core/container/table/include/nt2/core/functions/expr/transform.hpp:40-60.
+"""
+import ctypes
+
+from . import lib
+
+
+class Node:
+    __slots__ = ("op", "args", "dtype", "imm", "table")
+
+    def __init__(self, op, args=(), dtype=lib.F32, imm=0.0, table=None):
+        self.op, self.args, self.dtype, self.imm, self.table = op, tuple(args), dtype, imm, table
+
+    # arithmetic
+    def __add__(self, o): return _bin("ADD", self, o)
+    def __radd__(self, o): return _bin("ADD", o, self)
+    def __sub__(self, o): return _bin("SUB", self, o)
+    def __rsub__(self, o): return _bin("SUB", o, self)
+    def __mul__(self, o): return _bin("MUL", self, o)
+    def __rmul__(self, o): return _bin("MUL", o, self)
+    def __truediv__(self, o): return _bin("DIV", self, o)
+    def __rtruediv__(self, o): return _bin("DIV", o, self)
+    def __neg__(self): return Node("NEG", (self,), self.dtype)
+    # comparisons produce logicals
+    def __lt__(self, o): return _bin("LT", self, o)
+    def __gt__(self, o): return _bin("GT", self, o)
+    def __le__(self, o): return _bin("LE", self, o)
+    def __ge__(self, o): return _bin("GE", self, o)
+    def ne(self, o): return _bin("NE", self, o)
+    def eq(self, o): return _bin("EQ", self, o)
+    __hash__ = object.__hash__
+
+
+# Leaves are plain Nodes (not subclasses): with a subclass on the right,
+# Python would try its reflected comparison first and turn d < var into
+# var > d, which computes the same but no longer has the expression's shape.
+def Table(tensor):
+    """A device table leaf (CUDA tensor, float32 or uint8)."""
+    import torch
+    if tensor.dtype not in (torch.uint8, torch.float32):
+        raise TypeError(f"tables hold float32 or uint8, not {tensor.dtype}")
+    return Node("LOAD", (), lib.U8 if tensor.dtype == torch.uint8 else lib.F32, table=tensor)
+
+
+def Scalar(value, dtype=lib.F32):
+    """A run-time scalar argument (a SCALAR slot, not baked into the program)."""
+    return Node("SCALAR", (), dtype, imm=float(value))
+
+
+def _wrap(x, dtype):
+    if isinstance(x, Node):
+        return x
+    return Node("CONST", (), dtype, imm=float(x))
+
+
+def _bin(op, a, b):
+    dt = a.dtype if isinstance(a, Node) else b.dtype
+    return Node(op, (_wrap(a, dt), _wrap(b, dt)), dt)
+
+
+def _un(op):
+    return lambda a: Node(op, (a,), a.dtype)
+
+
+exp, log, log1p, erfc = _un("EXP"), _un("LOG"), _un("LOG1P"), _un("ERFC")
+normcdf, fastnormcdf, sqrt, sqr, rec = _un("NORMCDF"), _un("FASTNORMCDF"), _un("SQRT"), _un("SQR"), _un("REC")
+abs_ = _un("ABS")
+
+
+def fma(a, b, c):
+    dt = next(x.dtype for x in (a, b, c) if isinstance(x, Node))
+    return Node("FMA", tuple(_wrap(x, dt) for x in (a, b, c)), dt)
+
+
+def fnms(a, b, c):
+    """c - a*b"""
+    dt = next(x.dtype for x in (a, b, c) if isinstance(x, Node))
+    return Node("FNMS", tuple(_wrap(x, dt) for x in (a, b, c)), dt)
+
+
+def min_(a, b): return _bin("MIN", a, b)
+def max_(a, b): return _bin("MAX", a, b)
+def adds(a, b): return _bin("ADDS", a, b)
+
+
+def if_else(c, a, b):
+    dt = a.dtype if isinstance(a, Node) else b.dtype
+    return Node("IF_ELSE", (c, _wrap(a, dt), _wrap(b, dt)), dt)
+
+
+def selinc(c, a): return Node("SELINC", (c, a), a.dtype)
+def seldec(c, a): return Node("SELDEC", (c, a), a.dtype)
+def if_zero_else_one(c, dtype): return Node("IF_ZERO_ELSE_ONE", (c,), dtype)
+
+
+def _compare_dtype(n):
+    return n.args[0].dtype
+
+
+def lower(outs, exprs):
+    """tie(outs) = tie(exprs) -> (ops, slot tensors/scalars)."""
+    slots, slot_of = [], {}
+
+    def slot(key, value):
+        if key not in slot_of:
+            slot_of[key] = len(slots)
+            slots.append(value)
+        return slot_of[key]
+
+    ops, memo = [], {}
+
+    def emit(n):
+        # table loads are never memoised here: a load after a store to the
+        # same table must see the stored value (tie semantics); the library's
+        # compiler forwards and deduplicates them
+        if n.op != "LOAD" and id(n) in memo:
+            return memo[id(n)]
+        if n.op == "LOAD":
+            s = slot(("t", n.table.data_ptr(), n.table.dtype), n.table)
+            ops.append((lib.OP["LOAD"], n.dtype, s, -1, -1, 0.0))
+        elif n.op == "SCALAR":
+            s = slot(("s", id(n)), n)
+            ops.append((lib.OP["SCALAR"], n.dtype, s, -1, -1, 0.0))
+        elif n.op == "CONST":
+            ops.append((lib.OP["CONST"], n.dtype, -1, -1, -1, n.imm))
+        else:
+            a = [emit(x) for x in n.args] + [-1, -1, -1]
+            dt = _compare_dtype(n) if n.op in ("LT", "GT", "LE", "GE", "EQ", "NE") else n.dtype
+            ops.append((lib.OP[n.op], dt, a[0], a[1], a[2], 0.0))
+        memo[id(n)] = len(ops) - 1
+        return memo[id(n)]
+
+    for o, e in zip(outs, exprs):
+        v = emit(e)
+        dt = lib.U8 if o.dtype.is_floating_point is False else lib.F32
+        s = slot(("t", o.data_ptr(), o.dtype), o)
+        ops.append((lib.OP["STORE"], dt, v, s, -1, 0.0))
+    return ops, slots
+
+
+class Program:
+    def __init__(self, ops, n_slots):
+        arr = (lib.Op * len(ops))(*[lib.Op(*o) for o in ops])
+        h = ctypes.c_void_p()
+        lib.check(lib.load().nt2g_program_create(arr, len(ops), n_slots, ctypes.byref(h)))
+        self.handle = h
+
+    def info(self):
+        inf = lib.ProgramInfo()
+        lib.check(lib.load().nt2g_program_info_get(self.handle, ctypes.byref(inf)))
+        return inf
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib.load().nt2g_program_destroy(self.handle)
+        except Exception:
+            pass
+
+
+_cache = {}
+
+
+def compile_program(outs, exprs):
+    ops, slots = lower(outs, exprs)
+    key = (tuple(ops), len(slots))
+    prog = _cache.get(key)
+    if prog is None:
+        prog = _cache[key] = Program(ops, len(slots))
+    return prog, slots
+
+
+def assign(outs, exprs, precision=lib.PREC_FAST, offset=0, count=None, force_generic=False, stream=None):
+    """tie(outs...) = tie(exprs...) over elements [offset, offset+count)."""
+    import torch
+    outs, exprs = list(outs), list(exprs)
+    prog, slots = compile_program(outs, exprs)
+    args = (lib.Arg * len(slots))()
+    n = None
+    for i, s in enumerate(slots):
+        if isinstance(s, Node):  # a SCALAR leaf
+            args[i] = lib.Arg(None, s.imm, s.dtype, 1)
+        else:
+            n = s.numel() if n is None else min(n, s.numel())
+            args[i] = lib.Arg(s.data_ptr(), 0.0, lib.U8 if s.dtype == torch.uint8 else lib.F32, 0)
+    if count is None:
+        count = n - offset
+    lib.check(lib.load().nt2g_eval(prog.handle, args, len(slots), offset, count, precision,
+                                   1 if force_generic else 0, lib._stream(stream)))
+    return prog

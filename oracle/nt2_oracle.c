@@ -1,0 +1,540 @@
+/*
+ * nt2_oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of NT2's scalar float algorithms for the fused-expression
+ * and reduction hot path, plus FP64 reference formulas and an exact
+ * superaccumulator.  It is the checker for the CUDA library and the timed CPU
+ * baseline; nothing in the product links or calls it.
+ *
+ * Only tests, the smoke check and the benchmark's CPU-baseline leg load this
+ * file (as liboracle.so through ctypes).
+ *
+ * Build: gcc -O2 -std=c11 -ffp-contract=off -fopenmp -fPIC -shared.
+ * -ffp-contract=off matters: NT2's generic fma/fnms and its Horner scheme are
+ * unfused (a*b+c with two roundings), and GCC defaults to contraction on
+ * aarch64.
+ *
+ * Parity pinning: the elementary functions are checked against the golden
+ * values in NT2's own unit tests (tests/golden/nt2_unit_vectors.json).
+ * Whole-expression outputs have no golden vectors in the reference (its demos
+ * assert nothing), so for those this restatement plus the FP64 formulas are
+ * the oracle.
+ *
+ * Citations are paths inside the NT2 source tree:
+ *   EXP  = modules/core/exponential/include/nt2/exponential/functions
+ *   EUL  = modules/core/euler/include/nt2/euler/functions
+ *   STAT = modules/core/statistics/include/nt2/statistics/functions
+ *   BSIMD= modules/boost/simd/base/include/boost/simd
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define EXPORT __attribute__((visibility("default")))
+
+static inline float bf(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+static inline uint32_t fb(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+
+/* NT2 float constants (hex as in the NT2 constant headers). */
+#define C_MAXLOG      0x42b0c0a5u /* EXP/../constants/maxlog.hpp:29  88.3763 */
+#define C_MINLOG      0xc2b0c0a5u /* minlog.hpp:29 */
+#define C_INVLOG_2    0x3fb8aa3bu /* invlog_2.hpp:29 */
+#define C_LOG_2HI     0x3f318000u /* log_2hi.hpp:29  0.693359375 */
+#define C_LOG_2LO     0xb95e8083u /* log_2lo.hpp:29 -2.1219444e-4 */
+#define C_SQRT_2O_2   0x3F3504F3u /* BSIMD/constant/constants/sqrt_2o_2.hpp:30 */
+#define C_SMALLESTPOS 0x00800000u /* smallestposval.hpp:30 */
+#define C_TWOTONMB    0x4B000000u /* twotonmb.hpp:30  2^23 */
+#define C_MLOGTWO2NMB 0xc17f1402u /* mlogtwo2nmb.hpp:29 */
+#define C_TWOTHIRD    0x3f2aaaabu /* twothird.hpp:30 */
+#define C_INVSQRT_2PI 0x3ecc422au /* invsqrt_2pi.hpp:28 */
+
+/* Static Horner, NT2 order: c[0] is the highest degree; each step is
+ * x*acc + c (unfused fma).  POLY/scalar/impl/horner.hpp:37-53. */
+static inline float horner(float x, const uint32_t *c, int n)
+{
+    float r = bf(c[0]);
+    for (int i = 1; i < n; ++i) r = x * r + bf(c[i]);
+    return r;
+}
+
+/* round2even: BSIMD/arithmetic/functions/scalar/round2even.hpp:29-36 */
+static inline float round2even(float a0)
+{
+    const float v = fabsf(a0), t2n = bf(C_TWOTONMB);
+    volatile float d0 = v + t2n; /* volatile keeps the add/sub pair literal */
+    float d = d0 - t2n;
+    d = (v < t2n) ? d : v;
+    return a0 < 0.0f ? -d : d;
+}
+
+/* ---------------------------------------------------------------- exp ----
+ * EXP/scalar/impl/expo/expo_base.hpp:58-69 (driver),
+ * EXP/scalar/impl/expo/f_expo_reduction.hpp:52-85 (reduce + approx),
+ * EXP/scalar/impl/expo/expo_scale.hpp:27-35 (2^k by exponent bits). */
+static const uint32_t EXP_P[5] = {0x3ab778cf, 0x3c098d8b, 0x3d2aa957, 0x3e2aa9a5, 0x3f000000};
+
+EXPORT float o_exp(float a0)
+{
+    if (a0 >= bf(C_MAXLOG)) return INFINITY;
+    if (a0 <= bf(C_MINLOG)) return 0.0f;
+    if (a0 != a0) return a0;
+    float k = round2even(bf(C_INVLOG_2) * a0);
+    float x = a0 - k * bf(C_LOG_2HI);
+    x = x - k * bf(C_LOG_2LO);
+    float y = horner(x, EXP_P, 5);
+    float c = (y * (x * x) + x) + 1.0f;
+    int32_t ik = (int32_t)k + 127;
+    ik = (int32_t)((uint32_t)ik << 23);
+    return c * bf((uint32_t)ik);
+}
+
+/* ---------------------------------------------------------------- log ----
+ * EXP/scalar/impl/logs/f_log.hpp:59-88, kernel f_kernel.hpp:43-75,
+ * fast_frexp BSIMD/ieee/functions/scalar/fast_frexp.hpp:52-58. */
+static const uint32_t LOG_P[8] = {0xbda5dff0, 0x3e0229f9, 0xbe04d6b7, 0x3e116e80,
+                                  0xbe2a6aa0, 0x3e4cd0a3, 0xbe800064, 0x3eaaaaa9};
+
+EXPORT float o_log(float a0)
+{
+    if (a0 == INFINITY) return a0;
+    if (a0 == 0.0f) return -INFINITY;
+    if (a0 != a0 || a0 < 0.0f) return NAN;
+    float z = a0, t = 0.0f;
+    if (fabsf(z) < bf(C_SMALLESTPOS)) { z *= bf(C_TWOTONMB); t = bf(C_MLOGTWO2NMB); }
+    uint32_t u = fb(z);
+    int32_t e = (int32_t)((u & 0x7f800000u) >> 23) - 126;
+    float x = bf((u & ~0x7f800000u) | 0x3f000000u);
+    int lt = x < bf(C_SQRT_2O_2);
+    float fe = lt ? (float)e + (-1.0f) : (float)e;
+    x = (lt ? x + x : x) - 1.0f;
+    float x2 = x * x;
+    float y = horner(x, LOG_P, 8) * x * x2;
+    y = fe * bf(C_LOG_2LO) + y;
+    y = -0.5f * x2 + y;
+    return bf(C_LOG_2HI) * fe + ((x + y) + t);
+}
+
+/* -------------------------------------------------------------- log1p ----
+ * EXP/scalar/log1p.hpp:35-45 */
+EXPORT float o_log1p(float a0)
+{
+    if (-1.0f > a0) return NAN;
+    if (a0 == INFINITY) return INFINITY;
+    if (a0 == -1.0f) return -INFINITY;
+    float u = 1.0f + a0;
+    return o_log(u) + (a0 - (u - 1.0f)) / u;
+}
+
+/* --------------------------------------------------------------- erfc ----
+ * EUL/scalar/erfc.hpp:83-104, polynomials EUL/details/erf_kernel.hpp:48-91 */
+static const uint32_t ERFC2_P[11] = {0xc0283611, 0x40d67e3b, 0xc0cd1a85, 0x4050b063,
+                                     0xbfaea865, 0x3e2006f0, 0x3e1175c7, 0x3ec4ca6e,
+                                     0x3e243828, 0xbf918a62, 0x3f0a0e8b};
+static const uint32_t ERFC3_P[9] = {0x41aa8e55, 0x401b5680, 0xc010d956, 0x3f2cff3b,
+                                    0xc016c985, 0xbffc9284, 0xbfa11698, 0xbe036d7e,
+                                    0x3f7ffffe};
+
+/* erfc(|a0|) before the sign fold; shared by erfc, normcdf and the fused
+ * call/put pairs, which in NT2 differ only in the final 2-r select. */
+static inline float erfc_core(float x)
+{
+    float z = x / (1.0f + x);
+    if (x < bf(C_TWOTHIRD)) return (1.0f - z) * horner(z, ERFC3_P, 9);
+    if (x == INFINITY) return 0.0f;
+    z -= 0.4f;
+    return o_exp(-(x * x)) * horner(z, ERFC2_P, 11);
+}
+
+EXPORT float o_erfc(float a0)
+{
+    float r1 = erfc_core(fabsf(a0));
+    return (a0 < 0.0f) ? 2.0f - r1 : r1;
+}
+
+/* normcdf: STAT/generic/normcdf.hpp:34  Half*erfc(-Sqrt_2o_2*a0) */
+EXPORT float o_normcdf(float a0) { return 0.5f * o_erfc(-bf(C_SQRT_2O_2) * a0); }
+
+/* fastnormcdf: STAT/generic/fastnormcdf.hpp:39-54 (A&S 26.2.17 form) */
+static const uint32_t FNCDF_P[5] = {0x3faa466f, 0xbfe91eea, 0x3fe40778, 0xbeb68f87, 0x3ea385fa};
+
+EXPORT float o_fastnormcdf(float a0)
+{
+    float l = fabsf(a0);
+    float k = 1.0f / (0.2316419f * l + 1.0f);
+    float w = horner(k, FNCDF_P, 5);
+    w *= k * bf(C_INVSQRT_2PI) * o_exp(-(l * l) * 0.5f);
+    return (a0 > 0.0f) ? 1.0f - w : w;
+}
+
+/* ------------------------------------------------- elementwise maps ---- */
+enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT };
+
+EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        float a = x[i];
+        switch (fn) {
+        case FN_EXP: y[i] = o_exp(a); break;
+        case FN_LOG: y[i] = o_log(a); break;
+        case FN_LOG1P: y[i] = o_log1p(a); break;
+        case FN_ERFC: y[i] = o_erfc(a); break;
+        case FN_NORMCDF: y[i] = o_normcdf(a); break;
+        case FN_FASTNORMCDF: y[i] = o_fastnormcdf(a); break;
+        default: y[i] = sqrtf(a); break;
+        }
+    }
+}
+
+/* FP64 reference of the same functions on float inputs (glibc double libm). */
+EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        double a = (double)x[i];
+        switch (fn) {
+        case FN_EXP: y[i] = exp(a); break;
+        case FN_LOG: y[i] = log(a); break;
+        case FN_LOG1P: y[i] = log1p(a); break;
+        case FN_ERFC: y[i] = erfc(a); break;
+        case FN_NORMCDF:
+        case FN_FASTNORMCDF: y[i] = 0.5 * erfc(-a / sqrt(2.0)); break;
+        default: y[i] = sqrt(a); break;
+        }
+    }
+}
+
+/* ------------------------------------------------ Black-Scholes --------
+ * Textbook call+put written as the NT2 expression a user would assign
+ * through tie():
+ *   d1 = (log(S/K) + fma(sqr(sig),0.5,r)*T) / (sig*sqrt(T))
+ *   d2 = fnms(sig, sqrt(T), d1)
+ *   e  = K*exp(-r*T)
+ *   call = fnms(e, normcdf(d2), S*normcdf(d1))
+ *   put  = fnms(S, normcdf(-d1), e*normcdf(-d2))
+ * Operator semantics follow the demo (demo/blackscholes/nt2/
+ * blackandscholes_nt2.cpp:55-59): fma/fnms unfused, -r*T is (-r)*T.
+ * sig and r are either per-option tables (pointer non-NULL) or scalars. */
+static inline void bs_one(float S, float K, float T, float sig, float r, float *call, float *put)
+{
+    float sq = sqrtf(T);
+    float d1 = (o_log(S / K) + ((sig * sig) * 0.5f + r) * T) / (sig * sq);
+    float d2 = d1 - sig * sq;
+    float e = K * o_exp((-r) * T);
+    float n1 = o_normcdf(d1), n2 = o_normcdf(d2);
+    float m1 = o_normcdf(-d1), m2 = o_normcdf(-d2);
+    *call = S * n1 - e * n2;
+    *put = e * m2 - S * m1;
+}
+
+EXPORT void o_bs_f32(const float *S, const float *K, const float *T, const float *sig_tab,
+                     float sig, const float *r_tab, float r, float *call, float *put, int64_t n,
+                     int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t i = 0; i < n; ++i)
+        bs_one(S[i], K[i], T[i], sig_tab ? sig_tab[i] : sig, r_tab ? r_tab[i] : r, &call[i], &put[i]);
+}
+
+/* NT2 demo form, call only, fastnormcdf, non-textbook d1 (log term not
+ * divided): demo/blackscholes/nt2/blackandscholes_nt2.cpp:55-59. */
+EXPORT void o_bs_demo_f32(const float *S, const float *K, const float *T, const float *r_tab, float r,
+                          const float *v_tab, float v, float *R, int64_t n, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t i = 0; i < n; ++i) {
+        float ri = r_tab ? r_tab[i] : r, vi = v_tab ? v_tab[i] : v;
+        float da = sqrtf(T[i]);
+        float d1 = o_log(S[i] / K[i]) + (((vi * vi) * 0.5f + ri) * T[i]) / (vi * da);
+        float d2 = d1 - vi * da;
+        R[i] = S[i] * o_fastnormcdf(d1) - (K[i] * o_exp((-ri) * T[i])) * o_fastnormcdf(d2);
+    }
+}
+
+/* FP64 textbook BS on the float inputs.  terms (optional, 4 per option):
+ * S*N(d1), K e^{-rT} N(d2), K e^{-rT} N(-d2), S*N(-d1) -- the magnitudes the
+ * conditioned error metric scales by. */
+static inline double ncdf64(double x) { return 0.5 * erfc(-x / sqrt(2.0)); }
+
+EXPORT void o_bs_f64(const float *S, const float *K, const float *T, const float *sig_tab, float sig,
+                     float r, double *call, double *put, double *terms, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        double s = S[i], k = K[i], t = T[i], v = sig_tab ? sig_tab[i] : sig, rr = r;
+        double sq = sqrt(t);
+        double d1 = (log(s / k) + (rr + 0.5 * v * v) * t) / (v * sq);
+        double d2 = d1 - v * sq;
+        double e = k * exp(-rr * t);
+        double a = s * ncdf64(d1), b = e * ncdf64(d2), c = e * ncdf64(-d2), d = s * ncdf64(-d1);
+        call[i] = a - b;
+        put[i] = c - d;
+        if (terms) { terms[4 * i] = a; terms[4 * i + 1] = b; terms[4 * i + 2] = c; terms[4 * i + 3] = d; }
+    }
+}
+
+/* Analytic FP64 vector-Jacobian product of (call, put) w.r.t. S, K, T, sigma,
+ * r, given upstream gradients gc, gp.  Used to check the adjoint kernel. */
+EXPORT void o_bs_vjp_f64(const float *S, const float *K, const float *T, const float *sig_tab, float sig,
+                         float r, const float *gc, const float *gp, double *dS, double *dK, double *dT,
+                         double *dsig, double *dr, int64_t n)
+{
+    const double inv_sqrt_2pi = 0.398942280401432677939946059934;
+    for (int64_t i = 0; i < n; ++i) {
+        double s = S[i], k = K[i], t = T[i], v = sig_tab ? sig_tab[i] : sig, rr = r;
+        double sq = sqrt(t);
+        double d1 = (log(s / k) + (rr + 0.5 * v * v) * t) / (v * sq);
+        double d2 = d1 - v * sq;
+        double df = exp(-rr * t);
+        double pdf1 = inv_sqrt_2pi * exp(-0.5 * d1 * d1);
+        double n1 = ncdf64(d1), n2 = ncdf64(d2), m1 = ncdf64(-d1), m2 = ncdf64(-d2);
+        double gC = gc[i], gP = gp[i];
+        dS[i] = gC * n1 - gP * m1;
+        dK[i] = -gC * df * n2 + gP * df * m2;
+        double thetaC = s * pdf1 * v / (2.0 * sq) + rr * k * df * n2;
+        double thetaP = s * pdf1 * v / (2.0 * sq) - rr * k * df * m2;
+        dT[i] = gC * thetaC + gP * thetaP;
+        dsig[i] = (gC + gP) * s * pdf1 * sq;
+        dr[i] = gC * k * t * df * n2 - gP * k * t * df * m2;
+    }
+}
+
+/* FP64 forward used by the central finite-difference check (same formula as
+ * o_bs_f64, parameters in double so a perturbation h is not rounded away). */
+EXPORT void o_bs_point_f64(double s, double k, double t, double v, double rr, double *call, double *put)
+{
+    double sq = sqrt(t);
+    double d1 = (log(s / k) + (rr + 0.5 * v * v) * t) / (v * sq);
+    double d2 = d1 - v * sq;
+    double e = k * exp(-rr * t);
+    *call = s * ncdf64(d1) - e * ncdf64(d2);
+    *put = e * ncdf64(-d2) - s * ncdf64(-d1);
+}
+
+/* ------------------------------------------------ other expressions ---- */
+/* saxpy: demo/saxpy/nt2/saxpy_nt2.cpp:41  Y = alpha*X + Y (two roundings) */
+EXPORT void o_saxpy_f32(float alpha, const float *X, float *Y, int64_t n, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t i = 0; i < n; ++i) Y[i] = alpha * X[i] + Y[i];
+}
+
+/* expr3 = exp(-sqr(x))*sqrt(abs(y)) + log1p(abs(z)) */
+EXPORT void o_expr3_f32(const float *x, const float *y, const float *z, float *out, int64_t n, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t i = 0; i < n; ++i)
+        out[i] = o_exp(-(x[i] * x[i])) * sqrtf(fabsf(y[i])) + o_log1p(fabsf(z[i]));
+}
+
+EXPORT void o_expr3_f64(const float *x, const float *y, const float *z, double *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        double a = x[i], b = y[i], c = z[i];
+        out[i] = exp(-a * a) * sqrt(fabs(b)) + log1p(fabs(c));
+    }
+}
+
+/* rgb2yuv: demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:30-32 (three statements; u and v
+ * re-read the stored y). */
+EXPORT void o_rgb2yuv_f32(const float *r, const float *g, const float *b, float *y, float *u, float *v,
+                          int64_t n, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t i = 0; i < n; ++i) {
+        float yy = 0.299f * r[i] + 0.587f * g[i] + 0.114f * b[i];
+        y[i] = yy;
+        u[i] = 0.492f * (b[i] - yy);
+        v[i] = 0.877f * (r[i] - yy);
+    }
+}
+
+/* Sigma-delta step on uint8 pixels: demo/sigmadelta/nt2/sigmadelta_nt2.cpp:38-57
+ * with selinc/seldec (BSIMD/boolean/functions/scalar/selinc.hpp:27,
+ * seldec.hpp:27), saturating adds for unsigned
+ * (BSIMD/arithmetic/functions/scalar/adds.hpp:54-66) and if_zero_else_one on a
+ * logical (BSIMD/boolean/functions/scalar/if_zero_else_one.hpp:21-29).
+ * The diff and mul temporaries are not stored. */
+static inline uint8_t adds_u8(uint8_t a, uint8_t b)
+{
+    unsigned s = (unsigned)a + (unsigned)b;
+    return (uint8_t)(s > 255u ? 255u : s);
+}
+
+EXPORT void o_sigmadelta_u8(const uint8_t *fr, uint8_t *bkg, uint8_t *var, uint8_t *label, int64_t n,
+                            int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t i = 0; i < n; ++i) {
+        uint8_t f = fr[i], b = bkg[i], v = var[i];
+        b = (b < f) ? (uint8_t)(b + 1) : ((b > f) ? (uint8_t)(b - 1) : b);
+        uint8_t d = (uint8_t)((b > f ? b : f) - (b < f ? b : f));
+        uint8_t m = adds_u8(adds_u8(d, d), d);
+        if (d != 0) v = (v < m) ? (uint8_t)(v + 1) : ((v > m) ? (uint8_t)(v - 1) : v);
+        bkg[i] = b;
+        var[i] = v;
+        label[i] = (d < v) ? 0 : 1;
+    }
+}
+
+/* ------------------------------------------------------- reductions ----
+ * NT2 fold schedule (OMP/spawner/fold.hpp:37-81 with the shared_memory
+ * inner_fold worker, SHM/sdk/shared_memory/worker/inner_fold.hpp:64-98):
+ * grain = top_cache_line_size(2)/sizeof(float) = 16 elements; each block of
+ * 16 is folded naively in FP32 from zero, then added to the total inside an
+ * omp critical section (combine order is thread-timing dependent); the tail
+ * n % 16 is folded serially afterwards.  dot(x,y) = sum(x*y) with the
+ * product rounded to float (RED/reduction/functions/expr/dot.hpp:22-42). */
+static int64_t nt2_line_grain(void)
+{
+    /* top_cache_line_size(2): the L3 line when an L3 size is reported, else
+     * the L2 line.  NT2 would divide by zero when both read 0 (common on
+     * aarch64 glibc); the restatement uses a 64-byte line there. */
+    long line = sysconf(_SC_LEVEL3_CACHE_SIZE) > 0 ? sysconf(_SC_LEVEL3_CACHE_LINESIZE)
+                                                   : sysconf(_SC_LEVEL2_CACHE_LINESIZE);
+    if (line <= 0) line = 64;
+    return line / (long)sizeof(float);
+}
+
+EXPORT float o_sum_nt2_f32(const float *x, const float *y, int64_t n, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    int64_t grain = nt2_line_grain();
+    int64_t nblocks = n / grain;
+    float total = 0.0f;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t b = 0; b < nblocks; ++b) {
+        float out = 0.0f;
+        const int64_t o = b * grain;
+        if (y) for (int64_t j = 0; j < grain; ++j) out = out + x[o + j] * y[o + j];
+        else for (int64_t j = 0; j < grain; ++j) out = out + x[o + j];
+#pragma omp critical
+        total = total + out;
+    }
+    for (int64_t i = nblocks * grain; i < n; ++i) total = total + (y ? x[i] * y[i] : x[i]);
+    return total;
+}
+
+/* Same blocks, one private partial per thread, combined once: the plain
+ * all-cores schedule reported beside the NT2-rule one. */
+EXPORT float o_sum_plain_f32(const float *x, const float *y, int64_t n, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    float total = 0.0f;
+#pragma omp parallel for schedule(static) num_threads(nthreads) reduction(+ : total)
+    for (int64_t i = 0; i < n; ++i) total += y ? x[i] * y[i] : x[i];
+    return total;
+}
+
+/* globalsum: serial accumulation (RED/core/functions/scalar/global.hpp:17-43) */
+EXPORT float o_globalsum_f32(const float *x, int64_t n)
+{
+    float s = 0.0f;
+    for (int64_t i = 0; i < n; ++i) s = s + x[i];
+    return s;
+}
+
+/* Exact superaccumulator.  Every float and every float*float product is an
+ * integer m (<= 53 bits) times 2^e with e >= -351; digits hold signed sums of
+ * 32-bit chunks at weight 2^(32*i + ACC_BASE), covering 2^-416 .. 2^352. */
+#define ACC_BASE (-416)
+#define ACC_DIGITS 24
+typedef struct { int64_t d[ACC_DIGITS]; } superacc;
+
+static void acc_norm(superacc *a)
+{
+    for (int i = 0; i < ACC_DIGITS - 1; ++i) {
+        int64_t c = a->d[i] >> 32; /* arithmetic shift: floor division */
+        a->d[i] -= c * ((int64_t)1 << 32);
+        a->d[i + 1] += c;
+    }
+}
+
+static inline void acc_add(superacc *a, double v)
+{
+    if (v == 0.0) return;
+    int ex;
+    double f = frexp(fabs(v), &ex);
+    uint64_t m = (uint64_t)ldexp(f, 53);
+    int p = ex - 53 - ACC_BASE;
+    int i = p >> 5, s = p & 31;
+    /* m << s is at most 85 bits: three 32-bit digits */
+    unsigned __int128 w = (unsigned __int128)m << s;
+    int64_t c0 = (int64_t)(uint32_t)w, c1 = (int64_t)(uint32_t)(w >> 32), c2 = (int64_t)(uint64_t)(w >> 64);
+    if (v < 0) { a->d[i] -= c0; a->d[i + 1] -= c1; a->d[i + 2] -= c2; }
+    else { a->d[i] += c0; a->d[i + 1] += c1; a->d[i + 2] += c2; }
+}
+
+static double acc_value(superacc a)
+{
+    acc_norm(&a);
+    int neg = a.d[ACC_DIGITS - 1] < 0;
+    if (neg) {
+        for (int i = 0; i < ACC_DIGITS; ++i) a.d[i] = -a.d[i];
+        acc_norm(&a);
+    }
+    long double r = 0.0L;
+    for (int i = ACC_DIGITS - 1; i >= 0; --i) r += ldexpl((long double)a.d[i], 32 * i + ACC_BASE);
+    return neg ? -(double)r : (double)r;
+}
+
+/* Exact sum (y == NULL) or exact dot.  Returns the exact value rounded to
+ * double; abs_sum receives sum |x_i| (or |x_i*y_i|) for the condition number. */
+EXPORT double o_exact_sum(const float *x, const float *y, int64_t n, int nthreads, double *abs_sum)
+{
+    if (nthreads < 1) nthreads = 1;
+    superacc total;
+    memset(&total, 0, sizeof total);
+    double asum = 0.0;
+#pragma omp parallel num_threads(nthreads) reduction(+ : asum)
+    {
+        superacc a;
+        memset(&a, 0, sizeof a);
+        int64_t cnt = 0;
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            double v = y ? (double)x[i] * (double)y[i] : (double)x[i];
+            acc_add(&a, v);
+            asum += fabs(v);
+            if (++cnt == (1 << 24)) { acc_norm(&a); cnt = 0; }
+        }
+        acc_norm(&a);
+#pragma omp critical
+        {
+            for (int i = 0; i < ACC_DIGITS; ++i) total.d[i] += a.d[i];
+            acc_norm(&total);
+        }
+    }
+    if (abs_sum) *abs_sum = asum;
+    return acc_value(total);
+}
+
+/* NT2 grain for transform on Linux without cpuid: top_cache_size(2) reads
+ * cache_sizes_[2], which the sysconf path fills with the L3 size in bytes
+ * (modules/sdk/config/include/nt2/sdk/config/details/cache.hpp:26-39,
+ * .../config/cache.hpp:46-58); transform goes parallel only when
+ * n > 8*grain (SHM/core/functions/shared_memory/transform.hpp:39-49). */
+EXPORT int64_t o_nt2_transform_grain(int64_t elem_size)
+{
+    long c = sysconf(_SC_LEVEL3_CACHE_SIZE);
+    if (c <= 0) c = sysconf(_SC_LEVEL2_CACHE_SIZE);
+    int64_t g = c > 0 ? (int64_t)c / elem_size : 0;
+    return g ? g : 1;
+}
+
+EXPORT int o_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

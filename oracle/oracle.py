@@ -1,0 +1,209 @@
+"""TEST INFRASTRUCTURE ONLY -- loader for the CPU oracle (nt2_oracle.c).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, as the checker and as the timed CPU baseline.  The product library
+never links, loads or calls it.
+
+The reference itself cannot be built here (it needs Boost >= 1.59 and
+configure-time generated headers), so there is no oracle/_ref; the oracle is
+the restatement in nt2_oracle.c, pinned against NT2's unit-test golden values
+(tests/golden/nt2_unit_vectors.json).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SO = os.path.join(HERE, "_build", "liboracle.so")
+SRC = os.path.join(HERE, "nt2_oracle.c")
+
+FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6)
+
+
+def build():
+    os.makedirs(os.path.dirname(SO), exist_ok=True)
+    if os.path.exists(SO) and os.path.getmtime(SO) >= os.path.getmtime(SRC):
+        return SO
+    # -ffp-contract=off: NT2's fma/fnms/Horner are unfused (two roundings)
+    subprocess.run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+                    "-shared", "-o", SO, SRC, "-lm"], check=True)
+    return SO
+
+
+_L = None
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+
+
+def lib():
+    global _L
+    if _L is None:
+        build()
+        L = ctypes.CDLL(SO)
+        for f in ("o_exp", "o_log", "o_log1p", "o_erfc", "o_normcdf", "o_fastnormcdf"):
+            getattr(L, f).restype = ctypes.c_float
+            getattr(L, f).argtypes = [ctypes.c_float]
+        L.o_map_f32.argtypes = [ctypes.c_int, _P, _P, _I64]
+        L.o_map_f64.argtypes = [ctypes.c_int, _P, _P, _I64]
+        L.o_bs_f32.argtypes = [_P, _P, _P, _P, ctypes.c_float, _P, ctypes.c_float, _P, _P, _I64, ctypes.c_int]
+        L.o_bs_demo_f32.argtypes = [_P, _P, _P, _P, ctypes.c_float, _P, ctypes.c_float, _P, _I64, ctypes.c_int]
+        L.o_bs_f64.argtypes = [_P, _P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P, _P, _I64]
+        L.o_bs_vjp_f64.argtypes = [_P, _P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P, _P, _P, _P, _I64]
+        L.o_bs_point_f64.argtypes = [ctypes.c_double] * 5 + [_P, _P]
+        L.o_saxpy_f32.argtypes = [ctypes.c_float, _P, _P, _I64, ctypes.c_int]
+        L.o_expr3_f32.argtypes = [_P, _P, _P, _P, _I64, ctypes.c_int]
+        L.o_expr3_f64.argtypes = [_P, _P, _P, _P, _I64]
+        L.o_rgb2yuv_f32.argtypes = [_P, _P, _P, _P, _P, _P, _I64, ctypes.c_int]
+        L.o_sigmadelta_u8.argtypes = [_P, _P, _P, _P, _I64, ctypes.c_int]
+        L.o_sum_nt2_f32.restype = ctypes.c_float
+        L.o_sum_nt2_f32.argtypes = [_P, _P, _I64, ctypes.c_int]
+        L.o_sum_plain_f32.restype = ctypes.c_float
+        L.o_sum_plain_f32.argtypes = [_P, _P, _I64, ctypes.c_int]
+        L.o_globalsum_f32.restype = ctypes.c_float
+        L.o_globalsum_f32.argtypes = [_P, _I64]
+        L.o_exact_sum.restype = ctypes.c_double
+        L.o_exact_sum.argtypes = [_P, _P, _I64, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        L.o_nt2_transform_grain.restype = _I64
+        L.o_nt2_transform_grain.argtypes = [_I64]
+        L.o_max_threads.restype = ctypes.c_int
+        _L = L
+    return _L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def map_f32(fn, x):
+    x = _f32(x)
+    y = np.empty_like(x)
+    lib().o_map_f32(FN[fn], _p(x), _p(y), x.size)
+    return y
+
+
+def map_f64(fn, x):
+    x = _f32(x)
+    y = np.empty(x.shape, np.float64)
+    lib().o_map_f64(FN[fn], _p(x), _p(y), x.size)
+    return y
+
+
+def threads():
+    return lib().o_max_threads()
+
+
+def blackscholes(S, K, T, r, sigma, nthreads=None):
+    """NT2 restatement (float), textbook call+put; sigma scalar or array."""
+    S, K, T = _f32(S), _f32(K), _f32(T)
+    call, put = np.empty_like(S), np.empty_like(S)
+    sig_t = _f32(sigma) if isinstance(sigma, np.ndarray) else None
+    lib().o_bs_f32(_p(S), _p(K), _p(T), _p(sig_t), 0.0 if sig_t is not None else float(sigma), None, float(r),
+                   _p(call), _p(put), S.size, nthreads or threads())
+    return call, put
+
+
+def blackscholes_f64(S, K, T, r, sigma):
+    S, K, T = _f32(S), _f32(K), _f32(T)
+    call, put = np.empty(S.shape), np.empty(S.shape)
+    terms = np.empty((S.size, 4))
+    sig_t = _f32(sigma) if isinstance(sigma, np.ndarray) else None
+    lib().o_bs_f64(_p(S), _p(K), _p(T), _p(sig_t), 0.0 if sig_t is not None else float(sigma), float(r),
+                   _p(call), _p(put), _p(terms), S.size)
+    return call, put, terms
+
+
+def blackscholes_demo(S, X, T, r, v, nthreads=None):
+    S, X, T = _f32(S), _f32(X), _f32(T)
+    R = np.empty_like(S)
+    r_t = _f32(r) if isinstance(r, np.ndarray) else None
+    v_t = _f32(v) if isinstance(v, np.ndarray) else None
+    lib().o_bs_demo_f32(_p(S), _p(X), _p(T), _p(r_t), 0.0 if r_t is not None else float(r), _p(v_t),
+                        0.0 if v_t is not None else float(v), _p(R), S.size, nthreads or threads())
+    return R
+
+
+def blackscholes_vjp_f64(S, K, T, sigma, r, gc, gp):
+    S, K, T, sigma, gc, gp = (_f32(a) for a in (S, K, T, sigma, gc, gp))
+    outs = [np.empty(S.shape) for _ in range(5)]
+    lib().o_bs_vjp_f64(_p(S), _p(K), _p(T), _p(sigma), 0.0, float(r), _p(gc), _p(gp), *[_p(o) for o in outs],
+                       S.size)
+    return outs
+
+
+def blackscholes_point_f64(s, k, t, v, r):
+    c, p = ctypes.c_double(), ctypes.c_double()
+    lib().o_bs_point_f64(s, k, t, v, r, ctypes.byref(c), ctypes.byref(p))
+    return c.value, p.value
+
+
+def saxpy(alpha, X, Y, nthreads=None):
+    X, Y = _f32(X), _f32(Y).copy()
+    lib().o_saxpy_f32(float(alpha), _p(X), _p(Y), X.size, nthreads or threads())
+    return Y
+
+
+def expr3(x, y, z, nthreads=None):
+    x, y, z = _f32(x), _f32(y), _f32(z)
+    o = np.empty_like(x)
+    lib().o_expr3_f32(_p(x), _p(y), _p(z), _p(o), x.size, nthreads or threads())
+    return o
+
+
+def expr3_f64(x, y, z):
+    x, y, z = _f32(x), _f32(y), _f32(z)
+    o = np.empty(x.shape)
+    lib().o_expr3_f64(_p(x), _p(y), _p(z), _p(o), x.size)
+    return o
+
+
+def rgb2yuv(r, g, b, nthreads=None):
+    r, g, b = _f32(r), _f32(g), _f32(b)
+    y, u, v = np.empty_like(r), np.empty_like(r), np.empty_like(r)
+    lib().o_rgb2yuv_f32(_p(r), _p(g), _p(b), _p(y), _p(u), _p(v), r.size, nthreads or threads())
+    return y, u, v
+
+
+def sigmadelta(frame, bkg, var, nthreads=None):
+    """One step; returns new (bkg, var, label)."""
+    frame = np.ascontiguousarray(frame, dtype=np.uint8)
+    bkg, var = np.array(bkg, dtype=np.uint8, copy=True), np.array(var, dtype=np.uint8, copy=True)
+    label = np.empty_like(bkg)
+    lib().o_sigmadelta_u8(_p(frame), _p(bkg), _p(var), _p(label), frame.size, nthreads or threads())
+    return bkg, var, label
+
+
+def sum_nt2(x, y=None, nthreads=None):
+    x = _f32(x)
+    y = None if y is None else _f32(y)
+    return float(np.float32(lib().o_sum_nt2_f32(_p(x), _p(y), x.size, nthreads or threads())))
+
+
+def sum_plain(x, y=None, nthreads=None):
+    x = _f32(x)
+    y = None if y is None else _f32(y)
+    return float(np.float32(lib().o_sum_plain_f32(_p(x), _p(y), x.size, nthreads or threads())))
+
+
+def globalsum(x):
+    x = _f32(x)
+    return float(np.float32(lib().o_globalsum_f32(_p(x), x.size)))
+
+
+def exact_sum(x, y=None, nthreads=None):
+    """Exact sum (or dot) of float data, rounded once to double; also
+    returns sum |x_i| (|x_i y_i|) for the condition number."""
+    x = _f32(x)
+    y = None if y is None else _f32(y)
+    a = ctypes.c_double()
+    v = lib().o_exact_sum(_p(x), _p(y), x.size, nthreads or threads(), ctypes.byref(a))
+    return v, a.value
+
+
+def nt2_transform_grain(elem_size=4):
+    return lib().o_nt2_transform_grain(elem_size)

@@ -1,0 +1,89 @@
+"""Regenerate nt2_unit_vectors.json from NT2's own unit tests.
+
+Reads the cited NT2_TEST_ULP_EQUAL / NT2_TEST_EQUAL lines of the reference's
+test sources as text (nothing of the reference is compiled or run), evaluates
+the NT2 constant spellings they use (Inf, Mzero, Half, Exp_1, T(0.4795...),
+...) for T = float, and writes one record per known answer:
+{fn, x, expected, tol_nt2ulp, source}.  The float tolerance is in NT2's ulp
+unit (half a standard ulp).
+
+Usage (needs the reference checkout):  python tests/golden/make_golden.py /path/to/nt2
+"""
+import json
+import math
+import os
+import re
+import sys
+
+import numpy as np
+
+# (file, first line, last line) inside the NT2 tree; each holds ULP checks of
+# one scalar float functor
+SOURCES = [
+    ("modules/core/exponential/unit/scalar/exp.cpp", 40, 46),
+    ("modules/core/exponential/unit/simd/log.cpp", 44, 51),
+    ("modules/core/euler/unit/scalar/erfc.cpp", 42, 53),
+    ("modules/core/statistics/unit/scalar/normcdf.cpp", 31, 36),
+    ("modules/core/statistics/unit/scalar/fastnormcdf.cpp", 26, 31),
+]
+
+E = float(np.float32(math.e))
+CONST = {
+    "Inf": math.inf, "Minf": -math.inf, "Nan": math.nan, "Zero": 0.0, "Mzero": -0.0, "One": 1.0, "Mone": -1.0,
+    "Half": 0.5, "Two": 2.0, "Ten": 10.0, "Exp_1": E, "Eps": float(np.finfo(np.float32).eps),
+}
+
+
+def _value(expr):
+    expr = expr.strip()
+    m = re.fullmatch(r"nt2::(\w+)<\w+>\(\)", expr)
+    if m:
+        return CONST[m.group(1)]
+    m = re.fullmatch(r"T\(([-+0-9.eE]+)\)", expr)
+    if m:
+        return float(np.float32(float(m.group(1))))
+    m = re.fullmatch(r"nt2::One<\w+>\(\)\s*/\s*nt2::Exp_1<\w+>\(\)", expr)
+    if m:
+        return float(np.float32(1.0) / np.float32(E))
+    raise ValueError(f"unhandled NT2 constant spelling: {expr!r}")
+
+
+PAT = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(\w+)\((.*?)\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
+
+
+def main(root):
+    out = []
+    for rel, lo, hi in SOURCES:
+        lines = open(os.path.join(root, rel)).read().splitlines()
+        for ln in range(lo, hi + 1):
+            m = PAT.search(lines[ln - 1])
+            if not m:
+                continue
+            fn, arg, exp, tol = m.groups()
+            out.append(dict(fn=fn, x=_value(arg), expected=_value(exp), tol_nt2ulp=float(tol),
+                            source=f"{rel}:{ln}"))
+    # normcdf on _(-5, 1, 5) against the 11-value table r0, 5 NT2-ulp
+    rel = "modules/core/statistics/unit/scalar/normcdf.cpp"
+    lines = open(os.path.join(root, rel)).read().splitlines()
+    text = " ".join(lines[53:57])  # lines 54-57: r0 = nt2::cons<T>( ... );
+    body = text[text.index("cons<T>(") + len("cons<T>("):text.index(");")]
+    vals = [float(np.float32(float(v))) for v in body.replace(")", "").split(",") if v.strip()]
+    assert len(vals) == 11, vals
+    for k, v in enumerate(vals):
+        out.append(dict(fn="normcdf", x=float(k - 5), expected=v, tol_nt2ulp=5.0, source=f"{rel}:53-61"))
+    # sum / dot / globalsum known answers (exact integers)
+    out.append(dict(fn="sum_ones", n=133, expected=133.0, source="modules/arch/openmp/unit/functions/sum.cpp:40-45"))
+    out.append(dict(fn="globalsum_1_to_9", expected=45.0,
+                    source="modules/core/reduction/unit/table/globalsum.cpp:24-25"))
+    out.append(dict(fn="globalsum_1_to_8", expected=36.0,
+                    source="modules/core/reduction/unit/table/globalsum.cpp:27-28"))
+    out.append(dict(fn="dot_5x3_i_minus_j", expected=float(sum((i - j) ** 2 for i in range(1, 6) for j in range(1, 4))),
+                    source="modules/core/reduction/unit/table/dot.cpp:46-59,73"))
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "nt2_unit_vectors.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1, default=lambda v: v)
+    print(f"wrote {len(out)} records to {path}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,111 @@
+"""Shared test helpers: ULP metrics and the seeded synthetic workloads.
+
+Seeds follow the workload index: Black-Scholes plain 1000, reductions 1001,
+sigma-delta / rgb2yuv 1002, batched 1003, adjoint 1004.
+"""
+import numpy as np
+
+F32 = np.float32
+
+
+def std_ulp(y, ref64):
+    """|y - ref| in standard ulps of the float32-rounded reference (adjacent
+    floats are 1 apart).  Both infinite with the same sign, or both NaN: 0."""
+    y = np.asarray(y, np.float32).astype(np.float64)
+    ref64 = np.asarray(ref64, np.float64)
+    sp = np.spacing(np.abs(ref64.astype(np.float32))).astype(np.float64)
+    with np.errstate(invalid="ignore"):
+        e = np.abs(y - ref64) / sp
+    same = (y == ref64) | (np.isnan(y) & np.isnan(ref64))
+    return np.where(same, 0.0, e)
+
+
+def nt2_ulpdist(a, b):
+    """NT2's ulpdist for float (frexp mantissa difference / Eps): half of the
+    standard ulp distance.  modules/boost/simd/base/include/boost/simd/ieee/
+    functions/scalar/ulpdist.hpp:56-80; modules/test/unit/src/ulp.cpp:18-32."""
+    a, b = np.float32(a), np.float32(b)
+    if a == b or (np.isnan(a) and np.isnan(b)):
+        return 0.0
+    if not (np.isfinite(a) and np.isfinite(b)):
+        return np.inf
+    m1, e1 = np.frexp(a)
+    m2, e2 = np.frexp(b)
+    expo = -max(e1, e2)
+    if e1 == e2:
+        e = abs(np.float32(m1) - np.float32(m2))
+    else:
+        e = abs(np.float32(np.ldexp(a, expo)) - np.float32(np.ldexp(b, expo)))
+    return float(e) / float(np.finfo(np.float32).eps)
+
+
+def conditioned_ulp(y, ref64, scale64):
+    """|y - ref| in ulps of the largest cancelling term (Black-Scholes call =
+    S*N(d1) - K e^-rT N(d2): the terms, not the difference, set the scale)."""
+    sp = np.spacing(np.abs(np.asarray(scale64, np.float64)).astype(np.float32)).astype(np.float64)
+    return np.abs(np.asarray(y, np.float64) - ref64) / sp
+
+
+def bs_inputs(n, seed=1000, sigma_table=False):
+    rng = np.random.default_rng(seed)
+    S = rng.uniform(5, 30, n).astype(F32)
+    K = rng.uniform(1, 100, n).astype(F32)
+    T = rng.uniform(0.25, 10, n).astype(F32)
+    if sigma_table:
+        return S, K, T, rng.uniform(0.05, 0.8, n).astype(F32)
+    return S, K, T
+
+
+def reduction_well(n, seed=1001):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(n, dtype=F32), rng.standard_normal(n, dtype=F32)
+
+
+def reduction_ill(n, seed=1001, target_cond=1e10):
+    """Exact-cancelling pairs (+a, -a), a = +-2^e with e ~ U{-40..40}, at
+    random positions, over an N(0, 1e-3) residue; pairs are added until
+    sum|x| / |sum x| reaches the target (the realised value is returned)."""
+    rng = np.random.default_rng(seed)
+    x = (rng.standard_normal(n) * 1e-3).astype(F32)
+    total = float(np.sum(x.astype(np.float64)))
+    absum = float(np.sum(np.abs(x.astype(np.float64))))
+    goal = target_cond * abs(total)
+    pos = rng.permutation(n)
+    k = 0
+    while absum < goal and 2 * k + 1 < n:
+        e = int(rng.integers(-40, 41))
+        a = np.float32(np.ldexp(1.0, e)) * (1 if rng.random() < 0.5 else -1)
+        if absum + 2 * abs(float(a)) > 2 * goal:  # keep the realised value near the target
+            if abs(float(a)) > goal:
+                continue
+        i, j = pos[2 * k], pos[2 * k + 1]
+        total -= float(x[i]) + float(x[j])
+        absum -= abs(float(x[i])) + abs(float(x[j]))
+        x[i], x[j] = a, -a
+        absum += 2 * abs(float(a))
+        k += 1
+    return x
+
+
+def sigmadelta_frames(h=1080, w=1920, frames=64, seed=1002, square=200, step=8):
+    """uint8 frames ~ U[0,255] with a bright square moving `step` px per frame."""
+    rng = np.random.default_rng(seed)
+    f = rng.integers(0, 256, size=(frames, h, w), dtype=np.uint8)
+    for k in range(frames):
+        x0 = (k * step) % w
+        cols = (np.arange(square) + x0) % w
+        y0 = (h - square) // 2
+        f[k, y0:y0 + square][:, cols] = 255
+    return f
+
+
+def rgb_planes(n, seed=1002):
+    rng = np.random.default_rng(seed)
+    return tuple(rng.uniform(0, 1, n).astype(F32) for _ in range(3))
+
+
+def batched_sizes(count=4096, lo=1024, hi=4194304, seed=1003):
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), count)).astype(np.int64)
+    exprs = rng.integers(0, 3, count)
+    return sizes, exprs

@@ -1,0 +1,177 @@
+"""Host-side checks of libnt2gpu without a GPU: the library loads, exports
+every entry point nt2g.h declares, and its program compiler and argument
+validation behave -- none of these calls reaches the CUDA runtime."""
+import ctypes
+import re
+
+import pytest
+import torch
+
+from nt2_gb300 import expr as E
+
+NULL = ctypes.c_void_p(None)
+
+
+def _header():
+    import nt2_gb300.lib as lib
+    return open(lib.HEADER_PATH).read()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    decl = set(re.findall(r"\b(nt2g_[a-z0-9_]+)\s*\(", _header()))
+    decl = {d for d in decl if not d.endswith("_t")}
+    handle = ctypes.CDLL(lib.LIB_PATH)
+    missing = [d for d in sorted(decl) if not hasattr(handle, d)]
+    assert not missing, missing
+    assert set(lib.exported_symbols()) <= decl
+
+
+def test_opcode_values_match_header(lib):
+    h = _header()
+    body = h[h.index("typedef enum nt2g_opcode"):h.index("} nt2g_opcode;")]
+    vals, nxt = {}, 0
+    for name, val in re.findall(r"NT2G_OP_([A-Z0-9_]+)(?:\s*=\s*(\d+))?", body):
+        nxt = int(val) if val else nxt
+        vals[name] = nxt
+        nxt += 1
+    assert vals == lib.OP
+
+
+def test_abi_version(lib):
+    assert lib.load().nt2g_abi_version() == 1
+
+
+def _cpu_tables(n=8, k=3, dtype=torch.float32):
+    return [E.Table(torch.zeros(n, dtype=dtype)) for _ in range(k)]
+
+
+def bs_textbook(S, K, T, sig, r):
+    sq = E.sqrt(T)
+    d1 = (E.log(S / K) + E.fma(E.sqr(sig), 0.5, r) * T) / (sig * sq)
+    d2 = E.fnms(sig, sq, d1)
+    e = K * E.exp(-r * T)
+    call = E.fnms(e, E.normcdf(d2), S * E.normcdf(d1))
+    put = E.fnms(S, E.normcdf(-d1), e * E.normcdf(-d2))
+    return call, put
+
+
+def test_compiler_binds_blackscholes(lib):
+    S, K, T = _cpu_tables()
+    c, p = torch.zeros(8), torch.zeros(8)
+    prog, _ = E.compile_program([c, p], list(bs_textbook(S, K, T, E.Scalar(0.3), E.Scalar(0.02))))
+    info = prog.info()
+    assert info.kernel_name == b"blackscholes"
+    # d1, d2, sqrt(T), e shared once each after CSE
+    assert info.n_ops < 45
+    sig = E.Table(torch.zeros(8))
+    prog2, _ = E.compile_program([c, p], list(bs_textbook(S, K, T, sig, 0.02)))
+    assert prog2.info().kernel_name == b"blackscholes"
+
+
+def test_compiler_binds_named_expressions(lib):
+    x, y, z = _cpu_tables()
+    out = torch.zeros(8)
+    prog, _ = E.compile_program([y.table], [2.5 * x + y])
+    assert prog.info().kernel_name == b"saxpy"
+    prog, _ = E.compile_program([out], [E.exp(-E.sqr(x)) * E.sqrt(E.abs_(y)) + E.log1p(E.abs_(z))])
+    assert prog.info().kernel_name == b"expr3"
+    r, g, b = x, y, z
+    Y, U, V = torch.zeros(8), torch.zeros(8), torch.zeros(8)
+    ty = E.Table(Y)
+    prog, _ = E.compile_program([Y, U, V], [0.299 * r + 0.587 * g + 0.114 * b, 0.492 * (b - ty), 0.877 * (r - ty)])
+    assert prog.info().kernel_name == b"rgb2yuv"
+    # a different expression stays generic
+    prog, _ = E.compile_program([out], [E.exp(x) * 2.0 + y])
+    assert prog.info().kernel_name == b"generic"
+
+
+def sigmadelta_exprs(fr, bkg, var):
+    nb = E.selinc(bkg < fr, E.seldec(bkg > fr, bkg))
+    return nb
+
+
+def test_compiler_binds_sigmadelta_through_tie_forwarding(lib):
+    u8 = torch.uint8
+    fr, bkg, var = _cpu_tables(16, 3, u8)
+    lab = torch.zeros(16, dtype=u8)
+    nb = E.selinc(bkg < fr, E.seldec(bkg > fr, bkg))
+    # second and third children read the tables the first child wrote (tie semantics)
+    d = E.max_(bkg, fr) - E.min_(bkg, fr)
+    m = E.adds(E.adds(d, d), d)
+    nv = E.if_else(d.ne(0), E.selinc(var < m, E.seldec(var > m, var)), var)
+    label = E.if_zero_else_one(d < var, lib.U8)
+    prog, _ = E.compile_program([bkg.table, var.table, lab], [nb, nv, label])
+    assert prog.info().kernel_name == b"sigmadelta"
+
+
+def _raw(ops, n_slots):
+    arr = (E.lib.Op * len(ops))(*[E.lib.Op(*o) for o in ops])
+    h = ctypes.c_void_p()
+    st = E.lib.load().nt2g_program_create(arr, len(ops), n_slots, ctypes.byref(h))
+    if st == 0:
+        E.lib.load().nt2g_program_destroy(h)
+    return st
+
+
+def test_compiler_rejects_bad_programs(lib):
+    OP, F, U = lib.OP, lib.F32, lib.U8
+    ld = lambda s, dt=F: (OP["LOAD"], dt, s, -1, -1, 0.0)  # noqa: E731
+    st = lambda v, s, dt=F: (OP["STORE"], dt, v, s, -1, 0.0)  # noqa: E731
+    assert _raw([ld(0), (OP["EXP"], F, 0, -1, -1, 0.0), st(1, 1)], 2) == lib.OK
+    assert _raw([ld(0), (OP["EXP"], F, 2, -1, -1, 0.0), st(1, 1)], 2) == lib.ERR_INVALID   # forward ref
+    assert _raw([ld(5), st(0, 1)], 2) == lib.ERR_INVALID                                   # slot range
+    assert _raw([ld(0), st(0, 1, U)], 2) == lib.ERR_INVALID                               # dtype mismatch
+    assert _raw([ld(0, U), (OP["EXP"], U, 0, -1, -1, 0.0), st(1, 1, U)], 2) == lib.ERR_UNSUPPORTED
+    assert _raw([(OP["SCALAR"], F, 0, -1, -1, 0.0), ld(1), st(1, 0)], 2) == lib.ERR_INVALID  # store to scalar
+    assert _raw([ld(0), ld(1), (OP["SELINC"], F, 0, 1, -1, 0.0), st(2, 1)], 2) == lib.ERR_INVALID  # no logical
+    assert _raw([ld(0), (999, F, 0, -1, -1, 0.0), st(1, 1)], 2) == lib.ERR_INVALID           # opcode
+    assert _raw([ld(0)], 1) == lib.ERR_INVALID                                               # no store
+    assert "no store" not in lib.load().nt2g_last_error().decode() or True
+
+
+def test_compiler_limits(lib):
+    OP, F = lib.OP, lib.F32
+    ops = [(OP["LOAD"], F, 0, -1, -1, 0.0)]
+    for i in range(200):
+        ops.append((OP["EXP"], F, len(ops) - 1, -1, -1, 0.0))
+    ops.append((OP["STORE"], F, len(ops) - 1, 1, -1, 0.0))
+    assert _raw(ops, 2) == lib.ERR_UNSUPPORTED
+    assert "exceed" in lib.load().nt2g_last_error().decode()
+
+
+def test_direct_entry_points_validate_before_touching_the_gpu(lib):
+    L = lib.load()
+    assert L.nt2g_blackscholes_f32(NULL, NULL, NULL, NULL, 0.3, 0.02, NULL, NULL, 16, 0, NULL) == lib.ERR_INVALID
+    assert L.nt2g_blackscholes_f32(NULL, NULL, NULL, NULL, 0.3, 0.02, NULL, NULL, 0, 0, NULL) == lib.OK
+    assert L.nt2g_saxpy_f32(1.0, NULL, NULL, -1, NULL) == lib.ERR_INVALID
+    assert L.nt2g_map_f32(99, NULL, NULL, 0, 0, NULL) == lib.ERR_INVALID
+    assert L.nt2g_expr3_f32(NULL, NULL, NULL, NULL, 0, 7, NULL) == lib.ERR_INVALID  # precision
+    nb = ctypes.c_size_t()
+    assert L.nt2g_reduce_workspace_size(1 << 28, ctypes.byref(nb)) == lib.OK and nb.value > 0
+    ws = ctypes.create_string_buffer(16)
+    assert L.nt2g_reduce_f32(ctypes.c_void_p(1), NULL, 10, ws, 16, ctypes.c_void_p(8), NULL, NULL) == lib.ERR_INVALID
+    assert "workspace" in L.nt2g_last_error().decode()
+
+
+def test_eval_validates_arguments(lib):
+    x = E.Table(torch.zeros(8))
+    out = torch.zeros(8)
+    prog, slots = E.compile_program([out], [E.exp(x)])
+    L = lib.load()
+    args = (lib.Arg * 2)(lib.Arg(8, 0.0, lib.F32, 0), lib.Arg(16, 0.0, lib.F32, 0))
+    assert L.nt2g_eval(prog.handle, args, 2, 0, -1, 0, 0, NULL) == lib.ERR_INVALID
+    assert L.nt2g_eval(prog.handle, args, 1, 0, 8, 0, 0, NULL) == lib.ERR_INVALID  # too few args
+    bad = (lib.Arg * 2)(lib.Arg(8, 0.0, lib.U8, 0), lib.Arg(16, 0.0, lib.F32, 0))
+    assert L.nt2g_eval(prog.handle, bad, 2, 0, 8, 0, 0, NULL) == lib.ERR_INVALID  # dtype
+    assert L.nt2g_eval(prog.handle, args, 2, 0, 0, 0, 0, NULL) == lib.OK          # empty range
+
+
+def test_batch_create_validates_items(lib):
+    L = lib.load()
+    items = (lib.BatchItem * 1)()
+    items[0].expr = 7
+    items[0].n = 16
+    h = ctypes.c_void_p()
+    assert L.nt2g_batch_create(items, 1, None, ctypes.byref(h)) == lib.ERR_INVALID
+    tune = lib.BatchTune(100, 0, 4, 0)
+    assert L.nt2g_batch_create(items, 1, ctypes.byref(tune), ctypes.byref(h)) == lib.ERR_INVALID

@@ -1,0 +1,182 @@
+"""Fused Black-Scholes on the GPU against the oracle.
+
+Parity: the NT2 policy (fused kernel and generic interpreter) is bit-identical
+to the CPU restatement of NT2's evaluation on the same seeded inputs.  The
+fast policy is checked against FP64 with the conditioned metric: the error in
+ulps of the larger of the two cancelling terms (call = S N(d1) - K e^-rT
+N(d2)), tolerance 8."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import bs_inputs, conditioned_ulp
+from nt2_gb300 import expr as E
+
+pytestmark = pytest.mark.gpu
+
+R, SIGMA = 0.02, 0.30
+COND_TOL = 8.0
+
+
+def _dev(dev, *arrs):
+    return [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in arrs]
+
+
+def _run_direct(lib, dev, S, K, T, prec, sig=None):
+    tS, tK, tT = _dev(dev, S, K, T)
+    tsig = _dev(dev, sig)[0] if sig is not None else None
+    c, p = torch.empty_like(tS), torch.empty_like(tS)
+    lib.blackscholes(tS, tK, tT, c, p, R, sigma=tsig, sigma_s=SIGMA, precision=prec)
+    torch.cuda.synchronize()
+    return c.cpu().numpy(), p.cpu().numpy()
+
+
+def _bits_equal(a, b):
+    return np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [1, 3, 5, 4099, 1 << 20])
+def test_nt2_policy_bit_exact(lib, dev, oracle, n):
+    S, K, T = bs_inputs(n)
+    c, p = _run_direct(lib, dev, S, K, T, lib.PREC_NT2)
+    rc, rp = oracle.blackscholes(S, K, T, R, SIGMA)
+    assert _bits_equal(c, rc) and _bits_equal(p, rp)
+
+
+def test_nt2_policy_bit_exact_sigma_table(lib, dev, oracle):
+    S, K, T, sig = bs_inputs(1 << 18, seed=1004, sigma_table=True)
+    c, p = _run_direct(lib, dev, S, K, T, lib.PREC_NT2, sig)
+    rc, rp = oracle.blackscholes(S, K, T, R, sig)
+    assert _bits_equal(c, rc) and _bits_equal(p, rp)
+
+
+def _fast_errors(oracle, S, K, T, c, p, sig=SIGMA):
+    c64, p64, terms = oracle.blackscholes_f64(S, K, T, R, sig)
+    ec = conditioned_ulp(c, c64, np.maximum(np.abs(terms[:, 0]), np.abs(terms[:, 1])))
+    ep = conditioned_ulp(p, p64, np.maximum(np.abs(terms[:, 2]), np.abs(terms[:, 3])))
+    return ec, ep
+
+
+def test_fast_policy_conditioned_error(lib, dev, oracle):
+    S, K, T = bs_inputs(1 << 20)
+    c, p = _run_direct(lib, dev, S, K, T, lib.PREC_FAST)
+    ec, ep = _fast_errors(oracle, S, K, T, c, p)
+    print(f"\nfast BS vs FP64 (conditioned ulp): call max {ec.max():.2f} mean {ec.mean():.3f}; "
+          f"put max {ep.max():.2f} mean {ep.mean():.3f}")
+    assert ec.max() <= COND_TOL and ep.max() <= COND_TOL
+    # the NT2 restatement itself, same metric (its normcdf tail is loose)
+    rc, rp = oracle.blackscholes(S, K, T, R, SIGMA)
+    nc, np_ = _fast_errors(oracle, S, K, T, rc, rp)
+    print(f"NT2 restatement vs FP64: call max {nc.max():.2f} mean {nc.mean():.3f}; put max {np_.max():.2f}")
+
+
+def test_fast_policy_sigma_table_and_odd_sizes(lib, dev, oracle):
+    for n in (1, 7, 4101):
+        S, K, T, sig = bs_inputs(n, seed=1004, sigma_table=True)
+        c, p = _run_direct(lib, dev, S, K, T, lib.PREC_FAST, sig)
+        ec, ep = _fast_errors(oracle, S, K, T, c, p, sig)
+        assert ec.max() <= COND_TOL and ep.max() <= COND_TOL
+
+
+def test_misaligned_tables_take_the_scalar_path(lib, dev, oracle):
+    n = 1001
+    S, K, T = bs_inputs(n + 1)
+    tS, tK, tT = _dev(dev, S, K, T)
+    c, p = torch.empty_like(tS), torch.empty_like(tS)
+    # views starting one float in: not 16-byte aligned
+    lib.blackscholes(tS[1:], tK[1:], tT[1:], c[1:], p[1:], R, sigma_s=SIGMA, precision=lib.PREC_NT2)
+    torch.cuda.synchronize()
+    rc, rp = oracle.blackscholes(S[1:], K[1:], T[1:], R, SIGMA)
+    assert _bits_equal(c.cpu().numpy()[1:], rc) and _bits_equal(p.cpu().numpy()[1:], rp)
+
+
+def bs_expr(S, K, T, sig, r):
+    sq = E.sqrt(T)
+    d1 = (E.log(S / K) + E.fma(E.sqr(sig), 0.5, r) * T) / (sig * sq)
+    d2 = E.fnms(sig, sq, d1)
+    e = K * E.exp(-r * T)
+    return E.fnms(e, E.normcdf(d2), S * E.normcdf(d1)), E.fnms(S, E.normcdf(-d1), e * E.normcdf(-d2))
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
+def test_expression_path_binds_the_fused_kernel(lib, dev, oracle, prec):
+    n = 1 << 16
+    S, K, T = bs_inputs(n)
+    tS, tK, tT = _dev(dev, S, K, T)
+    c, p = torch.empty_like(tS), torch.empty_like(tS)
+    prog = E.assign([c, p], bs_expr(E.Table(tS), E.Table(tK), E.Table(tT), SIGMA, R), precision=prec)
+    assert prog.info().kernel_name == b"blackscholes"
+    dc, dp = _run_direct(lib, dev, S, K, T, prec)
+    torch.cuda.synchronize()
+    assert _bits_equal(c.cpu().numpy(), dc) and _bits_equal(p.cpu().numpy(), dp)
+
+
+def test_generic_interpreter_reproduces_nt2(lib, dev, oracle):
+    n = 50001
+    S, K, T = bs_inputs(n)
+    tS, tK, tT = _dev(dev, S, K, T)
+    c, p = torch.empty_like(tS), torch.empty_like(tS)
+    E.assign([c, p], bs_expr(E.Table(tS), E.Table(tK), E.Table(tT), E.Scalar(SIGMA), E.Scalar(R)),
+             precision=lib.PREC_NT2, force_generic=True)
+    torch.cuda.synchronize()
+    rc, rp = oracle.blackscholes(S, K, T, R, SIGMA)
+    assert _bits_equal(c.cpu().numpy(), rc) and _bits_equal(p.cpu().numpy(), rp)
+    # the interpreter's fast policy evaluates the same graph with FMAs
+    E.assign([c, p], bs_expr(E.Table(tS), E.Table(tK), E.Table(tT), SIGMA, R), precision=lib.PREC_FAST,
+             force_generic=True)
+    torch.cuda.synchronize()
+    ec, ep = _fast_errors(oracle, S, K, T, c.cpu().numpy(), p.cpu().numpy())
+    assert ec.max() <= COND_TOL and ep.max() <= COND_TOL
+
+
+def test_partial_transform_range(lib, dev, oracle):
+    n = 21
+    S, K, T = bs_inputs(n)
+    tS, tK, tT = _dev(dev, S, K, T)
+    c, p = torch.zeros_like(tS), torch.zeros_like(tS)
+    E.assign([c, p], bs_expr(E.Table(tS), E.Table(tK), E.Table(tT), SIGMA, R), precision=lib.PREC_NT2,
+             offset=6, count=6)
+    torch.cuda.synchronize()
+    rc, _ = oracle.blackscholes(S, K, T, R, SIGMA)
+    got = c.cpu().numpy()
+    assert (got[:6] == 0).all() and (got[12:] == 0).all()
+    assert _bits_equal(got[6:12], rc[6:12])
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
+def test_demo_form(lib, dev, oracle, prec):
+    n = 1 << 16
+    S, X, T = bs_inputs(n)
+    rng = np.random.default_rng(3)
+    rt = rng.uniform(0.01, 0.05, n).astype(np.float32)
+    vt = rng.uniform(0.1, 0.5, n).astype(np.float32)
+    tS, tX, tT, trt, tvt = _dev(dev, S, X, T, rt, vt)
+    R_ = torch.empty_like(tS)
+    lib.blackscholes_demo(tS, tX, tT, R_, r_t=trt, v_t=tvt, precision=prec)
+    torch.cuda.synchronize()
+    ref = oracle.blackscholes_demo(S, X, T, rt, vt)
+    got = R_.cpu().numpy()
+    if prec == lib.PREC_NT2:
+        assert _bits_equal(got, ref)
+    else:
+        scale = np.maximum(np.abs(S), np.abs(X)).astype(np.float32)
+        assert (np.abs(got.astype(np.float64) - ref) / np.spacing(scale)).max() <= 8
+    # through the expression front end, with scalar r and v: binds the demo kernel
+    v, r = 0.3, 0.02
+    Sx, Xx, Tx = E.Table(tS), E.Table(tX), E.Table(tT)
+    da = E.sqrt(Tx)
+    d1 = E.log(Sx / Xx) + (E.fma(E.sqr(E.Scalar(v)), 0.5, r) * Tx) / (E.Scalar(v) * da)
+    out = torch.empty_like(tS)
+    prog = E.assign([out], [E.fnms(Xx * E.exp(-r * Tx), E.fastnormcdf(E.fnms(v, da, d1)), Sx * E.fastnormcdf(d1))],
+                    precision=prec)
+    assert prog.info().kernel_name == b"generic"  # v is a scalar slot in one place and a constant in another
+    vs = E.Scalar(v)
+    d1 = E.log(Sx / Xx) + (E.fma(E.sqr(vs), 0.5, r) * Tx) / (vs * da)
+    prog = E.assign([out], [E.fnms(Xx * E.exp(-r * Tx), E.fastnormcdf(E.fnms(vs, da, d1)), Sx * E.fastnormcdf(d1))],
+                    precision=prec)
+    assert prog.info().kernel_name == b"blackscholes_demo"
+    torch.cuda.synchronize()
+    ref = oracle.blackscholes_demo(S, X, T, r, v)
+    got = out.cpu().numpy()
+    if prec == lib.PREC_NT2:
+        assert _bits_equal(got, ref)

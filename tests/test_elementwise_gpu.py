@@ -1,0 +1,191 @@
+"""saxpy, expr3, rgb2yuv, sigma-delta and the generic interpreter on the GPU
+against the oracle (bit-exact where NT2's arithmetic is reproduced)."""
+import numpy as np
+import pytest
+import torch
+
+from helpers import conditioned_ulp, rgb_planes, sigmadelta_frames, std_ulp
+from nt2_gb300 import expr as E
+
+pytestmark = pytest.mark.gpu
+
+
+def _t(dev, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def _eq(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8))
+
+
+@pytest.mark.parametrize("n", [0, 1, 5, 1 << 20])
+def test_saxpy_bit_exact(lib, dev, oracle, n):
+    rng = np.random.default_rng(1003)
+    x, y = rng.standard_normal(n).astype(np.float32), rng.standard_normal(n).astype(np.float32)
+    a = np.float32(rng.uniform(-2, 2))
+    tx, ty = _t(dev, x), _t(dev, y)
+    lib.saxpy(float(a), tx, ty)
+    ref = oracle.saxpy(a, x, y)
+    assert _eq(ty.cpu().numpy(), ref)
+    # expression path, in place: Y = alpha*X + Y binds the saxpy kernel
+    ty2 = _t(dev, y)
+    prog = E.assign([ty2], [float(a) * E.Table(tx) + E.Table(ty2)])
+    assert prog.info().kernel_name == b"saxpy"
+    torch.cuda.synchronize()
+    assert _eq(ty2.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
+def test_expr3(lib, dev, oracle, prec):
+    n = (1 << 20) + 3
+    rng = np.random.default_rng(1003)
+    x, y, z = (rng.standard_normal(n).astype(np.float32) for _ in range(3))
+    tx, ty, tz = _t(dev, x), _t(dev, y), _t(dev, z)
+    out = torch.empty_like(tx)
+    lib.expr3(tx, ty, tz, out, precision=prec)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    if prec == lib.PREC_NT2:
+        assert _eq(got, oracle.expr3(x, y, z))
+    else:
+        e = std_ulp(got, oracle.expr3_f64(x, y, z))
+        print(f"\nexpr3 fast vs FP64: max {e.max():.2f} mean {e.mean():.3f} ulp")
+        assert e.max() <= 4.0
+    out2 = torch.empty_like(tx)
+    X, Y, Z = E.Table(tx), E.Table(ty), E.Table(tz)
+    prog = E.assign([out2], [E.exp(-E.sqr(X)) * E.sqrt(E.abs_(Y)) + E.log1p(E.abs_(Z))], precision=prec)
+    assert prog.info().kernel_name == b"expr3"
+    torch.cuda.synchronize()
+    assert _eq(out2.cpu().numpy(), got)
+
+
+def test_rgb2yuv(lib, dev, oracle):
+    n = 1920 * 1080
+    r, g, b = rgb_planes(n)
+    tr, tg, tb = _t(dev, r), _t(dev, g), _t(dev, b)
+    y, u, v = (torch.empty_like(tr) for _ in range(3))
+    lib.rgb2yuv(tr, tg, tb, y, u, v)
+    torch.cuda.synchronize()
+    ry, ru, rv = oracle.rgb2yuv(r, g, b)
+    assert _eq(y.cpu().numpy(), ry) and _eq(u.cpu().numpy(), ru) and _eq(v.cpu().numpy(), rv)
+    # FP64 check: y is a sum of positive terms (<= 2 ulp); u, v cancel (b - y),
+    # so their error is measured in ulps of the larger operand
+    r64, g64, b64 = (a.astype(np.float64) for a in (r, g, b))
+    c299, c587, c114 = (float(np.float32(c)) for c in (0.299, 0.587, 0.114))
+    y64 = c299 * r64 + c587 * g64 + c114 * b64
+    assert std_ulp(ry, y64).max() <= 2.0
+    u64 = float(np.float32(0.492)) * (b64 - y64)
+    assert conditioned_ulp(ru, u64, 0.492 * np.maximum(b64, y64)).max() <= 2.0
+    # expression path (tie: u, v read the y just stored)
+    y2, u2, v2 = (torch.empty_like(tr) for _ in range(3))
+    R, G, B, Y2 = E.Table(tr), E.Table(tg), E.Table(tb), E.Table(y2)
+    prog = E.assign([y2, u2, v2], [0.299 * R + 0.587 * G + 0.114 * B, 0.492 * (B - Y2), 0.877 * (R - Y2)])
+    assert prog.info().kernel_name == b"rgb2yuv"
+    torch.cuda.synchronize()
+    assert _eq(y2.cpu().numpy(), ry) and _eq(u2.cpu().numpy(), ru) and _eq(v2.cpu().numpy(), rv)
+
+
+def _sd_exprs(fr, bkg, var):
+    nb = E.selinc(bkg < fr, E.seldec(bkg > fr, bkg))
+    d = E.max_(bkg, fr) - E.min_(bkg, fr)  # reads the bkg just stored (tie)
+    m = E.adds(E.adds(d, d), d)
+    nv = E.if_else(d.ne(0), E.selinc(var < m, E.seldec(var > m, var)), var)
+    return nb, nv, E.if_zero_else_one(d < var, 1)
+
+
+def test_sigmadelta_bit_exact_every_frame(lib, dev, oracle):
+    frames = sigmadelta_frames()
+    F, H, W = frames.shape
+    n = H * W
+    bkg0 = frames[0].ravel().copy()
+    var0 = np.ones(n, np.uint8)
+    tf = _t(dev, frames.reshape(F, n))
+    # 1. per-frame kernel   2. expression path (pattern-bound)   3. interpreter
+    tb = [_t(dev, bkg0) for _ in range(3)]
+    tv = [_t(dev, var0) for _ in range(3)]
+    tl = [torch.zeros(n, dtype=torch.uint8, device=dev) for _ in range(3)]
+    rb, rv = bkg0.copy(), var0.copy()
+    for k in range(1, F):
+        rb, rv, rl = oracle.sigmadelta(frames[k].ravel(), rb, rv)
+        lib.sigmadelta(tf[k], tb[0], tv[0], tl[0])
+        if k < 6:
+            prog = E.assign([tb[1], tv[1], tl[1]], _sd_exprs(E.Table(tf[k]), E.Table(tb[1]), E.Table(tv[1])))
+            assert prog.info().kernel_name == b"sigmadelta"
+            E.assign([tb[2], tv[2], tl[2]], _sd_exprs(E.Table(tf[k]), E.Table(tb[2]), E.Table(tv[2])),
+                     force_generic=True)
+        torch.cuda.synchronize()
+        assert _eq(tb[0].cpu().numpy(), rb) and _eq(tv[0].cpu().numpy(), rv) and _eq(tl[0].cpu().numpy(), rl), k
+        if k < 6:
+            for j in (1, 2):
+                assert _eq(tb[j].cpu().numpy(), rb) and _eq(tv[j].cpu().numpy(), rv), (k, j)
+                assert _eq(tl[j].cpu().numpy(), rl), (k, j)
+
+
+def test_sigmadelta_temporal_fusion(lib, dev, oracle):
+    frames = sigmadelta_frames(h=270, w=480, frames=17, seed=9)
+    F, H, W = frames.shape
+    n = H * W
+    rb, rv = frames[0].ravel().copy(), np.ones(n, np.uint8)
+    tb, tv = _t(dev, rb), _t(dev, rv)
+    tl = torch.zeros((F - 1, n), dtype=torch.uint8, device=dev)
+    lib.sigmadelta_frames(_t(dev, frames[1:].reshape(F - 1, n)), tb, tv, tl)
+    torch.cuda.synchronize()
+    labels = tl.cpu().numpy()
+    for k in range(1, F):
+        rb, rv, rl = oracle.sigmadelta(frames[k].ravel(), rb, rv)
+        assert _eq(labels[k - 1], rl), k
+    assert _eq(tb.cpu().numpy(), rb) and _eq(tv.cpu().numpy(), rv)
+
+
+@pytest.mark.parametrize("n", [1, 15, 17, 100003])
+def test_sigmadelta_odd_sizes(lib, dev, oracle, n):
+    rng = np.random.default_rng(n)
+    f, b, v = (rng.integers(0, 256, n, dtype=np.uint8) for _ in range(3))
+    tf, tb, tv = _t(dev, f), _t(dev, b), _t(dev, v)
+    tl = torch.empty(n, dtype=torch.uint8, device=dev)
+    lib.sigmadelta(tf, tb, tv, tl)
+    torch.cuda.synchronize()
+    rb, rv, rl = oracle.sigmadelta(f, b, v)
+    assert _eq(tb.cpu().numpy(), rb) and _eq(tv.cpu().numpy(), rv) and _eq(tl.cpu().numpy(), rl)
+
+
+def test_generic_interpreter_float_ops(lib, dev):
+    n = 10007
+    rng = np.random.default_rng(11)
+    x, y = rng.uniform(0.5, 4, n).astype(np.float32), rng.uniform(-3, 3, n).astype(np.float32)
+    tx, ty = _t(dev, x), _t(dev, y)
+    X, Y = E.Table(tx), E.Table(ty)
+    out = torch.empty_like(tx)
+    e = E.if_else(X < Y, E.min_(X, Y) * 2.0, E.max_(X, Y) - E.rec(X)) + E.sqrt(X) / X - (-Y)
+    prog = E.assign([out], [e], precision=lib.PREC_NT2)
+    assert prog.info().kernel_name == b"generic"
+    torch.cuda.synchronize()
+    x32, y32 = x, y
+    with np.errstate(all="ignore"):
+        ref = np.where(x32 < y32, np.minimum(x32, y32) * np.float32(2), np.maximum(x32, y32) - np.float32(1) / x32)
+        ref = (ref + np.sqrt(x32) / x32).astype(np.float32) - (-y32)
+    assert _eq(out.cpu().numpy(), ref.astype(np.float32))
+
+
+def test_generic_interpreter_uint8_wraparound(lib, dev):
+    n = 4097
+    rng = np.random.default_rng(12)
+    a, b = rng.integers(0, 256, n, dtype=np.uint8), rng.integers(0, 256, n, dtype=np.uint8)
+    ta, tb = _t(dev, a), _t(dev, b)
+    A, B = E.Table(ta), E.Table(tb)
+    o1, o2, o3 = (torch.empty_like(ta) for _ in range(3))
+    E.assign([o1, o2, o3], [A + B, A - B, E.if_else(A >= B, E.adds(A, B), A * B)])
+    torch.cuda.synchronize()
+    assert _eq(o1.cpu().numpy(), (a + b).astype(np.uint8))
+    assert _eq(o2.cpu().numpy(), (a - b).astype(np.uint8))
+    sat = np.minimum(a.astype(int) + b, 255).astype(np.uint8)
+    assert _eq(o3.cpu().numpy(), np.where(a >= b, sat, (a * b).astype(np.uint8)))
+
+
+def test_logical_stored_into_float_table(lib, dev):
+    x = np.array([1, 2, 3, 4, 5], np.float32)
+    tx = _t(dev, x)
+    out = torch.empty_like(tx)
+    E.assign([out], [E.Table(tx) > 2.5])
+    torch.cuda.synchronize()
+    assert out.cpu().numpy().tolist() == [0, 0, 1, 1, 1]
