@@ -153,9 +153,11 @@ nt2g_status nt2g_saxpy_f32(float alpha, const float *X, float *Y, int64_t n, voi
 nt2g_status nt2g_expr3_f32(const float *x, const float *y, const float *z, float *out, int64_t n,
                            int32_t precision, void *stream);
 
-/* y/u/v planes (demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:30-32), unfused as NT2. */
+/* y/u/v planes (demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:30-32).  NT2G_PREC_NT2:
+ * NT2's unfused left-to-right evaluation (bit-identical); NT2G_PREC_FAST: y
+ * carried as a double-float so u and v keep ~1 ulp under b-y cancellation. */
 nt2g_status nt2g_rgb2yuv_f32(const float *r, const float *g, const float *b, float *y, float *u,
-                             float *v, int64_t n, void *stream);
+                             float *v, int64_t n, int32_t precision, void *stream);
 
 /* One sigma-delta step on uint8 pixels, bkg/var updated in place, label
  * written (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:38-57).  Bit-exact. */

@@ -62,7 +62,11 @@ int device_sm_count()
 // scalar role -- a constant or scalar argument holding the negated value
 // (what C++ produces for -r*T with a float r: the negation happens before
 // the expression is built).
-enum PKind { P_OP, P_TABLE, P_SCALAR, P_TABSCAL, P_CVAL, P_NEG };
+// P_FOLD matches fma(sqr(x), c, y) -- or, when x and y are scalars, the
+// float constant C++ computes for it before building the expression (NT2's
+// scalar fma/sqr run on the host: x*x, *c, +y, each rounded); the constant is
+// checked against the bound x and y once the whole match is known.
+enum PKind { P_OP, P_TABLE, P_SCALAR, P_TABSCAL, P_CVAL, P_NEG, P_FOLD };
 
 struct PNode {
     PKind kind;
@@ -92,6 +96,11 @@ struct PB {
     int tabscal(int role) { return add(PNode{P_TABSCAL, 0, NT2G_F32, {-1, -1, -1}, role, 0.f}); }
     int cval(float v, int dt = NT2G_F32) { return add(PNode{P_CVAL, 0, dt, {-1, -1, -1}, -1, v}); }
     int neg(int a) { return add(PNode{P_NEG, NT2G_OP_NEG, NT2G_F32, {a, -1, -1}, -1, 0.f}); }
+    int fold_fma_sqr(int x, float c, int y)
+    {
+        int full = op(NT2G_OP_FMA, op(NT2G_OP_SQR, x), cval(c), y);
+        return add(PNode{P_FOLD, 0, NT2G_F32, {full, x, y}, -1, c});
+    }
     void out(int node, int role) { p.outs.push_back({node, role}); }
 };
 
@@ -104,7 +113,7 @@ static std::vector<Pattern> build_patterns()
         int S = b.table(0), K = b.table(1), T = b.table(2), sig = b.tabscal(3), r = b.scalar(4);
         int sq = b.op(NT2G_OP_SQRT, T);
         int lq = b.op(NT2G_OP_LOG, b.op(NT2G_OP_DIV, S, K));
-        int a = b.op(NT2G_OP_FMA, b.op(NT2G_OP_SQR, sig), b.cval(0.5f), r);
+        int a = b.fold_fma_sqr(sig, 0.5f, r);
         int d1 = b.op(NT2G_OP_DIV, b.op(NT2G_OP_ADD, lq, b.op(NT2G_OP_MUL, a, T)), b.op(NT2G_OP_MUL, sig, sq));
         int d2 = b.op(NT2G_OP_FNMS, sig, sq, d1);
         int e = b.op(NT2G_OP_MUL, K, b.op(NT2G_OP_EXP, b.op(NT2G_OP_MUL, b.neg(r), T)));
@@ -121,7 +130,7 @@ static std::vector<Pattern> build_patterns()
         int S = b.table(0), X = b.table(1), T = b.table(2), r = b.tabscal(3), va = b.tabscal(4);
         int da = b.op(NT2G_OP_SQRT, T);
         int d1 = b.op(NT2G_OP_ADD, b.op(NT2G_OP_LOG, b.op(NT2G_OP_DIV, S, X)),
-                      b.op(NT2G_OP_DIV, b.op(NT2G_OP_MUL, b.op(NT2G_OP_FMA, b.op(NT2G_OP_SQR, va), b.cval(0.5f), r), T),
+                      b.op(NT2G_OP_DIV, b.op(NT2G_OP_MUL, b.fold_fma_sqr(va, 0.5f, r), T),
                            b.op(NT2G_OP_MUL, va, da)));
         int d2 = b.op(NT2G_OP_FNMS, va, da, d1);
         int R = b.op(NT2G_OP_FNMS, b.op(NT2G_OP_MUL, X, b.op(NT2G_OP_EXP, b.op(NT2G_OP_MUL, b.neg(r), T))),
@@ -195,6 +204,22 @@ struct DeferredConst {
     float value;
 };
 
+// A folded fma(sqr(x), c, y) constant to verify against the roles x, y.
+struct DeferredFold {
+    float value, c;
+    int x_role, y_role;
+};
+
+// NT2's scalar fma(sqr(x), c, y) in float: three separately rounded steps
+// (volatile keeps the host compiler from contracting them).
+static float nt2_fold(float x, float c, float y)
+{
+    volatile float sq = x * x;
+    volatile float m = sq * c;
+    volatile float r = m + y;
+    return r;
+}
+
 }  // namespace nt2g
 
 using namespace nt2g;
@@ -251,6 +276,7 @@ struct Matcher {
     std::vector<int> pmap;  // pattern node -> program value
     std::vector<RoleBind> roles;
     std::vector<DeferredConst> deferred;
+    std::vector<DeferredFold> folds;
 
     Matcher(const nt2g_program &p, const Pattern &q)
         : prog(p), pat(q), pmap(q.nodes.size(), -1), roles(q.n_roles) {}
@@ -298,6 +324,15 @@ struct Matcher {
                 ok = bind_role(c.role, RoleBind{3, o.a, 0.f});
             break;
         }
+        case P_FOLD: {
+            if (o.code == NT2G_OP_CONST && o.dtype == NT2G_F32) {
+                folds.push_back(DeferredFold{o.imm, n.cval, pat.nodes[n.ch[1]].role, pat.nodes[n.ch[2]].role});
+                ok = true;
+            } else {
+                ok = match(v, n.ch[0]);
+            }
+            break;
+        }
         case P_OP:
             if (o.code != n.code || o.dtype != n.dtype) break;
             ok = true;
@@ -327,6 +362,10 @@ static bool try_bind(nt2g_program &p, const Pattern &pat)
     }
     for (const RoleBind &r : m.roles)
         if (r.kind < 0) return false;
+    for (const DeferredFold &f : m.folds) {
+        const RoleBind &x = m.roles[f.x_role], &y = m.roles[f.y_role];
+        if (x.kind != 1 || y.kind != 1 || nt2_fold(x.value, f.c, y.value) != f.value) return false;
+    }
     p.kernel = pat.kernel;
     p.kernel_name = pat.name;
     p.roles = m.roles;
@@ -636,7 +675,7 @@ extern "C" nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, in
                                   precision, st);
         case kSaxpy: return launch_saxpy(V(0), T(1), T(2), T(3), count, st);
         case kExpr3: return launch_expr3(T(0), T(1), T(2), T(3), count, precision, st);
-        case kRgb2Yuv: return launch_rgb2yuv(T(0), T(1), T(2), T(3), T(4), T(5), count, st);
+        case kRgb2Yuv: return launch_rgb2yuv(T(0), T(1), T(2), T(3), T(4), T(5), count, precision, st);
         case kSigmaDelta: {
             // the fused kernel updates bkg/var in place: it needs the output
             // roles to be the same tables as the inputs
@@ -697,10 +736,10 @@ extern "C" nt2g_status nt2g_expr3_f32(const float *x, const float *y, const floa
 }
 
 extern "C" nt2g_status nt2g_rgb2yuv_f32(const float *r, const float *g, const float *b, float *y, float *u, float *v,
-                                        int64_t n, void *stream)
+                                        int64_t n, int32_t precision, void *stream)
 {
-    NT2G_REQ_N(); NT2G_REQ(r); NT2G_REQ(g); NT2G_REQ(b); NT2G_REQ(y); NT2G_REQ(u); NT2G_REQ(v);
-    return launch_rgb2yuv(r, g, b, y, u, v, n, (cudaStream_t)stream);
+    NT2G_REQ_N(); NT2G_REQ(r); NT2G_REQ(g); NT2G_REQ(b); NT2G_REQ(y); NT2G_REQ(u); NT2G_REQ(v); NT2G_REQ_PREC();
+    return launch_rgb2yuv(r, g, b, y, u, v, n, precision, (cudaStream_t)stream);
 }
 
 extern "C" nt2g_status nt2g_sigmadelta_u8(const uint8_t *frame, uint8_t *bkg, uint8_t *var, uint8_t *label, int64_t n,

@@ -97,6 +97,7 @@ nt2g_status launch_expr3(const float *x, const float *y, const float *z, float *
 }
 
 // ---------------------------------------------------------------- rgb2yuv --
+template <class P>
 __global__ void __launch_bounds__(kThreads) k_rgb2yuv(const float *__restrict__ r, const float *__restrict__ g,
                                                       const float *__restrict__ b, float *__restrict__ y,
                                                       float *__restrict__ u, float *__restrict__ v, int64_t n,
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(kThreads) k_rgb2yuv(const float *__restrict__ 
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 float yy, uu, vv;
-                yuv_px(get(R, j), get(G, j), get(B, j), yy, uu, vv);
+                yuv_px<P>(get(R, j), get(G, j), get(B, j), yy, uu, vv);
                 set(Y, j, yy); set(U, j, uu); set(V, j, vv);
             }
             st_stream((float4 *)y + i, Y);
@@ -122,15 +123,18 @@ __global__ void __launch_bounds__(kThreads) k_rgb2yuv(const float *__restrict__ 
         }
         done = nv << 2;
     }
-    for (int64_t i = done + tid; i < n; i += stride) yuv_px(r[i], g[i], b[i], y[i], u[i], v[i]);
+    for (int64_t i = done + tid; i < n; i += stride) yuv_px<P>(r[i], g[i], b[i], y[i], u[i], v[i]);
 }
 
 nt2g_status launch_rgb2yuv(const float *r, const float *g, const float *b, float *y, float *u, float *v,
-                           int64_t n, cudaStream_t st)
+                           int64_t n, int precision, cudaStream_t st)
 {
     if (n == 0) return NT2G_OK;
     int vec = aligned16(r) && aligned16(g) && aligned16(b) && aligned16(y) && aligned16(u) && aligned16(v);
-    k_rgb2yuv<<<grid_for(k_rgb2yuv, (n + 3) / 4), kThreads, 0, st>>>(r, g, b, y, u, v, n, vec);
+    if (precision == NT2G_PREC_NT2)
+        k_rgb2yuv<Nt2><<<grid_for(k_rgb2yuv<Nt2>, (n + 3) / 4), kThreads, 0, st>>>(r, g, b, y, u, v, n, vec);
+    else
+        k_rgb2yuv<Fast><<<grid_for(k_rgb2yuv<Fast>, (n + 3) / 4), kThreads, 0, st>>>(r, g, b, y, u, v, n, vec);
     NT2G_LAUNCH_CHECK("rgb2yuv launch");
     return NT2G_OK;
 }

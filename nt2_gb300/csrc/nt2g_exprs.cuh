@@ -59,18 +59,45 @@ __device__ __forceinline__ float bs_demo_option(float S, float X, float T, float
 template <class P>
 __device__ __forceinline__ float expr3_elem(float x, float y, float z)
 {
-    return P::add(P::mul(exp<P>(-P::mul(x, x)), P::sqrt(fabsf(y))), log1p<P>(fabsf(z)));
+    return P::add(P::mul(exp_neg_sqr<P>(x), P::sqrt(fabsf(y))), log1p<P>(fabsf(z)));
 }
 
 // Y = alpha*X + Y, two roundings as NT2 (demo/saxpy/nt2/saxpy_nt2.cpp:41)
 __device__ __forceinline__ float saxpy_elem(float a, float x, float y) { return __fadd_rn(__fmul_rn(a, x), y); }
 
-// rgb2yuv (demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:30-32), left to right, unfused
+// rgb2yuv (demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:30-32).
+// Nt2: left to right, unfused, u and v from the rounded y (NT2's result,
+// whose b - y / r - y cancellation amplifies y's rounding).
+// Fast: y = 0.299r + 0.587g + 0.114b held exactly enough as yh + yl (each
+// product split exactly by FMA, the sum by TwoSum), so u = 0.492((b-yh)-yl)
+// and v = 0.877((r-yh)-yl) are within about one ulp of their own value even
+// when b or r nearly equals y; memory-bound, so the extra flops are free.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+template <class P>
 __device__ __forceinline__ void yuv_px(float r, float g, float b, float &y, float &u, float &v)
 {
-    y = __fadd_rn(__fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g)), __fmul_rn(0.114f, b));
-    u = __fmul_rn(0.492f, __fsub_rn(b, y));
-    v = __fmul_rn(0.877f, __fsub_rn(r, y));
+    if (P::exact) {
+        y = __fadd_rn(__fadd_rn(__fmul_rn(0.299f, r), __fmul_rn(0.587f, g)), __fmul_rn(0.114f, b));
+        u = __fmul_rn(0.492f, __fsub_rn(b, y));
+        v = __fmul_rn(0.877f, __fsub_rn(r, y));
+        return;
+    }
+    float p1 = __fmul_rn(0.299f, r), e1 = __fmaf_rn(0.299f, r, -p1);
+    float p2 = __fmul_rn(0.587f, g), e2 = __fmaf_rn(0.587f, g, -p2);
+    float p3 = __fmul_rn(0.114f, b), e3 = __fmaf_rn(0.114f, b, -p3);
+    float s1, t1, yh, t2;
+    two_sum(p1, p2, s1, t1);
+    two_sum(s1, p3, yh, t2);
+    float yl = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), __fadd_rn(e1, e2)), e3);
+    y = __fadd_rn(yh, yl);
+    u = __fmul_rn(0.492f, __fsub_rn(__fsub_rn(b, yh), yl));
+    v = __fmul_rn(0.877f, __fsub_rn(__fsub_rn(r, yh), yl));
 }
 
 // Sigma-delta step on four uint8 pixels packed in a word

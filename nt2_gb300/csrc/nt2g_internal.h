@@ -64,7 +64,7 @@ nt2g_status launch_reduce(const float *x, const float *y, int64_t n, void *ws, d
 nt2g_status launch_expr3(const float *x, const float *y, const float *z, float *out, int64_t n, int precision,
                          cudaStream_t st);
 nt2g_status launch_rgb2yuv(const float *r, const float *g, const float *b, float *y, float *u, float *v,
-                           int64_t n, cudaStream_t st);
+                           int64_t n, int precision, cudaStream_t st);
 nt2g_status launch_sigmadelta(const uint8_t *frame, uint8_t *bkg, uint8_t *var, uint8_t *label, int64_t n,
                               cudaStream_t st);
 nt2g_status launch_sigmadelta_frames(const uint8_t *frames, uint8_t *bkg, uint8_t *var, uint8_t *labels,

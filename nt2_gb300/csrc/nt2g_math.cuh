@@ -310,17 +310,19 @@ template <bool HALF_SQ> NT2G_HD float erfc_tail_fast(float a, float *expo = null
     const float s2 = HALF_SQ ? -0.5f : -1.0f;
     float scale;
     float e = exp_fast_parts(Fast::mul(s2, hi), scale);
-    // (1 + e) * (1 + L) - 1 = e + L*(1 + e), L = s2*lo (|L| < 2^-18)
-    float L = Fast::mul(s2, lo);
-    e = Fast::add(e, Fast::fma(L, e, L));
+    // fold the square's low part L = s2*lo (|L| < 2^-18) and the reciprocal
+    // residual r into the small term: (1+e)(1+L)(1+r) - 1 = e + c + c*e,
+    // c = L + r (c*e and L*r are below 2^-40 relative)
+    float c = Fast::fma(s2, lo, r);
+    e = Fast::add(e, Fast::fma(c, e, c));
     float wr = Fast::mul(w, erfc_tail_poly(w));
-    wr = Fast::fma(wr, r, wr);
     float res = Fast::mul(Fast::fma(e, wr, wr), scale);
     // past amax the exponential leaves the normal range (its 2^k scale would
     // underflow) and the true value is subnormal; the guard also keeps inf*0
     // out of the split for a = inf.
     const float amax = HALF_SQ ? 13.2f : 9.3f;
-    if (expo) *expo = (a < amax) ? Fast::mul(Fast::add(e, 1.0f), scale) : 0.0f;
+    // exp(-s^2 a^2) alone (without the reciprocal residual) for the adjoint
+    if (expo) *expo = (a < amax) ? Fast::mul(Fast::add(Fast::sub(e, Fast::fma(r, e, r)), 1.0f), scale) : 0.0f;
     return (a < amax) ? res : 0.0f;
 }
 
@@ -396,5 +398,20 @@ template <class P> NT2G_HD float fastnormcdf(float a0)
 }
 
 template <class P> NT2G_HD float sqr(float x) { return P::mul(x, x); }
+
+// exp(-sqr(x)).  NT2: the rounded square is exponentiated (its rounding is
+// amplified by x^2).  Fast: exp(-hi) * (1 - lo) with hi + lo = x^2 exactly.
+template <class P> NT2G_HD float exp_neg_sqr(float x)
+{
+    if (P::exact) return exp<P>(-P::mul(x, x));
+    float hi = Fast::mul(x, x);
+    float lo = Fast::fma(x, x, -hi);
+    float scale;
+    float s = exp_fast_parts(-hi, scale);
+    s = Fast::add(s, Fast::fma(-lo, s, -lo));  // (1+s)(1-lo) - 1
+    float r = Fast::mul(Fast::add(s, 1.0f), scale);
+    r = (-hi <= bits_f(NT2G_MINLOG)) ? 0.0f : r;
+    return is_nan(x) ? x : r;
+}
 
 }  // namespace nt2g

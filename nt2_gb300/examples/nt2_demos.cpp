@@ -1,0 +1,222 @@
+// nt2_demos.cpp -- NT2's hot-path demos written against nt2/table.hpp and run
+// by libnt2gpu.  The expressions are spelled as in NT2's demo sources:
+//   demo/blackscholes/nt2/blackandscholes_nt2.cpp:55-59   (bs_demo)
+//   demo/sdot/nt2/sdot_nt2.cpp:37                         (sdot)
+//   demo/saxpy/nt2/saxpy_nt2.cpp:41                       (saxpy)
+//   demo/rgb2yuv/nt2/rgb2yuv_nt2.cpp:30-32                (rgb2yuv, as one tie)
+//   demo/sigmadelta/nt2/sigmadelta_nt2.cpp:38-57          (sigmadelta, as one tie)
+// plus the textbook call+put of the fused Black-Scholes workload (bs).
+//
+// usage: nt2_demos lower
+//        nt2_demos bs|bs_host|bs_demo|saxpy|rgb2yuv DIR N
+//        nt2_demos sdot DIR N
+//        nt2_demos sigmadelta DIR PIXELS FRAMES
+// Inputs and outputs are raw little-endian arrays DIR/<name>.bin.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "nt2/table.hpp"
+
+using dtable = nt2::table<float, nt2::device_>;
+using htable = nt2::table<float>;
+using u8table = nt2::table<std::uint8_t, nt2::device_>;
+
+template <class T> static std::vector<T> read_bin(const std::string &path, std::size_t n)
+{
+    std::vector<T> v(n);
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f || std::fread(v.data(), sizeof(T), n, f) != n) {
+        std::fprintf(stderr, "cannot read %s\n", path.c_str());
+        std::exit(2);
+    }
+    std::fclose(f);
+    return v;
+}
+
+template <class T> static void write_bin(const std::string &path, const std::vector<T> &v)
+{
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f || std::fwrite(v.data(), sizeof(T), v.size(), f) != v.size()) {
+        std::fprintf(stderr, "cannot write %s\n", path.c_str());
+        std::exit(2);
+    }
+    std::fclose(f);
+}
+
+template <class Tab> static Tab load(const std::string &path, std::size_t n)
+{
+    using T = typename Tab::value_type;
+    nt2::table<T> h(nt2::of_size(n));
+    auto v = read_bin<T>(path, n);
+    std::memcpy(h.data(), v.data(), n * sizeof(T));
+    Tab t;
+    t = h;
+    return t;
+}
+
+template <class Tab> static void save(const std::string &path, const Tab &t)
+{
+    using T = typename Tab::value_type;
+    nt2::table<T> h;
+    h = t;
+    write_bin(path, std::vector<T>(h.data(), h.data() + h.numel()));
+}
+
+// textbook call + put as one fused assignment
+template <class Tab> static void blackscholes(Tab &C, Tab &P, const Tab &S, const Tab &K, const Tab &T, float r,
+                                              float sigma)
+{
+    auto sq = nt2::sqrt(T);
+    auto d1 = (nt2::log(S / K) + nt2::fma(nt2::sqr(sigma), 0.5f, r) * T) / (sigma * sq);
+    auto d2 = nt2::fnms(sigma, sq, d1);
+    auto e = K * nt2::exp(-r * T);
+    nt2::tie(C, P) = nt2::tie(nt2::fnms(e, nt2::normcdf(d2), S * nt2::normcdf(d1)),
+                              nt2::fnms(S, nt2::normcdf(-d1), e * nt2::normcdf(-d2)));
+}
+
+static int lower_only()
+{
+    const std::size_t n = 64;
+    htable S(nt2::of_size(n)), K(nt2::of_size(n)), T(nt2::of_size(n)), C(nt2::of_size(n)), P(nt2::of_size(n));
+    {
+        const float r = 0.02f, sigma = 0.30f;
+        auto sq = nt2::sqrt(T);
+        auto d1 = (nt2::log(S / K) + nt2::fma(nt2::sqr(sigma), 0.5f, r) * T) / (sigma * sq);
+        auto d2 = nt2::fnms(sigma, sq, d1);
+        auto e = K * nt2::exp(-r * T);
+        std::printf("bs %s\n", nt2::tie(C, P).explain(nt2::tie(nt2::fnms(e, nt2::normcdf(d2), S * nt2::normcdf(d1)),
+                                                           nt2::fnms(S, nt2::normcdf(-d1), e * nt2::normcdf(-d2))))
+                                   .c_str());
+    }
+    {
+        htable Sa(nt2::of_size(n)), Xa(nt2::of_size(n)), Ta(nt2::of_size(n)), ra(nt2::of_size(n)),
+            va(nt2::of_size(n)), R(nt2::of_size(n));
+        auto da = nt2::sqrt(Ta);
+        auto d1 = nt2::log(Sa / Xa) + (nt2::fma(nt2::sqr(va), 0.5f, ra) * Ta) / (va * da);
+        auto d2 = nt2::fnms(va, da, d1);
+        std::printf("bs_demo %s\n",
+                    nt2::tie(R).explain(nt2::tie(nt2::fnms(Xa * nt2::exp(-ra * Ta), nt2::fastnormcdf(d2),
+                                                           Sa * nt2::fastnormcdf(d1))))
+                        .c_str());
+    }
+    {
+        htable X(nt2::of_size(n)), Y(nt2::of_size(n));
+        std::printf("saxpy %s\n", nt2::tie(Y).explain(nt2::tie(2.5f * X + Y)).c_str());
+    }
+    {
+        htable r(nt2::of_size(n)), g(nt2::of_size(n)), b(nt2::of_size(n)), y(nt2::of_size(n)), u(nt2::of_size(n)),
+            v(nt2::of_size(n));
+        std::printf("rgb2yuv %s\n", nt2::tie(y, u, v)
+                                        .explain(nt2::tie(0.299f * r + 0.587f * g + 0.114f * b, 0.492f * (b - y),
+                                                          0.877f * (r - y)))
+                                        .c_str());
+    }
+    {
+        nt2::table<std::uint8_t> fr(nt2::of_size(n)), bkg(nt2::of_size(n)), var(nt2::of_size(n)),
+            out(nt2::of_size(n));
+        auto diff = nt2::max(bkg, fr) - nt2::min(bkg, fr);
+        auto mul = nt2::adds(nt2::adds(diff, diff), diff);
+        std::printf("sigmadelta %s\n",
+                    nt2::tie(bkg, var, out)
+                        .explain(nt2::tie(nt2::selinc(bkg < fr, nt2::seldec(bkg > fr, bkg)),
+                                          nt2::if_else(diff != std::uint8_t(0),
+                                                       nt2::selinc(var < mul, nt2::seldec(var > mul, var)), var),
+                                          nt2::if_zero_else_one(diff < var)))
+                        .c_str());
+    }
+    return 0;
+}
+
+int main(int argc, char **argv)
+{
+    if (argc < 2) {
+        std::fprintf(stderr, "usage: %s lower | bs|bs_host|bs_demo|saxpy|rgb2yuv|sdot DIR N | sigmadelta DIR PIXELS FRAMES\n",
+                     argv[0]);
+        return 2;
+    }
+    const std::string mode = argv[1];
+    if (mode == "lower") return lower_only();
+    if (argc < 4) return 2;
+    const std::string dir = std::string(argv[2]) + "/";
+    const std::size_t n = std::strtoull(argv[3], nullptr, 10);
+    if (const char *p = std::getenv("NT2G_PRECISION")) nt2::options().precision = std::atoi(p);
+    try {
+        if (mode == "bs") {
+            auto S = load<dtable>(dir + "S.bin", n), K = load<dtable>(dir + "K.bin", n), T = load<dtable>(dir + "T.bin", n);
+            dtable C(nt2::of_size(n)), P(nt2::of_size(n));
+            blackscholes(C, P, S, K, T, 0.02f, 0.30f);
+            save(dir + "call.bin", C);
+            save(dir + "put.bin", P);
+        } else if (mode == "bs_host") {  // host tables: staged to the device and back
+            auto S = load<htable>(dir + "S.bin", n), K = load<htable>(dir + "K.bin", n), T = load<htable>(dir + "T.bin", n);
+            htable C(nt2::of_size(n)), P(nt2::of_size(n));
+            blackscholes(C, P, S, K, T, 0.02f, 0.30f);
+            save(dir + "call.bin", C);
+            save(dir + "put.bin", P);
+        } else if (mode == "bs_demo") {
+            auto Sa = load<dtable>(dir + "S.bin", n), Xa = load<dtable>(dir + "K.bin", n),
+                 Ta = load<dtable>(dir + "T.bin", n), ra = load<dtable>(dir + "r.bin", n),
+                 va = load<dtable>(dir + "v.bin", n);
+            dtable R(nt2::of_size(n));
+            // as in the demo, da/d1/d2 are materialised tables
+            dtable da, d1, d2;
+            da = nt2::sqrt(Ta);
+            d1 = nt2::log(Sa / Xa) + (nt2::fma(nt2::sqr(va), 0.5f, ra) * Ta) / (va * da);
+            d2 = nt2::fnms(va, da, d1);
+            R = nt2::fnms(Xa * nt2::exp(-ra * Ta), nt2::fastnormcdf(d2), Sa * nt2::fastnormcdf(d1));
+            save(dir + "R.bin", R);
+        } else if (mode == "saxpy") {
+            auto X = load<dtable>(dir + "x.bin", n), Y = load<dtable>(dir + "y.bin", n);
+            const float alpha = read_bin<float>(dir + "alpha.bin", 1)[0];
+            Y = alpha * X + Y;
+            save(dir + "y_out.bin", Y);
+        } else if (mode == "rgb2yuv") {
+            auto r = load<dtable>(dir + "r.bin", n), g = load<dtable>(dir + "g.bin", n), b = load<dtable>(dir + "b.bin", n);
+            dtable y(nt2::of_size(n)), u(nt2::of_size(n)), v(nt2::of_size(n));
+            nt2::tie(y, u, v) = nt2::tie(0.299f * r + 0.587f * g + 0.114f * b, 0.492f * (b - y), 0.877f * (r - y));
+            save(dir + "y.bin", y);
+            save(dir + "u.bin", u);
+            save(dir + "v.bin", v);
+        } else if (mode == "sdot") {
+            auto X = load<dtable>(dir + "x.bin", n), Y = load<dtable>(dir + "y.bin", n);
+            std::printf("globalsum %.17g\nsum64 %.17g\ndot %.9g\nsum %.9g\n", (double)nt2::globalsum(X * Y),
+                        nt2::sum64(X * Y), (double)nt2::dot(X, Y), (double)nt2::sum(X));
+            // sum of a general expression goes through a temporary
+            std::printf("sum_expr %.17g\n", nt2::sum64(nt2::sqr(X) + Y));
+        } else if (mode == "sigmadelta") {
+            const std::size_t frames = std::strtoull(argv[4], nullptr, 10);
+            auto all = read_bin<std::uint8_t>(dir + "frames.bin", n * frames);
+            nt2::table<std::uint8_t> hf(nt2::of_size(n));
+            std::memcpy(hf.data(), all.data(), n);
+            u8table bkg, fr(nt2::of_size(n)), var(nt2::of_size(n)), out(nt2::of_size(n));
+            bkg = hf;
+            nt2::table<std::uint8_t> ones(nt2::of_size(n));
+            std::memset(ones.data(), 1, n);
+            var = ones;
+            for (std::size_t k = 1; k < frames; ++k) {
+                std::memcpy(hf.data(), all.data() + k * n, n);
+                fr = hf;
+                auto diff = nt2::max(bkg, fr) - nt2::min(bkg, fr);
+                auto mul = nt2::adds(nt2::adds(diff, diff), diff);
+                nt2::tie(bkg, var, out) =
+                    nt2::tie(nt2::selinc(bkg < fr, nt2::seldec(bkg > fr, bkg)),
+                             nt2::if_else(diff != std::uint8_t(0), nt2::selinc(var < mul, nt2::seldec(var > mul, var)),
+                                          var),
+                             nt2::if_zero_else_one(diff < var));
+            }
+            save(dir + "bkg.bin", bkg);
+            save(dir + "var.bin", var);
+            save(dir + "label.bin", out);
+        } else {
+            std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
+            return 2;
+        }
+    } catch (const nt2::gpu_error &e) {
+        std::fprintf(stderr, "nt2 gpu error: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}

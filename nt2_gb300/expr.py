@@ -76,17 +76,36 @@ def _un(op):
 
 
 exp, log, log1p, erfc = _un("EXP"), _un("LOG"), _un("LOG1P"), _un("ERFC")
-normcdf, fastnormcdf, sqrt, sqr, rec = _un("NORMCDF"), _un("FASTNORMCDF"), _un("SQRT"), _un("SQR"), _un("REC")
+normcdf, fastnormcdf, sqrt, rec = _un("NORMCDF"), _un("FASTNORMCDF"), _un("SQRT"), _un("REC")
 abs_ = _un("ABS")
+
+# Functors applied to plain numbers evaluate at once in float32 with NT2's
+# scalar semantics (each step rounded, no fusion), as NT2's scalar overloads
+# do in C++ before an expression is built.
+
+
+def _f32(x):
+    import numpy as np
+    return np.float32(x)
+
+
+def sqr(a):
+    if isinstance(a, Node):
+        return Node("SQR", (a,), a.dtype)
+    return float(_f32(a) * _f32(a))
 
 
 def fma(a, b, c):
+    if not any(isinstance(x, Node) for x in (a, b, c)):
+        return float(_f32(_f32(a) * _f32(b)) + _f32(c))
     dt = next(x.dtype for x in (a, b, c) if isinstance(x, Node))
     return Node("FMA", tuple(_wrap(x, dt) for x in (a, b, c)), dt)
 
 
 def fnms(a, b, c):
     """c - a*b"""
+    if not any(isinstance(x, Node) for x in (a, b, c)):
+        return float(_f32(c) - _f32(_f32(a) * _f32(b)))
     dt = next(x.dtype for x in (a, b, c) if isinstance(x, Node))
     return Node("FNMS", tuple(_wrap(x, dt) for x in (a, b, c)), dt)
 

