@@ -193,6 +193,23 @@ nt2g_status nt2g_reduce_workspace_size(int64_t n, size_t *bytes);
 nt2g_status nt2g_reduce_f32(const float *x, const float *y, int64_t n, void *workspace,
                             size_t workspace_bytes, double *out64, float *out32, void *stream);
 
+/* The same reduction for callers that cannot allocate device memory: hosts
+ * whose runtime owns every device allocation through its own pool, code that
+ * must not risk cudaMalloc/cudaFree synchronizing the device, thin wrappers
+ * with nowhere to keep a workspace.  Its scratch (a block ticket and one
+ * FP64 partial per block, at most 4864 blocks: 39,168 bytes) is a static
+ * device array inside the library, held by every GPU that loads it until the
+ * process exits; it never calls cudaMalloc or cudaFree.  The first call on a
+ * device looks up that array's device address (with the device current);
+ * make that first call before any stream capture.  All calls share the one
+ * array, so calls that overlap on the GPU (other streams, other threads) race
+ * and must be serialised by the caller.  A launch that would need more block
+ * partials than the array holds is rejected with NT2G_ERR_UNSUPPORTED.
+ * No counterpart in the reference (NT2 allocates its reduction temporaries
+ * on the host). */
+nt2g_status nt2g_reduce_f32_noalloc(const float *x, const float *y, int64_t n, double *out64,
+                                    float *out32, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Batched uneven tables: one persistent launch over many tables, each */
 /* with its own expression.                                             */

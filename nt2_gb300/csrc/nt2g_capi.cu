@@ -784,6 +784,14 @@ extern "C" nt2g_status nt2g_reduce_f32(const float *x, const float *y, int64_t n
     return launch_reduce(x, y, n, workspace, out64, out32, (cudaStream_t)stream);
 }
 
+extern "C" nt2g_status nt2g_reduce_f32_noalloc(const float *x, const float *y, int64_t n, double *out64, float *out32,
+                                               void *stream)
+{
+    NT2G_REQ_N(); NT2G_REQ(x);
+    NT2G_CHECK_ARG(out64 != nullptr, "nt2g_reduce_f32_noalloc: out64 is NULL");
+    return launch_reduce_noalloc(x, y, n, out64, out32, (cudaStream_t)stream);
+}
+
 // ------------------------------------------------------------- memory ----
 extern "C" nt2g_status nt2g_device_alloc(size_t bytes, void **ptr)
 {

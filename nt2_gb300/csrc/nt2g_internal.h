@@ -61,6 +61,8 @@ nt2g_status launch_saxpy(float alpha, const float *X, const float *Y, float *O, 
 nt2g_status reduce_workspace_bytes(size_t *bytes);
 nt2g_status launch_reduce(const float *x, const float *y, int64_t n, void *ws, double *out64, float *out32,
                           cudaStream_t st);
+nt2g_status launch_reduce_noalloc(const float *x, const float *y, int64_t n, double *out64, float *out32,
+                                  cudaStream_t st);
 nt2g_status launch_expr3(const float *x, const float *y, const float *z, float *out, int64_t n, int precision,
                          cudaStream_t st);
 nt2g_status launch_rgb2yuv(const float *r, const float *g, const float *b, float *y, float *u, float *v,

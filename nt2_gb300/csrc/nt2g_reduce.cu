@@ -14,6 +14,7 @@
 // ticket after a release fence) adds the block partials in FP64 in a fixed
 // order.  The result is deterministic for a given n and device.  No block
 // ever waits on another.
+#include <mutex>
 #include "nt2g_common.cuh"
 #include "nt2g_internal.h"
 
@@ -175,6 +176,69 @@ nt2g_status launch_reduce(const float *x, const float *y, int64_t n, void *ws, d
     if (y) k_reduce<true><<<g, kRThreads, 0, st>>>(x, y, n, vec, partials, ticket, out64, out32);
     else k_reduce<false><<<g, kRThreads, 0, st>>>(x, y, n, vec, partials, ticket, out64, out32);
     NT2G_LAUNCH_CHECK("reduce launch");
+    return NT2G_OK;
+}
+
+// ------------------------------------------------- no-allocation variant --
+// Same kernel, but its scratch (the block ticket and one FP64 partial per
+// block) lives in this file-scope device array instead of a caller workspace.
+// It is for callers that cannot allocate device memory: hosts whose runtime
+// owns every device allocation through its own pool and forbids others
+// (language runtimes behind an FFI, engines with a fixed device-memory
+// budget), code that must not risk cudaMalloc/cudaFree synchronizing the
+// device, and thin wrappers with nowhere to keep a workspace between calls.
+// Every GPU that loads the library holds these 39,168 bytes until exit.
+static __device__ __align__(256) unsigned char g_reduce_scratch[kWsBytes];
+
+// Device address of g_reduce_scratch for the current device.  Host code only
+// sees a host-side stand-in for the symbol, so the address is asked of the
+// runtime once per device (with that device current) and cached.
+static nt2g_status noalloc_scratch(void **out)
+{
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static void *addr[kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "nt2g_reduce_f32_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("nt2g_reduce_f32_noalloc: device %d beyond the %d devices it tracks", dev, kMaxDevices);
+        return NT2G_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_reduce_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "nt2g_reduce_f32_noalloc: cudaGetSymbolAddress");
+        addr[dev] = p;
+    }
+    *out = addr[dev];
+    return NT2G_OK;
+}
+
+nt2g_status launch_reduce_noalloc(const float *x, const float *y, int64_t n, double *out64, float *out32,
+                                  cudaStream_t st)
+{
+    void *ws = nullptr;
+    nt2g_status s = noalloc_scratch(&ws);
+    if (s != NT2G_OK) return s;
+    const bool dot = y != nullptr;
+    int g = dot ? persistent_blocks(k_reduce<true>, kRThreads, 0, kRThreads * 8, (n + 3) / 4)
+                : persistent_blocks(k_reduce<false>, kRThreads, 0, kRThreads * 8, (n + 3) / 4);
+    if (g > kMaxPartials) {
+        set_error("nt2g_reduce_f32_noalloc: the launch needs %d block partials, the static scratch holds %d", g,
+                  kMaxPartials);
+        return NT2G_ERR_UNSUPPORTED;
+    }
+    unsigned int *ticket = (unsigned int *)ws;
+    double *partials = (double *)((char *)ws + 256);
+    // the array keeps the previous call's contents: the ticket must restart at 0
+    cudaError_t e = cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return cuda_status(e, "nt2g_reduce_f32_noalloc: ticket reset");
+    int vec = aligned16(x) && (!y || aligned16(y));
+    if (dot) k_reduce<true><<<g, kRThreads, 0, st>>>(x, y, n, vec, partials, ticket, out64, out32);
+    else k_reduce<false><<<g, kRThreads, 0, st>>>(x, y, n, vec, partials, ticket, out64, out32);
+    NT2G_LAUNCH_CHECK("nt2g_reduce_f32_noalloc launch");
     return NT2G_OK;
 }
 

@@ -84,6 +84,7 @@ _SIGNATURES = {
     "nt2g_map_f32": (_I32, [_I32, _VP, _VP, _I64, _I32, _VP]),
     "nt2g_reduce_workspace_size": (_I32, [_I64, ctypes.POINTER(ctypes.c_size_t)]),
     "nt2g_reduce_f32": (_I32, [_VP, _VP, _I64, _VP, ctypes.c_size_t, _VP, _VP, _VP]),
+    "nt2g_reduce_f32_noalloc": (_I32, [_VP, _VP, _I64, _VP, _VP, _VP]),
     "nt2g_batch_create": (_I32, [ctypes.POINTER(BatchItem), _I32, ctypes.POINTER(BatchTune), ctypes.POINTER(_VP)]),
     "nt2g_batch_destroy": (None, [_VP]),
     "nt2g_batch_run": (_I32, [_VP, _VP]),
