@@ -113,6 +113,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# -------------------------------------------------------- multi-rank logic
+def max_over_ranks(ms, world, dist=None, device="cpu"):
+    """Slowest rank's time: every rank must have finished its batch."""
+    if world == 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(units_per_rank, steps, world, ms):
+    """Elements per second over all ranks (replicas: each rank its own batch)."""
+    return world * units_per_rank * steps / (ms / 1e3)
+
+
 # ----------------------------------------------------------------- workloads
 class Workload:
     name = ""
@@ -121,6 +137,7 @@ class Workload:
     launches = 1       # our kernels per step
     kernel = ""        # dominant kernel (for the roofline)
     flush = "inputs larger than L2"
+    independent = False  # consecutive steps touch disjoint buffers (may overlap on two streams)
 
     def step(self, i):
         raise NotImplementedError
@@ -129,6 +146,7 @@ class Workload:
 class BlackScholes(Workload):
     N = 1 << 20
     SETS = 32
+    independent = True
 
     def __init__(self, torch, lib, dev, precision):
         self.torch, self.lib, self.prec = torch, lib, precision
@@ -147,25 +165,36 @@ class BlackScholes(Workload):
         self.lib.blackscholes(self.S[k], self.K[k], self.T[k], self.C[k], self.P[k], 0.02, sigma_s=0.30,
                               precision=self.prec)
 
-    # end to end through the C ABI from pinned host buffers
+    # End to end through the C ABI from pinned host buffers: every step copies
+    # its S, K, T in, runs the kernel and copies call, put out.  Steps
+    # alternate between two streams with their own device buffers, so one
+    # step's copies overlap the other's kernel (double buffering).
+    LANES = 2
+
     def e2e_setup(self):
         t = self.torch
-        self.hS = self.S[0].cpu().pin_memory()
-        self.hK = self.K[0].cpu().pin_memory()
-        self.hT = self.T[0].cpu().pin_memory()
-        self.hC = t.empty(self.N, pin_memory=True)
-        self.hP = t.empty(self.N, pin_memory=True)
-        self.dS, self.dK, self.dT = (t.empty(self.N, device=self.S.device) for _ in range(3))
-        self.dC, self.dP = t.empty_like(self.dS), t.empty_like(self.dS)
+        dev = self.S.device
+        self.lanes = []
+        for k in range(self.LANES):
+            host_in = [self.S[k].cpu().pin_memory(), self.K[k].cpu().pin_memory(), self.T[k].cpu().pin_memory()]
+            host_out = [t.empty(self.N, pin_memory=True), t.empty(self.N, pin_memory=True)]
+            dev_in = [t.empty(self.N, device=dev) for _ in range(3)]
+            dev_out = [t.empty(self.N, device=dev) for _ in range(2)]
+            self.lanes.append((t.cuda.Stream(), host_in, host_out, dev_in, dev_out))
         return 12 * self.N, 8 * self.N
 
     def e2e_step(self, i):
-        self.dS.copy_(self.hS, non_blocking=True)
-        self.dK.copy_(self.hK, non_blocking=True)
-        self.dT.copy_(self.hT, non_blocking=True)
-        self.lib.blackscholes(self.dS, self.dK, self.dT, self.dC, self.dP, 0.02, sigma_s=0.30, precision=self.prec)
-        self.hC.copy_(self.dC, non_blocking=True)
-        self.hP.copy_(self.dP, non_blocking=True)
+        st, host_in, host_out, dev_in, dev_out = self.lanes[i % self.LANES]
+        with self.torch.cuda.stream(st):
+            for d, h in zip(dev_in, host_in):
+                d.copy_(h, non_blocking=True)
+            self.lib.blackscholes(dev_in[0], dev_in[1], dev_in[2], dev_out[0], dev_out[1], 0.02, sigma_s=0.30,
+                                  precision=self.prec, stream=st)
+            for h, d in zip(host_out, dev_out):
+                h.copy_(d, non_blocking=True)
+
+    def e2e_streams(self):
+        return [ln[0] for ln in self.lanes]
 
     @staticmethod
     def cpu(oracle, nthreads, sample_n):
@@ -227,7 +256,13 @@ class Batched(Workload):
             for j, t in enumerate(outs):
                 items[i].out[j] = t.data_ptr()
             items[i].s[0], items[i].s[1] = s
-        tn = tune or (256, 0, 4)
+        if tune:
+            tn, how = tune, "given"
+        else:  # the project's autotuner, cached per GPU and batch shape
+            from nt2_gb300 import autotune
+            best, _, cached = autotune.tuned(items, precision)
+            tn, how = (best.block_threads, best.blocks_per_sm, best.tile_vectors), \
+                ("autotuned (cache)" if cached else "autotuned")
         t = lib.BatchTune(tn[0], tn[1], tn[2], precision)
         self.h = ctypes.c_void_p()
         lib.check(lib.load().nt2g_batch_create(items, len(sizes), ctypes.byref(t), ctypes.byref(self.h)))
@@ -236,7 +271,8 @@ class Batched(Workload):
         self.launches = len(sizes) if per_table else 1
         self.kernel = "k_single" if per_table else "k_batch"
         self.name = (f"batched 4096 tables log-uniform [1024, 4194304] ({self.units} elements), "
-                     f"{'one plain launch per table' if per_table else 'one persistent launch'}, tune {tn}")
+                     f"{'one plain launch per table' if per_table else 'one persistent launch'}, "
+                     f"tune threads,blocks/SM,vectors/tile={tn} ({how})")
 
     def step(self, i):
         fn = self.lib.load().nt2g_batch_run_per_table if self.per_table else self.lib.load().nt2g_batch_run
@@ -286,8 +322,31 @@ class SigmaDelta(Workload):
         self.lib.sigmadelta(self.frames[1 + i % 63], self.bkg, self.var, self.lab)
 
 
+class SigmaDeltaFused(Workload):
+    """All 63 frame steps of the 64-frame sequence in one launch: bkg/var stay
+    in registers, each frame is read and each label written once."""
+
+    def __init__(self, torch, lib, dev):
+        self.torch, self.lib = torch, lib
+        h, w, f = 1080, 1920, 64
+        g = torch.Generator(device=dev).manual_seed(1002)
+        self.frames = torch.randint(0, 256, (f, h * w), dtype=torch.uint8, device=dev, generator=g)
+        self.bkg = self.frames[0].clone()
+        self.var = torch.ones_like(self.bkg)
+        self.labels = torch.empty((f - 1, h * w), dtype=torch.uint8, device=dev)
+        nf = f - 1
+        self.units = h * w * nf
+        self.bytes = h * w * (2 * nf + 4)
+        self.kernel = "k_sigmadelta_frames"
+        self.name = "sigmadelta 1920x1080 uint8, 63 frame steps fused in one launch per step"
+
+    def step(self, i):
+        self.lib.sigmadelta_frames(self.frames[1:], self.bkg, self.var, self.labels)
+
+
 class Rgb2Yuv(Workload):
     SETS = 8
+    independent = True
 
     def __init__(self, torch, lib, dev):
         self.torch, self.lib = torch, lib
@@ -306,7 +365,7 @@ class Rgb2Yuv(Workload):
         self.lib.rgb2yuv(r, g, b, y, u, v)
 
 
-def make(name, torch, lib, dev, precision):
+def make(name, torch, lib, dev, precision, tune=None):
     if name == "bs":
         return BlackScholes(torch, lib, dev, precision)
     if name in ("reduce", "dot"):
@@ -314,7 +373,7 @@ def make(name, torch, lib, dev, precision):
     if name == "sum":
         return Reduce(torch, lib, dev, dot=False)
     if name == "batched":
-        return Batched(torch, lib, dev, per_table=False, precision=precision)
+        return Batched(torch, lib, dev, per_table=False, precision=precision, tune=tune)
     if name == "pertable":
         return Batched(torch, lib, dev, per_table=True, precision=precision)
     if name == "adjoint":
@@ -325,6 +384,8 @@ def make(name, torch, lib, dev, precision):
         return SigmaDelta(torch, lib, dev)
     if name == "rgb2yuv":
         return Rgb2Yuv(torch, lib, dev)
+    if name == "sigmadelta_fused":
+        return SigmaDeltaFused(torch, lib, dev)
     raise SystemExit(f"unknown config {name}")
 
 
@@ -414,7 +475,8 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     lib.load()
     prec = lib.PREC_NT2 if args.precision == "nt2" else lib.PREC_FAST
-    wl = make(args.config, torch, lib, dev, prec)
+    tune = tuple(int(v) for v in args.tune.split(",")) if args.tune else None
+    wl = make(args.config, torch, lib, dev, prec, tune)
     stream = torch.cuda.current_stream()
 
     def barrier():
@@ -433,12 +495,27 @@ def run_ours(args):
     # The K timed steps are captured once into a CUDA graph and replayed, so
     # the measurement is the device's time for K launches rather than the
     # Python/ctypes cost of issuing them (each launch still happens, in order).
+    # Independent steps (disjoint rotating buffer sets) alternate between two
+    # streams inside the graph, so one step's tail overlaps the next step's
+    # head; steps that share buffers stay in order on one stream.
     graph = None
+    n_streams = max(1, args.streams) if wl.independent else 1
     if not args.no_graph:
         graph = torch.cuda.CUDAGraph()
+        extra = [torch.cuda.Stream() for _ in range(n_streams - 1)]
         with torch.cuda.graph(graph, stream=side, capture_error_mode="thread_local"):
+            fork = torch.cuda.Event()
+            fork.record(side)
+            for s_ in extra:
+                s_.wait_event(fork)
+            lanes = [side] + extra
             for i in range(args.steps):
-                wl.step(i)
+                with torch.cuda.stream(lanes[i % n_streams]):
+                    wl.step(i)
+            for s_ in extra:
+                join = torch.cuda.Event()
+                join.record(s_)
+                side.wait_event(join)
         barrier()
 
     def run_k():
@@ -460,17 +537,12 @@ def run_ours(args):
             run_k()
             e1.record(stream)
             barrier()
-            ms = e0.elapsed_time(e1)
-            if world > 1:
-                t = torch.tensor([ms], device=dev)
-                dist.all_reduce(t, op=dist.ReduceOp.MAX)
-                ms = float(t.item())
-            trials.append(ms)
+            trials.append(max_over_ranks(e0.elapsed_time(e1), world, dist, dev))
             if (time.perf_counter() - t_start > args.min_seconds and len(trials) >= 3) or len(trials) >= 100000:
                 break
     ms = float(np.median(trials))
     per_step = ms / args.steps
-    value = world * wl.units * args.steps / (ms / 1e3)
+    value = whole_job_value(wl.units, args.steps, world, ms)
     peak, peak_kind = peaks()
     achieved = wl.bytes / (per_step / 1e3) / 1e9
     out = {
@@ -480,7 +552,8 @@ def run_ours(args):
         "data": "synthetic (seeded, distributions per workload)",
         "config": {"workload": wl.name, "precision": args.precision, "l2": wl.flush,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "trials": len(trials), "launch": "CUDA graph of the K steps" if graph is not None else "eager"},
+                   "trials": len(trials),
+                   "launch": (f"CUDA graph of the K steps on {n_streams} stream(s)" if graph is not None else "eager")},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "kernel": wl.kernel,
                      "algorithmic_bytes_per_launch": wl.bytes // wl.launches,
@@ -496,12 +569,18 @@ def run_ours(args):
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
+        for s_ in wl.e2e_streams():
+            s_.wait_event(e0)
         for i in range(args.steps):
             wl.e2e_step(i)
+        for s_ in wl.e2e_streams():
+            done = torch.cuda.Event()
+            done.record(s_)
+            stream.wait_event(done)
         e1.record(stream)
         barrier()
-        ems = e0.elapsed_time(e1)
-        out["e2e"] = {"value": world * wl.units * args.steps / (ems / 1e3), "unit": UNIT,
+        ems = max_over_ranks(e0.elapsed_time(e1), world, dist, dev)
+        out["e2e"] = {"value": whole_job_value(wl.units, args.steps, world, ems), "unit": UNIT,
                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ems / args.steps}
     if rank == 0 and world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args.config, budget_s=args.cpu_budget)
@@ -522,6 +601,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-graph", action="store_true", help="issue the K steps eagerly instead of from a graph")
+    ap.add_argument("--streams", type=int, default=2, help="streams for independent steps inside the graph")
+    ap.add_argument("--tune", default="", help="batched: block_threads,blocks_per_sm,tile_vectors")
     ap.add_argument("--min-seconds", type=float, default=2.0, help="repeat K-step trials for at least this long")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -251,6 +251,14 @@ nt2g_status nt2g_batch_run_per_table(nt2g_batch *b, void *stream);
 /* Capture nt2g_batch_run into a CUDA graph on `stream` once; later calls
  * replay it. */
 nt2g_status nt2g_batch_run_graph(nt2g_batch *b, void *stream);
+/* Autotuner: times nt2g_batch_run for each candidate tune (NULL: a built-in
+ * grid over block size, float4 vectors per thread per tile and resident
+ * blocks per SM / static striding) and returns the fastest, with its time per
+ * run.  Plans are built per candidate (device memory allocated at tuning
+ * time); in-place expressions are applied once per timed run. */
+nt2g_status nt2g_batch_autotune(const nt2g_batch_item *items, int32_t n_items,
+                                const nt2g_batch_tune *candidates, int32_t n_candidates, int32_t reps,
+                                int32_t precision, void *stream, nt2g_batch_tune *best, float *best_ms);
 /* Total elements and algorithmic bytes of the batch. */
 nt2g_status nt2g_batch_stats(const nt2g_batch *b, int64_t *elements, int64_t *bytes);
 

@@ -33,21 +33,21 @@ __device__ __forceinline__ void run_tile(const DItem &it, int64_t start, int64_t
     const int64_t v1 = it.vec ? (end >> 2) : v0;
     switch (it.expr) {
     case NT2G_BATCH_BLACKSCHOLES: {
-        const float sig = it.s[0], r = it.s[1];
+        const float sig = it.s[0], r = it.s[1], inv_sig = P::exact ? 0.0f : inv_fast(sig);
         for (int64_t i = v0 + threadIdx.x; i < v1; i += blockDim.x) {
             float4 s = ld_stream((const float4 *)it.in[0] + i), k = ld_stream((const float4 *)it.in[1] + i),
                    t = ld_stream((const float4 *)it.in[2] + i), c, p;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 float cj, pj;
-                bs_option<P>(get(s, j), get(k, j), get(t, j), sig, r, cj, pj);
+                bs_option<P>(get(s, j), get(k, j), get(t, j), sig, inv_sig, r, cj, pj);
                 set(c, j, cj); set(p, j, pj);
             }
             st_stream((float4 *)it.out[0] + i, c);
             st_stream((float4 *)it.out[1] + i, p);
         }
         for (int64_t i = (v1 << 2) + threadIdx.x; i < end; i += blockDim.x)
-            bs_option<P>(it.in[0][i], it.in[1][i], it.in[2][i], sig, r, it.out[0][i], it.out[1][i]);
+            bs_option<P>(it.in[0][i], it.in[1][i], it.in[2][i], sig, inv_sig, r, it.out[0][i], it.out[1][i]);
         break;
     }
     case NT2G_BATCH_SAXPY: {
@@ -157,9 +157,9 @@ extern "C" nt2g_status nt2g_batch_create(const nt2g_batch_item *items, int32_t n
     NT2G_CHECK_ARG(out != nullptr, "nt2g_batch_create: out is NULL");
     *out = nullptr;
     NT2G_CHECK_ARG(items != nullptr && n_items > 0, "nt2g_batch_create: no items");
-    nt2g_batch_tune tn = tune ? *tune : nt2g_batch_tune{256, 0, 4, NT2G_PREC_FAST};
-    if (tn.block_threads == 0) tn.block_threads = 256;
-    if (tn.tile_vectors == 0) tn.tile_vectors = 4;
+    nt2g_batch_tune tn = tune ? *tune : nt2g_batch_tune{128, 0, 32, NT2G_PREC_FAST};
+    if (tn.block_threads == 0) tn.block_threads = 128;
+    if (tn.tile_vectors == 0) tn.tile_vectors = 32;
     NT2G_CHECK_ARG(tn.block_threads >= 64 && tn.block_threads <= 1024 && tn.block_threads % 32 == 0,
                    "nt2g_batch_create: block_threads %d not a multiple of 32 in [64,1024]", tn.block_threads);
     NT2G_CHECK_ARG(tn.tile_vectors >= 1 && tn.tile_vectors <= 64, "nt2g_batch_create: tile_vectors %d", tn.tile_vectors);
@@ -308,5 +308,63 @@ extern "C" nt2g_status nt2g_batch_stats(const nt2g_batch *b, int64_t *elements, 
     NT2G_CHECK_ARG(b != nullptr, "nt2g_batch_stats: NULL batch");
     if (elements) *elements = b->elements;
     if (bytes) *bytes = b->bytes;
+    return NT2G_OK;
+}
+
+// ---------------------------------------------------------------- tuning --
+// Times nt2g_batch_run for each candidate (block size, float4 vectors per
+// thread per tile -- i.e. elements per thread -- and resident blocks per SM,
+// negative for the static tile stride) with CUDA events, reps runs after one
+// warm-up each, and returns the fastest.  Each candidate builds its own plan,
+// so device memory is allocated here, at tuning time.  Every run executes the
+// whole batch: expressions that update a table in place (saxpy) are applied
+// (1 + reps) times per candidate.
+extern "C" nt2g_status nt2g_batch_autotune(const nt2g_batch_item *items, int32_t n_items,
+                                           const nt2g_batch_tune *candidates, int32_t n_candidates, int32_t reps,
+                                           int32_t precision, void *stream, nt2g_batch_tune *best, float *best_ms)
+{
+    NT2G_CHECK_ARG(best != nullptr, "nt2g_batch_autotune: best is NULL");
+    NT2G_CHECK_ARG(reps >= 1 && reps <= 100, "nt2g_batch_autotune: reps %d outside [1,100]", reps);
+    static const nt2g_batch_tune grid[] = {
+        {128, 0, 8, 0},  {128, 0, 16, 0}, {128, 0, 32, 0}, {128, 0, 64, 0}, {256, 0, 8, 0},  {256, 0, 16, 0},
+        {256, 0, 32, 0}, {256, 0, 64, 0}, {512, 0, 16, 0}, {512, 0, 32, 0}, {128, -1, 32, 0}, {256, -1, 16, 0},
+    };
+    const nt2g_batch_tune *cand = candidates ? candidates : grid;
+    const int nc = candidates ? n_candidates : (int)(sizeof grid / sizeof grid[0]);
+    NT2G_CHECK_ARG(nc >= 1, "nt2g_batch_autotune: no candidates");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return cuda_status(ce, "nt2g_batch_autotune: events");
+    }
+    float best_t = 0.f;
+    int best_i = -1;
+    nt2g_status status = NT2G_OK;
+    for (int c = 0; c < nc && status == NT2G_OK; ++c) {
+        nt2g_batch_tune t = cand[c];
+        t.precision = precision;
+        nt2g_batch *b = nullptr;
+        status = nt2g_batch_create(items, n_items, &t, &b);
+        if (status != NT2G_OK) break;
+        status = nt2g_batch_run(b, stream);  // warm-up
+        if (status == NT2G_OK) ce = cudaEventRecord(e0, st);
+        for (int r = 0; r < reps && status == NT2G_OK && ce == cudaSuccess; ++r) status = nt2g_batch_run(b, stream);
+        if (status == NT2G_OK && ce == cudaSuccess) ce = cudaEventRecord(e1, st);
+        if (status == NT2G_OK && ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (status == NT2G_OK && ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+        nt2g_batch_destroy(b);
+        if (status == NT2G_OK && ce != cudaSuccess) status = cuda_status(ce, "nt2g_batch_autotune: timing");
+        if (status == NT2G_OK && (best_i < 0 || ms < best_t)) { best_t = ms; best_i = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (status != NT2G_OK) return status;
+    *best = cand[best_i];
+    best->precision = precision;
+    if (best_ms) *best_ms = best_t / reps;
     return NT2G_OK;
 }

@@ -18,6 +18,7 @@ __global__ void __launch_bounds__(256) k_bs(const float *__restrict__ S, const f
                                             float sig_s, float r, float *__restrict__ call,
                                             float *__restrict__ put, int64_t n, int vec)
 {
+    const float inv_sig_s = P::exact ? 0.0f : inv_fast(sig_s);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (vec) {
@@ -30,7 +31,8 @@ __global__ void __launch_bounds__(256) k_bs(const float *__restrict__ S, const f
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 float cj, pj;
-                bs_option<P>(get(s, j), get(k, j), get(t, j), get(v, j), r, cj, pj);
+                const float sj = get(v, j);
+                bs_option<P>(get(s, j), get(k, j), get(t, j), sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
                 set(c, j, cj);
                 set(p, j, pj);
             }
@@ -39,14 +41,16 @@ __global__ void __launch_bounds__(256) k_bs(const float *__restrict__ S, const f
         }
         for (int64_t i = (nv << 2) + tid; i < n; i += stride) {
             float cj, pj;
-            bs_option<P>(S[i], K[i], T[i], SIG_TAB ? sig[i] : sig_s, r, cj, pj);
+            const float sj = SIG_TAB ? sig[i] : sig_s;
+            bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
             call[i] = cj;
             put[i] = pj;
         }
     } else {
         for (int64_t i = tid; i < n; i += stride) {
             float cj, pj;
-            bs_option<P>(S[i], K[i], T[i], SIG_TAB ? sig[i] : sig_s, r, cj, pj);
+            const float sj = SIG_TAB ? sig[i] : sig_s;
+            bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
             call[i] = cj;
             put[i] = pj;
         }
@@ -101,20 +105,15 @@ __device__ __forceinline__ void bs_vjp_option(float S, float K, float T, float s
                                               float gp, float &C, float &P_, float &dS, float &dK,
                                               float &dT, float &dsig, float &dr)
 {
-    // forward (as the fast forward kernel)
-    float sq = __fsqrt_rn(T);
-    float vs = Fast::mul(sig, sq);
-    float lq = log<Fast>(Fast::fdiv(S, K));
-    float a = Fast::fma(Fast::mul(sig, sig), 0.5f, r);
-    float d1 = Fast::fdiv(Fast::fma(a, T, lq), vs);
-    float d2 = Fast::fma(-sig, sq, d1);
-    float ert = exp<Fast>(Fast::mul(-r, T));
-    float e = Fast::mul(K, ert);
+    // forward (the fast forward kernel's arithmetic, bit for bit)
+    BsFwd f = bs_prefix_fast(S, K, T, sig, inv_fast(sig), r);
     float n1, m1, n2, m2, g1;  // g1 = exp(-d1^2/2)
-    normcdf_pair_pdf(d1, n1, m1, g1);
-    normcdf_pair<Fast>(d2, n2, m2);
+    normcdf_pair_pdf(f.d1, n1, m1, g1);
+    normcdf_pair_fast(f.d2, n2, m2);
+    const float sq = f.sq, ert = f.ert, e = f.e;
     C = Fast::fma(-e, n2, Fast::mul(S, n1));
     P_ = Fast::fma(-S, m1, Fast::mul(e, m2));
+    if (is_nan(f.d1) || is_nan(f.d2)) { C = f.d1 + f.d2; P_ = C; }
     // reverse
     const float inv_sqrt_2pi = 0.398942280401432678f;
     float gs = Fast::add(gc, gp);
@@ -124,7 +123,7 @@ __device__ __forceinline__ void bs_vjp_option(float S, float K, float T, float s
     dS = Fast::fma(gc, n1, -Fast::mul(gp, m1));
     dK = Fast::mul(be, ert);
     dsig = Fast::mul(bvs, sq);
-    dT = Fast::fma(Fast::mul(bvs, sig), Fast::fdiv(0.5f, sq), -Fast::mul(r, bee));
+    dT = Fast::fma(Fast::mul(bvs, sig), Fast::mul(0.5f, f.rs), -Fast::mul(r, bee));
     dr = -Fast::mul(T, bee);
 }
 

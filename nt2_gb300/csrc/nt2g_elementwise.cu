@@ -192,7 +192,20 @@ __global__ void __launch_bounds__(kThreads) k_sigmadelta_frames(const uint8_t *_
         const int64_t nv = n >> 4;
         for (int64_t i = tid; i < nv; i += stride) {
             uint4 b = ld_stream((const uint4 *)bkg + i), v = ld_stream((const uint4 *)var + i), l;
-            for (int k = 0; k < nf; ++k) {
+            // frames come in groups of 4 loaded before any is used, so each
+            // thread keeps four 16-byte loads in flight across the frame loop
+            int k = 0;
+            for (; k + 4 <= nf; k += 4) {
+                uint4 f[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) f[j] = ld_stream((const uint4 *)(frames + (int64_t)(k + j) * n) + i);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    sd_vec(f[j], b, v, l);
+                    st_stream((uint4 *)(labels + (int64_t)(k + j) * n) + i, l);
+                }
+            }
+            for (; k < nf; ++k) {
                 uint4 f = ld_stream((const uint4 *)(frames + (int64_t)k * n) + i);
                 sd_vec(f, b, v, l);
                 st_stream((uint4 *)(labels + (int64_t)k * n) + i, l);

@@ -41,6 +41,17 @@ class BlackScholesFn(torch.autograd.Function):
         return outs[2], outs[3], outs[4], outs[5]
 
 
+SCALE_FLOOR = 2.0 ** -100  # below this FP32 holds a gradient's terms only as subnormals
+
+
+def _scaled_err(got, ref, scale):
+    """|got - ref| / term scale, the scale floored at 2^-100: a gradient whose
+    terms all fall below the float normal range (phi(d) underflows for
+    |d| > 13.2) is only checked to be that small."""
+    err = np.abs(np.asarray(got, np.float64) - ref)
+    return err / np.maximum(scale, SCALE_FLOOR)
+
+
 def test_vjp_against_fp64_analytic(lib, dev, oracle):
     n = 1 << 20
     S, K, T, sig = bs_inputs(n, seed=1004, sigma_table=True)
@@ -55,8 +66,8 @@ def test_vjp_against_fp64_analytic(lib, dev, oracle):
     scale = oracle.blackscholes_vjp_scale_f64(S, K, T, sig, R, gc, gp)
     names = ["dS", "dK", "dT", "dsigma", "dr"]
     for name, g, r, sc in zip(names, got[2:], ref, scale):
-        e = np.abs(g.astype(np.float64) - r) / sc
-        plain = np.abs(g.astype(np.float64) - r) / np.abs(r)
+        e = _scaled_err(g, r, sc)
+        plain = np.abs(g.astype(np.float64) - r) / np.where(r != 0, np.abs(r), 1.0)
         print(f"\n{name}: max rel err (term scale) {e.max():.3e} mean {e.mean():.3e}; "
               f"plain rel err median {np.median(plain):.3e}")
         assert e.max() <= REL_TOL, name
@@ -91,8 +102,9 @@ def test_vjp_against_central_differences(lib, dev, oracle):
             fd[k, i] = (gc[i] * (cu - cd) + gp[i] * (pu - pd)) / (2 * h)
     scale = oracle.blackscholes_vjp_scale_f64(S, K, T, sig, R, gc, gp)
     for k in range(5):
-        # central differences with h = 1e-4 relative carry O(h^2) truncation
-        e = np.abs(got[k].astype(np.float64) - fd[k]) / scale[k]
+        # central differences carry O(h^2) truncation and ~1e-14/h of FP64
+        # cancellation noise (1e-9 absolute for h = 1e-4 * 0.05): floor 1e-4
+        e = np.abs(got[k].astype(np.float64) - fd[k]) / np.maximum(scale[k], 1e-4)
         assert e.max() <= 1e-5, (k, e.max())
 
 
@@ -106,4 +118,4 @@ def test_autograd_function_backward(lib, dev, oracle):
     ref = oracle.blackscholes_vjp_f64(S, K, T, sig, R, gc, gp)
     scale = oracle.blackscholes_vjp_scale_f64(S, K, T, sig, R, gc, gp)
     for tt, r, sc in zip(ts, ref[:4], scale[:4]):
-        assert (np.abs(tt.grad.cpu().numpy().astype(np.float64) - r) / sc).max() <= REL_TOL
+        assert _scaled_err(tt.grad.cpu().numpy(), r, sc).max() <= REL_TOL

@@ -116,3 +116,27 @@ def test_batched_matches_plain_kernels(lib, dev, tune):
             assert el.value == int(np.sum(sizes))
         finally:
             L.nt2g_batch_destroy(h)
+
+
+def test_autotuner_picks_a_candidate_and_caches(lib, dev, tmp_path, monkeypatch):
+    from nt2_gb300 import autotune
+    monkeypatch.setenv("NT2G_TUNE_CACHE", str(tmp_path / "tune.json"))
+    sizes, exprs = batched_sizes(count=64, lo=1000, hi=200000, seed=6)
+    tabs = _make(lib, dev, sizes, exprs)
+    items = _items(lib, tabs, _fresh_outs(lib, tabs))
+    best, ms, cached = autotune.tuned(items, lib.PREC_FAST, reps=2)
+    assert not cached and ms > 0 and best.block_threads in (128, 256, 512)
+    best2, ms2, cached2 = autotune.tuned(items, lib.PREC_FAST)
+    assert cached2 and (best2.block_threads, best2.tile_vectors) == (best.block_threads, best.tile_vectors)
+    # a run with the chosen tune is bit-identical to the plain kernels
+    ref = _reference(lib, tabs)
+    outs = _fresh_outs(lib, tabs)
+    h = ctypes.c_void_p()
+    L = lib.load()
+    lib.check(L.nt2g_batch_create(_items(lib, tabs, outs), len(tabs), ctypes.byref(best), ctypes.byref(h)))
+    try:
+        lib.check(L.nt2g_batch_run(h, lib._stream()))
+        torch.cuda.synchronize()
+        _check(outs, ref)
+    finally:
+        L.nt2g_batch_destroy(h)

@@ -107,7 +107,7 @@ def test_rgb2yuv_accuracy(lib, dev, oracle):
         mild = np.abs(ref64) >= 2.0 ** -20 * np.abs(sc64)
         e = std_ulp(got[mild], ref64[mild])
         print(f"fast {name}: max {e.max():.2f} ulp (mild cancellation), conditioned max {cond.max():.2f}")
-        assert e.max() <= 2.0 and cond.max() <= 1.0, name
+        assert e.max() <= 1.0 and cond.max() <= 1.0, name
 
 
 def _sd_exprs(fr, bkg, var):
