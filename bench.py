@@ -205,6 +205,30 @@ class BlackScholes(Workload):
         return lambda: oracle.blackscholes(S, K, T, 0.02, 0.30, nthreads=nthreads)
 
 
+class BlackScholesGeneric(BlackScholes):
+    """The same batch through the expression front end, forced onto the
+    generic interpreter instead of the fused kernel it would bind."""
+
+    def __init__(self, torch, lib, dev, precision):
+        super().__init__(torch, lib, dev, precision)
+        from nt2_gb300 import expr as E
+        self.E = E
+        self.name = f"blackscholes_plain N={self.N} call+put through the generic interpreter, {self.SETS} sets"
+        self.kernel = "k_interp"
+
+    def step(self, i):
+        E, k = self.E, i % self.SETS
+        S, K, T = E.Table(self.S[k]), E.Table(self.K[k]), E.Table(self.T[k])
+        sig, r = 0.30, 0.02
+        sq = E.sqrt(T)
+        d1 = (E.log(S / K) + E.fma(E.sqr(sig), 0.5, r) * T) / (sig * sq)
+        d2 = E.fnms(sig, sq, d1)
+        e = K * E.exp(-r * T)
+        E.assign([self.C[k], self.P[k]], [E.fnms(e, E.normcdf(d2), S * E.normcdf(d1)),
+                                         E.fnms(S, E.normcdf(-d1), e * E.normcdf(-d2))],
+                 precision=self.prec, force_generic=True)
+
+
 class Reduce(Workload):
     N = 1 << 28
 
@@ -368,6 +392,8 @@ class Rgb2Yuv(Workload):
 def make(name, torch, lib, dev, precision, tune=None):
     if name == "bs":
         return BlackScholes(torch, lib, dev, precision)
+    if name == "bs_generic":
+        return BlackScholesGeneric(torch, lib, dev, precision)
     if name in ("reduce", "dot"):
         return Reduce(torch, lib, dev, dot=True)
     if name == "sum":

@@ -110,19 +110,6 @@ __global__ void k_batch(const DItem *__restrict__ items, const int64_t *__restri
     }
 }
 
-// One table per launch (the comparison path): the same tile code over a
-// single item, grid sized to the table.
-template <class P>
-__global__ void k_single(const DItem *__restrict__ items, int k, int64_t tile_elems)
-{
-    const DItem it = items[k];
-    for (int64_t t = blockIdx.x; t * tile_elems < it.n; t += gridDim.x) {
-        int64_t start = t * tile_elems;
-        int64_t end = start + tile_elems < it.n ? start + tile_elems : it.n;
-        run_tile<P>(it, start, end);
-    }
-}
-
 }  // namespace nt2g
 
 struct nt2g_batch {
@@ -256,29 +243,31 @@ extern "C" nt2g_status nt2g_batch_run(nt2g_batch *b, void *stream)
     return b->tune.precision == NT2G_PREC_NT2 ? batch_launch<Nt2>(b, st) : batch_launch<Fast>(b, st);
 }
 
-template <class P>
+// The comparison path: each table through its expression's own plain kernel
+// (nt2g_blackscholes_f32 / nt2g_saxpy_f32 / nt2g_expr3_f32 launchers), one
+// launch per table, as a caller without the batched path would issue them.
 static nt2g_status per_table(nt2g_batch *b, cudaStream_t st)
 {
-    const int threads = b->tune.block_threads;
-    int per_sm = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_single<P>, threads, 0) != cudaSuccess || per_sm < 1)
-        per_sm = 1;
-    const int64_t full = (int64_t)device_sm_count() * per_sm;
+    const int prec = b->tune.precision;
     for (int k = 0; k < b->n_items; ++k) {
-        int64_t tiles = (b->host_items[k].n + b->tile_elems - 1) / b->tile_elems;
-        if (tiles == 0) continue;
-        int grid = (int)(tiles < full ? tiles : full);
-        k_single<P><<<grid, threads, 0, st>>>(b->d_items, k, b->tile_elems);
+        const DItem &it = b->host_items[k];
+        nt2g_status s;
+        switch (it.expr) {
+        case NT2G_BATCH_BLACKSCHOLES:
+            s = launch_bs(it.in[0], it.in[1], it.in[2], nullptr, it.s[0], it.s[1], it.out[0], it.out[1], it.n, prec, st);
+            break;
+        case NT2G_BATCH_SAXPY: s = launch_saxpy(it.s[0], it.in[0], it.out[0], it.out[0], it.n, st); break;
+        default: s = launch_expr3(it.in[0], it.in[1], it.in[2], it.out[0], it.n, prec, st); break;
+        }
+        if (s != NT2G_OK) return s;
     }
-    NT2G_LAUNCH_CHECK("per-table launches");
     return NT2G_OK;
 }
 
 extern "C" nt2g_status nt2g_batch_run_per_table(nt2g_batch *b, void *stream)
 {
     NT2G_CHECK_ARG(b != nullptr, "nt2g_batch_run_per_table: NULL batch");
-    cudaStream_t st = (cudaStream_t)stream;
-    return b->tune.precision == NT2G_PREC_NT2 ? per_table<Nt2>(b, st) : per_table<Fast>(b, st);
+    return per_table(b, (cudaStream_t)stream);
 }
 
 extern "C" nt2g_status nt2g_batch_run_graph(nt2g_batch *b, void *stream)

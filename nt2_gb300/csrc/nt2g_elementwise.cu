@@ -177,8 +177,12 @@ __global__ void __launch_bounds__(kThreads) k_sigmadelta(const uint8_t *__restri
     for (int64_t i = done + tid; i < n; i += stride) sd_px(fr[i], bkg[i], var[i], lab[i]);
 }
 
-// Temporal fusion: a thread keeps 16 pixels' bkg/var in registers across all
-// frames; per pixel-frame HBM traffic drops from 6 B to 2 + 4/F B.
+// Temporal fusion: a thread keeps 4 pixels' bkg/var (one 32-bit word each)
+// in registers across all frames, so the 2-Mpixel frame still spreads over
+// ~0.5 M threads; eight frames' loads are issued before any is used.  Per
+// pixel-frame HBM traffic drops from 6 B to 2 + 4/F B.
+constexpr int kFramePrefetch = 8;
+
 __global__ void __launch_bounds__(kThreads) k_sigmadelta_frames(const uint8_t *__restrict__ frames,
                                                                 uint8_t *__restrict__ bkg,
                                                                 uint8_t *__restrict__ var,
@@ -189,31 +193,30 @@ __global__ void __launch_bounds__(kThreads) k_sigmadelta_frames(const uint8_t *_
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t done = 0;
     if (vec) {
-        const int64_t nv = n >> 4;
-        for (int64_t i = tid; i < nv; i += stride) {
-            uint4 b = ld_stream((const uint4 *)bkg + i), v = ld_stream((const uint4 *)var + i), l;
-            // frames come in groups of 4 loaded before any is used, so each
-            // thread keeps four 16-byte loads in flight across the frame loop
+        const int64_t nw = n >> 2;  // 4 pixels per word
+        for (int64_t i = tid; i < nw; i += stride) {
+            uint32_t b = __ldcs((const unsigned int *)bkg + i), v = __ldcs((const unsigned int *)var + i), l;
             int k = 0;
-            for (; k + 4 <= nf; k += 4) {
-                uint4 f[4];
+            for (; k + kFramePrefetch <= nf; k += kFramePrefetch) {
+                uint32_t f[kFramePrefetch];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) f[j] = ld_stream((const uint4 *)(frames + (int64_t)(k + j) * n) + i);
+                for (int j = 0; j < kFramePrefetch; ++j)
+                    f[j] = __ldcs((const unsigned int *)(frames + (int64_t)(k + j) * n) + i);
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    sd_vec(f[j], b, v, l);
-                    st_stream((uint4 *)(labels + (int64_t)(k + j) * n) + i, l);
+                for (int j = 0; j < kFramePrefetch; ++j) {
+                    sd_word(f[j], b, v, l);
+                    __stcs((unsigned int *)(labels + (int64_t)(k + j) * n) + i, l);
                 }
             }
             for (; k < nf; ++k) {
-                uint4 f = ld_stream((const uint4 *)(frames + (int64_t)k * n) + i);
-                sd_vec(f, b, v, l);
-                st_stream((uint4 *)(labels + (int64_t)k * n) + i, l);
+                uint32_t f = __ldcs((const unsigned int *)(frames + (int64_t)k * n) + i);
+                sd_word(f, b, v, l);
+                __stcs((unsigned int *)(labels + (int64_t)k * n) + i, l);
             }
-            st_stream((uint4 *)bkg + i, b);
-            st_stream((uint4 *)var + i, v);
+            __stcs((unsigned int *)bkg + i, b);
+            __stcs((unsigned int *)var + i, v);
         }
-        done = nv << 4;
+        done = nw << 2;
     }
     for (int64_t i = done + tid; i < n; i += stride) {
         uint8_t b = bkg[i], v = var[i], l;
@@ -240,10 +243,11 @@ nt2g_status launch_sigmadelta_frames(const uint8_t *frames, uint8_t *bkg, uint8_
                                      int64_t n, int nf, cudaStream_t st)
 {
     if (n == 0 || nf == 0) return NT2G_OK;
-    // every frame plane must start 16-byte aligned for the vector path
-    int vec = aligned16(frames) && aligned16(bkg) && aligned16(var) && aligned16(labels) && (n % 16 == 0);
-    k_sigmadelta_frames<<<grid_for(k_sigmadelta_frames, (n + 15) / 16), kThreads, 0, st>>>(frames, bkg, var,
-                                                                                           labels, n, nf, vec);
+    // every frame plane must start 4-byte aligned for the word path
+    auto al4 = [](const void *p) { return ((uintptr_t)p & 3u) == 0; };
+    int vec = al4(frames) && al4(bkg) && al4(var) && al4(labels) && (n % 4 == 0);
+    k_sigmadelta_frames<<<grid_for(k_sigmadelta_frames, (n + 3) / 4), kThreads, 0, st>>>(frames, bkg, var, labels,
+                                                                                         n, nf, vec);
     NT2G_LAUNCH_CHECK("sigmadelta frames launch");
     return NT2G_OK;
 }
