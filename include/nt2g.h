@@ -114,9 +114,28 @@ void nt2g_program_destroy(nt2g_program *p);
 
 /* transform(out, expr, range): evaluate elements [offset, offset+count) of
  * every table slot (TABLE/core/functions/expr/transform.hpp:40-60 range
- * semantics).  force_generic != 0 skips the fused-kernel binding. */
+ * semantics).  Kernel choice:
+ *   force_generic = 0: the bound fused kernel; otherwise the program's
+ *                      run-time compiled kernel; otherwise the interpreter;
+ *   force_generic = 1: the run-time compiled kernel, else the interpreter;
+ *   force_generic = 2: the interpreter.
+ * The compiled kernel and the interpreter give bit-identical results.  The
+ * compiled kernel is built by NVRTC (loaded with dlopen) on first use per
+ * device, precision and program; NT2G_JIT=0 in the environment disables it. */
 nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t offset,
                       int64_t count, int32_t precision, int32_t force_generic, void *stream);
+
+/* The CUDA source of the program's run-time compiled kernel (no GPU needed).
+ * *len receives the size including the terminating NUL; cap = 0 only queries
+ * it.  NT2's planned per-expression CUDA generator:
+ * tools/external_kernel/backend.cpp:32-52 with tools/kernel_gen/kernel_gen.cpp:8-113. */
+nt2g_status nt2g_program_jit_source(const nt2g_program *p, int32_t precision, char *buf, size_t cap,
+                                    size_t *len);
+
+/* Compile and load the program's kernel now (before a stream capture, or to
+ * keep compilation out of a timed region).  NT2G_ERR_UNSUPPORTED, with the
+ * reason in nt2g_last_error(), when NVRTC is unavailable or rejects it. */
+nt2g_status nt2g_program_jit_prepare(const nt2g_program *p, int32_t precision);
 
 /* ------------------------------------------------------------------ */
 /* Fused kernels for the named expressions (also reached through      */

@@ -686,7 +686,34 @@ extern "C" nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, in
         default: break;
         }
     }
+    if (force_generic != 2) {
+        nt2g_status js = launch_jit(p->ops, p->logical, da, count, precision, st);
+        if (js != NT2G_ERR_UNSUPPORTED) return js;
+    }
     return launch_interp(p->dprog, da, count, precision, st);
+}
+
+extern "C" nt2g_status nt2g_program_jit_source(const nt2g_program *p, int32_t precision, char *buf, size_t cap,
+                                               size_t *len)
+{
+    NT2G_CHECK_ARG(p != nullptr, "nt2g_program_jit_source: NULL program");
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_program_jit_source: precision %d",
+                   precision);
+    NT2G_CHECK_ARG(buf != nullptr || cap == 0, "nt2g_program_jit_source: NULL buffer");
+    std::string src = jit_source(p->ops, p->logical, precision);
+    if (len) *len = src.size() + 1;
+    if (cap == 0) return NT2G_OK;
+    NT2G_CHECK_ARG(cap > src.size(), "nt2g_program_jit_source: %zu-byte buffer, %zu needed", cap, src.size() + 1);
+    memcpy(buf, src.c_str(), src.size() + 1);
+    return NT2G_OK;
+}
+
+extern "C" nt2g_status nt2g_program_jit_prepare(const nt2g_program *p, int32_t precision)
+{
+    NT2G_CHECK_ARG(p != nullptr, "nt2g_program_jit_prepare: NULL program");
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2,
+                   "nt2g_program_jit_prepare: precision %d", precision);
+    return jit_prepare(p->ops, p->logical, precision);
 }
 
 // ------------------------------------------------------- direct kernels ----

@@ -462,7 +462,8 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
 #pragma unroll
                 for (int j = 0; j < kV; ++j) {
                     if (f32) d[j] = __float_as_uint(f_unary<P>(in.op, __uint_as_float(A[j])));
-                    else d[j] = in.op == NT2G_OP_NEG ? ((0u - A[j]) & 255u) : A[j];
+                    else d[j] = in.op == NT2G_OP_NEG ? ((0u - A[j]) & 255u)
+                              : in.op == NT2G_OP_SQR ? ((A[j] * A[j]) & 255u) : A[j];  // ABS: identity
                 }
                 break;
             }

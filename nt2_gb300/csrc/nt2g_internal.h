@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string>
+#include <vector>
 #include "nt2g.h"
 
 namespace nt2g {
@@ -74,5 +76,13 @@ nt2g_status launch_sigmadelta_frames(const uint8_t *frames, uint8_t *bkg, uint8_
 nt2g_status launch_map(int fn, const float *x, float *y, int64_t n, int precision, cudaStream_t st);
 nt2g_status launch_interp(const DProgram &prog, const DArgs &args, int64_t count, int precision,
                           cudaStream_t st);
+
+// Run-time compiled kernels of generic programs (nt2g_jit.cu).  The program is
+// the canonical SSA form; logical[k] marks comparison results.
+std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision);
+bool jit_enabled();
+nt2g_status jit_prepare(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision);
+nt2g_status launch_jit(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, const DArgs &args,
+                       int64_t count, int precision, cudaStream_t st);
 
 }  // namespace nt2g

@@ -1,0 +1,322 @@
+// nt2g_jit.cu -- one fused kernel per generic expression, compiled at run time.
+//
+// NT2 planned GPU kernels as code generated per expression: its
+// external_kernel tool collects the expression symbols of a program and a
+// back-end writes a CUDA file that kernel_gen compiles with nvcc
+// (tools/external_kernel/backend.cpp:32-52, tools/kernel_gen/kernel_gen.cpp:8-113;
+// the CUDA back-end itself never shipped).  Here the library does it in
+// process: an expression program that binds none of the hand-written fused
+// kernels is turned into a straight-line CUDA kernel -- one statement per SSA
+// instruction, every value in a register, the same device math header as the
+// rest of the library -- compiled by NVRTC for sm_103a, loaded through the
+// runtime's library API and cached per device, policy and program text.
+//
+// Each statement computes exactly what the interpreter computes for the same
+// instruction, so both give bit-identical results; the JIT kernel just has no
+// dispatch and no register file in memory.  NVRTC is opened with dlopen: when
+// it is not installed the generic path stays on the interpreter.
+#include <dlfcn.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+#include "nt2g_common.cuh"
+#include "nt2g_internal.h"
+#include "nt2g_math_src.h"  // kNt2gMathSrc: nt2g_math.cuh as a string (generated at build)
+
+namespace nt2g {
+
+// ------------------------------------------------------------ nvrtc, dlopen --
+typedef int nvrtcResult_t;
+typedef struct _nvrtcProgram *nvrtcProgram_t;
+struct Nvrtc {
+    void *h = nullptr;
+    nvrtcResult_t (*create)(nvrtcProgram_t *, const char *, const char *, int, const char *const *,
+                            const char *const *) = nullptr;
+    nvrtcResult_t (*compile)(nvrtcProgram_t, int, const char *const *) = nullptr;
+    nvrtcResult_t (*cubin_size)(nvrtcProgram_t, size_t *) = nullptr;
+    nvrtcResult_t (*cubin)(nvrtcProgram_t, char *) = nullptr;
+    nvrtcResult_t (*log_size)(nvrtcProgram_t, size_t *) = nullptr;
+    nvrtcResult_t (*log)(nvrtcProgram_t, char *) = nullptr;
+    nvrtcResult_t (*destroy)(nvrtcProgram_t *) = nullptr;
+    std::string error;
+};
+
+static Nvrtc &nvrtc()
+{
+    static Nvrtc n;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char *env = getenv("NT2G_NVRTC");
+        std::vector<std::string> names;
+        if (env) names.push_back(env);
+        names.push_back("libnvrtc.so.13");
+        names.push_back("libnvrtc.so");
+        const char *home = getenv("CUDA_HOME");
+        names.push_back(std::string(home ? home : "/usr/local/cuda") + "/lib64/libnvrtc.so.13");
+        for (const std::string &nm : names)
+            if ((n.h = dlopen(nm.c_str(), RTLD_NOW | RTLD_LOCAL))) break;
+        if (!n.h) { n.error = "NVRTC not found (libnvrtc.so.13)"; return; }
+        n.create = (decltype(n.create))dlsym(n.h, "nvrtcCreateProgram");
+        n.compile = (decltype(n.compile))dlsym(n.h, "nvrtcCompileProgram");
+        n.cubin_size = (decltype(n.cubin_size))dlsym(n.h, "nvrtcGetCUBINSize");
+        n.cubin = (decltype(n.cubin))dlsym(n.h, "nvrtcGetCUBIN");
+        n.log_size = (decltype(n.log_size))dlsym(n.h, "nvrtcGetProgramLogSize");
+        n.log = (decltype(n.log))dlsym(n.h, "nvrtcGetProgramLog");
+        n.destroy = (decltype(n.destroy))dlsym(n.h, "nvrtcDestroyProgram");
+        if (!(n.create && n.compile && n.cubin_size && n.cubin && n.log_size && n.log && n.destroy)) {
+            n.error = "NVRTC is missing entry points";
+            n.h = nullptr;
+        }
+    });
+    return n;
+}
+
+// ----------------------------------------------------------------- codegen --
+// The kernel processes 4 consecutive elements per thread (one float4 per f32
+// table when every table is aligned, one 32-bit word per uint8 table), so a
+// value is a 4-lane array that the compiler keeps in registers.
+static const char kJitPrelude[] = R"NT2G_SRC(
+struct JitArgs { void *ptr[16]; float scal[16]; unsigned scal_u8[16]; int dtype[16]; };
+#define NT2G_L _Pragma("unroll") for (int j = 0; j < 4; ++j)
+template <bool FULL> __device__ __forceinline__ void jit_ldf(float (&d)[4], const void *p, long long i, int cnt)
+{
+    const float *q = (const float *)p + i;
+    if (FULL) { float4 t = __ldcs((const float4 *)q); d[0] = t.x; d[1] = t.y; d[2] = t.z; d[3] = t.w; }
+    else { NT2G_L d[j] = j < cnt ? q[j] : 0.0f; }
+}
+template <bool FULL> __device__ __forceinline__ void jit_ldb(unsigned (&d)[4], const void *p, long long i, int cnt)
+{
+    const unsigned char *q = (const unsigned char *)p + i;
+    if (FULL) { unsigned w = *(const unsigned *)q; NT2G_L d[j] = (w >> (8 * j)) & 255u; }
+    else { NT2G_L d[j] = j < cnt ? (unsigned)q[j] : 0u; }
+}
+template <bool FULL> __device__ __forceinline__ void jit_stf(void *p, long long i, int cnt, const float (&v)[4])
+{
+    float *q = (float *)p + i;
+    if (FULL) __stcs((float4 *)q, make_float4(v[0], v[1], v[2], v[3]));
+    else { NT2G_L if (j < cnt) q[j] = v[j]; }
+}
+template <bool FULL> __device__ __forceinline__ void jit_stb(void *p, long long i, int cnt, const unsigned (&v)[4])
+{
+    unsigned char *q = (unsigned char *)p + i;
+    if (FULL) *(unsigned *)q = (v[0] & 255u) | (v[1] & 255u) << 8 | (v[2] & 255u) << 16 | (v[3] & 255u) << 24;
+    else { NT2G_L if (j < cnt) q[j] = (unsigned char)v[j]; }
+}
+)NT2G_SRC";
+
+static std::string fconst(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    char b[40];
+    snprintf(b, sizeof b, "__uint_as_float(0x%08xu)", u);
+    return b;
+}
+
+std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision)
+{
+    std::string s;
+    s.reserve(sizeof kJitPrelude + 40000 + ops.size() * 96);
+    s += kNt2gMathSrc;
+    s += kJitPrelude;
+    s += "template <class P, bool FULL>\n__device__ __forceinline__ void jit_tile(const JitArgs &a, long long i, int cnt)\n{\n";
+    auto v = [](int x) { return "v" + std::to_string(x) + "[j]"; };
+    for (size_t k = 0; k < ops.size(); ++k) {
+        const nt2g_op &o = ops[k];
+        const bool f32 = o.dtype == NT2G_F32;
+        const bool u = logical[k] || !f32;  // uint32 lanes: uint8 data and logicals
+        const std::string A = o.a >= 0 ? v(o.a) : "", B = o.b >= 0 ? v(o.b) : "", C = o.c >= 0 ? v(o.c) : "";
+        const std::string slot = std::to_string(o.a);
+        std::string e;
+        switch (o.code) {
+        case NT2G_OP_LOAD:
+            s += (f32 ? "    float v" : "    unsigned v") + std::to_string(k) + "[4]; " +
+                 (f32 ? "jit_ldf<FULL>(v" : "jit_ldb<FULL>(v") + std::to_string(k) + ", a.ptr[" + slot + "], i, cnt);\n";
+            continue;
+        case NT2G_OP_STORE: {
+            const std::string src = "v" + std::to_string(o.a);
+            const std::string dst = std::to_string(o.b);
+            if (f32 && logical[o.a])  // a comparison result stored as 0.0f / 1.0f
+                s += "    { float t[4]; NT2G_L t[j] = (float)" + src + "[j]; jit_stf<FULL>(a.ptr[" + dst + "], i, cnt, t); }\n";
+            else
+                s += std::string(f32 ? "    jit_stf<FULL>(a.ptr[" : "    jit_stb<FULL>(a.ptr[") + dst + "], i, cnt, " +
+                     src + ");\n";
+            continue;
+        }
+        case NT2G_OP_SCALAR: e = f32 ? "a.scal[" + slot + "]" : "a.scal_u8[" + slot + "]"; break;
+        case NT2G_OP_CONST: e = f32 ? fconst(o.imm) : std::to_string((uint32_t)o.imm & 255u) + "u"; break;
+        case NT2G_OP_ADD: e = f32 ? "P::add(" + A + ", " + B + ")" : "(" + A + " + " + B + ") & 255u"; break;
+        case NT2G_OP_SUB: e = f32 ? "P::sub(" + A + ", " + B + ")" : "(" + A + " - " + B + ") & 255u"; break;
+        case NT2G_OP_MUL: e = f32 ? "P::mul(" + A + ", " + B + ")" : "(" + A + " * " + B + ") & 255u"; break;
+        case NT2G_OP_DIV: e = "P::div(" + A + ", " + B + ")"; break;
+        case NT2G_OP_MIN:
+            e = f32 ? "fminf(" + A + ", " + B + ")" : "(" + A + " < " + B + " ? " + A + " : " + B + ")";
+            break;
+        case NT2G_OP_MAX:
+            e = f32 ? "fmaxf(" + A + ", " + B + ")" : "(" + A + " > " + B + " ? " + A + " : " + B + ")";
+            break;
+        case NT2G_OP_ADDS: e = "((" + A + " + " + B + ") > 255u ? 255u : (" + A + " + " + B + "))"; break;
+        case NT2G_OP_FMA: e = "P::fma(" + A + ", " + B + ", " + C + ")"; break;
+        case NT2G_OP_FNMS: e = "P::fma(-" + A + ", " + B + ", " + C + ")"; break;
+        case NT2G_OP_LT: e = "(" + A + " < " + B + ") ? 1u : 0u"; break;
+        case NT2G_OP_GT: e = "(" + A + " > " + B + ") ? 1u : 0u"; break;
+        case NT2G_OP_LE: e = "(" + A + " <= " + B + ") ? 1u : 0u"; break;
+        case NT2G_OP_GE: e = "(" + A + " >= " + B + ") ? 1u : 0u"; break;
+        case NT2G_OP_EQ: e = "(" + A + " == " + B + ") ? 1u : 0u"; break;
+        case NT2G_OP_NE: e = "(" + A + " != " + B + ") ? 1u : 0u"; break;
+        case NT2G_OP_IF_ELSE: e = A + " ? " + B + " : " + C; break;
+        case NT2G_OP_SELINC:
+            e = f32 ? A + " ? P::add(" + B + ", 1.0f) : " + B : A + " ? ((" + B + " + 1u) & 255u) : " + B;
+            break;
+        case NT2G_OP_SELDEC:
+            e = f32 ? A + " ? P::add(" + B + ", -1.0f) : " + B : A + " ? ((" + B + " - 1u) & 255u) : " + B;
+            break;
+        case NT2G_OP_IF_ZERO_ELSE_ONE: e = f32 ? A + " ? 0.0f : 1.0f" : A + " ? 0u : 1u"; break;
+        case NT2G_OP_NEG: e = f32 ? "-" + A : "(0u - " + A + ") & 255u"; break;
+        case NT2G_OP_ABS: e = f32 ? "fabsf(" + A + ")" : A; break;
+        case NT2G_OP_SQR: e = f32 ? "P::mul(" + A + ", " + A + ")" : "(" + A + " * " + A + ") & 255u"; break;
+        case NT2G_OP_SQRT: e = "P::sqrt(" + A + ")"; break;
+        case NT2G_OP_REC: e = "P::div(1.0f, " + A + ")"; break;
+        case NT2G_OP_EXP: e = "nt2g::exp<P>(" + A + ")"; break;
+        case NT2G_OP_LOG: e = "nt2g::log<P>(" + A + ")"; break;
+        case NT2G_OP_LOG1P: e = "nt2g::log1p<P>(" + A + ")"; break;
+        case NT2G_OP_ERFC: e = "nt2g::erfc<P>(" + A + ")"; break;
+        case NT2G_OP_NORMCDF: e = "nt2g::normcdf<P>(" + A + ")"; break;
+        default: e = "nt2g::fastnormcdf<P>(" + A + ")"; break;
+        }
+        s += std::string(u ? "    unsigned v" : "    float v") + std::to_string(k) + "[4]; NT2G_L v" +
+             std::to_string(k) + "[j] = " + e + ";\n";
+    }
+    s += "}\n\nextern \"C\" __global__ void __launch_bounds__(256) nt2g_jit_kernel(const JitArgs a, long long n, int vec)\n{\n";
+    s += precision == NT2G_PREC_NT2 ? "    typedef nt2g::Nt2 P;\n" : "    typedef nt2g::Fast P;\n";
+    s += "    const long long stride = (long long)gridDim.x * blockDim.x * 4;\n"
+         "    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4; i < n; i += stride) {\n"
+         "        const int cnt = n - i < 4 ? (int)(n - i) : 4;\n"
+         "        if (vec && cnt == 4) jit_tile<P, true>(a, i, 4);\n"
+         "        else jit_tile<P, false>(a, i, cnt);\n"
+         "    }\n}\n";
+    return s;
+}
+
+// ------------------------------------------------------------------- cache --
+struct JitEntry {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t kernel = nullptr;
+    int blocks_per_sm = 0;
+    std::string error;
+};
+
+static std::mutex g_mu;
+static std::map<std::string, JitEntry> g_cache;  // key: device | precision | program text
+
+static std::string compile_cubin(const std::string &src, std::string &err)
+{
+    Nvrtc &nv = nvrtc();
+    if (!nv.h) { err = nv.error; return ""; }
+    nvrtcProgram_t prog = nullptr;
+    if (nv.create(&prog, src.c_str(), "nt2g_jit.cu", 0, nullptr, nullptr) != 0) {
+        err = "nvrtcCreateProgram failed";
+        return "";
+    }
+    // no fast-math flags: the statements must round exactly like the interpreter's
+    const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-default-device"};
+    int rc = nv.compile(prog, 3, opts);
+    std::string cubin;
+    if (rc != 0) {
+        size_t n = 0;
+        nv.log_size(prog, &n);
+        std::string log(n, '\0');
+        if (n) nv.log(prog, &log[0]);
+        err = "NVRTC compile failed: " + log.substr(0, 400);
+    } else {
+        size_t n = 0;
+        nv.cubin_size(prog, &n);
+        cubin.assign(n, '\0');
+        nv.cubin(prog, &cubin[0]);
+    }
+    nv.destroy(&prog);
+    return cubin;
+}
+
+// Compiled kernel for (device, precision, program); nullptr with *why set when
+// JIT is unavailable for it.
+static JitEntry *jit_get(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision,
+                         std::string *why)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::string key = std::to_string(dev) + "|" + std::to_string(precision) + "|";
+    key.append((const char *)ops.data(), ops.size() * sizeof(nt2g_op));
+    key.append((const char *)logical.data(), logical.size());
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_cache.find(key);
+    if (it == g_cache.end()) {
+        JitEntry e;
+        std::string src = jit_source(ops, logical, precision);
+        std::string cubin = compile_cubin(src, e.error);
+        if (!cubin.empty()) {
+            cudaError_t ce = cudaLibraryLoadData(&e.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+            if (ce == cudaSuccess) ce = cudaLibraryGetKernel(&e.kernel, e.lib, "nt2g_jit_kernel");
+            if (ce == cudaSuccess)
+                ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e.blocks_per_sm, (const void *)e.kernel, 256, 0);
+            if (ce != cudaSuccess) {
+                e.error = std::string("loading the JIT kernel: ") + cudaGetErrorString(ce);
+                cudaGetLastError();
+                e.kernel = nullptr;
+            }
+        }
+        it = g_cache.emplace(key, e).first;
+    }
+    if (!it->second.kernel) {
+        if (why) *why = it->second.error;
+        return nullptr;
+    }
+    return &it->second;
+}
+
+bool jit_enabled()
+{
+    const char *e = getenv("NT2G_JIT");
+    return !(e && e[0] == '0');
+}
+
+// Compile and load the kernel of a program ahead of its first evaluation
+// (compilation takes a fraction of a second; a stream capture must not be the
+// first use).
+nt2g_status jit_prepare(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision)
+{
+    if (!jit_enabled()) { set_error("JIT disabled (NT2G_JIT=0)"); return NT2G_ERR_UNSUPPORTED; }
+    std::string why;
+    if (!jit_get(ops, logical, precision, &why)) { set_error("%s", why.c_str()); return NT2G_ERR_UNSUPPORTED; }
+    return NT2G_OK;
+}
+
+// Launch the JIT kernel of a generic program.  Returns NT2G_ERR_UNSUPPORTED
+// when no JIT kernel can be had; the caller then interprets.
+nt2g_status launch_jit(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, const DArgs &args,
+                       int64_t count, int precision, cudaStream_t st)
+{
+    static_assert(sizeof(DArgs) == 16 * sizeof(void *) + 3 * 16 * 4, "JitArgs layout");
+    if (!jit_enabled()) return NT2G_ERR_UNSUPPORTED;
+    JitEntry *e = jit_get(ops, logical, precision, nullptr);
+    if (!e) return NT2G_ERR_UNSUPPORTED;
+    if (count == 0) return NT2G_OK;
+    // whole-vector accesses need every float table 16-byte and every uint8 table 4-byte aligned
+    int vec = 1;
+    for (int s = 0; s < kMaxSlots; ++s)
+        if (args.ptr[s]) vec &= ((uintptr_t)args.ptr[s] & (args.dtype[s] == NT2G_F32 ? 15u : 3u)) == 0;
+    int64_t full = (int64_t)device_sm_count() * (e->blocks_per_sm > 0 ? e->blocks_per_sm : 1);
+    int64_t need = (count + 1023) / 1024;  // 256 threads x 4 elements
+    int grid = (int)(need < full ? need : full);
+    long long n = count;
+    void *params[] = {(void *)&args, (void *)&n, (void *)&vec};
+    cudaError_t ce = cudaLaunchKernel((const void *)e->kernel, dim3(grid), dim3(256), params, 0, st);
+    if (ce != cudaSuccess) return cuda_status(ce, "JIT kernel launch");
+    return NT2G_OK;
+}
+
+}  // namespace nt2g

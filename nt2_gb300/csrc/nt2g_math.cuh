@@ -28,9 +28,15 @@
 //   normcdf / fastnormcdf  modules/core/statistics/include/nt2/statistics/
 //           functions/generic/{normcdf.hpp:34, fastnormcdf.hpp:39-54}
 #pragma once
+#if defined(__CUDACC_RTC__)
+// run-time compilation (the JIT path embeds this header): no host headers
+typedef unsigned int uint32_t;
+typedef int int32_t;
+#else
 #include <stdint.h>
 #include <string.h>
 #include <math.h>
+#endif
 
 #if defined(__CUDACC__)
 #define NT2G_HD __host__ __device__ __forceinline__

@@ -182,6 +182,18 @@ class Program:
         lib.check(lib.load().nt2g_program_info_get(self.handle, ctypes.byref(inf)))
         return inf
 
+    def jit_source(self, precision=lib.PREC_FAST):
+        """CUDA source of this program's run-time compiled kernel."""
+        L, n = lib.load(), ctypes.c_size_t()
+        lib.check(L.nt2g_program_jit_source(self.handle, precision, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        lib.check(L.nt2g_program_jit_source(self.handle, precision, buf, n.value, ctypes.byref(n)))
+        return buf.value.decode()
+
+    def jit_prepare(self, precision=lib.PREC_FAST):
+        """Compile and load the run-time compiled kernel now; raises Nt2gError when it is unavailable."""
+        lib.check(lib.load().nt2g_program_jit_prepare(self.handle, precision))
+
     def __del__(self):
         try:
             if self.handle:
@@ -203,7 +215,11 @@ def compile_program(outs, exprs):
 
 
 def assign(outs, exprs, precision=lib.PREC_FAST, offset=0, count=None, force_generic=False, stream=None):
-    """tie(outs...) = tie(exprs...) over elements [offset, offset+count)."""
+    """tie(outs...) = tie(exprs...) over elements [offset, offset+count).
+
+    force_generic: False/0 = bound fused kernel, else the run-time compiled
+    kernel, else the interpreter; True/1 = compiled kernel, else interpreter;
+    2 = interpreter only."""
     import torch
     outs, exprs = list(outs), list(exprs)
     prog, slots = compile_program(outs, exprs)
@@ -218,5 +234,5 @@ def assign(outs, exprs, precision=lib.PREC_FAST, offset=0, count=None, force_gen
     if count is None:
         count = n - offset
     lib.check(lib.load().nt2g_eval(prog.handle, args, len(slots), offset, count, precision,
-                                   1 if force_generic else 0, lib._stream(stream)))
+                                   int(force_generic), lib._stream(stream)))
     return prog

@@ -72,6 +72,8 @@ _SIGNATURES = {
     "nt2g_program_info_get": (_I32, [_VP, ctypes.POINTER(ProgramInfo)]),
     "nt2g_program_destroy": (None, [_VP]),
     "nt2g_eval": (_I32, [_VP, ctypes.POINTER(Arg), _I32, _I64, _I64, _I32, _I32, _VP]),
+    "nt2g_program_jit_source": (_I32, [_VP, _I32, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "nt2g_program_jit_prepare": (_I32, [_VP, _I32]),
     "nt2g_blackscholes_f32": (_I32, [_VP, _VP, _VP, _VP, _F, _F, _VP, _VP, _I64, _I32, _VP]),
     "nt2g_blackscholes_demo_f32": (_I32, [_VP, _VP, _VP, _VP, _F, _VP, _F, _VP, _I64, _I32, _VP]),
     "nt2g_blackscholes_vjp_f32": (_I32, [_VP, _VP, _VP, _VP, _F, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,

@@ -175,3 +175,62 @@ def test_batch_create_validates_items(lib):
     assert L.nt2g_batch_create(items, 1, None, ctypes.byref(h)) == lib.ERR_INVALID
     tune = lib.BatchTune(100, 0, 4, 0)
     assert L.nt2g_batch_create(items, 1, ctypes.byref(tune), ctypes.byref(h)) == lib.ERR_INVALID
+
+
+def _nvrtc():
+    for name in ("libnvrtc.so.13", "/usr/local/cuda/lib64/libnvrtc.so.13"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    pytest.skip("NVRTC not installed")
+
+
+def _nvrtc_compile(nv, src):
+    prog = ctypes.c_void_p()
+    assert nv.nvrtcCreateProgram(ctypes.byref(prog), src.encode(), b"nt2g_jit.cu", 0, None, None) == 0
+    opts = (ctypes.c_char_p * 3)(b"--gpu-architecture=sm_103a", b"-std=c++17", b"-default-device")
+    rc = nv.nvrtcCompileProgram(prog, 3, opts)
+    n = ctypes.c_size_t()
+    nv.nvrtcGetProgramLogSize(prog, ctypes.byref(n))
+    log = ctypes.create_string_buffer(n.value + 1)
+    nv.nvrtcGetProgramLog(prog, log)
+    size = ctypes.c_size_t()
+    if rc == 0:
+        nv.nvrtcGetCUBINSize(prog, ctypes.byref(size))
+    nv.nvrtcDestroyProgram(ctypes.byref(prog))
+    return rc, log.value.decode(errors="replace"), size.value
+
+
+def test_compiled_kernel_source_builds_for_sm103a(lib):
+    """The source the library hands to NVRTC for a generic program compiles
+    for sm_103a under both policies (NVRTC needs no GPU)."""
+    nv = _nvrtc()
+    S, K, T = _cpu_tables()
+    c, p = torch.zeros(8), torch.zeros(8)
+    bs, _ = E.compile_program([c, p], list(bs_textbook(S, K, T, E.Scalar(0.3), E.Scalar(0.02))))
+    u8 = torch.uint8
+    fr, bkg, var = _cpu_tables(16, 3, u8)
+    d = E.max_(bkg, fr) - E.min_(bkg, fr)
+    lab = torch.zeros(16, dtype=u8)
+    mixed, _ = E.compile_program([lab, c], [E.if_zero_else_one(d < var, lib.U8), E.Table(torch.zeros(8)) > 1.0])
+    for prog in (bs, mixed):
+        for prec in (lib.PREC_FAST, lib.PREC_NT2):
+            src = prog.jit_source(prec)
+            assert 'extern "C" __global__' in src and "nt2g_jit_kernel" in src
+            assert ("nt2g::Nt2" if prec == lib.PREC_NT2 else "nt2g::Fast") in src
+            rc, log, size = _nvrtc_compile(nv, src)
+            assert rc == 0, log[:2000]
+            assert size > 0
+
+
+def test_compiled_kernel_source_validates_arguments(lib):
+    x = E.Table(torch.zeros(8))
+    prog, _ = E.compile_program([torch.zeros(8)], [E.exp(x)])
+    L = lib.load()
+    n = ctypes.c_size_t()
+    assert L.nt2g_program_jit_source(prog.handle, 5, None, 0, ctypes.byref(n)) == lib.ERR_INVALID
+    assert L.nt2g_program_jit_source(prog.handle, 0, None, 0, ctypes.byref(n)) == lib.OK and n.value > 100
+    small = ctypes.create_string_buffer(10)
+    assert L.nt2g_program_jit_source(prog.handle, 0, small, 10, ctypes.byref(n)) == lib.ERR_INVALID
+    assert L.nt2g_program_jit_prepare(None, 0) == lib.ERR_INVALID

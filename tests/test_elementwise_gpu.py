@@ -205,6 +205,12 @@ def test_generic_interpreter_uint8_wraparound(lib, dev):
     assert _eq(o2.cpu().numpy(), (a - b).astype(np.uint8))
     sat = np.minimum(a.astype(int) + b, 255).astype(np.uint8)
     assert _eq(o3.cpu().numpy(), np.where(a >= b, sat, (a * b).astype(np.uint8)))
+    # unary uint8 functors wrap the same way (sqr(a) = a*a mod 256), in both generic kernels
+    for mode in (1, 2):
+        E.assign([o1, o2, o3], [E.sqr(A), -A, E.abs_(B)], force_generic=mode)
+        torch.cuda.synchronize()
+        assert _eq(o1.cpu().numpy(), (a * a).astype(np.uint8)), mode
+        assert _eq(o2.cpu().numpy(), (-a.astype(int)).astype(np.uint8)) and _eq(o3.cpu().numpy(), b), mode
 
 
 def test_logical_stored_into_float_table(lib, dev):
