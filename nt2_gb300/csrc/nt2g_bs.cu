@@ -4,16 +4,19 @@
 //
 // One pass over the option tables: 128-bit loads/stores of 4 options per
 // thread per step, grid-stride persistent blocks, every intermediate in
-// registers.  Work per option is ~140 FP32-pipe instructions (Fast) for 20
-// bytes of HBM traffic, so the kernel sits at the FP32-issue / HBM ridge.
+// registers.  The fast policy prices the 4 options as two pairs with packed
+// f32x2 arithmetic (nt2g_pair.cuh): ~115 instructions per option (174 one
+// option at a time) for 20 bytes of HBM traffic, so the kernel sits at the
+// FP32-pipe / HBM ridge.  5 blocks of 256 threads per SM (48 registers).
 #include "nt2g_common.cuh"
 #include "nt2g_exprs.cuh"
+#include "nt2g_pair.cuh"
 #include "nt2g_internal.h"
 
 namespace nt2g {
 
 template <class P, bool SIG_TAB>
-__global__ void __launch_bounds__(256) k_bs(const float *__restrict__ S, const float *__restrict__ K,
+__global__ void __launch_bounds__(256, SIG_TAB ? 4 : 5) k_bs(const float *__restrict__ S, const float *__restrict__ K,
                                             const float *__restrict__ T, const float *__restrict__ sig,
                                             float sig_s, float r, float *__restrict__ call,
                                             float *__restrict__ put, int64_t n, int vec)
@@ -28,13 +31,27 @@ __global__ void __launch_bounds__(256) k_bs(const float *__restrict__ S, const f
                    t = ld_stream((const float4 *)T + i);
             float4 v = SIG_TAB ? ld_stream((const float4 *)sig + i) : make_float4(sig_s, sig_s, sig_s, sig_s);
             float4 c, p;
+            if constexpr (!P::exact) {
+                // two options per packed instruction, bit-identical to bs_option<Fast>
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float cj, pj;
-                const float sj = get(v, j);
-                bs_option<P>(get(s, j), get(k, j), get(t, j), sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
-                set(c, j, cj);
-                set(p, j, pj);
+                for (int h = 0; h < 2; ++h) {
+                    const f2 sv = h ? pk(v.z, v.w) : pk(v.x, v.y);
+                    const f2 iv = SIG_TAB ? inv_fast2(sv, neg2(sv)) : dup(inv_sig_s);
+                    f2 c2, p2;
+                    bs_option_fast2(h ? pk(s.z, s.w) : pk(s.x, s.y), h ? pk(k.z, k.w) : pk(k.x, k.y),
+                                    h ? pk(t.z, t.w) : pk(t.x, t.y), sv, iv, r, c2, p2);
+                    if (h) { upk(c2, c.z, c.w); upk(p2, p.z, p.w); }
+                    else { upk(c2, c.x, c.y); upk(p2, p.x, p.y); }
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    float cj, pj;
+                    const float sj = get(v, j);
+                    bs_option<P>(get(s, j), get(k, j), get(t, j), sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
+                    set(c, j, cj);
+                    set(p, j, pj);
+                }
             }
             st_stream((float4 *)call + i, c);
             st_stream((float4 *)put + i, p);
@@ -108,8 +125,7 @@ __device__ __forceinline__ void bs_vjp_option(float S, float K, float T, float s
     // forward (the fast forward kernel's arithmetic, bit for bit)
     BsFwd f = bs_prefix_fast(S, K, T, sig, inv_fast(sig), r);
     float n1, m1, n2, m2, g1;  // g1 = exp(-d1^2/2)
-    normcdf_pair_pdf(f.d1, n1, m1, g1);
-    normcdf_pair_fast(f.d2, n2, m2);
+    bs_normcdfs_fast(f.d1, f.d2, S, f.e, n1, m1, n2, m2, &g1);
     const float sq = f.sq, ert = f.ert, e = f.e;
     C = Fast::fma(-e, n2, Fast::mul(S, n1));
     P_ = Fast::fma(-S, m1, Fast::mul(e, m2));

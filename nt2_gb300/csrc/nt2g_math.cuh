@@ -299,7 +299,7 @@ NT2G_HD float erfc_tail_poly(float w)
 // exp(-s^2*hi) = (1 + e) * 2^k with e corrected for lo, so the result is
 // 2^k * fma(e, wR, wR): one rounding for the exponential's "+1" and the
 // product together.
-template <bool HALF_SQ> NT2G_HD float erfc_tail_fast(float a, float *expo = nullptr)
+template <bool HALF_SQ> NT2G_HD float erfc_tail_fast(float a)
 {
     const float q = HALF_SQ ? 0.353553390593273762f : 0.5f;  // (1/2)*s
     // w ~ 1/den, den = 1 + q*a held as den + dlo.  The polynomial takes the
@@ -327,8 +327,6 @@ template <bool HALF_SQ> NT2G_HD float erfc_tail_fast(float a, float *expo = null
     // underflow) and the true value is subnormal; the guard also keeps inf*0
     // out of the split for a = inf.
     const float amax = HALF_SQ ? 13.2f : 9.3f;
-    // exp(-s^2 a^2) alone (without the reciprocal residual) for the adjoint
-    if (expo) *expo = (a < amax) ? Fast::mul(Fast::add(Fast::sub(e, Fast::fma(r, e, r)), 1.0f), scale) : 0.0f;
     return (a < amax) ? res : 0.0f;
 }
 
@@ -366,17 +364,6 @@ template <class P> NT2G_HD void normcdf_pair(float x, float &n_pos, float &n_neg
     n_pos = neg ? half_tail : other;
     n_neg = neg ? other : half_tail;
     if (is_nan(x)) { n_pos = x; n_neg = x; }
-}
-
-// Fast pair plus g = exp(-x^2/2) (the normal density times sqrt(2*pi)),
-// for the adjoint kernel.
-NT2G_HD void normcdf_pair_pdf(float x, float &n_pos, float &n_neg, float &g)
-{
-    float half_tail = Fast::mul(0.5f, erfc_tail_fast<true>(fabsf(x), &g));
-    float other = Fast::sub(1.0f, half_tail);
-    bool neg = x < 0.0f;
-    n_pos = neg ? half_tail : other;
-    n_neg = neg ? other : half_tail;
 }
 
 template <class P> NT2G_HD float normcdf(float x)

@@ -72,7 +72,7 @@ def _d12(S, K, T, sig):
     return d1, d1 - v * np.sqrt(t)
 
 
-def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label="", fast_vs_nt2=True):
+def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label="", mean_slack=0.0):
     ec, ep = _fast_errors(oracle, S, K, T, c, p, sig)
     rc, rp = oracle.blackscholes(S, K, T, R, sig)
     nc, np_ = _fast_errors(oracle, S, K, T, rc, rp, sig)
@@ -82,7 +82,7 @@ def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label="", fast_vs_nt2=True):
     print(f"{label} NT2 restatement vs FP64: call max {nc.max():.2f} mean {nc.mean():.3f} p99.9 {q(nc):.2f}; "
           f"put max {np_.max():.2f} mean {np_.mean():.3f} p99.9 {q(np_):.2f}")
     for f, nn in ((ec, nc), (ep, np_)):
-        assert f.mean() <= nn.mean() and q(f) <= q(nn) and f.max() <= nn.max()
+        assert f.mean() <= nn.mean() + mean_slack and q(f) <= q(nn) and f.max() <= nn.max()
     d1, d2 = _d12(S, K, T, np.broadcast_to(sig, S.shape))
     core = (np.abs(d1) <= 2) & (np.abs(d2) <= 2)
     print(f"{label} |d|<=2 ({core.mean():.0%} of options): call max {ec[core].max():.2f} put max {ep[core].max():.2f}")
@@ -106,6 +106,23 @@ def test_fast_policy_sigma_table_and_odd_sizes(lib, dev, oracle):
         assert np.array_equal(c, big[0][:n]) and np.array_equal(p, big[1][:n])
 
 
+def test_fast_policy_extreme_volatility(lib, dev, oracle):
+    """sigma up to 4 (sigma sqrt T up to 12.6): |d1| and |d2| far apart and
+    both tails reached; paired (aligned) and single (odd-size) evaluation
+    agree bit for bit."""
+    rng = np.random.default_rng(1010)
+    n = 1 << 18
+    S, K, T = bs_inputs(n, seed=1010)
+    sig = rng.uniform(1.0, 4.0, n).astype(np.float32)
+    c, p = _run_direct(lib, dev, S, K, T, lib.PREC_FAST, sig)
+    # here NT2's own errors are small too (the tails are not reached through
+    # cancellation): the mean may match NT2's within a hundredth of an ulp
+    _check_fast(oracle, S, K, T, c, p, sig, label="sigma~U[1,4]", mean_slack=0.01)
+    for m in (5, 4097):
+        cs, ps = _run_direct(lib, dev, S[:m], K[:m], T[:m], lib.PREC_FAST, sig[:m])
+        assert np.array_equal(cs, c[:m]) and np.array_equal(ps, p[:m])
+
+
 def test_misaligned_tables_take_the_scalar_path(lib, dev, oracle):
     n = 1001
     S, K, T = bs_inputs(n + 1)
@@ -116,6 +133,16 @@ def test_misaligned_tables_take_the_scalar_path(lib, dev, oracle):
     torch.cuda.synchronize()
     rc, rp = oracle.blackscholes(S[1:], K[1:], T[1:], R, SIGMA)
     assert _bits_equal(c.cpu().numpy()[1:], rc) and _bits_equal(p.cpu().numpy()[1:], rp)
+    # fast policy: the one-option-at-a-time path equals the paired path bit for bit
+    sig = np.random.default_rng(7).uniform(0.05, 4.0, n + 1).astype(np.float32)
+    tsig = _dev(dev, sig)[0]
+    for sigma, sig_s in ((None, SIGMA), (tsig, 0.0)):
+        c.zero_(), p.zero_()
+        lib.blackscholes(tS[1:], tK[1:], tT[1:], c[1:], p[1:], R, sigma=None if sigma is None else sigma[1:],
+                         sigma_s=sig_s, precision=lib.PREC_FAST)
+        ca, pa = _run_direct(lib, dev, S[1:], K[1:], T[1:], lib.PREC_FAST, None if sigma is None else sig[1:])
+        torch.cuda.synchronize()
+        assert _bits_equal(c.cpu().numpy()[1:], ca) and _bits_equal(p.cpu().numpy()[1:], pa)
 
 
 def bs_expr(S, K, T, sig, r):
