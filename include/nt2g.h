@@ -137,6 +137,19 @@ nt2g_status nt2g_program_jit_source(const nt2g_program *p, int32_t precision, ch
  * reason in nt2g_last_error(), when NVRTC is unavailable or rejects it. */
 nt2g_status nt2g_program_jit_prepare(const nt2g_program *p, int32_t precision);
 
+/* Host tables.  Every entry point accepts host pointers for its tables and
+ * workspaces where the current device can reach the memory: pinned or
+ * registered host memory (cudaMallocHost, cudaHostRegister) on any system,
+ * and any host memory, malloc'd included, on systems with pageable memory
+ * access (Grace-Blackwell over NVLink-C2C, or HMM).  The kernels then read
+ * and write the host tables in place over the host link: no staging copy and
+ * no device allocation (NT2's cuda copy path, CUDA/memory/functions/cuda/
+ * copy.hpp:24-100, stages every host table through a device buffer).  A host
+ * pointer the device cannot reach is rejected with NT2G_ERR_INVALID before
+ * any launch.  *pageable receives 1 when the current device has pageable
+ * memory access. */
+nt2g_status nt2g_host_access(int32_t *pageable);
+
 /* ------------------------------------------------------------------ */
 /* Fused kernels for the named expressions (also reached through      */
 /* nt2g_eval).  All tables have n elements.                           */

@@ -163,6 +163,13 @@ extern "C" nt2g_status nt2g_batch_create(const nt2g_batch_item *items, int32_t n
         bool ok = it.expr >= 0 && it.expr <= 2 && it.n >= 0 && it.in[0] && it.out[0] &&
                   (it.expr == NT2G_BATCH_SAXPY || (it.in[1] && it.in[2])) &&
                   (it.expr != NT2G_BATCH_BLACKSCHOLES || it.out[1]);
+        if (ok && it.n > 0)
+            for (int j = 0; j < 3; ++j)
+                if (!reachable(it.in[j]) || (j < 2 && !reachable(it.out[j]))) {
+                    delete b;
+                    set_error("nt2g_batch_create: item %d holds host memory the device cannot access", i);
+                    return NT2G_ERR_INVALID;
+                }
         if (!ok) {
             delete b;
             set_error("nt2g_batch_create: item %d is malformed (expr %d)", i, it.expr);

@@ -57,6 +57,34 @@ int device_sm_count()
     return cache_sms;
 }
 
+// ------------------------------------------------------------ host tables --
+// Tables may live in host memory the device can reach: pinned or registered
+// host memory everywhere, any host memory where the device has pageable
+// memory access (Grace-Blackwell's NVLink-C2C with ATS, or HMM).  The kernels
+// then read and write them in place over the host link.  A host pointer the
+// device cannot reach is rejected before a launch instead of faulting.
+static bool pageable_access()
+{
+    static thread_local int cache_dev = -1, cache_val = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return false; }
+    if (dev != cache_dev) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) { cudaGetLastError(); v = 0; }
+        cache_dev = dev;
+        cache_val = v;
+    }
+    return cache_val != 0;
+}
+
+bool reachable(const void *p)
+{
+    if (!p || pageable_access()) return true;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return a.type != cudaMemoryTypeUnregistered;
+}
+
 // ---------------------------------------------------------------- patterns --
 // P_NEG matches -x: a NEG node over its child, or -- when the child is a
 // scalar role -- a constant or scalar argument holding the negated value
@@ -656,6 +684,9 @@ extern "C" nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, in
         }
     }
     if (count == 0) return NT2G_OK;
+    for (int s = 0; s < p->n_slots; ++s)
+        NT2G_CHECK_ARG(!(p->slot_use[s] & 3) || reachable(da.ptr[s]),
+                       "nt2g_eval: slot %d is host memory the device cannot access (pin or register it)", s);
     int kernel = force_generic ? kGeneric : p->kernel;
     for (const DeferredConst &dc : p->deferred)
         if ((float)args[dc.slot].scalar != dc.value) kernel = kGeneric;
@@ -718,6 +749,10 @@ extern "C" nt2g_status nt2g_program_jit_prepare(const nt2g_program *p, int32_t p
 
 // ------------------------------------------------------- direct kernels ----
 #define NT2G_REQ(ptr) NT2G_CHECK_ARG((ptr) != nullptr || n == 0, "%s: " #ptr " is NULL", __func__)
+// after the other checks, for a non-empty call: every table the kernel touches is reachable
+#define NT2G_REACH(ptr)                                                                                        \
+    NT2G_CHECK_ARG(n == 0 || reachable(ptr), "%s: " #ptr " is host memory the device cannot access (pin or "   \
+                   "register it)", __func__)
 #define NT2G_REQ_N() NT2G_CHECK_ARG(n >= 0, "%s: negative size %lld", __func__, (long long)n)
 #define NT2G_REQ_PREC()                                                                                        \
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "%s: precision %d", __func__,     \
@@ -728,6 +763,7 @@ extern "C" nt2g_status nt2g_blackscholes_f32(const float *S, const float *K, con
                                              int32_t precision, void *stream)
 {
     NT2G_REQ_N(); NT2G_REQ(S); NT2G_REQ(K); NT2G_REQ(T); NT2G_REQ(call); NT2G_REQ(put); NT2G_REQ_PREC();
+    NT2G_REACH(S); NT2G_REACH(K); NT2G_REACH(T); NT2G_REACH(sigma); NT2G_REACH(call); NT2G_REACH(put);
     return launch_bs(S, K, T, sigma, sigma_s, r, call, put, n, precision, (cudaStream_t)stream);
 }
 
@@ -736,6 +772,7 @@ extern "C" nt2g_status nt2g_blackscholes_demo_f32(const float *S, const float *X
                                                   int32_t precision, void *stream)
 {
     NT2G_REQ_N(); NT2G_REQ(S); NT2G_REQ(X); NT2G_REQ(T); NT2G_REQ(R); NT2G_REQ_PREC();
+    NT2G_REACH(S); NT2G_REACH(X); NT2G_REACH(T); NT2G_REACH(r_t); NT2G_REACH(v_t); NT2G_REACH(R);
     return launch_bs_demo(S, X, T, r_t, r, v_t, v, R, n, precision, (cudaStream_t)stream);
 }
 
@@ -746,12 +783,16 @@ extern "C" nt2g_status nt2g_blackscholes_vjp_f32(const float *S, const float *K,
 {
     NT2G_REQ_N(); NT2G_REQ(S); NT2G_REQ(K); NT2G_REQ(T); NT2G_REQ(sigma); NT2G_REQ(gc); NT2G_REQ(gp);
     NT2G_REQ(call); NT2G_REQ(put); NT2G_REQ(dS); NT2G_REQ(dK); NT2G_REQ(dT); NT2G_REQ(dsigma); NT2G_REQ(dr);
+    NT2G_REACH(S); NT2G_REACH(K); NT2G_REACH(T); NT2G_REACH(sigma); NT2G_REACH(gc); NT2G_REACH(gp);
+    NT2G_REACH(call); NT2G_REACH(put); NT2G_REACH(dS); NT2G_REACH(dK); NT2G_REACH(dT); NT2G_REACH(dsigma);
+    NT2G_REACH(dr);
     return launch_bs_vjp(S, K, T, sigma, r, gc, gp, call, put, dS, dK, dT, dsigma, dr, n, (cudaStream_t)stream);
 }
 
 extern "C" nt2g_status nt2g_saxpy_f32(float alpha, const float *X, float *Y, int64_t n, void *stream)
 {
     NT2G_REQ_N(); NT2G_REQ(X); NT2G_REQ(Y);
+    NT2G_REACH(X); NT2G_REACH(Y);
     return launch_saxpy(alpha, X, Y, Y, n, (cudaStream_t)stream);
 }
 
@@ -759,6 +800,7 @@ extern "C" nt2g_status nt2g_expr3_f32(const float *x, const float *y, const floa
                                       int32_t precision, void *stream)
 {
     NT2G_REQ_N(); NT2G_REQ(x); NT2G_REQ(y); NT2G_REQ(z); NT2G_REQ(out); NT2G_REQ_PREC();
+    NT2G_REACH(x); NT2G_REACH(y); NT2G_REACH(z); NT2G_REACH(out);
     return launch_expr3(x, y, z, out, n, precision, (cudaStream_t)stream);
 }
 
@@ -766,6 +808,7 @@ extern "C" nt2g_status nt2g_rgb2yuv_f32(const float *r, const float *g, const fl
                                         int64_t n, int32_t precision, void *stream)
 {
     NT2G_REQ_N(); NT2G_REQ(r); NT2G_REQ(g); NT2G_REQ(b); NT2G_REQ(y); NT2G_REQ(u); NT2G_REQ(v); NT2G_REQ_PREC();
+    NT2G_REACH(r); NT2G_REACH(g); NT2G_REACH(b); NT2G_REACH(y); NT2G_REACH(u); NT2G_REACH(v);
     return launch_rgb2yuv(r, g, b, y, u, v, n, precision, (cudaStream_t)stream);
 }
 
@@ -773,6 +816,7 @@ extern "C" nt2g_status nt2g_sigmadelta_u8(const uint8_t *frame, uint8_t *bkg, ui
                                           void *stream)
 {
     NT2G_REQ_N(); NT2G_REQ(frame); NT2G_REQ(bkg); NT2G_REQ(var); NT2G_REQ(label);
+    NT2G_REACH(frame); NT2G_REACH(bkg); NT2G_REACH(var); NT2G_REACH(label);
     return launch_sigmadelta(frame, bkg, var, label, n, (cudaStream_t)stream);
 }
 
@@ -780,6 +824,7 @@ extern "C" nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t 
                                                  int64_t n, int32_t n_frames, void *stream)
 {
     NT2G_REQ_N(); NT2G_REQ(frames); NT2G_REQ(bkg); NT2G_REQ(var); NT2G_REQ(labels);
+    NT2G_REACH(frames); NT2G_REACH(bkg); NT2G_REACH(var); NT2G_REACH(labels);
     NT2G_CHECK_ARG(n_frames >= 0, "nt2g_sigmadelta_frames_u8: negative frame count %d", n_frames);
     return launch_sigmadelta_frames(frames, bkg, var, labels, n, n_frames, (cudaStream_t)stream);
 }
@@ -787,6 +832,7 @@ extern "C" nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t 
 extern "C" nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision, void *stream)
 {
     NT2G_REQ_N(); NT2G_REQ(x); NT2G_REQ(y); NT2G_REQ_PREC();
+    NT2G_REACH(x); NT2G_REACH(y);
     NT2G_CHECK_ARG(fn >= 0 && fn <= 7, "nt2g_map_f32: unknown function %d", fn);
     return launch_map(fn, x, y, n, precision, (cudaStream_t)stream);
 }
@@ -808,6 +854,7 @@ extern "C" nt2g_status nt2g_reduce_f32(const float *x, const float *y, int64_t n
     NT2G_CHECK_ARG(workspace != nullptr && workspace_bytes >= need,
                    "nt2g_reduce_f32: workspace of %zu bytes, %zu needed", workspace_bytes, need);
     NT2G_CHECK_ARG(((uintptr_t)workspace & 15u) == 0, "nt2g_reduce_f32: workspace not 16-byte aligned");
+    NT2G_REACH(x); NT2G_REACH(y); NT2G_REACH(workspace); NT2G_REACH(out64); NT2G_REACH(out32);
     return launch_reduce(x, y, n, workspace, out64, out32, (cudaStream_t)stream);
 }
 
@@ -816,7 +863,18 @@ extern "C" nt2g_status nt2g_reduce_f32_noalloc(const float *x, const float *y, i
 {
     NT2G_REQ_N(); NT2G_REQ(x);
     NT2G_CHECK_ARG(out64 != nullptr, "nt2g_reduce_f32_noalloc: out64 is NULL");
+    NT2G_REACH(x); NT2G_REACH(y); NT2G_REACH(out64); NT2G_REACH(out32);
     return launch_reduce_noalloc(x, y, n, out64, out32, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_host_access(int32_t *pageable)
+{
+    NT2G_CHECK_ARG(pageable != nullptr, "nt2g_host_access: pageable is NULL");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "nt2g_host_access");
+    *pageable = pageable_access() ? 1 : 0;
+    return NT2G_OK;
 }
 
 // ------------------------------------------------------------- memory ----

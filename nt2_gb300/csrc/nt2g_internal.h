@@ -51,6 +51,11 @@ enum FusedKernel {
     kSigmaDelta = 6,         // slots: frame bkg var | bkg var label
 };
 
+// True when the current device can read and write the memory at p in place
+// (device memory, pinned/registered host memory, or any host memory where the
+// device has pageable memory access).  NULL counts as reachable.
+bool reachable(const void *p);
+
 // -------------------------------------------------------------- launchers --
 nt2g_status launch_bs(const float *S, const float *K, const float *T, const float *sig, float sig_s, float r,
                       float *call, float *put, int64_t n, int precision, cudaStream_t st);

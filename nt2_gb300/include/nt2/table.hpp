@@ -361,6 +361,24 @@ inline std::string bound_kernel(const std::vector<node_ptr> &outs, const std::ve
     return info.kernel_name;
 }
 
+// Whether host tables are evaluated in place (the device reads and writes
+// pageable host memory directly), asked once per process.
+inline bool host_in_place()
+{
+    static const bool v = [] {
+        int32_t p = 0;
+        return nt2g_host_access(&p) == NT2G_OK && p != 0;
+    }();
+    return v;
+}
+
+template <class V> inline bool has_host_leaf(const V &slots)
+{
+    for (const node *l : slots)
+        if (!l->dev_ptr) return true;
+    return false;
+}
+
 // Evaluate tie(outs) = tie(exprs) over [offset, offset + count).
 inline void evaluate(const std::vector<node_ptr> &outs, const std::vector<node_ptr> &exprs,
                      const std::vector<int> &out_dtypes, std::size_t offset, std::size_t count)
@@ -369,8 +387,10 @@ inline void evaluate(const std::vector<node_ptr> &outs, const std::vector<node_p
     for (std::size_t k = 0; k < outs.size(); ++k) lw.store(lw.emit(exprs[k].get()), outs[k].get(), out_dtypes[k]);
     lw.finish();
     nt2g_program *prog = program_for(lw.L);
-    // arguments: device tables directly, host tables staged through device
-    // buffers (inputs up, outputs down)
+    // arguments: device tables directly; host tables in place when the device
+    // reaches host memory (pageable memory access), else staged through
+    // device buffers (inputs up, outputs down)
+    const bool in_place = host_in_place();
     const auto &slots = lw.L.slot_leaf;
     std::vector<nt2g_arg> args(slots.size());
     std::vector<device_buffer> staging;
@@ -386,6 +406,8 @@ inline void evaluate(const std::vector<node_ptr> &outs, const std::vector<node_p
         a.scalar = 0.0;
         if (l->dev_ptr) {
             a.ptr = l->dev_ptr;
+        } else if (in_place) {
+            a.ptr = (void *)l->host_ptr;
         } else {
             const std::size_t esz = l->dtype == NT2G_U8 ? 1 : 4;
             staging.emplace_back(l->numel * esz);
@@ -399,13 +421,15 @@ inline void evaluate(const std::vector<node_ptr> &outs, const std::vector<node_p
     bool staged_out = false;
     for (std::size_t s = 0; s < slots.size(); ++s) {
         const node *l = slots[s];
-        if (!l->dev_ptr && is_out[s]) {
+        if (!l->dev_ptr && is_out[s] && !in_place) {
             const std::size_t esz = l->dtype == NT2G_U8 ? 1 : 4;
             check(nt2g_memcpy((void *)l->host_ptr, args[s].ptr, l->numel * esz, 2, st), "unstage host table");
             staged_out = true;
         }
     }
-    if (staged_out || !staging.empty()) check(nt2g_stream_synchronize(st), "synchronize");
+    // host tables are the caller's to read as soon as the assignment returns
+    if (staged_out || !staging.empty() || (in_place && has_host_leaf(slots)))
+        check(nt2g_stream_synchronize(st), "synchronize");
 }
 
 }  // namespace detail
@@ -646,6 +670,7 @@ inline void view_of(const node *l, dev_view &v)
 {
     v.n = l->numel;
     if (l->dev_ptr) { v.p = (const float *)l->dev_ptr; return; }
+    if (host_in_place()) { v.p = (const float *)l->host_ptr; return; }
     v.hold = device_buffer(l->numel * sizeof(float));
     check(nt2g_memcpy(v.hold.p, l->host_ptr, l->numel * sizeof(float), 1, options().stream), "stage host table");
     v.p = (const float *)v.hold.p;

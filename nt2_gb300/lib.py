@@ -95,6 +95,7 @@ _SIGNATURES = {
     "nt2g_batch_autotune": (_I32, [ctypes.POINTER(BatchItem), _I32, ctypes.POINTER(BatchTune), _I32, _I32, _I32, _VP,
                                     ctypes.POINTER(BatchTune), ctypes.POINTER(ctypes.c_float)]),
     "nt2g_batch_stats": (_I32, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
+    "nt2g_host_access": (_I32, [ctypes.POINTER(_I32)]),
     "nt2g_device_alloc": (_I32, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "nt2g_device_free": (_I32, [_VP]),
     "nt2g_memcpy": (_I32, [_VP, _VP, ctypes.c_size_t, _I32, _VP]),
