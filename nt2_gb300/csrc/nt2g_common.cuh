@@ -27,6 +27,31 @@ __device__ __forceinline__ void set(float4 &v, int i, float x)
 
 inline bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
+// Programmatic dependent launch (sm_90+): a kernel launched with
+// launch_dependent() may start while the previous kernel in its stream is
+// still running; pdl_wait() returns once that kernel has completed and its
+// memory is visible (immediately when there is no such dependency).  A kernel
+// reads only inputs no earlier kernel writes before pdl_wait(), and writes
+// nothing before it.  pdl_trigger() lets the next dependent launch begin.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Persistent grid: resident blocks per SM (from the occupancy calculator)
 // times the SM count, capped by the work available.
 struct Geometry {

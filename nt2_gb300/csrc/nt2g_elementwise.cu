@@ -1,6 +1,8 @@
 // nt2g_elementwise.cu -- fused elementwise kernels other than Black-Scholes
 // (saxpy, expr3, rgb2yuv, sigma-delta), element maps, and the generic
 // program interpreter that evaluates any lowered nt2 expression in one pass.
+#include <cuda_fp16.h>
+#include <string.h>
 #include "nt2g_common.cuh"
 #include "nt2g_exprs.cuh"
 #include "nt2g_internal.h"
@@ -140,6 +142,69 @@ nt2g_status launch_rgb2yuv(const float *r, const float *g, const float *b, float
 }
 
 // ------------------------------------------------------------ sigma-delta --
+// The vector paths evaluate the uint8 step in packed fp16 (half2): every value
+// involved is an integer in [0, 1279], exact in fp16, and compare (1.0/0.0
+// results), min, add and fma are single two-lane instructions where the byte
+// SIMD intrinsics are multi-instruction sequences.  Pixels carry a +1024
+// offset: the fp16 pattern 0x64pp is 1024 + pp, so a byte permute against
+// 0x64 bytes unpacks four pixels into two half2 and another packs them back.
+// Differences cancel the offset; m and the label compare add it back.
+__device__ __forceinline__ __half2 h2_bits(uint32_t u)
+{
+    __half2 h;
+    memcpy(&h, &u, 4);
+    return h;
+}
+__device__ __forceinline__ uint32_t bits_h2(__half2 h)
+{
+    uint32_t u;
+    memcpy(&u, &h, 4);
+    return u;
+}
+// four pixels (bytes) -> (p0, p1) and (p2, p3), each as 1024 + p
+__device__ __forceinline__ void sd_unpack(uint32_t w, __half2 &lo, __half2 &hi)
+{
+    lo = h2_bits(__byte_perm(w, 0x64646464u, 0x5140));
+    hi = h2_bits(__byte_perm(w, 0x64646464u, 0x5342));
+}
+// inverse of sd_unpack (values 1024 + p, p in [0, 255])
+__device__ __forceinline__ uint32_t sd_pack(__half2 lo, __half2 hi)
+{
+    return __byte_perm(bits_h2(lo), bits_h2(hi), 0x6420);
+}
+
+// One sigma-delta step on two pixels (demo/sigmadelta/nt2/sigmadelta_nt2.cpp:38-57),
+// operands offset by 1024; lab receives 1024 + label.
+__device__ __forceinline__ void sd_h2(__half2 f, __half2 &b, __half2 &v, __half2 &lab)
+{
+    const __half2 k1024 = __float2half2_rn(1024.0f), k1279 = __float2half2_rn(1279.0f);
+    const __half2 k3 = __float2half2_rn(3.0f), k0 = __float2half2_rn(0.0f);
+    b = __hadd2(b, __hsub2(__hlt2(b, f), __hgt2(b, f)));       // selinc/seldec toward the frame
+    const __half2 d = __habs2(__hsub2(b, f));                  // max - min
+    const __half2 m = __hmin2(__hfma2(d, k3, k1024), k1279);   // 1024 + adds(adds(d,d),d)
+    const __half2 step = __hsub2(__hlt2(v, m), __hgt2(v, m));  // var toward m ...
+    v = __hfma2(step, __hne2(d, k0), v);                       // ... where d != 0
+    lab = __hadd2(__hle2(v, __hadd2(d, k1024)), k1024);        // if_zero_else_one(d < var)
+}
+
+// 16 pixels
+__device__ __forceinline__ void sd_vec_h(const uint4 &f, uint4 &b, uint4 &v, uint4 &l)
+{
+    uint32_t *fb = (uint32_t *)&f, *bb = (uint32_t *)&b, *vb = (uint32_t *)&v, *lb = (uint32_t *)&l;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        __half2 f0, f1, b0, b1, v0, v1, l0, l1;
+        sd_unpack(fb[w], f0, f1);
+        sd_unpack(bb[w], b0, b1);
+        sd_unpack(vb[w], v0, v1);
+        sd_h2(f0, b0, v0, l0);
+        sd_h2(f1, b1, v1, l1);
+        bb[w] = sd_pack(b0, b1);
+        vb[w] = sd_pack(v0, v1);
+        lb[w] = sd_pack(l0, l1);
+    }
+}
+
 __device__ __forceinline__ void sd_px(uint8_t f, uint8_t &b, uint8_t &v, uint8_t &lab)
 {
     uint32_t bb = b, vv = v, l;
@@ -155,35 +220,45 @@ __device__ __forceinline__ void sd_vec(const uint4 &f, uint4 &b, uint4 &v, uint4
     sd_word(f.w, b.w, v.w, l.w);
 }
 
-__global__ void __launch_bounds__(kThreads) k_sigmadelta(const uint8_t *__restrict__ fr, uint8_t *__restrict__ bkg,
+// One frame step.  Consecutive steps are chained with programmatic dependent
+// launch: a step's grid starts while the previous step runs, loads its frame
+// (which no earlier step writes), and waits for the previous step only before
+// it reads bkg/var.  One 16-pixel vector per thread, one wave.
+__global__ void __launch_bounds__(kThreads, 4) k_sigmadelta(const uint8_t *__restrict__ fr, uint8_t *__restrict__ bkg,
                                                          uint8_t *__restrict__ var, uint8_t *__restrict__ lab,
                                                          int64_t n, int vec)
 {
+    pdl_trigger();
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t done = 0;
     if (vec) {
         const int64_t nv = n >> 4;  // 16 pixels per uint4
+        uint4 f0 = make_uint4(0, 0, 0, 0);
+        if (tid < nv) f0 = ld_stream((const uint4 *)fr + tid);
+        pdl_wait();
         for (int64_t i = tid; i < nv; i += stride) {
-            uint4 f = ld_stream((const uint4 *)fr + i), b = ld_stream((const uint4 *)bkg + i),
+            uint4 f = i == tid ? f0 : ld_stream((const uint4 *)fr + i), b = ld_stream((const uint4 *)bkg + i),
                   v = ld_stream((const uint4 *)var + i), l;
-            sd_vec(f, b, v, l);
+            sd_vec_h(f, b, v, l);
             st_stream((uint4 *)bkg + i, b);
             st_stream((uint4 *)var + i, v);
             st_stream((uint4 *)lab + i, l);
         }
         done = nv << 4;
+    } else {
+        pdl_wait();
     }
     for (int64_t i = done + tid; i < n; i += stride) sd_px(fr[i], bkg[i], var[i], lab[i]);
 }
 
-// Temporal fusion: a thread keeps 4 pixels' bkg/var (one 32-bit word each)
-// in registers across all frames, so the 2-Mpixel frame still spreads over
-// ~0.5 M threads; eight frames' loads are issued before any is used.  Per
-// pixel-frame HBM traffic drops from 6 B to 2 + 4/F B.
+// Temporal fusion: a thread keeps 16 pixels' bkg/var (one uint4 each) in
+// registers across all frames; eight frames' loads are issued before any is
+// used.  Per pixel-frame HBM traffic drops from 6 B to 2 + 4/F B.  Planes
+// that are not 16-byte aligned take a 4-pixel word path, then single pixels.
 constexpr int kFramePrefetch = 8;
 
-__global__ void __launch_bounds__(kThreads) k_sigmadelta_frames(const uint8_t *__restrict__ frames,
+__global__ void __launch_bounds__(kThreads, 4) k_sigmadelta_frames(const uint8_t *__restrict__ frames,
                                                                 uint8_t *__restrict__ bkg,
                                                                 uint8_t *__restrict__ var,
                                                                 uint8_t *__restrict__ labels, int64_t n,
@@ -192,7 +267,48 @@ __global__ void __launch_bounds__(kThreads) k_sigmadelta_frames(const uint8_t *_
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int64_t done = 0;
-    if (vec) {
+    if (vec == 2) {
+        const int64_t nq = n >> 4;  // 16 pixels per uint4
+        for (int64_t i = tid; i < nq; i += stride) {
+            // bkg/var of 16 pixels as 8 + 8 offset half2, unpacked once
+            uint4 bw = ld_stream((const uint4 *)bkg + i), vw = ld_stream((const uint4 *)var + i);
+            __half2 b[8], v[8];
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+                sd_unpack(((const uint32_t *)&bw)[w], b[2 * w], b[2 * w + 1]);
+                sd_unpack(((const uint32_t *)&vw)[w], v[2 * w], v[2 * w + 1]);
+            }
+            auto frame_step = [&](const uint4 &f, int64_t k) {
+                uint4 l;
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    __half2 f0, f1, l0, l1;
+                    sd_unpack(((const uint32_t *)&f)[w], f0, f1);
+                    sd_h2(f0, b[2 * w], v[2 * w], l0);
+                    sd_h2(f1, b[2 * w + 1], v[2 * w + 1], l1);
+                    ((uint32_t *)&l)[w] = sd_pack(l0, l1);
+                }
+                st_stream((uint4 *)(labels + k * n) + i, l);
+            };
+            int k = 0;
+            for (; k + kFramePrefetch <= nf; k += kFramePrefetch) {
+                uint4 f[kFramePrefetch];
+#pragma unroll
+                for (int j = 0; j < kFramePrefetch; ++j) f[j] = ld_stream((const uint4 *)(frames + (int64_t)(k + j) * n) + i);
+#pragma unroll
+                for (int j = 0; j < kFramePrefetch; ++j) frame_step(f[j], k + j);
+            }
+            for (; k < nf; ++k) frame_step(ld_stream((const uint4 *)(frames + (int64_t)k * n) + i), k);
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+                ((uint32_t *)&bw)[w] = sd_pack(b[2 * w], b[2 * w + 1]);
+                ((uint32_t *)&vw)[w] = sd_pack(v[2 * w], v[2 * w + 1]);
+            }
+            st_stream((uint4 *)bkg + i, bw);
+            st_stream((uint4 *)var + i, vw);
+        }
+        done = nq << 4;
+    } else if (vec == 1) {
         const int64_t nw = n >> 2;  // 4 pixels per word
         for (int64_t i = tid; i < nw; i += stride) {
             uint32_t b = __ldcs((const unsigned int *)bkg + i), v = __ldcs((const unsigned int *)var + i), l;
@@ -234,8 +350,9 @@ nt2g_status launch_sigmadelta(const uint8_t *frame, uint8_t *bkg, uint8_t *var, 
 {
     if (n == 0) return NT2G_OK;
     int vec = aligned16(frame) && aligned16(bkg) && aligned16(var) && aligned16(label);
-    k_sigmadelta<<<grid_for(k_sigmadelta, (n + 15) / 16), kThreads, 0, st>>>(frame, bkg, var, label, n, vec);
-    NT2G_LAUNCH_CHECK("sigmadelta launch");
+    const int grid = persistent_blocks(k_sigmadelta, kThreads, 0, kThreads, (n + 15) / 16);
+    cudaError_t e = launch_dependent(k_sigmadelta, grid, kThreads, st, frame, bkg, var, label, n, vec);
+    if (e != cudaSuccess) return cuda_status(e, "sigmadelta launch");
     return NT2G_OK;
 }
 
@@ -243,11 +360,14 @@ nt2g_status launch_sigmadelta_frames(const uint8_t *frames, uint8_t *bkg, uint8_
                                      int64_t n, int nf, cudaStream_t st)
 {
     if (n == 0 || nf == 0) return NT2G_OK;
-    // every frame plane must start 4-byte aligned for the word path
-    auto al4 = [](const void *p) { return ((uintptr_t)p & 3u) == 0; };
-    int vec = al4(frames) && al4(bkg) && al4(var) && al4(labels) && (n % 4 == 0);
-    k_sigmadelta_frames<<<grid_for(k_sigmadelta_frames, (n + 3) / 4), kThreads, 0, st>>>(frames, bkg, var, labels,
-                                                                                         n, nf, vec);
+    // every frame plane must start 16-byte (4-byte) aligned for the vector (word) path
+    auto al = [](const void *p, unsigned m) { return ((uintptr_t)p & m) == 0; };
+    int vec = 0;
+    if (al(frames, 15) && al(bkg, 15) && al(var, 15) && al(labels, 15) && n % 16 == 0) vec = 2;
+    else if (al(frames, 3) && al(bkg, 3) && al(var, 3) && al(labels, 3) && n % 4 == 0) vec = 1;
+    const int64_t units = vec == 2 ? n / 16 : vec == 1 ? n / 4 : n;
+    const int grid = persistent_blocks(k_sigmadelta_frames, kThreads, 0, kThreads, units);
+    k_sigmadelta_frames<<<grid, kThreads, 0, st>>>(frames, bkg, var, labels, n, nf, vec);
     NT2G_LAUNCH_CHECK("sigmadelta frames launch");
     return NT2G_OK;
 }

@@ -162,6 +162,32 @@ def test_sigmadelta_temporal_fusion(lib, dev, oracle):
     assert _eq(tb.cpu().numpy(), rb) and _eq(tv.cpu().numpy(), rv)
 
 
+def test_sigmadelta_exhaustive_byte_triples(lib, dev, oracle):
+    """Every (frame, bkg, var) byte triple, 2^24 pixels: the per-frame kernel
+    (16-pixel vectors), the fused kernel on one frame (16-pixel and 4-pixel
+    paths) and the single-pixel path all equal the CPU restatement."""
+    i = np.arange(1 << 24, dtype=np.uint32)
+    f, b, v = (i & 255).astype(np.uint8), ((i >> 8) & 255).astype(np.uint8), (i >> 16).astype(np.uint8)
+    rb, rv, rl = oracle.sigmadelta(f, b, v)
+    tf = _t(dev, f)
+    # per-frame kernel
+    tb, tv, tl = _t(dev, b), _t(dev, v), torch.empty_like(tf)
+    lib.sigmadelta(tf, tb, tv, tl)
+    torch.cuda.synchronize()
+    assert _eq(tb.cpu().numpy(), rb) and _eq(tv.cpu().numpy(), rv) and _eq(tl.cpu().numpy(), rl)
+    # fused kernel, one frame: planes 16-byte aligned, then 4-byte (offset 4), then unaligned (offset 1)
+    for off, m in ((0, 1 << 24), (4, (1 << 24) - 16), (1, (1 << 20) - 1)):
+        tf2 = torch.zeros(m + 16, dtype=torch.uint8, device=dev)
+        tb2, tv2, tl2 = torch.zeros_like(tf2), torch.zeros_like(tf2), torch.zeros_like(tf2)
+        tf2[off:off + m] = tf[:m]
+        tb2[off:off + m] = _t(dev, b[:m])
+        tv2[off:off + m] = _t(dev, v[:m])
+        lib.sigmadelta_frames(tf2[off:off + m].view(1, m), tb2[off:off + m], tv2[off:off + m], tl2[off:off + m].view(1, m))
+        torch.cuda.synchronize()
+        assert _eq(tb2[off:off + m].cpu().numpy(), rb[:m]) and _eq(tv2[off:off + m].cpu().numpy(), rv[:m]), off
+        assert _eq(tl2[off:off + m].cpu().numpy(), rl[:m]), off
+
+
 @pytest.mark.parametrize("n", [1, 15, 17, 100003])
 def test_sigmadelta_odd_sizes(lib, dev, oracle, n):
     rng = np.random.default_rng(n)
