@@ -13,6 +13,7 @@
 #include "nt2g_common.cuh"
 #include "nt2g_exprs.cuh"
 #include "nt2g_internal.h"
+#include "nt2g_pair.cuh"
 
 namespace nt2g {
 
@@ -37,11 +38,16 @@ __device__ __forceinline__ void run_tile(const DItem &it, int64_t start, int64_t
         for (int64_t i = v0 + threadIdx.x; i < v1; i += blockDim.x) {
             float4 s = ld_stream((const float4 *)it.in[0] + i), k = ld_stream((const float4 *)it.in[1] + i),
                    t = ld_stream((const float4 *)it.in[2] + i), c, p;
+            if constexpr (!P::exact) {  // two options per packed instruction, as the plain kernel
+                bs_vec4_fast(s, k, t, make_float4(sig, sig, sig, sig), make_float4(inv_sig, inv_sig, inv_sig, inv_sig),
+                             r, c, p);
+            } else {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                float cj, pj;
-                bs_option<P>(get(s, j), get(k, j), get(t, j), sig, inv_sig, r, cj, pj);
-                set(c, j, cj); set(p, j, pj);
+                for (int j = 0; j < 4; ++j) {
+                    float cj, pj;
+                    bs_option<P>(get(s, j), get(k, j), get(t, j), sig, inv_sig, r, cj, pj);
+                    set(c, j, cj); set(p, j, pj);
+                }
             }
             st_stream((float4 *)it.out[0] + i, c);
             st_stream((float4 *)it.out[1] + i, p);

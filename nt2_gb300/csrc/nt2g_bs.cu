@@ -33,16 +33,13 @@ __global__ void __launch_bounds__(256, SIG_TAB ? 4 : 5) k_bs(const float *__rest
             float4 c, p;
             if constexpr (!P::exact) {
                 // two options per packed instruction, bit-identical to bs_option<Fast>
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const f2 sv = h ? pk(v.z, v.w) : pk(v.x, v.y);
-                    const f2 iv = SIG_TAB ? inv_fast2(sv, neg2(sv)) : dup(inv_sig_s);
-                    f2 c2, p2;
-                    bs_option_fast2(h ? pk(s.z, s.w) : pk(s.x, s.y), h ? pk(k.z, k.w) : pk(k.x, k.y),
-                                    h ? pk(t.z, t.w) : pk(t.x, t.y), sv, iv, r, c2, p2);
-                    if (h) { upk(c2, c.z, c.w); upk(p2, p.z, p.w); }
-                    else { upk(c2, c.x, c.y); upk(p2, p.x, p.y); }
+                float4 iv = make_float4(inv_sig_s, inv_sig_s, inv_sig_s, inv_sig_s);
+                if (SIG_TAB) {
+                    f2 a = inv_fast2(pk(v.x, v.y), neg2(pk(v.x, v.y))), b = inv_fast2(pk(v.z, v.w), neg2(pk(v.z, v.w)));
+                    upk(a, iv.x, iv.y);
+                    upk(b, iv.z, iv.w);
                 }
+                bs_vec4_fast(s, k, t, v, iv, r, c, p);
             } else {
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {

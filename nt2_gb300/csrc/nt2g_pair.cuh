@@ -270,4 +270,18 @@ __device__ __forceinline__ void bs_option_fast2(f2 S, f2 K, f2 T, f2 sig, f2 inv
     put = pk(p0, p1);
 }
 
+// Four options (one float4 of each table) as two pairs, sigma and 1/sigma
+// given per option (v, iv).  Bit-identical to bs_option<Fast> per option.
+__device__ __forceinline__ void bs_vec4_fast(const float4 &s, const float4 &k, const float4 &t, const float4 &v,
+                                             const float4 &iv, float r, float4 &c, float4 &p)
+{
+    f2 c2, p2;
+    bs_option_fast2(pk(s.x, s.y), pk(k.x, k.y), pk(t.x, t.y), pk(v.x, v.y), pk(iv.x, iv.y), r, c2, p2);
+    upk(c2, c.x, c.y);
+    upk(p2, p.x, p.y);
+    bs_option_fast2(pk(s.z, s.w), pk(k.z, k.w), pk(t.z, t.w), pk(v.z, v.w), pk(iv.z, iv.w), r, c2, p2);
+    upk(c2, c.z, c.w);
+    upk(p2, p.z, p.w);
+}
+
 }  // namespace nt2g
