@@ -148,8 +148,11 @@ class BlackScholes(Workload):
     SETS = 32
     independent = True
 
-    def __init__(self, torch, lib, dev, precision):
+    def __init__(self, torch, lib, dev, precision, n=None):
         self.torch, self.lib, self.prec = torch, lib, precision
+        if n:  # options per launch other than the standard 2^20; enough sets to exceed 640 MiB
+            self.N = int(n)
+            self.SETS = max(2, -(-(640 << 20) // (20 * self.N)))
         self.name = f"blackscholes_plain N={self.N} call+put, {self.SETS} rotating sets"
         self.units, self.bytes, self.kernel = self.N, 20 * self.N, "k_bs"
         self.flush = f"rotating {self.SETS} input/output sets ({self.SETS * 20 * self.N >> 20} MiB > L2)"
@@ -212,8 +215,8 @@ class BlackScholesGeneric(BlackScholes):
     binding skipped: the program's run-time compiled kernel (mode 1) or the
     generic interpreter (mode 2)."""
 
-    def __init__(self, torch, lib, dev, precision, mode=1):
-        super().__init__(torch, lib, dev, precision)
+    def __init__(self, torch, lib, dev, precision, mode=1, n=None):
+        super().__init__(torch, lib, dev, precision, n)
         from nt2_gb300 import expr as E
         self.E, self.mode = E, mode
         what = "run-time compiled kernel" if mode == 1 else "generic interpreter"
@@ -407,13 +410,13 @@ class Rgb2Yuv(Workload):
         self.lib.rgb2yuv(r, g, b, y, u, v)
 
 
-def make(name, torch, lib, dev, precision, tune=None):
+def make(name, torch, lib, dev, precision, tune=None, n=None):
     if name == "bs":
-        return BlackScholes(torch, lib, dev, precision)
+        return BlackScholes(torch, lib, dev, precision, n)
     if name == "bs_generic":
-        return BlackScholesGeneric(torch, lib, dev, precision, mode=1)
+        return BlackScholesGeneric(torch, lib, dev, precision, mode=1, n=n)
     if name == "bs_interp":
-        return BlackScholesGeneric(torch, lib, dev, precision, mode=2)
+        return BlackScholesGeneric(torch, lib, dev, precision, mode=2, n=n)
     if name in ("reduce", "dot"):
         return Reduce(torch, lib, dev, dot=True)
     if name == "sum":
@@ -522,7 +525,7 @@ def run_ours(args):
     lib.load()
     prec = lib.PREC_NT2 if args.precision == "nt2" else lib.PREC_FAST
     tune = tuple(int(v) for v in args.tune.split(",")) if args.tune else None
-    wl = make(args.config, torch, lib, dev, prec, tune)
+    wl = make(args.config, torch, lib, dev, prec, tune, args.n)
     stream = torch.cuda.current_stream()
 
     def barrier():
@@ -649,6 +652,7 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="issue the K steps eagerly instead of from a graph")
     ap.add_argument("--streams", type=int, default=2, help="streams for independent steps inside the graph")
     ap.add_argument("--tune", default="", help="batched: block_threads,blocks_per_sm,tile_vectors")
+    ap.add_argument("--n", type=int, default=0, help="bs, bs_generic, bs_interp: options per launch (default 2^20)")
     ap.add_argument("--min-seconds", type=float, default=2.0, help="repeat K-step trials for at least this long")
     args = ap.parse_args()
     if args.warmup < 3:
