@@ -389,6 +389,40 @@ class SigmaDeltaFused(Workload):
         self.lib.sigmadelta_frames(self.frames[1:], self.bkg, self.var, self.labels)
 
 
+class Fold(Workload):
+    """Reduction along one dimension of a 16384 x 16384 float table (1 GiB):
+    dim 1 = per-column (contiguous) sums, dim 2 = per-row (strided) sums; or a
+    global max over the same 2^28 elements."""
+
+    def __init__(self, torch, lib, dev, kind, precision):
+        import ctypes
+        self.torch, self.lib, self.prec = torch, lib, precision
+        m = n = 16384
+        g = torch.Generator(device=dev).manual_seed(1001)
+        self.x = torch.randn(m * n, device=dev, generator=g)
+        self.shape = {"col": (1, m, n), "row": (m, n, 1), "max": (1, m * n, 1)}[kind]
+        self.op = lib.FOLD["max" if kind == "max" else "sum"]
+        lo, inner, hi = self.shape
+        nb = ctypes.c_size_t()
+        lib.check(lib.load().nt2g_fold_workspace_size(lo, inner, hi, ctypes.byref(nb)))
+        self.ws = torch.empty(max(nb.value, 16), dtype=torch.uint8, device=dev)
+        self.out = torch.empty(lo * hi, device=dev)
+        self.units = m * n
+        self.bytes = 4 * m * n + 4 * lo * hi
+        self.kernel = {"col": "k_fold_inner", "row": "k_fold_outer", "max": "k_fold_inner"}[kind]
+        self.launches = 1 if kind == "col" else 2  # strided and global folds add the in-order combine
+        what = {"col": "sum(A, 1): 16384 column sums", "row": "sum(A, 2): 16384 row sums",
+                "max": "globalmax over 2^28"}[kind]
+        self.name = f"fold {what} of a 16384x16384 float32 table"
+        self.flush = "1 GiB input > L2"
+
+    def step(self, i):
+        lo, inner, hi = self.shape
+        L = self.lib
+        L.check(L.load().nt2g_fold_f32(L._ptr(self.x), lo, inner, hi, self.op, self.prec, L._ptr(self.ws),
+                                       self.ws.numel(), L._ptr(self.out), None, L._stream()))
+
+
 class Rgb2Yuv(Workload):
     SETS = 8
     independent = True
@@ -435,6 +469,8 @@ def make(name, torch, lib, dev, precision, tune=None, n=None):
         return Rgb2Yuv(torch, lib, dev)
     if name == "sigmadelta_fused":
         return SigmaDeltaFused(torch, lib, dev)
+    if name in ("fold_col", "fold_row", "gmax"):
+        return Fold(torch, lib, dev, {"fold_col": "col", "fold_row": "row", "gmax": "max"}[name], precision)
     raise SystemExit(f"unknown config {name}")
 
 

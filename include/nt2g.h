@@ -137,6 +137,41 @@ nt2g_status nt2g_program_jit_source(const nt2g_program *p, int32_t precision, ch
  * reason in nt2g_last_error(), when NVRTC is unavailable or rejects it. */
 nt2g_status nt2g_program_jit_prepare(const nt2g_program *p, int32_t precision);
 
+/* ------------------------------------------------------------------ */
+/* Reductions along one dimension (sum(a, dim), max(a, [], dim), ...)  */
+/* ------------------------------------------------------------------ */
+/* The table is viewed as [lo, inner, hi] (column-major) and folded over
+ * inner: out[l + lo*h] = fold_k x[l + lo*(k + inner*h)], lo*hi outputs.
+ * This is NT2's reshape before inner_fold / outer_fold
+ * (core/reduction/include/nt2/dsl/functions/reduction/run.hpp:51-89):
+ *   2-D m x n table, dim 1 (per column): lo = 1, inner = m, hi = n;
+ *   dim 2 (per row): lo = m, inner = n, hi = 1;  global*: lo = hi = 1.
+ * Ops follow NT2's definitions: MEAN = rec(n) * sum (expr/mean.hpp),
+ * ASUM1 = sum(abs), ASUM2 = sum(sqr_abs), NORM2 = sqrt(asum2); MAX/MIN fold
+ * with (acc > x) ? acc : x, and index (optional, 0-based along the fold,
+ * -1 if none) receives the first position equal to the result, as NT2's
+ * globalmax(a, i) = globalfind(a == max).
+ * precision NT2G_PREC_NT2: each output folded in index order with NT2's
+ * unfused float operations (NT2's own order when it spreads outputs over
+ * threads), one thread per output.  NT2G_PREC_FAST: compensated FP32 sums
+ * combined in FP64, FP64 products, exact max/min (equal to the NT2 order on
+ * NaN-free data; a NaN propagates); deterministic for a given shape.
+ * workspace: nt2g_fold_workspace_size bytes (0 means none is needed). */
+typedef enum nt2g_fold_op {
+    NT2G_FOLD_SUM = 0,
+    NT2G_FOLD_PROD = 1,
+    NT2G_FOLD_MAX = 2,
+    NT2G_FOLD_MIN = 3,
+    NT2G_FOLD_MEAN = 4,
+    NT2G_FOLD_ASUM1 = 5,
+    NT2G_FOLD_ASUM2 = 6,
+    NT2G_FOLD_NORM2 = 7
+} nt2g_fold_op;
+
+nt2g_status nt2g_fold_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
+nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t op, int32_t precision,
+                          void *workspace, size_t workspace_bytes, float *out, int64_t *index, void *stream);
+
 /* Host tables.  Every entry point accepts host pointers for its tables and
  * workspaces where the current device can reach the memory: pinned or
  * registered host memory (cudaMallocHost, cudaHostRegister) on any system,

@@ -517,8 +517,9 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                         case NT2G_OP_SUB: r = P::sub(x, y); break;
                         case NT2G_OP_MUL: r = P::mul(x, y); break;
                         case NT2G_OP_DIV: r = P::div(x, y); break;
-                        case NT2G_OP_MIN: r = fminf(x, y); break;
-                        default: r = fmaxf(x, y); break;
+                        // boost/simd/arithmetic/functions/scalar/{min,max}.hpp
+                        case NT2G_OP_MIN: r = (x < y) ? x : y; break;
+                        default: r = (x > y) ? x : y; break;
                         }
                         d[j] = __float_as_uint(r);
                     } else {

@@ -153,12 +153,8 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_SUB: e = f32 ? "P::sub(" + A + ", " + B + ")" : "(" + A + " - " + B + ") & 255u"; break;
         case NT2G_OP_MUL: e = f32 ? "P::mul(" + A + ", " + B + ")" : "(" + A + " * " + B + ") & 255u"; break;
         case NT2G_OP_DIV: e = "P::div(" + A + ", " + B + ")"; break;
-        case NT2G_OP_MIN:
-            e = f32 ? "fminf(" + A + ", " + B + ")" : "(" + A + " < " + B + " ? " + A + " : " + B + ")";
-            break;
-        case NT2G_OP_MAX:
-            e = f32 ? "fmaxf(" + A + ", " + B + ")" : "(" + A + " > " + B + " ? " + A + " : " + B + ")";
-            break;
+        case NT2G_OP_MIN: e = "(" + A + " < " + B + " ? " + A + " : " + B + ")"; break;  // NT2: a < b ? a : b
+        case NT2G_OP_MAX: e = "(" + A + " > " + B + " ? " + A + " : " + B + ")"; break;  // NT2: a > b ? a : b
         case NT2G_OP_ADDS: e = "((" + A + " + " + B + ") > 255u ? 255u : (" + A + " + " + B + "))"; break;
         case NT2G_OP_FMA: e = "P::fma(" + A + ", " + B + ", " + C + ")"; break;
         case NT2G_OP_FNMS: e = "P::fma(-" + A + ", " + B + ", " + C + ")"; break;

@@ -10,6 +10,7 @@
 // usage: nt2_demos lower
 //        nt2_demos bs|bs_host|bs_demo|saxpy|rgb2yuv DIR N
 //        nt2_demos sdot DIR N
+//        nt2_demos fold DIR M N
 //        nt2_demos sigmadelta DIR PIXELS FRAMES
 // Inputs and outputs are raw little-endian arrays DIR/<name>.bin.
 #include <cstdio>
@@ -186,6 +187,27 @@ int main(int argc, char **argv)
                         nt2::sum64(X * Y), (double)nt2::dot(X, Y), (double)nt2::sum(X));
             // sum of a general expression goes through a temporary
             std::printf("sum_expr %.17g\n", nt2::sum64(nt2::sqr(X) + Y));
+        } else if (mode == "fold") {
+            // an M x N table (N = argv[4]): per-column and per-row reductions, then the global forms
+            const std::size_t cols = std::strtoull(argv[4], nullptr, 10);
+            nt2::table<float> h(nt2::of_size(n, cols));
+            auto v = read_bin<float>(dir + "a.bin", n * cols);
+            std::memcpy(h.data(), v.data(), v.size() * sizeof(float));
+            dtable A;
+            A = h;
+            save(dir + "sum1.bin", nt2::sum(A, 1));
+            save(dir + "sum2.bin", nt2::sum(A, 2));
+            save(dir + "max1.bin", nt2::maximum(A, 1));
+            save(dir + "min2.bin", nt2::minimum(A, 2));
+            save(dir + "mean1.bin", nt2::mean(A, 1));
+            save(dir + "norm2_2.bin", nt2::norm2(A, 2));
+            save(dir + "hsum1.bin", nt2::sum(h, 1));  // a host table folded in place (or staged)
+            std::int64_t imax = 0, imin = 0;
+            const float gmax = nt2::globalmax(A, imax), gmin = nt2::globalmin(h, imin);
+            std::printf("globalmax %.9g %lld\nglobalmin %.9g %lld\nglobalmean %.9g\nglobalnorm2 %.9g\n"
+                        "globalasum1 %.9g\n",
+                        (double)gmax, (long long)imax, (double)gmin, (long long)imin, (double)nt2::globalmean(A),
+                        (double)nt2::globalnorm2(A), (double)nt2::globalasum1(A));
         } else if (mode == "sigmadelta") {
             const std::size_t frames = std::strtoull(argv[4], nullptr, 10);
             auto all = read_bin<std::uint8_t>(dir + "frames.bin", n * frames);

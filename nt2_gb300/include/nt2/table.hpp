@@ -712,4 +712,123 @@ template <class X> float sum(const X &x) { return (float)sum64(x); }
 template <class X> float globalsum(const X &x) { return (float)sum64(x); }
 template <class A, class B> float dot(const A &a, const B &b) { return (float)sum64(a * b); }
 
+// ------------------------------------------------ reductions along a dimension --
+// sum(a, dim), prod, maximum, minimum, mean, asum1, asum2, norm2 of a float
+// table, as NT2 folds them: the extent split into [lo, inner, hi] around dim
+// (core/reduction/include/nt2/dsl/functions/reduction/run.hpp:51-89), the result
+// a table of the same site with extent 1 along dim.  The global forms fold the
+// whole table.  options().precision selects NT2's in-order fold (NT2G_PREC_NT2)
+// or the compensated one.
+namespace detail {
+struct fold_shape {
+    std::int64_t lo = 1, inner = 1, hi = 1;
+};
+inline fold_shape split(const of_size_ &e, int dim)
+{
+    fold_shape f;
+    for (int k = 0; k < 4; ++k) {
+        if (k < dim - 1) f.lo *= (std::int64_t)e.d[k];
+        else if (k == dim - 1) f.inner = (std::int64_t)e.d[k];
+        else f.hi *= (std::int64_t)e.d[k];
+    }
+    return f;
+}
+// NT2's default reduction dimension: the first non-singleton one
+inline int first_non_singleton(const of_size_ &e)
+{
+    for (int k = 0; k < 4; ++k)
+        if (e.d[k] != 1) return k + 1;
+    return 1;
+}
+// fold x (device pointer, or host memory the device reaches) into out / index
+inline void fold_raw(const float *x, fold_shape f, int op, float *out, std::int64_t *index)
+{
+    std::size_t b = 0;
+    check(nt2g_fold_workspace_size(f.lo, f.inner, f.hi, &b), "fold workspace");
+    device_buffer ws(b);
+    check(nt2g_fold_f32(x, f.lo, f.inner, f.hi, op, options().precision, ws.p, b, out, index, options().stream),
+          "fold");
+    check(nt2g_stream_synchronize(options().stream), "fold");  // ws is released on return
+}
+template <class Site>
+inline table<float, Site> fold_dim(const table<float, Site> &t, int dim, int op)
+{
+    if (dim < 1 || dim > 4) throw gpu_error(NT2G_ERR_INVALID, "reduction dimension out of range");
+    of_size_ e = t.extent();
+    const fold_shape f = split(e, dim);
+    e.d[dim - 1] = 1;
+    table<float, Site> r(e);
+    const bool direct = table<float, Site>::on_device || host_in_place();
+    if (direct) {
+        fold_raw(t.data(), f, op, r.data(), nullptr);
+    } else {  // host tables the device cannot reach: through device buffers
+        table<float, device_> dt(t.extent()), dr(e);
+        dt = t;
+        fold_raw(dt.data(), f, op, dr.data(), nullptr);
+        r = dr;
+    }
+    return r;
+}
+template <class Site>
+inline float fold_all(const table<float, Site> &t, int op, std::int64_t *index1 = nullptr)
+{
+    const fold_shape f{1, (std::int64_t)t.numel(), 1};
+    device_buffer out(16);  // the float result at 0, the int64 position at 8
+    float *o = (float *)out.p;
+    std::int64_t *ix = index1 ? (std::int64_t *)((char *)out.p + 8) : nullptr;
+    if (table<float, Site>::on_device || host_in_place()) {
+        fold_raw(t.data(), f, op, o, ix);
+    } else {
+        table<float, device_> dt(t.extent());
+        dt = t;
+        fold_raw(dt.data(), f, op, o, ix);
+    }
+    float r = 0.0f;
+    check(nt2g_memcpy(&r, o, sizeof r, 2, options().stream), "fold result");
+    if (ix) {
+        check(nt2g_memcpy(index1, ix, sizeof *ix, 2, options().stream), "fold index");
+        *index1 += 1;  // NT2 positions are 1-based (0: none)
+    }
+    check(nt2g_stream_synchronize(options().stream), "fold result");
+    return r;
+}
+}  // namespace detail
+
+#define NT2G_DIM_FOLD(NAME, OP)                                                                            \
+    template <class Site> table<float, Site> NAME(const table<float, Site> &t, int dim)                     \
+    {                                                                                                       \
+        return detail::fold_dim(t, dim, OP);                                                                \
+    }
+NT2G_DIM_FOLD(sum, NT2G_FOLD_SUM)
+NT2G_DIM_FOLD(prod, NT2G_FOLD_PROD)
+NT2G_DIM_FOLD(maximum, NT2G_FOLD_MAX)
+NT2G_DIM_FOLD(minimum, NT2G_FOLD_MIN)
+NT2G_DIM_FOLD(mean, NT2G_FOLD_MEAN)
+NT2G_DIM_FOLD(asum1, NT2G_FOLD_ASUM1)
+NT2G_DIM_FOLD(asum2, NT2G_FOLD_ASUM2)
+NT2G_DIM_FOLD(norm2, NT2G_FOLD_NORM2)
+#undef NT2G_DIM_FOLD
+
+template <class Site> float globalmax(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_MAX); }
+template <class Site> float globalmin(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_MIN); }
+// globalmax(t, i): i receives the 1-based linear position of the first element equal to the maximum
+template <class Site> float globalmax(const table<float, Site> &t, std::int64_t &i)
+{
+    return detail::fold_all(t, NT2G_FOLD_MAX, &i);
+}
+template <class Site> float globalmin(const table<float, Site> &t, std::int64_t &i)
+{
+    return detail::fold_all(t, NT2G_FOLD_MIN, &i);
+}
+template <class Site> float globalprod(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_PROD); }
+template <class Site> float globalmean(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_MEAN); }
+template <class Site> float globalasum1(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ASUM1); }
+template <class Site> float globalasum2(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ASUM2); }
+template <class Site> float globalnorm2(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_NORM2); }
+// sum(a) of a table with more than one non-singleton dimension folds the first of them
+template <class Site> table<float, Site> sum_first(const table<float, Site> &t)
+{
+    return detail::fold_dim(t, detail::first_non_singleton(t.extent()), NT2G_FOLD_SUM);
+}
+
 }  // namespace nt2

@@ -96,6 +96,8 @@ _SIGNATURES = {
                                     ctypes.POINTER(BatchTune), ctypes.POINTER(ctypes.c_float)]),
     "nt2g_batch_stats": (_I32, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "nt2g_host_access": (_I32, [ctypes.POINTER(_I32)]),
+    "nt2g_fold_workspace_size": (_I32, [_I64, _I64, _I64, ctypes.POINTER(ctypes.c_size_t)]),
+    "nt2g_fold_f32": (_I32, [_VP, _I64, _I64, _I64, _I32, _I32, _VP, ctypes.c_size_t, _VP, _VP, _VP]),
     "nt2g_device_alloc": (_I32, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "nt2g_device_free": (_I32, [_VP]),
     "nt2g_memcpy": (_I32, [_VP, _VP, ctypes.c_size_t, _I32, _VP]),
@@ -182,6 +184,24 @@ def sigmadelta_frames(frames, bkg, var, labels, stream=None):
 
 def map_f32(fn, x, y, precision=PREC_FAST, stream=None):
     check(load().nt2g_map_f32(MAP_FN[fn], _ptr(x), _ptr(y), x.numel(), precision, _stream(stream)))
+
+
+FOLD = {"sum": 0, "prod": 1, "max": 2, "min": 3, "mean": 4, "asum1": 5, "asum2": 6, "norm2": 7}
+
+
+def fold(x, lo, inner, hi, op, precision=PREC_FAST, index=False, stream=None):
+    """Reduce x (viewed as [lo, inner, hi], column-major) over inner:
+    returns out[lo*hi] (and the int64 first-equal index for max/min)."""
+    import torch
+    nb = ctypes.c_size_t()
+    check(load().nt2g_fold_workspace_size(lo, inner, hi, ctypes.byref(nb)))
+    dev = x.device
+    ws = torch.empty(max(nb.value, 16), dtype=torch.uint8, device=dev)
+    out = torch.empty(lo * hi, dtype=torch.float32, device=dev)
+    idx = torch.empty(lo * hi, dtype=torch.int64, device=dev) if index else None
+    check(load().nt2g_fold_f32(_ptr(x), lo, inner, hi, FOLD[op], precision, _ptr(ws), ws.numel(), _ptr(out),
+                               _ptr(idx), _stream(stream)))
+    return (out, idx) if index else out
 
 
 class Reducer:

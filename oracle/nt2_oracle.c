@@ -543,6 +543,106 @@ EXPORT double o_exact_sum(const float *x, const float *y, int64_t n, int nthread
     return acc_value(total);
 }
 
+/* Reductions along one dimension, the table viewed as [lo, inner, hi]
+ * (core/reduction/include/nt2/dsl/functions/reduction/run.hpp:51-89).
+ * op: 0 sum, 1 prod, 2 max, 3 min, 4 mean, 5 asum1, 6 asum2, 7 norm2.
+ *
+ * o_fold_nt2_f32: each output folded in index order from the neutral element
+ * with unfused float operations, fold_step's acc = bop(acc, x)
+ * (core/reduction/include/nt2/core/functions/details/fold_step.hpp:31-43) as
+ * NT2's per-segment workers run it (arch/shared_memory/include/nt2/sdk/
+ * shared_memory/worker/inner_fold.hpp:47-80, worker/outer_fold.hpp);
+ * max = (a0 > a1) ? a0 : a1 (boost/simd/arithmetic/functions/scalar/max.hpp),
+ * mean = rec(float(n)) * sum (core/functions/expr/mean.hpp:22-33),
+ * asum2 = sum(sqr_abs), norm2 = sqrt(asum2).  index: first position equal to
+ * the result (common/globalmax.hpp:36-48), -1 if none. */
+EXPORT void o_fold_nt2_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int op, float *out,
+                           int64_t *index, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t o = 0; o < lo * hi; ++o) {
+        const int64_t h = o / lo, l = o - h * lo;
+        const float *p = x + l + lo * inner * h;
+        float acc = op == 1 ? 1.0f : op == 2 ? -INFINITY : op == 3 ? INFINITY : 0.0f;
+        for (int64_t k = 0; k < inner; ++k) {
+            const float v = p[lo * k];
+            switch (op) {
+            case 1: acc = acc * v; break;
+            case 2: acc = (acc > v) ? acc : v; break;
+            case 3: acc = (acc < v) ? acc : v; break;
+            case 5: acc = acc + fabsf(v); break;
+            case 6: case 7: acc = acc + v * v; break;
+            default: acc = acc + v; break;
+            }
+        }
+        if (op == 4) acc = (1.0f / (float)inner) * acc;
+        if (op == 7) acc = sqrtf(acc);
+        out[o] = acc;
+        if (index && (op == 2 || op == 3)) {
+            int64_t f = -1;
+            for (int64_t k = 0; k < inner && f < 0; ++k)
+                if (p[lo * k] == acc) f = k;
+            index[o] = f;
+        }
+    }
+}
+
+/* Reference values for the fast policy: sum-type ops exactly (superaccumulator;
+ * x*x is exact in double), rounded to double, with sum |term| for the error
+ * bound; prod in long double; max/min in NT2's order with NaN propagation
+ * (the first NaN), index = first position equal to the result. */
+EXPORT void o_fold_ref(const float *x, int64_t lo, int64_t inner, int64_t hi, int op, double *out, double *abs_sum,
+                       int64_t *index, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+    for (int64_t o = 0; o < lo * hi; ++o) {
+        const int64_t h = o / lo, l = o - h * lo;
+        const float *p = x + l + lo * inner * h;
+        if (op == 1) {
+            long double r = 1.0L;
+            for (int64_t k = 0; k < inner; ++k) r *= p[lo * k];
+            out[o] = (double)r;
+            if (abs_sum) abs_sum[o] = fabs((double)r);
+        } else if (op == 2 || op == 3) {
+            float best = op == 2 ? -INFINITY : INFINITY;
+            int nan = 0;
+            for (int64_t k = 0; k < inner; ++k) {
+                const float v = p[lo * k];
+                if (v != v) { best = v; nan = 1; break; }
+                if (op == 2 ? !(best > v) : !(best < v)) best = v;  /* NT2's order: an equal later value wins */
+            }
+            out[o] = best;
+            if (index) {
+                int64_t f = -1;
+                for (int64_t k = 0; k < inner && f < 0; ++k) {
+                    const float v = p[lo * k];
+                    if (nan ? v != v : v == best) f = k;
+                }
+                index[o] = f;
+            }
+        } else {
+            superacc a;
+            memset(&a, 0, sizeof a);
+            double as = 0.0;
+            int64_t cnt = 0;
+            for (int64_t k = 0; k < inner; ++k) {
+                const double v = p[lo * k];
+                const double t = op == 5 ? fabs(v) : (op == 6 || op == 7) ? v * v : v;
+                acc_add(&a, t);
+                as += fabs(t);
+                if (++cnt == (1 << 24)) { acc_norm(&a); cnt = 0; }
+            }
+            double r = acc_value(a);
+            if (op == 4) r = r / (double)inner;
+            if (op == 7) r = sqrt(r);
+            out[o] = r;
+            if (abs_sum) abs_sum[o] = as;
+        }
+    }
+}
+
 /* NT2 grain for transform on Linux without cpuid: top_cache_size(2) reads
  * cache_sizes_[2], which the sysconf path fills with the L3 size in bytes
  * (modules/sdk/config/include/nt2/sdk/config/details/cache.hpp:26-39,

@@ -63,6 +63,8 @@ def lib():
         L.o_sum_nt2_f32.argtypes = [_P, _P, _I64, ctypes.c_int]
         L.o_sum_plain_f32.restype = ctypes.c_float
         L.o_sum_plain_f32.argtypes = [_P, _P, _I64, ctypes.c_int]
+        L.o_fold_nt2_f32.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, ctypes.c_int]
+        L.o_fold_ref.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, _P, ctypes.c_int]
         L.o_globalsum_f32.restype = ctypes.c_float
         L.o_globalsum_f32.argtypes = [_P, _I64]
         L.o_exact_sum.restype = ctypes.c_double
@@ -203,6 +205,32 @@ def sum_plain(x, y=None, nthreads=None):
 def globalsum(x):
     x = _f32(x)
     return float(np.float32(lib().o_globalsum_f32(_p(x), x.size)))
+
+
+FOLD_OPS = {"sum": 0, "prod": 1, "max": 2, "min": 3, "mean": 4, "asum1": 5, "asum2": 6, "norm2": 7}
+
+
+def fold_nt2(x, lo, inner, hi, op, nthreads=None):
+    """NT2's in-order per-output fold of x viewed as [lo, inner, hi]:
+    (float32 out[lo*hi], int64 index[lo*hi] for max/min)."""
+    x = _f32(x)
+    assert x.size == lo * inner * hi
+    out = np.empty(lo * hi, np.float32)
+    idx = np.empty(lo * hi, np.int64)
+    lib().o_fold_nt2_f32(_p(x), lo, inner, hi, FOLD_OPS[op], _p(out), _p(idx), nthreads or threads())
+    return out, idx
+
+
+def fold_ref(x, lo, inner, hi, op, nthreads=None):
+    """Reference fold: exact sums (double), sum |term| per output, max/min exact
+    with NaN propagation and first-equal index."""
+    x = _f32(x)
+    assert x.size == lo * inner * hi
+    out = np.empty(lo * hi, np.float64)
+    asum = np.empty(lo * hi, np.float64)
+    idx = np.empty(lo * hi, np.int64)
+    lib().o_fold_ref(_p(x), lo, inner, hi, FOLD_OPS[op], _p(out), _p(asum), _p(idx), nthreads or threads())
+    return out, asum, idx
 
 
 def exact_sum(x, y=None, nthreads=None):

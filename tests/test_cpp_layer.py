@@ -32,7 +32,9 @@ def test_demo_expressions_bind_fused_kernels(demos):
 def _run(demos, *args, env=None):
     e = dict(os.environ)
     e.update(env or {})
-    return subprocess.run([demos, *map(str, args)], check=True, capture_output=True, text=True, env=e).stdout
+    r = subprocess.run([demos, *map(str, args)], capture_output=True, text=True, env=e)
+    assert r.returncode == 0, f"nt2_demos {args[0]} exited {r.returncode}: {r.stderr.strip()}"
+    return r.stdout
 
 
 def _eq(a, b):
@@ -110,3 +112,38 @@ def test_sigmadelta_through_tables(demos, oracle, tmp_path):
     assert _eq(np.fromfile(tmp_path / "bkg.bin", np.uint8), rb)
     assert _eq(np.fromfile(tmp_path / "var.bin", np.uint8), rv)
     assert _eq(np.fromfile(tmp_path / "label.bin", np.uint8), rl)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["1", "0"], ids=["nt2", "fast"])
+def test_folds_through_tables(demos, oracle, tmp_path, prec):
+    """sum(A, 1), sum(A, 2), maximum/minimum/mean/norm2 along a dimension and
+    the global forms of an M x N table through the C++ layer."""
+    m, n = 1000, 777
+    rng = np.random.default_rng(21)
+    a = (rng.standard_normal(m * n) * np.exp2(rng.integers(-6, 6, m * n))).astype(np.float32)
+    a.tofile(tmp_path / "a.bin")
+    lines = _run(demos, "fold", tmp_path, m, n, env={"NT2G_PRECISION": prec}).splitlines()
+    glob = {ln.split()[0]: ln.split()[1:] for ln in lines}
+    cases = [("sum1", (1, m, n), "sum"), ("sum2", (m, n, 1), "sum"), ("max1", (1, m, n), "max"),
+             ("min2", (m, n, 1), "min"), ("mean1", (1, m, n), "mean"), ("norm2_2", (m, n, 1), "norm2"),
+             ("hsum1", (1, m, n), "sum")]
+    for name, shape, op in cases:
+        got = np.fromfile(tmp_path / f"{name}.bin", np.float32)
+        if prec == "1":
+            ref, _ = oracle.fold_nt2(a, *shape, op)
+            assert _eq(got, ref), name
+        else:
+            ref, _, _ = oracle.fold_ref(a, *shape, op)
+            assert (np.abs(got - ref) <= np.spacing(np.abs(ref).astype(np.float32))).all(), name
+    gmax, imax = oracle.fold_nt2(a, 1, m * n, 1, "max")
+    gmin, imin = oracle.fold_nt2(a, 1, m * n, 1, "min")
+    assert np.float32(glob["globalmax"][0]) == gmax[0] and int(glob["globalmax"][1]) == imax[0] + 1
+    assert np.float32(glob["globalmin"][0]) == gmin[0] and int(glob["globalmin"][1]) == imin[0] + 1
+    for key, op in (("globalmean", "mean"), ("globalnorm2", "norm2"), ("globalasum1", "asum1")):
+        if prec == "1":
+            ref, _ = oracle.fold_nt2(a, 1, m * n, 1, op)
+            assert np.float32(glob[key][0]) == ref[0], key
+        else:
+            ref, _, _ = oracle.fold_ref(a, 1, m * n, 1, op)
+            assert abs(float(glob[key][0]) - ref[0]) <= np.spacing(np.float32(abs(ref[0]))), key

@@ -239,6 +239,25 @@ def test_generic_interpreter_uint8_wraparound(lib, dev):
         assert _eq(o2.cpu().numpy(), (-a.astype(int)).astype(np.uint8)) and _eq(o3.cpu().numpy(), b), mode
 
 
+def test_min_max_follow_nt2_operand_order(lib, dev):
+    """max(a, b) = (a > b) ? a : b and min(a, b) = (a < b) ? a : b
+    (boost/simd/arithmetic/functions/scalar/max.hpp, min.hpp): a NaN second
+    operand wins, a NaN first operand loses, and -0/+0 ties take b."""
+    a = np.array([1.0, np.nan, -0.0, 0.0, 2.0], np.float32)
+    b = np.array([np.nan, 1.0, 0.0, -0.0, 2.0], np.float32)
+    ta, tb = _t(dev, a), _t(dev, b)
+    mx, mn = torch.empty_like(ta), torch.empty_like(ta)
+    with np.errstate(invalid="ignore"):
+        rmax, rmin = np.where(a > b, a, b), np.where(a < b, a, b)
+    for mode in (1, 2):
+        E.assign([mx, mn], [E.max_(E.Table(ta), E.Table(tb)), E.min_(E.Table(ta), E.Table(tb))], force_generic=mode)
+        torch.cuda.synchronize()
+        for got, ref in ((mx, rmax), (mn, rmin)):
+            g = got.cpu().numpy()
+            assert np.array_equal(np.isnan(g), np.isnan(ref)), mode
+            assert np.array_equal(g[~np.isnan(g)].view(np.uint32), ref[~np.isnan(ref)].view(np.uint32)), mode
+
+
 def test_logical_stored_into_float_table(lib, dev):
     x = np.array([1, 2, 3, 4, 5], np.float32)
     tx = _t(dev, x)

@@ -1,0 +1,123 @@
+"""Reductions along one dimension (sum(a, dim), max(a, [], dim), mean, norm2,
+...) of tables viewed as [lo, inner, hi], against the oracle.
+
+NT2 policy: bit-identical to the oracle's restatement of NT2's in-order
+per-output fold (values and max/min positions).  Fast policy: sum-type results
+within one float ulp of the exact value (compensated FP32 chunks combined in
+FP64), products within two ulps, max/min and positions identical to NT2's
+order on NaN-free data, a NaN propagated with its first position.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [
+    (1, 4096, 4096),      # dim 1 of a 4096 x 4096 table: one chunk per column
+    (4096, 4096, 1),      # dim 2 of the same table: strided, 4 outputs per thread
+    (1, 1 << 22, 1),      # global: many chunks, two-pass combine
+    (1, 17, 10000),       # short columns: one thread per column
+    (1, 100003, 7),       # ragged, unaligned columns
+    (1001, 33, 77),       # middle dimension of a 3-D table, lo not a multiple of 4
+    (64, 1 << 16, 1),     # few long rows: chunked strided fold
+    (3, 5, 2),
+    (1, 0, 5),            # empty fold: neutral element
+]
+OPS = ["sum", "prod", "max", "min", "mean", "asum1", "asum2", "norm2"]
+
+
+def _data(shape, op, seed):
+    lo, inner, hi = shape
+    rng = np.random.default_rng(seed)
+    n = lo * inner * hi
+    if op == "prod":  # keep products finite: factors near 1
+        x = rng.uniform(0.999, 1.001, n)
+    else:
+        x = rng.standard_normal(n) * np.exp2(rng.integers(-8, 8, n))
+    x = x.astype(np.float32)
+    if op in ("max", "min") and n > 10:  # ties, signed zeros
+        x[rng.integers(0, n, n // 50)] = 0.0
+        x[rng.integers(0, n, n // 50)] = -0.0
+        x[rng.integers(0, n, n // 100)] = x.max() if op == "max" else x.min()
+    return x
+
+
+def _same_bits(a, b):
+    """Bitwise equality, any NaN equal to any NaN (NaN payloads differ by platform)."""
+    a, b = np.asarray(a, np.float32), np.asarray(b, np.float32)
+    return bool(np.all((a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))))
+
+
+def _ulp32(v):
+    return np.spacing(np.abs(v).astype(np.float32)).astype(np.float64)
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{a}x{b}x{c}" for a, b, c in SHAPES])
+@pytest.mark.parametrize("op", OPS)
+def test_fold_nt2_policy_bit_exact(lib, dev, oracle, shape, op):
+    lo, inner, hi = shape
+    if lo * inner * hi > (1 << 20) and op != "sum":
+        pytest.skip("large shapes: sum only under the sequential policy (one thread per output)")
+    x = _data(shape, op, 11)
+    tx = torch.from_numpy(x).to(dev)
+    want_idx = op in ("max", "min")
+    got = lib.fold(tx, lo, inner, hi, op, precision=lib.PREC_NT2, index=want_idx)
+    torch.cuda.synchronize()
+    ref, ridx = oracle.fold_nt2(x, lo, inner, hi, op)
+    out = (got[0] if want_idx else got).cpu().numpy()
+    assert _same_bits(out, ref)
+    if want_idx:
+        assert np.array_equal(got[1].cpu().numpy(), ridx)
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{a}x{b}x{c}" for a, b, c in SHAPES])
+@pytest.mark.parametrize("op", OPS)
+def test_fold_fast_policy(lib, dev, oracle, shape, op):
+    lo, inner, hi = shape
+    x = _data(shape, op, 12)
+    tx = torch.from_numpy(x).to(dev)
+    want_idx = op in ("max", "min")
+    got = lib.fold(tx, lo, inner, hi, op, index=want_idx)
+    torch.cuda.synchronize()
+    ref, asum, ridx = oracle.fold_ref(x, lo, inner, hi, op)
+    out = (got[0] if want_idx else got).cpu().numpy()
+    if inner == 0:
+        nt2, _ = oracle.fold_nt2(x, lo, inner, hi, op)
+        assert _same_bits(out, nt2)
+        return
+    if want_idx:
+        assert np.array_equal(out.view(np.uint32), ref.astype(np.float32).view(np.uint32))
+        assert np.array_equal(got[1].cpu().numpy(), ridx)
+        nt2, nidx = oracle.fold_nt2(x, lo, inner, hi, op)  # no NaN here: equal to NT2's order
+        assert np.array_equal(out.view(np.uint32), nt2.view(np.uint32)) and np.array_equal(got[1].cpu().numpy(), nidx)
+        return
+    err = np.abs(out.astype(np.float64) - ref)
+    tol = (2.0 if op == "prod" else 1.0) * _ulp32(ref)
+    assert (err <= tol).all(), (op, shape, float((err / _ulp32(ref)).max()))
+
+
+def test_fold_max_min_nan_propagates(lib, dev, oracle):
+    x = np.random.default_rng(13).standard_normal(3 * 1000 * 5).astype(np.float32)
+    x[[7, 2500, 9000, 9001]] = np.nan
+    tx = torch.from_numpy(x).to(dev)
+    for lo, inner, hi in ((1, 3000, 5), (3, 1000, 5)):
+        for op in ("max", "min"):
+            out, idx = lib.fold(tx, lo, inner, hi, op, index=True)
+            ref, _, ridx = oracle.fold_ref(x, lo, inner, hi, op)
+            torch.cuda.synchronize()
+            o = out.cpu().numpy()
+            assert np.array_equal(np.isnan(o), np.isnan(ref)) and np.array_equal(o[~np.isnan(o)],
+                                                                                 ref[~np.isnan(ref)].astype(np.float32))
+            assert np.array_equal(idx.cpu().numpy(), ridx)
+
+
+def test_fold_global_matches_reduce_entry(lib, dev):
+    """globalsum through the fold family agrees with the dedicated sum kernel
+    to within one float ulp of the exact value (both compensated)."""
+    n = (1 << 24) + 3
+    x = np.random.default_rng(14).standard_normal(n).astype(np.float32)
+    tx = torch.from_numpy(x).to(dev)
+    a = lib.fold(tx, 1, n, 1, "sum").item()
+    b = lib.Reducer(dev)(tx)[1].item()
+    assert abs(a - b) <= np.spacing(np.float32(abs(b)))
