@@ -423,6 +423,39 @@ class Fold(Workload):
                                        self.ws.numel(), L._ptr(self.out), None, L._stream()))
 
 
+class Scan(Workload):
+    """Cumulative op along one dimension of a 16384 x 16384 float table
+    (1 GiB in, 1 GiB out: 8 B/element algorithmic): cumsum per column, cumsum
+    of the whole table as one segment, or cummax per row (strided)."""
+
+    def __init__(self, torch, lib, dev, kind, precision):
+        import ctypes
+        self.torch, self.lib, self.prec = torch, lib, precision
+        m = n = 16384
+        g = torch.Generator(device=dev).manual_seed(1001)
+        self.x = torch.randn(m * n, device=dev, generator=g)
+        self.y = torch.empty_like(self.x)
+        self.shape = {"col": (1, m, n), "all": (1, m * n, 1), "rowmax": (m, n, 1)}[kind]
+        self.op = lib.SCAN["max" if kind == "rowmax" else "sum"]
+        lo, inner, hi = self.shape
+        nb = ctypes.c_size_t()
+        lib.check(lib.load().nt2g_scan_workspace_size(lo, inner, hi, ctypes.byref(nb)))
+        self.ws = torch.empty(max(nb.value, 16), dtype=torch.uint8, device=dev)
+        self.units, self.bytes = m * n, 8 * m * n
+        self.kernel = "k_scan_outer" if kind == "rowmax" else "k_scan_inner"
+        self.launches = 1 if nb.value == 0 else 3
+        what = {"col": "cumsum(A, 1): 16384 columns", "all": "cumsum over all 2^28 elements (one segment)",
+                "rowmax": "cummax(A, 2): 16384 rows, strided"}[kind]
+        self.name = f"scan {what} of a 16384x16384 float32 table"
+        self.flush = "1 GiB input > L2"
+
+    def step(self, i):
+        lo, inner, hi = self.shape
+        L = self.lib
+        L.check(L.load().nt2g_scan_f32(L._ptr(self.x), lo, inner, hi, self.op, self.prec, L._ptr(self.ws),
+                                       self.ws.numel(), L._ptr(self.y), L._stream()))
+
+
 class Rgb2Yuv(Workload):
     SETS = 8
     independent = True
@@ -469,6 +502,9 @@ def make(name, torch, lib, dev, precision, tune=None, n=None):
         return Rgb2Yuv(torch, lib, dev)
     if name == "sigmadelta_fused":
         return SigmaDeltaFused(torch, lib, dev)
+    if name in ("cumsum_col", "cumsum_all", "cummax_row"):
+        return Scan(torch, lib, dev, {"cumsum_col": "col", "cumsum_all": "all", "cummax_row": "rowmax"}[name],
+                    precision)
     if name in ("fold_col", "fold_row", "gmax"):
         return Fold(torch, lib, dev, {"fold_col": "col", "fold_row": "row", "gmax": "max"}[name], precision)
     raise SystemExit(f"unknown config {name}")

@@ -172,6 +172,29 @@ nt2g_status nt2g_fold_workspace_size(int64_t lo, int64_t inner, int64_t hi, size
 nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t op, int32_t precision,
                           void *workspace, size_t workspace_bytes, float *out, int64_t *index, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Cumulative functions along one dimension (cumsum, cumprod, ...)     */
+/* ------------------------------------------------------------------ */
+/* Same [lo, inner, hi] view as the folds; out has the shape of x (out may be
+ * x): out[l + lo*(k + inner*h)] = scan over k' <= k (NT2's run_assign of a
+ * cumulative node, core/swar/include/nt2/dsl/functions/cumulative/run.hpp:26-67;
+ * summary = bop(summary, x) in order from the neutral element,
+ * core/swar/include/nt2/core/functions/details/scan_step.hpp:27-43).
+ * NT2G_PREC_NT2: that order with NT2's unfused float operations, one thread
+ * per segment.  NT2G_PREC_FAST: compensated cumsum (within about an ulp of the
+ * exact prefix), FP64 cumprod, exact cummax/cummin equal to NT2's order (NaN
+ * included); deterministic for a given shape. */
+typedef enum nt2g_scan_op {
+    NT2G_SCAN_SUM = 0,
+    NT2G_SCAN_PROD = 1,
+    NT2G_SCAN_MAX = 2,
+    NT2G_SCAN_MIN = 3
+} nt2g_scan_op;
+
+nt2g_status nt2g_scan_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
+nt2g_status nt2g_scan_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t op, int32_t precision,
+                          void *workspace, size_t workspace_bytes, float *out, void *stream);
+
 /* Host tables.  Every entry point accepts host pointers for its tables and
  * workspaces where the current device can reach the memory: pinned or
  * registered host memory (cudaMallocHost, cudaHostRegister) on any system,

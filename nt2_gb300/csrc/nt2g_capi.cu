@@ -899,6 +899,35 @@ extern "C" nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, 
                        (cudaStream_t)stream);
 }
 
+extern "C" nt2g_status nt2g_scan_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes)
+{
+    NT2G_CHECK_ARG(bytes != nullptr, "nt2g_scan_workspace_size: bytes is NULL");
+    NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_scan_workspace_size: negative extent");
+    return scan_workspace_bytes(lo, inner, hi, bytes);
+}
+
+extern "C" nt2g_status nt2g_scan_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t op,
+                                     int32_t precision, void *workspace, size_t workspace_bytes, float *out,
+                                     void *stream)
+{
+    NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_scan_f32: negative extent (%lld, %lld, %lld)",
+                   (long long)lo, (long long)inner, (long long)hi);
+    NT2G_CHECK_ARG(op >= NT2G_SCAN_SUM && op <= NT2G_SCAN_MIN, "nt2g_scan_f32: op %d", op);
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_scan_f32: precision %d",
+                   precision);
+    const int64_t n = lo * inner * hi;
+    if (n == 0) return NT2G_OK;
+    NT2G_CHECK_ARG(x != nullptr && out != nullptr, "nt2g_scan_f32: NULL table");
+    NT2G_CHECK_ARG(out == x || (out + n <= x || x + n <= out), "nt2g_scan_f32: out partially overlaps x");
+    size_t need = 0;
+    scan_workspace_bytes(lo, inner, hi, &need);
+    NT2G_CHECK_ARG(precision == NT2G_PREC_NT2 || need == 0 || (workspace != nullptr && workspace_bytes >= need),
+                   "nt2g_scan_f32: workspace of %zu bytes, %zu needed", workspace_bytes, need);
+    NT2G_CHECK_ARG(((uintptr_t)workspace & 15u) == 0, "nt2g_scan_f32: workspace not 16-byte aligned");
+    NT2G_REACH(x); NT2G_REACH(out); NT2G_REACH(workspace);
+    return launch_scan(x, lo, inner, hi, op, precision, workspace, workspace_bytes, out, (cudaStream_t)stream);
+}
+
 extern "C" nt2g_status nt2g_host_access(int32_t *pageable)
 {
     NT2G_CHECK_ARG(pageable != nullptr, "nt2g_host_access: pageable is NULL");

@@ -24,6 +24,7 @@
 // with 128-bit loads) over chunks of the fold range.  With more than one
 // chunk per output, partials go to the caller's workspace and a second kernel
 // combines them in order, so results are deterministic for a given shape.
+#include "nt2g_accum.cuh"
 #include "nt2g_common.cuh"
 #include "nt2g_internal.h"
 
@@ -38,25 +39,6 @@ __host__ __device__ constexpr bool fold_is_sum(int op)
 {
     return op == NT2G_FOLD_SUM || op == NT2G_FOLD_MEAN || op == NT2G_FOLD_ASUM1 || op == NT2G_FOLD_ASUM2 ||
            op == NT2G_FOLD_NORM2;
-}
-
-// --------------------------------------------------------- accumulators --
-// Compensated sum: value = s + c, c collecting the exact rounding errors.
-struct CSum {
-    float s, c;
-};
-__device__ __forceinline__ void csum_add(CSum &a, float v)
-{
-    const float s = __fadd_rn(a.s, v);
-    const float bb = __fsub_rn(s, a.s);
-    const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bb)), __fsub_rn(v, bb));
-    a.s = s;
-    a.c = __fadd_rn(a.c, e);
-}
-__device__ __forceinline__ void csum_merge(CSum &a, const CSum &b)
-{
-    csum_add(a, b.s);
-    a.c = __fadd_rn(a.c, b.c);
 }
 
 // max/min in NT2's order: the fold keeps acc unless x is strictly better, so
@@ -142,15 +124,6 @@ template <int OP> __device__ __forceinline__ float finish_double(double t, int64
 }
 
 // ------------------------------------------- warp-shuffle merges (fast) --
-__device__ __forceinline__ CSum warp_csum(CSum a)
-{
-#pragma unroll
-    for (int off = 16; off; off >>= 1) {
-        CSum b{__shfl_down_sync(0xffffffffu, a.s, off), __shfl_down_sync(0xffffffffu, a.c, off)};
-        csum_merge(a, b);
-    }
-    return a;
-}
 __device__ __forceinline__ double warp_prod(double a)
 {
 #pragma unroll

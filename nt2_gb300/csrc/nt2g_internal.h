@@ -82,6 +82,9 @@ nt2g_status launch_map(int fn, const float *x, float *y, int64_t n, int precisio
 nt2g_status launch_interp(const DProgram &prog, const DArgs &args, int64_t count, int precision,
                           cudaStream_t st);
 nt2g_status fold_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
+nt2g_status scan_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
+nt2g_status launch_scan(const float *x, int64_t lo, int64_t inner, int64_t hi, int op, int precision, void *ws,
+                        size_t ws_bytes, float *out, cudaStream_t st);
 nt2g_status launch_fold(const float *x, int64_t lo, int64_t inner, int64_t hi, int op, int precision, void *ws,
                         size_t ws_bytes, float *out, int64_t *index, cudaStream_t st);
 

@@ -202,6 +202,8 @@ int main(int argc, char **argv)
             save(dir + "mean1.bin", nt2::mean(A, 1));
             save(dir + "norm2_2.bin", nt2::norm2(A, 2));
             save(dir + "hsum1.bin", nt2::sum(h, 1));  // a host table folded in place (or staged)
+            save(dir + "cumsum1.bin", nt2::cumsum(A, 1));
+            save(dir + "cummax2.bin", nt2::cummax(A, 2));
             std::int64_t imax = 0, imin = 0;
             const float gmax = nt2::globalmax(A, imax), gmin = nt2::globalmin(h, imin);
             std::printf("globalmax %.9g %lld\nglobalmin %.9g %lld\nglobalmean %.9g\nglobalnorm2 %.9g\n"

@@ -825,6 +825,41 @@ template <class Site> float globalmean(const table<float, Site> &t) { return det
 template <class Site> float globalasum1(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ASUM1); }
 template <class Site> float globalasum2(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ASUM2); }
 template <class Site> float globalnorm2(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_NORM2); }
+// cumsum(t, dim), cumprod, cummax, cummin: tables of the shape of t
+namespace detail {
+template <class Site> inline table<float, Site> scan_dim(const table<float, Site> &t, int dim, int op)
+{
+    if (dim < 1 || dim > 4) throw gpu_error(NT2G_ERR_INVALID, "cumulative dimension out of range");
+    const fold_shape f = split(t.extent(), dim);
+    table<float, Site> r(t.extent());
+    auto run = [&](const float *x, float *o) {
+        std::size_t b = 0;
+        check(nt2g_scan_workspace_size(f.lo, f.inner, f.hi, &b), "scan workspace");
+        device_buffer ws(b);
+        check(nt2g_scan_f32(x, f.lo, f.inner, f.hi, op, options().precision, ws.p, b, o, options().stream), "scan");
+        check(nt2g_stream_synchronize(options().stream), "scan");
+    };
+    if (table<float, Site>::on_device || host_in_place()) {
+        run(t.data(), r.data());
+    } else {
+        table<float, device_> dt(t.extent()), dr(t.extent());
+        dt = t;
+        run(dt.data(), dr.data());
+        r = dr;
+    }
+    return r;
+}
+}  // namespace detail
+template <class Site> table<float, Site> cumsum(const table<float, Site> &t, int dim) { return detail::scan_dim(t, dim, NT2G_SCAN_SUM); }
+template <class Site> table<float, Site> cumprod(const table<float, Site> &t, int dim) { return detail::scan_dim(t, dim, NT2G_SCAN_PROD); }
+template <class Site> table<float, Site> cummax(const table<float, Site> &t, int dim) { return detail::scan_dim(t, dim, NT2G_SCAN_MAX); }
+template <class Site> table<float, Site> cummin(const table<float, Site> &t, int dim) { return detail::scan_dim(t, dim, NT2G_SCAN_MIN); }
+// cumsum(t): along the first non-singleton dimension
+template <class Site> table<float, Site> cumsum(const table<float, Site> &t)
+{
+    return detail::scan_dim(t, detail::first_non_singleton(t.extent()), NT2G_SCAN_SUM);
+}
+
 // sum(a) of a table with more than one non-singleton dimension folds the first of them
 template <class Site> table<float, Site> sum_first(const table<float, Site> &t)
 {

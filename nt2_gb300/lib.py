@@ -98,6 +98,8 @@ _SIGNATURES = {
     "nt2g_host_access": (_I32, [ctypes.POINTER(_I32)]),
     "nt2g_fold_workspace_size": (_I32, [_I64, _I64, _I64, ctypes.POINTER(ctypes.c_size_t)]),
     "nt2g_fold_f32": (_I32, [_VP, _I64, _I64, _I64, _I32, _I32, _VP, ctypes.c_size_t, _VP, _VP, _VP]),
+    "nt2g_scan_workspace_size": (_I32, [_I64, _I64, _I64, ctypes.POINTER(ctypes.c_size_t)]),
+    "nt2g_scan_f32": (_I32, [_VP, _I64, _I64, _I64, _I32, _I32, _VP, ctypes.c_size_t, _VP, _VP]),
     "nt2g_device_alloc": (_I32, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "nt2g_device_free": (_I32, [_VP]),
     "nt2g_memcpy": (_I32, [_VP, _VP, ctypes.c_size_t, _I32, _VP]),
@@ -202,6 +204,22 @@ def fold(x, lo, inner, hi, op, precision=PREC_FAST, index=False, stream=None):
     check(load().nt2g_fold_f32(_ptr(x), lo, inner, hi, FOLD[op], precision, _ptr(ws), ws.numel(), _ptr(out),
                                _ptr(idx), _stream(stream)))
     return (out, idx) if index else out
+
+
+SCAN = {"sum": 0, "prod": 1, "max": 2, "min": 3}
+
+
+def scan(x, lo, inner, hi, op, precision=PREC_FAST, out=None, stream=None):
+    """Cumulative op of x viewed as [lo, inner, hi] along inner (cumsum, cumprod,
+    cummax, cummin); out may be x."""
+    import torch
+    nb = ctypes.c_size_t()
+    check(load().nt2g_scan_workspace_size(lo, inner, hi, ctypes.byref(nb)))
+    ws = torch.empty(max(nb.value, 16), dtype=torch.uint8, device=x.device)
+    out = torch.empty_like(x) if out is None else out
+    check(load().nt2g_scan_f32(_ptr(x), lo, inner, hi, SCAN[op], precision, _ptr(ws), ws.numel(), _ptr(out),
+                               _stream(stream)))
+    return out
 
 
 class Reducer:

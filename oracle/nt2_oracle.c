@@ -643,6 +643,55 @@ EXPORT void o_fold_ref(const float *x, int64_t lo, int64_t inner, int64_t hi, in
     }
 }
 
+/* Cumulative functions, the table viewed as [lo, inner, hi]: each segment in
+ * order from the neutral element, summary = bop(summary, x); out = summary
+ * (core/swar/include/nt2/core/functions/details/scan_step.hpp:27-43).
+ * op: 0 cumsum, 1 cumprod, 2 cummax, 3 cummin. */
+EXPORT void o_scan_nt2_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int op, float *out, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int64_t s = 0; s < lo * hi; ++s) {
+        const int64_t h = s / lo, l = s - h * lo;
+        const int64_t base = l + lo * inner * h;
+        float acc = op == 1 ? 1.0f : op == 2 ? -INFINITY : op == 3 ? INFINITY : 0.0f;
+        for (int64_t k = 0; k < inner; ++k) {
+            const float v = x[base + lo * k];
+            switch (op) {
+            case 1: acc = acc * v; break;
+            case 2: acc = (acc > v) ? acc : v; break;
+            case 3: acc = (acc < v) ? acc : v; break;
+            default: acc = acc + v; break;
+            }
+            out[base + lo * k] = acc;
+        }
+    }
+}
+
+/* Exact prefix sums (superaccumulator), rounded to double, for the fast
+ * policy's cumsum; |prefix| bound: running sum of |x|. */
+EXPORT void o_cumsum_exact(const float *x, int64_t lo, int64_t inner, int64_t hi, double *out, double *abs_run,
+                           int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (int64_t s = 0; s < lo * hi; ++s) {
+        const int64_t h = s / lo, l = s - h * lo;
+        const int64_t base = l + lo * inner * h;
+        superacc a;
+        memset(&a, 0, sizeof a);
+        double as = 0.0;
+        for (int64_t k = 0; k < inner; ++k) {
+            const double v = x[base + lo * k];
+            acc_add(&a, v);
+            acc_norm(&a);
+            as += fabs(v);
+            out[base + lo * k] = acc_value(a);
+            abs_run[base + lo * k] = as;
+        }
+    }
+}
+
 /* NT2 grain for transform on Linux without cpuid: top_cache_size(2) reads
  * cache_sizes_[2], which the sysconf path fills with the L3 size in bytes
  * (modules/sdk/config/include/nt2/sdk/config/details/cache.hpp:26-39,

@@ -65,6 +65,8 @@ def lib():
         L.o_sum_plain_f32.argtypes = [_P, _P, _I64, ctypes.c_int]
         L.o_fold_nt2_f32.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, ctypes.c_int]
         L.o_fold_ref.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, _P, ctypes.c_int]
+        L.o_scan_nt2_f32.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, ctypes.c_int]
+        L.o_cumsum_exact.argtypes = [_P, _I64, _I64, _I64, _P, _P, ctypes.c_int]
         L.o_globalsum_f32.restype = ctypes.c_float
         L.o_globalsum_f32.argtypes = [_P, _I64]
         L.o_exact_sum.restype = ctypes.c_double
@@ -231,6 +233,26 @@ def fold_ref(x, lo, inner, hi, op, nthreads=None):
     idx = np.empty(lo * hi, np.int64)
     lib().o_fold_ref(_p(x), lo, inner, hi, FOLD_OPS[op], _p(out), _p(asum), _p(idx), nthreads or threads())
     return out, asum, idx
+
+
+SCAN_OPS = {"sum": 0, "prod": 1, "max": 2, "min": 3}
+
+
+def scan_nt2(x, lo, inner, hi, op, nthreads=None):
+    """NT2's in-order cumulative op of x viewed as [lo, inner, hi]."""
+    x = _f32(x)
+    out = np.empty(x.size, np.float32)
+    lib().o_scan_nt2_f32(_p(x), lo, inner, hi, SCAN_OPS[op], _p(out), nthreads or threads())
+    return out
+
+
+def cumsum_exact(x, lo, inner, hi, nthreads=None):
+    """Exact prefix sums (double) and the running sum of |x|."""
+    x = _f32(x)
+    out = np.empty(x.size, np.float64)
+    ab = np.empty(x.size, np.float64)
+    lib().o_cumsum_exact(_p(x), lo, inner, hi, _p(out), _p(ab), nthreads or threads())
+    return out, ab
 
 
 def exact_sum(x, y=None, nthreads=None):

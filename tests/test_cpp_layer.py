@@ -136,6 +136,14 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
         else:
             ref, _, _ = oracle.fold_ref(a, *shape, op)
             assert (np.abs(got - ref) <= np.spacing(np.abs(ref).astype(np.float32))).all(), name
+    c1 = np.fromfile(tmp_path / "cumsum1.bin", np.float32)
+    c2 = np.fromfile(tmp_path / "cummax2.bin", np.float32)
+    assert _eq(c2, oracle.scan_nt2(a, m, n, 1, "max"))
+    if prec == "1":
+        assert _eq(c1, oracle.scan_nt2(a, 1, m, n, "sum"))
+    else:
+        ref, absrun = oracle.cumsum_exact(a, 1, m, n)
+        assert (np.abs(c1 - ref) <= np.spacing(np.abs(ref).astype(np.float32)) + 1e-12 * absrun).all()
     gmax, imax = oracle.fold_nt2(a, 1, m * n, 1, "max")
     gmin, imin = oracle.fold_nt2(a, 1, m * n, 1, "min")
     assert np.float32(glob["globalmax"][0]) == gmax[0] and int(glob["globalmax"][1]) == imax[0] + 1
