@@ -383,6 +383,9 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 4) return normcdf<P>(a);
     if (FN == 5) return fastnormcdf<P>(a);
     if (FN == 6) return P::sqrt(a);
+    if (FN == 8) return exp2<P>(a);
+    if (FN == 9) return exp10<P>(a);
+    if (FN == 10) return expm1<P>(a);
     float p, q;
     normcdf_pair<P>(a, p, q);
     return q;
@@ -408,6 +411,9 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 4: NT2G_MAP(4); break;
     case 5: NT2G_MAP(5); break;
     case 6: NT2G_MAP(6); break;
+    case 8: NT2G_MAP(8); break;
+    case 9: NT2G_MAP(9); break;
+    case 10: NT2G_MAP(10); break;
     default: NT2G_MAP(7); break;
     }
 #undef NT2G_MAP
@@ -443,6 +449,9 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_LOG1P: return log1p<P>(a);
     case NT2G_OP_ERFC: return erfc<P>(a);
     case NT2G_OP_NORMCDF: return normcdf<P>(a);
+    case NT2G_OP_EXP2: return exp2<P>(a);
+    case NT2G_OP_EXP10: return exp10<P>(a);
+    case NT2G_OP_EXPM1: return expm1<P>(a);
     default: return fastnormcdf<P>(a);
     }
 }

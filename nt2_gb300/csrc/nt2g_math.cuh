@@ -146,6 +146,15 @@ NT2G_HD float horner(float x, float acc, float c, R... rest)
 #define NT2G_MLOGTWO2NMB 0xc17f1402u
 #define NT2G_TWOTHIRD    0x3f2aaaabu
 #define NT2G_INVSQRT_2PI 0x3ecc422au
+#define NT2G_MAXLOG2     0x42fe0000u
+#define NT2G_MINLOG2     0xc2fe0000u
+#define NT2G_MAXLOG10    0x4218ec59u
+#define NT2G_MINLOG10    0xc2179999u
+#define NT2G_LOG_2       0x3f317218u
+#define NT2G_INVLOG10_2  0x40549a78u
+#define NT2G_LOG10_2HI   0x3e9a0000u
+#define NT2G_LOG10_2LO   0x39826a14u
+#define NT2G_LOGEPS      0xc17f1402u
 
 NT2G_HD float f_inf() { return bits_f(0x7f800000u); }
 NT2G_HD float f_nan() { return bits_f(0x7fc00000u); }
@@ -193,6 +202,92 @@ template <class P> NT2G_HD float exp(float a0)
     r = (a0 >= bits_f(NT2G_MAXLOG)) ? f_inf() : r;
     r = (a0 <= bits_f(NT2G_MINLOG)) ? 0.0f : r;
     return is_nan(a0) ? a0 : r;
+}
+
+// 2^k for k in [-126, 127] built in the exponent field (expo_scale.hpp:27-35)
+NT2G_HD float pow2i(float k) { return bits_f((uint32_t)((int32_t)k + 127) << 23); }
+
+// ----------------------------------------------------------- exp2, exp10 --
+// NT2: the float exponential driver of scalar/impl/expo/expo_base.hpp:55-69
+// with the two_ / ten_tag reductions of f_expo_reduction.hpp:88-126, 129-168:
+//   exp2:  k = round2even(x), r = x - k, 2^r = 1 + (P5(r) r^2 + r ln2);
+//   exp10: k = round2even(x log2(10)), r = x - k log10(2)hi - k log10(2)lo,
+//          10^r = 1 + P6(r) r;
+// each result scaled by 2^k; +inf from Maxlog2 / Maxlog10, 0 at Minlog2 /
+// Minlog10 and below.  Fast: the same steps with FMAs, specials by select.
+template <class P> NT2G_HD float exp2(float a0)
+{
+    if (P::exact) {
+        if (a0 >= bits_f(NT2G_MAXLOG2)) return f_inf();
+        if (a0 <= bits_f(NT2G_MINLOG2)) return 0.0f;
+        if (is_nan(a0)) return a0;
+    }
+    const float k = rintf(a0);
+    const float x = P::sub(a0, k);
+    const float y = horner<P>(x, bits_f(0x3922c8c4u), bits_f(0x3ab01218u), bits_f(0x3c1d9422u),
+                              bits_f(0x3d6356ebu), bits_f(0x3e75fdf1u));
+    const float c = P::add(P::fma(y, P::mul(x, x), P::mul(x, bits_f(NT2G_LOG_2))), 1.0f);
+    if (P::exact) return P::mul(c, pow2i(k));
+    float r = P::mul(c, pow2i(fminf(fmaxf(k, -127.0f), 127.0f)));
+    r = (a0 >= bits_f(NT2G_MAXLOG2)) ? f_inf() : r;
+    r = (a0 <= bits_f(NT2G_MINLOG2)) ? 0.0f : r;
+    return is_nan(a0) ? a0 : r;
+}
+
+template <class P> NT2G_HD float exp10(float a0)
+{
+    if (P::exact) {
+        if (a0 >= bits_f(NT2G_MAXLOG10)) return f_inf();
+        if (a0 <= bits_f(NT2G_MINLOG10)) return 0.0f;
+        if (is_nan(a0)) return a0;
+    }
+    const float k = rintf(P::mul(bits_f(NT2G_INVLOG10_2), a0));
+    float x = P::fma(-k, bits_f(NT2G_LOG10_2HI), a0);
+    x = P::sub(x, P::mul(k, bits_f(NT2G_LOG10_2LO)));
+    const float y = horner<P>(x, bits_f(0x3e54dff1u), bits_f(0x3f0aacefu), bits_f(0x3f95eb4cu),
+                              bits_f(0x400237dau), bits_f(0x4029a926u), bits_f(0x40135d8eu));
+    const float c = P::add(P::mul(y, x), 1.0f);
+    if (P::exact) return P::mul(c, pow2i(k));
+    float r = P::mul(c, pow2i(fminf(fmaxf(k, -127.0f), 127.0f)));
+    r = (a0 >= bits_f(NT2G_MAXLOG10)) ? f_inf() : r;
+    r = (a0 <= bits_f(NT2G_MINLOG10)) ? 0.0f : r;
+    return is_nan(a0) ? a0 : r;
+}
+
+// ----------------------------------------------------------------- expm1 --
+// NT2 (scalar/expm1.hpp:33-41, details/expm1_kernel.hpp:49-73): NaN -> NaN,
+// x < Logeps -> -1, x > Maxlog -> +inf, else k = round2even(x/ln2), r by
+// Cody-Waite, hx = r/2, hxs = r*hx, r1 = 1 + hxs*(c2 + hxs*c1),
+// t = 3 - r1*hx, e = hxs*((r1 - t)/(6 - r*t)), e = r*e - hxs,
+// y = (1 - 2^-k) - (e - r), expm1 = y * 2^k.
+template <class P> NT2G_HD float expm1(float a0)
+{
+    if (P::exact) {
+        if (is_nan(a0)) return f_nan();
+        if (a0 < bits_f(NT2G_LOGEPS)) return -1.0f;
+        if (a0 > bits_f(NT2G_MAXLOG)) return f_inf();
+    }
+    // out-of-range arguments take a harmless value through the kernel (fast: selected away)
+    const float a = P::exact ? a0 : fminf(fmaxf(a0, bits_f(NT2G_LOGEPS)), bits_f(NT2G_MAXLOG));
+    const float k = rintf(P::mul(bits_f(NT2G_INVLOG_2), a));
+    float x = P::fma(-k, bits_f(NT2G_LOG_2HI), a);
+    x = P::fma(-k, bits_f(NT2G_LOG_2LO), x);
+    const float hx = P::mul(x, 0.5f);
+    const float hxs = P::mul(x, hx);
+    const float r1 = horner<P>(hxs, bits_f(0x3acf6db4u), bits_f(0xbd08887fu), bits_f(0x3f800000u));
+    const float t = P::fma(-r1, hx, 3.0f);
+    float e = P::mul(hxs, P::div(P::sub(r1, t), P::fma(-x, t, 6.0f)));
+    e = P::fma(x, e, -hxs);
+    const int32_t ik = (int32_t)k;
+    const float two2mk = bits_f((uint32_t)(127 - ik) << 23);
+    const float y = P::sub(P::sub(1.0f, two2mk), P::sub(e, x));
+    float r = P::mul(y, pow2i(k));  // fast_ldexp: y * 2^k (boost/simd/ieee/functions/scalar/fast_ldexp.hpp)
+    if (!P::exact) {
+        r = (a0 < bits_f(NT2G_LOGEPS)) ? -1.0f : r;
+        r = (a0 > bits_f(NT2G_MAXLOG)) ? f_inf() : r;
+        r = is_nan(a0) ? f_nan() : r;
+    }
+    return r;
 }
 
 // ------------------------------------------------------------------ log --

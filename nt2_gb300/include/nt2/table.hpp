@@ -588,6 +588,9 @@ NT2G_UNARY(log1p, NT2G_OP_LOG1P)
 NT2G_UNARY(erfc, NT2G_OP_ERFC)
 NT2G_UNARY(normcdf, NT2G_OP_NORMCDF)
 NT2G_UNARY(fastnormcdf, NT2G_OP_FASTNORMCDF)
+NT2G_UNARY(exp2, NT2G_OP_EXP2)
+NT2G_UNARY(exp10, NT2G_OP_EXP10)
+NT2G_UNARY(expm1, NT2G_OP_EXPM1)
 #undef NT2G_UNARY
 
 // Functors on plain scalars evaluate at once, in float, with NT2's scalar

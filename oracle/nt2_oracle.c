@@ -171,8 +171,72 @@ EXPORT float o_fastnormcdf(float a0)
     return (a0 > 0.0f) ? 1.0f - w : w;
 }
 
+/* ------------------------------------------------- exp2, exp10, expm1 --
+ * NT2's float algorithms, every operation rounded: the two_tag and ten_tag
+ * reductions (EXP/scalar/impl/expo/f_expo_reduction.hpp:88-126, 129-168)
+ * under the float driver expo_base.hpp:55-69 and the scale expo_scale.hpp:34
+ * (a multiply by the bits (k+127)<<23); expm1 per EXP/scalar/expm1.hpp:33-41
+ * and EXP/details/expm1_kernel.hpp:49-73. */
+static float o_pow2i(float k) { return bf((uint32_t)((int32_t)k + 127) << 23); }
+
+EXPORT float o_exp2(float a0)
+{
+    if (a0 >= bf(0x42fe0000u)) return INFINITY;
+    if (a0 <= bf(0xc2fe0000u)) return 0.0f;
+    if (a0 != a0) return a0;
+    const float k = rintf(a0);
+    const float x = a0 - k;
+    float y = bf(0x3922c8c4u);
+    y = y * x + bf(0x3ab01218u);
+    y = y * x + bf(0x3c1d9422u);
+    y = y * x + bf(0x3d6356ebu);
+    y = y * x + bf(0x3e75fdf1u);
+    const float c = (y * (x * x) + x * bf(0x3f317218u)) + 1.0f;
+    return c * o_pow2i(k);
+}
+
+EXPORT float o_exp10(float a0)
+{
+    if (a0 >= bf(0x4218ec59u)) return INFINITY;
+    if (a0 <= bf(0xc2179999u)) return 0.0f;
+    if (a0 != a0) return a0;
+    const float k = rintf(bf(0x40549a78u) * a0);
+    float x = a0 - k * bf(0x3e9a0000u);
+    x = x - k * bf(0x39826a14u);
+    float y = bf(0x3e54dff1u);
+    y = y * x + bf(0x3f0aacefu);
+    y = y * x + bf(0x3f95eb4cu);
+    y = y * x + bf(0x400237dau);
+    y = y * x + bf(0x4029a926u);
+    y = y * x + bf(0x40135d8eu);
+    return (y * x + 1.0f) * o_pow2i(k);
+}
+
+EXPORT float o_expm1(float a0)
+{
+    if (a0 != a0) return bf(0x7fc00000u);
+    if (a0 < bf(0xc17f1402u)) return -1.0f;
+    if (a0 > bf(C_MAXLOG)) return INFINITY;
+    const float k = rintf(bf(C_INVLOG_2) * a0);
+    float x = a0 - k * bf(C_LOG_2HI);
+    x = x - k * bf(C_LOG_2LO);
+    const float hx = x * 0.5f;
+    const float hxs = x * hx;
+    float r1 = bf(0x3acf6db4u);
+    r1 = r1 * hxs + bf(0xbd08887fu);
+    r1 = r1 * hxs + 1.0f;
+    const float t = 3.0f - r1 * hx;
+    float e = hxs * ((r1 - t) / (6.0f - x * t));
+    e = x * e - hxs;
+    const int32_t ik = (int32_t)k;
+    const float two2mk = bf((uint32_t)(127 - ik) << 23);
+    const float y = (1.0f - two2mk) - (e - x);
+    return y * o_pow2i(k);
+}
+
 /* ------------------------------------------------- elementwise maps ---- */
-enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT };
+enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT, FN_EXP2 = 8, FN_EXP10,
+       FN_EXPM1 };
 
 EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
 {
@@ -185,6 +249,9 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_ERFC: y[i] = o_erfc(a); break;
         case FN_NORMCDF: y[i] = o_normcdf(a); break;
         case FN_FASTNORMCDF: y[i] = o_fastnormcdf(a); break;
+        case FN_EXP2: y[i] = o_exp2(a); break;
+        case FN_EXP10: y[i] = o_exp10(a); break;
+        case FN_EXPM1: y[i] = o_expm1(a); break;
         default: y[i] = sqrtf(a); break;
         }
     }
@@ -202,6 +269,9 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_ERFC: y[i] = erfc(a); break;
         case FN_NORMCDF:
         case FN_FASTNORMCDF: y[i] = 0.5 * erfc(-a / sqrt(2.0)); break;
+        case FN_EXP2: y[i] = exp2(a); break;
+        case FN_EXP10: y[i] = pow(10.0, a); break;
+        case FN_EXPM1: y[i] = expm1(a); break;
         default: y[i] = sqrt(a); break;
         }
     }

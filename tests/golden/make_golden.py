@@ -25,6 +25,9 @@ SOURCES = [
     ("modules/core/euler/unit/scalar/erfc.cpp", 42, 53),
     ("modules/core/statistics/unit/scalar/normcdf.cpp", 31, 36),
     ("modules/core/statistics/unit/scalar/fastnormcdf.cpp", 26, 31),
+    ("modules/core/exponential/unit/scalar/exp2.cpp", 42, 48),
+    ("modules/core/exponential/unit/scalar/exp10.cpp", 40, 46),
+    ("modules/core/exponential/unit/scalar/expm1.cpp", 40, 46),
 ]
 
 E = float(np.float32(math.e))
@@ -45,6 +48,15 @@ def _value(expr):
     m = re.fullmatch(r"nt2::One<\w+>\(\)\s*/\s*nt2::Exp_1<\w+>\(\)", expr)
     if m:
         return float(np.float32(1.0) / np.float32(E))
+    m = re.fullmatch(r"nt2::One<\w+>\(\)\s*/\s*nt2::Exp_1<\w+>\(\)\s*-\s*nt2::One<\w+>\(\)", expr)
+    if m:  # float arithmetic as the test writes it
+        return float(np.float32(np.float32(1.0) / np.float32(E)) - np.float32(1.0))
+    m = re.fullmatch(r"nt2::Exp_1<\w+>\(\)\s*-\s*nt2::One<\w+>\(\)", expr)
+    if m:
+        return float(np.float32(E) - np.float32(1.0))
+    m = re.fullmatch(r"nt2::One<\w+>\(\)\s*/\s*10", expr)
+    if m:
+        return float(np.float32(1.0) / np.float32(10.0))
     raise ValueError(f"unhandled NT2 constant spelling: {expr!r}")
 
 

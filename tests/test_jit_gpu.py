@@ -29,7 +29,8 @@ def _bits_equal(a, b):
     return bool(np.array_equal(a, b))
 
 
-_UNARY_F = ["NEG", "ABS", "SQR", "SQRT", "REC", "EXP", "LOG", "LOG1P", "ERFC", "NORMCDF", "FASTNORMCDF"]
+_UNARY_F = ["NEG", "ABS", "SQR", "SQRT", "REC", "EXP", "LOG", "LOG1P", "ERFC", "NORMCDF", "FASTNORMCDF", "EXP2",
+            "EXP10", "EXPM1"]
 _BINARY_F = ["ADD", "SUB", "MUL", "DIV", "MIN", "MAX"]
 _CMP = ["LT", "GT", "LE", "GE", "EQ", "NE"]
 

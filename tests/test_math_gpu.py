@@ -15,12 +15,15 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
 SPECIALS = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -1.0, 1e-40, -1e-40, 1e-45, 3e38, -3e38, 0.5,
-                     2 / 3, -2 / 3, 88.3763, -88.3763, 88.7, -103.0, 9.3, 13.2, -13.2, 0.6666666], np.float32)
+                     2 / 3, -2 / 3, 88.3763, -88.3763, 88.7, -103.0, 9.3, 13.2, -13.2, 0.6666666,
+                     127.0, -127.0, 126.6, -126.6, 128.0, 38.23, -37.9, 38.5, -38.5, -15.9424, -15.95, -17.0],
+                    np.float32)
 
 # domain of each function for the accuracy sweep (finite FP64 reference above
 # the float normal range)
 DOMAINS = dict(exp=(-87.3, 88.3), log=(1e-30, 1e30), log1p=(-0.999, 1e4), erfc=(-10, 9.2), normcdf=(-13, 9),
-               fastnormcdf=(-9, 9), sqrt=(0, 1e30))
+               fastnormcdf=(-9, 9), sqrt=(0, 1e30), exp2=(-126, 126.99), exp10=(-37.8, 38.2),
+               expm1=(-20, 88.37))
 
 
 def _sweep(fn, n=1 << 22, seed=5):
@@ -46,7 +49,8 @@ def _gpu_map(lib, dev, fn, x, prec):
     return ty.cpu().numpy()
 
 
-@pytest.mark.parametrize("fn", ["exp", "log", "log1p", "erfc", "normcdf", "fastnormcdf", "sqrt"])
+@pytest.mark.parametrize("fn", ["exp", "log", "log1p", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10",
+                                "expm1"])
 def test_nt2_policy_bit_exact(lib, dev, oracle, fn):
     x = _inputs(fn)
     got = _gpu_map(lib, dev, fn, x, lib.PREC_NT2)
@@ -56,7 +60,7 @@ def test_nt2_policy_bit_exact(lib, dev, oracle, fn):
 
 
 @pytest.mark.parametrize("fn,tol", [("exp", 1.5), ("log", 1.5), ("log1p", 2.0), ("erfc", 4.0), ("normcdf", 4.0),
-                                    ("sqrt", 0.5)])
+                                    ("sqrt", 0.5), ("exp2", 1.5), ("exp10", 2.0), ("expm1", 2.0)])
 def test_fast_policy_within_4ulp_of_fp64(lib, dev, oracle, fn, tol):
     """Accuracy over each function's sweep domain; the special values
     (including exp's +inf from NT2's Maxlog = 88.3763 on, as NT2) are
@@ -87,6 +91,7 @@ def test_fast_normcdf_pair_complement(lib, dev, oracle):
 
 @pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
 def test_golden_values_on_gpu(lib, dev, prec):
-    for rec in [r for r in GOLDEN if r["fn"] in ("exp", "log", "erfc", "normcdf", "fastnormcdf")]:
+    for rec in [r for r in GOLDEN if r["fn"] in ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10",
+                                                  "expm1")]:
         got = _gpu_map(lib, dev, rec["fn"], np.array([rec["x"]], np.float32), prec)[0]
         assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (rec, got)

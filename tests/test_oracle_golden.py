@@ -11,7 +11,7 @@ import pytest
 from helpers import nt2_ulpdist, std_ulp, reduction_ill
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
-FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf")
+FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
@@ -72,6 +72,20 @@ def test_oracle_accuracy_profile(oracle):
     x = np.linspace(-9, 9, 400001, dtype=np.float32)
     e = std_ulp(oracle.map_f32("erfc", x), oracle.map_f64("erfc", x))
     assert 4 < e.max() < 200
+    # exp2/exp10/expm1 inside NT2's float range (Minlog2, Maxlog2) = (-127, 127),
+    # (Minlog10, Maxlog10) ~ (-37.9, 38.23), expm1 up to Maxlog ~ 88.38.  NT2
+    # saturates to 0 / inf outside it (exp2(127) is inf although representable)
+    # and its scale step (a multiply by 2^k) flushes results below 2^-126.5 to 0.
+    # expm1 reaches 2 ulps just above Logeps, where the result is -1 + 2^-23.
+    for fn, lo, hi, tol in (("exp2", -126, 126.99, 1.5), ("exp10", -37.8, 38.2, 1.5),
+                            ("expm1", -20, 88.37, 2.0)):
+        x = np.linspace(lo, hi, 400001, dtype=np.float32)
+        assert std_ulp(oracle.map_f32(fn, x), oracle.map_f64(fn, x)).max() <= tol, fn
+    x = np.concatenate([np.geomspace(1e-30, 1, 20001), -np.geomspace(1e-30, 1, 20001)]).astype(np.float32)
+    assert std_ulp(oracle.map_f32("expm1", x), oracle.map_f64("expm1", x)).max() <= 1.5
+    assert oracle.map_f32("exp2", np.float32([127.5, -127.5, 200, -200])).tolist() == [np.inf, 0, np.inf, 0]
+    assert oracle.map_f32("exp10", np.float32([38.3, -38, 50, -50])).tolist() == [np.inf, 0, np.inf, 0]
+    assert oracle.map_f32("expm1", np.float32([88.5, -17.5, -1e30])).tolist() == [np.inf, -1, -1]
 
 
 def test_sigmadelta_oracle_semantics(oracle):
