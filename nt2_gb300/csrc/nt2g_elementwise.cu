@@ -386,6 +386,8 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 8) return exp2<P>(a);
     if (FN == 9) return exp10<P>(a);
     if (FN == 10) return expm1<P>(a);
+    if (FN == 11) return log2<P>(a);
+    if (FN == 12) return log10<P>(a);
     float p, q;
     normcdf_pair<P>(a, p, q);
     return q;
@@ -414,6 +416,8 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 8: NT2G_MAP(8); break;
     case 9: NT2G_MAP(9); break;
     case 10: NT2G_MAP(10); break;
+    case 11: NT2G_MAP(11); break;
+    case 12: NT2G_MAP(12); break;
     default: NT2G_MAP(7); break;
     }
 #undef NT2G_MAP
@@ -452,6 +456,8 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_EXP2: return exp2<P>(a);
     case NT2G_OP_EXP10: return exp10<P>(a);
     case NT2G_OP_EXPM1: return expm1<P>(a);
+    case NT2G_OP_LOG2: return log2<P>(a);
+    case NT2G_OP_LOG10: return log10<P>(a);
     default: return fastnormcdf<P>(a);
     }
 }

@@ -185,6 +185,8 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_EXP2: e = "nt2g::exp2<P>(" + A + ")"; break;
         case NT2G_OP_EXP10: e = "nt2g::exp10<P>(" + A + ")"; break;
         case NT2G_OP_EXPM1: e = "nt2g::expm1<P>(" + A + ")"; break;
+        case NT2G_OP_LOG2: e = "nt2g::log2<P>(" + A + ")"; break;
+        case NT2G_OP_LOG10: e = "nt2g::log10<P>(" + A + ")"; break;
         default: e = "nt2g::fastnormcdf<P>(" + A + ")"; break;
         }
         s += std::string(u ? "    unsigned v" : "    float v") + std::to_string(k) + "[4]; NT2G_L v" +

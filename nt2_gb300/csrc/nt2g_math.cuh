@@ -155,6 +155,11 @@ NT2G_HD float horner(float x, float acc, float c, R... rest)
 #define NT2G_LOG10_2HI   0x3e9a0000u
 #define NT2G_LOG10_2LO   0x39826a14u
 #define NT2G_LOGEPS      0xc17f1402u
+#define NT2G_LOG2_EM1    0x3ee2a8edu
+#define NT2G_LOG10_EHI   0x3ede0000u
+#define NT2G_LOG10_ELO   0x3a37b152u
+#define NT2G_MLOG2TWO2NMB  0xc1b80000u
+#define NT2G_MLOG10TWO2NMB 0xc0dd8edeu
 
 NT2G_HD float f_inf() { return bits_f(0x7f800000u); }
 NT2G_HD float f_nan() { return bits_f(0x7fc00000u); }
@@ -291,42 +296,91 @@ template <class P> NT2G_HD float expm1(float a0)
 }
 
 // ------------------------------------------------------------------ log --
-template <class P> NT2G_HD float log(float a0)
+// NT2's float logarithms (scalar/impl/logs/f_log.hpp:59-153) share one
+// reduction (f_kernel.hpp:43-75): a0 = 2^fe * (1 + x) with 1 + x in
+// [sqrt(1/2), sqrt(2)), x2 = x^2, y = P8(x) * x * x2.  Denormal arguments are
+// first scaled by 2^23 and the matching -23 log_b(2) is added back as t.
+struct LogParts { float fe, x, x2, y, t; };
+
+template <class P> NT2G_HD LogParts log_reduce(float a0, uint32_t mlog_two2nmb)
 {
-    if (P::exact) {
-        if (a0 == f_inf()) return a0;
-        if (a0 == 0.0f) return -f_inf();
-        if (is_nan(a0) || a0 < 0.0f) return f_nan();
-    }
-    float z = a0, t = 0.0f;
+    LogParts r;
+    float z = a0;
+    r.t = 0.0f;
     bool den = fabsf(z) < bits_f(NT2G_SMALLESTPOS);
     if (P::exact) {
-        if (den) { z = P::mul(z, bits_f(NT2G_TWOTONMB)); t = bits_f(NT2G_MLOGTWO2NMB); }
+        if (den) { z = P::mul(z, bits_f(NT2G_TWOTONMB)); r.t = bits_f(mlog_two2nmb); }
     } else {
         z = den ? P::mul(z, bits_f(NT2G_TWOTONMB)) : z;
-        t = den ? bits_f(NT2G_MLOGTWO2NMB) : 0.0f;
+        r.t = den ? bits_f(mlog_two2nmb) : 0.0f;
     }
     uint32_t u = f_bits(z);
     int32_t e = (int32_t)((u & 0x7f800000u) >> 23) - 126;
     float x = bits_f((u & ~0x7f800000u) | 0x3f000000u);
     bool lt = x < bits_f(NT2G_SQRT_2O_2);
-    float fe = lt ? P::add((float)e, -1.0f) : (float)e;
-    x = P::sub(lt ? P::add(x, x) : x, 1.0f);
-    float x2 = P::mul(x, x);
-    float y = horner<P>(x, bits_f(0xbda5dff0u), bits_f(0x3e0229f9u), bits_f(0xbe04d6b7u),
+    r.fe = lt ? P::add((float)e, -1.0f) : (float)e;
+    r.x = P::sub(lt ? P::add(x, x) : x, 1.0f);
+    r.x2 = P::mul(r.x, r.x);
+    float y = horner<P>(r.x, bits_f(0xbda5dff0u), bits_f(0x3e0229f9u), bits_f(0xbe04d6b7u),
                         bits_f(0x3e116e80u), bits_f(0xbe2a6aa0u), bits_f(0x3e4cd0a3u),
                         bits_f(0xbe800064u), bits_f(0x3eaaaaa9u));
-    y = P::mul(P::mul(y, x), x2);
-    y = P::fma(fe, bits_f(NT2G_LOG_2LO), y);
-    y = P::fma(-0.5f, x2, y);
-    float r = P::fma(bits_f(NT2G_LOG_2HI), fe, P::add(P::add(x, y), t));
-    if (!P::exact) {
-        r = (a0 == f_inf()) ? a0 : r;
-        r = (a0 == 0.0f) ? -f_inf() : r;
-        r = (is_nan(a0) || a0 < 0.0f) ? f_nan() : r;
-    }
+    r.y = P::mul(P::mul(y, r.x), r.x2);
     return r;
 }
+
+// The special values of every float logarithm: log_b(+inf) = +inf,
+// log_b(0) = -inf, NaN for NaN and negative arguments.
+template <class P> NT2G_HD float log_specials(float a0, float r)
+{
+    r = (a0 == f_inf()) ? a0 : r;
+    r = (a0 == 0.0f) ? -f_inf() : r;
+    return (is_nan(a0) || a0 < 0.0f) ? f_nan() : r;
+}
+
+#define NT2G_LOG_SPECIALS_EXACT(a0)                                   \
+    if (P::exact) {                                                   \
+        if (a0 == f_inf()) return a0;                                 \
+        if (a0 == 0.0f) return -f_inf();                              \
+        if (is_nan(a0) || a0 < 0.0f) return f_nan();                  \
+    }
+
+template <class P> NT2G_HD float log(float a0)
+{
+    NT2G_LOG_SPECIALS_EXACT(a0)
+    const LogParts k = log_reduce<P>(a0, NT2G_MLOGTWO2NMB);
+    float y = P::fma(k.fe, bits_f(NT2G_LOG_2LO), k.y);
+    y = P::fma(-0.5f, k.x2, y);
+    float r = P::fma(bits_f(NT2G_LOG_2HI), k.fe, P::add(P::add(k.x, y), k.t));
+    return P::exact ? r : log_specials<P>(a0, r);
+}
+
+// log2 (f_log.hpp:90-119): y += -x2/2, z = x*log2(e)-1 + y*(log2(e)-1),
+// log2 = ((z + y) + x) + fe (+ t)
+template <class P> NT2G_HD float log2(float a0)
+{
+    NT2G_LOG_SPECIALS_EXACT(a0)
+    const LogParts k = log_reduce<P>(a0, NT2G_MLOG2TWO2NMB);
+    const float y = P::fma(-0.5f, k.x2, k.y);
+    const float z = P::fma(k.x, bits_f(NT2G_LOG2_EM1), P::mul(y, bits_f(NT2G_LOG2_EM1)));
+    float r = P::add(P::add(P::add(P::add(z, y), k.x), k.fe), k.t);
+    return P::exact ? r : log_specials<P>(a0, r);
+}
+
+// log10 (f_log.hpp:121-153): with log10(e) = ehi + elo and log10(2) = 2hi + 2lo,
+// z = (x + y)*elo + y*ehi + x*ehi + fe*2hi, log10 = (z + t) + fe*2lo
+template <class P> NT2G_HD float log10(float a0)
+{
+    NT2G_LOG_SPECIALS_EXACT(a0)
+    const LogParts k = log_reduce<P>(a0, NT2G_MLOG10TWO2NMB);
+    const float y = P::fma(-0.5f, k.x2, k.y);
+    float z = P::mul(P::add(k.x, y), bits_f(NT2G_LOG10_ELO));
+    z = P::fma(y, bits_f(NT2G_LOG10_EHI), z);
+    z = P::fma(k.x, bits_f(NT2G_LOG10_EHI), z);
+    z = P::fma(k.fe, bits_f(NT2G_LOG10_2HI), z);
+    float r = P::fma(k.fe, bits_f(NT2G_LOG10_2LO), P::add(z, k.t));
+    return P::exact ? r : log_specials<P>(a0, r);
+}
+#undef NT2G_LOG_SPECIALS_EXACT
 
 // ---------------------------------------------------------------- log1p --
 template <class P> NT2G_HD float log1p(float a0)

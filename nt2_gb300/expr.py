@@ -1,7 +1,7 @@
 """A Python mirror of NT2's expression surface over device tables.
 
 ``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
-(exp, exp2, exp10, expm1, log, log1p, erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms,
+(exp, exp2, exp10, expm1, log, log2, log10, log1p, erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms,
 min, max, if_else, selinc, seldec, if_zero_else_one, adds) build an expression
 tree; ``assign(outs, exprs)`` is ``tie(outs...) = tie(exprs...)``: it lowers
 the trees to the SSA program of nt2g.h, compiles it once (cached by program
@@ -79,6 +79,7 @@ exp, log, log1p, erfc = _un("EXP"), _un("LOG"), _un("LOG1P"), _un("ERFC")
 normcdf, fastnormcdf, sqrt, rec = _un("NORMCDF"), _un("FASTNORMCDF"), _un("SQRT"), _un("REC")
 abs_ = _un("ABS")
 exp2, exp10, expm1 = _un("EXP2"), _un("EXP10"), _un("EXPM1")
+log2, log10 = _un("LOG2"), _un("LOG10")
 
 # Functors applied to plain numbers evaluate at once in float32 with NT2's
 # scalar semantics (each step rounded, no fusion), as NT2's scalar overloads

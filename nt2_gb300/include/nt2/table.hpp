@@ -591,6 +591,8 @@ NT2G_UNARY(fastnormcdf, NT2G_OP_FASTNORMCDF)
 NT2G_UNARY(exp2, NT2G_OP_EXP2)
 NT2G_UNARY(exp10, NT2G_OP_EXP10)
 NT2G_UNARY(expm1, NT2G_OP_EXPM1)
+NT2G_UNARY(log2, NT2G_OP_LOG2)
+NT2G_UNARY(log10, NT2G_OP_LOG10)
 #undef NT2G_UNARY
 
 // Functors on plain scalars evaluate at once, in float, with NT2's scalar

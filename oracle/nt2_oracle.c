@@ -99,24 +99,65 @@ EXPORT float o_exp(float a0)
 static const uint32_t LOG_P[8] = {0xbda5dff0, 0x3e0229f9, 0xbe04d6b7, 0x3e116e80,
                                   0xbe2a6aa0, 0x3e4cd0a3, 0xbe800064, 0x3eaaaaa9};
 
-EXPORT float o_log(float a0)
+/* The reduction every float logarithm shares (logs/f_kernel.hpp:43-75):
+ * a0 = 2^fe (1 + x), x2 = x*x, y = P8(x)*x*x2; denormals scaled by 2^23 first,
+ * with t = the matching -23 log_b(2) (f_log.hpp:70-78). */
+static void log_reduce(float a0, uint32_t mlog_two2nmb, float *fe, float *x, float *x2, float *y, float *t)
 {
-    if (a0 == INFINITY) return a0;
-    if (a0 == 0.0f) return -INFINITY;
-    if (a0 != a0 || a0 < 0.0f) return NAN;
-    float z = a0, t = 0.0f;
-    if (fabsf(z) < bf(C_SMALLESTPOS)) { z *= bf(C_TWOTONMB); t = bf(C_MLOGTWO2NMB); }
+    float z = a0;
+    *t = 0.0f;
+    if (fabsf(z) < bf(C_SMALLESTPOS)) { z *= bf(C_TWOTONMB); *t = bf(mlog_two2nmb); }
     uint32_t u = fb(z);
     int32_t e = (int32_t)((u & 0x7f800000u) >> 23) - 126;
-    float x = bf((u & ~0x7f800000u) | 0x3f000000u);
-    int lt = x < bf(C_SQRT_2O_2);
-    float fe = lt ? (float)e + (-1.0f) : (float)e;
-    x = (lt ? x + x : x) - 1.0f;
-    float x2 = x * x;
-    float y = horner(x, LOG_P, 8) * x * x2;
+    float m = bf((u & ~0x7f800000u) | 0x3f000000u);
+    int lt = m < bf(C_SQRT_2O_2);
+    *fe = lt ? (float)e + (-1.0f) : (float)e;
+    *x = (lt ? m + m : m) - 1.0f;
+    *x2 = *x * *x;
+    *y = horner(*x, LOG_P, 8) * *x * *x2;
+}
+
+#define LOG_SPECIALS(a0)                          \
+    if (a0 == INFINITY) return a0;                \
+    if (a0 == 0.0f) return -INFINITY;             \
+    if (a0 != a0 || a0 < 0.0f) return NAN;
+
+/* log: f_log.hpp:59-88 */
+EXPORT float o_log(float a0)
+{
+    LOG_SPECIALS(a0)
+    float fe, x, x2, y, t;
+    log_reduce(a0, C_MLOGTWO2NMB, &fe, &x, &x2, &y, &t);
     y = fe * bf(C_LOG_2LO) + y;
     y = -0.5f * x2 + y;
     return bf(C_LOG_2HI) * fe + ((x + y) + t);
+}
+
+/* log2: f_log.hpp:90-119, Log2_em1 = 0x3ee2a8ed, Mlog2two2nmb = 0xc1b80000 */
+EXPORT float o_log2(float a0)
+{
+    LOG_SPECIALS(a0)
+    float fe, x, x2, y, t;
+    log_reduce(a0, 0xc1b80000u, &fe, &x, &x2, &y, &t);
+    y = -0.5f * x2 + y;
+    float z = x * bf(0x3ee2a8edu) + y * bf(0x3ee2a8edu);
+    return (((z + y) + x) + fe) + t;
+}
+
+/* log10: f_log.hpp:121-153 (amul(a,b,c) = b*c + a), Log10_ehi = 0x3ede0000,
+ * Log10_elo = 0x3a37b152, Log10_2hi = 0x3e9a0000, Log10_2lo = 0x39826a14,
+ * Mlog10two2nmb = 0xc0dd8ede */
+EXPORT float o_log10(float a0)
+{
+    LOG_SPECIALS(a0)
+    float fe, x, x2, y, t;
+    log_reduce(a0, 0xc0dd8edeu, &fe, &x, &x2, &y, &t);
+    y = -0.5f * x2 + y;
+    float z = (x + y) * bf(0x3a37b152u);
+    z = y * bf(0x3ede0000u) + z;
+    z = x * bf(0x3ede0000u) + z;
+    z = fe * bf(0x3e9a0000u) + z;
+    return fe * bf(0x39826a14u) + (z + t);
 }
 
 /* -------------------------------------------------------------- log1p ----
@@ -236,7 +277,7 @@ EXPORT float o_expm1(float a0)
 
 /* ------------------------------------------------- elementwise maps ---- */
 enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT, FN_EXP2 = 8, FN_EXP10,
-       FN_EXPM1 };
+       FN_EXPM1, FN_LOG2, FN_LOG10 };
 
 EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
 {
@@ -252,6 +293,8 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_EXP2: y[i] = o_exp2(a); break;
         case FN_EXP10: y[i] = o_exp10(a); break;
         case FN_EXPM1: y[i] = o_expm1(a); break;
+        case FN_LOG2: y[i] = o_log2(a); break;
+        case FN_LOG10: y[i] = o_log10(a); break;
         default: y[i] = sqrtf(a); break;
         }
     }
@@ -272,6 +315,8 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_EXP2: y[i] = exp2(a); break;
         case FN_EXP10: y[i] = pow(10.0, a); break;
         case FN_EXPM1: y[i] = expm1(a); break;
+        case FN_LOG2: y[i] = log2(a); break;
+        case FN_LOG10: y[i] = log10(a); break;
         default: y[i] = sqrt(a); break;
         }
     }

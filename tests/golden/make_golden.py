@@ -28,6 +28,8 @@ SOURCES = [
     ("modules/core/exponential/unit/scalar/exp2.cpp", 42, 48),
     ("modules/core/exponential/unit/scalar/exp10.cpp", 40, 46),
     ("modules/core/exponential/unit/scalar/expm1.cpp", 40, 46),
+    ("modules/core/exponential/unit/scalar/log2.cpp", 39, 48),
+    ("modules/core/exponential/unit/scalar/log10.cpp", 39, 45),
 ]
 
 E = float(np.float32(math.e))

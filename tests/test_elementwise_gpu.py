@@ -268,10 +268,10 @@ def test_logical_stored_into_float_table(lib, dev):
 
 
 @pytest.mark.parametrize("mode", [1, 2], ids=["compiled", "interpreter"])
-def test_exp_family_in_expressions_nt2_policy(lib, dev, oracle, mode):
-    """exp2(x) + exp10(y) * expm1(x - y) under NT2's policy, through the
-    generic interpreter and the compiled kernel, bit-identical to the oracle's
-    composition of the same rounded operations."""
+def test_exp_log_family_in_expressions_nt2_policy(lib, dev, oracle, mode):
+    """exp2(x) + exp10(y) * expm1(x - y) and log2(|x|) - log10(|y|) under NT2's
+    policy, through the generic interpreter and the compiled kernel,
+    bit-identical to the oracle's composition of the same rounded operations."""
     n = 100003
     rng = np.random.default_rng(21)
     x = rng.uniform(-30, 30, n).astype(np.float32)
@@ -279,10 +279,12 @@ def test_exp_family_in_expressions_nt2_policy(lib, dev, oracle, mode):
     x[:6] = [np.nan, np.inf, -np.inf, 127.0, -127.5, 0.0]
     tx, ty = _t(dev, x), _t(dev, y)
     X, Y = E.Table(tx), E.Table(ty)
-    out = torch.empty_like(tx)
-    E.assign([out], [E.exp2(X) + E.exp10(Y) * E.expm1(X - Y)], precision=lib.PREC_NT2, force_generic=mode)
+    out, out2 = torch.empty_like(tx), torch.empty_like(tx)
+    E.assign([out, out2], [E.exp2(X) + E.exp10(Y) * E.expm1(X - Y), E.log2(E.abs_(X)) - E.log10(E.abs_(Y))],
+             precision=lib.PREC_NT2, force_generic=mode)
     torch.cuda.synchronize()
     with np.errstate(all="ignore"):
         ref = oracle.map_f32("exp2", x) + oracle.map_f32("exp10", y) * oracle.map_f32("expm1", (x - y).astype(np.float32))
-    got = out.cpu().numpy()
-    assert np.all((got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref)))
+        ref2 = oracle.map_f32("log2", np.abs(x)) - oracle.map_f32("log10", np.abs(y))
+    for got, r in ((out.cpu().numpy(), ref), (out2.cpu().numpy(), ref2)):
+        assert np.all((got.view(np.uint32) == r.view(np.uint32)) | (np.isnan(got) & np.isnan(r)))

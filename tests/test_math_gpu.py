@@ -23,13 +23,13 @@ SPECIALS = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -1.0, 1e-40, -1e-4
 # the float normal range)
 DOMAINS = dict(exp=(-87.3, 88.3), log=(1e-30, 1e30), log1p=(-0.999, 1e4), erfc=(-10, 9.2), normcdf=(-13, 9),
                fastnormcdf=(-9, 9), sqrt=(0, 1e30), exp2=(-126, 126.99), exp10=(-37.8, 38.2),
-               expm1=(-20, 88.37))
+               expm1=(-20, 88.37), log2=(1e-30, 1e30), log10=(1e-30, 1e30))
 
 
 def _sweep(fn, n=1 << 22, seed=5):
     lo, hi = DOMAINS[fn]
     rng = np.random.default_rng(seed)
-    if fn in ("log", "sqrt"):
+    if fn in ("log", "log2", "log10", "sqrt"):
         x = np.concatenate([np.geomspace(max(lo, 1e-38), hi, n // 2), rng.uniform(0, 4, n // 2)])
     else:
         x = np.concatenate([np.linspace(lo, hi, n // 2), rng.uniform(lo, hi, n // 4),
@@ -50,7 +50,7 @@ def _gpu_map(lib, dev, fn, x, prec):
 
 
 @pytest.mark.parametrize("fn", ["exp", "log", "log1p", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10",
-                                "expm1"])
+                                "expm1", "log2", "log10"])
 def test_nt2_policy_bit_exact(lib, dev, oracle, fn):
     x = _inputs(fn)
     got = _gpu_map(lib, dev, fn, x, lib.PREC_NT2)
@@ -60,7 +60,8 @@ def test_nt2_policy_bit_exact(lib, dev, oracle, fn):
 
 
 @pytest.mark.parametrize("fn,tol", [("exp", 1.5), ("log", 1.5), ("log1p", 2.0), ("erfc", 4.0), ("normcdf", 4.0),
-                                    ("sqrt", 0.5), ("exp2", 1.5), ("exp10", 2.0), ("expm1", 2.0)])
+                                    ("sqrt", 0.5), ("exp2", 2.0), ("exp10", 2.0), ("expm1", 2.0),
+                                    ("log2", 1.5), ("log10", 1.5)])
 def test_fast_policy_within_4ulp_of_fp64(lib, dev, oracle, fn, tol):
     """Accuracy over each function's sweep domain; the special values
     (including exp's +inf from NT2's Maxlog = 88.3763 on, as NT2) are
@@ -92,6 +93,6 @@ def test_fast_normcdf_pair_complement(lib, dev, oracle):
 @pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
 def test_golden_values_on_gpu(lib, dev, prec):
     for rec in [r for r in GOLDEN if r["fn"] in ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10",
-                                                  "expm1")]:
+                                                  "expm1", "log2", "log10")]:
         got = _gpu_map(lib, dev, rec["fn"], np.array([rec["x"]], np.float32), prec)[0]
         assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (rec, got)

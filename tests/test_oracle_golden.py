@@ -11,7 +11,7 @@ import pytest
 from helpers import nt2_ulpdist, std_ulp, reduction_ill
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
-FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1")
+FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1", "log2", "log10")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
@@ -69,6 +69,9 @@ def test_oracle_accuracy_profile(oracle):
     assert std_ulp(oracle.map_f32("exp", x), oracle.map_f64("exp", x)).max() <= 1.5
     x = np.geomspace(1e-30, 1e30, 400001).astype(np.float32)
     assert std_ulp(oracle.map_f32("log", x), oracle.map_f64("log", x)).max() <= 1.0
+    x = np.concatenate([x, np.geomspace(1e-45, 1e-37, 20001).astype(np.float32)])
+    for fn in ("log2", "log10"):  # NT2's float algorithms reach 1.22 and 1.43 ulp
+        assert std_ulp(oracle.map_f32(fn, x), oracle.map_f64(fn, x)).max() <= 1.5, fn
     x = np.linspace(-9, 9, 400001, dtype=np.float32)
     e = std_ulp(oracle.map_f32("erfc", x), oracle.map_f64("erfc", x))
     assert 4 < e.max() < 200
