@@ -388,6 +388,11 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 10) return expm1<P>(a);
     if (FN == 11) return log2<P>(a);
     if (FN == 12) return log10<P>(a);
+    if (FN == 13) return sin<P>(a);
+    if (FN == 14) return cos<P>(a);
+    if (FN == 15) return tan<P>(a);
+    if (FN == 16) return sinpi<P>(a);
+    if (FN == 17) return cospi<P>(a);
     float p, q;
     normcdf_pair<P>(a, p, q);
     return q;
@@ -418,6 +423,11 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 10: NT2G_MAP(10); break;
     case 11: NT2G_MAP(11); break;
     case 12: NT2G_MAP(12); break;
+    case 13: NT2G_MAP(13); break;
+    case 14: NT2G_MAP(14); break;
+    case 15: NT2G_MAP(15); break;
+    case 16: NT2G_MAP(16); break;
+    case 17: NT2G_MAP(17); break;
     default: NT2G_MAP(7); break;
     }
 #undef NT2G_MAP
@@ -458,6 +468,11 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_EXPM1: return expm1<P>(a);
     case NT2G_OP_LOG2: return log2<P>(a);
     case NT2G_OP_LOG10: return log10<P>(a);
+    case NT2G_OP_SIN: return sin<P>(a);
+    case NT2G_OP_COS: return cos<P>(a);
+    case NT2G_OP_TAN: return tan<P>(a);
+    case NT2G_OP_SINPI: return sinpi<P>(a);
+    case NT2G_OP_COSPI: return cospi<P>(a);
     default: return fastnormcdf<P>(a);
     }
 }

@@ -187,6 +187,11 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_EXPM1: e = "nt2g::expm1<P>(" + A + ")"; break;
         case NT2G_OP_LOG2: e = "nt2g::log2<P>(" + A + ")"; break;
         case NT2G_OP_LOG10: e = "nt2g::log10<P>(" + A + ")"; break;
+        case NT2G_OP_SIN: e = "nt2g::sin<P>(" + A + ")"; break;
+        case NT2G_OP_COS: e = "nt2g::cos<P>(" + A + ")"; break;
+        case NT2G_OP_TAN: e = "nt2g::tan<P>(" + A + ")"; break;
+        case NT2G_OP_SINPI: e = "nt2g::sinpi<P>(" + A + ")"; break;
+        case NT2G_OP_COSPI: e = "nt2g::cospi<P>(" + A + ")"; break;
         default: e = "nt2g::fastnormcdf<P>(" + A + ")"; break;
         }
         s += std::string(u ? "    unsigned v" : "    float v") + std::to_string(k) + "[4]; NT2G_L v" +

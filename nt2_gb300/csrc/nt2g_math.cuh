@@ -32,6 +32,8 @@
 // run-time compilation (the JIT path embeds this header): no host headers
 typedef unsigned int uint32_t;
 typedef int int32_t;
+typedef unsigned long long uint64_t;
+typedef long long int64_t;
 #else
 #include <stdint.h>
 #include <string.h>
@@ -554,6 +556,256 @@ template <class P> NT2G_HD float exp_neg_sqr(float x)
     float r = Fast::mul(Fast::add(s, 1.0f), scale);
     r = (-hi <= bits_f(NT2G_MINLOG)) ? 0.0f : r;
     return is_nan(x) ? x : r;
+}
+
+// ----------------------------------------------------------- trigonometry --
+// NT2 (modules/core/trigonometric/include/nt2/trigonometric/functions/):
+//   sin/cos/tan   scalar/impl/trigo/trig_base.hpp:131-176 (regular style,
+//                 big_ mode) over the radian cascade of trig_reduction.hpp:76-251:
+//                 |x| <= pi/4 as is, <= pi/2 one subtraction of pi/2 in three
+//                 parts (generic/rem_pio2_straight.hpp:60-66), <= 20 pi Cody-Waite
+//                 with k = round(x 2/pi) (rem_pio2_cephes.hpp:65-72), <= 2^6 pi the
+//                 error-compensated three-step form (rem_pio2_medium.hpp:68-84),
+//                 <= 2^18 pi the same three-step form in double, beyond that
+//                 fdlibm's Payne-Hanek reduction (scalar/rem_pio2.hpp).
+//   evaluation    f_trig_evaluation.hpp:40-72: NT2's degree-3 sin/cos and
+//                 degree-6 tan polynomials on [-pi/4, pi/4].
+//   sinpi/cospi   the pi_tag reduction trig_reduction.hpp:303-317: k = round(2x),
+//                 r = (x - k/2) pi.
+// The Payne-Hanek step here is this file's own: the float's 24-bit significand
+// times a 96-bit window of 2/pi in 64-bit integer pieces gives the quadrant and
+// at least 64 fraction bits, so r is the exactly reduced argument rounded once.
+
+// 2/pi in binary, 32 bits per word, after one word of zeros (word 1 holds the
+// first 32 fraction bits).  gen_twoopi.py prints these words.
+NT2G_HD uint32_t twoopi_word(int i)
+{
+    switch (i) {
+    case 1: return 0xA2F9836Eu;
+    case 2: return 0x4E441529u;
+    case 3: return 0xFC2757D1u;
+    case 4: return 0xF534DDC0u;
+    case 5: return 0xDB629599u;
+    case 6: return 0x3C439041u;
+    case 7: return 0xFE5163ABu;
+    case 8: return 0xDEBBC561u;
+    default: return 0u;
+    }
+}
+
+// Quadrant n (mod 4) and r = x - n pi/2 in double, |r| <= pi/4 (+2^-60), for a
+// finite x >= 2^-6 (the window below starts inside the table for those).
+NT2G_HD int trig_reduce_big(float x, double &r)
+{
+    const uint32_t u = f_bits(x);
+    const uint64_t m = (u & 0x007fffffu) | 0x00800000u;  // x = m 2^e
+    const int e = (int)(u >> 23) - 150;
+    // x 2/pi mod 4 only needs the bits b_i of 2/pi with i >= e - 1 (earlier ones
+    // contribute multiples of 4 m); b_i sits at bit i + 31 of the padded table.
+    const int j = e + 30;
+    const int w = j >> 5, sh = j & 31;
+    const uint64_t a0 = twoopi_word(w), a1 = twoopi_word(w + 1), a2 = twoopi_word(w + 2), a3 = twoopi_word(w + 3);
+    const uint64_t b2 = ((a0 << 32 | a1) << sh) >> 32;
+    const uint64_t b1 = ((a1 << 32 | a2) << sh) >> 32;
+    const uint64_t b0 = ((a2 << 32 | a3) << sh) >> 32;
+    // P = m (b2 b1 b0) = t2 2^64 + (t1 mod 2^32) 2^32 + (t0 mod 2^32); x 2/pi = P 2^-94 (mod 4)
+    const uint64_t t0 = m * b0;
+    const uint64_t t1 = m * b1 + (t0 >> 32);
+    const uint64_t t2 = m * b2 + (t1 >> 32);
+    int n = (int)(t2 >> 30) & 3;
+    const uint64_t f = (t2 << 34) | ((t1 & 0xffffffffu) << 2) | ((t0 & 0xffffffffu) >> 30);  // fraction bits 1..64
+    const uint32_t lo = (uint32_t)(t0 & 0x3fffffffu);                                      // bits 65..94
+    n = (n + (int)(f >> 63)) & 3;  // a fraction >= 1/2 rounds up to the next quadrant
+    const double q = (double)(int64_t)f * 0x1p-64 + (double)lo * 0x1p-94;
+    r = q * 0x1.921fb54442d18p+0;  // pi/2
+    return n;
+}
+
+// NT2's double helpers for the 2^6 pi .. 2^18 pi band (unfused, like its floats)
+#if defined(__CUDA_ARCH__)
+NT2G_HD double nt2_dmul(double a, double b) { return __dmul_rn(a, b); }
+NT2G_HD double nt2_dsub(double a, double b) { return __dsub_rn(a, b); }
+#else
+inline double nt2_dmul(double a, double b) { volatile double r = a * b; return r; }
+inline double nt2_dsub(double a, double b) { volatile double r = a - b; return r; }
+#endif
+
+// rem_pio2_medium.hpp:68-84 in float or double.  The first correction term
+// (fn * Pio2_1t) is computed and then overwritten in NT2, so it is not applied.
+template <class P> NT2G_HD int trig_medium_f(float t, float &xr)
+{
+    const float fn = rintf(P::mul(t, bits_f(0x3f22f984u)));  // Invpio_2
+    float r = P::sub(t, P::mul(fn, bits_f(0x3fc90f80u)));    // Pio2_1
+    float t2 = r;
+    float w = P::mul(fn, bits_f(0x37354400u));               // Pio2_2
+    r = P::sub(t2, w);
+    w = P::sub(P::mul(fn, bits_f(0x2e85a308u)), P::sub(P::sub(t2, r), w));  // Pio2_2t
+    t2 = r;
+    w = P::mul(fn, bits_f(0x2e85a300u));                     // Pio2_3
+    r = P::sub(t2, w);
+    w = P::sub(P::mul(fn, bits_f(0x248d3132u)), P::sub(P::sub(t2, r), w));  // Pio2_3t
+    xr = P::sub(r, w);
+    return (int)fn & 3;
+}
+
+NT2G_HD int trig_medium_d(double t, float &xr)
+{
+    const double fn = rint(nt2_dmul(t, 0x1.45f306dc9c883p-1));  // Invpio_2
+    double r = nt2_dsub(t, nt2_dmul(fn, 0x1.921fb544p+0));      // Pio2_1
+    double t2 = r;
+    double w = nt2_dmul(fn, 0x1.0b4611a6p-34);                   // Pio2_2
+    r = nt2_dsub(t2, w);
+    w = nt2_dsub(nt2_dmul(fn, 0x1.3198a2e037073p-69), nt2_dsub(nt2_dsub(t2, r), w));  // Pio2_2t
+    t2 = r;
+    w = nt2_dmul(fn, 0x1.3198a2ep-69);                           // Pio2_3
+    r = nt2_dsub(t2, w);
+    w = nt2_dsub(nt2_dmul(fn, 0x1.b839a252049c1p-104), nt2_dsub(nt2_dsub(t2, r), w));  // Pio2_3t
+    xr = (float)nt2_dsub(r, w);
+    return (int)(int64_t)fn & 3;
+}
+
+// Fast: below this bound a three-float Cody-Waite with FMAs (pi/2 = C1 + C2 + C3,
+// each the float nearest the remainder) keeps the reduced argument within an
+// ulp; above it the exact reduction runs.
+#define NT2G_TRIG_FAST_MAX 131072.0f
+
+// Quadrant n (mod 4) and the reduced argument xr of x = |a0| (finite).
+template <class P> NT2G_HD int trig_reduce(float x, float &xr)
+{
+    if (P::exact) {
+        if (!(x > bits_f(0x3f490fdbu))) { xr = x; return 0; }  // pi/4
+        if (!(x > bits_f(0x3fc90fdbu))) {                       // pi/2
+            xr = P::sub(P::sub(P::sub(x, bits_f(0x3fc90f80u)), bits_f(0x37354400u)), bits_f(0x2e85a300u));
+            return 1;
+        }
+        if (!(x > bits_f(0x427b53d1u))) {                       // 20 pi
+            const float xi = rintf(P::mul(x, bits_f(0x3f22f983u)));  // Twoopi
+            float r = P::sub(x, P::mul(xi, bits_f(0x3fc90f80u)));
+            r = P::sub(r, P::mul(xi, bits_f(0x37354400u)));
+            xr = P::sub(r, P::mul(xi, bits_f(0x2e85a300u)));
+            return (int)xi & 3;
+        }
+        if (!(x > bits_f(0x43490fdbu))) return trig_medium_f<P>(x, xr);  // 2^6 pi
+        if (!((double)x > 0x1.921fb54442d18p+19)) return trig_medium_d((double)x, xr);  // 2^18 pi in double
+        double r;
+        const int n = trig_reduce_big(x, r);
+        xr = (float)r;
+        return n;
+    }
+    if (x <= NT2G_TRIG_FAST_MAX) {
+        const float k = rintf(Fast::mul(x, 0x1.45f306p-1f));
+        float r = Fast::fma(-k, 0x1.921fb6p+0f, x);
+        r = Fast::fma(-k, -0x1.777a5cp-25f, r);
+        xr = Fast::fma(-k, -0x1.ee59dap-50f, r);
+        return (int)k & 3;
+    }
+    double r;
+    const int n = trig_reduce_big(x, r);
+    xr = (float)r;
+    return n;
+}
+
+template <class P> NT2G_HD float trig_cos_eval(float z)
+{
+    const float y = horner<P>(z, bits_f(0x37ccf5ceu), bits_f(0xbab60619u), bits_f(0x3d2aaaa5u));
+    return P::add(1.0f, P::fma(z, -0.5f, P::mul(y, P::mul(z, z))));
+}
+
+template <class P> NT2G_HD float trig_sin_eval(float z, float x)
+{
+    const float y1 = horner<P>(z, bits_f(0xb94ca1f9u), bits_f(0x3c08839du), bits_f(0xbe2aaaa2u));
+    return P::fma(P::mul(y1, z), x, x);
+}
+
+template <class P> NT2G_HD float trig_tan_eval(float z)
+{
+    const float zz = P::mul(z, z);
+    const float y = horner<P>(zz, bits_f(0x3c19c53bu), bits_f(0x3b4c779cu), bits_f(0x3cc821b5u),
+                              bits_f(0x3d5ac5c9u), bits_f(0x3e0896ddu), bits_f(0x3eaaaa6fu));
+    return P::add(P::mul(P::mul(y, zz), z), z);
+}
+
+// The shared tail of sin and cos: swap selects the other polynomial, sign is
+// xor-ed into the result.  Fast evaluates both and selects (no divergence).
+template <class P> NT2G_HD float trig_sincos_tail(float xr, bool use_cos, uint32_t sign)
+{
+    const float z = P::mul(xr, xr);
+    float v;
+    if (P::exact) v = use_cos ? trig_cos_eval<P>(z) : trig_sin_eval<P>(z, xr);
+    else {
+        const float c = trig_cos_eval<P>(z), s = trig_sin_eval<P>(z, xr);
+        v = use_cos ? c : s;
+    }
+    return bits_f(f_bits(v) ^ sign);
+}
+
+NT2G_HD bool trig_invalid(float a0) { return !(fabsf(a0) < f_inf()); }  // NaN or +-inf
+
+// pi_tag reduction: k = round(2x), xr = (x - k/2) pi.  The quadrant is k mod 4
+// (k is an even integer, hence a multiple of 4, once it leaves the int64 range).
+// NT2's 2x overflows for x >= 2^127 and its sinpi/cospi are NaN there; Fast
+// clamps x to 2^24 first (every float from 2^24 on is an even integer, as 2^24
+// is, so the results are unchanged below 2^127 and correct above).
+template <class P> NT2G_HD int trig_reduce_pi(float x, float &xr)
+{
+    if (!P::exact) x = fminf(x, 0x1p24f);
+    const float xi = rintf(P::mul(x, 2.0f));
+    const float x2 = P::sub(x, P::mul(xi, 0.5f));
+    xr = P::mul(x2, bits_f(0x40490fdbu));  // Pi
+    return (fabsf(xi) < 0x1p62f) ? (int)((int64_t)xi & 3) : 0;
+}
+
+template <class P, bool PI> NT2G_HD float cos_any(float a0)
+{
+    if (P::exact && trig_invalid(a0)) return f_nan();
+    const float x = (P::exact || !trig_invalid(a0)) ? fabsf(a0) : 0.0f;
+    float xr;
+    const int n = PI ? trig_reduce_pi<P>(x, xr) : trig_reduce<P>(x, xr);
+    const int swap = n & 1;
+    const float r = trig_sincos_tail<P>(xr, !swap, (uint32_t)(swap ^ ((n & 2) >> 1)) << 31);
+    return (!P::exact && trig_invalid(a0)) ? f_nan() : r;
+}
+
+template <class P, bool PI> NT2G_HD float sin_any(float a0)
+{
+    if (P::exact && trig_invalid(a0)) return f_nan();
+    const float x = (P::exact || !trig_invalid(a0)) ? fabsf(a0) : 0.0f;
+    float xr;
+    const int n = PI ? trig_reduce_pi<P>(x, xr) : trig_reduce<P>(x, xr);
+    const uint32_t sign = (f_bits(a0) & 0x80000000u) ^ ((uint32_t)(n & 2) << 30);
+    const float r = trig_sincos_tail<P>(xr, (n & 1) != 0, sign);
+    return (!P::exact && trig_invalid(a0)) ? f_nan() : r;
+}
+
+template <class P> NT2G_HD float cos(float a0) { return cos_any<P, false>(a0); }
+template <class P> NT2G_HD float sin(float a0) { return sin_any<P, false>(a0); }
+template <class P> NT2G_HD float cospi(float a0) { return cos_any<P, true>(a0); }
+template <class P> NT2G_HD float sinpi(float a0) { return sin_any<P, true>(a0); }
+
+// tan: NaN for NaN/inf, tan(+-0) = +-0, else tan(xr) or -1/tan(xr) by the
+// quadrant's parity, with a0's sign.
+template <class P> NT2G_HD float tan(float a0)
+{
+    if (P::exact) {
+        if (trig_invalid(a0)) return f_nan();
+        if (a0 == 0.0f) return a0;
+    }
+    const float x = (P::exact || !trig_invalid(a0)) ? fabsf(a0) : 0.0f;
+    float xr;
+    const int n = trig_reduce<P>(x, xr);
+    float y = trig_tan_eval<P>(xr);
+    if (P::exact) {
+        if (n & 1) y = -P::div(1.0f, y);
+    } else {
+        const float ry = -P::div(1.0f, y);
+        y = (n & 1) ? ry : y;
+    }
+    float r = bits_f(f_bits(y) ^ (f_bits(a0) & 0x80000000u));
+    if (!P::exact) {
+        r = (a0 == 0.0f) ? a0 : r;
+        r = trig_invalid(a0) ? f_nan() : r;
+    }
+    return r;
 }
 
 }  // namespace nt2g

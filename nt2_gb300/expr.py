@@ -1,8 +1,9 @@
 """A Python mirror of NT2's expression surface over device tables.
 
 ``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
-(exp, exp2, exp10, expm1, log, log2, log10, log1p, erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms,
-min, max, if_else, selinc, seldec, if_zero_else_one, adds) build an expression
+(exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, sinpi, cospi,
+erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms, min, max, if_else,
+selinc, seldec, if_zero_else_one, adds) build an expression
 tree; ``assign(outs, exprs)`` is ``tie(outs...) = tie(exprs...)``: it lowers
 the trees to the SSA program of nt2g.h, compiles it once (cached by program
 text) and evaluates it through ``nt2g_eval`` -- the same path the C++ table
@@ -80,6 +81,7 @@ normcdf, fastnormcdf, sqrt, rec = _un("NORMCDF"), _un("FASTNORMCDF"), _un("SQRT"
 abs_ = _un("ABS")
 exp2, exp10, expm1 = _un("EXP2"), _un("EXP10"), _un("EXPM1")
 log2, log10 = _un("LOG2"), _un("LOG10")
+sin, cos, tan, sinpi, cospi = _un("SIN"), _un("COS"), _un("TAN"), _un("SINPI"), _un("COSPI")
 
 # Functors applied to plain numbers evaluate at once in float32 with NT2's
 # scalar semantics (each step rounded, no fusion), as NT2's scalar overloads

@@ -593,6 +593,11 @@ NT2G_UNARY(exp10, NT2G_OP_EXP10)
 NT2G_UNARY(expm1, NT2G_OP_EXPM1)
 NT2G_UNARY(log2, NT2G_OP_LOG2)
 NT2G_UNARY(log10, NT2G_OP_LOG10)
+NT2G_UNARY(sin, NT2G_OP_SIN)
+NT2G_UNARY(cos, NT2G_OP_COS)
+NT2G_UNARY(tan, NT2G_OP_TAN)
+NT2G_UNARY(sinpi, NT2G_OP_SINPI)
+NT2G_UNARY(cospi, NT2G_OP_COSPI)
 #undef NT2G_UNARY
 
 // Functors on plain scalars evaluate at once, in float, with NT2's scalar

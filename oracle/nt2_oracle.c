@@ -25,6 +25,7 @@
  *   EUL  = modules/core/euler/include/nt2/euler/functions
  *   STAT = modules/core/statistics/include/nt2/statistics/functions
  *   BSIMD= modules/boost/simd/base/include/boost/simd
+ *   TRIG = modules/core/trigonometric/include/nt2/trigonometric/functions
  */
 #include <math.h>
 #include <stdint.h>
@@ -275,9 +276,153 @@ EXPORT float o_expm1(float a0)
     return y * o_pow2i(k);
 }
 
+/* ------------------------------------------------------- trigonometry ----
+ * NT2's float sin/cos/tan (TRIG/scalar/impl/trigo/trig_base.hpp:131-176,
+ * regular style, big_ mode) and sinpi/cospi (pi_tag), every operation rounded:
+ *   reduction cascade trig_reduction.hpp:76-251 --
+ *     |x| <= pi/4 as is; <= pi/2 rem_pio2_straight.hpp:60-66; <= 20 pi
+ *     rem_pio2_cephes.hpp:65-72; <= 2^6 pi rem_pio2_medium.hpp:68-84 in float;
+ *     <= 2^18 pi the same in double (use_conversion, :235-244); beyond, fdlibm's
+ *     __ieee754_rem_pio2f / __kernel_rem_pio2f (TRIG/scalar/rem_pio2.hpp).
+ *   evaluation f_trig_evaluation.hpp:40-72; pi_tag reduction
+ *   trig_reduction.hpp:303-317.
+ * Beyond 2^18 pi this oracle reduces exactly (a 2/pi table and 128-bit integer
+ * products) and rounds r once to float; NT2's fdlibm float kernel is taken to
+ * give that same rounded r.  That band is checked against FP64 libm only. */
+static const uint32_t TWOOPI[9] = {0u, 0xA2F9836Eu, 0x4E441529u, 0xFC2757D1u, 0xF534DDC0u,
+                                   0xDB629599u, 0x3C439041u, 0xFE5163ABu, 0xDEBBC561u};
+
+EXPORT uint32_t o_twoopi_word(int i) { return (i >= 0 && i < 9) ? TWOOPI[i] : 0u; }
+
+/* x = m 2^e; x (2/pi) = sum_i b_i m 2^(e-i).  Bits b_i with i <= e-2 add
+ * multiples of 4: start the 128-bit window at i = e-1 (table bit i+31). */
+static int big_reduce(float x, float *xr)
+{
+    uint32_t u = fb(x);
+    uint64_t m = (u & 0x7fffffu) | 0x800000u;
+    int e = (int)(u >> 23) - 150;
+    int j = e + 30;
+    unsigned __int128 win = 0;
+    for (int k = 0; k < 128; ++k) {  /* bit by bit: slow and plain */
+        int bit = j + k, w = bit >> 5, o = 31 - (bit & 31);
+        uint32_t word = (w >= 0 && w < 9) ? TWOOPI[w] : 0u;
+        win = (win << 1) | ((word >> o) & 1u);
+    }
+    /* window bit k is b_(e-1+k) with weight 2^(1-k): x 2/pi = m * win * 2^-126
+     * (mod 4), so the quadrant is bits 126..127 of the product and the fraction
+     * its 126 bits below (wrap-around above bit 127 only drops multiples of 4) */
+    unsigned __int128 plo = (unsigned __int128)m * (uint64_t)win + (((unsigned __int128)m * (uint64_t)(win >> 64)) << 64);
+    int n = (int)(plo >> 126) & 3;
+    unsigned __int128 frac = plo << 2;                                 /* fraction scaled by 2^128 */
+    long double q;
+    if (frac >> 127) { n = (n + 1) & 3; frac = ~frac + 1; q = -(long double)frac; }
+    else q = (long double)frac;
+    double qd = (double)(q * 0x1p-128L);
+    *xr = (float)(qd * 1.5707963267948966);
+    return n;
+}
+
+static double dmul(double a, double b) { volatile double r = a * b; return r; }
+static double dsub(double a, double b) { volatile double r = a - b; return r; }
+
+static int medium_f(float t, float *xr)
+{
+    float fn = rintf(t * bf(0x3f22f984u));
+    float r = t - fn * bf(0x3fc90f80u), t2, w;
+    t2 = r; w = fn * bf(0x37354400u); r = t2 - w; w = fn * bf(0x2e85a308u) - ((t2 - r) - w);
+    t2 = r; w = fn * bf(0x2e85a300u); r = t2 - w; w = fn * bf(0x248d3132u) - ((t2 - r) - w);
+    *xr = r - w;
+    return (int)fn & 3;
+}
+
+static double bd(uint64_t u) { double d; memcpy(&d, &u, 8); return d; }
+
+static int medium_d(double t, float *xr)
+{
+    double fn = rint(dmul(t, bd(0x3FE45F306DC9C883ull)));
+    double r = dsub(t, dmul(fn, bd(0x3FF921FB54400000ull))), t2, w;
+    t2 = r; w = dmul(fn, bd(0x3DD0B4611A600000ull)); r = dsub(t2, w);
+    w = dsub(dmul(fn, bd(0x3BA3198A2E037073ull)), dsub(dsub(t2, r), w));
+    t2 = r; w = dmul(fn, bd(0x3BA3198A2E000000ull)); r = dsub(t2, w);
+    w = dsub(dmul(fn, bd(0x397B839A252049C1ull)), dsub(dsub(t2, r), w));
+    *xr = (float)dsub(r, w);
+    return (int)(int64_t)fn & 3;
+}
+
+static int trig_reduce(float x, float *xr)
+{
+    if (!(x > bf(0x3f490fdbu))) { *xr = x; return 0; }
+    if (!(x > bf(0x3fc90fdbu))) { *xr = ((x - bf(0x3fc90f80u)) - bf(0x37354400u)) - bf(0x2e85a300u); return 1; }
+    if (!(x > bf(0x427b53d1u))) {
+        float xi = rintf(x * bf(0x3f22f983u));
+        float r = x - xi * bf(0x3fc90f80u);
+        r = r - xi * bf(0x37354400u);
+        *xr = r - xi * bf(0x2e85a300u);
+        return (int)xi & 3;
+    }
+    if (!(x > bf(0x43490fdbu))) return medium_f(x, xr);
+    if (!((double)x > bd(0x412921fb54442d18ull))) return medium_d((double)x, xr);
+    return big_reduce(x, xr);
+}
+
+static int trig_reduce_pi(float x, float *xr)
+{
+    float xi = rintf(x * 2.0f);
+    float x2 = x - xi * 0.5f;
+    *xr = x2 * bf(0x40490fdbu);
+    return (fabsf(xi) < 0x1p62f) ? (int)((int64_t)xi & 3) : 0;
+}
+
+static const uint32_t COS_P[3] = {0x37ccf5ce, 0xbab60619, 0x3d2aaaa5};
+static const uint32_t SIN_P[3] = {0xb94ca1f9, 0x3c08839d, 0xbe2aaaa2};
+static const uint32_t TAN_P[6] = {0x3c19c53b, 0x3b4c779c, 0x3cc821b5, 0x3d5ac5c9, 0x3e0896dd, 0x3eaaaa6f};
+
+static float cos_eval(float z) { float y = horner(z, COS_P, 3); return 1.0f + (z * -0.5f + y * (z * z)); }
+static float sin_eval(float z, float x) { float y1 = horner(z, SIN_P, 3); return (y1 * z) * x + x; }
+static float tan_eval(float z) { float zz = z * z; return (horner(zz, TAN_P, 6) * zz) * z + z; }
+
+static int invalid(float a) { return !(fabsf(a) < INFINITY); }
+
+static float cos_any(float a0, int pi)
+{
+    if (invalid(a0)) return NAN;
+    float xr;
+    int n = pi ? trig_reduce_pi(fabsf(a0), &xr) : trig_reduce(fabsf(a0), &xr);
+    int swap = n & 1;
+    float z = xr * xr;
+    float v = swap ? sin_eval(z, xr) : cos_eval(z);
+    return bf(fb(v) ^ ((uint32_t)(swap ^ ((n & 2) >> 1)) << 31));
+}
+
+static float sin_any(float a0, int pi)
+{
+    if (invalid(a0)) return NAN;
+    float xr;
+    int n = pi ? trig_reduce_pi(fabsf(a0), &xr) : trig_reduce(fabsf(a0), &xr);
+    float z = xr * xr;
+    float v = (n & 1) ? cos_eval(z) : sin_eval(z, xr);
+    return bf(fb(v) ^ (fb(a0) & 0x80000000u) ^ ((uint32_t)(n & 2) << 30));
+}
+
+EXPORT float o_cos(float a0) { return cos_any(a0, 0); }
+EXPORT float o_sin(float a0) { return sin_any(a0, 0); }
+EXPORT float o_cospi(float a0) { return cos_any(a0, 1); }
+EXPORT float o_sinpi(float a0) { return sin_any(a0, 1); }
+
+EXPORT float o_tan(float a0)
+{
+    if (invalid(a0)) return NAN;
+    if (a0 == 0.0f) return a0;
+    float xr;
+    int n = trig_reduce(fabsf(a0), &xr);
+    float y = tan_eval(xr);
+    if (n & 1) y = -(1.0f / y);
+    return bf(fb(y) ^ (fb(a0) & 0x80000000u));
+}
+
 /* ------------------------------------------------- elementwise maps ---- */
 enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT, FN_EXP2 = 8, FN_EXP10,
-       FN_EXPM1, FN_LOG2, FN_LOG10 };
+       FN_EXPM1, FN_LOG2, FN_LOG10, FN_SIN, FN_COS, FN_TAN, FN_SINPI, FN_COSPI };
 
 EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
 {
@@ -295,9 +440,32 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_EXPM1: y[i] = o_expm1(a); break;
         case FN_LOG2: y[i] = o_log2(a); break;
         case FN_LOG10: y[i] = o_log10(a); break;
+        case FN_SIN: y[i] = o_sin(a); break;
+        case FN_COS: y[i] = o_cos(a); break;
+        case FN_TAN: y[i] = o_tan(a); break;
+        case FN_SINPI: y[i] = o_sinpi(a); break;
+        case FN_COSPI: y[i] = o_cospi(a); break;
         default: y[i] = sqrtf(a); break;
         }
     }
+}
+
+/* sin(pi a), cos(pi a) in FP64 for a float a: a mod 2 is exact in double
+ * (fmod), then |r| <= 1/2 keeps the product pi r within an ulp. */
+static double sinpi_d(double a)
+{
+    double r = fmod(a, 2.0);           /* exact, sign of a */
+    if (r > 1.0) r -= 2.0; else if (r < -1.0) r += 2.0;
+    if (r > 0.5) return sin(M_PI * (1.0 - r));
+    if (r < -0.5) return -sin(M_PI * (1.0 + r));
+    return sin(M_PI * r);
+}
+static double cospi_d(double a)
+{
+    double r = fabs(fmod(a, 2.0));
+    if (r > 1.0) r = 2.0 - r;          /* [0, 1] */
+    if (r > 0.5) return -sin(M_PI * (r - 0.5));
+    return sin(M_PI * (0.5 - r));
 }
 
 /* FP64 reference of the same functions on float inputs (glibc double libm). */
@@ -317,6 +485,11 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_EXPM1: y[i] = expm1(a); break;
         case FN_LOG2: y[i] = log2(a); break;
         case FN_LOG10: y[i] = log10(a); break;
+        case FN_SIN: y[i] = sin(a); break;
+        case FN_COS: y[i] = cos(a); break;
+        case FN_TAN: y[i] = tan(a); break;
+        case FN_SINPI: y[i] = sinpi_d(a); break;
+        case FN_COSPI: y[i] = cospi_d(a); break;
         default: y[i] = sqrt(a); break;
         }
     }

@@ -30,17 +30,29 @@ SOURCES = [
     ("modules/core/exponential/unit/scalar/expm1.cpp", 40, 46),
     ("modules/core/exponential/unit/scalar/log2.cpp", 39, 48),
     ("modules/core/exponential/unit/scalar/log10.cpp", 39, 45),
+    ("modules/core/trigonometric/unit/scalar/sin.cpp", 44, 52),
+    ("modules/core/trigonometric/unit/scalar/cos.cpp", 45, 55),
+    ("modules/core/trigonometric/unit/scalar/tan.cpp", 41, 49),
+    ("modules/core/trigonometric/unit/scalar/sinpi.cpp", 45, 54),
+    ("modules/core/trigonometric/unit/scalar/cospi.cpp", 45, 54),
 ]
 
 E = float(np.float32(math.e))
 CONST = {
     "Inf": math.inf, "Minf": -math.inf, "Nan": math.nan, "Zero": 0.0, "Mzero": -0.0, "One": 1.0, "Mone": -1.0,
     "Half": 0.5, "Two": 2.0, "Ten": 10.0, "Exp_1": E, "Eps": float(np.finfo(np.float32).eps),
+    "Mhalf": -0.5, "Quarter": 0.25,
+    # NT2's float pi constants by bit pattern (boost/simd/constant/constants/*.hpp)
+    "Pi": float(np.uint32(0x40490fdb).view(np.float32)), "Pio_2": float(np.uint32(0x3fc90fdb).view(np.float32)),
+    "Pio_4": float(np.uint32(0x3f490fdb).view(np.float32)),
+    "Sqrt_2o_2": float(np.uint32(0x3f3504f3).view(np.float32)),
 }
 
 
 def _value(expr):
     expr = expr.strip()
+    if expr.startswith("-nt2::"):  # a negated constant
+        return -_value(expr[1:])
     m = re.fullmatch(r"nt2::(\w+)<\w+>\(\)", expr)
     if m:
         return CONST[m.group(1)]

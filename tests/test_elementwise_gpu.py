@@ -288,3 +288,24 @@ def test_exp_log_family_in_expressions_nt2_policy(lib, dev, oracle, mode):
         ref2 = oracle.map_f32("log2", np.abs(x)) - oracle.map_f32("log10", np.abs(y))
     for got, r in ((out.cpu().numpy(), ref), (out2.cpu().numpy(), ref2)):
         assert np.all((got.view(np.uint32) == r.view(np.uint32)) | (np.isnan(got) & np.isnan(r)))
+
+
+@pytest.mark.parametrize("mode", [1, 2], ids=["compiled", "interpreter"])
+def test_trig_in_expressions_nt2_policy(lib, dev, oracle, mode):
+    """sin(x) * cos(y) + tan(x) - sinpi(y) * cospi(x) under NT2's policy through
+    both generic paths, bit-identical to the oracle's composition."""
+    n = 65537
+    rng = np.random.default_rng(22)
+    x = (rng.standard_normal(n) * np.exp2(rng.integers(-4, 22, n))).astype(np.float32)
+    y = rng.uniform(-1e3, 1e3, n).astype(np.float32)
+    tx, ty = _t(dev, x), _t(dev, y)
+    X, Y = E.Table(tx), E.Table(ty)
+    out = torch.empty_like(tx)
+    E.assign([out], [E.sin(X) * E.cos(Y) + E.tan(X) - E.sinpi(Y) * E.cospi(X)], precision=lib.PREC_NT2,
+             force_generic=mode)
+    torch.cuda.synchronize()
+    f = oracle.map_f32
+    with np.errstate(all="ignore"):
+        ref = (f("sin", x) * f("cos", y) + f("tan", x)) - f("sinpi", y) * f("cospi", x)
+    got = out.cpu().numpy()
+    assert np.all((got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref)))

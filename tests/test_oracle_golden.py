@@ -1,5 +1,6 @@
 """The oracle (CPU restatement of NT2's float algorithms) against the known
 answers of NT2's own unit tests, and the test tooling itself."""
+import ctypes
 import json
 import math
 import os
@@ -11,7 +12,8 @@ import pytest
 from helpers import nt2_ulpdist, std_ulp, reduction_ill
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
-FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1", "log2", "log10")
+FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1", "log2", "log10", "sin", "cos",
+         "tan", "sinpi", "cospi")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
@@ -89,6 +91,51 @@ def test_oracle_accuracy_profile(oracle):
     assert oracle.map_f32("exp2", np.float32([127.5, -127.5, 200, -200])).tolist() == [np.inf, 0, np.inf, 0]
     assert oracle.map_f32("exp10", np.float32([38.3, -38, 50, -50])).tolist() == [np.inf, 0, np.inf, 0]
     assert oracle.map_f32("expm1", np.float32([88.5, -17.5, -1e30])).tolist() == [np.inf, -1, -1]
+
+
+def test_oracle_trig_accuracy_profile(oracle):
+    """NT2's float sin/cos/tan/sinpi/cospi as restated, against FP64 over every
+    reduction band (to 2^18 pi in NT2's float and double Cody-Waite forms,
+    beyond it the exact reduction): NT2's degree-3 sin/cos polynomials keep
+    about 1.9 ulp, tan 2.7."""
+    bands = [np.linspace(-1, 1, 100001), np.linspace(-63, 63, 100001), np.linspace(-201, 201, 100001),
+             np.linspace(-8e5, 8e5, 100001), np.geomspace(8e5, 3e38, 100001)]
+    x = np.concatenate(bands).astype(np.float32)
+    for fn, tol in (("sin", 2.0), ("cos", 2.0), ("tan", 3.5), ("sinpi", 2.0), ("cospi", 2.0)):
+        a, b = oracle.map_f32(fn, x), oracle.map_f64(fn, x)
+        m = np.isfinite(b) & (np.abs(b) > 1e-30)
+        if fn in ("sinpi", "cospi"):  # NT2 computes 2x first: NaN from 2^127 on
+            m &= np.abs(x) < 2.0 ** 127
+            assert np.isnan(oracle.map_f32(fn, np.float32([2.0 ** 127, -3e38]))).all()
+        assert std_ulp(a[m], b[m]).max() <= tol, fn
+    # the exact reduction agrees with NT2's double band on its last floats
+    x = np.float32([823549.5, 823549.5625, 823549.625])
+    assert std_ulp(oracle.map_f32("sin", x), oracle.map_f64("sin", x)).max() <= 1.0
+
+
+def test_twoopi_table_is_two_over_pi():
+    """The 2/pi words of the exact reduction, in the oracle and in the device
+    header, against 2/pi computed from Machin's formula in integers (and
+    against sympy where it is installed)."""
+    import importlib.util
+    import re
+    here = os.path.dirname(__file__)
+    spec = importlib.util.spec_from_file_location(
+        "gen_twoopi", os.path.join(here, "..", "nt2_gb300", "csrc", "gen_twoopi.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    want = gen.twoopi_words(8)
+    import oracle.oracle as O
+    L = O.lib()
+    L.o_twoopi_word.restype = ctypes.c_uint32
+    assert [L.o_twoopi_word(i) for i in range(1, 9)] == want and L.o_twoopi_word(0) == 0
+    src = open(os.path.join(here, "..", "nt2_gb300", "csrc", "nt2g_math.cuh")).read()
+    body = src[src.index("NT2G_HD uint32_t twoopi_word"):]
+    body = body[:body.index("default:")]
+    assert [int(h, 16) for h in re.findall(r"return (0x[0-9A-Fa-f]+)u;", body)] == want
+    sympy = pytest.importorskip("sympy")
+    v = int(sympy.floor(sympy.Integer(2) / sympy.pi * sympy.Integer(2) ** 256))
+    assert [(v >> (32 * (7 - i))) & 0xFFFFFFFF for i in range(8)] == want
 
 
 def test_sigmadelta_oracle_semantics(oracle):
