@@ -65,6 +65,9 @@ typedef enum nt2g_opcode {
     NT2G_OP_SCALAR = 2,    /* a = slot of a scalar argument (broadcast)      */
     NT2G_OP_CONST = 3,     /* imm                                            */
     NT2G_OP_STORE = 4,     /* a = value, b = slot of the output table        */
+    NT2G_OP_INDEX = 5,     /* the element's linear position p (offset + i) in
+                              the op's dtype: NT2's enumerate<T>(p), the leaf of
+                              colon / linspace / logspace (uint8: p mod 256)    */
     NT2G_OP_ADD = 10, NT2G_OP_SUB, NT2G_OP_MUL, NT2G_OP_DIV, NT2G_OP_NEG, NT2G_OP_ABS,
     NT2G_OP_SQR, NT2G_OP_SQRT, NT2G_OP_REC, NT2G_OP_MIN, NT2G_OP_MAX,
     NT2G_OP_FMA = 30,      /* a*b + c (unfused under NT2G_PREC_NT2)          */

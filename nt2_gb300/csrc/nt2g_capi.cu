@@ -272,7 +272,7 @@ static bool is_value_op(int code) { return code != NT2G_OP_STORE; }
 static int n_operands(int code)
 {
     switch (code) {
-    case NT2G_OP_LOAD: case NT2G_OP_SCALAR: case NT2G_OP_CONST: return 0;
+    case NT2G_OP_LOAD: case NT2G_OP_SCALAR: case NT2G_OP_CONST: case NT2G_OP_INDEX: return 0;
     case NT2G_OP_STORE: return 1;
     case NT2G_OP_NEG: case NT2G_OP_ABS: case NT2G_OP_SQR: case NT2G_OP_SQRT: case NT2G_OP_REC:
     case NT2G_OP_EXP: case NT2G_OP_LOG: case NT2G_OP_LOG1P: case NT2G_OP_ERFC: case NT2G_OP_NORMCDF:
@@ -496,7 +496,7 @@ extern "C" nt2g_status nt2g_program_create(const nt2g_op *ops, int32_t n_ops, in
         if (na >= 1 && o.code != NT2G_OP_LOAD && o.code != NT2G_OP_SCALAR) o.a = remap[o.a];
         if (na >= 2) o.b = remap[o.b];
         if (na >= 3) o.c = remap[o.c];
-        if (na < 1 && o.code == NT2G_OP_CONST) o.a = -1;
+        if (na < 1 && (o.code == NT2G_OP_CONST || o.code == NT2G_OP_INDEX)) o.a = -1;
         if (na < 2) o.b = -1;
         if (na < 3) o.c = -1;
         uint32_t immbits = 0;
@@ -668,6 +668,7 @@ extern "C" nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, in
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_eval: precision %d", precision);
     cudaStream_t st = (cudaStream_t)stream;
     DArgs da{};
+    da.pos0 = offset;
     for (int s = 0; s < p->n_slots; ++s) {
         const int use = p->slot_use[s];
         if (!use) continue;

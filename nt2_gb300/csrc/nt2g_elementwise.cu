@@ -516,6 +516,13 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
 #pragma unroll
                 for (int j = 0; j < kV; ++j) d[j] = f32 ? __float_as_uint(in.imm) : ((uint32_t)in.imm & 255u);
                 break;
+            case NT2G_OP_INDEX:  // enumerate<T>(p): float(p) rounds to nearest; uint8 wraps
+#pragma unroll
+                for (int j = 0; j < kV; ++j) {
+                    const long long p = args.pos0 + base + j;
+                    d[j] = f32 ? __float_as_uint(__ll2float_rn(p)) : (uint32_t)(p & 255);
+                }
+                break;
             case NT2G_OP_STORE:
                 if (f32) {
                     float *p = (float *)args.ptr[in.b] + base;

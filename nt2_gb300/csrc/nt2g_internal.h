@@ -38,6 +38,7 @@ struct DArgs {
     float scal[kMaxSlots];
     uint32_t scal_u8[kMaxSlots];
     int32_t dtype[kMaxSlots];
+    int64_t pos0;  // linear position of element 0 of the evaluated range (INDEX leaves)
 };
 
 // Fused kernels a program can bind to.

@@ -16,6 +16,7 @@
 // dispatch and no register file in memory.  NVRTC is opened with dlopen: when
 // it is not installed the generic path stays on the interpreter.
 #include <dlfcn.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -80,7 +81,7 @@ static Nvrtc &nvrtc()
 // table when every table is aligned, one 32-bit word per uint8 table), so a
 // value is a 4-lane array that the compiler keeps in registers.
 static const char kJitPrelude[] = R"NT2G_SRC(
-struct JitArgs { void *ptr[16]; float scal[16]; unsigned scal_u8[16]; int dtype[16]; };
+struct JitArgs { void *ptr[16]; float scal[16]; unsigned scal_u8[16]; int dtype[16]; long long pos0; };
 #define NT2G_L _Pragma("unroll") for (int j = 0; j < 4; ++j)
 template <bool FULL> __device__ __forceinline__ void jit_ldf(float (&d)[4], const void *p, long long i, int cnt)
 {
@@ -149,6 +150,7 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         }
         case NT2G_OP_SCALAR: e = f32 ? "a.scal[" + slot + "]" : "a.scal_u8[" + slot + "]"; break;
         case NT2G_OP_CONST: e = f32 ? fconst(o.imm) : std::to_string((uint32_t)o.imm & 255u) + "u"; break;
+        case NT2G_OP_INDEX: e = f32 ? "__ll2float_rn(a.pos0 + i + j)" : "(unsigned)((a.pos0 + i + j) & 255)"; break;
         case NT2G_OP_ADD: e = f32 ? "P::add(" + A + ", " + B + ")" : "(" + A + " + " + B + ") & 255u"; break;
         case NT2G_OP_SUB: e = f32 ? "P::sub(" + A + ", " + B + ")" : "(" + A + " - " + B + ") & 255u"; break;
         case NT2G_OP_MUL: e = f32 ? "P::mul(" + A + ", " + B + ")" : "(" + A + " * " + B + ") & 255u"; break;
@@ -306,7 +308,8 @@ nt2g_status jit_prepare(const std::vector<nt2g_op> &ops, const std::vector<uint8
 nt2g_status launch_jit(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, const DArgs &args,
                        int64_t count, int precision, cudaStream_t st)
 {
-    static_assert(sizeof(DArgs) == 16 * sizeof(void *) + 3 * 16 * 4, "JitArgs layout");
+    static_assert(sizeof(DArgs) == 16 * sizeof(void *) + 3 * 16 * 4 + 8 && offsetof(DArgs, pos0) == 16 * 8 + 3 * 16 * 4,
+                  "JitArgs layout");
     if (!jit_enabled()) return NT2G_ERR_UNSUPPORTED;
     JitEntry *e = jit_get(ops, logical, precision, nullptr);
     if (!e) return NT2G_ERR_UNSUPPORTED;

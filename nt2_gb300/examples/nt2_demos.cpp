@@ -11,6 +11,7 @@
 //        nt2_demos bs|bs_host|bs_demo|saxpy|rgb2yuv DIR N
 //        nt2_demos sdot DIR N
 //        nt2_demos fold DIR M N
+//        nt2_demos gen DIR N
 //        nt2_demos sigmadelta DIR PIXELS FRAMES
 // Inputs and outputs are raw little-endian arrays DIR/<name>.bin.
 #include <cstdio>
@@ -210,6 +211,22 @@ int main(int argc, char **argv)
                         "globalasum1 %.9g\n",
                         (double)gmax, (long long)imax, (double)gmin, (long long)imin, (double)nt2::globalmean(A),
                         (double)nt2::globalnorm2(A), (double)nt2::globalasum1(A));
+        } else if (mode == "gen") {
+            // generative leaves: NT2's colon (also spelled _), linspace, logspace, alone and in expressions
+            using nt2::_;
+            dtable c1, c2, c3, l1, l2, g1, g2, w;
+            c1 = _(0.f, 9.f);
+            c2 = _(0.f, 0.3f, 1.f);
+            c3 = nt2::colon(1.f, -0.3f, 0.f);
+            l1 = nt2::linspace(-1.f, 1.f, 257);
+            l2 = nt2::linspace(0.f, 1.f);
+            g1 = nt2::logspace(0.f, 1.f);
+            g2 = nt2::logspace(2.f, 3.14159274f, 7);
+            w = nt2::sinpi(nt2::linspace(0.f, 2.f, n)) * nt2::colon(1.f, (float)n);
+            for (auto *t : {&c1, &c2, &c3, &l1, &l2, &g1, &g2, &w}) std::printf("%zu\n", t->numel());
+            save(dir + "c1.bin", c1); save(dir + "c2.bin", c2); save(dir + "c3.bin", c3);
+            save(dir + "l1.bin", l1); save(dir + "l2.bin", l2); save(dir + "g1.bin", g1); save(dir + "g2.bin", g2);
+            save(dir + "w.bin", w);
         } else if (mode == "sigmadelta") {
             const std::size_t frames = std::strtoull(argv[4], nullptr, 10);
             auto all = read_bin<std::uint8_t>(dir + "frames.bin", n * frames);

@@ -20,10 +20,11 @@ from . import lib
 
 
 class Node:
-    __slots__ = ("op", "args", "dtype", "imm", "table")
+    __slots__ = ("op", "args", "dtype", "imm", "table", "numel")
 
-    def __init__(self, op, args=(), dtype=lib.F32, imm=0.0, table=None):
+    def __init__(self, op, args=(), dtype=lib.F32, imm=0.0, table=None, numel=None):
         self.op, self.args, self.dtype, self.imm, self.table = op, tuple(args), dtype, imm, table
+        self.numel = numel  # element count of a generative (INDEX) leaf
 
     # arithmetic
     def __add__(self, o): return _bin("ADD", self, o)
@@ -129,6 +130,108 @@ def seldec(c, a): return Node("SELDEC", (c, a), a.dtype)
 def if_zero_else_one(c, dtype): return Node("IF_ZERO_ELSE_ONE", (c,), dtype)
 
 
+# ------------------------------------------------------------------ generative
+# colon / linspace / logspace over the element position p (NT2's
+# enumerate<T>(p), the INDEX leaf); sizes and steps in float32 with every step
+# rounded, as NT2 computes them (modules/core/generative/include/nt2/core/
+# functions/scalar/{colon,linspace,logspace}.hpp, details/*.hpp,
+# modules/core/fuzzy/include/nt2/fuzzy/functions/scalar/tolerant_floor.hpp).
+
+def _index(n):
+    return Node("INDEX", (), lib.F32, numel=int(n))
+
+
+def _generative_sizes(e, seen=None):
+    seen = set() if seen is None else seen
+    if id(e) in seen or not isinstance(e, Node):
+        return []
+    seen.add(id(e))
+    out = [e.numel] if e.op == "INDEX" else []
+    for a in e.args:
+        out += _generative_sizes(a, seen)
+    return out
+
+
+
+def _tolerant_floor(a0):
+    import numpy as np
+    f = np.float32
+    ct = f(3) * f(np.finfo(np.float32).eps)
+    q = f(1) - ct if a0 < 0 else f(1)
+    rmax = q / (f(2) - ct)
+    t1 = f(1) + np.floor(a0)
+    t1 = (ct / q) * (-t1 if t1 < 0 else t1)
+    lo = rmax if rmax < t1 else t1
+    t1 = np.floor(a0 + (ct if ct > lo else lo))
+    return t1 if (a0 <= 0 or (t1 - a0) < rmax) else t1 - f(1)
+
+
+def _check_generative_sizes(exprs, count):
+    """NT2 assigns an expression only to a table of its own size: generative
+    leaves must have as many elements as the full assignment."""
+    sizes = {m for e in exprs for m in _generative_sizes(e)}
+    if sizes and sizes != {count}:
+        raise ValueError(f"generative operands of {sorted(sizes)} elements assigned to {count}")
+
+
+def colon_count(l, s, u):
+    """NT2's element count of colon(l, s, u) on floats."""
+    import numpy as np
+    f = np.float32
+    l, s, u = f(l), f(s), f(u)
+    if not s:
+        return int(u)
+    if not ((u - l) * s >= 0):
+        return 0
+    nelt = int(_tolerant_floor((u - l + s) / s))
+    eps3 = f(3) * f(np.finfo(np.float32).eps)
+
+    def feq(a, b):
+        return abs(a - b) <= eps3 * max(abs(a), abs(b))
+    if not feq(l + f(nelt - 1) * s, u):
+        if feq(l + f(nelt - 2) * s, u):
+            return nelt - 1
+        if feq(l + f(nelt) * s, u):
+            return nelt + 1
+    return nelt
+
+
+def colon(l, s_or_u, u=None):
+    """colon(l, u) = l + p over u-l+1 elements; colon(l, s, u) = fma(p, s, l)."""
+    import numpy as np
+    if u is None:
+        lf, uf = np.float32(l), np.float32(s_or_u)
+        n = int(uf - lf + np.float32(1)) if uf >= lf else 0
+        return Node("ADD", (_index(n), _wrap(float(lf), lib.F32)), lib.F32)
+    n = colon_count(l, s_or_u, u)
+    return Node("FMA", (_index(n), _wrap(float(np.float32(s_or_u)), lib.F32), _wrap(float(np.float32(l)), lib.F32)),
+                lib.F32)
+
+
+def linspace(l, u, n=100):
+    """n points from l to u: p == n-1 ? u : fma(p, (u-l)/(n-1), l)."""
+    import numpy as np
+    f = np.float32
+    lo = f(u) if n < 2 else f(l)
+    m = 2 if n < 2 else n
+    step = (f(u) - lo) / f(m - 1)
+    p = _index(n)
+    last = Node("EQ", (p, _wrap(float(f(m - 1)), lib.F32)), lib.F32)
+    return if_else(last, float(f(u)), Node("FMA", (p, _wrap(float(step), lib.F32), _wrap(float(lo), lib.F32)), lib.F32))
+
+
+def logspace(l, u, n=50, regular=False):
+    """exp10(fma(p, step, lower)); u == pi stands for log10(pi) unless regular."""
+    import numpy as np
+    f = np.float32
+    u = f(u)
+    if not regular and u == np.uint32(0x40490fdb).view(np.float32):
+        u = np.uint32(0x3efe8a6e).view(np.float32)
+    lower = f(l) if n != 1 else u
+    step = (u - f(l)) / f(n - 1) if n != 1 else f(0)
+    return exp10(Node("FMA", (_index(n), _wrap(float(step), lib.F32), _wrap(float(lower), lib.F32)), lib.F32))
+
+
 def _compare_dtype(n):
     return n.args[0].dtype
 
@@ -159,6 +262,8 @@ def lower(outs, exprs):
             ops.append((lib.OP["SCALAR"], n.dtype, s, -1, -1, 0.0))
         elif n.op == "CONST":
             ops.append((lib.OP["CONST"], n.dtype, -1, -1, -1, n.imm))
+        elif n.op == "INDEX":
+            ops.append((lib.OP["INDEX"], n.dtype, -1, -1, -1, 0.0))
         else:
             a = [emit(x) for x in n.args] + [-1, -1, -1]
             dt = _compare_dtype(n) if n.op in ("LT", "GT", "LE", "GE", "EQ", "NE") else n.dtype
@@ -237,6 +342,7 @@ def assign(outs, exprs, precision=lib.PREC_FAST, offset=0, count=None, force_gen
             args[i] = lib.Arg(s.data_ptr(), 0.0, lib.U8 if s.dtype == torch.uint8 else lib.F32, 0)
     if count is None:
         count = n - offset
+        _check_generative_sizes(exprs, count)
     lib.check(lib.load().nt2g_eval(prog.handle, args, len(slots), offset, count, precision,
                                    int(force_generic), lib._stream(stream)))
     return prog

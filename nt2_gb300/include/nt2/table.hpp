@@ -27,6 +27,7 @@
 // functions/cuda/copy.hpp:52-86).
 #pragma once
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -439,7 +440,7 @@ namespace detail {
 // agree (NT2 asserts the same in run_assign).
 inline std::size_t extent_of(const node *n)
 {
-    if (n->op == NT2G_OP_LOAD) return n->numel;
+    if (n->op == NT2G_OP_LOAD || n->op == NT2G_OP_INDEX) return n->numel;
     std::size_t e = 0;
     for (const node *c : {n->a.get(), n->b.get(), n->c.get()}) {
         if (!c) continue;
@@ -639,6 +640,99 @@ expr<T> seldec(const C &cond, const A &a)
     return expr<T>{detail::make(NT2G_OP_SELDEC, detail::dtype_of<T>::value, detail::lift(cond), detail::lift(a))};
 }
 
+// ------------------------------------------------------------ generative --
+// colon, linspace and logspace are expressions over the element's position p
+// (NT2's enumerate<T>(p), the INDEX leaf), with NT2's sizes and values:
+//   colon(l, u)     l + p, 1 x (u-l+1) elements      (generative/functions/scalar/colon.hpp:24-47,
+//                                                     details/colon.hpp unity_colon_size/value)
+//   colon(l, s, u)  fma(p, s, l), fuzzy element count (scalar/colon.hpp:127-160, details/colon.hpp
+//                                                     colon_value; fuzzy/scalar/tolerant_floor.hpp)
+//   linspace(l,u,n) p == n-1 ? u : fma(p, (u-l)/(n-1), l); n defaults to 100, n < 2 gives u
+//                                                    (scalar/linspace.hpp, details/linspace.hpp)
+//   logspace(l,u,n) exp10(fma(p, step, lower)), u == pi means log10(pi); n defaults to 50
+//                                                    (scalar/logspace.hpp, details/logspace.hpp)
+// The host-side sizes and steps use float arithmetic with every step rounded.
+namespace detail {
+inline float fsub(float a, float b) { volatile float r = a - b; return r; }
+inline float fadd(float a, float b) { volatile float r = a + b; return r; }
+inline float fmul(float a, float b) { volatile float r = a * b; return r; }
+inline float fdiv(float a, float b) { volatile float r = a / b; return r; }
+inline node_ptr index_leaf(std::size_t n)
+{
+    auto p = make(NT2G_OP_INDEX, NT2G_F32);
+    p->numel = n;
+    return p;
+}
+inline node_ptr cst(float v) { return lift_scalar<float>(v); }
+inline float bits_f(std::uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+// Hagerty's FL5 tolerant floor (fuzzy/functions/scalar/tolerant_floor.hpp:33-44)
+inline float tolerant_floor(float a0)
+{
+    const float ct = 3.0f * 1.1920929e-7f;  // Threeeps
+    const float q = a0 < 0.0f ? fsub(1.0f, ct) : 1.0f;
+    const float rmax = fdiv(q, fsub(2.0f, ct));
+    float t1 = fadd(1.0f, std::floor(a0));
+    t1 = fmul(fdiv(ct, q), t1 < 0.0f ? -t1 : t1);
+    const float lo = rmax < t1 ? rmax : t1;  // NT2 min(rmax, t1) = rmax < t1 ? rmax : t1
+    t1 = std::floor(fadd(a0, ct > lo ? ct : lo));
+    return (a0 <= 0.0f || fsub(t1, a0) < rmax) ? t1 : fsub(t1, 1.0f);
+}
+inline bool fuzzy_equal(float a, float b, float tol)
+{
+    const float d = std::fabs(fsub(a, b));
+    const float fa = std::fabs(a), fb = std::fabs(b);
+    return d <= fmul(tol, fa > fb ? fa : fb);
+}
+inline std::size_t colon_count(float l, float s, float u)
+{
+    if (!s) return (std::size_t)u;
+    if (!(fmul(fsub(u, l), s) >= 0.0f)) return 0;
+    const std::size_t nelt = (std::size_t)tolerant_floor(fdiv(fadd(fsub(u, l), s), s));
+    const float eps3 = 3.0f * 1.1920929e-7f;
+    if (!fuzzy_equal(fadd(l, fmul((float)(nelt - 1), s)), u, eps3)) {
+        if (fuzzy_equal(fadd(l, fmul((float)(nelt - 2), s)), u, eps3)) return nelt - 1;
+        if (fuzzy_equal(fadd(l, fmul((float)nelt, s)), u, eps3)) return nelt + 1;
+    }
+    return nelt;
+}
+}  // namespace detail
+
+inline expr<float> colon(float l, float u)
+{
+    const std::size_t n = u >= l ? (std::size_t)detail::fadd(detail::fsub(u, l), 1.0f) : 0;
+    return expr<float>{detail::make(NT2G_OP_ADD, NT2G_F32, detail::index_leaf(n), detail::cst(l))};
+}
+inline expr<float> colon(float l, float s, float u)
+{
+    return expr<float>{detail::make(NT2G_OP_FMA, NT2G_F32, detail::index_leaf(detail::colon_count(l, s, u)),
+                                    detail::cst(s), detail::cst(l))};
+}
+// NT2's _(l, u) / _(l, s, u) spelling of colon
+struct colon_placeholder {
+    expr<float> operator()(float l, float u) const { return colon(l, u); }
+    expr<float> operator()(float l, float s, float u) const { return colon(l, s, u); }
+};
+inline constexpr colon_placeholder _{};
+
+inline expr<float> linspace(float l, float u, std::size_t n = 100)
+{
+    const float lo = n < 2 ? u : l;
+    const std::size_t m = n < 2 ? 2 : n;
+    const float step = detail::fdiv(detail::fsub(u, lo), (float)(m - 1));
+    auto p = detail::index_leaf(n);
+    auto last = detail::make(NT2G_OP_EQ, NT2G_F32, p, detail::cst((float)(m - 1)));
+    auto line = detail::make(NT2G_OP_FMA, NT2G_F32, p, detail::cst(step), detail::cst(lo));
+    return expr<float>{detail::make(NT2G_OP_IF_ELSE, NT2G_F32, last, detail::cst(u), line)};
+}
+inline expr<float> logspace(float l, float u, std::size_t n = 50, bool regular = false)
+{
+    if (!regular && u == detail::bits_f(0x40490fdbu)) u = detail::bits_f(0x3efe8a6eu);  // Pi -> Log10_pi
+    const float lower = n != 1 ? l : u;
+    const float step = n != 1 ? detail::fdiv(detail::fsub(u, l), (float)(n - 1)) : 0.0f;
+    auto line = detail::make(NT2G_OP_FMA, NT2G_F32, detail::index_leaf(n), detail::cst(step), detail::cst(lower));
+    return expr<float>{detail::make(NT2G_OP_EXP10, NT2G_F32, line)};
+}
+
 // if_zero_else_one on a logical yields the element type of the comparison
 template <class T> expr<T> if_zero_else_one(const expr<T> &cond)
 {
@@ -705,7 +799,7 @@ inline double sum_node(const node_ptr &n)
     while (!stack.empty()) {
         const node *m = stack.back();
         stack.pop_back();
-        if (m->op == NT2G_OP_LOAD) numel = numel ? std::min(numel, m->numel) : m->numel;
+        if (m->op == NT2G_OP_LOAD || m->op == NT2G_OP_INDEX) numel = numel ? std::min(numel, m->numel) : m->numel;
         for (const node *c : {m->a.get(), m->b.get(), m->c.get()})
             if (c) stack.push_back(c);
     }

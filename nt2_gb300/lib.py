@@ -20,7 +20,7 @@ F32, U8 = 0, 1
 
 # opcodes (values fixed by nt2g.h; tests check they agree with the header)
 OP = dict(
-    LOAD=1, SCALAR=2, CONST=3, STORE=4,
+    LOAD=1, SCALAR=2, CONST=3, STORE=4, INDEX=5,
     ADD=10, SUB=11, MUL=12, DIV=13, NEG=14, ABS=15, SQR=16, SQRT=17, REC=18, MIN=19, MAX=20,
     FMA=30, FNMS=31,
     EXP=40, LOG=41, LOG1P=42, ERFC=43, NORMCDF=44, FASTNORMCDF=45, EXP2=46, EXP10=47, EXPM1=48, LOG2=49, LOG10=50,

@@ -269,3 +269,78 @@ def exact_sum(x, y=None, nthreads=None):
 
 def nt2_transform_grain(elem_size=4):
     return lib().o_nt2_transform_grain(elem_size)
+
+
+# --------------------------------------------------------------- generative
+# NT2's colon / linspace / logspace restated in numpy float32 (each operation
+# rounded, no fusion): values at positions 0..n-1 and NT2's element counts.
+#   unity colon  l + p, size (u >= l) ? size_t(u - l + 1) : 0
+#                (modules/core/generative/include/nt2/core/functions/scalar/colon.hpp:24-47,
+#                 details/colon.hpp unity_colon_size / unity_colon_value)
+#   colon        fma(p, s, l) = p*s + l, size by tolerant_floor and fuzzy_equal
+#                (scalar/colon.hpp:127-160, modules/core/fuzzy/include/nt2/fuzzy/functions/
+#                 scalar/{tolerant_floor,fuzzy_equal}.hpp)
+#   linspace     p == n-1 ? u : p*step + l, step = (u-l)/(n-1); n < 2 uses (u, u, 2)
+#                (scalar/linspace.hpp, details/linspace.hpp)
+#   logspace     exp10(p*step + lower) (scalar/logspace.hpp, details/logspace.hpp)
+
+def _tfloor(a0):
+    f = np.float32
+    ct = f(3.0) * f(2.0 ** -23)
+    q = f(1) - ct if a0 < 0 else f(1)
+    rmax = q / (f(2) - ct)
+    t1 = f(1) + f(np.floor(a0))
+    t1 = (ct / q) * (-t1 if t1 < 0 else t1)
+    t1 = f(np.floor(a0 + max(ct, min(rmax, t1))))
+    return t1 if (a0 <= 0 or (t1 - a0) < rmax) else t1 - f(1)
+
+
+def colon_size_nt2(l, s, u):
+    f = np.float32
+    l, s, u = f(l), f(s), f(u)
+    if s == 0:
+        return int(u)
+    if not ((u - l) * s >= 0):
+        return 0
+    nelt = int(_tfloor((u - l + s) / s))
+    e3 = f(3.0) * f(2.0 ** -23)
+    close = lambda a, b: abs(a - b) <= e3 * max(abs(a), abs(b))  # noqa: E731
+    if not close(l + f(nelt - 1) * s, u):
+        if close(l + f(nelt - 2) * s, u):
+            return nelt - 1
+        if close(l + f(nelt) * s, u):
+            return nelt + 1
+    return nelt
+
+
+def _pos(n, offset=0):
+    return (np.arange(offset, offset + n, dtype=np.int64)).astype(np.float32)
+
+
+def colon_nt2(l, s, u=None):
+    f = np.float32
+    if u is None:
+        l, u = f(l), f(s)
+        n = int(u - l + f(1)) if u >= l else 0
+        return _pos(n) + l
+    n = colon_size_nt2(l, s, u)
+    return _pos(n) * f(s) + f(l)
+
+
+def linspace_nt2(l, u, n=100):
+    f = np.float32
+    lo = f(u) if n < 2 else f(l)
+    m = 2 if n < 2 else n
+    step = (f(u) - lo) / f(m - 1)
+    p = _pos(n)
+    return np.where(p == f(m - 1), f(u), p * step + lo).astype(np.float32)
+
+
+def logspace_nt2(l, u, n=50, regular=False):
+    f = np.float32
+    u = f(u)
+    if not regular and u == np.uint32(0x40490fdb).view(np.float32):
+        u = np.uint32(0x3efe8a6e).view(np.float32)
+    lower = f(l) if n != 1 else u
+    step = (u - f(l)) / f(n - 1) if n != 1 else f(0)
+    return map_f32("exp10", _pos(n) * step + lower)
