@@ -76,6 +76,7 @@ typedef enum nt2g_opcode {
     NT2G_OP_FASTNORMCDF,
     NT2G_OP_EXP2 = 46, NT2G_OP_EXP10, NT2G_OP_EXPM1, NT2G_OP_LOG2, NT2G_OP_LOG10,
     NT2G_OP_SIN = 51, NT2G_OP_COS, NT2G_OP_TAN, NT2G_OP_SINPI, NT2G_OP_COSPI,
+    NT2G_OP_POW = 56,      /* a^b (float)                                    */
     NT2G_OP_LT = 60, NT2G_OP_GT, NT2G_OP_LE, NT2G_OP_GE, NT2G_OP_EQ, NT2G_OP_NE, /* -> logical */
     NT2G_OP_IF_ELSE = 70,  /* a ? b : c                                      */
     NT2G_OP_SELINC,        /* a ? b+1 : b                                    */

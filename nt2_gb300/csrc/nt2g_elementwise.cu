@@ -573,6 +573,10 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                     }
                 }
                 break;
+            case NT2G_OP_POW:
+                for (int j = 0; j < kV; ++j)
+                    d[j] = __float_as_uint(pow<P>(__uint_as_float(A[j]), __uint_as_float(B[j])));
+                break;
             case NT2G_OP_FMA: case NT2G_OP_FNMS:
 #pragma unroll
                 for (int j = 0; j < kV; ++j) {

@@ -159,6 +159,7 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_MAX: e = "(" + A + " > " + B + " ? " + A + " : " + B + ")"; break;  // NT2: a > b ? a : b
         case NT2G_OP_ADDS: e = "((" + A + " + " + B + ") > 255u ? 255u : (" + A + " + " + B + "))"; break;
         case NT2G_OP_FMA: e = "P::fma(" + A + ", " + B + ", " + C + ")"; break;
+        case NT2G_OP_POW: e = "nt2g::pow<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_FNMS: e = "P::fma(-" + A + ", " + B + ", " + C + ")"; break;
         case NT2G_OP_LT: e = "(" + A + " < " + B + ") ? 1u : 0u"; break;
         case NT2G_OP_GT: e = "(" + A + " > " + B + ") ? 1u : 0u"; break;

@@ -558,6 +558,188 @@ template <class P> NT2G_HD float exp_neg_sqr(float x)
     return is_nan(x) ? x : r;
 }
 
+// ------------------------------------------------------------------- pow --
+// NT2's float pow (exponential/functions/scalar/pow.hpp:28-36 over
+// pow_abs.hpp:31-84 and details/pow_kernel.hpp:43-125, Cephes' powf): x = |a|
+// split by frexp, log2 of the significand against a 2^(-i/16) table, the
+// product with b carried in multiples of 1/16 plus remainders, then 2^w from a
+// degree-4 polynomial, the table and ldexp.  Special values as NT2 has them:
+// pow(+-1 magnitude ...) = 1, pow(0, b) = (b == 0), NaN for a < 0 and a
+// non-integer b, the sign of a for odd integer b.
+NT2G_HD float pow_twomio16(int i)  // 2^(-i/16) rounded to 24 bits, i in [0, 16]
+{
+    switch (i) {
+    case 0: return bits_f(0x3f800000u);  case 1: return bits_f(0x3f75257du);
+    case 2: return bits_f(0x3f6ac0c7u);  case 3: return bits_f(0x3f60ccdfu);
+    case 4: return bits_f(0x3f5744fdu);  case 5: return bits_f(0x3f4e248cu);
+    case 6: return bits_f(0x3f45672au);  case 7: return bits_f(0x3f3d08a4u);
+    case 8: return bits_f(0x3f3504f3u);  case 9: return bits_f(0x3f2d583fu);
+    case 10: return bits_f(0x3f25fed7u); case 11: return bits_f(0x3f1ef532u);
+    case 12: return bits_f(0x3f1837f0u); case 13: return bits_f(0x3f11c3d3u);
+    case 14: return bits_f(0x3f0b95c2u); case 15: return bits_f(0x3f05aac3u);
+    default: return bits_f(0x3f000000u);
+    }
+}
+
+NT2G_HD float pow_continuation(int i)  // 2^(i/8) - twomio16(2i), i in [0, 8]
+{
+    switch (i) {
+    case 1: return bits_f(0xb1c116deu); case 2: return bits_f(0xb254a58au);
+    case 3: return bits_f(0x318aa837u); case 4: return bits_f(0x324fe77au);
+    case 5: return bits_f(0xb2ac9d5eu); case 6: return bits_f(0x32a31b71u);
+    case 7: return bits_f(0xb1e0aba1u); default: return 0.0f;
+    }
+}
+
+// NT2's ldexp (boost/simd/ieee/functions/scalar/ldexp.hpp:37-51): a * 2^e * f,
+// with f = 2^-126 carrying exponents below -126 and f = 2 the exponent 128.
+template <class P> NT2G_HD float nt2_ldexp(float a, int e)
+{
+    float f = 1.0f;
+    if (e < -126) { e += 126; f = bits_f(0x00800000u); }
+    const int b = e == 128;
+    f = P::add(f, (float)b);
+    e = e - b + 127;
+    return P::mul(P::mul(a, bits_f((uint32_t)e << 23)), f);
+}
+
+NT2G_HD bool is_flint(float x) { return (x - truncf(x)) == 0.0f; }      // false for +-inf, NaN
+NT2G_HD bool is_odd_f(float x) { return is_flint((x - 1.0f) * 0.5f); }
+
+// Fast: this file's own pow for finite x > 0, x != 1: log2(x) in float-float
+// (x = 2^e m, m in [sqrt(1/2), sqrt(2)], log m = 2 atanh(s), s = (m-1)/(m+1)
+// carried as s_hi + s_lo, the series tail in float), times b in float-float,
+// then 2^(k + f) with k = round(p_hi), a degree-7 Taylor polynomial of 2^f and
+// the scale applied in two exact halves so subnormal results round once.
+NT2G_HD float pow_core_fast(float x, float y)
+{
+    int e = 0;
+    if (x < 1.17549435e-38f) { x = Fast::mul(x, 8388608.0f); e = -23; }
+    const uint32_t u = f_bits(x);
+    e += (int)(u >> 23) - 127;
+    float m = bits_f((u & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421354f) { m = Fast::mul(m, 0.5f); e += 1; }
+    const float num = Fast::sub(m, 1.0f);                       // exact
+    const float den = Fast::add(m, 1.0f);
+    const float den_lo = Fast::sub(m, Fast::sub(den, 1.0f));    // m + 1 = den + den_lo exactly
+    const float r = Fast::div(1.0f, den);
+    const float s_hi = Fast::mul(num, r);
+    const float res = Fast::fma(-s_hi, den_lo, Fast::fma(-s_hi, den, num));
+    const float s_lo = Fast::mul(res, r);
+    // log m = 2 s + (2/3) s^3 + s^5 R(s^2): s^3 and its (2/3) in float-float, the
+    // rest in float (it is below 2e-4 of log m)
+    const float q_hi = Fast::mul(s_hi, s_hi);
+    const float q_lo = Fast::fma(s_hi, s_hi, -q_hi);
+    const float c3_hi = Fast::mul(s_hi, q_hi);
+    const float c3_lo = Fast::fma(s_hi, q_lo, Fast::fma(s_hi, q_hi, -c3_hi));
+    const float TT_hi = 0x1.555556p-1f, TT_lo = -0x1.555556p-26f;  // 2/3
+    const float t3_hi = Fast::mul(c3_hi, TT_hi);
+    const float t3_lo = Fast::fma(c3_lo, TT_hi, Fast::fma(c3_hi, TT_lo, Fast::fma(c3_hi, TT_hi, -t3_hi)));
+    const float rest = Fast::mul(Fast::mul(c3_hi, q_hi),
+                                 horner<Fast>(q_hi, 0x1.3b13b2p-3f, 0x1.745d18p-3f, 0x1.c71c72p-3f, 0x1.24924ap-2f,
+                                              0x1.99999ap-2f));
+    // 2 s_lo (1 + s^2) carries s_lo through the first two terms
+    const float lo_sum = Fast::add(Fast::fma(2.0f * s_lo, q_hi, 2.0f * s_lo), Fast::add(t3_lo, rest));
+    const float h0 = Fast::add(s_hi, s_hi);
+    const float h = Fast::add(h0, t3_hi);
+    const float l = Fast::add(Fast::add(Fast::sub(h0, h), t3_hi), lo_sum);
+    const float l_hi = Fast::add(h, l);
+    const float l_lo = Fast::add(Fast::sub(h, l_hi), l);
+    // log2 m = log m * log2(e), log2(e) = C_hi + C_lo
+    const float C_hi = 0x1.715476p+0f, C_lo = 0x1.4ae0c0p-26f;
+    const float g_hi = Fast::mul(l_hi, C_hi);
+    const float g_lo = Fast::add(Fast::fma(l_hi, C_hi, -g_hi), Fast::fma(l_lo, C_hi, Fast::mul(l_hi, C_lo)));
+    // + e (|e| >= 1 > |g_hi| unless e = 0): fast two-sum
+    const float fe = (float)e;
+    const float t_hi = Fast::add(fe, g_hi);
+    const float t_lo = Fast::add(Fast::add(Fast::sub(fe, t_hi), g_hi), g_lo);
+    // p = y log2 x
+    const float p_hi = Fast::mul(y, t_hi);
+    const float p_lo = Fast::fma(y, t_lo, Fast::fma(y, t_hi, -p_hi));
+    if (!(p_hi < 129.0f)) return f_inf();
+    if (!(p_hi > -152.0f)) return 0.0f;
+    const float k = rintf(p_hi);
+    const float f = Fast::add(Fast::sub(p_hi, k), p_lo);       // |f| <= 1/2 + tiny
+    const float c = horner<Fast>(f, 0x1.ffcbfcp-17f, 0x1.430912p-13f, 0x1.5d87fep-10f, 0x1.3b2ab6p-7f,
+                                 0x1.c6b08ep-5f, 0x1.ebfbe0p-3f, 0x1.62e430p-1f);
+    const float v = Fast::fma(c, f, 1.0f);
+    const int ki = (int)k, k1 = ki >> 1, k2 = ki - k1;             // each within [-76, 65]
+    return Fast::mul(Fast::mul(v, bits_f((uint32_t)(k1 + 127) << 23)), bits_f((uint32_t)(k2 + 127) << 23));
+}
+
+template <class P> NT2G_HD float pow_abs(float a0, float a1)
+{
+    float x = fabsf(a0);
+    if (x == 1.0f) return x;
+    if (x == 0.0f) return a1 == 0.0f ? 1.0f : 0.0f;
+    if (x == a1 && a1 == f_inf()) return f_inf();
+    if (x == f_inf() && a1 == -f_inf()) return 0.0f;
+    if (a1 == f_inf()) return (x < 1.0f) ? 0.0f : f_inf();
+    if (a1 == -f_inf()) return (x > 1.0f) ? 0.0f : f_inf();
+    if (x == f_inf()) return (a1 < 0.0f) ? 0.0f : ((a1 == 0.0f) ? 1.0f : f_inf());
+    if (is_nan(a0) || is_nan(a1)) return f_nan();
+    if (!P::exact) return pow_core_fast(x, a1);
+    // frexp: x = m 2^e, m in [1/2, 1) (denormals through a 2^23 scale)
+    int e;
+    {
+        uint32_t u = f_bits(x);
+        int t = 0;
+        if ((u & 0x7f800000u) == 0) { u = f_bits(P::mul(x, 8388608.0f)); t = 23; }
+        e = (int)((u & 0x7f800000u) >> 23) - 126 - t;
+        x = bits_f((u & ~0x7f800000u) | 0x3f000000u);
+    }
+    // select: the table entry nearest below m (pow_kernel.hpp:111-125)
+    int i = 1;
+    if (x <= pow_twomio16(9)) i = 9;
+    if (x <= pow_twomio16(i + 4)) i += 4;
+    if (x <= pow_twomio16(i + 2)) i += 2;
+    if (x >= pow_twomio16(1)) i = -1;
+    i += 1;
+    const float tmp = pow_twomio16(i);
+    x = P::sub(x, tmp);
+    x = P::sub(x, pow_continuation(i >> 1));
+    x = P::div(x, tmp);
+    float z = P::mul(x, x);
+    float w = P::mul(P::mul(z, x), horner<P>(x, bits_f(0xbe2a61b2u), bits_f(0x3e4d2fa3u), bits_f(0xbe800015u),
+                                                 bits_f(0x3eaaaaa3u)));
+    w = P::fma(-0.5f, z, w);
+    w = P::fma(bits_f(NT2G_LOG2_EM1), w, w);
+    z = P::fma(bits_f(NT2G_LOG2_EM1), x, w);
+    z = P::add(z, x);
+    w = P::fma((float)(-i), 0.0625f, (float)e);
+    // b log2(x) in multiples of 1/16 plus remainders (reduc: a multiple of 1/16 within 1/16)
+    const float ya = P::mul(0.0625f, floorf(P::mul(16.0f, a1)));
+    const float yb = P::sub(a1, ya);
+    float W = P::fma(z, a1, P::mul(w, yb));
+    float Wa = P::mul(0.0625f, floorf(P::mul(16.0f, W)));
+    float Wb = P::sub(W, Wa);
+    W = P::fma(w, ya, Wa);
+    Wa = P::mul(0.0625f, floorf(P::mul(16.0f, W)));
+    const float u = P::sub(W, Wa);
+    W = P::add(Wb, u);
+    Wb = P::mul(0.0625f, floorf(P::mul(16.0f, W)));
+    w = P::mul(16.0f, P::add(Wa, Wb));
+    if (w > bits_f(0x44ffe000u)) return f_inf();  // Powlargelim
+    if (w < bits_f(0xc5160000u)) return 0.0f;     // Powlowlim
+    e = (int)w;
+    Wb = P::sub(W, Wb);
+    if (Wb > 0.0f) { ++e; Wb = P::sub(Wb, 0.0625f); }
+    z = P::mul(horner<P>(Wb, bits_f(0x3c1a49bcu), bits_f(0x3d634d38u), bits_f(0x3e75fde1u), bits_f(0x3f317218u)), Wb);
+    i = e / 16 + (e >= 0);
+    e = i * 16 - e;
+    w = pow_twomio16(e);
+    z = P::fma(w, z, w);
+    return nt2_ldexp<P>(z, i);
+}
+
+template <class P> NT2G_HD float pow(float a0, float a1)
+{
+    const bool neg = a0 < 0.0f;
+    if (neg && !is_flint(a1)) return f_nan();
+    const float z = pow_abs<P>(a0, a1);
+    return (neg && is_odd_f(a1)) ? -z : z;
+}
+
 // ----------------------------------------------------------- trigonometry --
 // NT2 (modules/core/trigonometric/include/nt2/trigonometric/functions/):
 //   sin/cos/tan   scalar/impl/trigo/trig_base.hpp:131-176 (regular style,

@@ -1,7 +1,7 @@
 """A Python mirror of NT2's expression surface over device tables.
 
 ``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
-(exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, sinpi, cospi,
+(exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, sinpi, cospi, pow,
 erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms, min, max, if_else,
 selinc, seldec, if_zero_else_one, adds) build an expression
 tree; ``assign(outs, exprs)`` is ``tie(outs...) = tie(exprs...)``: it lowers
@@ -113,6 +113,13 @@ def fnms(a, b, c):
         return float(_f32(c) - _f32(_f32(a) * _f32(b)))
     dt = next(x.dtype for x in (a, b, c) if isinstance(x, Node))
     return Node("FNMS", tuple(_wrap(x, dt) for x in (a, b, c)), dt)
+
+
+def pow(a, b):
+    """a^b with NT2's semantics (NaN for a < 0 and non-integer b, pow(0, b) = (b == 0))."""
+    if not any(isinstance(x, Node) for x in (a, b)):
+        raise TypeError("pow of two numbers: use Python's ** (NT2's scalar pow is not mirrored here)")
+    return _bin("POW", a, b)
 
 
 def min_(a, b): return _bin("MIN", a, b)

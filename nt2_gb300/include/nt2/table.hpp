@@ -569,6 +569,7 @@ NT2G_BINARY(operator!=, NT2G_OP_NE, true)
 NT2G_BINARY(min, NT2G_OP_MIN, false)
 NT2G_BINARY(max, NT2G_OP_MAX, false)
 NT2G_BINARY(adds, NT2G_OP_ADDS, false)
+NT2G_BINARY(pow, NT2G_OP_POW, false)
 #undef NT2G_BINARY
 
 #define NT2G_UNARY(NAME, CODE)                                                                                   \

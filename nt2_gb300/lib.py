@@ -24,7 +24,7 @@ OP = dict(
     ADD=10, SUB=11, MUL=12, DIV=13, NEG=14, ABS=15, SQR=16, SQRT=17, REC=18, MIN=19, MAX=20,
     FMA=30, FNMS=31,
     EXP=40, LOG=41, LOG1P=42, ERFC=43, NORMCDF=44, FASTNORMCDF=45, EXP2=46, EXP10=47, EXPM1=48, LOG2=49, LOG10=50,
-    SIN=51, COS=52, TAN=53, SINPI=54, COSPI=55,
+    SIN=51, COS=52, TAN=53, SINPI=54, COSPI=55, POW=56,
     LT=60, GT=61, LE=62, GE=63, EQ=64, NE=65,
     IF_ELSE=70, SELINC=71, SELDEC=72, IF_ZERO_ELSE_ONE=73, ADDS=74,
 )

@@ -276,6 +276,108 @@ EXPORT float o_expm1(float a0)
     return y * o_pow2i(k);
 }
 
+/* ---------------------------------------------------------------- pow ----
+ * EXP/scalar/pow.hpp:28-36, EXP/scalar/pow_abs.hpp:31-84 and the float
+ * kernel EXP/details/pow_kernel.hpp:43-125 (Cephes powf: a 2^(-i/16) table,
+ * b log2|a| carried as multiples of 1/16 plus remainders), ldexp per
+ * BSIMD/ieee/functions/scalar/ldexp.hpp:37-51, frexp per frexp.hpp:30-60. */
+static const uint32_t POW_A[17] = {0x3f800000, 0x3f75257d, 0x3f6ac0c7, 0x3f60ccdf, 0x3f5744fd, 0x3f4e248c,
+                                   0x3f45672a, 0x3f3d08a4, 0x3f3504f3, 0x3f2d583f, 0x3f25fed7, 0x3f1ef532,
+                                   0x3f1837f0, 0x3f11c3d3, 0x3f0b95c2, 0x3f05aac3, 0x3f000000};
+static const uint32_t POW_B[9] = {0x0, 0xb1c116de, 0xb254a58a, 0x318aa837, 0x324fe77a,
+                                  0xb2ac9d5e, 0x32a31b71, 0xb1e0aba1, 0x0};
+static const uint32_t POW1_P[4] = {0xbe2a61b2, 0x3e4d2fa3, 0xbe800015, 0x3eaaaaa3};
+static const uint32_t POW2_P[4] = {0x3c1a49bc, 0x3d634d38, 0x3e75fde1, 0x3f317218};
+
+static float reduc16(float x) { return 0.0625f * floorf(16.0f * x); }
+
+static float nt2_ldexpf(float a, int e)
+{
+    float f = 1.0f;
+    if (e < -126) { e -= -126; f = bf(0x00800000u); }
+    int b = e == 128;
+    f += (float)b;
+    e -= b;
+    e += 127;
+    return a * bf((uint32_t)e << 23) * f;
+}
+
+static float pow_abs(float a0, float a1)
+{
+    float x = fabsf(a0);
+    if (x == 1.0f) return x;
+    if (x == 0.0f) return (float)(a1 == 0.0f);
+    if (x == a1 && a1 == INFINITY) return INFINITY;
+    if (x == INFINITY && a1 == -INFINITY) return 0.0f;
+    if (a1 == INFINITY) return (x < 1.0f) ? 0.0f : INFINITY;
+    if (a1 == -INFINITY) return (x > 1.0f) ? 0.0f : INFINITY;
+    if (x == INFINITY) return (a1 < 0.0f) ? 0.0f : ((a1 == 0.0f) ? 1.0f : INFINITY);
+    if (a0 != a0 || a1 != a1) return NAN;
+    int e = 0, t = 0;
+    uint32_t u = fb(x);
+    if ((u & 0x7f800000u) == 0) { x *= 8388608.0f; u = fb(x); t = 23; }
+    e = (int)((u & 0x7f800000u) >> 23) - 126 - t;
+    x = bf((u & ~0x7f800000u) | 0x3f000000u);
+    int i = 1;
+    if (x <= bf(POW_A[9])) i = 9;
+    if (x <= bf(POW_A[i + 4])) i += 4;
+    if (x <= bf(POW_A[i + 2])) i += 2;
+    if (x >= bf(POW_A[1])) i = -1;
+    i += 1;
+    float tmp = bf(POW_A[i]);
+    x -= tmp;
+    x -= bf(POW_B[i >> 1]);
+    x /= tmp;
+    float z = x * x;
+    float w = z * x * horner(x, POW1_P, 4);
+    w = -0.5f * z + w;
+    w = bf(0x3ee2a8edu) * w + w;
+    z = bf(0x3ee2a8edu) * x + w;
+    z += x;
+    w = (float)(-i) * 0.0625f + (float)e;
+    float ya = reduc16(a1), yb = a1 - ya;
+    float W = z * a1 + w * yb;
+    float Wa = reduc16(W), Wb = W - Wa;
+    W = w * ya + Wa;
+    Wa = reduc16(W);
+    float uu = W - Wa;
+    W = Wb + uu;
+    Wb = reduc16(W);
+    w = 16.0f * (Wa + Wb);
+    if (w > bf(0x44ffe000u)) return INFINITY;
+    if (w < bf(0xc5160000u)) return 0.0f;
+    e = (int)w;
+    Wb = W - Wb;
+    if (Wb > 0.0f) { ++e; Wb -= 0.0625f; }
+    z = horner(Wb, POW2_P, 4) * Wb;
+    i = e / 16 + (e >= 0);
+    e = i * 16 - e;
+    w = bf(POW_A[e]);
+    z = w * z + w;
+    return nt2_ldexpf(z, i);
+}
+
+static int flint(float x) { return (x - truncf(x)) == 0.0f; }
+
+EXPORT float o_pow(float a0, float a1)
+{
+    int ltz = a0 < 0.0f;
+    if (ltz && !flint(a1)) return NAN;
+    float z = pow_abs(a0, a1);
+    return (ltz && flint((a1 - 1.0f) * 0.5f)) ? -z : z;
+}
+
+EXPORT void o_pow_f32(const float *x, const float *y, float *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = o_pow(x[i], y[i]);
+}
+
+/* FP64 reference: libm pow on the float inputs */
+EXPORT void o_pow_f64(const float *x, const float *y, double *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = pow((double)x[i], (double)y[i]);
+}
+
 /* ------------------------------------------------------- trigonometry ----
  * NT2's float sin/cos/tan (TRIG/scalar/impl/trigo/trig_base.hpp:131-176,
  * regular style, big_ mode) and sinpi/cospi (pi_tag), every operation rounded:

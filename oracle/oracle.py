@@ -48,6 +48,10 @@ def lib():
             getattr(L, f).restype = ctypes.c_float
             getattr(L, f).argtypes = [ctypes.c_float]
         L.o_map_f32.argtypes = [ctypes.c_int, _P, _P, _I64]
+        L.o_pow.restype = ctypes.c_float
+        L.o_pow.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.o_pow_f32.argtypes = [_P, _P, _P, _I64]
+        L.o_pow_f64.argtypes = [_P, _P, _P, _I64]
         L.o_map_f64.argtypes = [ctypes.c_int, _P, _P, _I64]
         L.o_bs_f32.argtypes = [_P, _P, _P, _P, ctypes.c_float, _P, ctypes.c_float, _P, _P, _I64, ctypes.c_int]
         L.o_bs_demo_f32.argtypes = [_P, _P, _P, _P, ctypes.c_float, _P, ctypes.c_float, _P, _I64, ctypes.c_int]
@@ -100,6 +104,23 @@ def map_f64(fn, x):
     y = np.empty(x.shape, np.float64)
     lib().o_map_f64(FN[fn], _p(x), _p(y), x.size)
     return y
+
+
+def pow_f32(x, y):
+    """NT2's float pow restated (Cephes powf with NT2's special cases)."""
+    x, y = np.broadcast_arrays(_f32(x), _f32(y))
+    x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+    out = np.empty(x.size, np.float32)
+    lib().o_pow_f32(_p(x), _p(y), _p(out), x.size)
+    return out
+
+
+def pow_f64(x, y):
+    x, y = np.broadcast_arrays(_f32(x), _f32(y))
+    x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+    out = np.empty(x.size, np.float64)
+    lib().o_pow_f64(_p(x), _p(y), _p(out), x.size)
+    return out
 
 
 def threads():

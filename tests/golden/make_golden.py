@@ -75,6 +75,10 @@ def _value(expr):
 
 
 PAT = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(\w+)\((.*?)\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
+# two-argument functors: pow(a, b)
+ARG = r"((?:[^,()]|\([^()]*\))*)"
+PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow)\(" + ARG + r",\s*" + ARG + r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
+SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53)]
 
 
 def main(root):
@@ -87,6 +91,15 @@ def main(root):
                 continue
             fn, arg, exp, tol = m.groups()
             out.append(dict(fn=fn, x=_value(arg), expected=_value(exp), tol_nt2ulp=float(tol),
+                            source=f"{rel}:{ln}"))
+    for rel, lo, hi in SOURCES2:
+        lines = open(os.path.join(root, rel)).read().splitlines()
+        for ln in range(lo, hi + 1):
+            m = PAT2.search(lines[ln - 1])
+            if not m:
+                continue
+            fn, a0, a1, exp, tol = m.groups()
+            out.append(dict(fn=fn, x=_value(a0), y=_value(a1), expected=_value(exp), tol_nt2ulp=float(tol),
                             source=f"{rel}:{ln}"))
     # normcdf on _(-5, 1, 5) against the 11-value table r0, 5 NT2-ulp
     rel = "modules/core/statistics/unit/scalar/normcdf.cpp"

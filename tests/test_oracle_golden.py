@@ -23,6 +23,29 @@ def test_oracle_matches_nt2_unit_tests(oracle, rec):
     assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (got, rec)
 
 
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] == "pow"],
+                         ids=lambda r: f"pow({r['x']},{r['y']})@{r['source'].split('/')[-1]}")
+def test_oracle_pow_matches_nt2_unit_tests(oracle, rec):
+    got = oracle.lib().o_pow(rec["x"], rec["y"])
+    assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (got, rec)
+
+
+def test_oracle_pow_accuracy_profile(oracle):
+    """NT2's float pow (Cephes powf) as restated stays within 4 ulp of FP64
+    pow on finite normal results; its special cases as NT2 writes them."""
+    rng = np.random.default_rng(3)
+    x = np.exp(rng.uniform(-40, 40, 400000)).astype(np.float32)
+    y = rng.uniform(-4, 4, 400000).astype(np.float32)
+    a, b = oracle.pow_f32(x, y), oracle.pow_f64(x, y)
+    m = np.isfinite(b) & (np.abs(b) > 1.2e-38) & (np.abs(b) < 3e38)
+    assert std_ulp(a[m], b[m]).max() <= 4.0
+    p = oracle.lib().o_pow
+    assert p(0.0, -1.0) == 0.0 and p(0.0, 0.0) == 1.0       # pow(0, b) = (b == 0)
+    assert np.isnan(p(-8.0, 1.0 / 3.0)) and p(-2.0, 3.0) == -8.0
+    assert p(1.0, float("nan")) == 1.0                        # |a| == 1 first
+    assert np.isnan(p(2.0, 3e38))                             # NT2's 16*b overflows: NaN
+
+
 def test_nt2_ulp_convention_is_half_ulp():
     one = np.float32(1.0)
     assert nt2_ulpdist(one, np.nextafter(one, np.float32(2))) == 0.5
