@@ -77,12 +77,15 @@ typedef enum nt2g_opcode {
     NT2G_OP_EXP2 = 46, NT2G_OP_EXP10, NT2G_OP_EXPM1, NT2G_OP_LOG2, NT2G_OP_LOG10,
     NT2G_OP_SIN = 51, NT2G_OP_COS, NT2G_OP_TAN, NT2G_OP_SINPI, NT2G_OP_COSPI,
     NT2G_OP_POW = 56,      /* a^b (float)                                    */
+    NT2G_OP_SINH = 57, NT2G_OP_COSH, NT2G_OP_TANH,
     NT2G_OP_LT = 60, NT2G_OP_GT, NT2G_OP_LE, NT2G_OP_GE, NT2G_OP_EQ, NT2G_OP_NE, /* -> logical */
     NT2G_OP_IF_ELSE = 70,  /* a ? b : c                                      */
     NT2G_OP_SELINC,        /* a ? b+1 : b                                    */
     NT2G_OP_SELDEC,        /* a ? b-1 : b                                    */
     NT2G_OP_IF_ZERO_ELSE_ONE, /* a ? 0 : 1                                   */
-    NT2G_OP_ADDS           /* saturating add (uint8)                         */
+    NT2G_OP_ADDS,          /* saturating add (uint8)                         */
+    NT2G_OP_ASIN = 90, NT2G_OP_ACOS, NT2G_OP_ATAN,
+    NT2G_OP_ATAN2          /* atan2(a, b) (float)                            */
 } nt2g_opcode;
 
 typedef struct nt2g_op {
@@ -268,7 +271,8 @@ nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8
 /* Element functions y = f(x) for the accuracy tests and simple maps.
  * fn: 0 exp, 1 log, 2 log1p, 3 erfc, 4 normcdf, 5 fastnormcdf, 6 sqrt,
  * 7 normcdf(-x) through the shared pair core, 8 exp2, 9 exp10, 10 expm1, 11 log2, 12 log10,
- * 13 sin, 14 cos, 15 tan, 16 sinpi, 17 cospi. */
+ * 13 sin, 14 cos, 15 tan, 16 sinpi, 17 cospi, 18 sinh, 19 cosh, 20 tanh, 21 asin,
+ * 22 acos, 23 atan. */
 nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision,
                          void *stream);
 

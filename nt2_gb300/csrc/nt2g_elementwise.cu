@@ -393,6 +393,12 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 15) return tan<P>(a);
     if (FN == 16) return sinpi<P>(a);
     if (FN == 17) return cospi<P>(a);
+    if (FN == 18) return sinh<P>(a);
+    if (FN == 19) return cosh<P>(a);
+    if (FN == 20) return tanh<P>(a);
+    if (FN == 21) return asin<P>(a);
+    if (FN == 22) return acos<P>(a);
+    if (FN == 23) return atan<P>(a);
     float p, q;
     normcdf_pair<P>(a, p, q);
     return q;
@@ -428,6 +434,12 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 15: NT2G_MAP(15); break;
     case 16: NT2G_MAP(16); break;
     case 17: NT2G_MAP(17); break;
+    case 18: NT2G_MAP(18); break;
+    case 19: NT2G_MAP(19); break;
+    case 20: NT2G_MAP(20); break;
+    case 21: NT2G_MAP(21); break;
+    case 22: NT2G_MAP(22); break;
+    case 23: NT2G_MAP(23); break;
     default: NT2G_MAP(7); break;
     }
 #undef NT2G_MAP
@@ -473,6 +485,12 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_TAN: return tan<P>(a);
     case NT2G_OP_SINPI: return sinpi<P>(a);
     case NT2G_OP_COSPI: return cospi<P>(a);
+    case NT2G_OP_SINH: return sinh<P>(a);
+    case NT2G_OP_COSH: return cosh<P>(a);
+    case NT2G_OP_TANH: return tanh<P>(a);
+    case NT2G_OP_ASIN: return asin<P>(a);
+    case NT2G_OP_ACOS: return acos<P>(a);
+    case NT2G_OP_ATAN: return atan<P>(a);
     default: return fastnormcdf<P>(a);
     }
 }
@@ -573,9 +591,11 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                     }
                 }
                 break;
-            case NT2G_OP_POW:
-                for (int j = 0; j < kV; ++j)
-                    d[j] = __float_as_uint(pow<P>(__uint_as_float(A[j]), __uint_as_float(B[j])));
+            case NT2G_OP_POW: case NT2G_OP_ATAN2:
+                for (int j = 0; j < kV; ++j) {
+                    const float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]);
+                    d[j] = __float_as_uint(in.op == NT2G_OP_POW ? pow<P>(x, y) : atan2<P>(x, y));
+                }
                 break;
             case NT2G_OP_FMA: case NT2G_OP_FNMS:
 #pragma unroll

@@ -160,6 +160,7 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_ADDS: e = "((" + A + " + " + B + ") > 255u ? 255u : (" + A + " + " + B + "))"; break;
         case NT2G_OP_FMA: e = "P::fma(" + A + ", " + B + ", " + C + ")"; break;
         case NT2G_OP_POW: e = "nt2g::pow<P>(" + A + ", " + B + ")"; break;
+        case NT2G_OP_ATAN2: e = "nt2g::atan2<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_FNMS: e = "P::fma(-" + A + ", " + B + ", " + C + ")"; break;
         case NT2G_OP_LT: e = "(" + A + " < " + B + ") ? 1u : 0u"; break;
         case NT2G_OP_GT: e = "(" + A + " > " + B + ") ? 1u : 0u"; break;
@@ -195,6 +196,12 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_TAN: e = "nt2g::tan<P>(" + A + ")"; break;
         case NT2G_OP_SINPI: e = "nt2g::sinpi<P>(" + A + ")"; break;
         case NT2G_OP_COSPI: e = "nt2g::cospi<P>(" + A + ")"; break;
+        case NT2G_OP_SINH: e = "nt2g::sinh<P>(" + A + ")"; break;
+        case NT2G_OP_COSH: e = "nt2g::cosh<P>(" + A + ")"; break;
+        case NT2G_OP_TANH: e = "nt2g::tanh<P>(" + A + ")"; break;
+        case NT2G_OP_ASIN: e = "nt2g::asin<P>(" + A + ")"; break;
+        case NT2G_OP_ACOS: e = "nt2g::acos<P>(" + A + ")"; break;
+        case NT2G_OP_ATAN: e = "nt2g::atan<P>(" + A + ")"; break;
         default: e = "nt2g::fastnormcdf<P>(" + A + ")"; break;
         }
         s += std::string(u ? "    unsigned v" : "    float v") + std::to_string(k) + "[4]; NT2G_L v" +

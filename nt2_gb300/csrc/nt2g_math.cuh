@@ -740,6 +740,132 @@ template <class P> NT2G_HD float pow(float a0, float a1)
     return (neg && is_odd_f(a1)) ? -z : z;
 }
 
+// ------------------------------------------------------------ hyperbolic --
+// NT2 (modules/core/hyperbolic/include/nt2/hyperbolic/functions/):
+//   sinh  scalar/sinh.hpp:35-58, |x| < 1 by the degree-3 polynomial of
+//         details/sinh_kernel.hpp:24-35, else (e - 1/e)/2 with e = exp|x|, or
+//         (e^(x/2)/2) e^(x/2) beyond Maxlog - log 2; the sign of x
+//   cosh  generic/cosh.hpp:33-43, average(e, 1/e) or (e^(x/2)/2) e^(x/2)
+//   tanh  scalar/tanh.hpp:33-50, |x| < 5/8 by details/tanh_kernel.hpp:27-40,
+//         else 1 - 2/(1 + e^(2|x|)); the sign of x
+template <class P> NT2G_HD float sinh(float a0)
+{
+    const float x = fabsf(a0);
+    if (x < 1.0f) {
+        const float x2 = P::mul(x, x);
+        return P::mul(horner<P>(x2, bits_f(0x39559e2fu), bits_f(0x3c087bbeu), bits_f(0x3e2aaaccu), 1.0f), a0);
+    }
+    float r;
+    if (x > P::sub(bits_f(NT2G_MAXLOG), bits_f(NT2G_LOG_2))) {
+        const float t = exp<P>(P::mul(0.5f, x));
+        r = P::mul(P::mul(0.5f, t), t);
+    } else {
+        const float t = exp<P>(x);
+        r = P::fma(t, 0.5f, -P::mul(0.5f, P::div(1.0f, t)));
+    }
+    return bits_f(f_bits(r) ^ (f_bits(a0) & 0x80000000u));
+}
+
+template <class P> NT2G_HD float cosh(float a0)
+{
+    const float x = fabsf(a0);
+    const bool big = x > P::sub(bits_f(NT2G_MAXLOG), bits_f(NT2G_LOG_2));
+    const float t = exp<P>(P::mul(x, big ? 0.5f : 1.0f));
+    if (big) return P::mul(P::mul(0.5f, t), t);
+    return P::fma(t, 0.5f, P::mul(P::div(1.0f, t), 0.5f));
+}
+
+template <class P> NT2G_HD float tanh(float a0)
+{
+    const float x = fabsf(a0);
+    if (x < 0.625f) {
+        const float x2 = P::mul(x, x);
+        const float y = horner<P>(x2, bits_f(0xbbbaf0eau), bits_f(0x3ca9134eu), bits_f(0xbd5c1e2du),
+                                  bits_f(0x3e088393u), bits_f(0xbeaaaa99u));
+        return P::fma(P::mul(y, x2), a0, a0);
+    }
+    const float r = P::fma(-2.0f, P::div(1.0f, P::add(1.0f, exp<P>(P::add(x, x)))), 1.0f);
+    return bits_f(f_bits(r) ^ (f_bits(a0) & 0x80000000u));
+}
+
+// ------------------------------------------------- inverse trigonometry --
+// NT2 (trigonometric/functions/scalar/impl/invtrig/f_invtrig.hpp:33-128,
+// Cephes' asinf/atanf): asin by a degree-4 polynomial in x^2 (|x| <= 1/2) or
+// in (1-|x|)/2 with pi/2 - 2 asin(sqrt(.)); acos from asin in three bands;
+// atan reduced at tan(3pi/8) and tan(pi/8) with pi/2 and pi/4 carried in two
+// parts; atan2 (scalar/atan2.hpp:30-46) from the atan kernel of |a/b|.
+template <class P> NT2G_HD float asin(float a0)
+{
+    float x = fabsf(a0);
+    const uint32_t sign = f_bits(a0) & 0x80000000u;
+    if (x < bits_f(0x38d1b717u)) return a0;  // 1e-4
+    if (x > 1.0f) return f_nan();
+    const bool big = x > 0.5f;
+    float z;
+    if (big) {
+        z = P::mul(0.5f, P::sub(1.0f, x));
+        x = P::sqrt(z);
+    } else {
+        z = P::mul(x, x);
+    }
+    float z1 = horner<P>(z, bits_f(0x3d2cb352u), bits_f(0x3cc617e3u), bits_f(0x3d3a3ec7u), bits_f(0x3d9980f6u),
+                         bits_f(0x3e2aaae4u));
+    z1 = P::fma(z1, P::mul(z, x), x);
+    if (big) {
+        z1 = P::add(z1, z1);
+        z1 = P::sub(bits_f(0x3fc90fdbu), z1);  // Pio_2
+    }
+    return bits_f(f_bits(z1) ^ sign);
+}
+
+template <class P> NT2G_HD float acos(float a0)
+{
+    if (a0 < -0.5f)
+        return P::sub(bits_f(0x40490fdbu), P::mul(asin<P>(P::sqrt(P::mul(P::add(1.0f, a0), 0.5f))), 2.0f));
+    if (a0 > 0.5f) return P::mul(asin<P>(P::sqrt(P::mul(P::sub(1.0f, a0), 0.5f))), 2.0f);
+    return P::sub(bits_f(0x3fc90fdbu), asin<P>(a0));
+}
+
+// atan(|a0|) (NT2's kernel_atan: the sign is left to the caller)
+template <class P> NT2G_HD float atan_kernel(float a0)
+{
+    if (a0 == 0.0f) return 0.0f;
+    if (fabsf(a0) == f_inf()) return bits_f(0x3fc90fdbu);
+    float x = fabsf(a0), y = 0.0f, more = 0.0f;
+    if (x > bits_f(0x401a827au)) {  // tan(3 pi/8)
+        y = bits_f(0x3fc90fdbu);
+        more = bits_f(0xb33bbd2eu);
+        x = -P::div(1.0f, x);
+    } else if (x > bits_f(0x3ed413cdu)) {  // tan(pi/8)
+        y = bits_f(0x3f490fdbu);
+        more = bits_f(0xb2bbbd2eu);
+        x = P::div(P::sub(x, 1.0f), P::add(1.0f, x));
+    }
+    const float z = P::mul(x, x);
+    float z1 = horner<P>(z, bits_f(0x3da4f0d1u), bits_f(0xbe0e1b85u), bits_f(0x3e4c925fu), bits_f(0xbeaaaa2au));
+    z1 = P::fma(x, P::mul(z1, z), x);
+    return P::add(y, P::add(z1, more));
+}
+
+template <class P> NT2G_HD float atan(float a0)
+{
+    return bits_f(f_bits(atan_kernel<P>(a0)) ^ (f_bits(a0) & 0x80000000u));
+}
+
+template <class P> NT2G_HD float atan2(float a0, float a1)
+{
+    if (is_nan(a0) || is_nan(a1)) return f_nan();
+    if (fabsf(a0) == f_inf() && fabsf(a1) == f_inf()) {
+        a0 = copysignf(1.0f, a0);
+        a1 = copysignf(1.0f, a1);
+    }
+    float z = atan_kernel<P>(P::div(a0, a1));
+    z = (a1 > 0.0f) ? z : P::sub(bits_f(0x40490fdbu), z);
+    z = P::mul(z, (f_bits(a0) & 0x80000000u) ? -1.0f : 1.0f);  // signnz
+    if (a0 == 0.0f) return (a1 < 0.0f) ? bits_f(0x40490fdbu) : 0.0f;
+    return z;
+}
+
 // ----------------------------------------------------------- trigonometry --
 // NT2 (modules/core/trigonometric/include/nt2/trigonometric/functions/):
 //   sin/cos/tan   scalar/impl/trigo/trig_base.hpp:131-176 (regular style,

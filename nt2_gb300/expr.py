@@ -2,6 +2,7 @@
 
 ``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
 (exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, sinpi, cospi, pow,
+sinh, cosh, tanh, asin, acos, atan, atan2,
 erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms, min, max, if_else,
 selinc, seldec, if_zero_else_one, adds) build an expression
 tree; ``assign(outs, exprs)`` is ``tie(outs...) = tie(exprs...)``: it lowers
@@ -83,6 +84,8 @@ abs_ = _un("ABS")
 exp2, exp10, expm1 = _un("EXP2"), _un("EXP10"), _un("EXPM1")
 log2, log10 = _un("LOG2"), _un("LOG10")
 sin, cos, tan, sinpi, cospi = _un("SIN"), _un("COS"), _un("TAN"), _un("SINPI"), _un("COSPI")
+sinh, cosh, tanh = _un("SINH"), _un("COSH"), _un("TANH")
+asin, acos, atan = _un("ASIN"), _un("ACOS"), _un("ATAN")
 
 # Functors applied to plain numbers evaluate at once in float32 with NT2's
 # scalar semantics (each step rounded, no fusion), as NT2's scalar overloads
@@ -120,6 +123,11 @@ def pow(a, b):
     if not any(isinstance(x, Node) for x in (a, b)):
         raise TypeError("pow of two numbers: use Python's ** (NT2's scalar pow is not mirrored here)")
     return _bin("POW", a, b)
+
+
+def atan2(a, b):
+    """atan2(a, b) with NT2's semantics (atan2(+-0, b < 0) = pi)."""
+    return _bin("ATAN2", a, b)
 
 
 def min_(a, b): return _bin("MIN", a, b)

@@ -570,6 +570,7 @@ NT2G_BINARY(min, NT2G_OP_MIN, false)
 NT2G_BINARY(max, NT2G_OP_MAX, false)
 NT2G_BINARY(adds, NT2G_OP_ADDS, false)
 NT2G_BINARY(pow, NT2G_OP_POW, false)
+NT2G_BINARY(atan2, NT2G_OP_ATAN2, false)
 #undef NT2G_BINARY
 
 #define NT2G_UNARY(NAME, CODE)                                                                                   \
@@ -600,6 +601,12 @@ NT2G_UNARY(cos, NT2G_OP_COS)
 NT2G_UNARY(tan, NT2G_OP_TAN)
 NT2G_UNARY(sinpi, NT2G_OP_SINPI)
 NT2G_UNARY(cospi, NT2G_OP_COSPI)
+NT2G_UNARY(sinh, NT2G_OP_SINH)
+NT2G_UNARY(cosh, NT2G_OP_COSH)
+NT2G_UNARY(tanh, NT2G_OP_TANH)
+NT2G_UNARY(asin, NT2G_OP_ASIN)
+NT2G_UNARY(acos, NT2G_OP_ACOS)
+NT2G_UNARY(atan, NT2G_OP_ATAN)
 #undef NT2G_UNARY
 
 // Functors on plain scalars evaluate at once, in float, with NT2's scalar

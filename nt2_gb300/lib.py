@@ -24,13 +24,15 @@ OP = dict(
     ADD=10, SUB=11, MUL=12, DIV=13, NEG=14, ABS=15, SQR=16, SQRT=17, REC=18, MIN=19, MAX=20,
     FMA=30, FNMS=31,
     EXP=40, LOG=41, LOG1P=42, ERFC=43, NORMCDF=44, FASTNORMCDF=45, EXP2=46, EXP10=47, EXPM1=48, LOG2=49, LOG10=50,
-    SIN=51, COS=52, TAN=53, SINPI=54, COSPI=55, POW=56,
+    SIN=51, COS=52, TAN=53, SINPI=54, COSPI=55, POW=56, SINH=57, COSH=58, TANH=59,
     LT=60, GT=61, LE=62, GE=63, EQ=64, NE=65,
     IF_ELSE=70, SELINC=71, SELDEC=72, IF_ZERO_ELSE_ONE=73, ADDS=74,
+    ASIN=90, ACOS=91, ATAN=92, ATAN2=93,
 )
 
 MAP_FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, normcdf_neg=7, exp2=8, exp10=9,
-              expm1=10, log2=11, log10=12, sin=13, cos=14, tan=15, sinpi=16, cospi=17)
+              expm1=10, log2=11, log10=12, sin=13, cos=14, tan=15, sinpi=16, cospi=17,
+              sinh=18, cosh=19, tanh=20, asin=21, acos=22, atan=23)
 
 BATCH_BLACKSCHOLES, BATCH_SAXPY, BATCH_EXPR3 = 0, 1, 2
 

@@ -276,6 +276,112 @@ EXPORT float o_expm1(float a0)
     return y * o_pow2i(k);
 }
 
+/* --------------------------------------------------------- hyperbolic ----
+ * HYP = modules/core/hyperbolic/include/nt2/hyperbolic/functions:
+ * sinh HYP/scalar/sinh.hpp:35-58 + HYP/details/sinh_kernel.hpp:24-35,
+ * cosh HYP/generic/cosh.hpp:33-43 (average(a,b) = a*0.5 + b*0.5),
+ * tanh HYP/scalar/tanh.hpp:33-50 + HYP/details/tanh_kernel.hpp:27-40. */
+static const uint32_t SINH_P[4] = {0x39559e2f, 0x3c087bbe, 0x3e2aaacc, 0x3f800000};
+static const uint32_t TANH_P[5] = {0xbbbaf0ea, 0x3ca9134e, 0xbd5c1e2d, 0x3e088393, 0xbeaaaa99};
+
+EXPORT float o_sinh(float a0)
+{
+    float x = fabsf(a0), r;
+    if (x < 1.0f) return horner(x * x, SINH_P, 4) * a0;
+    if (x > bf(C_MAXLOG) - bf(0x3f317218u)) {
+        float t = o_exp(0.5f * x);
+        r = (0.5f * t) * t;
+    } else {
+        float t = o_exp(x);
+        r = t * 0.5f - 0.5f * (1.0f / t);
+    }
+    return bf(fb(r) ^ (fb(a0) & 0x80000000u));
+}
+
+EXPORT float o_cosh(float a0)
+{
+    float x = fabsf(a0);
+    int big = x > bf(C_MAXLOG) - bf(0x3f317218u);
+    float t = o_exp(x * (big ? 0.5f : 1.0f));
+    if (big) return (0.5f * t) * t;
+    return t * 0.5f + (1.0f / t) * 0.5f;
+}
+
+EXPORT float o_tanh(float a0)
+{
+    float x = fabsf(a0);
+    if (x < 0.625f) {
+        float x2 = x * x;
+        return (horner(x2, TANH_P, 5) * x2) * a0 + a0;
+    }
+    float r = -2.0f * (1.0f / (1.0f + o_exp(x + x))) + 1.0f;
+    return bf(fb(r) ^ (fb(a0) & 0x80000000u));
+}
+
+/* ------------------------------------------------ inverse trigonometry ----
+ * TRIG/scalar/impl/invtrig/f_invtrig.hpp:33-128 (Cephes asinf / atanf),
+ * atan2 TRIG/scalar/atan2.hpp:30-46 */
+static const uint32_t ASIN_P[5] = {0x3d2cb352, 0x3cc617e3, 0x3d3a3ec7, 0x3d9980f6, 0x3e2aaae4};
+static const uint32_t ATAN_P[4] = {0x3da4f0d1, 0xbe0e1b85, 0x3e4c925f, 0xbeaaaa2a};
+
+EXPORT float o_asin(float a0)
+{
+    float x = fabsf(a0), z;
+    uint32_t sign = fb(a0) & 0x80000000u;
+    if (x < bf(0x38d1b717u)) return a0;
+    if (x > 1.0f) return NAN;
+    int big = x > 0.5f;
+    if (big) { z = 0.5f * (1.0f - x); x = sqrtf(z); }
+    else z = x * x;
+    float z1 = horner(z, ASIN_P, 5);
+    z1 = z1 * (z * x) + x;
+    if (big) { z1 = z1 + z1; z1 = bf(0x3fc90fdbu) - z1; }
+    return bf(fb(z1) ^ sign);
+}
+
+EXPORT float o_acos(float a0)
+{
+    if (a0 < -0.5f) return bf(0x40490fdbu) - o_asin(sqrtf((a0 + 1.0f) * 0.5f)) * 2.0f;
+    if (a0 > 0.5f) return o_asin(sqrtf((1.0f - a0) * 0.5f)) * 2.0f;
+    return bf(0x3fc90fdbu) - o_asin(a0);
+}
+
+static float atan_kernel(float a0)
+{
+    if (a0 == 0.0f) return 0.0f;
+    if (fabsf(a0) == INFINITY) return bf(0x3fc90fdbu);
+    float x = fabsf(a0), y = 0.0f, more = 0.0f;
+    if (x > bf(0x401a827au)) { y = bf(0x3fc90fdbu); more = bf(0xb33bbd2eu); x = -(1.0f / x); }
+    else if (x > bf(0x3ed413cdu)) { y = bf(0x3f490fdbu); more = bf(0xb2bbbd2eu); x = (x - 1.0f) / (x + 1.0f); }
+    float z = x * x;
+    float z1 = horner(z, ATAN_P, 4);
+    z1 = x * (z1 * z) + x;
+    return y + (z1 + more);
+}
+
+EXPORT float o_atan(float a0) { return bf(fb(atan_kernel(a0)) ^ (fb(a0) & 0x80000000u)); }
+
+EXPORT float o_atan2(float a0, float a1)
+{
+    if (a0 != a0 || a1 != a1) return NAN;
+    if (fabsf(a0) == INFINITY && fabsf(a1) == INFINITY) { a0 = copysignf(1.0f, a0); a1 = copysignf(1.0f, a1); }
+    float z = atan_kernel(a0 / a1);
+    z = (a1 > 0.0f) ? z : bf(0x40490fdbu) - z;
+    z = z * ((fb(a0) & 0x80000000u) ? -1.0f : 1.0f);
+    if (a0 == 0.0f) return (a1 < 0.0f) ? bf(0x40490fdbu) : 0.0f;
+    return z;
+}
+
+EXPORT void o_atan2_f32(const float *x, const float *y, float *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = o_atan2(x[i], y[i]);
+}
+
+EXPORT void o_atan2_f64(const float *x, const float *y, double *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = atan2((double)x[i], (double)y[i]);
+}
+
 /* ---------------------------------------------------------------- pow ----
  * EXP/scalar/pow.hpp:28-36, EXP/scalar/pow_abs.hpp:31-84 and the float
  * kernel EXP/details/pow_kernel.hpp:43-125 (Cephes powf: a 2^(-i/16) table,
@@ -524,7 +630,8 @@ EXPORT float o_tan(float a0)
 
 /* ------------------------------------------------- elementwise maps ---- */
 enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT, FN_EXP2 = 8, FN_EXP10,
-       FN_EXPM1, FN_LOG2, FN_LOG10, FN_SIN, FN_COS, FN_TAN, FN_SINPI, FN_COSPI };
+       FN_EXPM1, FN_LOG2, FN_LOG10, FN_SIN, FN_COS, FN_TAN, FN_SINPI, FN_COSPI, FN_SINH, FN_COSH, FN_TANH,
+       FN_ASIN, FN_ACOS, FN_ATAN };
 
 EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
 {
@@ -547,6 +654,12 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_TAN: y[i] = o_tan(a); break;
         case FN_SINPI: y[i] = o_sinpi(a); break;
         case FN_COSPI: y[i] = o_cospi(a); break;
+        case FN_SINH: y[i] = o_sinh(a); break;
+        case FN_COSH: y[i] = o_cosh(a); break;
+        case FN_TANH: y[i] = o_tanh(a); break;
+        case FN_ASIN: y[i] = o_asin(a); break;
+        case FN_ACOS: y[i] = o_acos(a); break;
+        case FN_ATAN: y[i] = o_atan(a); break;
         default: y[i] = sqrtf(a); break;
         }
     }
@@ -592,6 +705,12 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_TAN: y[i] = tan(a); break;
         case FN_SINPI: y[i] = sinpi_d(a); break;
         case FN_COSPI: y[i] = cospi_d(a); break;
+        case FN_SINH: y[i] = sinh(a); break;
+        case FN_COSH: y[i] = cosh(a); break;
+        case FN_TANH: y[i] = tanh(a); break;
+        case FN_ASIN: y[i] = asin(a); break;
+        case FN_ACOS: y[i] = acos(a); break;
+        case FN_ATAN: y[i] = atan(a); break;
         default: y[i] = sqrt(a); break;
         }
     }

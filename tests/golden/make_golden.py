@@ -35,6 +35,12 @@ SOURCES = [
     ("modules/core/trigonometric/unit/scalar/tan.cpp", 41, 49),
     ("modules/core/trigonometric/unit/scalar/sinpi.cpp", 45, 54),
     ("modules/core/trigonometric/unit/scalar/cospi.cpp", 45, 54),
+    ("modules/core/hyperbolic/unit/scalar/sinh.cpp", 40, 44),
+    ("modules/core/hyperbolic/unit/scalar/cosh.cpp", 37, 41),
+    ("modules/core/hyperbolic/unit/scalar/tanh.cpp", 38, 44),
+    ("modules/core/trigonometric/unit/scalar/asin.cpp", 45, 53),
+    ("modules/core/trigonometric/unit/scalar/acos.cpp", 46, 54),
+    ("modules/core/trigonometric/unit/scalar/atan.cpp", 45, 53),
 ]
 
 E = float(np.float32(math.e))
@@ -46,6 +52,9 @@ CONST = {
     "Pi": float(np.uint32(0x40490fdb).view(np.float32)), "Pio_2": float(np.uint32(0x3fc90fdb).view(np.float32)),
     "Pio_4": float(np.uint32(0x3f490fdb).view(np.float32)),
     "Sqrt_2o_2": float(np.uint32(0x3f3504f3).view(np.float32)),
+    "Pio_6": float(np.uint32(0x3f060a92).view(np.float32)), "Pio_3": float(np.uint32(0x3f860a92).view(np.float32)),
+    "Twopio_3": float(np.uint32(0x40060a92).view(np.float32)),
+    "Threepio_4": float(np.uint32(0x4016cbe4).view(np.float32)),
 }
 
 
@@ -56,6 +65,9 @@ def _value(expr):
     m = re.fullmatch(r"nt2::(\w+)<\w+>\(\)", expr)
     if m:
         return CONST[m.group(1)]
+    m = re.fullmatch(r"[-+]?[0-9.]+[eE][-+]?[0-9]+", expr)
+    if m:  # a bare double literal, converted to the float r_t
+        return float(np.float32(float(expr)))
     m = re.fullmatch(r"T\(([-+0-9.eE]+)\)", expr)
     if m:
         return float(np.float32(float(m.group(1))))
@@ -77,8 +89,9 @@ def _value(expr):
 PAT = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(\w+)\((.*?)\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 # two-argument functors: pow(a, b)
 ARG = r"((?:[^,()]|\([^()]*\))*)"
-PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow)\(" + ARG + r",\s*" + ARG + r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
-SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53)]
+PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2)\(" + ARG + r",\s*" + ARG + r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
+SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
+            ("modules/core/trigonometric/unit/scalar/atan2.cpp", 47, 61)]
 
 
 def main(root):

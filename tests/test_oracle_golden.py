@@ -13,7 +13,7 @@ from helpers import nt2_ulpdist, std_ulp, reduction_ill
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
 FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1", "log2", "log10", "sin", "cos",
-         "tan", "sinpi", "cospi")
+         "tan", "sinpi", "cospi", "sinh", "cosh", "tanh", "asin", "acos", "atan")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
@@ -23,10 +23,10 @@ def test_oracle_matches_nt2_unit_tests(oracle, rec):
     assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (got, rec)
 
 
-@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] == "pow"],
-                         ids=lambda r: f"pow({r['x']},{r['y']})@{r['source'].split('/')[-1]}")
-def test_oracle_pow_matches_nt2_unit_tests(oracle, rec):
-    got = oracle.lib().o_pow(rec["x"], rec["y"])
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("pow", "atan2")],
+                         ids=lambda r: f"{r['fn']}({r['x']},{r['y']})@{r['source'].split('/')[-1]}")
+def test_oracle_binary_matches_nt2_unit_tests(oracle, rec):
+    got = getattr(oracle.lib(), "o_" + rec["fn"])(rec["x"], rec["y"])
     assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (got, rec)
 
 
@@ -134,6 +134,22 @@ def test_oracle_trig_accuracy_profile(oracle):
     # the exact reduction agrees with NT2's double band on its last floats
     x = np.float32([823549.5, 823549.5625, 823549.625])
     assert std_ulp(oracle.map_f32("sin", x), oracle.map_f64("sin", x)).max() <= 1.0
+
+
+def test_oracle_hyperbolic_inverse_trig_profile(oracle):
+    """NT2's float sinh/cosh/tanh and Cephes-style asin/acos/atan/atan2 as
+    restated, against FP64 libm."""
+    for fn, lo, hi, tol in (("sinh", -89, 89, 2.5), ("cosh", -89, 89, 2.5), ("tanh", -10, 10, 1.5),
+                            ("asin", -1, 1, 2.5), ("acos", -1, 1, 1.5), ("atan", -1e4, 1e4, 2.5)):
+        x = np.concatenate([np.linspace(lo, hi, 200001), np.linspace(-1, 1, 50001)]).astype(np.float32)
+        a, b = oracle.map_f32(fn, x), oracle.map_f64(fn, x)
+        m = np.isfinite(b) & (np.abs(b) > 1.2e-38) & (np.abs(b) < 3e38)
+        assert std_ulp(a[m], b[m]).max() <= tol, fn
+    rng = np.random.default_rng(0)
+    x, y = rng.standard_normal(100000).astype(np.float32), rng.standard_normal(100000).astype(np.float32)
+    assert std_ulp(oracle.atan2_f32(x, y), oracle.atan2_f64(x, y)).max() <= 2.5
+    at2 = oracle.lib().o_atan2
+    assert at2(-0.0, -1.0) == np.float32(np.pi) and at2(0.0, 1.0) == 0.0  # NT2: atan2(+-0, b<0) = +pi
 
 
 def test_twoopi_table_is_two_over_pi():

@@ -1,4 +1,4 @@
-"""pow(a, b) on the GPU through the expression paths.
+"""pow(a, b) and atan2(a, b) on the GPU through the expression paths.
 
 NT2 policy: bit-identical to the oracle's restatement of NT2's float pow
 (Cephes powf with NT2's special cases).  Fast policy: the float-float
@@ -100,3 +100,38 @@ def test_pow_golden_values(dev, prec):
     got = _pow(dev, x, y, prec, 1)
     for g, r in zip(got, recs):
         assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+    recs = [r for r in golden if r["fn"] == "atan2"]
+    assert len(recs) == 14
+    got = _atan2(dev, np.float32([r["x"] for r in recs]), np.float32([r["y"] for r in recs]), prec, 1)
+    for g, r in zip(got, recs):
+        assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+
+
+def _atan2(dev, x, y, prec, mode):
+    tx, ty = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
+    out = torch.empty_like(tx)
+    E.assign([out], [E.atan2(E.Table(tx), E.Table(ty))], precision=prec, force_generic=mode)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+@MODES
+def test_atan2_both_policies(dev, oracle, mode):
+    """atan2: NT2 policy bit-identical to the oracle, fast within 3 ulp of
+    FP64, NT2's conventions at zeros and infinities in both."""
+    rng = np.random.default_rng(53)
+    n = 1 << 18
+    x = (rng.standard_normal(n) * np.exp2(rng.integers(-20, 20, n))).astype(np.float32)
+    y = (rng.standard_normal(n) * np.exp2(rng.integers(-20, 20, n))).astype(np.float32)
+    sx, sy = _special_grid()
+    x, y = np.concatenate([x, sx, sy]), np.concatenate([y, sy, sx])
+    got = _atan2(dev, x, y, L.PREC_NT2, mode)
+    ref = oracle.atan2_f32(x, y)
+    assert np.all((got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref)))
+    fast = _atan2(dev, x, y, L.PREC_FAST, mode)
+    r64 = oracle.atan2_f64(x, y)
+    m = np.isfinite(r64) & (np.abs(r64) > 1.2e-38) & (x != 0)
+    e = np.abs(fast[m].astype(np.float64) - r64[m]) / np.spacing(np.abs(r64[m]).astype(np.float32))
+    assert e.max() <= 3.0, float(e.max())
+    z = (x == 0) | np.isnan(x) | np.isnan(y)
+    assert np.all((fast[z].view(np.uint32) == ref[z].view(np.uint32)) | (np.isnan(fast[z]) & np.isnan(ref[z])))
