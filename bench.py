@@ -529,14 +529,28 @@ def cpu_baseline(config, budget_s=10.0):
         what = f"{config} over {sample_n} floats, OpenMP reduction over {nthreads} threads"
     else:
         return None
-    f()
-    rates, t_end = [], time.perf_counter() + budget_s
-    while time.perf_counter() < t_end or len(rates) < 3:
-        t0 = time.perf_counter()
-        f()
-        rates.append(sample_n / (time.perf_counter() - t0))
-    return {"value": float(np.median(rates)), "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": what + f", median of {len(rates)} runs"}
+    def timed(fn, budget):
+        fn()
+        rates, t_end = [], time.perf_counter() + budget
+        while time.perf_counter() < t_end or len(rates) < 3:
+            t0 = time.perf_counter()
+            fn()
+            rates.append(sample_n / (time.perf_counter() - t0))
+        return float(np.median(rates)), len(rates)
+
+    value, runs = timed(f, budget_s)
+    out = {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+           "sample": what + f", median of {runs} runs"}
+    if config == "bs":
+        # NT2's own thread rule (shared_memory/transform.hpp: grain = top cache bytes / sizeof(T);
+        # n <= 8 grain runs on one thread) and a one-thread figure
+        grain = int(oracle.nt2_transform_grain(4))
+        nt2_threads = 1 if sample_n <= 8 * grain else nthreads
+        one, _ = timed(BlackScholes.cpu(oracle, 1, sample_n), budget_s / 4)
+        out["one_thread"] = one
+        out["nt2_rule"] = {"grain": grain, "threads": nt2_threads,
+                           "value": one if nt2_threads == 1 else value}
+    return out
 
 
 def run_reference(args):

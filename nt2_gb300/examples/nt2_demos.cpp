@@ -222,8 +222,11 @@ int main(int argc, char **argv)
             l2 = nt2::linspace(0.f, 1.f);
             g1 = nt2::logspace(0.f, 1.f);
             g2 = nt2::logspace(2.f, 3.14159274f, 7);
-            w = nt2::sinpi(nt2::linspace(0.f, 2.f, n)) * nt2::colon(1.f, (float)n);
-            for (auto *t : {&c1, &c2, &c3, &l1, &l2, &g1, &g2, &w}) std::printf("%zu\n", t->numel());
+            w = nt2::sinpi(nt2::linspace(0.f, 2.f, n)) * nt2::colon(1.f, (float)n) + nt2::ones(1, n);
+            dtable o1;
+            o1 = nt2::zeros(3) + 2.0f;  // a 3 x 3 table of twos
+            for (auto *t : {&c1, &c2, &c3, &l1, &l2, &g1, &g2, &w, &o1}) std::printf("%zu\n", t->numel());
+            save(dir + "o1.bin", o1);
             save(dir + "c1.bin", c1); save(dir + "c2.bin", c2); save(dir + "c3.bin", c3);
             save(dir + "l1.bin", l1); save(dir + "l2.bin", l2); save(dir + "g1.bin", g1); save(dir + "g2.bin", g2);
             save(dir + "w.bin", w);

@@ -161,7 +161,7 @@ def _generative_sizes(e, seen=None):
     if id(e) in seen or not isinstance(e, Node):
         return []
     seen.add(id(e))
-    out = [e.numel] if e.op == "INDEX" else []
+    out = [e.numel] if e.op in ("INDEX", "CONST") and e.numel is not None else []
     for a in e.args:
         out += _generative_sizes(a, seen)
     return out
@@ -187,6 +187,17 @@ def _check_generative_sizes(exprs, count):
     sizes = {m for e in exprs for m in _generative_sizes(e)}
     if sizes and sizes != {count}:
         raise ValueError(f"generative operands of {sorted(sizes)} elements assigned to {count}")
+
+
+def ones(*size):
+    """A constant table of ones: ones(n) is n x n, ones(a, b, ...) has a*b*... elements."""
+    import math
+    return Node("CONST", (), lib.F32, imm=1.0, numel=size[0] * size[0] if len(size) == 1 else math.prod(size))
+
+
+def zeros(*size):
+    import math
+    return Node("CONST", (), lib.F32, imm=0.0, numel=size[0] * size[0] if len(size) == 1 else math.prod(size))
 
 
 def colon_count(l, s, u):

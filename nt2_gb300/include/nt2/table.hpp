@@ -441,6 +441,7 @@ namespace detail {
 inline std::size_t extent_of(const node *n)
 {
     if (n->op == NT2G_OP_LOAD || n->op == NT2G_OP_INDEX) return n->numel;
+    if (n->op == NT2G_OP_CONST) return n->numel;  // ones / zeros carry a size; plain scalars 0
     std::size_t e = 0;
     for (const node *c : {n->a.get(), n->b.get(), n->c.get()}) {
         if (!c) continue;
@@ -741,6 +742,21 @@ inline expr<float> logspace(float l, float u, std::size_t n = 50, bool regular =
     return expr<float>{detail::make(NT2G_OP_EXP10, NT2G_F32, line)};
 }
 
+// ones / zeros (generative/functions/{ones,zeros}.hpp): a constant table of a
+// given size; ones(n) is n x n as in NT2 (and MATLAB)
+inline expr<float> filled(of_size_ s, float v)
+{
+    auto n = detail::cst(v);
+    n->numel = s.numel();
+    return expr<float>{n};
+}
+inline expr<float> ones(of_size_ s) { return filled(s, 1.0f); }
+inline expr<float> ones(std::size_t n) { return ones(of_size(n, n)); }
+inline expr<float> ones(std::size_t a, std::size_t b) { return ones(of_size(a, b)); }
+inline expr<float> zeros(of_size_ s) { return filled(s, 0.0f); }
+inline expr<float> zeros(std::size_t n) { return zeros(of_size(n, n)); }
+inline expr<float> zeros(std::size_t a, std::size_t b) { return zeros(of_size(a, b)); }
+
 // if_zero_else_one on a logical yields the element type of the comparison
 template <class T> expr<T> if_zero_else_one(const expr<T> &cond)
 {
@@ -807,7 +823,8 @@ inline double sum_node(const node_ptr &n)
     while (!stack.empty()) {
         const node *m = stack.back();
         stack.pop_back();
-        if (m->op == NT2G_OP_LOAD || m->op == NT2G_OP_INDEX) numel = numel ? std::min(numel, m->numel) : m->numel;
+        if ((m->op == NT2G_OP_LOAD || m->op == NT2G_OP_INDEX || m->op == NT2G_OP_CONST) && m->numel)
+            numel = numel ? std::min(numel, m->numel) : m->numel;
         for (const node *c : {m->a.get(), m->b.get(), m->c.get()})
             if (c) stack.push_back(c);
     }

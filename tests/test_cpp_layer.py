@@ -161,7 +161,8 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
 @pytest.mark.parametrize("prec", ["1", "0"], ids=["nt2", "fast"])
 def test_generative_through_tables(demos, oracle, tmp_path, prec):
     """_(0, 9), _(0, 0.3, 1), colon(1, -0.3, 0), linspace, logspace (with its
-    pi rule) and sinpi(linspace(0, 2, n)) * colon(1, n) through the C++ layer:
+    pi rule), sinpi(linspace(0, 2, n)) * colon(1, n) + ones(1, n) and
+    zeros(3) + 2 through the C++ layer:
     NT2's sizes, and under the NT2 policy NT2's values bit for bit."""
     n = 100003
     sizes = [int(v) for v in _run(demos, "gen", tmp_path, n, env={"NT2G_PRECISION": prec}).split()]
@@ -169,7 +170,8 @@ def test_generative_through_tables(demos, oracle, tmp_path, prec):
     want = dict(c1=oracle.colon_nt2(0, 9), c2=oracle.colon_nt2(0, 0.3, 1), c3=oracle.colon_nt2(1, -0.3, 0),
                 l1=oracle.linspace_nt2(-1, 1, 257), l2=oracle.linspace_nt2(0, 1), g1=oracle.logspace_nt2(0, 1),
                 g2=oracle.logspace_nt2(2, np.float32(np.pi), 7),
-                w=oracle.map_f32("sinpi", oracle.linspace_nt2(0, 2, n)) * (pos + np.float32(1)))
+                w=oracle.map_f32("sinpi", oracle.linspace_nt2(0, 2, n)) * (pos + np.float32(1)) + np.float32(1),
+                o1=np.full(9, 2.0, np.float32))
     assert sizes == [len(v) for v in want.values()]
     for name, ref in want.items():
         got = np.fromfile(tmp_path / f"{name}.bin", np.float32)
@@ -181,7 +183,7 @@ def test_generative_through_tables(demos, oracle, tmp_path, prec):
             # sinpi near its zeros turns it into ~pi/2 ulp(x) <= 4e-7, times (p + 1)
             ulp = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
             if name == "w":
-                tol = 4 * ulp + (pos.astype(np.float64) + 1) * 1e-6
+                tol = 4 * ulp + (pos.astype(np.float64) + 1) * 1e-6 + 1.2e-7
             else:
                 tol = {"g1": 4, "g2": 8}.get(name, 1) * ulp
             assert (np.abs(got.astype(np.float64) - ref) <= tol).all(), name

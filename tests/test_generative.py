@@ -154,3 +154,7 @@ def test_generative_fast_policy_is_correctly_rounded(dev, oracle):
 def test_generative_size_mismatch_raises():
     with pytest.raises(ValueError):
         E._check_generative_sizes([E.colon(0, 9)], 11)
+    with pytest.raises(ValueError):
+        E._check_generative_sizes([E.ones(3) + E.colon(0, 8)], 10)
+    E._check_generative_sizes([E.ones(3) + E.colon(0, 8)], 9)
+    E._check_generative_sizes([E.zeros(2, 5) * 2.0], 10)
