@@ -19,8 +19,9 @@
 //   3. each chunk is scanned again, starting from its prefix.
 // Contiguous segments (lo = 1) run one warp per chunk in tiles of 128
 // elements (a float4 per lane, an in-order warp scan of the lane totals);
-// strided ones run one thread per segment (four with float4) over chunks of
-// the scan range.  cumsum carries compensated sums (s + c; chunk prefixes in
+// phase 1 of cumsum/cumprod is a plain reduction (order does not matter to a
+// commutative aggregate).  Strided segments run one thread per segment (four
+// with float4) over chunks of the scan range, 8 rows of loads at a time.  cumsum carries compensated sums (s + c; chunk prefixes in
 // FP64), so each output is within about an ulp of the exact prefix; cumprod
 // carries FP64 products; cummax/cummin are exact: NT2's (s > x) ? s : x is
 // not associative once a NaN appears (a NaN summary is replaced by the next
@@ -152,6 +153,44 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_inner(const float *x, int
         const int64_t k0 = c * chunk, k1 = (k0 + chunk < inner) ? k0 + chunk : inner;
         const float *p = x + seg * inner;
         float *o = out + seg * inner;
+        if constexpr (PHASE == 1 && (OP == NT2G_SCAN_SUM || OP == NT2G_SCAN_PROD)) {
+            // the chunk aggregate of a commutative operation needs no scan: each
+            // lane folds its float4s (4 in flight), then the lanes combine in order
+            CSum acc{0.0f, 0.0f};
+            double prod = 1.0;
+            for (int64_t t0 = k0; t0 < k1; t0 += 512) {
+                float f[4][4];
+                int nn[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t e = t0 + 128 * u + 4 * lane;
+                    nn[u] = (int)(k1 - e < 4 ? (k1 - e > 0 ? k1 - e : 0) : 4);
+                    if (vec && nn[u] == 4) {
+                        const float4 v = ld_stream((const float4 *)(p + e));
+                        f[u][0] = v.x; f[u][1] = v.y; f[u][2] = v.z; f[u][3] = v.w;
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) f[u][j] = j < nn[u] ? p[e + j] : 0.0f;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        if (OP == NT2G_SCAN_SUM) csum_add(acc, f[u][j]);
+                        else if (j < nn[u]) prod *= (double)f[u][j];
+                    }
+            }
+            if (OP == NT2G_SCAN_SUM) {
+                acc = warp_csum(acc);
+                if (lane == 0) rec[item] = ScanRec{(double)acc.s + (double)acc.c, 0.0f, 0};
+            } else {
+#pragma unroll
+                for (int off = 16; off; off >>= 1) prod *= __shfl_down_sync(0xffffffffu, prod, off);
+                if (lane == 0) rec[item] = ScanRec{prod, 0.0f, 0};
+            }
+            continue;
+        }
         SE<OP> carry = (PHASE == 3 && q > 1) ? from_rec<OP>(rec[item]) : SE<OP>::id();
         // the next tile's loads are issued before this tile's scan
         auto load = [&](int64_t t, float (&f)[4]) -> int {
@@ -219,15 +258,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_outer(const float *x, int
             const int64_t seg = l + v + lo * h;
             carry[v] = (PHASE == 3 && q > 1) ? from_rec<OP>(rec[seg * q + c]) : SE<OP>::id();
         }
-#pragma unroll 4
-        for (int64_t k = k0; k < k1; ++k) {
-            float e[VEC];
-            if constexpr (VEC == 4) {
-                const float4 f = ld_stream((const float4 *)(x + base + lo * k));
-                e[0] = f.x; e[1] = f.y; e[2] = f.z; e[3] = f.w;
-            } else {
-                e[0] = ld_stream(x + base + lo * k);
-            }
+        // groups of kGroup rows: all loads of a group are issued before its scan
+        constexpr int kGroup = 8;
+        auto step = [&](int64_t k, const float (&e)[VEC]) {
             float r[VEC];
 #pragma unroll
             for (int v = 0; v < VEC; ++v) {
@@ -238,6 +271,27 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_outer(const float *x, int
                 if constexpr (VEC == 4) st_stream((float4 *)(out + base + lo * k), make_float4(r[0], r[1], r[2], r[3]));
                 else out[base + lo * k] = r[0];
             }
+        };
+        auto fetch = [&](int64_t k, float (&e)[VEC]) {
+            if constexpr (VEC == 4) {
+                const float4 f = ld_stream((const float4 *)(x + base + lo * k));
+                e[0] = f.x; e[1] = f.y; e[2] = f.z; e[3] = f.w;
+            } else {
+                e[0] = ld_stream(x + base + lo * k);
+            }
+        };
+        int64_t k = k0;
+        for (; k + kGroup <= k1; k += kGroup) {
+            float e[kGroup][VEC];
+#pragma unroll
+            for (int g = 0; g < kGroup; ++g) fetch(k + g, e[g]);
+#pragma unroll
+            for (int g = 0; g < kGroup; ++g) step(k + g, e[g]);
+        }
+        for (; k < k1; ++k) {
+            float e[VEC];
+            fetch(k, e);
+            step(k, e);
         }
         if (PHASE == 1) {
 #pragma unroll
