@@ -17,8 +17,9 @@
 //   1. each chunk of each segment reduces to an aggregate,
 //   2. per segment, the chunk aggregates are scanned in order (exclusive),
 //   3. each chunk is scanned again, starting from its prefix.
-// Contiguous segments (lo = 1) run one warp per chunk in tiles of 128
-// elements (a float4 per lane, an in-order warp scan of the lane totals);
+// Contiguous segments (lo = 1) run one warp per chunk in tiles of 512
+// elements (16 consecutive ones per lane, an in-order warp scan of the lane
+// totals);
 // phase 1 of cumsum/cumprod is a plain reduction (order does not matter to a
 // commutative aggregate).  Strided segments run one thread per segment (four
 // with float4) over chunks of the scan range, 8 rows of loads at a time.  cumsum carries compensated sums (s + c; chunk prefixes in
@@ -36,7 +37,7 @@
 namespace nt2g {
 
 constexpr int kScanThreads = 256;
-constexpr int64_t kScanChunk = 16384;  // multiple of the 128-element tile
+constexpr int64_t kScanChunk = 16384;  // multiple of the 512-element tile
 constexpr int64_t kScanTarget = 152 * 1024;
 
 // ------------------------------------------------------------- elements --
@@ -136,8 +137,8 @@ template <int OP> __device__ __forceinline__ SE<OP> warp_scan(SE<OP> x, int lane
 }
 
 // ----------------------------------------- contiguous segments (lo == 1) --
-// One warp per (segment, chunk): tiles of 128 elements, lane l owning
-// elements 4l..4l+3 of the tile.  PHASE 1 keeps the running carry and stores
+// One warp per (segment, chunk): tiles of 512 elements, lane l owning
+// elements 16l..16l+15 of the tile.  PHASE 1 keeps the running carry and stores
 // the chunk aggregate; PHASE 3 starts from the chunk's prefix (or the
 // identity when there is one chunk) and writes every inclusive value.
 template <int OP, int PHASE>
@@ -192,43 +193,45 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_inner(const float *x, int
             continue;
         }
         SE<OP> carry = (PHASE == 3 && q > 1) ? from_rec<OP>(rec[item]) : SE<OP>::id();
-        // the next tile's loads are issued before this tile's scan
-        auto load = [&](int64_t t, float (&f)[4]) -> int {
-            const int64_t e = t + 4 * lane;
-            const int n = (int)(k1 - e < 4 ? (k1 - e > 0 ? k1 - e : 0) : 4);
-            if (vec && n == 4) {
-                const float4 v = ld_stream((const float4 *)(p + e));
-                f[0] = v.x; f[1] = v.y; f[2] = v.z; f[3] = v.w;
+        // tiles of 512 elements, 16 consecutive ones per lane: the lane folds its
+        // run, one in-order warp scan of the lane totals gives every lane its
+        // prefix, and the lane's outputs follow in order from that prefix
+        for (int64_t t0 = k0; t0 < k1; t0 += 512) {
+            const int64_t e0 = t0 + 16 * lane;
+            const int cnt = (int)(k1 - e0 < 16 ? (k1 - e0 > 0 ? k1 - e0 : 0) : 16);
+            float f[16];
+            if (vec && cnt == 16) {
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const float4 w = ld_stream((const float4 *)(p + e0) + v);
+                    f[4 * v] = w.x; f[4 * v + 1] = w.y; f[4 * v + 2] = w.z; f[4 * v + 3] = w.w;
+                }
             } else {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) f[j] = j < n ? p[e + j] : 0.0f;
+                for (int j = 0; j < 16; ++j) f[j] = j < cnt ? p[e0 + j] : 0.0f;
             }
-            return n;
-        };
-        float fnext[4];
-        int cnext = load(k0, fnext);
-        for (int64_t t0 = k0; t0 < k1; t0 += 128) {
-            const int64_t e0 = t0 + 4 * lane;
-            float f[4] = {fnext[0], fnext[1], fnext[2], fnext[3]};
-            const int cnt = cnext;
-            if (t0 + 128 < k1) cnext = load(t0 + 128, fnext);
-            SE<OP> loc[4];
-            loc[0] = cnt > 0 ? SE<OP>::of(f[0]) : SE<OP>::id();
+            SE<OP> agg = SE<OP>::id();
 #pragma unroll
-            for (int j = 1; j < 4; ++j) loc[j] = j < cnt ? SE<OP>::combine(loc[j - 1], SE<OP>::of(f[j])) : loc[j - 1];
-            const SE<OP> inc = warp_scan<OP>(loc[3], lane);
+            for (int j = 0; j < 16; ++j)
+                if (j < cnt) agg = SE<OP>::combine(agg, SE<OP>::of(f[j]));
+            const SE<OP> inc = warp_scan<OP>(agg, lane);
             SE<OP> ex = inc.shfl_up(1);
             if (lane == 0) ex = SE<OP>::id();
-            const SE<OP> pre = SE<OP>::combine(carry, ex);
             if (PHASE == 3) {
-                float r[4];
+                SE<OP> run = SE<OP>::combine(carry, ex);
+                float r[16];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) r[j] = SE<OP>::combine(pre, loc[j]).out();
-                if (vec && cnt == 4) {
-                    st_stream((float4 *)(o + e0), make_float4(r[0], r[1], r[2], r[3]));
+                for (int j = 0; j < 16; ++j) {
+                    run = SE<OP>::combine(run, SE<OP>::of(f[j]));
+                    r[j] = run.out();
+                }
+                if (vec && cnt == 16) {
+#pragma unroll
+                    for (int v = 0; v < 4; ++v)
+                        st_stream((float4 *)(o + e0) + v, make_float4(r[4 * v], r[4 * v + 1], r[4 * v + 2], r[4 * v + 3]));
                 } else {
 #pragma unroll
-                    for (int j = 0; j < 4; ++j)
+                    for (int j = 0; j < 16; ++j)
                         if (j < cnt) o[e0 + j] = r[j];
                 }
             }
@@ -405,7 +408,7 @@ static ScanPlan plan_scan(int64_t lo, int64_t inner, int64_t hi, bool aligned)
             chunk = (inner + per - 1) / per;
             if (chunk < 1024) chunk = 1024;
         }
-        chunk = (chunk + 127) / 128 * 128;
+        chunk = (chunk + 511) / 512 * 512;
         p.chunk = chunk;
         p.q = inner > 0 ? (inner + chunk - 1) / chunk : 1;
         return p;
