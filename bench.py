@@ -17,7 +17,14 @@ in HBM.  Workloads (--config):
   adjoint   fused BS forward + reverse (VJP), N=2^26 options
   adjoint_fwd  the forward alone on the same options (the 2.2x reference)
   sigmadelta   1920x1080 uint8 frames, one fused step per frame
+  sigmadelta_fused  63 frame steps in one kernel
   rgb2yuv   1920x1080x3 float planes
+  bs_generic / bs_interp   the bs batch through the expression API's compiled
+            kernel / interpreter (fused binding skipped)
+  fold_col / fold_row / gmax   sum(A, 1), sum(A, 2), globalmax of a 16384^2 table
+  cumsum_col / cumsum_all / cummax_row   cumulative functions on that table
+  fn_trig / fn_pow / fn_gen   sin(x)*cos(y), pow(x, y), sinpi(linspace(0,2,n))*x
+            over 2^26 elements through the compiled kernel
 Each prints one JSON line (rank 0).  --impl reference times NT2's CPU path
 (the oracle's restatement of it: NT2 itself needs Boost, absent here) on the
 host cores for the same workload.
@@ -456,6 +463,39 @@ class Scan(Workload):
                                        self.ws.numel(), L._ptr(self.y), L._stream()))
 
 
+class Functors(Workload):
+    """A generic expression of the newer functors through the run-time compiled
+    kernel (the path any user expression takes), fast policy, over 2^26-element
+    tables: sin(x) * cos(y), pow(x, y), or sinpi(linspace(0, 2, n)) * x (a
+    generative leaf: no input bytes for it)."""
+
+    def __init__(self, torch, lib, dev, kind, precision):
+        import ctypes
+        from nt2_gb300 import expr as E
+        self.torch, self.lib, self.prec = torch, lib, precision
+        n = 1 << 26
+        g = torch.Generator(device=dev).manual_seed(1003)
+        self.x = torch.rand(n, device=dev, generator=g) * 4 + 0.25
+        self.y = torch.rand(n, device=dev, generator=g) * 4 - 2
+        self.out = torch.empty_like(self.x)
+        X, Y = E.Table(self.x), E.Table(self.y)
+        e = {"trig": E.sin(X) * E.cos(Y), "pow": E.pow(X, Y), "gen": E.sinpi(E.linspace(0, 2, n)) * X}[kind]
+        prog, slots = E.compile_program([self.out], [e])
+        prog.jit_prepare(precision)
+        self.prog = prog
+        self.args = (lib.Arg * len(slots))(*[lib.Arg(t.data_ptr(), 0.0, lib.F32, 0) for t in slots])
+        self.nslots, self.n = len(slots), n
+        reads = {"trig": 8, "pow": 8, "gen": 4}[kind]
+        self.units, self.bytes, self.kernel = n, (reads + 4) * n, "nt2g_jit_kernel"
+        self.name = {"trig": "sin(x) * cos(y)", "pow": "pow(x, y)", "gen": "sinpi(linspace(0, 2, n)) * x"}[kind] + \
+            " over 2^26 float32 elements, run-time compiled kernel"
+        self.flush = "inputs larger than L2"
+
+    def step(self, i):
+        L = self.lib
+        L.check(L.load().nt2g_eval(self.prog.handle, self.args, self.nslots, 0, self.n, self.prec, 1, L._stream()))
+
+
 class Rgb2Yuv(Workload):
     SETS = 8
     independent = True
@@ -496,6 +536,8 @@ def make(name, torch, lib, dev, precision, tune=None, n=None):
         return Adjoint(torch, lib, dev)
     if name == "adjoint_fwd":
         return Adjoint(torch, lib, dev, forward_only=True)
+    if name in ("fn_trig", "fn_pow", "fn_gen"):
+        return Functors(torch, lib, dev, name[3:], precision)
     if name == "sigmadelta":
         return SigmaDelta(torch, lib, dev)
     if name == "rgb2yuv":

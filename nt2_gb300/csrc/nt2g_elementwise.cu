@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
 #pragma unroll
                 for (int j = 0; j < kV; ++j) {
                     const long long p = args.pos0 + base + j;
-                    d[j] = f32 ? __float_as_uint(__ll2float_rn(p)) : (uint32_t)(p & 255);
+                    d[j] = f32 ? __float_as_uint(pos_to_float(p)) : (uint32_t)(p & 255);
                 }
                 break;
             case NT2G_OP_STORE:

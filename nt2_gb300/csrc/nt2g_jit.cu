@@ -126,6 +126,17 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
     s += kJitPrelude;
     s += "template <class P, bool FULL>\n__device__ __forceinline__ void jit_tile(const JitArgs &a, long long i, int cnt)\n{\n";
     auto v = [](int x) { return "v" + std::to_string(x) + "[j]"; };
+    // every table load first, so a tile's memory requests are in flight while its
+    // arithmetic runs (a load never follows a store to its table: the compiler
+    // forwards stored values)
+    for (size_t k = 0; k < ops.size(); ++k) {
+        const nt2g_op &o = ops[k];
+        if (o.code != NT2G_OP_LOAD) continue;
+        const bool f32 = o.dtype == NT2G_F32;
+        s += (f32 ? "    float v" : "    unsigned v") + std::to_string(k) + "[4]; " +
+             (f32 ? "jit_ldf<FULL>(v" : "jit_ldb<FULL>(v") + std::to_string(k) + ", a.ptr[" + std::to_string(o.a) +
+             "], i, cnt);\n";
+    }
     for (size_t k = 0; k < ops.size(); ++k) {
         const nt2g_op &o = ops[k];
         const bool f32 = o.dtype == NT2G_F32;
@@ -134,10 +145,7 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         const std::string slot = std::to_string(o.a);
         std::string e;
         switch (o.code) {
-        case NT2G_OP_LOAD:
-            s += (f32 ? "    float v" : "    unsigned v") + std::to_string(k) + "[4]; " +
-                 (f32 ? "jit_ldf<FULL>(v" : "jit_ldb<FULL>(v") + std::to_string(k) + ", a.ptr[" + slot + "], i, cnt);\n";
-            continue;
+        case NT2G_OP_LOAD: continue;  // emitted above
         case NT2G_OP_STORE: {
             const std::string src = "v" + std::to_string(o.a);
             const std::string dst = std::to_string(o.b);
@@ -150,7 +158,7 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         }
         case NT2G_OP_SCALAR: e = f32 ? "a.scal[" + slot + "]" : "a.scal_u8[" + slot + "]"; break;
         case NT2G_OP_CONST: e = f32 ? fconst(o.imm) : std::to_string((uint32_t)o.imm & 255u) + "u"; break;
-        case NT2G_OP_INDEX: e = f32 ? "__ll2float_rn(a.pos0 + i + j)" : "(unsigned)((a.pos0 + i + j) & 255)"; break;
+        case NT2G_OP_INDEX: e = f32 ? "nt2g::pos_to_float(a.pos0 + i + j)" : "(unsigned)((a.pos0 + i + j) & 255)"; break;
         case NT2G_OP_ADD: e = f32 ? "P::add(" + A + ", " + B + ")" : "(" + A + " + " + B + ") & 255u"; break;
         case NT2G_OP_SUB: e = f32 ? "P::sub(" + A + ", " + B + ")" : "(" + A + " - " + B + ") & 255u"; break;
         case NT2G_OP_MUL: e = f32 ? "P::mul(" + A + ", " + B + ")" : "(" + A + " * " + B + ") & 255u"; break;

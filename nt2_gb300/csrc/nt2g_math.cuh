@@ -211,6 +211,23 @@ template <class P> NT2G_HD float exp(float a0)
     return is_nan(a0) ? a0 : r;
 }
 
+// float(p) rounded to nearest for a position 0 <= p < 2^46 (NT2's
+// enumerate<float>(p)), without the 64-bit integer conversion: with
+// p = hi 2^23 + lo, float(hi) and float(lo) are exact (the 2^23 bit-pattern
+// trick) and one fused hi * 2^23 + lo rounds the exact sum once.
+NT2G_HD float pos_to_float(long long p)
+{
+#if defined(__CUDA_ARCH__)
+    if (p >= (1ll << 46)) return __ll2float_rn(p);
+    const uint32_t lo = (uint32_t)p & 0x7fffffu, hi = (uint32_t)(p >> 23);
+    const float flo = __fsub_rn(__uint_as_float(0x4B000000u | lo), 8388608.0f);
+    const float fhi = __fsub_rn(__uint_as_float(0x4B000000u | hi), 8388608.0f);
+    return __fmaf_rn(fhi, 8388608.0f, flo);
+#else
+    return (float)p;
+#endif
+}
+
 // 2^k for k in [-126, 127] built in the exponent field (expo_scale.hpp:27-35)
 NT2G_HD float pow2i(float k) { return bits_f((uint32_t)((int32_t)k + 127) << 23); }
 
@@ -1060,7 +1077,11 @@ template <class P> NT2G_HD int trig_reduce_pi(float x, float &xr)
     const float xi = rintf(P::mul(x, 2.0f));
     const float x2 = P::sub(x, P::mul(xi, 0.5f));
     xr = P::mul(x2, bits_f(0x40490fdbu));  // Pi
-    return (fabsf(xi) < 0x1p62f) ? (int)((int64_t)xi & 3) : 0;
+    // k mod 4 without a 64-bit conversion: exact below 2^24; in [2^24, 2^25) k
+    // is even and k/2 is odd exactly when the significand's last bit is set;
+    // from 2^25 on (and for inf, NaN) k is a multiple of 4
+    if (fabsf(xi) < 16777216.0f) return (int)xi & 3;
+    return ((f_bits(xi) & 1u) && fabsf(xi) < 33554432.0f) ? 2 : 0;
 }
 
 template <class P, bool PI> NT2G_HD float cos_any(float a0)
