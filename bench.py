@@ -401,10 +401,10 @@ class Fold(Workload):
     dim 1 = per-column (contiguous) sums, dim 2 = per-row (strided) sums; or a
     global max over the same 2^28 elements."""
 
-    def __init__(self, torch, lib, dev, kind, precision):
+    def __init__(self, torch, lib, dev, kind, precision, side=16384):
         import ctypes
         self.torch, self.lib, self.prec = torch, lib, precision
-        m = n = 16384
+        m = n = side
         g = torch.Generator(device=dev).manual_seed(1001)
         self.x = torch.randn(m * n, device=dev, generator=g)
         self.shape = {"col": (1, m, n), "row": (m, n, 1), "max": (1, m * n, 1)}[kind]
@@ -418,10 +418,10 @@ class Fold(Workload):
         self.bytes = 4 * m * n + 4 * lo * hi
         self.kernel = {"col": "k_fold_inner", "row": "k_fold_outer", "max": "k_fold_inner"}[kind]
         self.launches = 1 if kind == "col" else 2  # strided and global folds add the in-order combine
-        what = {"col": "sum(A, 1): 16384 column sums", "row": "sum(A, 2): 16384 row sums",
-                "max": "globalmax over 2^28"}[kind]
-        self.name = f"fold {what} of a 16384x16384 float32 table"
-        self.flush = "1 GiB input > L2"
+        what = {"col": f"sum(A, 1): {n} column sums", "row": f"sum(A, 2): {m} row sums",
+                "max": f"globalmax over {m * n}"}[kind]
+        self.name = f"fold {what} of a {m}x{n} float32 table"
+        self.flush = f"{4 * m * n >> 20} MiB input" + (" > L2" if 4 * m * n > 129 << 20 else " (below L2)")
 
     def step(self, i):
         lo, inner, hi = self.shape
@@ -435,10 +435,10 @@ class Scan(Workload):
     (1 GiB in, 1 GiB out: 8 B/element algorithmic): cumsum per column, cumsum
     of the whole table as one segment, or cummax per row (strided)."""
 
-    def __init__(self, torch, lib, dev, kind, precision):
+    def __init__(self, torch, lib, dev, kind, precision, side=16384):
         import ctypes
         self.torch, self.lib, self.prec = torch, lib, precision
-        m = n = 16384
+        m = n = side
         g = torch.Generator(device=dev).manual_seed(1001)
         self.x = torch.randn(m * n, device=dev, generator=g)
         self.y = torch.empty_like(self.x)
@@ -451,10 +451,10 @@ class Scan(Workload):
         self.units, self.bytes = m * n, 8 * m * n
         self.kernel = "k_scan_outer" if kind == "rowmax" else "k_scan_inner"
         self.launches = 1 if nb.value == 0 else 3
-        what = {"col": "cumsum(A, 1): 16384 columns", "all": "cumsum over all 2^28 elements (one segment)",
-                "rowmax": "cummax(A, 2): 16384 rows, strided"}[kind]
-        self.name = f"scan {what} of a 16384x16384 float32 table"
-        self.flush = "1 GiB input > L2"
+        what = {"col": f"cumsum(A, 1): {n} columns", "all": f"cumsum over all {m * n} elements (one segment)",
+                "rowmax": f"cummax(A, 2): {m} rows, strided"}[kind]
+        self.name = f"scan {what} of a {m}x{n} float32 table"
+        self.flush = f"{4 * m * n >> 20} MiB input" + (" > L2" if 4 * m * n > 129 << 20 else " (below L2)")
 
     def step(self, i):
         lo, inner, hi = self.shape
@@ -469,11 +469,10 @@ class Functors(Workload):
     tables: sin(x) * cos(y), pow(x, y), or sinpi(linspace(0, 2, n)) * x (a
     generative leaf: no input bytes for it)."""
 
-    def __init__(self, torch, lib, dev, kind, precision):
-        import ctypes
+    def __init__(self, torch, lib, dev, kind, precision, n=None):
         from nt2_gb300 import expr as E
         self.torch, self.lib, self.prec = torch, lib, precision
-        n = 1 << 26
+        n = n or 1 << 26
         g = torch.Generator(device=dev).manual_seed(1003)
         self.x = torch.rand(n, device=dev, generator=g) * 4 + 0.25
         self.y = torch.rand(n, device=dev, generator=g) * 4 - 2
@@ -488,7 +487,7 @@ class Functors(Workload):
         reads = {"trig": 8, "pow": 8, "gen": 4}[kind]
         self.units, self.bytes, self.kernel = n, (reads + 4) * n, "nt2g_jit_kernel"
         self.name = {"trig": "sin(x) * cos(y)", "pow": "pow(x, y)", "gen": "sinpi(linspace(0, 2, n)) * x"}[kind] + \
-            " over 2^26 float32 elements, run-time compiled kernel"
+            f" over {n} float32 elements, run-time compiled kernel"
         self.flush = "inputs larger than L2"
 
     def step(self, i):
@@ -517,6 +516,12 @@ class Rgb2Yuv(Workload):
         self.lib.rgb2yuv(r, g, b, y, u, v)
 
 
+def _side(n):
+    """Side of the square table holding about n elements (default 16384)."""
+    import math
+    return 16384 if not n else max(1, math.isqrt(n))
+
+
 def make(name, torch, lib, dev, precision, tune=None, n=None):
     if name == "bs":
         return BlackScholes(torch, lib, dev, precision, n)
@@ -537,7 +542,7 @@ def make(name, torch, lib, dev, precision, tune=None, n=None):
     if name == "adjoint_fwd":
         return Adjoint(torch, lib, dev, forward_only=True)
     if name in ("fn_trig", "fn_pow", "fn_gen"):
-        return Functors(torch, lib, dev, name[3:], precision)
+        return Functors(torch, lib, dev, name[3:], precision, n)
     if name == "sigmadelta":
         return SigmaDelta(torch, lib, dev)
     if name == "rgb2yuv":
@@ -546,9 +551,10 @@ def make(name, torch, lib, dev, precision, tune=None, n=None):
         return SigmaDeltaFused(torch, lib, dev)
     if name in ("cumsum_col", "cumsum_all", "cummax_row"):
         return Scan(torch, lib, dev, {"cumsum_col": "col", "cumsum_all": "all", "cummax_row": "rowmax"}[name],
-                    precision)
+                    precision, _side(n))
     if name in ("fold_col", "fold_row", "gmax"):
-        return Fold(torch, lib, dev, {"fold_col": "col", "fold_row": "row", "gmax": "max"}[name], precision)
+        return Fold(torch, lib, dev, {"fold_col": "col", "fold_row": "row", "gmax": "max"}[name], precision,
+                    _side(n))
     raise SystemExit(f"unknown config {name}")
 
 
@@ -780,7 +786,8 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="issue the K steps eagerly instead of from a graph")
     ap.add_argument("--streams", type=int, default=2, help="streams for independent steps inside the graph")
     ap.add_argument("--tune", default="", help="batched: block_threads,blocks_per_sm,tile_vectors")
-    ap.add_argument("--n", type=int, default=0, help="bs, bs_generic, bs_interp: options per launch (default 2^20)")
+    ap.add_argument("--n", type=int, default=0, help="bs, bs_generic, bs_interp: options per launch (default 2^20); "
+                    "fold/scan configs: elements of the square table (default 2^28); fn_*: elements (default 2^26)")
     ap.add_argument("--min-seconds", type=float, default=2.0, help="repeat K-step trials for at least this long")
     args = ap.parse_args()
     if args.warmup < 3:

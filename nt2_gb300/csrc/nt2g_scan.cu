@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_outer(const float *x, int
 #pragma unroll
         for (int v = 0; v < VEC; ++v) {
             const int64_t seg = l + v + lo * h;
-            carry[v] = (PHASE == 3 && q > 1) ? from_rec<OP>(rec[seg * q + c]) : SE<OP>::id();
+            carry[v] = (PHASE == 3 && q > 1) ? from_rec<OP>(rec[c * lo * hi + seg]) : SE<OP>::id();
         }
         // groups of kGroup rows: all loads of a group are issued before its scan
         constexpr int kGroup = 8;
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_outer(const float *x, int
         }
         if (PHASE == 1) {
 #pragma unroll
-            for (int v = 0; v < VEC; ++v) rec[(l + v + lo * h) * q + c] = to_rec<OP>(carry[v]);
+            for (int v = 0; v < VEC; ++v) rec[c * lo * hi + (l + v + lo * h)] = to_rec<OP>(carry[v]);
         }
     }
 }
@@ -320,51 +320,93 @@ template <int OP> __device__ __forceinline__ ScanRec rec_combine(const ScanRec &
 // Phase 2: per segment, replace the chunk aggregates by their exclusive
 // prefixes in order (few chunks: one thread per segment).
 template <int OP>
-__global__ void __launch_bounds__(kScanThreads) k_scan_prefix(ScanRec *__restrict__ rec, int64_t n_seg, int64_t q)
+__global__ void __launch_bounds__(kScanThreads) k_scan_prefix(ScanRec *__restrict__ rec, int64_t n_seg, int64_t q,
+                                                              int64_t cs)
 {
+    // record c of segment s at rec[s * ss + c * cs]: ss = q, cs = 1 for contiguous
+    // scans; ss = 1, cs = n_seg (chunk-major, coalesced over segments) for strided ones
+    const int64_t ss = cs == 1 ? q : 1;
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_seg; s += (int64_t)gridDim.x * blockDim.x) {
-        ScanRec *r = rec + s * q;
+        ScanRec *r = rec + s * ss;
         ScanRec acc = rec_id<OP>();
-        for (int64_t c = 0; c < q; ++c) {
-            const ScanRec a = r[c];
-            r[c] = acc;
+        int64_t c = 0;
+        for (; c + 8 <= q; c += 8) {  // eight independent loads in flight
+            ScanRec a[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a[u] = r[(c + u) * cs];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                r[(c + u) * cs] = acc;
+                acc = rec_combine<OP>(acc, a[u]);
+            }
+        }
+        for (; c < q; ++c) {
+            const ScanRec a = r[c * cs];
+            r[c * cs] = acc;
             acc = rec_combine<OP>(acc, a);
         }
     }
 }
 
-// Phase 2 for many chunks: one block per segment; thread t takes the
-// contiguous range [t*q/T, (t+1)*q/T), the block scans the thread totals in
-// thread order, and each thread rewrites its range as exclusive prefixes.
-// The combine order is fixed for a given q.
+// Phase 2 for many chunks: one block per segment (below).  The combine order
+// is fixed for a given q.
+template <int OP> __device__ __forceinline__ ScanRec rec_shfl_up(const ScanRec &a, int off)
+{
+    return ScanRec{__shfl_up_sync(0xffffffffu, a.d, off), __shfl_up_sync(0xffffffffu, a.v, off),
+                    __shfl_up_sync(0xffffffffu, a.h, off)};
+}
+
 template <int OP>
 __global__ void __launch_bounds__(kScanThreads) k_scan_prefix_block(ScanRec *__restrict__ rec, int64_t n_seg,
-                                                                    int64_t q)
+                                                                    int64_t q, int64_t cs)
 {
-    __shared__ ScanRec tot[kScanThreads];
+    // tiles of kScanThreads x 8 consecutive records: each thread loads its 8
+    // (independent loads), the thread totals are scanned in order across the
+    // block (warp shuffles, then the warp totals), and a carry runs over the tiles
+    constexpr int kPer = 8, kWarps = kScanThreads / 32;
+    __shared__ ScanRec wtot[kWarps];
+    __shared__ ScanRec carry_s;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (int64_t s = blockIdx.x; s < n_seg; s += gridDim.x) {
-        ScanRec *r = rec + s * q;
-        const int64_t c0 = q * threadIdx.x / blockDim.x, c1 = q * (threadIdx.x + 1) / blockDim.x;
-        ScanRec acc = rec_id<OP>();
-        for (int64_t c = c0; c < c1; ++c) acc = rec_combine<OP>(acc, r[c]);
-        tot[threadIdx.x] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            ScanRec run = rec_id<OP>();
-            for (int t = 0; t < (int)blockDim.x; ++t) {
-                const ScanRec a = tot[t];
-                tot[t] = run;
-                run = rec_combine<OP>(run, a);
+        ScanRec *r = rec + s * (cs == 1 ? q : 1);
+        ScanRec carry = rec_id<OP>();
+        for (int64_t t0 = 0; t0 < q; t0 += (int64_t)kScanThreads * kPer) {
+            const int64_t c0 = t0 + (int64_t)tid * kPer;
+            ScanRec a[kPer];
+#pragma unroll
+            for (int u = 0; u < kPer; ++u) a[u] = c0 + u < q ? r[(c0 + u) * cs] : rec_id<OP>();
+            ScanRec tot = rec_id<OP>();
+#pragma unroll
+            for (int u = 0; u < kPer; ++u) tot = rec_combine<OP>(tot, a[u]);
+            ScanRec inc = tot;  // in-order inclusive scan of the thread totals in the warp
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const ScanRec o = rec_shfl_up<OP>(inc, off);
+                if (lane >= off) inc = rec_combine<OP>(o, inc);
             }
+            if (lane == 31) wtot[wid] = inc;
+            __syncthreads();
+            if (tid == 0) {  // the warp totals in order, and the next tile's carry
+                ScanRec run = carry;
+                for (int w = 0; w < kWarps; ++w) {
+                    const ScanRec x = wtot[w];
+                    wtot[w] = run;
+                    run = rec_combine<OP>(run, x);
+                }
+                carry_s = run;
+            }
+            __syncthreads();
+            ScanRec ex = rec_shfl_up<OP>(inc, 1);
+            if (lane == 0) ex = rec_id<OP>();
+            ScanRec pre = rec_combine<OP>(wtot[wid], ex);
+#pragma unroll
+            for (int u = 0; u < kPer; ++u) {
+                if (c0 + u < q) r[(c0 + u) * cs] = pre;
+                pre = rec_combine<OP>(pre, a[u]);
+            }
+            carry = carry_s;
+            __syncthreads();
         }
-        __syncthreads();
-        ScanRec pre = tot[threadIdx.x];
-        for (int64_t c = c0; c < c1; ++c) {
-            const ScanRec a = r[c];
-            r[c] = pre;
-            pre = rec_combine<OP>(pre, a);
-        }
-        __syncthreads();
     }
 }
 
@@ -436,11 +478,11 @@ nt2g_status scan_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *
     return NT2G_OK;
 }
 
-template <int OP> static void launch_prefix(ScanRec *rec, int64_t n_seg, int64_t q, cudaStream_t st)
+template <int OP> static void launch_prefix(ScanRec *rec, int64_t n_seg, int64_t q, int64_t cs, cudaStream_t st)
 {
     auto cap = [](int64_t g) { return (int)(g < 152 * 32 ? (g > 0 ? g : 1) : 152 * 32); };
-    if (q >= 512) k_scan_prefix_block<OP><<<cap(n_seg), kScanThreads, 0, st>>>(rec, n_seg, q);
-    else k_scan_prefix<OP><<<cap((n_seg + kScanThreads - 1) / kScanThreads), kScanThreads, 0, st>>>(rec, n_seg, q);
+    if (q >= 512) k_scan_prefix_block<OP><<<cap(n_seg), kScanThreads, 0, st>>>(rec, n_seg, q, cs);
+    else k_scan_prefix<OP><<<cap((n_seg + kScanThreads - 1) / kScanThreads), kScanThreads, 0, st>>>(rec, n_seg, q, cs);
 }
 
 template <int OP>
@@ -464,7 +506,7 @@ static nt2g_status launch_scan_op(const float *x, int64_t lo, int64_t inner, int
         const int grid = cap((hi * p.q + 7) / 8);
         if (p.q > 1) {
             k_scan_inner<OP, 1><<<grid, kScanThreads, 0, st>>>(x, inner, hi, p.chunk, p.q, p.vec, rec, out);
-            launch_prefix<OP>(rec, n_seg, p.q, st);
+            launch_prefix<OP>(rec, n_seg, p.q, 1, st);
         }
         k_scan_inner<OP, 3><<<grid, kScanThreads, 0, st>>>(x, inner, hi, p.chunk, p.q, p.vec, rec, out);
     } else {
@@ -472,13 +514,13 @@ static nt2g_status launch_scan_op(const float *x, int64_t lo, int64_t inner, int
         if (p.vec == 4) {
             if (p.q > 1) {
                 k_scan_outer<OP, 4, 1><<<grid, kScanThreads, 0, st>>>(x, lo, inner, hi, p.chunk, p.q, rec, out);
-                launch_prefix<OP>(rec, n_seg, p.q, st);
+                launch_prefix<OP>(rec, n_seg, p.q, n_seg, st);
             }
             k_scan_outer<OP, 4, 3><<<grid, kScanThreads, 0, st>>>(x, lo, inner, hi, p.chunk, p.q, rec, out);
         } else {
             if (p.q > 1) {
                 k_scan_outer<OP, 1, 1><<<grid, kScanThreads, 0, st>>>(x, lo, inner, hi, p.chunk, p.q, rec, out);
-                launch_prefix<OP>(rec, n_seg, p.q, st);
+                launch_prefix<OP>(rec, n_seg, p.q, n_seg, st);
             }
             k_scan_outer<OP, 1, 3><<<grid, kScanThreads, 0, st>>>(x, lo, inner, hi, p.chunk, p.q, rec, out);
         }
