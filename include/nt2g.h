@@ -165,7 +165,9 @@ nt2g_status nt2g_program_jit_prepare(const nt2g_program *p, int32_t precision);
  * threads), one thread per output.  NT2G_PREC_FAST: compensated FP32 sums
  * combined in FP64, FP64 products, exact max/min (equal to the NT2 order on
  * NaN-free data; a NaN propagates); deterministic for a given shape.
- * workspace: nt2g_fold_workspace_size bytes (0 means none is needed). */
+ * workspace: nt2g_fold_workspace_size bytes (enough for every op; var and
+ * stdev keep each output's centre there, so they need it under either
+ * policy, the others only under NT2G_PREC_FAST and only for chunked shapes). */
 typedef enum nt2g_fold_op {
     NT2G_FOLD_SUM = 0,
     NT2G_FOLD_PROD = 1,
@@ -174,7 +176,11 @@ typedef enum nt2g_fold_op {
     NT2G_FOLD_MEAN = 4,
     NT2G_FOLD_ASUM1 = 5,
     NT2G_FOLD_ASUM2 = 6,
-    NT2G_FOLD_NORM2 = 7
+    NT2G_FOLD_NORM2 = 7,
+    NT2G_FOLD_VAR = 8,     /* asum2(a - mean(a)) / (n - 1)  (NT2's var(a))     */
+    NT2G_FOLD_STDEV = 9,   /* sqrt(var)                                       */
+    NT2G_FOLD_VAR1 = 10,   /* asum2(a - mean(a)) / n        (NT2's var(a, 1))  */
+    NT2G_FOLD_STDEV1 = 11  /* sqrt(var1)                                      */
 } nt2g_fold_op;
 
 nt2g_status nt2g_fold_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);

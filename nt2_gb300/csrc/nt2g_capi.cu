@@ -888,7 +888,7 @@ extern "C" nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, 
 {
     NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_fold_f32: negative extent (%lld, %lld, %lld)",
                    (long long)lo, (long long)inner, (long long)hi);
-    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_NORM2, "nt2g_fold_f32: op %d", op);
+    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_STDEV1, "nt2g_fold_f32: op %d", op);
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_fold_f32: precision %d",
                    precision);
     NT2G_CHECK_ARG(index == nullptr || op == NT2G_FOLD_MAX || op == NT2G_FOLD_MIN,
@@ -898,8 +898,11 @@ extern "C" nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, 
     NT2G_CHECK_ARG(out != nullptr, "nt2g_fold_f32: out is NULL");
     NT2G_CHECK_ARG(x != nullptr || inner == 0, "nt2g_fold_f32: x is NULL");
     size_t need = 0;
-    fold_workspace_bytes(lo, inner, hi, &need);
-    NT2G_CHECK_ARG(precision == NT2G_PREC_NT2 || need == 0 || (workspace != nullptr && workspace_bytes >= need),
+    const bool centred = op >= NT2G_FOLD_VAR;  // var/stdev keep each output's centre in the workspace
+    if (centred) fold_workspace_bytes(lo, inner, hi, &need);
+    else fold_partials_bytes(lo, inner, hi, &need);
+    NT2G_CHECK_ARG((precision == NT2G_PREC_NT2 && !centred) || need == 0 ||
+                       (workspace != nullptr && workspace_bytes >= need),
                    "nt2g_fold_f32: workspace of %zu bytes, %zu needed", workspace_bytes, need);
     NT2G_CHECK_ARG(((uintptr_t)workspace & 15u) == 0, "nt2g_fold_f32: workspace not 16-byte aligned");
     NT2G_REACH(x); NT2G_REACH(out); NT2G_REACH(index); NT2G_REACH(workspace);

@@ -1,5 +1,5 @@
 // nt2g_fold.cu -- reductions along one dimension: sum, prod, max, min, mean,
-// asum1, asum2, norm2 of a table viewed as [lo, inner, hi] (column-major),
+// asum1, asum2, norm2, var, stdev of a table viewed as [lo, inner, hi] (column-major),
 // folding over `inner`.  out[l + lo*h] = fold_k x[l + lo*(k + inner*h)].
 //
 // NT2 reshapes every reduction this way before folding
@@ -15,10 +15,15 @@
 // worker/outer_fold.hpp, details/fold_step.hpp:31-43): bit-identical to NT2
 // wherever NT2 spreads the outputs over threads.  mean = rec(float(n)) * sum
 // (core/functions/expr/mean.hpp:22-33), asum1 = sum(abs), asum2 = sum(sqr_abs),
-// norm2 = sqrt(asum2) (expr/asum1.hpp, expr/asum2.hpp, expr/norm2.hpp).
+// norm2 = sqrt(asum2) (expr/asum1.hpp, expr/asum2.hpp, expr/norm2.hpp),
+// var = f * asum2(a - mean(a)) with f = rec(n - 1) (rec(n) for var(a, 1); 1
+// when n <= 1) and stdev = sqrt(var) (expr/var.hpp, expr/stdev.hpp): a mean
+// pass, then the centred sum of squares.
 //
 // Fast policy: sums are compensated FP32 (TwoSum; squares carry their FMA
-// product error) per chunk, chunks combined in FP64 in index order; prod in
+// product error) per chunk, chunks combined in FP64 in index order; var/stdev
+// centre on the float mean and correct for its rounding error
+// (sum (x - m)^2 - n (mu - m)^2, mu the FP64 mean); prod in
 // FP64; max/min are exact.  Contiguous segments are cut into chunks, one warp
 // per chunk with 128-bit loads; strided folds run one thread per output (four
 // with 128-bit loads) over chunks of the fold range.  With more than one
@@ -35,10 +40,18 @@ constexpr int64_t kChunk = 16384;        // elements per warp work item (contigu
 constexpr int64_t kSmallSeg = 64;        // segments up to this length: one thread each
 constexpr int64_t kTargetThreads = 152 * 1024;
 
+// Internal: the mean of each output written with the rounding error of its
+// float value (the centre of a fast-policy variance).
+constexpr int kFoldMeanC = 100;
+
+__host__ __device__ constexpr bool fold_is_var(int op)
+{
+    return op == NT2G_FOLD_VAR || op == NT2G_FOLD_STDEV || op == NT2G_FOLD_VAR1 || op == NT2G_FOLD_STDEV1;
+}
 __host__ __device__ constexpr bool fold_is_sum(int op)
 {
     return op == NT2G_FOLD_SUM || op == NT2G_FOLD_MEAN || op == NT2G_FOLD_ASUM1 || op == NT2G_FOLD_ASUM2 ||
-           op == NT2G_FOLD_NORM2;
+           op == NT2G_FOLD_NORM2 || op == kFoldMeanC || fold_is_var(op);
 }
 
 // max/min in NT2's order: the fold keeps acc unless x is strictly better, so
@@ -109,6 +122,23 @@ template <int OP> __device__ __forceinline__ void sum_elem(CSum &a, float x)
     }
 }
 
+// variance terms: (x - m)^2 with the difference kept exactly as dh + dl
+// (TwoSum) and the square's rounding error carried, so the sum of squared
+// deviations is compensated like the other sums
+template <int OP> __device__ __forceinline__ void sum_elem_c(CSum &a, float x, float m)
+{
+    if constexpr (fold_is_var(OP)) {
+        const float dh = __fsub_rn(x, m);
+        const float bb = __fsub_rn(dh, x);
+        const float dl = __fadd_rn(__fsub_rn(x, __fsub_rn(dh, bb)), __fsub_rn(-m, bb));
+        const float p = __fmul_rn(dh, dh);
+        csum_add(a, p);
+        a.c = __fadd_rn(a.c, __fmaf_rn(2.0f * dh, dl, __fmaf_rn(dh, dh, -p)));
+    } else {
+        sum_elem<OP>(a, x);
+    }
+}
+
 // ---------------------------------------------------------------- partials --
 // 32 bytes per (output, chunk): a double (sums, prod) or a Best.
 struct Partial {
@@ -121,6 +151,31 @@ template <int OP> __device__ __forceinline__ float finish_double(double t, int64
     if (OP == NT2G_FOLD_MEAN) return (float)(t / (double)inner);
     if (OP == NT2G_FOLD_NORM2) return (float)sqrt(t);
     return (float)t;
+}
+
+// Writes output o of a sum-type (or product) fold from its FP64 total.
+// Variance: the sum of squares about the float centre m, corrected to the
+// exact mean mu = m + delta (sum (x - m)^2 = sum (x - mu)^2 + n delta^2),
+// divided by n - 1 (by n for VAR1/STDEV1; 1 when n <= 1).
+template <int OP>
+__device__ __forceinline__ void fold_put(float *out, int64_t o, int64_t n_out, double t, int64_t inner, const float *cen)
+{
+    if constexpr (OP == kFoldMeanC) {
+        const double mu = t / (double)inner;
+        const float m = (float)mu;
+        out[o] = m;
+        out[n_out + o] = (float)(mu - (double)m);
+    } else if constexpr (fold_is_var(OP)) {
+        const double d = (double)cen[n_out + o];
+        const double n = (double)inner;
+        double v = t - n * d * d;
+        v = v > 0.0 ? v : 0.0;
+        const bool by_n = OP == NT2G_FOLD_VAR1 || OP == NT2G_FOLD_STDEV1;
+        if (inner > 1) v /= by_n ? n : n - 1.0;
+        out[o] = (OP == NT2G_FOLD_STDEV || OP == NT2G_FOLD_STDEV1) ? (float)sqrt(v) : (float)v;
+    } else {
+        out[o] = finish_double<OP>(t, inner);
+    }
 }
 
 // ------------------------------------------- warp-shuffle merges (fast) --
@@ -148,7 +203,7 @@ template <int OP, bool FINAL, bool IDX>
 __global__ void __launch_bounds__(kFoldThreads) k_fold_inner(const float *__restrict__ x, int64_t inner, int64_t hi,
                                                              int64_t chunk, int64_t q, int vec,
                                                              Partial *__restrict__ part, float *__restrict__ out,
-                                                             int64_t *__restrict__ index)
+                                                             int64_t *__restrict__ index, const float *__restrict__ cen)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -159,9 +214,10 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_inner(const float *__rest
         const float *p = x + seg * inner;
         CSum acc{0.0f, 0.0f};
         double prod = 1.0;
+        const float m = fold_is_var(OP) ? cen[seg] : 0.0f;
         Run<OP == NT2G_FOLD_MAX, IDX> run[4];  // one per float4 component: four independent chains
         auto take = [&](int c, float v, int32_t k) {  // k: position relative to k0
-            if (fold_is_sum(OP)) sum_elem<OP>(acc, v);
+            if (fold_is_sum(OP)) sum_elem_c<OP>(acc, v, m);
             else if (OP == NT2G_FOLD_PROD) prod *= (double)v;
             else run[c].add(v, k);
         };
@@ -191,7 +247,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_inner(const float *__rest
         }
         if (lane == 0) {
             if (FINAL) {
-                if (fold_is_sum(OP) || OP == NT2G_FOLD_PROD) out[seg] = finish_double<OP>(r.d, inner);
+                if (fold_is_sum(OP) || OP == NT2G_FOLD_PROD) fold_put<OP>(out, seg, hi, r.d, inner, cen);
                 else { out[seg] = r.b.v; if (index) index[seg] = r.b.ifirst; }
             } else {
                 part[item] = r;
@@ -203,7 +259,8 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_inner(const float *__rest
 // Short contiguous segments: one thread per segment, in order.
 template <int OP>
 __global__ void __launch_bounds__(kFoldThreads) k_fold_short(const float *__restrict__ x, int64_t inner, int64_t hi,
-                                                             float *__restrict__ out, int64_t *__restrict__ index)
+                                                             float *__restrict__ out, int64_t *__restrict__ index,
+                                                             const float *__restrict__ cen)
 {
     for (int64_t seg = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; seg < hi;
          seg += (int64_t)gridDim.x * blockDim.x) {
@@ -211,13 +268,14 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_short(const float *__rest
         CSum acc{0.0f, 0.0f};
         double prod = 1.0;
         Run<OP == NT2G_FOLD_MAX> run;
+        const float m = fold_is_var(OP) ? cen[seg] : 0.0f;
         for (int64_t k = 0; k < inner; ++k) {
             const float v = p[k];
-            if (fold_is_sum(OP)) sum_elem<OP>(acc, v);
+            if (fold_is_sum(OP)) sum_elem_c<OP>(acc, v, m);
             else if (OP == NT2G_FOLD_PROD) prod *= (double)v;
             else run.add(v, (int32_t)k);
         }
-        if (fold_is_sum(OP)) out[seg] = finish_double<OP>((double)acc.s + (double)acc.c, inner);
+        if (fold_is_sum(OP)) fold_put<OP>(out, seg, hi, (double)acc.s + (double)acc.c, inner, cen);
         else if (OP == NT2G_FOLD_PROD) out[seg] = (float)prod;
         else {
             const Best b = run.to_best(0);
@@ -234,7 +292,7 @@ template <int OP, int VEC, bool FINAL>
 __global__ void __launch_bounds__(kFoldThreads) k_fold_outer(const float *__restrict__ x, int64_t lo, int64_t inner,
                                                              int64_t hi, int64_t ck, int64_t q,
                                                              Partial *__restrict__ part, float *__restrict__ out,
-                                                             int64_t *__restrict__ index)
+                                                             int64_t *__restrict__ index, const float *__restrict__ cen)
 {
     const int64_t lv = lo / VEC;  // thread columns per h
     const int64_t c = blockIdx.y;
@@ -245,8 +303,13 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_outer(const float *__rest
         CSum acc[VEC];
         double prod[VEC];
         Run<OP == NT2G_FOLD_MAX> run[VEC];
+        float m[VEC];
 #pragma unroll
-        for (int v = 0; v < VEC; ++v) { acc[v] = CSum{0.0f, 0.0f}; prod[v] = 1.0; }
+        for (int v = 0; v < VEC; ++v) {
+            acc[v] = CSum{0.0f, 0.0f};
+            prod[v] = 1.0;
+            m[v] = fold_is_var(OP) ? cen[l + v + lo * h] : 0.0f;
+        }
         for (int64_t k = k0; k < k1; ++k) {
             float e[VEC];
             if constexpr (VEC == 4) {
@@ -257,7 +320,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_outer(const float *__rest
             }
 #pragma unroll
             for (int v = 0; v < VEC; ++v) {
-                if (fold_is_sum(OP)) sum_elem<OP>(acc[v], e[v]);
+                if (fold_is_sum(OP)) sum_elem_c<OP>(acc[v], e[v], m[v]);
                 else if (OP == NT2G_FOLD_PROD) prod[v] *= (double)e[v];
                 else run[v].add(e[v], (int32_t)(k - k0));
             }
@@ -270,7 +333,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_outer(const float *__rest
             else if (OP == NT2G_FOLD_PROD) r.d = prod[v];
             else r.b = run[v].to_best(k0);
             if (FINAL) {
-                if (fold_is_sum(OP) || OP == NT2G_FOLD_PROD) out[o] = finish_double<OP>(r.d, inner);
+                if (fold_is_sum(OP) || OP == NT2G_FOLD_PROD) fold_put<OP>(out, o, lo * hi, r.d, inner, cen);
                 else { out[o] = r.b.v; if (index) index[o] = r.b.ifirst; }
             } else {
                 part[o * q + c] = r;
@@ -283,14 +346,14 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_outer(const float *__rest
 template <int OP>
 __global__ void __launch_bounds__(kFoldThreads) k_fold_finish(const Partial *__restrict__ part, int64_t n_out,
                                                               int64_t q, int64_t inner, float *__restrict__ out,
-                                                              int64_t *__restrict__ index)
+                                                              int64_t *__restrict__ index, const float *__restrict__ cen)
 {
     for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n_out; o += (int64_t)gridDim.x * blockDim.x) {
         const Partial *p = part + o * q;
         if (fold_is_sum(OP) || OP == NT2G_FOLD_PROD) {
             double t = OP == NT2G_FOLD_PROD ? 1.0 : 0.0;
             for (int64_t c = 0; c < q; ++c) t = OP == NT2G_FOLD_PROD ? t * p[c].d : t + p[c].d;
-            out[o] = finish_double<OP>(t, inner);
+            fold_put<OP>(out, o, n_out, t, inner, cen);
         } else {
             Best b{0.0f, -1, -1};
             for (int64_t c = 0; c < q; ++c)
@@ -307,7 +370,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_finish(const Partial *__r
 template <int OP>
 __global__ void __launch_bounds__(kFoldThreads) k_fold_finish_block(const Partial *__restrict__ part, int64_t n_out,
                                                                     int64_t q, int64_t inner, float *__restrict__ out,
-                                                                    int64_t *__restrict__ index)
+                                                                    int64_t *__restrict__ index, const float *__restrict__ cen)
 {
     constexpr bool DBL = fold_is_sum(OP) || OP == NT2G_FOLD_PROD;
     __shared__ double sd[kFoldThreads];
@@ -336,7 +399,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_finish_block(const Partia
         }
         if (threadIdx.x == 0) {
             if (DBL) {
-                out[o] = finish_double<OP>(sd[0], inner);
+                fold_put<OP>(out, o, n_out, sd[0], inner, cen);
             } else {
                 out[o] = sb[0].v;
                 if (index) index[o] = sb[0].ifirst;
@@ -350,7 +413,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_finish_block(const Partia
 template <int OP>
 __global__ void __launch_bounds__(kFoldThreads) k_fold_nt2(const float *__restrict__ x, int64_t lo, int64_t inner,
                                                            int64_t hi, float *__restrict__ out,
-                                                           int64_t *__restrict__ index)
+                                                           int64_t *__restrict__ index, const float *__restrict__ cen)
 {
     for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < lo * hi; o += (int64_t)gridDim.x * blockDim.x) {
         const int64_t h = o / lo, l = o - h * lo;
@@ -359,8 +422,14 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_nt2(const float *__restri
                   : OP == NT2G_FOLD_MAX  ? -__int_as_float(0x7f800000)
                   : OP == NT2G_FOLD_MIN  ? __int_as_float(0x7f800000)
                                          : 0.0f;
+        const float m = fold_is_var(OP) ? cen[o] : 0.0f;
         for (int64_t k = 0; k < inner; ++k) {
             const float v = p[lo * k];
+            if constexpr (fold_is_var(OP)) {  // asum2(center(a)): (x - mean(a))^2 in order
+                const float d = __fsub_rn(v, m);
+                acc = __fadd_rn(acc, __fmul_rn(d, d));
+                continue;
+            }
             switch (OP) {
             case NT2G_FOLD_PROD: acc = __fmul_rn(acc, v); break;
             case NT2G_FOLD_MAX: acc = (acc > v) ? acc : v; break;
@@ -372,6 +441,13 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_nt2(const float *__restri
         }
         if (OP == NT2G_FOLD_MEAN) acc = __fmul_rn(__fdiv_rn(1.0f, (float)inner), acc);
         if (OP == NT2G_FOLD_NORM2) acc = __fsqrt_rn(acc);
+        if constexpr (fold_is_var(OP)) {  // var = f * asum2, f = n <= 1 ? 1 : rec(n - 1) (rec(n) for w = 1)
+            const float n = (float)inner;
+            const bool by_n = OP == NT2G_FOLD_VAR1 || OP == NT2G_FOLD_STDEV1;
+            const float f = (n <= 1.0f) ? 1.0f : __fdiv_rn(1.0f, by_n ? n : __fsub_rn(n, 1.0f));
+            acc = __fmul_rn(f, acc);
+            if (OP == NT2G_FOLD_STDEV || OP == NT2G_FOLD_STDEV1) acc = __fsqrt_rn(acc);
+        }
         out[o] = acc;
         if ((OP == NT2G_FOLD_MAX || OP == NT2G_FOLD_MIN) && index) {
             int64_t f = -1;
@@ -426,24 +502,58 @@ static FoldPlan plan_fold(int64_t lo, int64_t inner, int64_t hi, bool aligned)
     return p;
 }
 
-nt2g_status fold_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes)
+// Workspace: the partials of the chunked plans, then (for var/stdev) each
+// output's centre and its rounding error, 16-byte aligned.
+static size_t fold_partial_bytes(int64_t lo, int64_t inner, int64_t hi)
 {
     FoldPlan p = plan_fold(lo, inner, hi, true);
     FoldPlan u = plan_fold(lo, inner, hi, false);
     int64_t q = p.q > u.q ? p.q : u.q;
-    *bytes = q > 1 ? (size_t)(lo * hi) * (size_t)q * sizeof(Partial) : 0;
+    return q > 1 ? (size_t)(lo * hi) * (size_t)q * sizeof(Partial) : 0;
+}
+static size_t fold_centre_offset(int64_t lo, int64_t inner, int64_t hi)
+{
+    return (fold_partial_bytes(lo, inner, hi) + 15) / 16 * 16;
+}
+
+nt2g_status fold_partials_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes)
+{
+    *bytes = fold_partial_bytes(lo, inner, hi);
+    return NT2G_OK;
+}
+
+nt2g_status fold_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes)
+{
+    *bytes = fold_centre_offset(lo, inner, hi) + (size_t)(lo * hi) * 2 * sizeof(float);
     return NT2G_OK;
 }
 
 template <int OP>
 static nt2g_status launch_fold_op(const float *x, int64_t lo, int64_t inner, int64_t hi, int precision, void *ws,
-                                  size_t ws_bytes, float *out, int64_t *index, cudaStream_t st)
+                                  size_t ws_bytes, float *out, int64_t *index, cudaStream_t st,
+                                  const float *cen = nullptr)
 {
     const int64_t n_out = lo * hi;
+    if constexpr (fold_is_var(OP)) {
+        if (!cen) {  // first the centre of every output: NT2's float mean, or (fast) the mean and its rounding error
+            const size_t off = fold_centre_offset(lo, inner, hi);
+            if (!ws || off + (size_t)n_out * 2 * sizeof(float) > ws_bytes) {
+                set_error("nt2g_fold_f32: workspace of %zu bytes, %zu needed", ws_bytes,
+                          off + (size_t)n_out * 2 * sizeof(float));
+                return NT2G_ERR_INVALID;
+            }
+            float *c = (float *)((char *)ws + off);
+            const nt2g_status s = (precision == NT2G_PREC_NT2 || inner == 0)
+                                      ? launch_fold_op<NT2G_FOLD_MEAN>(x, lo, inner, hi, precision, ws, off, c, nullptr, st)
+                                      : launch_fold_op<kFoldMeanC>(x, lo, inner, hi, precision, ws, off, c, nullptr, st);
+            if (s != NT2G_OK) return s;
+            return launch_fold_op<OP>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st, c);
+        }
+    }
     auto cap = [](int64_t g) { return (int)(g < 152 * 32 ? (g > 0 ? g : 1) : 152 * 32); };
     if (precision == NT2G_PREC_NT2 || inner == 0) {  // (an empty fold yields the neutral element)
         k_fold_nt2<OP><<<cap((n_out + kFoldThreads - 1) / kFoldThreads), kFoldThreads, 0, st>>>(x, lo, inner, hi, out,
-                                                                                               index);
+                                                                                               index, cen);
         NT2G_LAUNCH_CHECK("fold launch");
         return NT2G_OK;
     }
@@ -455,36 +565,37 @@ static nt2g_status launch_fold_op(const float *x, int64_t lo, int64_t inner, int
     }
     Partial *part = (Partial *)ws;
     if (p.kind == 0) {
-        k_fold_short<OP><<<cap((hi + kFoldThreads - 1) / kFoldThreads), kFoldThreads, 0, st>>>(x, inner, hi, out, index);
+        k_fold_short<OP><<<cap((hi + kFoldThreads - 1) / kFoldThreads), kFoldThreads, 0, st>>>(x, inner, hi, out, index,
+                                                                                                cen);
     } else if (p.kind == 1) {
         const int64_t items = hi * p.q;
         const int grid = cap((items + 7) / 8);
         const bool idx = index != nullptr && (OP == NT2G_FOLD_MAX || OP == NT2G_FOLD_MIN);
         if (p.q == 1) {
-            if (idx) k_fold_inner<OP, true, true><<<grid, kFoldThreads, 0, st>>>(x, inner, hi, p.chunk, 1, p.vec, part, out, index);
-            else k_fold_inner<OP, true, false><<<grid, kFoldThreads, 0, st>>>(x, inner, hi, p.chunk, 1, p.vec, part, out, index);
+            if (idx) k_fold_inner<OP, true, true><<<grid, kFoldThreads, 0, st>>>(x, inner, hi, p.chunk, 1, p.vec, part, out, index, cen);
+            else k_fold_inner<OP, true, false><<<grid, kFoldThreads, 0, st>>>(x, inner, hi, p.chunk, 1, p.vec, part, out, index, cen);
         } else {
-            if (idx) k_fold_inner<OP, false, true><<<grid, kFoldThreads, 0, st>>>(x, inner, hi, p.chunk, p.q, p.vec, part, out, index);
-            else k_fold_inner<OP, false, false><<<grid, kFoldThreads, 0, st>>>(x, inner, hi, p.chunk, p.q, p.vec, part, out, index);
+            if (idx) k_fold_inner<OP, false, true><<<grid, kFoldThreads, 0, st>>>(x, inner, hi, p.chunk, p.q, p.vec, part, out, index, cen);
+            else k_fold_inner<OP, false, false><<<grid, kFoldThreads, 0, st>>>(x, inner, hi, p.chunk, p.q, p.vec, part, out, index, cen);
         }
     } else {
         const int64_t threads = n_out / p.vec;
         dim3 grid(cap((threads + kFoldThreads - 1) / kFoldThreads), (unsigned)p.q);
         if (p.vec == 4) {
-            if (p.q == 1) k_fold_outer<OP, 4, true><<<grid, kFoldThreads, 0, st>>>(x, lo, inner, hi, p.chunk, 1, part, out, index);
-            else k_fold_outer<OP, 4, false><<<grid, kFoldThreads, 0, st>>>(x, lo, inner, hi, p.chunk, p.q, part, out, index);
+            if (p.q == 1) k_fold_outer<OP, 4, true><<<grid, kFoldThreads, 0, st>>>(x, lo, inner, hi, p.chunk, 1, part, out, index, cen);
+            else k_fold_outer<OP, 4, false><<<grid, kFoldThreads, 0, st>>>(x, lo, inner, hi, p.chunk, p.q, part, out, index, cen);
         } else {
-            if (p.q == 1) k_fold_outer<OP, 1, true><<<grid, kFoldThreads, 0, st>>>(x, lo, inner, hi, p.chunk, 1, part, out, index);
-            else k_fold_outer<OP, 1, false><<<grid, kFoldThreads, 0, st>>>(x, lo, inner, hi, p.chunk, p.q, part, out, index);
+            if (p.q == 1) k_fold_outer<OP, 1, true><<<grid, kFoldThreads, 0, st>>>(x, lo, inner, hi, p.chunk, 1, part, out, index, cen);
+            else k_fold_outer<OP, 1, false><<<grid, kFoldThreads, 0, st>>>(x, lo, inner, hi, p.chunk, p.q, part, out, index, cen);
         }
     }
     NT2G_LAUNCH_CHECK("fold launch");
     if (p.q > 1 && p.kind != 0) {
         if (p.q >= 512)
-            k_fold_finish_block<OP><<<cap(n_out), kFoldThreads, 0, st>>>(part, n_out, p.q, inner, out, index);
+            k_fold_finish_block<OP><<<cap(n_out), kFoldThreads, 0, st>>>(part, n_out, p.q, inner, out, index, cen);
         else
             k_fold_finish<OP><<<cap((n_out + kFoldThreads - 1) / kFoldThreads), kFoldThreads, 0, st>>>(
-                part, n_out, p.q, inner, out, index);
+                part, n_out, p.q, inner, out, index, cen);
         NT2G_LAUNCH_CHECK("fold combine launch");
     }
     return NT2G_OK;
@@ -502,7 +613,11 @@ nt2g_status launch_fold(const float *x, int64_t lo, int64_t inner, int64_t hi, i
     case NT2G_FOLD_MEAN: return launch_fold_op<NT2G_FOLD_MEAN>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
     case NT2G_FOLD_ASUM1: return launch_fold_op<NT2G_FOLD_ASUM1>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
     case NT2G_FOLD_ASUM2: return launch_fold_op<NT2G_FOLD_ASUM2>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
-    default: return launch_fold_op<NT2G_FOLD_NORM2>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_NORM2: return launch_fold_op<NT2G_FOLD_NORM2>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_VAR: return launch_fold_op<NT2G_FOLD_VAR>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_STDEV: return launch_fold_op<NT2G_FOLD_STDEV>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_VAR1: return launch_fold_op<NT2G_FOLD_VAR1>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    default: return launch_fold_op<NT2G_FOLD_STDEV1>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
     }
 }
 

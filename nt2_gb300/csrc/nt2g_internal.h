@@ -82,6 +82,7 @@ nt2g_status launch_sigmadelta_frames(const uint8_t *frames, uint8_t *bkg, uint8_
 nt2g_status launch_map(int fn, const float *x, float *y, int64_t n, int precision, cudaStream_t st);
 nt2g_status launch_interp(const DProgram &prog, const DArgs &args, int64_t count, int precision,
                           cudaStream_t st);
+nt2g_status fold_partials_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
 nt2g_status fold_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
 nt2g_status scan_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
 nt2g_status launch_scan(const float *x, int64_t lo, int64_t inner, int64_t hi, int op, int precision, void *ws,

@@ -205,12 +205,15 @@ int main(int argc, char **argv)
             save(dir + "hsum1.bin", nt2::sum(h, 1));  // a host table folded in place (or staged)
             save(dir + "cumsum1.bin", nt2::cumsum(A, 1));
             save(dir + "cummax2.bin", nt2::cummax(A, 2));
+            save(dir + "var1.bin", nt2::var(A, 0, 1));
+            save(dir + "stdev2_w1.bin", nt2::stdev(A, 1, 2));
             std::int64_t imax = 0, imin = 0;
             const float gmax = nt2::globalmax(A, imax), gmin = nt2::globalmin(h, imin);
             std::printf("globalmax %.9g %lld\nglobalmin %.9g %lld\nglobalmean %.9g\nglobalnorm2 %.9g\n"
-                        "globalasum1 %.9g\n",
+                        "globalasum1 %.9g\nglobalvar %.9g\nglobalstdev %.9g\n",
                         (double)gmax, (long long)imax, (double)gmin, (long long)imin, (double)nt2::globalmean(A),
-                        (double)nt2::globalnorm2(A), (double)nt2::globalasum1(A));
+                        (double)nt2::globalnorm2(A), (double)nt2::globalasum1(A), (double)nt2::globalvar(A),
+                        (double)nt2::globalstdev(h));
         } else if (mode == "gen") {
             // generative leaves: NT2's colon (also spelled _), linspace, logspace, alone and in expressions
             using nt2::_;

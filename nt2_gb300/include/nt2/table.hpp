@@ -938,6 +938,25 @@ NT2G_DIM_FOLD(asum2, NT2G_FOLD_ASUM2)
 NT2G_DIM_FOLD(norm2, NT2G_FOLD_NORM2)
 #undef NT2G_DIM_FOLD
 
+// var(t, w, dim), stdev(t, w, dim) (reduction/functions/expr/{var,stdev}.hpp):
+// w = 0 divides by n - 1, w = 1 by n
+template <class Site> table<float, Site> var(const table<float, Site> &t, int w, int dim)
+{
+    return detail::fold_dim(t, dim, w ? NT2G_FOLD_VAR1 : NT2G_FOLD_VAR);
+}
+template <class Site> table<float, Site> stdev(const table<float, Site> &t, int w, int dim)
+{
+    return detail::fold_dim(t, dim, w ? NT2G_FOLD_STDEV1 : NT2G_FOLD_STDEV);
+}
+template <class Site> table<float, Site> var(const table<float, Site> &t, int w = 0)
+{
+    return var(t, w, detail::first_non_singleton(t.extent()));
+}
+template <class Site> table<float, Site> stdev(const table<float, Site> &t, int w = 0)
+{
+    return stdev(t, w, detail::first_non_singleton(t.extent()));
+}
+
 template <class Site> float globalmax(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_MAX); }
 template <class Site> float globalmin(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_MIN); }
 // globalmax(t, i): i receives the 1-based linear position of the first element equal to the maximum
@@ -954,6 +973,14 @@ template <class Site> float globalmean(const table<float, Site> &t) { return det
 template <class Site> float globalasum1(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ASUM1); }
 template <class Site> float globalasum2(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ASUM2); }
 template <class Site> float globalnorm2(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_NORM2); }
+template <class Site> float globalvar(const table<float, Site> &t, int w = 0)
+{
+    return detail::fold_all(t, w ? NT2G_FOLD_VAR1 : NT2G_FOLD_VAR);
+}
+template <class Site> float globalstdev(const table<float, Site> &t, int w = 0)
+{
+    return detail::fold_all(t, w ? NT2G_FOLD_STDEV1 : NT2G_FOLD_STDEV);
+}
 // cumsum(t, dim), cumprod, cummax, cummin: tables of the shape of t
 namespace detail {
 template <class Site> inline table<float, Site> scan_dim(const table<float, Site> &t, int dim, int op)

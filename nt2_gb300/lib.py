@@ -192,7 +192,8 @@ def map_f32(fn, x, y, precision=PREC_FAST, stream=None):
     check(load().nt2g_map_f32(MAP_FN[fn], _ptr(x), _ptr(y), x.numel(), precision, _stream(stream)))
 
 
-FOLD = {"sum": 0, "prod": 1, "max": 2, "min": 3, "mean": 4, "asum1": 5, "asum2": 6, "norm2": 7}
+FOLD = {"sum": 0, "prod": 1, "max": 2, "min": 3, "mean": 4, "asum1": 5, "asum2": 6, "norm2": 7, "var": 8, "stdev": 9,
+        "var1": 10, "stdev1": 11}
 
 
 def fold(x, lo, inner, hi, op, precision=PREC_FAST, index=False, stream=None):

@@ -1063,7 +1063,9 @@ EXPORT double o_exact_sum(const float *x, const float *y, int64_t n, int nthread
  * shared_memory/worker/inner_fold.hpp:47-80, worker/outer_fold.hpp);
  * max = (a0 > a1) ? a0 : a1 (boost/simd/arithmetic/functions/scalar/max.hpp),
  * mean = rec(float(n)) * sum (core/functions/expr/mean.hpp:22-33),
- * asum2 = sum(sqr_abs), norm2 = sqrt(asum2).  index: first position equal to
+ * asum2 = sum(sqr_abs), norm2 = sqrt(asum2), var = f * asum2(a - mean(a)) with
+ * f = rec(n - 1) (ops 8, 9; rec(n) for 10, 11; 1 when n <= 1) and stdev = sqrt(var)
+ * (core/functions/expr/var.hpp, expr/stdev.hpp).  index: first position equal to
  * the result (common/globalmax.hpp:36-48), -1 if none. */
 EXPORT void o_fold_nt2_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int op, float *out,
                            int64_t *index, int nthreads)
@@ -1074,6 +1076,17 @@ EXPORT void o_fold_nt2_f32(const float *x, int64_t lo, int64_t inner, int64_t hi
         const int64_t h = o / lo, l = o - h * lo;
         const float *p = x + l + lo * inner * h;
         float acc = op == 1 ? 1.0f : op == 2 ? -INFINITY : op == 3 ? INFINITY : 0.0f;
+        if (op >= 8) {  /* var / stdev: f * asum2(a - mean(a)) (expr/var.hpp, expr/stdev.hpp) */
+            float sm = 0.0f;
+            for (int64_t k = 0; k < inner; ++k) sm = sm + p[lo * k];
+            const float m = (1.0f / (float)inner) * sm;
+            for (int64_t k = 0; k < inner; ++k) { const float d = p[lo * k] - m; acc = acc + d * d; }
+            const float n = (float)inner;
+            const float f = (n <= 1.0f) ? 1.0f : 1.0f / ((op == 10 || op == 11) ? n : n - 1.0f);
+            acc = f * acc;
+            out[o] = (op == 9 || op == 11) ? sqrtf(acc) : acc;
+            continue;
+        }
         for (int64_t k = 0; k < inner; ++k) {
             const float v = p[lo * k];
             switch (op) {
@@ -1131,6 +1144,21 @@ EXPORT void o_fold_ref(const float *x, int64_t lo, int64_t inner, int64_t hi, in
                 }
                 index[o] = f;
             }
+        } else if (op >= 8) {  /* var / stdev: exact mean (superaccumulator), then deviations in long double */
+            superacc a;
+            memset(&a, 0, sizeof a);
+            int64_t cnt = 0;
+            for (int64_t k = 0; k < inner; ++k) {
+                acc_add(&a, (double)p[lo * k]);
+                if (++cnt == (1 << 24)) { acc_norm(&a); cnt = 0; }
+            }
+            const long double mu = inner > 0 ? (long double)acc_value(a) / (long double)inner : 0.0L;
+            long double ss = 0.0L;
+            for (int64_t k = 0; k < inner; ++k) { const long double d = (long double)p[lo * k] - mu; ss += d * d; }
+            const long double n = (long double)inner;
+            if (inner > 1) ss /= (op == 10 || op == 11) ? n : n - 1.0L;
+            out[o] = (op == 9 || op == 11) ? (double)sqrtl(ss) : (double)ss;
+            if (abs_sum) abs_sum[o] = fabs(out[o]);
         } else {
             superacc a;
             memset(&a, 0, sizeof a);

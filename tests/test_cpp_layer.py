@@ -117,8 +117,8 @@ def test_sigmadelta_through_tables(demos, oracle, tmp_path):
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", ["1", "0"], ids=["nt2", "fast"])
 def test_folds_through_tables(demos, oracle, tmp_path, prec):
-    """sum(A, 1), sum(A, 2), maximum/minimum/mean/norm2 along a dimension and
-    the global forms of an M x N table through the C++ layer."""
+    """sum(A, 1), sum(A, 2), maximum/minimum/mean/norm2/var/stdev along a
+    dimension and the global forms of an M x N table through the C++ layer."""
     m, n = 1000, 777
     rng = np.random.default_rng(21)
     a = (rng.standard_normal(m * n) * np.exp2(rng.integers(-6, 6, m * n))).astype(np.float32)
@@ -127,7 +127,7 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
     glob = {ln.split()[0]: ln.split()[1:] for ln in lines}
     cases = [("sum1", (1, m, n), "sum"), ("sum2", (m, n, 1), "sum"), ("max1", (1, m, n), "max"),
              ("min2", (m, n, 1), "min"), ("mean1", (1, m, n), "mean"), ("norm2_2", (m, n, 1), "norm2"),
-             ("hsum1", (1, m, n), "sum")]
+             ("hsum1", (1, m, n), "sum"), ("var1", (1, m, n), "var"), ("stdev2_w1", (m, n, 1), "stdev1")]
     for name, shape, op in cases:
         got = np.fromfile(tmp_path / f"{name}.bin", np.float32)
         if prec == "1":
@@ -135,7 +135,8 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
             assert _eq(got, ref), name
         else:
             ref, _, _ = oracle.fold_ref(a, *shape, op)
-            assert (np.abs(got - ref) <= np.spacing(np.abs(ref).astype(np.float32))).all(), name
+            k = 2.0 if op in ("var", "stdev1") else 1.0
+            assert (np.abs(got - ref) <= k * np.spacing(np.abs(ref).astype(np.float32))).all(), name
     c1 = np.fromfile(tmp_path / "cumsum1.bin", np.float32)
     c2 = np.fromfile(tmp_path / "cummax2.bin", np.float32)
     assert _eq(c2, oracle.scan_nt2(a, m, n, 1, "max"))
@@ -148,13 +149,14 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
     gmin, imin = oracle.fold_nt2(a, 1, m * n, 1, "min")
     assert np.float32(glob["globalmax"][0]) == gmax[0] and int(glob["globalmax"][1]) == imax[0] + 1
     assert np.float32(glob["globalmin"][0]) == gmin[0] and int(glob["globalmin"][1]) == imin[0] + 1
-    for key, op in (("globalmean", "mean"), ("globalnorm2", "norm2"), ("globalasum1", "asum1")):
+    for key, op in (("globalmean", "mean"), ("globalnorm2", "norm2"), ("globalasum1", "asum1"), ("globalvar", "var"),
+                    ("globalstdev", "stdev")):
         if prec == "1":
             ref, _ = oracle.fold_nt2(a, 1, m * n, 1, op)
             assert np.float32(glob[key][0]) == ref[0], key
         else:
             ref, _, _ = oracle.fold_ref(a, 1, m * n, 1, op)
-            assert abs(float(glob[key][0]) - ref[0]) <= np.spacing(np.float32(abs(ref[0]))), key
+            assert abs(float(glob[key][0]) - ref[0]) <= 2 * np.spacing(np.float32(abs(ref[0]))), key
 
 
 @pytest.mark.gpu

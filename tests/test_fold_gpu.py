@@ -121,3 +121,46 @@ def test_fold_global_matches_reduce_entry(lib, dev):
     a = lib.fold(tx, 1, n, 1, "sum").item()
     b = lib.Reducer(dev)(tx)[1].item()
     assert abs(a - b) <= np.spacing(np.float32(abs(b)))
+
+
+VAR_OPS = ["var", "stdev", "var1", "stdev1"]
+
+
+def _offset_data(shape, seed):
+    lo, inner, hi = shape
+    rng = np.random.default_rng(seed)
+    # an offset far from zero exercises the centring; spreads vary per element
+    return (1000.0 + rng.standard_normal(lo * inner * hi) * np.exp2(rng.integers(-4, 4, lo * inner * hi))).astype(np.float32)
+
+
+@pytest.mark.parametrize("shape", [s for s in SHAPES if s[0] * s[1] * s[2] <= (1 << 20)],
+                         ids=lambda s: f"{s[0]}x{s[1]}x{s[2]}")
+@pytest.mark.parametrize("op", VAR_OPS)
+def test_fold_var_nt2_policy_bit_exact(lib, dev, oracle, shape, op):
+    """var/stdev under NT2's policy: NT2's float mean, the in-order sum of
+    squared deviations, f = rec(n - 1) (or rec(n)), bit-identical."""
+    lo, inner, hi = shape
+    x = _offset_data(shape, 21)
+    got = lib.fold(torch.from_numpy(x).to(dev), lo, inner, hi, op, precision=lib.PREC_NT2)
+    torch.cuda.synchronize()
+    ref, _ = oracle.fold_nt2(x, lo, inner, hi, op)
+    assert _same_bits(got.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{a}x{b}x{c}" for a, b, c in SHAPES])
+@pytest.mark.parametrize("op", VAR_OPS)
+def test_fold_var_fast_policy(lib, dev, oracle, shape, op):
+    """var/stdev under the fast policy: within 2 float ulps of the exact value
+    (FP64 reference about the exact mean), offset data included."""
+    lo, inner, hi = shape
+    x = _offset_data(shape, 22)
+    got = lib.fold(torch.from_numpy(x).to(dev), lo, inner, hi, op).cpu().numpy()
+    torch.cuda.synchronize()
+    ref, _, _ = oracle.fold_ref(x, lo, inner, hi, op)
+    if inner == 0:
+        nt2, _ = oracle.fold_nt2(x, lo, inner, hi, op)
+        assert _same_bits(got, nt2)
+        return
+    err = np.abs(got.astype(np.float64) - ref)
+    tol = 2.0 * _ulp32(ref) + 1e-30
+    assert (err <= tol).all(), (op, shape, float((err / _ulp32(ref)).max()))
