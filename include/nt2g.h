@@ -180,7 +180,13 @@ typedef enum nt2g_fold_op {
     NT2G_FOLD_VAR = 8,     /* asum2(a - mean(a)) / (n - 1)  (NT2's var(a))     */
     NT2G_FOLD_STDEV = 9,   /* sqrt(var)                                       */
     NT2G_FOLD_VAR1 = 10,   /* asum2(a - mean(a)) / n        (NT2's var(a, 1))  */
-    NT2G_FOLD_STDEV1 = 11  /* sqrt(var1)                                      */
+    NT2G_FOLD_STDEV1 = 11, /* sqrt(var1)                                      */
+    NT2G_FOLD_NBTRUE = 12, /* number of nonzero elements (NaN counts)         */
+    NT2G_FOLD_ALL = 13,    /* 1 if every element is nonzero, else 0           */
+    NT2G_FOLD_ANY = 14,    /* 1 if some element is nonzero                    */
+    NT2G_FOLD_NONE = 15,   /* 1 if no element is nonzero                      */
+    NT2G_FOLD_NANSUM = 16, /* sum of the non-NaN elements                     */
+    NT2G_FOLD_NANMEAN = 17 /* nansum / max(number of non-NaN elements, 1)     */
 } nt2g_fold_op;
 
 nt2g_status nt2g_fold_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);

@@ -888,7 +888,7 @@ extern "C" nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, 
 {
     NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_fold_f32: negative extent (%lld, %lld, %lld)",
                    (long long)lo, (long long)inner, (long long)hi);
-    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_STDEV1, "nt2g_fold_f32: op %d", op);
+    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_NANMEAN, "nt2g_fold_f32: op %d", op);
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_fold_f32: precision %d",
                    precision);
     NT2G_CHECK_ARG(index == nullptr || op == NT2G_FOLD_MAX || op == NT2G_FOLD_MIN,
@@ -898,7 +898,8 @@ extern "C" nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, 
     NT2G_CHECK_ARG(out != nullptr, "nt2g_fold_f32: out is NULL");
     NT2G_CHECK_ARG(x != nullptr || inner == 0, "nt2g_fold_f32: x is NULL");
     size_t need = 0;
-    const bool centred = op >= NT2G_FOLD_VAR;  // var/stdev keep each output's centre in the workspace
+    // var/stdev keep each output's centre in the workspace, nanmean its count
+    const bool centred = (op >= NT2G_FOLD_VAR && op <= NT2G_FOLD_STDEV1) || op == NT2G_FOLD_NANMEAN;
     if (centred) fold_workspace_bytes(lo, inner, hi, &need);
     else fold_partials_bytes(lo, inner, hi, &need);
     NT2G_CHECK_ARG((precision == NT2G_PREC_NT2 && !centred) || need == 0 ||

@@ -41,17 +41,27 @@ constexpr int64_t kSmallSeg = 64;        // segments up to this length: one thre
 constexpr int64_t kTargetThreads = 152 * 1024;
 
 // Internal: the mean of each output written with the rounding error of its
-// float value (the centre of a fast-policy variance).
+// float value (the centre of a fast-policy variance); the count of non-NaN
+// elements (the divisor of nanmean).
 constexpr int kFoldMeanC = 100;
+constexpr int kFoldNotNan = 101;
 
 __host__ __device__ constexpr bool fold_is_var(int op)
 {
     return op == NT2G_FOLD_VAR || op == NT2G_FOLD_STDEV || op == NT2G_FOLD_VAR1 || op == NT2G_FOLD_STDEV1;
 }
+// counts of elements: nbtrue and the logical folds all/any/none over x != 0
+__host__ __device__ constexpr bool fold_is_count(int op)
+{
+    return op == NT2G_FOLD_NBTRUE || op == NT2G_FOLD_ALL || op == NT2G_FOLD_ANY || op == NT2G_FOLD_NONE;
+}
+// folds that need a per-output value from a first pass (the centre, the count)
+__host__ __device__ constexpr bool fold_is_two_pass(int op) { return fold_is_var(op) || op == NT2G_FOLD_NANMEAN; }
 __host__ __device__ constexpr bool fold_is_sum(int op)
 {
     return op == NT2G_FOLD_SUM || op == NT2G_FOLD_MEAN || op == NT2G_FOLD_ASUM1 || op == NT2G_FOLD_ASUM2 ||
-           op == NT2G_FOLD_NORM2 || op == kFoldMeanC || fold_is_var(op);
+           op == NT2G_FOLD_NORM2 || op == kFoldMeanC || fold_is_var(op) || fold_is_count(op) ||
+           op == NT2G_FOLD_NANSUM || op == NT2G_FOLD_NANMEAN || op == kFoldNotNan;
 }
 
 // max/min in NT2's order: the fold keeps acc unless x is strictly better, so
@@ -117,6 +127,12 @@ template <int OP> __device__ __forceinline__ void sum_elem(CSum &a, float x)
         const float p = __fmul_rn(x, x);
         csum_add(a, p);
         a.c = __fadd_rn(a.c, __fmaf_rn(x, x, -p));  // exact product error
+    } else if (fold_is_count(OP)) {
+        csum_add(a, x != 0.0f ? 1.0f : 0.0f);  // NaN counts: NT2's is_nez(NaN) is true
+    } else if (OP == kFoldNotNan) {
+        csum_add(a, x == x ? 1.0f : 0.0f);
+    } else if (OP == NT2G_FOLD_NANSUM || OP == NT2G_FOLD_NANMEAN) {
+        csum_add(a, x == x ? x : 0.0f);
     } else {
         csum_add(a, x);
     }
@@ -165,6 +181,15 @@ __device__ __forceinline__ void fold_put(float *out, int64_t o, int64_t n_out, d
         const float m = (float)mu;
         out[o] = m;
         out[n_out + o] = (float)(mu - (double)m);
+    } else if constexpr (fold_is_count(OP)) {
+        const bool all = t == (double)inner, none = t == 0.0;
+        out[o] = OP == NT2G_FOLD_NBTRUE ? (float)t
+               : OP == NT2G_FOLD_ALL    ? (all ? 1.0f : 0.0f)
+               : OP == NT2G_FOLD_ANY    ? (none ? 0.0f : 1.0f)
+                                        : (none ? 1.0f : 0.0f);
+    } else if constexpr (OP == NT2G_FOLD_NANMEAN) {  // nansum / max(count, 1)
+        const double c = (double)cen[o];
+        out[o] = (float)(t / (c > 1.0 ? c : 1.0));
     } else if constexpr (fold_is_var(OP)) {
         const double d = (double)cen[n_out + o];
         const double n = (double)inner;
@@ -422,12 +447,24 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_nt2(const float *__restri
                   : OP == NT2G_FOLD_MAX  ? -__int_as_float(0x7f800000)
                   : OP == NT2G_FOLD_MIN  ? __int_as_float(0x7f800000)
                                          : 0.0f;
-        const float m = fold_is_var(OP) ? cen[o] : 0.0f;
+        const float m = fold_is_two_pass(OP) ? cen[o] : 0.0f;
         for (int64_t k = 0; k < inner; ++k) {
             const float v = p[lo * k];
             if constexpr (fold_is_var(OP)) {  // asum2(center(a)): (x - mean(a))^2 in order
                 const float d = __fsub_rn(v, m);
                 acc = __fadd_rn(acc, __fmul_rn(d, d));
+                continue;
+            }
+            if constexpr (fold_is_count(OP)) {  // nbtrue: the sum of is_nez(x)
+                acc = __fadd_rn(acc, v != 0.0f ? 1.0f : 0.0f);
+                continue;
+            }
+            if constexpr (OP == kFoldNotNan) {
+                acc = __fadd_rn(acc, v == v ? 1.0f : 0.0f);
+                continue;
+            }
+            if constexpr (OP == NT2G_FOLD_NANSUM || OP == NT2G_FOLD_NANMEAN) {  // sum(if_zero_else(is_nan(x), x))
+                acc = __fadd_rn(acc, v == v ? v : 0.0f);
                 continue;
             }
             switch (OP) {
@@ -441,6 +478,15 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_nt2(const float *__restri
         }
         if (OP == NT2G_FOLD_MEAN) acc = __fmul_rn(__fdiv_rn(1.0f, (float)inner), acc);
         if (OP == NT2G_FOLD_NORM2) acc = __fsqrt_rn(acc);
+        if constexpr (fold_is_count(OP)) {
+            const float n = (float)inner;
+            acc = OP == NT2G_FOLD_NBTRUE ? acc
+                : OP == NT2G_FOLD_ALL    ? (acc == n ? 1.0f : 0.0f)
+                : OP == NT2G_FOLD_ANY    ? (acc != 0.0f ? 1.0f : 0.0f)
+                                         : (acc == 0.0f ? 1.0f : 0.0f);
+        }
+        if constexpr (OP == NT2G_FOLD_NANMEAN)  // rec(max(nbtrue(is_not_nan(a)), 1)) * nansum(a)
+            acc = __fmul_rn(__fdiv_rn(1.0f, m > 1.0f ? m : 1.0f), acc);
         if constexpr (fold_is_var(OP)) {  // var = f * asum2, f = n <= 1 ? 1 : rec(n - 1) (rec(n) for w = 1)
             const float n = (float)inner;
             const bool by_n = OP == NT2G_FOLD_VAR1 || OP == NT2G_FOLD_STDEV1;
@@ -534,8 +580,9 @@ static nt2g_status launch_fold_op(const float *x, int64_t lo, int64_t inner, int
                                   const float *cen = nullptr)
 {
     const int64_t n_out = lo * hi;
-    if constexpr (fold_is_var(OP)) {
-        if (!cen) {  // first the centre of every output: NT2's float mean, or (fast) the mean and its rounding error
+    if constexpr (fold_is_two_pass(OP)) {
+        if (!cen) {  // first the centre of every output: NT2's float mean, or (fast) the mean and its rounding
+                     // error; for nanmean the count of non-NaN elements
             const size_t off = fold_centre_offset(lo, inner, hi);
             if (!ws || off + (size_t)n_out * 2 * sizeof(float) > ws_bytes) {
                 set_error("nt2g_fold_f32: workspace of %zu bytes, %zu needed", ws_bytes,
@@ -543,9 +590,13 @@ static nt2g_status launch_fold_op(const float *x, int64_t lo, int64_t inner, int
                 return NT2G_ERR_INVALID;
             }
             float *c = (float *)((char *)ws + off);
-            const nt2g_status s = (precision == NT2G_PREC_NT2 || inner == 0)
-                                      ? launch_fold_op<NT2G_FOLD_MEAN>(x, lo, inner, hi, precision, ws, off, c, nullptr, st)
-                                      : launch_fold_op<kFoldMeanC>(x, lo, inner, hi, precision, ws, off, c, nullptr, st);
+            nt2g_status s;
+            if constexpr (OP == NT2G_FOLD_NANMEAN)
+                s = launch_fold_op<kFoldNotNan>(x, lo, inner, hi, precision, ws, off, c, nullptr, st);
+            else if (precision == NT2G_PREC_NT2 || inner == 0)
+                s = launch_fold_op<NT2G_FOLD_MEAN>(x, lo, inner, hi, precision, ws, off, c, nullptr, st);
+            else
+                s = launch_fold_op<kFoldMeanC>(x, lo, inner, hi, precision, ws, off, c, nullptr, st);
             if (s != NT2G_OK) return s;
             return launch_fold_op<OP>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st, c);
         }
@@ -617,7 +668,13 @@ nt2g_status launch_fold(const float *x, int64_t lo, int64_t inner, int64_t hi, i
     case NT2G_FOLD_VAR: return launch_fold_op<NT2G_FOLD_VAR>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
     case NT2G_FOLD_STDEV: return launch_fold_op<NT2G_FOLD_STDEV>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
     case NT2G_FOLD_VAR1: return launch_fold_op<NT2G_FOLD_VAR1>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
-    default: return launch_fold_op<NT2G_FOLD_STDEV1>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_STDEV1: return launch_fold_op<NT2G_FOLD_STDEV1>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_NBTRUE: return launch_fold_op<NT2G_FOLD_NBTRUE>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_ALL: return launch_fold_op<NT2G_FOLD_ALL>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_ANY: return launch_fold_op<NT2G_FOLD_ANY>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_NONE: return launch_fold_op<NT2G_FOLD_NONE>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    case NT2G_FOLD_NANSUM: return launch_fold_op<NT2G_FOLD_NANSUM>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
+    default: return launch_fold_op<NT2G_FOLD_NANMEAN>(x, lo, inner, hi, precision, ws, ws_bytes, out, index, st);
     }
 }
 

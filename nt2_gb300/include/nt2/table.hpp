@@ -948,6 +948,25 @@ template <class Site> table<float, Site> stdev(const table<float, Site> &t, int 
 {
     return detail::fold_dim(t, dim, w ? NT2G_FOLD_STDEV1 : NT2G_FOLD_STDEV);
 }
+// nbtrue, all, any, none along a dimension (nonzero elements, NaN included);
+// nansum and nanmean (reduction/functions/expr/{nansum,nanmean}.hpp)
+#define NT2G_DIM_FOLD(NAME, OP)                                                                            \
+    template <class Site> table<float, Site> NAME(const table<float, Site> &t, int dim)                     \
+    {                                                                                                       \
+        return detail::fold_dim(t, dim, OP);                                                                \
+    }                                                                                                       \
+    template <class Site> table<float, Site> NAME(const table<float, Site> &t)                              \
+    {                                                                                                       \
+        return detail::fold_dim(t, detail::first_non_singleton(t.extent()), OP);                            \
+    }
+NT2G_DIM_FOLD(nbtrue, NT2G_FOLD_NBTRUE)
+NT2G_DIM_FOLD(all, NT2G_FOLD_ALL)
+NT2G_DIM_FOLD(any, NT2G_FOLD_ANY)
+NT2G_DIM_FOLD(none, NT2G_FOLD_NONE)
+NT2G_DIM_FOLD(nansum, NT2G_FOLD_NANSUM)
+NT2G_DIM_FOLD(nanmean, NT2G_FOLD_NANMEAN)
+#undef NT2G_DIM_FOLD
+
 template <class Site> table<float, Site> var(const table<float, Site> &t, int w = 0)
 {
     return var(t, w, detail::first_non_singleton(t.extent()));
@@ -973,6 +992,12 @@ template <class Site> float globalmean(const table<float, Site> &t) { return det
 template <class Site> float globalasum1(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ASUM1); }
 template <class Site> float globalasum2(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ASUM2); }
 template <class Site> float globalnorm2(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_NORM2); }
+template <class Site> bool globalall(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ALL) != 0.0f; }
+template <class Site> bool globalany(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_ANY) != 0.0f; }
+template <class Site> bool globalnone(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_NONE) != 0.0f; }
+template <class Site> float globalnbtrue(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_NBTRUE); }
+template <class Site> float globalnansum(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_NANSUM); }
+template <class Site> float globalnanmean(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_NANMEAN); }
 template <class Site> float globalvar(const table<float, Site> &t, int w = 0)
 {
     return detail::fold_all(t, w ? NT2G_FOLD_VAR1 : NT2G_FOLD_VAR);

@@ -1076,6 +1076,19 @@ EXPORT void o_fold_nt2_f32(const float *x, int64_t lo, int64_t inner, int64_t hi
         const int64_t h = o / lo, l = o - h * lo;
         const float *p = x + l + lo * inner * h;
         float acc = op == 1 ? 1.0f : op == 2 ? -INFINITY : op == 3 ? INFINITY : 0.0f;
+        if (op >= 12) {  /* nbtrue, all/any/none (sum of is_nez), nansum, nanmean (expr/nansum.hpp, nanmean.hpp) */
+            float cnt = 0.0f, sm = 0.0f, ok = 0.0f;
+            for (int64_t k = 0; k < inner; ++k) {
+                const float v = p[lo * k];
+                cnt = cnt + (v != 0.0f ? 1.0f : 0.0f);
+                ok = ok + (v == v ? 1.0f : 0.0f);
+                sm = sm + (v == v ? v : 0.0f);
+            }
+            const float n = (float)inner;
+            out[o] = op == 12 ? cnt : op == 13 ? (cnt == n ? 1.0f : 0.0f) : op == 14 ? (cnt != 0.0f ? 1.0f : 0.0f)
+                   : op == 15 ? (cnt == 0.0f ? 1.0f : 0.0f) : op == 16 ? sm : (1.0f / (ok > 1.0f ? ok : 1.0f)) * sm;
+            continue;
+        }
         if (op >= 8) {  /* var / stdev: f * asum2(a - mean(a)) (expr/var.hpp, expr/stdev.hpp) */
             float sm = 0.0f;
             for (int64_t k = 0; k < inner; ++k) sm = sm + p[lo * k];
@@ -1144,6 +1157,21 @@ EXPORT void o_fold_ref(const float *x, int64_t lo, int64_t inner, int64_t hi, in
                 }
                 index[o] = f;
             }
+        } else if (op >= 12) {  /* counts exactly; nansum exactly; nanmean = nansum / max(count, 1) */
+            superacc a;
+            memset(&a, 0, sizeof a);
+            int64_t cnt = 0, nz = 0, ok = 0;
+            double as = 0.0;
+            for (int64_t k = 0; k < inner; ++k) {
+                const float v = p[lo * k];
+                nz += v != 0.0f;
+                if (v == v) { ++ok; acc_add(&a, (double)v); as += fabs((double)v); }
+                if (++cnt == (1 << 24)) { acc_norm(&a); cnt = 0; }
+            }
+            const double sm = acc_value(a);
+            out[o] = op == 12 ? (double)nz : op == 13 ? (double)(nz == inner) : op == 14 ? (double)(nz != 0)
+                   : op == 15 ? (double)(nz == 0) : op == 16 ? sm : sm / (double)(ok > 1 ? ok : 1);
+            if (abs_sum) abs_sum[o] = op == 17 ? as / (double)(ok > 1 ? ok : 1) : op == 16 ? as : 0.0;
         } else if (op >= 8) {  /* var / stdev: exact mean (superaccumulator), then deviations in long double */
             superacc a;
             memset(&a, 0, sizeof a);

@@ -164,3 +164,65 @@ def test_fold_var_fast_policy(lib, dev, oracle, shape, op):
     err = np.abs(got.astype(np.float64) - ref)
     tol = 2.0 * _ulp32(ref) + 1e-30
     assert (err <= tol).all(), (op, shape, float((err / _ulp32(ref)).max()))
+
+
+COUNT_OPS = ["nbtrue", "all", "any", "none", "nansum", "nanmean"]
+
+
+def _zeros_nans(shape, seed, zeros=True):
+    lo, inner, hi = shape
+    n = lo * inner * hi
+    rng = np.random.default_rng(seed)
+    x = (rng.standard_normal(n) * np.exp2(rng.integers(-6, 6, n))).astype(np.float32)
+    if n > 10:
+        if zeros:
+            x[rng.integers(0, n, n // 3)] = 0.0
+            x[rng.integers(0, n, n // 50)] = -0.0
+        x[rng.integers(0, n, n // 40)] = np.nan
+    return x
+
+
+@pytest.mark.parametrize("shape", [s for s in SHAPES if s[0] * s[1] * s[2] <= (1 << 20)],
+                         ids=lambda s: f"{s[0]}x{s[1]}x{s[2]}")
+@pytest.mark.parametrize("op", COUNT_OPS)
+def test_fold_counts_nan_nt2_policy_bit_exact(lib, dev, oracle, shape, op):
+    lo, inner, hi = shape
+    x = _zeros_nans(shape, 31)
+    got = lib.fold(torch.from_numpy(x).to(dev), lo, inner, hi, op, precision=lib.PREC_NT2)
+    torch.cuda.synchronize()
+    ref, _ = oracle.fold_nt2(x, lo, inner, hi, op)
+    assert _same_bits(got.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{a}x{b}x{c}" for a, b, c in SHAPES])
+@pytest.mark.parametrize("op", COUNT_OPS)
+def test_fold_counts_nan_fast_policy(lib, dev, oracle, shape, op):
+    """Counts and the logical folds exact; nansum within one ulp of the exact
+    sum of the non-NaN elements, nanmean within two."""
+    lo, inner, hi = shape
+    x = _zeros_nans(shape, 32)
+    got = lib.fold(torch.from_numpy(x).to(dev), lo, inner, hi, op).cpu().numpy()
+    torch.cuda.synchronize()
+    ref, _, _ = oracle.fold_ref(x, lo, inner, hi, op)
+    if op in ("nbtrue", "all", "any", "none"):
+        assert np.array_equal(got, ref.astype(np.float32))
+        return
+    err = np.abs(got.astype(np.float64) - ref)
+    tol = (2.0 if op == "nanmean" else 1.0) * _ulp32(ref) + 1e-37
+    assert (err <= tol).all(), (op, shape, float((err / _ulp32(ref)).max()))
+
+
+def test_fold_all_any_none_edges(lib, dev):
+    """all of nonzero data is 1, any/none of zeros are 0/1, NaN counts as true,
+    and the empty fold gives all = 1, any = 0, none = 1."""
+    z = torch.zeros(3 * 4096, device=dev)
+    o = torch.ones(3 * 4096, device=dev)
+    nan = torch.full((3 * 4096,), float("nan"), device=dev)
+    for prec in (lib.PREC_FAST, lib.PREC_NT2):
+        f = lambda t, op: lib.fold(t, 3, 4096, 1, op, precision=prec).cpu().numpy()  # noqa: E731
+        assert (f(o, "all") == 1).all() and (f(z, "all") == 0).all() and (f(nan, "all") == 1).all()
+        assert (f(z, "any") == 0).all() and (f(o, "any") == 1).all() and (f(z, "none") == 1).all()
+        assert (f(nan, "nbtrue") == 4096).all() and (f(nan, "nansum") == 0).all() and (f(nan, "nanmean") == 0).all()
+        e = torch.zeros(0, device=dev)
+        g = lambda op: lib.fold(e, 1, 0, 5, op, precision=prec).cpu().numpy()  # noqa: E731
+        assert (g("all") == 1).all() and (g("any") == 0).all() and (g("none") == 1).all() and (g("nbtrue") == 0).all()
