@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(kFoldThreads) k_fold_inner(const float *__rest
         int64_t k = k0;
         if (vec) {  // segment starts and chunk bounds are 16-byte aligned: float4 per lane
             const int64_t v1 = k1 >> 2;
-#pragma unroll 4
+#pragma unroll 8
             for (int64_t j = (k0 >> 2) + lane; j < v1; j += 32) {
                 const float4 f = ld_stream((const float4 *)p + j);
                 const int32_t r0 = (int32_t)(4 * j - k0);
