@@ -156,14 +156,14 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_inner(const float *x, int
         float *o = out + seg * inner;
         if constexpr (PHASE == 1 && (OP == NT2G_SCAN_SUM || OP == NT2G_SCAN_PROD)) {
             // the chunk aggregate of a commutative operation needs no scan: each
-            // lane folds its float4s (4 in flight), then the lanes combine in order
+            // lane folds its float4s (8 in flight), then the lanes combine in order
             CSum acc{0.0f, 0.0f};
             double prod = 1.0;
-            for (int64_t t0 = k0; t0 < k1; t0 += 512) {
-                float f[4][4];
-                int nn[4];
+            for (int64_t t0 = k0; t0 < k1; t0 += 1024) {
+                float f[8][4];
+                int nn[8];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
+                for (int u = 0; u < 8; ++u) {
                     const int64_t e = t0 + 128 * u + 4 * lane;
                     nn[u] = (int)(k1 - e < 4 ? (k1 - e > 0 ? k1 - e : 0) : 4);
                     if (vec && nn[u] == 4) {
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_inner(const float *x, int
                     }
                 }
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
+                for (int u = 0; u < 8; ++u)
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
                         if (OP == NT2G_SCAN_SUM) csum_add(acc, f[u][j]);
