@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_outer(const float *x, int
             carry[v] = (PHASE == 3 && q > 1) ? from_rec<OP>(rec[c * lo * hi + seg]) : SE<OP>::id();
         }
         // groups of kGroup rows: all loads of a group are issued before its scan
-        constexpr int kGroup = 8;
+        constexpr int kGroup = (OP == NT2G_SCAN_PROD && VEC == 4) ? 4 : 8;  // FP64 products: fewer registers free
         auto step = [&](int64_t k, const float (&e)[VEC]) {
             float r[VEC];
 #pragma unroll
