@@ -399,6 +399,9 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 21) return asin<P>(a);
     if (FN == 22) return acos<P>(a);
     if (FN == 23) return atan<P>(a);
+    if (FN == 24) return asinh<P>(a);
+    if (FN == 25) return acosh<P>(a);
+    if (FN == 26) return atanh<P>(a);
     float p, q;
     normcdf_pair<P>(a, p, q);
     return q;
@@ -440,6 +443,9 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 21: NT2G_MAP(21); break;
     case 22: NT2G_MAP(22); break;
     case 23: NT2G_MAP(23); break;
+    case 24: NT2G_MAP(24); break;
+    case 25: NT2G_MAP(25); break;
+    case 26: NT2G_MAP(26); break;
     default: NT2G_MAP(7); break;
     }
 #undef NT2G_MAP
@@ -491,6 +497,9 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_ASIN: return asin<P>(a);
     case NT2G_OP_ACOS: return acos<P>(a);
     case NT2G_OP_ATAN: return atan<P>(a);
+    case NT2G_OP_ASINH: return asinh<P>(a);
+    case NT2G_OP_ACOSH: return acosh<P>(a);
+    case NT2G_OP_ATANH: return atanh<P>(a);
     default: return fastnormcdf<P>(a);
     }
 }

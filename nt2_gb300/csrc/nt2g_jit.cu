@@ -210,6 +210,9 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_ASIN: e = "nt2g::asin<P>(" + A + ")"; break;
         case NT2G_OP_ACOS: e = "nt2g::acos<P>(" + A + ")"; break;
         case NT2G_OP_ATAN: e = "nt2g::atan<P>(" + A + ")"; break;
+        case NT2G_OP_ASINH: e = "nt2g::asinh<P>(" + A + ")"; break;
+        case NT2G_OP_ACOSH: e = "nt2g::acosh<P>(" + A + ")"; break;
+        case NT2G_OP_ATANH: e = "nt2g::atanh<P>(" + A + ")"; break;
         default: e = "nt2g::fastnormcdf<P>(" + A + ")"; break;
         }
         s += std::string(u ? "    unsigned v" : "    float v") + std::to_string(k) + "[4]; NT2G_L v" +

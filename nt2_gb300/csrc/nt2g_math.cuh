@@ -883,6 +883,66 @@ template <class P> NT2G_HD float atan2(float a0, float a1)
     return z;
 }
 
+// -------------------------------------------------- inverse hyperbolic --
+// NT2 (hyperbolic/functions/scalar/{asinh,acosh,atanh}.hpp):
+//   asinh  |x| < 1/2: x P4(x^2) (Cephes' asinhf), |x| > 1/sqrt(eps): log|x| + log 2,
+//          else log(|x| + hypot(1, |x|)); the sign of x
+//   acosh  t = x - 1; t <= 1/(2 eps): log1p(t + sqrt(2t + t^2)), else log t + log 2
+//   atanh  sign(x) (1/2) log1p(|x| < 1/2 ? 2|x| + 2|x| |x|/(1 - |x|) : 2|x|/(1 - |x|))
+// hypot as NT2 computes it (arithmetic/functions/scalar/hypot.hpp:27-40): both
+// operands scaled by 2^-e, e the larger one's exponent, sqrt of the sum of
+// squares, scaled back (here for the finite, normal operands asinh gives it).
+template <class P> NT2G_HD float hypot_scaled(float r, float i)
+{
+    const float m = (i > r) ? i : r;
+    int e = (int)((f_bits(m) >> 23) & 0xff) - 127;
+    e = e < -126 ? -126 : (e > 126 ? 126 : e);
+    const float a = nt2_ldexp<P>(r, -e), b = nt2_ldexp<P>(i, -e);
+    return nt2_ldexp<P>(P::sqrt(P::add(P::mul(a, a), P::mul(b, b))), e);
+}
+
+template <class P> NT2G_HD float asinh(float a0)
+{
+    const float x = fabsf(a0);
+    float z;
+    if (x < 0.5f) {
+        const float x2 = P::mul(x, x);
+        z = P::mul(horner<P>(x2, bits_f(0x3ca4d6e6u), bits_f(0xbd2ee581u), bits_f(0x3d9949b1u), bits_f(0xbe2aa9adu),
+                             1.0f),
+                   x);
+    } else if (x > bits_f(0x453504f3u)) {  // 1/sqrt(eps)
+        z = P::add(log<P>(x), bits_f(NT2G_LOG_2));
+    } else {
+        if (P::exact) {
+            z = log<P>(P::add(x, hypot_scaled<P>(1.0f, x)));
+        } else {
+            // Fast: log1p(x + x^2 / (1 + sqrt(1 + x^2))) -- the same value, taken
+            // through log1p so the rounding of x + sqrt(1 + x^2) is not felt
+            const float h = Fast::sqrt(Fast::fma(x, x, 1.0f));  // x <= 2^11.5: no overflow
+            z = log1p<P>(Fast::fma(x, Fast::div(x, Fast::add(1.0f, h)), x));
+        }
+    }
+    return bits_f(f_bits(z) ^ (f_bits(a0) & 0x80000000u));
+}
+
+template <class P> NT2G_HD float acosh(float a0)
+{
+    const float t = P::sub(a0, 1.0f);
+    if (t <= bits_f(0x4a800000u))  // 1/(2 eps)
+        return log1p<P>(P::add(t, P::sqrt(P::add(P::add(t, t), P::mul(t, t)))));
+    return P::add(log<P>(t), bits_f(NT2G_LOG_2));
+}
+
+template <class P> NT2G_HD float atanh(float a0)
+{
+    const float x = fabsf(a0);
+    const float t = P::add(x, x);
+    const float z1 = P::sub(1.0f, x);
+    const float u = (x < 0.5f) ? P::fma(t, P::div(x, z1), t) : P::div(t, z1);
+    const float r = P::mul(0.5f, log1p<P>(u));
+    return bits_f(f_bits(r) ^ (f_bits(a0) & 0x80000000u));
+}
+
 // ----------------------------------------------------------- trigonometry --
 // NT2 (modules/core/trigonometric/include/nt2/trigonometric/functions/):
 //   sin/cos/tan   scalar/impl/trigo/trig_base.hpp:131-176 (regular style,

@@ -2,7 +2,7 @@
 
 ``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
 (exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, sinpi, cospi, pow,
-sinh, cosh, tanh, asin, acos, atan, atan2,
+sinh, cosh, tanh, asinh, acosh, atanh, asin, acos, atan, atan2,
 erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms, min, max, if_else,
 selinc, seldec, if_zero_else_one, adds) build an expression
 tree; ``assign(outs, exprs)`` is ``tie(outs...) = tie(exprs...)``: it lowers
@@ -86,6 +86,7 @@ log2, log10 = _un("LOG2"), _un("LOG10")
 sin, cos, tan, sinpi, cospi = _un("SIN"), _un("COS"), _un("TAN"), _un("SINPI"), _un("COSPI")
 sinh, cosh, tanh = _un("SINH"), _un("COSH"), _un("TANH")
 asin, acos, atan = _un("ASIN"), _un("ACOS"), _un("ATAN")
+asinh, acosh, atanh = _un("ASINH"), _un("ACOSH"), _un("ATANH")
 
 # Functors applied to plain numbers evaluate at once in float32 with NT2's
 # scalar semantics (each step rounded, no fusion), as NT2's scalar overloads

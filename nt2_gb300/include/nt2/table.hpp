@@ -608,6 +608,9 @@ NT2G_UNARY(tanh, NT2G_OP_TANH)
 NT2G_UNARY(asin, NT2G_OP_ASIN)
 NT2G_UNARY(acos, NT2G_OP_ACOS)
 NT2G_UNARY(atan, NT2G_OP_ATAN)
+NT2G_UNARY(asinh, NT2G_OP_ASINH)
+NT2G_UNARY(acosh, NT2G_OP_ACOSH)
+NT2G_UNARY(atanh, NT2G_OP_ATANH)
 #undef NT2G_UNARY
 
 // Functors on plain scalars evaluate at once, in float, with NT2's scalar

@@ -318,6 +318,46 @@ EXPORT float o_tanh(float a0)
     return bf(fb(r) ^ (fb(a0) & 0x80000000u));
 }
 
+/* ------------------------------------------------- inverse hyperbolic ----
+ * HYP/scalar/asinh.hpp (float overload, Cephes' asinhf polynomial), acosh.hpp,
+ * atanh.hpp; hypot per BSIMD/arithmetic/functions/scalar/hypot.hpp:27-40
+ * (both operands scaled by 2^-e, e the larger one's exponent clamped to
+ * [-126, 126]). */
+static const uint32_t ASINH_P[5] = {0x3ca4d6e6, 0xbd2ee581, 0x3d9949b1, 0xbe2aa9ad, 0x3f800000};
+static float nt2_ldexpf(float a, int e);
+
+static float hypot_nt2(float r, float i)
+{
+    float m = (i > r) ? i : r;
+    int e = (int)((fb(m) >> 23) & 0xff) - 127;
+    e = e < -126 ? -126 : (e > 126 ? 126 : e);
+    float a = nt2_ldexpf(r, -e), b = nt2_ldexpf(i, -e);
+    return nt2_ldexpf(sqrtf(a * a + b * b), e);
+}
+
+EXPORT float o_asinh(float a0)
+{
+    float x = fabsf(a0), z;
+    if (x < 0.5f) z = horner(x * x, ASINH_P, 5) * x;
+    else if (x > bf(0x453504f3u)) z = o_log(x) + bf(0x3f317218u);
+    else z = o_log(x + hypot_nt2(1.0f, x));
+    return bf(fb(z) ^ (fb(a0) & 0x80000000u));
+}
+
+EXPORT float o_acosh(float a0)
+{
+    float t = a0 - 1.0f;
+    if (t <= bf(0x4a800000u)) return o_log1p(t + sqrtf((t + t) + t * t));
+    return o_log(t) + bf(0x3f317218u);
+}
+
+EXPORT float o_atanh(float a0)
+{
+    float x = fabsf(a0), t = x + x, z1 = 1.0f - x;
+    float u = (x < 0.5f) ? t * (x / z1) + t : t / z1;
+    return bf(fb(0.5f * o_log1p(u)) ^ (fb(a0) & 0x80000000u));
+}
+
 /* ------------------------------------------------ inverse trigonometry ----
  * TRIG/scalar/impl/invtrig/f_invtrig.hpp:33-128 (Cephes asinf / atanf),
  * atan2 TRIG/scalar/atan2.hpp:30-46 */
@@ -631,7 +671,7 @@ EXPORT float o_tan(float a0)
 /* ------------------------------------------------- elementwise maps ---- */
 enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT, FN_EXP2 = 8, FN_EXP10,
        FN_EXPM1, FN_LOG2, FN_LOG10, FN_SIN, FN_COS, FN_TAN, FN_SINPI, FN_COSPI, FN_SINH, FN_COSH, FN_TANH,
-       FN_ASIN, FN_ACOS, FN_ATAN };
+       FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH };
 
 EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
 {
@@ -660,6 +700,9 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_ASIN: y[i] = o_asin(a); break;
         case FN_ACOS: y[i] = o_acos(a); break;
         case FN_ATAN: y[i] = o_atan(a); break;
+        case FN_ASINH: y[i] = o_asinh(a); break;
+        case FN_ACOSH: y[i] = o_acosh(a); break;
+        case FN_ATANH: y[i] = o_atanh(a); break;
         default: y[i] = sqrtf(a); break;
         }
     }
@@ -711,6 +754,9 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_ASIN: y[i] = asin(a); break;
         case FN_ACOS: y[i] = acos(a); break;
         case FN_ATAN: y[i] = atan(a); break;
+        case FN_ASINH: y[i] = asinh(a); break;
+        case FN_ACOSH: y[i] = acosh(a); break;
+        case FN_ATANH: y[i] = atanh(a); break;
         default: y[i] = sqrt(a); break;
         }
     }

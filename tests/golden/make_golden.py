@@ -41,6 +41,10 @@ SOURCES = [
     ("modules/core/trigonometric/unit/scalar/asin.cpp", 45, 53),
     ("modules/core/trigonometric/unit/scalar/acos.cpp", 46, 54),
     ("modules/core/trigonometric/unit/scalar/atan.cpp", 45, 53),
+    ("modules/core/hyperbolic/unit/scalar/asinh.cpp", 42, 46),
+    ("modules/core/hyperbolic/unit/scalar/asinh.cpp", 49, 49),
+    ("modules/core/hyperbolic/unit/scalar/acosh.cpp", 37, 42),
+    ("modules/core/hyperbolic/unit/scalar/atanh.cpp", 38, 44),
 ]
 
 E = float(np.float32(math.e))

@@ -13,7 +13,8 @@ from helpers import nt2_ulpdist, std_ulp, reduction_ill
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
 FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1", "log2", "log10", "sin", "cos",
-         "tan", "sinpi", "cospi", "sinh", "cosh", "tanh", "asin", "acos", "atan")
+         "tan", "sinpi", "cospi", "sinh", "cosh", "tanh", "asin", "acos", "atan",
+         "asinh", "acosh", "atanh")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
@@ -140,7 +141,8 @@ def test_oracle_hyperbolic_inverse_trig_profile(oracle):
     """NT2's float sinh/cosh/tanh and Cephes-style asin/acos/atan/atan2 as
     restated, against FP64 libm."""
     for fn, lo, hi, tol in (("sinh", -89, 89, 2.5), ("cosh", -89, 89, 2.5), ("tanh", -10, 10, 1.5),
-                            ("asin", -1, 1, 2.5), ("acos", -1, 1, 1.5), ("atan", -1e4, 1e4, 2.5)):
+                            ("asin", -1, 1, 2.5), ("acos", -1, 1, 1.5), ("atan", -1e4, 1e4, 2.5),
+                            ("asinh", -10, 10, 3.5), ("acosh", 1, 1e4, 2.0), ("atanh", -0.9999999, 0.9999999, 2.5)):
         x = np.concatenate([np.linspace(lo, hi, 200001), np.linspace(-1, 1, 50001)]).astype(np.float32)
         a, b = oracle.map_f32(fn, x), oracle.map_f64(fn, x)
         m = np.isfinite(b) & (np.abs(b) > 1.2e-38) & (np.abs(b) < 3e38)
