@@ -402,6 +402,7 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 24) return asinh<P>(a);
     if (FN == 25) return acosh<P>(a);
     if (FN == 26) return atanh<P>(a);
+    if (FN == 27) return cbrt<P>(a);
     float p, q;
     normcdf_pair<P>(a, p, q);
     return q;
@@ -446,6 +447,7 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 24: NT2G_MAP(24); break;
     case 25: NT2G_MAP(25); break;
     case 26: NT2G_MAP(26); break;
+    case 27: NT2G_MAP(27); break;
     default: NT2G_MAP(7); break;
     }
 #undef NT2G_MAP
@@ -500,6 +502,7 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_ASINH: return asinh<P>(a);
     case NT2G_OP_ACOSH: return acosh<P>(a);
     case NT2G_OP_ATANH: return atanh<P>(a);
+    case NT2G_OP_CBRT: return cbrt<P>(a);
     default: return fastnormcdf<P>(a);
     }
 }
@@ -600,10 +603,12 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                     }
                 }
                 break;
-            case NT2G_OP_POW: case NT2G_OP_ATAN2:
+            case NT2G_OP_POW: case NT2G_OP_ATAN2: case NT2G_OP_HYPOT:
                 for (int j = 0; j < kV; ++j) {
                     const float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]);
-                    d[j] = __float_as_uint(in.op == NT2G_OP_POW ? pow<P>(x, y) : atan2<P>(x, y));
+                    d[j] = __float_as_uint(in.op == NT2G_OP_POW     ? pow<P>(x, y)
+                                           : in.op == NT2G_OP_ATAN2 ? atan2<P>(x, y)
+                                                                    : hypot<P>(x, y));
                 }
                 break;
             case NT2G_OP_FMA: case NT2G_OP_FNMS:

@@ -169,6 +169,8 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_FMA: e = "P::fma(" + A + ", " + B + ", " + C + ")"; break;
         case NT2G_OP_POW: e = "nt2g::pow<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_ATAN2: e = "nt2g::atan2<P>(" + A + ", " + B + ")"; break;
+        case NT2G_OP_HYPOT: e = "nt2g::hypot<P>(" + A + ", " + B + ")"; break;
+        case NT2G_OP_CBRT: e = "nt2g::cbrt<P>(" + A + ")"; break;
         case NT2G_OP_FNMS: e = "P::fma(-" + A + ", " + B + ", " + C + ")"; break;
         case NT2G_OP_LT: e = "(" + A + " < " + B + ") ? 1u : 0u"; break;
         case NT2G_OP_GT: e = "(" + A + " > " + B + ") ? 1u : 0u"; break;

@@ -883,6 +883,67 @@ template <class P> NT2G_HD float atan2(float a0, float a1)
     return z;
 }
 
+// ------------------------------------------------------------ cbrt, hypot --
+// cbrt (exponential/functions/scalar/cbrt.hpp, float overload, Cephes' cbrtf):
+// x = m 2^e, a degree-4 polynomial for m^(1/3), 2^(e/3) from e / 3 and the
+// remainder's 2^(1/3) or 2^(2/3), one Newton step, denormals through a 2^23
+// scale; +-0 and +-inf return themselves.
+template <class P> NT2G_HD float cbrt(float a0)
+{
+    float z = fabsf(a0);
+    if (z == f_inf() || z == 0.0f) return a0;
+    float f = 1.0f;
+    if (z < bits_f(0x00800000u)) {
+        z = P::mul(z, 8388608.0f);
+        f = bits_f(0x3ba14518u);  // 2^(-23/3)
+    }
+    const uint32_t u = f_bits(z);
+    int e = (int)((u & 0x7f800000u) >> 23) - 126;
+    float x = bits_f((u & ~0x7f800000u) | 0x3f000000u);
+    x = horner<P>(x, bits_f(0xbe09e49au), bits_f(0x3f0bf0feu), bits_f(0xbf745265u), bits_f(0x3f91eb77u),
+                  bits_f(0x3ece0609u));
+    const bool flag = e >= 0;
+    int e1 = e < 0 ? -e : e;
+    int rem = e1;
+    e1 /= 3;
+    rem -= e1 * 3;
+    e = e < 0 ? -e1 : e1;
+    const float cbrt2 = flag ? bits_f(0x3fa14518u) : bits_f(0x3f4b2ff5u);
+    const float cbrt4 = flag ? bits_f(0x3fcb2ff5u) : bits_f(0x3f214518u);
+    float fact = rem == 1 ? cbrt2 : 1.0f;
+    fact = rem == 2 ? cbrt4 : fact;
+    x = P::mul(P::mul(x, fact), pow2i((float)e));  // fast_ldexp
+    x = P::sub(x, P::mul(P::sub(x, P::div(z, P::mul(x, x))), bits_f(0x3eaaaaabu)));
+    return P::mul(bits_f(f_bits(x) | (f_bits(a0) & 0x80000000u)), f);
+}
+
+// NT2's exponent(): 0 for zero, inf and NaN, else ilogb (denormals included)
+NT2G_HD int nt2_exponent(float x)
+{
+    const uint32_t u = f_bits(x) & 0x7fffffffu;
+    if (u == 0 || u >= 0x7f800000u) return 0;
+    if (u >= 0x00800000u) return (int)(u >> 23) - 127;
+#if defined(__CUDA_ARCH__)
+    return (31 - __clz((int)u)) - 149;
+#else
+    return (31 - __builtin_clz(u)) - 149;
+#endif
+}
+
+// hypot (boost/simd/arithmetic/functions/scalar/hypot.hpp:27-40): inf when one
+// operand is NaN and the other infinite, else both scaled by 2^-e, e the larger
+// one's exponent clamped to [-126, 126], and the root scaled back.
+template <class P> NT2G_HD float hypot(float a0, float a1)
+{
+    if ((is_nan(a0) && fabsf(a1) == f_inf()) || (fabsf(a0) == f_inf() && is_nan(a1))) return f_inf();
+    const float r = fabsf(a0), i = fabsf(a1);
+    int e = nt2_exponent((i > r) ? i : r);
+    e = e < -126 ? -126 : (e > 126 ? 126 : e);
+    const float a = nt2_ldexp<P>(r, -e), b = nt2_ldexp<P>(i, -e);
+    const float ss = P::exact ? P::add(P::mul(a, a), P::mul(b, b)) : Fast::fma(a, a, Fast::mul(b, b));
+    return nt2_ldexp<P>(P::sqrt(ss), e);
+}
+
 // -------------------------------------------------- inverse hyperbolic --
 // NT2 (hyperbolic/functions/scalar/{asinh,acosh,atanh}.hpp):
 //   asinh  |x| < 1/2: x P4(x^2) (Cephes' asinhf), |x| > 1/sqrt(eps): log|x| + log 2,

@@ -2,7 +2,7 @@
 
 ``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
 (exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, sinpi, cospi, pow,
-sinh, cosh, tanh, asinh, acosh, atanh, asin, acos, atan, atan2,
+sinh, cosh, tanh, asinh, acosh, atanh, asin, acos, atan, atan2, cbrt, hypot,
 erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms, min, max, if_else,
 selinc, seldec, if_zero_else_one, adds) build an expression
 tree; ``assign(outs, exprs)`` is ``tie(outs...) = tie(exprs...)``: it lowers
@@ -87,6 +87,7 @@ sin, cos, tan, sinpi, cospi = _un("SIN"), _un("COS"), _un("TAN"), _un("SINPI"), 
 sinh, cosh, tanh = _un("SINH"), _un("COSH"), _un("TANH")
 asin, acos, atan = _un("ASIN"), _un("ACOS"), _un("ATAN")
 asinh, acosh, atanh = _un("ASINH"), _un("ACOSH"), _un("ATANH")
+cbrt = _un("CBRT")
 
 # Functors applied to plain numbers evaluate at once in float32 with NT2's
 # scalar semantics (each step rounded, no fusion), as NT2's scalar overloads
@@ -124,6 +125,11 @@ def pow(a, b):
     if not any(isinstance(x, Node) for x in (a, b)):
         raise TypeError("pow of two numbers: use Python's ** (NT2's scalar pow is not mirrored here)")
     return _bin("POW", a, b)
+
+
+def hypot(a, b):
+    """sqrt(a^2 + b^2) without undue overflow (NT2's scaled form)."""
+    return _bin("HYPOT", a, b)
 
 
 def atan2(a, b):

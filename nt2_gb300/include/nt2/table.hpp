@@ -572,6 +572,7 @@ NT2G_BINARY(max, NT2G_OP_MAX, false)
 NT2G_BINARY(adds, NT2G_OP_ADDS, false)
 NT2G_BINARY(pow, NT2G_OP_POW, false)
 NT2G_BINARY(atan2, NT2G_OP_ATAN2, false)
+NT2G_BINARY(hypot, NT2G_OP_HYPOT, false)
 #undef NT2G_BINARY
 
 #define NT2G_UNARY(NAME, CODE)                                                                                   \
@@ -611,6 +612,7 @@ NT2G_UNARY(atan, NT2G_OP_ATAN)
 NT2G_UNARY(asinh, NT2G_OP_ASINH)
 NT2G_UNARY(acosh, NT2G_OP_ACOSH)
 NT2G_UNARY(atanh, NT2G_OP_ATANH)
+NT2G_UNARY(cbrt, NT2G_OP_CBRT)
 #undef NT2G_UNARY
 
 // Functors on plain scalars evaluate at once, in float, with NT2's scalar

@@ -318,6 +318,61 @@ EXPORT float o_tanh(float a0)
     return bf(fb(r) ^ (fb(a0) & 0x80000000u));
 }
 
+/* --------------------------------------------------------- cbrt, hypot ----
+ * cbrt: EXP/scalar/cbrt.hpp (float overload, Cephes' cbrtf); hypot:
+ * BSIMD/arithmetic/functions/scalar/hypot.hpp:27-40 with NT2's exponent()
+ * (0 for zero, inf, NaN, else ::ilogbf, BSIMD/ieee/functions/scalar/exponent.hpp). */
+static const uint32_t CBRT_P[5] = {0xbe09e49a, 0x3f0bf0fe, 0xbf745265, 0x3f91eb77, 0x3ece0609};
+static float nt2_ldexpf(float a, int e);
+
+EXPORT float o_cbrt(float a0)
+{
+    float z = fabsf(a0);
+    if (z == INFINITY || z == 0.0f) return a0;
+    float f = 1.0f;
+    if (z < bf(0x00800000u)) { z *= 8388608.0f; f = bf(0x3ba14518u); }
+    uint32_t u = fb(z);
+    int e = (int)((u & 0x7f800000u) >> 23) - 126;
+    float x = bf((u & ~0x7f800000u) | 0x3f000000u);
+    x = horner(x, CBRT_P, 5);
+    int flag = e >= 0, e1 = e < 0 ? -e : e, rem = e1;
+    e1 /= 3;
+    rem -= e1 * 3;
+    e = e < 0 ? -e1 : e1;
+    float cbrt2 = flag ? bf(0x3fa14518u) : bf(0x3f4b2ff5u), cbrt4 = flag ? bf(0x3fcb2ff5u) : bf(0x3f214518u);
+    float fact = rem == 1 ? cbrt2 : 1.0f;
+    fact = rem == 2 ? cbrt4 : fact;
+    x = (x * fact) * bf((uint32_t)(e + 127) << 23);
+    x = x - (x - z / (x * x)) * bf(0x3eaaaaabu);
+    return bf(fb(x) | (fb(a0) & 0x80000000u)) * f;
+}
+
+static int nt2_exponent(float x)
+{
+    if (x != x || fabsf(x) == INFINITY || x == 0.0f) return 0;
+    return ilogbf(x);
+}
+
+EXPORT float o_hypot(float a0, float a1)
+{
+    if ((a0 != a0 && fabsf(a1) == INFINITY) || (fabsf(a0) == INFINITY && a1 != a1)) return INFINITY;
+    float r = fabsf(a0), i = fabsf(a1);
+    int e = nt2_exponent((i > r) ? i : r);
+    e = e < -126 ? -126 : (e > 126 ? 126 : e);
+    float a = nt2_ldexpf(r, -e), b = nt2_ldexpf(i, -e);
+    return nt2_ldexpf(sqrtf(a * a + b * b), e);
+}
+
+EXPORT void o_hypot_f32(const float *x, const float *y, float *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = o_hypot(x[i], y[i]);
+}
+
+EXPORT void o_hypot_f64(const float *x, const float *y, double *out, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = hypot((double)x[i], (double)y[i]);
+}
+
 /* ------------------------------------------------- inverse hyperbolic ----
  * HYP/scalar/asinh.hpp (float overload, Cephes' asinhf polynomial), acosh.hpp,
  * atanh.hpp; hypot per BSIMD/arithmetic/functions/scalar/hypot.hpp:27-40
@@ -671,7 +726,7 @@ EXPORT float o_tan(float a0)
 /* ------------------------------------------------- elementwise maps ---- */
 enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT, FN_EXP2 = 8, FN_EXP10,
        FN_EXPM1, FN_LOG2, FN_LOG10, FN_SIN, FN_COS, FN_TAN, FN_SINPI, FN_COSPI, FN_SINH, FN_COSH, FN_TANH,
-       FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH };
+       FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT };
 
 EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
 {
@@ -703,6 +758,7 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_ASINH: y[i] = o_asinh(a); break;
         case FN_ACOSH: y[i] = o_acosh(a); break;
         case FN_ATANH: y[i] = o_atanh(a); break;
+        case FN_CBRT: y[i] = o_cbrt(a); break;
         default: y[i] = sqrtf(a); break;
         }
     }
@@ -757,6 +813,7 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_ASINH: y[i] = asinh(a); break;
         case FN_ACOSH: y[i] = acosh(a); break;
         case FN_ATANH: y[i] = atanh(a); break;
+        case FN_CBRT: y[i] = cbrt(a); break;
         default: y[i] = sqrt(a); break;
         }
     }

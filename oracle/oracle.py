@@ -21,7 +21,7 @@ SRC = os.path.join(HERE, "nt2_oracle.c")
 
 FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, exp2=8, exp10=9, expm1=10, log2=11, log10=12,
           sin=13, cos=14, tan=15, sinpi=16, cospi=17, sinh=18, cosh=19, tanh=20, asin=21, acos=22, atan=23,
-          asinh=24, acosh=25, atanh=26)
+          asinh=24, acosh=25, atanh=26, cbrt=27)
 
 
 def build():
@@ -47,7 +47,7 @@ def lib():
         for f in ("o_exp", "o_log", "o_log1p", "o_erfc", "o_normcdf", "o_fastnormcdf", "o_exp2", "o_exp10", "o_expm1",
                   "o_log2", "o_log10", "o_sin", "o_cos", "o_tan", "o_sinpi", "o_cospi",
                   "o_sinh", "o_cosh", "o_tanh", "o_asin", "o_acos", "o_atan",
-                  "o_asinh", "o_acosh", "o_atanh"):
+                  "o_asinh", "o_acosh", "o_atanh", "o_cbrt"):
             getattr(L, f).restype = ctypes.c_float
             getattr(L, f).argtypes = [ctypes.c_float]
         L.o_map_f32.argtypes = [ctypes.c_int, _P, _P, _I64]
@@ -59,6 +59,10 @@ def lib():
         L.o_atan2.argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_atan2_f32.argtypes = [_P, _P, _P, _I64]
         L.o_atan2_f64.argtypes = [_P, _P, _P, _I64]
+        L.o_hypot.restype = ctypes.c_float
+        L.o_hypot.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.o_hypot_f32.argtypes = [_P, _P, _P, _I64]
+        L.o_hypot_f64.argtypes = [_P, _P, _P, _I64]
         L.o_map_f64.argtypes = [ctypes.c_int, _P, _P, _I64]
         L.o_bs_f32.argtypes = [_P, _P, _P, _P, ctypes.c_float, _P, ctypes.c_float, _P, _P, _I64, ctypes.c_int]
         L.o_bs_demo_f32.argtypes = [_P, _P, _P, _P, ctypes.c_float, _P, ctypes.c_float, _P, _I64, ctypes.c_int]
@@ -144,6 +148,23 @@ def atan2_f64(x, y):
     x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
     out = np.empty(x.size, np.float64)
     lib().o_atan2_f64(_p(x), _p(y), _p(out), x.size)
+    return out
+
+
+def hypot_f32(x, y):
+    """NT2's float hypot restated."""
+    x, y = np.broadcast_arrays(_f32(x), _f32(y))
+    x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+    out = np.empty(x.size, np.float32)
+    lib().o_hypot_f32(_p(x), _p(y), _p(out), x.size)
+    return out
+
+
+def hypot_f64(x, y):
+    x, y = np.broadcast_arrays(_f32(x), _f32(y))
+    x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+    out = np.empty(x.size, np.float64)
+    lib().o_hypot_f64(_p(x), _p(y), _p(out), x.size)
     return out
 
 

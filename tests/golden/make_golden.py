@@ -45,6 +45,7 @@ SOURCES = [
     ("modules/core/hyperbolic/unit/scalar/asinh.cpp", 49, 49),
     ("modules/core/hyperbolic/unit/scalar/acosh.cpp", 37, 42),
     ("modules/core/hyperbolic/unit/scalar/atanh.cpp", 38, 44),
+    ("modules/core/exponential/unit/scalar/cbrt.cpp", 40, 47),
 ]
 
 E = float(np.float32(math.e))
@@ -59,6 +60,7 @@ CONST = {
     "Pio_6": float(np.uint32(0x3f060a92).view(np.float32)), "Pio_3": float(np.uint32(0x3f860a92).view(np.float32)),
     "Twopio_3": float(np.uint32(0x40060a92).view(np.float32)),
     "Threepio_4": float(np.uint32(0x4016cbe4).view(np.float32)),
+    "Sqrt_2": float(np.uint32(0x3fb504f3).view(np.float32)), "Valmax": float(np.finfo(np.float32).max),
 }
 
 
@@ -66,7 +68,7 @@ def _value(expr):
     expr = expr.strip()
     if expr.startswith("-nt2::"):  # a negated constant
         return -_value(expr[1:])
-    m = re.fullmatch(r"nt2::(\w+)<\w+>\(\)", expr)
+    m = re.fullmatch(r"(?:nt2|boost::simd)::(\w+)<\w+>\(\)", expr)
     if m:
         return CONST[m.group(1)]
     m = re.fullmatch(r"[-+]?[0-9.]+[eE][-+]?[0-9]+", expr)
@@ -93,9 +95,10 @@ def _value(expr):
 PAT = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(\w+)\((.*?)\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 # two-argument functors: pow(a, b)
 ARG = r"((?:[^,()]|\([^()]*\))*)"
-PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2)\(" + ARG + r",\s*" + ARG + r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
+PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2|hypot)\(" + ARG + r",\s*" + ARG + r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
-            ("modules/core/trigonometric/unit/scalar/atan2.cpp", 47, 61)]
+            ("modules/core/trigonometric/unit/scalar/atan2.cpp", 47, 61),
+            ("modules/boost/simd/base/unit/arithmetic/scalar/hypot.cpp", 42, 52)]
 
 
 def main(root):

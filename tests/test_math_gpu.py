@@ -25,7 +25,7 @@ DOMAINS = dict(exp=(-87.3, 88.3), log=(1e-30, 1e30), log1p=(-0.999, 1e4), erfc=(
                fastnormcdf=(-9, 9), sqrt=(0, 1e30), exp2=(-126, 126.99), exp10=(-37.8, 38.2),
                expm1=(-20, 88.37), log2=(1e-30, 1e30), log10=(1e-30, 1e30), sinh=(-89, 89), cosh=(-89, 89),
                tanh=(-12, 12), asin=(-1, 1), acos=(-1, 1), atan=(-1e4, 1e4), asinh=(-1e4, 1e4), acosh=(1, 1e4),
-               atanh=(-0.9999999, 0.9999999))
+               atanh=(-0.9999999, 0.9999999), cbrt=(-1e30, 1e30))
 
 
 def _sweep(fn, n=1 << 22, seed=5):
@@ -53,7 +53,7 @@ def _gpu_map(lib, dev, fn, x, prec):
 
 @pytest.mark.parametrize("fn", ["exp", "log", "log1p", "erfc", "normcdf", "fastnormcdf", "sqrt", "exp2", "exp10",
                                 "expm1", "log2", "log10", "sinh", "cosh", "tanh", "asin", "acos", "atan",
-                                "asinh", "acosh", "atanh"])
+                                "asinh", "acosh", "atanh", "cbrt"])
 def test_nt2_policy_bit_exact(lib, dev, oracle, fn):
     x = _inputs(fn)
     got = _gpu_map(lib, dev, fn, x, lib.PREC_NT2)
@@ -66,7 +66,7 @@ def test_nt2_policy_bit_exact(lib, dev, oracle, fn):
                                     ("sqrt", 0.5), ("exp2", 2.0), ("exp10", 2.0), ("expm1", 2.0),
                                     ("log2", 1.5), ("log10", 1.5), ("sinh", 3.0), ("cosh", 3.0), ("tanh", 2.0),
                                     ("asin", 3.0), ("acos", 2.0), ("atan", 3.0), ("asinh", 2.5), ("acosh", 3.0),
-                                    ("atanh", 3.0)])
+                                    ("atanh", 3.0), ("cbrt", 2.0)])
 def test_fast_policy_within_4ulp_of_fp64(lib, dev, oracle, fn, tol):
     """Accuracy over each function's sweep domain; the special values
     (including exp's +inf from NT2's Maxlog = 88.3763 on, as NT2) are
@@ -99,6 +99,6 @@ def test_fast_normcdf_pair_complement(lib, dev, oracle):
 def test_golden_values_on_gpu(lib, dev, prec):
     for rec in [r for r in GOLDEN if r["fn"] in ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10",
                                                   "expm1", "log2", "log10", "sinh", "cosh", "tanh", "asin",
-                                                  "acos", "atan", "asinh", "acosh", "atanh")]:
+                                                  "acos", "atan", "asinh", "acosh", "atanh", "cbrt")]:
         got = _gpu_map(lib, dev, rec["fn"], np.array([rec["x"]], np.float32), prec)[0]
         assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (rec, got)

@@ -14,7 +14,7 @@ from helpers import nt2_ulpdist, std_ulp, reduction_ill
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
 FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1", "log2", "log10", "sin", "cos",
          "tan", "sinpi", "cospi", "sinh", "cosh", "tanh", "asin", "acos", "atan",
-         "asinh", "acosh", "atanh")
+         "asinh", "acosh", "atanh", "cbrt")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
@@ -24,7 +24,7 @@ def test_oracle_matches_nt2_unit_tests(oracle, rec):
     assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (got, rec)
 
 
-@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("pow", "atan2")],
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("pow", "atan2", "hypot")],
                          ids=lambda r: f"{r['fn']}({r['x']},{r['y']})@{r['source'].split('/')[-1]}")
 def test_oracle_binary_matches_nt2_unit_tests(oracle, rec):
     got = getattr(oracle.lib(), "o_" + rec["fn"])(rec["x"], rec["y"])
@@ -142,7 +142,8 @@ def test_oracle_hyperbolic_inverse_trig_profile(oracle):
     restated, against FP64 libm."""
     for fn, lo, hi, tol in (("sinh", -89, 89, 2.5), ("cosh", -89, 89, 2.5), ("tanh", -10, 10, 1.5),
                             ("asin", -1, 1, 2.5), ("acos", -1, 1, 1.5), ("atan", -1e4, 1e4, 2.5),
-                            ("asinh", -10, 10, 3.5), ("acosh", 1, 1e4, 2.0), ("atanh", -0.9999999, 0.9999999, 2.5)):
+                            ("asinh", -10, 10, 3.5), ("acosh", 1, 1e4, 2.0), ("atanh", -0.9999999, 0.9999999, 2.5),
+                            ("cbrt", -1e6, 1e6, 2.0)):
         x = np.concatenate([np.linspace(lo, hi, 200001), np.linspace(-1, 1, 50001)]).astype(np.float32)
         a, b = oracle.map_f32(fn, x), oracle.map_f64(fn, x)
         m = np.isfinite(b) & (np.abs(b) > 1.2e-38) & (np.abs(b) < 3e38)

@@ -1,4 +1,4 @@
-"""pow(a, b) and atan2(a, b) on the GPU through the expression paths.
+"""pow(a, b), atan2(a, b) and hypot(a, b) on the GPU through the expression paths.
 
 NT2 policy: bit-identical to the oracle's restatement of NT2's float pow
 (Cephes powf with NT2's special cases).  Fast policy: the float-float
@@ -100,6 +100,13 @@ def test_pow_golden_values(dev, prec):
     got = _pow(dev, x, y, prec, 1)
     for g, r in zip(got, recs):
         assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+    recs = [r for r in golden if r["fn"] == "hypot"]
+    assert len(recs) == 10
+    hx, hy = torch.from_numpy(np.float32([r["x"] for r in recs])).to(dev), torch.from_numpy(np.float32([r["y"] for r in recs])).to(dev)
+    ho = torch.empty_like(hx)
+    E.assign([ho], [E.hypot(E.Table(hx), E.Table(hy))], precision=prec, force_generic=1)
+    for g, r in zip(ho.cpu().numpy(), recs):
+        assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
     recs = [r for r in golden if r["fn"] == "atan2"]
     assert len(recs) == 14
     got = _atan2(dev, np.float32([r["x"] for r in recs]), np.float32([r["y"] for r in recs]), prec, 1)
@@ -135,3 +142,32 @@ def test_atan2_both_policies(dev, oracle, mode):
     assert e.max() <= 3.0, float(e.max())
     z = (x == 0) | np.isnan(x) | np.isnan(y)
     assert np.all((fast[z].view(np.uint32) == ref[z].view(np.uint32)) | (np.isnan(fast[z]) & np.isnan(ref[z])))
+
+
+@MODES
+def test_hypot_both_policies(dev, oracle, mode):
+    """hypot: NT2 policy bit-identical to the oracle (NT2's scaled form), fast
+    within 1.5 ulp of FP64, no overflow or underflow in the intermediates,
+    inf when one operand is NaN and the other infinite."""
+    rng = np.random.default_rng(54)
+    n = 1 << 18
+    x = (rng.uniform(-2, 2, n) * np.exp2(rng.integers(-149, 127, n))).astype(np.float32)
+    y = (rng.uniform(-2, 2, n) * np.exp2(rng.integers(-149, 127, n))).astype(np.float32)
+    sx, sy = _special_grid()
+    x, y = np.concatenate([x, sx, sy]), np.concatenate([y, sy, sx])
+    tx, ty = torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)
+    for prec in (L.PREC_NT2, L.PREC_FAST):
+        out = torch.empty_like(tx)
+        E.assign([out], [E.hypot(E.Table(tx), E.Table(ty))], precision=prec, force_generic=mode)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        if prec == L.PREC_NT2:
+            ref = oracle.hypot_f32(x, y)
+            assert np.all((got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref)))
+        else:
+            r64 = oracle.hypot_f64(x, y)
+            fin = np.isfinite(r64) & (r64 < 3.4e38)
+            rf = r64[fin].astype(np.float32)
+            ulp = np.where(rf < 1.1754944e-38, 1.4e-45, np.spacing(rf)).astype(np.float64)
+            assert (np.abs(got[fin] - r64[fin]) / ulp).max() <= 1.5
+            assert np.array_equal(np.isnan(got), np.isnan(r64) & ~np.isinf(x) & ~np.isinf(y))
