@@ -88,7 +88,8 @@ typedef enum nt2g_opcode {
     NT2G_OP_ATAN2,         /* atan2(a, b) (float)                            */
     NT2G_OP_ASINH = 94, NT2G_OP_ACOSH, NT2G_OP_ATANH,
     NT2G_OP_CBRT = 97,
-    NT2G_OP_HYPOT = 98     /* hypot(a, b) (float)                            */
+    NT2G_OP_HYPOT = 98,    /* hypot(a, b) (float)                            */
+    NT2G_OP_COT = 100, NT2G_OP_SEC, NT2G_OP_CSC, NT2G_OP_SIND, NT2G_OP_COSD, NT2G_OP_TAND
 } nt2g_opcode;
 
 typedef struct nt2g_op {
@@ -287,7 +288,8 @@ nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8
  * fn: 0 exp, 1 log, 2 log1p, 3 erfc, 4 normcdf, 5 fastnormcdf, 6 sqrt,
  * 7 normcdf(-x) through the shared pair core, 8 exp2, 9 exp10, 10 expm1, 11 log2, 12 log10,
  * 13 sin, 14 cos, 15 tan, 16 sinpi, 17 cospi, 18 sinh, 19 cosh, 20 tanh, 21 asin,
- * 22 acos, 23 atan, 24 asinh, 25 acosh, 26 atanh, 27 cbrt. */
+ * 22 acos, 23 atan, 24 asinh, 25 acosh, 26 atanh, 27 cbrt, 28 cot, 29 sec, 30 csc, 31 sind,
+ * 32 cosd, 33 tand. */
 nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision,
                          void *stream);
 

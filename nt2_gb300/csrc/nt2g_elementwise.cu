@@ -403,6 +403,12 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 25) return acosh<P>(a);
     if (FN == 26) return atanh<P>(a);
     if (FN == 27) return cbrt<P>(a);
+    if (FN == 28) return cot<P>(a);
+    if (FN == 29) return sec<P>(a);
+    if (FN == 30) return csc<P>(a);
+    if (FN == 31) return sind<P>(a);
+    if (FN == 32) return cosd<P>(a);
+    if (FN == 33) return tand<P>(a);
     float p, q;
     normcdf_pair<P>(a, p, q);
     return q;
@@ -448,6 +454,12 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 25: NT2G_MAP(25); break;
     case 26: NT2G_MAP(26); break;
     case 27: NT2G_MAP(27); break;
+    case 28: NT2G_MAP(28); break;
+    case 29: NT2G_MAP(29); break;
+    case 30: NT2G_MAP(30); break;
+    case 31: NT2G_MAP(31); break;
+    case 32: NT2G_MAP(32); break;
+    case 33: NT2G_MAP(33); break;
     default: NT2G_MAP(7); break;
     }
 #undef NT2G_MAP
@@ -503,6 +515,12 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_ACOSH: return acosh<P>(a);
     case NT2G_OP_ATANH: return atanh<P>(a);
     case NT2G_OP_CBRT: return cbrt<P>(a);
+    case NT2G_OP_COT: return cot<P>(a);
+    case NT2G_OP_SEC: return sec<P>(a);
+    case NT2G_OP_CSC: return csc<P>(a);
+    case NT2G_OP_SIND: return sind<P>(a);
+    case NT2G_OP_COSD: return cosd<P>(a);
+    case NT2G_OP_TAND: return tand<P>(a);
     default: return fastnormcdf<P>(a);
     }
 }

@@ -171,6 +171,12 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_ATAN2: e = "nt2g::atan2<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_HYPOT: e = "nt2g::hypot<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_CBRT: e = "nt2g::cbrt<P>(" + A + ")"; break;
+        case NT2G_OP_COT: e = "nt2g::cot<P>(" + A + ")"; break;
+        case NT2G_OP_SEC: e = "nt2g::sec<P>(" + A + ")"; break;
+        case NT2G_OP_CSC: e = "nt2g::csc<P>(" + A + ")"; break;
+        case NT2G_OP_SIND: e = "nt2g::sind<P>(" + A + ")"; break;
+        case NT2G_OP_COSD: e = "nt2g::cosd<P>(" + A + ")"; break;
+        case NT2G_OP_TAND: e = "nt2g::tand<P>(" + A + ")"; break;
         case NT2G_OP_FNMS: e = "P::fma(-" + A + ", " + B + ", " + C + ")"; break;
         case NT2G_OP_LT: e = "(" + A + " < " + B + ") ? 1u : 0u"; break;
         case NT2G_OP_GT: e = "(" + A + " > " + B + ") ? 1u : 0u"; break;

@@ -1171,6 +1171,28 @@ template <class P> NT2G_HD float trig_tan_eval(float z)
     return P::add(P::mul(P::mul(y, zz), z), z);
 }
 
+// Fast: tan(z) as the unevaluated sum hi + lo of z and its odd tail (Fast2Sum,
+// |tail| < |z| on [-pi/4, pi/4]), so that a reciprocal sees the tail unrounded.
+template <class P> NT2G_HD float trig_tan_eval_ff(float z, float &lo)
+{
+    const float zz = P::mul(z, z);
+    const float y = horner<P>(zz, bits_f(0x3c19c53bu), bits_f(0x3b4c779cu), bits_f(0x3cc821b5u),
+                              bits_f(0x3d5ac5c9u), bits_f(0x3e0896ddu), bits_f(0x3eaaaa6fu));
+    const float t = P::mul(P::mul(y, zz), z);
+    const float hi = P::add(t, z);
+    lo = P::add(P::sub(z, hi), t);
+    return hi;
+}
+
+// Fast: 1/(hi + lo) with one Newton step on the residual 1 - r (hi + lo);
+// r itself where it is infinite (hi = 0 or subnormal).
+template <class P> NT2G_HD float rec_ff(float hi, float lo)
+{
+    const float r = P::div(1.0f, hi);
+    const float e = P::fma(-r, lo, P::fma(-r, hi, 1.0f));
+    return (fabsf(r) < bits_f(0x7f800000u)) ? P::fma(r, e, r) : r;
+}
+
 // The shared tail of sin and cos: swap selects the other polynomial, sign is
 // xor-ed into the result.  Fast evaluates both and selects (no divergence).
 template <class P> NT2G_HD float trig_sincos_tail(float xr, bool use_cos, uint32_t sign)
@@ -1205,54 +1227,121 @@ template <class P> NT2G_HD int trig_reduce_pi(float x, float &xr)
     return ((f_bits(xi) & 1u) && fabsf(xi) < 33554432.0f) ? 2 : 0;
 }
 
-template <class P, bool PI> NT2G_HD float cos_any(float a0)
+// degree_tag reduction (trig_reduction.hpp:254-266): k = round(x / 90),
+// xr = (x - 90 k) pi/180; the quadrant is k mod 4 (0 once k leaves int32, as
+// NT2's conversion gives on x86)
+template <class P> NT2G_HD int trig_reduce_deg(float x, float &xr)
+{
+    const float xi = rintf(P::mul(x, bits_f(0x3c360b61u)));  // Oneo_90
+    const float x2 = P::sub(x, P::mul(xi, 90.0f));
+    xr = P::mul(x2, bits_f(0x3c8efa35u));  // Deginrad
+    return (fabsf(xi) < 2147483648.0f) ? ((int)xi & 3) : 0;
+}
+
+// the unit of the argument: radians, multiples of pi, degrees
+enum TrigUnit { kRad = 0, kPi = 1, kDeg = 2 };
+template <class P, int U> NT2G_HD int trig_reduce_unit(float x, float &xr)
+{
+    if (U == kPi) return trig_reduce_pi<P>(x, xr);
+    if (U == kDeg) return trig_reduce_deg<P>(x, xr);
+    return trig_reduce<P>(x, xr);
+}
+
+template <class P, int U> NT2G_HD float cos_any(float a0)
 {
     if (P::exact && trig_invalid(a0)) return f_nan();
     const float x = (P::exact || !trig_invalid(a0)) ? fabsf(a0) : 0.0f;
     float xr;
-    const int n = PI ? trig_reduce_pi<P>(x, xr) : trig_reduce<P>(x, xr);
+    const int n = trig_reduce_unit<P, U>(x, xr);
     const int swap = n & 1;
     const float r = trig_sincos_tail<P>(xr, !swap, (uint32_t)(swap ^ ((n & 2) >> 1)) << 31);
     return (!P::exact && trig_invalid(a0)) ? f_nan() : r;
 }
 
-template <class P, bool PI> NT2G_HD float sin_any(float a0)
+template <class P, int U> NT2G_HD float sin_any(float a0)
 {
     if (P::exact && trig_invalid(a0)) return f_nan();
     const float x = (P::exact || !trig_invalid(a0)) ? fabsf(a0) : 0.0f;
     float xr;
-    const int n = PI ? trig_reduce_pi<P>(x, xr) : trig_reduce<P>(x, xr);
+    const int n = trig_reduce_unit<P, U>(x, xr);
     const uint32_t sign = (f_bits(a0) & 0x80000000u) ^ ((uint32_t)(n & 2) << 30);
     const float r = trig_sincos_tail<P>(xr, (n & 1) != 0, sign);
     return (!P::exact && trig_invalid(a0)) ? f_nan() : r;
 }
 
-template <class P> NT2G_HD float cos(float a0) { return cos_any<P, false>(a0); }
-template <class P> NT2G_HD float sin(float a0) { return sin_any<P, false>(a0); }
-template <class P> NT2G_HD float cospi(float a0) { return cos_any<P, true>(a0); }
-template <class P> NT2G_HD float sinpi(float a0) { return sin_any<P, true>(a0); }
+template <class P> NT2G_HD float cos(float a0) { return cos_any<P, kRad>(a0); }
+template <class P> NT2G_HD float sin(float a0) { return sin_any<P, kRad>(a0); }
+template <class P> NT2G_HD float cospi(float a0) { return cos_any<P, kPi>(a0); }
+template <class P> NT2G_HD float sinpi(float a0) { return sin_any<P, kPi>(a0); }
+template <class P> NT2G_HD float cosd(float a0) { return cos_any<P, kDeg>(a0); }
+template <class P> NT2G_HD float sind(float a0) { return sin_any<P, kDeg>(a0); }
+// sec = rec(cos), csc = rec(sin) (generic/sec.hpp, generic/csc.hpp)
+template <class P> NT2G_HD float sec(float a0) { return P::div(1.0f, cos<P>(a0)); }
+template <class P> NT2G_HD float csc(float a0) { return P::div(1.0f, sin<P>(a0)); }
 
 // tan: NaN for NaN/inf, tan(+-0) = +-0, else tan(xr) or -1/tan(xr) by the
 // quadrant's parity, with a0's sign.
-template <class P> NT2G_HD float tan(float a0)
+// tand is NaN at 90 + 180 k (NT2's tan_invalid for degrees: (x - 90)/180 an integer)
+NT2G_HD bool tand_invalid(float a0)
 {
+    const float q = (a0 - 90.0f) * bits_f(0x3bb60b61u);  // Oneo_180
+    return (q - truncf(q)) == 0.0f;
+}
+
+template <class P, int U> NT2G_HD float tan_any(float a0)
+{
+    const bool bad = trig_invalid(a0) || (U == kDeg && tand_invalid(a0));
     if (P::exact) {
-        if (trig_invalid(a0)) return f_nan();
+        if (bad) return f_nan();
         if (a0 == 0.0f) return a0;
     }
     const float x = (P::exact || !trig_invalid(a0)) ? fabsf(a0) : 0.0f;
     float xr;
-    const int n = trig_reduce<P>(x, xr);
-    float y = trig_tan_eval<P>(xr);
+    const int n = trig_reduce_unit<P, U>(x, xr);
+    float y;
     if (P::exact) {
+        y = trig_tan_eval<P>(xr);
         if (n & 1) y = -P::div(1.0f, y);
     } else {
-        const float ry = -P::div(1.0f, y);
-        y = (n & 1) ? ry : y;
+        float lo;
+        const float hi = trig_tan_eval_ff<P>(xr, lo);
+        y = (n & 1) ? -rec_ff<P>(hi, lo) : hi;
     }
     float r = bits_f(f_bits(y) ^ (f_bits(a0) & 0x80000000u));
     if (!P::exact) {
         r = (a0 == 0.0f) ? a0 : r;
+        r = bad ? f_nan() : r;
+    }
+    return r;
+}
+
+template <class P> NT2G_HD float tan(float a0) { return tan_any<P, kRad>(a0); }
+template <class P> NT2G_HD float tand(float a0) { return tan_any<P, kDeg>(a0); }
+
+// cot (trig_base.hpp:178-188): NaN for NaN/inf, +-inf at +-0, else 1/tan(xr)
+// or -tan(xr) by the quadrant's parity, with a0's sign
+template <class P> NT2G_HD float cot(float a0)
+{
+    const uint32_t bos = f_bits(a0) & 0x80000000u;
+    if (P::exact) {
+        if (trig_invalid(a0)) return f_nan();
+        if (a0 == 0.0f) return bits_f(0x7f800000u | bos);
+    }
+    const float x = (P::exact || !trig_invalid(a0)) ? fabsf(a0) : 0.0f;
+    float xr;
+    const int n = trig_reduce<P>(x, xr);
+    float y;
+    if (P::exact) {
+        y = trig_tan_eval<P>(xr);
+        y = (n & 1) ? -y : P::div(1.0f, y);
+    } else {
+        float lo;
+        const float hi = trig_tan_eval_ff<P>(xr, lo);
+        y = (n & 1) ? -hi : rec_ff<P>(hi, lo);
+    }
+    float r = bits_f(f_bits(y) ^ bos);
+    if (!P::exact) {
+        r = (a0 == 0.0f) ? bits_f(0x7f800000u | bos) : r;
         r = trig_invalid(a0) ? f_nan() : r;
     }
     return r;

@@ -1,7 +1,8 @@
 """A Python mirror of NT2's expression surface over device tables.
 
 ``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
-(exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, sinpi, cospi, pow,
+(exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, cot, sec, csc, sinpi, cospi,
+sind, cosd, tand, pow,
 sinh, cosh, tanh, asinh, acosh, atanh, asin, acos, atan, atan2, cbrt, hypot,
 erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms, min, max, if_else,
 selinc, seldec, if_zero_else_one, adds) build an expression
@@ -88,6 +89,8 @@ sinh, cosh, tanh = _un("SINH"), _un("COSH"), _un("TANH")
 asin, acos, atan = _un("ASIN"), _un("ACOS"), _un("ATAN")
 asinh, acosh, atanh = _un("ASINH"), _un("ACOSH"), _un("ATANH")
 cbrt = _un("CBRT")
+cot, sec, csc = _un("COT"), _un("SEC"), _un("CSC")
+sind, cosd, tand = _un("SIND"), _un("COSD"), _un("TAND")
 
 # Functors applied to plain numbers evaluate at once in float32 with NT2's
 # scalar semantics (each step rounded, no fusion), as NT2's scalar overloads

@@ -613,6 +613,12 @@ NT2G_UNARY(asinh, NT2G_OP_ASINH)
 NT2G_UNARY(acosh, NT2G_OP_ACOSH)
 NT2G_UNARY(atanh, NT2G_OP_ATANH)
 NT2G_UNARY(cbrt, NT2G_OP_CBRT)
+NT2G_UNARY(cot, NT2G_OP_COT)
+NT2G_UNARY(sec, NT2G_OP_SEC)
+NT2G_UNARY(csc, NT2G_OP_CSC)
+NT2G_UNARY(sind, NT2G_OP_SIND)
+NT2G_UNARY(cosd, NT2G_OP_COSD)
+NT2G_UNARY(tand, NT2G_OP_TAND)
 #undef NT2G_UNARY
 
 // Functors on plain scalars evaluate at once, in float, with NT2's scalar

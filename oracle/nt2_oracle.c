@@ -686,11 +686,27 @@ static float tan_eval(float z) { float zz = z * z; return (horner(zz, TAN_P, 6) 
 
 static int invalid(float a) { return !(fabsf(a) < INFINITY); }
 
+/* degree_tag (TRIG/scalar/impl/trigo/trig_reduction.hpp:254-266): k = round(x/90),
+ * xr = (x - 90 k) * Deginrad; the quadrant k mod 4, 0 once k leaves int32 (x86's
+ * conversion gives INT_MIN there) */
+static int trig_reduce_deg(float x, float *xr)
+{
+    float xi = rintf(x * bf(0x3c360b61u));
+    float x2 = x - xi * 90.0f;
+    *xr = x2 * bf(0x3c8efa35u);
+    return (fabsf(xi) < 2147483648.0f) ? ((int)xi & 3) : 0;
+}
+
+static int reduce_unit(float x, float *xr, int unit)
+{
+    return unit == 1 ? trig_reduce_pi(x, xr) : unit == 2 ? trig_reduce_deg(x, xr) : trig_reduce(x, xr);
+}
+
 static float cos_any(float a0, int pi)
 {
     if (invalid(a0)) return NAN;
     float xr;
-    int n = pi ? trig_reduce_pi(fabsf(a0), &xr) : trig_reduce(fabsf(a0), &xr);
+    int n = reduce_unit(fabsf(a0), &xr, pi);
     int swap = n & 1;
     float z = xr * xr;
     float v = swap ? sin_eval(z, xr) : cos_eval(z);
@@ -701,7 +717,7 @@ static float sin_any(float a0, int pi)
 {
     if (invalid(a0)) return NAN;
     float xr;
-    int n = pi ? trig_reduce_pi(fabsf(a0), &xr) : trig_reduce(fabsf(a0), &xr);
+    int n = reduce_unit(fabsf(a0), &xr, pi);
     float z = xr * xr;
     float v = (n & 1) ? cos_eval(z) : sin_eval(z, xr);
     return bf(fb(v) ^ (fb(a0) & 0x80000000u) ^ ((uint32_t)(n & 2) << 30));
@@ -712,21 +728,47 @@ EXPORT float o_sin(float a0) { return sin_any(a0, 0); }
 EXPORT float o_cospi(float a0) { return cos_any(a0, 1); }
 EXPORT float o_sinpi(float a0) { return sin_any(a0, 1); }
 
-EXPORT float o_tan(float a0)
+static float tan_any(float a0, int unit)
 {
     if (invalid(a0)) return NAN;
+    if (unit == 2) {  /* tan_invalid for degrees: (x - 90)/180 an integer */
+        float q = (a0 - 90.0f) * bf(0x3bb60b61u);
+        if (q - truncf(q) == 0.0f) return NAN;
+    }
     if (a0 == 0.0f) return a0;
     float xr;
-    int n = trig_reduce(fabsf(a0), &xr);
+    int n = reduce_unit(fabsf(a0), &xr, unit);
     float y = tan_eval(xr);
     if (n & 1) y = -(1.0f / y);
     return bf(fb(y) ^ (fb(a0) & 0x80000000u));
 }
 
+EXPORT float o_tan(float a0) { return tan_any(a0, 0); }
+EXPORT float o_tand(float a0) { return tan_any(a0, 2); }
+EXPORT float o_sind(float a0) { return sin_any(a0, 2); }
+EXPORT float o_cosd(float a0) { return cos_any(a0, 2); }
+/* sec = rec(cos), csc = rec(sin) (TRIG/generic/sec.hpp, csc.hpp) */
+EXPORT float o_sec(float a0) { return 1.0f / o_cos(a0); }
+EXPORT float o_csc(float a0) { return 1.0f / o_sin(a0); }
+
+/* cot: TRIG/scalar/impl/trigo/trig_base.hpp:178-188 */
+EXPORT float o_cot(float a0)
+{
+    if (invalid(a0)) return NAN;
+    uint32_t bos = fb(a0) & 0x80000000u;
+    if (a0 == 0.0f) return bf(0x7f800000u | bos);
+    float xr;
+    int n = trig_reduce(fabsf(a0), &xr);
+    float y = tan_eval(xr);
+    y = (n & 1) ? -y : 1.0f / y;
+    return bf(fb(y) ^ bos);
+}
+
 /* ------------------------------------------------- elementwise maps ---- */
 enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT, FN_EXP2 = 8, FN_EXP10,
        FN_EXPM1, FN_LOG2, FN_LOG10, FN_SIN, FN_COS, FN_TAN, FN_SINPI, FN_COSPI, FN_SINH, FN_COSH, FN_TANH,
-       FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT };
+       FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT, FN_COT, FN_SEC, FN_CSC, FN_SIND,
+       FN_COSD, FN_TAND };
 
 EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
 {
@@ -759,6 +801,12 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_ACOSH: y[i] = o_acosh(a); break;
         case FN_ATANH: y[i] = o_atanh(a); break;
         case FN_CBRT: y[i] = o_cbrt(a); break;
+        case FN_COT: y[i] = o_cot(a); break;
+        case FN_SEC: y[i] = o_sec(a); break;
+        case FN_CSC: y[i] = o_csc(a); break;
+        case FN_SIND: y[i] = o_sind(a); break;
+        case FN_COSD: y[i] = o_cosd(a); break;
+        case FN_TAND: y[i] = o_tand(a); break;
         default: y[i] = sqrtf(a); break;
         }
     }
@@ -780,6 +828,20 @@ static double cospi_d(double a)
     if (r > 1.0) r = 2.0 - r;          /* [0, 1] */
     if (r > 0.5) return -sin(M_PI * (r - 0.5));
     return sin(M_PI * (0.5 - r));
+}
+
+/* sin and cos of a float angle in degrees: a mod 360 is exact in double */
+static double sind_d(double a)
+{
+    double r = fmod(a, 360.0);
+    if (r == 0.0 || fabs(r) == 180.0) return copysign(0.0, a);
+    return sin(r * (M_PI / 180.0));
+}
+static double cosd_d(double a)
+{
+    double r = fabs(fmod(a, 360.0));
+    if (r == 90.0 || r == 270.0) return 0.0;
+    return cos(r * (M_PI / 180.0));
 }
 
 /* FP64 reference of the same functions on float inputs (glibc double libm). */
@@ -814,6 +876,12 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_ACOSH: y[i] = acosh(a); break;
         case FN_ATANH: y[i] = atanh(a); break;
         case FN_CBRT: y[i] = cbrt(a); break;
+        case FN_COT: y[i] = cos(a) / sin(a); break;
+        case FN_SEC: y[i] = 1.0 / cos(a); break;
+        case FN_CSC: y[i] = 1.0 / sin(a); break;
+        case FN_SIND: y[i] = sind_d(a); break;
+        case FN_COSD: y[i] = cosd_d(a); break;
+        case FN_TAND: y[i] = sind_d(a) / cosd_d(a); break;
         default: y[i] = sqrt(a); break;
         }
     }

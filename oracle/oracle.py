@@ -21,7 +21,7 @@ SRC = os.path.join(HERE, "nt2_oracle.c")
 
 FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, exp2=8, exp10=9, expm1=10, log2=11, log10=12,
           sin=13, cos=14, tan=15, sinpi=16, cospi=17, sinh=18, cosh=19, tanh=20, asin=21, acos=22, atan=23,
-          asinh=24, acosh=25, atanh=26, cbrt=27)
+          asinh=24, acosh=25, atanh=26, cbrt=27, cot=28, sec=29, csc=30, sind=31, cosd=32, tand=33)
 
 
 def build():
@@ -47,7 +47,7 @@ def lib():
         for f in ("o_exp", "o_log", "o_log1p", "o_erfc", "o_normcdf", "o_fastnormcdf", "o_exp2", "o_exp10", "o_expm1",
                   "o_log2", "o_log10", "o_sin", "o_cos", "o_tan", "o_sinpi", "o_cospi",
                   "o_sinh", "o_cosh", "o_tanh", "o_asin", "o_acos", "o_atan",
-                  "o_asinh", "o_acosh", "o_atanh", "o_cbrt"):
+                  "o_asinh", "o_acosh", "o_atanh", "o_cbrt", "o_cot", "o_sec", "o_csc", "o_sind", "o_cosd", "o_tand"):
             getattr(L, f).restype = ctypes.c_float
             getattr(L, f).argtypes = [ctypes.c_float]
         L.o_map_f32.argtypes = [ctypes.c_int, _P, _P, _I64]

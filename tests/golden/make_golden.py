@@ -46,6 +46,12 @@ SOURCES = [
     ("modules/core/hyperbolic/unit/scalar/acosh.cpp", 37, 42),
     ("modules/core/hyperbolic/unit/scalar/atanh.cpp", 38, 44),
     ("modules/core/exponential/unit/scalar/cbrt.cpp", 40, 47),
+    ("modules/core/trigonometric/unit/scalar/cot.cpp", 42, 51),
+    ("modules/core/trigonometric/unit/scalar/sec.cpp", 42, 50),
+    ("modules/core/trigonometric/unit/scalar/csc.cpp", 42, 51),
+    ("modules/core/trigonometric/unit/scalar/sind.cpp", 41, 51),
+    ("modules/core/trigonometric/unit/scalar/cosd.cpp", 42, 52),
+    ("modules/core/trigonometric/unit/scalar/tand.cpp", 40, 50),
 ]
 
 E = float(np.float32(math.e))
@@ -61,6 +67,7 @@ CONST = {
     "Twopio_3": float(np.uint32(0x40060a92).view(np.float32)),
     "Threepio_4": float(np.uint32(0x4016cbe4).view(np.float32)),
     "Sqrt_2": float(np.uint32(0x3fb504f3).view(np.float32)), "Valmax": float(np.finfo(np.float32).max),
+    "_45": 45.0, "_90": 90.0, "_180": 180.0,
 }
 
 

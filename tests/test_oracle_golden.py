@@ -14,7 +14,7 @@ from helpers import nt2_ulpdist, std_ulp, reduction_ill
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
 FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1", "log2", "log10", "sin", "cos",
          "tan", "sinpi", "cospi", "sinh", "cosh", "tanh", "asin", "acos", "atan",
-         "asinh", "acosh", "atanh", "cbrt")
+         "asinh", "acosh", "atanh", "cbrt", "cot", "sec", "csc", "sind", "cosd", "tand")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
@@ -135,6 +135,26 @@ def test_oracle_trig_accuracy_profile(oracle):
     # the exact reduction agrees with NT2's double band on its last floats
     x = np.float32([823549.5, 823549.5625, 823549.625])
     assert std_ulp(oracle.map_f32("sin", x), oracle.map_f64("sin", x)).max() <= 1.0
+
+
+def test_oracle_reciprocal_and_degree_trig_profile(oracle):
+    """cot, sec and csc share the radian reduction (cot ends in NT2's own
+    cotangent branch, sec and csc divide); sind, cosd and tand reduce by
+    round(x/90) and scale the remainder to radians, so they are meaningful
+    while x - 90 round(x/90) stays exact in float."""
+    bands = [np.linspace(-1, 1, 100001), np.linspace(-63, 63, 100001), np.linspace(-201, 201, 100001),
+             np.linspace(-8e5, 8e5, 100001), np.geomspace(8e5, 3e38, 100001)]
+    x = np.concatenate(bands).astype(np.float32)
+    deg = np.concatenate([np.linspace(-720, 720, 200001), np.linspace(-1e6, 1e6, 200001)]).astype(np.float32)
+    for fn, xs, tol in (("cot", x, 3.5), ("sec", x, 3.5), ("csc", x, 3.5),
+                        ("sind", deg, 1.75), ("cosd", deg, 1.75), ("tand", deg, 3.0)):
+        a, b = oracle.map_f32(fn, xs), oracle.map_f64(fn, xs)
+        m = np.isfinite(b) & (np.abs(b) > 1e-30) & (np.abs(b) < 3e38)
+        assert std_ulp(a[m], b[m]).max() <= tol, fn
+    lib = oracle.lib()
+    assert math.isnan(lib.o_tand(90.0)) and math.isnan(lib.o_tand(-270.0)) and lib.o_tand(180.0) == 0.0
+    assert lib.o_cot(-0.0) == -math.inf and lib.o_csc(0.0) == math.inf and lib.o_sec(0.0) == 1.0
+    assert lib.o_cosd(90.0) == 0.0 and lib.o_sind(-90.0) == -1.0
 
 
 def test_oracle_hyperbolic_inverse_trig_profile(oracle):
