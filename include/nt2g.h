@@ -89,7 +89,10 @@ typedef enum nt2g_opcode {
     NT2G_OP_ASINH = 94, NT2G_OP_ACOSH, NT2G_OP_ATANH,
     NT2G_OP_CBRT = 97,
     NT2G_OP_HYPOT = 98,    /* hypot(a, b) (float)                            */
-    NT2G_OP_COT = 100, NT2G_OP_SEC, NT2G_OP_CSC, NT2G_OP_SIND, NT2G_OP_COSD, NT2G_OP_TAND
+    NT2G_OP_COT = 100, NT2G_OP_SEC, NT2G_OP_CSC, NT2G_OP_SIND, NT2G_OP_COSD, NT2G_OP_TAND,
+    NT2G_OP_TANPI = 106, NT2G_OP_COTPI, NT2G_OP_COTD, NT2G_OP_SECPI, NT2G_OP_CSCPI, NT2G_OP_SECD, NT2G_OP_CSCD,
+    NT2G_OP_SINC = 113, NT2G_OP_SINCPI, NT2G_OP_ACOTD, NT2G_OP_ASEC, NT2G_OP_COTH, NT2G_OP_SINHC,
+    NT2G_OP_ACSC = 119, NT2G_OP_ASECH, NT2G_OP_ACOTH, NT2G_OP_ACSCH
 } nt2g_opcode;
 
 typedef struct nt2g_op {
@@ -289,7 +292,8 @@ nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8
  * 7 normcdf(-x) through the shared pair core, 8 exp2, 9 exp10, 10 expm1, 11 log2, 12 log10,
  * 13 sin, 14 cos, 15 tan, 16 sinpi, 17 cospi, 18 sinh, 19 cosh, 20 tanh, 21 asin,
  * 22 acos, 23 atan, 24 asinh, 25 acosh, 26 atanh, 27 cbrt, 28 cot, 29 sec, 30 csc, 31 sind,
- * 32 cosd, 33 tand. */
+ * 32 cosd, 33 tand, 34 tanpi, 35 cotpi, 36 cotd, 37 secpi, 38 cscpi, 39 secd, 40 cscd, 41 sinc,
+ * 42 sincpi, 43 acotd, 44 asec, 45 coth, 46 sinhc, 47 acsc, 48 asech, 49 acoth, 50 acsch. */
 nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision,
                          void *stream);
 

@@ -281,7 +281,11 @@ static int n_operands(int code)
     case NT2G_OP_TAN: case NT2G_OP_SINPI: case NT2G_OP_COSPI: case NT2G_OP_SINH: case NT2G_OP_COSH:
     case NT2G_OP_TANH: case NT2G_OP_ASIN: case NT2G_OP_ACOS: case NT2G_OP_ATAN: case NT2G_OP_ASINH:
     case NT2G_OP_ACOSH: case NT2G_OP_ATANH: case NT2G_OP_CBRT: case NT2G_OP_COT: case NT2G_OP_SEC:
-    case NT2G_OP_CSC: case NT2G_OP_SIND: case NT2G_OP_COSD: case NT2G_OP_TAND: return 1;
+    case NT2G_OP_CSC: case NT2G_OP_SIND: case NT2G_OP_COSD: case NT2G_OP_TAND:
+    case NT2G_OP_TANPI: case NT2G_OP_COTPI: case NT2G_OP_COTD: case NT2G_OP_SECPI: case NT2G_OP_CSCPI:
+    case NT2G_OP_SECD: case NT2G_OP_CSCD: case NT2G_OP_SINC: case NT2G_OP_SINCPI: case NT2G_OP_ACOTD:
+    case NT2G_OP_ASEC: case NT2G_OP_COTH: case NT2G_OP_SINHC:
+    case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH: return 1;
     case NT2G_OP_ADD: case NT2G_OP_SUB: case NT2G_OP_MUL: case NT2G_OP_DIV: case NT2G_OP_MIN: case NT2G_OP_MAX:
     case NT2G_OP_LT: case NT2G_OP_GT: case NT2G_OP_LE: case NT2G_OP_GE: case NT2G_OP_EQ: case NT2G_OP_NE:
     case NT2G_OP_SELINC: case NT2G_OP_SELDEC: case NT2G_OP_ADDS: case NT2G_OP_POW:
@@ -302,6 +306,10 @@ static bool float_only(int code)
     case NT2G_OP_TANH: case NT2G_OP_ASIN: case NT2G_OP_ACOS: case NT2G_OP_ATAN: case NT2G_OP_ATAN2:
     case NT2G_OP_ASINH: case NT2G_OP_ACOSH: case NT2G_OP_ATANH: case NT2G_OP_CBRT: case NT2G_OP_HYPOT:
     case NT2G_OP_COT: case NT2G_OP_SEC: case NT2G_OP_CSC: case NT2G_OP_SIND: case NT2G_OP_COSD: case NT2G_OP_TAND:
+    case NT2G_OP_TANPI: case NT2G_OP_COTPI: case NT2G_OP_COTD: case NT2G_OP_SECPI: case NT2G_OP_CSCPI:
+    case NT2G_OP_SECD: case NT2G_OP_CSCD: case NT2G_OP_SINC: case NT2G_OP_SINCPI: case NT2G_OP_ACOTD:
+    case NT2G_OP_ASEC: case NT2G_OP_COTH: case NT2G_OP_SINHC:
+    case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:
         return true;
     default: return false;
     }
@@ -846,7 +854,7 @@ extern "C" nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_
 {
     NT2G_REQ_N(); NT2G_REQ(x); NT2G_REQ(y); NT2G_REQ_PREC();
     NT2G_REACH(x); NT2G_REACH(y);
-    NT2G_CHECK_ARG(fn >= 0 && fn <= 33, "nt2g_map_f32: unknown function %d", fn);
+    NT2G_CHECK_ARG(fn >= 0 && fn <= 50, "nt2g_map_f32: unknown function %d", fn);
     return launch_map(fn, x, y, n, precision, (cudaStream_t)stream);
 }
 

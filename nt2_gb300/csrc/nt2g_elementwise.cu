@@ -409,6 +409,23 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 31) return sind<P>(a);
     if (FN == 32) return cosd<P>(a);
     if (FN == 33) return tand<P>(a);
+    if (FN == 34) return tanpi<P>(a);
+    if (FN == 35) return cotpi<P>(a);
+    if (FN == 36) return cotd<P>(a);
+    if (FN == 37) return secpi<P>(a);
+    if (FN == 38) return cscpi<P>(a);
+    if (FN == 39) return secd<P>(a);
+    if (FN == 40) return cscd<P>(a);
+    if (FN == 41) return sinc<P>(a);
+    if (FN == 42) return sincpi<P>(a);
+    if (FN == 43) return acotd<P>(a);
+    if (FN == 44) return asec<P>(a);
+    if (FN == 45) return coth<P>(a);
+    if (FN == 46) return sinhc<P>(a);
+    if (FN == 47) return acsc<P>(a);
+    if (FN == 48) return asech<P>(a);
+    if (FN == 49) return acoth<P>(a);
+    if (FN == 50) return acsch<P>(a);
     float p, q;
     normcdf_pair<P>(a, p, q);
     return q;
@@ -460,6 +477,23 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 31: NT2G_MAP(31); break;
     case 32: NT2G_MAP(32); break;
     case 33: NT2G_MAP(33); break;
+    case 34: NT2G_MAP(34); break;
+    case 35: NT2G_MAP(35); break;
+    case 36: NT2G_MAP(36); break;
+    case 37: NT2G_MAP(37); break;
+    case 38: NT2G_MAP(38); break;
+    case 39: NT2G_MAP(39); break;
+    case 40: NT2G_MAP(40); break;
+    case 41: NT2G_MAP(41); break;
+    case 42: NT2G_MAP(42); break;
+    case 43: NT2G_MAP(43); break;
+    case 44: NT2G_MAP(44); break;
+    case 45: NT2G_MAP(45); break;
+    case 46: NT2G_MAP(46); break;
+    case 47: NT2G_MAP(47); break;
+    case 48: NT2G_MAP(48); break;
+    case 49: NT2G_MAP(49); break;
+    case 50: NT2G_MAP(50); break;
     default: NT2G_MAP(7); break;
     }
 #undef NT2G_MAP
@@ -521,6 +555,23 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_SIND: return sind<P>(a);
     case NT2G_OP_COSD: return cosd<P>(a);
     case NT2G_OP_TAND: return tand<P>(a);
+    case NT2G_OP_TANPI: return tanpi<P>(a);
+    case NT2G_OP_COTPI: return cotpi<P>(a);
+    case NT2G_OP_COTD: return cotd<P>(a);
+    case NT2G_OP_SECPI: return secpi<P>(a);
+    case NT2G_OP_CSCPI: return cscpi<P>(a);
+    case NT2G_OP_SECD: return secd<P>(a);
+    case NT2G_OP_CSCD: return cscd<P>(a);
+    case NT2G_OP_SINC: return sinc<P>(a);
+    case NT2G_OP_SINCPI: return sincpi<P>(a);
+    case NT2G_OP_ACOTD: return acotd<P>(a);
+    case NT2G_OP_ASEC: return asec<P>(a);
+    case NT2G_OP_COTH: return coth<P>(a);
+    case NT2G_OP_SINHC: return sinhc<P>(a);
+    case NT2G_OP_ACSC: return acsc<P>(a);
+    case NT2G_OP_ASECH: return asech<P>(a);
+    case NT2G_OP_ACOTH: return acoth<P>(a);
+    case NT2G_OP_ACSCH: return acsch<P>(a);
     default: return fastnormcdf<P>(a);
     }
 }

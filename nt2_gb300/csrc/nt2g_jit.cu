@@ -177,6 +177,23 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_SIND: e = "nt2g::sind<P>(" + A + ")"; break;
         case NT2G_OP_COSD: e = "nt2g::cosd<P>(" + A + ")"; break;
         case NT2G_OP_TAND: e = "nt2g::tand<P>(" + A + ")"; break;
+        case NT2G_OP_TANPI: e = "nt2g::tanpi<P>(" + A + ")"; break;
+        case NT2G_OP_COTPI: e = "nt2g::cotpi<P>(" + A + ")"; break;
+        case NT2G_OP_COTD: e = "nt2g::cotd<P>(" + A + ")"; break;
+        case NT2G_OP_SECPI: e = "nt2g::secpi<P>(" + A + ")"; break;
+        case NT2G_OP_CSCPI: e = "nt2g::cscpi<P>(" + A + ")"; break;
+        case NT2G_OP_SECD: e = "nt2g::secd<P>(" + A + ")"; break;
+        case NT2G_OP_CSCD: e = "nt2g::cscd<P>(" + A + ")"; break;
+        case NT2G_OP_SINC: e = "nt2g::sinc<P>(" + A + ")"; break;
+        case NT2G_OP_SINCPI: e = "nt2g::sincpi<P>(" + A + ")"; break;
+        case NT2G_OP_ACOTD: e = "nt2g::acotd<P>(" + A + ")"; break;
+        case NT2G_OP_ASEC: e = "nt2g::asec<P>(" + A + ")"; break;
+        case NT2G_OP_COTH: e = "nt2g::coth<P>(" + A + ")"; break;
+        case NT2G_OP_SINHC: e = "nt2g::sinhc<P>(" + A + ")"; break;
+        case NT2G_OP_ACSC: e = "nt2g::acsc<P>(" + A + ")"; break;
+        case NT2G_OP_ASECH: e = "nt2g::asech<P>(" + A + ")"; break;
+        case NT2G_OP_ACOTH: e = "nt2g::acoth<P>(" + A + ")"; break;
+        case NT2G_OP_ACSCH: e = "nt2g::acsch<P>(" + A + ")"; break;
         case NT2G_OP_FNMS: e = "P::fma(-" + A + ", " + B + ", " + C + ")"; break;
         case NT2G_OP_LT: e = "(" + A + " < " + B + ") ? 1u : 0u"; break;
         case NT2G_OP_GT: e = "(" + A + " > " + B + ") ? 1u : 0u"; break;

@@ -805,6 +805,39 @@ template <class P> NT2G_HD float tanh(float a0)
     return bits_f(f_bits(r) ^ (f_bits(a0) & 0x80000000u));
 }
 
+// coth (scalar/coth.hpp): below 5/8 the reciprocal of the tanh kernel, else
+// 1 + 2/(e^(2|x|) - 1); the sign of x
+template <class P> NT2G_HD float coth(float a0)
+{
+    const float x = fabsf(a0);
+    float r;
+    if (x < 0.625f) {
+        const float x2 = P::mul(x, x);
+        const float y = horner<P>(x2, bits_f(0xbbbaf0eau), bits_f(0x3ca9134eu), bits_f(0xbd5c1e2du),
+                                  bits_f(0x3e088393u), bits_f(0xbeaaaa99u));
+        r = P::div(1.0f, P::fma(P::mul(y, x2), x, x));
+    } else {
+        r = P::fma(2.0f, P::div(1.0f, P::sub(exp<P>(P::add(x, x)), 1.0f)), 1.0f);
+    }
+    return bits_f(f_bits(r) ^ (f_bits(a0) & 0x80000000u));
+}
+
+// sinhc = sinh(x)/x (scalar/sinhc.hpp): +inf at +-inf; below 1 the degree-3
+// polynomial of details/sinhc_kernel.hpp in x^2; else average(e, -1/e)/x with
+// e = e^|x|, or ((e/2)/|x|) e with e = e^(|x|/2) beyond Maxlog - log 2
+template <class P> NT2G_HD float sinhc(float a0)
+{
+    const float x = fabsf(a0);
+    if (x == f_inf()) return x;
+    if (x < 1.0f)
+        return horner<P>(P::mul(x, x), bits_f(0x39559e2fu), bits_f(0x3c087bbeu), bits_f(0x3e2aaaccu), 1.0f);
+    const bool big = x > P::sub(bits_f(NT2G_MAXLOG), bits_f(NT2G_LOG_2));
+    const float t = exp<P>(P::mul(x, big ? 0.5f : 1.0f));
+    if (big) return P::mul(P::div(P::mul(0.5f, t), x), t);
+    const float avg = P::fma(t, 0.5f, P::mul(-P::div(1.0f, t), 0.5f));  // average(t, -1/t)
+    return P::div(avg, x);
+}
+
 // ------------------------------------------------- inverse trigonometry --
 // NT2 (trigonometric/functions/scalar/impl/invtrig/f_invtrig.hpp:33-128,
 // Cephes' asinf/atanf): asin by a degree-4 polynomial in x^2 (|x| <= 1/2) or
@@ -827,6 +860,17 @@ template <class P> NT2G_HD float asin(float a0)
     }
     float z1 = horner<P>(z, bits_f(0x3d2cb352u), bits_f(0x3cc617e3u), bits_f(0x3d3a3ec7u), bits_f(0x3d9980f6u),
                          bits_f(0x3e2aaae4u));
+    if (!P::exact && big) {
+        // Fast: pi/2 - 2 (s + s z p(z)) with s's rounding error (from the
+        // residual z - s^2) and pi/2's low part carried, and the subtraction
+        // from pi/2 split exactly (Fast2Sum: 2s <= 1 < pi/2): 2.3 -> 0.6 ulp
+        const float slo = (z > 0.0f) ? P::mul(P::fma(-x, x, z), P::div(0.5f, x)) : 0.0f;
+        const float t = P::fma(P::mul(z1, z), x, slo);
+        const float hi = P::fma(-2.0f, x, bits_f(0x3fc90fdbu));
+        const float err = P::fma(-2.0f, x, P::sub(bits_f(0x3fc90fdbu), hi));
+        z1 = P::add(hi, P::add(err, P::fma(-2.0f, t, bits_f(0xb33bbd2eu))));
+        return bits_f(f_bits(z1) ^ sign);
+    }
     z1 = P::fma(z1, P::mul(z, x), x);
     if (big) {
         z1 = P::add(z1, z1);
@@ -844,8 +888,48 @@ template <class P> NT2G_HD float acos(float a0)
 }
 
 // atan(|a0|) (NT2's kernel_atan: the sign is left to the caller)
+// Fast: the reduced argument carried as xr + xl (the reciprocal's and the
+// quotient's rounding errors from FMA residuals, (x-1)/(x+1) from exact sums)
+// and the final y + xr split exactly, so that only the polynomial's own error
+// and one rounding remain
+NT2G_HD void two_sum_f(float a, float b, float &s, float &t)
+{
+    s = a + b;
+    const float bb = s - a;
+    t = (a - (s - bb)) + (b - bb);
+}
+NT2G_HD float atan_kernel_fast(float a0)
+{
+    if (a0 == 0.0f) return 0.0f;
+    if (fabsf(a0) == f_inf()) return bits_f(0x3fc90fdbu);
+    const float x = fabsf(a0);
+    float y = 0.0f, more = 0.0f, xr = x, xl = 0.0f;
+    if (x > bits_f(0x401a827au)) {  // tan(3 pi/8): pi/2 - atan(1/x)
+        y = bits_f(0x3fc90fdbu);
+        more = bits_f(0xb33bbd2eu);
+        xr = Fast::div(-1.0f, x);
+        xl = Fast::mul(Fast::fma(xr, x, 1.0f), xr);
+    } else if (x > bits_f(0x3ed413cdu)) {  // tan(pi/8): pi/4 + atan((x-1)/(x+1))
+        y = bits_f(0x3f490fdbu);
+        more = bits_f(0xb2bbbd2eu);
+        float nh, nl, dh, dl;
+        two_sum_f(x, -1.0f, nh, nl);
+        two_sum_f(x, 1.0f, dh, dl);
+        xr = Fast::div(nh, dh);
+        const float rho = Fast::fma(-xr, dh, nh);
+        xl = Fast::div(Fast::fma(-xr, dl, Fast::add(rho, nl)), dh);
+    }
+    const float z = Fast::mul(xr, xr);
+    const float p = horner<Fast>(z, bits_f(0x3da4f0d1u), bits_f(0xbe0e1b85u), bits_f(0x3e4c925fu), bits_f(0xbeaaaa2au));
+    const float corr = Fast::fma(Fast::mul(p, z), xr, xl);
+    const float sh = Fast::add(y, xr);
+    const float sl = Fast::sub(xr, Fast::sub(sh, y));
+    return Fast::add(sh, Fast::add(sl, Fast::add(corr, more)));
+}
+
 template <class P> NT2G_HD float atan_kernel(float a0)
 {
+    if (!P::exact) return atan_kernel_fast(a0);
     if (a0 == 0.0f) return 0.0f;
     if (fabsf(a0) == f_inf()) return bits_f(0x3fc90fdbu);
     float x = fabsf(a0), y = 0.0f, more = 0.0f;
@@ -1002,6 +1086,38 @@ template <class P> NT2G_HD float atanh(float a0)
     const float u = (x < 0.5f) ? P::fma(t, P::div(x, z1), t) : P::div(t, z1);
     const float r = P::mul(0.5f, log1p<P>(u));
     return bits_f(f_bits(r) ^ (f_bits(a0) & 0x80000000u));
+}
+
+// asech, acoth (hyperbolic/functions/generic/asech.hpp, acoth.hpp): acosh(1/x)
+// and atanh(1/x).  Fast: with u = (1 - x)/x (1 - x exact near 1),
+// asech = log1p(u + sqrt(u (u + 2))), and log 2 - log x below 2^-12;
+// acoth = log1p(2/(|x| - 1))/2 with x's sign.  Both keep NT2's domain: NaN
+// outside (0, 1] (asech; +inf at +0) and inside (-1, 1) (acoth; +-inf at +-1).
+template <class P> NT2G_HD float asech(float a0)
+{
+    if (P::exact) return acosh<P>(P::div(1.0f, a0));
+    const float u = P::div(P::sub(1.0f, a0), a0);
+    const float mid = log1p<P>(P::add(u, P::sqrt(P::mul(u, P::add(u, 2.0f)))));
+    const float tiny = P::sub(bits_f(NT2G_LOG_2), log<P>(a0));
+    const float r = (a0 < 0x1p-12f) ? tiny : mid;
+    return (a0 >= 0.0f && a0 <= 1.0f && !(a0 == 0.0f && (f_bits(a0) >> 31))) ? r : f_nan();
+}
+// acsch (hyperbolic/functions/generic/acsch.hpp): asinh(1/x).  Fast: below
+// 2^-12 in magnitude log 2 - log|x| (1/x would overflow for the smallest x)
+template <class P> NT2G_HD float acsch(float a0)
+{
+    if (P::exact) return asinh<P>(P::div(1.0f, a0));
+    const float ax = fabsf(a0);
+    const float tiny = bits_f(f_bits(P::sub(bits_f(NT2G_LOG_2), log<P>(ax))) ^ (f_bits(a0) & 0x80000000u));
+    const float r = asinh<P>(P::div(1.0f, a0));
+    return (ax < 0x1p-12f) ? tiny : r;
+}
+template <class P> NT2G_HD float acoth(float a0)
+{
+    if (P::exact) return atanh<P>(P::div(1.0f, a0));
+    const float ax = fabsf(a0);
+    const float r = P::mul(0.5f, log1p<P>(P::div(2.0f, P::sub(ax, 1.0f))));
+    return (ax >= 1.0f) ? bits_f(f_bits(r) ^ (f_bits(a0) & 0x80000000u)) : f_nan();
 }
 
 // ----------------------------------------------------------- trigonometry --
@@ -1288,9 +1404,25 @@ NT2G_HD bool tand_invalid(float a0)
     return (q - truncf(q)) == 0.0f;
 }
 
+// tan_invalid / cot_invalid of each unit (trig_reduction.hpp:89-90, 268-269,
+// 308-309): radians none; pi: x - 1/2 integral, or x a nonzero integer;
+// degrees: (x - 90)/180 integral, or x/180 a nonzero integer (in float)
+template <int U> NT2G_HD bool tan_invalid_u(float a0)
+{
+    if (U == kPi) return is_flint(a0 - 0.5f);
+    if (U == kDeg) return tand_invalid(a0);
+    return false;
+}
+template <int U> NT2G_HD bool cot_invalid_u(float a0)
+{
+    if (U == kPi) return a0 != 0.0f && is_flint(a0);
+    if (U == kDeg) return a0 != 0.0f && is_flint(a0 * bits_f(0x3bb60b61u));  // Oneo_180
+    return false;
+}
+
 template <class P, int U> NT2G_HD float tan_any(float a0)
 {
-    const bool bad = trig_invalid(a0) || (U == kDeg && tand_invalid(a0));
+    const bool bad = trig_invalid(a0) || tan_invalid_u<U>(a0);
     if (P::exact) {
         if (bad) return f_nan();
         if (a0 == 0.0f) return a0;
@@ -1317,19 +1449,21 @@ template <class P, int U> NT2G_HD float tan_any(float a0)
 
 template <class P> NT2G_HD float tan(float a0) { return tan_any<P, kRad>(a0); }
 template <class P> NT2G_HD float tand(float a0) { return tan_any<P, kDeg>(a0); }
+template <class P> NT2G_HD float tanpi(float a0) { return tan_any<P, kPi>(a0); }
 
-// cot (trig_base.hpp:178-188): NaN for NaN/inf, +-inf at +-0, else 1/tan(xr)
-// or -tan(xr) by the quadrant's parity, with a0's sign
-template <class P> NT2G_HD float cot(float a0)
+// cot (trig_base.hpp:178-188): NaN for NaN/inf and the unit's poles, +-inf at
+// +-0, else 1/tan(xr) or -tan(xr) by the quadrant's parity, with a0's sign
+template <class P, int U> NT2G_HD float cot_any(float a0)
 {
     const uint32_t bos = f_bits(a0) & 0x80000000u;
+    const bool bad = trig_invalid(a0) || cot_invalid_u<U>(a0);
     if (P::exact) {
-        if (trig_invalid(a0)) return f_nan();
+        if (bad) return f_nan();
         if (a0 == 0.0f) return bits_f(0x7f800000u | bos);
     }
     const float x = (P::exact || !trig_invalid(a0)) ? fabsf(a0) : 0.0f;
     float xr;
-    const int n = trig_reduce<P>(x, xr);
+    const int n = trig_reduce_unit<P, U>(x, xr);
     float y;
     if (P::exact) {
         y = trig_tan_eval<P>(xr);
@@ -1342,9 +1476,115 @@ template <class P> NT2G_HD float cot(float a0)
     float r = bits_f(f_bits(y) ^ bos);
     if (!P::exact) {
         r = (a0 == 0.0f) ? bits_f(0x7f800000u | bos) : r;
-        r = trig_invalid(a0) ? f_nan() : r;
+        r = bad ? f_nan() : r;
     }
     return r;
+}
+
+template <class P> NT2G_HD float cot(float a0) { return cot_any<P, kRad>(a0); }
+template <class P> NT2G_HD float cotpi(float a0) { return cot_any<P, kPi>(a0); }
+template <class P> NT2G_HD float cotd(float a0) { return cot_any<P, kDeg>(a0); }
+
+// secpi (generic/secpi.hpp): NaN where 2x is odd, else 1/cospi(x); cscpi
+// (generic/cscpi.hpp): NaN at nonzero integers, else 1/sinpi(x); secd
+// (generic/secd.hpp): 1/cosd(x), NaN where cosd(x) is zero; cscd
+// (generic/cscd.hpp): cscpi(x/180).  NT2's is_odd(y) is is_flint((y - 1)/2).
+template <class P> NT2G_HD float secpi(float a0)
+{
+    const float r = P::div(1.0f, cospi<P>(a0));
+    return is_odd_f(P::mul(a0, 2.0f)) ? f_nan() : r;
+}
+template <class P> NT2G_HD float cscpi(float a0)
+{
+    const float r = P::div(1.0f, sinpi<P>(a0));
+    return (is_flint(a0) && a0 != 0.0f) ? f_nan() : r;
+}
+template <class P> NT2G_HD float secd(float a0)
+{
+    const float c = cosd<P>(a0);
+    return P::div(1.0f, (c == 0.0f) ? f_nan() : c);
+}
+template <class P> NT2G_HD float cscd(float a0)
+{
+    const float y = P::mul(bits_f(0x3bb60b61u), a0);
+    if (P::exact) return cscpi<P>(y);
+    // Fast: NT2's poles (x/180 a nonzero integer in float), the value from
+    // sind, whose reduction is exact, instead of sinpi of the rounded x/180
+    const float r = P::div(1.0f, sind<P>(a0));
+    return (is_flint(y) && y != 0.0f) ? f_nan() : r;
+}
+
+// sinc, sincpi (scalar/sinc.hpp, scalar/sincpi.hpp): 0 at +-inf, 1 below Eps
+// in magnitude, else sin(x)/x and (sinpi(x)/pi)/x
+template <class P> NT2G_HD float sinc(float a0)
+{
+    const float ax = fabsf(a0);
+    const float r = P::div(sin<P>(a0), a0);
+    return (ax == f_inf()) ? 0.0f : (ax < bits_f(0x34000000u)) ? 1.0f : r;
+}
+template <class P> NT2G_HD float sincpi(float a0)
+{
+    const float ax = fabsf(a0);
+    const float r = P::div(P::mul(bits_f(0x3ea2f983u), sinpi<P>(a0)), a0);  // Invpi
+    return (ax == f_inf()) ? 0.0f : (ax < bits_f(0x34000000u)) ? 1.0f : r;
+}
+
+// acsc (generic/acsc.hpp): asin(1/x).  Fast: asin(1/|x|) from |x| = 2 on,
+// below it atan(1/sqrt(x^2 - 1)) (x^2 - 1 by one FMA), which stays accurate
+// at 1 where 1/x's rounding would be magnified by asin
+template <class P> NT2G_HD float acsc(float a0)
+{
+    if (P::exact) return asin<P>(P::div(1.0f, a0));
+    const float ax = fabsf(a0);
+    const float near = atan<P>(P::div(1.0f, P::sqrt(P::fma(ax, ax, -1.0f))));
+    const float r = (ax >= 2.0f) ? asin<P>(P::div(1.0f, ax)) : near;
+    return (ax < 1.0f) ? f_nan() : bits_f(f_bits(r) ^ (f_bits(a0) & 0x80000000u));
+}
+
+// indeg (generic/indeg.hpp): x Radindeg - x Radindegr, the constant in two parts
+template <class P> NT2G_HD float indeg(float a)
+{
+    return P::sub(P::mul(a, bits_f(0x42652ee1u)), P::mul(a, bits_f(0xb53387c1u)));
+}
+
+// acotd (generic/acotd.hpp): 90 - atand|x| (90 at 0, 0 at +-inf) with x's sign
+template <class P> NT2G_HD float acotd(float a0)
+{
+    const float ax = fabsf(a0);
+    float z;
+    if (P::exact) {
+        const float t = indeg<P>(atan<P>(ax));
+        z = P::sub(90.0f, (a0 != 0.0f) ? t : 0.0f);
+    } else {
+        // Fast: atand(1/|x|) from 1 on, where 90 - atand|x| would cancel
+        z = (ax >= 1.0f) ? indeg<P>(atan<P>(P::div(1.0f, ax))) : P::sub(90.0f, indeg<P>(atan<P>(ax)));
+    }
+    z = (ax == f_inf()) ? 0.0f : z;
+    return bits_f(f_bits(z) | (f_bits(a0) & 0x80000000u));
+}
+
+// asec (float: scalar/asec.hpp, single_ overload): NaN inside (-1, 1); a
+// series in sqrt(2(|x| - 1)) just above 1 (pi minus it for x < 0); 0 at 1;
+// else pi/2 - acsc(x) with acsc(x) = asin(1/x)
+template <class P> NT2G_HD float asec(float a0)
+{
+    const float ax = fabsf(a0);
+    if (ax < 1.0f) return f_nan();
+    if (!P::exact) {
+        // Fast: atan(sqrt(x^2 - 1)) with x^2 - 1 rounded once (an FMA), pi
+        // minus it for x < 0 with pi's low part carried; no cancellation at 1
+        const float t = atan<P>(P::sqrt(P::fma(ax, ax, -1.0f)));
+        return (a0 < 0.0f) ? P::add(P::sub(bits_f(0x40490fdbu), t), bits_f(0xb3bbbd2eu)) : t;
+    }
+    const float ax1 = P::sub(ax, 1.0f);
+    if (ax1 < 0.001f) {
+        const float c1 = 5 / 12.0f, c2 = 43 / 160.0f, c3 = 177 / 896.0f, c4 = 2867 / 18432.0f;
+        const float q = P::add(c1, P::mul(ax1, P::sub(c2, P::mul(ax1, P::add(c3, P::mul(ax1, c4))))));
+        const float t = P::mul(P::sqrt(P::mul(2.0f, ax1)), P::sub(1.0f, P::mul(ax1, q)));
+        return (a0 < 0.0f) ? P::sub(bits_f(0x40490fdbu), t) : t;  // Pi
+    }
+    if (a0 == 1.0f) return 0.0f;
+    return P::sub(bits_f(0x3fc90fdbu), asin<P>(P::div(1.0f, a0)));  // Pio_2
 }
 
 }  // namespace nt2g

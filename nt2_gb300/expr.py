@@ -2,8 +2,10 @@
 
 ``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
 (exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, cot, sec, csc, sinpi, cospi,
-sind, cosd, tand, pow,
-sinh, cosh, tanh, asinh, acosh, atanh, asin, acos, atan, atan2, cbrt, hypot,
+tanpi, cotpi, secpi, cscpi, sind, cosd, tand, cotd, secd, cscd, sinc, sincpi, pow,
+sinh, cosh, tanh, coth, sech, csch, sinhc, asinh, acosh, atanh, asech, acsch, acoth,
+asin, acos, atan, acot, asec, acsc, asind, acosd, atand, acotd, asecd, acscd,
+asinpi, acospi, atanpi, atan2, atan2d, indeg, inrad, cbrt, hypot,
 erfc, normcdf, fastnormcdf, sqrt, sqr, abs, rec, fma, fnms, min, max, if_else,
 selinc, seldec, if_zero_else_one, adds) build an expression
 tree; ``assign(outs, exprs)`` is ``tie(outs...) = tie(exprs...)``: it lowers
@@ -91,6 +93,52 @@ asinh, acosh, atanh = _un("ASINH"), _un("ACOSH"), _un("ATANH")
 cbrt = _un("CBRT")
 cot, sec, csc = _un("COT"), _un("SEC"), _un("CSC")
 sind, cosd, tand = _un("SIND"), _un("COSD"), _un("TAND")
+tanpi = _un("TANPI")
+cotpi = _un("COTPI")
+cotd = _un("COTD")
+secpi = _un("SECPI")
+cscpi = _un("CSCPI")
+secd = _un("SECD")
+cscd = _un("CSCD")
+sinc = _un("SINC")
+sincpi = _un("SINCPI")
+acotd = _un("ACOTD")
+asec = _un("ASEC")
+coth = _un("COTH")
+sinhc = _un("SINHC")
+acsc = _un("ACSC")
+asech = _un("ASECH")
+acoth = _un("ACOTH")
+acsch = _un("ACSCH")
+
+
+# NT2's generic compositions, built as the same programs of the functors above,
+# operation for operation (hyperbolic/functions/generic/{sech,csch}.hpp;
+# trigonometric/functions/generic/{acot,indeg,inrad,asind,acosd,atand,asecd,
+# acscd,atan2d,asinpi,acospi,atanpi}.hpp)
+def _bits_f32(u):
+    import struct
+    return struct.unpack("<f", struct.pack("<I", u))[0]
+
+
+_RADINDEG, _RADINDEGR = _bits_f32(0x42652ee1), _bits_f32(0xb53387c1)
+_DEGINRAD, _INVPI = _bits_f32(0x3c8efa35), _bits_f32(0x3ea2f983)
+
+
+def sech(a): return rec(cosh(a))
+def csch(a): return rec(sinh(a))
+def acot(a): return atan(rec(a))
+def indeg(a): return a * _RADINDEG - a * _RADINDEGR
+def inrad(a): return a * _DEGINRAD
+def asind(a): return indeg(asin(a))
+def acosd(a): return indeg(acos(a))
+def atand(a): return indeg(atan(a))
+def asecd(a): return indeg(asec(a))
+def acscd(a): return indeg(acsc(a))
+def atan2d(a, b): return indeg(atan2(a, b))
+def asinpi(a): return _INVPI * asin(a)
+def acospi(a): return _INVPI * acos(a)
+def atanpi(a): return _INVPI * atan(a)
 
 # Functors applied to plain numbers evaluate at once in float32 with NT2's
 # scalar semantics (each step rounded, no fusion), as NT2's scalar overloads

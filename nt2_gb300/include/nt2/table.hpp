@@ -619,7 +619,65 @@ NT2G_UNARY(csc, NT2G_OP_CSC)
 NT2G_UNARY(sind, NT2G_OP_SIND)
 NT2G_UNARY(cosd, NT2G_OP_COSD)
 NT2G_UNARY(tand, NT2G_OP_TAND)
+NT2G_UNARY(tanpi, NT2G_OP_TANPI)
+NT2G_UNARY(cotpi, NT2G_OP_COTPI)
+NT2G_UNARY(cotd, NT2G_OP_COTD)
+NT2G_UNARY(secpi, NT2G_OP_SECPI)
+NT2G_UNARY(cscpi, NT2G_OP_CSCPI)
+NT2G_UNARY(secd, NT2G_OP_SECD)
+NT2G_UNARY(cscd, NT2G_OP_CSCD)
+NT2G_UNARY(sinc, NT2G_OP_SINC)
+NT2G_UNARY(sincpi, NT2G_OP_SINCPI)
+NT2G_UNARY(acotd, NT2G_OP_ACOTD)
+NT2G_UNARY(asec, NT2G_OP_ASEC)
+NT2G_UNARY(coth, NT2G_OP_COTH)
+NT2G_UNARY(sinhc, NT2G_OP_SINHC)
+NT2G_UNARY(acsc, NT2G_OP_ACSC)
+NT2G_UNARY(asech, NT2G_OP_ASECH)
+NT2G_UNARY(acoth, NT2G_OP_ACOTH)
+NT2G_UNARY(acsch, NT2G_OP_ACSCH)
 #undef NT2G_UNARY
+
+// NT2's generic compositions, built as the same programs of the functors
+// above, operation for operation (hyperbolic/functions/generic/{sech,
+// csch}.hpp; trigonometric/functions/generic/{acot,indeg,inrad,asind,acosd,
+// atand,asecd,acscd,atan2d,asinpi,acospi,atanpi}.hpp)
+namespace detail {
+inline float f32_of_bits(std::uint32_t u)
+{
+    float f;
+    std::memcpy(&f, &u, sizeof f);
+    return f;
+}
+}  // namespace detail
+
+#define NT2G_COMPOSED(NAME, BODY)                                                                                \
+    template <class A, class T = typename detail::elem_of<std::decay_t<A>>::type>                               \
+    expr<T> NAME(const A &a)                                                                                     \
+    {                                                                                                            \
+        const expr<T> x{detail::lift(a)};                                                                        \
+        return BODY;                                                                                             \
+    }
+NT2G_COMPOSED(sech, rec(cosh(x)))
+NT2G_COMPOSED(csch, rec(sinh(x)))
+NT2G_COMPOSED(acot, atan(rec(x)))
+NT2G_COMPOSED(indeg, x * detail::f32_of_bits(0x42652ee1u) - x * detail::f32_of_bits(0xb53387c1u))
+NT2G_COMPOSED(inrad, x * detail::f32_of_bits(0x3c8efa35u))
+NT2G_COMPOSED(asind, indeg(asin(x)))
+NT2G_COMPOSED(acosd, indeg(acos(x)))
+NT2G_COMPOSED(atand, indeg(atan(x)))
+NT2G_COMPOSED(asecd, indeg(asec(x)))
+NT2G_COMPOSED(acscd, indeg(acsc(x)))
+NT2G_COMPOSED(asinpi, detail::f32_of_bits(0x3ea2f983u) * asin(x))
+NT2G_COMPOSED(acospi, detail::f32_of_bits(0x3ea2f983u) * acos(x))
+NT2G_COMPOSED(atanpi, detail::f32_of_bits(0x3ea2f983u) * atan(x))
+#undef NT2G_COMPOSED
+
+template <class A, class B, class T = typename detail::common<A, B>::type>
+expr<T> atan2d(const A &a, const B &b)
+{
+    return indeg(atan2(a, b));
+}
 
 // Functors on plain scalars evaluate at once, in float, with NT2's scalar
 // semantics (unfused; volatile keeps the host compiler from contracting), as

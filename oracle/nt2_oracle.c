@@ -318,6 +318,41 @@ EXPORT float o_tanh(float a0)
     return bf(fb(r) ^ (fb(a0) & 0x80000000u));
 }
 
+/* coth HYP/scalar/coth.hpp (tanh_kernel::coth = rec(tanh kernel)) */
+EXPORT float o_coth(float a0)
+{
+    float x = fabsf(a0), r;
+    if (x < 0.625f) {
+        float x2 = x * x;
+        r = 1.0f / ((horner(x2, TANH_P, 5) * x2) * x + x);
+    } else {
+        r = 2.0f * (1.0f / (o_exp(x + x) - 1.0f)) + 1.0f;
+    }
+    return bf(fb(r) ^ (fb(a0) & 0x80000000u));
+}
+
+/* sinhc HYP/scalar/sinhc.hpp + HYP/details/sinhc_kernel.hpp (the sinh kernel's coefficients) */
+EXPORT float o_sinhc(float a0)
+{
+    float x = fabsf(a0);
+    if (isinf(x)) return x;
+    if (x < 1.0f) return horner(x * x, SINH_P, 4);
+    int big = x > bf(C_MAXLOG) - bf(0x3f317218u);
+    float t = o_exp(x * (big ? 0.5f : 1.0f));
+    if (big) return ((0.5f * t) / x) * t;
+    return (t * 0.5f + (-(1.0f / t)) * 0.5f) / x;
+}
+
+/* sech, csch, asech, acsch, acoth: HYP/generic/{sech,csch,asech,acsch,acoth}.hpp */
+EXPORT float o_asinh(float a0);
+EXPORT float o_acosh(float a0);
+EXPORT float o_atanh(float a0);
+EXPORT float o_sech(float a0) { return 1.0f / o_cosh(a0); }
+EXPORT float o_csch(float a0) { return 1.0f / o_sinh(a0); }
+EXPORT float o_asech(float a0) { return o_acosh(1.0f / a0); }
+EXPORT float o_acsch(float a0) { return o_asinh(1.0f / a0); }
+EXPORT float o_acoth(float a0) { return o_atanh(1.0f / a0); }
+
 /* --------------------------------------------------------- cbrt, hypot ----
  * cbrt: EXP/scalar/cbrt.hpp (float overload, Cephes' cbrtf); hypot:
  * BSIMD/arithmetic/functions/scalar/hypot.hpp:27-40 with NT2's exponent()
@@ -728,13 +763,30 @@ EXPORT float o_sin(float a0) { return sin_any(a0, 0); }
 EXPORT float o_cospi(float a0) { return cos_any(a0, 1); }
 EXPORT float o_sinpi(float a0) { return sin_any(a0, 1); }
 
+/* NT2's is_flint (frac(x) == 0, false for +-inf and NaN) and is_odd(x) =
+ * is_flint((x - 1)/2) (BSIMD/predicates/functions/scalar/is_odd.hpp:50,
+ * is_even.hpp:50, is_flint.hpp:50) */
+static int flintf(float x) { return (x - truncf(x)) == 0.0f; }
+static int oddf(float x) { return flintf((x - 1.0f) * 0.5f); }
+
+/* tan_invalid / cot_invalid per unit (trig_reduction.hpp:89-90, 268-269, 308-309) */
+static int tan_invalid_u(float a0, int unit)
+{
+    if (unit == 1) return flintf(a0 - 0.5f);
+    if (unit == 2) return flintf((a0 - 90.0f) * bf(0x3bb60b61u));
+    return 0;
+}
+static int cot_invalid_u(float a0, int unit)
+{
+    if (unit == 1) return a0 != 0.0f && flintf(a0);
+    if (unit == 2) return a0 != 0.0f && flintf(a0 * bf(0x3bb60b61u));
+    return 0;
+}
+
 static float tan_any(float a0, int unit)
 {
     if (invalid(a0)) return NAN;
-    if (unit == 2) {  /* tan_invalid for degrees: (x - 90)/180 an integer */
-        float q = (a0 - 90.0f) * bf(0x3bb60b61u);
-        if (q - truncf(q) == 0.0f) return NAN;
-    }
+    if (tan_invalid_u(a0, unit)) return NAN;
     if (a0 == 0.0f) return a0;
     float xr;
     int n = reduce_unit(fabsf(a0), &xr, unit);
@@ -751,24 +803,92 @@ EXPORT float o_cosd(float a0) { return cos_any(a0, 2); }
 EXPORT float o_sec(float a0) { return 1.0f / o_cos(a0); }
 EXPORT float o_csc(float a0) { return 1.0f / o_sin(a0); }
 
-/* cot: TRIG/scalar/impl/trigo/trig_base.hpp:178-188 */
-EXPORT float o_cot(float a0)
+/* cot, cotpi, cotd: TRIG/scalar/impl/trigo/trig_base.hpp:178-188 */
+static float cot_any(float a0, int unit)
 {
-    if (invalid(a0)) return NAN;
+    if (invalid(a0) || cot_invalid_u(a0, unit)) return NAN;
     uint32_t bos = fb(a0) & 0x80000000u;
     if (a0 == 0.0f) return bf(0x7f800000u | bos);
     float xr;
-    int n = trig_reduce(fabsf(a0), &xr);
+    int n = reduce_unit(fabsf(a0), &xr, unit);
     float y = tan_eval(xr);
     y = (n & 1) ? -y : 1.0f / y;
     return bf(fb(y) ^ bos);
 }
+EXPORT float o_cot(float a0) { return cot_any(a0, 0); }
+EXPORT float o_cotpi(float a0) { return cot_any(a0, 1); }
+EXPORT float o_cotd(float a0) { return cot_any(a0, 2); }
+EXPORT float o_tanpi(float a0) { return tan_any(a0, 1); }
+
+/* secpi TRIG/generic/secpi.hpp, cscpi TRIG/generic/cscpi.hpp, secd
+ * TRIG/generic/secd.hpp, cscd TRIG/generic/cscd.hpp */
+EXPORT float o_secpi(float a0) { float r = 1.0f / o_cospi(a0); return oddf(a0 * 2.0f) ? NAN : r; }
+EXPORT float o_cscpi(float a0) { float r = 1.0f / o_sinpi(a0); return (flintf(a0) && a0 != 0.0f) ? NAN : r; }
+EXPORT float o_secd(float a0) { float c = o_cosd(a0); return 1.0f / (c == 0.0f ? NAN : c); }
+EXPORT float o_cscd(float a0) { return o_cscpi(bf(0x3bb60b61u) * a0); }
+
+/* sinc TRIG/scalar/sinc.hpp, sincpi TRIG/scalar/sincpi.hpp (Eps = 2^-23) */
+EXPORT float o_sinc(float a0)
+{
+    if (isinf(a0)) return 0.0f;
+    return (fabsf(a0) < bf(0x34000000u)) ? 1.0f : o_sin(a0) / a0;
+}
+EXPORT float o_sincpi(float a0)
+{
+    if (isinf(a0)) return 0.0f;
+    return (fabsf(a0) < bf(0x34000000u)) ? 1.0f : (bf(0x3ea2f983u) * o_sinpi(a0)) / a0;
+}
+
+/* indeg TRIG/generic/indeg.hpp (Radindeg, Radindegr), inrad TRIG/generic/inrad.hpp */
+EXPORT float o_indeg(float a0) { return a0 * bf(0x42652ee1u) - a0 * bf(0xb53387c1u); }
+EXPORT float o_inrad(float a0) { return a0 * bf(0x3c8efa35u); }
+
+/* acotd TRIG/generic/acotd.hpp */
+EXPORT float o_acotd(float a0)
+{
+    float z = 90.0f - (a0 != 0.0f ? o_indeg(o_atan(fabsf(a0))) : 0.0f);
+    if (isinf(a0)) z = 0.0f;
+    return bf(fb(z) | (fb(a0) & 0x80000000u));
+}
+
+/* acsc TRIG/generic/acsc.hpp; asec TRIG/scalar/asec.hpp (single_ overload) */
+EXPORT float o_acsc(float a0) { return o_asin(1.0f / a0); }
+EXPORT float o_asec(float a0)
+{
+    float ax = fabsf(a0);
+    if (ax < 1.0f) return NAN;
+    float ax1 = ax - 1.0f;
+    if (ax1 < 0.001f) {
+        float t = sqrtf(2.0f * ax1) * (1.0f - ax1 * ((5 / 12.0f) + ax1 * ((43 / 160.0f) - ax1 * ((177 / 896.0f)
+                                                                           + ax1 * (2867 / 18432.0f)))));
+        return (a0 < 0.0f) ? bf(0x40490fdbu) - t : t;
+    }
+    if (a0 == 1.0f) return 0.0f;
+    return bf(0x3fc90fdbu) - o_acsc(a0);
+}
+
+/* the inverse functions in degrees and in multiples of pi, and acot
+ * (TRIG/generic/{asind,acosd,atand,asecd,acscd,asinpi,acospi,atanpi,acot}.hpp) */
+EXPORT float o_asind(float a0) { return o_indeg(o_asin(a0)); }
+EXPORT float o_acosd(float a0) { return o_indeg(o_acos(a0)); }
+EXPORT float o_atand(float a0) { return o_indeg(o_atan(a0)); }
+EXPORT float o_asecd(float a0) { return o_indeg(o_asec(a0)); }
+EXPORT float o_acscd(float a0) { return o_indeg(o_acsc(a0)); }
+EXPORT float o_asinpi(float a0) { return bf(0x3ea2f983u) * o_asin(a0); }
+EXPORT float o_acospi(float a0) { return bf(0x3ea2f983u) * o_acos(a0); }
+EXPORT float o_atanpi(float a0) { return bf(0x3ea2f983u) * o_atan(a0); }
+EXPORT float o_acot(float a0) { return o_atan(1.0f / a0); }
+EXPORT float o_atan2d(float a0, float a1) { return o_indeg(o_atan2(a0, a1)); }
 
 /* ------------------------------------------------- elementwise maps ---- */
 enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT, FN_EXP2 = 8, FN_EXP10,
        FN_EXPM1, FN_LOG2, FN_LOG10, FN_SIN, FN_COS, FN_TAN, FN_SINPI, FN_COSPI, FN_SINH, FN_COSH, FN_TANH,
        FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT, FN_COT, FN_SEC, FN_CSC, FN_SIND,
-       FN_COSD, FN_TAND };
+       FN_COSD, FN_TAND, FN_TANPI, FN_COTPI, FN_COTD, FN_SECPI, FN_CSCPI, FN_SECD, FN_CSCD, FN_SINC, FN_SINCPI,
+       FN_ACOTD, FN_ASEC, FN_COTH, FN_SINHC, FN_ACSC, FN_ASECH, FN_ACOTH, FN_ACSCH,
+       /* compositions of the above, oracle only (the front ends lower them to programs) */
+       FN_SECH = 51, FN_CSCH, FN_ACOT, FN_ASIND, FN_ACOSD, FN_ATAND, FN_ASECD, FN_ACSCD, FN_ASINPI, FN_ACOSPI,
+       FN_ATANPI, FN_INDEG, FN_INRAD };
 
 EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
 {
@@ -807,6 +927,36 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_SIND: y[i] = o_sind(a); break;
         case FN_COSD: y[i] = o_cosd(a); break;
         case FN_TAND: y[i] = o_tand(a); break;
+        case FN_TANPI: y[i] = o_tanpi(a); break;
+        case FN_COTPI: y[i] = o_cotpi(a); break;
+        case FN_COTD: y[i] = o_cotd(a); break;
+        case FN_SECPI: y[i] = o_secpi(a); break;
+        case FN_CSCPI: y[i] = o_cscpi(a); break;
+        case FN_SECD: y[i] = o_secd(a); break;
+        case FN_CSCD: y[i] = o_cscd(a); break;
+        case FN_SINC: y[i] = o_sinc(a); break;
+        case FN_SINCPI: y[i] = o_sincpi(a); break;
+        case FN_ACOTD: y[i] = o_acotd(a); break;
+        case FN_ASEC: y[i] = o_asec(a); break;
+        case FN_COTH: y[i] = o_coth(a); break;
+        case FN_SINHC: y[i] = o_sinhc(a); break;
+        case FN_SECH: y[i] = o_sech(a); break;
+        case FN_CSCH: y[i] = o_csch(a); break;
+        case FN_ASECH: y[i] = o_asech(a); break;
+        case FN_ACSCH: y[i] = o_acsch(a); break;
+        case FN_ACOTH: y[i] = o_acoth(a); break;
+        case FN_ACOT: y[i] = o_acot(a); break;
+        case FN_ACSC: y[i] = o_acsc(a); break;
+        case FN_ASIND: y[i] = o_asind(a); break;
+        case FN_ACOSD: y[i] = o_acosd(a); break;
+        case FN_ATAND: y[i] = o_atand(a); break;
+        case FN_ASECD: y[i] = o_asecd(a); break;
+        case FN_ACSCD: y[i] = o_acscd(a); break;
+        case FN_ASINPI: y[i] = o_asinpi(a); break;
+        case FN_ACOSPI: y[i] = o_acospi(a); break;
+        case FN_ATANPI: y[i] = o_atanpi(a); break;
+        case FN_INDEG: y[i] = o_indeg(a); break;
+        case FN_INRAD: y[i] = o_inrad(a); break;
         default: y[i] = sqrtf(a); break;
         }
     }
@@ -842,6 +992,14 @@ static double cosd_d(double a)
     double r = fabs(fmod(a, 360.0));
     if (r == 90.0 || r == 270.0) return 0.0;
     return cos(r * (M_PI / 180.0));
+}
+
+/* acot in degrees: 90 - atan|x| in degrees with x's sign (+-90 at +-0) */
+static double acotd_d(double a)
+{
+    if (isinf(a)) return copysign(0.0, a);
+    double t = fabs(a) >= 1.0 ? atan(1.0 / fabs(a)) * (180.0 / M_PI) : 90.0 - atan(fabs(a)) * (180.0 / M_PI);
+    return copysign(t, a);
 }
 
 /* FP64 reference of the same functions on float inputs (glibc double libm). */
@@ -882,6 +1040,36 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_SIND: y[i] = sind_d(a); break;
         case FN_COSD: y[i] = cosd_d(a); break;
         case FN_TAND: y[i] = sind_d(a) / cosd_d(a); break;
+        case FN_TANPI: y[i] = sinpi_d(a) / cospi_d(a); break;
+        case FN_COTPI: y[i] = cospi_d(a) / sinpi_d(a); break;
+        case FN_COTD: y[i] = cosd_d(a) / sind_d(a); break;
+        case FN_SECPI: y[i] = 1.0 / cospi_d(a); break;
+        case FN_CSCPI: y[i] = 1.0 / sinpi_d(a); break;
+        case FN_SECD: y[i] = 1.0 / cosd_d(a); break;
+        case FN_CSCD: y[i] = 1.0 / sind_d(a); break;
+        case FN_SINC: y[i] = a == 0.0 ? 1.0 : isinf(a) ? 0.0 : sin(a) / a; break;
+        case FN_SINCPI: y[i] = a == 0.0 ? 1.0 : isinf(a) ? 0.0 : sinpi_d(a) / (M_PI * a); break;
+        case FN_ACOTD: y[i] = acotd_d(a); break;
+        case FN_ASEC: y[i] = fabs(a) < 1.0 ? NAN : acos(1.0 / a); break;
+        case FN_COTH: y[i] = 1.0 / tanh(a); break;
+        case FN_SINHC: y[i] = a == 0.0 ? 1.0 : isinf(a) ? INFINITY : sinh(a) / a; break;
+        case FN_SECH: y[i] = 1.0 / cosh(a); break;
+        case FN_CSCH: y[i] = 1.0 / sinh(a); break;
+        case FN_ASECH: y[i] = acosh(1.0 / a); break;
+        case FN_ACSCH: y[i] = asinh(1.0 / a); break;
+        case FN_ACOTH: y[i] = atanh(1.0 / a); break;
+        case FN_ACOT: y[i] = atan(1.0 / a); break;
+        case FN_ACSC: y[i] = asin(1.0 / a); break;
+        case FN_ASIND: y[i] = asin(a) * (180.0 / M_PI); break;
+        case FN_ACOSD: y[i] = acos(a) * (180.0 / M_PI); break;
+        case FN_ATAND: y[i] = atan(a) * (180.0 / M_PI); break;
+        case FN_ASECD: y[i] = (fabs(a) < 1.0 ? NAN : acos(1.0 / a)) * (180.0 / M_PI); break;
+        case FN_ACSCD: y[i] = asin(1.0 / a) * (180.0 / M_PI); break;
+        case FN_ASINPI: y[i] = asin(a) / M_PI; break;
+        case FN_ACOSPI: y[i] = acos(a) / M_PI; break;
+        case FN_ATANPI: y[i] = atan(a) / M_PI; break;
+        case FN_INDEG: y[i] = a * (180.0 / M_PI); break;
+        case FN_INRAD: y[i] = a * (M_PI / 180.0); break;
         default: y[i] = sqrt(a); break;
         }
     }

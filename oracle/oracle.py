@@ -21,7 +21,12 @@ SRC = os.path.join(HERE, "nt2_oracle.c")
 
 FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, exp2=8, exp10=9, expm1=10, log2=11, log10=12,
           sin=13, cos=14, tan=15, sinpi=16, cospi=17, sinh=18, cosh=19, tanh=20, asin=21, acos=22, atan=23,
-          asinh=24, acosh=25, atanh=26, cbrt=27, cot=28, sec=29, csc=30, sind=31, cosd=32, tand=33)
+          asinh=24, acosh=25, atanh=26, cbrt=27, cot=28, sec=29, csc=30, sind=31, cosd=32, tand=33,
+          tanpi=34, cotpi=35, cotd=36, secpi=37, cscpi=38, secd=39, cscd=40, sinc=41, sincpi=42, acotd=43, asec=44,
+          coth=45, sinhc=46, acsc=47, asech=48, acoth=49, acsch=50,
+          # NT2's generic compositions of the functors above
+          sech=51, csch=52, acot=53, asind=54, acosd=55, atand=56, asecd=57, acscd=58, asinpi=59, acospi=60,
+          atanpi=61, indeg=62, inrad=63)
 
 
 def build():
@@ -47,7 +52,8 @@ def lib():
         for f in ("o_exp", "o_log", "o_log1p", "o_erfc", "o_normcdf", "o_fastnormcdf", "o_exp2", "o_exp10", "o_expm1",
                   "o_log2", "o_log10", "o_sin", "o_cos", "o_tan", "o_sinpi", "o_cospi",
                   "o_sinh", "o_cosh", "o_tanh", "o_asin", "o_acos", "o_atan",
-                  "o_asinh", "o_acosh", "o_atanh", "o_cbrt", "o_cot", "o_sec", "o_csc", "o_sind", "o_cosd", "o_tand"):
+                  "o_asinh", "o_acosh", "o_atanh", "o_cbrt", "o_cot", "o_sec", "o_csc", "o_sind", "o_cosd", "o_tand",
+                  *("o_" + k for k, v in FN.items() if v >= 34)):
             getattr(L, f).restype = ctypes.c_float
             getattr(L, f).argtypes = [ctypes.c_float]
         L.o_map_f32.argtypes = [ctypes.c_int, _P, _P, _I64]
@@ -59,6 +65,8 @@ def lib():
         L.o_atan2.argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_atan2_f32.argtypes = [_P, _P, _P, _I64]
         L.o_atan2_f64.argtypes = [_P, _P, _P, _I64]
+        L.o_atan2d.restype = ctypes.c_float
+        L.o_atan2d.argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_hypot.restype = ctypes.c_float
         L.o_hypot.argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_hypot_f32.argtypes = [_P, _P, _P, _I64]

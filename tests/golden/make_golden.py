@@ -52,6 +52,37 @@ SOURCES = [
     ("modules/core/trigonometric/unit/scalar/sind.cpp", 41, 51),
     ("modules/core/trigonometric/unit/scalar/cosd.cpp", 42, 52),
     ("modules/core/trigonometric/unit/scalar/tand.cpp", 40, 50),
+    # whole files from here on (1-200: every float ULP_EQUAL line they hold)
+    ("modules/core/trigonometric/unit/scalar/tanpi.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/cotpi.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/cotd.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/secpi.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/cscpi.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/secd.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/cscd.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/sinc.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/sincpi.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/acotd.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/asec.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/acsc.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/asind.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/acosd.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/atand.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/asecd.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/acscd.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/asinpi.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/acospi.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/atanpi.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/acot.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/indeg.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/inrad.cpp", 1, 200),
+    ("modules/core/hyperbolic/unit/scalar/coth.cpp", 1, 200),
+    ("modules/core/hyperbolic/unit/scalar/sinhc.cpp", 1, 200),
+    ("modules/core/hyperbolic/unit/scalar/sech.cpp", 1, 200),
+    ("modules/core/hyperbolic/unit/scalar/csch.cpp", 1, 200),
+    ("modules/core/hyperbolic/unit/scalar/asech.cpp", 1, 200),
+    ("modules/core/hyperbolic/unit/scalar/acsch.cpp", 1, 200),
+    ("modules/core/hyperbolic/unit/scalar/acoth.cpp", 1, 200),
 ]
 
 E = float(np.float32(math.e))
@@ -67,7 +98,8 @@ CONST = {
     "Twopio_3": float(np.uint32(0x40060a92).view(np.float32)),
     "Threepio_4": float(np.uint32(0x4016cbe4).view(np.float32)),
     "Sqrt_2": float(np.uint32(0x3fb504f3).view(np.float32)), "Valmax": float(np.finfo(np.float32).max),
-    "_45": 45.0, "_90": 90.0, "_180": 180.0,
+    "_45": 45.0, "_90": 90.0, "_135": 135.0, "_180": 180.0,
+    "Mindenormal": float(np.uint32(1).view(np.float32)),
 }
 
 
@@ -96,27 +128,46 @@ def _value(expr):
     m = re.fullmatch(r"nt2::One<\w+>\(\)\s*/\s*10", expr)
     if m:
         return float(np.float32(1.0) / np.float32(10.0))
+    m = re.fullmatch(r"[-+]?[0-9]+(\.[0-9]*)?", expr)
+    if m:  # an integer or decimal literal converted to the float r_t
+        return float(np.float32(float(expr)))
+    m = re.fullmatch(r"(-?)T\(([0-9]+)\)\s*/\s*(?:T\()?([0-9]+)\)?", expr)
+    if m:  # a quotient in float: T(1)/T(4), -T(1)/6
+        q = np.float32(float(m.group(2))) / np.float32(float(m.group(3)))
+        return float(-q if m.group(1) else q)
+    m = re.fullmatch(r"T\(2\)\s*/\s*\(nt2::Pi<\w+>\(\)\)", expr)
+    if m:
+        return float(np.float32(2.0) / np.float32(CONST["Pi"]))
+    m = re.fullmatch(r"nt2::rec\(nt2::Eps<\w+>\(\)\)", expr)
+    if m:
+        return float(np.float32(1.0) / np.float32(CONST["Eps"]))
     raise ValueError(f"unhandled NT2 constant spelling: {expr!r}")
 
 
 PAT = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(\w+)\((.*?)\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 # two-argument functors: pow(a, b)
 ARG = r"((?:[^,()]|\([^()]*\))*)"
-PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2|hypot)\(" + ARG + r",\s*" + ARG + r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
+PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2d?|hypot)\(" + ARG + r",\s*" + ARG + r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
             ("modules/core/trigonometric/unit/scalar/atan2.cpp", 47, 61),
-            ("modules/boost/simd/base/unit/arithmetic/scalar/hypot.cpp", 42, 52)]
+            ("modules/boost/simd/base/unit/arithmetic/scalar/hypot.cpp", 42, 52),
+            ("modules/core/trigonometric/unit/scalar/atan2d.cpp", 46, 60)]
+# expected values that are themselves results of NT2 functors (sin(Pio_4)/Pio_4)
+# are left out: they would pin the oracle to itself
+SELF_REFERENCE = re.compile(r"nt2::(sin|sinpi|cos|exp)\(")
 
 
 def main(root):
     out = []
     for rel, lo, hi in SOURCES:
         lines = open(os.path.join(root, rel)).read().splitlines()
-        for ln in range(lo, hi + 1):
+        for ln in range(lo, min(hi, len(lines)) + 1):
             m = PAT.search(lines[ln - 1])
             if not m:
                 continue
             fn, arg, exp, tol = m.groups()
+            if SELF_REFERENCE.search(exp):
+                continue
             out.append(dict(fn=fn, x=_value(arg), expected=_value(exp), tol_nt2ulp=float(tol),
                             source=f"{rel}:{ln}"))
     for rel, lo, hi in SOURCES2:

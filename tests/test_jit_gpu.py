@@ -32,7 +32,8 @@ def _bits_equal(a, b):
 _UNARY_F = ["NEG", "ABS", "SQR", "SQRT", "REC", "EXP", "LOG", "LOG1P", "ERFC", "NORMCDF", "FASTNORMCDF", "EXP2",
             "EXP10", "EXPM1", "LOG2", "LOG10", "SIN", "COS", "TAN", "SINPI", "COSPI",
             "SINH", "COSH", "TANH", "ASIN", "ACOS", "ATAN", "ASINH", "ACOSH", "ATANH", "CBRT",
-            "COT", "SEC", "CSC", "SIND", "COSD", "TAND"]
+            "COT", "SEC", "CSC", "SIND", "COSD", "TAND", "TANPI", "COTPI", "COTD", "SECPI", "CSCPI", "SECD", "CSCD",
+            "SINC", "SINCPI", "ACOTD", "ASEC", "COTH", "SINHC", "ACSC", "ASECH", "ACOTH", "ACSCH"]
 _BINARY_F = ["ADD", "SUB", "MUL", "DIV", "MIN", "MAX", "POW", "ATAN2", "HYPOT"]
 _CMP = ["LT", "GT", "LE", "GE", "EQ", "NE"]
 

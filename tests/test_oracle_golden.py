@@ -14,7 +14,10 @@ from helpers import nt2_ulpdist, std_ulp, reduction_ill
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
 FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1", "log2", "log10", "sin", "cos",
          "tan", "sinpi", "cospi", "sinh", "cosh", "tanh", "asin", "acos", "atan",
-         "asinh", "acosh", "atanh", "cbrt", "cot", "sec", "csc", "sind", "cosd", "tand")
+         "asinh", "acosh", "atanh", "cbrt", "cot", "sec", "csc", "sind", "cosd", "tand",
+         "tanpi", "cotpi", "cotd", "secpi", "cscpi", "secd", "cscd", "sinc", "sincpi", "acotd", "asec", "acsc",
+         "asind", "acosd", "atand", "asecd", "acscd", "asinpi", "acospi", "atanpi", "acot", "indeg", "inrad",
+         "coth", "sinhc", "sech", "csch", "asech", "acsch", "acoth")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
@@ -24,7 +27,7 @@ def test_oracle_matches_nt2_unit_tests(oracle, rec):
     assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (got, rec)
 
 
-@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("pow", "atan2", "hypot")],
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("pow", "atan2", "atan2d", "hypot")],
                          ids=lambda r: f"{r['fn']}({r['x']},{r['y']})@{r['source'].split('/')[-1]}")
 def test_oracle_binary_matches_nt2_unit_tests(oracle, rec):
     got = getattr(oracle.lib(), "o_" + rec["fn"])(rec["x"], rec["y"])
