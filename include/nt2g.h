@@ -39,7 +39,9 @@ typedef enum nt2g_status {
 /* Arithmetic policy of the float math.
  * NT2G_PREC_FAST: fused multiply-add, approximate-reciprocal division with a
  *   Newton step where the operands are known normal, erfc/normcdf on an exact
- *   split of x^2; every functor within 4 ulp of FP64.
+ *   split of x^2; every functor within 4 ulp of FP64 (gammaln excepted: NT2's
+ *   form, 6.3 ulp near Gamma's minimum), away from the poles and zeros where
+ *   a function's own conditioning decides.
  * NT2G_PREC_NT2: NT2's own scalar algorithms and operation order (unfused
  *   fma/Horner, IEEE division and sqrt); bit-identical to NT2's CPU result. */
 typedef enum nt2g_precision { NT2G_PREC_FAST = 0, NT2G_PREC_NT2 = 1 } nt2g_precision;
@@ -92,7 +94,9 @@ typedef enum nt2g_opcode {
     NT2G_OP_COT = 100, NT2G_OP_SEC, NT2G_OP_CSC, NT2G_OP_SIND, NT2G_OP_COSD, NT2G_OP_TAND,
     NT2G_OP_TANPI = 106, NT2G_OP_COTPI, NT2G_OP_COTD, NT2G_OP_SECPI, NT2G_OP_CSCPI, NT2G_OP_SECD, NT2G_OP_CSCD,
     NT2G_OP_SINC = 113, NT2G_OP_SINCPI, NT2G_OP_ACOTD, NT2G_OP_ASEC, NT2G_OP_COTH, NT2G_OP_SINHC,
-    NT2G_OP_ACSC = 119, NT2G_OP_ASECH, NT2G_OP_ACOTH, NT2G_OP_ACSCH
+    NT2G_OP_ACSC = 119, NT2G_OP_ASECH, NT2G_OP_ACOTH, NT2G_OP_ACSCH,
+    NT2G_OP_ERF = 123, NT2G_OP_ERFCX, NT2G_OP_EXPX2, NT2G_OP_GAMMA, NT2G_OP_GAMMALN, NT2G_OP_EXPRECNEG,
+    NT2G_OP_EXPRECNEGC, NT2G_OP_SQRT1PM1
 } nt2g_opcode;
 
 typedef struct nt2g_op {
@@ -293,7 +297,8 @@ nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8
  * 13 sin, 14 cos, 15 tan, 16 sinpi, 17 cospi, 18 sinh, 19 cosh, 20 tanh, 21 asin,
  * 22 acos, 23 atan, 24 asinh, 25 acosh, 26 atanh, 27 cbrt, 28 cot, 29 sec, 30 csc, 31 sind,
  * 32 cosd, 33 tand, 34 tanpi, 35 cotpi, 36 cotd, 37 secpi, 38 cscpi, 39 secd, 40 cscd, 41 sinc,
- * 42 sincpi, 43 acotd, 44 asec, 45 coth, 46 sinhc, 47 acsc, 48 asech, 49 acoth, 50 acsch. */
+ * 42 sincpi, 43 acotd, 44 asec, 45 coth, 46 sinhc, 47 acsc, 48 asech, 49 acoth, 50 acsch, 64 erf, 65 erfcx, 66 expx2, 67 gamma, 68 gammaln,
+ * 80 exprecneg, 81 exprecnegc, 82 sqrt1pm1. */
 nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision,
                          void *stream);
 

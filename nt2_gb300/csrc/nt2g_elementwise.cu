@@ -426,6 +426,14 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 48) return asech<P>(a);
     if (FN == 49) return acoth<P>(a);
     if (FN == 50) return acsch<P>(a);
+    if (FN == 64) return erf<P>(a);
+    if (FN == 65) return erfcx<P>(a);
+    if (FN == 66) return expx2<P>(a);
+    if (FN == 67) return gamma<P>(a);
+    if (FN == 68) return gammaln<P>(a);
+    if (FN == 80) return exprecneg<P>(a);
+    if (FN == 81) return exprecnegc<P>(a);
+    if (FN == 82) return sqrt1pm1<P>(a);
     float p, q;
     normcdf_pair<P>(a, p, q);
     return q;
@@ -494,6 +502,14 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 48: NT2G_MAP(48); break;
     case 49: NT2G_MAP(49); break;
     case 50: NT2G_MAP(50); break;
+    case 64: NT2G_MAP(64); break;
+    case 65: NT2G_MAP(65); break;
+    case 66: NT2G_MAP(66); break;
+    case 67: NT2G_MAP(67); break;
+    case 68: NT2G_MAP(68); break;
+    case 80: NT2G_MAP(80); break;
+    case 81: NT2G_MAP(81); break;
+    case 82: NT2G_MAP(82); break;
     default: NT2G_MAP(7); break;
     }
 #undef NT2G_MAP
@@ -572,6 +588,14 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_ASECH: return asech<P>(a);
     case NT2G_OP_ACOTH: return acoth<P>(a);
     case NT2G_OP_ACSCH: return acsch<P>(a);
+    case NT2G_OP_ERF: return erf<P>(a);
+    case NT2G_OP_ERFCX: return erfcx<P>(a);
+    case NT2G_OP_EXPX2: return expx2<P>(a);
+    case NT2G_OP_GAMMA: return gamma<P>(a);
+    case NT2G_OP_GAMMALN: return gammaln<P>(a);
+    case NT2G_OP_EXPRECNEG: return exprecneg<P>(a);
+    case NT2G_OP_EXPRECNEGC: return exprecnegc<P>(a);
+    case NT2G_OP_SQRT1PM1: return sqrt1pm1<P>(a);
     default: return fastnormcdf<P>(a);
     }
 }

@@ -194,6 +194,14 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_ASECH: e = "nt2g::asech<P>(" + A + ")"; break;
         case NT2G_OP_ACOTH: e = "nt2g::acoth<P>(" + A + ")"; break;
         case NT2G_OP_ACSCH: e = "nt2g::acsch<P>(" + A + ")"; break;
+        case NT2G_OP_ERF: e = "nt2g::erf<P>(" + A + ")"; break;
+        case NT2G_OP_ERFCX: e = "nt2g::erfcx<P>(" + A + ")"; break;
+        case NT2G_OP_EXPX2: e = "nt2g::expx2<P>(" + A + ")"; break;
+        case NT2G_OP_GAMMA: e = "nt2g::gamma<P>(" + A + ")"; break;
+        case NT2G_OP_GAMMALN: e = "nt2g::gammaln<P>(" + A + ")"; break;
+        case NT2G_OP_EXPRECNEG: e = "nt2g::exprecneg<P>(" + A + ")"; break;
+        case NT2G_OP_EXPRECNEGC: e = "nt2g::exprecnegc<P>(" + A + ")"; break;
+        case NT2G_OP_SQRT1PM1: e = "nt2g::sqrt1pm1<P>(" + A + ")"; break;
         case NT2G_OP_FNMS: e = "P::fma(-" + A + ", " + B + ", " + C + ")"; break;
         case NT2G_OP_LT: e = "(" + A + " < " + B + ") ? 1u : 0u"; break;
         case NT2G_OP_GT: e = "(" + A + " > " + B + ") ? 1u : 0u"; break;

@@ -1587,4 +1587,281 @@ template <class P> NT2G_HD float asec(float a0)
     return P::sub(bits_f(0x3fc90fdbu), asin<P>(P::div(1.0f, a0)));  // Pio_2
 }
 
+// ------------------------------------------------------------ euler --
+// erf2 kernel: erfc(x) e^(x^2) for x >= 2/3 as a polynomial in x/(1+x) - 0.4
+// (euler/functions/details/erf_kernel.hpp:48-66, the one erfc uses)
+template <class P> NT2G_HD float erfc2_kernel(float z)
+{
+    return horner<P>(z, bits_f(0xc0283611u), bits_f(0x40d67e3bu), bits_f(0xc0cd1a85u), bits_f(0x4050b063u),
+                     bits_f(0xbfaea865u), bits_f(0x3e2006f0u), bits_f(0x3e1175c7u), bits_f(0x3ec4ca6eu),
+                     bits_f(0x3e243828u), bits_f(0xbf918a62u), bits_f(0x3f0a0e8bu));
+}
+
+// erf (euler/functions/scalar/erf.hpp, single_): x erf1(x^2) below 2/3, else
+// 1 - e^(-x^2) erfc2(x/(1+x) - 0.4) with x's sign; +-1 at +-inf.  Fast: the
+// same small branch with FMAs, 1 - erfc(|x|) from the fast erfc tail above it.
+template <class P> NT2G_HD float erf(float a0)
+{
+    if (is_nan(a0)) return a0;
+    const float x = fabsf(a0);
+    if (x == f_inf()) return copysignf(1.0f, a0);
+    if (x < bits_f(NT2G_TWOTHIRD))
+        return P::mul(a0, horner<P>(P::mul(x, x), bits_f(0xba1fc83bu), bits_f(0x3ba4468du), bits_f(0xbcdb61f4u),
+                                    bits_f(0x3de70f22u), bits_f(0xbec0937eu), bits_f(0x3f906ebau)));
+    float r2;
+    if (P::exact) {
+        const float z = P::sub(P::div(x, P::add(x, 1.0f)), 0.4f);
+        r2 = P::sub(1.0f, P::mul(exp<P>(-P::mul(x, x)), erfc2_kernel<P>(z)));
+    } else {
+        r2 = Fast::sub(1.0f, erfc_tail_fast<false>(x));
+    }
+    return (a0 < 0.0f) ? -r2 : r2;
+}
+
+// expx2 = e^(x^2) (exponential/functions/scalar/expx2.hpp, one argument):
+// e^(m^2) e^(2mf + f^2) with m = 32 floor(x/32 + 1/2) (NT2's float constants
+// Expx2c1 = 32, Expx2c2 = 1/32), +inf past Maxlog.  Fast: x^2 split exactly
+// by an FMA, e^hi (1 + lo), so the rounding of x^2 is not magnified by e^.
+template <class P> NT2G_HD float expx2(float a0)
+{
+    const float x = fabsf(a0);
+    if (x == f_inf()) return f_inf();
+    if (!P::exact) {
+        const float hi = Fast::mul(x, x), lo = Fast::fma(x, x, -hi);
+        const float e = exp<Fast>(hi);
+        return (e < f_inf()) ? Fast::fma(e, lo, e) : e;
+    }
+    const float m = P::mul(32.0f, floorf(P::add(P::mul(0.03125f, x), 0.5f)));
+    const float f = P::sub(x, m);
+    const float u = P::mul(m, m);
+    const float u1 = P::add(P::mul(P::mul(2.0f, m), f), P::mul(f, f));
+    if (P::add(u, u1) > bits_f(NT2G_MAXLOG)) return f_inf();
+    return P::mul(exp<P>(u), exp<P>(u1));
+}
+
+// erfcx = e^(x^2) erfc(x) (euler/functions/scalar/erfcx.hpp, single_):
+// expx2(x) erfc(x) below 2/3, else the erfc2 kernel; 0 at +inf.  Fast: for
+// x >= 0 the fast erfc tail without its exponential, w R(w) (1 + r); below 0,
+// 2 e^(x^2) - erfcx(-x).
+template <class P> NT2G_HD float erfcx(float a0)
+{
+    if (a0 == f_inf()) return 0.0f;
+    if (is_nan(a0)) return a0;
+    if (P::exact) {
+        if (a0 < bits_f(NT2G_TWOTHIRD)) return P::mul(expx2<P>(a0), erfc<P>(a0));
+        return erfc2_kernel<P>(P::sub(P::div(a0, P::add(a0, 1.0f)), 0.4f));
+    }
+    const float a = fabsf(a0);
+    const float den = Fast::fma(0.5f, a, 1.0f);
+    const float dlo = Fast::fma(0.5f, a, Fast::sub(1.0f, den));
+    float w = Fast::div(1.0f, den);
+    const float r = Fast::fma(-dlo, w, Fast::fma(-den, w, 1.0f));
+    const float wr = Fast::mul(w, erfc_tail_poly(w));
+    const float t = (a < f_inf()) ? Fast::fma(r, wr, wr) : 0.0f;
+    return (a0 < 0.0f) ? Fast::fma(2.0f, expx2<Fast>(a0), -t) : t;
+}
+
+// exprecneg = e^(-1/x), exprecnegc = 1 - e^(-1/x) (exponential/functions/
+// generic/exprecneg.hpp, exprecnegc.hpp: exp(-rec(x)), -expm1(-rec(x))).
+// Fast: 1/x carried as hi + lo (the division's residual), so its rounding is
+// not magnified by the exponential: e^(-hi) (1 - lo).
+template <class P> NT2G_HD float exprecneg(float a0)
+{
+    const float hi = P::div(1.0f, a0);
+    if (P::exact) return exp<P>(-hi);
+    const bool fin = fabsf(hi) < f_inf() && fabsf(a0) < f_inf();
+    const float lo = fin ? Fast::mul(Fast::fma(-hi, a0, 1.0f), hi) : 0.0f;
+    const float e = exp<Fast>(-hi);
+    return (e < f_inf()) ? Fast::fma(-e, lo, e) : e;
+}
+template <class P> NT2G_HD float exprecnegc(float a0)
+{
+    const float hi = P::div(1.0f, a0);
+    if (P::exact) return -expm1<P>(-hi);
+    const bool fin = fabsf(hi) < f_inf() && fabsf(a0) < f_inf();
+    const float lo = fin ? Fast::mul(Fast::fma(-hi, a0, 1.0f), hi) : 0.0f;
+    const float em1 = expm1<Fast>(-hi);
+    // 1 - e^(-hi-lo) = -em1 + (em1 + 1) lo
+    return (fabsf(em1) < f_inf()) ? Fast::fma(Fast::add(em1, 1.0f), lo, -em1) : -em1;
+}
+
+// sqrt1pm1 = sqrt(1+x) - 1 (exponential/functions/generic/sqrt1pm1.hpp):
+// x/(1 + sqrt(1+x)) below 1/2 in magnitude, sqrt(1+x) - 1 above.  Fast: the
+// quotient everywhere (no cancellation), +inf at +inf.
+template <class P> NT2G_HD float sqrt1pm1(float a0)
+{
+    const float t = P::sqrt(P::add(a0, 1.0f));
+    const float q = P::div(a0, P::add(t, 1.0f));
+    if (P::exact) return (fabsf(a0) < 0.5f) ? q : P::sub(t, 1.0f);
+    return (a0 == f_inf()) ? a0 : q;
+}
+
+// gamma (euler/functions/scalar/gamma.hpp): below -33 the reflection with
+// Stirling's formula (scalar/stirling.hpp + details/stirling_kernel.hpp),
+// else x stepped into [2, 3) one unit at a time, the product of the steps
+// times the degree-7 polynomial of details/gamma_kernel.hpp.  NT2's steps from
+// a large x make the product +inf long before the end (and never end from 2^24
+// on, where x - 1 == x): from 64 on the result is +inf at once.  Fast: the
+// product carried as a float-float pair (x - 1 and x + 1 are exact in this
+// range, each multiply or divide adds only its residual), and the reflection
+// below -33 from that same product for |x| instead of Stirling's formula.
+template <class P> NT2G_HD float stirling(float a0)
+{
+    if (is_nan(a0)) return a0;
+    if (a0 > bits_f(0x420c28f3u)) return f_inf();  // Stirlinglargelim
+    float w = P::div(1.0f, a0);
+    w = P::fma(w, horner<P>(w, bits_f(0xb970b359u), bits_f(0xbb2fb930u), bits_f(0x3b638e39u), bits_f(0x3daaaaabu)),
+               1.0f);
+    float y = exp<P>(-a0);
+    if (y == 0.0f) return f_inf();
+    const float z = P::sub(a0, 0.5f);
+    if (a0 >= bits_f(0x41d628f6u)) {  // Stirlingsplitlim
+        const float v = pow<P>(a0, P::mul(z, 0.5f));
+        y = P::mul(y, v);
+        y = P::mul(y, v);
+    } else {
+        y = P::mul(y, pow<P>(a0, z));
+    }
+    return P::mul(y, P::mul(bits_f(0x40206c99u), w));  // Sqrt_2pi
+}
+
+// Gamma(x) for x in [-33, 64] by NT2's stepping; Fast keeps the product as zh + zl
+template <class P> NT2G_HD float gamma_steps(float x)
+{
+    float zh = 1.0f, zl = 0.0f;
+    while (x >= 3.0f) {
+        x = P::sub(x, 1.0f);
+        if (P::exact) {
+            zh = P::mul(zh, x);
+        } else {
+            const float p = Fast::mul(zh, x);
+            zl = Fast::fma(zl, x, Fast::fma(zh, x, -p));
+            zh = p;
+        }
+    }
+    for (int k = 0; k < 2; ++k) {  // x < 0 steps, then up to two below 2
+        while (k == 0 ? (x < 0.0f) : (x < 2.0f)) {
+            if (k == 1 && x == 0.0f) return f_nan();
+            if (P::exact) {
+                zh = P::div(zh, x);
+            } else {
+                const float q = Fast::div(zh, x);
+                zl = Fast::div(Fast::add(Fast::fma(-q, x, zh), zl), x);
+                zh = q;
+            }
+            x = P::add(x, 1.0f);
+        }
+    }
+    // (Fast: once the product is +inf its low part is NaN and is dropped)
+    const bool fin = P::exact || fabsf(zh) < f_inf();
+    if (x == 2.0f) return fin ? (P::exact ? zh : Fast::add(zh, zl)) : zh;
+    x = P::sub(x, 2.0f);
+    const float g = horner<P>(x, bits_f(0x3ad28b22u), bits_f(0x3ba90c99u), bits_f(0x3b91db14u), bits_f(0x3d93ae7cu),
+                              bits_f(0x3da82a34u), bits_f(0x3ed2d411u), bits_f(0x3ed87799u), 1.0f);
+    if (P::exact || !fin) return P::mul(zh, g);
+    return Fast::fma(zh, g, Fast::mul(zl, g));
+}
+
+template <class P> NT2G_HD float gamma(float a0)
+{
+    if (a0 == 0.0f) return copysignf(f_inf(), a0);
+    if (is_nan(a0) || a0 == -f_inf()) return f_nan();
+    if (a0 == f_inf()) return a0;
+    const float q = fabsf(a0);
+    if (a0 < -33.0f) {
+        float p = floorf(q);
+        if (p == q) return f_nan();
+        const bool iseven = !(((int)p) & 1);
+        float z = P::sub(q, p);
+        if (z > 0.5f) {
+            p = P::add(p, 1.0f);
+            z = P::sub(q, p);
+        }
+        z = P::mul(q, sinpi<P>(z));
+        if (z == 0.0f) return f_nan();
+        const float st = P::exact ? stirling<P>(q) : gamma_steps<P>(q);
+        const float r = P::div(bits_f(0x40490fdbu), P::mul(fabsf(z), st));
+        return iseven ? -r : r;
+    }
+    if (a0 > 64.0f) return f_inf();
+    return gamma_steps<P>(a0);
+}
+
+// gammaln (euler/functions/scalar/gammaln.hpp, single_): the reflection for
+// x < 0, the polynomials of details/gammaln_kernel.hpp around 1 and 2 below
+// 6.5 (with up to four steps), else Stirling's series with its correction up
+// to 1e4.  Both policies follow it (Fast with FMAs).
+template <class P> NT2G_HD float gammaln_b(float x)
+{
+    return horner<P>(x, bits_f(0x3a1ebb94u), bits_f(0xbaabeab1u), bits_f(0x3b3ba883u), bits_f(0xbbf164fdu),
+                     bits_f(0x3ca89ed8u), bits_f(0xbd89f07eu), bits_f(0x3ea51a64u), bits_f(0x3ed87730u));
+}
+
+template <class P> NT2G_HD float gammaln_pos(float x)
+{
+    if (x < 6.5f) {
+        float z = 1.0f, tx = x, nx = 0.0f;
+        if (x >= 1.5f) {
+            while (tx > 2.5f) {
+                nx = P::sub(nx, 1.0f);
+                tx = P::add(x, nx);
+                z = P::mul(z, tx);
+            }
+            x = P::add(x, P::sub(nx, 2.0f));
+            return P::add(P::mul(x, gammaln_b<P>(x)), log<P>(z));
+        }
+        if (x >= 1.25f) {
+            z = P::mul(z, x);
+            x = P::sub(x, 1.0f);
+            return P::sub(P::mul(x, gammaln_b<P>(x)), log<P>(z));
+        }
+        if (x >= 0.75f) {
+            x = P::sub(x, 1.0f);
+            return P::mul(x, horner<P>(x, bits_f(0x3e0c3c4fu), bits_f(0xbe22d329u), bits_f(0x3e2d4dabu),
+                                          bits_f(0xbe53c04fu), bits_f(0x3e8a898bu), bits_f(0xbecd27a8u),
+                                          bits_f(0x3f528d34u), bits_f(0xbf13c468u)));
+        }
+        while (tx < 1.5f) {
+            if (tx == 0.0f) return f_inf();
+            z = P::mul(z, tx);
+            nx = P::add(nx, 1.0f);
+            tx = P::add(x, nx);
+        }
+        x = P::add(x, P::sub(nx, 2.0f));
+        const float p = P::mul(x, gammaln_b<P>(x));
+        return P::sub(p, log<P>(z));
+    }
+    float r = P::fma(P::sub(x, 0.5f), log<P>(x), P::sub(bits_f(0x3f6b3f8eu), x));  // Logsqrt2pi
+    if (x <= 1.0e4f) {
+        const float z = P::div(1.0f, x);
+        const float p = P::mul(z, z);
+        r = P::fma(z, horner<P>(p, bits_f(0x3a31fd69u), bits_f(0xbb358701u), bits_f(0x3daaaa94u)), r);
+    }
+    return r;
+}
+
+template <class P> NT2G_HD float gammaln(float a0)
+{
+    if (a0 > bits_f(0x7bc3f8eau) || a0 == 0.0f) return f_inf();  // Maxgammaln
+    const float q = fabsf(a0);
+    // Fast: below 2^-20 in magnitude -log|x| (NT2's q sinpi(q) underflows to
+    // 0 for the smallest negative x and gives +inf there)
+    if (!P::exact && q < 0x1p-20f) return -log<P>(q);
+    if (a0 < 0.0f) {
+        if (q > bits_f(0x7bc3f8eau)) return f_nan();
+        const float w = gammaln_pos<P>(q);
+        float p = floorf(q);
+        if (p == q) return f_inf();
+        float z = P::sub(q, p);
+        if (z > 0.5f) {
+            p = P::add(p, 1.0f);
+            z = P::sub(p, q);
+        }
+        z = P::mul(q, sinpi<P>(z));
+        if (z == 0.0f) return f_inf();
+        return P::sub(-log<P>(P::mul(bits_f(0x3ea2f983u), fabsf(z))), w);
+    }
+    return gammaln_pos<P>(a0);
+}
+
 }  // namespace nt2g

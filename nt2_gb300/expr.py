@@ -110,6 +110,14 @@ acsc = _un("ACSC")
 asech = _un("ASECH")
 acoth = _un("ACOTH")
 acsch = _un("ACSCH")
+erf = _un("ERF")
+erfcx = _un("ERFCX")
+expx2 = _un("EXPX2")
+gamma = _un("GAMMA")
+gammaln = _un("GAMMALN")
+exprecneg = _un("EXPRECNEG")
+exprecnegc = _un("EXPRECNEGC")
+sqrt1pm1 = _un("SQRT1PM1")
 
 
 # NT2's generic compositions, built as the same programs of the functors above,
@@ -139,6 +147,25 @@ def atan2d(a, b): return indeg(atan2(a, b))
 def asinpi(a): return _INVPI * asin(a)
 def acospi(a): return _INVPI * acos(a)
 def atanpi(a): return _INVPI * atan(a)
+
+
+# logspace_add, logspace_sub (exponential/functions/scalar/logspace_add.hpp,
+# logspace_sub.hpp) in NT2's forms; NT2's max(a, b) is a > b ? a : b.  The
+# real* functors are NT2's assertion-only aliases of sqrt, log and pow.
+def logspace_add(a, b):
+    t = -abs_(a - b)
+    return if_else(_bin("NE", t, t), a + b, max_(a, b) + log1p(exp(t)))
+
+
+def logspace_sub(a, b):
+    d = b - a
+    return a + if_else(d > -_bits_f32(0x3f317218), log(-expm1(d)), log1p(-exp(d)))
+
+
+realsqrt, reallog = sqrt, log
+
+
+def realpow(a, b): return pow(a, b)
 
 # Functors applied to plain numbers evaluate at once in float32 with NT2's
 # scalar semantics (each step rounded, no fusion), as NT2's scalar overloads

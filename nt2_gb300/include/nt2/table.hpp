@@ -636,6 +636,14 @@ NT2G_UNARY(acsc, NT2G_OP_ACSC)
 NT2G_UNARY(asech, NT2G_OP_ASECH)
 NT2G_UNARY(acoth, NT2G_OP_ACOTH)
 NT2G_UNARY(acsch, NT2G_OP_ACSCH)
+NT2G_UNARY(erf, NT2G_OP_ERF)
+NT2G_UNARY(erfcx, NT2G_OP_ERFCX)
+NT2G_UNARY(expx2, NT2G_OP_EXPX2)
+NT2G_UNARY(gamma, NT2G_OP_GAMMA)
+NT2G_UNARY(gammaln, NT2G_OP_GAMMALN)
+NT2G_UNARY(exprecneg, NT2G_OP_EXPRECNEG)
+NT2G_UNARY(exprecnegc, NT2G_OP_EXPRECNEGC)
+NT2G_UNARY(sqrt1pm1, NT2G_OP_SQRT1PM1)
 #undef NT2G_UNARY
 
 // NT2's generic compositions, built as the same programs of the functors
@@ -677,6 +685,39 @@ template <class A, class B, class T = typename detail::common<A, B>::type>
 expr<T> atan2d(const A &a, const B &b)
 {
     return indeg(atan2(a, b));
+}
+
+// logspace_add, logspace_sub (exponential/functions/scalar/logspace_add.hpp,
+// logspace_sub.hpp): log(e^a + e^b) and log(e^a - e^b) in NT2's forms; the
+// real* functors are NT2's assertion-only aliases of sqrt, log and pow
+template <class A, class B, class T = typename detail::common<A, B>::type>
+expr<T> logspace_add(const A &a, const B &b)
+{
+    const expr<T> x{detail::any<T>(a)}, y{detail::any<T>(b)};
+    const expr<T> t = -abs(x - y);
+    return if_else(t != t, x + y, max(x, y) + log1p(exp(t)));
+}
+template <class A, class B, class T = typename detail::common<A, B>::type>
+expr<T> logspace_sub(const A &a, const B &b)
+{
+    const expr<T> x{detail::any<T>(a)}, y{detail::any<T>(b)};
+    const expr<T> d = y - x;
+    return x + if_else(d > -detail::f32_of_bits(0x3f317218u), log(-expm1(d)), log1p(-exp(d)));
+}
+template <class A, class T = typename detail::elem_of<std::decay_t<A>>::type>
+expr<T> realsqrt(const A &a)
+{
+    return sqrt(a);
+}
+template <class A, class T = typename detail::elem_of<std::decay_t<A>>::type>
+expr<T> reallog(const A &a)
+{
+    return log(a);
+}
+template <class A, class B, class T = typename detail::common<A, B>::type>
+expr<T> realpow(const A &a, const B &b)
+{
+    return pow(a, b);
 }
 
 // Functors on plain scalars evaluate at once, in float, with NT2's scalar

@@ -198,6 +198,45 @@ EXPORT float o_erfc(float a0)
     return (a0 < 0.0f) ? 2.0f - r1 : r1;
 }
 
+/* erf EUL/scalar/erf.hpp (single_), erf1 kernel EUL/details/erf_kernel.hpp:34-44 */
+static const uint32_t ERF1_P[6] = {0xba1fc83b, 0x3ba4468d, 0xbcdb61f4, 0x3de70f22, 0xbec0937e, 0x3f906eba};
+EXPORT float o_exp(float a0);
+
+EXPORT float o_erf(float a0)
+{
+    if (isnan(a0)) return a0;
+    if (isinf(a0)) return a0 > 0.0f ? 1.0f : -1.0f;
+    float x = fabsf(a0);
+    if (x < bf(C_TWOTHIRD)) return a0 * horner(x * x, ERF1_P, 6);
+    float z = x / (1.0f + x) - 0.4f;
+    float r2 = 1.0f - o_exp(-(x * x)) * horner(z, ERFC2_P, 11);
+    return (a0 < 0.0f) ? -r2 : r2;
+}
+
+/* expx2 EXP/scalar/expx2.hpp (one argument): exp(x^2) as exp(m^2) exp(2mf + f^2)
+ * with m = Expx2c1 floor(Expx2c2 x + 1/2) (float constants 32 and 1/32) */
+EXPORT float o_expx2(float a0)
+{
+    if (isinf(a0)) return INFINITY;
+    float x = fabsf(a0);
+    float m = 32.0f * floorf(0.03125f * x + 0.5f);
+    x -= m;
+    float u = m * m;
+    float u1 = (2.0f * m) * x + x * x;
+    if (u + u1 > bf(C_MAXLOG)) return INFINITY;
+    return o_exp(u) * o_exp(u1);
+}
+
+/* erfcx EUL/scalar/erfcx.hpp (single_): exp(x^2) erfc(x) below 2/3, else the erfc2 kernel */
+EXPORT float o_erfcx(float a0)
+{
+    if (a0 == INFINITY) return 0.0f;
+    if (isnan(a0)) return a0;
+    if (a0 < bf(C_TWOTHIRD)) return o_expx2(a0) * o_erfc(a0);
+    float z = a0 / (1.0f + a0) - 0.4f;
+    return horner(z, ERFC2_P, 11);
+}
+
 /* normcdf: STAT/generic/normcdf.hpp:34  Half*erfc(-Sqrt_2o_2*a0) */
 EXPORT float o_normcdf(float a0) { return 0.5f * o_erfc(-bf(C_SQRT_2O_2) * a0); }
 
@@ -880,12 +919,175 @@ EXPORT float o_atanpi(float a0) { return bf(0x3ea2f983u) * o_atan(a0); }
 EXPORT float o_acot(float a0) { return o_atan(1.0f / a0); }
 EXPORT float o_atan2d(float a0, float a1) { return o_indeg(o_atan2(a0, a1)); }
 
+/* ------------------------------------------------------ gamma family ----
+ * stirling EUL/scalar/stirling.hpp + EUL/details/stirling_kernel.hpp (float),
+ * gamma EUL/scalar/gamma.hpp + EUL/details/gamma_kernel.hpp (float),
+ * gammaln EUL/scalar/gammaln.hpp (single_) + EUL/details/gammaln_kernel.hpp. */
+static const uint32_t STIRLING_P[4] = {0xb970b359, 0xbb2fb930, 0x3b638e39, 0x3daaaaab};
+static const uint32_t GAMMA1_P[8] = {0x3ad28b22, 0x3ba90c99, 0x3b91db14, 0x3d93ae7c,
+                                     0x3da82a34, 0x3ed2d411, 0x3ed87799, 0x3f800000};
+static const uint32_t GAMMALNB_P[8] = {0x3a1ebb94, 0xbaabeab1, 0x3b3ba883, 0xbbf164fd,
+                                       0x3ca89ed8, 0xbd89f07e, 0x3ea51a64, 0x3ed87730};
+static const uint32_t GAMMALNC_P[8] = {0x3e0c3c4f, 0xbe22d329, 0x3e2d4dab, 0xbe53c04f,
+                                       0x3e8a898b, 0xbecd27a8, 0x3f528d34, 0xbf13c468};
+static const uint32_t GAMMALN2_P[3] = {0x3a31fd69, 0xbb358701, 0x3daaaa94};
+
+EXPORT float o_stirling(float a0)
+{
+    if (isnan(a0)) return a0;
+    if (a0 > bf(0x420c28f3u)) return INFINITY;  /* Stirlinglargelim */
+    float w = 1.0f / a0;
+    w = w * horner(w, STIRLING_P, 4) + 1.0f;
+    float y = o_exp(-a0);
+    if (y == 0.0f) return INFINITY;
+    float z = a0 - 0.5f;
+    if (a0 >= bf(0x41d628f6u)) {  /* Stirlingsplitlim */
+        float v = o_pow(a0, z * 0.5f);
+        y *= v;
+        y *= v;
+    } else {
+        y *= o_pow(a0, z);
+    }
+    return y * (bf(0x40206c99u) * w);  /* Sqrt_2pi */
+}
+
+EXPORT float o_gamma(float a0)
+{
+    if (a0 == 0.0f) return copysignf(INFINITY, a0);
+    if (isnan(a0) || a0 == -INFINITY) return NAN;
+    if (a0 == INFINITY) return a0;
+    float x = a0, q = fabsf(x);
+    if (x < -33.0f) {
+        float st = o_stirling(q);
+        float p = floorf(q);
+        if (p == q) return NAN;
+        int iseven = (((int32_t)p) & 1) == 0;
+        float z = q - p;
+        if (z > 0.5f) {
+            p += 1.0f;
+            z = q - p;
+        }
+        z = q * o_sinpi(z);
+        if (z == 0.0f) return NAN;
+        st = bf(0x40490fdbu) / (fabsf(z) * st);
+        return iseven ? -st : st;
+    }
+    /* NT2 counts x down one by one; its product is +inf long before x = 64
+     * is reached (and from 2^24 on, x - 1 == x and the loop never ends) */
+    if (x > 64.0f) return INFINITY;
+    float z = 1.0f;
+    while (x >= 3.0f) {
+        x -= 1.0f;
+        z *= x;
+    }
+    while (x < 0.0f) {
+        z /= x;
+        x += 1.0f;
+    }
+    while (x < 2.0f) {
+        if (x == 0.0f) return NAN;
+        z /= x;
+        x += 1.0f;
+    }
+    if (x == 2.0f) return z;
+    x -= 2.0f;
+    return z * horner(x, GAMMA1_P, 8);
+}
+
+EXPORT float o_gammaln(float a0)
+{
+    if (a0 > bf(0x7bc3f8eau) || a0 == 0.0f) return INFINITY;  /* Maxgammaln */
+    float x = a0, q = fabsf(x);
+    if (x < 0.0f) {
+        if (q > bf(0x7bc3f8eau)) return NAN;
+        float w = o_gammaln(q);
+        float p = floorf(q);
+        if (p == q) return INFINITY;
+        float z = q - p;
+        if (z > 0.5f) {
+            p += 1.0f;
+            z = p - q;
+        }
+        z = q * o_sinpi(z);
+        if (z == 0.0f) return INFINITY;
+        return -o_log(bf(0x3ea2f983u) * fabsf(z)) - w;
+    }
+    if (x < 6.5f) {
+        float z = 1.0f, tx = x, nx = 0.0f;
+        if (x >= 1.5f) {
+            while (tx > 2.5f) {
+                nx = nx - 1.0f;
+                tx = x + nx;
+                z *= tx;
+            }
+            x += nx - 2.0f;
+            return x * horner(x, GAMMALNB_P, 8) + o_log(z);
+        }
+        if (x >= 1.25f) {
+            z *= x;
+            x = x - 1.0f;
+            return x * horner(x, GAMMALNB_P, 8) - o_log(z);
+        }
+        if (x >= 0.75f) {
+            x = x - 1.0f;
+            return x * horner(x, GAMMALNC_P, 8);
+        }
+        while (tx < 1.5f) {
+            if (tx == 0.0f) return INFINITY;
+            z *= tx;
+            nx = nx + 1.0f;
+            tx = x + nx;
+        }
+        x += nx - 2.0f;
+        float p = x * horner(x, GAMMALNB_P, 8);
+        return p - o_log(z);
+    }
+    float r = (x - 0.5f) * o_log(x) + (bf(0x3f6b3f8eu) - x);  /* Logsqrt2pi */
+    if (x <= 1.0e4f) {
+        float z = 1.0f / x;
+        float p = z * z;
+        r = z * horner(p, GAMMALN2_P, 3) + r;
+    }
+    return r;
+}
+
+/* exprecneg, exprecnegc EXP/generic/{exprecneg,exprecnegc}.hpp; sqrt1pm1
+ * EXP/generic/sqrt1pm1.hpp (compositions the front ends build as programs) */
+EXPORT float o_exprecneg(float a0) { return o_exp(-(1.0f / a0)); }
+EXPORT float o_exprecnegc(float a0) { return -o_expm1(-(1.0f / a0)); }
+EXPORT float o_sqrt1pm1(float a0)
+{
+    float t = sqrtf(1.0f + a0);
+    return (fabsf(a0) < 0.5f) ? a0 / (1.0f + t) : t - 1.0f;
+}
+
+/* realsqrt, reallog: EXP/generic/{realsqrt,reallog}.hpp (sqrt and log behind an assertion) */
+EXPORT float o_realsqrt(float a0) { return sqrtf(a0); }
+EXPORT float o_reallog(float a0) { return o_log(a0); }
+
+/* logspace_add, logspace_sub EXP/scalar/{logspace_add,logspace_sub}.hpp;
+ * NT2's max(a, b) is a > b ? a : b */
+EXPORT float o_logspace_add(float a0, float a1)
+{
+    float t = -fabsf(a0 - a1);
+    float r = (a0 > a1 ? a0 : a1) + o_log1p(o_exp(t));
+    return isnan(t) ? a0 + a1 : r;
+}
+EXPORT float o_logspace_sub(float a0, float a1)
+{
+    float x = a1 - a0;
+    float t = (x > -bf(0x3f317218u)) ? o_log(-o_expm1(x)) : o_log1p(-o_exp(x));
+    return a0 + t;
+}
+
 /* ------------------------------------------------- elementwise maps ---- */
 enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQRT, FN_EXP2 = 8, FN_EXP10,
        FN_EXPM1, FN_LOG2, FN_LOG10, FN_SIN, FN_COS, FN_TAN, FN_SINPI, FN_COSPI, FN_SINH, FN_COSH, FN_TANH,
        FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT, FN_COT, FN_SEC, FN_CSC, FN_SIND,
        FN_COSD, FN_TAND, FN_TANPI, FN_COTPI, FN_COTD, FN_SECPI, FN_CSCPI, FN_SECD, FN_CSCD, FN_SINC, FN_SINCPI,
        FN_ACOTD, FN_ASEC, FN_COTH, FN_SINHC, FN_ACSC, FN_ASECH, FN_ACOTH, FN_ACSCH,
+       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_STIRLING, FN_EXPRECNEG = 80, FN_EXPRECNEGC,
+       FN_SQRT1PM1,
        /* compositions of the above, oracle only (the front ends lower them to programs) */
        FN_SECH = 51, FN_CSCH, FN_ACOT, FN_ASIND, FN_ACOSD, FN_ATAND, FN_ASECD, FN_ACSCD, FN_ASINPI, FN_ACOSPI,
        FN_ATANPI, FN_INDEG, FN_INRAD };
@@ -957,6 +1159,15 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_ATANPI: y[i] = o_atanpi(a); break;
         case FN_INDEG: y[i] = o_indeg(a); break;
         case FN_INRAD: y[i] = o_inrad(a); break;
+        case FN_ERF: y[i] = o_erf(a); break;
+        case FN_ERFCX: y[i] = o_erfcx(a); break;
+        case FN_EXPX2: y[i] = o_expx2(a); break;
+        case FN_GAMMA: y[i] = o_gamma(a); break;
+        case FN_GAMMALN: y[i] = o_gammaln(a); break;
+        case FN_STIRLING: y[i] = o_stirling(a); break;
+        case FN_EXPRECNEG: y[i] = o_exprecneg(a); break;
+        case FN_EXPRECNEGC: y[i] = o_exprecnegc(a); break;
+        case FN_SQRT1PM1: y[i] = o_sqrt1pm1(a); break;
         default: y[i] = sqrtf(a); break;
         }
     }
@@ -993,6 +1204,25 @@ static double cosd_d(double a)
     if (r == 90.0 || r == 270.0) return 0.0;
     return cos(r * (M_PI / 180.0));
 }
+
+/* exp(x^2) erfc(x): the product below 2, the continued fraction of erfc above
+ * (A&S 7.1.14: exp(x^2) erfc(x) = (1/sqrt(pi)) 1/(x + 1/2/(x + 1/(x + 3/2/(x + ...))))) */
+static double erfcx_d(double a)
+{
+    if (a < 2.0) return exp(a * a) * erfc(a);
+    double f = a;
+    for (int k = 200; k >= 1; --k) f = a + (k * 0.5) / f;
+    return 1.0 / (f * sqrt(M_PI));
+}
+/* Stirling's formula sqrt(2 pi) x^(x - 1/2) e^-x (1 + 1/(12x) + ...) as NT2 defines it:
+ * tgamma(x) / x * x, i.e. Gamma(x) for the x NT2 uses it on, in logs to avoid overflow */
+static double stirling_d(double a)
+{
+    if (!(a > 0.0)) return NAN;
+    return exp(lgamma(a));
+}
+/* sqrt(1 + x) - 1 without cancellation */
+static double sqrt1pm1_d(double a) { return a / (1.0 + sqrt(1.0 + a)); }
 
 /* acot in degrees: 90 - atan|x| in degrees with x's sign (+-90 at +-0) */
 static double acotd_d(double a)
@@ -1070,6 +1300,15 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_ATANPI: y[i] = atan(a) / M_PI; break;
         case FN_INDEG: y[i] = a * (180.0 / M_PI); break;
         case FN_INRAD: y[i] = a * (M_PI / 180.0); break;
+        case FN_ERF: y[i] = erf(a); break;
+        case FN_ERFCX: y[i] = erfcx_d(a); break;
+        case FN_EXPX2: y[i] = exp(a * a); break;
+        case FN_GAMMA: y[i] = tgamma(a); break;
+        case FN_GAMMALN: y[i] = lgamma(a); break;
+        case FN_STIRLING: y[i] = stirling_d(a); break;
+        case FN_EXPRECNEG: y[i] = exp(-1.0 / a); break;
+        case FN_EXPRECNEGC: y[i] = -expm1(-1.0 / a); break;
+        case FN_SQRT1PM1: y[i] = sqrt1pm1_d(a); break;
         default: y[i] = sqrt(a); break;
         }
     }

@@ -26,7 +26,10 @@ FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, exp2=
           coth=45, sinhc=46, acsc=47, asech=48, acoth=49, acsch=50,
           # NT2's generic compositions of the functors above
           sech=51, csch=52, acot=53, asind=54, acosd=55, atand=56, asecd=57, acscd=58, asinpi=59, acospi=60,
-          atanpi=61, indeg=62, inrad=63)
+          atanpi=61, indeg=62, inrad=63,
+          erf=64, erfcx=65, expx2=66, gamma=67, gammaln=68, stirling=69,
+          exprecneg=80, exprecnegc=81, sqrt1pm1=82)
+SCALAR_ONLY = ("o_realsqrt", "o_reallog")
 
 
 def build():
@@ -53,7 +56,7 @@ def lib():
                   "o_log2", "o_log10", "o_sin", "o_cos", "o_tan", "o_sinpi", "o_cospi",
                   "o_sinh", "o_cosh", "o_tanh", "o_asin", "o_acos", "o_atan",
                   "o_asinh", "o_acosh", "o_atanh", "o_cbrt", "o_cot", "o_sec", "o_csc", "o_sind", "o_cosd", "o_tand",
-                  *("o_" + k for k, v in FN.items() if v >= 34)):
+                  *("o_" + k for k, v in FN.items() if v >= 34), *SCALAR_ONLY):
             getattr(L, f).restype = ctypes.c_float
             getattr(L, f).argtypes = [ctypes.c_float]
         L.o_map_f32.argtypes = [ctypes.c_int, _P, _P, _I64]
@@ -65,6 +68,9 @@ def lib():
         L.o_atan2.argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_atan2_f32.argtypes = [_P, _P, _P, _I64]
         L.o_atan2_f64.argtypes = [_P, _P, _P, _I64]
+        for f in ("o_logspace_add", "o_logspace_sub"):
+            getattr(L, f).restype = ctypes.c_float
+            getattr(L, f).argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_atan2d.restype = ctypes.c_float
         L.o_atan2d.argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_hypot.restype = ctypes.c_float

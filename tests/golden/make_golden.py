@@ -83,6 +83,16 @@ SOURCES = [
     ("modules/core/hyperbolic/unit/scalar/asech.cpp", 1, 200),
     ("modules/core/hyperbolic/unit/scalar/acsch.cpp", 1, 200),
     ("modules/core/hyperbolic/unit/scalar/acoth.cpp", 1, 200),
+    ("modules/core/euler/unit/scalar/erf.cpp", 1, 200),
+    ("modules/core/euler/unit/scalar/erfcx.cpp", 1, 200),
+    ("modules/core/euler/unit/scalar/gamma.cpp", 1, 200),
+    ("modules/core/euler/unit/scalar/gammaln.cpp", 1, 200),
+    ("modules/core/exponential/unit/scalar/expx2.cpp", 1, 200),
+    ("modules/core/exponential/unit/scalar/exprecneg.cpp", 1, 200),
+    ("modules/core/exponential/unit/scalar/exprecnegc.cpp", 1, 200),
+    ("modules/core/exponential/unit/scalar/sqrt1pm1.cpp", 1, 200),
+    ("modules/core/exponential/unit/scalar/realsqrt.cpp", 1, 200),
+    ("modules/core/exponential/unit/scalar/reallog.cpp", 1, 200),
 ]
 
 E = float(np.float32(math.e))
@@ -99,12 +109,13 @@ CONST = {
     "Threepio_4": float(np.uint32(0x4016cbe4).view(np.float32)),
     "Sqrt_2": float(np.uint32(0x3fb504f3).view(np.float32)), "Valmax": float(np.finfo(np.float32).max),
     "_45": 45.0, "_90": 90.0, "_135": 135.0, "_180": 180.0,
-    "Mindenormal": float(np.uint32(1).view(np.float32)),
+    "Mindenormal": float(np.uint32(1).view(np.float32)), "Mtwo": -2.0,
+    "Log_2": float(np.uint32(0x3f317218).view(np.float32)),
 }
 
 
 def _value(expr):
-    expr = expr.strip()
+    expr = re.sub(r"\s+<", "<", expr.strip())
     if expr.startswith("-nt2::"):  # a negated constant
         return -_value(expr[1:])
     m = re.fullmatch(r"(?:nt2|boost::simd)::(\w+)<\w+>\(\)", expr)
@@ -113,7 +124,7 @@ def _value(expr):
     m = re.fullmatch(r"[-+]?[0-9.]+[eE][-+]?[0-9]+", expr)
     if m:  # a bare double literal, converted to the float r_t
         return float(np.float32(float(expr)))
-    m = re.fullmatch(r"T\(([-+0-9.eE]+)\)", expr)
+    m = re.fullmatch(r"T\(\s*([-+0-9.eE]+)\s*\)", expr)
     if m:
         return float(np.float32(float(m.group(1))))
     m = re.fullmatch(r"nt2::One<\w+>\(\)\s*/\s*nt2::Exp_1<\w+>\(\)", expr)
@@ -138,20 +149,26 @@ def _value(expr):
     m = re.fullmatch(r"T\(2\)\s*/\s*\(nt2::Pi<\w+>\(\)\)", expr)
     if m:
         return float(np.float32(2.0) / np.float32(CONST["Pi"]))
-    m = re.fullmatch(r"nt2::rec\(nt2::Eps<\w+>\(\)\)", expr)
+    m = re.fullmatch(r"nt2::rec\(nt2::(Eps|Exp_1)<\w+>\(\)\)", expr)
     if m:
-        return float(np.float32(1.0) / np.float32(CONST["Eps"]))
+        return float(np.float32(1.0) / np.float32(CONST[m.group(1)]))
+    m = re.fullmatch(r"(nt2::\w+<\w+>\(\))\s*([-+])\s*(nt2::\w+<\w+>\(\))", expr)
+    if m:  # a sum or difference of two constants, in float
+        a, b = np.float32(_value(m.group(1))), np.float32(_value(m.group(3)))
+        return float(a + b if m.group(2) == "+" else a - b)
     raise ValueError(f"unhandled NT2 constant spelling: {expr!r}")
 
 
 PAT = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(\w+)\((.*?)\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 # two-argument functors: pow(a, b)
 ARG = r"((?:[^,()]|\([^()]*\))*)"
-PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2d?|hypot)\(" + ARG + r",\s*" + ARG + r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
+PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2d?|hypot|logspace_add|logspace_sub)\(" + ARG + r",\s*" + ARG + r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
             ("modules/core/trigonometric/unit/scalar/atan2.cpp", 47, 61),
             ("modules/boost/simd/base/unit/arithmetic/scalar/hypot.cpp", 42, 52),
-            ("modules/core/trigonometric/unit/scalar/atan2d.cpp", 46, 60)]
+            ("modules/core/trigonometric/unit/scalar/atan2d.cpp", 46, 60),
+            ("modules/core/exponential/unit/scalar/logspace_add.cpp", 1, 200),
+            ("modules/core/exponential/unit/scalar/logspace_sub.cpp", 1, 200)]
 # expected values that are themselves results of NT2 functors (sin(Pio_4)/Pio_4)
 # are left out: they would pin the oracle to itself
 SELF_REFERENCE = re.compile(r"nt2::(sin|sinpi|cos|exp)\(")
@@ -172,7 +189,7 @@ def main(root):
                             source=f"{rel}:{ln}"))
     for rel, lo, hi in SOURCES2:
         lines = open(os.path.join(root, rel)).read().splitlines()
-        for ln in range(lo, hi + 1):
+        for ln in range(lo, min(hi, len(lines)) + 1):
             m = PAT2.search(lines[ln - 1])
             if not m:
                 continue

@@ -1,0 +1,157 @@
+"""erf, erfcx, gamma, gammaln and the exponential extras (expx2, exprecneg,
+exprecnegc, sqrt1pm1; logspace_add, logspace_sub and the real* aliases as
+NT2's compositions) on the GPU.
+
+NT2 policy: bit-identical to the oracle's restatement of NT2's float
+algorithms.  Fast policy: against FP64 within the tolerances below, with
+NT2's NaN positions.  Where NT2's float algorithm loses accuracy the fast
+policy computes the function another way: erf above 2/3 and erfcx from the fast
+erfc tail, e^(x^2) and e^(-1/x) with the argument split exactly, sqrt1pm1
+without the cancelling branch, gamma with its product carried in float-float.
+gammaln follows NT2's algorithm in both policies; around Gamma's minimum
+(x = 1.46) its x B(x) - log(x) form cancels to 6.3 ulp, and on the negative
+axis its reflection cancels near the zeros and poles (an absolute error of a
+few ulp of the terms there).
+NT2's gamma steps x down one unit at a time; its product is +inf long before
+64 and the steps never end from 2^24 on, so both policies return +inf from 64.
+NT2's exp overflows from Maxlog (88.376) on, below log(FLT_MAX); results past
+e^Maxlog are +inf in both policies and are not compared with FP64.  NT2's
+expx2 is NaN from about 1.7e38 on (its 2m overflows while f is 0), and so is
+erfcx below -1.7e38; the fast policy returns +inf there.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import nt2_ulpdist, std_ulp
+
+pytestmark = pytest.mark.gpu
+
+DEVICE = ["erf", "erfcx", "expx2", "gamma", "gammaln", "exprecneg", "exprecnegc", "sqrt1pm1"]
+FAST_TOL = dict(erf=2.5, erfcx=3.0, expx2=2.0, gamma=3.5, gammaln=6.5, exprecneg=2.0, exprecnegc=2.5,
+                sqrt1pm1=2.0)
+
+
+def domain(fn, n, seed):
+    """Seeded inputs covering each function's bands and edges."""
+    rng = np.random.default_rng(seed)
+    if fn == "erf":
+        parts = [rng.uniform(-1, 1, n), rng.uniform(-6, 6, n), np.exp(rng.uniform(np.log(1e-30), 0, n))]
+    elif fn == "erfcx":
+        parts = [rng.uniform(-2, 2, n), rng.uniform(-9.5, 30, n), np.exp(rng.uniform(0, np.log(1e30), n))]
+    elif fn == "expx2":
+        parts = [rng.uniform(-9.5, 9.5, n), rng.uniform(-1, 1, n)]
+    elif fn == "gamma":
+        parts = [rng.uniform(0, 36, n), rng.uniform(-42, 0, n), np.exp(rng.uniform(np.log(1e-30), 0, n)),
+                 rng.integers(-40, 40, n).astype(np.float64)]
+    elif fn == "gammaln":
+        parts = [rng.uniform(0, 10, n), rng.uniform(-50, 0, n), np.exp(rng.uniform(np.log(1e-30), np.log(1e36), n))]
+    elif fn in ("exprecneg", "exprecnegc"):
+        parts = [rng.uniform(-2, 2, n), np.exp(rng.uniform(np.log(1e-3), np.log(1e30), n)) * rng.choice([-1.0, 1.0], n)]
+    else:  # sqrt1pm1
+        parts = [rng.uniform(-1, 1, n), np.exp(rng.uniform(np.log(1e-30), np.log(1e30), n)), rng.uniform(-1, 3, n)]
+    return np.concatenate(parts).astype(np.float32)
+
+
+SPECIALS = np.float32([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -1.0, 0.5, -0.5, 2.0, -2.0, 0.6666666, 0.6666667,
+                       3.0, 6.5, 1.5, 1.25, 0.75, 2.5, 9.4, 9.5, 16.0, 33.0, -33.0, -33.5, 35.0, 35.04, 36.0, 64.0,
+                       65.0, 1e4, 1e-45, 1e-38, 1e30, 3.4e38, -3.4e38, 16777216.0, 33554432.0])
+
+
+def _run(lib, dev, fn, x, prec):
+    tx = torch.from_numpy(x).to(dev)
+    ty = torch.empty_like(tx)
+    lib.map_f32(fn, tx, ty, precision=prec)
+    torch.cuda.synchronize()
+    return ty.cpu().numpy()
+
+
+def _same(a, b):
+    return (a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))
+
+
+@pytest.mark.parametrize("fn", DEVICE)
+def test_nt2_policy_bit_exact(lib, dev, oracle, fn):
+    x = np.concatenate([domain(fn, 1 << 17, 11), SPECIALS, -SPECIALS])
+    got = _run(lib, dev, fn, x, lib.PREC_NT2)
+    ref = oracle.map_f32(fn, x)
+    same = _same(got, ref)
+    assert same.all(), f"{(~same).sum()} differ, first at x={x[~same][:5]} got {got[~same][:5]} want {ref[~same][:5]}"
+
+
+@pytest.mark.parametrize("fn", DEVICE)
+def test_fast_policy_accuracy(lib, dev, oracle, fn):
+    x = np.concatenate([domain(fn, 1 << 17, 12), SPECIALS, -SPECIALS])
+    got = _run(lib, dev, fn, x, lib.PREC_FAST)
+    ref = oracle.map_f64(fn, x)
+    nt2 = oracle.map_f32(fn, x)
+    keep = ~(np.abs(x) > 1e38) if fn in ("expx2", "erfcx") else np.ones(x.shape, bool)
+    nan_got, nan_nt2 = np.isnan(got[keep]), np.isnan(nt2[keep])
+    assert np.array_equal(nan_got, nan_nt2), x[keep][nan_got != nan_nt2][:8]
+    maxexp = np.exp(np.float64(np.uint32(0x42b0c0a5).view(np.float32)))
+    m = np.isfinite(ref) & (np.abs(ref) >= np.finfo(np.float32).tiny) & (np.abs(ref) < maxexp) & ~np.isnan(nt2)
+    m &= np.abs(ref) < maxexp * (1 - 1e-5)  # results at the threshold round either way
+    dist = np.abs(x - np.round(np.where(np.isfinite(x), x, 0)))  # to the nearest integer
+    if fn == "gamma":  # within 1e-3 of a pole the float argument itself decides the value
+        m &= ~((x < 0) & (dist < 1e-3))
+    if fn == "gammaln":
+        # on the negative axis NT2's reflection -log|x sinpi(x)/pi| - gammaln(|x|) cancels near the zeros and
+        # the poles: there the error is absolute, a few ulp of the terms (which grow like |x| log|x|)
+        near = m & (x < 0) & ((np.abs(ref) <= 1.0) | (dist < 1e-3))
+        scale = np.maximum(1.0, np.abs(x[near]) * np.log1p(np.abs(x[near])))
+        assert (np.abs(got[near] - ref[near]) <= 5e-6 * scale).all()
+        m &= ~near
+    e = std_ulp(got[m], ref[m])
+    print(f"\n{fn}: fast policy vs FP64 max {e.max():.3f} mean {e.mean():.4f} ulp over {m.sum()} points")
+    assert e.max() <= FAST_TOL[fn], f"max {e.max()} ulp at x={x[m][np.argmax(e)]}"
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
+def test_golden_values(lib, dev, prec):
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
+    recs = [r for r in golden if r["fn"] in DEVICE]
+    assert len(recs) >= 55
+    for fn in sorted({r["fn"] for r in recs}):
+        rs = [r for r in recs if r["fn"] == fn]
+        got = _run(lib, dev, fn, np.float32([r["x"] for r in rs]), prec)
+        for g, r in zip(got, rs):
+            assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
+def test_logspace_and_real_aliases(lib, dev, oracle, prec):
+    from nt2_gb300 import expr as E
+    rng = np.random.default_rng(13)
+    a = np.concatenate([rng.uniform(-80, 80, 1 << 16), SPECIALS, SPECIALS]).astype(np.float32)
+    b = np.concatenate([rng.uniform(-80, 80, 1 << 16), SPECIALS, SPECIALS[::-1]]).astype(np.float32)
+    ta, tb = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+    outs = [torch.empty_like(ta) for _ in range(4)]
+    A, B = E.Table(ta), E.Table(tb)
+    E.assign(outs, [E.logspace_add(A, B), E.logspace_sub(A, B), E.realsqrt(E.abs_(A)), E.reallog(E.abs_(B))],
+             precision=prec)
+    got = [o.cpu().numpy() for o in outs]
+    L = oracle.lib()
+    want_add = np.float32([L.o_logspace_add(float(p), float(q)) for p, q in zip(a, b)])
+    want_sub = np.float32([L.o_logspace_sub(float(p), float(q)) for p, q in zip(a, b)])
+    if prec == 1:
+        assert _same(got[0], want_add).all() and _same(got[1], want_sub).all()
+        assert _same(got[2], oracle.map_f32("sqrt", np.abs(a))).all()
+        assert _same(got[3], oracle.map_f32("log", np.abs(b))).all()
+    else:
+        with np.errstate(invalid="ignore"):
+            ref = np.logaddexp(a.astype(np.float64), b.astype(np.float64))
+        m = np.isfinite(ref) & (np.abs(ref) > 1e-30) & np.isfinite(a) & np.isfinite(b)
+        assert std_ulp(got[0][m], ref[m]).max() <= 3.5
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
+    for name in ("logspace_add", "logspace_sub"):
+        recs = [r for r in golden if r["fn"] == name]
+        assert len(recs) >= 7
+        ta = torch.tensor([r["x"] for r in recs], dtype=torch.float32, device=dev)
+        tb = torch.tensor([r["y"] for r in recs], dtype=torch.float32, device=dev)
+        ty = torch.empty_like(ta)
+        E.assign([ty], [getattr(E, name)(E.Table(ta), E.Table(tb))], precision=prec)
+        for g, r in zip(ty.cpu().numpy(), recs):
+            assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)

@@ -17,7 +17,8 @@ FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1
          "asinh", "acosh", "atanh", "cbrt", "cot", "sec", "csc", "sind", "cosd", "tand",
          "tanpi", "cotpi", "cotd", "secpi", "cscpi", "secd", "cscd", "sinc", "sincpi", "acotd", "asec", "acsc",
          "asind", "acosd", "atand", "asecd", "acscd", "asinpi", "acospi", "atanpi", "acot", "indeg", "inrad",
-         "coth", "sinhc", "sech", "csch", "asech", "acsch", "acoth")
+         "coth", "sinhc", "sech", "csch", "asech", "acsch", "acoth",
+         "erf", "erfcx", "gamma", "gammaln", "expx2", "exprecneg", "exprecnegc", "sqrt1pm1", "realsqrt", "reallog")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
@@ -27,7 +28,8 @@ def test_oracle_matches_nt2_unit_tests(oracle, rec):
     assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (got, rec)
 
 
-@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("pow", "atan2", "atan2d", "hypot")],
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("pow", "atan2", "atan2d", "hypot", "logspace_add",
+                                                              "logspace_sub")],
                          ids=lambda r: f"{r['fn']}({r['x']},{r['y']})@{r['source'].split('/')[-1]}")
 def test_oracle_binary_matches_nt2_unit_tests(oracle, rec):
     got = getattr(oracle.lib(), "o_" + rec["fn"])(rec["x"], rec["y"])
