@@ -96,7 +96,7 @@ typedef enum nt2g_opcode {
     NT2G_OP_SINC = 113, NT2G_OP_SINCPI, NT2G_OP_ACOTD, NT2G_OP_ASEC, NT2G_OP_COTH, NT2G_OP_SINHC,
     NT2G_OP_ACSC = 119, NT2G_OP_ASECH, NT2G_OP_ACOTH, NT2G_OP_ACSCH,
     NT2G_OP_ERF = 123, NT2G_OP_ERFCX, NT2G_OP_EXPX2, NT2G_OP_GAMMA, NT2G_OP_GAMMALN, NT2G_OP_EXPRECNEG,
-    NT2G_OP_EXPRECNEGC, NT2G_OP_SQRT1PM1
+    NT2G_OP_EXPRECNEGC, NT2G_OP_SQRT1PM1, NT2G_OP_ERFINV, NT2G_OP_ERFCINV
 } nt2g_opcode;
 
 typedef struct nt2g_op {
@@ -298,6 +298,7 @@ nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8
  * 22 acos, 23 atan, 24 asinh, 25 acosh, 26 atanh, 27 cbrt, 28 cot, 29 sec, 30 csc, 31 sind,
  * 32 cosd, 33 tand, 34 tanpi, 35 cotpi, 36 cotd, 37 secpi, 38 cscpi, 39 secd, 40 cscd, 41 sinc,
  * 42 sincpi, 43 acotd, 44 asec, 45 coth, 46 sinhc, 47 acsc, 48 asech, 49 acoth, 50 acsch, 64 erf, 65 erfcx, 66 expx2, 67 gamma, 68 gammaln,
+ * 69 erfinv, 70 erfcinv,
  * 80 exprecneg, 81 exprecnegc, 82 sqrt1pm1. */
 nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision,
                          void *stream);

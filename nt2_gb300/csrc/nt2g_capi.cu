@@ -287,7 +287,8 @@ static int n_operands(int code)
     case NT2G_OP_ASEC: case NT2G_OP_COTH: case NT2G_OP_SINHC:
     case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:
     case NT2G_OP_ERF: case NT2G_OP_ERFCX: case NT2G_OP_EXPX2: case NT2G_OP_GAMMA: case NT2G_OP_GAMMALN:
-    case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: return 1;
+    case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: case NT2G_OP_ERFINV:
+    case NT2G_OP_ERFCINV: return 1;
     case NT2G_OP_ADD: case NT2G_OP_SUB: case NT2G_OP_MUL: case NT2G_OP_DIV: case NT2G_OP_MIN: case NT2G_OP_MAX:
     case NT2G_OP_LT: case NT2G_OP_GT: case NT2G_OP_LE: case NT2G_OP_GE: case NT2G_OP_EQ: case NT2G_OP_NE:
     case NT2G_OP_SELINC: case NT2G_OP_SELDEC: case NT2G_OP_ADDS: case NT2G_OP_POW:
@@ -313,7 +314,8 @@ static bool float_only(int code)
     case NT2G_OP_ASEC: case NT2G_OP_COTH: case NT2G_OP_SINHC:
     case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:
     case NT2G_OP_ERF: case NT2G_OP_ERFCX: case NT2G_OP_EXPX2: case NT2G_OP_GAMMA: case NT2G_OP_GAMMALN:
-    case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1:
+    case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: case NT2G_OP_ERFINV:
+    case NT2G_OP_ERFCINV:
         return true;
     default: return false;
     }
@@ -858,7 +860,7 @@ extern "C" nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_
 {
     NT2G_REQ_N(); NT2G_REQ(x); NT2G_REQ(y); NT2G_REQ_PREC();
     NT2G_REACH(x); NT2G_REACH(y);
-    NT2G_CHECK_ARG((fn >= 0 && fn <= 50) || (fn >= 64 && fn <= 68) || (fn >= 80 && fn <= 82), "nt2g_map_f32: unknown function %d", fn);
+    NT2G_CHECK_ARG((fn >= 0 && fn <= 50) || (fn >= 64 && fn <= 70) || (fn >= 80 && fn <= 82), "nt2g_map_f32: unknown function %d", fn);
     return launch_map(fn, x, y, n, precision, (cudaStream_t)stream);
 }
 

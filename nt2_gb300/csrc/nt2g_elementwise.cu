@@ -431,6 +431,8 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 66) return expx2<P>(a);
     if (FN == 67) return gamma<P>(a);
     if (FN == 68) return gammaln<P>(a);
+    if (FN == 69) return erfinv<P>(a);
+    if (FN == 70) return erfcinv<P>(a);
     if (FN == 80) return exprecneg<P>(a);
     if (FN == 81) return exprecnegc<P>(a);
     if (FN == 82) return sqrt1pm1<P>(a);
@@ -507,6 +509,8 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 66: NT2G_MAP(66); break;
     case 67: NT2G_MAP(67); break;
     case 68: NT2G_MAP(68); break;
+    case 69: NT2G_MAP(69); break;
+    case 70: NT2G_MAP(70); break;
     case 80: NT2G_MAP(80); break;
     case 81: NT2G_MAP(81); break;
     case 82: NT2G_MAP(82); break;
@@ -593,6 +597,8 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_EXPX2: return expx2<P>(a);
     case NT2G_OP_GAMMA: return gamma<P>(a);
     case NT2G_OP_GAMMALN: return gammaln<P>(a);
+    case NT2G_OP_ERFINV: return erfinv<P>(a);
+    case NT2G_OP_ERFCINV: return erfcinv<P>(a);
     case NT2G_OP_EXPRECNEG: return exprecneg<P>(a);
     case NT2G_OP_EXPRECNEGC: return exprecnegc<P>(a);
     case NT2G_OP_SQRT1PM1: return sqrt1pm1<P>(a);

@@ -199,6 +199,8 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_EXPX2: e = "nt2g::expx2<P>(" + A + ")"; break;
         case NT2G_OP_GAMMA: e = "nt2g::gamma<P>(" + A + ")"; break;
         case NT2G_OP_GAMMALN: e = "nt2g::gammaln<P>(" + A + ")"; break;
+        case NT2G_OP_ERFINV: e = "nt2g::erfinv<P>(" + A + ")"; break;
+        case NT2G_OP_ERFCINV: e = "nt2g::erfcinv<P>(" + A + ")"; break;
         case NT2G_OP_EXPRECNEG: e = "nt2g::exprecneg<P>(" + A + ")"; break;
         case NT2G_OP_EXPRECNEGC: e = "nt2g::exprecnegc<P>(" + A + ")"; break;
         case NT2G_OP_SQRT1PM1: e = "nt2g::sqrt1pm1<P>(" + A + ")"; break;

@@ -1696,6 +1696,58 @@ template <class P> NT2G_HD float sqrt1pm1(float a0)
     return (a0 == f_inf()) ? a0 : q;
 }
 
+// erfinv, erfcinv (euler/functions/scalar/erfinv.hpp, erfcinv.hpp, single_:
+// Giles' approximation): w = -log((1-x)(1+x)) (erfcinv: -log(x(2-x)) and
+// 1 - x as the argument), a degree-8 polynomial in w - 2.5 below 5, else a
+// degree-8 polynomial in sqrt(w) - 3 (erfcinv: a 5/5 rational in sqrt(w))
+// (details/erfinv_kernel.hpp); +-inf at the ends.  Fast: the same with FMAs
+// and 1 - x^2 (2x - x^2) rounded once.
+template <class P> NT2G_HD float erfinv1(float w)
+{
+    return horner<P>(w, bits_f(0x32f16588u), bits_f(0x34b84b36u), bits_f(0xb66c7357u), bits_f(0xb6935ac1u),
+                     bits_f(0x396532dbu), bits_f(0xbaa45408u), bits_f(0xbb88e4efu), bits_f(0x3e7c8f63u),
+                     bits_f(0x3fc02e2fu));
+}
+template <class P> NT2G_HD float erfinv2(float w)
+{
+    return horner<P>(w, bits_f(0xb951f09bu), bits_f(0x38d3b56bu), bits_f(0x3ab0dc72u), bits_f(0xbb70bde7u),
+                     bits_f(0x3bbc127bu), bits_f(0xbbf9c5d7u), bits_f(0x3c1aa57eu), bits_f(0x3f8036dbu),
+                     bits_f(0x40354f7eu));
+}
+template <class P> NT2G_HD float erfinv(float a0)
+{
+    const float q = P::exact ? P::mul(P::sub(1.0f, a0), P::add(a0, 1.0f)) : Fast::fma(-a0, a0, 1.0f);
+    float w = -log<P>(q);
+    if (w == f_inf()) return copysignf(1.0f, a0) * w;
+    if (w < 5.0f) return P::mul(a0, erfinv1<P>(P::sub(w, 2.5f)));
+    return P::mul(a0, erfinv2<P>(P::sub(P::sqrt(w), 3.0f)));
+}
+template <class P> NT2G_HD float erfcinv(float a0)
+{
+    const float a00 = P::sub(1.0f, a0);
+    const float q = P::exact ? P::mul(a0, P::sub(2.0f, a0))
+                             : ((a0 > 2.0f) ? f_nan() : Fast::fma(-a0, a0, Fast::add(a0, a0)));
+    float w = -log<P>(q);
+    if (w == f_inf()) return copysignf(1.0f, a00) * w;
+    if (w < 5.0f) return P::mul(a00, erfinv1<P>(P::sub(w, 2.5f)));
+    if (!P::exact && w < 16.0f)  // Fast: erfinv's second polynomial, where it holds, for both ends
+        return Fast::mul(a00, erfinv2<Fast>(Fast::sub(Fast::sqrt(w), 3.0f)));
+    w = P::sqrt(w);
+    const float num = horner<P>(w, bits_f(0x3b3a8aeeu), bits_f(0x3ba62c57u), bits_f(0xbc8bcf63u), bits_f(0x3c98e17cu),
+                                bits_f(0xbbaf8bfeu));
+    const float den = horner<P>(w, bits_f(0x321631b2u), bits_f(0x3b3a73c1u), bits_f(0x3ba9025fu), bits_f(0xbc5d80aau),
+                                bits_f(0x3c2f4022u));
+    float r = P::div(num, den);
+    if (!P::exact && r < 9.3f) {
+        // Fast: one Newton step on erfc(r) = t (t = x, or 2 - x exactly at the
+        // other end): r += (erfcx(r) - t e^(r^2)) sqrt(pi)/2, both factors
+        // accurate where erfc itself would underflow
+        const float t = (a00 > 0.0f) ? a0 : Fast::sub(2.0f, a0);
+        r = Fast::fma(Fast::fma(-t, expx2<Fast>(r), erfcx<Fast>(r)), 0.886226925f, r);
+    }
+    return copysignf(r, a00);
+}
+
 // gamma (euler/functions/scalar/gamma.hpp): below -33 the reflection with
 // Stirling's formula (scalar/stirling.hpp + details/stirling_kernel.hpp),
 // else x stepped into [2, 3) one unit at a time, the product of the steps

@@ -115,6 +115,8 @@ erfcx = _un("ERFCX")
 expx2 = _un("EXPX2")
 gamma = _un("GAMMA")
 gammaln = _un("GAMMALN")
+erfinv = _un("ERFINV")
+erfcinv = _un("ERFCINV")
 exprecneg = _un("EXPRECNEG")
 exprecnegc = _un("EXPRECNEGC")
 sqrt1pm1 = _un("SQRT1PM1")

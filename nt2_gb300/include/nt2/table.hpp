@@ -641,6 +641,8 @@ NT2G_UNARY(erfcx, NT2G_OP_ERFCX)
 NT2G_UNARY(expx2, NT2G_OP_EXPX2)
 NT2G_UNARY(gamma, NT2G_OP_GAMMA)
 NT2G_UNARY(gammaln, NT2G_OP_GAMMALN)
+NT2G_UNARY(erfinv, NT2G_OP_ERFINV)
+NT2G_UNARY(erfcinv, NT2G_OP_ERFCINV)
 NT2G_UNARY(exprecneg, NT2G_OP_EXPRECNEG)
 NT2G_UNARY(exprecnegc, NT2G_OP_EXPRECNEGC)
 NT2G_UNARY(sqrt1pm1, NT2G_OP_SQRT1PM1)

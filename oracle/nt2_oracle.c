@@ -1051,6 +1051,32 @@ EXPORT float o_gammaln(float a0)
     return r;
 }
 
+/* erfinv EUL/scalar/erfinv.hpp, erfcinv EUL/scalar/erfcinv.hpp (single_, Giles),
+ * kernels EUL/details/erfinv_kernel.hpp */
+static const uint32_t ERFINV1_P[9] = {0x32f16588, 0x34b84b36, 0xb66c7357, 0xb6935ac1, 0x396532db,
+                                      0xbaa45408, 0xbb88e4ef, 0x3e7c8f63, 0x3fc02e2f};
+static const uint32_t ERFINV2_P[9] = {0xb951f09b, 0x38d3b56b, 0x3ab0dc72, 0xbb70bde7, 0x3bbc127b,
+                                      0xbbf9c5d7, 0x3c1aa57e, 0x3f8036db, 0x40354f7e};
+static const uint32_t ERFCINV2_P[5] = {0x3b3a8aee, 0x3ba62c57, 0xbc8bcf63, 0x3c98e17c, 0xbbaf8bfe};
+static const uint32_t ERFCINV2_Q[5] = {0x321631b2, 0x3b3a73c1, 0x3ba9025f, 0xbc5d80aa, 0x3c2f4022};
+
+EXPORT float o_erfinv(float a0)
+{
+    float w = -o_log((1.0f - a0) * (a0 + 1.0f));
+    if (w == INFINITY) return copysignf(1.0f, a0) * w;
+    if (w < 5.0f) return a0 * horner(w - 2.5f, ERFINV1_P, 9);
+    return a0 * horner(sqrtf(w) - 3.0f, ERFINV2_P, 9);
+}
+EXPORT float o_erfcinv(float a0)
+{
+    float a00 = 1.0f - a0;
+    float w = -o_log(a0 * (2.0f - a0));
+    if (w == INFINITY) return copysignf(1.0f, a00) * w;
+    if (w < 5.0f) return a00 * horner(w - 2.5f, ERFINV1_P, 9);
+    w = sqrtf(w);
+    return copysignf(horner(w, ERFCINV2_P, 5) / horner(w, ERFCINV2_Q, 5), a00);
+}
+
 /* exprecneg, exprecnegc EXP/generic/{exprecneg,exprecnegc}.hpp; sqrt1pm1
  * EXP/generic/sqrt1pm1.hpp (compositions the front ends build as programs) */
 EXPORT float o_exprecneg(float a0) { return o_exp(-(1.0f / a0)); }
@@ -1086,7 +1112,7 @@ enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQR
        FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT, FN_COT, FN_SEC, FN_CSC, FN_SIND,
        FN_COSD, FN_TAND, FN_TANPI, FN_COTPI, FN_COTD, FN_SECPI, FN_CSCPI, FN_SECD, FN_CSCD, FN_SINC, FN_SINCPI,
        FN_ACOTD, FN_ASEC, FN_COTH, FN_SINHC, FN_ACSC, FN_ASECH, FN_ACOTH, FN_ACSCH,
-       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_STIRLING, FN_EXPRECNEG = 80, FN_EXPRECNEGC,
+       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_ERFINV, FN_ERFCINV, FN_EXPRECNEG = 80, FN_EXPRECNEGC,
        FN_SQRT1PM1,
        /* compositions of the above, oracle only (the front ends lower them to programs) */
        FN_SECH = 51, FN_CSCH, FN_ACOT, FN_ASIND, FN_ACOSD, FN_ATAND, FN_ASECD, FN_ACSCD, FN_ASINPI, FN_ACOSPI,
@@ -1164,7 +1190,8 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_EXPX2: y[i] = o_expx2(a); break;
         case FN_GAMMA: y[i] = o_gamma(a); break;
         case FN_GAMMALN: y[i] = o_gammaln(a); break;
-        case FN_STIRLING: y[i] = o_stirling(a); break;
+        case FN_ERFINV: y[i] = o_erfinv(a); break;
+        case FN_ERFCINV: y[i] = o_erfcinv(a); break;
         case FN_EXPRECNEG: y[i] = o_exprecneg(a); break;
         case FN_EXPRECNEGC: y[i] = o_exprecnegc(a); break;
         case FN_SQRT1PM1: y[i] = o_sqrt1pm1(a); break;
@@ -1214,12 +1241,26 @@ static double erfcx_d(double a)
     for (int k = 200; k >= 1; --k) f = a + (k * 0.5) / f;
     return 1.0 / (f * sqrt(M_PI));
 }
-/* Stirling's formula sqrt(2 pi) x^(x - 1/2) e^-x (1 + 1/(12x) + ...) as NT2 defines it:
- * tgamma(x) / x * x, i.e. Gamma(x) for the x NT2 uses it on, in logs to avoid overflow */
-static double stirling_d(double a)
+/* inverse error functions by Newton's method on erf / erfc in FP64 from a
+ * bracket-free start (the float algorithm's own result, refined) */
+static double erfinv_d(double y)
 {
-    if (!(a > 0.0)) return NAN;
-    return exp(lgamma(a));
+    if (!(fabs(y) <= 1.0)) return NAN;
+    if (fabs(y) == 1.0) return copysign(INFINITY, y);
+    double x = (double)o_erfinv((float)y);
+    if (!isfinite(x)) x = copysign(4.0, y);
+    for (int k = 0; k < 6; ++k) x -= (erf(x) - y) / (1.1283791670955126 * exp(-x * x));
+    return x;
+}
+static double erfcinv_d(double y)
+{
+    if (!(y >= 0.0 && y <= 2.0)) return NAN;
+    if (y == 0.0) return INFINITY;
+    if (y == 2.0) return -INFINITY;
+    double x = (double)o_erfcinv((float)y);
+    if (!isfinite(x)) x = y < 1.0 ? 10.0 : -4.0;
+    for (int k = 0; k < 8; ++k) x += (erfc(x) - y) / (1.1283791670955126 * exp(-x * x));
+    return x;
 }
 /* sqrt(1 + x) - 1 without cancellation */
 static double sqrt1pm1_d(double a) { return a / (1.0 + sqrt(1.0 + a)); }
@@ -1305,7 +1346,8 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_EXPX2: y[i] = exp(a * a); break;
         case FN_GAMMA: y[i] = tgamma(a); break;
         case FN_GAMMALN: y[i] = lgamma(a); break;
-        case FN_STIRLING: y[i] = stirling_d(a); break;
+        case FN_ERFINV: y[i] = erfinv_d(a); break;
+        case FN_ERFCINV: y[i] = erfcinv_d(a); break;
         case FN_EXPRECNEG: y[i] = exp(-1.0 / a); break;
         case FN_EXPRECNEGC: y[i] = -expm1(-1.0 / a); break;
         case FN_SQRT1PM1: y[i] = sqrt1pm1_d(a); break;

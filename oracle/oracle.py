@@ -27,7 +27,7 @@ FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, exp2=
           # NT2's generic compositions of the functors above
           sech=51, csch=52, acot=53, asind=54, acosd=55, atand=56, asecd=57, acscd=58, asinpi=59, acospi=60,
           atanpi=61, indeg=62, inrad=63,
-          erf=64, erfcx=65, expx2=66, gamma=67, gammaln=68, stirling=69,
+          erf=64, erfcx=65, expx2=66, gamma=67, gammaln=68, erfinv=69, erfcinv=70,
           exprecneg=80, exprecnegc=81, sqrt1pm1=82)
 SCALAR_ONLY = ("o_realsqrt", "o_reallog")
 

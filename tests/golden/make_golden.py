@@ -87,6 +87,8 @@ SOURCES = [
     ("modules/core/euler/unit/scalar/erfcx.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/gamma.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/gammaln.cpp", 1, 200),
+    ("modules/core/euler/unit/scalar/erfinv.cpp", 1, 200),
+    ("modules/core/euler/unit/scalar/erfcinv.cpp", 1, 200),
     ("modules/core/exponential/unit/scalar/expx2.cpp", 1, 200),
     ("modules/core/exponential/unit/scalar/exprecneg.cpp", 1, 200),
     ("modules/core/exponential/unit/scalar/exprecnegc.cpp", 1, 200),
@@ -124,6 +126,9 @@ def _value(expr):
     m = re.fullmatch(r"[-+]?[0-9.]+[eE][-+]?[0-9]+", expr)
     if m:  # a bare double literal, converted to the float r_t
         return float(np.float32(float(expr)))
+    m = re.fullmatch(r"T\(\s*1\s*-\s*([0-9.]+)\s*\)", expr)
+    if m:  # a double difference converted to T
+        return float(np.float32(1.0 - float(m.group(1))))
     m = re.fullmatch(r"T\(\s*([-+0-9.eE]+)\s*\)", expr)
     if m:
         return float(np.float32(float(m.group(1))))

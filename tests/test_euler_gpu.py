@@ -7,7 +7,9 @@ algorithms.  Fast policy: against FP64 within the tolerances below, with
 NT2's NaN positions.  Where NT2's float algorithm loses accuracy the fast
 policy computes the function another way: erf above 2/3 and erfcx from the fast
 erfc tail, e^(x^2) and e^(-1/x) with the argument split exactly, sqrt1pm1
-without the cancelling branch, gamma with its product carried in float-float.
+without the cancelling branch, gamma with its product carried in float-float,
+erfcinv with erfinv's second polynomial up to w = 16 and one Newton step on
+erfcx beyond it.
 gammaln follows NT2's algorithm in both policies; around Gamma's minimum
 (x = 1.46) its x B(x) - log(x) form cancels to 6.3 ulp, and on the negative
 axis its reflection cancels near the zeros and poles (an absolute error of a
@@ -30,9 +32,9 @@ from helpers import nt2_ulpdist, std_ulp
 
 pytestmark = pytest.mark.gpu
 
-DEVICE = ["erf", "erfcx", "expx2", "gamma", "gammaln", "exprecneg", "exprecnegc", "sqrt1pm1"]
+DEVICE = ["erf", "erfcx", "expx2", "gamma", "gammaln", "exprecneg", "exprecnegc", "sqrt1pm1", "erfinv", "erfcinv"]
 FAST_TOL = dict(erf=2.5, erfcx=3.0, expx2=2.0, gamma=3.5, gammaln=6.5, exprecneg=2.0, exprecnegc=2.5,
-                sqrt1pm1=2.0)
+                sqrt1pm1=2.0, erfinv=3.5, erfcinv=4.0)
 
 
 def domain(fn, n, seed):
@@ -49,6 +51,10 @@ def domain(fn, n, seed):
                  rng.integers(-40, 40, n).astype(np.float64)]
     elif fn == "gammaln":
         parts = [rng.uniform(0, 10, n), rng.uniform(-50, 0, n), np.exp(rng.uniform(np.log(1e-30), np.log(1e36), n))]
+    elif fn == "erfinv":
+        parts = [rng.uniform(-1, 1, n), 1 - np.exp(rng.uniform(np.log(1e-7), 0, n)), rng.uniform(-1.01, -0.99, n)]
+    elif fn == "erfcinv":
+        parts = [rng.uniform(0, 2, n), np.exp(rng.uniform(np.log(1e-38), 0, n)), 2 - np.exp(rng.uniform(np.log(1e-7), 0, n))]
     elif fn in ("exprecneg", "exprecnegc"):
         parts = [rng.uniform(-2, 2, n), np.exp(rng.uniform(np.log(1e-3), np.log(1e30), n)) * rng.choice([-1.0, 1.0], n)]
     else:  # sqrt1pm1

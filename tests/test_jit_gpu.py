@@ -34,7 +34,8 @@ _UNARY_F = ["NEG", "ABS", "SQR", "SQRT", "REC", "EXP", "LOG", "LOG1P", "ERFC", "
             "SINH", "COSH", "TANH", "ASIN", "ACOS", "ATAN", "ASINH", "ACOSH", "ATANH", "CBRT",
             "COT", "SEC", "CSC", "SIND", "COSD", "TAND", "TANPI", "COTPI", "COTD", "SECPI", "CSCPI", "SECD", "CSCD",
             "SINC", "SINCPI", "ACOTD", "ASEC", "COTH", "SINHC", "ACSC", "ASECH", "ACOTH", "ACSCH",
-            "ERF", "ERFCX", "EXPX2", "GAMMA", "GAMMALN", "EXPRECNEG", "EXPRECNEGC", "SQRT1PM1"]
+            "ERF", "ERFCX", "EXPX2", "GAMMA", "GAMMALN", "EXPRECNEG", "EXPRECNEGC", "SQRT1PM1",
+            "ERFINV", "ERFCINV"]
 _BINARY_F = ["ADD", "SUB", "MUL", "DIV", "MIN", "MAX", "POW", "ATAN2", "HYPOT"]
 _CMP = ["LT", "GT", "LE", "GE", "EQ", "NE"]
 

@@ -18,7 +18,7 @@ FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1
          "tanpi", "cotpi", "cotd", "secpi", "cscpi", "secd", "cscd", "sinc", "sincpi", "acotd", "asec", "acsc",
          "asind", "acosd", "atand", "asecd", "acscd", "asinpi", "acospi", "atanpi", "acot", "indeg", "inrad",
          "coth", "sinhc", "sech", "csch", "asech", "acsch", "acoth",
-         "erf", "erfcx", "gamma", "gammaln", "expx2", "exprecneg", "exprecnegc", "sqrt1pm1", "realsqrt", "reallog")
+         "erf", "erfcx", "gamma", "gammaln", "erfinv", "erfcinv", "expx2", "exprecneg", "exprecnegc", "sqrt1pm1", "realsqrt", "reallog")
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in FUNCS],
