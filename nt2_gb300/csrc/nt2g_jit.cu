@@ -137,10 +137,40 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
              (f32 ? "jit_ldf<FULL>(v" : "jit_ldb<FULL>(v") + std::to_string(k) + ", a.ptr[" + std::to_string(o.a) +
              "], i, cnt);\n";
     }
+    // normcdf(y) and normcdf(-y) in one program share one erfc core
+    // (normcdf_pair: bit-identical to the two calls in both policies, as
+    // |-c y| == |c y| and only the final select differs); the pair is emitted
+    // at the first of the two, the second is skipped
+    std::vector<int> partner(ops.size(), -1);
+    {
+        std::vector<int> ncdf_of(ops.size(), -1);  // argument value -> normcdf value
+        for (size_t k = 0; k < ops.size(); ++k)
+            if (ops[k].code == NT2G_OP_NORMCDF && ncdf_of[ops[k].a] < 0) ncdf_of[ops[k].a] = (int)k;
+        for (size_t k = 0; k < ops.size(); ++k) {
+            if (ops[k].code != NT2G_OP_NORMCDF || partner[k] >= 0) continue;
+            const nt2g_op &arg = ops[ops[k].a];
+            if (arg.code != NT2G_OP_NEG || arg.dtype != NT2G_F32) continue;
+            const int j = ncdf_of[arg.a];
+            if (j >= 0 && partner[j] < 0 && j != (int)k) {
+                partner[j] = (int)k;
+                partner[k] = j;
+            }
+        }
+    }
     for (size_t k = 0; k < ops.size(); ++k) {
         const nt2g_op &o = ops[k];
         const bool f32 = o.dtype == NT2G_F32;
         const bool u = logical[k] || !f32;  // uint32 lanes: uint8 data and logicals
+        if (partner[k] >= 0) {
+            const int p = partner[k];
+            if (p < (int)k) continue;  // emitted with its partner
+            // the positive side is the one whose argument is y itself
+            const bool k_is_neg = ops[o.a].code == NT2G_OP_NEG && ops[o.a].a == ops[p].a;
+            const int pos = k_is_neg ? p : (int)k, neg = k_is_neg ? (int)k : p;
+            s += "    float v" + std::to_string(k) + "[4], v" + std::to_string(p) + "[4]; NT2G_L nt2g::normcdf_pair<P>(" +
+                 v(ops[pos].a) + ", " + v(pos) + ", " + v(neg) + ");\n";
+            continue;
+        }
         const std::string A = o.a >= 0 ? v(o.a) : "", B = o.b >= 0 ? v(o.b) : "", C = o.c >= 0 ? v(o.c) : "";
         const std::string slot = std::to_string(o.a);
         std::string e;

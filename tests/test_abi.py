@@ -219,6 +219,8 @@ def test_compiled_kernel_source_builds_for_sm103a(lib):
             src = prog.jit_source(prec)
             assert 'extern "C" __global__' in src and "nt2g_jit_kernel" in src
             assert ("nt2g::Nt2" if prec == lib.PREC_NT2 else "nt2g::Fast") in src
+            if prog is bs:  # N(d1)/N(-d1) and N(d2)/N(-d2) each from one erfc core
+                assert src.count("nt2g::normcdf_pair<P>(") == 2 and "nt2g::normcdf<P>(" not in src
             rc, log, size = _nvrtc_compile(nv, src)
             assert rc == 0, log[:2000]
             assert size > 0
