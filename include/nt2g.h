@@ -96,7 +96,10 @@ typedef enum nt2g_opcode {
     NT2G_OP_SINC = 113, NT2G_OP_SINCPI, NT2G_OP_ACOTD, NT2G_OP_ASEC, NT2G_OP_COTH, NT2G_OP_SINHC,
     NT2G_OP_ACSC = 119, NT2G_OP_ASECH, NT2G_OP_ACOTH, NT2G_OP_ACSCH,
     NT2G_OP_ERF = 123, NT2G_OP_ERFCX, NT2G_OP_EXPX2, NT2G_OP_GAMMA, NT2G_OP_GAMMALN, NT2G_OP_EXPRECNEG,
-    NT2G_OP_EXPRECNEGC, NT2G_OP_SQRT1PM1, NT2G_OP_ERFINV, NT2G_OP_ERFCINV
+    NT2G_OP_EXPRECNEGC, NT2G_OP_SQRT1PM1, NT2G_OP_ERFINV, NT2G_OP_ERFCINV,
+    NT2G_OP_FLOOR = 133, NT2G_OP_CEIL, NT2G_OP_TRUNC, NT2G_OP_ROUND, NT2G_OP_ROUND2EVEN, NT2G_OP_FRAC, NT2G_OP_SIGN,
+    NT2G_OP_SIGNNZ,
+    NT2G_OP_COPYSIGN = 141 /* copysign(a, b) (float)                    */
 } nt2g_opcode;
 
 typedef struct nt2g_op {

@@ -288,11 +288,13 @@ static int n_operands(int code)
     case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:
     case NT2G_OP_ERF: case NT2G_OP_ERFCX: case NT2G_OP_EXPX2: case NT2G_OP_GAMMA: case NT2G_OP_GAMMALN:
     case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: case NT2G_OP_ERFINV:
-    case NT2G_OP_ERFCINV: return 1;
+    case NT2G_OP_ERFCINV:
+    case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
+    case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: return 1;
     case NT2G_OP_ADD: case NT2G_OP_SUB: case NT2G_OP_MUL: case NT2G_OP_DIV: case NT2G_OP_MIN: case NT2G_OP_MAX:
     case NT2G_OP_LT: case NT2G_OP_GT: case NT2G_OP_LE: case NT2G_OP_GE: case NT2G_OP_EQ: case NT2G_OP_NE:
     case NT2G_OP_SELINC: case NT2G_OP_SELDEC: case NT2G_OP_ADDS: case NT2G_OP_POW:
-    case NT2G_OP_ATAN2: case NT2G_OP_HYPOT: return 2;
+    case NT2G_OP_ATAN2: case NT2G_OP_HYPOT: case NT2G_OP_COPYSIGN: return 2;
     case NT2G_OP_FMA: case NT2G_OP_FNMS: case NT2G_OP_IF_ELSE: return 3;
     default: return -1;
     }
@@ -316,6 +318,8 @@ static bool float_only(int code)
     case NT2G_OP_ERF: case NT2G_OP_ERFCX: case NT2G_OP_EXPX2: case NT2G_OP_GAMMA: case NT2G_OP_GAMMALN:
     case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: case NT2G_OP_ERFINV:
     case NT2G_OP_ERFCINV:
+    case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
+    case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: case NT2G_OP_COPYSIGN:
         return true;
     default: return false;
     }

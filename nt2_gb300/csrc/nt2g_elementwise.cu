@@ -599,6 +599,14 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_GAMMALN: return gammaln<P>(a);
     case NT2G_OP_ERFINV: return erfinv<P>(a);
     case NT2G_OP_ERFCINV: return erfcinv<P>(a);
+    case NT2G_OP_FLOOR: return floorf(a);
+    case NT2G_OP_CEIL: return ceilf(a);
+    case NT2G_OP_TRUNC: return truncf(a);
+    case NT2G_OP_ROUND: return roundf(a);
+    case NT2G_OP_ROUND2EVEN: return nt2_round2even(a);
+    case NT2G_OP_FRAC: return nt2_frac<P>(a);
+    case NT2G_OP_SIGN: return nt2_sign(a);
+    case NT2G_OP_SIGNNZ: return nt2_signnz(a);
     case NT2G_OP_EXPRECNEG: return exprecneg<P>(a);
     case NT2G_OP_EXPRECNEGC: return exprecnegc<P>(a);
     case NT2G_OP_SQRT1PM1: return sqrt1pm1<P>(a);
@@ -702,12 +710,13 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                     }
                 }
                 break;
-            case NT2G_OP_POW: case NT2G_OP_ATAN2: case NT2G_OP_HYPOT:
+            case NT2G_OP_POW: case NT2G_OP_ATAN2: case NT2G_OP_HYPOT: case NT2G_OP_COPYSIGN:
                 for (int j = 0; j < kV; ++j) {
                     const float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]);
                     d[j] = __float_as_uint(in.op == NT2G_OP_POW     ? pow<P>(x, y)
                                            : in.op == NT2G_OP_ATAN2 ? atan2<P>(x, y)
-                                                                    : hypot<P>(x, y));
+                                           : in.op == NT2G_OP_HYPOT ? hypot<P>(x, y)
+                                                                    : copysignf(x, y));
                 }
                 break;
             case NT2G_OP_FMA: case NT2G_OP_FNMS:

@@ -231,6 +231,15 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_GAMMALN: e = "nt2g::gammaln<P>(" + A + ")"; break;
         case NT2G_OP_ERFINV: e = "nt2g::erfinv<P>(" + A + ")"; break;
         case NT2G_OP_ERFCINV: e = "nt2g::erfcinv<P>(" + A + ")"; break;
+        case NT2G_OP_FLOOR: e = "floorf(" + A + ")"; break;
+        case NT2G_OP_CEIL: e = "ceilf(" + A + ")"; break;
+        case NT2G_OP_TRUNC: e = "truncf(" + A + ")"; break;
+        case NT2G_OP_ROUND: e = "roundf(" + A + ")"; break;
+        case NT2G_OP_ROUND2EVEN: e = "nt2g::nt2_round2even(" + A + ")"; break;
+        case NT2G_OP_FRAC: e = "nt2g::nt2_frac<P>(" + A + ")"; break;
+        case NT2G_OP_SIGN: e = "nt2g::nt2_sign(" + A + ")"; break;
+        case NT2G_OP_SIGNNZ: e = "nt2g::nt2_signnz(" + A + ")"; break;
+        case NT2G_OP_COPYSIGN: e = "copysignf(" + A + ", " + B + ")"; break;
         case NT2G_OP_EXPRECNEG: e = "nt2g::exprecneg<P>(" + A + ")"; break;
         case NT2G_OP_EXPRECNEGC: e = "nt2g::exprecnegc<P>(" + A + ")"; break;
         case NT2G_OP_SQRT1PM1: e = "nt2g::sqrt1pm1<P>(" + A + ")"; break;

@@ -1587,6 +1587,29 @@ template <class P> NT2G_HD float asec(float a0)
     return P::sub(bits_f(0x3fc90fdbu), asin<P>(P::div(1.0f, a0)));  // Pio_2
 }
 
+// ---------------------------------------------------- rounding, sign --
+// boost/simd arithmetic/functions/scalar/{floor,ceil,round}.hpp (::floorf,
+// ::ceilf, ::roundf), trunc = floor|x| with x's sign bit, round2even: |x| +
+// 2^23 - 2^23 below 2^23 (ties to even) with the sign of x < 0 (so -0 gives
+// +0), frac = x - trunc(x); ieee/functions/scalar/{sign,signnz,copysign}.hpp:
+// sign = (x > 0) - (x < 0) (NaN kept), signnz = +-1 by the sign bit (NaN
+// kept).  Exact in both policies.
+NT2G_HD float nt2_round2even(float a0)
+{
+    const float v = fabsf(a0);
+    const float d = (v < 8388608.0f) ? rintf(v) : v;
+    return (a0 < 0.0f) ? -d : d;
+}
+template <class P> NT2G_HD float nt2_frac(float a0) { return P::sub(a0, truncf(a0)); }
+NT2G_HD float nt2_sign(float a0)
+{
+    return is_nan(a0) ? a0 : (float)(a0 > 0.0f) - (float)(a0 < 0.0f);
+}
+NT2G_HD float nt2_signnz(float a0)
+{
+    return is_nan(a0) ? a0 : bits_f(0x3f800000u | (f_bits(a0) & 0x80000000u));
+}
+
 // ------------------------------------------------------------ euler --
 // erf2 kernel: erfc(x) e^(x^2) for x >= 2/3 as a polynomial in x/(1+x) - 0.4
 // (euler/functions/details/erf_kernel.hpp:48-66, the one erfc uses)

@@ -117,6 +117,28 @@ gamma = _un("GAMMA")
 gammaln = _un("GAMMALN")
 erfinv = _un("ERFINV")
 erfcinv = _un("ERFCINV")
+floor = _un("FLOOR")
+ceil = _un("CEIL")
+trunc = _un("TRUNC")
+round = _un("ROUND")
+round2even = _un("ROUND2EVEN")
+frac = _un("FRAC")
+sign = _un("SIGN")
+signnz = _un("SIGNNZ")
+fix = trunc
+
+
+def copysign(a, b): return _bin("COPYSIGN", a, b)
+
+
+# oneplus, oneminus, minusone, sqr_abs, dist, average: boost/simd/arithmetic/
+# functions/generic/{oneplus,oneminus,minusone,sqr_abs,average}.hpp, scalar/dist.hpp
+def oneplus(a): return a + 1.0
+def oneminus(a): return 1.0 - a
+def minusone(a): return a - 1.0
+def sqr_abs(a): return sqr(a)
+def dist(a, b): return abs_(a - b)
+def average(a, b): return fma(a, 0.5, b * 0.5)
 exprecneg = _un("EXPRECNEG")
 exprecnegc = _un("EXPRECNEGC")
 sqrt1pm1 = _un("SQRT1PM1")

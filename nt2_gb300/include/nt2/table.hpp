@@ -573,6 +573,7 @@ NT2G_BINARY(adds, NT2G_OP_ADDS, false)
 NT2G_BINARY(pow, NT2G_OP_POW, false)
 NT2G_BINARY(atan2, NT2G_OP_ATAN2, false)
 NT2G_BINARY(hypot, NT2G_OP_HYPOT, false)
+NT2G_BINARY(copysign, NT2G_OP_COPYSIGN, false)
 #undef NT2G_BINARY
 
 #define NT2G_UNARY(NAME, CODE)                                                                                   \
@@ -643,6 +644,14 @@ NT2G_UNARY(gamma, NT2G_OP_GAMMA)
 NT2G_UNARY(gammaln, NT2G_OP_GAMMALN)
 NT2G_UNARY(erfinv, NT2G_OP_ERFINV)
 NT2G_UNARY(erfcinv, NT2G_OP_ERFCINV)
+NT2G_UNARY(floor, NT2G_OP_FLOOR)
+NT2G_UNARY(ceil, NT2G_OP_CEIL)
+NT2G_UNARY(trunc, NT2G_OP_TRUNC)
+NT2G_UNARY(round, NT2G_OP_ROUND)
+NT2G_UNARY(round2even, NT2G_OP_ROUND2EVEN)
+NT2G_UNARY(frac, NT2G_OP_FRAC)
+NT2G_UNARY(sign, NT2G_OP_SIGN)
+NT2G_UNARY(signnz, NT2G_OP_SIGNNZ)
 NT2G_UNARY(exprecneg, NT2G_OP_EXPRECNEG)
 NT2G_UNARY(exprecnegc, NT2G_OP_EXPRECNEGC)
 NT2G_UNARY(sqrt1pm1, NT2G_OP_SQRT1PM1)
@@ -681,7 +690,25 @@ NT2G_COMPOSED(acscd, indeg(acsc(x)))
 NT2G_COMPOSED(asinpi, detail::f32_of_bits(0x3ea2f983u) * asin(x))
 NT2G_COMPOSED(acospi, detail::f32_of_bits(0x3ea2f983u) * acos(x))
 NT2G_COMPOSED(atanpi, detail::f32_of_bits(0x3ea2f983u) * atan(x))
+NT2G_COMPOSED(fix, trunc(x))
+NT2G_COMPOSED(oneplus, x + 1.0f)
+NT2G_COMPOSED(oneminus, 1.0f - x)
+NT2G_COMPOSED(minusone, x - 1.0f)
+NT2G_COMPOSED(sqr_abs, sqr(x))
 #undef NT2G_COMPOSED
+
+// dist = |a - b|, average = fma(a, 1/2, b/2) with NT2's fma (boost/simd/
+// arithmetic/functions/scalar/dist.hpp, generic/average.hpp)
+template <class A, class B, class T = typename detail::common<A, B>::type>
+expr<T> dist(const A &a, const B &b)
+{
+    return abs(a - b);
+}
+template <class A, class B, class T = typename detail::common<A, B>::type>
+expr<T> average(const A &a, const B &b)
+{
+    return fma(a, 0.5f, b * 0.5f);
+}
 
 template <class A, class B, class T = typename detail::common<A, B>::type>
 expr<T> atan2d(const A &a, const B &b)

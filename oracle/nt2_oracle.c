@@ -1087,6 +1087,32 @@ EXPORT float o_sqrt1pm1(float a0)
     return (fabsf(a0) < 0.5f) ? a0 / (1.0f + t) : t - 1.0f;
 }
 
+/* rounding and sign: BSIMD/arithmetic/functions/scalar/{floor,ceil,round,round2even,trunc}.hpp,
+ * BSIMD/ieee/functions/scalar/{frac,sign,signnz,copysign}.hpp; oneplus, oneminus, minusone, sqr_abs,
+ * dist, average: BSIMD/arithmetic/functions/{generic,scalar}/ */
+EXPORT float o_floor(float a0) { return floorf(a0); }
+EXPORT float o_ceil(float a0) { return ceilf(a0); }
+EXPORT float o_trunc(float a0) { return truncf(a0); }
+EXPORT float o_fix(float a0) { return truncf(a0); }
+EXPORT float o_round(float a0) { return roundf(a0); }
+EXPORT float o_round2even(float a0)
+{
+    float v = fabsf(a0), t2n = 8388608.0f;
+    float d = (v + t2n) - t2n;
+    d = (v < t2n) ? d : v;
+    return (a0 < 0.0f) ? -d : d;
+}
+EXPORT float o_frac(float a0) { return a0 - truncf(a0); }
+EXPORT float o_sign(float a0) { return isnan(a0) ? a0 : (float)(a0 > 0.0f) - (float)(a0 < 0.0f); }
+EXPORT float o_signnz(float a0) { return isnan(a0) ? a0 : bf(0x3f800000u | (fb(a0) & 0x80000000u)); }
+EXPORT float o_oneplus(float a0) { return a0 + 1.0f; }
+EXPORT float o_oneminus(float a0) { return 1.0f - a0; }
+EXPORT float o_minusone(float a0) { return a0 - 1.0f; }
+EXPORT float o_sqr_abs(float a0) { return a0 * a0; }
+EXPORT float o_copysign(float a0, float a1) { return copysignf(a0, a1); }
+EXPORT float o_dist(float a0, float a1) { return fabsf(a0 - a1); }
+EXPORT float o_average(float a0, float a1) { return a0 * 0.5f + a1 * 0.5f; }
+
 /* realsqrt, reallog: EXP/generic/{realsqrt,reallog}.hpp (sqrt and log behind an assertion) */
 EXPORT float o_realsqrt(float a0) { return sqrtf(a0); }
 EXPORT float o_reallog(float a0) { return o_log(a0); }

@@ -111,7 +111,8 @@ CONST = {
     "Threepio_4": float(np.uint32(0x4016cbe4).view(np.float32)),
     "Sqrt_2": float(np.uint32(0x3fb504f3).view(np.float32)), "Valmax": float(np.finfo(np.float32).max),
     "_45": 45.0, "_90": 90.0, "_135": 135.0, "_180": 180.0,
-    "Mindenormal": float(np.uint32(1).view(np.float32)), "Mtwo": -2.0,
+    "Mindenormal": float(np.uint32(1).view(np.float32)), "Mtwo": -2.0, "Maxflint": 16777216.0, "Valmin": -float(np.finfo(np.float32).max),
+    "Three": 3.0, "Four": 4.0, "Five": 5.0, "Mthree": -3.0,
     "Log_2": float(np.uint32(0x3f317218).view(np.float32)),
 }
 
@@ -157,7 +158,7 @@ def _value(expr):
     m = re.fullmatch(r"nt2::rec\(nt2::(Eps|Exp_1)<\w+>\(\)\)", expr)
     if m:
         return float(np.float32(1.0) / np.float32(CONST[m.group(1)]))
-    m = re.fullmatch(r"(nt2::\w+<\w+>\(\))\s*([-+])\s*(nt2::\w+<\w+>\(\))", expr)
+    m = re.fullmatch(r"((?:nt2|boost::simd)::\w+<\w+>\(\))\s*([-+])\s*((?:nt2|boost::simd)::\w+<\w+>\(\))", expr)
     if m:  # a sum or difference of two constants, in float
         a, b = np.float32(_value(m.group(1))), np.float32(_value(m.group(3)))
         return float(a + b if m.group(2) == "+" else a - b)
@@ -177,6 +178,38 @@ SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
 # expected values that are themselves results of NT2 functors (sin(Pio_4)/Pio_4)
 # are left out: they would pin the oracle to itself
 SELF_REFERENCE = re.compile(r"nt2::(sin|sinpi|cos|exp)\(")
+
+
+# exact functors: NT2_TEST_EQUAL(fn(args), expected) in the float (_real) test
+# case of boost.simd's unit tests (the integer cases are out of scope)
+EQ = re.compile(r"NT2_TEST_EQUAL\(\s*(\w+)\(" + r"((?:[^,()]|\([^()]*\))*)" + r"(?:,\s*((?:[^,()]|\([^()]*\))*))?\)\s*,\s*(.*?)\s*\);")
+EQ_SOURCES = [f"modules/boost/simd/base/unit/arithmetic/scalar/{f}.cpp" for f in
+              ("floor", "ceil", "trunc", "round", "round2even", "oneplus", "oneminus", "minusone", "dist", "average",
+               "sqr_abs")] + [f"modules/boost/simd/base/unit/ieee/scalar/{f}.cpp" for f in ("frac", "sign", "signnz",
+                                                                                           "copysign")]
+
+
+def _real_block_equalities(root, rel):
+    out, skipped, inside = [], 0, False
+    for ln, line in enumerate(open(os.path.join(root, rel)).read().splitlines(), 1):
+        if "NT2_TEST_CASE_TPL" in line:
+            inside = "_real" in line
+            continue
+        m = EQ.search(line) if inside else None
+        if not m:
+            continue
+        fn, a0, a1, exp = m.groups()
+        if (a1 is not None) != (fn in ("copysign", "dist", "average")):
+            continue  # another arity (round(x, n) rounds to n digits): not these functors
+        try:
+            rec = dict(fn=fn, x=_value(a0), expected=_value(exp), tol_nt2ulp=0.0, source=f"{rel}:{ln}")
+            if a1 is not None:
+                rec["y"] = _value(a1)
+        except (ValueError, KeyError):
+            skipped += 1
+            continue
+        out.append(rec)
+    return out, skipped
 
 
 def main(root):
@@ -201,6 +234,12 @@ def main(root):
             fn, a0, a1, exp, tol = m.groups()
             out.append(dict(fn=fn, x=_value(a0), y=_value(a1), expected=_value(exp), tol_nt2ulp=float(tol),
                             source=f"{rel}:{ln}"))
+    skipped = 0
+    for rel in EQ_SOURCES:
+        recs, k = _real_block_equalities(root, rel)
+        out += recs
+        skipped += k
+    print(f"exact functors: {skipped} lines with expressions this parser does not evaluate were left out")
     # normcdf on _(-5, 1, 5) against the 11-value table r0, 5 NT2-ulp
     rel = "modules/core/statistics/unit/scalar/normcdf.cpp"
     lines = open(os.path.join(root, rel)).read().splitlines()

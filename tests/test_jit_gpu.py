@@ -35,8 +35,8 @@ _UNARY_F = ["NEG", "ABS", "SQR", "SQRT", "REC", "EXP", "LOG", "LOG1P", "ERFC", "
             "COT", "SEC", "CSC", "SIND", "COSD", "TAND", "TANPI", "COTPI", "COTD", "SECPI", "CSCPI", "SECD", "CSCD",
             "SINC", "SINCPI", "ACOTD", "ASEC", "COTH", "SINHC", "ACSC", "ASECH", "ACOTH", "ACSCH",
             "ERF", "ERFCX", "EXPX2", "GAMMA", "GAMMALN", "EXPRECNEG", "EXPRECNEGC", "SQRT1PM1",
-            "ERFINV", "ERFCINV"]
-_BINARY_F = ["ADD", "SUB", "MUL", "DIV", "MIN", "MAX", "POW", "ATAN2", "HYPOT"]
+            "ERFINV", "ERFCINV", "FLOOR", "CEIL", "TRUNC", "ROUND", "ROUND2EVEN", "FRAC", "SIGN", "SIGNNZ"]
+_BINARY_F = ["ADD", "SUB", "MUL", "DIV", "MIN", "MAX", "POW", "ATAN2", "HYPOT", "COPYSIGN"]
 _CMP = ["LT", "GT", "LE", "GE", "EQ", "NE"]
 
 
