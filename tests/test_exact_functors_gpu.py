@@ -67,7 +67,6 @@ def test_binary(lib, dev, oracle, fn, prec):
     want = np.float32([f(float(p), float(q)) for p, q in zip(a, b)])
     if fn == "average" and prec == 0:  # fused: within half an ulp of NT2's twice-rounded form
         with np.errstate(invalid="ignore"):
-            with np.errstate(invalid="ignore"):
             ok = _same(got, want) | (np.abs(got.astype(np.float64) - want) <= np.spacing(np.abs(want)))
     else:
         ok = _same(got, want)
