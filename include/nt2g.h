@@ -99,7 +99,11 @@ typedef enum nt2g_opcode {
     NT2G_OP_EXPRECNEGC, NT2G_OP_SQRT1PM1, NT2G_OP_ERFINV, NT2G_OP_ERFCINV,
     NT2G_OP_FLOOR = 133, NT2G_OP_CEIL, NT2G_OP_TRUNC, NT2G_OP_ROUND, NT2G_OP_ROUND2EVEN, NT2G_OP_FRAC, NT2G_OP_SIGN,
     NT2G_OP_SIGNNZ,
-    NT2G_OP_COPYSIGN = 141 /* copysign(a, b) (float)                    */
+    NT2G_OP_COPYSIGN = 141, /* copysign(a, b) (float)                   */
+    /* predicates of a float -> logical (boost/simd predicates: is_nan, is_inf, is_finite = x - x == 0,
+       is_eqz, is_nez, is_ltz, is_gtz) */
+    NT2G_OP_IS_NAN = 142, NT2G_OP_IS_INF, NT2G_OP_IS_FINITE, NT2G_OP_IS_EQZ, NT2G_OP_IS_NEZ, NT2G_OP_IS_LTZ,
+    NT2G_OP_IS_GTZ
 } nt2g_opcode;
 
 typedef struct nt2g_op {

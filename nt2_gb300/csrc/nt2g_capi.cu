@@ -290,7 +290,9 @@ static int n_operands(int code)
     case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: case NT2G_OP_ERFINV:
     case NT2G_OP_ERFCINV:
     case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
-    case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: return 1;
+    case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ:
+    case NT2G_OP_IS_NAN: case NT2G_OP_IS_INF: case NT2G_OP_IS_FINITE: case NT2G_OP_IS_EQZ: case NT2G_OP_IS_NEZ:
+    case NT2G_OP_IS_LTZ: case NT2G_OP_IS_GTZ: return 1;
     case NT2G_OP_ADD: case NT2G_OP_SUB: case NT2G_OP_MUL: case NT2G_OP_DIV: case NT2G_OP_MIN: case NT2G_OP_MAX:
     case NT2G_OP_LT: case NT2G_OP_GT: case NT2G_OP_LE: case NT2G_OP_GE: case NT2G_OP_EQ: case NT2G_OP_NE:
     case NT2G_OP_SELINC: case NT2G_OP_SELDEC: case NT2G_OP_ADDS: case NT2G_OP_POW:
@@ -320,12 +322,17 @@ static bool float_only(int code)
     case NT2G_OP_ERFCINV:
     case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
     case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: case NT2G_OP_COPYSIGN:
+    case NT2G_OP_IS_NAN: case NT2G_OP_IS_INF: case NT2G_OP_IS_FINITE: case NT2G_OP_IS_EQZ: case NT2G_OP_IS_NEZ:
+    case NT2G_OP_IS_LTZ: case NT2G_OP_IS_GTZ:
         return true;
     default: return false;
     }
 }
 
-static bool is_compare(int code) { return code >= NT2G_OP_LT && code <= NT2G_OP_NE; }
+static bool is_compare(int code)
+{
+    return (code >= NT2G_OP_LT && code <= NT2G_OP_NE) || (code >= NT2G_OP_IS_NAN && code <= NT2G_OP_IS_GTZ);
+}
 
 // Structural match of program value v against pattern node pn.
 struct Matcher {

@@ -743,6 +743,21 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                     d[j] = r ? 1u : 0u;
                 }
                 break;
+            case NT2G_OP_IS_NAN: case NT2G_OP_IS_INF: case NT2G_OP_IS_FINITE: case NT2G_OP_IS_EQZ:
+            case NT2G_OP_IS_NEZ: case NT2G_OP_IS_LTZ: case NT2G_OP_IS_GTZ:
+#pragma unroll
+                for (int j = 0; j < kV; ++j) {
+                    const float x = __uint_as_float(A[j]);
+                    const bool r = in.op == NT2G_OP_IS_NAN      ? x != x
+                                 : in.op == NT2G_OP_IS_INF      ? fabsf(x) == f_inf()
+                                 : in.op == NT2G_OP_IS_FINITE   ? (x - x) == 0.0f
+                                 : in.op == NT2G_OP_IS_EQZ      ? x == 0.0f
+                                 : in.op == NT2G_OP_IS_NEZ      ? x != 0.0f
+                                 : in.op == NT2G_OP_IS_LTZ      ? x < 0.0f
+                                                                : x > 0.0f;
+                    d[j] = r ? 1u : 0u;
+                }
+                break;
             case NT2G_OP_IF_ELSE:
 #pragma unroll
                 for (int j = 0; j < kV; ++j) d[j] = A[j] ? B[j] : C[j];

@@ -240,6 +240,13 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_SIGN: e = "nt2g::nt2_sign(" + A + ")"; break;
         case NT2G_OP_SIGNNZ: e = "nt2g::nt2_signnz(" + A + ")"; break;
         case NT2G_OP_COPYSIGN: e = "copysignf(" + A + ", " + B + ")"; break;
+        case NT2G_OP_IS_NAN: e = "(" + A + " != " + A + ") ? 1u : 0u"; break;
+        case NT2G_OP_IS_INF: e = "(fabsf(" + A + ") == __int_as_float(0x7f800000)) ? 1u : 0u"; break;
+        case NT2G_OP_IS_FINITE: e = "((" + A + " - " + A + ") == 0.0f) ? 1u : 0u"; break;
+        case NT2G_OP_IS_EQZ: e = "(" + A + " == 0.0f) ? 1u : 0u"; break;
+        case NT2G_OP_IS_NEZ: e = "(" + A + " != 0.0f) ? 1u : 0u"; break;
+        case NT2G_OP_IS_LTZ: e = "(" + A + " < 0.0f) ? 1u : 0u"; break;
+        case NT2G_OP_IS_GTZ: e = "(" + A + " > 0.0f) ? 1u : 0u"; break;
         case NT2G_OP_EXPRECNEG: e = "nt2g::exprecneg<P>(" + A + ")"; break;
         case NT2G_OP_EXPRECNEGC: e = "nt2g::exprecnegc<P>(" + A + ")"; break;
         case NT2G_OP_SQRT1PM1: e = "nt2g::sqrt1pm1<P>(" + A + ")"; break;

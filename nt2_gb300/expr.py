@@ -128,6 +128,15 @@ signnz = _un("SIGNNZ")
 fix = trunc
 
 
+# predicates (boost/simd/predicates/functions): logical results for if_else
+def _pred(op):
+    return lambda a: Node(op, (a,), a.dtype)
+
+
+is_nan, is_inf, is_finite = _pred("IS_NAN"), _pred("IS_INF"), _pred("IS_FINITE")
+is_eqz, is_nez, is_ltz, is_gtz = _pred("IS_EQZ"), _pred("IS_NEZ"), _pred("IS_LTZ"), _pred("IS_GTZ")
+
+
 def copysign(a, b): return _bin("COPYSIGN", a, b)
 
 
@@ -245,7 +254,7 @@ def adds(a, b): return _bin("ADDS", a, b)
 
 
 def if_else(c, a, b):
-    dt = a.dtype if isinstance(a, Node) else b.dtype
+    dt = a.dtype if isinstance(a, Node) else b.dtype if isinstance(b, Node) else lib.F32
     return Node("IF_ELSE", (c, _wrap(a, dt), _wrap(b, dt)), dt)
 
 
@@ -367,6 +376,10 @@ def logspace(l, u, n=50, regular=False):
     return exp10(Node("FMA", (_index(n), _wrap(float(step), lib.F32), _wrap(float(lower), lib.F32)), lib.F32))
 
 
+_LOGICAL_OPS = ("LT", "GT", "LE", "GE", "EQ", "NE", "IS_NAN", "IS_INF", "IS_FINITE", "IS_EQZ", "IS_NEZ", "IS_LTZ",
+                "IS_GTZ")
+
+
 def _compare_dtype(n):
     return n.args[0].dtype
 
@@ -401,7 +414,7 @@ def lower(outs, exprs):
             ops.append((lib.OP["INDEX"], n.dtype, -1, -1, -1, 0.0))
         else:
             a = [emit(x) for x in n.args] + [-1, -1, -1]
-            dt = _compare_dtype(n) if n.op in ("LT", "GT", "LE", "GE", "EQ", "NE") else n.dtype
+            dt = _compare_dtype(n) if n.op in _LOGICAL_OPS else n.dtype
             ops.append((lib.OP[n.op], dt, a[0], a[1], a[2], 0.0))
         memo[id(n)] = len(ops) - 1
         return memo[id(n)]

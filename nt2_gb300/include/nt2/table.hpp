@@ -576,6 +576,22 @@ NT2G_BINARY(hypot, NT2G_OP_HYPOT, false)
 NT2G_BINARY(copysign, NT2G_OP_COPYSIGN, false)
 #undef NT2G_BINARY
 
+// predicates (boost/simd/predicates/functions): logical results for if_else
+#define NT2G_PREDICATE(NAME, CODE)                                                                               \
+    template <class A, class T = typename detail::elem_of<std::decay_t<A>>::type>                               \
+    expr<T> NAME(const A &a)                                                                                     \
+    {                                                                                                            \
+        return expr<T>{detail::make(CODE, detail::dtype_of<T>::value, detail::lift(a)), true};                   \
+    }
+NT2G_PREDICATE(is_nan, NT2G_OP_IS_NAN)
+NT2G_PREDICATE(is_inf, NT2G_OP_IS_INF)
+NT2G_PREDICATE(is_finite, NT2G_OP_IS_FINITE)
+NT2G_PREDICATE(is_eqz, NT2G_OP_IS_EQZ)
+NT2G_PREDICATE(is_nez, NT2G_OP_IS_NEZ)
+NT2G_PREDICATE(is_ltz, NT2G_OP_IS_LTZ)
+NT2G_PREDICATE(is_gtz, NT2G_OP_IS_GTZ)
+#undef NT2G_PREDICATE
+
 #define NT2G_UNARY(NAME, CODE)                                                                                   \
     template <class A, class T = typename detail::elem_of<std::decay_t<A>>::type>                               \
     expr<T> NAME(const A &a)                                                                                     \

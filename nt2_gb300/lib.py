@@ -32,6 +32,7 @@ OP = dict(
     TANPI=106, COTPI=107, COTD=108, SECPI=109, CSCPI=110, SECD=111, CSCD=112, SINC=113, SINCPI=114, ACOTD=115, ASEC=116, COTH=117, SINHC=118, ACSC=119, ASECH=120, ACOTH=121, ACSCH=122,
     ERF=123, ERFCX=124, EXPX2=125, GAMMA=126, GAMMALN=127, EXPRECNEG=128, EXPRECNEGC=129, SQRT1PM1=130, ERFINV=131, ERFCINV=132,
     FLOOR=133, CEIL=134, TRUNC=135, ROUND=136, ROUND2EVEN=137, FRAC=138, SIGN=139, SIGNNZ=140, COPYSIGN=141,
+    IS_NAN=142, IS_INF=143, IS_FINITE=144, IS_EQZ=145, IS_NEZ=146, IS_LTZ=147, IS_GTZ=148,
 )
 
 MAP_FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, normcdf_neg=7, exp2=8, exp10=9,

@@ -83,3 +83,26 @@ def test_golden_values(lib, dev, prec):
         xs = [np.float32([arg(r["x"])])] + ([np.float32([arg(r["y"])])] if "y" in r else [])
         got = _eval(dev, lambda E, *t: getattr(E, r["fn"])(*t), xs, prec)[0]
         assert nt2_ulpdist(got, r["expected"]) <= r["tol_nt2ulp"], (r, got)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["fused-or-jit", "jit", "interp"])
+def test_predicates(lib, dev, mode):
+    """is_nan, is_inf, is_finite (NT2: x - x == 0), is_eqz, is_nez, is_ltz, is_gtz as logical values: selected
+    by if_else and stored directly (0.0 / 1.0), identical in the compiled kernel and the interpreter."""
+    from nt2_gb300 import expr as E
+    x = _inputs(24)
+    tx = torch.from_numpy(x).to(dev)
+    names = ["is_nan", "is_inf", "is_finite", "is_eqz", "is_nez", "is_ltz", "is_gtz"]
+    with np.errstate(invalid="ignore"):
+        want = {"is_nan": np.isnan(x), "is_inf": np.isinf(x), "is_finite": np.isfinite(x), "is_eqz": x == 0,
+                "is_nez": x != 0, "is_ltz": x < 0, "is_gtz": x > 0}
+    outs = [torch.empty_like(tx) for _ in range(2 * len(names))]
+    X = E.Table(tx)
+    exprs = []
+    for n in names:
+        exprs += [E.if_else(getattr(E, n)(X), 2.0, -3.0), getattr(E, n)(X)]
+    E.assign(outs, exprs, force_generic=mode)
+    for k, n in enumerate(names):
+        sel, raw = outs[2 * k].cpu().numpy(), outs[2 * k + 1].cpu().numpy()
+        assert np.array_equal(sel, np.where(want[n], 2.0, -3.0).astype(np.float32)), n
+        assert np.array_equal(raw, want[n].astype(np.float32)), n
