@@ -24,6 +24,7 @@ in HBM.  Workloads (--config):
   fold_col / fold_row / gmax   sum(A, 1), sum(A, 2), globalmax of a 16384^2 table
   cumsum_col / cumsum_all / cummax_row   cumulative functions on that table
   fn_trig / fn_pow / fn_gen   sin(x)*cos(y), pow(x, y), sinpi(linspace(0,2,n))*x
+  fn_special                  erf(y) + gammaln(x)
             over 2^26 elements through the compiled kernel
 Each prints one JSON line (rank 0).  --impl reference times NT2's CPU path
 (the oracle's restatement of it: NT2 itself needs Boost, absent here) on the
@@ -466,8 +467,8 @@ class Scan(Workload):
 class Functors(Workload):
     """A generic expression of the newer functors through the run-time compiled
     kernel (the path any user expression takes), fast policy, over 2^26-element
-    tables: sin(x) * cos(y), pow(x, y), or sinpi(linspace(0, 2, n)) * x (a
-    generative leaf: no input bytes for it)."""
+    tables: sin(x) * cos(y), pow(x, y), sinpi(linspace(0, 2, n)) * x (a
+    generative leaf: no input bytes for it), or erf(y) + gammaln(x)."""
 
     def __init__(self, torch, lib, dev, kind, precision, n=None):
         from nt2_gb300 import expr as E
@@ -478,15 +479,17 @@ class Functors(Workload):
         self.y = torch.rand(n, device=dev, generator=g) * 4 - 2
         self.out = torch.empty_like(self.x)
         X, Y = E.Table(self.x), E.Table(self.y)
-        e = {"trig": E.sin(X) * E.cos(Y), "pow": E.pow(X, Y), "gen": E.sinpi(E.linspace(0, 2, n)) * X}[kind]
+        e = {"trig": E.sin(X) * E.cos(Y), "pow": E.pow(X, Y), "gen": E.sinpi(E.linspace(0, 2, n)) * X,
+             "special": E.erf(Y) + E.gammaln(X)}[kind]
         prog, slots = E.compile_program([self.out], [e])
         prog.jit_prepare(precision)
         self.prog = prog
         self.args = (lib.Arg * len(slots))(*[lib.Arg(t.data_ptr(), 0.0, lib.F32, 0) for t in slots])
         self.nslots, self.n = len(slots), n
-        reads = {"trig": 8, "pow": 8, "gen": 4}[kind]
+        reads = {"trig": 8, "pow": 8, "gen": 4, "special": 8}[kind]
         self.units, self.bytes, self.kernel = n, (reads + 4) * n, "nt2g_jit_kernel"
-        self.name = {"trig": "sin(x) * cos(y)", "pow": "pow(x, y)", "gen": "sinpi(linspace(0, 2, n)) * x"}[kind] + \
+        self.name = {"trig": "sin(x) * cos(y)", "pow": "pow(x, y)", "gen": "sinpi(linspace(0, 2, n)) * x",
+                     "special": "erf(y) + gammaln(x)"}[kind] + \
             f" over {n} float32 elements, run-time compiled kernel"
         self.flush = "inputs larger than L2"
 
@@ -541,7 +544,7 @@ def make(name, torch, lib, dev, precision, tune=None, n=None):
         return Adjoint(torch, lib, dev)
     if name == "adjoint_fwd":
         return Adjoint(torch, lib, dev, forward_only=True)
-    if name in ("fn_trig", "fn_pow", "fn_gen"):
+    if name in ("fn_trig", "fn_pow", "fn_gen", "fn_special"):
         return Functors(torch, lib, dev, name[3:], precision, n)
     if name == "sigmadelta":
         return SigmaDelta(torch, lib, dev)
