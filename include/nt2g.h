@@ -336,7 +336,9 @@ nt2g_status nt2g_reduce_f32(const float *x, const float *y, int64_t n, void *wor
  * device array inside the library, held by every GPU that loads it until the
  * process exits; it never calls cudaMalloc or cudaFree.  The first call on a
  * device looks up that array's device address (with the device current);
- * make that first call before any stream capture.  All calls share the one
+ * make that first call before any stream capture.  The address is cached per
+ * device and context: after cudaDeviceReset the next call looks it up again
+ * in the new context (make that call before a capture too).  All calls share the one
  * array, so calls that overlap on the GPU (other streams, other threads) race
  * and must be serialised by the caller.  A launch that would need more block
  * partials than the array holds is rejected with NT2G_ERR_UNSUPPORTED.

@@ -237,10 +237,12 @@ static nt2g_status batch_launch(nt2g_batch *b, cudaStream_t st)
         k_batch<P, true><<<grid, threads, 0, st>>>(b->d_items, b->d_prefix, b->n_items, b->total_tiles,
                                                    b->tile_elems, b->d_counter);
     } else {
-        int per_sm = -b->tune.blocks_per_sm;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<P, false>, threads, 0) != cudaSuccess ||
-            per_sm < 1)
-            per_sm = 1;
+        // -blocks_per_sm resident blocks per SM, capped by what the SM holds
+        int per_sm = -b->tune.blocks_per_sm, limit = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&limit, k_batch<P, false>, threads, 0) != cudaSuccess ||
+            limit < 1)
+            limit = 1;
+        if (per_sm < 1 || per_sm > limit) per_sm = limit;
         grid = device_sm_count() * per_sm;
         k_batch<P, false><<<grid, threads, 0, st>>>(b->d_items, b->d_prefix, b->n_items, b->total_tiles,
                                                     b->tile_elems, b->d_counter);

@@ -791,6 +791,10 @@ extern "C" nt2g_status nt2g_program_jit_prepare(const nt2g_program *p, int32_t p
 #define NT2G_REACH(ptr)                                                                                        \
     NT2G_CHECK_ARG(n == 0 || reachable(ptr), "%s: " #ptr " is host memory the device cannot access (pin or "   \
                    "register it)", __func__)
+// for what a kernel writes even when n == 0 (a reduction's result and workspace)
+#define NT2G_REACH_ALWAYS(ptr)                                                                                 \
+    NT2G_CHECK_ARG(reachable(ptr), "%s: " #ptr " is host memory the device cannot access (pin or register it)", \
+                   __func__)
 #define NT2G_REQ_N() NT2G_CHECK_ARG(n >= 0, "%s: negative size %lld", __func__, (long long)n)
 #define NT2G_REQ_PREC()                                                                                        \
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "%s: precision %d", __func__,     \
@@ -892,7 +896,8 @@ extern "C" nt2g_status nt2g_reduce_f32(const float *x, const float *y, int64_t n
     NT2G_CHECK_ARG(workspace != nullptr && workspace_bytes >= need,
                    "nt2g_reduce_f32: workspace of %zu bytes, %zu needed", workspace_bytes, need);
     NT2G_CHECK_ARG(((uintptr_t)workspace & 15u) == 0, "nt2g_reduce_f32: workspace not 16-byte aligned");
-    NT2G_REACH(x); NT2G_REACH(y); NT2G_REACH(workspace); NT2G_REACH(out64); NT2G_REACH(out32);
+    NT2G_REACH(x); NT2G_REACH(y);
+    NT2G_REACH_ALWAYS(workspace); NT2G_REACH_ALWAYS(out64); NT2G_REACH_ALWAYS(out32);
     return launch_reduce(x, y, n, workspace, out64, out32, (cudaStream_t)stream);
 }
 
@@ -901,7 +906,7 @@ extern "C" nt2g_status nt2g_reduce_f32_noalloc(const float *x, const float *y, i
 {
     NT2G_REQ_N(); NT2G_REQ(x);
     NT2G_CHECK_ARG(out64 != nullptr, "nt2g_reduce_f32_noalloc: out64 is NULL");
-    NT2G_REACH(x); NT2G_REACH(y); NT2G_REACH(out64); NT2G_REACH(out32);
+    NT2G_REACH(x); NT2G_REACH(y); NT2G_REACH_ALWAYS(out64); NT2G_REACH_ALWAYS(out32);
     return launch_reduce_noalloc(x, y, n, out64, out32, (cudaStream_t)stream);
 }
 

@@ -14,6 +14,7 @@
 // ticket after a release fence) adds the block partials in FP64 in a fixed
 // order.  The result is deterministic for a given n and device.  No block
 // ever waits on another.
+#include <cuda.h>
 #include <mutex>
 #include "nt2g_common.cuh"
 #include "nt2g_internal.h"
@@ -190,14 +191,46 @@ nt2g_status launch_reduce(const float *x, const float *y, int64_t n, void *ws, d
 // Every GPU that loads the library holds these 39,168 bytes until exit.
 static __device__ __align__(256) unsigned char g_reduce_scratch[kWsBytes];
 
+// Identity of the calling thread's current context, through the driver entry
+// points the runtime hands out (no link against the driver library).  Context
+// IDs are unique for the life of the process, so a context created after
+// cudaDeviceReset never matches the one an address was cached for.
+static bool current_context_id(unsigned long long *id)
+{
+    typedef CUresult (*get_current_t)(CUcontext *);
+    typedef CUresult (*get_id_t)(CUcontext, unsigned long long *);
+    static get_current_t get_current = nullptr;
+    static get_id_t get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (get_current_t)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (get_id_t)f;
+        cudaGetLastError();
+    });
+    CUcontext ctx = nullptr;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return get_id(ctx, id) == CUDA_SUCCESS;
+}
+
 // Device address of g_reduce_scratch for the current device.  Host code only
 // sees a host-side stand-in for the symbol, so the address is asked of the
-// runtime once per device (with that device current) and cached.
+// runtime with the device current and cached per device together with the
+// identity of the context it belongs to; a new context on that device (after
+// cudaDeviceReset) triggers a fresh lookup.  Without a context identity the
+// lookup runs on every call.
 static nt2g_status noalloc_scratch(void **out)
 {
     constexpr int kMaxDevices = 64;
     static std::mutex mu;
     static void *addr[kMaxDevices] = {};
+    static unsigned long long ctx_of[kMaxDevices] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_status(e, "nt2g_reduce_f32_noalloc: cudaGetDevice");
@@ -205,12 +238,18 @@ static nt2g_status noalloc_scratch(void **out)
         set_error("nt2g_reduce_f32_noalloc: device %d beyond the %d devices it tracks", dev, kMaxDevices);
         return NT2G_ERR_UNSUPPORTED;
     }
+    unsigned long long id = 0;
+    bool have_id = current_context_id(&id);
     std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
+    if (!have_id || !addr[dev] || ctx_of[dev] != id) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_reduce_scratch);
         if (e != cudaSuccess) return cuda_status(e, "nt2g_reduce_f32_noalloc: cudaGetSymbolAddress");
-        addr[dev] = p;
+        if (!have_id) have_id = current_context_id(&id);  // the lookup made the device's context current
+        addr[dev] = have_id ? p : nullptr;
+        ctx_of[dev] = id;
+        *out = p;
+        return NT2G_OK;
     }
     *out = addr[dev];
     return NT2G_OK;

@@ -1439,6 +1439,7 @@ static inline double ncdf64(double x) { return 0.5 * erfc(-x / sqrt(2.0)); }
 EXPORT void o_bs_f64(const float *S, const float *K, const float *T, const float *sig_tab, float sig,
                      float r, double *call, double *put, double *terms, int64_t n)
 {
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
         double s = S[i], k = K[i], t = T[i], v = sig_tab ? sig_tab[i] : sig, rr = r;
         double sq = sqrt(t);
@@ -1459,6 +1460,7 @@ EXPORT void o_bs_vjp_f64(const float *S, const float *K, const float *T, const f
                          double *dsig, double *dr, int64_t n)
 {
     const double inv_sqrt_2pi = 0.398942280401432677939946059934;
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
         double s = S[i], k = K[i], t = T[i], v = sig_tab ? sig_tab[i] : sig, rr = r;
         double sq = sqrt(t);
@@ -1486,6 +1488,7 @@ EXPORT void o_bs_vjp_scale_f64(const float *S, const float *K, const float *T, c
                                double *ssig, double *sr, int64_t n)
 {
     const double inv_sqrt_2pi = 0.398942280401432677939946059934;
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
         double s = S[i], k = K[i], t = T[i], v = sig_tab ? sig_tab[i] : sig, rr = r;
         double sq = sqrt(t);

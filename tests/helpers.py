@@ -87,6 +87,36 @@ def reduction_ill(n, seed=1001, target_cond=1e10):
     return x
 
 
+def reduction_ill_dot(n, seed=1001, target_cond=1e10):
+    """dot(x, y) with condition number sum|x*y| / |sum x*y| near target_cond:
+    over an x ~ N(0,1), y ~ N(0,1e-3) residue, pairs of positions carry
+    products that cancel exactly, (a, b) and (-a, b) with a = +-m 2^e,
+    b = m' 2^e' (m, m' ~ U[1,2), e, e' ~ U{-20..20}).  Float products are
+    exact in FP64, so the exact dot is the residue's."""
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(n).astype(F32)
+    y = (rng.standard_normal(n) * 1e-3).astype(F32)
+    p = x.astype(np.float64) * y.astype(np.float64)
+    total = float(np.sum(p))
+    absum = float(np.sum(np.abs(p)))
+    goal = target_cond * abs(total)
+    pos = rng.permutation(n)
+    k = 0
+    while absum < goal and 2 * k + 1 < n:
+        a = np.float32(np.ldexp(rng.uniform(1, 2), int(rng.integers(-20, 21)))) * (1 if rng.random() < 0.5 else -1)
+        b = np.float32(np.ldexp(rng.uniform(1, 2), int(rng.integers(-20, 21))))
+        mag = abs(float(a) * float(b))
+        if absum + 2 * mag > 2 * goal and mag > goal:
+            continue
+        i, j = pos[2 * k], pos[2 * k + 1]
+        total -= float(p[i]) + float(p[j])
+        absum -= abs(float(p[i])) + abs(float(p[j]))
+        x[i], y[i], x[j], y[j] = a, b, -a, b
+        absum += 2 * mag
+        k += 1
+    return x, y
+
+
 def sigmadelta_frames(h=1080, w=1920, frames=64, seed=1002, square=200, step=8):
     """uint8 frames ~ U[0,255] with a bright square moving `step` px per frame."""
     rng = np.random.default_rng(seed)

@@ -87,6 +87,66 @@ def test_vjp_against_fp64_analytic(lib, dev, oracle):
     assert np.array_equal(fp.cpu().numpy().view(np.uint32), got[1].view(np.uint32))
 
 
+PLAIN_FLOOR = 1e-3  # of each gradient's RMS over the batch
+
+
+def test_vjp_plain_relative_error_2e26(lib, dev, oracle):
+    """The adjoint workload itself: N = 2^26 options (S~U[5,30], K~U[1,100],
+    T~U[0.25,10], sigma~U[0.05,0.8] per option, r = 0.02), seeds gc, gp ~
+    U[-1,1].  Plain relative error |got - ref| / |ref| against the FP64
+    analytic VJP, at most 1e-5 for every gradient whose magnitude is at least
+    the floor; one floor per gradient, 1e-3 of that gradient's RMS over the
+    batch (the seeds make each gradient pass through zero, where no FP32
+    evaluation has a relative error).  Below the floor the absolute error is
+    at most 1e-5 times the floor.  A 4096-option sample is also checked
+    against FP64 central differences with the same plain relative error."""
+    n = 1 << 26
+    S, K, T, sig = bs_inputs(n, seed=1004, sigma_table=True)
+    rng = np.random.default_rng(1005)
+    gc, gp = rng.uniform(-1, 1, n).astype(np.float32), rng.uniform(-1, 1, n).astype(np.float32)
+    t = [torch.from_numpy(a).to(dev) for a in (S, K, T, sig, gc, gp)]
+    outs = [torch.empty_like(t[0]) for _ in range(7)]
+    lib.blackscholes_vjp(t[0], t[1], t[2], t[3], R, t[4], t[5], outs)
+    torch.cuda.synchronize()
+    del t
+    got = [o.cpu().numpy() for o in outs[2:]]
+    del outs
+    ref = oracle.blackscholes_vjp_f64(S, K, T, sig, R, gc, gp)
+    names = ["dS", "dK", "dT", "dsigma", "dr"]
+    for name, g, r in zip(names, got, ref):
+        floor = PLAIN_FLOOR * float(np.sqrt(np.mean(r * r)))
+        a = np.abs(r)
+        err = np.abs(g.astype(np.float64) - r)
+        big = a >= floor
+        rel = err[big] / a[big]
+        below = err[~big].max() / floor if (~big).any() else 0.0
+        print(f"\n{name}: floor {floor:.3e} ({(~big).mean():.2e} of options below); plain rel err max "
+              f"{rel.max():.3e} p99.99 {np.quantile(rel, 0.9999):.3e} median {np.median(rel):.3e}; "
+              f"below floor max |err|/floor {below:.3e}")
+        assert rel.max() <= REL_TOL, name
+        assert below <= REL_TOL, name
+    # central differences (h = 1e-4 relative) on a seeded sample of the batch
+    idx = np.random.default_rng(1006).choice(n, 4096, replace=False)
+    fd = np.zeros((5, idx.size))
+    for j, i in enumerate(idx):
+        p = [float(S[i]), float(K[i]), float(T[i]), float(sig[i]), R]
+        for k in range(5):
+            h = 1e-4 * abs(p[k])
+            up, dn = list(p), list(p)
+            up[k] += h
+            dn[k] -= h
+            cu, pu = oracle.blackscholes_point_f64(*up)
+            cd, pd = oracle.blackscholes_point_f64(*dn)
+            fd[k, j] = (float(gc[i]) * (cu - cd) + float(gp[i]) * (pu - pd)) / (2 * h)
+    for k, name in enumerate(names):
+        r = ref[k]
+        floor = PLAIN_FLOOR * float(np.sqrt(np.mean(r * r)))
+        # FD truncation O(h^2) plus FP64 cancellation noise ~1e-16 * |V| / h
+        e = np.abs(got[k][idx].astype(np.float64) - fd[k]) / np.maximum(np.abs(fd[k]), floor)
+        print(f"{name}: vs central differences, plain rel err max {e.max():.3e}")
+        assert e.max() <= REL_TOL, name
+
+
 def test_vjp_against_central_differences(lib, dev, oracle):
     n = 256
     S, K, T, sig = bs_inputs(n, seed=77, sigma_table=True)

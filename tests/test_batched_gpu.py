@@ -118,6 +118,71 @@ def test_batched_matches_plain_kernels(lib, dev, tune):
             L.nt2g_batch_destroy(h)
 
 
+@pytest.mark.parametrize("prec", ["nt2", "fast"])
+def test_batched_against_oracle(lib, dev, oracle, prec):
+    """The first 256 tables of the benchmark's own 4096-table mix (seed 1003:
+    sizes log-uniform in [1024, 4194304], ~1.3e8 elements, the three
+    expressions interleaved) through one persistent launch, checked against
+    the oracle rather than against this library's plain kernels:
+      NT2 policy: every table bit-identical to the CPU restatement of NT2's
+        evaluation (Black-Scholes, saxpy, expr3);
+      fast policy: saxpy bit-identical (it is NT2's arithmetic), expr3 within
+        4 ulp of FP64, Black-Scholes no worse than NT2's own float evaluation
+        of the same options in the conditioned metric (mean, p99.9, max)."""
+    from helpers import F32, conditioned_ulp, std_ulp
+    sizes, exprs = batched_sizes()
+    sizes, exprs = sizes[:256], exprs[:256]
+    p = lib.PREC_NT2 if prec == "nt2" else lib.PREC_FAST
+    tabs = _make(lib, dev, sizes, exprs)
+    outs = _fresh_outs(lib, tabs)
+    items = _items(lib, tabs, outs)
+    L = lib.load()
+    t = lib.BatchTune(256, 0, 16, p)
+    h = ctypes.c_void_p()
+    lib.check(L.nt2g_batch_create(items, len(tabs), ctypes.byref(t), ctypes.byref(h)))
+    try:
+        torch.cuda.synchronize()
+        lib.check(L.nt2g_batch_run(h, lib._stream()))
+        torch.cuda.synchronize()
+    finally:
+        L.nt2g_batch_destroy(h)
+    bs_in, bs_out, bs_ref = [], [], []
+    for k, ((ex, n, ins, s, y0), o) in enumerate(zip(tabs, outs)):
+        a = [x.cpu().numpy() for x in ins]
+        got = [x.cpu().numpy() for x in o]
+        if ex == lib.BATCH_SAXPY:
+            ref = oracle.saxpy(np.float32(s[0]), a[0], y0.cpu().numpy())
+            assert np.array_equal(got[0].view(np.uint32), np.asarray(ref, F32).view(np.uint32)), k
+        elif ex == lib.BATCH_EXPR3:
+            if p == lib.PREC_NT2:
+                assert np.array_equal(got[0].view(np.uint32), oracle.expr3(*a).view(np.uint32)), k
+            else:
+                e = std_ulp(got[0], oracle.expr3_f64(*a))
+                assert e.max() <= 4.0, (k, e.max())
+        else:
+            if p == lib.PREC_NT2:
+                rc, rp = oracle.blackscholes(a[0], a[1], a[2], s[1], s[0])
+                assert np.array_equal(got[0].view(np.uint32), rc.view(np.uint32)), k
+                assert np.array_equal(got[1].view(np.uint32), rp.view(np.uint32)), k
+            else:
+                bs_in.append(a)
+                bs_out.append(got)
+    if p == lib.PREC_FAST:
+        S, K, T = (np.concatenate([a[j] for a in bs_in]) for j in range(3))
+        c, pp = (np.concatenate([g[j] for g in bs_out]) for j in range(2))
+        c64, p64, terms = oracle.blackscholes_f64(S, K, T, 0.02, 0.3)
+        rc, rp = oracle.blackscholes(S, K, T, 0.02, 0.3)
+        fl = 2.0 ** -102
+        sc = np.maximum(np.maximum(np.abs(terms[:, 0]), np.abs(terms[:, 1])), fl)
+        sp = np.maximum(np.maximum(np.abs(terms[:, 2]), np.abs(terms[:, 3])), fl)
+        for got, ref64, scale, nt2 in ((c, c64, sc, rc), (pp, p64, sp, rp)):
+            e, en = conditioned_ulp(got, ref64, scale), conditioned_ulp(nt2, ref64, scale)
+            q = lambda v: np.quantile(v, 0.999)  # noqa: E731
+            print(f"\nbatched fast BS ({S.size} options): max {e.max():.2f} mean {e.mean():.3f} p99.9 {q(e):.2f}; "
+                  f"NT2's own: max {en.max():.2f} mean {en.mean():.3f} p99.9 {q(en):.2f}")
+            assert e.mean() <= en.mean() and q(e) <= q(en) and e.max() <= en.max()
+
+
 def test_autotuner_picks_a_candidate_and_caches(lib, dev, tmp_path, monkeypatch):
     from nt2_gb300 import autotune
     monkeypatch.setenv("NT2G_TUNE_CACHE", str(tmp_path / "tune.json"))

@@ -79,3 +79,39 @@ def test_ill_conditioned(red, dev, oracle, n):
     # compensated FP32: error bounded by a small multiple of eps^2 * sum|x|
     assert err <= 64 * EPS32 ** 2 * absum
     assert _run(red, dev, x)[0] == got64
+
+
+def _noalloc(lib, dev, x, y=None):
+    import ctypes
+    tx = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+    ty = None if y is None else torch.from_numpy(np.ascontiguousarray(y)).to(dev)
+    o64 = torch.zeros(1, dtype=torch.float64, device=dev)
+    o32 = torch.zeros(1, dtype=torch.float32, device=dev)
+    lib.check(lib.load().nt2g_reduce_f32_noalloc(ctypes.c_void_p(tx.data_ptr()),
+                                                  None if ty is None else ctypes.c_void_p(ty.data_ptr()),
+                                                  tx.numel(), ctypes.c_void_p(o64.data_ptr()),
+                                                  ctypes.c_void_p(o32.data_ptr()), lib._stream()))
+    torch.cuda.synchronize()
+    return float(o64.item()), float(o32.item())
+
+
+@pytest.mark.parametrize("n", [1 << 22, 1 << 28])
+def test_ill_conditioned_dot(red, lib, dev, oracle, n):
+    """dot(x, y) at condition number ~1e10 against the exact dot (FP32
+    products are exact in FP64, accumulated exactly), through the workspace
+    and the no-allocation entry points.  Compensated dot (TwoProd + TwoSum):
+    error within 64 eps^2 sum|x*y|; NT2's naive fold loses every digit."""
+    from helpers import reduction_ill_dot
+    x, y = reduction_ill_dot(n)
+    exact, absum = oracle.exact_sum(x, y)
+    cond = absum / abs(exact)
+    assert cond > 1e9
+    naive = oracle.sum_nt2(x, y)
+    for name, fn in (("workspace", lambda: _run(red, dev, x, y)), ("noalloc", lambda: _noalloc(lib, dev, x, y))):
+        got64, got32 = fn()
+        err = abs(got64 - exact)
+        print(f"\nill dot n={n} ({name}): cond {cond:.3g} exact {exact:.10g} got {got64:.10g} "
+              f"rel err {err / abs(exact):.3e}; NT2 fold rel err {abs(naive - exact) / abs(exact):.3e}")
+        assert err <= 64 * EPS32 ** 2 * absum
+        assert got32 == np.float32(got64)
+        assert fn()[0] == got64  # deterministic
