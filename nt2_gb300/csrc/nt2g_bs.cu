@@ -3,11 +3,11 @@
 // forward + reverse-mode (vector-Jacobian) kernel.
 //
 // One pass over the option tables: 128-bit loads/stores of 4 options per
-// thread per step, grid-stride persistent blocks, every intermediate in
-// registers.  The fast policy prices the 4 options as two pairs with packed
-// f32x2 arithmetic (nt2g_pair.cuh): ~115 instructions per option (174 one
-// option at a time) for 20 bytes of HBM traffic, so the kernel sits at the
-// FP32-pipe / HBM ridge.  5 blocks of 256 threads per SM (48 registers).
+// thread, every intermediate in registers.  The fast policy prices the 4
+// options as two pairs with packed f32x2 arithmetic (nt2g_pair.cuh), with
+// e^-rT and exp(-d^2/2) from the SFU's 2^x: ~95 instructions per option for
+// 20 bytes of HBM traffic, so the kernel sits at the FP32-pipe / HBM ridge.
+// 5 blocks of 256 threads per SM (48 registers).
 #include "nt2g_common.cuh"
 #include "nt2g_exprs.cuh"
 #include "nt2g_pair.cuh"
@@ -16,58 +16,69 @@
 namespace nt2g {
 
 template <class P, bool SIG_TAB>
+__device__ __forceinline__ void bs_float4(const float *__restrict__ S, const float *__restrict__ K,
+                                          const float *__restrict__ T, const float *__restrict__ sig, float sig_s,
+                                          float inv_sig_s, float r, float *__restrict__ call,
+                                          float *__restrict__ put, int64_t i)
+{
+    float4 s = ld_stream((const float4 *)S + i), k = ld_stream((const float4 *)K + i),
+           t = ld_stream((const float4 *)T + i);
+    float4 v = SIG_TAB ? ld_stream((const float4 *)sig + i) : make_float4(sig_s, sig_s, sig_s, sig_s);
+    float4 c, p;
+    if constexpr (!P::exact) {
+        // two options per packed instruction, bit-identical to bs_option<Fast>
+        float4 iv = make_float4(inv_sig_s, inv_sig_s, inv_sig_s, inv_sig_s);
+        if (SIG_TAB) {
+            f2 a = inv_fast2(pk(v.x, v.y), neg2(pk(v.x, v.y))), b = inv_fast2(pk(v.z, v.w), neg2(pk(v.z, v.w)));
+            upk(a, iv.x, iv.y);
+            upk(b, iv.z, iv.w);
+        }
+        bs_vec4_fast(s, k, t, v, iv, r, c, p);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float cj, pj;
+            const float sj = get(v, j);
+            bs_option<P>(get(s, j), get(k, j), get(t, j), sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
+            set(c, j, cj);
+            set(p, j, pj);
+        }
+    }
+    st_stream((float4 *)call + i, c);
+    st_stream((float4 *)put + i, p);
+}
+
+// vec: the tables are 16-byte aligned and the grid has one thread per float4
+// (n/4 of them, rounded up to whole blocks): each thread prices its four
+// options and exits, so a block retires as soon as its options are written
+// and the next launch's blocks take its place (no sweep tail inside a launch).
+// The 0-3 trailing options go to the first threads.  Otherwise (a misaligned
+// view) a persistent grid strides over single options.
+template <class P, bool SIG_TAB>
 __global__ void __launch_bounds__(256, SIG_TAB ? 4 : 5) k_bs(const float *__restrict__ S, const float *__restrict__ K,
                                             const float *__restrict__ T, const float *__restrict__ sig,
                                             float sig_s, float r, float *__restrict__ call,
                                             float *__restrict__ put, int64_t n, int vec)
 {
     const float inv_sig_s = P::exact ? 0.0f : inv_fast(sig_s);
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (vec) {
         const int64_t nv = n >> 2;
-        for (int64_t i = tid; i < nv; i += stride) {
-            float4 s = ld_stream((const float4 *)S + i), k = ld_stream((const float4 *)K + i),
-                   t = ld_stream((const float4 *)T + i);
-            float4 v = SIG_TAB ? ld_stream((const float4 *)sig + i) : make_float4(sig_s, sig_s, sig_s, sig_s);
-            float4 c, p;
-            if constexpr (!P::exact) {
-                // two options per packed instruction, bit-identical to bs_option<Fast>
-                float4 iv = make_float4(inv_sig_s, inv_sig_s, inv_sig_s, inv_sig_s);
-                if (SIG_TAB) {
-                    f2 a = inv_fast2(pk(v.x, v.y), neg2(pk(v.x, v.y))), b = inv_fast2(pk(v.z, v.w), neg2(pk(v.z, v.w)));
-                    upk(a, iv.x, iv.y);
-                    upk(b, iv.z, iv.w);
-                }
-                bs_vec4_fast(s, k, t, v, iv, r, c, p);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    float cj, pj;
-                    const float sj = get(v, j);
-                    bs_option<P>(get(s, j), get(k, j), get(t, j), sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
-                    set(c, j, cj);
-                    set(p, j, pj);
-                }
-            }
-            st_stream((float4 *)call + i, c);
-            st_stream((float4 *)put + i, p);
-        }
-        for (int64_t i = (nv << 2) + tid; i < n; i += stride) {
-            float cj, pj;
+        if (tid < nv) bs_float4<P, SIG_TAB>(S, K, T, sig, sig_s, inv_sig_s, r, call, put, tid);
+        if (tid < (n & 3)) {
+            const int64_t i = (nv << 2) + tid;
             const float sj = SIG_TAB ? sig[i] : sig_s;
-            bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
-            call[i] = cj;
-            put[i] = pj;
+            bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, call[i], put[i]);
         }
-    } else {
-        for (int64_t i = tid; i < n; i += stride) {
-            float cj, pj;
-            const float sj = SIG_TAB ? sig[i] : sig_s;
-            bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
-            call[i] = cj;
-            put[i] = pj;
-        }
+        return;
+    }
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = tid; i < n; i += stride) {
+        float cj, pj;
+        const float sj = SIG_TAB ? sig[i] : sig_s;
+        bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
+        call[i] = cj;
+        put[i] = pj;
     }
 }
 
@@ -115,6 +126,72 @@ __global__ void __launch_bounds__(256) k_bs_demo(const float *__restrict__ S, co
 //   e-bar  = gp N(-d2) - gc N(d2)  ->  K-bar = e-bar e^{-rT}
 //   sig-bar = vs-bar sq;  T-bar = vs-bar sig/(2 sq) - r e-bar e
 //   r-bar   = -T e-bar e
+// s + e = a + b exactly (Knuth's TwoSum).
+__device__ __forceinline__ float two_sum_err(float a, float b, float s)
+{
+    const float bb = Fast::sub(s, a);
+    return Fast::add(Fast::sub(a, Fast::sub(s, bb)), Fast::sub(b, bb));
+}
+
+// log_pos_fast(z) (returned, bit for bit) and the rounding error of its two
+// final additions, so that hi + lo carries log(z) to about 2^-30 relative.
+__device__ __forceinline__ float log_pos_fast_ff(float z, float &lo)
+{
+    const uint32_t u = f_bits(z);
+    float x = bits_f((u & 0x007fffffu) | 0x3f000000u);
+    const bool lt = x < bits_f(NT2G_SQRT_2O_2);
+    const float fe = Fast::sub(bits_f(0x4B000000u | (u >> 23)), lt ? 8388735.0f : 8388734.0f);
+    x = Fast::sub(lt ? Fast::add(x, x) : x, 1.0f);
+    const float x2 = Fast::mul(x, x);
+    float y = horner<Fast>(x, bits_f(0xbda5dff0u), bits_f(0x3e0229f9u), bits_f(0xbe04d6b7u), bits_f(0x3e116e80u),
+                           bits_f(0xbe2a6aa0u), bits_f(0x3e4cd0a3u), bits_f(0xbe800064u), bits_f(0x3eaaaaa9u));
+    y = Fast::mul(Fast::mul(y, x), x2);
+    y = Fast::fma(fe, bits_f(NT2G_LOG_2LO), y);
+    y = Fast::fma(-0.5f, x2, y);
+    const float s1 = Fast::add(x, y);
+    const float p = Fast::mul(bits_f(NT2G_LOG_2HI), fe);  // exact: LOG_2HI has 9 significant bits
+    const float hi = Fast::add(p, s1);                   // = fma(LOG_2HI, fe, s1)
+    lo = Fast::add(two_sum_err(x, y, s1), two_sum_err(p, s1, hi));
+    return hi;
+}
+
+// d1 and d2 of the fast forward are each within a few ulps, but the
+// gradients' N(d) and phi(d) amplify an absolute error in d by phi/N (up to
+// |d| in the tails) and by 1/(sigma sqrt T) through log(S/K) (40x for
+// sigma = 0.05, T = 0.25).  This recovers dd1 = d1* - d1 and dd2 = d2* - d2,
+// the exact values' distance from the rounded ones, to first order: the
+// quotient S/K's residual, the log's rounding, (r + sigma^2/2) T + log(S/K)
+// as a float pair, sqrt(T) refined once, sigma sqrt(T) as a float pair, and
+// the residual of d1 * sigma sqrt(T) against that numerator.
+__device__ __forceinline__ void bs_d_residuals(float S, float K, float T, float sig, float r, const BsFwd &f,
+                                               float &dd1, float &dd2)
+{
+    const float q = Fast::fdiv(S, K);
+    float lq_lo;
+    const float lq = log_pos_fast_ff(q, lq_lo);
+    lq_lo = Fast::fma(Fast::fma(-q, K, S), Fast::rcp(S), lq_lo);  // log(S/K) - log(q) ~ (S - qK)/S
+    // a = r + sigma^2/2 as a + a_lo
+    const float ss = Fast::mul(sig, sig), ss_lo = Fast::fma(sig, sig, -ss);
+    const float h = Fast::mul(0.5f, ss);
+    const float a = Fast::fma(ss, 0.5f, r);
+    const float a_lo = Fast::fma(0.5f, ss_lo, two_sum_err(h, r, a));
+    // numerator N = fma(a, T, lq) and its error against a* T + log(S/K)
+    const float N = Fast::fma(a, T, lq);
+    const float p = Fast::mul(a, T), pe = Fast::fma(a, T, -p);
+    const float s = Fast::add(p, lq), se = two_sum_err(p, lq, s);
+    const float N_lo = Fast::fma(a_lo, T, Fast::add(Fast::add(Fast::sub(s, N), se), Fast::add(pe, lq_lo)));
+    // sigma sqrt(T) = vh + vl
+    const float sq_lo = Fast::mul(Fast::fma(-f.sq, f.sq, T), Fast::mul(0.5f, f.rs));
+    const float vh = Fast::mul(sig, f.sq);
+    const float vl = Fast::fma(sig, sq_lo, Fast::fma(sig, f.sq, -vh));
+    // d1* - d1 = (N + N_lo - d1 (vh + vl)) / (sigma sqrt T)
+    const float res = Fast::fma(-f.d1, vl, Fast::add(Fast::fma(-f.d1, vh, N), N_lo));
+    dd1 = Fast::mul(res, Fast::mul(f.rs, inv_fast(sig)));
+    // d2 = RN(d1 - sigma sq): d2* - d2 = (t - d2) + t_lo + dd1 - vl, t + t_lo = d1 - vh
+    const float t = Fast::sub(f.d1, vh), t_lo = two_sum_err(f.d1, -vh, t);
+    dd2 = Fast::add(Fast::add(Fast::sub(t, f.d2), t_lo), Fast::sub(dd1, vl));
+}
+
 __device__ __forceinline__ void bs_vjp_option(float S, float K, float T, float sig, float r, float gc,
                                               float gp, float &C, float &P_, float &dS, float &dK,
                                               float &dT, float &dsig, float &dr)
@@ -126,9 +203,23 @@ __device__ __forceinline__ void bs_vjp_option(float S, float K, float T, float s
     const float sq = f.sq, ert = f.ert, e = f.e;
     C = Fast::fma(-e, n2, Fast::mul(S, n1));
     P_ = Fast::fma(-S, m1, Fast::mul(e, m2));
-    if (is_nan(f.d1) || is_nan(f.d2)) { C = f.d1 + f.d2; P_ = C; }
-    // reverse
+    const float z = Fast::sub(f.d1, f.d1);  // as the forward kernel: NaN unless d1 is finite
+    C = Fast::add(C, z);
+    P_ = Fast::add(P_, z);
+    // the gradients take N(d) and phi(d) at the exact d: first-order
+    // corrections N(d + dd) = N(d) + phi(d) dd, phi(d + dd) = phi(d)(1 - d dd)
     const float inv_sqrt_2pi = 0.398942280401432678f;
+    float dd1, dd2;
+    bs_d_residuals(S, K, T, sig, r, f, dd1, dd2);
+    const float phi1 = Fast::mul(inv_sqrt_2pi, g1);
+    const float phi2 = Fast::mul(phi1, Fast::mul(S, Fast::rcp(e)));  // S phi(d1) = e phi(d2)
+    const float c1 = Fast::mul(phi1, dd1), c2 = Fast::mul(phi2, dd2);
+    n1 = Fast::add(n1, c1);
+    m1 = Fast::sub(m1, c1);
+    n2 = Fast::add(n2, c2);
+    m2 = Fast::sub(m2, c2);
+    g1 = Fast::fma(Fast::mul(-f.d1, dd1), g1, g1);
+    // reverse
     float gs = Fast::add(gc, gp);
     float bvs = Fast::mul(Fast::mul(Fast::mul(inv_sqrt_2pi, g1), S), gs);
     float be = Fast::fma(gp, m2, -Fast::mul(gc, n2));
@@ -195,13 +286,19 @@ nt2g_status launch_bs(const float *S, const float *K, const float *T, const floa
     if (n == 0) return NT2G_OK;
     int vec = aligned16(S) && aligned16(K) && aligned16(T) && aligned16(call) && aligned16(put) &&
               (!sig || aligned16(sig));
+    // vec: one thread per float4 (at least one block, for the trailing options)
+    const int64_t exact_grid = ((n >> 2) + 255) / 256 > 0 ? ((n >> 2) + 255) / 256 : 1;
+#define NT2G_BS(PP, TAB)                                                                                       \
+    k_bs<PP, TAB><<<vec ? (int)exact_grid : grid_for(k_bs<PP, TAB>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r,   \
+                                                                                    call, put, n, vec)
     if (precision == NT2G_PREC_NT2) {
-        if (sig) k_bs<Nt2, true><<<grid_for(k_bs<Nt2, true>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r, call, put, n, vec);
-        else k_bs<Nt2, false><<<grid_for(k_bs<Nt2, false>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r, call, put, n, vec);
+        if (sig) NT2G_BS(Nt2, true);
+        else NT2G_BS(Nt2, false);
     } else {
-        if (sig) k_bs<Fast, true><<<grid_for(k_bs<Fast, true>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r, call, put, n, vec);
-        else k_bs<Fast, false><<<grid_for(k_bs<Fast, false>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r, call, put, n, vec);
+        if (sig) NT2G_BS(Fast, true);
+        else NT2G_BS(Fast, false);
     }
+#undef NT2G_BS
     NT2G_LAUNCH_CHECK("blackscholes launch");
     return NT2G_OK;
 }

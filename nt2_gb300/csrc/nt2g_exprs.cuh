@@ -9,8 +9,9 @@ namespace nt2g {
 // ---------------------------------------------------------------------------
 // Helpers of the fast Black-Scholes path.  Its operands are a priceable
 // option's: S, K, T, sigma positive, finite and normal.  Other inputs give NaN
-// call/put (one check on d1/d2 replaces the functors' special-value selects);
-// the NT2 policy keeps NT2's full IEEE handling.
+// call/put: d1 - d1 (0 for a finite d1, NaN for a NaN or infinite one) is
+// added to both outputs in place of the functors' special-value selects; the
+// NT2 policy keeps NT2's full IEEE handling.
 
 // log for a positive normal x: NT2's kernel (f_kernel.hpp:43-75) with FMAs,
 // without the zero/negative/inf/NaN/subnormal branches; the exponent becomes
@@ -32,15 +33,6 @@ __device__ __forceinline__ float log_pos_fast(float z)
     return Fast::fma(bits_f(NT2G_LOG_2HI), fe, Fast::add(x, y));
 }
 
-// exp for an argument already known finite; clamped to NT2's [Minlog, Maxlog].
-__device__ __forceinline__ float exp_clamped_fast(float a0)
-{
-    a0 = fminf(fmaxf(a0, bits_f(NT2G_MINLOG)), bits_f(NT2G_MAXLOG));
-    float scale;
-    float s = exp_fast_parts(a0, scale);
-    return Fast::mul(Fast::add(s, 1.0f), scale);
-}
-
 // 1/sqrt(t) to about one ulp: rsqrt.approx refined by one Newton step.
 __device__ __forceinline__ float rsqrt_fast(float t)
 {
@@ -48,6 +40,48 @@ __device__ __forceinline__ float rsqrt_fast(float t)
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(t));
     float h = Fast::mul(t, y);
     return Fast::fma(Fast::mul(0.5f, y), Fast::fma(-h, y, 1.0f), y);
+}
+
+// 2^x from the special-function unit (ex2.approx.ftz.f32, about 2 ulp).
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// exp(-a^2/2) = (1 + eL) * scale for 0 <= a < 13.26.  The exponent
+// t = a^2 log2(e)/2 is carried as th + tl: a^2 split exactly by FMA
+// (hi + lo), log2(e)/2 as the float pair LH + LL, and the rounding of
+// th = hi*LH recovered by FMA.  t = k + f with k = rint(th) (1.5*2^23
+// shifter), f = (th - k) + tl (th - k exact), |f| <= 1/2; 2^-f comes from the
+// SFU and scale = 2^-k is built in the exponent field.  Past 13.2 the
+// callers zero the tail (k would leave the normal range).
+__device__ __forceinline__ float bs_exp_half_sq(float a, float &scale)
+{
+    const float LH = 0x1.715476p-1f, LL = 0x1.4ae0c0p-27f, shifter = 12582912.0f;
+    const float hi = Fast::mul(a, a), lo = Fast::fma(a, a, -hi);
+    const float th = Fast::mul(hi, LH);
+    float tl = Fast::fma(hi, LH, -th);
+    tl = Fast::fma(hi, LL, tl);
+    tl = Fast::fma(lo, LH, tl);
+    const float kf = Fast::add(th, shifter);
+    const float f = Fast::add(Fast::sub(th, Fast::sub(kf, shifter)), tl);
+    scale = bits_f((127u - (f_bits(kf) - 0x4B400000u)) << 23);
+    return Fast::sub(ex2_approx(-f), 1.0f);
+}
+
+// w = 1/(1 + q a) refined once, and its residual r = 1 - den*w against the
+// rounded den = 1 + q a, formed from the negated nd = RN(-q a - 1) = -den.
+// The multiplier w (1 + r) is exact to first order up to den's own rounding
+// (2^-24 relative); the polynomial takes the refined w.
+__device__ __forceinline__ void bs_tail_recip(float a, float &w, float &r)
+{
+    const float q = 0.353553390593273762f;  // 1/(2 sqrt 2)
+    const float nd = Fast::fma(-q, a, -1.0f);
+    w = Fast::rcp(-nd);
+    w = Fast::fma(w, Fast::fma(nd, w, 1.0f), w);
+    r = Fast::fma(nd, w, 1.0f);
 }
 
 // The four normal CDF values of a Black-Scholes option, N(+-d1) and N(+-d2),
@@ -63,26 +97,6 @@ __device__ __forceinline__ float rsqrt_fast(float t)
 // their errors cancel instead of adding (on the standard test mixes, max error
 // of call/put relative to the larger term drops from ~90 ulp to ~10).
 // g1 (optional) receives exp(-d1^2/2) for the adjoint.
-__device__ __forceinline__ float bs_exp_half_sq(float a, float &scale)
-{
-    // exp(-a^2/2) = (1 + eL) * scale with the exact split a^2 = hi + lo
-    float hi = Fast::mul(a, a), lo = Fast::fma(a, a, -hi);
-    float s = exp_fast_parts(Fast::mul(-0.5f, hi), scale);
-    float cl = Fast::mul(-0.5f, lo);
-    return Fast::add(s, Fast::fma(cl, s, cl));
-}
-
-// w = 1/(1 + q a) refined once and its residual r against 1 + q a, formed from
-// the negated parts: RN(-q a - 1) = -RN(q a + 1), RN(-1 - (-den)) = -RN(1 - den).
-__device__ __forceinline__ void bs_tail_recip(float a, float &w, float &r)
-{
-    const float q = 0.353553390593273762f;  // 1/(2 sqrt 2)
-    float nd = Fast::fma(-q, a, -1.0f), nl = Fast::fma(-q, a, Fast::sub(-1.0f, nd));
-    w = Fast::rcp(-nd);
-    w = Fast::fma(w, Fast::fma(nd, w, 1.0f), w);
-    r = Fast::fma(nl, w, Fast::fma(nd, w, 1.0f));
-}
-
 __device__ __forceinline__ void bs_normcdfs_fast(float d1, float d2, float S, float e, float &n1, float &m1,
                                                  float &n2, float &m2, float *g1 = nullptr)
 {
@@ -116,6 +130,9 @@ __device__ __forceinline__ void bs_normcdfs_fast(float d1, float d2, float S, fl
     m2 = d2 < 0.0f ? o2 : h2;
 }
 
+// -r log2(e), the factor of T in the exponent of e^-rT = 2^(-r log2(e) T).
+__device__ __forceinline__ float bs_neg_rate_log2e(float r) { return Fast::mul(-r, 0x1.715476p+0f); }
+
 // Shared forward prefix of the fast call/put and its adjoint.
 struct BsFwd {
     float sq, rs, d1, d2, ert, e;
@@ -130,7 +147,7 @@ __device__ __forceinline__ BsFwd bs_prefix_fast(float S, float K, float T, float
     float a = Fast::fma(Fast::mul(sig, sig), 0.5f, r);
     f.d1 = Fast::mul(Fast::fma(a, T, lq), Fast::mul(f.rs, inv_sig));  // / (sigma sqrt T)
     f.d2 = Fast::fma(-sig, f.sq, f.d1);
-    f.ert = exp_clamped_fast(Fast::mul(-r, T));
+    f.ert = ex2_approx(Fast::mul(bs_neg_rate_log2e(r), T));  // e^-rT = 2^(-r log2(e) T)
     f.e = Fast::mul(K, f.ert);
     return f;
 }
@@ -143,7 +160,8 @@ __device__ __forceinline__ BsFwd bs_prefix_fast(float S, float K, float T, float
 //   put  = fnms(S, normcdf(-d1), e*normcdf(-d2))
 // Nt2 policy: exactly that operation sequence.  Fast policy: the same graph
 // with FMAs, rsqrt-based sqrt(T) and 1/(sig sqrt T), approximate-reciprocal
-// S/K, and one erfc core shared by N(d) and N(-d).  inv_sig is 1/sig (the
+// S/K, e^-rT and exp(-d^2/2) from the SFU's 2^x, and one erfc core shared by
+// N(d) and N(-d).  inv_sig is 1/sig (the
 // caller hoists it when sigma is a scalar); the Nt2 policy ignores it.
 template <class P>
 __device__ __forceinline__ void bs_option(float S, float K, float T, float sig, float inv_sig, float r, float &call,
@@ -168,7 +186,9 @@ __device__ __forceinline__ void bs_option(float S, float K, float T, float sig, 
     bs_normcdfs_fast(f.d1, f.d2, S, f.e, n1, m1, n2, m2);
     call = Fast::fma(-f.e, n2, Fast::mul(S, n1));
     put = Fast::fma(-S, m1, Fast::mul(f.e, m2));
-    if (is_nan(f.d1) || is_nan(f.d2)) { call = f.d1 + f.d2; put = call; }
+    const float z = Fast::sub(f.d1, f.d1);  // NaN unless d1 is finite (d2 follows d1)
+    call = Fast::add(call, z);
+    put = Fast::add(put, z);
 }
 
 // 1/sigma per option when sigma is a table (rcp.approx + one Newton step).

@@ -55,6 +55,13 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c)
     return d;
 }
 __device__ __forceinline__ f2 neg2(f2 a) { return mul2(a, dup(-1.0f)); }  // exact
+// -a by flipping both sign bits (integer pipe, exact, no FP32 slot)
+__device__ __forceinline__ f2 negx2(f2 a)
+{
+    f2 r;
+    r.v = a.v ^ 0x8000000080000000ull;
+    return r;
+}
 template <class F> __device__ __forceinline__ f2 lanes(f2 a, F f)
 {
     float x, y;
@@ -132,31 +139,6 @@ __device__ __forceinline__ f2 log_pos_fast2(f2 z)
     return fma2(dup(bits_f(NT2G_LOG_2HI)), fe, add2(x, y));
 }
 
-// exp_fast_parts, lane for lane: returns s with e^a = (1 + s) * scale.
-// -k is formed as shifter - kf (exact, like k = kf - shifter).
-__device__ __forceinline__ f2 exp_fast_parts2(f2 a, f2 &scale)
-{
-    const float shifter = 12582912.0f;
-    f2 kf = fma2(a, dup(bits_f(NT2G_INVLOG_2)), dup(shifter));
-    f2 nk = sub2(dup(shifter), kf);
-    float kf0, kf1;
-    upk(kf, kf0, kf1);
-    // (ik + 127) << 23 with ik = bits(kf) - bits(1.5 * 2^23)
-    scale = pk(bits_f((f_bits(kf0) - 0x4B400000u + 127u) << 23), bits_f((f_bits(kf1) - 0x4B400000u + 127u) << 23));
-    f2 x = fma2(nk, dup(bits_f(NT2G_LOG_2HI)), a);
-    x = fma2(nk, dup(bits_f(NT2G_LOG_2LO)), x);
-    f2 q = horner2(x, dup(0x1.a157b2p-13f), 0x1.6d4926p-10f, 0x1.1110c4p-7f, 0x1.5554e4p-5f, 0x1.555556p-3f, 0.5f);
-    return fma2(q, mul2(x, x), x);
-}
-
-__device__ __forceinline__ f2 exp_clamped_fast2(f2 a)
-{
-    a = lanes(a, [](float v) { return fminf(fmaxf(v, bits_f(NT2G_MINLOG)), bits_f(NT2G_MAXLOG)); });
-    f2 scale;
-    f2 s = exp_fast_parts2(a, scale);
-    return mul2(add2(s, dup(1.0f)), scale);
-}
-
 __device__ __forceinline__ f2 erfc_tail_poly2(f2 w)
 {
     f2 d = sub2(w, dup(0.5f));
@@ -164,25 +146,32 @@ __device__ __forceinline__ f2 erfc_tail_poly2(f2 w)
                    -0x1.a94032p-4f, -0x1.604ccep-3f, 0x1.2a8c2ep-3f, 0x1.1e2dc2p-1f, 0x1.5fd384p-1f, 0x1.058672p-1f);
 }
 
-// bs_exp_half_sq, lane for lane (-lo = fma(-a, a, hi); -0.5*lo = 0.5*(-lo)).
+// bs_exp_half_sq, lane for lane (-x as a sign flip, exact).
 __device__ __forceinline__ f2 bs_exp_half_sq2(f2 a, f2 &scale)
 {
-    f2 hi = mul2(a, a);
-    f2 nlo = fma2(neg2(a), a, hi);
-    f2 s = exp_fast_parts2(mul2(dup(-0.5f), hi), scale);
-    f2 cl = mul2(dup(0.5f), nlo);
-    return add2(s, fma2(cl, s, cl));
+    const float LH = 0x1.715476p-1f, LL = 0x1.4ae0c0p-27f, shifter = 12582912.0f;
+    const f2 hi = mul2(a, a), lo = fma2(a, a, negx2(hi));
+    const f2 th = mul2(hi, dup(LH));
+    f2 tl = fma2(hi, dup(LH), negx2(th));
+    tl = fma2(hi, dup(LL), tl);
+    tl = fma2(lo, dup(LH), tl);
+    const f2 kf = add2(th, dup(shifter));
+    const f2 f = add2(sub2(th, sub2(kf, dup(shifter))), tl);
+    float f0, f1, k0, k1;
+    upk(f, f0, f1);
+    upk(kf, k0, k1);
+    scale = pk(bits_f((127u - (f_bits(k0) - 0x4B400000u)) << 23), bits_f((127u - (f_bits(k1) - 0x4B400000u)) << 23));
+    return sub2(pk(ex2_approx(-f0), ex2_approx(-f1)), dup(1.0f));
 }
 
 // bs_tail_recip, lane for lane.
 __device__ __forceinline__ void bs_tail_recip2(f2 a, f2 &w, f2 &r)
 {
     const float q = 0.353553390593273762f;
-    f2 nd = fma2(dup(-q), a, dup(-1.0f));
-    f2 nl = fma2(dup(-q), a, sub2(dup(-1.0f), nd));
+    const f2 nd = fma2(dup(-q), a, dup(-1.0f));
     w = lanes(nd, [](float v) { return rcp_approx(-v); });
     w = fma2(w, fma2(nd, w, dup(1.0f)), w);
-    r = fma2(nl, w, fma2(nd, w, dup(1.0f)));
+    r = fma2(nd, w, dup(1.0f));
 }
 
 // bs_normcdfs_fast for two options (lane for lane; without g1).
@@ -251,23 +240,16 @@ __device__ __forceinline__ void bs_option_fast2(f2 S, f2 K, f2 T, f2 sig, f2 inv
     f2 a = fma2(mul2(sig, sig), dup(0.5f), dup(r));
     f2 d1 = mul2(fma2(a, T, lq), mul2(rs, inv_sig));
     f2 d2 = fma2(neg2(sig), sq, d1);
-    f2 ert = exp_clamped_fast2(mul2(dup(-r), T));
+    f2 ert = lanes(mul2(dup(bs_neg_rate_log2e(r)), T), ex2_approx);
     f2 e = mul2(K, ert);
     f2 ne = mul2(nK, ert);
     f2 n1, m1, n2, m2;
     bs_normcdfs_fast2(d1, d2, S, e, n1, m1, n2, m2);
     call = fma2(ne, n2, mul2(S, n1));
     put = fma2(neg2(S), m1, mul2(e, m2));
-    float a0, a1, b0, b1, c0, c1;
-    upk(d1, a0, a1);
-    upk(d2, b0, b1);
-    upk(call, c0, c1);
-    float p0, p1;
-    upk(put, p0, p1);
-    if (is_nan(a0) || is_nan(b0)) { c0 = a0 + b0; p0 = c0; }
-    if (is_nan(a1) || is_nan(b1)) { c1 = a1 + b1; p1 = c1; }
-    call = pk(c0, c1);
-    put = pk(p0, p1);
+    const f2 z = sub2(d1, d1);  // NaN unless d1 is finite
+    call = add2(call, z);
+    put = add2(put, z);
 }
 
 // Four options (one float4 of each table) as two pairs, sigma and 1/sigma
