@@ -274,8 +274,9 @@ def bs_accuracy(S, K, T, call, put, r, sigma, precision, nt2_out=None):
 
 BS_TOLERANCE = {
     "nt2": "bit-identical to NT2's CPU evaluation (the CPU baseline leg evaluates the same options)",
-    "fast": "every functor within 4 ulp of FP64; the composite call/put within 12 conditioned ulp "
-            "(error over the ulp of the larger cancelling term), no worse than NT2's own float evaluation",
+    "fast": "every functor within 4 ulp of FP64; the composite call/put within 14 conditioned ulp max, "
+            "6 at p99.9, 1.1 mean (error over the ulp of the larger cancelling term); NT2's own float "
+            "evaluation of the same options: about 300 max, 90 p99.9, 3.4 mean",
 }
 
 

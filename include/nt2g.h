@@ -44,7 +44,14 @@ typedef enum nt2g_status {
  *   a function's own conditioning decides.
  * NT2G_PREC_NT2: NT2's own scalar algorithms and operation order (unfused
  *   fma/Horner, IEEE division and sqrt); bit-identical to NT2's CPU result. */
-typedef enum nt2g_precision { NT2G_PREC_FAST = 0, NT2G_PREC_NT2 = 1 } nt2g_precision;
+typedef enum nt2g_precision {
+    NT2G_PREC_FAST = 0,
+    NT2G_PREC_NT2 = 1,
+    /* folds of an expression only (nt2g_eval_fold): NT2's element arithmetic,
+       folded by the compensated fast-policy fold (what sum(), dot() and
+       globalsum() do with NT2 elements) */
+    NT2G_PREC_NT2_ELEMENTS = 2
+} nt2g_precision;
 
 typedef enum nt2g_dtype { NT2G_F32 = 0, NT2G_U8 = 1 } nt2g_dtype;
 
@@ -70,6 +77,9 @@ typedef enum nt2g_opcode {
     NT2G_OP_INDEX = 5,     /* the element's linear position p (offset + i) in
                               the op's dtype: NT2's enumerate<T>(p), the leaf of
                               colon / linspace / logspace (uint8: p mod 256)    */
+    NT2G_OP_FOLD = 6,      /* a = the float value nt2g_eval_fold folds (a
+                              comparison folds as 0/1); a program has at most
+                              one FOLD and then no STORE                       */
     NT2G_OP_ADD = 10, NT2G_OP_SUB, NT2G_OP_MUL, NT2G_OP_DIV, NT2G_OP_NEG, NT2G_OP_ABS,
     NT2G_OP_SQR, NT2G_OP_SQRT, NT2G_OP_REC, NT2G_OP_MIN, NT2G_OP_MAX,
     NT2G_OP_FMA = 30,      /* a*b + c (unfused under NT2G_PREC_NT2)          */
@@ -210,6 +220,36 @@ typedef enum nt2g_fold_op {
 nt2g_status nt2g_fold_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
 nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t op, int32_t precision,
                           void *workspace, size_t workspace_bytes, float *out, int64_t *index, void *stream);
+
+/* The same fold over an expression: x at linear position p is the value of
+ * the program's FOLD instruction for element p of its tables (every table
+ * slot holds lo*inner*hi elements in the same column-major layout; INDEX
+ * leaves read p).  NT2's folds take the expression itself
+ * (RED/core/functions/scalar/inner_fold.hpp:23-49 with fold_step over the
+ * AST, RED/core/functions/simd/global.hpp:27-69): here every element is
+ * evaluated in registers inside the fold kernels -- sum(exp(x)*y),
+ * globalsum(a*b+c), sum(abs(x-y), 1) read their input tables once and write
+ * no temporary.  Results equal nt2g_fold_f32 of the expression evaluated into
+ * an aligned table by nt2g_eval's run-time compiled kernel (same policy,
+ * force_generic = 1), bit for bit.  out64 (optional, may be
+ * NULL; not under NT2G_PREC_NT2) receives the FP64 result of each output of a
+ * sum-type fold (sum, mean, asum1/2, norm2, var, stdev, counts, nansum,
+ * nanmean) or of prod, before rounding to float.  The kernels are compiled at
+ * run time (NVRTC) on first use per device, policy, op and program: make that
+ * first call outside any stream capture.  NT2G_ERR_UNSUPPORTED when NVRTC is
+ * unavailable.  precision: NT2G_PREC_FAST, NT2G_PREC_NT2 (NT2's elements folded
+ * in NT2's index order), or NT2G_PREC_NT2_ELEMENTS (NT2's elements, compensated
+ * fold).  workspace: nt2g_fold_workspace_size bytes. */
+nt2g_status nt2g_eval_fold(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t lo, int64_t inner,
+                           int64_t hi, int32_t op, int32_t precision, void *workspace, size_t workspace_bytes,
+                           float *out, int64_t *index, double *out64, void *stream);
+
+/* The CUDA source nt2g_eval_fold compiles for a program and fold op (no GPU
+ * needed; *len receives the size including the terminating NUL, cap = 0 only
+ * queries it).  No counterpart in the reference: it exposes the generated
+ * code for inspection and for compile checks. */
+nt2g_status nt2g_program_fold_source(const nt2g_program *p, int32_t precision, int32_t op, char *buf, size_t cap,
+                                     size_t *len);
 
 /* ------------------------------------------------------------------ */
 /* Cumulative functions along one dimension (cumsum, cumprod, ...)     */
@@ -409,6 +449,13 @@ nt2g_status nt2g_device_free(void *ptr);
 /* kind: 1 host->device, 2 device->host, 3 device->device */
 nt2g_status nt2g_memcpy(void *dst, const void *src, size_t bytes, int32_t kind, void *stream);
 nt2g_status nt2g_stream_synchronize(void *stream);
+/* The calling thread's current device (the table layer keys its per-thread
+ * reduction scratch on it; NT2 keeps its device in CUDA/sdk/cuda/settings). */
+nt2g_status nt2g_device_current(int32_t *device);
+/* A non-blocking stream for the table layer's evaluation options (callers
+ * that do not link the CUDA runtime themselves). */
+nt2g_status nt2g_stream_create(void **stream);
+nt2g_status nt2g_stream_destroy(void *stream);
 
 #ifdef __cplusplus
 }

@@ -2,7 +2,9 @@
 // scan kernels: a running sum carried as s + c, c collecting the exact
 // rounding error of every addition (TwoSum).
 #pragma once
+#if !defined(__CUDACC_RTC__)  // the run-time compiler (folds of expressions) embeds this header
 #include <cuda_runtime.h>
+#endif
 
 namespace nt2g {
 

@@ -48,21 +48,21 @@ __device__ __forceinline__ void bs_float4(const float *__restrict__ S, const flo
     st_stream((float4 *)put + i, p);
 }
 
-// vec: the tables are 16-byte aligned and the grid has one thread per float4
+// VEC: the tables are 16-byte aligned and the grid has one thread per float4
 // (n/4 of them, rounded up to whole blocks): each thread prices its four
 // options and exits, so a block retires as soon as its options are written
 // and the next launch's blocks take its place (no sweep tail inside a launch).
 // The 0-3 trailing options go to the first threads.  Otherwise (a misaligned
 // view) a persistent grid strides over single options.
-template <class P, bool SIG_TAB>
+template <class P, bool SIG_TAB, bool VEC>
 __global__ void __launch_bounds__(256, SIG_TAB ? 4 : 5) k_bs(const float *__restrict__ S, const float *__restrict__ K,
                                             const float *__restrict__ T, const float *__restrict__ sig,
                                             float sig_s, float r, float *__restrict__ call,
-                                            float *__restrict__ put, int64_t n, int vec)
+                                            float *__restrict__ put, int64_t n)
 {
     const float inv_sig_s = P::exact ? 0.0f : inv_fast(sig_s);
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (vec) {
+    if constexpr (VEC) {
         const int64_t nv = n >> 2;
         if (tid < nv) bs_float4<P, SIG_TAB>(S, K, T, sig, sig_s, inv_sig_s, r, call, put, tid);
         if (tid < (n & 3)) {
@@ -70,15 +70,15 @@ __global__ void __launch_bounds__(256, SIG_TAB ? 4 : 5) k_bs(const float *__rest
             const float sj = SIG_TAB ? sig[i] : sig_s;
             bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, call[i], put[i]);
         }
-        return;
-    }
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = tid; i < n; i += stride) {
-        float cj, pj;
-        const float sj = SIG_TAB ? sig[i] : sig_s;
-        bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
-        call[i] = cj;
-        put[i] = pj;
+    } else {
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t i = tid; i < n; i += stride) {
+            float cj, pj;
+            const float sj = SIG_TAB ? sig[i] : sig_s;
+            bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
+            call[i] = cj;
+            put[i] = pj;
+        }
     }
 }
 
@@ -111,21 +111,6 @@ __global__ void __launch_bounds__(256) k_bs_demo(const float *__restrict__ S, co
 }
 
 // ------------------------------------------------------------ adjoint ----
-// Hand-derived reverse sweep of the forward graph
-//   sq = sqrt(T), vs = sig*sq, d1 = (log(S/K) + (r + sig^2/2) T)/vs, d2 = d1 - vs,
-//   e = K exp(-rT), C = S N(d1) - e N(d2), P = e N(-d2) - S N(-d1)
-// with seeds gc, gp and every intermediate recomputed in registers.
-// The adjoint reaching d1 through N(d1), N(-d1) is  S phi(d1) (gc+gp)  and
-// through d2 = d1 - vs it is  -e phi(d2) (gc+gp); since S phi(d1) =
-// K e^{-rT} phi(d2) holds exactly for the model, their sum is identically
-// zero and the sweep drops it symbolically instead of computing two nearly
-// equal FP32 products (whose rounding noise, divided by vs, would dominate
-// every gradient for short-dated low-volatility options).  What survives:
-//   vs-bar = S phi(d1) (gc+gp)               (from d2 = d1 - vs)
-//   S-bar  = gc N(d1) - gp N(-d1)
-//   e-bar  = gp N(-d2) - gc N(d2)  ->  K-bar = e-bar e^{-rT}
-//   sig-bar = vs-bar sq;  T-bar = vs-bar sig/(2 sq) - r e-bar e
-//   r-bar   = -T e-bar e
 // s + e = a + b exactly (Knuth's TwoSum).
 __device__ __forceinline__ float two_sum_err(float a, float b, float s)
 {
@@ -192,6 +177,21 @@ __device__ __forceinline__ void bs_d_residuals(float S, float K, float T, float 
     dd2 = Fast::add(Fast::add(Fast::sub(t, f.d2), t_lo), Fast::sub(dd1, vl));
 }
 
+// Hand-derived reverse sweep of the forward graph
+//   sq = sqrt(T), vs = sig*sq, d1 = (log(S/K) + (r + sig^2/2) T)/vs, d2 = d1 - vs,
+//   e = K exp(-rT), C = S N(d1) - e N(d2), P = e N(-d2) - S N(-d1)
+// with seeds gc, gp and every intermediate recomputed in registers.
+// The adjoint reaching d1 through N(d1), N(-d1) is  S phi(d1) (gc+gp)  and
+// through d2 = d1 - vs it is  -e phi(d2) (gc+gp); since S phi(d1) =
+// K e^{-rT} phi(d2) holds exactly for the model, their sum is identically
+// zero and the sweep drops it symbolically instead of computing two nearly
+// equal FP32 products (whose rounding noise, divided by vs, would dominate
+// every gradient for short-dated low-volatility options).  What survives:
+//   vs-bar = S phi(d1) (gc+gp)               (from d2 = d1 - vs)
+//   S-bar  = gc N(d1) - gp N(-d1)
+//   e-bar  = gp N(-d2) - gc N(d2)  ->  K-bar = e-bar e^{-rT}
+//   sig-bar = vs-bar sq;  T-bar = vs-bar sig/(2 sq) - r e-bar e
+//   r-bar   = -T e-bar e
 __device__ __forceinline__ void bs_vjp_option(float S, float K, float T, float sig, float r, float gc,
                                               float gp, float &C, float &P_, float &dS, float &dK,
                                               float &dT, float &dsig, float &dr)
@@ -289,8 +289,11 @@ nt2g_status launch_bs(const float *S, const float *K, const float *T, const floa
     // vec: one thread per float4 (at least one block, for the trailing options)
     const int64_t exact_grid = ((n >> 2) + 255) / 256 > 0 ? ((n >> 2) + 255) / 256 : 1;
 #define NT2G_BS(PP, TAB)                                                                                       \
-    k_bs<PP, TAB><<<vec ? (int)exact_grid : grid_for(k_bs<PP, TAB>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r,   \
-                                                                                    call, put, n, vec)
+    do {                                                                                                       \
+        if (vec) k_bs<PP, TAB, true><<<(int)exact_grid, 256, 0, st>>>(S, K, T, sig, sig_s, r, call, put, n);   \
+        else k_bs<PP, TAB, false><<<grid_for(k_bs<PP, TAB, false>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r,   \
+                                                                                      call, put, n);           \
+    } while (0)
     if (precision == NT2G_PREC_NT2) {
         if (sig) NT2G_BS(Nt2, true);
         else NT2G_BS(Nt2, false);

@@ -263,17 +263,18 @@ struct nt2g_program {
     const char *kernel_name = "generic";
     std::vector<RoleBind> roles;
     std::vector<DeferredConst> deferred;
+    bool folds = false;  // the program's value is folded (nt2g_eval_fold), it stores nothing
 };
 
 namespace nt2g {
 
-static bool is_value_op(int code) { return code != NT2G_OP_STORE; }
+static bool is_value_op(int code) { return code != NT2G_OP_STORE && code != NT2G_OP_FOLD; }
 
 static int n_operands(int code)
 {
     switch (code) {
     case NT2G_OP_LOAD: case NT2G_OP_SCALAR: case NT2G_OP_CONST: case NT2G_OP_INDEX: return 0;
-    case NT2G_OP_STORE: return 1;
+    case NT2G_OP_STORE: case NT2G_OP_FOLD: return 1;
     case NT2G_OP_NEG: case NT2G_OP_ABS: case NT2G_OP_SQR: case NT2G_OP_SQRT: case NT2G_OP_REC:
     case NT2G_OP_EXP: case NT2G_OP_LOG: case NT2G_OP_LOG1P: case NT2G_OP_ERFC: case NT2G_OP_NORMCDF:
     case NT2G_OP_FASTNORMCDF: case NT2G_OP_IF_ZERO_ELSE_ONE: case NT2G_OP_EXP2: case NT2G_OP_EXP10:
@@ -453,6 +454,7 @@ extern "C" nt2g_status nt2g_program_create(const nt2g_op *ops, int32_t n_ops, in
                    kMaxSlots);
     std::vector<int> slot_use(n_slots, 0), slot_dtype(n_slots, -1);
     std::vector<uint8_t> logical(n_ops, 0);
+    int n_fold = 0;
     // 1. validation
     for (int i = 0; i < n_ops; ++i) {
         const nt2g_op &o = ops[i];
@@ -487,6 +489,12 @@ extern "C" nt2g_status nt2g_program_create(const nt2g_op *ops, int32_t n_ops, in
                            ops[o.a].dtype, o.dtype);
             slot_use[o.b] |= 2;
             slot_dtype[o.b] = o.dtype;
+            continue;
+        }
+        if (o.code == NT2G_OP_FOLD) {
+            NT2G_CHECK_ARG(o.a >= 0 && o.a < i && is_value_op(ops[o.a].code), "op %d: fold of invalid value %d", i, o.a);
+            NT2G_CHECK_ARG(logical[o.a] || ops[o.a].dtype == NT2G_F32, "op %d: the folded value is not a float", i);
+            NT2G_CHECK_ARG(++n_fold == 1, "op %d: a program folds one value", i);
             continue;
         }
         for (int k = 0; k < na; ++k) {
@@ -526,6 +534,13 @@ extern "C" nt2g_status nt2g_program_create(const nt2g_op *ops, int32_t n_ops, in
             cse_logical.push_back(logical[i]);
             continue;
         }
+        if (o.code == NT2G_OP_FOLD) {
+            o.a = remap[o.a];
+            o.b = o.c = -1;
+            cse.push_back(o);
+            cse_logical.push_back(0);
+            continue;
+        }
         if (na >= 1 && o.code != NT2G_OP_LOAD && o.code != NT2G_OP_SCALAR) o.a = remap[o.a];
         if (na >= 2) o.b = remap[o.b];
         if (na >= 3) o.c = remap[o.c];
@@ -552,6 +567,11 @@ extern "C" nt2g_status nt2g_program_create(const nt2g_op *ops, int32_t n_ops, in
         const nt2g_op &o = cse[i];
         if (o.code == NT2G_OP_STORE) {
             if (final_store[o.b] != i) continue;
+            live[i] = 1;
+            live[o.a] = 1;
+            continue;
+        }
+        if (o.code == NT2G_OP_FOLD) {
             live[i] = 1;
             live[o.a] = 1;
             continue;
@@ -583,13 +603,18 @@ extern "C" nt2g_status nt2g_program_create(const nt2g_op *ops, int32_t n_ops, in
     p->n_slots = n_slots;
     p->slot_use = slot_use;
     p->slot_dtype = slot_dtype;
-    bool has_store = false;
-    for (const nt2g_op &o : p->ops) has_store |= o.code == NT2G_OP_STORE;
-    if (!has_store) {
+    bool has_store = false, has_fold = false;
+    for (const nt2g_op &o : p->ops) {
+        has_store |= o.code == NT2G_OP_STORE;
+        has_fold |= o.code == NT2G_OP_FOLD;
+    }
+    if (has_store == has_fold) {
         delete p;
-        set_error("nt2g_program_create: the program stores nothing");
+        set_error(has_fold ? "nt2g_program_create: a program either folds one value or stores"
+                           : "nt2g_program_create: the program stores nothing");
         return NT2G_ERR_INVALID;
     }
+    p->folds = has_fold;
     // 4. register allocation for the interpreter
     const int n = (int)p->ops.size();
     if (n > kMaxInstr) {
@@ -667,9 +692,10 @@ extern "C" nt2g_status nt2g_program_create(const nt2g_op *ops, int32_t n_ops, in
         set_error("nt2g_program_create: %d live values exceed the %d interpreter registers", n_regs, kMaxRegs);
         return NT2G_ERR_UNSUPPORTED;
     }
-    // 5. fused-kernel binding
-    for (const Pattern &pat : patterns())
-        if (try_bind(*p, pat)) break;
+    // 5. fused-kernel binding (transforms only)
+    if (!p->folds)
+        for (const Pattern &pat : patterns())
+            if (try_bind(*p, pat)) break;
     *out = p;
     return NT2G_OK;
 }
@@ -690,6 +716,40 @@ extern "C" void nt2g_program_destroy(nt2g_program *p) { delete p; }
 
 static size_t dtype_size(int dt) { return dt == NT2G_U8 ? 1 : 4; }
 
+// The device arguments of a program over elements [offset, offset + count):
+// scalars converted, table pointers advanced to element `offset`, and (for a
+// non-empty range) every table checked reachable from the device.
+static nt2g_status bind_args(const nt2g_program *p, const nt2g_arg *args, int64_t offset, int64_t count,
+                             const char *who, DArgs &da)
+{
+    da = DArgs{};
+    da.pos0 = offset;
+    for (int s = 0; s < p->n_slots; ++s) {
+        const int use = p->slot_use[s];
+        if (!use) continue;
+        const nt2g_arg &a = args[s];
+        if (use & 4) {
+            NT2G_CHECK_ARG(a.kind == 1, "%s: slot %d must be a scalar", who, s);
+            da.scal[s] = (float)a.scalar;
+            double u = a.scalar;
+            da.scal_u8[s] = (uint32_t)(u < 0 ? 0 : u > 255 ? 255 : u);
+            da.dtype[s] = p->slot_dtype[s];
+        } else {
+            NT2G_CHECK_ARG(a.kind == 0, "%s: slot %d must be a table", who, s);
+            NT2G_CHECK_ARG(a.dtype == p->slot_dtype[s], "%s: slot %d has dtype %d, program expects %d", who, s,
+                           a.dtype, p->slot_dtype[s]);
+            NT2G_CHECK_ARG(a.ptr != nullptr || count == 0, "%s: slot %d table pointer is NULL", who, s);
+            da.ptr[s] = a.ptr ? (char *)a.ptr + offset * dtype_size(a.dtype) : nullptr;
+            da.dtype[s] = a.dtype;
+        }
+    }
+    if (count == 0) return NT2G_OK;
+    for (int s = 0; s < p->n_slots; ++s)
+        NT2G_CHECK_ARG(!(p->slot_use[s] & 3) || reachable(da.ptr[s]),
+                       "%s: slot %d is host memory the device cannot access (pin or register it)", who, s);
+    return NT2G_OK;
+}
+
 extern "C" nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t offset,
                                  int64_t count, int32_t precision, int32_t force_generic, void *stream)
 {
@@ -699,32 +759,12 @@ extern "C" nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, in
     NT2G_CHECK_ARG(offset >= 0 && count >= 0, "nt2g_eval: negative range (%lld, %lld)", (long long)offset,
                    (long long)count);
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_eval: precision %d", precision);
+    NT2G_CHECK_ARG(!p->folds, "nt2g_eval: the program folds its value (nt2g_eval_fold)");
     cudaStream_t st = (cudaStream_t)stream;
     DArgs da{};
-    da.pos0 = offset;
-    for (int s = 0; s < p->n_slots; ++s) {
-        const int use = p->slot_use[s];
-        if (!use) continue;
-        const nt2g_arg &a = args[s];
-        if (use & 4) {
-            NT2G_CHECK_ARG(a.kind == 1, "nt2g_eval: slot %d must be a scalar", s);
-            da.scal[s] = (float)a.scalar;
-            double u = a.scalar;
-            da.scal_u8[s] = (uint32_t)(u < 0 ? 0 : u > 255 ? 255 : u);
-            da.dtype[s] = p->slot_dtype[s];
-        } else {
-            NT2G_CHECK_ARG(a.kind == 0, "nt2g_eval: slot %d must be a table", s);
-            NT2G_CHECK_ARG(a.dtype == p->slot_dtype[s], "nt2g_eval: slot %d has dtype %d, program expects %d", s,
-                           a.dtype, p->slot_dtype[s]);
-            NT2G_CHECK_ARG(a.ptr != nullptr || count == 0, "nt2g_eval: slot %d table pointer is NULL", s);
-            da.ptr[s] = a.ptr ? (char *)a.ptr + offset * dtype_size(a.dtype) : nullptr;
-            da.dtype[s] = a.dtype;
-        }
-    }
+    nt2g_status bs = bind_args(p, args, offset, count, "nt2g_eval", da);
+    if (bs != NT2G_OK) return bs;
     if (count == 0) return NT2G_OK;
-    for (int s = 0; s < p->n_slots; ++s)
-        NT2G_CHECK_ARG(!(p->slot_use[s] & 3) || reachable(da.ptr[s]),
-                       "nt2g_eval: slot %d is host memory the device cannot access (pin or register it)", s);
     int kernel = force_generic ? kGeneric : p->kernel;
     for (const DeferredConst &dc : p->deferred)
         if ((float)args[dc.slot].scalar != dc.value) kernel = kGeneric;
@@ -762,10 +802,48 @@ extern "C" nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, in
     return launch_interp(p->dprog, da, count, precision, st);
 }
 
+extern "C" nt2g_status nt2g_eval_fold(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t lo,
+                                      int64_t inner, int64_t hi, int32_t op, int32_t precision, void *workspace,
+                                      size_t workspace_bytes, float *out, int64_t *index, double *out64, void *stream)
+{
+    NT2G_CHECK_ARG(p != nullptr, "nt2g_eval_fold: NULL program");
+    NT2G_CHECK_ARG(p->folds, "nt2g_eval_fold: the program has no FOLD instruction");
+    NT2G_CHECK_ARG(n_args >= p->n_slots && (args != nullptr || p->n_slots == 0),
+                   "nt2g_eval_fold: %d arguments for %d slots", n_args, p->n_slots);
+    NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_eval_fold: negative extent (%lld, %lld, %lld)",
+                   (long long)lo, (long long)inner, (long long)hi);
+    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_NANMEAN, "nt2g_eval_fold: op %d", op);
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2 || precision == NT2G_PREC_NT2_ELEMENTS,
+                   "nt2g_eval_fold: precision %d", precision);
+    NT2G_CHECK_ARG(index == nullptr || op == NT2G_FOLD_MAX || op == NT2G_FOLD_MIN,
+                   "nt2g_eval_fold: an index is defined for max and min only");
+    NT2G_CHECK_ARG(out64 == nullptr || (precision != NT2G_PREC_NT2 && op != NT2G_FOLD_MAX && op != NT2G_FOLD_MIN),
+                   "nt2g_eval_fold: FP64 results are given for sum-type and product folds of the compensated fold");
+    const int64_t n_out = lo * hi;
+    DArgs da{};
+    nt2g_status bs = bind_args(p, args, 0, n_out * inner, "nt2g_eval_fold", da);
+    if (bs != NT2G_OK) return bs;
+    if (n_out == 0) return NT2G_OK;
+    NT2G_CHECK_ARG(out != nullptr, "nt2g_eval_fold: out is NULL");
+    size_t need = 0;
+    const bool centred = (op >= NT2G_FOLD_VAR && op <= NT2G_FOLD_STDEV1) || op == NT2G_FOLD_NANMEAN;
+    if (centred) fold_workspace_bytes(lo, inner, hi, &need);
+    else fold_partials_bytes(lo, inner, hi, &need);
+    NT2G_CHECK_ARG((precision == NT2G_PREC_NT2 && !centred) || need == 0 ||
+                       (workspace != nullptr && workspace_bytes >= need),
+                   "nt2g_eval_fold: workspace of %zu bytes, %zu needed", workspace_bytes, need);
+    NT2G_CHECK_ARG(((uintptr_t)workspace & 15u) == 0, "nt2g_eval_fold: workspace not 16-byte aligned");
+    NT2G_CHECK_ARG(reachable(out) && reachable(index) && reachable(out64) && reachable(workspace),
+                   "nt2g_eval_fold: an output or the workspace is host memory the device cannot access");
+    return launch_fold_expr(p->ops, p->logical, da, lo, inner, hi, op, precision, workspace, workspace_bytes, out,
+                            index, out64, (cudaStream_t)stream);
+}
+
 extern "C" nt2g_status nt2g_program_jit_source(const nt2g_program *p, int32_t precision, char *buf, size_t cap,
                                                size_t *len)
 {
     NT2G_CHECK_ARG(p != nullptr, "nt2g_program_jit_source: NULL program");
+    NT2G_CHECK_ARG(!p->folds, "nt2g_program_jit_source: the program folds its value (nt2g_program_fold_source)");
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_program_jit_source: precision %d",
                    precision);
     NT2G_CHECK_ARG(buf != nullptr || cap == 0, "nt2g_program_jit_source: NULL buffer");
@@ -773,6 +851,23 @@ extern "C" nt2g_status nt2g_program_jit_source(const nt2g_program *p, int32_t pr
     if (len) *len = src.size() + 1;
     if (cap == 0) return NT2G_OK;
     NT2G_CHECK_ARG(cap > src.size(), "nt2g_program_jit_source: %zu-byte buffer, %zu needed", cap, src.size() + 1);
+    memcpy(buf, src.c_str(), src.size() + 1);
+    return NT2G_OK;
+}
+
+extern "C" nt2g_status nt2g_program_fold_source(const nt2g_program *p, int32_t precision, int32_t op, char *buf,
+                                                size_t cap, size_t *len)
+{
+    NT2G_CHECK_ARG(p != nullptr, "nt2g_program_fold_source: NULL program");
+    NT2G_CHECK_ARG(p->folds, "nt2g_program_fold_source: the program has no FOLD instruction");
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2 || precision == NT2G_PREC_NT2_ELEMENTS,
+                   "nt2g_program_fold_source: precision %d", precision);
+    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_NANMEAN, "nt2g_program_fold_source: op %d", op);
+    NT2G_CHECK_ARG(buf != nullptr || cap == 0, "nt2g_program_fold_source: NULL buffer");
+    std::string src = jit_fold_source(p->ops, p->logical, precision, op);
+    if (len) *len = src.size() + 1;
+    if (cap == 0) return NT2G_OK;
+    NT2G_CHECK_ARG(cap > src.size(), "nt2g_program_fold_source: %zu-byte buffer, %zu needed", cap, src.size() + 1);
     memcpy(buf, src.c_str(), src.size() + 1);
     return NT2G_OK;
 }
@@ -1015,6 +1110,33 @@ extern "C" nt2g_status nt2g_memcpy(void *dst, const void *src, size_t bytes, int
     cudaMemcpyKind k = kind == 1 ? cudaMemcpyHostToDevice : kind == 2 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     cudaError_t e = cudaMemcpyAsync(dst, src, bytes, k, (cudaStream_t)stream);
     return e == cudaSuccess ? NT2G_OK : cuda_status(e, "nt2g_memcpy");
+}
+
+extern "C" nt2g_status nt2g_device_current(int32_t *device)
+{
+    NT2G_CHECK_ARG(device != nullptr, "nt2g_device_current: device is NULL");
+    int d = 0;
+    cudaError_t e = cudaGetDevice(&d);
+    if (e != cudaSuccess) return cuda_status(e, "nt2g_device_current");
+    *device = d;
+    return NT2G_OK;
+}
+
+extern "C" nt2g_status nt2g_stream_create(void **stream)
+{
+    NT2G_CHECK_ARG(stream != nullptr, "nt2g_stream_create: stream is NULL");
+    cudaStream_t st = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e, "nt2g_stream_create");
+    *stream = st;
+    return NT2G_OK;
+}
+
+extern "C" nt2g_status nt2g_stream_destroy(void *stream)
+{
+    NT2G_CHECK_ARG(stream != nullptr, "nt2g_stream_destroy: NULL stream");
+    cudaError_t e = cudaStreamDestroy((cudaStream_t)stream);
+    return e == cudaSuccess ? NT2G_OK : cuda_status(e, "nt2g_stream_destroy");
 }
 
 extern "C" nt2g_status nt2g_stream_synchronize(void *stream)

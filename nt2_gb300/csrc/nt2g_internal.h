@@ -89,9 +89,30 @@ nt2g_status launch_scan(const float *x, int64_t lo, int64_t inner, int64_t hi, i
                         size_t ws_bytes, float *out, cudaStream_t st);
 nt2g_status launch_fold(const float *x, int64_t lo, int64_t inner, int64_t hi, int op, int precision, void *ws,
                         size_t ws_bytes, float *out, int64_t *index, cudaStream_t st);
+// The same fold over the FOLD value of a program (its element function
+// compiled at run time); out64 (optional, fast policy) receives the FP64
+// results of sum-type and product folds.
+nt2g_status launch_fold_expr(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, const DArgs &args,
+                             int64_t lo, int64_t inner, int64_t hi, int op, int precision, void *ws, size_t ws_bytes,
+                             float *out, int64_t *index, double *out64, cudaStream_t st);
 
 // Run-time compiled kernels of generic programs (nt2g_jit.cu).  The program is
 // the canonical SSA form; logical[k] marks comparison results.
+//
+// Fold kernels of a program with a FOLD instruction: the first-phase kernels
+// of nt2g_fold_kernels.cuh (NT2-order, short-segment, contiguous inner[FINAL][IDX],
+// strided outer[VEC == 4][FINAL]) instantiated over the program's element
+// function, for one fold op; nullptr, with the reason in *why, when NVRTC is
+// unavailable or rejects the source.
+struct JitFoldKernels {
+    cudaKernel_t nt2 = nullptr, shrt = nullptr;
+    cudaKernel_t inner[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    cudaKernel_t outer[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+};
+const JitFoldKernels *jit_fold_kernels(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical,
+                                       int precision, int op, std::string *why);
+std::string jit_fold_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision,
+                            int op);
 std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision);
 bool jit_enabled();
 nt2g_status jit_prepare(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision);

@@ -26,7 +26,9 @@
 #include <vector>
 #include "nt2g_common.cuh"
 #include "nt2g_internal.h"
-#include "nt2g_math_src.h"  // kNt2gMathSrc: nt2g_math.cuh as a string (generated at build)
+#include "nt2g_math_src.h"   // kNt2gMathSrc: nt2g_math.cuh as a string (generated at build)
+#include "nt2g_accum_src.h"  // kNt2gAccumSrc: nt2g_accum.cuh
+#include "nt2g_fold_src.h"   // kNt2gFoldSrc: nt2g_fold_kernels.cuh
 
 namespace nt2g {
 
@@ -83,6 +85,7 @@ static Nvrtc &nvrtc()
 static const char kJitPrelude[] = R"NT2G_SRC(
 struct JitArgs { void *ptr[16]; float scal[16]; unsigned scal_u8[16]; int dtype[16]; long long pos0; };
 #define NT2G_L _Pragma("unroll") for (int j = 0; j < 4; ++j)
+#define NT2G_LL _Pragma("unroll") for (int j = 0; j < L; ++j)
 template <bool FULL> __device__ __forceinline__ void jit_ldf(float (&d)[4], const void *p, long long i, int cnt)
 {
     const float *q = (const float *)p + i;
@@ -118,13 +121,11 @@ static std::string fconst(float f)
     return b;
 }
 
-std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision)
+// The statements of a program over L lanes (4 consecutive elements per call
+// in a transform; 1 or 4 in a fold's element function).  STORE writes the
+// output tables; FOLD (fold programs) hands the folded value to out[].
+static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical)
 {
-    std::string s;
-    s.reserve(sizeof kJitPrelude + 40000 + ops.size() * 96);
-    s += kNt2gMathSrc;
-    s += kJitPrelude;
-    s += "template <class P, bool FULL>\n__device__ __forceinline__ void jit_tile(const JitArgs &a, long long i, int cnt)\n{\n";
     auto v = [](int x) { return "v" + std::to_string(x) + "[j]"; };
     // every table load first, so a tile's memory requests are in flight while its
     // arithmetic runs (a load never follows a store to its table: the compiler
@@ -167,7 +168,7 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
             // the positive side is the one whose argument is y itself
             const bool k_is_neg = ops[o.a].code == NT2G_OP_NEG && ops[o.a].a == ops[p].a;
             const int pos = k_is_neg ? p : (int)k, neg = k_is_neg ? (int)k : p;
-            s += "    float v" + std::to_string(k) + "[4], v" + std::to_string(p) + "[4]; NT2G_L nt2g::normcdf_pair<P>(" +
+            s += "    float v" + std::to_string(k) + "[4], v" + std::to_string(p) + "[4]; NT2G_LL nt2g::normcdf_pair<P>(" +
                  v(ops[pos].a) + ", " + v(pos) + ", " + v(neg) + ");\n";
             continue;
         }
@@ -176,11 +177,14 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         std::string e;
         switch (o.code) {
         case NT2G_OP_LOAD: continue;  // emitted above
+        case NT2G_OP_FOLD:  // a comparison result folds as 0.0f / 1.0f
+            s += "    NT2G_LL out[j] = (float)v" + std::to_string(o.a) + "[j];\n";
+            continue;
         case NT2G_OP_STORE: {
             const std::string src = "v" + std::to_string(o.a);
             const std::string dst = std::to_string(o.b);
             if (f32 && logical[o.a])  // a comparison result stored as 0.0f / 1.0f
-                s += "    { float t[4]; NT2G_L t[j] = (float)" + src + "[j]; jit_stf<FULL>(a.ptr[" + dst + "], i, cnt, t); }\n";
+                s += "    { float t[4]; NT2G_LL t[j] = (float)" + src + "[j]; jit_stf<FULL>(a.ptr[" + dst + "], i, cnt, t); }\n";
             else
                 s += std::string(f32 ? "    jit_stf<FULL>(a.ptr[" : "    jit_stb<FULL>(a.ptr[") + dst + "], i, cnt, " +
                      src + ");\n";
@@ -296,9 +300,20 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
         case NT2G_OP_ATANH: e = "nt2g::atanh<P>(" + A + ")"; break;
         default: e = "nt2g::fastnormcdf<P>(" + A + ")"; break;
         }
-        s += std::string(u ? "    unsigned v" : "    float v") + std::to_string(k) + "[4]; NT2G_L v" +
+        s += std::string(u ? "    unsigned v" : "    float v") + std::to_string(k) + "[4]; NT2G_LL v" +
              std::to_string(k) + "[j] = " + e + ";\n";
     }
+}
+
+std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision)
+{
+    std::string s;
+    s.reserve(sizeof kJitPrelude + 40000 + ops.size() * 96);
+    s += kNt2gMathSrc;
+    s += kJitPrelude;
+    s += "template <class P, bool FULL>\n__device__ __forceinline__ void jit_tile(const JitArgs &a, long long i, int cnt)\n{\n"
+         "    constexpr int L = 4;\n";
+    emit_body(s, ops, logical);
     s += "}\n\nextern \"C\" __global__ void __launch_bounds__(256) nt2g_jit_kernel(const JitArgs a, long long n, int vec)\n{\n";
     s += precision == NT2G_PREC_NT2 ? "    typedef nt2g::Nt2 P;\n" : "    typedef nt2g::Fast P;\n";
     s += "    const long long stride = (long long)gridDim.x * blockDim.x * 4;\n"
@@ -307,6 +322,66 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
          "        if (vec && cnt == 4) jit_tile<P, true>(a, i, 4);\n"
          "        else jit_tile<P, false>(a, i, cnt);\n"
          "    }\n}\n";
+    return s;
+}
+
+// A fold of a program's FOLD value: the program becomes the element function
+// jit_value (L = 1: one element; L = 4: four consecutive elements, 128-bit
+// table reads when FULL), wrapped as the fold source ExprSrc, and the fold
+// bodies of nt2g_fold_kernels.cuh are instantiated over it for op.  The NT2
+// policy folds in index order (fold_nt2) only; the fast policy and NT2's
+// elements under the compensated fold also get the short-segment, contiguous
+// (FINAL x IDX) and strided (VEC x FINAL) kernels.
+std::string jit_fold_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision,
+                            int op)
+{
+    std::string s;
+    s.reserve(sizeof kJitPrelude + sizeof kNt2gAccumSrc + sizeof kNt2gFoldSrc + 40000 + ops.size() * 96);
+    s += kNt2gMathSrc;
+    s += kJitPrelude;
+    s += kNt2gAccumSrc;
+    s += kNt2gFoldSrc;
+    s += "template <class P, bool FULL, int L>\n__device__ __forceinline__ void jit_value(const JitArgs &a, long long i, "
+         "int cnt, float (&out)[4])\n{\n";
+    emit_body(s, ops, logical);
+    s += "}\n\n";
+    s += precision == NT2G_PREC_FAST ? "typedef nt2g::Fast P;\n" : "typedef nt2g::Nt2 P;\n";
+    s += "struct ExprSrc {\n"
+         "    JitArgs a;\n"
+         "    __device__ __forceinline__ float at(long long pos) const { float o[4]; jit_value<P, false, 1>(a, pos, 1, o); "
+         "return o[0]; }\n"
+         "    __device__ __forceinline__ float4 at4(long long pos) const { float o[4]; jit_value<P, true, 4>(a, pos, 4, o); "
+         "return make_float4(o[0], o[1], o[2], o[3]); }\n"
+         "};\n";
+    s += "#define NT2G_FOP " + std::to_string(op) + "\n";
+    s += "using nt2g::fold::Partial;\n"
+         "extern \"C\" __global__ void __launch_bounds__(256) fold_nt2(const JitArgs a, long long lo, long long inner, "
+         "long long hi, float *out, long long *index, const float *cen)\n"
+         "{ nt2g::fold::nt2_body<ExprSrc, NT2G_FOP>(ExprSrc{a}, lo, inner, hi, out, index, cen); }\n";
+    if (precision == NT2G_PREC_NT2) return s;
+    s += "extern \"C\" __global__ void __launch_bounds__(256) fold_short(const JitArgs a, long long inner, long long hi, "
+         "float *out, long long *index, const float *cen, double *out64)\n"
+         "{ nt2g::fold::short_body<ExprSrc, NT2G_FOP>(ExprSrc{a}, inner, hi, out, index, cen, out64); }\n";
+    for (int fin = 0; fin < 2; ++fin)
+        for (int idx = 0; idx < 2; ++idx) {
+            const std::string F = fin ? "true" : "false", I = idx ? "true" : "false";
+            s += "extern \"C\" __global__ void __launch_bounds__(256) fold_inner_" + std::to_string(fin) +
+                 std::to_string(idx) +
+                 "(const JitArgs a, long long inner, long long hi, long long chunk, long long q, int vec, Partial *part, "
+                 "float *out, long long *index, const float *cen, double *out64)\n"
+                 "{ nt2g::fold::inner_body<ExprSrc, NT2G_FOP, " + F + ", " + I +
+                 ">(ExprSrc{a}, inner, hi, chunk, q, vec, part, out, index, cen, out64); }\n";
+        }
+    for (int v4 = 0; v4 < 2; ++v4)
+        for (int fin = 0; fin < 2; ++fin) {
+            const std::string V = v4 ? "4" : "1", F = fin ? "true" : "false";
+            s += "extern \"C\" __global__ void __launch_bounds__(256) fold_outer_" + std::to_string(v4) +
+                 std::to_string(fin) +
+                 "(const JitArgs a, long long lo, long long inner, long long hi, long long ck, long long q, "
+                 "Partial *part, float *out, long long *index, const float *cen, double *out64)\n"
+                 "{ nt2g::fold::outer_body<ExprSrc, NT2G_FOP, " + V + ", " + F +
+                 ">(ExprSrc{a}, lo, inner, hi, ck, q, part, out, index, cen, out64); }\n";
+        }
     return s;
 }
 
@@ -384,6 +459,59 @@ static JitEntry *jit_get(const std::vector<nt2g_op> &ops, const std::vector<uint
         return nullptr;
     }
     return &it->second;
+}
+
+struct JitFoldEntry {
+    cudaLibrary_t lib = nullptr;
+    JitFoldKernels k;
+    bool ok = false;
+    std::string error;
+};
+static std::map<std::string, JitFoldEntry> g_fold_cache;  // key: device | precision | op | program text
+
+const JitFoldKernels *jit_fold_kernels(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical,
+                                       int precision, int op, std::string *why)
+{
+    if (!jit_enabled()) {
+        if (why) *why = "JIT disabled (NT2G_JIT=0)";
+        return nullptr;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::string key = std::to_string(dev) + "|" + std::to_string(precision) + "|" + std::to_string(op) + "|";
+    key.append((const char *)ops.data(), ops.size() * sizeof(nt2g_op));
+    key.append((const char *)logical.data(), logical.size());
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_fold_cache.find(key);
+    if (it == g_fold_cache.end()) {
+        JitFoldEntry e;
+        std::string cubin = compile_cubin(jit_fold_source(ops, logical, precision, op), e.error);
+        if (!cubin.empty()) {
+            cudaError_t ce = cudaLibraryLoadData(&e.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+            if (ce == cudaSuccess) ce = cudaLibraryGetKernel(&e.k.nt2, e.lib, "fold_nt2");
+            if (precision != NT2G_PREC_NT2) {
+                if (ce == cudaSuccess) ce = cudaLibraryGetKernel(&e.k.shrt, e.lib, "fold_short");
+                for (int a = 0; a < 2; ++a)
+                    for (int b = 0; b < 2; ++b) {
+                        const std::string ab = std::to_string(a) + std::to_string(b);
+                        if (ce == cudaSuccess) ce = cudaLibraryGetKernel(&e.k.inner[a][b], e.lib, ("fold_inner_" + ab).c_str());
+                        if (ce == cudaSuccess) ce = cudaLibraryGetKernel(&e.k.outer[a][b], e.lib, ("fold_outer_" + ab).c_str());
+                    }
+            }
+            if (ce == cudaSuccess) {
+                e.ok = true;
+            } else {
+                e.error = std::string("loading the JIT fold kernels: ") + cudaGetErrorString(ce);
+                cudaGetLastError();
+            }
+        }
+        it = g_fold_cache.emplace(key, e).first;
+    }
+    if (!it->second.ok) {
+        if (why) *why = it->second.error;
+        return nullptr;
+    }
+    return &it->second.k;
 }
 
 bool jit_enabled()

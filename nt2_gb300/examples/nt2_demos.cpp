@@ -10,7 +10,8 @@
 // usage: nt2_demos lower
 //        nt2_demos bs|bs_host|bs_demo|saxpy|rgb2yuv DIR N
 //        nt2_demos sdot DIR N
-//        nt2_demos fold DIR M N
+//        nt2_demos threads|streams DIR N   (reductions from two host threads / on two streams)
+//        nt2_demos fold|fold_expr DIR M N
 //        nt2_demos gen DIR N
 //        nt2_demos sigmadelta DIR PIXELS FRAMES
 // Inputs and outputs are raw little-endian arrays DIR/<name>.bin.
@@ -18,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "nt2/table.hpp"
@@ -135,7 +137,8 @@ static int lower_only()
 int main(int argc, char **argv)
 {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: %s lower | bs|bs_host|bs_demo|saxpy|rgb2yuv|sdot DIR N | sigmadelta DIR PIXELS FRAMES\n",
+        std::fprintf(stderr, "usage: %s lower | bs|bs_host|bs_demo|saxpy|rgb2yuv|sdot|threads|streams DIR N | "
+                             "fold|fold_expr DIR M N | sigmadelta DIR PIXELS FRAMES\n",
                      argv[0]);
         return 2;
     }
@@ -186,8 +189,72 @@ int main(int argc, char **argv)
             auto X = load<dtable>(dir + "x.bin", n), Y = load<dtable>(dir + "y.bin", n);
             std::printf("globalsum %.17g\nsum64 %.17g\ndot %.9g\nsum %.9g\n", (double)nt2::globalsum(X * Y),
                         nt2::sum64(X * Y), (double)nt2::dot(X, Y), (double)nt2::sum(X));
-            // sum of a general expression goes through a temporary
+            // a sum of a general expression is folded in one pass (no temporary)
             std::printf("sum_expr %.17g\n", nt2::sum64(nt2::sqr(X) + Y));
+        } else if (mode == "fold_expr") {
+            // reductions of expressions over an M x N pair of tables (N = argv[4]), in one pass each
+            const std::size_t cols = std::strtoull(argv[4], nullptr, 10);
+            nt2::table<float> ha(nt2::of_size(n, cols)), hb(nt2::of_size(n, cols));
+            auto va = read_bin<float>(dir + "a.bin", n * cols), vb = read_bin<float>(dir + "b.bin", n * cols);
+            std::memcpy(ha.data(), va.data(), va.size() * sizeof(float));
+            std::memcpy(hb.data(), vb.data(), vb.size() * sizeof(float));
+            dtable A, B;
+            A = ha;
+            B = hb;
+            save(dir + "sumabs1.bin", nt2::sum(nt2::abs(A - B), 1));
+            save(dir + "maxexp2.bin", nt2::maximum(nt2::exp(A) - B, 2));
+            save(dir + "var1.bin", nt2::var(A * B + 1.0f, 0, 1));
+            std::int64_t imax = 0;
+            const float gmax = nt2::globalmax(A * B + 1.0f, imax);
+            std::printf("globalmax %.9g %lld\nglobalsum %.17g\nglobalmean %.9g\n", (double)gmax, (long long)imax,
+                        nt2::sum64(nt2::exp(A) * B), (double)nt2::globalmean(nt2::abs(A - B)));
+        } else if (mode == "threads") {
+            // two host threads, each on its own stream with its own tables, reduce concurrently:
+            // every repetition must reproduce that thread's first results bit for bit
+            auto X = load<dtable>(dir + "x.bin", n), Y = load<dtable>(dir + "y.bin", n);
+            auto worker = [&](int id, double *res) {
+                void *st = nullptr;
+                nt2::check(nt2g_stream_create(&st), "stream");
+                nt2::options().stream = st;
+                dtable x(nt2::of_size(n)), y(nt2::of_size(n));
+                x = X * (float)(id + 1);
+                y = Y + (float)id;
+                res[0] = nt2::sum64(x);
+                res[1] = nt2::sum64(x * y);
+                res[2] = nt2::sum64(nt2::exp(y) * x);
+                int bad = 0;
+                for (int k = 0; k < 40; ++k)
+                    bad += nt2::sum64(x) != res[0] || nt2::sum64(x * y) != res[1] ||
+                           nt2::sum64(nt2::exp(y) * x) != res[2];
+                res[3] = bad;
+                nt2::check(nt2g_stream_synchronize(st), "stream");
+                nt2g_stream_destroy(st);
+            };
+            double r0[4] = {}, r1[4] = {};
+            std::thread t0(worker, 0, r0), t1(worker, 1, r1);
+            t0.join();
+            t1.join();
+            for (const double *r : {r0, r1}) std::printf("%.17g %.17g %.17g %d\n", r[0], r[1], r[2], (int)r[3]);
+        } else if (mode == "streams") {
+            // one thread, two streams: asynchronous sums in flight on both at once, each stream its own scratch
+            auto X = load<dtable>(dir + "x.bin", n), Y = load<dtable>(dir + "y.bin", n);
+            void *st[2] = {nullptr, nullptr};
+            for (auto &s : st) nt2::check(nt2g_stream_create(&s), "stream");
+            nt2::detail::device_buffer res(2 * 16 * sizeof(double));
+            double *d = (double *)res.p;
+            for (int k = 0; k < 16; ++k)
+                for (int s = 0; s < 2; ++s) {
+                    nt2::options().stream = st[s];
+                    if (s == 0) nt2::sum64_async(X * Y, d + k);
+                    else nt2::sum64_async(nt2::exp(X) * Y, d + 16 + k);
+                }
+            std::vector<double> h(32);
+            for (auto s : st) nt2::check(nt2g_stream_synchronize(s), "stream");
+            nt2::options().stream = nullptr;
+            nt2::check(nt2g_memcpy(h.data(), d, 32 * sizeof(double), 2, nullptr), "results");
+            nt2::check(nt2g_stream_synchronize(nullptr), "results");
+            for (auto s : st) nt2g_stream_destroy(s);
+            for (double v : h) std::printf("%.17g\n", v);
         } else if (mode == "fold") {
             // an M x N table (N = argv[4]): per-column and per-row reductions, then the global forms
             const std::size_t cols = std::strtoull(argv[4], nullptr, 10);

@@ -384,8 +384,9 @@ def _compare_dtype(n):
     return n.args[0].dtype
 
 
-def lower(outs, exprs):
-    """tie(outs) = tie(exprs) -> (ops, slot tensors/scalars)."""
+def lower(outs, exprs, fold=None):
+    """tie(outs) = tie(exprs) -> (ops, slot tensors/scalars); with fold (and
+    no outs), the program that folds that expression's value."""
     slots, slot_of = [], {}
 
     def slot(key, value):
@@ -424,6 +425,8 @@ def lower(outs, exprs):
         dt = lib.U8 if o.dtype.is_floating_point is False else lib.F32
         s = slot(("t", o.data_ptr(), o.dtype), o)
         ops.append((lib.OP["STORE"], dt, v, s, -1, 0.0))
+    if fold is not None:
+        ops.append((lib.OP["FOLD"], lib.F32, emit(fold), -1, -1, 0.0))
     return ops, slots
 
 
@@ -447,6 +450,14 @@ class Program:
         lib.check(L.nt2g_program_jit_source(self.handle, precision, buf, n.value, ctypes.byref(n)))
         return buf.value.decode()
 
+    def fold_source(self, op="sum", precision=lib.PREC_FAST):
+        """CUDA source of this fold program's run-time compiled fold kernels."""
+        L, n = lib.load(), ctypes.c_size_t()
+        lib.check(L.nt2g_program_fold_source(self.handle, precision, lib.FOLD[op], None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        lib.check(L.nt2g_program_fold_source(self.handle, precision, lib.FOLD[op], buf, n.value, ctypes.byref(n)))
+        return buf.value.decode()
+
     def jit_prepare(self, precision=lib.PREC_FAST):
         """Compile and load the run-time compiled kernel now; raises Nt2gError when it is unavailable."""
         lib.check(lib.load().nt2g_program_jit_prepare(self.handle, precision))
@@ -462,8 +473,8 @@ class Program:
 _cache = {}
 
 
-def compile_program(outs, exprs):
-    ops, slots = lower(outs, exprs)
+def compile_program(outs, exprs, fold=None):
+    ops, slots = lower(outs, exprs, fold)
     key = (tuple(ops), len(slots))
     prog = _cache.get(key)
     if prog is None:
@@ -494,3 +505,45 @@ def assign(outs, exprs, precision=lib.PREC_FAST, offset=0, count=None, force_gen
     lib.check(lib.load().nt2g_eval(prog.handle, args, len(slots), offset, count, precision,
                                    int(force_generic), lib._stream(stream)))
     return prog
+
+
+def _args_of(slots):
+    import torch
+    args = (lib.Arg * len(slots))()
+    n = None
+    for i, s in enumerate(slots):
+        if isinstance(s, Node):  # a SCALAR leaf
+            args[i] = lib.Arg(None, s.imm, s.dtype, 1)
+        else:
+            n = s.numel() if n is None else min(n, s.numel())
+            args[i] = lib.Arg(s.data_ptr(), 0.0, lib.U8 if s.dtype == torch.uint8 else lib.F32, 0)
+    return args, n
+
+
+def fold(e, op="sum", shape=None, precision=lib.PREC_FAST, index=False, out64=False, stream=None):
+    """NT2's fold of an expression along one dimension in one pass
+    (nt2g_eval_fold): e's value at every element is computed inside the fold
+    kernels, no temporary table.  shape = (lo, inner, hi), the column-major
+    view folded over inner (default: every element, lo = hi = 1).  Returns the
+    float results (lo*hi), then the 0-based first index of max/min (index=True)
+    and the FP64 results (out64=True) when asked."""
+    import torch
+    prog, slots = compile_program([], [], fold=e)
+    args, n = _args_of(slots)
+    if shape is None:
+        if n is None:
+            n = _generative_sizes(e).pop()
+        shape = (1, n, 1)
+    lo, inner, hi = (int(v) for v in shape)
+    dev = next((s.device for s in slots if not isinstance(s, Node)), torch.device("cuda"))
+    nb = ctypes.c_size_t()
+    lib.check(lib.load().nt2g_fold_workspace_size(lo, inner, hi, ctypes.byref(nb)))
+    ws = torch.empty(max(nb.value, 16), dtype=torch.uint8, device=dev)
+    out = torch.empty(lo * hi, dtype=torch.float32, device=dev)
+    idx = torch.empty(lo * hi, dtype=torch.int64, device=dev) if index else None
+    o64 = torch.empty(lo * hi, dtype=torch.float64, device=dev) if out64 else None
+    lib.check(lib.load().nt2g_eval_fold(prog.handle, args, len(slots), lo, inner, hi, lib.FOLD[op], precision,
+                                        lib._ptr(ws), ws.numel(), lib._ptr(out), lib._ptr(idx), lib._ptr(o64),
+                                        lib._stream(stream)))
+    res = [out] + ([idx] if index else []) + ([o64] if out64 else [])
+    return res[0] if len(res) == 1 else tuple(res)

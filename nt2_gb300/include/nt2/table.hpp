@@ -70,14 +70,16 @@ inline of_size_ of_size(std::size_t a, std::size_t b = 1, std::size_t c = 1, std
     return s;
 }
 
-// Evaluation options: arithmetic policy and the stream every call uses.
+// Evaluation options: arithmetic policy and the stream every call uses, per
+// host thread (each thread evaluates on its own stream; a new thread starts
+// with the fast policy on the default stream).
 struct gpu_options {
     int precision = NT2G_PREC_FAST;
     void *stream = nullptr;
 };
 inline gpu_options &options()
 {
-    static gpu_options o;
+    thread_local gpu_options o;
     return o;
 }
 
@@ -96,6 +98,7 @@ struct node {
     void *dev_ptr = nullptr;           // device storage of a device table leaf
     const void *host_ptr = nullptr;    // host storage of a host table leaf
     std::size_t numel = 0;
+    std::size_t ext[4] = {0, 0, 0, 0};  // extent of a table leaf
     std::shared_ptr<node> a, b, c;
 };
 using node_ptr = std::shared_ptr<node>;
@@ -269,6 +272,7 @@ template <class T, class S> node_ptr leaf(const table<T, S> &t)
     auto n = make(NT2G_OP_LOAD, dtype_of<T>::value);
     n->table_key = t.data();
     n->numel = t.numel();
+    for (int k = 0; k < 4; ++k) n->ext[k] = t.extent().d[k];
     if constexpr (table<T, S>::on_device) n->dev_ptr = (void *)t.data();
     else n->host_ptr = t.data();
     return n;
@@ -920,26 +924,23 @@ template <class T> expr<T> if_zero_else_one(const expr<T> &cond)
 
 // ------------------------------------------------------------ reductions --
 namespace detail {
-struct reduce_ws {
+// Reduction scratch (workspace and result words) of the calling thread on the
+// current device and stream, allocated on first use and kept for the thread's
+// lifetime: no two host threads share one, a call after a device switch gets
+// that device's memory, and reductions in flight on two streams never share
+// one (one stream's are ordered by the stream).
+struct scratch {
     device_buffer ws, out;
-    reduce_ws()
-    {
-        std::size_t b = 0;
-        check(nt2g_reduce_workspace_size(0, &b), "reduce workspace");
-        ws = device_buffer(b);
-        out = device_buffer(16);
-    }
 };
-
-inline double reduce_dev(const float *x, const float *y, std::size_t n)
+inline scratch &thread_scratch(std::size_t ws_bytes)
 {
-    static reduce_ws w;
-    void *st = options().stream;
-    check(nt2g_reduce_f32(x, y, (int64_t)n, w.ws.p, w.ws.bytes, (double *)w.out.p, nullptr, st), "reduce");
-    double r = 0;
-    check(nt2g_memcpy(&r, w.out.p, sizeof r, 2, st), "reduce result");
-    check(nt2g_stream_synchronize(st), "reduce result");
-    return r;
+    int32_t dev = 0;
+    check(nt2g_device_current(&dev), "current device");
+    thread_local std::map<std::pair<int32_t, void *>, scratch> cache;
+    scratch &s = cache[{dev, options().stream}];
+    if (s.ws.bytes < ws_bytes) s.ws = device_buffer(ws_bytes < 256 ? 256 : ws_bytes);
+    if (!s.out.p) s.out = device_buffer(64);
+    return s;
 }
 
 // A table operand of a reduction as a device pointer (staged if on the host).
@@ -959,20 +960,60 @@ inline void view_of(const node *l, dev_view &v)
     v.p = (const float *)v.hold.p;
 }
 
-inline double sum_node(const node_ptr &n)
+// The arguments of a lowered program's table leaves: device tables directly,
+// host tables in place when the device reaches host memory, else staged.
+inline std::vector<nt2g_arg> input_args(const lowered &L, std::vector<device_buffer> &staging)
 {
-    if (n->op == NT2G_OP_LOAD) {
-        dev_view v;
-        view_of(n.get(), v);
-        return reduce_dev(v.p, nullptr, v.n);
+    std::vector<nt2g_arg> args(L.slot_leaf.size());
+    staging.reserve(L.slot_leaf.size());
+    for (std::size_t s = 0; s < L.slot_leaf.size(); ++s) {
+        const node *l = L.slot_leaf[s];
+        nt2g_arg &a = args[s];
+        a.dtype = l->dtype;
+        a.kind = 0;
+        a.scalar = 0.0;
+        if (l->dev_ptr) a.ptr = l->dev_ptr;
+        else if (host_in_place()) a.ptr = (void *)l->host_ptr;
+        else {
+            const std::size_t esz = l->dtype == NT2G_U8 ? 1 : 4;
+            staging.emplace_back(l->numel * esz);
+            a.ptr = staging.back().p;
+            check(nt2g_memcpy(a.ptr, l->host_ptr, l->numel * esz, 1, options().stream), "stage host table");
+        }
     }
-    if (n->op == NT2G_OP_MUL && n->a->op == NT2G_OP_LOAD && n->b->op == NT2G_OP_LOAD) {  // dot
-        dev_view x, y;
-        view_of(n->a.get(), x);
-        view_of(n->b.get(), y);
-        return reduce_dev(x.p, y.p, x.n);
-    }
-    // any other expression: evaluate it once into a temporary, then sum
+    return args;
+}
+
+struct fold_shape {
+    std::int64_t lo = 1, inner = 1, hi = 1;
+};
+
+// The fold of an expression in one pass (nt2g_eval_fold): the expression's
+// value at every element is computed inside the fold kernels, NT2's fold over
+// the AST itself (reduction/.../scalar/inner_fold.hpp:23-49).  out, index,
+// out64 are device (or device-reachable) memory; the call is asynchronous on
+// options().stream unless host tables had to be staged.
+inline void fold_expr(const node_ptr &n, fold_shape f, int op, int precision, float *out, std::int64_t *index,
+                      double *out64)
+{
+    lowering lw;
+    lw.push(NT2G_OP_FOLD, NT2G_F32, lw.emit(n.get()));
+    lw.finish();
+    nt2g_program *prog = program_for(lw.L);
+    std::vector<device_buffer> staging;
+    std::vector<nt2g_arg> args = input_args(lw.L, staging);
+    std::size_t b = 0;
+    check(nt2g_fold_workspace_size(f.lo, f.inner, f.hi, &b), "fold workspace");
+    scratch &sc = thread_scratch(b);
+    check(nt2g_eval_fold(prog, args.data(), (int32_t)args.size(), f.lo, f.inner, f.hi, op, precision, sc.ws.p,
+                         sc.ws.bytes, out, index, out64, options().stream),
+          "fold of an expression");
+    if (!staging.empty()) check(nt2g_stream_synchronize(options().stream), "fold of an expression");
+}
+
+// Element count of an expression: its table / generative leaves' (they agree).
+inline std::size_t numel_of(const node_ptr &n)
+{
     std::size_t numel = 0;
     std::vector<const node *> stack{n.get()};
     while (!stack.empty()) {
@@ -983,18 +1024,60 @@ inline double sum_node(const node_ptr &n)
         for (const node *c : {m->a.get(), m->b.get(), m->c.get()})
             if (c) stack.push_back(c);
     }
-    table<float, device_> tmp(of_size(numel));
-    evaluate({leaf(tmp)}, {n}, {NT2G_F32}, 0, numel);
-    return reduce_dev(tmp.data(), nullptr, numel);
+    return numel;
+}
+
+// The FP64 sum of an expression, left on the device at *dev_result:
+// sum(x) and dot(x, y) of tables through nt2g_reduce_f32, any other
+// expression folded in one pass.  Elements follow options().precision (NT2's
+// own arithmetic or the fast policy); the sum is the compensated one.
+inline void sum_to(const node_ptr &n, double *dev_result)
+{
+    const bool plain = n->op == NT2G_OP_LOAD;
+    const bool dot = n->op == NT2G_OP_MUL && n->a->op == NT2G_OP_LOAD && n->b->op == NT2G_OP_LOAD;
+    if (plain || dot) {
+        dev_view x, y;
+        view_of(plain ? n.get() : n->a.get(), x);
+        if (dot) view_of(n->b.get(), y);
+        std::size_t b = 0;
+        check(nt2g_reduce_workspace_size((int64_t)x.n, &b), "reduce workspace");
+        scratch &sc = thread_scratch(b);
+        check(nt2g_reduce_f32(x.p, dot ? y.p : nullptr, (int64_t)x.n, sc.ws.p, sc.ws.bytes, dev_result, nullptr,
+                              options().stream),
+              "reduce");
+        if (x.hold.p || y.hold.p) check(nt2g_stream_synchronize(options().stream), "reduce");  // staging released
+        return;
+    }
+    const std::int64_t numel = (std::int64_t)numel_of(n);
+    const int prec = options().precision == NT2G_PREC_NT2 ? NT2G_PREC_NT2_ELEMENTS : NT2G_PREC_FAST;
+    scratch &sc = thread_scratch(0);
+    fold_expr(n, fold_shape{1, numel, 1}, NT2G_FOLD_SUM, prec, (float *)((char *)sc.out.p + 32), nullptr, dev_result);
+}
+
+inline double sum_node(const node_ptr &n)
+{
+    scratch &sc = thread_scratch(0);
+    double *d = (double *)sc.out.p;
+    sum_to(n, d);
+    double r = 0;
+    check(nt2g_memcpy(&r, d, sizeof r, 2, options().stream), "reduce result");
+    check(nt2g_stream_synchronize(options().stream), "reduce result");
+    return r;
 }
 }  // namespace detail
 
 // NT2's sum over a vector / globalsum: the compensated device reduction,
-// returned as T (NT2's result type) -- sum64 keeps the FP64 combine.
+// returned as T (NT2's result type) -- sum64 keeps the FP64 combine.  A sum of
+// an expression (sum(exp(x)*y), globalsum(a*b+c)) is folded in one pass, the
+// expression evaluated inside the fold: no temporary table.
 template <class X> double sum64(const X &x) { return detail::sum_node(detail::lift(x)); }
 template <class X> float sum(const X &x) { return (float)sum64(x); }
 template <class X> float globalsum(const X &x) { return (float)sum64(x); }
 template <class A, class B> float dot(const A &a, const B &b) { return (float)sum64(a * b); }
+// sum64 without a host round trip: the FP64 result is written to dev_result
+// (device or device-reachable memory) in stream order on options().stream;
+// read it after synchronizing that stream.
+template <class X> void sum64_async(const X &x, double *dev_result) { detail::sum_to(detail::lift(x), dev_result); }
 
 // ------------------------------------------------ reductions along a dimension --
 // sum(a, dim), prod, maximum, minimum, mean, asum1, asum2, norm2 of a float
@@ -1004,9 +1087,6 @@ template <class A, class B> float dot(const A &a, const B &b) { return (float)su
 // whole table.  options().precision selects NT2's in-order fold (NT2G_PREC_NT2)
 // or the compensated one.
 namespace detail {
-struct fold_shape {
-    std::int64_t lo = 1, inner = 1, hi = 1;
-};
 inline fold_shape split(const of_size_ &e, int dim)
 {
     fold_shape f;
@@ -1029,10 +1109,10 @@ inline void fold_raw(const float *x, fold_shape f, int op, float *out, std::int6
 {
     std::size_t b = 0;
     check(nt2g_fold_workspace_size(f.lo, f.inner, f.hi, &b), "fold workspace");
-    device_buffer ws(b);
-    check(nt2g_fold_f32(x, f.lo, f.inner, f.hi, op, options().precision, ws.p, b, out, index, options().stream),
+    scratch &sc = thread_scratch(b);
+    check(nt2g_fold_f32(x, f.lo, f.inner, f.hi, op, options().precision, sc.ws.p, sc.ws.bytes, out, index,
+                        options().stream),
           "fold");
-    check(nt2g_stream_synchronize(options().stream), "fold");  // ws is released on return
 }
 template <class Site>
 inline table<float, Site> fold_dim(const table<float, Site> &t, int dim, int op)
@@ -1057,9 +1137,9 @@ template <class Site>
 inline float fold_all(const table<float, Site> &t, int op, std::int64_t *index1 = nullptr)
 {
     const fold_shape f{1, (std::int64_t)t.numel(), 1};
-    device_buffer out(16);  // the float result at 0, the int64 position at 8
-    float *o = (float *)out.p;
-    std::int64_t *ix = index1 ? (std::int64_t *)((char *)out.p + 8) : nullptr;
+    scratch &sc = thread_scratch(0);  // the float result at 16, the int64 position at 24
+    float *o = (float *)((char *)sc.out.p + 16);
+    std::int64_t *ix = index1 ? (std::int64_t *)((char *)sc.out.p + 24) : nullptr;
     if (table<float, Site>::on_device || host_in_place()) {
         fold_raw(t.data(), f, op, o, ix);
     } else {
@@ -1076,7 +1156,99 @@ inline float fold_all(const table<float, Site> &t, int op, std::int64_t *index1 
     check(nt2g_stream_synchronize(options().stream), "fold result");
     return r;
 }
+
+// Folds of an expression (one pass, no temporary).  Its extent is its first
+// table leaf's (a row of numel elements when it has only generative leaves).
+inline of_size_ extent_of(const node_ptr &n)
+{
+    std::vector<const node *> stack{n.get()};
+    while (!stack.empty()) {
+        const node *m = stack.back();
+        stack.pop_back();
+        if (m->op == NT2G_OP_LOAD && m->ext[0]) return of_size(m->ext[0], m->ext[1], m->ext[2], m->ext[3]);
+        for (const node *c : {m->c.get(), m->b.get(), m->a.get()})
+            if (c) stack.push_back(c);
+    }
+    return of_size(1, numel_of(n));
+}
+inline table<float, device_> fold_dim_expr(const node_ptr &n, int dim, int op)
+{
+    if (dim < 1 || dim > 4) throw gpu_error(NT2G_ERR_INVALID, "reduction dimension out of range");
+    of_size_ e = extent_of(n);
+    const fold_shape f = split(e, dim);
+    e.d[dim - 1] = 1;
+    table<float, device_> r(e);
+    fold_expr(n, f, op, options().precision, r.data(), nullptr, nullptr);
+    return r;
+}
+inline float fold_all_expr(const node_ptr &n, int op, std::int64_t *index1 = nullptr)
+{
+    scratch &sc = thread_scratch(0);
+    float *o = (float *)((char *)sc.out.p + 16);
+    std::int64_t *ix = index1 ? (std::int64_t *)((char *)sc.out.p + 24) : nullptr;
+    fold_expr(n, fold_shape{1, (std::int64_t)numel_of(n), 1}, op, options().precision, o, ix, nullptr);
+    float r = 0.0f;
+    check(nt2g_memcpy(&r, o, sizeof r, 2, options().stream), "fold result");
+    if (ix) {
+        check(nt2g_memcpy(index1, ix, sizeof *ix, 2, options().stream), "fold index");
+        *index1 += 1;  // NT2 positions are 1-based (0: none)
+    }
+    check(nt2g_stream_synchronize(options().stream), "fold result");
+    return r;
+}
 }  // namespace detail
+
+// The reductions of an expression: sum(exp(x)*y, 1), maximum(abs(a - b), 2),
+// globalmax(a*b + c), ... fold the expression in one pass (the tables are read
+// once, no temporary), as NT2's folds take the expression itself.  The result
+// of a reduction along a dimension is a device table.
+#define NT2G_EXPR_FOLD(NAME, OP)                                                                           \
+    template <class T> table<float, device_> NAME(const expr<T> &e, int dim)                                \
+    {                                                                                                       \
+        return detail::fold_dim_expr(e.n, dim, OP);                                                         \
+    }
+NT2G_EXPR_FOLD(sum, NT2G_FOLD_SUM)
+NT2G_EXPR_FOLD(prod, NT2G_FOLD_PROD)
+NT2G_EXPR_FOLD(maximum, NT2G_FOLD_MAX)
+NT2G_EXPR_FOLD(minimum, NT2G_FOLD_MIN)
+NT2G_EXPR_FOLD(mean, NT2G_FOLD_MEAN)
+NT2G_EXPR_FOLD(asum1, NT2G_FOLD_ASUM1)
+NT2G_EXPR_FOLD(asum2, NT2G_FOLD_ASUM2)
+NT2G_EXPR_FOLD(norm2, NT2G_FOLD_NORM2)
+NT2G_EXPR_FOLD(nbtrue, NT2G_FOLD_NBTRUE)
+NT2G_EXPR_FOLD(nansum, NT2G_FOLD_NANSUM)
+#undef NT2G_EXPR_FOLD
+#define NT2G_EXPR_GLOBAL(NAME, OP)                                                                         \
+    template <class T> float NAME(const expr<T> &e) { return detail::fold_all_expr(e.n, OP); }
+NT2G_EXPR_GLOBAL(globalmax, NT2G_FOLD_MAX)
+NT2G_EXPR_GLOBAL(globalmin, NT2G_FOLD_MIN)
+NT2G_EXPR_GLOBAL(globalprod, NT2G_FOLD_PROD)
+NT2G_EXPR_GLOBAL(globalmean, NT2G_FOLD_MEAN)
+NT2G_EXPR_GLOBAL(globalasum1, NT2G_FOLD_ASUM1)
+NT2G_EXPR_GLOBAL(globalasum2, NT2G_FOLD_ASUM2)
+NT2G_EXPR_GLOBAL(globalnorm2, NT2G_FOLD_NORM2)
+NT2G_EXPR_GLOBAL(globalnbtrue, NT2G_FOLD_NBTRUE)
+NT2G_EXPR_GLOBAL(globalnansum, NT2G_FOLD_NANSUM)
+NT2G_EXPR_GLOBAL(globalnanmean, NT2G_FOLD_NANMEAN)
+#undef NT2G_EXPR_GLOBAL
+template <class T> float globalmax(const expr<T> &e, std::int64_t &i) { return detail::fold_all_expr(e.n, NT2G_FOLD_MAX, &i); }
+template <class T> float globalmin(const expr<T> &e, std::int64_t &i) { return detail::fold_all_expr(e.n, NT2G_FOLD_MIN, &i); }
+template <class T> float globalvar(const expr<T> &e, int w = 0)
+{
+    return detail::fold_all_expr(e.n, w ? NT2G_FOLD_VAR1 : NT2G_FOLD_VAR);
+}
+template <class T> float globalstdev(const expr<T> &e, int w = 0)
+{
+    return detail::fold_all_expr(e.n, w ? NT2G_FOLD_STDEV1 : NT2G_FOLD_STDEV);
+}
+template <class T> table<float, device_> var(const expr<T> &e, int w, int dim)
+{
+    return detail::fold_dim_expr(e.n, dim, w ? NT2G_FOLD_VAR1 : NT2G_FOLD_VAR);
+}
+template <class T> table<float, device_> stdev(const expr<T> &e, int w, int dim)
+{
+    return detail::fold_dim_expr(e.n, dim, w ? NT2G_FOLD_STDEV1 : NT2G_FOLD_STDEV);
+}
 
 #define NT2G_DIM_FOLD(NAME, OP)                                                                            \
     template <class Site> table<float, Site> NAME(const table<float, Site> &t, int dim)                     \
@@ -1171,9 +1343,10 @@ template <class Site> inline table<float, Site> scan_dim(const table<float, Site
     auto run = [&](const float *x, float *o) {
         std::size_t b = 0;
         check(nt2g_scan_workspace_size(f.lo, f.inner, f.hi, &b), "scan workspace");
-        device_buffer ws(b);
-        check(nt2g_scan_f32(x, f.lo, f.inner, f.hi, op, options().precision, ws.p, b, o, options().stream), "scan");
-        check(nt2g_stream_synchronize(options().stream), "scan");
+        scratch &sc = thread_scratch(b);
+        check(nt2g_scan_f32(x, f.lo, f.inner, f.hi, op, options().precision, sc.ws.p, sc.ws.bytes, o,
+                            options().stream),
+              "scan");
     };
     if (table<float, Site>::on_device || host_in_place()) {
         run(t.data(), r.data());

@@ -15,12 +15,12 @@ LIB_PATH = os.path.join(_HERE, "_build", "libnt2gpu.so")
 HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "nt2g.h")
 
 OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_DEVICE_FLAG, ERR_NOMEM = range(6)
-PREC_FAST, PREC_NT2 = 0, 1
+PREC_FAST, PREC_NT2, PREC_NT2_ELEMENTS = 0, 1, 2
 F32, U8 = 0, 1
 
 # opcodes (values fixed by nt2g.h; tests check they agree with the header)
 OP = dict(
-    LOAD=1, SCALAR=2, CONST=3, STORE=4, INDEX=5,
+    LOAD=1, SCALAR=2, CONST=3, STORE=4, INDEX=5, FOLD=6,
     ADD=10, SUB=11, MUL=12, DIV=13, NEG=14, ABS=15, SQR=16, SQRT=17, REC=18, MIN=19, MAX=20,
     FMA=30, FNMS=31,
     EXP=40, LOG=41, LOG1P=42, ERFC=43, NORMCDF=44, FASTNORMCDF=45, EXP2=46, EXP10=47, EXPM1=48, LOG2=49, LOG10=50,
@@ -110,12 +110,19 @@ _SIGNATURES = {
     "nt2g_host_access": (_I32, [ctypes.POINTER(_I32)]),
     "nt2g_fold_workspace_size": (_I32, [_I64, _I64, _I64, ctypes.POINTER(ctypes.c_size_t)]),
     "nt2g_fold_f32": (_I32, [_VP, _I64, _I64, _I64, _I32, _I32, _VP, ctypes.c_size_t, _VP, _VP, _VP]),
+    "nt2g_eval_fold": (_I32, [_VP, ctypes.POINTER(Arg), _I32, _I64, _I64, _I64, _I32, _I32, _VP, ctypes.c_size_t, _VP,
+                              _VP, _VP, _VP]),
+    "nt2g_program_fold_source": (_I32, [_VP, _I32, _I32, ctypes.c_char_p, ctypes.c_size_t,
+                                        ctypes.POINTER(ctypes.c_size_t)]),
     "nt2g_scan_workspace_size": (_I32, [_I64, _I64, _I64, ctypes.POINTER(ctypes.c_size_t)]),
     "nt2g_scan_f32": (_I32, [_VP, _I64, _I64, _I64, _I32, _I32, _VP, ctypes.c_size_t, _VP, _VP]),
     "nt2g_device_alloc": (_I32, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "nt2g_device_free": (_I32, [_VP]),
     "nt2g_memcpy": (_I32, [_VP, _VP, ctypes.c_size_t, _I32, _VP]),
     "nt2g_stream_synchronize": (_I32, [_VP]),
+    "nt2g_device_current": (_I32, [ctypes.POINTER(_I32)]),
+    "nt2g_stream_create": (_I32, [ctypes.POINTER(_VP)]),
+    "nt2g_stream_destroy": (_I32, [_VP]),
 }
 
 _lib = None

@@ -46,6 +46,14 @@ def conditioned_ulp(y, ref64, scale64):
     return np.abs(np.asarray(y, np.float64) - ref64) / sp
 
 
+# Stated accuracy of the fast-policy Black-Scholes call/put against FP64, in
+# conditioned ulps (error over the ulp of the larger cancelling term): the
+# bound the GPU tests assert (measured maxima: 12.3 over the 5.7e7 options of
+# the batched mix, about 10.8 over the 2^20 bench options; NT2's own float
+# evaluation of the same options: 300-400).
+BS_FAST_MAX, BS_FAST_P999, BS_FAST_MEAN, BS_FAST_CORE = 14.0, 6.0, 1.1, 8.0
+
+
 def bs_inputs(n, seed=1000, sigma_table=False):
     rng = np.random.default_rng(seed)
     S = rng.uniform(5, 30, n).astype(F32)

@@ -236,3 +236,51 @@ def test_compiled_kernel_source_validates_arguments(lib):
     small = ctypes.create_string_buffer(10)
     assert L.nt2g_program_jit_source(prog.handle, 0, small, 10, ctypes.byref(n)) == lib.ERR_INVALID
     assert L.nt2g_program_jit_prepare(None, 0) == lib.ERR_INVALID
+
+
+def test_fold_kernel_source_builds_for_sm103a(lib):
+    """The fold kernels nt2g_eval_fold compiles for a program's FOLD value
+    (the fold bodies instantiated over the expression's element function)
+    build for sm_103a, for sum-type, max/min, two-pass and logical folds under
+    the three element/fold policies (NVRTC needs no GPU)."""
+    import time
+    nv = _nvrtc()
+    x, y = E.Table(torch.zeros(8)), E.Table(torch.zeros(8))
+    u8 = torch.uint8
+    fr, bkg = E.Table(torch.zeros(8, dtype=u8)), E.Table(torch.zeros(8, dtype=u8))
+    cases = [(E.exp(x) * y, "sum", lib.PREC_FAST), (E.abs_(x - y), "max", lib.PREC_NT2),
+             (E.exp(x) * y, "var", lib.PREC_NT2_ELEMENTS), (fr > bkg, "nbtrue", lib.PREC_FAST)]
+    for e, op, prec in cases:
+        prog, _ = E.compile_program([], [], fold=e)
+        src = prog.fold_source(op, prec)
+        assert "fold_nt2" in src and ("fold_inner_11" in src) == (prec != lib.PREC_NT2)
+        t0 = time.time()
+        rc, log, size = _nvrtc_compile(nv, src)
+        assert rc == 0, (op, prec, log[:2000])
+        assert size > 0
+        print(f"\nfold {op} policy {prec}: {time.time() - t0:.1f} s to compile, cubin {size} bytes")
+
+
+def test_fold_programs_validate(lib):
+    L = lib.load()
+    x = E.Table(torch.zeros(8))
+    prog, slots = E.compile_program([], [], fold=E.exp(x))
+    args = (lib.Arg * 1)(lib.Arg(slots[0].data_ptr(), 0.0, lib.F32, 0))
+    out = torch.zeros(1)
+    # a fold program does not evaluate as a transform, and a transform does not fold
+    assert L.nt2g_eval(prog.handle, args, 1, 0, 8, 0, 0, None) == lib.ERR_INVALID
+    tprog, _ = E.compile_program([torch.zeros(8)], [E.exp(x)])
+    assert L.nt2g_eval_fold(tprog.handle, args, 1, 1, 8, 1, 0, 0, None, 0, lib._ptr(out), None, None,
+                            None) == lib.ERR_INVALID
+    # op, precision and index / FP64 requests are checked before any launch
+    for op, prec, idx, o64 in ((18, 0, None, None), (0, 3, None, None), (0, 0, lib._ptr(out), None),
+                               (2, 0, None, lib._ptr(out)), (0, 1, None, lib._ptr(out))):
+        assert L.nt2g_eval_fold(prog.handle, args, 1, 1, 8, 1, op, prec, None, 0, lib._ptr(out), idx, o64,
+                                None) == lib.ERR_INVALID
+    # two FOLDs, or a FOLD and a STORE, in one program
+    ops = (lib.Op * 4)(lib.Op(lib.OP["LOAD"], 0, 0, -1, -1, 0.0), lib.Op(lib.OP["FOLD"], 0, 0, -1, -1, 0.0),
+                       lib.Op(lib.OP["FOLD"], 0, 0, -1, -1, 0.0), lib.Op(lib.OP["STORE"], 0, 0, 1, -1, 0.0))
+    h = ctypes.c_void_p()
+    assert L.nt2g_program_create(ops, 3, 2, ctypes.byref(h)) == lib.ERR_INVALID
+    ops[2] = lib.Op(lib.OP["STORE"], 0, 0, 1, -1, 0.0)
+    assert L.nt2g_program_create(ops, 3, 2, ctypes.byref(h)) == lib.ERR_INVALID

@@ -8,20 +8,19 @@ in ulps of the larger of the two cancelling terms (call = S N(d1) - K e^-rT
 N(d2)), the terms floored at 2^-102 (below that N(d) itself is subnormal in
 FP32 and both NT2 and the kernel flush it).  Rounding of d1/d2 is amplified
 by |d| times N(d)'s log-derivative (~d^2 in the tail) for any FP32
-evaluation, NT2's included, so the checks compare the fast policy's error
-distribution with NT2's own on the same options: mean, p99.9 and max no
-worse than NT2's, and below 1 ulp on the options whose |d1|, |d2| <= 2."""
+evaluation, NT2's included.  Stated bound (helpers.BS_FAST_*): max <= 14,
+p99.9 <= 6, mean <= 1.1, and <= 8 on the options whose |d1|, |d2| <= 2; the
+max is also no worse than NT2's own float evaluation of the same options."""
 import numpy as np
 import pytest
 import torch
 
-from helpers import bs_inputs, conditioned_ulp
+from helpers import BS_FAST_CORE, BS_FAST_MAX, BS_FAST_MEAN, BS_FAST_P999, bs_inputs, conditioned_ulp
 from nt2_gb300 import expr as E
 
 pytestmark = pytest.mark.gpu
 
 R, SIGMA = 0.02, 0.30
-COND_TOL = 8.0
 
 
 def _dev(dev, *arrs):
@@ -72,7 +71,7 @@ def _d12(S, K, T, sig):
     return d1, d1 - v * np.sqrt(t)
 
 
-def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label="", mean_slack=0.0):
+def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label=""):
     ec, ep = _fast_errors(oracle, S, K, T, c, p, sig)
     rc, rp = oracle.blackscholes(S, K, T, R, sig)
     nc, np_ = _fast_errors(oracle, S, K, T, rc, rp, sig)
@@ -82,11 +81,12 @@ def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label="", mean_slack=0.0):
     print(f"{label} NT2 restatement vs FP64: call max {nc.max():.2f} mean {nc.mean():.3f} p99.9 {q(nc):.2f}; "
           f"put max {np_.max():.2f} mean {np_.mean():.3f} p99.9 {q(np_):.2f}")
     for f, nn in ((ec, nc), (ep, np_)):
-        assert f.mean() <= nn.mean() + mean_slack and q(f) <= q(nn) and f.max() <= nn.max()
+        assert f.max() <= BS_FAST_MAX and f.max() <= nn.max()
+        assert q(f) <= BS_FAST_P999 and f.mean() <= BS_FAST_MEAN
     d1, d2 = _d12(S, K, T, np.broadcast_to(sig, S.shape))
     core = (np.abs(d1) <= 2) & (np.abs(d2) <= 2)
     print(f"{label} |d|<=2 ({core.mean():.0%} of options): call max {ec[core].max():.2f} put max {ep[core].max():.2f}")
-    assert ec[core].max() <= COND_TOL and ep[core].max() <= COND_TOL
+    assert ec[core].max() <= BS_FAST_CORE and ep[core].max() <= BS_FAST_CORE
     return ec, ep
 
 
@@ -115,9 +115,7 @@ def test_fast_policy_extreme_volatility(lib, dev, oracle):
     S, K, T = bs_inputs(n, seed=1010)
     sig = rng.uniform(1.0, 4.0, n).astype(np.float32)
     c, p = _run_direct(lib, dev, S, K, T, lib.PREC_FAST, sig)
-    # here NT2's own errors are small too (the tails are not reached through
-    # cancellation): the mean may match NT2's within a hundredth of an ulp
-    _check_fast(oracle, S, K, T, c, p, sig, label="sigma~U[1,4]", mean_slack=0.01)
+    _check_fast(oracle, S, K, T, c, p, sig, label="sigma~U[1,4]")
     for m in (5, 4097):
         cs, ps = _run_direct(lib, dev, S[:m], K[:m], T[:m], lib.PREC_FAST, sig[:m])
         assert np.array_equal(cs, c[:m]) and np.array_equal(ps, p[:m])

@@ -189,3 +189,72 @@ def test_generative_through_tables(demos, oracle, tmp_path, prec):
             else:
                 tol = {"g1": 4, "g2": 8}.get(name, 1) * ulp
             assert (np.abs(got.astype(np.float64) - ref) <= tol).all(), name
+
+
+def _gpu_tensor(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda:0")
+
+
+@pytest.mark.gpu
+def test_expression_folds_through_tables(demos, lib, tmp_path):
+    """sum(abs(A - B), 1), maximum(exp(A) - B, 2), var(A*B + 1, 0, 1),
+    globalmax(A*B + 1, i), sum64(exp(A)*B) and globalmean(abs(A - B)) through
+    the C++ table layer: each folds its expression in one pass, and equals the
+    same fold through the C ABI from Python bit for bit."""
+    from nt2_gb300 import expr as E
+    m, n = 1000, 300
+    rng = np.random.default_rng(31)
+    a, b = rng.standard_normal(m * n).astype(np.float32), rng.standard_normal(m * n).astype(np.float32)
+    a.tofile(tmp_path / "a.bin"); b.tofile(tmp_path / "b.bin")
+    out = dict((ln.split()[0], ln.split()[1:]) for ln in _run(demos, "fold_expr", tmp_path, m, n).splitlines())
+    A, B = E.Table(_gpu_tensor(a)), E.Table(_gpu_tensor(b))
+    f32 = lambda p: np.fromfile(tmp_path / p, np.float32)  # noqa: E731
+    assert _eq(f32("sumabs1.bin"), E.fold(E.abs_(A - B), "sum", (1, m, n)).cpu().numpy())
+    assert _eq(f32("maxexp2.bin"), E.fold(E.exp(A) - B, "max", (m, n, 1)).cpu().numpy())
+    assert _eq(f32("var1.bin"), E.fold(A * B + 1.0, "var", (1, m, n)).cpu().numpy())
+    v, i = E.fold(A * B + 1.0, "max", index=True)
+    assert np.float32(out["globalmax"][0]) == v.item() and int(out["globalmax"][1]) == i.item() + 1
+    _, s64 = E.fold(E.exp(A) * B, "sum", out64=True)
+    assert float(out["globalsum"][0]) == s64.item()
+    assert np.float32(out["globalmean"][0]) == E.fold(E.abs_(A - B), "mean").item()
+    np.testing.assert_allclose(f32("sumabs1.bin"), np.abs(a - b).reshape(n, m).astype(np.float64).sum(1), rtol=1e-6)
+
+
+@pytest.mark.gpu
+def test_reductions_from_two_host_threads(demos, lib, tmp_path):
+    """Two host threads, each on its own stream with its own per-thread
+    scratch, reduce concurrently (plain sum, dot, a fused expression sum): 40
+    repetitions reproduce each thread's first results, which equal the same
+    reductions through the C ABI."""
+    from nt2_gb300 import expr as E
+    n = 1 << 22
+    rng = np.random.default_rng(32)
+    x, y = rng.standard_normal(n).astype(np.float32), rng.standard_normal(n).astype(np.float32)
+    x.tofile(tmp_path / "x.bin"); y.tofile(tmp_path / "y.bin")
+    lines = _run(demos, "threads", tmp_path, n).splitlines()
+    red = lib.Reducer("cuda:0")
+    for tid, ln in enumerate(lines):
+        r0, r1, r2, bad = ln.split()
+        assert int(bad) == 0
+        tx, ty = _gpu_tensor(x * np.float32(tid + 1)), _gpu_tensor(y + np.float32(tid))
+        assert float(r0) == red(tx)[0].item()
+        assert float(r1) == red(tx, ty)[0].item()
+        assert float(r2) == E.fold(E.exp(E.Table(ty)) * E.Table(tx), "sum", out64=True)[1].item()
+
+
+@pytest.mark.gpu
+def test_async_sums_on_two_streams(demos, lib, tmp_path):
+    """sum64_async in flight on two streams at once (per-stream scratch): 16
+    dot products on one stream and 16 fused expression sums on the other all
+    equal their single-stream values."""
+    from nt2_gb300 import expr as E
+    n = 1 << 22
+    rng = np.random.default_rng(33)
+    x, y = rng.standard_normal(n).astype(np.float32), rng.standard_normal(n).astype(np.float32)
+    x.tofile(tmp_path / "x.bin"); y.tofile(tmp_path / "y.bin")
+    vals = [float(v) for v in _run(demos, "streams", tmp_path, n).split()]
+    tx, ty = _gpu_tensor(x), _gpu_tensor(y)
+    dot = lib.Reducer("cuda:0")(tx, ty)[0].item()
+    fused = E.fold(E.exp(E.Table(tx)) * E.Table(ty), "sum", out64=True)[1].item()
+    assert vals[:16] == [dot] * 16 and vals[16:] == [fused] * 16

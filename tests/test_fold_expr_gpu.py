@@ -1,0 +1,126 @@
+"""Folds of an expression in one pass (nt2g_eval_fold): the expression's value
+at every element is computed inside the fold kernels, so sum(exp(x)*y),
+sum(abs(x - y), 1), globalmax(exp(x) - y) read their input tables once and
+write no temporary.
+
+Parity:
+  - equal, bit for bit, to nt2g_fold_f32 of the same expression first
+    evaluated into an aligned table by the run-time compiled transform (same
+    element policy and fold order): the fold kernels and their plan are the
+    same, only the element source differs;
+  - NT2 policy: bit-identical to the oracle's NT2 fold (index order, NT2's
+    unfused float operations) of the oracle's NT2 evaluation of the elements;
+  - fast policy: the FP64 result within 4 eps^2 sum|x| of the exact sum of the
+    elements (the compensated fold's bound).
+NT2's folds take the expression itself
+(core/reduction/include/nt2/core/functions/scalar/inner_fold.hpp:23-49,
+core/functions/details/fold_step.hpp:32-43, core/functions/simd/global.hpp:27-69)."""
+import numpy as np
+import pytest
+import torch
+
+from nt2_gb300 import expr as E
+
+pytestmark = pytest.mark.gpu
+
+EPS32 = float(np.finfo(np.float32).eps)
+
+
+def _t(dev, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def _materialized(lib, e_fn, tabs, elem_prec):
+    """e evaluated into a fresh aligned table by the compiled transform."""
+    out = torch.empty(tabs[0].numel(), device=tabs[0].device)
+    E.assign([out], [e_fn(*[E.Table(t) for t in tabs])], precision=elem_prec, force_generic=1)
+    return out
+
+
+def _bits(t):
+    return t.cpu().numpy().view(np.uint32) if t.dtype == torch.float32 else t.cpu().numpy()
+
+
+PRECS = [("fast", 0, 0, 0), ("nt2", 1, 1, 1), ("nt2_elements", 2, 1, 0)]  # (name, fold prec, elements, order)
+
+
+@pytest.mark.parametrize("name,prec,elem,order", PRECS, ids=[p[0] for p in PRECS])
+@pytest.mark.parametrize("shape", [(1, 1 << 20, 1), (1, 4096, 256), (300, 2000, 3), (64, 512, 8), (1, 37, 3000),
+                                   (5, 7, 1)],
+                         ids=["global", "columns", "strided", "strided4", "short", "tiny"])
+@pytest.mark.parametrize("op", ["sum", "max", "var", "nbtrue", "asum2"])
+def test_fused_fold_equals_fold_of_materialized(lib, dev, name, prec, elem, order, shape, op):
+    lo, inner, hi = shape
+    if prec == 1 and lo * hi < 16 and inner > 1 << 16:
+        pytest.skip("NT2-order global fold of 2^20 elements: one thread, covered at 2^16 below")
+    n = lo * inner * hi
+    rng = np.random.default_rng(7 + n)
+    x, y = _t(dev, rng.standard_normal(n, dtype=np.float32)), _t(dev, rng.standard_normal(n, dtype=np.float32))
+    fns = {"sum": lambda a, b: E.exp(a) * b, "max": lambda a, b: E.exp(a) - b, "var": lambda a, b: a * b + 1.0,
+           "nbtrue": lambda a, b: a > b, "asum2": lambda a, b: E.abs_(a - b)}
+    fn = fns[op]
+    idx = op == "max"
+    got = E.fold(fn(E.Table(x), E.Table(y)), op, shape, precision=prec, index=idx)
+    m = _materialized(lib, fn, [x, y], elem)
+    ref = lib.fold(m, lo, inner, hi, op, precision=order, index=idx)
+    torch.cuda.synchronize()
+    if idx:
+        assert np.array_equal(_bits(got[0]), _bits(ref[0])) and np.array_equal(_bits(got[1]), _bits(ref[1]))
+    else:
+        assert np.array_equal(_bits(got), _bits(ref))
+
+
+def test_nt2_policy_matches_the_oracle(lib, dev, oracle):
+    """NT2's elements folded in NT2's order: sum(exp(x)*y) over 2^16 elements
+    and sum(abs(x - y), 1) over a 256 x 300 table, bit-identical to the
+    oracle's NT2 evaluation and fold."""
+    rng = np.random.default_rng(11)
+    n = 1 << 16
+    x, y = rng.standard_normal(n, dtype=np.float32), rng.standard_normal(n, dtype=np.float32)
+    got = E.fold(E.exp(E.Table(_t(dev, x))) * E.Table(_t(dev, y)), "sum", precision=lib.PREC_NT2)
+    elems = (oracle.map_f32("exp", x) * y).astype(np.float32)
+    ref = oracle.fold_nt2(elems, 1, n, 1, "sum")[0]
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), np.asarray(ref, np.float32).view(np.uint32))
+    m, k = 256, 300
+    a, b = rng.standard_normal(m * k, dtype=np.float32), rng.standard_normal(m * k, dtype=np.float32)
+    got = E.fold(E.abs_(E.Table(_t(dev, a)) - E.Table(_t(dev, b))), "sum", (1, m, k), precision=lib.PREC_NT2)
+    ref = oracle.fold_nt2(np.abs(a - b).astype(np.float32), 1, m, k, "sum")[0]
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), np.asarray(ref, np.float32).view(np.uint32))
+    got = E.fold(E.abs_(E.Table(_t(dev, a)) - E.Table(_t(dev, b))), "max", (m, k, 1), precision=lib.PREC_NT2)
+    ref = oracle.fold_nt2(np.abs(a - b).astype(np.float32), m, k, 1, "max")[0]
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), np.asarray(ref, np.float32).view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [1 << 24, (1 << 22) + 3])
+def test_fast_sum_against_the_exact_sum(lib, dev, oracle, n):
+    """sum(exp(x)*y) in one pass: the FP64 result within the compensated
+    fold's bound of the exact sum of the same float elements; dot(x*2, y+1)
+    likewise; misaligned views (one element in) give the same elements."""
+    rng = np.random.default_rng(12)
+    x, y = _t(dev, rng.standard_normal(n + 1, dtype=np.float32)), _t(dev, rng.standard_normal(n + 1, dtype=np.float32))
+    for xs, ys in ((x[:n], y[:n]), (x[1:], y[1:])):
+        for fn in (lambda a, b: E.exp(a) * b, lambda a, b: (a * 2.0) * (b + 1.0)):
+            out, o64 = E.fold(fn(E.Table(xs), E.Table(ys)), "sum", out64=True)
+            elems = _materialized(lib, fn, [xs, ys], 0).cpu().numpy()
+            exact, absum = oracle.exact_sum(elems)
+            err = abs(float(o64.item()) - exact)
+            assert err <= 4 * EPS32 ** 2 * absum + 1e-15 * abs(exact), (err, exact, absum)
+            assert float(out.item()) == np.float32(float(o64.item()))
+
+
+def test_generative_and_uint8_folds(lib, dev, oracle):
+    """A generative leaf folds without memory: sum(sinpi(linspace(0, 2, n)) * x);
+    uint8 tables fold through a comparison: nbtrue(frame > bkg)."""
+    n = 1 << 20
+    rng = np.random.default_rng(13)
+    x = _t(dev, rng.standard_normal(n, dtype=np.float32))
+    e = E.sinpi(E.linspace(0, 2, n)) * E.Table(x)
+    got = E.fold(e, "sum")
+    out = torch.empty(n, device=dev)
+    E.assign([out], [E.sinpi(E.linspace(0, 2, n)) * E.Table(x)], force_generic=1)
+    assert np.array_equal(got.cpu().numpy().view(np.uint32), lib.fold(out, 1, n, 1, "sum").cpu().numpy().view(np.uint32))
+    fr = _t(dev, rng.integers(0, 256, n, dtype=np.uint8))
+    bkg = _t(dev, rng.integers(0, 256, n, dtype=np.uint8))
+    for prec in (lib.PREC_FAST, lib.PREC_NT2):
+        cnt = E.fold(E.Table(fr) > E.Table(bkg), "nbtrue", precision=prec)
+        assert float(cnt.item()) == float(np.count_nonzero(fr.cpu().numpy() > bkg.cpu().numpy()))
