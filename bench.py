@@ -26,6 +26,8 @@ in HBM.  Workloads (--config):
   fn_trig / fn_pow / fn_gen   sin(x)*cos(y), pow(x, y), sinpi(linspace(0,2,n))*x
   fn_special                  erf(y) + gammaln(x)
             over 2^26 elements through the compiled kernel
+  fold_expr / fold_expr_col   sum(exp(x)*y) over 2^28 elements, sum(abs(x - y), 1)
+            of two 16384^2 tables: folds of an expression in one pass
 Each prints one JSON line (rank 0).  --impl reference times NT2's CPU path
 (the oracle's restatement of it: NT2 itself needs Boost, absent here) on the
 host cores for the same workload.
@@ -560,6 +562,50 @@ class Functors(Workload):
         L.check(L.load().nt2g_eval(self.prog.handle, self.args, self.nslots, 0, self.n, self.prec, 1, L._stream()))
 
 
+class FoldExpr(Workload):
+    """A fold of an expression in one pass (nt2g_eval_fold): the expression is
+    evaluated inside the fold kernels, so the algorithmic bytes are the input
+    tables' only (8 B/element, no temporary).  kind "sum": sum(exp(x)*y) over
+    2^28 elements (FP64 result); kind "col": sum(abs(x - y), 1) over a
+    16384 x 16384 table (16384 column sums)."""
+
+    def __init__(self, torch, lib, dev, kind, precision, n=None):
+        from nt2_gb300 import expr as E
+        self.torch, self.lib, self.prec, self.E = torch, lib, precision, E
+        n = n or 1 << 28
+        g = torch.Generator(device=dev).manual_seed(1001)
+        self.x = torch.randn(n, device=dev, generator=g)
+        self.y = torch.randn(n, device=dev, generator=g)
+        X, Y = E.Table(self.x), E.Table(self.y)
+        if kind == "sum":
+            e, self.shape, op, what = E.exp(X) * Y, (1, n, 1), "sum", f"sum(exp(x)*y) over {n} float32"
+        else:
+            side = _side(n)
+            n = side * side
+            e, self.shape, op, what = E.abs_(X - Y), (1, side, side), "sum", \
+                f"sum(abs(x - y), 1) of two {side}x{side} float32 tables"
+        prog, slots = E.compile_program([], [], fold=e)
+        self.prog, self.slots = prog, slots
+        self.args = (lib.Arg * len(slots))(*[lib.Arg(t.data_ptr(), 0.0, lib.F32, 0) for t in slots])
+        lo, inner, hi = self.shape
+        nb = ctypes.c_size_t()
+        lib.check(lib.load().nt2g_fold_workspace_size(lo, inner, hi, ctypes.byref(nb)))
+        self.ws = torch.empty(max(nb.value, 16), dtype=torch.uint8, device=dev)
+        self.out = torch.empty(lo * hi, device=dev)
+        self.out64 = torch.empty(lo * hi, dtype=torch.float64, device=dev) if precision != lib.PREC_NT2 else None
+        self.op = lib.FOLD[op]
+        self.units, self.bytes, self.kernel = n, 8 * n, "fold_inner (run-time compiled)"
+        self.launches = 2 if kind == "sum" else 1  # chunk partials, then the in-order combine
+        self.name = what + ", one pass through nt2g_eval_fold (no temporary)"
+
+    def step(self, i):
+        L = self.lib
+        lo, inner, hi = self.shape
+        L.check(L.load().nt2g_eval_fold(self.prog.handle, self.args, len(self.slots), lo, inner, hi, self.op, self.prec,
+                                        L._ptr(self.ws), self.ws.numel(), L._ptr(self.out), None, L._ptr(self.out64),
+                                        L._stream()))
+
+
 class Rgb2Yuv(Workload):
     SETS = 8
     independent = True
@@ -617,6 +663,8 @@ def make(name, torch, lib, dev, precision, tune=None, n=None):
     if name in ("cumsum_col", "cumsum_all", "cummax_row"):
         return Scan(torch, lib, dev, {"cumsum_col": "col", "cumsum_all": "all", "cummax_row": "rowmax"}[name],
                     precision, _side(n))
+    if name in ("fold_expr", "fold_expr_col"):
+        return FoldExpr(torch, lib, dev, "sum" if name == "fold_expr" else "col", precision, n)
     if name in ("fold_col", "fold_row", "gmax"):
         return Fold(torch, lib, dev, {"fold_col": "col", "fold_row": "row", "gmax": "max"}[name], precision,
                     _side(n))
