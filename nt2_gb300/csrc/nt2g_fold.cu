@@ -218,6 +218,7 @@ nt2g_status fold_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *
 // Where a fold's elements come from: a table, or the FOLD value of a program
 // whose element function is compiled at run time.
 struct FoldInput {
+    bool expr = false;  // the elements are an expression's (else the table x)
     const float *x = nullptr;
     const std::vector<nt2g_op> *ops = nullptr;
     const std::vector<uint8_t> *logical = nullptr;
@@ -260,7 +261,7 @@ static nt2g_status launch_fold_op(const FoldInput &in, int64_t lo, int64_t inner
         }
     }
     const JitFoldKernels *jk = nullptr;
-    if (!in.x) {
+    if (in.expr) {
         std::string why;
         jk = jit_fold_kernels(*in.ops, *in.logical, in.elem_precision, OP, &why);
         if (!jk) {
@@ -274,7 +275,7 @@ static nt2g_status launch_fold_op(const FoldInput &in, int64_t lo, int64_t inner
     cudaError_t ce = cudaSuccess;
     if (precision == NT2G_PREC_NT2 || inner == 0) {  // (an empty fold yields the neutral element)
         const dim3 g(cap((n_out + kFoldThreads - 1) / kFoldThreads));
-        if (in.x) {
+        if (!in.expr) {
             k_fold_nt2<OP><<<g, kFoldThreads, 0, st>>>(src, lo, inner, hi, out, index, cen);
             ce = cudaGetLastError();
         } else {
@@ -292,7 +293,7 @@ static nt2g_status launch_fold_op(const FoldInput &in, int64_t lo, int64_t inner
     Partial *part = (Partial *)ws;
     if (p.kind == 0) {
         const dim3 g(cap((hi + kFoldThreads - 1) / kFoldThreads));
-        if (in.x) {
+        if (!in.expr) {
             k_fold_short<OP><<<g, kFoldThreads, 0, st>>>(src, inner, hi, out, index, cen, out64);
             ce = cudaGetLastError();
         } else {
@@ -306,7 +307,7 @@ static nt2g_status launch_fold_op(const FoldInput &in, int64_t lo, int64_t inner
         const bool fin = p.q == 1;
         int64_t chunk = p.chunk, q = p.q;
         int vec = p.vec;
-        if (in.x) {
+        if (!in.expr) {
 #define NT2G_INNER(F, I) k_fold_inner<OP, F, I><<<g, kFoldThreads, 0, st>>>(src, inner, hi, chunk, q, vec, part, out, \
                                                                             index, cen, out64)
             if (fin) { if (idx) NT2G_INNER(true, true); else NT2G_INNER(true, false); }
@@ -322,7 +323,7 @@ static nt2g_status launch_fold_op(const FoldInput &in, int64_t lo, int64_t inner
         const dim3 g(cap((threads + kFoldThreads - 1) / kFoldThreads), (unsigned)p.q);
         const bool fin = p.q == 1;
         int64_t chunk = p.chunk, q = p.q;
-        if (in.x) {
+        if (!in.expr) {
 #define NT2G_OUTER(V, F) k_fold_outer<OP, V, F><<<g, kFoldThreads, 0, st>>>(src, lo, inner, hi, chunk, q, part, out, \
                                                                             index, cen, out64)
             if (p.vec == 4) { if (fin) NT2G_OUTER(4, true); else NT2G_OUTER(4, false); }
@@ -377,6 +378,7 @@ nt2g_status launch_fold_expr(const std::vector<nt2g_op> &ops, const std::vector<
                              float *out, int64_t *index, double *out64, cudaStream_t st)
 {
     FoldInput in;
+    in.expr = true;
     in.ops = &ops;
     in.logical = &logical;
     in.args = &args;

@@ -1008,7 +1008,9 @@ inline void fold_expr(const node_ptr &n, fold_shape f, int op, int precision, fl
     check(nt2g_eval_fold(prog, args.data(), (int32_t)args.size(), f.lo, f.inner, f.hi, op, precision, sc.ws.p,
                          sc.ws.bytes, out, index, out64, options().stream),
           "fold of an expression");
-    if (!staging.empty()) check(nt2g_stream_synchronize(options().stream), "fold of an expression");
+    // staging buffers are released on return, and host tables read in place are the caller's again
+    if (!staging.empty() || has_host_leaf(lw.L.slot_leaf))
+        check(nt2g_stream_synchronize(options().stream), "fold of an expression");
 }
 
 // Element count of an expression: its table / generative leaves' (they agree).
@@ -1045,7 +1047,9 @@ inline void sum_to(const node_ptr &n, double *dev_result)
         check(nt2g_reduce_f32(x.p, dot ? y.p : nullptr, (int64_t)x.n, sc.ws.p, sc.ws.bytes, dev_result, nullptr,
                               options().stream),
               "reduce");
-        if (x.hold.p || y.hold.p) check(nt2g_stream_synchronize(options().stream), "reduce");  // staging released
+        // staging buffers are released on return, host tables read in place are the caller's again
+        const bool host = !(plain ? n : n->a)->dev_ptr || (dot && !n->b->dev_ptr);
+        if (host) check(nt2g_stream_synchronize(options().stream), "reduce");
         return;
     }
     const std::int64_t numel = (std::int64_t)numel_of(n);
@@ -1104,8 +1108,10 @@ inline int first_non_singleton(const of_size_ &e)
         if (e.d[k] != 1) return k + 1;
     return 1;
 }
-// fold x (device pointer, or host memory the device reaches) into out / index
-inline void fold_raw(const float *x, fold_shape f, int op, float *out, std::int64_t *index)
+// fold x (device pointer, or host memory the device reaches) into out / index;
+// host: x or out is host memory, which the caller may read or free as soon as
+// the call returns (the fold is then waited for)
+inline void fold_raw(const float *x, fold_shape f, int op, float *out, std::int64_t *index, bool host)
 {
     std::size_t b = 0;
     check(nt2g_fold_workspace_size(f.lo, f.inner, f.hi, &b), "fold workspace");
@@ -1113,6 +1119,7 @@ inline void fold_raw(const float *x, fold_shape f, int op, float *out, std::int6
     check(nt2g_fold_f32(x, f.lo, f.inner, f.hi, op, options().precision, sc.ws.p, sc.ws.bytes, out, index,
                         options().stream),
           "fold");
+    if (host) check(nt2g_stream_synchronize(options().stream), "fold");
 }
 template <class Site>
 inline table<float, Site> fold_dim(const table<float, Site> &t, int dim, int op)
@@ -1124,11 +1131,11 @@ inline table<float, Site> fold_dim(const table<float, Site> &t, int dim, int op)
     table<float, Site> r(e);
     const bool direct = table<float, Site>::on_device || host_in_place();
     if (direct) {
-        fold_raw(t.data(), f, op, r.data(), nullptr);
+        fold_raw(t.data(), f, op, r.data(), nullptr, !table<float, Site>::on_device);
     } else {  // host tables the device cannot reach: through device buffers
         table<float, device_> dt(t.extent()), dr(e);
         dt = t;
-        fold_raw(dt.data(), f, op, dr.data(), nullptr);
+        fold_raw(dt.data(), f, op, dr.data(), nullptr, false);
         r = dr;
     }
     return r;
@@ -1141,11 +1148,11 @@ inline float fold_all(const table<float, Site> &t, int op, std::int64_t *index1 
     float *o = (float *)((char *)sc.out.p + 16);
     std::int64_t *ix = index1 ? (std::int64_t *)((char *)sc.out.p + 24) : nullptr;
     if (table<float, Site>::on_device || host_in_place()) {
-        fold_raw(t.data(), f, op, o, ix);
+        fold_raw(t.data(), f, op, o, ix, false);  // waited for below
     } else {
         table<float, device_> dt(t.extent());
         dt = t;
-        fold_raw(dt.data(), f, op, o, ix);
+        fold_raw(dt.data(), f, op, o, ix, false);
     }
     float r = 0.0f;
     check(nt2g_memcpy(&r, o, sizeof r, 2, options().stream), "fold result");
@@ -1347,6 +1354,8 @@ template <class Site> inline table<float, Site> scan_dim(const table<float, Site
         check(nt2g_scan_f32(x, f.lo, f.inner, f.hi, op, options().precision, sc.ws.p, sc.ws.bytes, o,
                             options().stream),
               "scan");
+        // a host table read or written in place is the caller's as soon as this returns
+        if (!table<float, Site>::on_device) check(nt2g_stream_synchronize(options().stream), "scan");
     };
     if (table<float, Site>::on_device || host_in_place()) {
         run(t.data(), r.data());

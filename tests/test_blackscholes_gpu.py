@@ -71,7 +71,11 @@ def _d12(S, K, T, sig):
     return d1, d1 - v * np.sqrt(t)
 
 
-def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label=""):
+def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label="", fused=True):
+    """fused: the fused kernel's stated bound (helpers.BS_FAST_*).  Otherwise
+    (the expression evaluated as written, four normcdf calls through the
+    compiled kernel or the interpreter): no worse than NT2's own float
+    evaluation in mean, p99.9 and max."""
     ec, ep = _fast_errors(oracle, S, K, T, c, p, sig)
     rc, rp = oracle.blackscholes(S, K, T, R, sig)
     nc, np_ = _fast_errors(oracle, S, K, T, rc, rp, sig)
@@ -81,8 +85,11 @@ def _check_fast(oracle, S, K, T, c, p, sig=SIGMA, label=""):
     print(f"{label} NT2 restatement vs FP64: call max {nc.max():.2f} mean {nc.mean():.3f} p99.9 {q(nc):.2f}; "
           f"put max {np_.max():.2f} mean {np_.mean():.3f} p99.9 {q(np_):.2f}")
     for f, nn in ((ec, nc), (ep, np_)):
-        assert f.max() <= BS_FAST_MAX and f.max() <= nn.max()
-        assert q(f) <= BS_FAST_P999 and f.mean() <= BS_FAST_MEAN
+        if fused:
+            assert f.max() <= BS_FAST_MAX and f.max() <= nn.max()
+            assert q(f) <= BS_FAST_P999 and f.mean() <= BS_FAST_MEAN
+        else:
+            assert f.mean() <= nn.mean() and q(f) <= q(nn) and f.max() <= nn.max()
     d1, d2 = _d12(S, K, T, np.broadcast_to(sig, S.shape))
     core = (np.abs(d1) <= 2) & (np.abs(d2) <= 2)
     print(f"{label} |d|<=2 ({core.mean():.0%} of options): call max {ec[core].max():.2f} put max {ep[core].max():.2f}")
@@ -178,7 +185,7 @@ def test_generic_interpreter_reproduces_nt2(lib, dev, oracle):
     E.assign([c, p], bs_expr(E.Table(tS), E.Table(tK), E.Table(tT), SIGMA, R), precision=lib.PREC_FAST,
              force_generic=True)
     torch.cuda.synchronize()
-    _check_fast(oracle, S, K, T, c.cpu().numpy(), p.cpu().numpy(), label="interpreter")
+    _check_fast(oracle, S, K, T, c.cpu().numpy(), p.cpu().numpy(), label="interpreter", fused=False)
 
 
 def test_partial_transform_range(lib, dev, oracle):
