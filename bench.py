@@ -14,6 +14,8 @@ in HBM.  Workloads (--config):
   batched   4096 tables, sizes log-uniform in [1024, 4194304], one of BS /
             saxpy / expr3 each; one persistent launch per step
   pertable  the same batch, one plain launch per table per step
+  batched_programs  the same batch with every table a user program (its
+            expression written out), linked into one compiled batch kernel
   adjoint   fused BS forward + reverse (VJP), N=2^26 options
   adjoint_fwd  the forward alone on the same options (the 2.2x reference)
   sigmadelta   1920x1080 uint8 frames, one fused step per frame
@@ -338,14 +340,23 @@ class Reduce(Workload):
         self.red(self.x, self.y)
 
 
+def _bs_program_exprs(E, S, K, T, sig, r):
+    """Black-Scholes call/put as NT2 writes the expression (the textbook form)."""
+    sq = E.sqrt(T)
+    d1 = (E.log(S / K) + E.fma(E.sqr(sig), 0.5, r) * T) / (sig * sq)
+    d2 = E.fnms(sig, sq, d1)
+    e = K * E.exp(-r * T)
+    return [E.fnms(e, E.normcdf(d2), S * E.normcdf(d1)), E.fnms(S, E.normcdf(-d1), e * E.normcdf(-d2))]
+
+
 class Batched(Workload):
-    def __init__(self, torch, lib, dev, per_table=False, precision=0, tune=None):
+    def __init__(self, torch, lib, dev, per_table=False, precision=0, tune=None, programs=False):
         from tests.helpers import batched_sizes
         self.torch, self.lib, self.per_table = torch, lib, per_table
         sizes, exprs = batched_sizes()
         self.sizes, self.exprs = sizes, exprs
         g = torch.Generator(device=dev).manual_seed(1003)
-        self.tabs = []
+        self.tabs, self.keep = [], []
         items = (lib.BatchItem * len(sizes))()
         total_bytes = 0
         for i, (n, ex) in enumerate(zip(sizes, exprs)):
@@ -367,6 +378,19 @@ class Batched(Workload):
                 s = (0.0, 0.0)
                 total_bytes += 16 * n
             self.tabs.append((ins, outs))
+            if programs:  # the same table as a user program (its expression written out)
+                from nt2_gb300 import expr as E
+                T = [E.Table(t) for t in ins]
+                if ex == lib.BATCH_BLACKSCHOLES:
+                    ex_outs = _bs_program_exprs(E, T[0], T[1], T[2], E.Scalar(s[0]), E.Scalar(s[1]))
+                elif ex == lib.BATCH_SAXPY:
+                    ex_outs = [E.Scalar(s[0]) * T[0] + E.Table(outs[0])]
+                else:
+                    ex_outs = [E.exp(-E.sqr(T[0])) * E.sqrt(E.abs_(T[1])) + E.log1p(E.abs_(T[2]))]
+                it, prog, args = E.batch_item(outs, ex_outs)
+                self.keep.append((prog, args))
+                items[i] = it
+                continue
             items[i].expr, items[i].n = int(ex), n
             for j, t in enumerate(ins):
                 items[i].inp[j] = t.data_ptr()
@@ -378,18 +402,19 @@ class Batched(Workload):
         else:  # the project's autotuner, cached per GPU and batch shape
             from nt2_gb300 import autotune
             best, _, cached = autotune.tuned(items, precision)
-            tn, how = (best.block_threads, best.blocks_per_sm, best.tile_vectors), \
+            tn, how = (best.block_threads, best.blocks_per_sm, best.tile_vectors, best.vector_width), \
                 ("autotuned (cache)" if cached else "autotuned")
-        t = lib.BatchTune(tn[0], tn[1], tn[2], precision)
+        t = lib.BatchTune(tn[0], tn[1], tn[2], precision, tn[3] if len(tn) > 3 else 1)
         self.h = ctypes.c_void_p()
         lib.check(lib.load().nt2g_batch_create(items, len(sizes), ctypes.byref(t), ctypes.byref(self.h)))
         self.units = int(np.sum(sizes))
         self.bytes = total_bytes
         self.launches = len(sizes) if per_table else 1
-        self.kernel = "k_single" if per_table else "k_batch"
-        self.name = (f"batched 4096 tables log-uniform [1024, 4194304] ({self.units} elements), "
+        self.kernel = "k_single" if per_table else ("batch_" if programs else "k_batch")
+        self.name = (f"batched 4096 tables log-uniform [1024, 4194304] ({self.units} elements)"
+                     f"{', every table a user program' if programs else ''}, "
                      f"{'one plain launch per table' if per_table else 'one persistent launch'}, "
-                     f"tune threads,blocks/SM,vectors/tile={tn} ({how})")
+                     f"tune threads,blocks/SM,vectors/tile,vectors/step={tn} ({how})")
 
     def step(self, i):
         fn = self.lib.load().nt2g_batch_run_per_table if self.per_table else self.lib.load().nt2g_batch_run
@@ -648,6 +673,8 @@ def make(name, torch, lib, dev, precision, tune=None, n=None):
         return Batched(torch, lib, dev, per_table=False, precision=precision, tune=tune)
     if name == "pertable":
         return Batched(torch, lib, dev, per_table=True, precision=precision)
+    if name == "batched_programs":
+        return Batched(torch, lib, dev, per_table=False, precision=precision, tune=tune, programs=True)
     if name == "adjoint":
         return Adjoint(torch, lib, dev)
     if name == "adjoint_fwd":
@@ -922,7 +949,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-graph", action="store_true", help="issue the K steps eagerly instead of from a graph")
     ap.add_argument("--streams", type=int, default=2, help="streams for independent steps inside the graph")
-    ap.add_argument("--tune", default="", help="batched: block_threads,blocks_per_sm,tile_vectors")
+    ap.add_argument("--tune", default="", help="batched: block_threads,blocks_per_sm,tile_vectors[,vector_width]")
     ap.add_argument("--n", type=int, default=0, help="bs, bs_generic, bs_interp: options per launch (default 2^20); "
                     "fold/scan configs: elements of the square table (default 2^28); fn_*: elements (default 2^26)")
     ap.add_argument("--min-seconds", type=float, default=2.0, help="repeat K-step trials for at least this long")

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define NT2G_ABI_VERSION 1
+#define NT2G_ABI_VERSION 2
 
 typedef enum nt2g_status {
     NT2G_OK = 0,
@@ -391,20 +391,31 @@ nt2g_status nt2g_reduce_f32_noalloc(const float *x, const float *y, int64_t n, d
 /* Batched uneven tables: one persistent launch over many tables, each */
 /* with its own expression.                                             */
 /* ------------------------------------------------------------------ */
+/* Items name one of the three library expressions, or carry a compiled
+ * program (NT2G_BATCH_PROGRAM) with its arguments -- NT2's one generated
+ * kernel per expression (tools/kernel_gen/kernel_gen.cpp:64-76), here every
+ * distinct program of the batch linked into one run-time compiled kernel
+ * that dispatches on the program block-uniformly, one tile at a time.  A run
+ * is one persistent launch for the library expressions and one for the
+ * programs (either absent when it has no items).  Program items evaluate
+ * exactly as nt2g_eval with force_generic = 1 does. */
 
 typedef enum nt2g_batch_expr {
     NT2G_BATCH_BLACKSCHOLES = 0, /* in0=S in1=K in2=T, out0=call out1=put, s0=sigma s1=r */
     NT2G_BATCH_SAXPY = 1,        /* in0=X, out0=Y (in place), s0=alpha */
-    NT2G_BATCH_EXPR3 = 2         /* in0=x in1=y in2=z, out0 */
+    NT2G_BATCH_EXPR3 = 2,        /* in0=x in1=y in2=z, out0 */
+    NT2G_BATCH_PROGRAM = 3       /* program over args: any compiled elementwise program without FOLD */
 } nt2g_batch_expr;
 
 typedef struct nt2g_batch_item {
-    int32_t expr;
-    int32_t reserved;
-    int64_t n;
+    int32_t expr;                /* nt2g_batch_expr */
+    int32_t n_args;              /* NT2G_BATCH_PROGRAM: entries of args */
+    int64_t n;                   /* elements of the table */
     const float *in[3];
     float *out[2];
     float s[2];
+    const nt2g_program *program; /* NT2G_BATCH_PROGRAM: the element program (outlives the batch) */
+    const nt2g_arg *args;        /* NT2G_BATCH_PROGRAM: its slots, read by nt2g_batch_create */
 } nt2g_batch_item;
 
 typedef struct nt2g_batch_tune {
@@ -412,6 +423,8 @@ typedef struct nt2g_batch_tune {
     int32_t blocks_per_sm;     /* resident blocks per SM of the persistent grid */
     int32_t tile_vectors;      /* float4 vectors per tile per thread */
     int32_t precision;         /* nt2g_precision */
+    int32_t vector_width;      /* float4 vectors a thread has in flight per step: 1 or 2 (0 = 1) */
+    int32_t reserved;
 } nt2g_batch_tune;
 
 typedef struct nt2g_batch nt2g_batch;
@@ -438,6 +451,13 @@ nt2g_status nt2g_batch_autotune(const nt2g_batch_item *items, int32_t n_items,
                                 int32_t precision, void *stream, nt2g_batch_tune *best, float *best_ms);
 /* Total elements and algorithmic bytes of the batch. */
 nt2g_status nt2g_batch_stats(const nt2g_batch *b, int64_t *elements, int64_t *bytes);
+/* The CUDA source nt2g_batch_create compiles for a batch whose distinct
+ * programs are programs[0..n_programs) (no GPU needed; *len receives the size
+ * including the terminating NUL, cap = 0 only queries it).  Exposes the
+ * generated code for inspection and compile checks; no counterpart in the
+ * reference. */
+nt2g_status nt2g_batch_source(const nt2g_program *const *programs, int32_t n_programs, int32_t precision,
+                              int32_t block_threads, char *buf, size_t cap, size_t *len);
 
 /* ------------------------------------------------------------------ */
 /* Device memory for the table layer: nt2::table<T, device_> storage   */

@@ -1,7 +1,9 @@
 """Batched-launch tuning with a JSON cache.
 
-``tuned(items, precision)`` returns the fastest ``BatchTune`` for a batch
-shape on the current GPU, measuring with ``nt2g_batch_autotune`` the first
+``tuned(items, precision)`` returns the fastest ``BatchTune`` (block size,
+resident blocks per SM or static striding, float4 vectors per thread per
+tile, float4 vectors in flight per thread) for a batch shape on the current
+GPU, measuring with ``nt2g_batch_autotune`` the first
 time and reading the cache afterwards.  The key is the GPU name, the
 precision, the expression mix and the table-size histogram (log2 buckets), so
 batches of the same shape share one entry.  Cache file: $NT2G_TUNE_CACHE, or
@@ -26,7 +28,7 @@ def shape_key(items, precision):
     sizes = np.array([it.n for it in items], np.int64)
     exprs = np.array([it.expr for it in items], np.int64)
     hist = np.bincount(np.log2(np.maximum(sizes, 1)).astype(np.int64), minlength=32)
-    mix = np.bincount(exprs, minlength=3)
+    mix = np.bincount(exprs, minlength=4)
     return json.dumps([torch.cuda.get_device_name(), int(precision), mix.tolist(), hist.tolist()])
 
 
@@ -41,11 +43,13 @@ def tuned(items, precision=lib.PREC_FAST, reps=3, stream=None):
             cache = {}
     if key in cache:
         t = cache[key]["tune"]
-        return lib.BatchTune(t[0], t[1], t[2], precision), cache[key]["ms"], True
+        vw = t[3] if len(t) > 3 else 1
+        return lib.BatchTune(t[0], t[1], t[2], precision, vw), cache[key]["ms"], True
     best, ms = lib.BatchTune(), ctypes.c_float()
     lib.check(lib.load().nt2g_batch_autotune(items, len(items), None, 0, reps, precision, lib._stream(stream),
                                              ctypes.byref(best), ctypes.byref(ms)))
-    cache[key] = {"tune": [best.block_threads, best.blocks_per_sm, best.tile_vectors], "ms": ms.value}
+    cache[key] = {"tune": [best.block_threads, best.blocks_per_sm, best.tile_vectors, best.vector_width],
+                  "ms": ms.value}
     os.makedirs(os.path.dirname(path), exist_ok=True)
     with open(path, "w") as f:
         json.dump(cache, f, indent=1)

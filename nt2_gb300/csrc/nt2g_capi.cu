@@ -750,6 +750,41 @@ static nt2g_status bind_args(const nt2g_program *p, const nt2g_arg *args, int64_
     return NT2G_OK;
 }
 
+namespace nt2g {
+
+const std::vector<nt2g_op> &program_ops(const nt2g_program *p) { return p->ops; }
+const std::vector<uint8_t> &program_logical(const nt2g_program *p) { return p->logical; }
+bool program_folds(const nt2g_program *p) { return p->folds; }
+
+nt2g_status program_bind(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t count, const char *who,
+                         DArgs &da)
+{
+    NT2G_CHECK_ARG(n_args >= p->n_slots && (args != nullptr || p->n_slots == 0), "%s: %d arguments for %d slots", who,
+                   n_args, p->n_slots);
+    return bind_args(p, args, 0, count, who, da);
+}
+
+int64_t program_bytes_per_element(const nt2g_program *p)
+{
+    int64_t b = 0;
+    for (int s = 0; s < p->n_slots; ++s) {
+        const int use = p->slot_use[s];
+        if (use & 4) continue;
+        b += (int64_t)(((use & 1) ? 1 : 0) + ((use & 2) ? 1 : 0)) * (int64_t)dtype_size(p->slot_dtype[s]);
+    }
+    return b;
+}
+
+nt2g_status program_eval(const nt2g_program *p, const DArgs &da, int64_t count, int precision, cudaStream_t st)
+{
+    if (count == 0) return NT2G_OK;
+    nt2g_status js = launch_jit(p->ops, p->logical, da, count, precision, st);
+    if (js != NT2G_ERR_UNSUPPORTED) return js;
+    return launch_interp(p->dprog, da, count, precision, st);
+}
+
+}  // namespace nt2g
+
 extern "C" nt2g_status nt2g_eval(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t offset,
                                  int64_t count, int32_t precision, int32_t force_generic, void *stream)
 {

@@ -114,9 +114,36 @@ const JitFoldKernels *jit_fold_kernels(const std::vector<nt2g_op> &ops, const st
 std::string jit_fold_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision,
                             int op);
 std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision);
+// A batch's programs linked into one persistent kernel per (dynamic | static
+// tile schedule) x (1 | 2 float4 vectors per thread), compiled for one block
+// size; per_sm holds each kernel's resident blocks per SM at that size.
+struct ProgramCode {
+    const std::vector<nt2g_op> *ops;
+    const std::vector<uint8_t> *logical;
+};
+struct BatchJitKernels {
+    cudaKernel_t k[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [dynamic][vectors - 1]
+    int per_sm[2][2] = {{0, 0}, {0, 0}};
+};
+std::string jit_batch_source(const std::vector<ProgramCode> &progs, int precision, int block_threads);
+const BatchJitKernels *jit_batch_kernels(const std::vector<ProgramCode> &progs, int precision, int block_threads,
+                                         std::string *why);
 bool jit_enabled();
 nt2g_status jit_prepare(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision);
 nt2g_status launch_jit(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, const DArgs &args,
                        int64_t count, int precision, cudaStream_t st);
+
+// Compiled programs as the batch sees them (nt2g_capi.cu owns their layout).
+const std::vector<nt2g_op> &program_ops(const nt2g_program *p);
+const std::vector<uint8_t> &program_logical(const nt2g_program *p);
+bool program_folds(const nt2g_program *p);
+// Bind n_args arguments over elements [0, count) (nt2g_eval's checks).
+nt2g_status program_bind(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t count, const char *who,
+                         DArgs &da);
+// Table bytes one element moves: each loaded slot read once, each stored slot written once.
+int64_t program_bytes_per_element(const nt2g_program *p);
+// The program's generic evaluation (run-time compiled kernel, else the
+// interpreter): what nt2g_eval does with force_generic = 1.
+nt2g_status program_eval(const nt2g_program *p, const DArgs &da, int64_t count, int precision, cudaStream_t st);
 
 }  // namespace nt2g

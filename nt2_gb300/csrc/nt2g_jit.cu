@@ -110,6 +110,38 @@ template <bool FULL> __device__ __forceinline__ void jit_stb(void *p, long long 
     if (FULL) *(unsigned *)q = (v[0] & 255u) | (v[1] & 255u) << 8 | (v[2] & 255u) << 16 | (v[3] & 255u) << 24;
     else { NT2G_L if (j < cnt) q[j] = (unsigned char)v[j]; }
 }
+// Two vectors per thread (batched tiles): lanes 0-3 at element i, lanes 4-7 a
+// block-width of vectors further (i + 4 blockDim.x), so a warp's accesses stay
+// contiguous; only whole, aligned pairs take this form.
+template <int L> __device__ __forceinline__ long long jit_pos(long long i, int j)
+{
+    return L <= 4 ? i + j : i + (j & 3) + (long long)(j >> 2) * blockDim.x * 4;
+}
+template <bool FULL> __device__ __forceinline__ void jit_ldf(float (&d)[8], const void *p, long long i, int)
+{
+    const float *q = (const float *)p + i;
+    const float4 t = __ldcs((const float4 *)q), u = __ldcs((const float4 *)(q + (long long)blockDim.x * 4));
+    d[0] = t.x; d[1] = t.y; d[2] = t.z; d[3] = t.w; d[4] = u.x; d[5] = u.y; d[6] = u.z; d[7] = u.w;
+}
+template <bool FULL> __device__ __forceinline__ void jit_ldb(unsigned (&d)[8], const void *p, long long i, int)
+{
+    const unsigned char *q = (const unsigned char *)p + i;
+    const unsigned w0 = *(const unsigned *)q, w1 = *(const unsigned *)(q + (long long)blockDim.x * 4);
+    NT2G_L { d[j] = (w0 >> (8 * j)) & 255u; d[j + 4] = (w1 >> (8 * j)) & 255u; }
+}
+template <bool FULL> __device__ __forceinline__ void jit_stf(void *p, long long i, int, const float (&v)[8])
+{
+    float *q = (float *)p + i;
+    __stcs((float4 *)q, make_float4(v[0], v[1], v[2], v[3]));
+    __stcs((float4 *)(q + (long long)blockDim.x * 4), make_float4(v[4], v[5], v[6], v[7]));
+}
+template <bool FULL> __device__ __forceinline__ void jit_stb(void *p, long long i, int, const unsigned (&v)[8])
+{
+    unsigned char *q = (unsigned char *)p + i;
+    *(unsigned *)q = (v[0] & 255u) | (v[1] & 255u) << 8 | (v[2] & 255u) << 16 | (v[3] & 255u) << 24;
+    *(unsigned *)(q + (long long)blockDim.x * 4) =
+        (v[4] & 255u) | (v[5] & 255u) << 8 | (v[6] & 255u) << 16 | (v[7] & 255u) << 24;
+}
 )NT2G_SRC";
 
 static std::string fconst(float f)
@@ -134,7 +166,7 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         const nt2g_op &o = ops[k];
         if (o.code != NT2G_OP_LOAD) continue;
         const bool f32 = o.dtype == NT2G_F32;
-        s += (f32 ? "    float v" : "    unsigned v") + std::to_string(k) + "[4]; " +
+        s += (f32 ? "    float v" : "    unsigned v") + std::to_string(k) + "[A]; " +
              (f32 ? "jit_ldf<FULL>(v" : "jit_ldb<FULL>(v") + std::to_string(k) + ", a.ptr[" + std::to_string(o.a) +
              "], i, cnt);\n";
     }
@@ -168,7 +200,7 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
             // the positive side is the one whose argument is y itself
             const bool k_is_neg = ops[o.a].code == NT2G_OP_NEG && ops[o.a].a == ops[p].a;
             const int pos = k_is_neg ? p : (int)k, neg = k_is_neg ? (int)k : p;
-            s += "    float v" + std::to_string(k) + "[4], v" + std::to_string(p) + "[4]; NT2G_LL nt2g::normcdf_pair<P>(" +
+            s += "    float v" + std::to_string(k) + "[A], v" + std::to_string(p) + "[A]; NT2G_LL nt2g::normcdf_pair<P>(" +
                  v(ops[pos].a) + ", " + v(pos) + ", " + v(neg) + ");\n";
             continue;
         }
@@ -184,7 +216,7 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
             const std::string src = "v" + std::to_string(o.a);
             const std::string dst = std::to_string(o.b);
             if (f32 && logical[o.a])  // a comparison result stored as 0.0f / 1.0f
-                s += "    { float t[4]; NT2G_LL t[j] = (float)" + src + "[j]; jit_stf<FULL>(a.ptr[" + dst + "], i, cnt, t); }\n";
+                s += "    { float t[A]; NT2G_LL t[j] = (float)" + src + "[j]; jit_stf<FULL>(a.ptr[" + dst + "], i, cnt, t); }\n";
             else
                 s += std::string(f32 ? "    jit_stf<FULL>(a.ptr[" : "    jit_stb<FULL>(a.ptr[") + dst + "], i, cnt, " +
                      src + ");\n";
@@ -192,7 +224,9 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         }
         case NT2G_OP_SCALAR: e = f32 ? "a.scal[" + slot + "]" : "a.scal_u8[" + slot + "]"; break;
         case NT2G_OP_CONST: e = f32 ? fconst(o.imm) : std::to_string((uint32_t)o.imm & 255u) + "u"; break;
-        case NT2G_OP_INDEX: e = f32 ? "nt2g::pos_to_float(a.pos0 + i + j)" : "(unsigned)((a.pos0 + i + j) & 255)"; break;
+        case NT2G_OP_INDEX:
+            e = f32 ? "nt2g::pos_to_float(a.pos0 + jit_pos<L>(i, j))" : "(unsigned)((a.pos0 + jit_pos<L>(i, j)) & 255)";
+            break;
         case NT2G_OP_ADD: e = f32 ? "P::add(" + A + ", " + B + ")" : "(" + A + " + " + B + ") & 255u"; break;
         case NT2G_OP_SUB: e = f32 ? "P::sub(" + A + ", " + B + ")" : "(" + A + " - " + B + ") & 255u"; break;
         case NT2G_OP_MUL: e = f32 ? "P::mul(" + A + ", " + B + ")" : "(" + A + " * " + B + ") & 255u"; break;
@@ -300,7 +334,7 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         case NT2G_OP_ATANH: e = "nt2g::atanh<P>(" + A + ")"; break;
         default: e = "nt2g::fastnormcdf<P>(" + A + ")"; break;
         }
-        s += std::string(u ? "    unsigned v" : "    float v") + std::to_string(k) + "[4]; NT2G_LL v" +
+        s += std::string(u ? "    unsigned v" : "    float v") + std::to_string(k) + "[A]; NT2G_LL v" +
              std::to_string(k) + "[j] = " + e + ";\n";
     }
 }
@@ -312,7 +346,7 @@ std::string jit_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_
     s += kNt2gMathSrc;
     s += kJitPrelude;
     s += "template <class P, bool FULL>\n__device__ __forceinline__ void jit_tile(const JitArgs &a, long long i, int cnt)\n{\n"
-         "    constexpr int L = 4;\n";
+         "    constexpr int L = 4, A = 4;\n";
     emit_body(s, ops, logical);
     s += "}\n\nextern \"C\" __global__ void __launch_bounds__(256) nt2g_jit_kernel(const JitArgs a, long long n, int vec)\n{\n";
     s += precision == NT2G_PREC_NT2 ? "    typedef nt2g::Nt2 P;\n" : "    typedef nt2g::Fast P;\n";
@@ -342,7 +376,7 @@ std::string jit_fold_source(const std::vector<nt2g_op> &ops, const std::vector<u
     s += kNt2gAccumSrc;
     s += kNt2gFoldSrc;
     s += "template <class P, bool FULL, int L>\n__device__ __forceinline__ void jit_value(const JitArgs &a, long long i, "
-         "int cnt, float (&out)[4])\n{\n";
+         "int cnt, float (&out)[4])\n{\n    constexpr int A = 4;\n";
     emit_body(s, ops, logical);
     s += "}\n\n";
     s += precision == NT2G_PREC_FAST ? "typedef nt2g::Fast P;\n" : "typedef nt2g::Nt2 P;\n";
@@ -382,6 +416,74 @@ std::string jit_fold_source(const std::vector<nt2g_op> &ops, const std::vector<u
                  "{ nt2g::fold::outer_body<ExprSrc, NT2G_FOP, " + V + ", " + F +
                  ">(ExprSrc{a}, lo, inner, hi, ck, q, part, out, index, cen, out64); }\n";
         }
+    return s;
+}
+
+// The programs of a batch linked into one persistent kernel.  Each program
+// becomes prog<k>_tile (W float4 vectors per thread: 4 W lanes, the second
+// vector a block-width further); the kernel takes tiles of the batch's items
+// (a static stride over the grid or an atomic counter) and switches on the
+// item's program once per tile, so the dispatch is block-uniform.  A tile is
+// run in whole aligned pairs of vectors while they last (W = 2), then one
+// vector at a time, the ragged end by element.  The statements are those of
+// jit_source, so every element is bit-identical to the program's own kernel.
+std::string jit_batch_source(const std::vector<ProgramCode> &progs, int precision, int block_threads)
+{
+    std::string s;
+    s.reserve(sizeof kJitPrelude + 40000 + progs.size() * 4096);
+    s += kNt2gMathSrc;
+    s += kJitPrelude;
+    s += "struct BItem { JitArgs a; long long n; int prog; int vec; };\n";
+    for (size_t k = 0; k < progs.size(); ++k) {
+        s += "template <class P, bool FULL, int W>\n__device__ __forceinline__ void prog" + std::to_string(k) +
+             "_tile(const JitArgs &a, long long i, int cnt)\n{\n    constexpr int L = 4 * W, A = 4 * W;\n";
+        emit_body(s, *progs[k].ops, *progs[k].logical);
+        s += "}\n";
+    }
+    s += precision == NT2G_PREC_NT2 ? "typedef nt2g::Nt2 P;\n" : "typedef nt2g::Fast P;\n";
+    s += "#define NT2G_RUN(fn) { \\\n"
+         "    const long long step = (long long)blockDim.x * 4; \\\n"
+         "    long long i = start + (long long)threadIdx.x * 4; \\\n"
+         "    if constexpr (W == 2) { \\\n"
+         "        if (it.vec) for (; i + step + 4 <= end; i += 2 * step) fn<P, true, 2>(it.a, i, 8); } \\\n"
+         "    for (; i < end; i += step) { \\\n"
+         "        const int cnt = end - i < 4 ? (int)(end - i) : 4; \\\n"
+         "        if (it.vec && cnt == 4) fn<P, true, 1>(it.a, i, 4); else fn<P, false, 1>(it.a, i, cnt); } }\n";
+    s += "__device__ __forceinline__ int find_item(const long long *prefix, int n_items, long long t)\n{\n"
+         "    int lo = 0, hi = n_items;\n"
+         "    while (hi - lo > 1) { const int mid = (lo + hi) >> 1; if (__ldg(prefix + mid) <= t) lo = mid; else hi = mid; }\n"
+         "    return lo;\n}\n";
+    s += "template <bool DYNAMIC, int W>\n__device__ __forceinline__ void batch_body(const BItem *items, "
+         "const long long *prefix, int n_items, long long total_tiles, long long tile_elems, "
+         "unsigned long long *counter)\n{\n"
+         "    __shared__ long long s_tile;\n"
+         "    long long t = DYNAMIC ? 0 : blockIdx.x;\n"
+         "    while (true) {\n"
+         "        if (DYNAMIC) {\n"
+         "            if (threadIdx.x == 0) s_tile = (long long)atomicAdd(counter, 1ull);\n"
+         "            __syncthreads();\n"
+         "            t = s_tile;\n"
+         "            __syncthreads();\n"
+         "        }\n"
+         "        if (t >= total_tiles) return;\n"
+         "        const int k = find_item(prefix, n_items, t);\n"
+         "        const BItem it = items[k];\n"
+         "        const long long start = (t - __ldg(prefix + k)) * tile_elems;\n"
+         "        const long long end = start + tile_elems < it.n ? start + tile_elems : it.n;\n"
+         "        switch (it.prog) {\n";
+    for (size_t k = 0; k < progs.size(); ++k)
+        s += "        case " + std::to_string(k) + ": NT2G_RUN(prog" + std::to_string(k) + "_tile); break;\n";
+    s += "        default: break;\n"
+         "        }\n"
+         "        if (!DYNAMIC) t += gridDim.x;\n"
+         "    }\n}\n";
+    const std::string bt = std::to_string(block_threads);
+    for (int dyn = 0; dyn < 2; ++dyn)
+        for (int w = 1; w <= 2; ++w)
+            s += "extern \"C\" __global__ void __launch_bounds__(" + bt + ") batch_" + std::to_string(dyn) +
+                 std::to_string(w) + "(const BItem *items, const long long *prefix, int n_items, long long total_tiles, "
+                 "long long tile_elems, unsigned long long *counter)\n{ batch_body<" + (dyn ? "true" : "false") + ", " +
+                 std::to_string(w) + ">(items, prefix, n_items, total_tiles, tile_elems, counter); }\n";
     return s;
 }
 
@@ -506,6 +608,60 @@ const JitFoldKernels *jit_fold_kernels(const std::vector<nt2g_op> &ops, const st
             }
         }
         it = g_fold_cache.emplace(key, e).first;
+    }
+    if (!it->second.ok) {
+        if (why) *why = it->second.error;
+        return nullptr;
+    }
+    return &it->second.k;
+}
+
+struct JitBatchEntry {
+    cudaLibrary_t lib = nullptr;
+    BatchJitKernels k;
+    bool ok = false;
+    std::string error;
+};
+static std::map<std::string, JitBatchEntry> g_batch_cache;  // key: device | precision | block | programs
+
+const BatchJitKernels *jit_batch_kernels(const std::vector<ProgramCode> &progs, int precision, int block_threads,
+                                         std::string *why)
+{
+    if (!jit_enabled()) {
+        if (why) *why = "JIT disabled (NT2G_JIT=0)";
+        return nullptr;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::string key = std::to_string(dev) + "|" + std::to_string(precision) + "|" + std::to_string(block_threads);
+    for (const ProgramCode &pc : progs) {
+        key += "|" + std::to_string(pc.ops->size()) + ":";
+        key.append((const char *)pc.ops->data(), pc.ops->size() * sizeof(nt2g_op));
+        key.append((const char *)pc.logical->data(), pc.logical->size());
+    }
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_batch_cache.find(key);
+    if (it == g_batch_cache.end()) {
+        JitBatchEntry e;
+        std::string cubin = compile_cubin(jit_batch_source(progs, precision, block_threads), e.error);
+        if (!cubin.empty()) {
+            cudaError_t ce = cudaLibraryLoadData(&e.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+            for (int d = 0; d < 2; ++d)
+                for (int w = 0; w < 2; ++w) {
+                    const std::string name = "batch_" + std::to_string(d) + std::to_string(w + 1);
+                    if (ce == cudaSuccess) ce = cudaLibraryGetKernel(&e.k.k[d][w], e.lib, name.c_str());
+                    if (ce == cudaSuccess)
+                        ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e.k.per_sm[d][w], (const void *)e.k.k[d][w],
+                                                                           block_threads, 0);
+                }
+            if (ce == cudaSuccess) {
+                e.ok = true;
+            } else {
+                e.error = std::string("loading the JIT batch kernels: ") + cudaGetErrorString(ce);
+                cudaGetLastError();
+            }
+        }
+        it = g_batch_cache.emplace(key, e).first;
     }
     if (!it->second.ok) {
         if (why) *why = it->second.error;

@@ -520,6 +520,34 @@ def _args_of(slots):
     return args, n
 
 
+def batch_item(outs, exprs):
+    """A program item of a batch (nt2g_batch_item, NT2G_BATCH_PROGRAM):
+    tie(outs...) = tie(exprs...) over the whole tables.  Returns (item,
+    program, args): args must stay alive until nt2g_batch_create returns, the
+    program (also held by this module's cache) as long as the batch."""
+    outs, exprs = list(outs), list(exprs)
+    prog, slots = compile_program(outs, exprs)
+    args, n = _args_of(slots)
+    if n is None:
+        n = _generative_sizes(exprs[0]).pop()
+    _check_generative_sizes(exprs, n)
+    it = lib.BatchItem()
+    it.expr, it.n, it.n_args = lib.BATCH_PROGRAM, n, len(slots)
+    it.program = prog.handle.value
+    it.args = ctypes.cast(args, ctypes.POINTER(lib.Arg))
+    return it, prog, args
+
+
+def batch_source(programs, precision=lib.PREC_FAST, block_threads=256):
+    """CUDA source of the batch kernel that links these programs."""
+    L, n = lib.load(), ctypes.c_size_t()
+    hs = (ctypes.c_void_p * len(programs))(*[p.handle.value for p in programs])
+    lib.check(L.nt2g_batch_source(hs, len(programs), precision, block_threads, None, 0, ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value)
+    lib.check(L.nt2g_batch_source(hs, len(programs), precision, block_threads, buf, n.value, ctypes.byref(n)))
+    return buf.value.decode()
+
+
 def fold(e, op="sum", shape=None, precision=lib.PREC_FAST, index=False, out64=False, stream=None):
     """NT2's fold of an expression along one dimension in one pass
     (nt2g_eval_fold): e's value at every element is computed inside the fold

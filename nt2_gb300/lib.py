@@ -42,7 +42,7 @@ MAP_FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, n
               tanpi=34, cotpi=35, cotd=36, secpi=37, cscpi=38, secd=39, cscd=40, sinc=41, sincpi=42, acotd=43, asec=44, coth=45, sinhc=46, acsc=47, asech=48, acoth=49, acsch=50,
               erf=64, erfcx=65, expx2=66, gamma=67, gammaln=68, erfinv=69, erfcinv=70, exprecneg=80, exprecnegc=81, sqrt1pm1=82)
 
-BATCH_BLACKSCHOLES, BATCH_SAXPY, BATCH_EXPR3 = 0, 1, 2
+BATCH_BLACKSCHOLES, BATCH_SAXPY, BATCH_EXPR3, BATCH_PROGRAM = 0, 1, 2, 3
 
 
 class Op(ctypes.Structure):
@@ -61,13 +61,15 @@ class ProgramInfo(ctypes.Structure):
 
 
 class BatchItem(ctypes.Structure):
-    _fields_ = [("expr", ctypes.c_int32), ("reserved", ctypes.c_int32), ("n", ctypes.c_int64),
-                ("inp", ctypes.c_void_p * 3), ("out", ctypes.c_void_p * 2), ("s", ctypes.c_float * 2)]
+    _fields_ = [("expr", ctypes.c_int32), ("n_args", ctypes.c_int32), ("n", ctypes.c_int64),
+                ("inp", ctypes.c_void_p * 3), ("out", ctypes.c_void_p * 2), ("s", ctypes.c_float * 2),
+                ("program", ctypes.c_void_p), ("args", ctypes.POINTER(Arg))]
 
 
 class BatchTune(ctypes.Structure):
     _fields_ = [("block_threads", ctypes.c_int32), ("blocks_per_sm", ctypes.c_int32),
-                ("tile_vectors", ctypes.c_int32), ("precision", ctypes.c_int32)]
+                ("tile_vectors", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("vector_width", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Nt2gError(RuntimeError):
@@ -104,6 +106,8 @@ _SIGNATURES = {
     "nt2g_batch_run": (_I32, [_VP, _VP]),
     "nt2g_batch_run_per_table": (_I32, [_VP, _VP]),
     "nt2g_batch_run_graph": (_I32, [_VP, _VP]),
+    "nt2g_batch_source": (_I32, [ctypes.POINTER(_VP), _I32, _I32, _I32, ctypes.c_char_p, ctypes.c_size_t,
+                                  ctypes.POINTER(ctypes.c_size_t)]),
     "nt2g_batch_autotune": (_I32, [ctypes.POINTER(BatchItem), _I32, ctypes.POINTER(BatchTune), _I32, _I32, _I32, _VP,
                                     ctypes.POINTER(BatchTune), ctypes.POINTER(ctypes.c_float)]),
     "nt2g_batch_stats": (_I32, [_VP, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),

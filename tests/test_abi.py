@@ -38,7 +38,7 @@ def test_opcode_values_match_header(lib):
 
 
 def test_abi_version(lib):
-    assert lib.load().nt2g_abi_version() == 1
+    assert lib.load().nt2g_abi_version() == 2
 
 
 def _cpu_tables(n=8, k=3, dtype=torch.float32):
@@ -177,6 +177,29 @@ def test_batch_create_validates_items(lib):
     assert L.nt2g_batch_create(items, 1, ctypes.byref(tune), ctypes.byref(h)) == lib.ERR_INVALID
 
 
+def test_batch_create_validates_program_items(lib):
+    """Program items: a missing program, a fold program, too few arguments and
+    an unknown vector width are refused before anything reaches the device."""
+    L = lib.load()
+    h = ctypes.c_void_p()
+    x = E.Table(torch.zeros(8))
+    prog, slots = E.compile_program([torch.zeros(8)], [E.exp(x)])
+    fold_prog, _ = E.compile_program([], [], fold=E.exp(x))
+    args = (lib.Arg * 2)(lib.Arg(8, 0.0, lib.F32, 0), lib.Arg(16, 0.0, lib.F32, 0))
+    items = (lib.BatchItem * 1)()
+    items[0].expr, items[0].n, items[0].n_args = lib.BATCH_PROGRAM, 8, 2
+    items[0].args = ctypes.cast(args, ctypes.POINTER(lib.Arg))
+    assert L.nt2g_batch_create(items, 1, None, ctypes.byref(h)) == lib.ERR_INVALID  # no program
+    items[0].program = fold_prog.handle.value
+    assert L.nt2g_batch_create(items, 1, None, ctypes.byref(h)) == lib.ERR_INVALID  # folds
+    assert b"folds" in lib.load().nt2g_last_error()
+    items[0].program, items[0].n_args = prog.handle.value, 1
+    assert L.nt2g_batch_create(items, 1, None, ctypes.byref(h)) == lib.ERR_INVALID  # 1 argument, 2 slots
+    tune = lib.BatchTune(256, 0, 4, 0, 3)
+    assert L.nt2g_batch_create(items, 1, ctypes.byref(tune), ctypes.byref(h)) == lib.ERR_INVALID  # width 3
+    assert not h.value
+
+
 def _nvrtc():
     for name in ("libnvrtc.so.13", "/usr/local/cuda/lib64/libnvrtc.so.13"):
         try:
@@ -284,3 +307,33 @@ def test_fold_programs_validate(lib):
     assert L.nt2g_program_create(ops, 3, 2, ctypes.byref(h)) == lib.ERR_INVALID
     ops[2] = lib.Op(lib.OP["STORE"], 0, 0, 1, -1, 0.0)
     assert L.nt2g_program_create(ops, 3, 2, ctypes.byref(h)) == lib.ERR_INVALID
+
+
+def test_batch_kernel_source_builds_for_sm103a(lib):
+    """The kernel a batch of user programs is linked into (every program a
+    tile function, a block-uniform switch, dynamic/static schedules, one and
+    two float4 vectors per thread) compiles for sm_103a under both policies."""
+    nv = _nvrtc()
+    S, K, T = _cpu_tables()
+    c, p = torch.zeros(8), torch.zeros(8)
+    bs, _ = E.compile_program([c, p], list(bs_textbook(S, K, T, E.Scalar(0.3), E.Scalar(0.02))))
+    u8 = torch.uint8
+    fr, bkg, var = _cpu_tables(16, 3, u8)
+    d = E.max_(bkg, fr) - E.min_(bkg, fr)
+    lab = torch.zeros(16, dtype=u8)
+    mixed, _ = E.compile_program([lab, c], [E.if_zero_else_one(d < var, lib.U8), E.Table(torch.zeros(8)) > 1.0])
+    gen, _ = E.compile_program([c], [E.sinpi(E.linspace(0, 2, 8)) * E.Table(torch.zeros(8))])
+    for prec, bt in ((lib.PREC_FAST, 256), (lib.PREC_NT2, 128)):
+        src = E.batch_source([bs, mixed, gen], prec, bt)
+        for k in range(3):
+            assert f"case {k}: NT2G_RUN(prog{k}_tile)" in src
+        for name in ("batch_01", "batch_02", "batch_11", "batch_12"):
+            assert f"__launch_bounds__({bt}) {name}(" in src
+        rc, log, size = _nvrtc_compile(nv, src)
+        assert rc == 0, log[:2000]
+        assert size > 0
+    n = ctypes.c_size_t()
+    hs = (ctypes.c_void_p * 1)(bs.handle.value)
+    L = lib.load()
+    assert L.nt2g_batch_source(hs, 1, 0, 100, None, 0, ctypes.byref(n)) == lib.ERR_INVALID  # block size
+    assert L.nt2g_batch_source(hs, 0, 0, 256, None, 0, ctypes.byref(n)) == lib.ERR_INVALID

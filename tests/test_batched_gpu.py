@@ -1,7 +1,9 @@
 """Batched persistent launch over uneven tables: every table's result is
 bit-identical to the plain kernel on that table, through the persistent
-kernel (dynamic and static tile schedules), the per-table launches and the
-CUDA-graph replay."""
+kernel (dynamic and static tile schedules, one and two float4 vectors per
+thread), the per-table launches and the CUDA-graph replay; batches of user
+programs match the programs' own evaluation and, under the NT2 policy, the
+oracle."""
 import ctypes
 
 import numpy as np
@@ -9,6 +11,7 @@ import pytest
 import torch
 
 from helpers import batched_sizes
+from nt2_gb300 import expr as E
 
 pytestmark = pytest.mark.gpu
 
@@ -82,15 +85,16 @@ def _check(outs, ref):
             assert torch.equal(a.view(torch.int32), b.view(torch.int32)), k
 
 
-@pytest.mark.parametrize("tune", [(256, 0, 4), (128, 0, 1), (512, -1, 2), (256, 2, 8)],
-                         ids=["dyn256x4", "dyn128x1", "static512x2", "dyn256x8_2perSM"])
+@pytest.mark.parametrize("tune", [(256, 0, 4, 1), (128, 0, 1, 1), (512, -1, 2, 1), (256, 2, 8, 1), (256, 0, 8, 2),
+                                  (128, -1, 3, 2)],
+                         ids=["dyn256x4", "dyn128x1", "static512x2", "dyn256x8_2perSM", "dyn256x8_w2", "static128x3_w2"])
 def test_batched_matches_plain_kernels(lib, dev, tune):
     sizes, exprs = batched_sizes(count=96, lo=1, hi=300000, seed=5)
     sizes[:3] = [1, 3, 5]
     tabs = _make(lib, dev, sizes, exprs)
     ref = _reference(lib, tabs)
     L = lib.load()
-    t = lib.BatchTune(tune[0], tune[1], tune[2], lib.PREC_FAST)
+    t = lib.BatchTune(tune[0], tune[1], tune[2], lib.PREC_FAST, tune[3])
     stream = torch.cuda.Stream()
     for mode in ("run", "per_table", "graph"):
         outs = _fresh_outs(lib, tabs)
@@ -207,3 +211,206 @@ def test_autotuner_picks_a_candidate_and_caches(lib, dev, tmp_path, monkeypatch)
         _check(outs, ref)
     finally:
         L.nt2g_batch_destroy(h)
+
+
+# ------------------------------------------------------------ user programs --
+F32 = np.float32
+PROGRAM_KINDS = ("sincos", "branch", "rgb2yuv", "sigmadelta", "generative")
+
+
+def _program_arrays(kind, n, rng):
+    """Inputs and initial outputs (host arrays) of one user-program table."""
+    if kind == "sincos":
+        return {"x": (rng.standard_normal(n) * 3).astype(F32), "y": (rng.standard_normal(n) * 3).astype(F32),
+                "o": np.zeros(n, F32)}
+    if kind == "branch":
+        return {"x": (rng.standard_normal(n) * 2).astype(F32), "o": np.zeros(n, F32)}
+    if kind == "rgb2yuv":
+        return {"r": rng.uniform(0, 1, n).astype(F32), "g": rng.uniform(0, 1, n).astype(F32),
+                "b": rng.uniform(0, 1, n).astype(F32), "Y": np.zeros(n, F32), "U": np.zeros(n, F32),
+                "V": np.zeros(n, F32)}
+    if kind == "sigmadelta":
+        return {"fr": rng.integers(0, 256, n, dtype=np.uint8), "bkg": rng.integers(0, 256, n, dtype=np.uint8),
+                "var": rng.integers(1, 40, n, dtype=np.uint8), "lab": np.zeros(n, np.uint8)}
+    return {"x": rng.standard_normal(n).astype(F32), "o": np.zeros(n, F32)}
+
+
+def _device(dev, arrays, misaligned):
+    """Device copies; misaligned tables start one element into their buffer."""
+    out = {}
+    for k, a in arrays.items():
+        t = torch.from_numpy(a.copy())
+        if misaligned:
+            buf = torch.zeros(a.size + 1, dtype=t.dtype, device=dev)
+            buf[1:].copy_(t)
+            out[k] = buf[1:]
+        else:
+            out[k] = t.to(dev)
+    return out
+
+
+def _program(kind, t, n):
+    """(outs, exprs) of the user program over device tables t."""
+    T = {k: E.Table(v) for k, v in t.items()}
+    if kind == "sincos":
+        return [t["o"]], [E.sin(T["x"]) * E.cos(T["y"])]
+    if kind == "branch":
+        return [t["o"]], [E.if_else(T["x"] > 0.0, E.exp(-T["x"]), E.log1p(E.abs_(T["x"])))]
+    if kind == "rgb2yuv":  # tie: u and v read the y just stored
+        R, G, B, Y = T["r"], T["g"], T["b"], T["Y"]
+        return [t["Y"], t["U"], t["V"]], [0.299 * R + 0.587 * G + 0.114 * B, 0.492 * (B - Y), 0.877 * (R - Y)]
+    if kind == "sigmadelta":  # one sigma-delta step, background and variance updated in place
+        fr, bkg, var = T["fr"], T["bkg"], T["var"]
+        nb = E.selinc(bkg < fr, E.seldec(bkg > fr, bkg))
+        d = E.max_(bkg, fr) - E.min_(bkg, fr)
+        m = E.adds(E.adds(d, d), d)
+        nv = E.if_else(d.ne(0), E.selinc(var < m, E.seldec(var > m, var)), var)
+        return [t["bkg"], t["var"], t["lab"]], [nb, nv, E.if_zero_else_one(d < var, 1)]
+    return [t["o"]], [E.sinpi(E.linspace(0, 2, n)) * T["x"]]
+
+
+def _program_oracle(oracle, kind, a, n):
+    """NT2's evaluation of the program (CPU restatement), outputs in order."""
+    if kind == "sincos":
+        return [(oracle.map_f32("sin", a["x"]) * oracle.map_f32("cos", a["y"])).astype(F32)]
+    if kind == "branch":
+        x = a["x"]
+        return [np.where(x > 0, oracle.map_f32("exp", -x), oracle.map_f32("log1p", np.abs(x))).astype(F32)]
+    if kind == "rgb2yuv":
+        return list(oracle.rgb2yuv(a["r"], a["g"], a["b"]))
+    if kind == "sigmadelta":
+        return list(oracle.sigmadelta(a["fr"], a["bkg"], a["var"]))
+    lin = np.asarray(oracle.linspace_nt2(0.0, 2.0, n), F32)
+    return [(oracle.map_f32("sinpi", lin) * a["x"]).astype(F32)]
+
+
+def _u32(t):
+    a = t.cpu().numpy()
+    return a.view(np.uint32) if a.dtype == np.float32 else a
+
+
+@pytest.mark.parametrize("prec", ["fast", "nt2"])
+@pytest.mark.parametrize("tune", [(256, 0, 8, 1), (128, 0, 16, 2), (256, -1, 4, 2)],
+                         ids=["dyn256x8", "dyn128x16_w2", "static256x4_w2"])
+@pytest.mark.parametrize("mode", ["run", "graph"])
+def test_batched_user_programs(lib, dev, oracle, prec, tune, mode):
+    """Five user programs beyond the library's three (sin*cos; a branch of exp
+    and log1p; rgb2yuv as a tie whose u, v read the stored y; one uint8
+    sigma-delta step updating its tables in place; sinpi of a generative
+    linspace times a table), 40 tables of ragged sizes (1 .. 2^20 elements,
+    every third one misaligned), interleaved with library-expression items,
+    in one batch: every program table bit-identical to nt2g_eval of the same
+    program with force_generic = 1; under the NT2 policy also bit-identical to
+    the oracle's restatement of NT2's evaluation."""
+    p = lib.PREC_NT2 if prec == "nt2" else lib.PREC_FAST
+    rng = np.random.default_rng(17)
+    sizes = [1, 3, 5, 4096, 70001, 300000, 1 << 20]
+    cases = []
+    for i in range(40):
+        kind, n = PROGRAM_KINDS[i % 5], sizes[i % 7]
+        arrays = _program_arrays(kind, n, rng)
+        mis = i % 3 == 2
+        cases.append((kind, n, arrays, _device(dev, arrays, mis), _device(dev, arrays, mis)))
+    lsizes, lexprs = batched_sizes(count=12, lo=1, hi=200000, seed=9)
+    ltabs = _make(lib, dev, lsizes, lexprs)
+    louts = _fresh_outs(lib, ltabs)
+    litems = _items(lib, ltabs, louts)
+    items = (lib.BatchItem * (len(cases) + len(ltabs)))()
+    keep, k, li = [], 0, 0
+    for i, (kind, n, arrays, tb, tr) in enumerate(cases):
+        outs, exprs = _program(kind, tb, n)
+        it, prog, args = E.batch_item(outs, exprs)
+        keep.append((prog, args))
+        items[k] = it
+        k += 1
+        if i % 4 == 3 and li < len(ltabs):  # a library item after every fourth program
+            items[k] = litems[li]
+            k, li = k + 1, li + 1
+    while li < len(ltabs):
+        items[k] = litems[li]
+        k, li = k + 1, li + 1
+    L = lib.load()
+    t = lib.BatchTune(tune[0], tune[1], tune[2], p, tune[3])
+    h = ctypes.c_void_p()
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    lib.check(L.nt2g_batch_create(items, len(items), ctypes.byref(t), ctypes.byref(h)))
+    try:
+        fn = L.nt2g_batch_run if mode == "run" else L.nt2g_batch_run_graph
+        lib.check(fn(h, ctypes.c_void_p(stream.cuda_stream)))
+        stream.synchronize()
+        el = ctypes.c_int64()
+        lib.check(L.nt2g_batch_stats(h, ctypes.byref(el), None))
+        assert el.value == sum(c[1] for c in cases) + int(np.sum(lsizes))
+    finally:
+        L.nt2g_batch_destroy(h)
+    # the programs' own evaluation on the twin tables
+    for kind, n, arrays, tb, tr in cases:
+        outs, exprs = _program(kind, tr, n)
+        E.assign(outs, exprs, precision=p, force_generic=1)
+    torch.cuda.synchronize()
+    for c, (kind, n, arrays, tb, tr) in enumerate(cases):
+        got, _ = _program(kind, tb, n)
+        ref, _ = _program(kind, tr, n)
+        for g, r in zip(got, ref):
+            assert np.array_equal(_u32(g), _u32(r)), (c, kind, n)
+        if p == lib.PREC_NT2:
+            for g, o in zip(got, _program_oracle(oracle, kind, arrays, n)):
+                assert np.array_equal(_u32(g), o.view(np.uint32) if o.dtype == np.float32 else o), (c, kind, n)
+    # the library items of the same batch
+    _check(louts, _reference_prec(lib, ltabs, p))
+
+
+def _reference_prec(lib, tabs, p):
+    ref = []
+    for ex, n, ins, s, y0 in tabs:
+        if ex == lib.BATCH_BLACKSCHOLES:
+            c, q = torch.empty_like(ins[0]), torch.empty_like(ins[0])
+            lib.blackscholes(ins[0], ins[1], ins[2], c, q, s[1], sigma_s=s[0], precision=p)
+            ref.append([c, q])
+        elif ex == lib.BATCH_SAXPY:
+            y = y0.clone()
+            lib.saxpy(s[0], ins[0], y)
+            ref.append([y])
+        else:
+            o = torch.empty_like(ins[0])
+            lib.expr3(ins[0], ins[1], ins[2], o, precision=p)
+            ref.append([o])
+    torch.cuda.synchronize()
+    return ref
+
+
+def test_batch_of_programs_per_table_and_autotune(lib, dev, tmp_path, monkeypatch):
+    """The per-table comparison path runs program items through their own
+    kernels in the caller's order, and the autotuner's search (including two
+    float4 vectors per thread) accepts a batch of programs."""
+    from nt2_gb300 import autotune
+    monkeypatch.setenv("NT2G_TUNE_CACHE", str(tmp_path / "tune.json"))
+    rng = np.random.default_rng(23)
+    cases = []
+    for i, n in enumerate([5000, 123457, 1 << 18, 77]):
+        kind = PROGRAM_KINDS[i % 5]
+        arrays = _program_arrays(kind, n, rng)
+        cases.append((kind, n, _device(dev, arrays, False), _device(dev, arrays, False)))
+    items = (lib.BatchItem * len(cases))()
+    keep = []
+    for k, (kind, n, tb, tr) in enumerate(cases):
+        it, prog, args = E.batch_item(*_program(kind, tb, n))
+        keep.append((prog, args))
+        items[k] = it
+    L = lib.load()
+    h = ctypes.c_void_p()
+    lib.check(L.nt2g_batch_create(items, len(items), None, ctypes.byref(h)))
+    try:
+        lib.check(L.nt2g_batch_run_per_table(h, lib._stream()))
+        torch.cuda.synchronize()
+    finally:
+        L.nt2g_batch_destroy(h)
+    for kind, n, tb, tr in cases:
+        E.assign(*_program(kind, tr, n), force_generic=1)
+    torch.cuda.synchronize()
+    for kind, n, tb, tr in cases:
+        for g, r in zip(_program(kind, tb, n)[0], _program(kind, tr, n)[0]):
+            assert np.array_equal(_u32(g), _u32(r)), (kind, n)
+    best, ms, cached = autotune.tuned(items, lib.PREC_FAST, reps=1)
+    assert not cached and ms > 0 and best.vector_width in (1, 2)
