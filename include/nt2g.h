@@ -244,6 +244,35 @@ nt2g_status nt2g_eval_fold(const nt2g_program *p, const nt2g_arg *args, int32_t 
                            int64_t hi, int32_t op, int32_t precision, void *workspace, size_t workspace_bytes,
                            float *out, int64_t *index, double *out64, void *stream);
 
+/* Reverse mode of a program: the vector-Jacobian product over elements
+ * [0, count).  All three arrays are indexed by slot (n_args entries):
+ *   cotangents[s]  device table of the cotangent of the value the program
+ *                  stores into float output slot s (NULL: zero);
+ *   table_grads[s] device table receiving, for a float table slot s the
+ *                  program reads, the gradient with respect to that input
+ *                  (NULL: not wanted; zeros when no output depends on it);
+ *   scalar_grads   device array of n_args doubles, or NULL: entry s receives
+ *                  the gradient with respect to float scalar slot s summed
+ *                  over the elements (the same bits on every run); the other
+ *                  entries are left alone.
+ * Forward values are recomputed, not stored, exactly as nt2g_eval with
+ * force_generic = 1 computes them under `precision`; the derivative
+ * arithmetic is the fast policy's, in FP32.  Gradient tables may be the
+ * program's input or cotangent tables (each element's inputs are read before
+ * its gradients are written).  workspace: nt2g_program_vjp_workspace_size
+ * bytes (8-byte aligned) when scalar_grads is given, else unused.  Needs the
+ * run-time compiler (NVRTC): NT2G_ERR_UNSUPPORTED without it.  Programs that
+ * fold (FOLD) are refused.  No counterpart in the reference (NT2 has no
+ * reverse mode); NT2G_OP_* rules are the derivatives of the functions as
+ * this library evaluates them (fastnormcdf: of NT2's approximation). */
+nt2g_status nt2g_program_vjp(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t count,
+                             const float *const *cotangents, float *const *table_grads, double *scalar_grads,
+                             int32_t precision, void *workspace, size_t workspace_bytes, void *stream);
+nt2g_status nt2g_program_vjp_workspace_size(const nt2g_program *p, int64_t count, size_t *bytes);
+/* The CUDA source of the program's reverse-mode kernel (no GPU needed; *len
+ * receives the size including the terminating NUL, cap = 0 only queries it). */
+nt2g_status nt2g_program_vjp_source(const nt2g_program *p, int32_t precision, char *buf, size_t cap, size_t *len);
+
 /* The CUDA source nt2g_eval_fold compiles for a program and fold op (no GPU
  * needed; *len receives the size including the terminating NUL, cap = 0 only
  * queries it).  No counterpart in the reference: it exposes the generated

@@ -874,6 +874,77 @@ extern "C" nt2g_status nt2g_eval_fold(const nt2g_program *p, const nt2g_arg *arg
                             index, out64, (cudaStream_t)stream);
 }
 
+extern "C" nt2g_status nt2g_program_vjp(const nt2g_program *p, const nt2g_arg *args, int32_t n_args, int64_t count,
+                                        const float *const *cotangents, float *const *table_grads,
+                                        double *scalar_grads, int32_t precision, void *workspace,
+                                        size_t workspace_bytes, void *stream)
+{
+    NT2G_CHECK_ARG(p != nullptr, "nt2g_program_vjp: NULL program");
+    NT2G_CHECK_ARG(!p->folds, "nt2g_program_vjp: the program folds its value");
+    NT2G_CHECK_ARG(n_args >= p->n_slots && (args != nullptr || p->n_slots == 0),
+                   "nt2g_program_vjp: %d arguments for %d slots", n_args, p->n_slots);
+    NT2G_CHECK_ARG(count >= 0, "nt2g_program_vjp: negative count %lld", (long long)count);
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_program_vjp: precision %d",
+                   precision);
+    DArgs da{};
+    nt2g_status bs = bind_args(p, args, 0, count, "nt2g_program_vjp", da);
+    if (bs != NT2G_OK) return bs;
+    const float *ct[kMaxSlots] = {};
+    float *gr[kMaxSlots] = {};
+    std::vector<int> float_scalars;
+    for (int s = 0; s < p->n_slots; ++s) {
+        const int use = p->slot_use[s];
+        const bool f32 = p->slot_dtype[s] == NT2G_F32;
+        if ((use & 4) && f32) float_scalars.push_back(s);
+        if (cotangents && cotangents[s]) {
+            NT2G_CHECK_ARG((use & 2) && f32, "nt2g_program_vjp: slot %d is not a float output, it takes no cotangent",
+                           s);
+            NT2G_CHECK_ARG(count == 0 || reachable(cotangents[s]),
+                           "nt2g_program_vjp: cotangent %d is host memory the device cannot access", s);
+            ct[s] = cotangents[s];
+        }
+        if (table_grads && table_grads[s]) {
+            NT2G_CHECK_ARG((use & 1) && !(use & 4) && f32,
+                           "nt2g_program_vjp: slot %d is not a float table the program reads", s);
+            NT2G_CHECK_ARG(count == 0 || reachable(table_grads[s]),
+                           "nt2g_program_vjp: gradient %d is host memory the device cannot access", s);
+            gr[s] = table_grads[s];
+        }
+    }
+    NT2G_CHECK_ARG(reachable(scalar_grads), "nt2g_program_vjp: scalar_grads is host memory the device cannot access");
+    return launch_vjp(p->ops, p->logical, da, ct, gr, scalar_grads, float_scalars, count, precision, workspace,
+                      workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_program_vjp_workspace_size(const nt2g_program *p, int64_t count, size_t *bytes)
+{
+    NT2G_CHECK_ARG(p != nullptr && bytes != nullptr, "nt2g_program_vjp_workspace_size: NULL argument");
+    NT2G_CHECK_ARG(count >= 0, "nt2g_program_vjp_workspace_size: negative count");
+    *bytes = vjp_workspace_bytes(p->ops, p->logical, count);
+    return NT2G_OK;
+}
+
+extern "C" nt2g_status nt2g_program_vjp_source(const nt2g_program *p, int32_t precision, char *buf, size_t cap,
+                                               size_t *len)
+{
+    NT2G_CHECK_ARG(p != nullptr, "nt2g_program_vjp_source: NULL program");
+    NT2G_CHECK_ARG(!p->folds, "nt2g_program_vjp_source: the program folds its value");
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_program_vjp_source: precision %d",
+                   precision);
+    NT2G_CHECK_ARG(buf != nullptr || cap == 0, "nt2g_program_vjp_source: NULL buffer");
+    std::string why;
+    std::string src = jit_vjp_source(p->ops, p->logical, precision, &why);
+    if (src.empty()) {
+        set_error("nt2g_program_vjp_source: %s", why.c_str());
+        return NT2G_ERR_UNSUPPORTED;
+    }
+    if (len) *len = src.size() + 1;
+    if (cap == 0) return NT2G_OK;
+    NT2G_CHECK_ARG(cap > src.size(), "nt2g_program_vjp_source: %zu-byte buffer, %zu needed", cap, src.size() + 1);
+    memcpy(buf, src.c_str(), src.size() + 1);
+    return NT2G_OK;
+}
+
 extern "C" nt2g_status nt2g_program_jit_source(const nt2g_program *p, int32_t precision, char *buf, size_t cap,
                                                size_t *len)
 {

@@ -128,6 +128,17 @@ struct BatchJitKernels {
 std::string jit_batch_source(const std::vector<ProgramCode> &progs, int precision, int block_threads);
 const BatchJitKernels *jit_batch_kernels(const std::vector<ProgramCode> &progs, int precision, int block_threads,
                                          std::string *why);
+// Reverse mode (nt2g_program_vjp): the run-time compiled kernel's source
+// (empty, with the reason in *why, when an opcode has no adjoint rule), the
+// float scalar slots whose gradients it sums, its workspace, its launch.
+std::string jit_vjp_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision,
+                           std::string *why);
+std::vector<int> vjp_scalar_slots(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical);
+size_t vjp_workspace_bytes(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int64_t count);
+nt2g_status launch_vjp(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, const DArgs &args,
+                       const float *const ct[kMaxSlots], float *const grad[kMaxSlots], double *scalar_grads,
+                       const std::vector<int> &float_scalars, int64_t count, int precision, void *ws, size_t ws_bytes,
+                       cudaStream_t st);
 bool jit_enabled();
 nt2g_status jit_prepare(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision);
 nt2g_status launch_jit(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, const DArgs &args,

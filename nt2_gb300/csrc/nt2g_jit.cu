@@ -20,6 +20,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <string>
@@ -29,6 +30,7 @@
 #include "nt2g_math_src.h"   // kNt2gMathSrc: nt2g_math.cuh as a string (generated at build)
 #include "nt2g_accum_src.h"  // kNt2gAccumSrc: nt2g_accum.cuh
 #include "nt2g_fold_src.h"   // kNt2gFoldSrc: nt2g_fold_kernels.cuh
+#include "nt2g_vjp_src.h"    // kNt2gVjpSrc: nt2g_vjp.cuh
 
 namespace nt2g {
 
@@ -156,7 +158,8 @@ static std::string fconst(float f)
 // The statements of a program over L lanes (4 consecutive elements per call
 // in a transform; 1 or 4 in a fold's element function).  STORE writes the
 // output tables; FOLD (fold programs) hands the folded value to out[].
-static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical)
+static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical,
+                      bool stores = true)
 {
     auto v = [](int x) { return "v" + std::to_string(x) + "[j]"; };
     // every table load first, so a tile's memory requests are in flight while its
@@ -210,9 +213,10 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         switch (o.code) {
         case NT2G_OP_LOAD: continue;  // emitted above
         case NT2G_OP_FOLD:  // a comparison result folds as 0.0f / 1.0f
-            s += "    NT2G_LL out[j] = (float)v" + std::to_string(o.a) + "[j];\n";
+            if (stores) s += "    NT2G_LL out[j] = (float)v" + std::to_string(o.a) + "[j];\n";
             continue;
         case NT2G_OP_STORE: {
+            if (!stores) continue;  // the reverse sweep recomputes values, it stores none
             const std::string src = "v" + std::to_string(o.a);
             const std::string dst = std::to_string(o.b);
             if (f32 && logical[o.a])  // a comparison result stored as 0.0f / 1.0f
@@ -487,6 +491,274 @@ std::string jit_batch_source(const std::vector<ProgramCode> &progs, int precisio
     return s;
 }
 
+// ------------------------------------------------------------ reverse mode --
+// The adjoint rule of one instruction: the statements that add its result's
+// adjoint G (g<k>) times the local partial derivatives into the adjoints of
+// its active operands.  Forward values are the v<k> registers; D is the fast
+// policy, used for the derivative arithmetic.  Empty when the instruction
+// passes no gradient (comparisons, rounding, sign, constants); false when the
+// opcode has no rule.
+static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k, const std::vector<uint8_t> &active)
+{
+    const nt2g_op &o = ops[k];
+    auto v = [](int x) { return "v" + std::to_string(x) + "[j]"; };
+    auto g = [](int x) { return "g" + std::to_string(x) + "[j]"; };
+    const std::string G = g(k), Y = v(k);
+    const std::string A = o.a >= 0 ? v(o.a) : "", B = o.b >= 0 ? v(o.b) : "", C = o.c >= 0 ? v(o.c) : "";
+    std::vector<std::pair<int, std::string>> add;  // (operand, partial derivative term to add: G * d)
+    auto to = [&](int operand, const std::string &term) {
+        if (operand >= 0 && active[operand]) add.emplace_back(operand, term);
+    };
+    const std::string pi = "nt2g::vjp::kPi", deg = "nt2g::vjp::kDegToRad";
+    switch (o.code) {
+    case NT2G_OP_ADD: to(o.a, G); to(o.b, G); break;
+    case NT2G_OP_SUB: to(o.a, G); to(o.b, "-" + G); break;
+    case NT2G_OP_MUL: to(o.a, G + " * " + B); to(o.b, G + " * " + A); break;
+    case NT2G_OP_DIV: to(o.a, G + " / " + B); to(o.b, "-" + G + " * " + Y + " / " + B); break;
+    case NT2G_OP_NEG: to(o.a, "-" + G); break;
+    case NT2G_OP_ABS: to(o.a, "(" + A + " > 0.0f ? " + G + " : " + A + " < 0.0f ? -" + G + " : 0.0f)"); break;
+    case NT2G_OP_SQR: to(o.a, "2.0f * " + A + " * " + G); break;
+    case NT2G_OP_SQRT: to(o.a, G + " * 0.5f / " + Y); break;
+    case NT2G_OP_REC: to(o.a, "-" + G + " * " + Y + " * " + Y); break;
+    case NT2G_OP_MIN: to(o.a, "(" + A + " < " + B + " ? " + G + " : 0.0f)"); to(o.b, "(" + A + " < " + B + " ? 0.0f : " + G + ")"); break;
+    case NT2G_OP_MAX: to(o.a, "(" + A + " > " + B + " ? " + G + " : 0.0f)"); to(o.b, "(" + A + " > " + B + " ? 0.0f : " + G + ")"); break;
+    case NT2G_OP_FMA: to(o.a, G + " * " + B); to(o.b, G + " * " + A); to(o.c, G); break;
+    case NT2G_OP_FNMS: to(o.a, "-" + G + " * " + B); to(o.b, "-" + G + " * " + A); to(o.c, G); break;
+    case NT2G_OP_EXP: to(o.a, G + " * " + Y); break;
+    case NT2G_OP_LOG: to(o.a, G + " / " + A); break;
+    case NT2G_OP_LOG1P: to(o.a, G + " / (1.0f + " + A + ")"); break;
+    case NT2G_OP_ERF: to(o.a, G + " * nt2g::vjp::kTwoOverSqrtPi * nt2g::exp<D>(-" + A + " * " + A + ")"); break;
+    case NT2G_OP_ERFC: to(o.a, "-" + G + " * nt2g::vjp::kTwoOverSqrtPi * nt2g::exp<D>(-" + A + " * " + A + ")"); break;
+    case NT2G_OP_NORMCDF:
+        to(o.a, G + " * nt2g::vjp::kInvSqrt2Pi * nt2g::exp<D>(-0.5f * " + A + " * " + A + ")");
+        break;
+    case NT2G_OP_FASTNORMCDF: to(o.a, G + " * nt2g::vjp::fastnormcdf_grad<D>(" + A + ")"); break;
+    case NT2G_OP_EXP2: to(o.a, G + " * " + Y + " * nt2g::vjp::kLn2"); break;
+    case NT2G_OP_EXP10: to(o.a, G + " * " + Y + " * nt2g::vjp::kLn10"); break;
+    case NT2G_OP_EXPM1: to(o.a, G + " * (" + Y + " + 1.0f)"); break;
+    case NT2G_OP_LOG2: to(o.a, G + " / (" + A + " * nt2g::vjp::kLn2)"); break;
+    case NT2G_OP_LOG10: to(o.a, G + " / (" + A + " * nt2g::vjp::kLn10)"); break;
+    case NT2G_OP_SIN: to(o.a, G + " * nt2g::cos<D>(" + A + ")"); break;
+    case NT2G_OP_COS: to(o.a, "-" + G + " * nt2g::sin<D>(" + A + ")"); break;
+    case NT2G_OP_TAN: to(o.a, G + " * (1.0f + " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_SINPI: to(o.a, G + " * " + pi + " * nt2g::cospi<D>(" + A + ")"); break;
+    case NT2G_OP_COSPI: to(o.a, "-" + G + " * " + pi + " * nt2g::sinpi<D>(" + A + ")"); break;
+    case NT2G_OP_TANPI: to(o.a, G + " * " + pi + " * (1.0f + " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_SIND: to(o.a, G + " * " + deg + " * nt2g::cosd<D>(" + A + ")"); break;
+    case NT2G_OP_COSD: to(o.a, "-" + G + " * " + deg + " * nt2g::sind<D>(" + A + ")"); break;
+    case NT2G_OP_TAND: to(o.a, G + " * " + deg + " * (1.0f + " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_COT: to(o.a, "-" + G + " * (1.0f + " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_COTPI: to(o.a, "-" + G + " * " + pi + " * (1.0f + " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_COTD: to(o.a, "-" + G + " * " + deg + " * (1.0f + " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_SEC: to(o.a, G + " * " + Y + " * nt2g::tan<D>(" + A + ")"); break;
+    case NT2G_OP_SECPI: to(o.a, G + " * " + pi + " * " + Y + " * nt2g::tanpi<D>(" + A + ")"); break;
+    case NT2G_OP_SECD: to(o.a, G + " * " + deg + " * " + Y + " * nt2g::tand<D>(" + A + ")"); break;
+    case NT2G_OP_CSC: to(o.a, "-" + G + " * " + Y + " * nt2g::cot<D>(" + A + ")"); break;
+    case NT2G_OP_CSCPI: to(o.a, "-" + G + " * " + pi + " * " + Y + " * nt2g::cotpi<D>(" + A + ")"); break;
+    case NT2G_OP_CSCD: to(o.a, "-" + G + " * " + deg + " * " + Y + " * nt2g::cotd<D>(" + A + ")"); break;
+    case NT2G_OP_SINC: to(o.a, G + " * nt2g::vjp::sinc_grad<D>(" + A + ", " + Y + ")"); break;
+    case NT2G_OP_SINCPI: to(o.a, G + " * nt2g::vjp::sincpi_grad<D>(" + A + ", " + Y + ")"); break;
+    case NT2G_OP_SINHC: to(o.a, G + " * nt2g::vjp::sinhc_grad<D>(" + A + ", " + Y + ")"); break;
+    case NT2G_OP_POW:  // b a^(b-1); a^b ln a (0 where a^b is 0, NaN for a < 0)
+        to(o.a, G + " * " + B + " * nt2g::pow<D>(" + A + ", " + B + " - 1.0f)");
+        to(o.b, "(" + A + " > 0.0f ? " + G + " * " + Y + " * nt2g::log<D>(" + A + ") : " + Y + " == 0.0f ? 0.0f : __int_as_float(0x7fc00000))");
+        break;
+    case NT2G_OP_SINH: to(o.a, G + " * nt2g::cosh<D>(" + A + ")"); break;
+    case NT2G_OP_COSH: to(o.a, G + " * nt2g::sinh<D>(" + A + ")"); break;
+    case NT2G_OP_TANH: to(o.a, G + " * (1.0f - " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_COTH: to(o.a, G + " * (1.0f - " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_ASIN: to(o.a, G + " / sqrtf(1.0f - " + A + " * " + A + ")"); break;
+    case NT2G_OP_ACOS: to(o.a, "-" + G + " / sqrtf(1.0f - " + A + " * " + A + ")"); break;
+    case NT2G_OP_ATAN: to(o.a, G + " / (1.0f + " + A + " * " + A + ")"); break;
+    case NT2G_OP_ATAN2: {  // atan2(a, b): (b, -a) / (a^2 + b^2)
+        const std::string r2 = "(" + A + " * " + A + " + " + B + " * " + B + ")";
+        to(o.a, G + " * " + B + " / " + r2);
+        to(o.b, "-" + G + " * " + A + " / " + r2);
+        break;
+    }
+    case NT2G_OP_HYPOT:
+        to(o.a, "(" + Y + " == 0.0f ? 0.0f : " + G + " * " + A + " / " + Y + ")");
+        to(o.b, "(" + Y + " == 0.0f ? 0.0f : " + G + " * " + B + " / " + Y + ")");
+        break;
+    case NT2G_OP_ASINH: to(o.a, G + " / sqrtf(" + A + " * " + A + " + 1.0f)"); break;
+    case NT2G_OP_ACOSH: to(o.a, G + " / (sqrtf(" + A + " - 1.0f) * sqrtf(" + A + " + 1.0f))"); break;
+    case NT2G_OP_ATANH: to(o.a, G + " / (1.0f - " + A + " * " + A + ")"); break;
+    case NT2G_OP_ACOTD: to(o.a, "-" + G + " * nt2g::vjp::kRadToDeg / (1.0f + " + A + " * " + A + ")"); break;
+    case NT2G_OP_ASEC:
+        to(o.a, G + " / (fabsf(" + A + ") * sqrtf(" + A + " * " + A + " - 1.0f))");
+        break;
+    case NT2G_OP_ACSC:
+        to(o.a, "-" + G + " / (fabsf(" + A + ") * sqrtf(" + A + " * " + A + " - 1.0f))");
+        break;
+    case NT2G_OP_ASECH: to(o.a, "-" + G + " / (" + A + " * sqrtf(1.0f - " + A + " * " + A + "))"); break;
+    case NT2G_OP_ACOTH: to(o.a, G + " / (1.0f - " + A + " * " + A + ")"); break;
+    case NT2G_OP_ACSCH: to(o.a, "-" + G + " / (fabsf(" + A + ") * sqrtf(1.0f + " + A + " * " + A + "))"); break;
+    case NT2G_OP_CBRT: to(o.a, G + " / (3.0f * " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_ERFCX: to(o.a, G + " * (2.0f * " + A + " * " + Y + " - nt2g::vjp::kTwoOverSqrtPi)"); break;
+    case NT2G_OP_EXPX2: to(o.a, G + " * 2.0f * " + A + " * " + Y); break;
+    case NT2G_OP_GAMMA: to(o.a, G + " * " + Y + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
+    case NT2G_OP_GAMMALN: to(o.a, G + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
+    case NT2G_OP_EXPRECNEG: to(o.a, G + " * " + Y + " / (" + A + " * " + A + ")"); break;
+    case NT2G_OP_EXPRECNEGC: to(o.a, G + " * (" + Y + " - 1.0f) / (" + A + " * " + A + ")"); break;
+    case NT2G_OP_SQRT1PM1: to(o.a, G + " * 0.5f / (" + Y + " + 1.0f)"); break;
+    case NT2G_OP_ERFINV: to(o.a, G + " * nt2g::vjp::kHalfSqrtPi * nt2g::exp<D>(" + Y + " * " + Y + ")"); break;
+    case NT2G_OP_ERFCINV: to(o.a, "-" + G + " * nt2g::vjp::kHalfSqrtPi * nt2g::exp<D>(" + Y + " * " + Y + ")"); break;
+    case NT2G_OP_FRAC: to(o.a, G); break;
+    case NT2G_OP_COPYSIGN:  // |a| with b's sign: sign(a) sign(b)
+        to(o.a, "((__float_as_uint(" + A + ") ^ __float_as_uint(" + B + ")) & 0x80000000u ? -" + G + " : " + G + ")");
+        break;
+    case NT2G_OP_IF_ELSE: to(o.b, "(" + A + " ? " + G + " : 0.0f)"); to(o.c, "(" + A + " ? 0.0f : " + G + ")"); break;
+    case NT2G_OP_SELINC: case NT2G_OP_SELDEC: to(o.b, G); break;
+    case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
+    case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: case NT2G_OP_IF_ZERO_ELSE_ONE:
+        break;  // piecewise constant: no gradient
+    default: return false;
+    }
+    for (const auto &t : add) s += "    NT2G_L g" + std::to_string(t.first) + "[j] += " + t.second + ";\n";
+    return true;
+}
+
+// Which values carry an adjoint: float (not logical) values that depend on a
+// float table or scalar argument and reach a stored value.
+static std::vector<uint8_t> active_values(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical)
+{
+    const size_t n = ops.size();
+    std::vector<uint8_t> dep(n, 0), live(n, 0), act(n, 0);
+    auto is_float = [&](size_t k) { return ops[k].dtype == NT2G_F32 && !logical[k]; };
+    for (size_t k = 0; k < n; ++k) {
+        const nt2g_op &o = ops[k];
+        if (o.code == NT2G_OP_STORE || o.code == NT2G_OP_FOLD) continue;
+        if (o.code == NT2G_OP_LOAD || o.code == NT2G_OP_SCALAR) { dep[k] = is_float(k); continue; }
+        if (o.code == NT2G_OP_CONST || o.code == NT2G_OP_INDEX) continue;
+        for (int x : {o.a, o.b, o.c})
+            if (x >= 0 && dep[x]) dep[k] = 1;
+        dep[k] &= is_float(k);
+    }
+    for (size_t k = n; k-- > 0;) {
+        const nt2g_op &o = ops[k];
+        if (o.code == NT2G_OP_STORE) { live[o.a] = 1; continue; }
+        if (!live[k]) continue;
+        for (int x : {o.a, o.b, o.c})
+            if (x >= 0 && o.code != NT2G_OP_LOAD && o.code != NT2G_OP_SCALAR && o.code != NT2G_OP_CONST &&
+                o.code != NT2G_OP_INDEX)
+                live[x] = 1;
+    }
+    for (size_t k = 0; k < n; ++k) act[k] = dep[k] && live[k];
+    return act;
+}
+
+// The float scalar slots a program's gradient sums over (in slot order).
+std::vector<int> vjp_scalar_slots(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical)
+{
+    const std::vector<uint8_t> act = active_values(ops, logical);
+    std::vector<int> slots;
+    for (size_t k = 0; k < ops.size(); ++k)
+        if (ops[k].code == NT2G_OP_SCALAR && act[k]) {
+            bool seen = false;
+            for (int s : slots) seen |= s == ops[k].a;
+            if (!seen) slots.push_back(ops[k].a);
+        }
+    std::sort(slots.begin(), slots.end());
+    return slots;
+}
+
+// The reverse-mode kernel of a program: each thread recomputes the forward
+// values of 4 consecutive elements (the statements of jit_source, so the
+// same bits as nt2g_eval), seeds the adjoints of the values stored into each
+// output slot with that slot's cotangent table, runs the adjoint rules in
+// reverse instruction order, and writes the adjoints of the loaded values to
+// the slots' gradient tables.  Adjoints of float scalars are summed per
+// thread in FP64, then per block (fixed order) into partials[block][scalar].
+std::string jit_vjp_source(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision,
+                           std::string *why)
+{
+    const std::vector<uint8_t> act = active_values(ops, logical);
+    const std::vector<int> sslots = vjp_scalar_slots(ops, logical);
+    const int ns = (int)sslots.size();
+    std::string s;
+    s.reserve(sizeof kJitPrelude + sizeof kNt2gVjpSrc + 40000 + ops.size() * 256);
+    s += kNt2gMathSrc;
+    s += kNt2gVjpSrc;
+    s += kJitPrelude;
+    s += "struct VjpArgs { const float *ct[16]; float *grad[16]; };\n";
+    s += "#define NT2G_NS " + std::to_string(ns > 0 ? ns : 1) + "\n";
+    s += "template <class P, bool FULL>\n__device__ __forceinline__ void vjp_tile(const JitArgs &a, const VjpArgs &g, "
+         "long long i, int cnt, double (&sacc)[NT2G_NS])\n{\n    typedef nt2g::Fast D;\n    constexpr int L = 4, A = 4;\n";
+    emit_body(s, ops, logical, false);
+    for (size_t k = 0; k < ops.size(); ++k)
+        if (act[k]) s += "    float g" + std::to_string(k) + "[4] = {0.0f, 0.0f, 0.0f, 0.0f};\n";
+    // seeds: the cotangent of each output slot flows into the last value stored there
+    std::vector<int> last_store(kMaxSlots, -1);
+    for (size_t k = 0; k < ops.size(); ++k)
+        if (ops[k].code == NT2G_OP_STORE) last_store[ops[k].b] = (int)k;
+    for (int slot = 0; slot < kMaxSlots; ++slot) {
+        const int st = last_store[slot];
+        if (st < 0 || !act[ops[st].a]) continue;
+        const std::string sl = std::to_string(slot), val = std::to_string(ops[st].a);
+        s += "    if (g.ct[" + sl + "]) { float t[4]; jit_ldf<FULL>(t, g.ct[" + sl + "], i, cnt); NT2G_L g" + val +
+             "[j] += t[j]; }\n";
+    }
+    for (size_t k = ops.size(); k-- > 0;) {
+        const nt2g_op &o = ops[k];
+        if (!act[k] || o.code == NT2G_OP_LOAD || o.code == NT2G_OP_SCALAR) continue;
+        if (!adjoint_rule(s, ops, (int)k, act)) {
+            if (why) *why = "opcode " + std::to_string(o.code) + " has no adjoint rule";
+            return "";
+        }
+    }
+    // gradients: each loaded float table slot (its loads summed), each scalar slot
+    std::vector<std::string> grad_of(kMaxSlots);
+    for (size_t k = 0; k < ops.size(); ++k) {
+        if (!act[k]) continue;
+        const std::string gk = "g" + std::to_string(k) + "[j]";
+        if (ops[k].code == NT2G_OP_LOAD) {
+            std::string &e = grad_of[ops[k].a];
+            e = e.empty() ? gk : e + " + " + gk;
+        }
+    }
+    std::vector<uint8_t> read_f32(kMaxSlots, 0);
+    for (size_t k = 0; k < ops.size(); ++k)
+        if (ops[k].code == NT2G_OP_LOAD && ops[k].dtype == NT2G_F32) read_f32[ops[k].a] = 1;
+    for (int slot = 0; slot < kMaxSlots; ++slot) {
+        if (!read_f32[slot]) continue;
+        const std::string sl = std::to_string(slot);
+        const std::string val = grad_of[slot].empty() ? "0.0f" : grad_of[slot];  // no output depends on it
+        s += "    if (g.grad[" + sl + "]) { float t[4]; NT2G_L t[j] = " + val + "; jit_stf<FULL>(g.grad[" + sl +
+             "], i, cnt, t); }\n";
+    }
+    for (int q = 0; q < ns; ++q)
+        for (size_t k = 0; k < ops.size(); ++k)
+            if (ops[k].code == NT2G_OP_SCALAR && act[k] && ops[k].a == sslots[q])
+                s += "    NT2G_L if (j < cnt) sacc[" + std::to_string(q) + "] += (double)g" + std::to_string(k) + "[j];\n";
+    s += "}\n\n";
+    s += "extern \"C\" __global__ void __launch_bounds__(256) nt2g_vjp_kernel(const JitArgs a, const VjpArgs g, "
+         "long long n, int vec, double *partials)\n{\n";
+    s += precision == NT2G_PREC_NT2 ? "    typedef nt2g::Nt2 P;\n" : "    typedef nt2g::Fast P;\n";
+    s += "    double sacc[NT2G_NS];\n"
+         "    for (int q = 0; q < NT2G_NS; ++q) sacc[q] = 0.0;\n"
+         "    const long long stride = (long long)gridDim.x * blockDim.x * 4;\n"
+         "    for (long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4; i < n; i += stride) {\n"
+         "        const int cnt = n - i < 4 ? (int)(n - i) : 4;\n"
+         "        if (vec && cnt == 4) vjp_tile<P, true>(a, g, i, 4, sacc);\n"
+         "        else vjp_tile<P, false>(a, g, i, cnt, sacc);\n"
+         "    }\n";
+    if (ns > 0)
+        s += "    __shared__ double red[8][NT2G_NS];\n"
+             "    for (int q = 0; q < NT2G_NS; ++q) {\n"
+             "        double x = sacc[q];\n"
+             "        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);\n"
+             "        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][q] = x;\n"
+             "    }\n"
+             "    __syncthreads();\n"
+             "    if (partials && threadIdx.x < NT2G_NS) {\n"
+             "        double x = 0.0;\n"
+             "        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += red[w][threadIdx.x];\n"
+             "        partials[(long long)blockIdx.x * NT2G_NS + threadIdx.x] = x;\n"
+             "    }\n";
+    s += "}\n";
+    return s;
+}
+
 // ------------------------------------------------------------------- cache --
 struct JitEntry {
     cudaLibrary_t lib = nullptr;
@@ -668,6 +940,149 @@ const BatchJitKernels *jit_batch_kernels(const std::vector<ProgramCode> &progs, 
         return nullptr;
     }
     return &it->second.k;
+}
+
+struct JitVjpEntry {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t kernel = nullptr;
+    int blocks_per_sm = 0;
+    std::string error;
+};
+static std::map<std::string, JitVjpEntry> g_vjp_cache;  // key: device | precision | program text
+
+static JitVjpEntry *jit_vjp_get(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int precision,
+                                std::string *why)
+{
+    if (!jit_enabled()) {
+        if (why) *why = "JIT disabled (NT2G_JIT=0)";
+        return nullptr;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::string key = std::to_string(dev) + "|" + std::to_string(precision) + "|";
+    key.append((const char *)ops.data(), ops.size() * sizeof(nt2g_op));
+    key.append((const char *)logical.data(), logical.size());
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_vjp_cache.find(key);
+    if (it == g_vjp_cache.end()) {
+        JitVjpEntry e;
+        std::string src = jit_vjp_source(ops, logical, precision, &e.error);
+        std::string cubin = src.empty() ? std::string() : compile_cubin(src, e.error);
+        if (!cubin.empty()) {
+            cudaError_t ce = cudaLibraryLoadData(&e.lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+            if (ce == cudaSuccess) ce = cudaLibraryGetKernel(&e.kernel, e.lib, "nt2g_vjp_kernel");
+            if (ce == cudaSuccess)
+                ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e.blocks_per_sm, (const void *)e.kernel, 256, 0);
+            if (ce != cudaSuccess) {
+                e.error = std::string("loading the reverse-mode kernel: ") + cudaGetErrorString(ce);
+                cudaGetLastError();
+                e.kernel = nullptr;
+            }
+        }
+        it = g_vjp_cache.emplace(key, e).first;
+    }
+    if (!it->second.kernel) {
+        if (why) *why = it->second.error;
+        return nullptr;
+    }
+    return &it->second;
+}
+
+// Blocks of the reverse-mode grid: 256 threads x 4 elements each, at most
+// 8 resident blocks (2048 threads) per SM.
+static int64_t vjp_grid_bound(int64_t count)
+{
+    const int64_t need = (count + 1023) / 1024;
+    const int64_t full = (int64_t)device_sm_count() * 8;
+    return need < full ? need : full;
+}
+
+size_t vjp_workspace_bytes(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, int64_t count)
+{
+    const size_t ns = vjp_scalar_slots(ops, logical).size();
+    return ns == 0 ? 0 : (size_t)vjp_grid_bound(count) * ns * sizeof(double);
+}
+
+struct VjpSlotMap {
+    int slot[kMaxSlots];  // accumulator q -> scalar slot
+    int zero[kMaxSlots];  // float scalar slots no output depends on
+    int nzero;
+};
+
+// One block per accumulator, summing the blocks' partials in a fixed order
+// (thread-strided, then warp shuffles, then warps in index order), so the
+// gradient of a scalar is the same bits on every run; one more block writes
+// the zero gradients.
+__global__ void __launch_bounds__(256) k_vjp_finish(const double *partials, int blocks, int ns, VjpSlotMap map,
+                                                    double *out)
+{
+    __shared__ double red[8];
+    const int q = blockIdx.x;
+    if (q == ns) {
+        if (threadIdx.x < map.nzero) out[map.zero[threadIdx.x]] = 0.0;
+        return;
+    }
+    double x = 0.0;
+    for (int b = threadIdx.x; b < blocks; b += blockDim.x) x += partials[(long long)b * ns + q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        out[map.slot[q]] = t;
+    }
+}
+
+nt2g_status launch_vjp(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, const DArgs &args,
+                       const float *const ct[kMaxSlots], float *const grad[kMaxSlots], double *scalar_grads,
+                       const std::vector<int> &float_scalars, int64_t count, int precision, void *ws, size_t ws_bytes,
+                       cudaStream_t st)
+{
+    std::string why;
+    JitVjpEntry *e = jit_vjp_get(ops, logical, precision, &why);
+    if (!e) {
+        set_error("reverse mode needs the run-time compiler: %s", why.c_str());
+        return NT2G_ERR_UNSUPPORTED;
+    }
+    const std::vector<int> sslots = vjp_scalar_slots(ops, logical);
+    const int ns = (int)sslots.size();
+    const int64_t bound = vjp_grid_bound(count);
+    int64_t full = (int64_t)device_sm_count() * (e->blocks_per_sm > 0 ? e->blocks_per_sm : 1);
+    const int grid = (int)(bound < full ? bound : full);
+    double *partials = nullptr;
+    if (scalar_grads && ns > 0) {
+        const size_t need = (size_t)grid * ns * sizeof(double);
+        if (!ws || ws_bytes < need || ((uintptr_t)ws & 7u)) {
+            set_error("nt2g_program_vjp: workspace of %zu bytes, %zu needed (8-byte aligned)", ws_bytes, need);
+            return NT2G_ERR_INVALID;
+        }
+        partials = (double *)ws;
+    }
+    struct { const float *ct[kMaxSlots]; float *grad[kMaxSlots]; } g;
+    int vec = 1;
+    for (int s = 0; s < kMaxSlots; ++s) {
+        g.ct[s] = ct[s];
+        g.grad[s] = grad[s];
+        if (args.ptr[s]) vec &= ((uintptr_t)args.ptr[s] & (args.dtype[s] == NT2G_F32 ? 15u : 3u)) == 0;
+        if (ct[s]) vec &= ((uintptr_t)ct[s] & 15u) == 0;
+        if (grad[s]) vec &= ((uintptr_t)grad[s] & 15u) == 0;
+    }
+    if (grid > 0) {
+        long long n = count;
+        void *params[] = {(void *)&args, (void *)&g, (void *)&n, (void *)&vec, (void *)&partials};
+        cudaError_t ce = cudaLaunchKernel((const void *)e->kernel, dim3(grid), dim3(256), params, 0, st);
+        if (ce != cudaSuccess) return cuda_status(ce, "reverse-mode kernel launch");
+    }
+    if (scalar_grads && !float_scalars.empty()) {
+        VjpSlotMap map{};
+        for (int q = 0; q < ns; ++q) map.slot[q] = sslots[q];
+        for (int s : float_scalars)
+            if (std::find(sslots.begin(), sslots.end(), s) == sslots.end()) map.zero[map.nzero++] = s;
+        k_vjp_finish<<<ns + 1, 256, 0, st>>>(partials, grid, ns, map, scalar_grads);
+        NT2G_LAUNCH_CHECK("reverse-mode finish");
+    }
+    return NT2G_OK;
 }
 
 bool jit_enabled()

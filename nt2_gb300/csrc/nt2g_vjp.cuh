@@ -1,0 +1,108 @@
+// nt2g_vjp.cuh -- derivatives the reverse sweep of a program needs beyond
+// what the forward values give directly (nt2g_jit.cu emits the per-opcode
+// adjoint rules; this header is embedded into the run-time compiled source
+// after nt2g_math.cuh).
+//
+// NT2 has no reverse mode: these are the derivatives of the functions as the
+// library computes them, written from their mathematical definitions.
+#pragma once
+
+namespace nt2g {
+namespace vjp {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kLn2 = 0.693147180559945309417f;
+constexpr float kLn10 = 2.30258509299404568402f;
+constexpr float kTwoOverSqrtPi = 1.12837916709551257390f;
+constexpr float kHalfSqrtPi = 0.886226925452758013649f;
+constexpr float kInvSqrt2Pi = 0.398942280401432677940f;
+constexpr float kDegToRad = 0.0174532925199432957692f;
+constexpr float kRadToDeg = 57.2957795130823208768f;
+
+// d/dx of NT2's Abramowitz-Stegun 26.2.17 fastnormcdf (the approximation
+// itself, not the normal density it approximates).  With l = |x|,
+// k = 1/(1 + p l), w(l) = c k q(k) e^(-l^2/2) (q the quintic of the
+// approximation, c = 1/sqrt(2 pi)): fastnormcdf = 1 - w for x > 0, w
+// otherwise, so its derivative is -w'(l) in both halves:
+//   -w'(l) = c e^(-l^2/2) k [l q(k) + p k (q(k) + k q'(k))].
+template <class D> NT2G_HD float fastnormcdf_grad(float x)
+{
+    const float p = 0.2316419f;
+    const float l = fminf(fabsf(x), 100.0f);
+    const float k = 1.0f / (1.0f + p * l);
+    // the approximation's coefficients b1..b5 (A&S 26.2.17, as NT2 stores them)
+    const float b1 = bits_f(0x3ea385fau), b2 = bits_f(0xbeb68f87u), b3 = bits_f(0x3fe40778u),
+                b4 = bits_f(0xbfe91eeau), b5 = bits_f(0x3faa466fu);
+    const float q = b1 + k * (b2 + k * (b3 + k * (b4 + k * b5)));
+    const float dq = b2 + k * (2.0f * b3 + k * (3.0f * b4 + k * 4.0f * b5));
+    const float e = kInvSqrt2Pi * exp<D>(-0.5f * l * l);
+    const float r = e * k * (l * q + p * k * (q + k * dq));
+    return is_nan(x) ? x : r;
+}
+
+// The digamma function psi = Gamma'/Gamma, for the derivatives of gamma
+// (Gamma psi) and gammaln (psi).  Reflection psi(x) = psi(1 - x) - pi cot(pi x)
+// below 1/2, the recurrence psi(x) = psi(x + 1) - 1/x up to x >= 6, then the
+// asymptotic series ln x - 1/(2x) - sum B_2k / (2k x^2k) (Bernoulli numbers
+// 1/6, -1/30, 1/42, -1/30: terms 1/12, -1/120, 1/252, -1/240).  NaN at the
+// poles (zero and the negative integers).
+template <class D> NT2G_HD float digamma(float x)
+{
+    if (is_nan(x) || (x <= 0.0f && x == floorf(x))) return f_nan();
+    if (x == f_inf()) return x;
+    float acc = 0.0f;
+    if (x < 0.5f) {
+        acc = -kPi * cotpi<D>(x);
+        x = 1.0f - x;
+    }
+    while (x < 6.0f) {
+        acc -= 1.0f / x;
+        x += 1.0f;
+    }
+    const float r = 1.0f / x, r2 = r * r;
+    const float series = r2 * (1.0f / 12.0f - r2 * (1.0f / 120.0f - r2 * (1.0f / 252.0f - r2 * (1.0f / 240.0f))));
+    return acc + log<D>(x) - 0.5f * r - series;
+}
+
+// d/dx sin(x)/x = (cos x - sinc x)/x, which cancels as x -> 0: below 1/2 in
+// magnitude the derivative of the Taylor series 1 - x^2/6 + x^4/120 -
+// x^6/5040 + x^8/362880 instead, -x/3 + x^3/30 - x^5/840 + x^7/45360.
+// sinc is constant (1) below Eps and 0 at infinity: no gradient there.
+template <class D> NT2G_HD float sinc_grad(float x, float y)
+{
+    const float ax = fabsf(x);
+    if (ax < bits_f(0x34000000u) || ax == f_inf()) return 0.0f;
+    if (ax < 0.5f) {
+        const float x2 = x * x;
+        return x * (-1.0f / 3.0f + x2 * (1.0f / 30.0f + x2 * (-1.0f / 840.0f + x2 * (1.0f / 45360.0f))));
+    }
+    return (cos<D>(x) - y) / x;
+}
+
+// sincpi(x) = sinc(pi x): pi sinc'(pi x), the quotient (cospi x - sincpi x)/x
+// from |pi x| = 1/2 on.
+template <class D> NT2G_HD float sincpi_grad(float x, float y)
+{
+    const float ax = fabsf(x);
+    if (ax < bits_f(0x34000000u) || ax == f_inf()) return 0.0f;
+    const float u = kPi * x;
+    if (fabsf(u) < 0.5f) {
+        const float u2 = u * u;
+        return kPi * u * (-1.0f / 3.0f + u2 * (1.0f / 30.0f + u2 * (-1.0f / 840.0f + u2 * (1.0f / 45360.0f))));
+    }
+    return (cospi<D>(x) - y) / x;
+}
+
+// d/dx sinh(x)/x = (cosh x - sinhc x)/x; below 1/2 the series
+// x/3 + x^3/30 + x^5/840 + x^7/45360.
+template <class D> NT2G_HD float sinhc_grad(float x, float y)
+{
+    if (fabsf(x) < 0.5f) {
+        const float x2 = x * x;
+        return x * (1.0f / 3.0f + x2 * (1.0f / 30.0f + x2 * (1.0f / 840.0f + x2 * (1.0f / 45360.0f))));
+    }
+    return (cosh<D>(x) - y) / x;
+}
+
+}  // namespace vjp
+}  // namespace nt2g

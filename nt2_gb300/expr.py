@@ -458,6 +458,14 @@ class Program:
         lib.check(L.nt2g_program_fold_source(self.handle, precision, lib.FOLD[op], buf, n.value, ctypes.byref(n)))
         return buf.value.decode()
 
+    def vjp_source(self, precision=lib.PREC_FAST):
+        """CUDA source of this program's reverse-mode kernel."""
+        L, n = lib.load(), ctypes.c_size_t()
+        lib.check(L.nt2g_program_vjp_source(self.handle, precision, None, 0, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        lib.check(L.nt2g_program_vjp_source(self.handle, precision, buf, n.value, ctypes.byref(n)))
+        return buf.value.decode()
+
     def jit_prepare(self, precision=lib.PREC_FAST):
         """Compile and load the run-time compiled kernel now; raises Nt2gError when it is unavailable."""
         lib.check(lib.load().nt2g_program_jit_prepare(self.handle, precision))
@@ -518,6 +526,56 @@ def _args_of(slots):
             n = s.numel() if n is None else min(n, s.numel())
             args[i] = lib.Arg(s.data_ptr(), 0.0, lib.U8 if s.dtype == torch.uint8 else lib.F32, 0)
     return args, n
+
+
+def _slot_of(slots, x):
+    import torch
+    for i, s in enumerate(slots):
+        if isinstance(x, torch.Tensor):
+            if not isinstance(s, Node) and s.data_ptr() == x.data_ptr() and s.dtype == x.dtype:
+                return i
+        elif s is x:
+            return i
+    raise ValueError("not an argument of the program")
+
+
+def vjp(outs, exprs, cotangents, inputs, precision=lib.PREC_FAST, stream=None):
+    """Reverse mode of tie(outs...) = tie(exprs...) (nt2g_program_vjp):
+    cotangents holds one float table per output (None: zero); returns the
+    gradient with respect to each of `inputs` -- a float table (a fresh
+    table of its shape) or a Scalar leaf (a 0-d float64 tensor: the gradient
+    summed over the elements).  Forward values are recomputed on the fly;
+    the output tables are not written."""
+    import torch
+    outs, exprs = list(outs), list(exprs)
+    prog, slots = compile_program(outs, exprs)
+    args, n = _args_of(slots)
+    ns = len(slots)
+    ct, tg = (ctypes.c_void_p * ns)(), (ctypes.c_void_p * ns)()
+    for o, c in zip(outs, cotangents):
+        if c is not None:
+            ct[_slot_of(slots, o)] = c.data_ptr()
+    dev = next(s.device for s in slots if not isinstance(s, Node))
+    res, scalars = [], []
+    for x in inputs:
+        k = _slot_of(slots, x)
+        if isinstance(x, torch.Tensor):
+            g = torch.empty_like(x)
+            tg[k] = g.data_ptr()
+            res.append(g)
+        else:
+            scalars.append((len(res), k))
+            res.append(None)
+    sg = torch.zeros(max(ns, 1), dtype=torch.float64, device=dev) if scalars else None
+    nb = ctypes.c_size_t()
+    L = lib.load()
+    lib.check(L.nt2g_program_vjp_workspace_size(prog.handle, n, ctypes.byref(nb)))
+    ws = torch.empty(max(nb.value, 16), dtype=torch.uint8, device=dev)
+    lib.check(L.nt2g_program_vjp(prog.handle, args, ns, n, ct, tg, lib._ptr(sg), precision, lib._ptr(ws), ws.numel(),
+                                 lib._stream(stream)))
+    for i, k in scalars:
+        res[i] = sg[k]
+    return res
 
 
 def batch_item(outs, exprs):

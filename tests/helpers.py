@@ -147,3 +147,137 @@ def batched_sizes(count=4096, lo=1024, hi=4194304, seed=1003):
     sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), count)).astype(np.int64)
     exprs = rng.integers(0, 3, count)
     return sizes, exprs
+
+
+# ------------------------------------------------------------ reverse mode --
+# FP64 forward-mode dual numbers: the reference the program-level VJP is
+# checked against (a method independent of the kernel's reverse sweep).  A
+# Dual carries its value, the tangents along each input direction, and the
+# absolute tangents -- the sum over the expression's paths of |product of the
+# local partials| -- which are the gradient's term scale: the size of the terms
+# its chain-rule sum adds, the gradient's own magnitude except where they
+# cancel.
+class Dual:
+    __slots__ = ("v", "t", "a")
+
+    def __init__(self, v, t, a):
+        self.v, self.t, self.a = v, t, a
+
+    @staticmethod
+    def var(x, i, k):
+        x = np.asarray(x, np.float64)
+        t = np.zeros((k,) + x.shape)
+        t[i] = 1.0
+        return Dual(x, t, t.copy())
+
+    @staticmethod
+    def lift(c, like):
+        if isinstance(c, Dual):
+            return c
+        return Dual(np.broadcast_to(np.float64(c), like.v.shape), np.zeros_like(like.t), np.zeros_like(like.a))
+
+    def _un(self, v, d):
+        return Dual(v, d * self.t, np.abs(d) * self.a)
+
+    def __add__(self, o):
+        o = Dual.lift(o, self)
+        return Dual(self.v + o.v, self.t + o.t, self.a + o.a)
+
+    __radd__ = __add__
+
+    def __sub__(self, o):
+        o = Dual.lift(o, self)
+        return Dual(self.v - o.v, self.t - o.t, self.a + o.a)
+
+    def __rsub__(self, o):
+        return Dual.lift(o, self) - self
+
+    def __neg__(self):
+        return Dual(-self.v, -self.t, self.a)
+
+    def __mul__(self, o):
+        o = Dual.lift(o, self)
+        return Dual(self.v * o.v, self.t * o.v + self.v * o.t, self.a * np.abs(o.v) + np.abs(self.v) * o.a)
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, o):
+        o = Dual.lift(o, self)
+        q = self.v / o.v
+        return Dual(q, (self.t - q * o.t) / o.v, self.a / np.abs(o.v) + np.abs(q / o.v) * o.a)
+
+    def __rtruediv__(self, o):
+        return Dual.lift(o, self) / self
+
+
+def d_sqrt(x):
+    r = np.sqrt(x.v)
+    return x._un(r, 0.5 / r)
+
+
+def d_log(x):
+    return x._un(np.log(x.v), 1.0 / x.v)
+
+
+def d_log1p(x):
+    return x._un(np.log1p(x.v), 1.0 / (1.0 + x.v))
+
+
+def d_exp(x):
+    e = np.exp(x.v)
+    return x._un(e, e)
+
+
+def d_abs(x):
+    return x._un(np.abs(x.v), np.sign(x.v))
+
+
+def d_sqr(x):
+    return x * x
+
+
+def d_fma(a, b, c):
+    return a * b + c
+
+
+def d_fnms(a, b, c):
+    return c - a * b
+
+
+def d_normcdf(x):
+    from scipy.special import ndtr
+    return x._un(ndtr(x.v), np.exp(-0.5 * x.v * x.v) / np.sqrt(2 * np.pi))
+
+
+# NT2's fastnormcdf (Abramowitz-Stegun 26.2.17 with NT2's float coefficients)
+# and its exact derivative, in FP64.
+_AS_P = float(np.float32(0.2316419))
+_AS_B = [float(np.uint32(u).view(np.float32)) for u in (0x3ea385fa, 0xbeb68f87, 0x3fe40778, 0xbfe91eea, 0x3faa466f)]
+
+
+def fastnormcdf64(x):
+    x = np.asarray(x, np.float64)
+    b1, b2, b3, b4, b5 = _AS_B
+    l = np.abs(x)
+    k = 1.0 / (1.0 + _AS_P * l)
+    q = b1 + k * (b2 + k * (b3 + k * (b4 + k * b5)))
+    dq = b2 + k * (2 * b3 + k * (3 * b4 + k * 4 * b5))
+    e = np.exp(-0.5 * l * l) / np.sqrt(2 * np.pi)
+    w = e * k * q
+    f = np.where(x > 0, 1.0 - w, w)
+    df = e * k * (l * q + _AS_P * k * (q + k * dq))
+    return f, df
+
+
+def d_fastnormcdf(x):
+    f, df = fastnormcdf64(x.v)
+    return x._un(f, df)
+
+
+def bs_demo_dual(S, X, T, r, v):
+    """The NT2 demo's Black-Scholes expression (demo/blackscholes/nt2/
+    blackandscholes_nt2.cpp:55-59), operation for operation, on Duals."""
+    da = d_sqrt(T)
+    d1 = d_log(S / X) + (d_fma(d_sqr(v), 0.5, r) * T) / (v * da)
+    d2 = d_fnms(v, da, d1)
+    return d_fnms(X * d_exp(-r * T), d_fastnormcdf(d2), S * d_fastnormcdf(d1))

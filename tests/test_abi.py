@@ -337,3 +337,70 @@ def test_batch_kernel_source_builds_for_sm103a(lib):
     L = lib.load()
     assert L.nt2g_batch_source(hs, 1, 0, 100, None, 0, ctypes.byref(n)) == lib.ERR_INVALID  # block size
     assert L.nt2g_batch_source(hs, 0, 0, 256, None, 0, ctypes.byref(n)) == lib.ERR_INVALID
+
+
+UNARY_VJP_OPS = ["exp", "log", "log1p", "erfc", "normcdf", "fastnormcdf", "sqrt", "rec", "abs_", "exp2", "exp10",
+                 "expm1", "log2", "log10", "sin", "cos", "tan", "sinpi", "cospi", "sinh", "cosh", "tanh", "asin",
+                 "acos", "atan", "asinh", "acosh", "atanh", "cbrt", "cot", "sec", "csc", "sind", "cosd", "tand",
+                 "tanpi", "cotpi", "cotd", "secpi", "cscpi", "secd", "cscd", "sinc", "sincpi", "acotd", "asec", "coth",
+                 "sinhc", "acsc", "asech", "acoth", "acsch", "erf", "erfcx", "expx2", "gamma", "gammaln", "erfinv",
+                 "erfcinv", "exprecneg", "exprecnegc", "sqrt1pm1", "floor", "ceil", "trunc", "round", "round2even",
+                 "frac", "sign", "signnz", "sqr"]
+
+
+def _vjp_programs(lib):
+    """Programs that together use every opcode with an adjoint rule."""
+    n = 8
+    progs = []
+    S, K, T = _cpu_tables()
+    c, p = torch.zeros(n), torch.zeros(n)
+    progs.append(E.compile_program([c, p], list(bs_textbook(S, K, T, E.Scalar(0.3), E.Scalar(0.02))))[0])
+    x, y, z = (E.Table(torch.zeros(n)) for _ in range(3))
+    for k in range(0, len(UNARY_VJP_OPS), 24):
+        acc = None
+        for name in UNARY_VJP_OPS[k:k + 24]:
+            t = getattr(E, name)(x)
+            acc = t if acc is None else acc + t
+        progs.append(E.compile_program([torch.zeros(n)], [acc])[0])
+    e = (E.pow(x, y) + E.atan2(x, y) + E.hypot(x, y) + x / y + E.min_(x, y) + E.max_(x, y) + E.copysign(x, y)
+         + E.fma(x, y, z) + E.fnms(x, y, z) + E.if_else(x > y, y, z) + E.selinc(x < z, y) + E.seldec(x > z, z)
+         + E.if_zero_else_one(x < y, lib.F32) - (-x))
+    progs.append(E.compile_program([torch.zeros(n)], [e])[0])
+    return progs
+
+
+def test_vjp_kernel_source_builds_for_sm103a(lib):
+    """The reverse-mode kernels of programs covering every opcode's adjoint
+    rule compile for sm_103a (NVRTC needs no GPU); fold programs are refused."""
+    nv = _nvrtc()
+    for i, prog in enumerate(_vjp_programs(lib)):
+        for prec in ((lib.PREC_FAST, lib.PREC_NT2) if i == 0 else (lib.PREC_FAST,)):
+            src = prog.vjp_source(prec)
+            assert "nt2g_vjp_kernel" in src and "vjp_tile" in src
+            rc, log, size = _nvrtc_compile(nv, src)
+            assert rc == 0, log[:2000]
+            assert size > 0
+    x = E.Table(torch.zeros(8))
+    fold_prog, _ = E.compile_program([], [], fold=E.exp(x))
+    n = ctypes.c_size_t()
+    assert lib.load().nt2g_program_vjp_source(fold_prog.handle, 0, None, 0, ctypes.byref(n)) == lib.ERR_INVALID
+
+
+def test_vjp_validates_slots(lib):
+    """Cotangents only on float outputs, gradients only of float tables the
+    program reads; refused before anything reaches the device."""
+    L = lib.load()
+    X, Y = torch.zeros(8), torch.zeros(8)
+    prog, slots = E.compile_program([Y], [E.exp(E.Table(X)) * E.Scalar(2.0)])
+    args = (lib.Arg * len(slots))()
+    for i, s in enumerate(slots):
+        args[i] = lib.Arg(None, 2.0, lib.F32, 1) if isinstance(s, E.Node) else lib.Arg(8 * (i + 1), 0.0, lib.F32, 0)
+    sx, sy = E._slot_of(slots, X), E._slot_of(slots, Y)
+    ct, tg = (ctypes.c_void_p * len(slots))(), (ctypes.c_void_p * len(slots))()
+    ct[sx] = 64  # a cotangent on an input slot
+    assert L.nt2g_program_vjp(prog.handle, args, len(slots), 0, ct, tg, None, 0, None, 0, None) == lib.ERR_INVALID
+    ct[sx], tg[sy] = None, 64  # a gradient of an output-only slot
+    assert L.nt2g_program_vjp(prog.handle, args, len(slots), 0, ct, tg, None, 0, None, 0, None) == lib.ERR_INVALID
+    tg[sy] = None
+    assert L.nt2g_program_vjp(prog.handle, args, len(slots), -1, ct, tg, None, 0, None, 0, None) == lib.ERR_INVALID
+    assert L.nt2g_program_vjp(prog.handle, args, len(slots), 0, ct, tg, None, 7, None, 0, None) == lib.ERR_INVALID
