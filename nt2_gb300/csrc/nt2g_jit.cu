@@ -535,7 +535,7 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
     case NT2G_OP_FASTNORMCDF: to(o.a, G + " * nt2g::vjp::fastnormcdf_grad<D>(" + A + ")"); break;
     case NT2G_OP_EXP2: to(o.a, G + " * " + Y + " * nt2g::vjp::kLn2"); break;
     case NT2G_OP_EXP10: to(o.a, G + " * " + Y + " * nt2g::vjp::kLn10"); break;
-    case NT2G_OP_EXPM1: to(o.a, G + " * (" + Y + " + 1.0f)"); break;
+    case NT2G_OP_EXPM1: to(o.a, G + " * nt2g::exp<D>(" + A + ")"); break;  // not y + 1: it cancels as y -> -1
     case NT2G_OP_LOG2: to(o.a, G + " / (" + A + " * nt2g::vjp::kLn2)"); break;
     case NT2G_OP_LOG10: to(o.a, G + " / (" + A + " * nt2g::vjp::kLn10)"); break;
     case NT2G_OP_SIN: to(o.a, G + " * nt2g::cos<D>(" + A + ")"); break;
@@ -565,10 +565,13 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
         break;
     case NT2G_OP_SINH: to(o.a, G + " * nt2g::cosh<D>(" + A + ")"); break;
     case NT2G_OP_COSH: to(o.a, G + " * nt2g::sinh<D>(" + A + ")"); break;
-    case NT2G_OP_TANH: to(o.a, G + " * (1.0f - " + Y + " * " + Y + ")"); break;
-    case NT2G_OP_COTH: to(o.a, G + " * (1.0f - " + Y + " * " + Y + ")"); break;
-    case NT2G_OP_ASIN: to(o.a, G + " / sqrtf(1.0f - " + A + " * " + A + ")"); break;
-    case NT2G_OP_ACOS: to(o.a, "-" + G + " / sqrtf(1.0f - " + A + " * " + A + ")"); break;
+    // 1 - tanh^2 = 1/cosh^2 and 1 - coth^2 = -1/sinh^2: the forms in y would
+    // magnify y's rounding where |y| nears 1
+    case NT2G_OP_TANH: to(o.a, G + " / (nt2g::cosh<D>(" + A + ") * nt2g::cosh<D>(" + A + "))"); break;
+    case NT2G_OP_COTH: to(o.a, "-" + G + " / (nt2g::sinh<D>(" + A + ") * nt2g::sinh<D>(" + A + "))"); break;
+    // 1 - a^2 as (1 - a)(1 + a), a^2 - 1 as (a - 1)(a + 1): exact differences near |a| = 1
+    case NT2G_OP_ASIN: to(o.a, G + " / sqrtf((1.0f - " + A + ") * (1.0f + " + A + "))"); break;
+    case NT2G_OP_ACOS: to(o.a, "-" + G + " / sqrtf((1.0f - " + A + ") * (1.0f + " + A + "))"); break;
     case NT2G_OP_ATAN: to(o.a, G + " / (1.0f + " + A + " * " + A + ")"); break;
     case NT2G_OP_ATAN2: {  // atan2(a, b): (b, -a) / (a^2 + b^2)
         const std::string r2 = "(" + A + " * " + A + " + " + B + " * " + B + ")";
@@ -582,16 +585,16 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
         break;
     case NT2G_OP_ASINH: to(o.a, G + " / sqrtf(" + A + " * " + A + " + 1.0f)"); break;
     case NT2G_OP_ACOSH: to(o.a, G + " / (sqrtf(" + A + " - 1.0f) * sqrtf(" + A + " + 1.0f))"); break;
-    case NT2G_OP_ATANH: to(o.a, G + " / (1.0f - " + A + " * " + A + ")"); break;
+    case NT2G_OP_ATANH: to(o.a, G + " / ((1.0f - " + A + ") * (1.0f + " + A + "))"); break;
     case NT2G_OP_ACOTD: to(o.a, "-" + G + " * nt2g::vjp::kRadToDeg / (1.0f + " + A + " * " + A + ")"); break;
     case NT2G_OP_ASEC:
-        to(o.a, G + " / (fabsf(" + A + ") * sqrtf(" + A + " * " + A + " - 1.0f))");
+        to(o.a, G + " / (fabsf(" + A + ") * sqrtf((fabsf(" + A + ") - 1.0f) * (fabsf(" + A + ") + 1.0f)))");
         break;
     case NT2G_OP_ACSC:
-        to(o.a, "-" + G + " / (fabsf(" + A + ") * sqrtf(" + A + " * " + A + " - 1.0f))");
+        to(o.a, "-" + G + " / (fabsf(" + A + ") * sqrtf((fabsf(" + A + ") - 1.0f) * (fabsf(" + A + ") + 1.0f)))");
         break;
-    case NT2G_OP_ASECH: to(o.a, "-" + G + " / (" + A + " * sqrtf(1.0f - " + A + " * " + A + "))"); break;
-    case NT2G_OP_ACOTH: to(o.a, G + " / (1.0f - " + A + " * " + A + ")"); break;
+    case NT2G_OP_ASECH: to(o.a, "-" + G + " / (" + A + " * sqrtf((1.0f - " + A + ") * (1.0f + " + A + ")))"); break;
+    case NT2G_OP_ACOTH: to(o.a, G + " / ((1.0f - " + A + ") * (1.0f + " + A + "))"); break;
     case NT2G_OP_ACSCH: to(o.a, "-" + G + " / (fabsf(" + A + ") * sqrtf(1.0f + " + A + " * " + A + "))"); break;
     case NT2G_OP_CBRT: to(o.a, G + " / (3.0f * " + Y + " * " + Y + ")"); break;
     case NT2G_OP_ERFCX: to(o.a, G + " * (2.0f * " + A + " * " + Y + " - nt2g::vjp::kTwoOverSqrtPi)"); break;
@@ -599,8 +602,9 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
     case NT2G_OP_GAMMA: to(o.a, G + " * " + Y + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
     case NT2G_OP_GAMMALN: to(o.a, G + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
     case NT2G_OP_EXPRECNEG: to(o.a, G + " * " + Y + " / (" + A + " * " + A + ")"); break;
-    case NT2G_OP_EXPRECNEGC: to(o.a, G + " * (" + Y + " - 1.0f) / (" + A + " * " + A + ")"); break;
-    case NT2G_OP_SQRT1PM1: to(o.a, G + " * 0.5f / (" + Y + " + 1.0f)"); break;
+    // -e^(-1/x)/x^2 and 1/(2 sqrt(1 + x)) directly: y - 1 and y + 1 would cancel
+    case NT2G_OP_EXPRECNEGC: to(o.a, "-" + G + " * nt2g::exprecneg<D>(" + A + ") / (" + A + " * " + A + ")"); break;
+    case NT2G_OP_SQRT1PM1: to(o.a, G + " * 0.5f / sqrtf(1.0f + " + A + ")"); break;
     case NT2G_OP_ERFINV: to(o.a, G + " * nt2g::vjp::kHalfSqrtPi * nt2g::exp<D>(" + Y + " * " + Y + ")"); break;
     case NT2G_OP_ERFCINV: to(o.a, "-" + G + " * nt2g::vjp::kHalfSqrtPi * nt2g::exp<D>(" + Y + " * " + Y + ")"); break;
     case NT2G_OP_FRAC: to(o.a, G); break;

@@ -544,7 +544,7 @@ def vjp(outs, exprs, cotangents, inputs, precision=lib.PREC_FAST, stream=None):
     cotangents holds one float table per output (None: zero); returns the
     gradient with respect to each of `inputs` -- a float table (a fresh
     table of its shape) or a Scalar leaf (a 0-d float64 tensor: the gradient
-    summed over the elements).  Forward values are recomputed on the fly;
+    summed over the elements); zeros for an input the program does not read.  Forward values are recomputed on the fly;
     the output tables are not written."""
     import torch
     outs, exprs = list(outs), list(exprs)
@@ -558,7 +558,12 @@ def vjp(outs, exprs, cotangents, inputs, precision=lib.PREC_FAST, stream=None):
     dev = next(s.device for s in slots if not isinstance(s, Node))
     res, scalars = [], []
     for x in inputs:
-        k = _slot_of(slots, x)
+        try:
+            k = _slot_of(slots, x)
+        except ValueError:  # the program does not read it: a zero gradient
+            res.append(torch.zeros_like(x) if isinstance(x, torch.Tensor)
+                       else torch.zeros((), dtype=torch.float64, device=dev))
+            continue
         if isinstance(x, torch.Tensor):
             g = torch.empty_like(x)
             tg[k] = g.data_ptr()

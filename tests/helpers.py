@@ -281,3 +281,13 @@ def bs_demo_dual(S, X, T, r, v):
     d1 = d_log(S / X) + (d_fma(d_sqr(v), 0.5, r) * T) / (v * da)
     d2 = d_fnms(v, da, d1)
     return d_fnms(X * d_exp(-r * T), d_fastnormcdf(d2), S * d_fastnormcdf(d1))
+
+
+def bs_textbook_dual(S, K, T, sig, r):
+    """Textbook Black-Scholes call and put (normcdf), operation for operation
+    as the tests write the expression, on Duals."""
+    sq = d_sqrt(T)
+    d1 = (d_log(S / K) + d_fma(d_sqr(sig), 0.5, r) * T) / (sig * sq)
+    d2 = d_fnms(sig, sq, d1)
+    e = K * d_exp(-r * T)
+    return d_fnms(e, d_normcdf(d2), S * d_normcdf(d1)), d_fnms(S, d_normcdf(-d1), e * d_normcdf(-d2))
