@@ -18,6 +18,8 @@ in HBM.  Workloads (--config):
             expression written out), linked into one compiled batch kernel
   adjoint   fused BS forward + reverse (VJP), N=2^26 options
   adjoint_fwd  the forward alone on the same options (the 2.2x reference)
+  adjoint_program / adjoint_demo   reverse mode of a user program (nt2g_program_vjp)
+            on 2^26 options: textbook BS (sigma table, r scalar) / NT2's demo form
   sigmadelta   1920x1080 uint8 frames, one fused step per frame
   sigmadelta_fused  63 frame steps in one kernel
   rgb2yuv   1920x1080x3 float planes
@@ -447,6 +449,74 @@ class Adjoint(Workload):
             self.lib.blackscholes_vjp(self.S, self.K, self.T, self.sig, 0.02, self.gc, self.gp, self.outs)
 
 
+class ProgramAdjoint(Workload):
+    """Reverse mode of a user program (nt2g_program_vjp) over 2^26 options:
+    the textbook Black-Scholes call and put (sigma a table, r a scalar, both
+    cotangents; gradients of S, K, T, sigma and the summed dr), or the NT2
+    demo form (all five inputs tables, one cotangent).  Forward values are
+    recomputed in registers: nothing but the inputs, the cotangents and the
+    gradients moves."""
+    N = 1 << 26
+
+    def __init__(self, torch, lib, dev, form="textbook", precision=0):
+        import ctypes as C
+        from nt2_gb300 import expr as E
+        self.torch, self.lib = torch, lib
+        g = torch.Generator(device=dev).manual_seed(1004)
+        n = self.N
+        rnd = lambda lo, hi: torch.rand(n, device=dev, generator=g) * (hi - lo) + lo  # noqa: E731
+        if form == "textbook":
+            S, K, T, sig = rnd(5, 30), rnd(1, 100), rnd(0.25, 10), rnd(0.05, 0.8)
+            cts = [rnd(-1, 1), rnd(-1, 1)]
+            outs = [torch.empty(n, device=dev), torch.empty(n, device=dev)]
+            St, Kt, Tt, st = (E.Table(x) for x in (S, K, T, sig))
+            rs = E.Scalar(0.02)
+            exprs = _bs_program_exprs(E, St, Kt, Tt, st, rs)
+            wrt = [S, K, T, sig]
+            self.bytes = (6 * 4 + 4 * 4) * n
+            what = "textbook call+put, sigma table, r scalar: dS dK dT dsigma (tables) + dr (summed)"
+        else:
+            S, X, T, r, v = rnd(5, 30), rnd(1, 100), rnd(0.25, 10), rnd(0.01, 0.05), rnd(0.1, 0.6)
+            cts = [rnd(-1, 1)]
+            outs = [torch.empty(n, device=dev)]
+            da = E.sqrt(E.Table(T))
+            Sa, Xa, Ta, ra, va = (E.Table(x) for x in (S, X, T, r, v))
+            d1 = E.log(Sa / Xa) + (E.fma(E.sqr(va), 0.5, ra) * Ta) / (va * da)
+            d2 = E.fnms(va, da, d1)
+            exprs = [E.fnms(Xa * E.exp(-ra * Ta), E.fastnormcdf(d2), Sa * E.fastnormcdf(d1))]
+            wrt = [S, X, T, r, v]
+            self.bytes = (6 * 4 + 5 * 4) * n
+            what = "NT2 demo form, five input tables: all five gradients"
+        self.keep = (S, T, cts, outs, wrt, exprs)
+        prog, slots = E.compile_program(outs, exprs)
+        self.prog = prog
+        self.args, _ = E._args_of(slots)
+        ns = len(slots)
+        self.ns = ns
+        self.ct, self.tg = (C.c_void_p * ns)(), (C.c_void_p * ns)()
+        for o, c in zip(outs, cts):
+            self.ct[E._slot_of(slots, o)] = c.data_ptr()
+        self.grads = []
+        for x in wrt:
+            gx = torch.empty_like(x)
+            self.tg[E._slot_of(slots, x)] = gx.data_ptr()
+            self.grads.append(gx)
+        self.sg = torch.zeros(ns, dtype=torch.float64, device=dev)
+        nb = C.c_size_t()
+        lib.check(lib.load().nt2g_program_vjp_workspace_size(prog.handle, n, C.byref(nb)))
+        self.ws = torch.empty(max(nb.value, 16), dtype=torch.uint8, device=dev)
+        self.prec = precision
+        self.units = n
+        self.launches = 2 if form == "textbook" else 1  # + the scalar gradients' fixed-order sum
+        self.kernel = "nt2g_vjp_kernel"
+        self.name = f"program VJP N=2^26, {what}"
+
+    def step(self, i):
+        L = self.lib
+        L.check(L.load().nt2g_program_vjp(self.prog.handle, self.args, self.ns, self.N, self.ct, self.tg,
+                                          L._ptr(self.sg), self.prec, L._ptr(self.ws), self.ws.numel(), L._stream()))
+
+
 class SigmaDelta(Workload):
     def __init__(self, torch, lib, dev):
         self.torch, self.lib = torch, lib
@@ -679,6 +749,8 @@ def make(name, torch, lib, dev, precision, tune=None, n=None):
         return Adjoint(torch, lib, dev)
     if name == "adjoint_fwd":
         return Adjoint(torch, lib, dev, forward_only=True)
+    if name in ("adjoint_program", "adjoint_demo"):
+        return ProgramAdjoint(torch, lib, dev, "textbook" if name == "adjoint_program" else "demo", precision)
     if name in ("fn_trig", "fn_pow", "fn_gen", "fn_special"):
         return Functors(torch, lib, dev, name[3:], precision, n)
     if name == "sigmadelta":

@@ -498,7 +498,8 @@ std::string jit_batch_source(const std::vector<ProgramCode> &progs, int precisio
 // policy, used for the derivative arithmetic.  Empty when the instruction
 // passes no gradient (comparisons, rounding, sign, constants); false when the
 // opcode has no rule.
-static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k, const std::vector<uint8_t> &active)
+static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k, const std::vector<uint8_t> &active,
+                         std::vector<uint8_t> &phi_done)
 {
     const nt2g_op &o = ops[k];
     auto v = [](int x) { return "v" + std::to_string(x) + "[j]"; };
@@ -506,38 +507,59 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
     const std::string G = g(k), Y = v(k);
     const std::string A = o.a >= 0 ? v(o.a) : "", B = o.b >= 0 ? v(o.b) : "", C = o.c >= 0 ? v(o.c) : "";
     std::vector<std::pair<int, std::string>> add;  // (operand, partial derivative term to add: G * d)
+    std::string pre;  // per-lane temporaries the terms share
     auto to = [&](int operand, const std::string &term) {
         if (operand >= 0 && active[operand]) add.emplace_back(operand, term);
     };
+    auto act = [&](int operand) { return operand >= 0 && active[operand]; };
     const std::string pi = "nt2g::vjp::kPi", deg = "nt2g::vjp::kDegToRad";
+    auto rcp = [](const std::string &x) { return "nt2g::vjp::grcp(" + x + ")"; };
+    auto rsq = [](const std::string &x) { return "nt2g::vjp::grsqrt(" + x + ")"; };
+    const std::string one_m_a2 = "((1.0f - " + A + ") * (1.0f + " + A + "))";  // exact difference near |a| = 1
+    const std::string abs_a2_m1 = "((fabsf(" + A + ") - 1.0f) * (fabsf(" + A + ") + 1.0f))";
     switch (o.code) {
     case NT2G_OP_ADD: to(o.a, G); to(o.b, G); break;
     case NT2G_OP_SUB: to(o.a, G); to(o.b, "-" + G); break;
     case NT2G_OP_MUL: to(o.a, G + " * " + B); to(o.b, G + " * " + A); break;
-    case NT2G_OP_DIV: to(o.a, G + " / " + B); to(o.b, "-" + G + " * " + Y + " / " + B); break;
+    case NT2G_OP_DIV:  // a/b: G/b and -G (a/b) / b, one reciprocal
+        pre = "const float q = " + G + " * " + rcp(B) + ";";
+        to(o.a, "q");
+        to(o.b, "-q * " + Y);
+        break;
     case NT2G_OP_NEG: to(o.a, "-" + G); break;
     case NT2G_OP_ABS: to(o.a, "(" + A + " > 0.0f ? " + G + " : " + A + " < 0.0f ? -" + G + " : 0.0f)"); break;
     case NT2G_OP_SQR: to(o.a, "2.0f * " + A + " * " + G); break;
-    case NT2G_OP_SQRT: to(o.a, G + " * 0.5f / " + Y); break;
+    case NT2G_OP_SQRT: to(o.a, "0.5f * " + G + " * " + rcp(Y)); break;
     case NT2G_OP_REC: to(o.a, "-" + G + " * " + Y + " * " + Y); break;
     case NT2G_OP_MIN: to(o.a, "(" + A + " < " + B + " ? " + G + " : 0.0f)"); to(o.b, "(" + A + " < " + B + " ? 0.0f : " + G + ")"); break;
     case NT2G_OP_MAX: to(o.a, "(" + A + " > " + B + " ? " + G + " : 0.0f)"); to(o.b, "(" + A + " > " + B + " ? 0.0f : " + G + ")"); break;
     case NT2G_OP_FMA: to(o.a, G + " * " + B); to(o.b, G + " * " + A); to(o.c, G); break;
     case NT2G_OP_FNMS: to(o.a, "-" + G + " * " + B); to(o.b, "-" + G + " * " + A); to(o.c, G); break;
     case NT2G_OP_EXP: to(o.a, G + " * " + Y); break;
-    case NT2G_OP_LOG: to(o.a, G + " / " + A); break;
-    case NT2G_OP_LOG1P: to(o.a, G + " / (1.0f + " + A + ")"); break;
+    case NT2G_OP_LOG: to(o.a, G + " * " + rcp(A)); break;
+    case NT2G_OP_LOG1P: to(o.a, G + " * " + rcp("1.0f + " + A)); break;
     case NT2G_OP_ERF: to(o.a, G + " * nt2g::vjp::kTwoOverSqrtPi * nt2g::exp<D>(-" + A + " * " + A + ")"); break;
     case NT2G_OP_ERFC: to(o.a, "-" + G + " * nt2g::vjp::kTwoOverSqrtPi * nt2g::exp<D>(-" + A + " * " + A + ")"); break;
-    case NT2G_OP_NORMCDF:
-        to(o.a, G + " * nt2g::vjp::kInvSqrt2Pi * nt2g::exp<D>(-0.5f * " + A + " * " + A + ")");
+    case NT2G_OP_NORMCDF: {
+        // phi(y) once for normcdf(y) and normcdf(-y) (the pair of a
+        // call/put): the density is even
+        const bool neg = ops[o.a].code == NT2G_OP_NEG && ops[o.a].dtype == NT2G_F32;
+        const int base = neg ? ops[o.a].a : o.a;
+        const std::string phi = "phi" + std::to_string(base);
+        if (act(o.a) && !phi_done[base]) {
+            phi_done[base] = 1;
+            s += "    float " + phi + "[4]; NT2G_L " + phi + "[j] = nt2g::vjp::kInvSqrt2Pi * nt2g::exp<D>(-0.5f * " +
+                 v(base) + " * " + v(base) + ");\n";
+        }
+        to(o.a, G + " * " + phi + "[j]");
         break;
+    }
     case NT2G_OP_FASTNORMCDF: to(o.a, G + " * nt2g::vjp::fastnormcdf_grad<D>(" + A + ")"); break;
     case NT2G_OP_EXP2: to(o.a, G + " * " + Y + " * nt2g::vjp::kLn2"); break;
     case NT2G_OP_EXP10: to(o.a, G + " * " + Y + " * nt2g::vjp::kLn10"); break;
     case NT2G_OP_EXPM1: to(o.a, G + " * nt2g::exp<D>(" + A + ")"); break;  // not y + 1: it cancels as y -> -1
-    case NT2G_OP_LOG2: to(o.a, G + " / (" + A + " * nt2g::vjp::kLn2)"); break;
-    case NT2G_OP_LOG10: to(o.a, G + " / (" + A + " * nt2g::vjp::kLn10)"); break;
+    case NT2G_OP_LOG2: to(o.a, G + " * " + rcp(A) + " * nt2g::vjp::kInvLn2"); break;
+    case NT2G_OP_LOG10: to(o.a, G + " * " + rcp(A) + " * nt2g::vjp::kInvLn10"); break;
     case NT2G_OP_SIN: to(o.a, G + " * nt2g::cos<D>(" + A + ")"); break;
     case NT2G_OP_COS: to(o.a, "-" + G + " * nt2g::sin<D>(" + A + ")"); break;
     case NT2G_OP_TAN: to(o.a, G + " * (1.0f + " + Y + " * " + Y + ")"); break;
@@ -567,44 +589,46 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
     case NT2G_OP_COSH: to(o.a, G + " * nt2g::sinh<D>(" + A + ")"); break;
     // 1 - tanh^2 = 1/cosh^2 and 1 - coth^2 = -1/sinh^2: the forms in y would
     // magnify y's rounding where |y| nears 1
-    case NT2G_OP_TANH: to(o.a, G + " / (nt2g::cosh<D>(" + A + ") * nt2g::cosh<D>(" + A + "))"); break;
-    case NT2G_OP_COTH: to(o.a, "-" + G + " / (nt2g::sinh<D>(" + A + ") * nt2g::sinh<D>(" + A + "))"); break;
-    // 1 - a^2 as (1 - a)(1 + a), a^2 - 1 as (a - 1)(a + 1): exact differences near |a| = 1
-    case NT2G_OP_ASIN: to(o.a, G + " / sqrtf((1.0f - " + A + ") * (1.0f + " + A + "))"); break;
-    case NT2G_OP_ACOS: to(o.a, "-" + G + " / sqrtf((1.0f - " + A + ") * (1.0f + " + A + "))"); break;
-    case NT2G_OP_ATAN: to(o.a, G + " / (1.0f + " + A + " * " + A + ")"); break;
-    case NT2G_OP_ATAN2: {  // atan2(a, b): (b, -a) / (a^2 + b^2)
-        const std::string r2 = "(" + A + " * " + A + " + " + B + " * " + B + ")";
-        to(o.a, G + " * " + B + " / " + r2);
-        to(o.b, "-" + G + " * " + A + " / " + r2);
+    case NT2G_OP_TANH:
+        pre = "const float c = nt2g::cosh<D>(" + A + ");";
+        to(o.a, G + " * " + rcp("c * c"));
         break;
-    }
+    case NT2G_OP_COTH:
+        pre = "const float c = nt2g::sinh<D>(" + A + ");";
+        to(o.a, "-" + G + " * " + rcp("c * c"));
+        break;
+    // 1 - a^2 as (1 - a)(1 + a), a^2 - 1 as (|a| - 1)(|a| + 1): exact differences near |a| = 1
+    case NT2G_OP_ASIN: to(o.a, G + " * " + rsq(one_m_a2)); break;
+    case NT2G_OP_ACOS: to(o.a, "-" + G + " * " + rsq(one_m_a2)); break;
+    case NT2G_OP_ATAN: to(o.a, G + " * " + rcp("1.0f + " + A + " * " + A)); break;
+    case NT2G_OP_ATAN2:  // atan2(a, b): (b, -a) / (a^2 + b^2)
+        pre = "const float q = " + G + " * " + rcp(A + " * " + A + " + " + B + " * " + B) + ";";
+        to(o.a, "q * " + B);
+        to(o.b, "-q * " + A);
+        break;
     case NT2G_OP_HYPOT:
-        to(o.a, "(" + Y + " == 0.0f ? 0.0f : " + G + " * " + A + " / " + Y + ")");
-        to(o.b, "(" + Y + " == 0.0f ? 0.0f : " + G + " * " + B + " / " + Y + ")");
+        pre = "const float q = " + Y + " == 0.0f ? 0.0f : " + G + " * " + rcp(Y) + ";";
+        to(o.a, "q * " + A);
+        to(o.b, "q * " + B);
         break;
-    case NT2G_OP_ASINH: to(o.a, G + " / sqrtf(" + A + " * " + A + " + 1.0f)"); break;
-    case NT2G_OP_ACOSH: to(o.a, G + " / (sqrtf(" + A + " - 1.0f) * sqrtf(" + A + " + 1.0f))"); break;
-    case NT2G_OP_ATANH: to(o.a, G + " / ((1.0f - " + A + ") * (1.0f + " + A + "))"); break;
-    case NT2G_OP_ACOTD: to(o.a, "-" + G + " * nt2g::vjp::kRadToDeg / (1.0f + " + A + " * " + A + ")"); break;
-    case NT2G_OP_ASEC:
-        to(o.a, G + " / (fabsf(" + A + ") * sqrtf((fabsf(" + A + ") - 1.0f) * (fabsf(" + A + ") + 1.0f)))");
-        break;
-    case NT2G_OP_ACSC:
-        to(o.a, "-" + G + " / (fabsf(" + A + ") * sqrtf((fabsf(" + A + ") - 1.0f) * (fabsf(" + A + ") + 1.0f)))");
-        break;
-    case NT2G_OP_ASECH: to(o.a, "-" + G + " / (" + A + " * sqrtf((1.0f - " + A + ") * (1.0f + " + A + ")))"); break;
-    case NT2G_OP_ACOTH: to(o.a, G + " / ((1.0f - " + A + ") * (1.0f + " + A + "))"); break;
-    case NT2G_OP_ACSCH: to(o.a, "-" + G + " / (fabsf(" + A + ") * sqrtf(1.0f + " + A + " * " + A + "))"); break;
-    case NT2G_OP_CBRT: to(o.a, G + " / (3.0f * " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_ASINH: to(o.a, G + " * " + rsq(A + " * " + A + " + 1.0f")); break;
+    case NT2G_OP_ACOSH: to(o.a, G + " * " + rsq(A + " - 1.0f") + " * " + rsq(A + " + 1.0f")); break;
+    case NT2G_OP_ATANH: to(o.a, G + " * " + rcp(one_m_a2)); break;
+    case NT2G_OP_ACOTD: to(o.a, "-" + G + " * nt2g::vjp::kRadToDeg * " + rcp("1.0f + " + A + " * " + A)); break;
+    case NT2G_OP_ASEC: to(o.a, G + " * " + rcp("fabsf(" + A + ")") + " * " + rsq(abs_a2_m1)); break;
+    case NT2G_OP_ACSC: to(o.a, "-" + G + " * " + rcp("fabsf(" + A + ")") + " * " + rsq(abs_a2_m1)); break;
+    case NT2G_OP_ASECH: to(o.a, "-" + G + " * " + rcp(A) + " * " + rsq(one_m_a2)); break;
+    case NT2G_OP_ACOTH: to(o.a, G + " * " + rcp(one_m_a2)); break;
+    case NT2G_OP_ACSCH: to(o.a, "-" + G + " * " + rcp("fabsf(" + A + ")") + " * " + rsq("1.0f + " + A + " * " + A)); break;
+    case NT2G_OP_CBRT: to(o.a, G + " * " + rcp("3.0f * " + Y + " * " + Y)); break;
     case NT2G_OP_ERFCX: to(o.a, G + " * (2.0f * " + A + " * " + Y + " - nt2g::vjp::kTwoOverSqrtPi)"); break;
     case NT2G_OP_EXPX2: to(o.a, G + " * 2.0f * " + A + " * " + Y); break;
     case NT2G_OP_GAMMA: to(o.a, G + " * " + Y + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
     case NT2G_OP_GAMMALN: to(o.a, G + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
-    case NT2G_OP_EXPRECNEG: to(o.a, G + " * " + Y + " / (" + A + " * " + A + ")"); break;
+    case NT2G_OP_EXPRECNEG: to(o.a, G + " * " + Y + " * " + rcp(A + " * " + A)); break;
     // -e^(-1/x)/x^2 and 1/(2 sqrt(1 + x)) directly: y - 1 and y + 1 would cancel
-    case NT2G_OP_EXPRECNEGC: to(o.a, "-" + G + " * nt2g::exprecneg<D>(" + A + ") / (" + A + " * " + A + ")"); break;
-    case NT2G_OP_SQRT1PM1: to(o.a, G + " * 0.5f / sqrtf(1.0f + " + A + ")"); break;
+    case NT2G_OP_EXPRECNEGC: to(o.a, "-" + G + " * nt2g::exprecneg<D>(" + A + ") * " + rcp(A + " * " + A)); break;
+    case NT2G_OP_SQRT1PM1: to(o.a, "0.5f * " + G + " * " + rsq("1.0f + " + A)); break;
     case NT2G_OP_ERFINV: to(o.a, G + " * nt2g::vjp::kHalfSqrtPi * nt2g::exp<D>(" + Y + " * " + Y + ")"); break;
     case NT2G_OP_ERFCINV: to(o.a, "-" + G + " * nt2g::vjp::kHalfSqrtPi * nt2g::exp<D>(" + Y + " * " + Y + ")"); break;
     case NT2G_OP_FRAC: to(o.a, G); break;
@@ -618,7 +642,14 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
         break;  // piecewise constant: no gradient
     default: return false;
     }
-    for (const auto &t : add) s += "    NT2G_L g" + std::to_string(t.first) + "[j] += " + t.second + ";\n";
+    if (add.empty()) return true;
+    if (pre.empty()) {
+        for (const auto &t : add) s += "    NT2G_L g" + std::to_string(t.first) + "[j] += " + t.second + ";\n";
+    } else {
+        s += "    NT2G_L { " + pre;
+        for (const auto &t : add) s += " g" + std::to_string(t.first) + "[j] += " + t.second + ";";
+        s += " }\n";
+    }
     return true;
 }
 
@@ -702,10 +733,11 @@ std::string jit_vjp_source(const std::vector<nt2g_op> &ops, const std::vector<ui
         s += "    if (g.ct[" + sl + "]) { float t[4]; jit_ldf<FULL>(t, g.ct[" + sl + "], i, cnt); NT2G_L g" + val +
              "[j] += t[j]; }\n";
     }
+    std::vector<uint8_t> phi_done(ops.size(), 0);
     for (size_t k = ops.size(); k-- > 0;) {
         const nt2g_op &o = ops[k];
         if (!act[k] || o.code == NT2G_OP_LOAD || o.code == NT2G_OP_SCALAR) continue;
-        if (!adjoint_rule(s, ops, (int)k, act)) {
+        if (!adjoint_rule(s, ops, (int)k, act, phi_done)) {
             if (why) *why = "opcode " + std::to_string(o.code) + " has no adjoint rule";
             return "";
         }

@@ -18,6 +18,36 @@ constexpr float kHalfSqrtPi = 0.886226925452758013649f;
 constexpr float kInvSqrt2Pi = 0.398942280401432677940f;
 constexpr float kDegToRad = 0.0174532925199432957692f;
 constexpr float kRadToDeg = 57.2957795130823208768f;
+constexpr float kInvLn2 = 1.44269504088896340736f;
+constexpr float kInvLn10 = 0.434294481903251827651f;
+
+// 1/x for the derivative arithmetic: the SFU's approximate reciprocal and one
+// Newton step (within an ulp of 1/x); where the step would make a NaN (x = 0
+// or +-inf) the approximation's own +-inf or 0.  Flushes subnormal x (and a
+// subnormal 1/x) to zero first.
+NT2G_HD float grcp(float x)
+{
+#if defined(__CUDA_ARCH__)
+    float r0;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(x));
+    const float r1 = __fmaf_rn(r0, __fmaf_rn(-x, r0, 1.0f), r0);
+    return r1 == r1 ? r1 : r0;
+#else
+    return 1.0f / x;
+#endif
+}
+
+// 1/sqrt(x) from the SFU (relative error below 2^-22): +inf at 0, NaN below.
+NT2G_HD float grsqrt(float x)
+{
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / sqrtf(x);
+#endif
+}
 
 // d/dx of NT2's Abramowitz-Stegun 26.2.17 fastnormcdf (the approximation
 // itself, not the normal density it approximates).  With l = |x|,
@@ -29,7 +59,7 @@ template <class D> NT2G_HD float fastnormcdf_grad(float x)
 {
     const float p = 0.2316419f;
     const float l = fminf(fabsf(x), 100.0f);
-    const float k = 1.0f / (1.0f + p * l);
+    const float k = grcp(1.0f + p * l);
     // the approximation's coefficients b1..b5 (A&S 26.2.17, as NT2 stores them)
     const float b1 = bits_f(0x3ea385fau), b2 = bits_f(0xbeb68f87u), b3 = bits_f(0x3fe40778u),
                 b4 = bits_f(0xbfe91eeau), b5 = bits_f(0x3faa466fu);
@@ -76,7 +106,7 @@ template <class D> NT2G_HD float sinc_grad(float x, float y)
         const float x2 = x * x;
         return x * (-1.0f / 3.0f + x2 * (1.0f / 30.0f + x2 * (-1.0f / 840.0f + x2 * (1.0f / 45360.0f))));
     }
-    return (cos<D>(x) - y) / x;
+    return (cos<D>(x) - y) * grcp(x);
 }
 
 // sincpi(x) = sinc(pi x): pi sinc'(pi x), the quotient (cospi x - sincpi x)/x
@@ -90,7 +120,7 @@ template <class D> NT2G_HD float sincpi_grad(float x, float y)
         const float u2 = u * u;
         return kPi * u * (-1.0f / 3.0f + u2 * (1.0f / 30.0f + u2 * (-1.0f / 840.0f + u2 * (1.0f / 45360.0f))));
     }
-    return (cospi<D>(x) - y) / x;
+    return (cospi<D>(x) - y) * grcp(x);
 }
 
 // d/dx sinh(x)/x = (cosh x - sinhc x)/x; below 1/2 the series
@@ -101,7 +131,7 @@ template <class D> NT2G_HD float sinhc_grad(float x, float y)
         const float x2 = x * x;
         return x * (1.0f / 3.0f + x2 * (1.0f / 30.0f + x2 * (1.0f / 840.0f + x2 * (1.0f / 45360.0f))));
     }
-    return (cosh<D>(x) - y) / x;
+    return (cosh<D>(x) - y) * grcp(x);
 }
 
 }  // namespace vjp
