@@ -59,13 +59,8 @@ __device__ __forceinline__ void run_tile(const DItem &it, int64_t start, int64_t
             if constexpr (!P::exact) {  // two options per packed instruction, as the plain kernel
                 bs_vec4_fast(s, k, t, make_float4(sig, sig, sig, sig), make_float4(inv_sig, inv_sig, inv_sig, inv_sig),
                              r, c, p);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    float cj, pj;
-                    bs_option<P>(get(s, j), get(k, j), get(t, j), sig, inv_sig, r, cj, pj);
-                    set(c, j, cj); set(p, j, pj);
-                }
+            } else {  // NT2's unfused arithmetic, two options per packed instruction
+                bs_vec4_nt2(s, k, t, make_float4(sig, sig, sig, sig), r, c, p);
             }
             st_stream((float4 *)it.out[0] + at, c);
             st_stream((float4 *)it.out[1] + at, p);

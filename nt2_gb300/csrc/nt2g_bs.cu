@@ -35,14 +35,9 @@ __device__ __forceinline__ void bs_float4(const float *__restrict__ S, const flo
         }
         bs_vec4_fast(s, k, t, v, iv, r, c, p);
     } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            float cj, pj;
-            const float sj = get(v, j);
-            bs_option<P>(get(s, j), get(k, j), get(t, j), sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, cj, pj);
-            set(c, j, cj);
-            set(p, j, pj);
-        }
+        // NT2's unfused arithmetic two options per packed instruction,
+        // bit-identical to bs_option<Nt2>
+        bs_vec4_nt2(s, k, t, v, r, c, p);
     }
     st_stream((float4 *)call + i, c);
     st_stream((float4 *)put + i, p);

@@ -266,4 +266,178 @@ __device__ __forceinline__ void bs_vec4_fast(const float4 &s, const float4 &k, c
     upk(p2, p.z, p.w);
 }
 
+// ------------------------------------------------------------ NT2 policy --
+// The bit-exact policy two options at a time.  NT2's arithmetic is unfused
+// (its fma is a rounded product and a rounded sum), and add/sub.rn.f32x2
+// round each lane exactly as the scalar __fadd_rn / __fsub_rn do.  A packed
+// product is different: the code generator merges a mul.rn.f32x2 into the
+// add.rn.f32x2 that consumes it (one rounding instead of NT2's two), even
+// with the explicit rounding mode and with contraction disabled.  So every
+// product here is fma.rn.f32x2(a, b, z) with z = -0 in both lanes, loaded from
+// memory where the code generator cannot see its value: RN(a*b + -0) is
+// RN(a*b) bit for bit (a zero product keeps its own sign), and an FMA whose
+// addend is unknown has nothing to merge with.  IEEE division and square
+// root, rint, the conversions and all bit manipulation stay per lane.  These
+// functions reproduce Nt2's scalar results bit for bit.
+
+static __device__ unsigned long long g_pair_negzero = 0x8000000080000000ull;
+
+// -0 in both lanes, through a load the code generator cannot fold
+__device__ __forceinline__ f2 pair_negzero()
+{
+    f2 z;
+    asm volatile("ld.b64 %0, [%1];" : "=l"(z.v) : "l"(&g_pair_negzero));
+    return z;
+}
+// RN(a*b) in each lane, never merged with a following add
+__device__ __forceinline__ f2 nmul2(f2 a, f2 b, f2 nz) { return fma2(a, b, nz); }
+__device__ __forceinline__ f2 nt2_fma2(f2 a, f2 b, f2 c, f2 nz) { return add2(nmul2(a, b, nz), c); }
+__device__ __forceinline__ f2 nt2_horner2(f2, f2, f2 acc) { return acc; }
+template <class... R> __device__ __forceinline__ f2 nt2_horner2(f2 nz, f2 x, f2 acc, uint32_t c, R... rest)
+{
+    return nt2_horner2(nz, x, add2(nmul2(x, acc, nz), dup(bits_f(c))), rest...);
+}
+
+__device__ __forceinline__ f2 div_rn2(f2 a, f2 b)
+{
+    return lanes(a, b, [](float x, float y) { return __fdiv_rn(x, y); });
+}
+__device__ __forceinline__ f2 sqrt_rn2(f2 a) { return lanes(a, [](float x) { return __fsqrt_rn(x); }); }
+__device__ __forceinline__ f2 abs2(f2 a)
+{
+    f2 r;
+    r.v = a.v & 0x7fffffff7fffffffull;
+    return r;
+}
+// per-lane select: c0 ? a.lo : b.lo, c1 ? a.hi : b.hi
+__device__ __forceinline__ f2 sel2(bool c0, bool c1, f2 a, f2 b)
+{
+    float a0, a1, b0, b1;
+    upk(a, a0, a1);
+    upk(b, b0, b1);
+    return pk(c0 ? a0 : b0, c1 ? a1 : b1);
+}
+
+// exp<Nt2>, lane for lane.
+__device__ __forceinline__ f2 exp_nt2_2(f2 a0, f2 nz)
+{
+    const f2 kf = lanes(nmul2(dup(bits_f(NT2G_INVLOG_2)), a0, nz), [](float v) { return rintf(v); });
+    f2 x = sub2(a0, nmul2(kf, dup(bits_f(NT2G_LOG_2HI)), nz));
+    x = sub2(x, nmul2(kf, dup(bits_f(NT2G_LOG_2LO)), nz));
+    const f2 y = nt2_horner2(nz, x, dup(bits_f(0x3ab778cfu)), 0x3c098d8bu, 0x3d2aa957u, 0x3e2aa9a5u, 0x3f000000u);
+    const f2 c = add2(nt2_fma2(y, nmul2(x, x, nz), x, nz), dup(1.0f));
+    float k0, k1, a, b;
+    upk(kf, k0, k1);
+    upk(a0, a, b);
+    float r0, r1;
+    upk(nmul2(c, pk(bits_f((uint32_t)((int32_t)k0 + 127) << 23), bits_f((uint32_t)((int32_t)k1 + 127) << 23)), nz), r0,
+        r1);
+    auto fix = [](float a0s, float r) {
+        return (a0s >= bits_f(NT2G_MAXLOG)) ? f_inf() : (a0s <= bits_f(NT2G_MINLOG)) ? 0.0f : is_nan(a0s) ? a0s : r;
+    };
+    return pk(fix(a, r0), fix(b, r1));
+}
+
+// log<Nt2>, lane for lane (log_reduce with NT2's log constants).
+__device__ __forceinline__ f2 log_nt2_2(f2 a0, f2 nz)
+{
+    float z0, z1;
+    upk(a0, z0, z1);
+    const bool den0 = fabsf(z0) < bits_f(NT2G_SMALLESTPOS), den1 = fabsf(z1) < bits_f(NT2G_SMALLESTPOS);
+    const f2 zs = nmul2(a0, dup(bits_f(NT2G_TWOTONMB)), nz);
+    float s0, s1;
+    upk(zs, s0, s1);
+    const float w0 = den0 ? s0 : z0, w1 = den1 ? s1 : z1;
+    const f2 t = pk(den0 ? bits_f(NT2G_MLOGTWO2NMB) : 0.0f, den1 ? bits_f(NT2G_MLOGTWO2NMB) : 0.0f);
+    const uint32_t u0 = f_bits(w0), u1 = f_bits(w1);
+    const int32_t e0 = (int32_t)((u0 & 0x7f800000u) >> 23) - 126, e1 = (int32_t)((u1 & 0x7f800000u) >> 23) - 126;
+    const float x0 = bits_f((u0 & ~0x7f800000u) | 0x3f000000u), x1 = bits_f((u1 & ~0x7f800000u) | 0x3f000000u);
+    const bool lt0 = x0 < bits_f(NT2G_SQRT_2O_2), lt1 = x1 < bits_f(NT2G_SQRT_2O_2);
+    const f2 ef = pk((float)e0, (float)e1);
+    const f2 fe = sel2(lt0, lt1, add2(ef, dup(-1.0f)), ef);
+    const f2 xm = pk(x0, x1);
+    const f2 x = sub2(sel2(lt0, lt1, add2(xm, xm), xm), dup(1.0f));
+    const f2 x2 = nmul2(x, x, nz);
+    f2 y = nt2_horner2(nz, x, dup(bits_f(0xbda5dff0u)), 0x3e0229f9u, 0xbe04d6b7u, 0x3e116e80u, 0xbe2a6aa0u, 0x3e4cd0a3u,
+                       0xbe800064u, 0x3eaaaaa9u);
+    y = nmul2(nmul2(y, x, nz), x2, nz);
+    y = nt2_fma2(fe, dup(bits_f(NT2G_LOG_2LO)), y, nz);
+    y = nt2_fma2(dup(-0.5f), x2, y, nz);
+    const f2 r = nt2_fma2(dup(bits_f(NT2G_LOG_2HI)), fe, add2(add2(x, y), t), nz);
+    float r0, r1;
+    upk(r, r0, r1);
+    auto fix = [](float a, float v) {
+        return (a == f_inf()) ? a : (a == 0.0f) ? -f_inf() : (is_nan(a) || a < 0.0f) ? f_nan() : v;
+    };
+    return pk(fix(z0, r0), fix(z1, r1));
+}
+
+// erfc_core_nt2 for x >= 0, lane for lane.  The scalar code branches on
+// x < 2/3; a warp holding both kinds issues both paths anyway, so here both
+// polynomials are evaluated (two lanes per instruction) and each lane keeps
+// its own.
+__device__ __forceinline__ f2 erfc_core_nt2_2(f2 x, f2 nz)
+{
+    const f2 z = div_rn2(x, add2(x, dup(1.0f)));
+    const f2 b1 = nmul2(sub2(dup(1.0f), z),
+                       nt2_horner2(nz, z, dup(bits_f(0x41aa8e55u)), 0x401b5680u, 0xc010d956u, 0x3f2cff3bu, 0xc016c985u,
+                                   0xbffc9284u, 0xbfa11698u, 0xbe036d7eu, 0x3f7ffffeu), nz);
+    const f2 zz = sub2(z, dup(0.4f));
+    const f2 b2 = nmul2(exp_nt2_2(negx2(nmul2(x, x, nz)), nz),
+                       nt2_horner2(nz, zz, dup(bits_f(0xc0283611u)), 0x40d67e3bu, 0xc0cd1a85u, 0x4050b063u, 0xbfaea865u,
+                                   0x3e2006f0u, 0x3e1175c7u, 0x3ec4ca6eu, 0x3e243828u, 0xbf918a62u, 0x3f0a0e8bu), nz);
+    float x0, x1, p0, p1, q0, q1;
+    upk(x, x0, x1);
+    upk(b1, p0, p1);
+    upk(b2, q0, q1);
+    const float two3 = bits_f(NT2G_TWOTHIRD);
+    return pk(x0 < two3 ? p0 : (x0 == f_inf() ? 0.0f : q0), x1 < two3 ? p1 : (x1 == f_inf() ? 0.0f : q1));
+}
+
+// normcdf_pair<Nt2>, lane for lane.
+__device__ __forceinline__ void normcdf_pair_nt2_2(f2 x, f2 &n_pos, f2 &n_neg, f2 nz)
+{
+    const f2 t = nmul2(dup(-bits_f(NT2G_SQRT_2O_2)), x, nz);
+    const f2 r1 = erfc_core_nt2_2(abs2(t), nz);
+    const f2 r2 = sub2(dup(2.0f), r1);
+    float t0, t1;
+    upk(t, t0, t1);
+    n_pos = nmul2(dup(0.5f), sel2(t0 < 0.0f, t1 < 0.0f, r2, r1), nz);
+    n_neg = nmul2(dup(0.5f), sel2(-t0 < 0.0f, -t1 < 0.0f, r2, r1), nz);
+}
+
+// bs_option<Nt2> for two options; a = fma(sig^2, 1/2, r) given per lane.
+__device__ __forceinline__ void bs_option_nt2_2(f2 S, f2 K, f2 T, f2 sig, f2 a, float r, f2 &call, f2 &put,
+                                                f2 nz)
+{
+    const f2 sq = sqrt_rn2(T);
+    const f2 lq = log_nt2_2(div_rn2(S, K), nz);
+    const f2 ssq = nmul2(sig, sq, nz);
+    const f2 d1 = div_rn2(add2(lq, nmul2(a, T, nz)), ssq);
+    const f2 d2 = sub2(d1, ssq);
+    const f2 e = nmul2(K, exp_nt2_2(nmul2(dup(-r), T, nz), nz), nz);
+    f2 n1, m1, n2, m2;
+    normcdf_pair_nt2_2(d1, n1, m1, nz);
+    normcdf_pair_nt2_2(d2, n2, m2, nz);
+    call = sub2(nmul2(S, n1, nz), nmul2(e, n2, nz));
+    put = sub2(nmul2(e, m2, nz), nmul2(S, m1, nz));
+}
+
+// Four options as two pairs under the NT2 policy; sigma per option.
+__device__ __forceinline__ void bs_vec4_nt2(const float4 &s, const float4 &k, const float4 &t, const float4 &v, float r,
+                                            float4 &c, float4 &p)
+{
+    const f2 nz = pair_negzero();
+    const f2 v01 = pk(v.x, v.y), v23 = pk(v.z, v.w);
+    // fma(sig*sig, 0.5, r) unfused
+    const f2 a01 = add2(nmul2(nmul2(v01, v01, nz), dup(0.5f), nz), dup(r)), a23 = add2(nmul2(nmul2(v23, v23, nz), dup(0.5f), nz), dup(r));
+    f2 c2, p2;
+    bs_option_nt2_2(pk(s.x, s.y), pk(k.x, k.y), pk(t.x, t.y), v01, a01, r, c2, p2, nz);
+    upk(c2, c.x, c.y);
+    upk(p2, p.x, p.y);
+    bs_option_nt2_2(pk(s.z, s.w), pk(k.z, k.w), pk(t.z, t.w), v23, a23, r, c2, p2, nz);
+    upk(c2, c.z, c.w);
+    upk(p2, p.z, p.w);
+}
+
 }  // namespace nt2g

@@ -115,3 +115,25 @@ def test_ill_conditioned_dot(red, lib, dev, oracle, n):
         assert err <= 64 * EPS32 ** 2 * absum
         assert got32 == np.float32(got64)
         assert fn()[0] == got64  # deterministic
+
+
+def test_zero_length_writes_zero(red, lib, dev):
+    """n = 0 through both entry points: the outputs, pre-filled with garbage,
+    read 0 (the kernel still runs and writes them; the outputs are checked
+    reachable even for an empty reduction)."""
+    import ctypes
+    x = torch.empty(0, device=dev)
+    for entry in ("workspace", "noalloc"):
+        o64 = torch.full((1,), 123.5, dtype=torch.float64, device=dev)
+        o32 = torch.full((1,), -7.0, dtype=torch.float32, device=dev)
+        if entry == "workspace":
+            ws = torch.empty(red.ws.numel(), dtype=torch.uint8, device=dev)
+            lib.check(lib.load().nt2g_reduce_f32(ctypes.c_void_p(x.data_ptr()), None, 0, ctypes.c_void_p(ws.data_ptr()),
+                                                 ws.numel(), ctypes.c_void_p(o64.data_ptr()),
+                                                 ctypes.c_void_p(o32.data_ptr()), lib._stream()))
+        else:
+            lib.check(lib.load().nt2g_reduce_f32_noalloc(ctypes.c_void_p(x.data_ptr()), None, 0,
+                                                          ctypes.c_void_p(o64.data_ptr()),
+                                                          ctypes.c_void_p(o32.data_ptr()), lib._stream()))
+        torch.cuda.synchronize()
+        assert o64.item() == 0.0 and o32.item() == 0.0, entry
