@@ -488,6 +488,12 @@ nt2g_status nt2g_batch_stats(const nt2g_batch *b, int64_t *elements, int64_t *by
 nt2g_status nt2g_batch_source(const nt2g_program *const *programs, int32_t n_programs, int32_t precision,
                               int32_t block_threads, char *buf, size_t cap, size_t *len);
 
+/* Bounded waits that gave up so far, process-wide (kernels that wait on an
+ * mbarrier -- the pipelined Black-Scholes -- poll a limited number of times,
+ * count a timeout here and return; nothing ever spins forever).  0 on a
+ * healthy device.  Synchronises with the device. */
+nt2g_status nt2g_wait_timeouts(uint64_t *count);
+
 /* ------------------------------------------------------------------ */
 /* Device memory for the table layer: nt2::table<T, device_> storage   */
 /* (CUDA/sdk/memory/cuda/allocator.hpp:59-74, copies                   */

@@ -8,6 +8,7 @@
 // e^-rT and exp(-d^2/2) from the SFU's 2^x: ~95 instructions per option for
 // 20 bytes of HBM traffic, so the kernel sits at the FP32-pipe / HBM ridge.
 // 5 blocks of 256 threads per SM (48 registers).
+#include "nt2g_async.cuh"
 #include "nt2g_common.cuh"
 #include "nt2g_exprs.cuh"
 #include "nt2g_pair.cuh"
@@ -15,16 +16,11 @@
 
 namespace nt2g {
 
+// Four options already in registers (sigma per option when SIG_TAB).
 template <class P, bool SIG_TAB>
-__device__ __forceinline__ void bs_float4(const float *__restrict__ S, const float *__restrict__ K,
-                                          const float *__restrict__ T, const float *__restrict__ sig, float sig_s,
-                                          float inv_sig_s, float r, float *__restrict__ call,
-                                          float *__restrict__ put, int64_t i)
+__device__ __forceinline__ void bs_compute4(const float4 &s, const float4 &k, const float4 &t, const float4 &v,
+                                            float inv_sig_s, float r, float4 &c, float4 &p)
 {
-    float4 s = ld_stream((const float4 *)S + i), k = ld_stream((const float4 *)K + i),
-           t = ld_stream((const float4 *)T + i);
-    float4 v = SIG_TAB ? ld_stream((const float4 *)sig + i) : make_float4(sig_s, sig_s, sig_s, sig_s);
-    float4 c, p;
     if constexpr (!P::exact) {
         // two options per packed instruction, bit-identical to bs_option<Fast>
         float4 iv = make_float4(inv_sig_s, inv_sig_s, inv_sig_s, inv_sig_s);
@@ -39,8 +35,103 @@ __device__ __forceinline__ void bs_float4(const float *__restrict__ S, const flo
         // bit-identical to bs_option<Nt2>
         bs_vec4_nt2(s, k, t, v, r, c, p);
     }
+}
+
+template <class P, bool SIG_TAB>
+__device__ __forceinline__ void bs_float4(const float *__restrict__ S, const float *__restrict__ K,
+                                          const float *__restrict__ T, const float *__restrict__ sig, float sig_s,
+                                          float inv_sig_s, float r, float *__restrict__ call,
+                                          float *__restrict__ put, int64_t i)
+{
+    float4 s = ld_stream((const float4 *)S + i), k = ld_stream((const float4 *)K + i),
+           t = ld_stream((const float4 *)T + i);
+    float4 v = SIG_TAB ? ld_stream((const float4 *)sig + i) : make_float4(sig_s, sig_s, sig_s, sig_s);
+    float4 c, p;
+    bs_compute4<P, SIG_TAB>(s, k, t, v, inv_sig_s, r, c, p);
     st_stream((float4 *)call + i, c);
     st_stream((float4 *)put + i, p);
+}
+
+// Waits of this file's kernels that gave up (nt2g_wait_timeouts).
+__device__ unsigned long long g_bs_wait_timeouts = 0;
+
+// Pipelined form for aligned tables: a persistent grid walks tiles of 1024
+// options (one float4 per thread of a 256-thread block).  Thread 0 keeps the
+// block's next STAGES - 1 tiles of S, K, T (and sigma) in flight as bulk
+// copies into shared memory, each stage completing on its mbarrier, so the
+// loads of later tiles overlap the pricing of the current one and no warp
+// waits on HBM latency once the pipeline is primed.  Results go straight to
+// global memory (streaming float4 stores).  One block barrier per tile: after
+// it every thread has read the previous stage, which thread 0 then refills.
+// The options past the last whole tile (fewer than 1024) are priced by block
+// 0 with plain loads.
+template <class P, bool SIG_TAB, int STAGES>
+__global__ void __launch_bounds__(256, SIG_TAB ? 4 : 5) k_bs_pipe(const float *__restrict__ S, const float *__restrict__ K,
+                                                 const float *__restrict__ T, const float *__restrict__ sig,
+                                                 float sig_s, float r, float *__restrict__ call,
+                                                 float *__restrict__ put, int64_t n)
+{
+    constexpr int NT = SIG_TAB ? 4 : 3;  // tables per tile
+    constexpr int TILE = 1024;           // options per tile
+    constexpr uint32_t TILE_BYTES = TILE * 4;
+    extern __shared__ __align__(128) float4 stage_buf[];  // [STAGES][NT][256]
+    uint64_t *full = reinterpret_cast<uint64_t *>(stage_buf + STAGES * NT * 256);
+    const int tid = threadIdx.x;
+    const int64_t ntiles = n / TILE, G = gridDim.x;
+    const float inv_sig_s = P::exact || SIG_TAB ? 0.0f : inv_fast(sig_s);
+    auto issue = [&](int s, int64_t t) {
+        mbar_arrive_expect_tx(&full[s], NT * TILE_BYTES);
+        bulk_copy_g2s(stage_buf + (s * NT + 0) * 256, S + t * TILE, TILE_BYTES, &full[s]);
+        bulk_copy_g2s(stage_buf + (s * NT + 1) * 256, K + t * TILE, TILE_BYTES, &full[s]);
+        bulk_copy_g2s(stage_buf + (s * NT + 2) * 256, T + t * TILE, TILE_BYTES, &full[s]);
+        if (SIG_TAB) bulk_copy_g2s(stage_buf + (s * NT + 3) * 256, sig + t * TILE, TILE_BYTES, &full[s]);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+        mbar_init_fence();
+        for (int s = 0; s < STAGES; ++s)
+            if (blockIdx.x + s * G < ntiles) issue(s, blockIdx.x + s * G);
+    }
+    __syncthreads();
+    int64_t it = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += G, ++it) {
+        const int s = (int)(it % STAGES);
+        const bool ok = mbar_wait_bounded(&full[s], (uint32_t)((it / STAGES) & 1));
+        if (__syncthreads_or(!ok)) {
+            // gave up: count it, let this block's copies still in flight land
+            // (tiles it .. it + STAGES - 2 were issued), then leave
+            if (tid == 0) {
+                atomicAdd(&g_bs_wait_timeouts, 1ull);
+                for (int64_t k = it; k < it + STAGES - 1 && blockIdx.x + k * G < ntiles; ++k)
+                    mbar_wait_bounded(&full[k % STAGES], (uint32_t)((k / STAGES) & 1));
+            }
+            return;
+        }
+        // every thread has read the previous stage: refill it with the tile
+        // STAGES - 1 ahead of this one
+        if (tid == 0 && it > 0 && t + (STAGES - 1) * G < ntiles) {
+            fence_proxy_async_smem();
+            issue((int)((it - 1) % STAGES), t + (STAGES - 1) * G);
+        }
+        const float4 sv = stage_buf[(s * NT + 0) * 256 + tid], kv = stage_buf[(s * NT + 1) * 256 + tid],
+                     tv = stage_buf[(s * NT + 2) * 256 + tid];
+        const float4 vv = SIG_TAB ? stage_buf[(s * NT + 3) * 256 + tid] : make_float4(sig_s, sig_s, sig_s, sig_s);
+        float4 c, p;
+        bs_compute4<P, SIG_TAB>(sv, kv, tv, vv, inv_sig_s, r, c, p);
+        const int64_t o = t * 256 + tid;
+        st_stream((float4 *)call + o, c);
+        st_stream((float4 *)put + o, p);
+    }
+    if (blockIdx.x == 0) {
+        const int64_t nv = n >> 2;
+        for (int64_t i = ntiles * 256 + tid; i < nv; i += blockDim.x)
+            bs_float4<P, SIG_TAB>(S, K, T, sig, sig_s, inv_sig_s, r, call, put, i);
+        if (tid < (n & 3)) {
+            const int64_t i = (nv << 2) + tid;
+            const float sj = SIG_TAB ? sig[i] : sig_s;
+            bs_option<P>(S[i], K[i], T[i], sj, SIG_TAB ? inv_fast(sj) : inv_sig_s, r, call[i], put[i]);
+        }
+    }
 }
 
 // VEC: the tables are 16-byte aligned and the grid has one thread per float4
@@ -275,6 +366,33 @@ static int grid_for(KERN k, int64_t n)
     return persistent_blocks(k, 256, 0, 256 * 4, n);
 }
 
+// The pipelined kernel takes aligned batches from 2^22 options on: it keeps
+// bulk copies of three tiles per block in flight, which matches the
+// one-float4-per-thread kernel's throughput there (both are issue-bound at
+// ~98 instructions per option) while reading HBM through the copy engine;
+// below it the persistent grid's ramp costs more than it saves.
+constexpr int64_t kBsPipeMin = 1ll << 22;
+constexpr int kBsPipeStages = 3;
+
+template <class P, bool SIG_TAB, int STAGES>
+static nt2g_status launch_bs_pipe_n(const float *S, const float *K, const float *T, const float *sig, float sig_s,
+                                    float r, float *call, float *put, int64_t n, cudaStream_t st)
+{
+    const size_t smem = (size_t)STAGES * (SIG_TAB ? 4 : 3) * 256 * sizeof(float4) + STAGES * sizeof(uint64_t);
+    static const cudaError_t attr = cudaFuncSetAttribute(k_bs_pipe<P, SIG_TAB, STAGES>,
+                                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr != cudaSuccess) return cuda_status(attr, "blackscholes pipeline: shared memory");
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bs_pipe<P, SIG_TAB, STAGES>, 256, smem) !=
+            cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const int64_t tiles = n / 1024, full = (int64_t)device_sm_count() * per_sm;
+    const int grid = (int)(tiles < full ? tiles : full);
+    k_bs_pipe<P, SIG_TAB, STAGES><<<grid, 256, smem, st>>>(S, K, T, sig, sig_s, r, call, put, n);
+    NT2G_LAUNCH_CHECK("blackscholes pipeline launch");
+    return NT2G_OK;
+}
+
 nt2g_status launch_bs(const float *S, const float *K, const float *T, const float *sig, float sig_s, float r,
                       float *call, float *put, int64_t n, int precision, cudaStream_t st)
 {
@@ -289,6 +407,14 @@ nt2g_status launch_bs(const float *S, const float *K, const float *T, const floa
         else k_bs<PP, TAB, false><<<grid_for(k_bs<PP, TAB, false>, n), 256, 0, st>>>(S, K, T, sig, sig_s, r,   \
                                                                                       call, put, n);           \
     } while (0)
+    if (vec && n >= kBsPipeMin) {
+        constexpr int ST = kBsPipeStages;
+        if (precision == NT2G_PREC_NT2)
+            return sig ? launch_bs_pipe_n<Nt2, true, ST>(S, K, T, sig, sig_s, r, call, put, n, st)
+                       : launch_bs_pipe_n<Nt2, false, ST>(S, K, T, sig, sig_s, r, call, put, n, st);
+        return sig ? launch_bs_pipe_n<Fast, true, ST>(S, K, T, sig, sig_s, r, call, put, n, st)
+                   : launch_bs_pipe_n<Fast, false, ST>(S, K, T, sig, sig_s, r, call, put, n, st);
+    }
     if (precision == NT2G_PREC_NT2) {
         if (sig) NT2G_BS(Nt2, true);
         else NT2G_BS(Nt2, false);
@@ -298,6 +424,16 @@ nt2g_status launch_bs(const float *S, const float *K, const float *T, const floa
     }
 #undef NT2G_BS
     NT2G_LAUNCH_CHECK("blackscholes launch");
+    return NT2G_OK;
+}
+
+extern "C" nt2g_status nt2g_wait_timeouts(uint64_t *count)
+{
+    NT2G_CHECK_ARG(count != nullptr, "nt2g_wait_timeouts: count is NULL");
+    unsigned long long v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_bs_wait_timeouts, sizeof v);
+    if (e != cudaSuccess) return cuda_status(e, "nt2g_wait_timeouts");
+    *count = v;
     return NT2G_OK;
 }
 

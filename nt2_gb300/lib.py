@@ -114,6 +114,7 @@ _SIGNATURES = {
     "nt2g_host_access": (_I32, [ctypes.POINTER(_I32)]),
     "nt2g_fold_workspace_size": (_I32, [_I64, _I64, _I64, ctypes.POINTER(ctypes.c_size_t)]),
     "nt2g_fold_f32": (_I32, [_VP, _I64, _I64, _I64, _I32, _I32, _VP, ctypes.c_size_t, _VP, _VP, _VP]),
+    "nt2g_wait_timeouts": (_I32, [ctypes.POINTER(ctypes.c_uint64)]),
     "nt2g_program_vjp": (_I32, [_VP, ctypes.POINTER(Arg), _I32, _I64, ctypes.POINTER(_VP), ctypes.POINTER(_VP), _VP,
                                 _I32, _VP, ctypes.c_size_t, _VP]),
     "nt2g_program_vjp_workspace_size": (_I32, [_VP, _I64, ctypes.POINTER(ctypes.c_size_t)]),

@@ -239,3 +239,30 @@ def test_demo_form(lib, dev, oracle, prec):
     got = out.cpu().numpy()
     if prec == lib.PREC_NT2:
         assert _bits_equal(got, ref)
+
+
+@pytest.mark.parametrize("sigma_table", [False, True], ids=["sigma_scalar", "sigma_table"])
+def test_pipelined_kernel_tile_boundaries(lib, dev, oracle, sigma_table):
+    """The bulk-copy pipelined kernel (aligned tables of 2^22 options or more:
+    persistent blocks over tiles of 1024 options, the part past the last whole
+    tile priced with plain loads) at sizes around its tile boundaries and
+    either side of its threshold: NT2 policy bit-identical to the oracle, and
+    no bounded wait ever gave up."""
+    import ctypes
+    from helpers import bs_inputs
+    for n in (1025, (1 << 22) - 1, 1 << 22, (1 << 22) + 1023, (1 << 22) + 1024 * 777 + 3):
+        ins = bs_inputs(n, seed=n, sigma_table=sigma_table)
+        t = [torch.from_numpy(a).to(dev) for a in ins]
+        c, p = torch.empty_like(t[0]), torch.empty_like(t[0])
+        if sigma_table:
+            lib.blackscholes(t[0], t[1], t[2], c, p, 0.02, sigma=t[3], precision=lib.PREC_NT2)
+            rc, rp = oracle.blackscholes(ins[0], ins[1], ins[2], 0.02, ins[3])
+        else:
+            lib.blackscholes(t[0], t[1], t[2], c, p, 0.02, sigma_s=0.3, precision=lib.PREC_NT2)
+            rc, rp = oracle.blackscholes(ins[0], ins[1], ins[2], 0.02, 0.3)
+        torch.cuda.synchronize()
+        assert np.array_equal(c.cpu().numpy().view(np.uint32), rc.view(np.uint32)), n
+        assert np.array_equal(p.cpu().numpy().view(np.uint32), rp.view(np.uint32)), n
+    count = ctypes.c_uint64()
+    lib.check(lib.load().nt2g_wait_timeouts(ctypes.byref(count)))
+    assert count.value == 0
