@@ -329,11 +329,17 @@ __device__ __forceinline__ f2 exp_nt2_2(f2 a0, f2 nz)
     float k0, k1, a, b;
     upk(kf, k0, k1);
     upk(a0, a, b);
+    const f2 r = nmul2(c, pk(bits_f((uint32_t)((int32_t)k0 + 127) << 23), bits_f((uint32_t)((int32_t)k1 + 127) << 23)),
+                       nz);
+    // the special values (+inf from Maxlog, 0 from Minlog, NaN) only when a
+    // lane leaves (Minlog, Maxlog): one range test per lane on the common path
+    const bool in0 = a > bits_f(NT2G_MINLOG) && a < bits_f(NT2G_MAXLOG);
+    const bool in1 = b > bits_f(NT2G_MINLOG) && b < bits_f(NT2G_MAXLOG);
+    if (in0 && in1) return r;
     float r0, r1;
-    upk(nmul2(c, pk(bits_f((uint32_t)((int32_t)k0 + 127) << 23), bits_f((uint32_t)((int32_t)k1 + 127) << 23)), nz), r0,
-        r1);
-    auto fix = [](float a0s, float r) {
-        return (a0s >= bits_f(NT2G_MAXLOG)) ? f_inf() : (a0s <= bits_f(NT2G_MINLOG)) ? 0.0f : is_nan(a0s) ? a0s : r;
+    upk(r, r0, r1);
+    auto fix = [](float a0s, float v) {
+        return (a0s >= bits_f(NT2G_MAXLOG)) ? f_inf() : (a0s <= bits_f(NT2G_MINLOG)) ? 0.0f : is_nan(a0s) ? a0s : v;
     };
     return pk(fix(a, r0), fix(b, r1));
 }
@@ -364,6 +370,8 @@ __device__ __forceinline__ f2 log_nt2_2(f2 a0, f2 nz)
     y = nt2_fma2(fe, dup(bits_f(NT2G_LOG_2LO)), y, nz);
     y = nt2_fma2(dup(-0.5f), x2, y, nz);
     const f2 r = nt2_fma2(dup(bits_f(NT2G_LOG_2HI)), fe, add2(add2(x, y), t), nz);
+    // +inf, 0, negative and NaN arguments only when a lane is outside (0, +inf)
+    if (z0 > 0.0f && z0 < f_inf() && z1 > 0.0f && z1 < f_inf()) return r;
     float r0, r1;
     upk(r, r0, r1);
     auto fix = [](float a, float v) {

@@ -51,8 +51,6 @@ PRECS = [("fast", 0, 0, 0), ("nt2", 1, 1, 1), ("nt2_elements", 2, 1, 0)]  # (nam
 @pytest.mark.parametrize("op", ["sum", "max", "var", "nbtrue", "asum2"])
 def test_fused_fold_equals_fold_of_materialized(lib, dev, name, prec, elem, order, shape, op):
     lo, inner, hi = shape
-    if prec == 1 and lo * hi < 16 and inner > 1 << 16:
-        pytest.skip("NT2-order global fold of 2^20 elements: one thread, covered at 2^16 below")
     n = lo * inner * hi
     rng = np.random.default_rng(7 + n)
     x, y = _t(dev, rng.standard_normal(n, dtype=np.float32)), _t(dev, rng.standard_normal(n, dtype=np.float32))
