@@ -113,7 +113,9 @@ typedef enum nt2g_opcode {
     /* predicates of a float -> logical (boost/simd predicates: is_nan, is_inf, is_finite = x - x == 0,
        is_eqz, is_nez, is_ltz, is_gtz) */
     NT2G_OP_IS_NAN = 142, NT2G_OP_IS_INF, NT2G_OP_IS_FINITE, NT2G_OP_IS_EQZ, NT2G_OP_IS_NEZ, NT2G_OP_IS_LTZ,
-    NT2G_OP_IS_GTZ
+    NT2G_OP_IS_GTZ,
+    NT2G_OP_SIGNGAM = 149, /* sign of Gamma (NaN at the poles)             */
+    NT2G_OP_DIGAMMA = 150  /* psi = Gamma'/Gamma, NT2's double algorithm    */
 } nt2g_opcode;
 
 typedef struct nt2g_op {
@@ -375,7 +377,7 @@ nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8
  * 32 cosd, 33 tand, 34 tanpi, 35 cotpi, 36 cotd, 37 secpi, 38 cscpi, 39 secd, 40 cscd, 41 sinc,
  * 42 sincpi, 43 acotd, 44 asec, 45 coth, 46 sinhc, 47 acsc, 48 asech, 49 acoth, 50 acsch, 64 erf, 65 erfcx, 66 expx2, 67 gamma, 68 gammaln,
  * 69 erfinv, 70 erfcinv,
- * 80 exprecneg, 81 exprecnegc, 82 sqrt1pm1. */
+ * 71 digamma, 72 signgam, 80 exprecneg, 81 exprecnegc, 82 sqrt1pm1. */
 nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision,
                          void *stream);
 

@@ -433,6 +433,8 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 68) return gammaln<P>(a);
     if (FN == 69) return erfinv<P>(a);
     if (FN == 70) return erfcinv<P>(a);
+    if (FN == 71) return digamma<P>(a);
+    if (FN == 72) return signgam(a);
     if (FN == 80) return exprecneg<P>(a);
     if (FN == 81) return exprecnegc<P>(a);
     if (FN == 82) return sqrt1pm1<P>(a);
@@ -511,6 +513,8 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 68: NT2G_MAP(68); break;
     case 69: NT2G_MAP(69); break;
     case 70: NT2G_MAP(70); break;
+    case 71: NT2G_MAP(71); break;
+    case 72: NT2G_MAP(72); break;
     case 80: NT2G_MAP(80); break;
     case 81: NT2G_MAP(81); break;
     case 82: NT2G_MAP(82); break;
@@ -599,6 +603,8 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_GAMMALN: return gammaln<P>(a);
     case NT2G_OP_ERFINV: return erfinv<P>(a);
     case NT2G_OP_ERFCINV: return erfcinv<P>(a);
+    case NT2G_OP_SIGNGAM: return signgam(a);
+    case NT2G_OP_DIGAMMA: return digamma<P>(a);
     case NT2G_OP_FLOOR: return floorf(a);
     case NT2G_OP_CEIL: return ceilf(a);
     case NT2G_OP_TRUNC: return truncf(a);

@@ -271,6 +271,8 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         case NT2G_OP_EXPX2: e = "nt2g::expx2<P>(" + A + ")"; break;
         case NT2G_OP_GAMMA: e = "nt2g::gamma<P>(" + A + ")"; break;
         case NT2G_OP_GAMMALN: e = "nt2g::gammaln<P>(" + A + ")"; break;
+        case NT2G_OP_SIGNGAM: e = "nt2g::signgam(" + A + ")"; break;
+        case NT2G_OP_DIGAMMA: e = "nt2g::digamma<P>(" + A + ")"; break;
         case NT2G_OP_ERFINV: e = "nt2g::erfinv<P>(" + A + ")"; break;
         case NT2G_OP_ERFCINV: e = "nt2g::erfcinv<P>(" + A + ")"; break;
         case NT2G_OP_FLOOR: e = "floorf(" + A + ")"; break;
@@ -638,7 +640,7 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
     case NT2G_OP_IF_ELSE: to(o.b, "(" + A + " ? " + G + " : 0.0f)"); to(o.c, "(" + A + " ? 0.0f : " + G + ")"); break;
     case NT2G_OP_SELINC: case NT2G_OP_SELDEC: to(o.b, G); break;
     case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
-    case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: case NT2G_OP_IF_ZERO_ELSE_ONE:
+    case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: case NT2G_OP_IF_ZERO_ELSE_ONE: case NT2G_OP_SIGNGAM:
         break;  // piecewise constant: no gradient
     default: return false;
     }

@@ -1963,4 +1963,119 @@ template <class P> NT2G_HD float gammaln(float a0)
     return gammaln_pos<P>(a0);
 }
 
+// ------------------------------------------------------------- signgam --
+// NT2's sign of Gamma (EUL/scalar/signgam.hpp): NaN at the non-positive
+// integers and at -inf; below zero 1 - 2 is_odd(floor(x)), with boost.simd's
+// float is_odd(f) = is_flint((f - 1) * 1/2) and is_flint(y) = frac(y) == 0;
+// NaN passes through; 1 above zero.  Both policies.
+NT2G_HD float signgam(float a0)
+{
+    if (a0 <= 0.0f) {
+        if (a0 - truncf(a0) == 0.0f || a0 == -f_inf()) return f_nan();
+        const float h = (floorf(a0) - 1.0f) * 0.5f;
+        return (h - truncf(h) == 0.0f) ? -1.0f : 1.0f;
+    }
+    return is_nan(a0) ? a0 : 1.0f;
+}
+
+// ------------------------------------------------------------- digamma --
+// NT2's float digamma evaluates its double algorithm and rounds the result
+// (EUL/scalar/digamma.hpp: the single_ overload calls the double one), so
+// both policies do the same here.  The double algorithm, with NT2's unfused
+// double arithmetic: below 0 the reflection pi / tanpi(r) of the fractional
+// part of 1 - x (NaN at the poles); from Digammalargelim = 20 on the
+// asymptotic series of digamma_kernel::digamma_imp_large; otherwise down to
+// [1, 2] by psi(x) = psi(x - 1) + 1/(x - 1) (or up by -1/x) and NT2's
+// rational approximation digamma_1_2 about the root 1.4616..., held as three
+// parts (EUL/details/digamma_kernel.hpp).  NT2's double log and tanpi are
+// taken as the platform's double log and sinpi / cospi: the float result is
+// NT2's unless the two double values straddle a float rounding boundary.
+struct D64 {
+#if defined(__CUDA_ARCH__)
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+    static __device__ __forceinline__ double tanpi(double r) { return __ddiv_rn(::sinpi(r), ::cospi(r)); }
+#else
+    static inline double mul(double a, double b) { volatile double r = a * b; return r; }
+    static inline double add(double a, double b) { volatile double r = a + b; return r; }
+    static inline double sub(double a, double b) { volatile double r = a - b; return r; }
+    static inline double div(double a, double b) { volatile double r = a / b; return r; }
+    static inline double tanpi(double r)
+    {
+        return div(::sin(3.14159265358979323846 * r), ::cos(3.14159265358979323846 * r));
+    }
+#endif
+    static NT2G_HD double fma(double a, double b, double c) { return add(mul(a, b), c); }
+};
+
+NT2G_HD double bits_d(uint64_t u)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double d; memcpy(&d, &u, 8); return d;
+#endif
+}
+
+// Horner over NT2's coefficient order (highest degree first), unfused
+template <int N> NT2G_HD double horner_d(double x, const uint64_t (&c)[N])
+{
+    double acc = bits_d(c[0]);
+    for (int i = 1; i < N; ++i) acc = D64::fma(x, acc, bits_d(c[i]));
+    return acc;
+}
+
+NT2G_HD double digamma_d(double a0)
+{
+    const double pi = bits_d(0x400921fb54442d18ull);
+    double result = 0.0, x = a0;
+    if (a0 == 0.0) return ::copysign(bits_d(0x7ff0000000000000ull), a0);
+    if (x < 0.0) {
+        x = D64::sub(1.0, x);
+        result = D64::sub(x, ::floor(x));
+        if (result > 0.5) result = D64::sub(result, 1.0);
+        if (result == 0.5) result = 0.0;
+        else if (result != 0.0) result = D64::div(pi, D64::tanpi(result));
+        else result = bits_d(0x7ff8000000000000ull);
+    }
+    if (x >= 20.0) {  // digamma_imp_large
+        const uint64_t c[8] = {0xbfdc5e5e5e5e5e5eull, 0x3fb5555555555555ull, 0xbf95995995995996ull,
+                               0x3f7f07c1f07c1f08ull, 0xbf71111111111111ull, 0x3f70410410410410ull,
+                               0xbf81111111111111ull, 0x3fb5555555555555ull};
+        const double xm = D64::sub(x, 1.0);
+        double r = ::log(xm);
+        r = D64::add(r, D64::div(1.0, D64::mul(2.0, xm)));
+        const double z = D64::div(1.0, D64::mul(xm, xm));
+        r = D64::sub(r, D64::mul(z, horner_d(z, c)));
+        return D64::add(r, result);
+    }
+    while (x > 2.0) {
+        x = D64::sub(x, 1.0);
+        result = D64::add(result, D64::div(1.0, x));
+    }
+    if (x < 1.0) {
+        result = D64::div(-1.0, x);
+        x = D64::add(x, 1.0);
+    }
+    // digamma_1_2
+    const double Y = (double)0.99558162689208984f;
+    const double root1 = 1569415565.0 / 1073741824.0, root2 = (381566830.0 / 1073741824.0) / 1073741824.0,
+                 root3 = 0.9016312093258695918615325266959189453125e-19;
+    const uint64_t P6[6] = {0xbf60f7e5f66c2537ull, 0xbfa72b2e63723c78ull, 0xbfd2821c13c5e2bfull,
+                            0xbfe4cf68d26e295aull, 0xbfd4d5d0f9ab412full, 0x3fd04e9e69894978ull};
+    const uint64_t Q7[7] = {0xbea2b84f95bbf448ull, 0x3f616fc90a0a1908ull, 0x3fabb9c8cc612ca3ull,
+                            0x3fdbe65d28de361cull, 0x3ff75eb79397c930ull, 0x40009d1b06674d41ull,
+                            0x3ff0000000000000ull};
+    double g = D64::sub(x, root1);
+    g = D64::sub(g, root2);
+    g = D64::sub(g, root3);
+    const double xm = D64::sub(x, 1.0);
+    const double r = D64::div(horner_d(xm, P6), horner_d(xm, Q7));
+    return D64::add(D64::fma(g, Y, D64::mul(g, r)), result);
+}
+
+template <class P> NT2G_HD float digamma(float a0) { return (float)digamma_d((double)a0); }
+
 }  // namespace nt2g

@@ -115,6 +115,21 @@ erfcx = _un("ERFCX")
 expx2 = _un("EXPX2")
 gamma = _un("GAMMA")
 gammaln = _un("GAMMALN")
+digamma = _un("DIGAMMA")
+signgam = _un("SIGNGAM")
+
+
+# NT2's beta and betaln, built as NT2 writes them (EUL/scalar/beta.hpp:
+# sign*exp(gammaln(a0)+gammaln(a1)-gammaln(y)) with y = a0+a1 and sign =
+# signgam(a0)*signgam(a1)*signgam(y); EUL/simd/common/betaln.hpp:
+# gammaln(a0)+gammaln(a1)-gammaln(a0+a1))
+def beta(a, b):
+    y = a + b
+    return (signgam(a) * signgam(b)) * signgam(y) * exp(gammaln(a) + gammaln(b) - gammaln(y))
+
+
+def betaln(a, b):
+    return gammaln(a) + gammaln(b) - gammaln(a + b)
 erfinv = _un("ERFINV")
 erfcinv = _un("ERFCINV")
 floor = _un("FLOOR")

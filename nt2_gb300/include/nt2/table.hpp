@@ -662,6 +662,8 @@ NT2G_UNARY(erfcx, NT2G_OP_ERFCX)
 NT2G_UNARY(expx2, NT2G_OP_EXPX2)
 NT2G_UNARY(gamma, NT2G_OP_GAMMA)
 NT2G_UNARY(gammaln, NT2G_OP_GAMMALN)
+NT2G_UNARY(digamma, NT2G_OP_DIGAMMA)
+NT2G_UNARY(signgam, NT2G_OP_SIGNGAM)
 NT2G_UNARY(erfinv, NT2G_OP_ERFINV)
 NT2G_UNARY(erfcinv, NT2G_OP_ERFCINV)
 NT2G_UNARY(floor, NT2G_OP_FLOOR)
@@ -752,6 +754,22 @@ expr<T> logspace_sub(const A &a, const B &b)
     const expr<T> x{detail::any<T>(a)}, y{detail::any<T>(b)};
     const expr<T> d = y - x;
     return x + if_else(d > -detail::f32_of_bits(0x3f317218u), log(-expm1(d)), log1p(-exp(d)));
+}
+// beta and betaln (euler/functions/scalar/beta.hpp, simd/common/betaln.hpp):
+// sign*exp(gammaln(a)+gammaln(b)-gammaln(y)), y = a+b, sign the product of the
+// three signgam; betaln = gammaln(a)+gammaln(b)-gammaln(a+b)
+template <class A, class B, class T = typename detail::common<A, B>::type>
+expr<T> beta(const A &a, const B &b)
+{
+    const expr<T> x{detail::any<T>(a)}, w{detail::any<T>(b)};
+    const expr<T> y = x + w;
+    return signgam(x) * signgam(w) * signgam(y) * exp(gammaln(x) + gammaln(w) - gammaln(y));
+}
+template <class A, class B, class T = typename detail::common<A, B>::type>
+expr<T> betaln(const A &a, const B &b)
+{
+    const expr<T> x{detail::any<T>(a)}, w{detail::any<T>(b)};
+    return gammaln(x) + gammaln(w) - gammaln(x + w);
 }
 template <class A, class T = typename detail::elem_of<std::decay_t<A>>::type>
 expr<T> realsqrt(const A &a)

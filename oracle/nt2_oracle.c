@@ -1051,6 +1051,92 @@ EXPORT float o_gammaln(float a0)
     return r;
 }
 
+/* signgam EUL/scalar/signgam.hpp (floating_): NaN at the non-positive
+ * integers and -inf, 1 - 2 is_odd(floor(x)) below zero (boost.simd's float
+ * is_odd(f) = is_even(f - 1) = is_flint((f - 1) * 1/2), is_flint(y) = frac(y) == 0),
+ * NaN through, 1 above zero. */
+EXPORT float o_signgam(float a0)
+{
+    if (a0 <= 0.0f) {
+        if (a0 - truncf(a0) == 0.0f || a0 == -INFINITY) return NAN;
+        float h = (floorf(a0) - 1.0f) * 0.5f;
+        return (h - truncf(h) == 0.0f) ? -1.0f : 1.0f;
+    }
+    return isnan(a0) ? a0 : 1.0f;
+}
+
+/* digamma EUL/scalar/digamma.hpp: the float overload returns the double
+ * algorithm rounded (double_ overload), which reflects below zero
+ * (pi / tanpi of the fractional part of 1 - x), uses digamma_imp_large from
+ * Digammalargelim = 20 on, else reduces to [1, 2] and evaluates digamma_1_2
+ * (EUL/details/digamma_kernel.hpp, double coefficients by bit pattern).  The
+ * double log and tanpi are libm's (NT2's own double versions differ from
+ * them by an ulp of double at most). */
+static double horner_bd(double x, const uint64_t *c, int n)
+{
+    double acc = bd(c[0]);
+    for (int i = 1; i < n; ++i) acc = x * acc + bd(c[i]);
+    return acc;
+}
+EXPORT double o_digamma_d(double a0)
+{
+    static const uint64_t LARGE[8] = {0xbfdc5e5e5e5e5e5eull, 0x3fb5555555555555ull, 0xbf95995995995996ull,
+                                      0x3f7f07c1f07c1f08ull, 0xbf71111111111111ull, 0x3f70410410410410ull,
+                                      0xbf81111111111111ull, 0x3fb5555555555555ull};
+    static const uint64_t P6[6] = {0xbf60f7e5f66c2537ull, 0xbfa72b2e63723c78ull, 0xbfd2821c13c5e2bfull,
+                                   0xbfe4cf68d26e295aull, 0xbfd4d5d0f9ab412full, 0x3fd04e9e69894978ull};
+    static const uint64_t Q7[7] = {0xbea2b84f95bbf448ull, 0x3f616fc90a0a1908ull, 0x3fabb9c8cc612ca3ull,
+                                   0x3fdbe65d28de361cull, 0x3ff75eb79397c930ull, 0x40009d1b06674d41ull,
+                                   0x3ff0000000000000ull};
+    const double pi = bd(0x400921fb54442d18ull);
+    double result = 0.0, x = a0;
+    if (a0 == 0.0) return copysign(INFINITY, a0);
+    if (x < 0.0) {
+        x = 1.0 - x;
+        result = x - floor(x);
+        if (result > 0.5) result -= 1.0;
+        if (result == 0.5) result = 0.0;
+        else if (result != 0.0) result = pi / (sin(pi * result) / cos(pi * result));
+        else result = NAN;
+    }
+    if (x >= 20.0) {
+        double xm = x - 1.0, r = log(xm);
+        r += 1.0 / (2.0 * xm);
+        double z = 1.0 / (xm * xm);
+        r -= z * horner_bd(z, LARGE, 8);
+        return r + result;
+    }
+    while (x > 2.0) {
+        x -= 1.0;
+        result += 1.0 / x;
+    }
+    if (x < 1.0) {
+        result = -1.0 / x;
+        x += 1.0;
+    }
+    const double Y = (double)0.99558162689208984f;
+    const double root1 = 1569415565.0 / 1073741824.0, root2 = (381566830.0 / 1073741824.0) / 1073741824.0,
+                 root3 = 0.9016312093258695918615325266959189453125e-19;
+    double g = x - root1;
+    g -= root2;
+    g -= root3;
+    double xm = x - 1.0;
+    double r = horner_bd(xm, P6, 6) / horner_bd(xm, Q7, 7);
+    return (g * Y + g * r) + result;
+}
+EXPORT float o_digamma(float a0) { return (float)o_digamma_d((double)a0); }
+
+/* beta EUL/scalar/beta.hpp: sign*exp(gammaln(a0)+gammaln(a1)-gammaln(y)),
+ * y = a0+a1, sign = signgam(a0)*signgam(a1)*signgam(y); betaln
+ * EUL/simd/common/betaln.hpp: gammaln(a0)+gammaln(a1)-gammaln(a0+a1). */
+EXPORT float o_beta(float a0, float a1)
+{
+    float y = a0 + a1;
+    float sign = o_signgam(a0) * o_signgam(a1) * o_signgam(y);
+    return sign * o_exp(o_gammaln(a0) + o_gammaln(a1) - o_gammaln(y));
+}
+EXPORT float o_betaln(float a0, float a1) { return o_gammaln(a0) + o_gammaln(a1) - o_gammaln(a0 + a1); }
+
 /* erfinv EUL/scalar/erfinv.hpp, erfcinv EUL/scalar/erfcinv.hpp (single_, Giles),
  * kernels EUL/details/erfinv_kernel.hpp */
 static const uint32_t ERFINV1_P[9] = {0x32f16588, 0x34b84b36, 0xb66c7357, 0xb6935ac1, 0x396532db,
@@ -1138,7 +1224,8 @@ enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQR
        FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT, FN_COT, FN_SEC, FN_CSC, FN_SIND,
        FN_COSD, FN_TAND, FN_TANPI, FN_COTPI, FN_COTD, FN_SECPI, FN_CSCPI, FN_SECD, FN_CSCD, FN_SINC, FN_SINCPI,
        FN_ACOTD, FN_ASEC, FN_COTH, FN_SINHC, FN_ACSC, FN_ASECH, FN_ACOTH, FN_ACSCH,
-       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_ERFINV, FN_ERFCINV, FN_EXPRECNEG = 80, FN_EXPRECNEGC,
+       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_ERFINV, FN_ERFCINV, FN_DIGAMMA, FN_SIGNGAM,
+       FN_EXPRECNEG = 80, FN_EXPRECNEGC,
        FN_SQRT1PM1,
        /* compositions of the above, oracle only (the front ends lower them to programs) */
        FN_SECH = 51, FN_CSCH, FN_ACOT, FN_ASIND, FN_ACOSD, FN_ATAND, FN_ASECD, FN_ACSCD, FN_ASINPI, FN_ACOSPI,
@@ -1216,6 +1303,8 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_EXPX2: y[i] = o_expx2(a); break;
         case FN_GAMMA: y[i] = o_gamma(a); break;
         case FN_GAMMALN: y[i] = o_gammaln(a); break;
+        case FN_DIGAMMA: y[i] = o_digamma(a); break;
+        case FN_SIGNGAM: y[i] = o_signgam(a); break;
         case FN_ERFINV: y[i] = o_erfinv(a); break;
         case FN_ERFCINV: y[i] = o_erfcinv(a); break;
         case FN_EXPRECNEG: y[i] = o_exprecneg(a); break;
@@ -1372,6 +1461,8 @@ EXPORT void o_map_f64(int fn, const float *x, double *y, int64_t n)
         case FN_EXPX2: y[i] = exp(a * a); break;
         case FN_GAMMA: y[i] = tgamma(a); break;
         case FN_GAMMALN: y[i] = lgamma(a); break;
+        case FN_DIGAMMA: y[i] = o_digamma_d(a); break;
+        case FN_SIGNGAM: y[i] = o_signgam((float)a); break;
         case FN_ERFINV: y[i] = erfinv_d(a); break;
         case FN_ERFCINV: y[i] = erfcinv_d(a); break;
         case FN_EXPRECNEG: y[i] = exp(-1.0 / a); break;

@@ -404,3 +404,23 @@ def test_vjp_validates_slots(lib):
     tg[sy] = None
     assert L.nt2g_program_vjp(prog.handle, args, len(slots), -1, ct, tg, None, 0, None, 0, None) == lib.ERR_INVALID
     assert L.nt2g_program_vjp(prog.handle, args, len(slots), 0, ct, tg, None, 7, None, 0, None) == lib.ERR_INVALID
+
+
+def test_digamma_signgam_programs_compile_and_vjp_refuses_digamma(lib):
+    """A program using digamma (double arithmetic inside), signgam and NT2's
+    beta composition compiles for sm_103a; digamma has no adjoint rule, so
+    its reverse mode is refused with NT2G_ERR_UNSUPPORTED, while signgam
+    (piecewise constant) differentiates to zero."""
+    nv = _nvrtc()
+    x, y = E.Table(torch.zeros(8)), E.Table(torch.zeros(8))
+    prog, _ = E.compile_program([torch.zeros(8), torch.zeros(8)], [E.beta(x, y), E.digamma(x) + E.signgam(y)])
+    for prec in (lib.PREC_FAST, lib.PREC_NT2):
+        rc, log, size = _nvrtc_compile(nv, prog.jit_source(prec))
+        assert rc == 0, log[:2000]
+    n = ctypes.c_size_t()
+    assert lib.load().nt2g_program_vjp_source(prog.handle, 0, None, 0, ctypes.byref(n)) == lib.ERR_UNSUPPORTED
+    assert b"opcode 150" in lib.load().nt2g_last_error()
+    sg, _ = E.compile_program([torch.zeros(8)], [E.signgam(x) * E.exp(y)])
+    src = sg.vjp_source(0)
+    rc, log, size = _nvrtc_compile(nv, src)
+    assert rc == 0, log[:2000]

@@ -161,3 +161,59 @@ def test_logspace_and_real_aliases(lib, dev, oracle, prec):
         E.assign([ty], [getattr(E, name)(E.Table(ta), E.Table(tb))], precision=prec)
         for g, r in zip(ty.cpu().numpy(), recs):
             assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
+def test_digamma_signgam_beta_betaln(lib, dev, oracle, prec):
+    """digamma (NT2's double algorithm rounded to float, in both policies) and
+    signgam: bit-identical to the oracle; beta and betaln as NT2 composes them
+    (signgam, gammaln, exp): bit-identical to the oracle under the NT2 policy,
+    within a few ulp of the cancelling gammaln terms of FP64 under the fast
+    one; NT2's own known answers (digamma.cpp, signgam.cpp, beta.cpp,
+    betaln.cpp) in both."""
+    from nt2_gb300 import expr as E
+    rng = np.random.default_rng(21)
+    x = np.concatenate([rng.uniform(-30, 40, 1 << 17), np.exp(rng.uniform(-20, 30, 1 << 15)), SPECIALS,
+                        -SPECIALS, np.arange(-8, 9, dtype=np.float64)]).astype(np.float32)
+    for fn in ("digamma", "signgam"):
+        got = _run(lib, dev, fn, x, prec)
+        ref = oracle.map_f32(fn, x)
+        same = _same(got, ref)
+        assert same.all(), (fn, x[~same][:5], got[~same][:5], ref[~same][:5])
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
+    for fn in ("digamma", "signgam"):
+        rs = [r for r in golden if r["fn"] == fn]
+        assert len(rs) >= 4
+        got = _run(lib, dev, fn, np.float32([r["x"] for r in rs]), prec)
+        for g, r in zip(got, rs):
+            assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+    a = np.concatenate([rng.uniform(0.1, 12, 1 << 16), rng.uniform(-6, 6, 1 << 12)]).astype(np.float32)
+    b = np.concatenate([rng.uniform(0.1, 12, 1 << 16), rng.uniform(-6, 6, 1 << 12)]).astype(np.float32)
+    ta, tb = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+    ob, ol = torch.empty_like(ta), torch.empty_like(ta)
+    E.assign([ob, ol], [E.beta(E.Table(ta), E.Table(tb)), E.betaln(E.Table(ta), E.Table(tb))], precision=prec)
+    got_b, got_l = ob.cpu().numpy(), ol.cpu().numpy()
+    L = oracle.lib()
+    want_b = np.float32([L.o_beta(float(p), float(q)) for p, q in zip(a, b)])
+    want_l = np.float32([L.o_betaln(float(p), float(q)) for p, q in zip(a, b)])
+    if prec == 1:
+        assert _same(got_b, want_b).all() and _same(got_l, want_l).all()
+    else:
+        sp = pytest.importorskip("scipy.special")
+        pos = (a > 0) & (b > 0)
+        a64, b64 = a[pos].astype(np.float64), b[pos].astype(np.float64)
+        terms = np.abs(sp.gammaln(a64)) + np.abs(sp.gammaln(b64)) + np.abs(sp.gammaln(a64 + b64))
+        eps = float(np.finfo(np.float32).eps)
+        assert np.max(np.abs(got_l[pos] - sp.betaln(a64, b64)) / terms) < 8 * eps
+        rb = sp.beta(a64, b64)
+        assert np.max(np.abs(got_b[pos] - rb) / np.abs(rb) / np.maximum(terms, 1.0)) < 16 * eps
+        assert np.array_equal(np.isnan(got_b), np.isnan(want_b))
+    for fn, out in (("beta", got_b), ("betaln", got_l)):
+        rs = [r for r in golden if r["fn"] == fn]
+        assert len(rs) >= 2
+        tx = torch.tensor([r["x"] for r in rs], dtype=torch.float32, device=dev)
+        ty = torch.tensor([r["y"] for r in rs], dtype=torch.float32, device=dev)
+        o = torch.empty_like(tx)
+        E.assign([o], [getattr(E, fn)(E.Table(tx), E.Table(ty))], precision=prec)
+        for g, r in zip(o.cpu().numpy(), rs):
+            assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)

@@ -20,7 +20,7 @@ FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1
          "coth", "sinhc", "sech", "csch", "asech", "acsch", "acoth",
          "floor", "ceil", "trunc", "round", "frac", "sign", "signnz", "sqr_abs",
          "erf", "erfcx", "gamma", "gammaln", "erfinv", "erfcinv", "expx2", "exprecneg", "exprecnegc", "sqrt1pm1",
-         "realsqrt", "reallog")
+         "realsqrt", "reallog", "digamma", "signgam")
 # NT2's Nan<T>() has every bit set (its sign bit too): copysign(1, Nan) is -1
 NT2_NAN = float(np.uint32(0xffffffff).view(np.float32))
 
@@ -37,7 +37,8 @@ def test_oracle_matches_nt2_unit_tests(oracle, rec):
 
 
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("pow", "atan2", "atan2d", "hypot", "logspace_add",
-                                                              "logspace_sub", "copysign", "dist", "average")],
+                                                              "logspace_sub", "copysign", "dist", "average", "beta",
+                                                              "betaln")],
                          ids=lambda r: f"{r['fn']}({r['x']},{r['y']})@{r['source'].split('/')[-1]}")
 def test_oracle_binary_matches_nt2_unit_tests(oracle, rec):
     got = getattr(oracle.lib(), "o_" + rec["fn"])(_arg(rec["x"]), _arg(rec["y"]))
@@ -232,3 +233,45 @@ def test_nt2_transform_grain_rule(oracle):
     g = oracle.nt2_transform_grain(4)
     assert g >= 1
     assert not math.isnan(g)
+
+
+def test_oracle_digamma_against_fp64_and_nt2s_boost_points(oracle):
+    """digamma: NT2's double algorithm rounded to float, against scipy's FP64
+    digamma -- within 1 ulp away from the root and the poles -- and at the
+    points NT2's unit test checks against Boost.Math (digamma.cpp:40-44, 0.5
+    NT2-ulp; 7.5 at the root 1.4616...), whose expected values need Boost and
+    so come from scipy here."""
+    sp = pytest.importorskip("scipy.special")
+    rng = np.random.default_rng(5)
+    x = np.concatenate([rng.uniform(-20, 40, 200000), np.exp(rng.uniform(-10, 12, 100000))]).astype(np.float32)
+    x = x[np.abs(x - np.round(x)) > 1e-3]  # off the poles
+    ref = sp.digamma(x.astype(np.float64))
+    got = oracle.map_f32("digamma", x)
+    ok = np.abs(ref) > 1e-3  # relative error is meaningless at the root
+    assert std_ulp(got[ok], ref[ok]).max() <= 1.0
+    for v, tol in ((1.0, 0.5), (1.4669020846486091614, 0.5), (1.461632133, 7.5), (-3.5, 0.5), (-3.51, 0.5)):
+        f = np.float32(v)
+        assert nt2_ulpdist(oracle.lib().o_digamma(f), np.float32(sp.digamma(float(f)))) <= tol, v
+
+
+def test_oracle_signgam_and_beta(oracle):
+    """signgam against the sign of FP64 Gamma; beta and betaln as NT2 composes
+    them, against FP64 (scipy), within a few ulp of the gammaln terms they
+    cancel."""
+    sp = pytest.importorskip("scipy.special")
+    rng = np.random.default_rng(6)
+    x = rng.uniform(-30, 30, 100000).astype(np.float32)
+    x = x[np.abs(x - np.round(x)) > 1e-4]
+    got = np.array([oracle.lib().o_signgam(float(v)) for v in x[:20000]])
+    assert np.array_equal(got, np.sign(sp.gamma(x[:20000].astype(np.float64))))
+    a, b = rng.uniform(0.5, 8, 5000).astype(np.float32), rng.uniform(0.5, 8, 5000).astype(np.float32)
+    be = np.array([oracle.lib().o_beta(float(p), float(q)) for p, q in zip(a, b)])
+    bl = np.array([oracle.lib().o_betaln(float(p), float(q)) for p, q in zip(a, b)])
+    a64, b64 = a.astype(np.float64), b.astype(np.float64)
+    rb, rl = sp.beta(a64, b64), sp.betaln(a64, b64)
+    # NT2's form cancels three gammaln terms: the error is a few ulp of their
+    # size, absolute for betaln and relative (through exp) for beta
+    terms = np.abs(sp.gammaln(a64)) + np.abs(sp.gammaln(b64)) + np.abs(sp.gammaln(a64 + b64))
+    eps = float(np.finfo(np.float32).eps)
+    assert np.max(np.abs(bl - rl) / terms) < 4 * eps
+    assert np.max(np.abs(be - rb) / np.abs(rb) / np.maximum(terms, 1.0)) < 8 * eps
