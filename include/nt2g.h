@@ -216,7 +216,8 @@ typedef enum nt2g_fold_op {
     NT2G_FOLD_ANY = 14,    /* 1 if some element is nonzero                    */
     NT2G_FOLD_NONE = 15,   /* 1 if no element is nonzero                      */
     NT2G_FOLD_NANSUM = 16, /* sum of the non-NaN elements                     */
-    NT2G_FOLD_NANMEAN = 17 /* nansum / max(number of non-NaN elements, 1)     */
+    NT2G_FOLD_NANMEAN = 17, /* nansum / max(number of non-NaN elements, 1)    */
+    NT2G_FOLD_MEANAD = 18   /* mean(abs(a - mean(a))) (NT2's meanad)          */
 } nt2g_fold_op;
 
 nt2g_status nt2g_fold_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);

@@ -847,7 +847,7 @@ extern "C" nt2g_status nt2g_eval_fold(const nt2g_program *p, const nt2g_arg *arg
                    "nt2g_eval_fold: %d arguments for %d slots", n_args, p->n_slots);
     NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_eval_fold: negative extent (%lld, %lld, %lld)",
                    (long long)lo, (long long)inner, (long long)hi);
-    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_NANMEAN, "nt2g_eval_fold: op %d", op);
+    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_MEANAD, "nt2g_eval_fold: op %d", op);
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2 || precision == NT2G_PREC_NT2_ELEMENTS,
                    "nt2g_eval_fold: precision %d", precision);
     NT2G_CHECK_ARG(index == nullptr || op == NT2G_FOLD_MAX || op == NT2G_FOLD_MIN,
@@ -861,7 +861,8 @@ extern "C" nt2g_status nt2g_eval_fold(const nt2g_program *p, const nt2g_arg *arg
     if (n_out == 0) return NT2G_OK;
     NT2G_CHECK_ARG(out != nullptr, "nt2g_eval_fold: out is NULL");
     size_t need = 0;
-    const bool centred = (op >= NT2G_FOLD_VAR && op <= NT2G_FOLD_STDEV1) || op == NT2G_FOLD_NANMEAN;
+    const bool centred = (op >= NT2G_FOLD_VAR && op <= NT2G_FOLD_STDEV1) || op == NT2G_FOLD_NANMEAN ||
+                         op == NT2G_FOLD_MEANAD;
     if (centred) fold_workspace_bytes(lo, inner, hi, &need);
     else fold_partials_bytes(lo, inner, hi, &need);
     NT2G_CHECK_ARG((precision == NT2G_PREC_NT2 && !centred) || need == 0 ||
@@ -968,7 +969,7 @@ extern "C" nt2g_status nt2g_program_fold_source(const nt2g_program *p, int32_t p
     NT2G_CHECK_ARG(p->folds, "nt2g_program_fold_source: the program has no FOLD instruction");
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2 || precision == NT2G_PREC_NT2_ELEMENTS,
                    "nt2g_program_fold_source: precision %d", precision);
-    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_NANMEAN, "nt2g_program_fold_source: op %d", op);
+    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_MEANAD, "nt2g_program_fold_source: op %d", op);
     NT2G_CHECK_ARG(buf != nullptr || cap == 0, "nt2g_program_fold_source: NULL buffer");
     std::string src = jit_fold_source(p->ops, p->logical, precision, op);
     if (len) *len = src.size() + 1;
@@ -1124,7 +1125,7 @@ extern "C" nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, 
 {
     NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_fold_f32: negative extent (%lld, %lld, %lld)",
                    (long long)lo, (long long)inner, (long long)hi);
-    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_NANMEAN, "nt2g_fold_f32: op %d", op);
+    NT2G_CHECK_ARG(op >= NT2G_FOLD_SUM && op <= NT2G_FOLD_MEANAD, "nt2g_fold_f32: op %d", op);
     NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_fold_f32: precision %d",
                    precision);
     NT2G_CHECK_ARG(index == nullptr || op == NT2G_FOLD_MAX || op == NT2G_FOLD_MIN,
@@ -1135,7 +1136,8 @@ extern "C" nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, 
     NT2G_CHECK_ARG(x != nullptr || inner == 0, "nt2g_fold_f32: x is NULL");
     size_t need = 0;
     // var/stdev keep each output's centre in the workspace, nanmean its count
-    const bool centred = (op >= NT2G_FOLD_VAR && op <= NT2G_FOLD_STDEV1) || op == NT2G_FOLD_NANMEAN;
+    const bool centred = (op >= NT2G_FOLD_VAR && op <= NT2G_FOLD_STDEV1) || op == NT2G_FOLD_NANMEAN ||
+                         op == NT2G_FOLD_MEANAD;
     if (centred) fold_workspace_bytes(lo, inner, hi, &need);
     else fold_partials_bytes(lo, inner, hi, &need);
     NT2G_CHECK_ARG((precision == NT2G_PREC_NT2 && !centred) || need == 0 ||

@@ -26,7 +26,8 @@ static_assert((int)SUM == (int)NT2G_FOLD_SUM &&
               (int)ANY == (int)NT2G_FOLD_ANY &&
               (int)NONE == (int)NT2G_FOLD_NONE &&
               (int)NANSUM == (int)NT2G_FOLD_NANSUM &&
-              (int)NANMEAN == (int)NT2G_FOLD_NANMEAN,
+              (int)NANMEAN == (int)NT2G_FOLD_NANMEAN &&
+              (int)MEANAD == (int)NT2G_FOLD_MEANAD,
               "fold op numbering");
 
 constexpr int kFoldThreads = kThreads;
@@ -357,7 +358,7 @@ static nt2g_status fold_dispatch(const FoldInput &in, int64_t lo, int64_t inner,
     NT2G_OP_CASE(SUM) NT2G_OP_CASE(PROD) NT2G_OP_CASE(MAX) NT2G_OP_CASE(MIN) NT2G_OP_CASE(MEAN)
     NT2G_OP_CASE(ASUM1) NT2G_OP_CASE(ASUM2) NT2G_OP_CASE(NORM2) NT2G_OP_CASE(VAR) NT2G_OP_CASE(STDEV)
     NT2G_OP_CASE(VAR1) NT2G_OP_CASE(STDEV1) NT2G_OP_CASE(NBTRUE) NT2G_OP_CASE(ALL) NT2G_OP_CASE(ANY)
-    NT2G_OP_CASE(NONE) NT2G_OP_CASE(NANSUM)
+    NT2G_OP_CASE(NONE) NT2G_OP_CASE(NANSUM) NT2G_OP_CASE(MEANAD)
     default: return launch_fold_op<NANMEAN>(in, lo, inner, hi, ws, ws_bytes, out, index, out64, st);
     }
 #undef NT2G_OP_CASE

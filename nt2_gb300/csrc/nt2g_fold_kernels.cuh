@@ -58,7 +58,7 @@ namespace fold {
 // run-time compiled source cannot include the C header)
 enum : int {
     SUM = 0, PROD = 1, MAX = 2, MIN = 3, MEAN = 4, ASUM1 = 5, ASUM2 = 6, NORM2 = 7, VAR = 8, STDEV = 9,
-    VAR1 = 10, STDEV1 = 11, NBTRUE = 12, ALL = 13, ANY = 14, NONE = 15, NANSUM = 16, NANMEAN = 17,
+    VAR1 = 10, STDEV1 = 11, NBTRUE = 12, ALL = 13, ANY = 14, NONE = 15, NANSUM = 16, NANMEAN = 17, MEANAD = 18,
     // internal: the mean of each output written with the rounding error of its
     // float value (the centre of a fast-policy variance); the count of non-NaN
     // elements (the divisor of nanmean)
@@ -70,12 +70,14 @@ constexpr int kThreads = 256;
 __host__ __device__ constexpr bool is_var(int op) { return op == VAR || op == STDEV || op == VAR1 || op == STDEV1; }
 // counts of elements: nbtrue and the logical folds all/any/none over x != 0
 __host__ __device__ constexpr bool is_count(int op) { return op == NBTRUE || op == ALL || op == ANY || op == NONE; }
+// folds of the deviations from each output's mean
+__host__ __device__ constexpr bool is_centred(int op) { return is_var(op) || op == MEANAD; }
 // folds that need a per-output value from a first pass (the centre, the count)
-__host__ __device__ constexpr bool is_two_pass(int op) { return is_var(op) || op == NANMEAN; }
+__host__ __device__ constexpr bool is_two_pass(int op) { return is_centred(op) || op == NANMEAN; }
 __host__ __device__ constexpr bool is_sum(int op)
 {
     return op == SUM || op == MEAN || op == ASUM1 || op == ASUM2 || op == NORM2 || op == MEAN_C || is_var(op) ||
-           is_count(op) || op == NANSUM || op == NANMEAN || op == NOT_NAN;
+           is_count(op) || op == NANSUM || op == NANMEAN || op == NOT_NAN || op == MEANAD;
 }
 
 // max/min in NT2's order: the fold keeps acc unless x is strictly better, so
@@ -154,10 +156,19 @@ template <int OP> __device__ __forceinline__ void sum_elem(CSum &a, float x)
 
 // variance terms: (x - m)^2 with the difference kept exactly as dh + dl
 // (TwoSum) and the square's rounding error carried, so the sum of squared
-// deviations is compensated like the other sums
-template <int OP> __device__ __forceinline__ void sum_elem_c(CSum &a, float x, float m)
+// deviations is compensated like the other sums.  Mean absolute deviation
+// terms: |x - mu| with mu = m + md (the float mean and its rounding error),
+// as |dh| plus the low part dl - md with the sign of dh (|lo| where dh is 0).
+template <int OP> __device__ __forceinline__ void sum_elem_c(CSum &a, float x, float m, float md = 0.0f)
 {
-    if constexpr (is_var(OP)) {
+    if constexpr (OP == MEANAD) {
+        const float dh = __fsub_rn(x, m);
+        const float bb = __fsub_rn(dh, x);
+        const float dl = __fadd_rn(__fsub_rn(x, __fsub_rn(dh, bb)), __fsub_rn(-m, bb));
+        const float lo = __fsub_rn(dl, md);
+        csum_add(a, fabsf(dh));
+        a.c = __fadd_rn(a.c, dh > 0.0f ? lo : dh < 0.0f ? -lo : fabsf(lo));
+    } else if constexpr (is_var(OP)) {
         const float dh = __fsub_rn(x, m);
         const float bb = __fsub_rn(dh, x);
         const float dl = __fadd_rn(__fsub_rn(x, __fsub_rn(dh, bb)), __fsub_rn(-m, bb));
@@ -180,7 +191,7 @@ struct Partial {
 // float output: mean = t/n, norm2 = sqrt(t), a count or a sum as is.
 template <int OP> __device__ __forceinline__ double finish_double(double t, int64_t inner)
 {
-    if (OP == MEAN) return t / (double)inner;
+    if (OP == MEAN || OP == MEANAD) return t / (double)inner;
     if (OP == NORM2) return sqrt(t);
     return t;
 }
@@ -260,10 +271,11 @@ __device__ __forceinline__ void inner_body(const Src &src, int64_t inner, int64_
         const int64_t base = seg * inner;
         CSum acc{0.0f, 0.0f};
         double prod = 1.0;
-        const float m = is_var(OP) ? cen[seg] : 0.0f;
+        const float m = is_centred(OP) ? cen[seg] : 0.0f;
+        const float md = OP == MEANAD ? cen[hi + seg] : 0.0f;
         Run<OP == MAX, IDX> run[4];  // one per float4 component: four independent chains
         auto take = [&](int cc, float v, int32_t k) {  // k: position relative to k0
-            if (is_sum(OP)) sum_elem_c<OP>(acc, v, m);
+            if (is_sum(OP)) sum_elem_c<OP>(acc, v, m, md);
             else if (OP == PROD) prod *= (double)v;
             else run[cc].add(v, k);
         };
@@ -314,10 +326,11 @@ __device__ __forceinline__ void short_body(const Src &src, int64_t inner, int64_
         CSum acc{0.0f, 0.0f};
         double prod = 1.0;
         Run<OP == MAX> run;
-        const float m = is_var(OP) ? cen[seg] : 0.0f;
+        const float m = is_centred(OP) ? cen[seg] : 0.0f;
+        const float md = OP == MEANAD ? cen[hi + seg] : 0.0f;
         for (int64_t k = 0; k < inner; ++k) {
             const float v = src.at(base + k);
-            if (is_sum(OP)) sum_elem_c<OP>(acc, v, m);
+            if (is_sum(OP)) sum_elem_c<OP>(acc, v, m, md);
             else if (OP == PROD) prod *= (double)v;
             else run.add(v, (int32_t)k);
         }
@@ -349,12 +362,13 @@ __device__ __forceinline__ void outer_body(const Src &src, int64_t lo, int64_t i
         CSum acc[VEC];
         double prod[VEC];
         Run<OP == MAX> run[VEC];
-        float m[VEC];
+        float m[VEC], md[VEC];
 #pragma unroll
         for (int v = 0; v < VEC; ++v) {
             acc[v] = CSum{0.0f, 0.0f};
             prod[v] = 1.0;
-            m[v] = is_var(OP) ? cen[l + v + lo * h] : 0.0f;
+            m[v] = is_centred(OP) ? cen[l + v + lo * h] : 0.0f;
+            md[v] = OP == MEANAD ? cen[lo * hi + l + v + lo * h] : 0.0f;
         }
         for (int64_t k = k0; k < k1; ++k) {
             float e[VEC];
@@ -366,7 +380,7 @@ __device__ __forceinline__ void outer_body(const Src &src, int64_t lo, int64_t i
             }
 #pragma unroll
             for (int v = 0; v < VEC; ++v) {
-                if (is_sum(OP)) sum_elem_c<OP>(acc[v], e[v], m[v]);
+                if (is_sum(OP)) sum_elem_c<OP>(acc[v], e[v], m[v], md[v]);
                 else if (OP == PROD) prod[v] *= (double)e[v];
                 else run[v].add(e[v], (int32_t)(k - k0));
             }
@@ -410,6 +424,10 @@ __device__ __forceinline__ void nt2_body(const Src &src, int64_t lo, int64_t inn
                 acc = __fadd_rn(acc, __fmul_rn(d, d));
                 continue;
             }
+            if constexpr (OP == MEANAD) {  // sum(abs(center(a))) in order
+                acc = __fadd_rn(acc, fabsf(__fsub_rn(v, m)));
+                continue;
+            }
             if constexpr (is_count(OP)) {  // nbtrue: the sum of is_nez(x)
                 acc = __fadd_rn(acc, v != 0.0f ? 1.0f : 0.0f);
                 continue;
@@ -431,7 +449,7 @@ __device__ __forceinline__ void nt2_body(const Src &src, int64_t lo, int64_t inn
             default: acc = __fadd_rn(acc, v); break;
             }
         }
-        if (OP == MEAN) acc = __fmul_rn(__fdiv_rn(1.0f, (float)inner), acc);
+        if (OP == MEAN || OP == MEANAD) acc = __fmul_rn(__fdiv_rn(1.0f, (float)inner), acc);  // mean: rec(n) * sum
         if (OP == NORM2) acc = __fsqrt_rn(acc);
         if constexpr (is_count(OP)) {
             const float n = (float)inner;

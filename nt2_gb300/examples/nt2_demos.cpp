@@ -274,6 +274,11 @@ int main(int argc, char **argv)
             save(dir + "cummax2.bin", nt2::cummax(A, 2));
             save(dir + "var1.bin", nt2::var(A, 0, 1));
             save(dir + "stdev2_w1.bin", nt2::stdev(A, 1, 2));
+            save(dir + "meanad1.bin", nt2::meanad(A, 1));
+            save(dir + "meanad2.bin", nt2::meanad(A, 2));
+            dtable W;
+            W = nt2::abs(A);
+            save(dir + "wmean1.bin", nt2::wmean(A, W, 1));
             std::int64_t imax = 0, imin = 0;
             const float gmax = nt2::globalmax(A, imax), gmin = nt2::globalmin(h, imin);
             std::printf("globalmax %.9g %lld\nglobalmin %.9g %lld\nglobalmean %.9g\nglobalnorm2 %.9g\n"

@@ -616,6 +616,20 @@ def batch_item(outs, exprs):
     return it, prog, args
 
 
+def wmean(a, w, shape=None, precision=lib.PREC_FAST):
+    """NT2's wmean(a, w, dim) (reduction/functions/expr/wmean.hpp):
+    rec(globalsum(w)) times the fold of a .* w along the view's inner
+    dimension (shape = (lo, inner, hi), default every element), the product
+    folded in one pass and the scaling by this library's multiply."""
+    import numpy as np
+    import torch
+    f = np.float32(1.0) / np.float32(fold(Table(w), "sum", precision=precision).item())
+    s = fold(Table(a) * Table(w), "sum", shape, precision=precision)
+    out = torch.empty_like(s)
+    assign([out], [Scalar(float(f)) * Table(s)], precision=precision)
+    return out
+
+
 def batch_source(programs, precision=lib.PREC_FAST, block_threads=256):
     """CUDA source of the batch kernel that links these programs."""
     L, n = lib.load(), ctypes.c_size_t()

@@ -1317,7 +1317,23 @@ NT2G_DIM_FOLD(any, NT2G_FOLD_ANY)
 NT2G_DIM_FOLD(none, NT2G_FOLD_NONE)
 NT2G_DIM_FOLD(nansum, NT2G_FOLD_NANSUM)
 NT2G_DIM_FOLD(nanmean, NT2G_FOLD_NANMEAN)
+NT2G_DIM_FOLD(meanad, NT2G_FOLD_MEANAD)  // mean(abs(center(t, dim)), dim) (reduction/functions/expr/meanad.hpp)
 #undef NT2G_DIM_FOLD
+
+// wmean(t, w[, dim]) (reduction/functions/expr/wmean.hpp): rec(globalsum(w))
+// times sum(t .* w, dim), the product folded in one pass
+template <class Site> table<float, device_> wmean(const table<float, Site> &t, const table<float, Site> &w, int dim)
+{
+    const float f = 1.0f / globalsum(w);
+    const table<float, device_> s = sum(t * w, dim);
+    table<float, device_> r(s.extent());
+    r = f * s;
+    return r;
+}
+template <class Site> table<float, device_> wmean(const table<float, Site> &t, const table<float, Site> &w)
+{
+    return wmean(t, w, detail::first_non_singleton(t.extent()));
+}
 
 template <class Site> table<float, Site> var(const table<float, Site> &t, int w = 0)
 {

@@ -217,7 +217,7 @@ def map_f32(fn, x, y, precision=PREC_FAST, stream=None):
 
 
 FOLD = {"sum": 0, "prod": 1, "max": 2, "min": 3, "mean": 4, "asum1": 5, "asum2": 6, "norm2": 7, "var": 8, "stdev": 9,
-        "var1": 10, "stdev1": 11, "nbtrue": 12, "all": 13, "any": 14, "none": 15, "nansum": 16, "nanmean": 17}
+        "var1": 10, "stdev1": 11, "nbtrue": 12, "all": 13, "any": 14, "none": 15, "nansum": 16, "nanmean": 17, "meanad": 18}
 
 
 def fold(x, lo, inner, hi, op, precision=PREC_FAST, index=False, stream=None):

@@ -1825,7 +1825,8 @@ EXPORT double o_exact_sum(const float *x, const float *y, int64_t n, int nthread
  * mean = rec(float(n)) * sum (core/functions/expr/mean.hpp:22-33),
  * asum2 = sum(sqr_abs), norm2 = sqrt(asum2), var = f * asum2(a - mean(a)) with
  * f = rec(n - 1) (ops 8, 9; rec(n) for 10, 11; 1 when n <= 1) and stdev = sqrt(var)
- * (core/functions/expr/var.hpp, expr/stdev.hpp).  index: first position equal to
+ * (core/functions/expr/var.hpp, expr/stdev.hpp), meanad = mean(abs(a - mean(a)))
+ * (op 18, core/functions/expr/meanad.hpp).  index: first position equal to
  * the result (common/globalmax.hpp:36-48), -1 if none. */
 EXPORT void o_fold_nt2_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int op, float *out,
                            int64_t *index, int nthreads)
@@ -1836,6 +1837,14 @@ EXPORT void o_fold_nt2_f32(const float *x, int64_t lo, int64_t inner, int64_t hi
         const int64_t h = o / lo, l = o - h * lo;
         const float *p = x + l + lo * inner * h;
         float acc = op == 1 ? 1.0f : op == 2 ? -INFINITY : op == 3 ? INFINITY : 0.0f;
+        if (op == 18) {  /* meanad = mean(abs(center(a))) (expr/meanad.hpp): NT2's mean, then in order */
+            float sm = 0.0f;
+            for (int64_t k = 0; k < inner; ++k) sm = sm + p[lo * k];
+            const float m = (1.0f / (float)inner) * sm;
+            for (int64_t k = 0; k < inner; ++k) acc = acc + fabsf(p[lo * k] - m);
+            out[o] = (1.0f / (float)inner) * acc;
+            continue;
+        }
         if (op >= 12) {  /* nbtrue, all/any/none (sum of is_nez), nansum, nanmean (expr/nansum.hpp, nanmean.hpp) */
             float cnt = 0.0f, sm = 0.0f, ok = 0.0f;
             for (int64_t k = 0; k < inner; ++k) {
@@ -1917,6 +1926,19 @@ EXPORT void o_fold_ref(const float *x, int64_t lo, int64_t inner, int64_t hi, in
                 }
                 index[o] = f;
             }
+        } else if (op == 18) {  /* meanad: exact mean, then |x - mu| in long double, / n */
+            superacc a;
+            memset(&a, 0, sizeof a);
+            int64_t cnt = 0;
+            for (int64_t k = 0; k < inner; ++k) {
+                acc_add(&a, (double)p[lo * k]);
+                if (++cnt == (1 << 24)) { acc_norm(&a); cnt = 0; }
+            }
+            const long double mu = inner > 0 ? (long double)acc_value(a) / (long double)inner : 0.0L;
+            long double sa = 0.0L;
+            for (int64_t k = 0; k < inner; ++k) sa += fabsl((long double)p[lo * k] - mu);
+            out[o] = (double)(sa / (long double)inner);
+            if (abs_sum) abs_sum[o] = out[o];
         } else if (op >= 12) {  /* counts exactly; nansum exactly; nanmean = nansum / max(count, 1) */
             superacc a;
             memset(&a, 0, sizeof a);

@@ -127,7 +127,8 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
     glob = {ln.split()[0]: ln.split()[1:] for ln in lines}
     cases = [("sum1", (1, m, n), "sum"), ("sum2", (m, n, 1), "sum"), ("max1", (1, m, n), "max"),
              ("min2", (m, n, 1), "min"), ("mean1", (1, m, n), "mean"), ("norm2_2", (m, n, 1), "norm2"),
-             ("hsum1", (1, m, n), "sum"), ("var1", (1, m, n), "var"), ("stdev2_w1", (m, n, 1), "stdev1")]
+             ("hsum1", (1, m, n), "sum"), ("var1", (1, m, n), "var"), ("stdev2_w1", (m, n, 1), "stdev1"),
+             ("meanad1", (1, m, n), "meanad"), ("meanad2", (m, n, 1), "meanad")]
     for name, shape, op in cases:
         got = np.fromfile(tmp_path / f"{name}.bin", np.float32)
         if prec == "1":
@@ -135,8 +136,19 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
             assert _eq(got, ref), name
         else:
             ref, _, _ = oracle.fold_ref(a, *shape, op)
-            k = 2.0 if op in ("var", "stdev1") else 1.0
+            k = 2.0 if op in ("var", "stdev1", "meanad") else 1.0
             assert (np.abs(got - ref) <= k * np.spacing(np.abs(ref).astype(np.float32))).all(), name
+    # wmean(A, abs(A), 1) = rec(globalsum(w)) * sum(A .* w, 1)
+    w = np.abs(a)
+    wm = np.fromfile(tmp_path / "wmean1.bin", np.float32)
+    if prec == "1":
+        f = np.float32(1.0) / oracle.fold_nt2(w, 1, m * n, 1, "sum")[0][0]
+        assert _eq(wm, (f * oracle.fold_nt2((a * w).astype(np.float32), 1, m, n, "sum")[0]).astype(np.float32))
+    else:
+        gw = oracle.fold_ref(w, 1, m * n, 1, "sum")[0][0]
+        s, sa, _ = oracle.fold_ref((a * w).astype(np.float32), 1, m, n, "sum")
+        ref = s / gw
+        assert (np.abs(wm - ref) <= 2 * np.spacing(np.abs(ref).astype(np.float32)) + 2e-7 * sa / gw).all()
     c1 = np.fromfile(tmp_path / "cumsum1.bin", np.float32)
     c2 = np.fromfile(tmp_path / "cummax2.bin", np.float32)
     assert _eq(c2, oracle.scan_nt2(a, m, n, 1, "max"))

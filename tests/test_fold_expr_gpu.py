@@ -122,3 +122,35 @@ def test_generative_and_uint8_folds(lib, dev, oracle):
     for prec in (lib.PREC_FAST, lib.PREC_NT2):
         cnt = E.fold(E.Table(fr) > E.Table(bkg), "nbtrue", precision=prec)
         assert float(cnt.item()) == float(np.count_nonzero(fr.cpu().numpy() > bkg.cpu().numpy()))
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
+def test_meanad_and_wmean(lib, dev, oracle, prec):
+    """meanad of an expression (its two passes -- the mean, then |e - mean| --
+    both over the expression's elements, no temporary) and NT2's wmean(a, w,
+    dim) = rec(globalsum(w)) * sum(a .* w, dim): under the NT2 policy
+    bit-identical to the oracle's NT2 folds of the same float elements; under
+    the fast one within 2 ulp of the exact value."""
+    rng = np.random.default_rng(31)
+    m, k = 300, 1000
+    a = (50.0 + rng.standard_normal(m * k)).astype(np.float32)
+    b = rng.uniform(0.5, 2.0, m * k).astype(np.float32)
+    ta, tb = _t(dev, a), _t(dev, b)
+    elems = (a * b).astype(np.float32)  # a .* b rounded, as both policies compute it
+    for shape in ((1, m, k), (m, k, 1)):
+        got = E.fold(E.Table(ta) * E.Table(tb), "meanad", shape, precision=prec).cpu().numpy()
+        if prec == 1:
+            ref, _ = oracle.fold_nt2(elems, *shape, "meanad")
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), shape
+        else:
+            ref, _, _ = oracle.fold_ref(elems, *shape, "meanad")
+            assert (np.abs(got - ref) <= 2 * np.spacing(np.abs(ref).astype(np.float32))).all(), shape
+        wm = E.wmean(ta, tb, shape, precision=prec).cpu().numpy()
+        if prec == 1:
+            f = np.float32(1.0) / oracle.fold_nt2(b, 1, m * k, 1, "sum")[0][0]
+            want = (f * oracle.fold_nt2(elems, *shape, "sum")[0]).astype(np.float32)
+            assert np.array_equal(wm.view(np.uint32), want.view(np.uint32)), shape
+        else:
+            s, _, _ = oracle.fold_ref(elems, *shape, "sum")
+            ref = s / oracle.fold_ref(b, 1, m * k, 1, "sum")[0][0]
+            assert (np.abs(wm - ref) <= 2 * np.spacing(np.abs(ref).astype(np.float32))).all(), shape

@@ -121,7 +121,7 @@ def test_fold_global_matches_reduce_entry(lib, dev):
     assert abs(a - b) <= np.spacing(np.float32(abs(b)))
 
 
-VAR_OPS = ["var", "stdev", "var1", "stdev1"]
+VAR_OPS = ["var", "stdev", "var1", "stdev1", "meanad"]  # the folds of deviations from each output's mean
 
 
 def _offset_data(shape, seed):
@@ -136,7 +136,8 @@ def _offset_data(shape, seed):
 @pytest.mark.parametrize("op", VAR_OPS)
 def test_fold_var_nt2_policy_bit_exact(lib, dev, oracle, shape, op):
     """var/stdev under NT2's policy: NT2's float mean, the in-order sum of
-    squared deviations, f = rec(n - 1) (or rec(n)), bit-identical."""
+    squared deviations, f = rec(n - 1) (or rec(n)), bit-identical; meanad:
+    rec(n) times the in-order sum of |x - mean| (mean(abs(center(a))))."""
     lo, inner, hi = shape
     x = _offset_data(shape, 21)
     got = lib.fold(torch.from_numpy(x).to(dev), lo, inner, hi, op, precision=lib.PREC_NT2)
@@ -148,8 +149,9 @@ def test_fold_var_nt2_policy_bit_exact(lib, dev, oracle, shape, op):
 @pytest.mark.parametrize("shape", SHAPES, ids=[f"{a}x{b}x{c}" for a, b, c in SHAPES])
 @pytest.mark.parametrize("op", VAR_OPS)
 def test_fold_var_fast_policy(lib, dev, oracle, shape, op):
-    """var/stdev under the fast policy: within 2 float ulps of the exact value
-    (FP64 reference about the exact mean), offset data included."""
+    """var/stdev/meanad under the fast policy: within 2 float ulps of the
+    exact value (FP64 reference about the exact mean), offset data included
+    (meanad carries the mean's rounding error into every deviation)."""
     lo, inner, hi = shape
     x = _offset_data(shape, 22)
     got = lib.fold(torch.from_numpy(x).to(dev), lo, inner, hi, op).cpu().numpy()
