@@ -115,7 +115,13 @@ typedef enum nt2g_opcode {
     NT2G_OP_IS_NAN = 142, NT2G_OP_IS_INF, NT2G_OP_IS_FINITE, NT2G_OP_IS_EQZ, NT2G_OP_IS_NEZ, NT2G_OP_IS_LTZ,
     NT2G_OP_IS_GTZ,
     NT2G_OP_SIGNGAM = 149, /* sign of Gamma (NaN at the poles)             */
-    NT2G_OP_DIGAMMA = 150  /* psi = Gamma'/Gamma, NT2's double algorithm    */
+    NT2G_OP_DIGAMMA = 150, /* psi = Gamma'/Gamma, NT2's double algorithm    */
+    NT2G_OP_DAWSON = 151,  /* Dawson's integral                            */
+    /* integer operands (n) ride in a float, truncated toward zero (NaN -> 0) */
+    NT2G_OP_NTHROOT = 152, /* nthroot(a, n = b): real n-th root           */
+    NT2G_OP_EXPNI = 153,   /* expni(n = a, b): exponential integral E_n(b) */
+    NT2G_OP_GAMMAINC = 154 /* gammainc(a, b): regularised lower incomplete
+                              gamma P(b, a), evaluated in double          */
 } nt2g_opcode;
 
 typedef struct nt2g_op {
@@ -221,6 +227,22 @@ typedef enum nt2g_fold_op {
 } nt2g_fold_op;
 
 nt2g_status nt2g_fold_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
+
+/* median(a, dim) and medianad(a, dim) = median(abs(a - median(a, dim)), dim)
+ * over the same [lo, inner, hi] view
+ * (core/reduction/include/nt2/core/functions/expr/median.hpp:37-50,
+ *  expr/medianad.hpp:38-54; globalmedian / globalmedianad: lo = hi = 1).
+ * NT2 sorts each slice and takes the middle element (odd inner) or meanof of
+ * the two middle ones (even inner); the result is an order statistic, the
+ * same under either arithmetic policy, found here by radix selection.  A
+ * slice holding a NaN gives NaN (NT2's sort leaves that case unspecified);
+ * an empty slice (inner = 0) gives NaN.  workspace: 0 bytes for
+ * inner <= 40960 (each slice in one block's shared memory), else
+ * nt2g_median_workspace_size bytes (slice histograms). */
+typedef enum nt2g_median_op { NT2G_MEDIAN = 0, NT2G_MEDIANAD = 1 } nt2g_median_op;
+nt2g_status nt2g_median_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
+nt2g_status nt2g_median_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t op, void *workspace,
+                            size_t workspace_bytes, float *out, void *stream);
 nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t op, int32_t precision,
                           void *workspace, size_t workspace_bytes, float *out, int64_t *index, void *stream);
 
@@ -378,7 +400,7 @@ nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8
  * 32 cosd, 33 tand, 34 tanpi, 35 cotpi, 36 cotd, 37 secpi, 38 cscpi, 39 secd, 40 cscd, 41 sinc,
  * 42 sincpi, 43 acotd, 44 asec, 45 coth, 46 sinhc, 47 acsc, 48 asech, 49 acoth, 50 acsch, 64 erf, 65 erfcx, 66 expx2, 67 gamma, 68 gammaln,
  * 69 erfinv, 70 erfcinv,
- * 71 digamma, 72 signgam, 80 exprecneg, 81 exprecnegc, 82 sqrt1pm1. */
+ * 71 digamma, 72 signgam, 73 dawson, 80 exprecneg, 81 exprecnegc, 82 sqrt1pm1. */
 nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision,
                          void *stream);
 

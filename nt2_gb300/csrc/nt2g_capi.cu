@@ -289,7 +289,7 @@ static int n_operands(int code)
     case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:
     case NT2G_OP_ERF: case NT2G_OP_ERFCX: case NT2G_OP_EXPX2: case NT2G_OP_GAMMA: case NT2G_OP_GAMMALN:
     case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: case NT2G_OP_ERFINV:
-    case NT2G_OP_ERFCINV: case NT2G_OP_SIGNGAM: case NT2G_OP_DIGAMMA:
+    case NT2G_OP_ERFCINV: case NT2G_OP_SIGNGAM: case NT2G_OP_DIGAMMA: case NT2G_OP_DAWSON:
     case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
     case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ:
     case NT2G_OP_IS_NAN: case NT2G_OP_IS_INF: case NT2G_OP_IS_FINITE: case NT2G_OP_IS_EQZ: case NT2G_OP_IS_NEZ:
@@ -297,7 +297,8 @@ static int n_operands(int code)
     case NT2G_OP_ADD: case NT2G_OP_SUB: case NT2G_OP_MUL: case NT2G_OP_DIV: case NT2G_OP_MIN: case NT2G_OP_MAX:
     case NT2G_OP_LT: case NT2G_OP_GT: case NT2G_OP_LE: case NT2G_OP_GE: case NT2G_OP_EQ: case NT2G_OP_NE:
     case NT2G_OP_SELINC: case NT2G_OP_SELDEC: case NT2G_OP_ADDS: case NT2G_OP_POW:
-    case NT2G_OP_ATAN2: case NT2G_OP_HYPOT: case NT2G_OP_COPYSIGN: return 2;
+    case NT2G_OP_ATAN2: case NT2G_OP_HYPOT: case NT2G_OP_COPYSIGN: case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI:
+    case NT2G_OP_GAMMAINC: return 2;
     case NT2G_OP_FMA: case NT2G_OP_FNMS: case NT2G_OP_IF_ELSE: return 3;
     default: return -1;
     }
@@ -320,7 +321,8 @@ static bool float_only(int code)
     case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:
     case NT2G_OP_ERF: case NT2G_OP_ERFCX: case NT2G_OP_EXPX2: case NT2G_OP_GAMMA: case NT2G_OP_GAMMALN:
     case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: case NT2G_OP_ERFINV:
-    case NT2G_OP_ERFCINV: case NT2G_OP_SIGNGAM: case NT2G_OP_DIGAMMA:
+    case NT2G_OP_ERFCINV: case NT2G_OP_SIGNGAM: case NT2G_OP_DIGAMMA: case NT2G_OP_DAWSON:
+    case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI: case NT2G_OP_GAMMAINC:
     case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
     case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: case NT2G_OP_COPYSIGN:
     case NT2G_OP_IS_NAN: case NT2G_OP_IS_INF: case NT2G_OP_IS_FINITE: case NT2G_OP_IS_EQZ: case NT2G_OP_IS_NEZ:
@@ -1077,7 +1079,7 @@ extern "C" nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_
 {
     NT2G_REQ_N(); NT2G_REQ(x); NT2G_REQ(y); NT2G_REQ_PREC();
     NT2G_REACH(x); NT2G_REACH(y);
-    NT2G_CHECK_ARG((fn >= 0 && fn <= 50) || (fn >= 64 && fn <= 72) || (fn >= 80 && fn <= 82), "nt2g_map_f32: unknown function %d", fn);
+    NT2G_CHECK_ARG((fn >= 0 && fn <= 50) || (fn >= 64 && fn <= 73) || (fn >= 80 && fn <= 82), "nt2g_map_f32: unknown function %d", fn);
     return launch_map(fn, x, y, n, precision, (cudaStream_t)stream);
 }
 
@@ -1147,6 +1149,35 @@ extern "C" nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, 
     NT2G_REACH(x); NT2G_REACH(out); NT2G_REACH(index); NT2G_REACH(workspace);
     return launch_fold(x, lo, inner, hi, op, precision, workspace, workspace_bytes, out, index,
                        (cudaStream_t)stream);
+}
+
+extern "C" nt2g_status nt2g_median_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes)
+{
+    NT2G_CHECK_ARG(bytes != nullptr, "nt2g_median_workspace_size: bytes is NULL");
+    NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_median_workspace_size: negative extent");
+    *bytes = median_workspace_bytes(lo, inner, hi);
+    return NT2G_OK;
+}
+
+extern "C" nt2g_status nt2g_median_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t op,
+                                       void *workspace, size_t workspace_bytes, float *out, void *stream)
+{
+    NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_median_f32: negative extent (%lld, %lld, %lld)",
+                   (long long)lo, (long long)inner, (long long)hi);
+    NT2G_CHECK_ARG(op == NT2G_MEDIAN || op == NT2G_MEDIANAD, "nt2g_median_f32: op %d", op);
+    const int64_t S = lo * hi;
+    if (S == 0) return NT2G_OK;
+    NT2G_CHECK_ARG(S < ((int64_t)1 << 31), "nt2g_median_f32: %lld slices (at most 2^31 - 1)", (long long)S);
+    NT2G_CHECK_ARG(out != nullptr, "nt2g_median_f32: out is NULL");
+    NT2G_CHECK_ARG(x != nullptr || inner == 0, "nt2g_median_f32: x is NULL");
+    NT2G_CHECK_ARG(out + S <= x || x + lo * inner * hi <= out || inner == 0, "nt2g_median_f32: out overlaps x");
+    const size_t need = median_workspace_bytes(lo, inner, hi);
+    NT2G_CHECK_ARG(need == 0 || (workspace != nullptr && workspace_bytes >= need),
+                   "nt2g_median_f32: workspace of %zu bytes, %zu needed", workspace_bytes, need);
+    NT2G_CHECK_ARG(((uintptr_t)workspace & 15u) == 0, "nt2g_median_f32: workspace not 16-byte aligned");
+    const int64_t n = S;  // the pointer checks below apply to non-empty calls
+    NT2G_REACH(x); NT2G_REACH(out); NT2G_REACH(workspace);
+    return launch_median(x, lo, inner, hi, op, workspace, out, (cudaStream_t)stream);
 }
 
 extern "C" nt2g_status nt2g_scan_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes)

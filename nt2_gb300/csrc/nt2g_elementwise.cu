@@ -435,6 +435,7 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 70) return erfcinv<P>(a);
     if (FN == 71) return digamma<P>(a);
     if (FN == 72) return signgam(a);
+    if (FN == 73) return dawson<P>(a);
     if (FN == 80) return exprecneg<P>(a);
     if (FN == 81) return exprecnegc<P>(a);
     if (FN == 82) return sqrt1pm1<P>(a);
@@ -515,6 +516,7 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 70: NT2G_MAP(70); break;
     case 71: NT2G_MAP(71); break;
     case 72: NT2G_MAP(72); break;
+    case 73: NT2G_MAP(73); break;
     case 80: NT2G_MAP(80); break;
     case 81: NT2G_MAP(81); break;
     case 82: NT2G_MAP(82); break;
@@ -605,6 +607,7 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_ERFCINV: return erfcinv<P>(a);
     case NT2G_OP_SIGNGAM: return signgam(a);
     case NT2G_OP_DIGAMMA: return digamma<P>(a);
+    case NT2G_OP_DAWSON: return dawson<P>(a);
     case NT2G_OP_FLOOR: return floorf(a);
     case NT2G_OP_CEIL: return ceilf(a);
     case NT2G_OP_TRUNC: return truncf(a);
@@ -723,6 +726,14 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                                            : in.op == NT2G_OP_ATAN2 ? atan2<P>(x, y)
                                            : in.op == NT2G_OP_HYPOT ? hypot<P>(x, y)
                                                                     : copysignf(x, y));
+                }
+                break;
+            case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI: case NT2G_OP_GAMMAINC:
+                for (int j = 0; j < kV; ++j) {
+                    const float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]);
+                    d[j] = __float_as_uint(in.op == NT2G_OP_NTHROOT ? nthroot<P>(x, int_operand(y))
+                                           : in.op == NT2G_OP_EXPNI ? expni<P>(int_operand(x), y)
+                                                                    : gammainc<P>(x, y));
                 }
                 break;
             case NT2G_OP_FMA: case NT2G_OP_FNMS:

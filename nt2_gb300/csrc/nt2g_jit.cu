@@ -273,6 +273,10 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         case NT2G_OP_GAMMALN: e = "nt2g::gammaln<P>(" + A + ")"; break;
         case NT2G_OP_SIGNGAM: e = "nt2g::signgam(" + A + ")"; break;
         case NT2G_OP_DIGAMMA: e = "nt2g::digamma<P>(" + A + ")"; break;
+        case NT2G_OP_DAWSON: e = "nt2g::dawson<P>(" + A + ")"; break;
+        case NT2G_OP_NTHROOT: e = "nt2g::nthroot<P>(" + A + ", nt2g::int_operand(" + B + "))"; break;
+        case NT2G_OP_EXPNI: e = "nt2g::expni<P>(nt2g::int_operand(" + A + "), " + B + ")"; break;
+        case NT2G_OP_GAMMAINC: e = "nt2g::gammainc<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_ERFINV: e = "nt2g::erfinv<P>(" + A + ")"; break;
         case NT2G_OP_ERFCINV: e = "nt2g::erfcinv<P>(" + A + ")"; break;
         case NT2G_OP_FLOOR: e = "floorf(" + A + ")"; break;
@@ -627,6 +631,17 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
     case NT2G_OP_EXPX2: to(o.a, G + " * 2.0f * " + A + " * " + Y); break;
     case NT2G_OP_GAMMA: to(o.a, G + " * " + Y + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
     case NT2G_OP_GAMMALN: to(o.a, G + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
+    case NT2G_OP_DAWSON: to(o.a, G + " * (1.0f - 2.0f * " + A + " * " + Y + ")"); break;
+    case NT2G_OP_NTHROOT:  // y / (n x); the integer n passes no gradient
+        to(o.a, G + " * " + Y + " * " + rcp("(float)nt2g::int_operand(" + B + ") * " + A));
+        break;
+    case NT2G_OP_EXPNI:  // dE_n/dx = -E_(n-1)(x); E_0 = e^-x / x: -E_0 (1 + 1/x)
+        to(o.b, G + " * nt2g::vjp::expni_grad<D>(nt2g::int_operand(" + A + "), " + B + ", " + Y + ")");
+        break;
+    case NT2G_OP_GAMMAINC:  // dP(a, x)/dx = x^(a-1) e^-x / Gamma(a); no rule for a
+        if (act(o.b)) return false;
+        to(o.a, G + " * nt2g::vjp::gammainc_dx(" + A + ", " + B + ")");
+        break;
     case NT2G_OP_EXPRECNEG: to(o.a, G + " * " + Y + " * " + rcp(A + " * " + A)); break;
     // -e^(-1/x)/x^2 and 1/(2 sqrt(1 + x)) directly: y - 1 and y + 1 would cancel
     case NT2G_OP_EXPRECNEGC: to(o.a, "-" + G + " * nt2g::exprecneg<D>(" + A + ") * " + rcp(A + " * " + A)); break;

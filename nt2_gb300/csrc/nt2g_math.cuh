@@ -2078,4 +2078,248 @@ NT2G_HD double digamma_d(double a0)
 
 template <class P> NT2G_HD float digamma(float a0) { return (float)digamma_d((double)a0); }
 
+// -------------------------------------------------------------- dawson --
+// NT2's float Dawson integral (EUL/scalar/dawson.hpp with the float rational
+// approximations of EUL/details/dawson_kernel.hpp, Cephes' dawsnf): below
+// |x| = 3.25 x P(x^2)/Q(x^2); below 6.25 and up to 1e9 copysign(y/2, x) with
+// y = 1/|x| + x^-2 N(x^-2) / (D(x^-2) |x|); beyond, copysign(1/(2|x|), x).
+template <class P> NT2G_HD float dawson(float a0)
+{
+    const float x = fabsf(a0);
+    float xx = P::mul(x, x);
+    if (x < 3.25f) {
+        const float n = horner<P>(xx, bits_f(0x2d47fd98u), bits_f(0x30697185u), bits_f(0x32a70489u),
+                                  bits_f(0x357fdc17u), bits_f(0x364e9480u), bits_f(0x39b8d18bu), bits_f(0xba5edc97u),
+                                  bits_f(0x3d2d1abcu), bits_f(0xbdbbe665u), bits_f(0x3f800000u));
+        const float d = horner<P>(xx, bits_f(0x2dd36efbu), bits_f(0x30cc991au), bits_f(0x335fe1b9u),
+                                  bits_f(0x35aacdaeu), bits_f(0x37c306e7u), bits_f(0x39aaab31u), bits_f(0x3b6497e8u),
+                                  bits_f(0x3ce4ec9bu), bits_f(0x3e22afeeu), bits_f(0x3f132ddeu), bits_f(0x3f800000u));
+        return P::mul(a0, P::div(n, d));
+    }
+    xx = P::div(1.0f, xx);
+    float n, d;
+    if (x < 6.25f) {
+        n = horner<P>(xx, bits_f(0x3f024ae3u), bits_f(0xbe7aa0e7u), bits_f(0x3dc0d25du), bits_f(0xbcb32b13u),
+                      bits_f(0x3b6fff71u), bits_f(0xb9dde22au), bits_f(0x3816d831u), bits_f(0xb6100aefu),
+                      bits_f(0x33c36c5fu), bits_f(0xb1251d8au), bits_f(0x2e1dfe15u));
+        d = horner<P>(xx, bits_f(0x3f800000u), bits_f(0xbf21c042u), bits_f(0x3e726344u), bits_f(0xbd59d3f0u),
+                      bits_f(0x3c0af173u), bits_f(0xba7882fcu), bits_f(0x38a3cafeu), bits_f(0xb698f761u),
+                      bits_f(0x344b0b83u), bits_f(0xb1a8d160u), bits_f(0x2e9dfe10u));
+    } else {
+        if (x > 1.0e9f) return P::mul(0.5f, copysignf(P::div(1.0f, x), a0));
+        n = horner<P>(xx, bits_f(0xbf173118u), bits_f(0x3f211590u), bits_f(0xbe3101f1u), bits_f(0x3c8708d6u),
+                      bits_f(0xb9ff3ce5u));
+        d = horner<P>(xx, bits_f(0x3f800000u), bits_f(0xc02caf51u), bits_f(0x3fddc960u), bits_f(0xbec9942cu),
+                      bits_f(0x3d0d0443u), bits_f(0xba7f3ce5u));
+    }
+    const float y = P::add(P::div(1.0f, x), P::div(P::mul(xx, n), P::mul(d, x)));
+    return copysignf(P::mul(0.5f, y), a0);
+}
+
+// An integer operand carried in a float (nthroot's n, expni's n): truncated
+// toward zero, saturated to the int32 range, NaN as 0.
+NT2G_HD int32_t int_operand(float b)
+{
+    if (!(b == b)) return 0;
+    if (b >= 2147483648.0f) return 2147483647;
+    if (b <= -2147483648.0f) return (int32_t)(-2147483647 - 1);
+    return (int32_t)b;
+}
+
+// NT2's pow of a float by an integer (EXP/generic/pow.hpp:111-140): binary
+// powering of |n| (the base squared after every bit, the last square
+// unused), the reciprocal for n < 0.
+template <class P> NT2G_HD float pow_int(float a0, int32_t n)
+{
+    uint32_t e = n < 0 ? 0u - (uint32_t)n : (uint32_t)n;
+    float base = a0, r = 1.0f;
+    while (e) {
+        if (e & 1u) r = P::mul(r, base);
+        e >>= 1;
+        base = P::mul(base, base);
+    }
+    return n < 0 ? P::div(1.0f, r) : r;
+}
+
+// ------------------------------------------------------------- nthroot --
+// NT2's float nthroot(x, n) (EXP/scalar/nthroot.hpp:29-49): NaN for x < 0
+// and even n; x for |x| = 1; n = 0: 0 below |x| = 1, sign(x) inf above; 0 for
+// x = 0; x for x = +-inf; else y = pow(|x|, 1/n) refined by one Newton step
+// y -= (y^n - |x|) / (n y^(n-1)) (integer powers), negated for x < 0.
+template <class P> NT2G_HD float nthroot(float a0, int32_t n)
+{
+    const bool neg = a0 < 0.0f, odd = (n & 1) != 0;
+    if (neg && !odd) return f_nan();
+    const float x = fabsf(a0);
+    if (x == 1.0f) return a0;
+    if (n == 0) return x < 1.0f ? 0.0f : P::mul(nt2_sign(a0), f_inf());
+    if (a0 == 0.0f) return 0.0f;
+    if (x == f_inf()) return a0;
+    const float an = (float)n;
+    float y = pow<P>(x, P::div(1.0f, an));
+    if (y != 0.0f)
+        y = P::sub(y, P::div(P::sub(pow_int<P>(y, n), x), P::mul(an, pow_int<P>(y, n - 1))));
+    return (neg && odd) ? -y : y;
+}
+
+// --------------------------------------------------------------- expni --
+// NT2's float exponential integral E_n(x) (EUL/scalar/expni.hpp:37-127,
+// Cephes' expn in float): NaN for n < 0 or x < 0; 0 above Maxlog; at x = 0
+// inf (n < 2) or 1/(n - 1); e^-x / x for n = 0; an asymptotic expansion for
+// n > 5000; the power series with psi(n) for x <= 1; else the continued
+// fraction, rescaled by Halfeps when |p_k| exceeds Expnibig = 2^24.  Both
+// loops stop when the relative change falls to Halfeps = 2^-24 -- NT2's
+// loops have no other bound; here they also stop after kExpniTerms terms.
+constexpr int kExpniTerms = 10000;
+
+template <class P> NT2G_HD float expni(int32_t n, float x)
+{
+    const float halfeps = bits_f(0x33800000u), big = bits_f(0x4b800000u);
+    if (n < 0 || x < 0.0f) return f_nan();
+    if (x > bits_f(NT2G_MAXLOG)) return 0.0f;
+    if (x == 0.0f) return n < 2 ? f_inf() : P::div(1.0f, P::sub((float)n, 1.0f));
+    if (n == 0) return P::div(exp<P>(-x), x);
+    if (n > 5000) {
+        const float xk = P::add(x, (float)n), yk = P::div(1.0f, P::mul(xk, xk)), t = (float)n;
+        const float inner = P::add(P::sub(P::mul(6.0f, P::mul(x, x)), P::mul(P::mul(8.0f, t), x)), P::mul(t, t));
+        float ans = P::mul(P::mul(yk, t), inner);
+        ans = P::mul(yk, P::add(ans, P::mul(t, P::sub(t, P::mul(2.0f, x)))));
+        ans = P::mul(yk, P::add(ans, t));
+        return P::div(P::mul(P::add(1.0f, ans), exp<P>(-x)), xk);
+    }
+    if (x <= 1.0f) {
+        float psi = P::sub(-bits_f(0x3f13c468u), log<P>(x));  // -Euler - log(x)
+        for (int32_t i = n - 1; i; --i) psi = P::add(psi, P::div(1.0f, (float)i));
+        const float z = -x;
+        float xk = 0.0f, yk = 1.0f, pk = P::sub(1.0f, (float)n), t;
+        float ans = (n == 1) ? 0.0f : P::div(1.0f, pk);
+        int it = 0;
+        do {
+            xk = P::add(xk, 1.0f);
+            yk = P::mul(yk, P::div(z, xk));
+            pk = P::add(pk, 1.0f);
+            if (pk != 0.0f) ans = P::add(ans, P::div(yk, pk));
+            t = ans != 0.0f ? fabsf(P::div(yk, ans)) : 1.0f;
+        } while (t > halfeps && ++it < kExpniTerms);
+        const float tn = (float)n, r = (float)(n - 1);
+        return P::sub(P::div(P::mul(pow<P>(z, r), psi), gamma<P>(tn)), ans);
+    }
+    int32_t k = 1;
+    float t, pkm2 = 1.0f, qkm2 = x, pkm1 = 1.0f, qkm1 = P::add(x, (float)n);
+    float ans = P::div(pkm1, qkm1);
+    int it = 0;
+    do {
+        const bool odd = ((++k) & 1) != 0;
+        const float yk = odd ? 1.0f : x;
+        const float xk = odd ? (float)(n + (k - 1) / 2) : (float)(k / 2);
+        const float pk = P::add(P::mul(pkm1, yk), P::mul(pkm2, xk));
+        const float qk = P::add(P::mul(qkm1, yk), P::mul(qkm2, xk));
+        if (qk != 0.0f) {
+            const float r = P::div(pk, qk);
+            t = fabsf(P::div(P::sub(ans, r), r));
+            ans = r;
+        } else {
+            t = 1.0f;
+        }
+        pkm2 = pkm1;
+        pkm1 = pk;
+        qkm2 = qkm1;
+        qkm1 = qk;
+        if (fabsf(pk) > big) {
+            pkm2 = P::mul(pkm2, halfeps);
+            pkm1 = P::mul(pkm1, halfeps);
+            qkm2 = P::mul(qkm2, halfeps);
+            qkm1 = P::mul(qkm1, halfeps);
+        }
+    } while (t > halfeps && ++it < kExpniTerms);
+    return P::mul(ans, exp<P>(-x));
+}
+
+// ------------------------------------------------------------ gammainc --
+// NT2's gammainc(x, a) (EUL/scalar/gammainc.hpp:37-43) is 1 for a = 0 or
+// x = +inf and otherwise Boost.Math's gamma_p(a, x), the regularised lower
+// incomplete gamma function, which for float arguments works in double and
+// rounds (Boost's default promote_float policy; domain errors -- a < 0,
+// x < 0, a not finite -- give NaN under NT2's errno policy).  Boost.Math is
+// not part of NT2's tree, so this is this library's own double evaluation,
+// after the published methods: the power series
+//   P = D sum_k x^k / ((a+1)...(a+k)),  D = x^a e^-x / Gamma(a+1),
+// below x = a + 1; the continued fraction of Q = 1 - P (Legendre's, by the
+// modified Lentz method) above; and for a > 1e6 Temme's uniform asymptotic
+// expansion (DLMF 8.12.8-8.12.10, first correction term c0).  D is taken as
+// exp(a log1pmx(t) - log(2 pi a)/2 - S(a)) with x = a(1 + t), S the Stirling
+// series of log Gamma, so that it keeps double accuracy for large a.
+NT2G_HD double log1pmx_d(double t)  // log(1 + t) - t
+{
+    if (fabs(t) > 0.5) return ::log1p(t) - t;
+    double term = t, sum = 0.0;
+    for (int k = 2; k < 80; ++k) {
+        term *= -t;
+        const double c = term / k;
+        sum += c;
+        if (fabs(c) <= 1e-17 * fabs(sum)) break;
+    }
+    return sum;
+}
+
+NT2G_HD double stirling_series_d(double a)  // log Gamma(a) - ((a - 1/2) log a - a + log(2 pi)/2), a >= 10
+{
+    const double r = 1.0 / a, r2 = r * r;
+    return r * (1.0 / 12 - r2 * (1.0 / 360 - r2 * (1.0 / 1260 - r2 * (1.0 / 1680 - r2 * (1.0 / 1188)))));
+}
+
+NT2G_HD double gammainc_prefix_d(double x, double a)  // x^a e^-x / Gamma(a + 1)
+{
+    if (a < 10.0) return ::exp(a * ::log(x) - x - ::lgamma(a + 1.0));
+    const double t = (x - a) / a;
+    return ::exp(a * log1pmx_d(t) - 0.5 * ::log(6.283185307179586476925 * a) - stirling_series_d(a));
+}
+
+NT2G_HD double gammainc_d(double x, double a)
+{
+    if (a == 0.0 || x == (double)f_inf()) return 1.0;
+    if (x != x || a != a || a < 0.0 || x < 0.0 || a == (double)f_inf()) return (double)f_nan();
+    if (x == 0.0) return 0.0;
+    if (a > 1.0e6) {  // Temme: P = erfc(-eta sqrt(a/2))/2 - e^(-a eta^2/2) c0(eta) / sqrt(2 pi a)
+        const double lam = x / a, t = lam - 1.0;
+        const double h = -log1pmx_d(t);  // lam - 1 - log(lam) >= 0
+        const double eta = (t < 0.0 ? -1.0 : 1.0) * ::sqrt(2.0 * h);
+        double c0;
+        if (fabs(eta) < 1e-3)
+            c0 = -1.0 / 3 + eta * (1.0 / 12 - eta * (2.0 / 135 - eta * (1.0 / 864)));
+        else
+            c0 = 1.0 / t - 1.0 / eta;
+        const double e = ::exp(-a * h) / ::sqrt(6.283185307179586476925 * a);
+        return 0.5 * ::erfc(-eta * ::sqrt(0.5 * a)) - e * c0;
+    }
+    const double d = gammainc_prefix_d(x, a);
+    if (x < a + 1.0) {
+        double term = 1.0, sum = 1.0;
+        for (int k = 1; k < 100000; ++k) {
+            term *= x / (a + k);
+            sum += term;
+            if (term <= 1e-17 * sum) break;
+        }
+        return d * sum;
+    }
+    // Q = a D h, h = 1/(x+1-a- 1(1-a)/(x+3-a- 2(2-a)/(x+5-a- ...)))
+    const double tiny = 1e-300;
+    double b = x + 1.0 - a, c = 1.0 / tiny, dd = 1.0 / b, h = dd;
+    for (int i = 1; i < 100000; ++i) {
+        const double an = -i * (i - a);
+        b += 2.0;
+        dd = an * dd + b;
+        if (fabs(dd) < tiny) dd = tiny;
+        c = b + an / c;
+        if (fabs(c) < tiny) c = tiny;
+        dd = 1.0 / dd;
+        const double del = dd * c;
+        h *= del;
+        if (fabs(del - 1.0) <= 1e-16) break;
+    }
+    return 1.0 - a * d * h;
+}
+
+template <class P> NT2G_HD float gammainc(float x, float a) { return (float)gammainc_d((double)x, (double)a); }
+
 }  // namespace nt2g

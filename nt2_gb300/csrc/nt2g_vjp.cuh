@@ -134,5 +134,21 @@ template <class D> NT2G_HD float sinhc_grad(float x, float y)
     return (cosh<D>(x) - y) * grcp(x);
 }
 
+// d/dx E_n(x) = -E_(n-1)(x) for n >= 1 (Abramowitz & Stegun 5.1.26);
+// for n = 0, E_0 = e^-x/x and the derivative is -E_0 (1 + 1/x).
+template <class D> NT2G_HD float expni_grad(int32_t n, float x, float y)
+{
+    if (n == 0) return -y * (1.0f + grcp(x));
+    return -expni<D>(n - 1, x);
+}
+
+// d/dx P(a, x) = x^(a-1) e^-x / Gamma(a), in double (0 at x = 0 for a > 1).
+NT2G_HD float gammainc_dx(float x, float a)
+{
+    const double xd = x, ad = a;
+    if (xd == 0.0) return ad < 1.0 ? f_inf() : ad == 1.0 ? 1.0f : 0.0f;
+    return (float)::exp((ad - 1.0) * ::log(xd) - xd - ::lgamma(ad));
+}
+
 }  // namespace vjp
 }  // namespace nt2g

@@ -279,6 +279,11 @@ int main(int argc, char **argv)
             dtable W;
             W = nt2::abs(A);
             save(dir + "wmean1.bin", nt2::wmean(A, W, 1));
+            save(dir + "median1.bin", nt2::median(A, 1));
+            save(dir + "median2.bin", nt2::median(h, 2));  // a host table, along its rows
+            save(dir + "medianad1.bin", nt2::medianad(A));
+            std::printf("globalmedian %.9g\nglobalmedianad %.9g\n", (double)nt2::globalmedian(A),
+                        (double)nt2::globalmedianad(h));
             std::int64_t imax = 0, imin = 0;
             const float gmax = nt2::globalmax(A, imax), gmin = nt2::globalmin(h, imin);
             std::printf("globalmax %.9g %lld\nglobalmin %.9g %lld\nglobalmean %.9g\nglobalnorm2 %.9g\n"

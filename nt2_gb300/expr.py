@@ -117,6 +117,7 @@ gamma = _un("GAMMA")
 gammaln = _un("GAMMALN")
 digamma = _un("DIGAMMA")
 signgam = _un("SIGNGAM")
+dawson = _un("DAWSON")
 
 
 # NT2's beta and betaln, built as NT2 writes them (EUL/scalar/beta.hpp:
@@ -256,6 +257,21 @@ def pow(a, b):
 def hypot(a, b):
     """sqrt(a^2 + b^2) without undue overflow (NT2's scaled form)."""
     return _bin("HYPOT", a, b)
+
+
+def nthroot(x, n):
+    """NT2's real n-th root of x (n truncated toward zero; NaN for x < 0 and even n)."""
+    return _bin("NTHROOT", x, n)
+
+
+def expni(n, x):
+    """NT2's exponential integral E_n(x) (n truncated toward zero)."""
+    return _bin("EXPNI", n, x)
+
+
+def gammainc(x, a):
+    """NT2's regularised lower incomplete gamma function P(a, x), evaluated in double."""
+    return _bin("GAMMAINC", x, a)
 
 
 def atan2(a, b):
@@ -628,6 +644,18 @@ def wmean(a, w, shape=None, precision=lib.PREC_FAST):
     out = torch.empty_like(s)
     assign([out], [Scalar(float(f)) * Table(s)], precision=precision)
     return out
+
+
+def median(a, shape=None):
+    """NT2's median(a, dim) of a device table viewed as shape = (lo, inner, hi)
+    along inner (default every element: globalmedian); the same under either
+    arithmetic policy (an order statistic, or meanof of two)."""
+    return lib.median(a, *(shape or (1, a.numel(), 1)), "median")
+
+
+def medianad(a, shape=None):
+    """NT2's medianad(a, dim) = median(abs(a - median(a, dim)), dim)."""
+    return lib.median(a, *(shape or (1, a.numel(), 1)), "medianad")
 
 
 def batch_source(programs, precision=lib.PREC_FAST, block_threads=256):

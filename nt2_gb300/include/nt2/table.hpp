@@ -578,6 +578,11 @@ NT2G_BINARY(pow, NT2G_OP_POW, false)
 NT2G_BINARY(atan2, NT2G_OP_ATAN2, false)
 NT2G_BINARY(hypot, NT2G_OP_HYPOT, false)
 NT2G_BINARY(copysign, NT2G_OP_COPYSIGN, false)
+// nthroot(x, n), expni(n, x), gammainc(x, a): the integer n is truncated
+// toward zero (EXP/scalar/nthroot.hpp, EUL/scalar/expni.hpp, EUL/scalar/gammainc.hpp)
+NT2G_BINARY(nthroot, NT2G_OP_NTHROOT, false)
+NT2G_BINARY(expni, NT2G_OP_EXPNI, false)
+NT2G_BINARY(gammainc, NT2G_OP_GAMMAINC, false)
 #undef NT2G_BINARY
 
 // predicates (boost/simd/predicates/functions): logical results for if_else
@@ -664,6 +669,7 @@ NT2G_UNARY(gamma, NT2G_OP_GAMMA)
 NT2G_UNARY(gammaln, NT2G_OP_GAMMALN)
 NT2G_UNARY(digamma, NT2G_OP_DIGAMMA)
 NT2G_UNARY(signgam, NT2G_OP_SIGNGAM)
+NT2G_UNARY(dawson, NT2G_OP_DAWSON)
 NT2G_UNARY(erfinv, NT2G_OP_ERFINV)
 NT2G_UNARY(erfcinv, NT2G_OP_ERFCINV)
 NT2G_UNARY(floor, NT2G_OP_FLOOR)
@@ -1402,6 +1408,71 @@ template <class Site> inline table<float, Site> scan_dim(const table<float, Site
     return r;
 }
 }  // namespace detail
+// median(t, dim), medianad(t, dim) (core/functions/expr/median.hpp,
+// expr/medianad.hpp): the middle element of each slice along dim (meanof
+// of the two middle ones for an even length), by selection on the device;
+// globalmedian / globalmedianad over all elements.
+namespace detail {
+template <class Site> inline void median_raw(const table<float, Site> &t, fold_shape f, int op, float *o)
+{
+    auto run = [&](const float *x) {
+        std::size_t b = 0;
+        check(nt2g_median_workspace_size(f.lo, f.inner, f.hi, &b), "median workspace");
+        scratch &sc = thread_scratch(b);
+        check(nt2g_median_f32(x, f.lo, f.inner, f.hi, op, sc.ws.p, sc.ws.bytes, o, options().stream), "median");
+        if (!table<float, Site>::on_device) check(nt2g_stream_synchronize(options().stream), "median");
+    };
+    if (table<float, Site>::on_device || host_in_place()) {
+        run(t.data());
+    } else {
+        table<float, device_> dt(t.extent());
+        dt = t;
+        run(dt.data());
+    }
+}
+template <class Site> inline table<float, device_> median_dim(const table<float, Site> &t, int dim, int op)
+{
+    if (dim < 1 || dim > 4) throw gpu_error(NT2G_ERR_INVALID, "median dimension out of range");
+    of_size_ e = t.extent();
+    const fold_shape f = split(e, dim);
+    e.d[dim - 1] = 1;
+    table<float, device_> r(e);
+    median_raw(t, f, op, r.data());
+    return r;
+}
+template <class Site> inline float median_all(const table<float, Site> &t, int op)
+{
+    scratch &sc = thread_scratch(0);
+    float *o = (float *)((char *)sc.out.p + 16);
+    median_raw(t, fold_shape{1, (std::int64_t)t.numel(), 1}, op, o);
+    float r = 0.0f;
+    check(nt2g_memcpy(&r, o, sizeof r, 2, options().stream), "median result");
+    check(nt2g_stream_synchronize(options().stream), "median result");
+    return r;
+}
+}  // namespace detail
+template <class Site> table<float, device_> median(const table<float, Site> &t, int dim)
+{
+    return detail::median_dim(t, dim, NT2G_MEDIAN);
+}
+template <class Site> table<float, device_> median(const table<float, Site> &t)
+{
+    return detail::median_dim(t, detail::first_non_singleton(t.extent()), NT2G_MEDIAN);
+}
+template <class Site> table<float, device_> medianad(const table<float, Site> &t, int dim)
+{
+    return detail::median_dim(t, dim, NT2G_MEDIANAD);
+}
+template <class Site> table<float, device_> medianad(const table<float, Site> &t)
+{
+    return detail::median_dim(t, detail::first_non_singleton(t.extent()), NT2G_MEDIANAD);
+}
+template <class Site> float globalmedian(const table<float, Site> &t) { return detail::median_all(t, NT2G_MEDIAN); }
+template <class Site> float globalmedianad(const table<float, Site> &t)
+{
+    return detail::median_all(t, NT2G_MEDIANAD);
+}
+
 template <class Site> table<float, Site> cumsum(const table<float, Site> &t, int dim) { return detail::scan_dim(t, dim, NT2G_SCAN_SUM); }
 template <class Site> table<float, Site> cumprod(const table<float, Site> &t, int dim) { return detail::scan_dim(t, dim, NT2G_SCAN_PROD); }
 template <class Site> table<float, Site> cummax(const table<float, Site> &t, int dim) { return detail::scan_dim(t, dim, NT2G_SCAN_MAX); }

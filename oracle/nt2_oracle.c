@@ -1137,6 +1137,147 @@ EXPORT float o_beta(float a0, float a1)
 }
 EXPORT float o_betaln(float a0, float a1) { return o_gammaln(a0) + o_gammaln(a1) - o_gammaln(a0 + a1); }
 
+/* dawson EUL/scalar/dawson.hpp:27-55 with the float rational approximations
+ * of EUL/details/dawson_kernel.hpp:22-107 (NT2_HORNER_RAT = horner(P)/horner(Q),
+ * POLY/scalar/impl/horner.hpp:107-110). */
+static const uint32_t DAW1_P[10] = {0x2d47fd98, 0x30697185, 0x32a70489, 0x357fdc17, 0x364e9480,
+                                    0x39b8d18b, 0xba5edc97, 0x3d2d1abc, 0xbdbbe665, 0x3f800000};
+static const uint32_t DAW1_Q[11] = {0x2dd36efb, 0x30cc991a, 0x335fe1b9, 0x35aacdae, 0x37c306e7, 0x39aaab31,
+                                    0x3b6497e8, 0x3ce4ec9b, 0x3e22afee, 0x3f132dde, 0x3f800000};
+static const uint32_t DAW2_N[11] = {0x3f024ae3, 0xbe7aa0e7, 0x3dc0d25d, 0xbcb32b13, 0x3b6fff71, 0xb9dde22a,
+                                    0x3816d831, 0xb6100aef, 0x33c36c5f, 0xb1251d8a, 0x2e1dfe15};
+static const uint32_t DAW2_D[11] = {0x3f800000, 0xbf21c042, 0x3e726344, 0xbd59d3f0, 0x3c0af173, 0xba7882fc,
+                                    0x38a3cafe, 0xb698f761, 0x344b0b83, 0xb1a8d160, 0x2e9dfe10};
+static const uint32_t DAW3_N[5] = {0xbf173118, 0x3f211590, 0xbe3101f1, 0x3c8708d6, 0xb9ff3ce5};
+static const uint32_t DAW3_D[6] = {0x3f800000, 0xc02caf51, 0x3fddc960, 0xbec9942c, 0x3d0d0443, 0xba7f3ce5};
+
+EXPORT float o_dawson(float a0)
+{
+    float x = fabsf(a0), xx = x * x;
+    if (x < 3.25f) return a0 * (horner(xx, DAW1_P, 10) / horner(xx, DAW1_Q, 11));
+    xx = 1.0f / xx;
+    if (x < 6.25f) {
+        float y = 1.0f / x + xx * horner(xx, DAW2_N, 11) / (horner(xx, DAW2_D, 11) * x);
+        return copysignf(0.5f * y, a0);
+    }
+    if (x > 1.0e9f) return 0.5f * copysignf(1.0f / x, a0);
+    float y = 1.0f / x + xx * horner(xx, DAW3_N, 5) / (horner(xx, DAW3_D, 6) * x);
+    return copysignf(0.5f * y, a0);
+}
+
+/* An integer operand carried in a float: truncated toward zero, saturated
+ * to int32, NaN as 0 (the library's convention for nthroot's and expni's n). */
+static int32_t int_operand(float b)
+{
+    if (isnan(b)) return 0;
+    if (b >= 2147483648.0f) return INT32_MAX;
+    if (b <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)b;
+}
+
+/* pow(float, int) EXP/generic/pow.hpp:111-140: binary powering of |n|, the
+ * base squared after each bit; the reciprocal for n < 0. */
+static float powi(float a0, int32_t n)
+{
+    uint32_t e = n < 0 ? 0u - (uint32_t)n : (uint32_t)n;
+    float base = a0, r = 1.0f;
+    for (; e; e >>= 1) {
+        if (e & 1u) r *= base;
+        base = base * base;
+    }
+    return n < 0 ? 1.0f / r : r;
+}
+
+EXPORT float o_sign(float a0);
+
+/* nthroot EXP/scalar/nthroot.hpp:29-49 */
+EXPORT float o_nthroot(float a0, int32_t n)
+{
+    int ltz = a0 < 0.0f, odd = (n % 2) != 0;
+    if (ltz && !odd) return NAN;
+    float x = fabsf(a0);
+    if (x == 1.0f) return a0;
+    if (n == 0) return (x < 1.0f) ? 0.0f : o_sign(a0) * INFINITY;
+    if (a0 == 0.0f) return 0.0f;
+    if (isinf(a0)) return a0;
+    float an = (float)n;
+    float y = o_pow(x, 1.0f / an);
+    if (y != 0.0f) y -= (powi(y, n) - x) / (an * powi(y, n - 1));
+    return (ltz && odd) ? -y : y;
+}
+
+/* expni EUL/scalar/expni.hpp:37-127 (Cephes expn in float).  NT2's two
+ * loops end when the relative change reaches Halfeps = 2^-24; like the
+ * library, this stops them after 10000 terms as well. */
+EXPORT float o_expni(int32_t n, float x)
+{
+    const float halfeps = bf(0x33800000u), big = bf(0x4b800000u), euler = bf(0x3f13c468u);
+    if (n < 0 || x < 0.0f) return NAN;
+    if (x > bf(C_MAXLOG)) return 0.0f;
+    if (x == 0.0f) return (n < 2) ? INFINITY : 1.0f / ((float)n - 1.0f);
+    if (n == 0) return o_exp(-x) / x;
+    if (n > 5000) {
+        float xk = x + (float)n, yk = 1.0f / (xk * xk), t = (float)n;
+        float ans = yk * t * (6.0f * (x * x) - 8.0f * t * x + t * t);
+        ans = yk * (ans + t * (t - 2.0f * x));
+        ans = yk * (ans + t);
+        return (1.0f + ans) * o_exp(-x) / xk;
+    }
+    if (x <= 1.0f) {
+        float psi = -euler - o_log(x);
+        for (int32_t i = n - 1; i; --i) psi += 1.0f / (float)i;
+        float z = -x, xk = 0.0f, yk = 1.0f, pk = 1.0f - (float)n, t;
+        float ans = (n == 1) ? 0.0f : 1.0f / pk;
+        int it = 0;
+        do {
+            xk += 1.0f;
+            yk *= z / xk;
+            pk += 1.0f;
+            if (pk != 0.0f) ans += yk / pk;
+            t = (ans != 0.0f) ? fabsf(yk / ans) : 1.0f;
+        } while (t > halfeps && ++it < 10000);
+        return (o_pow(z, (float)(n - 1)) * psi / o_gamma((float)n)) - ans;
+    }
+    int32_t k = 1;
+    float t, pkm2 = 1.0f, qkm2 = x, pkm1 = 1.0f, qkm1 = x + (float)n;
+    float ans = pkm1 / qkm1;
+    int it = 0;
+    do {
+        int odd = (++k) % 2 != 0;
+        float yk = odd ? 1.0f : x;
+        float xk = odd ? (float)(n + (k - 1) / 2) : (float)(k / 2);
+        float pk = pkm1 * yk + pkm2 * xk;
+        float qk = qkm1 * yk + qkm2 * xk;
+        if (qk != 0.0f) {
+            float r = pk / qk;
+            t = fabsf((ans - r) / r);
+            ans = r;
+        } else {
+            t = 1.0f;
+        }
+        pkm2 = pkm1;
+        pkm1 = pk;
+        qkm2 = qkm1;
+        qkm1 = qk;
+        if (fabsf(pk) > big) {
+            pkm2 *= halfeps;
+            pkm1 *= halfeps;
+            qkm2 *= halfeps;
+            qkm1 *= halfeps;
+        }
+    } while (t > halfeps && ++it < 10000);
+    return ans * o_exp(-x);
+}
+
+EXPORT void o_nthroot_f32(const float *x, const float *n, float *out, int64_t m)
+{
+    for (int64_t i = 0; i < m; ++i) out[i] = o_nthroot(x[i], int_operand(n[i]));
+}
+EXPORT void o_expni_f32(const float *n, const float *x, float *out, int64_t m)
+{
+    for (int64_t i = 0; i < m; ++i) out[i] = o_expni(int_operand(n[i]), x[i]);
+}
+
 /* erfinv EUL/scalar/erfinv.hpp, erfcinv EUL/scalar/erfcinv.hpp (single_, Giles),
  * kernels EUL/details/erfinv_kernel.hpp */
 static const uint32_t ERFINV1_P[9] = {0x32f16588, 0x34b84b36, 0xb66c7357, 0xb6935ac1, 0x396532db,
@@ -1224,7 +1365,7 @@ enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQR
        FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT, FN_COT, FN_SEC, FN_CSC, FN_SIND,
        FN_COSD, FN_TAND, FN_TANPI, FN_COTPI, FN_COTD, FN_SECPI, FN_CSCPI, FN_SECD, FN_CSCD, FN_SINC, FN_SINCPI,
        FN_ACOTD, FN_ASEC, FN_COTH, FN_SINHC, FN_ACSC, FN_ASECH, FN_ACOTH, FN_ACSCH,
-       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_ERFINV, FN_ERFCINV, FN_DIGAMMA, FN_SIGNGAM,
+       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_ERFINV, FN_ERFCINV, FN_DIGAMMA, FN_SIGNGAM, FN_DAWSON,
        FN_EXPRECNEG = 80, FN_EXPRECNEGC,
        FN_SQRT1PM1,
        /* compositions of the above, oracle only (the front ends lower them to programs) */
@@ -1305,6 +1446,7 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_GAMMALN: y[i] = o_gammaln(a); break;
         case FN_DIGAMMA: y[i] = o_digamma(a); break;
         case FN_SIGNGAM: y[i] = o_signgam(a); break;
+        case FN_DAWSON: y[i] = o_dawson(a); break;
         case FN_ERFINV: y[i] = o_erfinv(a); break;
         case FN_ERFCINV: y[i] = o_erfcinv(a); break;
         case FN_EXPRECNEG: y[i] = o_exprecneg(a); break;
@@ -1810,6 +1952,55 @@ EXPORT double o_exact_sum(const float *x, const float *y, int64_t n, int nthread
     }
     if (abs_sum) *abs_sum = asum;
     return acc_value(total);
+}
+
+/* median / medianad along a dimension (core/reduction/include/nt2/core/
+ * functions/expr/median.hpp:37-50, expr/medianad.hpp:38-54): each slice of
+ * the [lo, inner, hi] view sorted ascending (NT2's sort, std::sort with
+ * operator<), the middle element for odd inner, meanof of the two middle ones
+ * for even inner (boost.simd generic/meanof.hpp:21-33: m + (max - m) * 1/2
+ * for finite values, else average = a0 * 1/2 + a1 * 1/2, unfused).  NT2's
+ * result for a slice holding a NaN is unspecified (operator< orders no NaN);
+ * here it is NaN, as for an empty slice.  medianad is the median of
+ * |x - median| per slice. */
+static int cmp_float_lt(const void *a, const void *b)
+{
+    float x = *(const float *)a, y = *(const float *)b;
+    return x < y ? -1 : (y < x ? 1 : 0);
+}
+
+static float nt2_meanof_f(float a0, float a1)
+{
+    float m = a0 < a1 ? a0 : a1, M = a0 > a1 ? a0 : a1;
+    if (a0 - a0 == 0.0f && a1 - a1 == 0.0f) return m + (M - m) * 0.5f;
+    return a0 * 0.5f + a1 * 0.5f;
+}
+
+static float median_of(float *v, int64_t n)
+{
+    if (n == 0) return NAN;
+    for (int64_t k = 0; k < n; ++k)
+        if (isnan(v[k])) return NAN;
+    qsort(v, (size_t)n, sizeof(float), cmp_float_lt);
+    int64_t mid = n >> 1;
+    return (n & 1) ? v[mid] : nt2_meanof_f(v[mid - 1], v[mid]);
+}
+
+EXPORT void o_median_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int ad, float *out)
+{
+    float *v = (float *)malloc((size_t)(inner > 0 ? inner : 1) * sizeof(float));
+    for (int64_t h = 0; h < hi; ++h)
+        for (int64_t l = 0; l < lo; ++l) {
+            const float *base = x + l + lo * inner * h;
+            for (int64_t k = 0; k < inner; ++k) v[k] = base[lo * k];
+            float m = median_of(v, inner);
+            if (ad) {
+                for (int64_t k = 0; k < inner; ++k) v[k] = fabsf(base[lo * k] - m);
+                m = median_of(v, inner);
+            }
+            out[l + lo * h] = m;
+        }
+    free(v);
 }
 
 /* Reductions along one dimension, the table viewed as [lo, inner, hi]

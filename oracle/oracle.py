@@ -27,7 +27,7 @@ FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, exp2=
           # NT2's generic compositions of the functors above
           sech=51, csch=52, acot=53, asind=54, acosd=55, atand=56, asecd=57, acscd=58, asinpi=59, acospi=60,
           atanpi=61, indeg=62, inrad=63,
-          erf=64, erfcx=65, expx2=66, gamma=67, gammaln=68, erfinv=69, erfcinv=70, digamma=71, signgam=72,
+          erf=64, erfcx=65, expx2=66, gamma=67, gammaln=68, erfinv=69, erfcinv=70, digamma=71, signgam=72, dawson=73,
           exprecneg=80, exprecnegc=81, sqrt1pm1=82)
 SCALAR_ONLY = ("o_realsqrt", "o_reallog", "o_floor", "o_ceil", "o_trunc", "o_fix", "o_round", "o_round2even",
                "o_frac", "o_sign", "o_signnz", "o_oneplus", "o_oneminus", "o_minusone", "o_sqr_abs")
@@ -72,6 +72,12 @@ def lib():
         for f in ("o_logspace_add", "o_logspace_sub", "o_copysign", "o_dist", "o_average", "o_beta", "o_betaln"):
             getattr(L, f).restype = ctypes.c_float
             getattr(L, f).argtypes = [ctypes.c_float, ctypes.c_float]
+        L.o_nthroot.restype = ctypes.c_float
+        L.o_nthroot.argtypes = [ctypes.c_float, ctypes.c_int32]
+        L.o_expni.restype = ctypes.c_float
+        L.o_expni.argtypes = [ctypes.c_int32, ctypes.c_float]
+        L.o_nthroot_f32.argtypes = [_P, _P, _P, _I64]
+        L.o_expni_f32.argtypes = [_P, _P, _P, _I64]
         L.o_atan2d.restype = ctypes.c_float
         L.o_atan2d.argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_hypot.restype = ctypes.c_float
@@ -97,6 +103,7 @@ def lib():
         L.o_sum_plain_f32.argtypes = [_P, _P, _I64, ctypes.c_int]
         L.o_fold_nt2_f32.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, ctypes.c_int]
         L.o_fold_ref.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, _P, ctypes.c_int]
+        L.o_median_f32.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P]
         L.o_scan_nt2_f32.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, ctypes.c_int]
         L.o_cumsum_exact.argtypes = [_P, _I64, _I64, _I64, _P, _P, ctypes.c_int]
         L.o_globalsum_f32.restype = ctypes.c_float
@@ -146,6 +153,22 @@ def pow_f64(x, y):
     x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
     out = np.empty(x.size, np.float64)
     lib().o_pow_f64(_p(x), _p(y), _p(out), x.size)
+    return out
+
+
+def nthroot_f32(x, n):
+    """NT2's float nthroot(x, n) restated, n given as floats (truncated)."""
+    x, n = _f32(x), _f32(n)
+    out = np.empty_like(x)
+    lib().o_nthroot_f32(_p(x), _p(n), _p(out), x.size)
+    return out
+
+
+def expni_f32(n, x):
+    """NT2's float expni(n, x) restated, n given as floats (truncated)."""
+    n, x = _f32(n), _f32(x)
+    out = np.empty_like(x)
+    lib().o_expni_f32(_p(n), _p(x), _p(out), x.size)
     return out
 
 
@@ -294,6 +317,14 @@ def globalsum(x):
 
 FOLD_OPS = {"sum": 0, "prod": 1, "max": 2, "min": 3, "mean": 4, "asum1": 5, "asum2": 6, "norm2": 7, "var": 8, "stdev": 9, "var1": 10, "stdev1": 11,
             "nbtrue": 12, "all": 13, "any": 14, "none": 15, "nansum": 16, "nanmean": 17, "meanad": 18}
+
+
+def median(x, lo, inner, hi, ad=False):
+    """NT2's median (ad: medianad) of x viewed as [lo, inner, hi] along inner."""
+    x = _f32(x)
+    out = np.empty(lo * hi, np.float32)
+    lib().o_median_f32(_p(x), lo, inner, hi, int(ad), _p(out))
+    return out
 
 
 def fold_nt2(x, lo, inner, hi, op, nthreads=None):

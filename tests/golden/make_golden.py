@@ -89,6 +89,7 @@ SOURCES = [
     ("modules/core/euler/unit/scalar/gammaln.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/digamma.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/signgam.cpp", 1, 200),
+    ("modules/core/euler/unit/scalar/dawson.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/erfinv.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/erfcinv.cpp", 1, 200),
     ("modules/core/exponential/unit/scalar/expx2.cpp", 1, 200),
@@ -116,6 +117,7 @@ CONST = {
     "Mindenormal": float(np.uint32(1).view(np.float32)), "Mtwo": -2.0, "Maxflint": 16777216.0, "Valmin": -float(np.finfo(np.float32).max),
     "Three": 3.0, "Four": 4.0, "Five": 5.0, "Mthree": -3.0,
     "Log_2": float(np.uint32(0x3f317218).view(np.float32)),
+    "Invexp_1": float(np.uint32(0x3ebc5ab2).view(np.float32)),
 }
 
 
@@ -147,6 +149,9 @@ def _value(expr):
     m = re.fullmatch(r"nt2::One<\w+>\(\)\s*/\s*10", expr)
     if m:
         return float(np.float32(1.0) / np.float32(10.0))
+    m = re.fullmatch(r"iT\(\s*(-?[0-9]+)\s*\)", expr)
+    if m:  # an integer argument (nthroot's n)
+        return float(int(m.group(1)))
     m = re.fullmatch(r"[-+]?[0-9]+(\.[0-9]*)?", expr)
     if m:  # an integer or decimal literal converted to the float r_t
         return float(np.float32(float(expr)))
@@ -170,7 +175,7 @@ def _value(expr):
 PAT = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(\w+)\((.*?)\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 # two-argument functors: pow(a, b)
 ARG = r"((?:[^,()]|\([^()]*\))*)"
-PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2d?|hypot|logspace_add|logspace_sub|beta|betaln)\(" + ARG + r",\s*" + ARG +
+PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2d?|hypot|logspace_add|logspace_sub|beta|betaln|nthroot|expni|gammainc)\(" + ARG + r",\s*" + ARG +
                   r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
             ("modules/core/trigonometric/unit/scalar/atan2.cpp", 47, 61),
@@ -179,7 +184,10 @@ SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
             ("modules/core/exponential/unit/scalar/logspace_add.cpp", 1, 200),
             ("modules/core/exponential/unit/scalar/logspace_sub.cpp", 1, 200),
             ("modules/core/euler/unit/scalar/beta.cpp", 1, 200),
-            ("modules/core/euler/unit/scalar/betaln.cpp", 1, 200)]
+            ("modules/core/euler/unit/scalar/betaln.cpp", 1, 200),
+            ("modules/core/exponential/unit/scalar/nthroot.cpp", 1, 200),
+            ("modules/core/euler/unit/scalar/expni.cpp", 1, 200),
+            ("modules/core/euler/unit/scalar/gammainc.cpp", 1, 200)]
 # expected values that are themselves results of NT2 functors (sin(Pio_4)/Pio_4)
 # are left out: they would pin the oracle to itself; so are values from
 # Boost.Math (boost::math::digamma), which is not part of the reference
@@ -277,6 +285,20 @@ def main(root):
                     source="modules/core/reduction/unit/table/globalsum.cpp:27-28"))
     out.append(dict(fn="dot_5x3_i_minus_j", expected=float(sum((i - j) ** 2 for i in range(1, 6) for j in range(1, 4))),
                     source="modules/core/reduction/unit/table/dot.cpp:46-59,73"))
+    # median / medianad of the 4 x 3 table y(i, j) = 4(j - 1) + i along each
+    # dimension (NT2_TEST_EQUAL, exact), and of [ones(4,1) zeros(4,1) ones(4,1)]
+    # along 2; the tables are column-major, [lo, inner, hi] as the fold ABI
+    y = [float(k) for k in range(1, 13)]
+    rel = "modules/core/reduction/unit/table/median.cpp"
+    for dim, shape, exp, lines in ((1, (1, 4, 3), [2.5, 6.5, 10.5], "42,48-53"), (2, (4, 3, 1), [5., 6., 7., 8.], "43,54-56"),
+                                   (3, (12, 1, 1), y, "57-59"), (4, (12, 1, 1), y, "60-62")):
+        out.append(dict(fn="median", x=y, shape=list(shape), expected=exp, source=f"{rel}:{lines}"))
+    out.append(dict(fn="median", x=[1.] * 4 + [0.] * 4 + [1.] * 4, shape=[4, 3, 1], expected=[1.] * 4,
+                    source=f"{rel}:64-77"))
+    rel = "modules/core/reduction/unit/table/medianad.cpp"
+    for dim, shape, exp, lines in ((1, (1, 4, 3), [1.] * 3, "41,48-51"), (2, (4, 3, 1), [4.] * 4, "42,53-54"),
+                                   (3, (12, 1, 1), [0.] * 12, "55-56"), (4, (12, 1, 1), [0.] * 12, "58-59")):
+        out.append(dict(fn="medianad", x=y, shape=list(shape), expected=exp, source=f"{rel}:{lines}"))
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "nt2_unit_vectors.json")
     with open(path, "w") as f:
         json.dump(out, f, indent=1, default=lambda v: v)

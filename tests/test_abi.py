@@ -345,7 +345,7 @@ UNARY_VJP_OPS = ["exp", "log", "log1p", "erfc", "normcdf", "fastnormcdf", "sqrt"
                  "tanpi", "cotpi", "cotd", "secpi", "cscpi", "secd", "cscd", "sinc", "sincpi", "acotd", "asec", "coth",
                  "sinhc", "acsc", "asech", "acoth", "acsch", "erf", "erfcx", "expx2", "gamma", "gammaln", "erfinv",
                  "erfcinv", "exprecneg", "exprecnegc", "sqrt1pm1", "floor", "ceil", "trunc", "round", "round2even",
-                 "frac", "sign", "signnz", "sqr"]
+                 "frac", "sign", "signnz", "sqr", "dawson"]
 
 
 def _vjp_programs(lib):
@@ -366,6 +366,8 @@ def _vjp_programs(lib):
          + E.fma(x, y, z) + E.fnms(x, y, z) + E.if_else(x > y, y, z) + E.selinc(x < z, y) + E.seldec(x > z, z)
          + E.if_zero_else_one(x < y, lib.F32) - (-x))
     progs.append(E.compile_program([torch.zeros(n)], [e])[0])
+    e = E.nthroot(x, 3.0) + E.nthroot(y, z) + E.expni(2.0, x) + E.expni(z, y) + E.gammainc(x, 2.5)
+    progs.append(E.compile_program([torch.zeros(n)], [e])[0])
     return progs
 
 
@@ -384,6 +386,22 @@ def test_vjp_kernel_source_builds_for_sm103a(lib):
     fold_prog, _ = E.compile_program([], [], fold=E.exp(x))
     n = ctypes.c_size_t()
     assert lib.load().nt2g_program_vjp_source(fold_prog.handle, 0, None, 0, ctypes.byref(n)) == lib.ERR_INVALID
+
+
+def test_integer_operand_and_incomplete_gamma_programs(lib):
+    """dawson, nthroot, expni and gammainc (double arithmetic inside) compile
+    for sm_103a in both policies; gammainc has a rule for x only, so reverse
+    mode through its a operand is refused with NT2G_ERR_UNSUPPORTED."""
+    nv = _nvrtc()
+    x, y = E.Table(torch.zeros(8)), E.Table(torch.zeros(8))
+    prog, _ = E.compile_program([torch.zeros(8), torch.zeros(8)],
+                                [E.dawson(x) + E.nthroot(x, y), E.expni(y, x) * E.gammainc(x, y)])
+    for prec in (lib.PREC_FAST, lib.PREC_NT2):
+        rc, log, size = _nvrtc_compile(nv, prog.jit_source(prec))
+        assert rc == 0, log[:2000]
+    n = ctypes.c_size_t()
+    assert lib.load().nt2g_program_vjp_source(prog.handle, 0, None, 0, ctypes.byref(n)) == lib.ERR_UNSUPPORTED
+    assert b"opcode 154" in lib.load().nt2g_last_error()
 
 
 def test_vjp_validates_slots(lib):

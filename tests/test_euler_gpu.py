@@ -217,3 +217,125 @@ def test_digamma_signgam_beta_betaln(lib, dev, oracle, prec):
         E.assign([o], [getattr(E, fn)(E.Table(tx), E.Table(ty))], precision=prec)
         for g, r in zip(o.cpu().numpy(), rs):
             assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+
+
+@pytest.mark.parametrize("prec", [1, 0], ids=["nt2", "fast"])
+def test_dawson_nthroot_expni(lib, dev, oracle, prec):
+    """dawson (map and program), nthroot(x, n) and expni(n, x) (programs; the
+    integer n carried in a float table): bit-identical to the oracle's
+    restatement of NT2's float algorithms under the NT2 policy; under the fast
+    one within a few ulp of FP64 (scipy's dawsn and expn, the double root) --
+    dawson 4, nthroot 2, expni 12 (NT2's own float expni reaches 10) -- with
+    NT2's NaN positions; NT2's known answers (dawson.cpp, nthroot.cpp,
+    expni.cpp) in both."""
+    from nt2_gb300 import expr as E
+    sp = pytest.importorskip("scipy.special")
+    rng = np.random.default_rng(33)
+    x = np.concatenate([rng.uniform(-12, 12, 1 << 16), np.exp(rng.uniform(-20, 25, 1 << 12)), SPECIALS,
+                        -SPECIALS]).astype(np.float32)
+    got = _run(lib, dev, "dawson", x, prec)
+    tx = torch.from_numpy(x).to(dev)
+    o = torch.empty_like(tx)
+    E.assign([o], [E.dawson(E.Table(tx))], precision=prec)
+    assert _same(o.cpu().numpy(), got).all()
+    ref = oracle.map_f32("dawson", x)
+    if prec == 1:
+        assert _same(got, ref).all()
+    else:
+        r64 = sp.dawsn(x.astype(np.float64))
+        ok = np.isfinite(r64) & (r64 != 0)
+        assert (np.abs(got[ok] - r64[ok]) / np.spacing(np.abs(r64[ok]).astype(np.float32))).max() <= 4.0
+        assert np.array_equal(np.isnan(got), np.isnan(ref))
+    # nthroot: x over both signs and many scales, n in [-7, 7] (0 and the even
+    # n of negative x included)
+    xs = np.concatenate([rng.uniform(-50, 50, 1 << 15), np.exp(rng.uniform(-30, 30, 1 << 13)), SPECIALS,
+                         -SPECIALS]).astype(np.float32)
+    ns = rng.integers(-7, 8, xs.size).astype(np.float32)
+    tx, tn = torch.from_numpy(xs).to(dev), torch.from_numpy(ns).to(dev)
+    o = torch.empty_like(tx)
+    E.assign([o], [E.nthroot(E.Table(tx), E.Table(tn))], precision=prec)
+    got = o.cpu().numpy()
+    ref = oracle.nthroot_f32(xs, ns)
+    if prec == 1:
+        assert _same(got, ref).all()
+    else:
+        assert np.array_equal(np.isnan(got), np.isnan(ref))
+        ok = np.isfinite(ref) & (ref != 0) & (ns != 0)
+        r64 = np.sign(xs[ok]).astype(np.float64) * np.abs(xs[ok].astype(np.float64)) ** (1.0 / ns[ok])
+        ulp = np.abs(got[ok] - r64) / np.spacing(np.abs(r64).astype(np.float32))
+        assert ulp.max() <= 2.0, (xs[ok][np.argmax(ulp)], ns[ok][np.argmax(ulp)], ulp.max())
+    # expni: n in [0, 40] and 6000 (the large-n expansion), x in (0, 90]
+    xe = np.concatenate([rng.uniform(0, 1, 1 << 13), rng.uniform(1, 90, 1 << 14), [0, -1, np.inf, np.nan]])
+    ne = np.concatenate([rng.integers(0, 41, xe.size - 1024), np.full(1024, 6000)]).astype(np.float32)
+    xe = xe.astype(np.float32)
+    tx, tn = torch.from_numpy(xe).to(dev), torch.from_numpy(ne).to(dev)
+    o = torch.empty_like(tx)
+    E.assign([o], [E.expni(E.Table(tn), E.Table(tx))], precision=prec)
+    got = o.cpu().numpy()
+    ref = oracle.expni_f32(ne, xe)
+    if prec == 1:
+        assert _same(got, ref).all()
+    else:
+        assert np.array_equal(np.isnan(got), np.isnan(ref))
+        r64 = sp.expn(ne.astype(np.int64), xe.astype(np.float64))
+        ok = np.isfinite(r64) & (r64 > 1e-37) & np.isfinite(ref)
+        ulp = np.abs(got[ok] - r64[ok]) / np.spacing(np.abs(r64[ok]).astype(np.float32))
+        assert ulp.max() <= 12.0, (xe[ok][np.argmax(ulp)], ne[ok][np.argmax(ulp)], ulp.max())
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
+    rs = [r for r in golden if r["fn"] == "dawson"]
+    for g, r in zip(_run(lib, dev, "dawson", np.float32([r["x"] for r in rs]), prec), rs):
+        assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+    for fn in ("nthroot", "expni"):
+        rs = [r for r in golden if r["fn"] == fn]
+        assert len(rs) >= 5
+        ta = torch.tensor([r["x"] for r in rs], dtype=torch.float32, device=dev)
+        tb = torch.tensor([r["y"] for r in rs], dtype=torch.float32, device=dev)
+        o = torch.empty_like(ta)
+        E.assign([o], [getattr(E, fn)(E.Table(ta), E.Table(tb))], precision=prec)
+        for g, r in zip(o.cpu().numpy(), rs):
+            assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+
+
+@pytest.mark.parametrize("prec", [1, 0], ids=["nt2", "fast"])
+def test_gammainc(lib, dev, prec):
+    """gammainc(x, a) = P(a, x) (NT2 calls Boost.Math's gamma_p, which works
+    in double for float arguments; this library's own double evaluation):
+    within 1 ulp of scipy's FP64 value for a up to 1e4, within 1 ulp of the
+    50-digit values of tests/golden/gammainc_large_a.json for a from 2e5 to
+    1e9 (where scipy itself is off by up to 1e6 ulp), identical bits in both
+    policies, NT2's special cases and known answers (gammainc.cpp)."""
+    from nt2_gb300 import expr as E
+    sp = pytest.importorskip("scipy.special")
+    rng = np.random.default_rng(44)
+    a = np.exp(rng.uniform(np.log(1e-3), np.log(1e4), 1 << 15))
+    x = a * np.exp(rng.uniform(-3, 1.5, a.size))
+    a = np.concatenate([a, [0, 0, 1, 1, 1, 1, 2, np.nan, -1, np.inf]]).astype(np.float32)
+    x = np.concatenate([x, [5, np.inf, np.inf, 0, -0.0, np.nan, -1, 1, 1, 1]]).astype(np.float32)
+
+    def run(xv, av, p):
+        tx, ta = torch.from_numpy(xv).to(dev), torch.from_numpy(av).to(dev)
+        o = torch.empty_like(tx)
+        E.assign([o], [E.gammainc(E.Table(tx), E.Table(ta))], precision=p)
+        return o.cpu().numpy()
+
+    got = run(x, a, prec)
+    assert _same(got, run(x, a, 1 - prec)).all()
+    with np.errstate(invalid="ignore"):
+        r64 = np.where((a == 0) | (x == np.inf), 1.0, sp.gammainc(a.astype(np.float64), x.astype(np.float64)))
+    r64 = np.where(np.isnan(x) | np.isnan(a) | (x < 0) | (a < 0) | np.isinf(a), np.nan, r64)
+    r64 = np.where((a == 0) | (x == np.inf), 1.0, r64)
+    assert np.array_equal(np.isnan(got), np.isnan(r64))
+    ok = np.isfinite(r64) & (r64 > 1e-37)
+    ulp = np.abs(got[ok] - r64[ok]) / np.spacing(np.abs(r64[ok]).astype(np.float32))
+    assert ulp.max() <= 1.0, (x[ok][np.argmax(ulp)], a[ok][np.argmax(ulp)], ulp.max())
+    assert (np.abs(got[~ok & ~np.isnan(r64)]) <= np.float32(2e-37)).all()  # P underflows to 0 there
+    big = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "gammainc_large_a.json")))
+    g = run(np.float32([r["x"] for r in big]), np.float32([r["a"] for r in big]), prec)
+    p = np.float64([r["p"] for r in big])
+    keep = p > 1e-37
+    assert (np.abs(g[keep] - p[keep]) / np.spacing(p[keep].astype(np.float32))).max() <= 1.0
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
+    rs = [r for r in golden if r["fn"] == "gammainc"]
+    assert len(rs) >= 5
+    for v, r in zip(run(np.float32([r["x"] for r in rs]), np.float32([r["y"] for r in rs]), prec), rs):
+        assert nt2_ulpdist(v, r["expected"]) <= r["tol_nt2ulp"], (r, v)

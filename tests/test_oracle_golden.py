@@ -20,7 +20,7 @@ FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1
          "coth", "sinhc", "sech", "csch", "asech", "acsch", "acoth",
          "floor", "ceil", "trunc", "round", "frac", "sign", "signnz", "sqr_abs",
          "erf", "erfcx", "gamma", "gammaln", "erfinv", "erfcinv", "expx2", "exprecneg", "exprecnegc", "sqrt1pm1",
-         "realsqrt", "reallog", "digamma", "signgam")
+         "realsqrt", "reallog", "digamma", "signgam", "dawson")
 # NT2's Nan<T>() has every bit set (its sign bit too): copysign(1, Nan) is -1
 NT2_NAN = float(np.uint32(0xffffffff).view(np.float32))
 
@@ -43,6 +43,85 @@ def test_oracle_matches_nt2_unit_tests(oracle, rec):
 def test_oracle_binary_matches_nt2_unit_tests(oracle, rec):
     got = getattr(oracle.lib(), "o_" + rec["fn"])(_arg(rec["x"]), _arg(rec["y"]))
     assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (got, rec)
+
+
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("nthroot", "expni")],
+                         ids=lambda r: f"{r['fn']}({r['x']},{r['y']})@{r['source'].split('/')[-1]}")
+def test_oracle_integer_operand_functors_match_nt2_unit_tests(oracle, rec):
+    """nthroot(x, n) and expni(n, x): NT2's integer operand as an int."""
+    L = oracle.lib()
+    if rec["fn"] == "nthroot":
+        got = L.o_nthroot(_arg(rec["x"]), int(rec["y"]))
+    else:
+        got = L.o_expni(int(rec["x"]), _arg(rec["y"]))
+    assert nt2_ulpdist(got, rec["expected"]) <= rec["tol_nt2ulp"], (got, rec)
+
+
+def gammainc_ref(x, a):
+    """NT2's gammainc(x, a) special cases (EUL/scalar/gammainc.hpp:37-43:
+    1 for a = 0 or x = +inf) over scipy's double P(a, x), rounded to float."""
+    sp = pytest.importorskip("scipy.special")
+    x, a = np.float64(x), np.float64(a)
+    if a == 0 or x == np.inf:
+        return np.float32(1.0)
+    if np.isnan(x) or np.isnan(a) or x < 0 or a < 0:
+        return np.float32(np.nan)
+    return np.float32(sp.gammainc(a, x))
+
+
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] == "gammainc"],
+                         ids=lambda r: f"gammainc({r['x']},{r['y']})")
+def test_gammainc_reference_matches_nt2_unit_tests(rec):
+    """The FP64 reference the GPU gammainc is checked against gives NT2's own
+    known answers (Boost.Math, which NT2 calls, is not in the reference)."""
+    assert nt2_ulpdist(gammainc_ref(rec["x"], rec["y"]), rec["expected"]) <= rec["tol_nt2ulp"], rec
+
+
+def test_oracle_dawson_nthroot_expni_accuracy_profile(oracle):
+    """NT2's float dawson, nthroot and expni as restated stay near FP64
+    (scipy's dawsn and expn, the double root): dawson within 4 ulp, nthroot
+    within 1, expni within 10 (NT2's float continued fraction and series)."""
+    sp = pytest.importorskip("scipy.special")
+    x = np.linspace(-20, 20, 4001).astype(np.float32)
+    got = oracle.map_f32("dawson", x)
+    ref = sp.dawsn(x.astype(np.float64))
+    nz = ref != 0
+    assert (np.abs(got[nz] - ref[nz]) / np.spacing(np.abs(ref[nz]).astype(np.float32))).max() <= 4.0
+    xs = np.linspace(0.001, 1000, 2000).astype(np.float32)
+    for n in (2, 3, 5, -3):
+        r = xs.astype(np.float64) ** (1.0 / n)
+        e = oracle.nthroot_f32(xs, np.full_like(xs, n))
+        assert (np.abs(e - r) / np.spacing(np.abs(r).astype(np.float32))).max() <= 1.0, n
+    xs = np.concatenate([np.linspace(0.01, 1, 100), np.linspace(1.01, 60, 400)]).astype(np.float32)
+    for n in (0, 1, 2, 5, 30, 6000):
+        r = sp.expn(n, xs.astype(np.float64))
+        e = oracle.expni_f32(np.full_like(xs, n), xs)
+        ok = r > 1e-37
+        assert (np.abs(e[ok] - r[ok]) / np.spacing(np.abs(r[ok]).astype(np.float32))).max() <= 10.0, n
+
+
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("median", "medianad")],
+                         ids=lambda r: f"{r['fn']}{tuple(r['shape'])}@{r['source'].split('/')[-1]}")
+def test_oracle_median_matches_nt2_unit_tests(oracle, rec):
+    """median / medianad of NT2's test tables along every dimension, exact."""
+    got = oracle.median(np.float32(rec["x"]), *rec["shape"], ad=rec["fn"] == "medianad")
+    assert np.array_equal(got, np.float32(rec["expected"])), (got, rec)
+
+
+def test_oracle_median_against_numpy(oracle):
+    """The oracle's median of random slices equals numpy's sorted middle
+    (numpy's median averages the two middle elements as (a + b) / 2, which
+    for finite floats equals meanof's m + (M - m) / 2 up to one rounding:
+    compared within one ulp), NaN for slices holding a NaN."""
+    rng = np.random.default_rng(5)
+    for lo, inner, hi in ((1, 7, 5), (1, 8, 5), (3, 10, 4), (6, 1, 2), (1, 1001, 3), (5, 64, 1)):
+        x = rng.standard_normal(lo * inner * hi).astype(np.float32)
+        got = oracle.median(x, lo, inner, hi)
+        ref = np.median(x.reshape(hi, inner, lo), axis=1).astype(np.float64).reshape(hi, lo).ravel()
+        out = got.reshape(hi, lo).ravel()
+        assert (np.abs(out - ref) <= np.spacing(np.abs(ref).astype(np.float32))).all(), (lo, inner, hi)
+    x = np.float32([1, 2, np.nan, 4, 5, 6])
+    assert np.isnan(oracle.median(x, 1, 3, 2)[0]) and oracle.median(x, 1, 3, 2)[1] == 5.0
 
 
 def test_oracle_pow_accuracy_profile(oracle):

@@ -295,14 +295,17 @@ def _unary_cases():
         "exprecneg": (lambda x: np.exp(-1 / x), 0.2, 5), "exprecnegc": (lambda x: 1 - np.exp(-1 / x), 0.2, 5),
         "sqrt1pm1": (lambda x: np.sqrt(1 + x) - 1, -0.5, 5), "normcdf": (sp.ndtr, -5, 5),
         "fastnormcdf": (lambda x: fastnormcdf64(x)[0], -5, 5), "frac": (lambda x: x - np.trunc(x), -10, 10),
+        "dawson": (sp.dawsn, -6, 6),
     }
 
 
 SIGNED = {"abs_", "cbrt", "rec", "acotd", "asec", "acsc", "acoth", "acsch", "coth"}
 UNARY_TOL = 4e-6  # |error| / (|derivative| + floor), away from each function's singularities
 # erfcx' = 2x erfcx(x) - 2/sqrt(pi) cancels as x grows: erfcx's own rounding
-# is magnified ~x^2 times (2e-5 at x = 5)
-UNARY_TOL_OF = {"erfcx": 2e-5}
+# is magnified ~x^2 times (2e-5 at x = 5); dawson' = 1 - 2x D(x) cancels to
+# zero at D's maximum (|x| = 0.924), where one rounding of 1 is 1.2e-5 of the
+# floor
+UNARY_TOL_OF = {"erfcx": 2e-5, "dawson": 2e-5}
 
 
 def _floor(name, x64, ref):
@@ -357,6 +360,7 @@ def test_binary_and_select_rules(lib, dev):
     """pow, atan2, hypot, division, min, max, copysign, fma, fnms, if_else,
     selinc, seldec: both (all three) operands' gradients against FP64 central
     differences; piecewise-constant operations pass no gradient."""
+    from scipy import special as sp
     n = 4096
     rng = np.random.default_rng(1010)
     x = rng.uniform(0.5, 3, n).astype(F32)
@@ -376,6 +380,14 @@ def test_binary_and_select_rules(lib, dev):
          lambda a, b, c: np.where(b > c, a * b, c) + np.where(a > 1, c + 1, c) + np.where(a < 2, b - 1, b)),
         (lambda a, b, c: E.floor(a) * b + E.sign(c) + E.round(b),
          lambda a, b, c: np.floor(a) * b + np.sign(c) + np.round(b)),
+        # integer operands (n) pass no gradient; gammainc's rule is for x only.
+        # One function a case: a sum of them would cross zero, where the
+        # terms' own rounding is no longer small against the 1e-3 floor
+        (lambda a, b, c: E.nthroot(a, 3.0) * b, lambda a, b, c: np.cbrt(a) * b),
+        (lambda a, b, c: E.nthroot(a, -2.0), lambda a, b, c: a ** -0.5),
+        (lambda a, b, c: E.expni(2.0, a), lambda a, b, c: sp.expn(2, a)),
+        (lambda a, b, c: E.expni(0.0, a), lambda a, b, c: sp.expn(0, a)),
+        (lambda a, b, c: E.gammainc(a, 2.5), lambda a, b, c: sp.gammainc(2.5, a)),
     ]
     ins = [x, y, z]
     t = [_t(dev, a) for a in ins]
