@@ -28,6 +28,7 @@ namespace nt2g {
 
 constexpr int64_t kSmemKeys = 40960;  // 160 KB of keys per block
 constexpr int64_t kChunk = 1 << 16;   // elements per block in the global passes
+constexpr int kLoadBatch = 8;         // loads a thread issues before it uses them
 
 // Order-preserving key: all bits of a negative float flipped, the sign bit
 // of a positive one set; unsigned comparison of keys is the float order.
@@ -102,10 +103,23 @@ __global__ void k_median_smem(const float *__restrict__ x, int64_t lo, int64_t n
     const float *base = x + l + lo * n * h;
     const float c = AD ? centre[s] : 0.0f;
     int nan = 0;
-    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
-        const float v = med_elem<AD>(base, lo, k, c);
-        nan |= v != v;
-        keys[k] = med_key(v);
+    // kLoadBatch loads in flight per thread before any is used: one at a time,
+    // the loop would wait a memory latency per element
+    for (int64_t k0 = threadIdx.x; k0 < n; k0 += kLoadBatch * (int64_t)blockDim.x) {
+        float v[kLoadBatch];
+#pragma unroll
+        for (int j = 0; j < kLoadBatch; ++j) {
+            const int64_t k = k0 + j * (int64_t)blockDim.x;
+            v[j] = k < n ? med_elem<AD>(base, lo, k, c) : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < kLoadBatch; ++j) {
+            const int64_t k = k0 + j * (int64_t)blockDim.x;
+            if (k < n) {
+                nan |= v[j] != v[j];
+                keys[k] = med_key(v[j]);
+            }
+        }
     }
     if (__syncthreads_or(nan)) {
         if (threadIdx.x == 0) out[s] = __uint_as_float(0x7fc00000u);
@@ -191,11 +205,22 @@ __global__ void __launch_bounds__(256) k_median_hist(const float *__restrict__ x
     __syncthreads();
     const int64_t k0 = blockIdx.x * kChunk, k1 = k0 + kChunk < n ? k0 + kChunk : n;
     int nan = 0;
-    for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-        const float v = med_elem<AD>(base, lo, k, c);
-        nan |= v != v;
-        const uint32_t key = med_key(v);
-        if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+    for (int64_t kb = k0 + threadIdx.x; kb < k1; kb += kLoadBatch * (int64_t)blockDim.x) {
+        float v[kLoadBatch];
+#pragma unroll
+        for (int j = 0; j < kLoadBatch; ++j) {
+            const int64_t k = kb + j * (int64_t)blockDim.x;
+            v[j] = k < k1 ? med_elem<AD>(base, lo, k, c) : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < kLoadBatch; ++j) {
+            const int64_t k = kb + j * (int64_t)blockDim.x;
+            if (k < k1) {
+                nan |= v[j] != v[j];
+                const uint32_t key = med_key(v[j]);
+                if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+            }
+        }
     }
     if (shift == 24 && __syncthreads_or(nan) && threadIdx.x == 0) atomicOr(&st[s].nan, 1u);
     __syncthreads();
@@ -235,9 +260,18 @@ __global__ void __launch_bounds__(256) k_median_next(const float *__restrict__ x
     const uint32_t prefix = st[s].prefix;
     const int64_t k0 = blockIdx.x * kChunk, k1 = k0 + kChunk < n ? k0 + kChunk : n;
     uint32_t m = 0xffffffffu;
-    for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-        const uint32_t key = med_key(med_elem<AD>(base, lo, k, c));
-        if (key > prefix && key < m) m = key;
+    for (int64_t kb = k0 + threadIdx.x; kb < k1; kb += kLoadBatch * (int64_t)blockDim.x) {
+        float v[kLoadBatch];
+#pragma unroll
+        for (int j = 0; j < kLoadBatch; ++j) {
+            const int64_t k = kb + j * (int64_t)blockDim.x;
+            v[j] = k < k1 ? med_elem<AD>(base, lo, k, c) : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < kLoadBatch; ++j) {
+            const uint32_t key = med_key(v[j]);
+            if (kb + j * (int64_t)blockDim.x < k1 && key > prefix && key < m) m = key;
+        }
     }
     m = __reduce_min_sync(0xffffffffu, m);
     if ((threadIdx.x & 31) == 0 && m != 0xffffffffu) atomicMin(&st[s].key2, m);

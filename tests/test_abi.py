@@ -153,6 +153,26 @@ def test_direct_entry_points_validate_before_touching_the_gpu(lib):
     assert "workspace" in L.nt2g_last_error().decode()
 
 
+def test_median_validates_before_touching_the_gpu(lib):
+    """nt2g_median_f32: op, extents, NULL tables, overlap and the workspace of
+    long slices are checked first; no slices is no work; slices up to 40960
+    elements need no workspace."""
+    L = lib.load()
+    nb = ctypes.c_size_t()
+    assert L.nt2g_median_workspace_size(1, 40960, 7, ctypes.byref(nb)) == lib.OK and nb.value == 0
+    assert L.nt2g_median_workspace_size(3, 40961, 2, ctypes.byref(nb)) == lib.OK and nb.value == 6 * (2048 + 32)
+    assert L.nt2g_median_workspace_size(-1, 4, 2, ctypes.byref(nb)) == lib.ERR_INVALID
+    x, out = ctypes.c_void_p(1 << 20), ctypes.c_void_p(1 << 30)
+    assert L.nt2g_median_f32(x, 1, 10, 4, 2, NULL, 0, out, NULL) == lib.ERR_INVALID  # op
+    assert L.nt2g_median_f32(x, 1, -10, 4, 0, NULL, 0, out, NULL) == lib.ERR_INVALID
+    assert L.nt2g_median_f32(x, 1, 10, 4, 0, NULL, 0, NULL, NULL) == lib.ERR_INVALID  # out
+    assert L.nt2g_median_f32(NULL, 1, 10, 4, 0, NULL, 0, out, NULL) == lib.ERR_INVALID  # x
+    assert L.nt2g_median_f32(x, 1, 10, 4, 0, NULL, 0, ctypes.c_void_p((1 << 20) + 8), NULL) == lib.ERR_INVALID
+    assert L.nt2g_median_f32(x, 1, 50000, 2, 0, NULL, 0, out, NULL) == lib.ERR_INVALID  # workspace
+    assert "workspace" in L.nt2g_last_error().decode()
+    assert L.nt2g_median_f32(NULL, 0, 10, 4, 1, NULL, 0, NULL, NULL) == lib.OK  # no slices
+
+
 def test_eval_validates_arguments(lib):
     x = E.Table(torch.zeros(8))
     out = torch.zeros(8)

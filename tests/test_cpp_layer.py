@@ -117,8 +117,9 @@ def test_sigmadelta_through_tables(demos, oracle, tmp_path):
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", ["1", "0"], ids=["nt2", "fast"])
 def test_folds_through_tables(demos, oracle, tmp_path, prec):
-    """sum(A, 1), sum(A, 2), maximum/minimum/mean/norm2/var/stdev along a
-    dimension and the global forms of an M x N table through the C++ layer."""
+    """sum(A, 1), sum(A, 2), maximum/minimum/mean/norm2/var/stdev/meanad/
+    median/medianad along a dimension, wmean, and the global forms of an M x N
+    table through the C++ layer."""
     m, n = 1000, 777
     rng = np.random.default_rng(21)
     a = (rng.standard_normal(m * n) * np.exp2(rng.integers(-6, 6, m * n))).astype(np.float32)
@@ -173,6 +174,14 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
         else:
             ref, _, _ = oracle.fold_ref(a, 1, m * n, 1, op)
             assert abs(float(glob[key][0]) - ref[0]) <= 2 * np.spacing(np.float32(abs(ref[0]))), key
+    # median(A, 1), median(h, 2) of the host table, medianad(A) and the global
+    # forms: the same order statistics under either policy
+    for name, shape, ad in (("median1", (1, m, n), False), ("median2", (m, n, 1), False),
+                            ("medianad1", (1, m, n), True)):
+        got = np.fromfile(tmp_path / f"{name}.bin", np.float32)
+        assert np.array_equal(got, oracle.median(a, *shape, ad=ad)), name
+    assert np.float32(glob["globalmedian"][0]) == oracle.median(a, 1, m * n, 1)[0]
+    assert np.float32(glob["globalmedianad"][0]) == oracle.median(a, 1, m * n, 1, ad=True)[0]
 
 
 @pytest.mark.gpu
