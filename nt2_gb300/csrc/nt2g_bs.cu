@@ -185,9 +185,18 @@ __global__ void __launch_bounds__(256) k_bs_demo(const float *__restrict__ S, co
             float4 rr = RT ? ld_stream((const float4 *)rt + i) : make_float4(r, r, r, r);
             float4 vv = VT ? ld_stream((const float4 *)vt + i) : make_float4(v, v, v, v);
             float4 o;
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                set(o, j, bs_demo_option<P>(get(s, j), get(x, j), get(t, j), get(rr, j), get(vv, j)));
+            if constexpr (!P::exact) {  // two options per packed instruction
+                f2 c2 = bs_demo_fast2(pk(s.x, s.y), pk(x.x, x.y), pk(t.x, t.y), pk(rr.x, rr.y), pk(vv.x, vv.y));
+                upk(c2, o.x, o.y);
+                c2 = bs_demo_fast2(pk(s.z, s.w), pk(x.z, x.w), pk(t.z, t.w), pk(rr.z, rr.w), pk(vv.z, vv.w));
+                upk(c2, o.z, o.w);
+            } else {  // NT2's unfused arithmetic two options per packed instruction, bit for bit
+                const f2 nz = pair_negzero();
+                f2 c2 = bs_demo_nt2_2(pk(s.x, s.y), pk(x.x, x.y), pk(t.x, t.y), pk(rr.x, rr.y), pk(vv.x, vv.y), nz);
+                upk(c2, o.x, o.y);
+                c2 = bs_demo_nt2_2(pk(s.z, s.w), pk(x.z, x.w), pk(t.z, t.w), pk(rr.z, rr.w), pk(vv.z, vv.w), nz);
+                upk(c2, o.z, o.w);
+            }
             st_stream((float4 *)R + i, o);
         }
         done = nv << 2;

@@ -541,7 +541,18 @@ nt2g_status launch_map(int fn, const float *x, float *y, int64_t n, int precisio
 // the opcode switch never diverges.
 constexpr int kV = 4;
 
-template <class P>
+// The functors that work in double or loop (digamma, dawson, nthroot, expni,
+// gammainc) are compiled only into the RARE instance of the interpreter, which
+// runs the programs that use them: in the opcode switch of every program they
+// would raise the kernel's register count from 42 to 62 and cut its
+// occupancy.
+NT2G_HD bool interp_rare_op(int op)
+{
+    return op == NT2G_OP_DIGAMMA || op == NT2G_OP_DAWSON || op == NT2G_OP_NTHROOT || op == NT2G_OP_EXPNI ||
+           op == NT2G_OP_GAMMAINC;
+}
+
+template <class P, bool RARE>
 __device__ __forceinline__ float f_unary(int op, float a)
 {
     switch (op) {
@@ -606,8 +617,8 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_ERFINV: return erfinv<P>(a);
     case NT2G_OP_ERFCINV: return erfcinv<P>(a);
     case NT2G_OP_SIGNGAM: return signgam(a);
-    case NT2G_OP_DIGAMMA: return digamma<P>(a);
-    case NT2G_OP_DAWSON: return dawson<P>(a);
+    case NT2G_OP_DIGAMMA: if constexpr (RARE) return digamma<P>(a); else return f_nan();
+    case NT2G_OP_DAWSON: if constexpr (RARE) return dawson<P>(a); else return f_nan();
     case NT2G_OP_FLOOR: return floorf(a);
     case NT2G_OP_CEIL: return ceilf(a);
     case NT2G_OP_TRUNC: return truncf(a);
@@ -623,7 +634,7 @@ __device__ __forceinline__ float f_unary(int op, float a)
     }
 }
 
-template <class P>
+template <class P, bool RARE>
 __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs args, int64_t n, int vec)
 {
     uint32_t R[kMaxRegs][kV];
@@ -731,9 +742,12 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
             case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI: case NT2G_OP_GAMMAINC:
                 for (int j = 0; j < kV; ++j) {
                     const float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]);
-                    d[j] = __float_as_uint(in.op == NT2G_OP_NTHROOT ? nthroot<P>(x, int_operand(y))
-                                           : in.op == NT2G_OP_EXPNI ? expni<P>(int_operand(x), y)
-                                                                    : gammainc<P>(x, y));
+                    float r = f_nan();
+                    if constexpr (RARE)
+                        r = in.op == NT2G_OP_NTHROOT ? nthroot<P>(x, int_operand(y))
+                          : in.op == NT2G_OP_EXPNI   ? expni<P>(int_operand(x), y)
+                                                     : gammainc<P>(x, y);
+                    d[j] = __float_as_uint(r);
                 }
                 break;
             case NT2G_OP_FMA: case NT2G_OP_FNMS:
@@ -797,7 +811,7 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
             default:  // unary float functions
 #pragma unroll
                 for (int j = 0; j < kV; ++j) {
-                    if (f32) d[j] = __float_as_uint(f_unary<P>(in.op, __uint_as_float(A[j])));
+                    if (f32) d[j] = __float_as_uint(f_unary<P, RARE>(in.op, __uint_as_float(A[j])));
                     else d[j] = in.op == NT2G_OP_NEG ? ((0u - A[j]) & 255u)
                               : in.op == NT2G_OP_SQR ? ((A[j] * A[j]) & 255u) : A[j];  // ABS: identity
                 }
@@ -814,10 +828,18 @@ nt2g_status launch_interp(const DProgram &prog, const DArgs &args, int64_t count
     for (int s = 0; s < kMaxSlots; ++s)
         if (args.ptr[s] && args.dtype[s] == NT2G_F32) vec &= aligned16(args.ptr[s]);
     int64_t units = (count + kV - 1) / kV;
-    if (precision == NT2G_PREC_NT2)
-        k_interp<Nt2><<<persistent_blocks(k_interp<Nt2>, 128, 0, 128, units), 128, 0, st>>>(prog, args, count, vec);
-    else
-        k_interp<Fast><<<persistent_blocks(k_interp<Fast>, 128, 0, 128, units), 128, 0, st>>>(prog, args, count, vec);
+    bool rare = false;
+    for (int i = 0; i < prog.n; ++i) rare |= interp_rare_op(prog.ins[i].op);
+#define NT2G_INTERP(PP, R)                                                                                      \
+    k_interp<PP, R><<<persistent_blocks(k_interp<PP, R>, 128, 0, 128, units), 128, 0, st>>>(prog, args, count, vec)
+    if (precision == NT2G_PREC_NT2) {
+        if (rare) NT2G_INTERP(Nt2, true);
+        else NT2G_INTERP(Nt2, false);
+    } else {
+        if (rare) NT2G_INTERP(Fast, true);
+        else NT2G_INTERP(Fast, false);
+    }
+#undef NT2G_INTERP
     NT2G_LAUNCH_CHECK("interpreter launch");
     return NT2G_OK;
 }

@@ -266,6 +266,49 @@ __device__ __forceinline__ void bs_vec4_fast(const float4 &s, const float4 &k, c
     upk(p2, p.z, p.w);
 }
 
+// fastnormcdf (STAT/generic/fastnormcdf.hpp:33-55) for two lanes under the
+// fast policy: k = 1/(1 + 0.2316419 l), l = |x| (the SFU reciprocal and one
+// Newton step), w = k H(k) phi(l) with H NT2's degree-4 polynomial and
+// phi(l) = e^(-l^2/2)/sqrt(2 pi) from the exactly split exponent and the
+// SFU's 2^x (bs_exp_half_sq2); 1 - w above 0.  From |x| = 13 on, phi is below
+// 1e-37: the result is 1 or 0 there (the scalar form's w is a subnormal).
+__device__ __forceinline__ f2 fastnormcdf_fast2(f2 x)
+{
+    float x0, x1;
+    upk(x, x0, x1);
+    const f2 l = pk(fminf(fabsf(x0), 13.0f), fminf(fabsf(x1), 13.0f));
+    const f2 k = inv_fast2(fma2(dup(0.2316419f), l, dup(1.0f)), fma2(dup(-0.2316419f), l, dup(-1.0f)));
+    const f2 h = horner2(k, dup(bits_f(0x3faa466fu)), bits_f(0xbfe91eeau), bits_f(0x3fe40778u), bits_f(0xbeb68f87u),
+                         bits_f(0x3ea385fau));
+    f2 sc;
+    const f2 el = bs_exp_half_sq2(l, sc);
+    const f2 w = mul2(mul2(h, k), mul2(fma2(el, sc, sc), dup(bits_f(NT2G_INVSQRT_2PI))));
+    float w0, w1;
+    upk(w, w0, w1);
+    float r0 = x0 > 0.0f ? 1.0f - w0 : w0, r1 = x1 > 0.0f ? 1.0f - w1 : w1;
+    r0 = fabsf(x0) >= 13.0f ? (x0 > 0.0f ? 1.0f : 0.0f) : r0;
+    r1 = fabsf(x1) >= 13.0f ? (x1 > 0.0f ? 1.0f : 0.0f) : r1;
+    return pk(is_nan(x0) ? x0 : r0, is_nan(x1) ? x1 : r1);
+}
+
+// NT2's demo Black-Scholes (demo/blackscholes/nt2/blackandscholes_nt2.cpp:55-59)
+// for two options under the fast policy: call only, fastnormcdf,
+// d1 = log(S/X) + fma(v^2, 1/2, r) T / (v sqrt(T)), d2 = d1 - v sqrt(T),
+// R = S N(d1) - X e^(-rT) N(d2); sqrt(T) as T rsqrt(T), e^(-rT) from the
+// SFU's 2^x, the log on the split mantissa (log_pos_fast2).
+__device__ __forceinline__ f2 bs_demo_fast2(f2 S, f2 X, f2 T, f2 r, f2 v)
+{
+    const f2 da = mul2(T, rsqrt_fast2(T));
+    const f2 lq = log_pos_fast2(fdiv2(S, X, neg2(X)));
+    const f2 num = mul2(fma2(mul2(v, v), dup(0.5f), r), T);
+    const f2 vda = mul2(v, da);
+    const f2 d1 = add2(lq, fdiv2(num, vda, neg2(vda)));
+    const f2 d2 = fma2(neg2(v), da, d1);
+    const f2 ert = lanes(mul2(mul2(r, dup(-0x1.715476p+0f)), T), ex2_approx);
+    const f2 a = mul2(S, fastnormcdf_fast2(d1));
+    return fma2(neg2(mul2(X, ert)), fastnormcdf_fast2(d2), a);
+}
+
 // ------------------------------------------------------------ NT2 policy --
 // The bit-exact policy two options at a time.  NT2's arithmetic is unfused
 // (its fma is a rounded product and a rounded sum), and add/sub.rn.f32x2
@@ -429,6 +472,34 @@ __device__ __forceinline__ void bs_option_nt2_2(f2 S, f2 K, f2 T, f2 sig, f2 a, 
     normcdf_pair_nt2_2(d2, n2, m2, nz);
     call = sub2(nmul2(S, n1, nz), nmul2(e, n2, nz));
     put = sub2(nmul2(e, m2, nz), nmul2(S, m1, nz));
+}
+
+// fastnormcdf<Nt2>, lane for lane: k = 1/(0.2316419 l + 1), NT2's unfused
+// Horner, w *= (k / sqrt(2 pi)) exp(-(l*l) * 1/2), 1 - w above 0.
+__device__ __forceinline__ f2 fastnormcdf_nt2_2(f2 x, f2 nz)
+{
+    const f2 l = abs2(x);
+    const f2 k = div_rn2(dup(1.0f), add2(nmul2(dup(0.2316419f), l, nz), dup(1.0f)));
+    f2 w = nt2_horner2(nz, k, dup(bits_f(0x3faa466fu)), 0xbfe91eeau, 0x3fe40778u, 0xbeb68f87u, 0x3ea385fau);
+    const f2 e = exp_nt2_2(nmul2(negx2(nmul2(l, l, nz)), dup(0.5f), nz), nz);
+    w = nmul2(w, nmul2(nmul2(k, dup(bits_f(NT2G_INVSQRT_2PI)), nz), e, nz), nz);
+    const f2 o = sub2(dup(1.0f), w);
+    float x0, x1;
+    upk(x, x0, x1);
+    return sel2(x0 > 0.0f, x1 > 0.0f, o, w);
+}
+
+// bs_demo_option<Nt2> for two options, lane for lane.
+__device__ __forceinline__ f2 bs_demo_nt2_2(f2 S, f2 X, f2 T, f2 r, f2 v, f2 nz)
+{
+    const f2 da = sqrt_rn2(T);
+    const f2 a = add2(nmul2(nmul2(v, v, nz), dup(0.5f), nz), r);  // fma(sqr(v), 0.5, r), unfused
+    const f2 vda = nmul2(v, da, nz);
+    const f2 d1 = add2(log_nt2_2(div_rn2(S, X), nz), div_rn2(nmul2(a, T, nz), vda));
+    const f2 d2 = sub2(d1, vda);
+    const f2 p = nmul2(S, fastnormcdf_nt2_2(d1, nz), nz);
+    const f2 b = nmul2(X, exp_nt2_2(nmul2(negx2(r), T, nz), nz), nz);
+    return sub2(p, nmul2(b, fastnormcdf_nt2_2(d2, nz), nz));
 }
 
 // Four options as two pairs under the NT2 policy; sigma per option.
