@@ -298,9 +298,9 @@ __device__ __forceinline__ void bs_vjp_option(float S, float K, float T, float s
     const float sq = f.sq, ert = f.ert, e = f.e;
     C = Fast::fma(-e, n2, Fast::mul(S, n1));
     P_ = Fast::fma(-S, m1, Fast::mul(e, m2));
-    const float z = Fast::sub(f.d1, f.d1);  // as the forward kernel: NaN unless d1 is finite
-    C = Fast::add(C, z);
-    P_ = Fast::add(P_, z);
+    const bool bad = !(fabsf(f.d1) < f_inf());  // as the forward kernel: NaN unless d1 is finite
+    C = bad ? f_nan() : C;
+    P_ = bad ? f_nan() : P_;
     // the gradients take N(d) and phi(d) at the exact d: first-order
     // corrections N(d + dd) = N(d) + phi(d) dd, phi(d + dd) = phi(d)(1 - d dd)
     const float inv_sqrt_2pi = 0.398942280401432678f;

@@ -186,9 +186,9 @@ __device__ __forceinline__ void bs_option(float S, float K, float T, float sig, 
     bs_normcdfs_fast(f.d1, f.d2, S, f.e, n1, m1, n2, m2);
     call = Fast::fma(-f.e, n2, Fast::mul(S, n1));
     put = Fast::fma(-S, m1, Fast::mul(f.e, m2));
-    const float z = Fast::sub(f.d1, f.d1);  // NaN unless d1 is finite (d2 follows d1)
-    call = Fast::add(call, z);
-    put = Fast::add(put, z);
+    const bool bad = !(fabsf(f.d1) < f_inf());  // NaN unless d1 is finite (d2 follows d1)
+    call = bad ? f_nan() : call;
+    put = bad ? f_nan() : put;
 }
 
 // 1/sigma per option when sigma is a table (rcp.approx + one Newton step).

@@ -54,7 +54,6 @@ __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c)
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d.v) : "l"(a.v), "l"(b.v), "l"(c.v));
     return d;
 }
-__device__ __forceinline__ f2 neg2(f2 a) { return mul2(a, dup(-1.0f)); }  // exact
 // -a by flipping both sign bits (integer pipe, exact, no FP32 slot)
 __device__ __forceinline__ f2 negx2(f2 a)
 {
@@ -62,6 +61,7 @@ __device__ __forceinline__ f2 negx2(f2 a)
     r.v = a.v ^ 0x8000000080000000ull;
     return r;
 }
+__device__ __forceinline__ f2 neg2(f2 a) { return negx2(a); }
 template <class F> __device__ __forceinline__ f2 lanes(f2 a, F f)
 {
     float x, y;
@@ -242,14 +242,19 @@ __device__ __forceinline__ void bs_option_fast2(f2 S, f2 K, f2 T, f2 sig, f2 inv
     f2 d2 = fma2(neg2(sig), sq, d1);
     f2 ert = lanes(mul2(dup(bs_neg_rate_log2e(r)), T), ex2_approx);
     f2 e = mul2(K, ert);
-    f2 ne = mul2(nK, ert);
     f2 n1, m1, n2, m2;
     bs_normcdfs_fast2(d1, d2, S, e, n1, m1, n2, m2);
-    call = fma2(ne, n2, mul2(S, n1));
-    put = fma2(neg2(S), m1, mul2(e, m2));
-    const f2 z = sub2(d1, d1);  // NaN unless d1 is finite
-    call = add2(call, z);
-    put = add2(put, z);
+    call = fma2(negx2(e), n2, mul2(S, n1));  // -(K e^-rT) exactly, on the integer pipe
+    put = fma2(negx2(S), m1, mul2(e, m2));
+    // NaN unless d1 is finite (d2 follows d1): a test and a select per lane
+    // on the integer pipe rather than FP32 work
+    float d10, d11, c0, c1, p0, p1;
+    upk(d1, d10, d11);
+    upk(call, c0, c1);
+    upk(put, p0, p1);
+    const bool bad0 = !(fabsf(d10) < f_inf()), bad1 = !(fabsf(d11) < f_inf());
+    call = pk(bad0 ? f_nan() : c0, bad1 ? f_nan() : c1);
+    put = pk(bad0 ? f_nan() : p0, bad1 ? f_nan() : p1);
 }
 
 // Four options (one float4 of each table) as two pairs, sigma and 1/sigma
