@@ -436,6 +436,7 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 71) return digamma<P>(a);
     if (FN == 72) return signgam(a);
     if (FN == 73) return dawson<P>(a);
+    if (FN == 74) return spence<P>(a);
     if (FN == 80) return exprecneg<P>(a);
     if (FN == 81) return exprecnegc<P>(a);
     if (FN == 82) return sqrt1pm1<P>(a);
@@ -517,6 +518,7 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 71: NT2G_MAP(71); break;
     case 72: NT2G_MAP(72); break;
     case 73: NT2G_MAP(73); break;
+    case 74: NT2G_MAP(74); break;
     case 80: NT2G_MAP(80); break;
     case 81: NT2G_MAP(81); break;
     case 82: NT2G_MAP(82); break;
@@ -541,15 +543,15 @@ nt2g_status launch_map(int fn, const float *x, float *y, int64_t n, int precisio
 // the opcode switch never diverges.
 constexpr int kV = 4;
 
-// The functors that work in double or loop (digamma, dawson, nthroot, expni,
-// gammainc) are compiled only into the RARE instance of the interpreter, which
+// The functors that work in double or loop (digamma, dawson, spence, nthroot,
+// expni, gammainc) are compiled only into the RARE instance of the interpreter, which
 // runs the programs that use them: in the opcode switch of every program they
 // would raise the kernel's register count from 42 to 62 and cut its
 // occupancy.
 NT2G_HD bool interp_rare_op(int op)
 {
     return op == NT2G_OP_DIGAMMA || op == NT2G_OP_DAWSON || op == NT2G_OP_NTHROOT || op == NT2G_OP_EXPNI ||
-           op == NT2G_OP_GAMMAINC;
+           op == NT2G_OP_GAMMAINC || op == NT2G_OP_SPENCE;
 }
 
 template <class P, bool RARE>
@@ -619,6 +621,7 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_SIGNGAM: return signgam(a);
     case NT2G_OP_DIGAMMA: if constexpr (RARE) return digamma<P>(a); else return f_nan();
     case NT2G_OP_DAWSON: if constexpr (RARE) return dawson<P>(a); else return f_nan();
+    case NT2G_OP_SPENCE: if constexpr (RARE) return spence<P>(a); else return f_nan();
     case NT2G_OP_FLOOR: return floorf(a);
     case NT2G_OP_CEIL: return ceilf(a);
     case NT2G_OP_TRUNC: return truncf(a);

@@ -274,6 +274,7 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         case NT2G_OP_SIGNGAM: e = "nt2g::signgam(" + A + ")"; break;
         case NT2G_OP_DIGAMMA: e = "nt2g::digamma<P>(" + A + ")"; break;
         case NT2G_OP_DAWSON: e = "nt2g::dawson<P>(" + A + ")"; break;
+        case NT2G_OP_SPENCE: e = "nt2g::spence<P>(" + A + ")"; break;
         case NT2G_OP_NTHROOT: e = "nt2g::nthroot<P>(" + A + ", nt2g::int_operand(" + B + "))"; break;
         case NT2G_OP_EXPNI: e = "nt2g::expni<P>(nt2g::int_operand(" + A + "), " + B + ")"; break;
         case NT2G_OP_GAMMAINC: e = "nt2g::gammainc<P>(" + A + ", " + B + ")"; break;
@@ -632,6 +633,9 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
     case NT2G_OP_GAMMA: to(o.a, G + " * " + Y + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
     case NT2G_OP_GAMMALN: to(o.a, G + " * nt2g::vjp::digamma<D>(" + A + ")"); break;
     case NT2G_OP_DAWSON: to(o.a, G + " * (1.0f - 2.0f * " + A + " * " + Y + ")"); break;
+    case NT2G_OP_SPENCE:  // -log(x) / (x - 1), -1 at x = 1 (x - 1 exact near 1)
+        to(o.a, "(" + A + " == 1.0f ? -" + G + " : -" + G + " * nt2g::log<D>(" + A + ") * " + rcp(A + " - 1.0f") + ")");
+        break;
     case NT2G_OP_NTHROOT:  // y / (n x); the integer n passes no gradient
         to(o.a, G + " * " + Y + " * " + rcp("(float)nt2g::int_operand(" + B + ") * " + A));
         break;

@@ -2116,6 +2116,46 @@ template <class P> NT2G_HD float dawson(float a0)
     return copysignf(P::mul(0.5f, y), a0);
 }
 
+// -------------------------------------------------------------- spence --
+// NT2's float dilogarithm (EUL/scalar/spence.hpp:27-70, Cephes' spencef):
+// NaN below 0, 0 at 1, pi^2/6 at 0; x > 2 maps to 1/x and x > 1.5 to
+// w = 1/x - 1 (flag 2), x < 1/2 to w = -x (flag 1), else w = x - 1;
+// y = -w P(w) (degree 10), then pi^2/6 - log(x) log(1 - x) - y for flag 1 and
+// -(1/2) log(x)^2 - y for flag 2.
+template <class P> NT2G_HD float spence(float a0)
+{
+    float x = a0;
+    if (x < 0.0f) return f_nan();
+    if (x == 1.0f) return 0.0f;
+    const float pi2o6 = bits_f(0x3fd28d33u);
+    if (x == 0.0f) return pi2o6;
+    int flag = 0;
+    if (x > 2.0f) {
+        x = P::div(1.0f, x);
+        flag |= 2;
+    }
+    float w;
+    if (x > 1.5f) {
+        w = P::sub(P::div(1.0f, x), 1.0f);
+        flag |= 2;
+    } else if (x < 0.5f) {
+        w = -x;
+        flag |= 1;
+    } else {
+        w = P::sub(x, 1.0f);
+    }
+    float y = P::mul(-w, horner<P>(w, bits_f(0x3c80e79eu), bits_f(0xbc8a8ad6u), bits_f(0x3c1f4a7fu),
+                                   bits_f(0xbc604c2fu), bits_f(0x3caa7af5u), bits_f(0xbce56409u),
+                                   bits_f(0x3d23ba15u), bits_f(0xbd7ff525u), bits_f(0x3de38e97u),
+                                   bits_f(0xbe800004u), bits_f(0x3f800000u)));
+    if (flag & 1) y = P::sub(P::sub(pi2o6, P::mul(log<P>(x), log<P>(P::sub(1.0f, x)))), y);
+    if (flag & 2) {
+        const float z = log<P>(x);
+        y = P::sub(P::mul(-0.5f, P::mul(z, z)), y);
+    }
+    return y;
+}
+
 // An integer operand carried in a float (nthroot's n, expni's n): truncated
 // toward zero, saturated to the int32 range, NaN as 0.
 NT2G_HD int32_t int_operand(float b)

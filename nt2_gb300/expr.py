@@ -118,6 +118,7 @@ gammaln = _un("GAMMALN")
 digamma = _un("DIGAMMA")
 signgam = _un("SIGNGAM")
 dawson = _un("DAWSON")
+spence = _un("SPENCE")
 
 
 # NT2's beta and betaln, built as NT2 writes them (EUL/scalar/beta.hpp:

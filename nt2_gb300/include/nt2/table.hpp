@@ -670,6 +670,7 @@ NT2G_UNARY(gammaln, NT2G_OP_GAMMALN)
 NT2G_UNARY(digamma, NT2G_OP_DIGAMMA)
 NT2G_UNARY(signgam, NT2G_OP_SIGNGAM)
 NT2G_UNARY(dawson, NT2G_OP_DAWSON)
+NT2G_UNARY(spence, NT2G_OP_SPENCE)
 NT2G_UNARY(erfinv, NT2G_OP_ERFINV)
 NT2G_UNARY(erfcinv, NT2G_OP_ERFCINV)
 NT2G_UNARY(floor, NT2G_OP_FLOOR)

@@ -1165,6 +1165,41 @@ EXPORT float o_dawson(float a0)
     return copysignf(0.5f * y, a0);
 }
 
+/* spence EUL/scalar/spence.hpp:27-70 (Cephes spencef, the float coefficients
+ * by bit pattern; Pi2o_6 = 0x3fd28d33). */
+static const uint32_t SPENCE_P[11] = {0x3c80e79e, 0xbc8a8ad6, 0x3c1f4a7f, 0xbc604c2f, 0x3caa7af5, 0xbce56409,
+                                      0x3d23ba15, 0xbd7ff525, 0x3de38e97, 0xbe800004, 0x3f800000};
+EXPORT float o_spence(float a0)
+{
+    float x = a0;
+    const float pi2o6 = bf(0x3fd28d33u);
+    if (x < 0.0f) return NAN;
+    if (x == 1.0f) return 0.0f;
+    if (x == 0.0f) return pi2o6;
+    int flag = 0;
+    if (x > 2.0f) {
+        x = 1.0f / x;
+        flag |= 2;
+    }
+    float w;
+    if (x > 1.5f) {
+        w = 1.0f / x - 1.0f;
+        flag |= 2;
+    } else if (x < 0.5f) {
+        w = -x;
+        flag |= 1;
+    } else {
+        w = x - 1.0f;
+    }
+    float y = -w * horner(w, SPENCE_P, 11);
+    if (flag & 1) y = pi2o6 - o_log(x) * o_log(1.0f - x) - y;
+    if (flag & 2) {
+        float z = o_log(x);
+        y = -0.5f * (z * z) - y;
+    }
+    return y;
+}
+
 /* An integer operand carried in a float: truncated toward zero, saturated
  * to int32, NaN as 0 (the library's convention for nthroot's and expni's n). */
 static int32_t int_operand(float b)
@@ -1365,7 +1400,7 @@ enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQR
        FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT, FN_COT, FN_SEC, FN_CSC, FN_SIND,
        FN_COSD, FN_TAND, FN_TANPI, FN_COTPI, FN_COTD, FN_SECPI, FN_CSCPI, FN_SECD, FN_CSCD, FN_SINC, FN_SINCPI,
        FN_ACOTD, FN_ASEC, FN_COTH, FN_SINHC, FN_ACSC, FN_ASECH, FN_ACOTH, FN_ACSCH,
-       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_ERFINV, FN_ERFCINV, FN_DIGAMMA, FN_SIGNGAM, FN_DAWSON,
+       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_ERFINV, FN_ERFCINV, FN_DIGAMMA, FN_SIGNGAM, FN_DAWSON, FN_SPENCE,
        FN_EXPRECNEG = 80, FN_EXPRECNEGC,
        FN_SQRT1PM1,
        /* compositions of the above, oracle only (the front ends lower them to programs) */
@@ -1447,6 +1482,7 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_DIGAMMA: y[i] = o_digamma(a); break;
         case FN_SIGNGAM: y[i] = o_signgam(a); break;
         case FN_DAWSON: y[i] = o_dawson(a); break;
+        case FN_SPENCE: y[i] = o_spence(a); break;
         case FN_ERFINV: y[i] = o_erfinv(a); break;
         case FN_ERFCINV: y[i] = o_erfcinv(a); break;
         case FN_EXPRECNEG: y[i] = o_exprecneg(a); break;

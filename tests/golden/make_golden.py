@@ -90,6 +90,7 @@ SOURCES = [
     ("modules/core/euler/unit/scalar/digamma.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/signgam.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/dawson.cpp", 1, 200),
+    ("modules/core/euler/unit/scalar/spence.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/erfinv.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/erfcinv.cpp", 1, 200),
     ("modules/core/exponential/unit/scalar/expx2.cpp", 1, 200),
@@ -118,6 +119,7 @@ CONST = {
     "Three": 3.0, "Four": 4.0, "Five": 5.0, "Mthree": -3.0,
     "Log_2": float(np.uint32(0x3f317218).view(np.float32)),
     "Invexp_1": float(np.uint32(0x3ebc5ab2).view(np.float32)),
+    "Pi2o_6": float(np.uint32(0x3fd28d33).view(np.float32)),
 }
 
 

@@ -365,7 +365,7 @@ UNARY_VJP_OPS = ["exp", "log", "log1p", "erfc", "normcdf", "fastnormcdf", "sqrt"
                  "tanpi", "cotpi", "cotd", "secpi", "cscpi", "secd", "cscd", "sinc", "sincpi", "acotd", "asec", "coth",
                  "sinhc", "acsc", "asech", "acoth", "acsch", "erf", "erfcx", "expx2", "gamma", "gammaln", "erfinv",
                  "erfcinv", "exprecneg", "exprecnegc", "sqrt1pm1", "floor", "ceil", "trunc", "round", "round2even",
-                 "frac", "sign", "signnz", "sqr", "dawson"]
+                 "frac", "sign", "signnz", "sqr", "dawson", "spence"]
 
 
 def _vjp_programs(lib):

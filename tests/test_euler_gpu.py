@@ -346,3 +346,36 @@ def test_gammainc(lib, dev, prec):
     assert len(rs) >= 5
     for v, r in zip(run(np.float32([r["x"] for r in rs]), np.float32([r["y"] for r in rs]), prec), rs):
         assert nt2_ulpdist(v, r["expected"]) <= r["tol_nt2ulp"], (r, v)
+
+
+@pytest.mark.parametrize("prec", [1, 0], ids=["nt2", "fast"])
+def test_spence(lib, dev, oracle, prec):
+    """spence (NT2's float dilogarithm, Cephes' coefficients): bit-identical to
+    the oracle under the NT2 policy (map and program), within 6 ulp of FP64
+    (scipy's spence; NT2's own float result reaches 4.5) under the fast one;
+    NT2's known answers (spence.cpp) in both."""
+    from nt2_gb300 import expr as E
+    sp = pytest.importorskip("scipy.special")
+    rng = np.random.default_rng(55)
+    x = np.concatenate([rng.uniform(0, 3, 1 << 16), np.exp(rng.uniform(-30, 40, 1 << 13)), SPECIALS,
+                        -SPECIALS]).astype(np.float32)
+    got = _run(lib, dev, "spence", x, prec)
+    tx = torch.from_numpy(x).to(dev)
+    o = torch.empty_like(tx)
+    E.assign([o], [E.spence(E.Table(tx))], precision=prec)
+    assert _same(o.cpu().numpy(), got).all()
+    ref = oracle.map_f32("spence", x)
+    if prec == 1:
+        assert _same(got, ref).all()
+    else:
+        assert np.array_equal(np.isnan(got), np.isnan(ref))
+        with np.errstate(invalid="ignore"):
+            r64 = sp.spence(x.astype(np.float64))
+        ok = np.isfinite(r64) & (np.abs(r64) > 1e-30)
+        ulp = np.abs(got[ok] - r64[ok]) / np.spacing(np.abs(r64[ok]).astype(np.float32))
+        assert ulp.max() <= 6.0, (x[ok][np.argmax(ulp)], ulp.max())
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
+    rs = [r for r in golden if r["fn"] == "spence"]
+    assert len(rs) >= 5
+    for g, r in zip(_run(lib, dev, "spence", np.float32([r["x"] for r in rs]), prec), rs):
+        assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)

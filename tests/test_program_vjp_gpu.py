@@ -295,7 +295,7 @@ def _unary_cases():
         "exprecneg": (lambda x: np.exp(-1 / x), 0.2, 5), "exprecnegc": (lambda x: 1 - np.exp(-1 / x), 0.2, 5),
         "sqrt1pm1": (lambda x: np.sqrt(1 + x) - 1, -0.5, 5), "normcdf": (sp.ndtr, -5, 5),
         "fastnormcdf": (lambda x: fastnormcdf64(x)[0], -5, 5), "frac": (lambda x: x - np.trunc(x), -10, 10),
-        "dawson": (sp.dawsn, -6, 6),
+        "dawson": (sp.dawsn, -6, 6), "spence": (sp.spence, 0.05, 4),
     }
 
 
