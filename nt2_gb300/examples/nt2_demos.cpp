@@ -282,6 +282,10 @@ int main(int argc, char **argv)
             save(dir + "median1.bin", nt2::median(A, 1));
             save(dir + "median2.bin", nt2::median(h, 2));  // a host table, along its rows
             save(dir + "medianad1.bin", nt2::medianad(A));
+            save(dir + "asump1.bin", nt2::asump(A, 3.0f, 1));
+            save(dir + "normp2.bin", nt2::normp(h, 1.5f, 2));
+            std::printf("globalasump %.9g\nglobalnormp %.9g\n", (double)nt2::globalasump(A, 3.0f),
+                        (double)nt2::globalnormp(h, 1.5f));
             std::printf("globalmedian %.9g\nglobalmedianad %.9g\n", (double)nt2::globalmedian(A),
                         (double)nt2::globalmedianad(h));
             std::int64_t imax = 0, imin = 0;

@@ -647,6 +647,22 @@ def wmean(a, w, shape=None, precision=lib.PREC_FAST):
     return out
 
 
+def asump(a, p, shape=None, precision=lib.PREC_FAST):
+    """NT2's asump(a, p, dim) = sum(pow_abs(a, p), dim) of a device table viewed as
+    shape = (lo, inner, hi) (default every element): pow(abs(a), p) folded in one pass."""
+    return fold(pow(abs_(Table(a)), float(p)), "sum", shape, precision=precision)
+
+
+def normp(a, p, shape=None, precision=lib.PREC_FAST):
+    """NT2's normp(a, p, dim) = pow(asump(a, p, dim), rec(p)), rec(p) in float."""
+    import numpy as np
+    import torch
+    s = asump(a, p, shape, precision)
+    out = torch.empty_like(s)
+    assign([out], [pow(Table(s), float(np.float32(1.0) / np.float32(p)))], precision=precision)
+    return out
+
+
 def median(a, shape=None):
     """NT2's median(a, dim) of a device table viewed as shape = (lo, inner, hi)
     along inner (default every element: globalmedian); the same under either

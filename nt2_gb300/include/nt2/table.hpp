@@ -1342,6 +1342,41 @@ template <class Site> table<float, device_> wmean(const table<float, Site> &t, c
     return wmean(t, w, detail::first_non_singleton(t.extent()));
 }
 
+// asump(t, p[, dim]) = sum(pow_abs(t, p), dim) and normp(t, p[, dim]) =
+// pow(asump, rec(p)) (core/functions/expr/asump.hpp:17-49, normp.hpp:17-49);
+// NT2's pow_abs(a, p) is its pow of the non-negative |a|, so the fold takes
+// pow(abs(t), p) in one pass.  globalasump / globalnormp fold every element
+// (globalasump is a global sum, the compensated reduction; NT2's pow of the
+// result is evaluated on the device).
+template <class Site> table<float, device_> asump(const table<float, Site> &t, float p, int dim)
+{
+    return sum(pow(abs(t), p), dim);
+}
+template <class Site> table<float, device_> asump(const table<float, Site> &t, float p)
+{
+    return asump(t, p, detail::first_non_singleton(t.extent()));
+}
+template <class Site> table<float, device_> normp(const table<float, Site> &t, float p, int dim)
+{
+    const table<float, device_> s = asump(t, p, dim);
+    table<float, device_> r(s.extent());
+    r = pow(s, 1.0f / p);
+    return r;
+}
+template <class Site> table<float, device_> normp(const table<float, Site> &t, float p)
+{
+    return normp(t, p, detail::first_non_singleton(t.extent()));
+}
+template <class Site> float globalasump(const table<float, Site> &t, float p) { return globalsum(pow(abs(t), p)); }
+template <class Site> float globalnormp(const table<float, Site> &t, float p)
+{
+    table<float> h(of_size(1));
+    h(1) = globalasump(t, p);
+    table<float> r(of_size(1));
+    r = pow(h, 1.0f / p);
+    return r(1);
+}
+
 template <class Site> table<float, Site> var(const table<float, Site> &t, int w = 0)
 {
     return var(t, w, detail::first_non_singleton(t.extent()));

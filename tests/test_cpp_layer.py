@@ -182,6 +182,34 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
         assert np.array_equal(got, oracle.median(a, *shape, ad=ad)), name
     assert np.float32(glob["globalmedian"][0]) == oracle.median(a, 1, m * n, 1)[0]
     assert np.float32(glob["globalmedianad"][0]) == oracle.median(a, 1, m * n, 1, ad=True)[0]
+    # asump(A, 3, 1) = sum(pow(abs(A), 3), 1), normp(h, 1.5, 2) = pow(asump(h, 1.5, 2), rec(1.5)), and
+    # the global forms (globalasump a compensated global sum)
+    p3, p15 = np.float32(3.0), np.float32(1.5)
+    a3 = oracle.pow_f32(np.abs(a), np.full_like(a, p3))
+    a15 = oracle.pow_f32(np.abs(a), np.full_like(a, p15))
+    inv15 = np.float32(1.0) / p15
+    got_as = np.fromfile(tmp_path / "asump1.bin", np.float32)
+    got_np = np.fromfile(tmp_path / "normp2.bin", np.float32)
+    a64 = np.abs(a.astype(np.float64))
+    if prec == "1":
+        assert _eq(got_as, oracle.fold_nt2(a3, 1, m, n, "sum")[0])
+        s15 = oracle.fold_nt2(a15, m, n, 1, "sum")[0]
+        assert _eq(got_np, oracle.pow_f32(s15, np.full_like(s15, inv15)))
+        ga = np.float32(glob["globalasump"][0])
+        assert abs(float(ga) - oracle.exact_sum(a3)[0]) <= np.spacing(ga)  # NT2's elements, compensated sum
+        gs = np.float32([oracle.exact_sum(a15)[0]])
+        gn = oracle.pow_f32(gs, np.float32([inv15]))[0]  # NT2's pow of the (float-nearest) sum
+        assert abs(np.float32(glob["globalnormp"][0]) - gn) <= 2 * np.spacing(gn)
+    else:
+        # positive terms each within 4 ulp: sums within 5, their 1/1.5 roots within 4 + 5/1.5
+        ref = (a64 ** 3).reshape(n, m).sum(axis=1)
+        assert (np.abs(got_as - ref) <= 5 * np.spacing(ref.astype(np.float32))).all()
+        ref = ((a64 ** 1.5).reshape(n, m).sum(axis=0)) ** (1 / 1.5)
+        assert (np.abs(got_np - ref) <= 8 * np.spacing(ref.astype(np.float32))).all()
+        ga = (a64 ** 3).sum()
+        assert abs(float(glob["globalasump"][0]) - ga) <= 5 * np.spacing(np.float32(ga))
+        gn = (a64 ** 1.5).sum() ** (1 / 1.5)
+        assert abs(float(glob["globalnormp"][0]) - gn) <= 8 * np.spacing(np.float32(gn))
 
 
 @pytest.mark.gpu

@@ -154,3 +154,36 @@ def test_meanad_and_wmean(lib, dev, oracle, prec):
             s, _, _ = oracle.fold_ref(elems, *shape, "sum")
             ref = s / oracle.fold_ref(b, 1, m * k, 1, "sum")[0][0]
             assert (np.abs(wm - ref) <= 2 * np.spacing(np.abs(ref).astype(np.float32))).all(), shape
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
+def test_asump_and_normp(lib, dev, oracle, prec):
+    """NT2's asump(a, p, dim) = sum(pow_abs(a, p), dim) and normp = pow(asump,
+    rec(p)), pow(abs(a), p) folded in one pass: under the NT2 policy
+    bit-identical to the oracle's NT2 pow and in-order fold; under the fast one
+    asump within 5 ulp of FP64 (each term within 4, all positive: no
+    cancellation) and normp within 4 + 5/p."""
+    rng = np.random.default_rng(41)
+    m, k = 300, 1000
+    a = (rng.standard_normal(m * k) * np.exp2(rng.integers(-4, 4, m * k))).astype(np.float32)
+    ta = _t(dev, a)
+    a64 = np.abs(a.astype(np.float64))
+    for p in (3.0, 1.5, 0.5):
+        elems = oracle.pow_f32(np.abs(a), np.full_like(a, np.float32(p)))
+        inv = np.float32(1.0) / np.float32(p)
+        for shape in ((1, m, k), (m, k, 1)):
+            got_s = E.asump(ta, p, shape, precision=prec).cpu().numpy()
+            got_n = E.normp(ta, p, shape, precision=prec).cpu().numpy()
+            if prec == 1:
+                ref, _ = oracle.fold_nt2(elems, *shape, "sum")
+                assert np.array_equal(got_s.view(np.uint32), ref.view(np.uint32)), (p, shape)
+                want = oracle.pow_f32(ref, np.full_like(ref, inv))
+                assert np.array_equal(got_n.view(np.uint32), want.view(np.uint32)), (p, shape)
+            else:
+                lo, inner, hi = shape
+                s64 = (a64 ** p).reshape(hi, inner, lo).sum(axis=1).ravel()
+                assert (np.abs(got_s - s64) <= 5 * np.spacing(s64.astype(np.float32))).all(), (p, shape)
+                # the sum's 5 ulp scaled by 1/p through the root, plus the root's own 4
+                n64 = s64 ** (1.0 / p)
+                tol = 4 + 5 / p
+                assert (np.abs(got_n - n64) <= tol * np.spacing(n64.astype(np.float32))).all(), (p, shape)
