@@ -122,7 +122,11 @@ typedef enum nt2g_opcode {
     NT2G_OP_EXPNI = 153,   /* expni(n = a, b): exponential integral E_n(b) */
     NT2G_OP_GAMMAINC = 154, /* gammainc(a, b): regularised lower incomplete
                               gamma P(b, a), evaluated in double          */
-    NT2G_OP_SPENCE = 155   /* spence(a): dilogarithm (Cephes' spence)     */
+    NT2G_OP_SPENCE = 155,  /* spence(a): dilogarithm (Cephes' spence)     */
+    NT2G_OP_GAMMAINCINV = 156, /* gammaincinv(a, b): the x with P(b, x) = a,
+                                  evaluated in double                     */
+    NT2G_OP_STIRLING = 157 /* stirling(a): NT2's Stirling approximation of
+                              Gamma                                       */
 } nt2g_opcode;
 
 typedef struct nt2g_op {
@@ -401,7 +405,7 @@ nt2g_status nt2g_sigmadelta_frames_u8(const uint8_t *frames, uint8_t *bkg, uint8
  * 32 cosd, 33 tand, 34 tanpi, 35 cotpi, 36 cotd, 37 secpi, 38 cscpi, 39 secd, 40 cscd, 41 sinc,
  * 42 sincpi, 43 acotd, 44 asec, 45 coth, 46 sinhc, 47 acsc, 48 asech, 49 acoth, 50 acsch, 64 erf, 65 erfcx, 66 expx2, 67 gamma, 68 gammaln,
  * 69 erfinv, 70 erfcinv,
- * 71 digamma, 72 signgam, 73 dawson, 74 spence, 80 exprecneg, 81 exprecnegc, 82 sqrt1pm1. */
+ * 71 digamma, 72 signgam, 73 dawson, 74 spence, 75 stirling, 80 exprecneg, 81 exprecnegc, 82 sqrt1pm1. */
 nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_t n, int32_t precision,
                          void *stream);
 

@@ -289,7 +289,7 @@ static int n_operands(int code)
     case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:
     case NT2G_OP_ERF: case NT2G_OP_ERFCX: case NT2G_OP_EXPX2: case NT2G_OP_GAMMA: case NT2G_OP_GAMMALN:
     case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: case NT2G_OP_ERFINV:
-    case NT2G_OP_ERFCINV: case NT2G_OP_SIGNGAM: case NT2G_OP_DIGAMMA: case NT2G_OP_DAWSON: case NT2G_OP_SPENCE:
+    case NT2G_OP_ERFCINV: case NT2G_OP_SIGNGAM: case NT2G_OP_DIGAMMA: case NT2G_OP_DAWSON: case NT2G_OP_SPENCE: case NT2G_OP_STIRLING:
     case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
     case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ:
     case NT2G_OP_IS_NAN: case NT2G_OP_IS_INF: case NT2G_OP_IS_FINITE: case NT2G_OP_IS_EQZ: case NT2G_OP_IS_NEZ:
@@ -298,7 +298,7 @@ static int n_operands(int code)
     case NT2G_OP_LT: case NT2G_OP_GT: case NT2G_OP_LE: case NT2G_OP_GE: case NT2G_OP_EQ: case NT2G_OP_NE:
     case NT2G_OP_SELINC: case NT2G_OP_SELDEC: case NT2G_OP_ADDS: case NT2G_OP_POW:
     case NT2G_OP_ATAN2: case NT2G_OP_HYPOT: case NT2G_OP_COPYSIGN: case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI:
-    case NT2G_OP_GAMMAINC: return 2;
+    case NT2G_OP_GAMMAINC: case NT2G_OP_GAMMAINCINV: return 2;
     case NT2G_OP_FMA: case NT2G_OP_FNMS: case NT2G_OP_IF_ELSE: return 3;
     default: return -1;
     }
@@ -321,8 +321,8 @@ static bool float_only(int code)
     case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:
     case NT2G_OP_ERF: case NT2G_OP_ERFCX: case NT2G_OP_EXPX2: case NT2G_OP_GAMMA: case NT2G_OP_GAMMALN:
     case NT2G_OP_EXPRECNEG: case NT2G_OP_EXPRECNEGC: case NT2G_OP_SQRT1PM1: case NT2G_OP_ERFINV:
-    case NT2G_OP_ERFCINV: case NT2G_OP_SIGNGAM: case NT2G_OP_DIGAMMA: case NT2G_OP_DAWSON: case NT2G_OP_SPENCE:
-    case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI: case NT2G_OP_GAMMAINC:
+    case NT2G_OP_ERFCINV: case NT2G_OP_SIGNGAM: case NT2G_OP_DIGAMMA: case NT2G_OP_DAWSON: case NT2G_OP_SPENCE: case NT2G_OP_STIRLING:
+    case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI: case NT2G_OP_GAMMAINC: case NT2G_OP_GAMMAINCINV:
     case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
     case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: case NT2G_OP_COPYSIGN:
     case NT2G_OP_IS_NAN: case NT2G_OP_IS_INF: case NT2G_OP_IS_FINITE: case NT2G_OP_IS_EQZ: case NT2G_OP_IS_NEZ:
@@ -1079,7 +1079,7 @@ extern "C" nt2g_status nt2g_map_f32(int32_t fn, const float *x, float *y, int64_
 {
     NT2G_REQ_N(); NT2G_REQ(x); NT2G_REQ(y); NT2G_REQ_PREC();
     NT2G_REACH(x); NT2G_REACH(y);
-    NT2G_CHECK_ARG((fn >= 0 && fn <= 50) || (fn >= 64 && fn <= 74) || (fn >= 80 && fn <= 82), "nt2g_map_f32: unknown function %d", fn);
+    NT2G_CHECK_ARG((fn >= 0 && fn <= 50) || (fn >= 64 && fn <= 75) || (fn >= 80 && fn <= 82), "nt2g_map_f32: unknown function %d", fn);
     return launch_map(fn, x, y, n, precision, (cudaStream_t)stream);
 }
 

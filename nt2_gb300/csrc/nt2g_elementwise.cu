@@ -437,6 +437,7 @@ __device__ __forceinline__ float map_elem(float a)
     if (FN == 72) return signgam(a);
     if (FN == 73) return dawson<P>(a);
     if (FN == 74) return spence<P>(a);
+    if (FN == 75) return stirling<P>(a);
     if (FN == 80) return exprecneg<P>(a);
     if (FN == 81) return exprecnegc<P>(a);
     if (FN == 82) return sqrt1pm1<P>(a);
@@ -519,6 +520,7 @@ static void map_dispatch(int fn, const float *x, float *y, int64_t n, cudaStream
     case 72: NT2G_MAP(72); break;
     case 73: NT2G_MAP(73); break;
     case 74: NT2G_MAP(74); break;
+    case 75: NT2G_MAP(75); break;
     case 80: NT2G_MAP(80); break;
     case 81: NT2G_MAP(81); break;
     case 82: NT2G_MAP(82); break;
@@ -543,15 +545,15 @@ nt2g_status launch_map(int fn, const float *x, float *y, int64_t n, int precisio
 // the opcode switch never diverges.
 constexpr int kV = 4;
 
-// The functors that work in double or loop (digamma, dawson, spence, nthroot,
-// expni, gammainc) are compiled only into the RARE instance of the interpreter, which
+// The functors that work in double or loop (digamma, dawson, spence, stirling,
+// nthroot, expni, gammainc, gammaincinv) are compiled only into the RARE instance of the interpreter, which
 // runs the programs that use them: in the opcode switch of every program they
 // would raise the kernel's register count from 42 to 62 and cut its
 // occupancy.
 NT2G_HD bool interp_rare_op(int op)
 {
     return op == NT2G_OP_DIGAMMA || op == NT2G_OP_DAWSON || op == NT2G_OP_NTHROOT || op == NT2G_OP_EXPNI ||
-           op == NT2G_OP_GAMMAINC || op == NT2G_OP_SPENCE;
+           op == NT2G_OP_GAMMAINC || op == NT2G_OP_SPENCE || op == NT2G_OP_GAMMAINCINV || op == NT2G_OP_STIRLING;
 }
 
 template <class P, bool RARE>
@@ -622,6 +624,7 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_DIGAMMA: if constexpr (RARE) return digamma<P>(a); else return f_nan();
     case NT2G_OP_DAWSON: if constexpr (RARE) return dawson<P>(a); else return f_nan();
     case NT2G_OP_SPENCE: if constexpr (RARE) return spence<P>(a); else return f_nan();
+    case NT2G_OP_STIRLING: if constexpr (RARE) return stirling<P>(a); else return f_nan();
     case NT2G_OP_FLOOR: return floorf(a);
     case NT2G_OP_CEIL: return ceilf(a);
     case NT2G_OP_TRUNC: return truncf(a);
@@ -742,14 +745,15 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                                                                     : copysignf(x, y));
                 }
                 break;
-            case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI: case NT2G_OP_GAMMAINC:
+            case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI: case NT2G_OP_GAMMAINC: case NT2G_OP_GAMMAINCINV:
                 for (int j = 0; j < kV; ++j) {
                     const float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]);
                     float r = f_nan();
                     if constexpr (RARE)
                         r = in.op == NT2G_OP_NTHROOT ? nthroot<P>(x, int_operand(y))
                           : in.op == NT2G_OP_EXPNI   ? expni<P>(int_operand(x), y)
-                                                     : gammainc<P>(x, y);
+                          : in.op == NT2G_OP_GAMMAINC ? gammainc<P>(x, y)
+                                                     : gammaincinv<P>(x, y);
                     d[j] = __float_as_uint(r);
                 }
                 break;

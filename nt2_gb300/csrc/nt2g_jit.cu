@@ -275,6 +275,8 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         case NT2G_OP_DIGAMMA: e = "nt2g::digamma<P>(" + A + ")"; break;
         case NT2G_OP_DAWSON: e = "nt2g::dawson<P>(" + A + ")"; break;
         case NT2G_OP_SPENCE: e = "nt2g::spence<P>(" + A + ")"; break;
+        case NT2G_OP_STIRLING: e = "nt2g::stirling<P>(" + A + ")"; break;
+        case NT2G_OP_GAMMAINCINV: e = "nt2g::gammaincinv<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_NTHROOT: e = "nt2g::nthroot<P>(" + A + ", nt2g::int_operand(" + B + "))"; break;
         case NT2G_OP_EXPNI: e = "nt2g::expni<P>(nt2g::int_operand(" + A + "), " + B + ")"; break;
         case NT2G_OP_GAMMAINC: e = "nt2g::gammainc<P>(" + A + ", " + B + ")"; break;
@@ -641,6 +643,10 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
         break;
     case NT2G_OP_EXPNI:  // dE_n/dx = -E_(n-1)(x); E_0 = e^-x / x: -E_0 (1 + 1/x)
         to(o.b, G + " * nt2g::vjp::expni_grad<D>(nt2g::int_operand(" + A + "), " + B + ", " + Y + ")");
+        break;
+    case NT2G_OP_GAMMAINCINV:  // dx/dp = 1 / P'(x) at x = y; no rule for a
+        if (act(o.b)) return false;
+        to(o.a, G + " * " + rcp("nt2g::vjp::gammainc_dx(" + Y + ", " + B + ")"));
         break;
     case NT2G_OP_GAMMAINC:  // dP(a, x)/dx = x^(a-1) e^-x / Gamma(a); no rule for a
         if (act(o.b)) return false;

@@ -2362,4 +2362,56 @@ NT2G_HD double gammainc_d(double x, double a)
 
 template <class P> NT2G_HD float gammainc(float x, float a) { return (float)gammainc_d((double)x, (double)a); }
 
+// --------------------------------------------------------- gammaincinv --
+// NT2's gammaincinv(p, a) (EUL/scalar/gammaincinv.hpp:37-43): +inf for p = 1,
+// otherwise Boost.Math's gamma_p_inv(a, p), the x with P(a, x) = p, in double
+// for float arguments (NaN outside p in [0, 1], a > 0 finite).  This
+// library's own double evaluation: a starting point from the normal quantile
+// (Abramowitz & Stegun 26.2.23) through Wilson and Hilferty's cube for
+// a >= 1, or from P ~ x^a / Gamma(a + 1) near 0, then Halley steps on
+// P(a, x) - p (P' = x^(a-1) e^-x / Gamma(a), P''/P' = (a - 1)/x - 1) kept
+// inside the bracket the signs establish (bisected, or doubled while it is
+// open above, when a step would leave it) until a step is below 4e-16 of x.
+NT2G_HD double gammaincinv_d(double p, double a)
+{
+    if (p == 1.0) return (double)f_inf();
+    if (p != p || a != a || p < 0.0 || p > 1.0 || !(a > 0.0) || a == (double)f_inf()) return (double)f_nan();
+    if (p == 0.0) return 0.0;
+    double x;
+    if (a >= 1.0) {
+        const double q = p < 0.5 ? p : 1.0 - p, t = ::sqrt(-2.0 * ::log(q));
+        double z = t - (2.515517 + t * (0.802853 + t * 0.010328)) / (1.0 + t * (1.432788 + t * (0.189269 + t * 0.001308)));
+        if (p < 0.5) z = -z;
+        const double c = 1.0 / (9.0 * a), w = 1.0 - c + z * ::sqrt(c);
+        x = a * w * w * w;
+        if (!(x > 0.0)) x = 0.5 * a;
+    } else {
+        x = ::exp((::log(p) + ::lgamma(a + 1.0)) / a);
+        if (!(x > 0.0)) x = 1e-300;
+    }
+    const double lga = ::lgamma(a);
+    double lo = 0.0, hi = (double)f_inf();
+    for (int it = 0; it < 200; ++it) {
+        const double f = gammainc_d(x, a) - p;
+        if (f == 0.0) break;
+        if (f < 0.0) lo = x;
+        else hi = x;
+        const double d = ::exp((a - 1.0) * ::log(x) - x - lga);  // P'(x)
+        double xn = x;
+        if (d > 0.0) {
+            const double u = f / d, h = u / (1.0 - 0.5 * u * ((a - 1.0) / x - 1.0));
+            xn = x - (h == h ? h : u);
+        }
+        if (fabs(xn - x) <= 4e-16 * fabs(x)) {  // converged (the step may land on the bracket's end)
+            x = xn;
+            break;
+        }
+        if (!(xn > lo && xn < hi)) xn = hi == (double)f_inf() ? 2.0 * x : 0.5 * (lo + hi);
+        x = xn;
+    }
+    return x;
+}
+
+template <class P> NT2G_HD float gammaincinv(float p, float a) { return (float)gammaincinv_d((double)p, (double)a); }
+
 }  // namespace nt2g

@@ -119,6 +119,7 @@ digamma = _un("DIGAMMA")
 signgam = _un("SIGNGAM")
 dawson = _un("DAWSON")
 spence = _un("SPENCE")
+stirling = _un("STIRLING")
 
 
 # NT2's beta and betaln, built as NT2 writes them (EUL/scalar/beta.hpp:
@@ -273,6 +274,11 @@ def expni(n, x):
 def gammainc(x, a):
     """NT2's regularised lower incomplete gamma function P(a, x), evaluated in double."""
     return _bin("GAMMAINC", x, a)
+
+
+def gammaincinv(p, a):
+    """NT2's gammaincinv(p, a): the x with P(a, x) = p (+inf for p = 1), in double."""
+    return _bin("GAMMAINCINV", p, a)
 
 
 def atan2(a, b):

@@ -578,11 +578,12 @@ NT2G_BINARY(pow, NT2G_OP_POW, false)
 NT2G_BINARY(atan2, NT2G_OP_ATAN2, false)
 NT2G_BINARY(hypot, NT2G_OP_HYPOT, false)
 NT2G_BINARY(copysign, NT2G_OP_COPYSIGN, false)
-// nthroot(x, n), expni(n, x), gammainc(x, a): the integer n is truncated
+// nthroot(x, n), expni(n, x), gammainc(x, a), gammaincinv(p, a): the integer n is truncated
 // toward zero (EXP/scalar/nthroot.hpp, EUL/scalar/expni.hpp, EUL/scalar/gammainc.hpp)
 NT2G_BINARY(nthroot, NT2G_OP_NTHROOT, false)
 NT2G_BINARY(expni, NT2G_OP_EXPNI, false)
 NT2G_BINARY(gammainc, NT2G_OP_GAMMAINC, false)
+NT2G_BINARY(gammaincinv, NT2G_OP_GAMMAINCINV, false)
 #undef NT2G_BINARY
 
 // predicates (boost/simd/predicates/functions): logical results for if_else
@@ -671,6 +672,7 @@ NT2G_UNARY(digamma, NT2G_OP_DIGAMMA)
 NT2G_UNARY(signgam, NT2G_OP_SIGNGAM)
 NT2G_UNARY(dawson, NT2G_OP_DAWSON)
 NT2G_UNARY(spence, NT2G_OP_SPENCE)
+NT2G_UNARY(stirling, NT2G_OP_STIRLING)
 NT2G_UNARY(erfinv, NT2G_OP_ERFINV)
 NT2G_UNARY(erfcinv, NT2G_OP_ERFCINV)
 NT2G_UNARY(floor, NT2G_OP_FLOOR)

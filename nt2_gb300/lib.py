@@ -30,7 +30,7 @@ OP = dict(
     ASIN=90, ACOS=91, ATAN=92, ATAN2=93, ASINH=94, ACOSH=95, ATANH=96, CBRT=97, HYPOT=98,
     COT=100, SEC=101, CSC=102, SIND=103, COSD=104, TAND=105,
     TANPI=106, COTPI=107, COTD=108, SECPI=109, CSCPI=110, SECD=111, CSCD=112, SINC=113, SINCPI=114, ACOTD=115, ASEC=116, COTH=117, SINHC=118, ACSC=119, ASECH=120, ACOTH=121, ACSCH=122,
-    ERF=123, ERFCX=124, EXPX2=125, GAMMA=126, GAMMALN=127, EXPRECNEG=128, EXPRECNEGC=129, SQRT1PM1=130, ERFINV=131, ERFCINV=132, SIGNGAM=149, DIGAMMA=150, DAWSON=151, NTHROOT=152, EXPNI=153, GAMMAINC=154, SPENCE=155,
+    ERF=123, ERFCX=124, EXPX2=125, GAMMA=126, GAMMALN=127, EXPRECNEG=128, EXPRECNEGC=129, SQRT1PM1=130, ERFINV=131, ERFCINV=132, SIGNGAM=149, DIGAMMA=150, DAWSON=151, NTHROOT=152, EXPNI=153, GAMMAINC=154, SPENCE=155, GAMMAINCINV=156, STIRLING=157,
     FLOOR=133, CEIL=134, TRUNC=135, ROUND=136, ROUND2EVEN=137, FRAC=138, SIGN=139, SIGNNZ=140, COPYSIGN=141,
     IS_NAN=142, IS_INF=143, IS_FINITE=144, IS_EQZ=145, IS_NEZ=146, IS_LTZ=147, IS_GTZ=148,
 )
@@ -40,7 +40,7 @@ MAP_FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, n
               sinh=18, cosh=19, tanh=20, asin=21, acos=22, atan=23, asinh=24, acosh=25, atanh=26, cbrt=27,
               cot=28, sec=29, csc=30, sind=31, cosd=32, tand=33,
               tanpi=34, cotpi=35, cotd=36, secpi=37, cscpi=38, secd=39, cscd=40, sinc=41, sincpi=42, acotd=43, asec=44, coth=45, sinhc=46, acsc=47, asech=48, acoth=49, acsch=50,
-              erf=64, erfcx=65, expx2=66, gamma=67, gammaln=68, erfinv=69, erfcinv=70, digamma=71, signgam=72, dawson=73, spence=74, exprecneg=80, exprecnegc=81, sqrt1pm1=82)
+              erf=64, erfcx=65, expx2=66, gamma=67, gammaln=68, erfinv=69, erfcinv=70, digamma=71, signgam=72, dawson=73, spence=74, stirling=75, exprecneg=80, exprecnegc=81, sqrt1pm1=82)
 
 BATCH_BLACKSCHOLES, BATCH_SAXPY, BATCH_EXPR3, BATCH_PROGRAM = 0, 1, 2, 3
 

@@ -1400,7 +1400,7 @@ enum { FN_EXP = 0, FN_LOG, FN_LOG1P, FN_ERFC, FN_NORMCDF, FN_FASTNORMCDF, FN_SQR
        FN_ASIN, FN_ACOS, FN_ATAN, FN_ASINH, FN_ACOSH, FN_ATANH, FN_CBRT, FN_COT, FN_SEC, FN_CSC, FN_SIND,
        FN_COSD, FN_TAND, FN_TANPI, FN_COTPI, FN_COTD, FN_SECPI, FN_CSCPI, FN_SECD, FN_CSCD, FN_SINC, FN_SINCPI,
        FN_ACOTD, FN_ASEC, FN_COTH, FN_SINHC, FN_ACSC, FN_ASECH, FN_ACOTH, FN_ACSCH,
-       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_ERFINV, FN_ERFCINV, FN_DIGAMMA, FN_SIGNGAM, FN_DAWSON, FN_SPENCE,
+       FN_ERF = 64, FN_ERFCX, FN_EXPX2, FN_GAMMA, FN_GAMMALN, FN_ERFINV, FN_ERFCINV, FN_DIGAMMA, FN_SIGNGAM, FN_DAWSON, FN_SPENCE, FN_STIRLING,
        FN_EXPRECNEG = 80, FN_EXPRECNEGC,
        FN_SQRT1PM1,
        /* compositions of the above, oracle only (the front ends lower them to programs) */
@@ -1483,6 +1483,7 @@ EXPORT void o_map_f32(int fn, const float *x, float *y, int64_t n)
         case FN_SIGNGAM: y[i] = o_signgam(a); break;
         case FN_DAWSON: y[i] = o_dawson(a); break;
         case FN_SPENCE: y[i] = o_spence(a); break;
+        case FN_STIRLING: y[i] = o_stirling(a); break;
         case FN_ERFINV: y[i] = o_erfinv(a); break;
         case FN_ERFCINV: y[i] = o_erfcinv(a); break;
         case FN_EXPRECNEG: y[i] = o_exprecneg(a); break;

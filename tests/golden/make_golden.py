@@ -91,6 +91,7 @@ SOURCES = [
     ("modules/core/euler/unit/scalar/signgam.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/dawson.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/spence.cpp", 1, 200),
+    ("modules/core/euler/unit/scalar/stirling.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/erfinv.cpp", 1, 200),
     ("modules/core/euler/unit/scalar/erfcinv.cpp", 1, 200),
     ("modules/core/exponential/unit/scalar/expx2.cpp", 1, 200),
@@ -177,7 +178,7 @@ def _value(expr):
 PAT = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(\w+)\((.*?)\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 # two-argument functors: pow(a, b)
 ARG = r"((?:[^,()]|\([^()]*\))*)"
-PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2d?|hypot|logspace_add|logspace_sub|beta|betaln|nthroot|expni|gammainc)\(" + ARG + r",\s*" + ARG +
+PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2d?|hypot|logspace_add|logspace_sub|beta|betaln|nthroot|expni|gammainc|gammaincinv)\(" + ARG + r",\s*" + ARG +
                   r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
             ("modules/core/trigonometric/unit/scalar/atan2.cpp", 47, 61),
@@ -189,7 +190,8 @@ SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
             ("modules/core/euler/unit/scalar/betaln.cpp", 1, 200),
             ("modules/core/exponential/unit/scalar/nthroot.cpp", 1, 200),
             ("modules/core/euler/unit/scalar/expni.cpp", 1, 200),
-            ("modules/core/euler/unit/scalar/gammainc.cpp", 1, 200)]
+            ("modules/core/euler/unit/scalar/gammainc.cpp", 1, 200),
+            ("modules/core/euler/unit/scalar/gammaincinv.cpp", 1, 200)]
 # expected values that are themselves results of NT2 functors (sin(Pio_4)/Pio_4)
 # are left out: they would pin the oracle to itself; so are values from
 # Boost.Math (boost::math::digamma), which is not part of the reference

@@ -386,7 +386,8 @@ def _vjp_programs(lib):
          + E.fma(x, y, z) + E.fnms(x, y, z) + E.if_else(x > y, y, z) + E.selinc(x < z, y) + E.seldec(x > z, z)
          + E.if_zero_else_one(x < y, lib.F32) - (-x))
     progs.append(E.compile_program([torch.zeros(n)], [e])[0])
-    e = E.nthroot(x, 3.0) + E.nthroot(y, z) + E.expni(2.0, x) + E.expni(z, y) + E.gammainc(x, 2.5)
+    e = (E.nthroot(x, 3.0) + E.nthroot(y, z) + E.expni(2.0, x) + E.expni(z, y) + E.gammainc(x, 2.5)
+         + E.gammaincinv(x, 2.5))
     progs.append(E.compile_program([torch.zeros(n)], [e])[0])
     return progs
 
@@ -422,6 +423,12 @@ def test_integer_operand_and_incomplete_gamma_programs(lib):
     n = ctypes.c_size_t()
     assert lib.load().nt2g_program_vjp_source(prog.handle, 0, None, 0, ctypes.byref(n)) == lib.ERR_UNSUPPORTED
     assert b"opcode 154" in lib.load().nt2g_last_error()
+    st, _ = E.compile_program([torch.zeros(8)], [E.stirling(x) + E.gammaincinv(y, 2.0)])
+    for prec in (lib.PREC_FAST, lib.PREC_NT2):
+        rc, log, size = _nvrtc_compile(nv, st.jit_source(prec))
+        assert rc == 0, log[:2000]
+    assert lib.load().nt2g_program_vjp_source(st.handle, 0, None, 0, ctypes.byref(n)) == lib.ERR_UNSUPPORTED
+    assert b"opcode 157" in lib.load().nt2g_last_error()  # stirling: no adjoint rule
 
 
 def test_vjp_validates_slots(lib):

@@ -379,3 +379,75 @@ def test_spence(lib, dev, oracle, prec):
     assert len(rs) >= 5
     for g, r in zip(_run(lib, dev, "spence", np.float32([r["x"] for r in rs]), prec), rs):
         assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)
+
+
+@pytest.mark.parametrize("prec", [1, 0], ids=["nt2", "fast"])
+def test_gammaincinv_and_stirling(lib, dev, oracle, prec):
+    """gammaincinv(p, a), the x with P(a, x) = p (NT2 calls Boost.Math's
+    gamma_p_inv, in double for float arguments; this library's own double
+    Halley iteration): within 1 ulp of scipy's FP64 inverse for a up to 1e4,
+    gammainc(gammaincinv(p, a), a) back within 2 ulp of p where P is not flat,
+    identical bits in both policies, NT2's known answers (gammaincinv.cpp).
+    stirling (NT2's Stirling approximation of Gamma): bit-identical to the
+    oracle under the NT2 policy; under the fast one no more than 4 ulp beyond
+    NT2's own distance from the same formula in FP64; NT2's known answers
+    (stirling.cpp)."""
+    from nt2_gb300 import expr as E
+    sp = pytest.importorskip("scipy.special")
+    rng = np.random.default_rng(66)
+    a = np.exp(rng.uniform(np.log(1e-2), np.log(1e4), 1 << 14)).astype(np.float32)
+    p = rng.uniform(0, 1, a.size).astype(np.float32)
+    p[:64] = np.float32([0, 1, np.nan, -0.5, 1.5] + [1e-30] * 59)
+    ta, tp = torch.from_numpy(a).to(dev), torch.from_numpy(p).to(dev)
+
+    def run(e, q):
+        o = torch.empty_like(ta)
+        E.assign([o], [e], precision=q)
+        return o.cpu().numpy()
+
+    got = run(E.gammaincinv(E.Table(tp), E.Table(ta)), prec)
+    assert _same(got, run(E.gammaincinv(E.Table(tp), E.Table(ta)), 1 - prec)).all()
+    with np.errstate(invalid="ignore"):
+        r64 = sp.gammaincinv(a.astype(np.float64), p.astype(np.float64))
+    r64 = np.where(p == 1, np.inf, np.where(np.isnan(p) | (p < 0) | (p > 1), np.nan, r64))
+    assert np.array_equal(np.isnan(got), np.isnan(r64))
+    ok = np.isfinite(r64) & (r64 > 1e-37)
+    ulp = np.abs(got[ok] - r64[ok]) / np.spacing(r64[ok].astype(np.float32))
+    assert ulp.max() <= 1.0, (a[ok][np.argmax(ulp)], p[ok][np.argmax(ulp)], ulp.max())
+    back = run(E.gammainc(E.Table(torch.from_numpy(got).to(dev)), E.Table(ta)), prec)
+    fin = np.isfinite(got) & (got > 1e-30) & (p > 1e-6) & (p < 1 - 1e-6)
+    # |dP/dx| * spacing(x) bounds how far P moves between neighbouring floats of x
+    dpdx = np.exp((a[fin].astype(np.float64) - 1) * np.log(got[fin].astype(np.float64)) - got[fin] - sp.gammaln(a[fin].astype(np.float64)))
+    slack = dpdx * np.spacing(got[fin]) + 2 * np.spacing(p[fin])
+    assert (np.abs(back[fin].astype(np.float64) - p[fin]) <= slack).all()
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "nt2_unit_vectors.json")))
+    rs = [r for r in golden if r["fn"] == "gammaincinv"]
+    assert len(rs) >= 4
+    tx = torch.tensor([r["x"] for r in rs], dtype=torch.float32, device=dev)
+    ty = torch.tensor([r["y"] for r in rs], dtype=torch.float32, device=dev)
+    o = torch.empty_like(tx)
+    E.assign([o], [E.gammaincinv(E.Table(tx), E.Table(ty))], precision=prec)
+    for v, r in zip(o.cpu().numpy(), rs):
+        assert nt2_ulpdist(v, r["expected"]) <= r["tol_nt2ulp"], (r, v)
+    # stirling
+    x = np.concatenate([rng.uniform(0.5, 36, 1 << 15), SPECIALS, -SPECIALS]).astype(np.float32)
+    got = _run(lib, dev, "stirling", x, prec)
+    ref = oracle.map_f32("stirling", x)
+    if prec == 1:
+        assert _same(got, ref).all()
+    else:
+        assert np.array_equal(np.isnan(got), np.isnan(ref))
+        c = np.float32([np.uint32(v).view(np.float32) for v in (0xb970b359, 0xbb2fb930, 0x3b638e39, 0x3daaaaab)])
+        x64 = x.astype(np.float64)
+        with np.errstate(all="ignore"):
+            w = 1.0 / x64
+            w = w * (((c[0] * w + c[1]) * w + c[2]) * w + c[3]) + 1.0
+            f64 = np.sqrt(2 * np.pi) * w * np.exp(-x64) * x64 ** (x64 - 0.5)
+        ok = np.isfinite(f64) & (f64 > 1e-30) & np.isfinite(ref) & (x > 0)
+        sp32 = np.spacing(f64[ok].astype(np.float32))
+        e_fast, e_nt2 = np.abs(got[ok] - f64[ok]) / sp32, np.abs(ref[ok] - f64[ok]) / sp32
+        assert (e_fast <= e_nt2 + 4.0).all(), (x[ok][np.argmax(e_fast - e_nt2)], (e_fast - e_nt2).max())
+    rs = [r for r in golden if r["fn"] == "stirling"]
+    assert len(rs) >= 4
+    for g, r in zip(_run(lib, dev, "stirling", np.float32([r["x"] for r in rs]), prec), rs):
+        assert nt2_ulpdist(g, r["expected"]) <= r["tol_nt2ulp"], (r, g)

@@ -20,7 +20,7 @@ FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1
          "coth", "sinhc", "sech", "csch", "asech", "acsch", "acoth",
          "floor", "ceil", "trunc", "round", "frac", "sign", "signnz", "sqr_abs",
          "erf", "erfcx", "gamma", "gammaln", "erfinv", "erfcinv", "expx2", "exprecneg", "exprecnegc", "sqrt1pm1",
-         "realsqrt", "reallog", "digamma", "signgam", "dawson", "spence")
+         "realsqrt", "reallog", "digamma", "signgam", "dawson", "spence", "stirling")
 # NT2's Nan<T>() has every bit set (its sign bit too): copysign(1, Nan) is -1
 NT2_NAN = float(np.uint32(0xffffffff).view(np.float32))
 
@@ -75,6 +75,25 @@ def test_gammainc_reference_matches_nt2_unit_tests(rec):
     """The FP64 reference the GPU gammainc is checked against gives NT2's own
     known answers (Boost.Math, which NT2 calls, is not in the reference)."""
     assert nt2_ulpdist(gammainc_ref(rec["x"], rec["y"]), rec["expected"]) <= rec["tol_nt2ulp"], rec
+
+
+def gammaincinv_ref(p, a):
+    """NT2's gammaincinv(p, a) special case (EUL/scalar/gammaincinv.hpp:37-43:
+    +inf for p = 1) over scipy's double inverse of P(a, .), rounded to float."""
+    sp = pytest.importorskip("scipy.special")
+    p, a = np.float64(p), np.float64(a)
+    if p == 1:
+        return np.float32(np.inf)
+    if np.isnan(p) or np.isnan(a) or p < 0 or p > 1 or not a > 0:
+        return np.float32(np.nan)
+    return np.float32(sp.gammaincinv(a, p))
+
+
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] == "gammaincinv"],
+                         ids=lambda r: f"gammaincinv({r['x']},{r['y']})")
+def test_gammaincinv_reference_matches_nt2_unit_tests(rec):
+    """The FP64 reference of the GPU gammaincinv gives NT2's own known answers."""
+    assert nt2_ulpdist(gammaincinv_ref(rec["x"], rec["y"]), rec["expected"]) <= rec["tol_nt2ulp"], rec
 
 
 def test_oracle_dawson_nthroot_expni_accuracy_profile(oracle):
