@@ -286,6 +286,9 @@ int main(int argc, char **argv)
             save(dir + "normp2.bin", nt2::normp(h, 1.5f, 2));
             std::printf("globalasump %.9g\nglobalnormp %.9g\n", (double)nt2::globalasump(A, 3.0f),
                         (double)nt2::globalnormp(h, 1.5f));
+            save(dir + "nanasum2_2.bin", nt2::nanasum2(A, 2));
+            std::printf("globalmeanad %.9g\nglobalnorm_inf %.9g\nglobalnorm_1 %.9g\n", (double)nt2::globalmeanad(A),
+                        (double)nt2::globalnorm(h, INFINITY), (double)nt2::globalnorm(A, 1.0f));
             std::printf("globalmedian %.9g\nglobalmedianad %.9g\n", (double)nt2::globalmedian(A),
                         (double)nt2::globalmedianad(h));
             std::int64_t imax = 0, imin = 0;

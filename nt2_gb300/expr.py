@@ -669,6 +669,12 @@ def normp(a, p, shape=None, precision=lib.PREC_FAST):
     return out
 
 
+def nanasum2(a, shape=None, precision=lib.PREC_FAST):
+    """NT2's nanasum2(a, dim) = sum(if_zero_else(is_nan(a), sqr_abs(a)), dim), in one pass."""
+    t = Table(a)
+    return fold(if_else(is_nan(t), 0.0, t * t), "sum", shape, precision=precision)
+
+
 def median(a, shape=None):
     """NT2's median(a, dim) of a device table viewed as shape = (lo, inner, hi)
     along inner (default every element: globalmedian); the same under either

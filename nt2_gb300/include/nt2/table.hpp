@@ -1418,6 +1418,32 @@ template <class Site> float globalstdev(const table<float, Site> &t, int w = 0)
 {
     return detail::fold_all(t, w ? NT2G_FOLD_STDEV1 : NT2G_FOLD_STDEV);
 }
+// globalmeanad(t) = meanad(t(:)) (core/functions/globalmeanad.hpp)
+template <class Site> float globalmeanad(const table<float, Site> &t) { return detail::fold_all(t, NT2G_FOLD_MEANAD); }
+// nanasum2(t[, dim]) = sum(if_zero_else(is_nan(t), sqr_abs(t)), dim)
+// (core/functions/expr/nanasum2.hpp), folded in one pass
+template <class Site> table<float, device_> nanasum2(const table<float, Site> &t, int dim)
+{
+    return sum(if_else(is_nan(t), 0.0f, t * t), dim);
+}
+template <class Site> table<float, device_> nanasum2(const table<float, Site> &t)
+{
+    return nanasum2(t, detail::first_non_singleton(t.extent()));
+}
+// globalnorm(t[, p]) (core/functions/expr/globalnorm.hpp): globalnorm2 by
+// default and for p = 2, globalasum1 for p = 1, the largest / smallest |t|
+// for p = +inf / -inf, else globalnormp(t, p)
+template <class Site> float globalnorm(const table<float, Site> &t, float p = 2.0f)
+{
+    if (p == 2.0f) return globalnorm2(t);
+    if (p == 1.0f) return globalasum1(t);
+    if (p == INFINITY || p == -INFINITY) {
+        table<float, device_> a(t.extent());
+        a = abs(t);
+        return p > 0 ? globalmax(a) : globalmin(a);
+    }
+    return globalnormp(t, p);
+}
 // cumsum(t, dim), cumprod, cummax, cummin: tables of the shape of t
 namespace detail {
 template <class Site> inline table<float, Site> scan_dim(const table<float, Site> &t, int dim, int op)

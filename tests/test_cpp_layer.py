@@ -210,6 +210,21 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
         assert abs(float(glob["globalasump"][0]) - ga) <= 5 * np.spacing(np.float32(ga))
         gn = (a64 ** 1.5).sum() ** (1 / 1.5)
         assert abs(float(glob["globalnormp"][0]) - gn) <= 8 * np.spacing(np.float32(gn))
+    # nanasum2(A, 2) = sum(is_nan(A) ? 0 : A*A, 2); globalmeanad, globalnorm(h, inf), globalnorm(A, 1)
+    sq = np.where(np.isnan(a), np.float32(0), (a * a).astype(np.float32)).astype(np.float32)
+    got = np.fromfile(tmp_path / "nanasum2_2.bin", np.float32)
+    if prec == "1":
+        assert _eq(got, oracle.fold_nt2(sq, m, n, 1, "sum")[0])
+        assert np.float32(glob["globalmeanad"][0]) == oracle.fold_nt2(a, 1, m * n, 1, "meanad")[0][0]
+        assert np.float32(glob["globalnorm_1"][0]) == oracle.fold_nt2(a, 1, m * n, 1, "asum1")[0][0]
+    else:
+        ref, _, _ = oracle.fold_ref(sq, m, n, 1, "sum")
+        assert (np.abs(got - ref) <= np.spacing(np.abs(ref).astype(np.float32))).all()
+        ref = oracle.fold_ref(a, 1, m * n, 1, "meanad")[0][0]
+        assert abs(float(glob["globalmeanad"][0]) - ref) <= 2 * np.spacing(np.float32(abs(ref)))
+        ref = oracle.fold_ref(a, 1, m * n, 1, "asum1")[0][0]
+        assert abs(float(glob["globalnorm_1"][0]) - ref) <= np.spacing(np.float32(abs(ref)))
+    assert np.float32(glob["globalnorm_inf"][0]) == np.abs(a).max()
 
 
 @pytest.mark.gpu

@@ -187,3 +187,23 @@ def test_asump_and_normp(lib, dev, oracle, prec):
                 n64 = s64 ** (1.0 / p)
                 tol = 4 + 5 / p
                 assert (np.abs(got_n - n64) <= tol * np.spacing(n64.astype(np.float32))).all(), (p, shape)
+
+
+@pytest.mark.parametrize("prec", [0, 1], ids=["fast", "nt2"])
+def test_nanasum2(lib, dev, oracle, prec):
+    """NT2's nanasum2(a, dim) = sum(if_zero_else(is_nan(a), sqr_abs(a)), dim),
+    the select and the square folded in one pass: NaNs contribute nothing;
+    NT2 policy bit-identical to the oracle's in-order fold, fast within 1 ulp."""
+    rng = np.random.default_rng(43)
+    m, k = 300, 1000
+    a = rng.standard_normal(m * k).astype(np.float32)
+    a[rng.integers(0, a.size, 5000)] = np.nan
+    sq = np.where(np.isnan(a), np.float32(0), (a * a).astype(np.float32)).astype(np.float32)
+    for shape in ((1, m, k), (m, k, 1), (1, m * k, 1)):
+        got = E.nanasum2(_t(dev, a), shape, precision=prec).cpu().numpy()
+        if prec == 1:
+            ref, _ = oracle.fold_nt2(sq, *shape, "sum")
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), shape
+        else:
+            ref, _, _ = oracle.fold_ref(sq, *shape, "sum")
+            assert (np.abs(got - ref) <= np.spacing(np.abs(ref).astype(np.float32))).all(), shape
