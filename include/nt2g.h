@@ -233,6 +233,17 @@ typedef enum nt2g_fold_op {
 
 nt2g_status nt2g_fold_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
 
+/* trapz(a, dim): the trapezoidal integral with unit spacing over the same
+ * [lo, inner, hi] view (core/functions/expr/trapz.hpp:24-50: half the sum of
+ * adjfun(plus, a, dim), the n - 1 sums of neighbours).  NT2G_PREC_NT2: those
+ * float sums folded in index order, halved, bit-identical to NT2;
+ * NT2G_PREC_FAST: sum(a) by the compensated fold less half of the two ends,
+ * rounded once.  inner < 2 gives 0.  workspace: nt2g_trapz_workspace_size
+ * bytes (none needed under NT2G_PREC_NT2). */
+nt2g_status nt2g_trapz_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
+nt2g_status nt2g_trapz_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t precision,
+                           void *workspace, size_t workspace_bytes, float *out, void *stream);
+
 /* median(a, dim) and medianad(a, dim) = median(abs(a - median(a, dim)), dim)
  * over the same [lo, inner, hi] view
  * (core/reduction/include/nt2/core/functions/expr/median.hpp:37-50,

@@ -1151,6 +1151,33 @@ extern "C" nt2g_status nt2g_fold_f32(const float *x, int64_t lo, int64_t inner, 
                        (cudaStream_t)stream);
 }
 
+extern "C" nt2g_status nt2g_trapz_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes)
+{
+    NT2G_CHECK_ARG(bytes != nullptr, "nt2g_trapz_workspace_size: bytes is NULL");
+    NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_trapz_workspace_size: negative extent");
+    return trapz_workspace_bytes(lo, inner, hi, bytes);
+}
+
+extern "C" nt2g_status nt2g_trapz_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int32_t precision,
+                                      void *workspace, size_t workspace_bytes, float *out, void *stream)
+{
+    NT2G_CHECK_ARG(lo >= 0 && inner >= 0 && hi >= 0, "nt2g_trapz_f32: negative extent (%lld, %lld, %lld)",
+                   (long long)lo, (long long)inner, (long long)hi);
+    NT2G_CHECK_ARG(precision == NT2G_PREC_FAST || precision == NT2G_PREC_NT2, "nt2g_trapz_f32: precision %d",
+                   precision);
+    const int64_t n = lo * hi;
+    if (n == 0) return NT2G_OK;
+    NT2G_CHECK_ARG(out != nullptr, "nt2g_trapz_f32: out is NULL");
+    NT2G_CHECK_ARG(x != nullptr || inner == 0, "nt2g_trapz_f32: x is NULL");
+    size_t need = 0;
+    trapz_workspace_bytes(lo, inner, hi, &need);
+    NT2G_CHECK_ARG(precision == NT2G_PREC_NT2 || inner < 2 || (workspace != nullptr && workspace_bytes >= need),
+                   "nt2g_trapz_f32: workspace of %zu bytes, %zu needed", workspace_bytes, need);
+    NT2G_CHECK_ARG(((uintptr_t)workspace & 15u) == 0, "nt2g_trapz_f32: workspace not 16-byte aligned");
+    NT2G_REACH(x); NT2G_REACH(out); NT2G_REACH(workspace);
+    return launch_trapz(x, lo, inner, hi, precision, workspace, workspace_bytes, out, (cudaStream_t)stream);
+}
+
 extern "C" nt2g_status nt2g_median_workspace_size(int64_t lo, int64_t inner, int64_t hi, size_t *bytes)
 {
     NT2G_CHECK_ARG(bytes != nullptr, "nt2g_median_workspace_size: bytes is NULL");

@@ -374,6 +374,69 @@ nt2g_status launch_fold(const float *x, int64_t lo, int64_t inner, int64_t hi, i
     return fold_dispatch(in, lo, inner, hi, op, ws, ws_bytes, out, index, nullptr, st);
 }
 
+// trapz(y, dim) (core/functions/expr/trapz.hpp:24-50): NT2 folds adjfun(plus,
+// y, dim) -- the n - 1 float sums y_k + y_(k+1) of neighbours along the
+// dimension -- and halves the sum.  NT2 policy: one thread per output, those
+// sums folded in index order from 0, times 1/2.  Fast policy: the
+// compensated fold of y (FP64 combine) less half of the two ends,
+// sum(y) - (y_0 + y_(n-1))/2, NT2's value in exact arithmetic, rounded once;
+// a non-finite sum is kept as it is (an infinity at an end is NT2's result).
+__global__ void __launch_bounds__(kFoldThreads) k_trapz_nt2(const float *__restrict__ x, int64_t lo, int64_t n,
+                                                             int64_t hi, float *__restrict__ out)
+{
+    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < lo * hi;
+         o += (int64_t)gridDim.x * blockDim.x) {
+        const float *b = x + o % lo + lo * n * (o / lo);
+        float s = 0.0f;
+        for (int64_t k = 0; k + 1 < n; ++k) s = __fadd_rn(s, __fadd_rn(b[lo * k], b[lo * (k + 1)]));
+        out[o] = __fmul_rn(0.5f, s);
+    }
+}
+
+__global__ void __launch_bounds__(kFoldThreads) k_trapz_finish(const float *__restrict__ x, int64_t lo, int64_t n,
+                                                                int64_t hi, const double *__restrict__ s64,
+                                                                float *__restrict__ out)
+{
+    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < lo * hi;
+         o += (int64_t)gridDim.x * blockDim.x) {
+        const float *b = x + o % lo + lo * n * (o / lo);
+        const double s = s64[o];
+        out[o] = n < 2 ? 0.0f
+                       : (s - s == 0.0 ? (float)(s - 0.5 * ((double)b[0] + (double)b[lo * (n - 1)])) : (float)s);
+    }
+}
+
+nt2g_status trapz_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes)
+{
+    *bytes = (fold_partial_bytes(lo, inner, hi) + 15) / 16 * 16 + (size_t)(lo * hi) * sizeof(double);
+    return NT2G_OK;
+}
+
+nt2g_status launch_trapz(const float *x, int64_t lo, int64_t inner, int64_t hi, int precision, void *ws,
+                         size_t ws_bytes, float *out, cudaStream_t st)
+{
+    const int64_t n_out = lo * hi;
+    if (n_out == 0) return NT2G_OK;
+    const int g = (int)((n_out + kFoldThreads - 1) / kFoldThreads < 152 * 32 ? (n_out + kFoldThreads - 1) / kFoldThreads
+                                                                              : 152 * 32);
+    if (precision == NT2G_PREC_NT2 || inner < 2) {
+        k_trapz_nt2<<<g, kFoldThreads, 0, st>>>(x, lo, inner, hi, out);
+        NT2G_LAUNCH_CHECK("trapz launch");
+        return NT2G_OK;
+    }
+    const size_t off = (fold_partial_bytes(lo, inner, hi) + 15) / 16 * 16;
+    double *s64 = (double *)((char *)ws + off);
+    FoldInput in;
+    in.x = x;
+    in.precision = NT2G_PREC_FAST;
+    in.aligned = aligned16(x);
+    nt2g_status s = fold_dispatch(in, lo, inner, hi, SUM, ws, off, out, nullptr, s64, st);
+    if (s != NT2G_OK) return s;
+    k_trapz_finish<<<g, kFoldThreads, 0, st>>>(x, lo, inner, hi, s64, out);
+    NT2G_LAUNCH_CHECK("trapz launch");
+    return NT2G_OK;
+}
+
 nt2g_status launch_fold_expr(const std::vector<nt2g_op> &ops, const std::vector<uint8_t> &logical, const DArgs &args,
                              int64_t lo, int64_t inner, int64_t hi, int op, int precision, void *ws, size_t ws_bytes,
                              float *out, int64_t *index, double *out64, cudaStream_t st)

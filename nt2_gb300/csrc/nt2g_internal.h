@@ -157,6 +157,11 @@ int64_t program_bytes_per_element(const nt2g_program *p);
 // interpreter): what nt2g_eval does with force_generic = 1.
 nt2g_status program_eval(const nt2g_program *p, const DArgs &da, int64_t count, int precision, cudaStream_t st);
 
+// trapz along a dimension (nt2g_fold.cu)
+nt2g_status trapz_workspace_bytes(int64_t lo, int64_t inner, int64_t hi, size_t *bytes);
+nt2g_status launch_trapz(const float *x, int64_t lo, int64_t inner, int64_t hi, int precision, void *ws,
+                         size_t ws_bytes, float *out, cudaStream_t st);
+
 // median / medianad along a dimension (nt2g_median.cu)
 size_t median_workspace_bytes(int64_t lo, int64_t n, int64_t hi);
 nt2g_status launch_median(const float *x, int64_t lo, int64_t n, int64_t hi, int32_t op, void *ws, float *out,

@@ -287,6 +287,8 @@ int main(int argc, char **argv)
             std::printf("globalasump %.9g\nglobalnormp %.9g\n", (double)nt2::globalasump(A, 3.0f),
                         (double)nt2::globalnormp(h, 1.5f));
             save(dir + "nanasum2_2.bin", nt2::nanasum2(A, 2));
+            save(dir + "trapz1.bin", nt2::trapz(A));
+            save(dir + "trapz2.bin", nt2::trapz(h, 2));
             std::printf("globalmeanad %.9g\nglobalnorm_inf %.9g\nglobalnorm_1 %.9g\n", (double)nt2::globalmeanad(A),
                         (double)nt2::globalnorm(h, INFINITY), (double)nt2::globalnorm(A, 1.0f));
             std::printf("globalmedian %.9g\nglobalmedianad %.9g\n", (double)nt2::globalmedian(A),

@@ -1515,6 +1515,38 @@ template <class Site> inline float median_all(const table<float, Site> &t, int o
     return r;
 }
 }  // namespace detail
+// trapz(t[, dim]) (core/functions/expr/trapz.hpp): half the sum of the sums
+// of neighbours along dim (unit spacing)
+template <class Site> table<float, device_> trapz(const table<float, Site> &t, int dim)
+{
+    if (dim < 1 || dim > 4) throw gpu_error(NT2G_ERR_INVALID, "trapz dimension out of range");
+    of_size_ e = t.extent();
+    const detail::fold_shape f = detail::split(e, dim);
+    e.d[dim - 1] = 1;
+    table<float, device_> r(e);
+    auto run = [&](const float *x) {
+        std::size_t b = 0;
+        check(nt2g_trapz_workspace_size(f.lo, f.inner, f.hi, &b), "trapz workspace");
+        detail::scratch &sc = detail::thread_scratch(b);
+        check(nt2g_trapz_f32(x, f.lo, f.inner, f.hi, options().precision, sc.ws.p, sc.ws.bytes, r.data(),
+                             options().stream),
+              "trapz");
+        if (!table<float, Site>::on_device) check(nt2g_stream_synchronize(options().stream), "trapz");
+    };
+    if (table<float, Site>::on_device || detail::host_in_place()) {
+        run(t.data());
+    } else {
+        table<float, device_> dt(t.extent());
+        dt = t;
+        run(dt.data());
+    }
+    return r;
+}
+template <class Site> table<float, device_> trapz(const table<float, Site> &t)
+{
+    return trapz(t, detail::first_non_singleton(t.extent()));
+}
+
 template <class Site> table<float, device_> median(const table<float, Site> &t, int dim)
 {
     return detail::median_dim(t, dim, NT2G_MEDIAN);

@@ -115,6 +115,8 @@ _SIGNATURES = {
     "nt2g_fold_workspace_size": (_I32, [_I64, _I64, _I64, ctypes.POINTER(ctypes.c_size_t)]),
     "nt2g_fold_f32": (_I32, [_VP, _I64, _I64, _I64, _I32, _I32, _VP, ctypes.c_size_t, _VP, _VP, _VP]),
     "nt2g_median_workspace_size": (_I32, [_I64, _I64, _I64, ctypes.POINTER(ctypes.c_size_t)]),
+    "nt2g_trapz_workspace_size": (_I32, [_I64, _I64, _I64, ctypes.POINTER(ctypes.c_size_t)]),
+    "nt2g_trapz_f32": (_I32, [_VP, _I64, _I64, _I64, _I32, _VP, ctypes.c_size_t, _VP, _VP]),
     "nt2g_median_f32": (_I32, [_VP, _I64, _I64, _I64, _I32, _VP, ctypes.c_size_t, _VP, _VP]),
     "nt2g_wait_timeouts": (_I32, [ctypes.POINTER(ctypes.c_uint64)]),
     "nt2g_program_vjp": (_I32, [_VP, ctypes.POINTER(Arg), _I32, _I64, ctypes.POINTER(_VP), ctypes.POINTER(_VP), _VP,
@@ -238,6 +240,17 @@ def fold(x, lo, inner, hi, op, precision=PREC_FAST, index=False, stream=None):
 
 
 MEDIAN = {"median": 0, "medianad": 1}
+
+
+def trapz(x, lo, inner, hi, precision=PREC_FAST, stream=None):
+    """NT2's trapz (unit spacing) of x viewed as [lo, inner, hi] along inner: out[lo*hi]."""
+    import torch
+    nb = ctypes.c_size_t()
+    check(load().nt2g_trapz_workspace_size(lo, inner, hi, ctypes.byref(nb)))
+    ws = torch.empty(max(nb.value, 16), dtype=torch.uint8, device=x.device)
+    out = torch.empty(lo * hi, dtype=torch.float32, device=x.device)
+    check(load().nt2g_trapz_f32(_ptr(x), lo, inner, hi, precision, _ptr(ws), ws.numel(), _ptr(out), _stream(stream)))
+    return out
 
 
 def median(x, lo, inner, hi, op="median", out=None, stream=None):

@@ -2023,6 +2023,19 @@ static float median_of(float *v, int64_t n)
     return (n & 1) ? v[mid] : nt2_meanof_f(v[mid - 1], v[mid]);
 }
 
+/* trapz (core/functions/expr/trapz.hpp:24-50): per slice the float sums of
+ * neighbours y_k + y_(k+1) (adjfun(plus)), folded in index order, times 1/2. */
+EXPORT void o_trapz_nt2_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, float *out)
+{
+    for (int64_t h = 0; h < hi; ++h)
+        for (int64_t l = 0; l < lo; ++l) {
+            const float *b = x + l + lo * inner * h;
+            float s = 0.0f;
+            for (int64_t k = 0; k + 1 < inner; ++k) s += b[lo * k] + b[lo * (k + 1)];
+            out[l + lo * h] = 0.5f * s;
+        }
+}
+
 EXPORT void o_median_f32(const float *x, int64_t lo, int64_t inner, int64_t hi, int ad, float *out)
 {
     float *v = (float *)malloc((size_t)(inner > 0 ? inner : 1) * sizeof(float));

@@ -104,6 +104,7 @@ def lib():
         L.o_fold_nt2_f32.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, ctypes.c_int]
         L.o_fold_ref.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, _P, _P, ctypes.c_int]
         L.o_median_f32.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P]
+        L.o_trapz_nt2_f32.argtypes = [_P, _I64, _I64, _I64, _P]
         L.o_scan_nt2_f32.argtypes = [_P, _I64, _I64, _I64, ctypes.c_int, _P, ctypes.c_int]
         L.o_cumsum_exact.argtypes = [_P, _I64, _I64, _I64, _P, _P, ctypes.c_int]
         L.o_globalsum_f32.restype = ctypes.c_float
@@ -317,6 +318,14 @@ def globalsum(x):
 
 FOLD_OPS = {"sum": 0, "prod": 1, "max": 2, "min": 3, "mean": 4, "asum1": 5, "asum2": 6, "norm2": 7, "var": 8, "stdev": 9, "var1": 10, "stdev1": 11,
             "nbtrue": 12, "all": 13, "any": 14, "none": 15, "nansum": 16, "nanmean": 17, "meanad": 18}
+
+
+def trapz_nt2(x, lo, inner, hi):
+    """NT2's trapz (unit spacing) of x viewed as [lo, inner, hi] along inner."""
+    x = _f32(x)
+    out = np.empty(lo * hi, np.float32)
+    lib().o_trapz_nt2_f32(_p(x), lo, inner, hi, _p(out))
+    return out
 
 
 def median(x, lo, inner, hi, ad=False):

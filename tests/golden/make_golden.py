@@ -303,6 +303,13 @@ def main(root):
     for dim, shape, exp, lines in ((1, (1, 4, 3), [1.] * 3, "41,48-51"), (2, (4, 3, 1), [4.] * 4, "42,53-54"),
                                    (3, (12, 1, 1), [0.] * 12, "55-56"), (4, (12, 1, 1), [0.] * 12, "58-59")):
         out.append(dict(fn="medianad", x=y, shape=list(shape), expected=exp, source=f"{rel}:{lines}"))
+    # trapz of reshape(1:15, 5, 3): over every element, along dimension 1 and
+    # along dimension 2 (unit spacing, the x1 = 1:3 form), exact
+    rel = "modules/core/reduction/unit/table/trapz.cpp"
+    y15 = [float(k) for k in range(1, 16)]
+    for shape, exp, lines in (((1, 15, 1), [112.0], "34-38"), ((1, 5, 3), [12.0, 32.0, 52.0], "31,40-42"),
+                              ((5, 3, 1), [12.0, 14.0, 16.0, 18.0, 20.0], "29,32,48-50")):
+        out.append(dict(fn="trapz", x=y15, shape=list(shape), expected=exp, source=f"{rel}:{lines}"))
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "nt2_unit_vectors.json")
     with open(path, "w") as f:
         json.dump(out, f, indent=1, default=lambda v: v)

@@ -173,6 +173,23 @@ def test_median_validates_before_touching_the_gpu(lib):
     assert L.nt2g_median_f32(NULL, 0, 10, 4, 1, NULL, 0, NULL, NULL) == lib.OK  # no slices
 
 
+def test_trapz_validates_before_touching_the_gpu(lib):
+    """nt2g_trapz_f32: extents, precision, NULL tables and the fast policy's
+    workspace are checked first; no outputs is no work."""
+    L = lib.load()
+    nb = ctypes.c_size_t()
+    assert L.nt2g_trapz_workspace_size(1, 1 << 20, 1, ctypes.byref(nb)) == lib.OK and nb.value >= 8
+    assert L.nt2g_trapz_workspace_size(-1, 4, 2, ctypes.byref(nb)) == lib.ERR_INVALID
+    x, out = ctypes.c_void_p(1 << 20), ctypes.c_void_p(1 << 30)
+    assert L.nt2g_trapz_f32(x, 1, 10, 4, 5, NULL, 0, out, NULL) == lib.ERR_INVALID  # precision
+    assert L.nt2g_trapz_f32(x, 1, -10, 4, 0, NULL, 0, out, NULL) == lib.ERR_INVALID
+    assert L.nt2g_trapz_f32(x, 1, 10, 4, 0, NULL, 0, NULL, NULL) == lib.ERR_INVALID  # out
+    assert L.nt2g_trapz_f32(NULL, 1, 10, 4, 0, NULL, 0, out, NULL) == lib.ERR_INVALID  # x
+    assert L.nt2g_trapz_f32(x, 1, 1 << 20, 1, 0, NULL, 0, out, NULL) == lib.ERR_INVALID  # fast: workspace
+    assert "workspace" in L.nt2g_last_error().decode()
+    assert L.nt2g_trapz_f32(NULL, 0, 10, 4, 1, NULL, 0, NULL, NULL) == lib.OK
+
+
 def test_eval_validates_arguments(lib):
     x = E.Table(torch.zeros(8))
     out = torch.zeros(8)

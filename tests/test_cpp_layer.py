@@ -225,6 +225,17 @@ def test_folds_through_tables(demos, oracle, tmp_path, prec):
         ref = oracle.fold_ref(a, 1, m * n, 1, "asum1")[0][0]
         assert abs(float(glob["globalnorm_1"][0]) - ref) <= np.spacing(np.float32(abs(ref)))
     assert np.float32(glob["globalnorm_inf"][0]) == np.abs(a).max()
+    # trapz(A) along the first dimension, trapz(h, 2) of the host table along the rows
+    for name, shape in (("trapz1", (1, m, n)), ("trapz2", (m, n, 1))):
+        got = np.fromfile(tmp_path / f"{name}.bin", np.float32)
+        if prec == "1":
+            assert _eq(got, oracle.trapz_nt2(a, *shape)), name
+        else:
+            lo, inner, hi = shape
+            v = a.astype(np.float64).reshape(hi, inner, lo)
+            ref = (0.5 * (v[:, 1:, :] + v[:, :-1, :]).sum(axis=1)).ravel()
+            mag = np.abs(v).sum(axis=1).ravel()
+            assert (np.abs(got - ref) <= np.spacing(np.abs(ref).astype(np.float32)) + 2e-7 * mag).all(), name
 
 
 @pytest.mark.gpu

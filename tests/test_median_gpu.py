@@ -94,3 +94,28 @@ def test_global_median_large(lib, dev):
             a, b = p[mid - 1], p[mid]
             want = np.float32(a + np.float32(np.float32(b - a) * np.float32(0.5)))
         assert got == want, (n, got, want)
+
+
+
+@pytest.mark.parametrize("prec", [1, 0], ids=["nt2", "fast"])
+def test_trapz(lib, dev, oracle, prec):
+    """trapz (unit spacing) along every kind of dimension: under the NT2 policy
+    bit-identical to the oracle's NT2 order (neighbour sums folded in index
+    order, halved); under the fast one within 1 ulp of the FP64 value plus the
+    float rounding of the sum's magnitude; slices of 0 and 1 elements give 0;
+    NT2's known answers (trapz.cpp)."""
+    rng = np.random.default_rng(71)
+    for shape in ((1, 1000, 300), (300, 1000, 1), (7, 33, 5), (1, 1 << 20, 1), (4, 1, 3), (3, 0, 2), (1, 2, 5)):
+        lo, inner, hi = shape
+        x = rng.standard_normal(max(lo * inner * hi, 1)).astype(np.float32)
+        got = lib.trapz(torch.from_numpy(x).to(dev), lo, inner, hi, precision=prec).cpu().numpy()
+        if prec == 1:
+            assert np.array_equal(got.view(np.uint32), oracle.trapz_nt2(x, lo, inner, hi).view(np.uint32)), shape
+        else:
+            v = x[:lo * inner * hi].astype(np.float64).reshape(hi, inner, lo)
+            ref = (0.5 * (v[:, 1:, :] + v[:, :-1, :]).sum(axis=1)).ravel() if inner > 1 else np.zeros(lo * hi)
+            mag = (np.abs(v).sum(axis=1)).ravel()
+            assert (np.abs(got - ref) <= np.spacing(np.abs(ref).astype(np.float32)) + 2e-7 * mag).all(), shape
+    for rec in [r for r in GOLDEN if r["fn"] == "trapz"]:
+        got = lib.trapz(torch.tensor(rec["x"], dtype=torch.float32, device=dev), *rec["shape"], precision=prec)
+        assert np.array_equal(got.cpu().numpy(), np.float32(rec["expected"])), rec

@@ -127,6 +127,12 @@ def test_oracle_median_matches_nt2_unit_tests(oracle, rec):
     assert np.array_equal(got, np.float32(rec["expected"])), (got, rec)
 
 
+@pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] == "trapz"], ids=lambda r: f"trapz{tuple(r['shape'])}")
+def test_oracle_trapz_matches_nt2_unit_tests(oracle, rec):
+    got = oracle.trapz_nt2(np.float32(rec["x"]), *rec["shape"])
+    assert np.array_equal(got, np.float32(rec["expected"])), (got, rec)
+
+
 def test_oracle_median_against_numpy(oracle):
     """The oracle's median of random slices equals numpy's sorted middle
     (numpy's median averages the two middle elements as (a + b) / 2, which
