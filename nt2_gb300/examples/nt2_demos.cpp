@@ -300,6 +300,30 @@ int main(int argc, char **argv)
                         (double)gmax, (long long)imax, (double)gmin, (long long)imin, (double)nt2::globalmean(A),
                         (double)nt2::globalnorm2(A), (double)nt2::globalasum1(A), (double)nt2::globalvar(A),
                         (double)nt2::globalstdev(h));
+        } else if (mode == "stat") {
+            // NT2's distribution functions through the table layer: X on the real line, P in [0, 1]
+            auto X = load<dtable>(dir + "x.bin", n), P = load<dtable>(dir + "p.bin", n);
+            dtable o(nt2::of_size(n));
+            o = nt2::normpdf(X, 0.5f, 1.75f); save(dir + "normpdf3.bin", o);
+            o = nt2::norminv(P, 0.5f, 1.75f); save(dir + "norminv3.bin", o);
+            o = nt2::expcdf(X, 1.75f); save(dir + "expcdf2.bin", o);
+            o = nt2::exppdf(X, 1.75f); save(dir + "exppdf2.bin", o);
+            o = nt2::expinv(P, 1.75f); save(dir + "expinv2.bin", o);
+            o = nt2::logncdf(X, 0.5f, 1.75f); save(dir + "logncdf3.bin", o);
+            o = nt2::lognpdf(X, 0.5f, 1.75f); save(dir + "lognpdf3.bin", o);
+            o = nt2::logninv(P, 0.5f, 1.75f); save(dir + "logninv3.bin", o);
+            o = nt2::unifcdf(X, -1.25f, 2.5f); save(dir + "unifcdf3.bin", o);
+            o = nt2::unifpdf(X); save(dir + "unifpdf.bin", o);
+            o = nt2::unifinv(P); save(dir + "unifinv.bin", o);
+            o = nt2::caucdf(X, 0.5f, 1.75f); save(dir + "caucdf3.bin", o);
+            o = nt2::caupdf(X, 0.5f, 1.75f); save(dir + "caupdf3.bin", o);
+            o = nt2::evcdf(X, 0.5f, 1.75f); save(dir + "evcdf3.bin", o);
+            o = nt2::evpdf(X, 0.5f, 1.75f); save(dir + "evpdf3.bin", o);
+            o = nt2::evinv(P, 0.5f, 1.75f); save(dir + "evinv3.bin", o);
+            o = nt2::normpdf(X) + nt2::norminv(P) + nt2::expcdf(X) + nt2::exppdf(X) + nt2::expinv(P) + nt2::logncdf(X) +
+                nt2::lognpdf(X) + nt2::logninv(P) + nt2::unifcdf(X) + nt2::caucdf(X) + nt2::caupdf(X) + nt2::evcdf(X) +
+                nt2::evpdf(X) + nt2::evinv(P);
+            save(dir + "one_param_sum.bin", o);
         } else if (mode == "gen") {
             // generative leaves: NT2's colon (also spelled _), linspace, logspace, alone and in expressions
             using nt2::_;

@@ -200,6 +200,168 @@ def acospi(a): return _INVPI * acos(a)
 def atanpi(a): return _INVPI * atan(a)
 
 
+# Distribution functions of NT2's statistics module as NT2 composes them
+# (modules/core/statistics/include/nt2/statistics/functions/generic/*.hpp), every operation in NT2's order:
+# if_zero_else(c, x) = c ? 0 : x, if_allbits_else(c, x) = c ? NaN : x, and
+# is_not_greater(a, b) = !(a > b).  Parameters are numbers or expressions.
+_INVSQRT_2PI, _SQRT_2, _SQRT_2O_2 = _bits_f32(0x3ecc422a), _bits_f32(0x3fb504f3), _bits_f32(0x3f3504f3)
+_NAN = float("nan")
+
+
+def _is_negative(a):  # the sign bit (boost.simd is_negative: -0 included)
+    return copysign(1.0, a) < 0.0
+
+
+def is_lez(a):
+    """boost.simd is_lez: a <= 0 (false for NaN)."""
+    return a <= 0.0
+
+
+def _p(v):
+    """A parameter as a node: numbers become run-time float scalars, so that
+    every operation on them is NT2's float operation on the device."""
+    return v if v is None or isinstance(v, Node) else Scalar(v)
+
+
+def normpdf(x, m=None, s=None):
+    """normpdf.hpp: exp(-1/2 sqr((x - m) rec(s))) / sqrt(2 pi) rec(s)."""
+    m, s = _p(m), _p(s)
+    if s is not None:
+        inv = rec(s)
+        return exp(-0.5 * sqr((x - m) * inv)) * _INVSQRT_2PI * inv
+    return exp(-0.5 * sqr(x if m is None else x - m)) * _INVSQRT_2PI
+
+
+def norminv(p, m=None, s=None):
+    """norminv.hpp: -sqrt(2) erfcinv(2 p), then + m or fma(., s, m)."""
+    m, s = _p(m), _p(s)
+    z = -_SQRT_2 * erfcinv(2.0 * p)
+    if s is not None:
+        return fma(z, s, m)
+    return z if m is None else z + m
+
+
+def expcdf(x, mu=None):
+    """expcdf.hpp: -expm1(-if_zero_else(is_ltz(x), x)) of x (or x / mu)."""
+    mu = _p(mu)
+    if mu is not None:
+        x = x / mu
+    return -expm1(-if_else(is_ltz(x), 0.0, x))
+
+
+def exppdf(x, lam=None):
+    """exppdf.hpp: if_zero_else(is_ltz(x), exp(-x)) or lam exp(-x lam)."""
+    lam = _p(lam)
+    return if_else(is_ltz(x), 0.0, exp(-x) if lam is None else lam * exp(-x * lam))
+
+
+def expinv(p, mu=None):
+    """expinv.hpp: if_allbits_else(is_ltz(p), -log1p(-p)), times mu."""
+    mu = _p(mu)
+    r = if_else(is_ltz(p), _NAN, -log1p(-p))
+    return r if mu is None else mu * r
+
+
+def logncdf(x, m=None, s=None):
+    """logncdf.hpp: erfc(-sqrt(1/2) log(x)) / 2, log(x) -> (m - log(x)) [/ s]; x <= 0 read as 0."""
+    m, s = _p(m), _p(s)
+    lx = log(if_else(is_lez(x), 0.0, x))
+    if m is None:
+        return 0.5 * erfc(-_SQRT_2O_2 * lx)
+    t = m - lx
+    return 0.5 * erfc(_SQRT_2O_2 * (t if s is None else t / s))
+
+
+def lognpdf(x, m=None, s=None):
+    """lognpdf.hpp: normpdf(log(x)[, m[, s]]) / x, x <= 0 read as +inf."""
+    m, s = _p(m), _p(s)
+    xx = if_else(is_lez(x), float("inf"), x)
+    return normpdf(log(xx), m, s) / xx
+
+
+def logninv(p, m=None, s=None):
+    """logninv.hpp: exp(-sqrt(2) [s] erfcinv(2 p) [+ m])."""
+    m, s = _p(m), _p(s)
+    c = -_SQRT_2 if s is None else -_SQRT_2 * s
+    z = c * erfcinv(2.0 * p)
+    return exp(z if m is None else z + m)
+
+
+def unifcdf(x, a=None, b=None):
+    """unifcdf.hpp: x clamped to [0, 1]; with [a, b]: NaN for b <= a, else 0 below a,
+    (x - a) / (b - a) up to b, 1 above."""
+    a, b = _p(a), _p(b)
+    if a is None:
+        return if_else(is_ltz(x), 0.0, if_else(x > 1.0, 1.0, x))
+    z = b - a
+    return if_else(is_lez(z), _NAN, if_else(x < a, 0.0, if_else(x > b, 1.0, (x - a) / z)))
+
+
+def unifpdf(x, a=None, b=None):
+    """unifpdf.hpp: 1 on [0, 1] (not at -0), NaN for NaN; with [a, b]: rec(b - a) inside,
+    0 outside, NaN for b <= a or a NaN x."""
+    a, b = _p(a), _p(b)
+    if a is None:
+        return if_else(is_nan(x), x, if_else(x <= 1.0, if_else(_is_negative(x), 0.0, 1.0), 0.0))
+    z = b - a
+    return if_else(is_lez(z), _NAN, if_else(is_nan(x), _NAN, if_else(x < a, 0.0, if_else(x > b, 0.0, rec(z)))))
+
+
+def unifinv(p, a=None, b=None):
+    """unifinv.hpp: p on [0, 1], else NaN; with [a, b] NT2's fma(p, if_allbits_else(p > b or
+    p < a, b - a), a) as written."""
+    a, b = _p(a), _p(b)
+    if a is None:
+        return if_else(p < 0.0, _NAN, if_else(p <= 1.0, p, _NAN))
+    return fma(p, if_else(p > b, _NAN, if_else(p < a, _NAN, b - a)), a)
+
+
+def caucdf(x, m=None, s=None):
+    """caucdf.hpp: 1/2 + atanpi(x), x -> x - m or (x - m) / s."""
+    m, s = _p(m), _p(s)
+    if m is not None:
+        x = x - m if s is None else (x - m) / s
+    return 0.5 + atanpi(x)
+
+
+def caupdf(x, m=None, s=None):
+    """caupdf.hpp: rec(oneplus(sqr(x))) / pi (x -> x - m), or (s / pi) / (sqr(s) + sqr(x - m))."""
+    m, s = _p(m), _p(s)
+    if s is None:
+        return rec(1.0 + sqr(x if m is None else x - m)) * _INVPI
+    return (s * _INVPI) / (sqr(s) + sqr(x - m))
+
+
+def evcdf(x, m=None, s=None):
+    """evcdf.hpp: -expm1(-exp(x)), x -> x - m or (x - m) / s."""
+    m, s = _p(m), _p(s)
+    if m is not None:
+        x = x - m if s is None else (x - m) / s
+    return -expm1(-exp(x))
+
+
+def evpdf(x, m=None, s=None):
+    """evpdf.hpp: t = exp(x'), t * exp(-t) [* rec(s)], 0 at x = +inf."""
+    m, s = _p(m), _p(s)
+    if s is not None:
+        inv = rec(s)
+        t = exp((x - m) * inv)
+        t = t * (exp(-t) * inv)
+    else:
+        t = exp(x if m is None else x - m)
+        t = t * exp(-t)
+    return if_else(x.eq(float("inf")), 0.0, t)
+
+
+def evinv(p, m=None, s=None):
+    """evinv.hpp: log(-log1p(-p)) [* s] [+ m]."""
+    m, s = _p(m), _p(s)
+    z = log(-log1p(-p))
+    if s is not None:
+        z = z * s
+    return z if m is None else z + m
+
+
 # logspace_add, logspace_sub (exponential/functions/scalar/logspace_add.hpp,
 # logspace_sub.hpp) in NT2's forms; NT2's max(a, b) is a > b ? a : b.  The
 # real* functors are NT2's assertion-only aliases of sqrt, log and pow.

@@ -1097,6 +1097,195 @@ inline double sum_node(const node_ptr &n)
 }
 }  // namespace detail
 
+// Distribution functions of NT2's statistics module as NT2 composes them
+// (modules/core/statistics/include/nt2/statistics/functions/generic/{norm,exp,logn,unif,cau,ev}{pdf,cdf,inv}.hpp),
+// every operation in NT2's order; parameters are floats or expressions.
+// if_zero_else(c, x) = c ? 0 : x, if_allbits_else(c, x) = c ? NaN : x,
+// is_not_greater(a, b) = !(a > b), is_negative = the sign bit.
+namespace detail {
+inline float stat_c(std::uint32_t b) { return f32_of_bits(b); }
+constexpr std::uint32_t kInvsqrt2pi = 0x3ecc422au, kSqrt2 = 0x3fb504f3u, kSqrt2o2 = 0x3f3504f3u, kInvpi = 0x3ea2f983u;
+template <class X> expr<float> lift_expr(const X &x) { return expr<float>{lift(x)}; }
+inline expr<float> as_expr(float v) { return expr<float>{any<float>(v)}; }
+inline expr<float> as_expr(const expr<float> &e) { return e; }
+// a select on a condition known on the host (parameters given as numbers) or per element
+template <class A, class B> expr<float> sel(bool c, const A &a, const B &b) { return c ? as_expr(a) : as_expr(b); }
+template <class T, class A, class B> expr<float> sel(const expr<T> &c, const A &a, const B &b)
+{
+    return if_else(c, as_expr(a), as_expr(b));
+}
+}  // namespace detail
+template <class X> expr<float> normpdf(const X &x)
+{
+    const expr<float> a{detail::lift(x)};
+    return exp(-0.5f * sqr(a)) * detail::stat_c(detail::kInvsqrt2pi);
+}
+template <class X, class M> expr<float> normpdf(const X &x, const M &m)
+{
+    const expr<float> a{detail::lift(x)};
+    return exp(-0.5f * sqr(a - m)) * detail::stat_c(detail::kInvsqrt2pi);
+}
+template <class X, class M, class S> expr<float> normpdf(const X &x, const M &m, const S &s)
+{
+    const expr<float> a{detail::lift(x)};
+    const auto inv = 1.0f / s;
+    return exp(-0.5f * sqr((a - m) * inv)) * detail::stat_c(detail::kInvsqrt2pi) * inv;
+}
+template <class X> expr<float> norminv(const X &p)
+{
+    const expr<float> a{detail::lift(p)};
+    return -detail::stat_c(detail::kSqrt2) * erfcinv(2.0f * a);
+}
+template <class X, class M> expr<float> norminv(const X &p, const M &m) { return norminv(p) + m; }
+template <class X, class M, class S> expr<float> norminv(const X &p, const M &m, const S &s)
+{
+    return fma(norminv(p), s, m);
+}
+template <class X> expr<float> expcdf(const X &x)
+{
+    const expr<float> a{detail::lift(x)};
+    return -expm1(-detail::sel(is_ltz(a), 0.0f, a));
+}
+template <class X, class M> expr<float> expcdf(const X &x, const M &mu) { return expcdf(detail::lift_expr(x) / mu); }
+template <class X> expr<float> exppdf(const X &x)
+{
+    const expr<float> a{detail::lift(x)};
+    return detail::sel(is_ltz(a), 0.0f, exp(-a));
+}
+template <class X, class L> expr<float> exppdf(const X &x, const L &l)
+{
+    const expr<float> a{detail::lift(x)};
+    return detail::sel(is_ltz(a), 0.0f, l * exp(-a * l));
+}
+template <class X> expr<float> expinv(const X &p)
+{
+    const expr<float> a{detail::lift(p)};
+    return detail::sel(is_ltz(a), NAN, -log1p(-a));
+}
+template <class X, class M> expr<float> expinv(const X &p, const M &mu) { return mu * expinv(p); }
+template <class X> expr<float> logncdf(const X &x)
+{
+    const expr<float> a{detail::lift(x)};
+    return 0.5f * erfc(-detail::stat_c(detail::kSqrt2o2) * log(detail::sel(a <= 0.0f, 0.0f, a)));
+}
+template <class X, class M> expr<float> logncdf(const X &x, const M &m)
+{
+    const expr<float> a{detail::lift(x)};
+    return 0.5f * erfc(detail::stat_c(detail::kSqrt2o2) * (m - log(detail::sel(a <= 0.0f, 0.0f, a))));
+}
+template <class X, class M, class S> expr<float> logncdf(const X &x, const M &m, const S &s)
+{
+    const expr<float> a{detail::lift(x)};
+    return 0.5f * erfc(detail::stat_c(detail::kSqrt2o2) * ((m - log(detail::sel(a <= 0.0f, 0.0f, a))) / s));
+}
+template <class X> expr<float> lognpdf(const X &x)
+{
+    const expr<float> a{detail::lift(x)};
+    const expr<float> xx = detail::sel(a <= 0.0f, INFINITY, a);
+    return normpdf(log(xx)) / xx;
+}
+template <class X, class M> expr<float> lognpdf(const X &x, const M &m)
+{
+    const expr<float> a{detail::lift(x)};
+    const expr<float> xx = detail::sel(a <= 0.0f, INFINITY, a);
+    return normpdf(log(xx), m) / xx;
+}
+template <class X, class M, class S> expr<float> lognpdf(const X &x, const M &m, const S &s)
+{
+    const expr<float> a{detail::lift(x)};
+    const expr<float> xx = detail::sel(a <= 0.0f, INFINITY, a);
+    return normpdf(log(xx), m, s) / xx;
+}
+template <class X> expr<float> logninv(const X &p)
+{
+    const expr<float> a{detail::lift(p)};
+    return exp(-detail::stat_c(detail::kSqrt2) * erfcinv(2.0f * a));
+}
+template <class X, class M> expr<float> logninv(const X &p, const M &m)
+{
+    const expr<float> a{detail::lift(p)};
+    return exp(-detail::stat_c(detail::kSqrt2) * erfcinv(2.0f * a) + m);
+}
+template <class X, class M, class S> expr<float> logninv(const X &p, const M &m, const S &s)
+{
+    const expr<float> a{detail::lift(p)};
+    return exp(-detail::stat_c(detail::kSqrt2) * s * erfcinv(2.0f * a) + m);
+}
+template <class X> expr<float> unifcdf(const X &x)
+{
+    const expr<float> a{detail::lift(x)};
+    return detail::sel(is_ltz(a), 0.0f, detail::sel(a > 1.0f, 1.0f, a));
+}
+template <class X, class A, class B> expr<float> unifcdf(const X &x, const A &lo, const B &hi)
+{
+    const expr<float> a{detail::lift(x)};
+    const auto z = hi - lo;
+    return detail::sel(z <= 0.0f, NAN, detail::sel(a < lo, 0.0f, detail::sel(a > hi, 1.0f, (a - lo) / z)));
+}
+template <class X> expr<float> unifpdf(const X &x)
+{
+    const expr<float> a{detail::lift(x)};
+    return detail::sel(is_nan(a), a, detail::sel(a <= 1.0f, detail::sel(copysign(1.0f, a) < 0.0f, 0.0f, 1.0f), 0.0f));
+}
+template <class X> expr<float> unifinv(const X &p)
+{
+    const expr<float> a{detail::lift(p)};
+    return detail::sel(a < 0.0f, NAN, detail::sel(a <= 1.0f, a, NAN));
+}
+template <class X, class M, class S> expr<float> caucdf(const X &x, const M &m, const S &s)
+{
+    const expr<float> a{detail::lift(x)};
+    return 0.5f + atanpi((a - m) / s);
+}
+template <class X> expr<float> caucdf(const X &x) { return 0.5f + atanpi(detail::lift_expr(x)); }
+template <class X, class M> expr<float> caucdf(const X &x, const M &m) { return caucdf(detail::lift_expr(x) - m); }
+template <class X> expr<float> caupdf(const X &x)
+{
+    const expr<float> a{detail::lift(x)};
+    return rec(1.0f + sqr(a)) * detail::stat_c(detail::kInvpi);
+}
+template <class X, class M> expr<float> caupdf(const X &x, const M &m) { return caupdf(detail::lift_expr(x) - m); }
+template <class X, class M, class S> expr<float> caupdf(const X &x, const M &m, const S &s)
+{
+    const expr<float> a{detail::lift(x)};
+    return (s * detail::stat_c(detail::kInvpi)) / (s * s + sqr(a - m));
+}
+template <class X> expr<float> evcdf(const X &x) { return -expm1(-exp(detail::lift_expr(x))); }
+template <class X, class M> expr<float> evcdf(const X &x, const M &m) { return evcdf(detail::lift_expr(x) - m); }
+template <class X, class M, class S> expr<float> evcdf(const X &x, const M &m, const S &s)
+{
+    return evcdf((detail::lift_expr(x) - m) / s);
+}
+template <class X> expr<float> evpdf(const X &x)
+{
+    const expr<float> a{detail::lift(x)};
+    const expr<float> t = exp(a);
+    return detail::sel(a == INFINITY, 0.0f, t * exp(-t));
+}
+template <class X, class M> expr<float> evpdf(const X &x, const M &m)
+{
+    const expr<float> a{detail::lift(x)};
+    const expr<float> t = exp(a - m);
+    return detail::sel(a == INFINITY, 0.0f, t * exp(-t));
+}
+template <class X, class M, class S> expr<float> evpdf(const X &x, const M &m, const S &s)
+{
+    const expr<float> a{detail::lift(x)};
+    const auto inv = 1.0f / s;
+    const expr<float> t = exp((a - m) * inv);
+    return detail::sel(a == INFINITY, 0.0f, t * (exp(-t) * inv));
+}
+template <class X> expr<float> evinv(const X &p)
+{
+    const expr<float> a{detail::lift(p)};
+    return log(-log1p(-a));
+}
+template <class X, class M> expr<float> evinv(const X &p, const M &m) { return evinv(p) + m; }
+template <class X, class M, class S> expr<float> evinv(const X &p, const M &m, const S &s)
+{
+    return evinv(p) * s + m;
+}
+
 // NT2's sum over a vector / globalsum: the compensated device reduction,
 // returned as T (NT2's result type) -- sum64 keeps the FP64 combine.  A sum of
 // an expression (sum(exp(x)*y), globalsum(a*b+c)) is folded in one pass, the

@@ -337,3 +337,40 @@ def test_async_sums_on_two_streams(demos, lib, tmp_path):
     dot = lib.Reducer("cuda:0")(tx, ty)[0].item()
     fused = E.fold(E.exp(E.Table(tx)) * E.Table(ty), "sum", out64=True)[1].item()
     assert vals[:16] == [dot] * 16 and vals[16:] == [fused] * 16
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["1", "0"], ids=["nt2", "fast"])
+def test_distribution_functions_through_tables(demos, tmp_path, prec):
+    """NT2's distribution functions through the C++ layer (parameters as
+    numbers, resolved on the host where NT2's selects test them) give the same
+    bits as the Python front end's compositions (parameters as run-time
+    scalars) under the same policy."""
+    import torch
+    from nt2_gb300 import expr as E
+    n = 50000
+    rng = np.random.default_rng(81)
+    x = np.concatenate([rng.uniform(-6, 6, n - 8), [0, -0.0, 1, -1, np.inf, -np.inf, np.nan, 2.5]]).astype(np.float32)
+    p = np.concatenate([rng.uniform(0, 1, n - 6), [0, 1, -0.5, 1.5, np.nan, 0.5]]).astype(np.float32)
+    x.tofile(tmp_path / "x.bin")
+    p.tofile(tmp_path / "p.bin")
+    _run(demos, "stat", tmp_path, n, env={"NT2G_PRECISION": prec})
+    tx, tp = torch.from_numpy(x).cuda(), torch.from_numpy(p).cuda()
+    X, P = E.Table(tx), E.Table(tp)
+    m, s = 0.5, 1.75
+    cases = {"normpdf3": E.normpdf(X, m, s), "norminv3": E.norminv(P, m, s), "expcdf2": E.expcdf(X, s),
+             "exppdf2": E.exppdf(X, s), "expinv2": E.expinv(P, s), "logncdf3": E.logncdf(X, m, s),
+             "lognpdf3": E.lognpdf(X, m, s), "logninv3": E.logninv(P, m, s), "unifcdf3": E.unifcdf(X, -1.25, 2.5),
+             "unifpdf": E.unifpdf(X), "unifinv": E.unifinv(P), "caucdf3": E.caucdf(X, m, s),
+             "caupdf3": E.caupdf(X, m, s), "evcdf3": E.evcdf(X, m, s), "evpdf3": E.evpdf(X, m, s),
+             "evinv3": E.evinv(P, m, s),
+             "one_param_sum": (E.normpdf(X) + E.norminv(P) + E.expcdf(X) + E.exppdf(X) + E.expinv(P) + E.logncdf(X)
+                               + E.lognpdf(X) + E.logninv(P) + E.unifcdf(X) + E.caucdf(X) + E.caupdf(X) + E.evcdf(X)
+                               + E.evpdf(X) + E.evinv(P))}
+    for name, e in cases.items():
+        out = torch.empty_like(tx)
+        E.assign([out], [e], precision=int(prec))
+        want = out.cpu().numpy()
+        got = np.fromfile(tmp_path / f"{name}.bin", np.float32)
+        same = (got.view(np.uint32) == want.view(np.uint32)) | (np.isnan(got) & np.isnan(want))
+        assert same.all(), (name, x[~same][:3], p[~same][:3], got[~same][:3], want[~same][:3])
