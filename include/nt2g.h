@@ -125,8 +125,10 @@ typedef enum nt2g_opcode {
     NT2G_OP_SPENCE = 155,  /* spence(a): dilogarithm (Cephes' spence)     */
     NT2G_OP_GAMMAINCINV = 156, /* gammaincinv(a, b): the x with P(b, x) = a,
                                   evaluated in double                     */
-    NT2G_OP_STIRLING = 157 /* stirling(a): NT2's Stirling approximation of
-                              Gamma                                       */
+    NT2G_OP_STIRLING = 157, /* stirling(a): NT2's Stirling approximation of
+                               Gamma                                      */
+    NT2G_OP_PROPER_TANPI = 158 /* proper_tanpi(a): tan(pi a) on [-1/2, 1/2],
+                                  NaN outside, +-inf at +-1/2             */
 } nt2g_opcode;
 
 typedef struct nt2g_op {

@@ -283,7 +283,8 @@ static int n_operands(int code)
     case NT2G_OP_TANH: case NT2G_OP_ASIN: case NT2G_OP_ACOS: case NT2G_OP_ATAN: case NT2G_OP_ASINH:
     case NT2G_OP_ACOSH: case NT2G_OP_ATANH: case NT2G_OP_CBRT: case NT2G_OP_COT: case NT2G_OP_SEC:
     case NT2G_OP_CSC: case NT2G_OP_SIND: case NT2G_OP_COSD: case NT2G_OP_TAND:
-    case NT2G_OP_TANPI: case NT2G_OP_COTPI: case NT2G_OP_COTD: case NT2G_OP_SECPI: case NT2G_OP_CSCPI:
+    case NT2G_OP_TANPI: case NT2G_OP_PROPER_TANPI: case NT2G_OP_COTPI: case NT2G_OP_COTD: case NT2G_OP_SECPI:
+    case NT2G_OP_CSCPI:
     case NT2G_OP_SECD: case NT2G_OP_CSCD: case NT2G_OP_SINC: case NT2G_OP_SINCPI: case NT2G_OP_ACOTD:
     case NT2G_OP_ASEC: case NT2G_OP_COTH: case NT2G_OP_SINHC:
     case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:
@@ -315,7 +316,8 @@ static bool float_only(int code)
     case NT2G_OP_TANH: case NT2G_OP_ASIN: case NT2G_OP_ACOS: case NT2G_OP_ATAN: case NT2G_OP_ATAN2:
     case NT2G_OP_ASINH: case NT2G_OP_ACOSH: case NT2G_OP_ATANH: case NT2G_OP_CBRT: case NT2G_OP_HYPOT:
     case NT2G_OP_COT: case NT2G_OP_SEC: case NT2G_OP_CSC: case NT2G_OP_SIND: case NT2G_OP_COSD: case NT2G_OP_TAND:
-    case NT2G_OP_TANPI: case NT2G_OP_COTPI: case NT2G_OP_COTD: case NT2G_OP_SECPI: case NT2G_OP_CSCPI:
+    case NT2G_OP_TANPI: case NT2G_OP_PROPER_TANPI: case NT2G_OP_COTPI: case NT2G_OP_COTD: case NT2G_OP_SECPI:
+    case NT2G_OP_CSCPI:
     case NT2G_OP_SECD: case NT2G_OP_CSCD: case NT2G_OP_SINC: case NT2G_OP_SINCPI: case NT2G_OP_ACOTD:
     case NT2G_OP_ASEC: case NT2G_OP_COTH: case NT2G_OP_SINHC:
     case NT2G_OP_ACSC: case NT2G_OP_ASECH: case NT2G_OP_ACOTH: case NT2G_OP_ACSCH:

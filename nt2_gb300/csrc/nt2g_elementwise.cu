@@ -597,6 +597,7 @@ __device__ __forceinline__ float f_unary(int op, float a)
     case NT2G_OP_COSD: return cosd<P>(a);
     case NT2G_OP_TAND: return tand<P>(a);
     case NT2G_OP_TANPI: return tanpi<P>(a);
+    case NT2G_OP_PROPER_TANPI: return proper_tanpi<P>(a);
     case NT2G_OP_COTPI: return cotpi<P>(a);
     case NT2G_OP_COTD: return cotd<P>(a);
     case NT2G_OP_SECPI: return secpi<P>(a);

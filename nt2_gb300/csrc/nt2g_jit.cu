@@ -250,6 +250,7 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         case NT2G_OP_COSD: e = "nt2g::cosd<P>(" + A + ")"; break;
         case NT2G_OP_TAND: e = "nt2g::tand<P>(" + A + ")"; break;
         case NT2G_OP_TANPI: e = "nt2g::tanpi<P>(" + A + ")"; break;
+        case NT2G_OP_PROPER_TANPI: e = "nt2g::proper_tanpi<P>(" + A + ")"; break;
         case NT2G_OP_COTPI: e = "nt2g::cotpi<P>(" + A + ")"; break;
         case NT2G_OP_COTD: e = "nt2g::cotd<P>(" + A + ")"; break;
         case NT2G_OP_SECPI: e = "nt2g::secpi<P>(" + A + ")"; break;
@@ -574,7 +575,9 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
     case NT2G_OP_TAN: to(o.a, G + " * (1.0f + " + Y + " * " + Y + ")"); break;
     case NT2G_OP_SINPI: to(o.a, G + " * " + pi + " * nt2g::cospi<D>(" + A + ")"); break;
     case NT2G_OP_COSPI: to(o.a, "-" + G + " * " + pi + " * nt2g::sinpi<D>(" + A + ")"); break;
-    case NT2G_OP_TANPI: to(o.a, G + " * " + pi + " * (1.0f + " + Y + " * " + Y + ")"); break;
+    case NT2G_OP_TANPI: case NT2G_OP_PROPER_TANPI:
+        to(o.a, G + " * " + pi + " * (1.0f + " + Y + " * " + Y + ")");
+        break;
     case NT2G_OP_SIND: to(o.a, G + " * " + deg + " * nt2g::cosd<D>(" + A + ")"); break;
     case NT2G_OP_COSD: to(o.a, "-" + G + " * " + deg + " * nt2g::sind<D>(" + A + ")"); break;
     case NT2G_OP_TAND: to(o.a, G + " * " + deg + " * (1.0f + " + Y + " * " + Y + ")"); break;

@@ -1451,6 +1451,30 @@ template <class P> NT2G_HD float tan(float a0) { return tan_any<P, kRad>(a0); }
 template <class P> NT2G_HD float tand(float a0) { return tan_any<P, kDeg>(a0); }
 template <class P> NT2G_HD float tanpi(float a0) { return tan_any<P, kPi>(a0); }
 
+// proper_tanpi (TRIG/scalar/proper_tanpi.hpp:25-36): tan(pi x) for x in
+// [-1/2, 1/2], NaN outside and +-inf at +-1/2.  NT2 evaluates the unreduced
+// tangent polynomial at |x| pi (one rounded product: the fast-style tana of
+// trig_base.hpp:236-242 under clipped_pio4_) for |x| <= 1/4, else at
+// (1/2 - |x|) pi and takes the reciprocal; x's sign goes on before the
+// reciprocal.  Fast: tanpi's reduction and float-float reciprocal, which
+// agree with it inside the interval.
+template <class P> NT2G_HD float proper_tanpi(float a0)
+{
+    float ab = fabsf(a0);
+    if (P::exact) {
+        if (is_nan(a0)) return a0;
+        if (ab > 0.5f) return f_nan();
+        const bool test = ab <= 0.25f;
+        ab = test ? ab : P::sub(0.5f, ab);
+        float t = trig_tan_eval<P>(P::mul(ab, bits_f(0x40490fdbu)));
+        t = a0 < 0.0f ? -t : t;
+        return test ? t : P::div(1.0f, t);
+    }
+    const float r = tanpi<P>(a0);
+    const float inf = bits_f(0x7f800000u | (f_bits(a0) & 0x80000000u));
+    return ab > 0.5f ? f_nan() : (ab == 0.5f ? inf : r);
+}
+
 // cot (trig_base.hpp:178-188): NaN for NaN/inf and the unit's poles, +-inf at
 // +-0, else 1/tan(xr) or -tan(xr) by the quadrant's parity, with a0's sign
 template <class P, int U> NT2G_HD float cot_any(float a0)

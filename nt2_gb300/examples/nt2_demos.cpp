@@ -317,12 +317,14 @@ int main(int argc, char **argv)
             o = nt2::unifinv(P); save(dir + "unifinv.bin", o);
             o = nt2::caucdf(X, 0.5f, 1.75f); save(dir + "caucdf3.bin", o);
             o = nt2::caupdf(X, 0.5f, 1.75f); save(dir + "caupdf3.bin", o);
+            o = nt2::cauinv(P, 0.5f, 1.75f); save(dir + "cauinv3.bin", o);
+            o = nt2::cauinv(P, 0.5f); save(dir + "cauinv2.bin", o);
             o = nt2::evcdf(X, 0.5f, 1.75f); save(dir + "evcdf3.bin", o);
             o = nt2::evpdf(X, 0.5f, 1.75f); save(dir + "evpdf3.bin", o);
             o = nt2::evinv(P, 0.5f, 1.75f); save(dir + "evinv3.bin", o);
             o = nt2::normpdf(X) + nt2::norminv(P) + nt2::expcdf(X) + nt2::exppdf(X) + nt2::expinv(P) + nt2::logncdf(X) +
                 nt2::lognpdf(X) + nt2::logninv(P) + nt2::unifcdf(X) + nt2::caucdf(X) + nt2::caupdf(X) + nt2::evcdf(X) +
-                nt2::evpdf(X) + nt2::evinv(P);
+                nt2::evpdf(X) + nt2::evinv(P) + nt2::cauinv(P);
             save(dir + "one_param_sum.bin", o);
         } else if (mode == "gen") {
             // generative leaves: NT2's colon (also spelled _), linspace, logspace, alone and in expressions

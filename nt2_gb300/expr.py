@@ -2,7 +2,7 @@
 
 ``Table`` wraps a CUDA tensor; arithmetic operators and the NT2 functor names
 (exp, exp2, exp10, expm1, log, log2, log10, log1p, sin, cos, tan, cot, sec, csc, sinpi, cospi,
-tanpi, cotpi, secpi, cscpi, sind, cosd, tand, cotd, secd, cscd, sinc, sincpi, pow,
+tanpi, proper_tanpi, cotpi, secpi, cscpi, sind, cosd, tand, cotd, secd, cscd, sinc, sincpi, pow,
 sinh, cosh, tanh, coth, sech, csch, sinhc, asinh, acosh, atanh, asech, acsch, acoth,
 asin, acos, atan, acot, asec, acsc, asind, acosd, atand, acotd, asecd, acscd,
 asinpi, acospi, atanpi, atan2, atan2d, indeg, inrad, cbrt, hypot,
@@ -94,6 +94,7 @@ cbrt = _un("CBRT")
 cot, sec, csc = _un("COT"), _un("SEC"), _un("CSC")
 sind, cosd, tand = _un("SIND"), _un("COSD"), _un("TAND")
 tanpi = _un("TANPI")
+proper_tanpi = _un("PROPER_TANPI")
 cotpi = _un("COTPI")
 cotd = _un("COTD")
 secpi = _un("SECPI")
@@ -322,6 +323,15 @@ def caucdf(x, m=None, s=None):
     if m is not None:
         x = x - m if s is None else (x - m) / s
     return 0.5 + atanpi(x)
+
+
+def cauinv(p, m=None, s=None):
+    """cauinv.hpp: proper_tanpi(p - 1/2), then + m or fma(., s, m)."""
+    m, s = _p(m), _p(s)
+    z = proper_tanpi(p - 0.5)
+    if s is not None:
+        return fma(z, s, m)
+    return z if m is None else z + m
 
 
 def caupdf(x, m=None, s=None):

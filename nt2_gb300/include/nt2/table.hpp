@@ -647,6 +647,7 @@ NT2G_UNARY(sind, NT2G_OP_SIND)
 NT2G_UNARY(cosd, NT2G_OP_COSD)
 NT2G_UNARY(tand, NT2G_OP_TAND)
 NT2G_UNARY(tanpi, NT2G_OP_TANPI)
+NT2G_UNARY(proper_tanpi, NT2G_OP_PROPER_TANPI)
 NT2G_UNARY(cotpi, NT2G_OP_COTPI)
 NT2G_UNARY(cotd, NT2G_OP_COTD)
 NT2G_UNARY(secpi, NT2G_OP_SECPI)
@@ -1239,6 +1240,12 @@ template <class X, class M, class S> expr<float> caucdf(const X &x, const M &m, 
 }
 template <class X> expr<float> caucdf(const X &x) { return 0.5f + atanpi(detail::lift_expr(x)); }
 template <class X, class M> expr<float> caucdf(const X &x, const M &m) { return caucdf(detail::lift_expr(x) - m); }
+template <class X> expr<float> cauinv(const X &p) { return proper_tanpi(detail::lift_expr(p) - 0.5f); }
+template <class X, class M> expr<float> cauinv(const X &p, const M &m) { return cauinv(p) + m; }
+template <class X, class M, class S> expr<float> cauinv(const X &p, const M &m, const S &s)
+{
+    return fma(cauinv(p), s, m);
+}
 template <class X> expr<float> caupdf(const X &x)
 {
     const expr<float> a{detail::lift(x)};

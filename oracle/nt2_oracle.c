@@ -859,6 +859,26 @@ EXPORT float o_cotpi(float a0) { return cot_any(a0, 1); }
 EXPORT float o_cotd(float a0) { return cot_any(a0, 2); }
 EXPORT float o_tanpi(float a0) { return tan_any(a0, 1); }
 
+/* proper_tanpi TRIG/scalar/proper_tanpi.hpp:25-36: NaN outside [-1/2, 1/2];
+ * the fast-style tana of trig_base.hpp:236-242 (clipped_pio4_: the tangent
+ * polynomial at |x| * Pi, no reduction) for |x| <= 1/4, else the reciprocal
+ * of it at 1/2 - |x|, x's sign applied before the reciprocal */
+EXPORT float o_proper_tanpi(float a0)
+{
+    if (a0 != a0) return a0;
+    float ab = fabsf(a0);
+    if (ab > 0.5f) return NAN;
+    int test = ab <= 0.25f;
+    ab = test ? ab : 0.5f - ab;
+    float t = tan_eval(ab * bf(0x40490fdbu));
+    t = a0 < 0.0f ? -t : t;
+    return test ? t : 1.0f / t;
+}
+EXPORT void o_proper_tanpi_f32(const float *x, float *out, int64_t m)
+{
+    for (int64_t i = 0; i < m; ++i) out[i] = o_proper_tanpi(x[i]);
+}
+
 /* secpi TRIG/generic/secpi.hpp, cscpi TRIG/generic/cscpi.hpp, secd
  * TRIG/generic/secd.hpp, cscd TRIG/generic/cscd.hpp */
 EXPORT float o_secpi(float a0) { float r = 1.0f / o_cospi(a0); return oddf(a0 * 2.0f) ? NAN : r; }

@@ -30,7 +30,7 @@ FN = dict(exp=0, log=1, log1p=2, erfc=3, normcdf=4, fastnormcdf=5, sqrt=6, exp2=
           erf=64, erfcx=65, expx2=66, gamma=67, gammaln=68, erfinv=69, erfcinv=70, digamma=71, signgam=72, dawson=73, spence=74, stirling=75,
           exprecneg=80, exprecnegc=81, sqrt1pm1=82)
 SCALAR_ONLY = ("o_realsqrt", "o_reallog", "o_floor", "o_ceil", "o_trunc", "o_fix", "o_round", "o_round2even",
-               "o_frac", "o_sign", "o_signnz", "o_oneplus", "o_oneminus", "o_minusone", "o_sqr_abs")
+               "o_frac", "o_sign", "o_signnz", "o_oneplus", "o_oneminus", "o_minusone", "o_sqr_abs", "o_proper_tanpi")
 
 
 def build():
@@ -78,6 +78,7 @@ def lib():
         L.o_expni.argtypes = [ctypes.c_int32, ctypes.c_float]
         L.o_nthroot_f32.argtypes = [_P, _P, _P, _I64]
         L.o_expni_f32.argtypes = [_P, _P, _P, _I64]
+        L.o_proper_tanpi_f32.argtypes = [_P, _P, _I64]
         L.o_atan2d.restype = ctypes.c_float
         L.o_atan2d.argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_hypot.restype = ctypes.c_float
@@ -162,6 +163,14 @@ def nthroot_f32(x, n):
     x, n = _f32(x), _f32(n)
     out = np.empty_like(x)
     lib().o_nthroot_f32(_p(x), _p(n), _p(out), x.size)
+    return out
+
+
+def proper_tanpi_f32(x):
+    """NT2's float proper_tanpi(x) restated (tan(pi x) on [-1/2, 1/2])."""
+    x = _f32(x)
+    out = np.empty_like(x)
+    lib().o_proper_tanpi_f32(_p(x), _p(out), x.size)
     return out
 
 

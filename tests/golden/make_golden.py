@@ -54,6 +54,7 @@ SOURCES = [
     ("modules/core/trigonometric/unit/scalar/tand.cpp", 40, 50),
     # whole files from here on (1-200: every float ULP_EQUAL line they hold)
     ("modules/core/trigonometric/unit/scalar/tanpi.cpp", 1, 200),
+    ("modules/core/trigonometric/unit/scalar/proper_tanpi.cpp", 1, 200),
     ("modules/core/trigonometric/unit/scalar/cotpi.cpp", 1, 200),
     ("modules/core/trigonometric/unit/scalar/cotd.cpp", 1, 200),
     ("modules/core/trigonometric/unit/scalar/secpi.cpp", 1, 200),
@@ -179,12 +180,12 @@ def _value(expr):
 PAT = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(\w+)\((.*?)\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 # two-argument functors: pow(a, b)
 ARG = r"((?:[^,()]|\([^()]*\))*)"
-PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2d?|hypot|logspace_add|logspace_sub|beta|betaln|nthroot|expni|gammainc|gammaincinv|normpdf|norminv|expcdf|exppdf|expinv|logncdf|lognpdf|logninv|caucdf|caupdf|evcdf|evpdf|evinv)\(" + ARG + r",\s*" + ARG +
+PAT2 = re.compile(r"NT2_TEST_ULP_EQUAL\(\s*(pow|atan2d?|hypot|logspace_add|logspace_sub|beta|betaln|nthroot|expni|gammainc|gammaincinv|normpdf|norminv|expcdf|exppdf|expinv|logncdf|lognpdf|logninv|caucdf|cauinv|caupdf|evcdf|evpdf|evinv)\(" + ARG + r",\s*" + ARG +
                   r"\)\s*,\s*(.*?)\s*,\s*([0-9.]+)\s*\);")
 # NT2's distribution functions (statistics/unit/scalar): their one-argument
 # known answers above, the two-argument ones (fn(x, p1)) in the second pass
 STAT_FNS = ("normpdf", "norminv", "expcdf", "exppdf", "expinv", "logncdf", "lognpdf", "logninv", "unifcdf", "unifpdf",
-            "unifinv", "caucdf", "caupdf", "evcdf", "evpdf", "evinv")
+            "unifinv", "caucdf", "cauinv", "caupdf", "evcdf", "evpdf", "evinv")
 SOURCES += [(f"modules/core/statistics/unit/scalar/{f}.cpp", 1, 200) for f in STAT_FNS]
 SOURCES2 = [("modules/core/exponential/unit/scalar/pow.cpp", 43, 53),
             ("modules/core/trigonometric/unit/scalar/atan2.cpp", 47, 61),

@@ -363,10 +363,10 @@ def test_distribution_functions_through_tables(demos, tmp_path, prec):
              "lognpdf3": E.lognpdf(X, m, s), "logninv3": E.logninv(P, m, s), "unifcdf3": E.unifcdf(X, -1.25, 2.5),
              "unifpdf": E.unifpdf(X), "unifinv": E.unifinv(P), "caucdf3": E.caucdf(X, m, s),
              "caupdf3": E.caupdf(X, m, s), "evcdf3": E.evcdf(X, m, s), "evpdf3": E.evpdf(X, m, s),
-             "evinv3": E.evinv(P, m, s),
+             "evinv3": E.evinv(P, m, s), "cauinv3": E.cauinv(P, m, s), "cauinv2": E.cauinv(P, m),
              "one_param_sum": (E.normpdf(X) + E.norminv(P) + E.expcdf(X) + E.exppdf(X) + E.expinv(P) + E.logncdf(X)
                                + E.lognpdf(X) + E.logninv(P) + E.unifcdf(X) + E.caucdf(X) + E.caupdf(X) + E.evcdf(X)
-                               + E.evpdf(X) + E.evinv(P))}
+                               + E.evpdf(X) + E.evinv(P) + E.cauinv(P))}
     for name, e in cases.items():
         out = torch.empty_like(tx)
         E.assign([out], [e], precision=int(prec))

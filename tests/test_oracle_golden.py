@@ -20,7 +20,7 @@ FUNCS = ("exp", "log", "erfc", "normcdf", "fastnormcdf", "exp2", "exp10", "expm1
          "coth", "sinhc", "sech", "csch", "asech", "acsch", "acoth",
          "floor", "ceil", "trunc", "round", "frac", "sign", "signnz", "sqr_abs",
          "erf", "erfcx", "gamma", "gammaln", "erfinv", "erfcinv", "expx2", "exprecneg", "exprecnegc", "sqrt1pm1",
-         "realsqrt", "reallog", "digamma", "signgam", "dawson", "spence", "stirling")
+         "realsqrt", "reallog", "digamma", "signgam", "dawson", "spence", "stirling", "proper_tanpi")
 # NT2's Nan<T>() has every bit set (its sign bit too): copysign(1, Nan) is -1
 NT2_NAN = float(np.uint32(0xffffffff).view(np.float32))
 

@@ -274,7 +274,8 @@ def _unary_cases():
         "exp2": (np.exp2, -5, 5), "exp10": (lambda x: 10.0 ** x, -2, 2), "log2": (np.log2, 0.1, 10),
         "log10": (np.log10, 0.1, 10), "sin": (np.sin, -10, 10), "cos": (np.cos, -10, 10), "tan": (np.tan, -1.2, 1.2),
         "sinpi": (lambda x: np.sin(pi * x), -3, 3), "cospi": (lambda x: np.cos(pi * x), -3, 3),
-        "tanpi": (lambda x: np.tan(pi * x), -0.4, 0.4), "cot": (lambda x: 1 / np.tan(x), 0.2, 2.9),
+        "tanpi": (lambda x: np.tan(pi * x), -0.4, 0.4),
+        "proper_tanpi": (lambda x: np.tan(pi * x), -0.45, 0.45), "cot": (lambda x: 1 / np.tan(x), 0.2, 2.9),
         "sec": (lambda x: 1 / np.cos(x), -1.2, 1.2), "csc": (lambda x: 1 / np.sin(x), 0.3, 2.8),
         "cotpi": (lambda x: 1 / np.tan(pi * x), 0.1, 0.9), "secpi": (lambda x: 1 / np.cos(pi * x), -0.4, 0.4),
         "cscpi": (lambda x: 1 / np.sin(pi * x), 0.1, 0.9), "sind": (lambda x: np.sin(rad * x), -400, 400),

@@ -1,6 +1,7 @@
 """NT2's distribution functions (statistics/functions/generic/*.hpp) as NT2
 composes them: normal pdf/inverse, exponential, lognormal, uniform, Cauchy and
-extreme-value cdf/pdf/inverse, with one- and multi-parameter forms.
+extreme-value cdf/pdf/inverse (cauinv on proper_tanpi, NT2's tangent of pi x
+restricted to [-1/2, 1/2]), with one- and multi-parameter forms.
 
 NT2 policy: bit-identical to the same composition of the oracle's NT2 float
 functors with float32 arithmetic in NT2's operation order.  Fast policy:
@@ -84,6 +85,13 @@ def cases(oracle, sp):
         "caucdf3": (lambda X: E.caucdf(X, float(m), float(s)),
                     lambda x: (F(0.5) + INVPI * atan(((x - m) / s).astype(F))).astype(F),
                     lambda x: 0.5 + np.arctan((x - d(m)) / d(s)) / np.pi, "real"),
+        "proper_tanpi": (lambda X: E.proper_tanpi(X), lambda x: oracle.proper_tanpi_f32(x),
+                         lambda x: np.where(np.abs(x) <= 0.5, np.tan(np.pi * x), np.nan), "half"),
+        "cauinv": (lambda X: E.cauinv(X), lambda x: oracle.proper_tanpi_f32((x - F(0.5)).astype(F)),
+                   lambda x: np.tan(np.pi * (x - 0.5)), "prob"),
+        "cauinv3": (lambda X: E.cauinv(X, float(m), float(s)),
+                    lambda x: ((oracle.proper_tanpi_f32((x - F(0.5)).astype(F)) * s).astype(F) + m).astype(F),
+                    lambda x: np.tan(np.pi * (x - 0.5)) * d(s) + d(m), "prob"),
         "caupdf3": (lambda X: E.caupdf(X, float(m), float(s)),
                     lambda x: ((s * INVPI) / (s * s + np.square((x - m).astype(F)))).astype(F),
                     lambda x: d(s) / np.pi / (d(s) ** 2 + (x - d(m)) ** 2), "real"),
@@ -99,6 +107,8 @@ def cases(oracle, sp):
 def _inputs(kind, rng):
     if kind == "prob":
         x = rng.uniform(0, 1, 1 << 15)
+    elif kind == "half":
+        x = rng.uniform(-0.5, 0.5, 1 << 15)
     elif kind == "pos":
         x = np.exp(rng.uniform(-8, 5, 1 << 15))
     else:
@@ -109,7 +119,7 @@ def _inputs(kind, rng):
 
 @pytest.mark.parametrize("name", ["normpdf", "normpdf3", "norminv", "norminv3", "expcdf", "expcdf2", "exppdf2",
                                   "expinv2", "logncdf3", "lognpdf3", "logninv3", "unifcdf3", "unifpdf", "caucdf3",
-                                  "caupdf3", "evcdf3", "evpdf3", "evinv3"])
+                                  "proper_tanpi", "cauinv", "cauinv3", "caupdf3", "evcdf3", "evpdf3", "evinv3"])
 @pytest.mark.parametrize("prec", [1, 0], ids=["nt2", "fast"])
 def test_distribution(lib, dev, oracle, name, prec):
     sp = pytest.importorskip("scipy.special")
@@ -146,7 +156,7 @@ def test_distribution(lib, dev, oracle, name, prec):
 
 
 STAT_FNS = ("normpdf", "norminv", "expcdf", "exppdf", "expinv", "logncdf", "lognpdf", "logninv", "unifcdf", "unifpdf",
-            "unifinv", "caucdf", "caupdf", "evcdf", "evpdf", "evinv")
+            "unifinv", "caucdf", "cauinv", "caupdf", "evcdf", "evpdf", "evinv", "proper_tanpi")
 
 
 @pytest.mark.parametrize("prec", [1, 0], ids=["nt2", "fast"])
