@@ -127,8 +127,11 @@ typedef enum nt2g_opcode {
                                   evaluated in double                     */
     NT2G_OP_STIRLING = 157, /* stirling(a): NT2's Stirling approximation of
                                Gamma                                      */
-    NT2G_OP_PROPER_TANPI = 158 /* proper_tanpi(a): tan(pi a) on [-1/2, 1/2],
-                                  NaN outside, +-inf at +-1/2             */
+    NT2G_OP_PROPER_TANPI = 158, /* proper_tanpi(a): tan(pi a) on [-1/2, 1/2],
+                                   NaN outside, +-inf at +-1/2            */
+    NT2G_OP_MOD = 159, /* mod(a, b): a - floor(a/b) b (a where b == 0)      */
+    NT2G_OP_REM = 160  /* rem(a, b): a - b trunc(a/b), the quotient through
+                          a saturating int32 (a where b == 0)              */
 } nt2g_opcode;
 
 typedef struct nt2g_op {

@@ -242,6 +242,8 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         case NT2G_OP_POW: e = "nt2g::pow<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_ATAN2: e = "nt2g::atan2<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_HYPOT: e = "nt2g::hypot<P>(" + A + ", " + B + ")"; break;
+        case NT2G_OP_MOD: e = "nt2g::mod_<P>(" + A + ", " + B + ")"; break;
+        case NT2G_OP_REM: e = "nt2g::rem_<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_CBRT: e = "nt2g::cbrt<P>(" + A + ")"; break;
         case NT2G_OP_COT: e = "nt2g::cot<P>(" + A + ")"; break;
         case NT2G_OP_SEC: e = "nt2g::sec<P>(" + A + ")"; break;
@@ -617,6 +619,14 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
         pre = "const float q = " + G + " * " + rcp(A + " * " + A + " + " + B + " * " + B) + ";";
         to(o.a, "q * " + B);
         to(o.b, "-q * " + A);
+        break;
+    case NT2G_OP_MOD:  // a - floor(a/b) b: 1 and -floor(a/b) between the jumps (b = 0: 1 and 0)
+        to(o.a, G);
+        to(o.b, "(" + B + " != 0.0f ? -" + G + " * floorf(" + A + " / " + B + ") : 0.0f)");
+        break;
+    case NT2G_OP_REM:  // a - b trunc(a/b): 1 and -trunc(a/b) between the jumps
+        to(o.a, G);
+        to(o.b, "(" + B + " != 0.0f ? -" + G + " * (float)nt2g::toints(" + A + " / " + B + ") : 0.0f)");
         break;
     case NT2G_OP_HYPOT:
         pre = "const float q = " + Y + " == 0.0f ? 0.0f : " + G + " * " + rcp(Y) + ";";

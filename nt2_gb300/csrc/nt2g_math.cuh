@@ -1451,6 +1451,29 @@ template <class P> NT2G_HD float tan(float a0) { return tan_any<P, kRad>(a0); }
 template <class P> NT2G_HD float tand(float a0) { return tan_any<P, kDeg>(a0); }
 template <class P> NT2G_HD float tanpi(float a0) { return tan_any<P, kPi>(a0); }
 
+// mod (boost/simd/arithmetic/functions/generic/mod.hpp:22-31 with the float
+// divfloor of scalar/divfloor.hpp:89-100): selsub(b != 0, a, floor(a/b)*b),
+// each operation rounded once; rem (scalar/rem.hpp:27-37 with idivfix,
+// generic/idivfix.hpp:38-49): b != 0 ? a - b*q : a, q = itrunc(a/b), the
+// saturating float -> int32 conversion (NaN -> 0) converted back to float.
+// Both policies compute NT2's sequence: a faster quotient could move floor or
+// trunc across an integer.
+template <class P> NT2G_HD float mod_(float a, float b)
+{
+    return b != 0.0f ? Nt2::sub(a, Nt2::mul(floorf(Nt2::div(a, b)), b)) : a;
+}
+NT2G_HD int32_t toints(float v)
+{
+    if (is_nan(v)) return 0;
+    if (v >= 2147483648.0f) return 2147483647;
+    if (v <= -2147483648.0f) return (int32_t)0x80000000u;
+    return (int32_t)v;
+}
+template <class P> NT2G_HD float rem_(float a, float b)
+{
+    return b != 0.0f ? Nt2::sub(a, Nt2::mul(b, (float)toints(Nt2::div(a, b)))) : a;
+}
+
 // proper_tanpi (TRIG/scalar/proper_tanpi.hpp:25-36): tan(pi x) for x in
 // [-1/2, 1/2], NaN outside and +-inf at +-1/2.  NT2 evaluates the unreduced
 // tangent polynomial at |x| pi (one rounded product: the fast-style tana of

@@ -159,6 +159,16 @@ is_eqz, is_nez, is_ltz, is_gtz = _pred("IS_EQZ"), _pred("IS_NEZ"), _pred("IS_LTZ
 def copysign(a, b): return _bin("COPYSIGN", a, b)
 
 
+def mod(a, b):
+    """NT2's mod: a - floor(a/b) b, a where b == 0."""
+    return _bin("MOD", a, b)
+
+
+def rem(a, b):
+    """NT2's rem: a - b itrunc(a/b) (the quotient through a saturating int32), a where b == 0."""
+    return _bin("REM", a, b)
+
+
 # oneplus, oneminus, minusone, sqr_abs, dist, average: boost/simd/arithmetic/
 # functions/generic/{oneplus,oneminus,minusone,sqr_abs,average}.hpp, scalar/dist.hpp
 def oneplus(a): return a + 1.0

@@ -578,6 +578,10 @@ NT2G_BINARY(pow, NT2G_OP_POW, false)
 NT2G_BINARY(atan2, NT2G_OP_ATAN2, false)
 NT2G_BINARY(hypot, NT2G_OP_HYPOT, false)
 NT2G_BINARY(copysign, NT2G_OP_COPYSIGN, false)
+// mod(a, b) = a - floor(a/b) b, rem(a, b) = a - b itrunc(a/b) (boost/simd/arithmetic/functions/
+// generic/mod.hpp, scalar/rem.hpp): a where b == 0
+NT2G_BINARY(mod, NT2G_OP_MOD, false)
+NT2G_BINARY(rem, NT2G_OP_REM, false)
 // nthroot(x, n), expni(n, x), gammainc(x, a), gammaincinv(p, a): the integer n is truncated
 // toward zero (EXP/scalar/nthroot.hpp, EUL/scalar/expni.hpp, EUL/scalar/gammainc.hpp)
 NT2G_BINARY(nthroot, NT2G_OP_NTHROOT, false)

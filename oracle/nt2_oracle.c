@@ -859,6 +859,20 @@ EXPORT float o_cotpi(float a0) { return cot_any(a0, 1); }
 EXPORT float o_cotd(float a0) { return cot_any(a0, 2); }
 EXPORT float o_tanpi(float a0) { return tan_any(a0, 1); }
 
+/* mod boost/simd/arithmetic/functions/generic/mod.hpp:22-31 (float divfloor
+ * scalar/divfloor.hpp:89-100 = floor(a/b)): b != 0 ? a - floor(a/b)*b : a;
+ * rem scalar/rem.hpp:27-37 (idivfix generic/idivfix.hpp:38-49 = itrunc(a/b),
+ * toints scalar/toints.hpp:36-46: NaN -> 0, saturating): b != 0 ? a - b*q : a */
+EXPORT float o_mod(float a, float b) { return b != 0.0f ? a - floorf(a / b) * b : a; }
+static int32_t o_toints(float v)
+{
+    if (v != v) return 0;
+    if (v >= 2147483648.0f) return INT32_MAX;
+    if (v <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)v;
+}
+EXPORT float o_rem(float a, float b) { return b != 0.0f ? a - b * (float)o_toints(a / b) : a; }
+
 /* proper_tanpi TRIG/scalar/proper_tanpi.hpp:25-36: NaN outside [-1/2, 1/2];
  * the fast-style tana of trig_base.hpp:236-242 (clipped_pio4_: the tangent
  * polynomial at |x| * Pi, no reduction) for |x| <= 1/4, else the reciprocal
