@@ -130,8 +130,12 @@ typedef enum nt2g_opcode {
     NT2G_OP_PROPER_TANPI = 158, /* proper_tanpi(a): tan(pi a) on [-1/2, 1/2],
                                    NaN outside, +-inf at +-1/2            */
     NT2G_OP_MOD = 159, /* mod(a, b): a - floor(a/b) b (a where b == 0)      */
-    NT2G_OP_REM = 160  /* rem(a, b): a - b trunc(a/b), the quotient through
+    NT2G_OP_REM = 160, /* rem(a, b): a - b trunc(a/b), the quotient through
                           a saturating int32 (a where b == 0)              */
+    NT2G_OP_POW2 = 161 /* pow2(a, b): a * 2^n, n = b truncated to int32, by
+                          NT2's fast_ldexp: (n + 127) << 23 in wrapping int32
+                          arithmetic as the scale's bits (n outside
+                          [-127, 128] gives that bit pattern)              */
 } nt2g_opcode;
 
 typedef struct nt2g_op {

@@ -299,7 +299,8 @@ static int n_operands(int code)
     case NT2G_OP_LT: case NT2G_OP_GT: case NT2G_OP_LE: case NT2G_OP_GE: case NT2G_OP_EQ: case NT2G_OP_NE:
     case NT2G_OP_SELINC: case NT2G_OP_SELDEC: case NT2G_OP_ADDS: case NT2G_OP_POW:
     case NT2G_OP_ATAN2: case NT2G_OP_HYPOT: case NT2G_OP_COPYSIGN: case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI:
-    case NT2G_OP_GAMMAINC: case NT2G_OP_GAMMAINCINV: case NT2G_OP_MOD: case NT2G_OP_REM: return 2;
+    case NT2G_OP_GAMMAINC: case NT2G_OP_GAMMAINCINV: case NT2G_OP_MOD: case NT2G_OP_REM:
+    case NT2G_OP_POW2: return 2;
     case NT2G_OP_FMA: case NT2G_OP_FNMS: case NT2G_OP_IF_ELSE: return 3;
     default: return -1;
     }
@@ -327,7 +328,7 @@ static bool float_only(int code)
     case NT2G_OP_NTHROOT: case NT2G_OP_EXPNI: case NT2G_OP_GAMMAINC: case NT2G_OP_GAMMAINCINV:
     case NT2G_OP_FLOOR: case NT2G_OP_CEIL: case NT2G_OP_TRUNC: case NT2G_OP_ROUND: case NT2G_OP_ROUND2EVEN:
     case NT2G_OP_FRAC: case NT2G_OP_SIGN: case NT2G_OP_SIGNNZ: case NT2G_OP_COPYSIGN: case NT2G_OP_MOD:
-    case NT2G_OP_REM:
+    case NT2G_OP_REM: case NT2G_OP_POW2:
     case NT2G_OP_IS_NAN: case NT2G_OP_IS_INF: case NT2G_OP_IS_FINITE: case NT2G_OP_IS_EQZ: case NT2G_OP_IS_NEZ:
     case NT2G_OP_IS_LTZ: case NT2G_OP_IS_GTZ:
         return true;

@@ -738,7 +738,7 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                 }
                 break;
             case NT2G_OP_POW: case NT2G_OP_ATAN2: case NT2G_OP_HYPOT: case NT2G_OP_COPYSIGN: case NT2G_OP_MOD:
-            case NT2G_OP_REM:
+            case NT2G_OP_REM: case NT2G_OP_POW2:
                 for (int j = 0; j < kV; ++j) {
                     const float x = __uint_as_float(A[j]), y = __uint_as_float(B[j]);
                     d[j] = __float_as_uint(in.op == NT2G_OP_POW     ? pow<P>(x, y)
@@ -746,6 +746,7 @@ __global__ void __launch_bounds__(128) k_interp(const DProgram prog, const DArgs
                                            : in.op == NT2G_OP_HYPOT ? hypot<P>(x, y)
                                            : in.op == NT2G_OP_MOD   ? mod_<P>(x, y)
                                            : in.op == NT2G_OP_REM   ? rem_<P>(x, y)
+                                           : in.op == NT2G_OP_POW2  ? pow2_<P>(x, y)
                                                                     : copysignf(x, y));
                 }
                 break;

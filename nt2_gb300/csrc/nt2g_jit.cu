@@ -244,6 +244,7 @@ static void emit_body(std::string &s, const std::vector<nt2g_op> &ops, const std
         case NT2G_OP_HYPOT: e = "nt2g::hypot<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_MOD: e = "nt2g::mod_<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_REM: e = "nt2g::rem_<P>(" + A + ", " + B + ")"; break;
+        case NT2G_OP_POW2: e = "nt2g::pow2_<P>(" + A + ", " + B + ")"; break;
         case NT2G_OP_CBRT: e = "nt2g::cbrt<P>(" + A + ")"; break;
         case NT2G_OP_COT: e = "nt2g::cot<P>(" + A + ")"; break;
         case NT2G_OP_SEC: e = "nt2g::sec<P>(" + A + ")"; break;
@@ -627,6 +628,9 @@ static bool adjoint_rule(std::string &s, const std::vector<nt2g_op> &ops, int k,
     case NT2G_OP_REM:  // a - b trunc(a/b): 1 and -trunc(a/b) between the jumps
         to(o.a, G);
         to(o.b, "(" + B + " != 0.0f ? -" + G + " * (float)nt2g::toints(" + A + " / " + B + ") : 0.0f)");
+        break;
+    case NT2G_OP_POW2:  // a 2^n: the scale for a; n is piecewise constant
+        to(o.a, G + " * nt2g::pow2_<D>(1.0f, " + B + ")");
         break;
     case NT2G_OP_HYPOT:
         pre = "const float q = " + Y + " == 0.0f ? 0.0f : " + G + " * " + rcp(Y) + ";";

@@ -1474,6 +1474,20 @@ template <class P> NT2G_HD float rem_(float a, float b)
     return b != 0.0f ? Nt2::sub(a, Nt2::mul(b, (float)toints(Nt2::div(a, b)))) : a;
 }
 
+// pow2 (EXP/generic/pow2.hpp:21-70): fast_ldexp(a, toint(b)), i.e. a times
+// the float whose bits are (n + Maxexponent) << Nbmantissabits in wrapping
+// int32 arithmetic (boost/simd/ieee/functions/scalar/fast_ldexp.hpp:33-43);
+// toint is C's truncating conversion, INT_MIN outside the int32 range and for
+// NaN (the x86 conversion NT2 runs on).  pow2(x) is pow2(1, x).
+NT2G_HD int32_t toint_x86(float v)
+{
+    return (v >= -2147483648.0f && v < 2147483648.0f) ? (int32_t)v : (int32_t)0x80000000u;
+}
+template <class P> NT2G_HD float pow2_(float a, float b)
+{
+    return Nt2::mul(a, bits_f(((uint32_t)toint_x86(b) + 127u) << 23));
+}
+
 // proper_tanpi (TRIG/scalar/proper_tanpi.hpp:25-36): tan(pi x) for x in
 // [-1/2, 1/2], NaN outside and +-inf at +-1/2.  NT2 evaluates the unreduced
 // tangent polynomial at |x| pi (one rounded product: the fast-style tana of

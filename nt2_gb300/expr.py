@@ -164,6 +164,11 @@ def mod(a, b):
     return _bin("MOD", a, b)
 
 
+def pow2(a, b=None):
+    """NT2's pow2: a * 2^trunc(b) by fast_ldexp (pow2(x) = 2^trunc(x))."""
+    return _bin("POW2", 1.0, a) if b is None else _bin("POW2", a, b)
+
+
 def rem(a, b):
     """NT2's rem: a - b itrunc(a/b) (the quotient through a saturating int32), a where b == 0."""
     return _bin("REM", a, b)

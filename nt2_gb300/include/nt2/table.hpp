@@ -582,6 +582,9 @@ NT2G_BINARY(copysign, NT2G_OP_COPYSIGN, false)
 // generic/mod.hpp, scalar/rem.hpp): a where b == 0
 NT2G_BINARY(mod, NT2G_OP_MOD, false)
 NT2G_BINARY(rem, NT2G_OP_REM, false)
+// pow2(a, b) = a * 2^trunc(b), pow2(x) = 2^trunc(x) (EXP/generic/pow2.hpp, NT2's fast_ldexp)
+NT2G_BINARY(pow2, NT2G_OP_POW2, false)
+template <class A> expr<float> pow2(const A &a) { return pow2(1.0f, a); }
 // nthroot(x, n), expni(n, x), gammainc(x, a), gammaincinv(p, a): the integer n is truncated
 // toward zero (EXP/scalar/nthroot.hpp, EUL/scalar/expni.hpp, EUL/scalar/gammainc.hpp)
 NT2G_BINARY(nthroot, NT2G_OP_NTHROOT, false)

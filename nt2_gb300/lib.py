@@ -30,7 +30,7 @@ OP = dict(
     ASIN=90, ACOS=91, ATAN=92, ATAN2=93, ASINH=94, ACOSH=95, ATANH=96, CBRT=97, HYPOT=98,
     COT=100, SEC=101, CSC=102, SIND=103, COSD=104, TAND=105,
     TANPI=106, COTPI=107, COTD=108, SECPI=109, CSCPI=110, SECD=111, CSCD=112, SINC=113, SINCPI=114, ACOTD=115, ASEC=116, COTH=117, SINHC=118, ACSC=119, ASECH=120, ACOTH=121, ACSCH=122,
-    ERF=123, ERFCX=124, EXPX2=125, GAMMA=126, GAMMALN=127, EXPRECNEG=128, EXPRECNEGC=129, SQRT1PM1=130, ERFINV=131, ERFCINV=132, SIGNGAM=149, DIGAMMA=150, DAWSON=151, NTHROOT=152, EXPNI=153, GAMMAINC=154, SPENCE=155, GAMMAINCINV=156, STIRLING=157, PROPER_TANPI=158, MOD=159, REM=160,
+    ERF=123, ERFCX=124, EXPX2=125, GAMMA=126, GAMMALN=127, EXPRECNEG=128, EXPRECNEGC=129, SQRT1PM1=130, ERFINV=131, ERFCINV=132, SIGNGAM=149, DIGAMMA=150, DAWSON=151, NTHROOT=152, EXPNI=153, GAMMAINC=154, SPENCE=155, GAMMAINCINV=156, STIRLING=157, PROPER_TANPI=158, MOD=159, REM=160, POW2=161,
     FLOOR=133, CEIL=134, TRUNC=135, ROUND=136, ROUND2EVEN=137, FRAC=138, SIGN=139, SIGNNZ=140, COPYSIGN=141,
     IS_NAN=142, IS_INF=143, IS_FINITE=144, IS_EQZ=145, IS_NEZ=146, IS_LTZ=147, IS_GTZ=148,
 )

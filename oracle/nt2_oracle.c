@@ -873,6 +873,16 @@ static int32_t o_toints(float v)
 }
 EXPORT float o_rem(float a, float b) { return b != 0.0f ? a - b * (float)o_toints(a / b) : a; }
 
+/* pow2 EXP/generic/pow2.hpp:21-70: fast_ldexp(a, toint(b)) =
+ * a * bits((n + 127) << 23) in wrapping int32 arithmetic
+ * (boost/simd/ieee/functions/scalar/fast_ldexp.hpp:33-43); toint truncates,
+ * INT_MIN outside int32 and for NaN (x86's conversion) */
+EXPORT float o_pow2(float a, float b)
+{
+    int32_t n = (b >= -2147483648.0f && b < 2147483648.0f) ? (int32_t)b : INT32_MIN;
+    return a * bf(((uint32_t)n + 127u) << 23);
+}
+
 /* proper_tanpi TRIG/scalar/proper_tanpi.hpp:25-36: NaN outside [-1/2, 1/2];
  * the fast-style tana of trig_base.hpp:236-242 (clipped_pio4_: the tangent
  * polynomial at |x| * Pi, no reduction) for |x| <= 1/4, else the reciprocal

@@ -212,20 +212,21 @@ EQ = re.compile(r"NT2_TEST_EQUAL\(\s*(\w+)\(" + r"((?:[^,()]|\([^()]*\))*)" + r"
 EQ_SOURCES = [f"modules/boost/simd/base/unit/arithmetic/scalar/{f}.cpp" for f in
               ("floor", "ceil", "trunc", "round", "round2even", "oneplus", "oneminus", "minusone", "dist", "average",
                "sqr_abs", "mod", "rem")] + [f"modules/boost/simd/base/unit/ieee/scalar/{f}.cpp" for f in ("frac", "sign", "signnz",
-                                                                                           "copysign")]
+                                                                                           "copysign")] + \
+             ["modules/core/exponential/unit/scalar/pow2.cpp"]
 
 
 def _real_block_equalities(root, rel):
     out, skipped, inside = [], 0, False
     for ln, line in enumerate(open(os.path.join(root, rel)).read().splitlines(), 1):
         if "NT2_TEST_CASE_TPL" in line:
-            inside = "_real" in line
+            inside = "_real" in line or "REAL_TYPES" in line
             continue
         m = EQ.search(line) if inside else None
         if not m:
             continue
         fn, a0, a1, exp = m.groups()
-        if (a1 is not None) != (fn in ("copysign", "dist", "average", "mod", "rem")):
+        if (a1 is not None) != (fn in ("copysign", "dist", "average", "mod", "rem", "pow2")):
             continue  # another arity (round(x, n) rounds to n digits): not these functors
         try:
             rec = dict(fn=fn, x=_value(a0), expected=_value(exp), tol_nt2ulp=0.0, source=f"{rel}:{ln}")

@@ -401,7 +401,7 @@ def _vjp_programs(lib):
         progs.append(E.compile_program([torch.zeros(n)], [acc])[0])
     e = (E.pow(x, y) + E.atan2(x, y) + E.hypot(x, y) + x / y + E.min_(x, y) + E.max_(x, y) + E.copysign(x, y)
          + E.fma(x, y, z) + E.fnms(x, y, z) + E.if_else(x > y, y, z) + E.selinc(x < z, y) + E.seldec(x > z, z)
-         + E.if_zero_else_one(x < y, lib.F32) - (-x) + E.mod(x, y) + E.rem(y, z))
+         + E.if_zero_else_one(x < y, lib.F32) - (-x) + E.mod(x, y) + E.rem(y, z) + E.pow2(x, y) + E.pow2(z))
     progs.append(E.compile_program([torch.zeros(n)], [e])[0])
     e = (E.nthroot(x, 3.0) + E.nthroot(y, z) + E.expni(2.0, x) + E.expni(z, y) + E.gammainc(x, 2.5)
          + E.gammaincinv(x, 2.5))

@@ -1,5 +1,5 @@
 """NT2's exact arithmetic functors on the GPU: floor, ceil, trunc (fix), round,
-round2even, frac, sign, signnz, copysign, mod, rem and the compositions oneplus,
+round2even, frac, sign, signnz, copysign, mod, rem, pow2 and the compositions oneplus,
 oneminus, minusone, sqr_abs, dist, average (boost/simd arithmetic and ieee
 functors).  Each is correctly rounded (or exact), so both policies must equal
 the oracle bit for bit -- average excepted under the fast policy, whose fma is
@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 
 UNARY = ["floor", "ceil", "trunc", "fix", "round", "round2even", "frac", "sign", "signnz", "oneplus", "oneminus",
          "minusone", "sqr_abs"]
-BINARY = ["copysign", "dist", "average", "mod", "rem"]
+BINARY = ["copysign", "dist", "average", "mod", "rem", "pow2"]
 NT2_NAN = float(np.uint32(0xffffffff).view(np.float32))  # NT2's Nan<T>(): every bit set
 
 
