@@ -319,6 +319,15 @@ int main(int argc, char **argv)
             o = nt2::caupdf(X, 0.5f, 1.75f); save(dir + "caupdf3.bin", o);
             o = nt2::cauinv(P, 0.5f, 1.75f); save(dir + "cauinv3.bin", o);
             o = nt2::cauinv(P, 0.5f); save(dir + "cauinv2.bin", o);
+            // boost.simd's selects, minmod, negate, fms and fnma over the same tables
+            o = nt2::maxnum(X, P); save(dir + "maxnum.bin", o);
+            o = nt2::minnum(P, X); save(dir + "minnum.bin", o);
+            o = nt2::maxmag(X, P); save(dir + "maxmag.bin", o);
+            o = nt2::minmag(X, P); save(dir + "minmag.bin", o);
+            o = nt2::minmod(X, P - 0.5f); save(dir + "minmod.bin", o);
+            o = nt2::negate(P, X); save(dir + "negate.bin", o);
+            o = nt2::fms(X, P, 0.25f); save(dir + "fms.bin", o);
+            o = nt2::fnma(X, P, X); save(dir + "fnma.bin", o);
             o = nt2::evcdf(X, 0.5f, 1.75f); save(dir + "evcdf3.bin", o);
             o = nt2::evpdf(X, 0.5f, 1.75f); save(dir + "evpdf3.bin", o);
             o = nt2::evinv(P, 0.5f, 1.75f); save(dir + "evinv3.bin", o);

@@ -483,6 +483,55 @@ def if_else(c, a, b):
     return Node("IF_ELSE", (c, _wrap(a, dt), _wrap(b, dt)), dt)
 
 
+# boost.simd's NaN-ignoring and magnitude selects, minmod, negate, fms and fnma
+# as their scalar float definitions compose them
+# (boost/simd/ieee/functions/scalar/{maxnum,minnum,maxmag,minmag,negate}.hpp,
+# boost/simd/arithmetic/functions/{scalar/minmod,generic/fms,generic/fnma}.hpp)
+def maxnum(a, b):
+    """is_nan(a) ? b : max(b, a)."""
+    a, b = _p(a), _p(b)
+    return if_else(is_nan(a), b, max_(b, a))
+
+
+def minnum(a, b):
+    """is_nan(a) ? b : min(b, a)."""
+    a, b = _p(a), _p(b)
+    return if_else(is_nan(a), b, min_(b, a))
+
+
+def maxmag(a, b):
+    """|a| > |b| ? a : |b| > |a| ? b : max(a, b)."""
+    a, b = _p(a), _p(b)
+    return if_else(abs_(a) > abs_(b), a, if_else(abs_(b) > abs_(a), b, max_(a, b)))
+
+
+def minmag(a, b):
+    """|a| < |b| ? a : |b| < |a| ? b : min(a, b)."""
+    a, b = _p(a), _p(b)
+    return if_else(abs_(a) < abs_(b), a, if_else(abs_(b) < abs_(a), b, min_(a, b)))
+
+
+def minmod(a, b):
+    """is_nltz(a*b) ? min(a, b) : 0."""
+    a, b = _p(a), _p(b)
+    return if_else(a * b < 0.0, 0.0, min_(a, b))
+
+
+def negate(a, b):
+    """a * sign(b)."""
+    return _p(a) * sign(_p(b))
+
+
+def fms(a, b, c):
+    """a*b - c (a product and a difference, as NT2 writes it)."""
+    return _p(a) * _p(b) - _p(c)
+
+
+def fnma(a, b, c):
+    """-c - a*b."""
+    return -_p(c) - _p(a) * _p(b)
+
+
 def selinc(c, a): return Node("SELINC", (c, a), a.dtype)
 def seldec(c, a): return Node("SELDEC", (c, a), a.dtype)
 def if_zero_else_one(c, dtype): return Node("IF_ZERO_ELSE_ONE", (c,), dtype)

@@ -1247,6 +1247,46 @@ template <class X, class M, class S> expr<float> caucdf(const X &x, const M &m, 
 }
 template <class X> expr<float> caucdf(const X &x) { return 0.5f + atanpi(detail::lift_expr(x)); }
 template <class X, class M> expr<float> caucdf(const X &x, const M &m) { return caucdf(detail::lift_expr(x) - m); }
+// boost.simd's NaN-ignoring and magnitude selects, minmod, negate, fms and
+// fnma as their scalar float definitions compose them
+// (boost/simd/ieee/functions/scalar/{maxnum,minnum,maxmag,minmag,negate}.hpp,
+// boost/simd/arithmetic/functions/{scalar/minmod,generic/fms,generic/fnma}.hpp)
+template <class A, class B> expr<float> maxnum(const A &a, const B &b)
+{
+    return if_else(is_nan(detail::lift_expr(a)), b, max(b, a));
+}
+template <class A, class B> expr<float> minnum(const A &a, const B &b)
+{
+    return if_else(is_nan(detail::lift_expr(a)), b, min(b, a));
+}
+template <class A, class B> expr<float> maxmag(const A &a, const B &b)
+{
+    const expr<float> x = detail::lift_expr(a), y = detail::lift_expr(b);
+    return if_else(abs(x) > abs(y), x, if_else(abs(y) > abs(x), y, max(x, y)));
+}
+template <class A, class B> expr<float> minmag(const A &a, const B &b)
+{
+    const expr<float> x = detail::lift_expr(a), y = detail::lift_expr(b);
+    return if_else(abs(x) < abs(y), x, if_else(abs(y) < abs(x), y, min(x, y)));
+}
+template <class A, class B> expr<float> minmod(const A &a, const B &b)
+{
+    const expr<float> x = detail::lift_expr(a), y = detail::lift_expr(b);
+    return if_else(x * y < 0.0f, 0.0f, min(x, y));
+}
+template <class A, class B> expr<float> negate(const A &a, const B &b)
+{
+    return detail::lift_expr(a) * sign(detail::lift_expr(b));
+}
+template <class A, class B, class C> expr<float> fms(const A &a, const B &b, const C &c)
+{
+    return detail::lift_expr(a) * b - c;
+}
+template <class A, class B, class C> expr<float> fnma(const A &a, const B &b, const C &c)
+{
+    return -detail::lift_expr(c) - detail::lift_expr(a) * b;
+}
+
 template <class X> expr<float> cauinv(const X &p) { return proper_tanpi(detail::lift_expr(p) - 0.5f); }
 template <class X, class M> expr<float> cauinv(const X &p, const M &m) { return cauinv(p) + m; }
 template <class X, class M, class S> expr<float> cauinv(const X &p, const M &m, const S &s)

@@ -873,6 +873,29 @@ static int32_t o_toints(float v)
 }
 EXPORT float o_rem(float a, float b) { return b != 0.0f ? a - b * (float)o_toints(a / b) : a; }
 
+/* boost.simd's scalar float selects, minmod and negate:
+ * ieee/functions/scalar/maxnum.hpp, minnum.hpp (is_nan(a) ? b : max/min(b, a),
+ * max(x, y) = x > y ? x : y), maxmag.hpp, minmag.hpp (by magnitude, ties to
+ * max/min), arithmetic/functions/scalar/minmod.hpp (is_nltz(a*b) ? min : 0),
+ * ieee/functions/scalar/negate.hpp (a * sign(b)) */
+EXPORT float o_sign(float a0);
+static float o_max2(float x, float y) { return x > y ? x : y; }
+static float o_min2(float x, float y) { return x < y ? x : y; }
+EXPORT float o_maxnum(float a, float b) { return (a != a) ? b : o_max2(b, a); }
+EXPORT float o_minnum(float a, float b) { return (a != a) ? b : o_min2(b, a); }
+EXPORT float o_maxmag(float a, float b)
+{
+    float x = fabsf(a), y = fabsf(b);
+    return x > y ? a : y > x ? b : o_max2(a, b);
+}
+EXPORT float o_minmag(float a, float b)
+{
+    float x = fabsf(a), y = fabsf(b);
+    return x < y ? a : y < x ? b : o_min2(a, b);
+}
+EXPORT float o_minmod(float a, float b) { return !(a * b < 0.0f) ? o_min2(a, b) : 0.0f; }
+EXPORT float o_negate(float a, float b) { return a * o_sign(b); }
+
 /* pow2 EXP/generic/pow2.hpp:21-70: fast_ldexp(a, toint(b)) =
  * a * bits((n + 127) << 23) in wrapping int32 arithmetic
  * (boost/simd/ieee/functions/scalar/fast_ldexp.hpp:33-43); toint truncates,

@@ -211,8 +211,9 @@ SELF_REFERENCE = re.compile(r"nt2::(sin|sinpi|cos|exp)\(|boost::math::")
 EQ = re.compile(r"NT2_TEST_EQUAL\(\s*(\w+)\(" + r"((?:[^,()]|\([^()]*\))*)" + r"(?:,\s*((?:[^,()]|\([^()]*\))*))?\)\s*,\s*(.*?)\s*\);")
 EQ_SOURCES = [f"modules/boost/simd/base/unit/arithmetic/scalar/{f}.cpp" for f in
               ("floor", "ceil", "trunc", "round", "round2even", "oneplus", "oneminus", "minusone", "dist", "average",
-               "sqr_abs", "mod", "rem")] + [f"modules/boost/simd/base/unit/ieee/scalar/{f}.cpp" for f in ("frac", "sign", "signnz",
-                                                                                           "copysign")] + \
+               "sqr_abs", "mod", "rem", "minmod")] + [f"modules/boost/simd/base/unit/ieee/scalar/{f}.cpp" for f in ("frac", "sign", "signnz",
+                                                                                           "copysign", "maxnum", "minnum",
+                                                                                           "maxmag", "minmag", "negate")] + \
              ["modules/core/exponential/unit/scalar/pow2.cpp"]
 
 
@@ -226,7 +227,8 @@ def _real_block_equalities(root, rel):
         if not m:
             continue
         fn, a0, a1, exp = m.groups()
-        if (a1 is not None) != (fn in ("copysign", "dist", "average", "mod", "rem", "pow2")):
+        if (a1 is not None) != (fn in ("copysign", "dist", "average", "mod", "rem", "pow2", "maxnum", "minnum",
+                                                 "maxmag", "minmag", "minmod", "negate")):
             continue  # another arity (round(x, n) rounds to n digits): not these functors
         try:
             rec = dict(fn=fn, x=_value(a0), expected=_value(exp), tol_nt2ulp=0.0, source=f"{rel}:{ln}")

@@ -364,6 +364,9 @@ def test_distribution_functions_through_tables(demos, tmp_path, prec):
              "unifpdf": E.unifpdf(X), "unifinv": E.unifinv(P), "caucdf3": E.caucdf(X, m, s),
              "caupdf3": E.caupdf(X, m, s), "evcdf3": E.evcdf(X, m, s), "evpdf3": E.evpdf(X, m, s),
              "evinv3": E.evinv(P, m, s), "cauinv3": E.cauinv(P, m, s), "cauinv2": E.cauinv(P, m),
+             "maxnum": E.maxnum(X, P), "minnum": E.minnum(P, X), "maxmag": E.maxmag(X, P), "minmag": E.minmag(X, P),
+             "minmod": E.minmod(X, P - 0.5), "negate": E.negate(P, X), "fms": E.fms(X, P, 0.25),
+             "fnma": E.fnma(X, P, X),
              "one_param_sum": (E.normpdf(X) + E.norminv(P) + E.expcdf(X) + E.exppdf(X) + E.expinv(P) + E.logncdf(X)
                                + E.lognpdf(X) + E.logninv(P) + E.unifcdf(X) + E.caucdf(X) + E.caupdf(X) + E.evcdf(X)
                                + E.evpdf(X) + E.evinv(P) + E.cauinv(P))}
