@@ -328,6 +328,8 @@ int main(int argc, char **argv)
             o = nt2::negate(P, X); save(dir + "negate.bin", o);
             o = nt2::fms(X, P, 0.25f); save(dir + "fms.bin", o);
             o = nt2::fnma(X, P, X); save(dir + "fnma.bin", o);
+            o = nt2::divfloor(X, P); save(dir + "divfloor.bin", o);
+            o = nt2::divround2even(X, 0.75f); save(dir + "divround2even.bin", o);
             o = nt2::evcdf(X, 0.5f, 1.75f); save(dir + "evcdf3.bin", o);
             o = nt2::evpdf(X, 0.5f, 1.75f); save(dir + "evpdf3.bin", o);
             o = nt2::evinv(P, 0.5f, 1.75f); save(dir + "evinv3.bin", o);

@@ -532,6 +532,16 @@ def fnma(a, b, c):
     return -_p(c) - _p(a) * _p(b)
 
 
+# boost.simd's rounded quotients for floats (boost/simd/arithmetic/functions/
+# scalar/{divfloor,divceil,divfix,divround,divround2even}.hpp): the rounding
+# of the correctly rounded a/b (both policies divide correctly rounded)
+def divfloor(a, b): return floor(_p(a) / _p(b))
+def divceil(a, b): return ceil(_p(a) / _p(b))
+def divfix(a, b): return trunc(_p(a) / _p(b))
+def divround(a, b): return round(_p(a) / _p(b))
+def divround2even(a, b): return round2even(_p(a) / _p(b))
+
+
 def selinc(c, a): return Node("SELINC", (c, a), a.dtype)
 def seldec(c, a): return Node("SELDEC", (c, a), a.dtype)
 def if_zero_else_one(c, dtype): return Node("IF_ZERO_ELSE_ONE", (c,), dtype)

@@ -1251,6 +1251,17 @@ template <class X, class M> expr<float> caucdf(const X &x, const M &m) { return 
 // fnma as their scalar float definitions compose them
 // (boost/simd/ieee/functions/scalar/{maxnum,minnum,maxmag,minmag,negate}.hpp,
 // boost/simd/arithmetic/functions/{scalar/minmod,generic/fms,generic/fnma}.hpp)
+// boost.simd's rounded quotients for floats (boost/simd/arithmetic/functions/
+// scalar/{divfloor,divceil,divfix,divround,divround2even}.hpp): the rounding of
+// the correctly rounded a/b
+template <class A, class B> expr<float> divfloor(const A &a, const B &b) { return floor(detail::lift_expr(a) / b); }
+template <class A, class B> expr<float> divceil(const A &a, const B &b) { return ceil(detail::lift_expr(a) / b); }
+template <class A, class B> expr<float> divfix(const A &a, const B &b) { return trunc(detail::lift_expr(a) / b); }
+template <class A, class B> expr<float> divround(const A &a, const B &b) { return round(detail::lift_expr(a) / b); }
+template <class A, class B> expr<float> divround2even(const A &a, const B &b)
+{
+    return round2even(detail::lift_expr(a) / b);
+}
 template <class A, class B> expr<float> maxnum(const A &a, const B &b)
 {
     return if_else(is_nan(detail::lift_expr(a)), b, max(b, a));

@@ -895,6 +895,14 @@ EXPORT float o_minmag(float a, float b)
 }
 EXPORT float o_minmod(float a, float b) { return !(a * b < 0.0f) ? o_min2(a, b) : 0.0f; }
 EXPORT float o_negate(float a, float b) { return a * o_sign(b); }
+/* divfloor, divceil, divfix, divround, divround2even for floats
+ * (arithmetic/functions/scalar/div*.hpp): the rounding of a/b */
+EXPORT float o_round2even(float a0);
+EXPORT float o_divfloor(float a, float b) { return floorf(a / b); }
+EXPORT float o_divceil(float a, float b) { return ceilf(a / b); }
+EXPORT float o_divfix(float a, float b) { return truncf(a / b); }
+EXPORT float o_divround(float a, float b) { return roundf(a / b); }
+EXPORT float o_divround2even(float a, float b) { return o_round2even(a / b); }
 
 /* pow2 EXP/generic/pow2.hpp:21-70: fast_ldexp(a, toint(b)) =
  * a * bits((n + 127) << 23) in wrapping int32 arithmetic

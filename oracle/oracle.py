@@ -71,7 +71,7 @@ def lib():
         L.o_atan2_f64.argtypes = [_P, _P, _P, _I64]
         for f in ("o_logspace_add", "o_logspace_sub", "o_copysign", "o_dist", "o_average", "o_beta", "o_betaln",
                   "o_mod", "o_rem", "o_pow2", "o_maxnum", "o_minnum", "o_maxmag", "o_minmag", "o_minmod",
-                  "o_negate"):
+                  "o_negate", "o_divfloor", "o_divceil", "o_divfix", "o_divround", "o_divround2even"):
             getattr(L, f).restype = ctypes.c_float
             getattr(L, f).argtypes = [ctypes.c_float, ctypes.c_float]
         L.o_nthroot.restype = ctypes.c_float

@@ -211,7 +211,8 @@ SELF_REFERENCE = re.compile(r"nt2::(sin|sinpi|cos|exp)\(|boost::math::")
 EQ = re.compile(r"NT2_TEST_EQUAL\(\s*(\w+)\(" + r"((?:[^,()]|\([^()]*\))*)" + r"(?:,\s*((?:[^,()]|\([^()]*\))*))?\)\s*,\s*(.*?)\s*\);")
 EQ_SOURCES = [f"modules/boost/simd/base/unit/arithmetic/scalar/{f}.cpp" for f in
               ("floor", "ceil", "trunc", "round", "round2even", "oneplus", "oneminus", "minusone", "dist", "average",
-               "sqr_abs", "mod", "rem", "minmod")] + [f"modules/boost/simd/base/unit/ieee/scalar/{f}.cpp" for f in ("frac", "sign", "signnz",
+               "sqr_abs", "mod", "rem", "minmod", "divfloor", "divceil", "divfix", "divround",
+               "divround2even")] + [f"modules/boost/simd/base/unit/ieee/scalar/{f}.cpp" for f in ("frac", "sign", "signnz",
                                                                                            "copysign", "maxnum", "minnum",
                                                                                            "maxmag", "minmag", "negate")] + \
              ["modules/core/exponential/unit/scalar/pow2.cpp"]
@@ -228,7 +229,8 @@ def _real_block_equalities(root, rel):
             continue
         fn, a0, a1, exp = m.groups()
         if (a1 is not None) != (fn in ("copysign", "dist", "average", "mod", "rem", "pow2", "maxnum", "minnum",
-                                                 "maxmag", "minmag", "minmod", "negate")):
+                                                 "maxmag", "minmag", "minmod", "negate", "divfloor",
+                                                 "divceil", "divfix", "divround", "divround2even")):
             continue  # another arity (round(x, n) rounds to n digits): not these functors
         try:
             rec = dict(fn=fn, x=_value(a0), expected=_value(exp), tol_nt2ulp=0.0, source=f"{rel}:{ln}")

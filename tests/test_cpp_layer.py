@@ -366,7 +366,7 @@ def test_distribution_functions_through_tables(demos, tmp_path, prec):
              "evinv3": E.evinv(P, m, s), "cauinv3": E.cauinv(P, m, s), "cauinv2": E.cauinv(P, m),
              "maxnum": E.maxnum(X, P), "minnum": E.minnum(P, X), "maxmag": E.maxmag(X, P), "minmag": E.minmag(X, P),
              "minmod": E.minmod(X, P - 0.5), "negate": E.negate(P, X), "fms": E.fms(X, P, 0.25),
-             "fnma": E.fnma(X, P, X),
+             "fnma": E.fnma(X, P, X), "divfloor": E.divfloor(X, P), "divround2even": E.divround2even(X, 0.75),
              "one_param_sum": (E.normpdf(X) + E.norminv(P) + E.expcdf(X) + E.exppdf(X) + E.expinv(P) + E.logncdf(X)
                                + E.lognpdf(X) + E.logninv(P) + E.unifcdf(X) + E.caucdf(X) + E.caupdf(X) + E.evcdf(X)
                                + E.evpdf(X) + E.evinv(P) + E.cauinv(P))}

@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 UNARY = ["floor", "ceil", "trunc", "fix", "round", "round2even", "frac", "sign", "signnz", "oneplus", "oneminus",
          "minusone", "sqr_abs"]
 BINARY = ["copysign", "dist", "average", "mod", "rem", "pow2", "maxnum", "minnum", "maxmag", "minmag", "minmod",
-          "negate"]
+          "negate", "divfloor", "divceil", "divfix", "divround", "divround2even"]
 NT2_NAN = float(np.uint32(0xffffffff).view(np.float32))  # NT2's Nan<T>(): every bit set
 
 

@@ -39,7 +39,8 @@ def test_oracle_matches_nt2_unit_tests(oracle, rec):
 @pytest.mark.parametrize("rec", [r for r in GOLDEN if r["fn"] in ("pow", "atan2", "atan2d", "hypot", "logspace_add",
                                                               "logspace_sub", "copysign", "dist", "average", "beta",
                                                               "betaln", "mod", "rem", "pow2", "maxnum", "minnum",
-                                                              "maxmag", "minmag", "minmod", "negate")],
+                                                              "maxmag", "minmag", "minmod", "negate", "divfloor",
+                                                              "divceil", "divfix", "divround", "divround2even")],
                          ids=lambda r: f"{r['fn']}({r['x']},{r['y']})@{r['source'].split('/')[-1]}")
 def test_oracle_binary_matches_nt2_unit_tests(oracle, rec):
     got = getattr(oracle.lib(), "o_" + rec["fn"])(_arg(rec["x"]), _arg(rec["y"]))
