@@ -381,3 +381,27 @@ def test_oracle_signgam_and_beta(oracle):
     eps = float(np.finfo(np.float32).eps)
     assert np.max(np.abs(bl - rl) / terms) < 4 * eps
     assert np.max(np.abs(be - rb) / np.abs(rb) / np.maximum(terms, 1.0)) < 8 * eps
+
+
+def test_oracle_proper_tanpi_pow2_mod_rem_profile(oracle):
+    """The restated proper_tanpi stays within 3 ulp of tan(pi x) in FP64 on
+    (-1/2, 1/2); pow2(a, b) is ldexp(a, trunc(b)) wherever that is a normal
+    float; mod and rem satisfy a = q b + r with q the floor / truncated
+    quotient where every step is exact (small integers)."""
+    x = np.linspace(-0.49, 0.49, 100001).astype(np.float32)
+    y = oracle.proper_tanpi_f32(x)
+    r = np.tan(np.pi * x.astype(np.float64))
+    assert (np.abs(y - r) / np.spacing(np.abs(r).astype(np.float32))).max() <= 3.0
+    L = oracle.lib()
+    rng = np.random.default_rng(5)
+    a = rng.uniform(-100, 100, 2000).astype(np.float32)
+    b = rng.uniform(-60, 60, 2000).astype(np.float32)
+    want = np.ldexp(a.astype(np.float64), np.trunc(b).astype(np.int64))
+    got = np.float64([L.o_pow2(float(p), float(q)) for p, q in zip(a, b)])
+    assert np.array_equal(got, want)
+    ia = rng.integers(-1000, 1000, 2000).astype(np.float32)
+    ib = rng.integers(1, 50, 2000).astype(np.float32) * rng.choice([-1, 1], 2000).astype(np.float32)
+    m = np.float32([L.o_mod(float(p), float(q)) for p, q in zip(ia, ib)])
+    rr = np.float32([L.o_rem(float(p), float(q)) for p, q in zip(ia, ib)])
+    assert np.array_equal(m, ia - np.floor(ia / ib) * ib) and np.array_equal(m, np.mod(ia, ib))
+    assert np.array_equal(rr, np.fmod(ia, ib))
