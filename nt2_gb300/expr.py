@@ -179,6 +179,17 @@ def rem(a, b):
 def oneplus(a): return a + 1.0
 def oneminus(a): return 1.0 - a
 def minusone(a): return a - 1.0
+
+
+# the saturating and increment forms of boost.simd as they are for floats
+# (boost/simd/arithmetic/functions/{generic/inc,generic/dec,generic/abss,
+# scalar/negs,scalar/sqrs,generic/conj}.hpp): a + 1, a - 1, abs, -a, sqr, a
+def inc(a): return a + 1.0
+def dec(a): return a - 1.0
+def abss(a): return abs_(a)
+def negs(a): return -a
+def sqrs(a): return sqr(a)
+def conj(a): return a
 def sqr_abs(a): return sqr(a)
 def dist(a, b): return abs_(a - b)
 def average(a, b): return fma(a, 0.5, b * 0.5)

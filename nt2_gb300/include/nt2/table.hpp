@@ -734,6 +734,13 @@ NT2G_COMPOSED(oneplus, x + 1.0f)
 NT2G_COMPOSED(oneminus, 1.0f - x)
 NT2G_COMPOSED(minusone, x - 1.0f)
 NT2G_COMPOSED(sqr_abs, sqr(x))
+// boost.simd's inc, dec, abss, negs and sqrs as they are for floats
+// (arithmetic/functions/{generic/inc,generic/dec,generic/abss,scalar/negs,scalar/sqrs}.hpp)
+NT2G_COMPOSED(inc, x + 1.0f)
+NT2G_COMPOSED(dec, x - 1.0f)
+NT2G_COMPOSED(abss, abs(x))
+NT2G_COMPOSED(negs, -x)
+NT2G_COMPOSED(sqrs, sqr(x))
 #undef NT2G_COMPOSED
 
 // dist = |a - b|, average = fma(a, 1/2, b/2) with NT2's fma (boost/simd/
